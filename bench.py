@@ -1,0 +1,332 @@
+"""bench.py -- the headline benchmark: Mpaths/s of the path-traced SDF room on one GB300.
+
+Workload (the second of the reference's benchmark configurations): a 6 x 4 x 3 m room of 24 seeded SDF primitives
+(boxes, spheres, tori, rounded prisms, smooth-unioned), GGX metal and plastic, a 100 klx sun and a sky through one
+window; 1920 x 1080, 64 samples per pixel, max depth 8, march tolerance 1e-4 m, FP64 pixel tallies. One STEP is
+the whole render -- 64 samples of every pixel, 132.7 M camera paths -- folded into the FP64 accumulation.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference] [--small]
+
+value: paths / s with the scene resident on the GPU (graph replays; the timed region brackets K renders with a
+       synchronize). e2e: the same through the C ABI as a host calls it -- scene, settings and camera uploaded from
+       host memory, the render, and the FP64 picture and its error bar read back to host memory, every step.
+roofline: the march kernel (the dominant one), FP32 arithmetic: evaluations counted on the device x the FLOPs of
+       one evaluation counted from the scene table (shadytracer_gb300/flops.py) / its CUDA-event time on its own
+       stream, in a second pass over the same K renders with per-kernel events on.
+cpu_baseline: the oracle (oracle/, the CPU restatement of the reference's path) in f32 on every host core, over a
+       bounded band of the same picture's paths.
+--impl reference: the reference's own implementation cannot run here (JavaScript + WGSL through WebGPU); its CPU
+       restatement, the oracle, is timed instead on the host's cores, on the same workload and metric.
+Multi-GPU (torchrun): replicas -- each rank renders the whole workload on its own GPU; value sums the ranks' paths
+       over the slowest rank's time (weak scaling). There is no data exchange in the path tracer.
+"""
+import argparse
+import ctypes as C
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--small", action="store_true", help="a 480 x 270, 4-spp render (profiling runs)")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def workload(small):
+    from shadytracer_gb300 import scenes
+    if small:
+        s = scenes.sdf_room(width=480, height=270, spp=4, maxbounce=8)
+    else:
+        s = scenes.sdf_room(width=1920, height=1080, spp=64, maxbounce=8)
+    return s
+
+
+def config_of(s):
+    p = s.params
+    return {"workload": "room24 SDF room %dx%d, %d spp, max depth %d, eps 1e-4 m" % (p.width, p.height,
+                                                                                     s.info["spp"], p.maxbounce),
+            "width": p.width, "height": p.height, "spp": s.info["spp"], "maxbounce": p.maxbounce,
+            "paths_per_step": p.width * p.height * s.info["spp"], "primitives": 24,
+            "l2": "working set above L2: path state + queues of 2.07 M paths are 300 MB a wave (> 129 MB L2)"}
+
+
+# ---------------------------------------------------------------------------------------------------------------
+# clocks during the timed region (nvidia-smi sampled every 200 ms)
+# ---------------------------------------------------------------------------------------------------------------
+class Clocks:
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.path or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        rows = []
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                rows.append((float(f[1]), float(f[2]), float(f[3]) if f[3] not in ("[N/A]", "N/A") else 0.0, f[5:9]))
+            except ValueError:
+                continue
+        os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        load = [r for r in rows if r[2] > 200] or rows
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i, v in enumerate(r[3]) if v.lower() == "active"})
+        return {"sm_mhz": float(np.median([r[0] for r in load])), "sm_max_mhz": max(r[1] for r in rows),
+                "reasons": reasons, "samples": len(rows)}
+
+
+def peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        return None
+
+
+# ---------------------------------------------------------------------------------------------------------------
+# the CPU baseline: the oracle in f32 over a band of the picture's paths, all host threads
+# ---------------------------------------------------------------------------------------------------------------
+def cpu_baseline(s, budget_s=15.0):
+    from oracle import oracle
+    threads = os.cpu_count() or 1
+    p = s.params
+    P = p.width * p.height
+    acc = oracle.Accum(p.width, p.height)
+    probe = min(P, 8192)
+    t = time.perf_counter()
+    oracle.render(s, 1, acc, fp64=False, threads=threads, sample0=0, path_first=P // 2, path_count=probe)
+    rate = probe / max(time.perf_counter() - t, 1e-6)
+    n = int(min(P, max(probe, rate * budget_s)))
+    first = max(0, P // 2 - n // 2)
+    t = time.perf_counter()
+    oracle.render(s, 1, acc, fp64=False, threads=threads, sample0=1, path_first=first, path_count=n)
+    dt = time.perf_counter() - t
+    return {"value": n / dt / 1e6, "unit": "Mpaths/s", "cores": threads, "kind": "port",
+            "sample": "1 sample of %d consecutive paths (rows %d-%d of %dx%d), %.1f s" % (
+                n, first // p.width, (first + n) // p.width, p.width, p.height, dt)}
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    s = workload(args.small)
+    metric = "Mpaths/s"
+    for _ in range(max(args.warmup, 0)):
+        cpu_baseline(s, budget_s=3.0)
+    vals, samples = [], []
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        cb = cpu_baseline(s, budget_s=10.0)
+        vals.append(cb["value"])
+        samples.append(cb["sample"])
+    dt = time.perf_counter() - t0
+    v = float(np.mean(vals))
+    line = {"impl": "reference", "metric": metric, "value": v, "unit": "Mpaths/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / max(args.steps, 1),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": config_of(s),
+            "cpu_baseline": {"value": v, "unit": "Mpaths/s", "cores": os.cpu_count(), "kind": "port",
+                             "sample": "each step: " + samples[-1]},
+            "e2e": {"value": v, "unit": "Mpaths/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "note": "the reference is JavaScript + WGSL run by WebGPU (no JS runtime or graphics stack here); its "
+                    "path is timed through the oracle, its CPU restatement, on every host core"}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args):
+    rank, world, local = dist_env()
+    import torch
+    dev = local if world > 1 else 0
+    torch.cuda.set_device(dev)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", dev))
+    from shadytracer_gb300 import flops
+    from shadytracer_gb300.renderer import create_path_tracer
+    s = workload(args.small)
+    spp = s.info["spp"]
+    p = s.params
+    P = p.width * p.height
+    paths_per_step = P * spp
+    rt = create_path_tracer(s, device=dev)
+    stream = torch.cuda.ExternalStream(rt.stream(), device=torch.device("cuda", dev))
+
+    def barrier():
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    def one_step():
+        rt.invalidate()
+        rt.step_async(spp)
+
+    # ---- warm-up ----
+    for _ in range(max(args.warmup, 3)):
+        one_step()
+        rt.sync()
+    # ---- timed: value (device-resident scene; graph replays) ----
+    barrier()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with Clocks(dev) as clk:
+        e0.record(stream)
+        for _ in range(args.steps):
+            one_step()
+        e1.record(stream)
+        rt.sync()
+        barrier()
+    ms = e0.elapsed_time(e1) / args.steps
+    clocks = clk.summary()
+    c = rt.counters()
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * paths_per_step / (ms / 1e3) / 1e6
+
+    # ---- e2e: through the C ABI from host memory, the picture read back every step ----
+    rgb = np.zeros((p.height, p.width, 3), np.float64)
+    V = np.zeros((p.height, p.width), np.float64)
+    S = np.zeros((p.height, p.width), np.float64)
+    cnt = np.zeros((p.height, p.width), np.uint32)
+    Pv = C.c_void_p
+    L = rt.L
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        rt.set_scene(s)                     # scene table + materials, host -> device
+        rt.set_params(p)                    # the settings (resets the accumulation)
+        rt.set_view(s.view)
+        rt.step(spp)
+        L.st_read_accum(rt.ctx, rgb.ctypes.data_as(Pv), V.ctypes.data_as(Pv), S.ctypes.data_as(Pv),
+                        cnt.ctypes.data_as(Pv))
+    barrier()
+    e2e_s = (time.perf_counter() - t0) / args.steps
+    if dist:
+        t = torch.tensor([e2e_s], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    h2d = (C.sizeof(type(s.prims)) + C.sizeof(type(s.materials)) + C.sizeof(p) + C.sizeof(s.view))
+    d2h = P * (32 + 16)
+    Lmean = float((rgb @ np.array([0.2126, 0.7152, 0.0722])).mean())
+
+    # ---- per-kernel times (CUDA events on the library's stream) over the same K renders ----
+    rt.enable_kernel_times(True)
+    rt.reset_kernel_times()
+    c0 = rt.counters()
+    for _ in range(args.steps):
+        one_step()
+        rt.sync()
+    kt = rt.kernel_times()
+    c1 = rt.counters()
+    rt.enable_kernel_times(False)
+    evals = c1["march_steps"] - c0["march_steps"]
+    if c1["samples"] < c0["samples"]:
+        evals = c1["march_steps"]
+    f_eval, sfu_eval = flops.march_step_flops(s)
+    m_launches, m_ms = kt.get("march", (0, 0.0))
+    tot_ms = sum(v[1] for v in kt.values()) or 1.0
+    achieved = (evals * f_eval) / (m_ms / 1e3) / 1e12 if m_ms > 0 else 0.0   # TFLOP/s over the march's time
+    pk = peaks()
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    if pk and pk.get("sm_max_mhz"):
+        peak = sms * 128 * 2 * pk["sm_max_mhz"] * 1e6 / 1e12
+        peak_src = "FP32 FMA peak from MEASURED_PEAKS.json's sm_max_mhz: %d SMs x 128 lanes x 2 x %.0f MHz" % (
+            sms, pk["sm_max_mhz"])
+    else:
+        peak = sms * 128 * 2 * 2070e6 / 1e12
+        peak_src = "FP32 FMA peak at the nominal 2070 MHz (fallback)"
+    launches_per_sample = 2 + 4 * (p.budget or (p.maxbounce + 1 + (p.maxiter + 31) // 32))
+    line = {"metric": "Mpaths/s", "value": value, "unit": "Mpaths/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32 (FP64 pixel tallies)", "data": "synthetic (seeded scene)",
+            "config": dict(config_of(s), parallelism="replicas" if world > 1 else "1 GPU"),
+            "e2e": {"value": world * paths_per_step / e2e_s / 1e6, "unit": "Mpaths/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h},
+            "gpu_launches": launches_per_sample * spp * args.steps,
+            "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                         "frac": achieved / peak if peak else None, "traffic": None,
+                         "kernel": "k_march", "flops_per_eval": f_eval, "sfu_per_eval": sfu_eval,
+                         "evals_per_launch": evals / max(m_launches, 1),
+                         "avg_launch_ms": m_ms / max(m_launches, 1), "peak_source": peak_src},
+            "kernel_share": {k: round(v[1] / tot_ms, 4) for k, v in kt.items()},
+            "clocks": clocks,
+            "stats": {"mean_luma": Lmean, "segments_per_path": c["segments"] / max(c["paths"], 1),
+                      "steps_per_segment": c["march_steps"] / max(c["segments"], 1),
+                      "shadow_steps_per_ray": c["shadow_steps"] / max(c["shadow_rays"], 1),
+                      "flushed": c["flushed"], "nonfinite": c["nonfinite"]}}
+    if rank == 0 and world == 1 and not args.no_cpu:
+        line["cpu_baseline"] = cpu_baseline(s)
+    elif rank == 0:
+        line["cpu_baseline"] = None
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    rt.close()
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

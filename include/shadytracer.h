@@ -1,0 +1,316 @@
+/*
+ * shadytracer.h -- the C ABI of the GB300 rendering hot path (libshadytracer.so).
+ *
+ * Plain C types only: no CUDA, no C++ and no torch types cross this boundary, so a JavaScript host
+ * (an N-API addon), Python (ctypes) or C can bind it. Every call returns an int status: 0 (ST_OK) or
+ * a negative ST_ERR_* code; st_last_error() says why in words. No C++ exception crosses it.
+ *
+ * What each entry point replaces in the reference (lampmaker/ShadyTracer v0.88.0, paths relative to
+ * its root):
+ *   st_create / st_destroy       createPathTracer + RT.init / RT.dispose      lib/pathtracer/index.js:90,
+ *                                                                             core/raytrace_main.js:121,1291
+ *   st_set_scene                 RT.setScene(scene) (the scene contract)      lib/pathtracer/index.js (setScene),
+ *                                                                             core/raytrace_main.js:1145,
+ *                                                                             lib/pathtracer/README.md:126-145
+ *   st_set_params                RT.set(values) -> unknown keys               lib/pathtracer/README.md:56,
+ *                                                                             core/uniforms.schema.js (UniformSpec)
+ *   st_set_view                  the camera uniforms genrays reads            core/genrays.js:65-92
+ *   st_invalidate                RT.invalidate()                              lib/pathtracer/README.md:38-124
+ *   st_step / st_step_async /    RT.step(n) (resolves when the GPU finished)  lib/pathtracer/index.js:1005,
+ *   st_sync                                                                   core/raytrace_main.js:1574 (R.trace)
+ *   st_read_accum                the accumulation + error-bar moments read    core/wavefront.js:414-494 (prog_resolve),
+ *                                                                             core/measure.js:36-66
+ *   st_image_stats               R.imageStats()                               core/raytrace_main.js:876-950
+ *   st_read_counters             the Counters struct readback                    core/wavefront.js:150
+ *   st_kernel_times              per-kernel GPU time (kerneltime.js)          core/kerneltime.js:1-25
+ *   st_sppm_*                    the photon map's store / grid / gather       core/sppm.js:305-511
+ *   st_optics_*                  createOptics(RT, WG): O.setSources/setFar/run optics/index.js:92,434-475,
+ *                                                                             optics/kernels.js:288-408,571-699
+ *   st_last_error                the JS exception's message                   core/raytrace_main.js:1580-1581
+ *
+ * Threading: one CUDA stream per context; a context is not thread-safe (the JS host is single-threaded).
+ * Memory: caller-owned output buffers; the library owns its device memory.
+ */
+#ifndef SHADYTRACER_H
+#define SHADYTRACER_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ST_ABI_VERSION 1
+
+/* status codes */
+#define ST_OK            0
+#define ST_ERR_ARG      -1   /* a bad argument: null pointer, size out of range, unknown enum */
+#define ST_ERR_OOM      -2   /* device memory could not be allocated */
+#define ST_ERR_CUDA     -3   /* a CUDA call failed (no device, launch failure) */
+#define ST_ERR_TIMEOUT  -4   /* st_sync ran out of time, or a device-side wait ran out of iterations */
+#define ST_ERR_BUSY     -5   /* a trace is in flight (st_step_async without st_sync) */
+#define ST_ERR_COMPILE  -6   /* a scene failed to build; the previous scene is kept */
+#define ST_ERR_STATE    -7   /* called in the wrong state (no scene, no view) */
+
+typedef struct st_ctx st_ctx;
+
+/* ---------------------------------------------------------------------------------------------
+ * THE SCENE, AS DATA: a table of primitives folded the way the reference's scene prelude folds a
+ * scene (core/scene_api.js:28-80 add_new / fold): each item is one primitive, or a CSG chain of them
+ * (smooth union / union / subtraction into the item before), and the items are folded by the nearest
+ * surface (argmin |d|), the medium being the least-deep item the point is inside.
+ * --------------------------------------------------------------------------------------------- */
+enum st_prim_type {
+    ST_PRIM_PLANE    = 0,  /* z = 0 in the local frame, +z out                                     */
+    ST_PRIM_SPHERE   = 1,  /* p0 radius                                              sdf.js:217     */
+    ST_PRIM_BOX      = 2,  /* p0..p2 half sizes                                       sdf.js:220    */
+    ST_PRIM_ROUNDBOX = 3,  /* p0..p2 half sizes, p3 rounding                          sdf.js:224    */
+    ST_PRIM_TORUS    = 4,  /* p0 ring radius R, p1 tube radius r (xy plane)           sdf.js:602    */
+    ST_PRIM_PRISM    = 5,  /* p0 sides, p1 corner radius, p2 height (z), p3 rounding  shapes.js:266-287 */
+    ST_PRIM_ASPHERE  = 6,  /* p0 D, p1 t, p2 R1, p3 k1, p4 a4_1, p5 a6_1, p6 R2, p7 k2, p8 a4_2, p9 a6_2
+                                                                                      shapes.js:621-660 */
+    ST_PRIM_CYLINDER = 7   /* p0 half height (z), p1 radius                           sdf.js:228    */
+};
+enum st_prim_op {
+    ST_OP_ITEM   = 0,      /* starts a new fold item                                               */
+    ST_OP_SMOOTH = 1,      /* smooth union into the current item, radius k            sdf.js:252    */
+    ST_OP_UNION  = 2,      /* hard union into the current item                                     */
+    ST_OP_SUB    = 3       /* subtracted from the current item                                     */
+};
+
+/* 128 bytes, 16-byte aligned fields: staged whole into shared memory by a bulk copy. */
+typedef struct st_prim {
+    uint32_t type, op, material, flags;  /* flags: bit 0 = emits a detector tag (optics), reserved  */
+    float    pos[3];                     /* centre, metres                                          */
+    float    k;                          /* smooth-union radius, metres (ST_OP_SMOOTH)               */
+    float    rot[9];                     /* world -> local rotation, row major                      */
+    float    pad0[3];
+    float    p[12];                      /* shape parameters (st_prim_type)                          */
+} st_prim;
+
+/* A material: the fields of the reference's Material2 (core/materials.js:12-60) the hot path reads. */
+typedef struct st_material {
+    float base[3];        /* baseColor                                                            */
+    float metallic;
+    float roughness;      /* perceptual; alpha = roughness^2, delta below alpha 1e-3               */
+    float specular;       /* 0.5 = the physical interface, 0 = no coat                            */
+    float specular_tint;
+    float transmission;
+    float ior;
+    float abbe;           /* Abbe number V_d; 0 = not dispersive (spectral.js cauchyN)             */
+    float attenuation;    /* attenuationDistance (m); 0 = tint at each crossing                    */
+    float detector;       /* optics: > 0.5 stops and records a ray (optics/kernels.js optIsDetector)*/
+    float emissive[3];    /* cd/m^2                                                               */
+    float pad;
+} st_material;
+
+typedef struct st_scene_desc {
+    const st_prim*     prims;
+    uint32_t           n_prims;        /* at most ST_MAX_PRIMS                                      */
+    const st_material* materials;
+    uint32_t           n_materials;    /* at most ST_MAX_MATERIALS; material 0 is the air           */
+    float              env_radius;     /* metres; where the scene stops (photometry.js:158)         */
+    float              tolerance;      /* metres; 0 = the automatic 1 mm (photometry.js:141-150)    */
+    /* THE HAZE BOX (core/haze.js:64-80 hazeUniforms), metres; sigma_t 0 = none */
+    float              haze_centre[3];
+    float              haze_sigma_t;   /* 1 / mean free path, per metre                            */
+    float              haze_axes[9];   /* the box's unit axes, rows                                */
+    float              haze_half[3];
+    float              haze_albedo[3];
+    float              haze_g;         /* Henyey-Greenstein asymmetry, |g| <= 0.95                  */
+} st_scene_desc;
+
+#define ST_MAX_PRIMS      256
+#define ST_MAX_MATERIALS  256
+
+/* ---------------------------------------------------------------------------------------------
+ * THE SETTINGS the hot path reads (core/uniforms.schema.js UniformSpec; their derived uniforms are
+ * computed on the host in double precision, as core/photometry.js:182-237 derive() does).
+ * --------------------------------------------------------------------------------------------- */
+typedef struct st_params {
+    uint32_t width, height;       /* the picture                                                   */
+    uint32_t maxbounce;           /* 10                                                            */
+    uint32_t maxiter;             /* 400: march steps a path may take in all                       */
+    float    stepscale;           /* 0.9                                                           */
+    uint32_t nee;                 /* 1: next-event estimation                                      */
+    uint32_t rr;                  /* 0: Russian roulette after 3 bounces                           */
+    float    nee_sun_pick;        /* 0.5: share of light samples sent at the sun's cone            */
+    float    sun_elevation;       /* degrees                                                       */
+    float    sun_azimuth;         /* degrees                                                       */
+    float    sun_diameter;        /* degrees (0.53)                                                */
+    float    sun_illuminance;     /* lux at normal incidence (the disc's)                           */
+    float    sky_luminance;       /* cd/m^2 of the uniform sky above the horizon                    */
+    float    ground_luminance;    /* cd/m^2 below the horizon                                      */
+    float    env_uniform;         /* > 0: the white-furnace environment, this luminance everywhere  */
+    float    env_sun_gain;        /* 1                                                             */
+    float    env_sky_gain;        /* 1                                                             */
+    uint32_t sun_hint;            /* 1: the sun's cone is sampled                                  */
+    uint32_t seed;                /* base seed of the sample sequence                              */
+    uint32_t maxaverages;         /* 0: a true mean; N: an EMA window of N                          */
+    float    eps;                 /* surface tolerance setting, metres; 0 = the scene's             */
+    uint32_t budget;              /* wavefront iterations a sample runs; 0 = the worst case,
+                                     maxbounce + 1 + ceil(maxiter / 32) (raytrace_main.js:1815)   */
+    uint32_t samples_per_wave;    /* 0 = automatic                                                 */
+} st_params;
+
+/* The camera, as genrays reads it (core/genrays.js:65-92): the basis from invView's columns and the
+ * two diagonal entries of invProjection. */
+typedef struct st_view {
+    float    cam_pos[3];
+    float    right[3];
+    float    up[3];
+    float    fwd[3];              /* from the target to the camera: the view looks down -fwd         */
+    float    fx, fy;              /* invProjection[0][0], [1][1]: tan(fov/2) * aspect, tan(fov/2)    */
+    uint32_t camtype;             /* 0 perspective, 1 orthographic                                 */
+} st_view;
+
+typedef struct st_counters_t {
+    uint64_t paths;               /* camera paths deposited                                        */
+    uint64_t segments;            /* path segments marched                                         */
+    uint64_t march_steps;         /* SDF evaluations of the march                                  */
+    uint64_t shadow_rays;         /* shadow rays traced                                            */
+    uint64_t shadow_steps;        /* SDF evaluations of the occlusion pass                         */
+    uint32_t nonfinite;           /* deposits refused (NaN, inf, negative luminance)               */
+    uint32_t flushed;             /* paths the last iteration had to end                           */
+    uint32_t shadowcut;           /* shadow rays out of steps                                      */
+    uint32_t samples;             /* samples folded since the last invalidate                      */
+} st_counters_t;
+
+typedef struct st_image_stats_t {
+    double mean_luma;             /* over sampled pixels                                           */
+    double median_luma;
+    double trimmed_mean_luma;     /* the middle 98 %                                               */
+    double mean_rel_se;           /* mean of se / L over pixels with L > 0                          */
+    uint32_t sampled;             /* pixels with a sample                                          */
+    uint32_t samples;             /* samples folded                                                */
+} st_image_stats_t;
+
+typedef struct st_kernel_time {
+    char     name[24];
+    uint32_t launches;
+    double   ms;                  /* summed CUDA-event time on the context's stream                 */
+} st_kernel_time;
+
+/* ---- life cycle ---- */
+int  st_create(int device, st_ctx** out);
+int  st_destroy(st_ctx* ctx);
+const char* st_last_error(const st_ctx* ctx);
+int  st_abi_version(void);
+
+/* ---- the scene, the settings, the camera ---- */
+/* cuda_src: NULL for a scene given as a primitive table (desc); the table is copied. On failure the
+ * previous scene is kept and errbuf (if given) holds the reason. */
+int  st_set_scene(st_ctx* ctx, const char* cuda_src, const st_scene_desc* desc, char* errbuf, size_t errlen);
+/* unknown_mask: reserved (0); the struct has no unknown keys. Changing the picture size or the
+ * settings resets the accumulation. */
+int  st_set_params(st_ctx* ctx, const st_params* p, uint64_t* unknown_mask);
+int  st_set_view(st_ctx* ctx, const st_view* v);
+int  st_invalidate(st_ctx* ctx);
+
+/* ---- tracing ---- */
+int  st_step(st_ctx* ctx, int n);             /* n samples; returns when the GPU has finished       */
+int  st_step_async(st_ctx* ctx, int n);       /* queue n samples                                    */
+int  st_sync(st_ctx* ctx, int timeout_ms);    /* wait for the queued samples; <0 waits forever      */
+
+/* ---- readings (caller-owned buffers, width*height entries each; NULL skips one) ---- */
+int  st_read_accum(st_ctx* ctx, double* rgb, double* V, double* S, uint32_t* count);
+int  st_image_stats(st_ctx* ctx, st_image_stats_t* out);
+int  st_read_counters(st_ctx* ctx, st_counters_t* out);
+/* Per-kernel GPU time, CUDA events on the context's stream around every launch while enabled (launches then
+ * run directly rather than as a replayed graph). */
+int  st_enable_kernel_times(st_ctx* ctx, int on);
+int  st_kernel_times(st_ctx* ctx, st_kernel_time* out, int max, int* n_out);
+int  st_reset_kernel_times(st_ctx* ctx);
+/* The microfacet albedo tables the context built at init (microfacet.js:245-330): 16*32*32 Ec,
+ * 16*32 Ec_avg, 32*32 E1 floats. */
+int  st_mf_tables(st_ctx* ctx, float* ec, float* ecavg, float* e1);
+
+/* ---- the photon map (core/sppm.js) ----
+ * Records are SoA: pos (3 floats), power (3), the direction it came from and its surface normal as
+ * octahedral words, bounce|flags|sub word. st_sppm_build sorts n records into the grid of cell size
+ * `cell` (metres) over 2^20 hashed cells by a counting sort; st_sppm_read_grid returns each record's
+ * hash (key), the per-cell counts and the cell-ordered record permutation. */
+typedef struct st_sppm_stats {
+    uint32_t stored;              /* records in the grid                                           */
+    uint32_t gathers;             /* gathers run                                                   */
+    uint32_t cut;                 /* gathers that reached the hard cap                             */
+    uint32_t visits_max;          /* most records one gather looked at                              */
+    uint64_t visits;              /* records looked at in all                                      */
+} st_sppm_stats;
+
+int  st_sppm_build(st_ctx* ctx, const float* pos, const float* power, const uint32_t* dir_oct,
+                   const uint32_t* nrm_oct, const uint32_t* flags, uint32_t n, float cell);
+int  st_sppm_read_grid(st_ctx* ctx, uint32_t* key, uint32_t* cell_count, uint32_t* cell_start,
+                       uint32_t* order);
+/* gather at m query points: pos (3m), normal (3m), radius, the surface's albedo (Lambertian f =
+ * albedo/pi) and bounce of each query; out (3m) = sum f * power within r on a facing surface
+ * (core/sppm.js:305-346,475-494, budget 0 = unlimited). */
+int  st_sppm_gather(st_ctx* ctx, const float* qpos, const float* qnrm, const float* qalbedo,
+                    const uint32_t* qbounce, uint32_t m, float radius, uint32_t maxbounce,
+                    uint32_t budget, uint32_t seed, float* out);
+int  st_sppm_stats_read(st_ctx* ctx, st_sppm_stats* out);
+
+/* ---- the optics bench (optics/index.js, optics/kernels.js) ---- */
+typedef struct st_optics_source {
+    float    centre[3];           /* metres                                                        */
+    float    flux;                /* lm: its share of the rays follows it                          */
+    float    axis[3];             /* emission axis, unit                                           */
+    uint32_t shape;               /* 0 point, 1 disc, 2 rectangle                                   */
+    float    tangent[3];          /* first tangent                                                 */
+    float    size_x;              /* disc radius / rectangle half width                            */
+    float    size_y;              /* rectangle half height                                          */
+    uint32_t dist;                /* 0 collimated, 1 uniform cone, 2 cos^n                          */
+    float    cos_half;            /* cos of the cone's half angle                                   */
+    float    n_exp;               /* the cos^n exponent (1: Lambertian)                             */
+    float    emit_n;              /* the index it emits into                                        */
+    uint32_t two_sided;
+    uint32_t on_surface;          /* start 2 march tolerances off the sheet                          */
+    uint32_t instance;            /* which instance of a batch it belongs to                        */
+} st_optics_source;
+
+typedef struct st_optics_far {
+    uint32_t nC, nG;              /* type C grid: nC about the axis, nG from 0 to 180 degrees       */
+    float    axis[3];             /* gamma = 0                                                      */
+    float    c0[3];               /* C = 0, square to the axis                                      */
+} st_optics_far;
+
+/* A batch of independent instances traced in one launch chain: instance i owns rays
+ * [ray_first[i], ray_first[i] + ray_count[i]) and the scene items whose st_prim.flags >> 8 == i
+ * (0xFFFFFF: shared by all). */
+typedef struct st_optics_batch {
+    uint32_t n_instances;
+    const uint32_t* ray_count;    /* rays per instance                                             */
+    uint32_t lux_cells;           /* the lux map is lux_cells^2 per instance (0 none)               */
+    float    lux_half;            /* its half width, metres                                         */
+    float    lux_height;          /* its distance from the source along the axis, metres            */
+    uint32_t maxbounce;           /* 0 = 32                                                         */
+    uint32_t seed;
+} st_optics_batch;
+
+typedef struct st_optics_totals {
+    double   emitted;             /* weight emitted (rays)                                          */
+    double   escaped, lost, detected, absorbed;   /* weight                                         */
+    uint64_t interactions;
+    uint64_t rays;
+} st_optics_totals;
+
+int  st_optics_set_sources(st_ctx* ctx, const st_optics_source* src, uint32_t n);
+int  st_optics_set_far(st_ctx* ctx, const st_optics_far* far);
+/* Traces every instance of the batch; far (n_instances*nG*nC) and lux (n_instances*cells^2) are the
+ * FP64 tallies in ray weight (the host multiplies by flux / rays); totals per instance. */
+int  st_optics_run(st_ctx* ctx, const st_optics_batch* batch, double* far, double* lux,
+                   st_optics_totals* totals);
+
+/* ---- the binding's checks ---- */
+/* The sizes of the structs above as this library was built (st_prim, st_material, st_scene_desc, st_params,
+ * st_view, st_counters_t, st_image_stats_t, st_kernel_time, st_sppm_stats, st_optics_source, st_optics_far,
+ * st_optics_batch, st_optics_totals, in that order); returns how many it has. */
+int  st_struct_sizes(uint32_t* out, int max);
+/* The context's CUDA stream (a cudaStream_t), for a host that orders or times its own work against it. */
+void* st_stream(st_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SHADYTRACER_H */

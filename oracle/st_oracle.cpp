@@ -1,0 +1,500 @@
+// TEST INFRASTRUCTURE ONLY -- the oracle's entry points (extern "C", loaded by oracle/oracle.py through ctypes).
+// Only tests/, __graft_entry__.smoke() and bench.py's cpu_baseline leg call these, as the checker and the CPU
+// baseline; the product (libshadytracer.so) never links or runs any of it.
+//
+// The path tracer restates, for one path at a time, what the reference's wavefront does to it:
+//   genrays            core/genrays.js:36-97
+//   march              core/wavefront.js:834-1005 (sphere tracing, marchTol hit test, escape test, lmax, maxiter)
+//   shade              core/wavefront.js:1244-1442, core/tracebasics.js:834-1100 (pathBegin..pathEnd),
+//                      core/materials_pbr.js:1110-1440 (processMaterial_advanced: NEE + MIS + the lobe draw)
+//   occlude            core/wavefront.js:1481-1692
+//   deposit            core/wavefront.js:162-245 (refused: NaN, inf, negative luminance)
+//   resolve            core/wavefront.js:414-494 and core/measure.js:36-51 (EMA mean, V and S moments), in FP64
+// A wavefront processes every live path one segment per iteration, so "the i-th iteration" is the path's i-th
+// segment here too; the last iteration takes no light sample (UB.lastpass) and ends what is left (THE FLUSH).
+#include "st_oracle_render.h"
+#include "st_oracle_extra.h"
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+#include <atomic>
+
+using namespace sto;
+
+namespace {
+
+const uint32_t RAY_ACTIVE = 0, RAY_ABSORBED = 1, RAY_ESCAPED = 2, RAY_MAXITER = 4, RAY_SOURCE = 5,
+               RAY_TERMINATED = 8, RAY_SCATTER = 9;
+
+struct Stats {
+    std::atomic<uint64_t> paths{0}, segments{0}, march_steps{0}, shadow_rays{0}, shadow_steps{0};
+    std::atomic<uint32_t> nonfinite{0}, flushed{0}, shadowcut{0};
+};
+
+template <class T> struct Ctx {
+    const st_scene_desc* s;
+    st_params p;
+    Derived d;
+    Env<T> env;
+    const MfTables* tb;
+    T tol, envR2, stepscale;
+    uint32_t budget;
+    HazeBox<T> haze;
+};
+
+template <class T> struct Ray {
+    V3<T> pos, dir, beta, rad;
+    T ltot, n, sunmis, tmax, absLtot;
+    uint32_t bounces, steps, state, pix;
+};
+
+template <class T> inline void move_by(Ray<T>& r, const V3<T>& off) {       // tracebasics.js:562-567 moveBy
+    r.pos += off;
+    r.ltot += length(off) * r.n;
+}
+
+// badDeposit (wavefront.js:181-188): NaN or inf in a channel, or negative luminance
+template <class T> inline bool bad_deposit(const V3<T>& c) {
+    return !std::isfinite(c.x) || !std::isfinite(c.y) || !std::isfinite(c.z) || luma(c) < T(0);
+}
+
+template <class T> struct Frame {
+    std::vector<double> rgb;   // per sample: the deposits (the reference's f32 frame; summed in double here)
+    std::vector<uint32_t> cnt;
+};
+
+template <class T> inline void deposit(Frame<T>& f, uint32_t pix, const V3<T>& c, Stats& st) {
+    if (bad_deposit(c)) { st.nonfinite++; return; }
+#pragma omp atomic
+    f.rgb[pix * 3 + 0] += (double)c.x;
+#pragma omp atomic
+    f.rgb[pix * 3 + 1] += (double)c.y;
+#pragma omp atomic
+    f.rgb[pix * 3 + 2] += (double)c.z;
+}
+
+// the march (wavefront.js:866-947): to the surface, the sky, lmax or maxiter
+template <class T> inline T march(const Ctx<T>& C, Ray<T>& r, Stats& st, bool use_haze) {
+    uint64_t steps = 0;
+    T dh = T(1e7);
+    for (;;) {
+        if (use_haze && haze_arrived(r.tmax, r.ltot)) {                       // haze.js:280-288 hazeArrived / hazeAt
+            r.pos = r.pos - r.dir * ((r.ltot - r.tmax) / std::max(r.n, T(1e-4)));
+            r.ltot = r.tmax;
+            r.state = RAY_SCATTER;
+            break;
+        }
+        SceneHit<T> h = scene_eval(*C.s, r.pos);
+        T ea = std::fabs(h.d);
+        T eps = march_tol(r.pos, C.tol);
+        steps++;
+        if (r.ltot > T(1000) || r.steps > C.p.maxiter) r.state = RAY_MAXITER;
+        if (dot(r.pos, r.dir) > T(0) && dot(r.pos, r.pos) > C.envR2) r.state = RAY_ESCAPED;
+        if (ea < eps || r.state != RAY_ACTIVE) { dh = h.d; break; }
+        r.steps += 1;
+        T d = ea * C.stepscale;
+        move_by(r, r.dir * d);
+    }
+    st.march_steps += steps;
+    return dh;
+}
+
+// the occlusion pass (wavefront.js:1481-1692), distance only: true when the shadow ray reaches the light
+template <class T> inline bool occlude(const Ctx<T>& C, V3<T> pos, const V3<T>& dir, T n, Stats& st) {
+    T ltot = 0;
+    uint32_t steps = 0;
+    bool reached = false, cut = false;
+    uint64_t evals = 0;
+    for (;;) {
+        SceneHit<T> h = scene_eval(*C.s, pos);
+        evals++;
+        T ea = std::fabs(h.d);
+        T eps = march_tol(pos, C.tol);
+        if (ea < eps) break;                                                           // blocked
+        if (dot(pos, dir) > T(0) && dot(pos, pos) > C.envR2) { reached = true; break; }
+        steps += 1;
+        if (ltot > T(1000) || steps > C.p.maxiter) { reached = true; cut = steps > C.p.maxiter; break; }
+        T step = ea * C.stepscale;
+        V3<T> off = dir * step;
+        pos += off;
+        ltot += length(off) * n;
+    }
+    st.shadow_rays++;
+    st.shadow_steps += evals;
+    if (cut) st.shadowcut++;
+    return reached;
+}
+
+// the normal by three forward differences at normalTol (tracebasics.js:1310-1322 calcNormals_fast)
+template <class T> inline V3<T> hit_normal(const Ctx<T>& C, const V3<T>& p, T d) {
+    T eps = march_tol(p, C.tol);
+    T gx = scene_eval(*C.s, V3<T>(p.x + eps, p.y, p.z)).d - d;
+    T gy = scene_eval(*C.s, V3<T>(p.x, p.y + eps, p.z)).d - d;
+    T gz = scene_eval(*C.s, V3<T>(p.x, p.y, p.z + eps)).d - d;
+    return normalize(V3<T>(gx, gy, gz));
+}
+
+// a path's hit, shaded: pathBegin..pathEnd (tracebasics.js:834-1100) with processMaterial_advanced
+// (materials_pbr.js:1110-1440). The light sample's shadow ray is traced here and its deposit made at once.
+template <class T>
+inline void shade_hit(const Ctx<T>& C, Ray<T>& r, T dhit, Rng& rng, bool last, Frame<T>& fr, Stats& st) {
+    V3<T> n = hit_normal(C, r.pos, dhit);
+    bool inside = dhit < T(0);
+    V3<T> nrm = inside ? -n : n;                                                   // scene_api.js:127-135 pathFacing
+    T otol = T(10) * march_tol(r.pos, C.tol);                                      // offsetTol
+    if (dot(-r.dir, nrm) < T(0)) {                                                 // leaving: moved on, no bounce
+        move_by(r, r.dir * otol);
+        return;
+    }
+    r.bounces += 1;
+    SceneHit<T> h = scene_eval(*C.s, r.pos);
+    const st_material& m = C.s->materials[std::min(h.m, C.s->n_materials - 1)];
+    V3<T> emis(T(m.emissive[0]), T(m.emissive[1]), T(m.emissive[2]));
+    if (max3(emis) > T(0)) {                                                       // materials_pbr.js:1014-1075 emitterHit
+        r.rad += r.beta * emis;
+        r.state = RAY_SOURCE;
+        move_by(r, r.dir * (otol * T(2)));
+        return;
+    }
+    T n0 = r.n;
+    T n1 = std::max(T(m.ior), n0);                                                 // ownMedium (materials_pbr.js:1080)
+    if (m.transmission > 0 && m.metallic < 1) {                                    // asksMedium (materials.js:114)
+        SceneHit<T> mb = scene_eval(*C.s, r.pos + (-nrm) * (otol * T(2)));         // mediumBeyond (tracebasics.js:1332)
+        n1 = T(C.s->materials[std::min(mb.a, C.s->n_materials - 1)].ior);
+    }
+    // A FACE THAT BOTH REFRACTS AND DIFFUSES, SEEN FROM INSIDE (materials_pbr.js:1150-1165): one part drawn
+    T pG = refract_share<T>(m);
+    T trans = T(m.transmission), specv = T(m.specular);
+    bool diffFace = false;
+    if (inside && pG > T(0) && pG < T(1)) {
+        T k = mixT(T(2) * T(m.specular), T(1), pG);
+        T u4[4]; rng.next4(u4);
+        if (u4[0] < pG) { trans = T(1); }
+        else { trans = T(0); specv = T(0.5) * k; diffFace = true; }
+    }
+    T etaFace = diffFace ? std::min(n0, n1) / std::max(n0, n1) : n0 / n1;
+    Lobes<T> lb = make_lobes(nrm, -r.dir, m, etaFace, C.tb, trans, specv);
+    lb.etaT = n0 / n1;
+
+    // LIGHT SAMPLING (materials_pbr.js:1196-1330): the environment only (no faces, no discovered emitters)
+    if (C.p.nee != 0 && !last) {
+        T u0[4], u1[4];
+        rng.next4(u0);                                                             // pick00
+        rng.next4(u1);                                                             // uL
+        if (!lobes_none<T>(m, trans)) {
+            T pick = u0[0];
+            V3<T> L = env_sample_dir(C.env, nrm, pick, u1[0], u1[1]);
+            T NoL = dot(nrm, L);
+            T pL = env_pdf(C.env, L, nrm);
+            if (NoL > T(0) && pL > T(0)) {
+                V3<T> le = C.env.radiance(L);
+                V3<T> f = lobes_eval(lb, L, T(0));
+                T pB = lobes_pdf(lb, L);
+                T w = mis_weight(pL, pB);
+                V3<T> contrib = r.beta * f * le * (std::fabs(NoL) * (w / pL));
+                if (max3(contrib) > T(1e-7)) {
+                    V3<T> o = r.pos + nrm * (otol * T(2));
+                    T tr = T(1);
+                    if (C.haze.on && std::fabs(r.n - T(1)) <= T(1e-3)) {                   // haze.js:472-485 hazeShadow
+                        T R = T(C.d.env_radius);
+                        tr = C.haze.transmittance(r.pos, L, T(2) * R + length(r.pos), R);
+                    }
+                    if (occlude(C, o, L, r.n, st)) deposit(fr, r.pix, contrib * tr, st);
+                }
+            }
+        }
+    }
+    // THE BOUNCE (materials_pbr.js:1332-1345)
+    T ur[4]; rng.next4(ur);
+    LobeSample<T> smp = lobes_sample(lb, ur);
+    r.dir = smp.dir;
+    r.beta *= smp.w;
+    if (smp.transmitted) r.n = n1;
+    if (max3(smp.w) <= T(0)) r.state = RAY_ABSORBED;
+    bool misOut = C.p.nee != 0 && !last;
+    if (misOut) {                                                                  // materials_pbr.js:1370-1395
+        bool above = dot(nrm, r.dir) > T(0) && !smp.isDelta;
+        T pOut = smp.isDelta ? T(0) : lobes_pdf(lb, smp.dir);
+        T pLout = above ? env_pdf(C.env, r.dir, nrm) : T(0);
+        r.sunmis = pLout <= T(0) ? T(1) : mis_weight(pOut, pLout);
+    } else {
+        r.sunmis = T(1);
+    }
+    move_by(r, r.dir * otol);
+    // pathEnd's tail (tracebasics.js:1040-1103): the bounce cap, Russian roulette
+    if (r.bounces > C.p.maxbounce) r.state = RAY_TERMINATED;
+    if (C.p.rr != 0 && r.bounces >= 3 && r.state == RAY_ACTIVE) {
+        T p = clampT(max3(r.beta), T(0.1), T(0.95));
+        T u[4]; rng.next4(u);
+        if (u[0] > p) r.state = RAY_TERMINATED;
+        else r.beta = r.beta / p;
+    }
+}
+
+// ------------------------------------------------------------------------------------------------------------
+// THE MEDIUM VERTEX -- core/haze.js:493-596 mediumVertex, mediumNee: a point in the dust, its light sample
+// (sun's cone or the uniform sphere, power heuristic against the phase function) and its phase-function draw
+// ------------------------------------------------------------------------------------------------------------
+template <class T>
+void medium_vertex(const Ctx<T>& C, Ray<T>& r, Rng& rng, bool last, Frame<T>& fr, Stats& st) {
+    r.state = RAY_ACTIVE;
+    r.bounces += 1;
+    T g = clampT(C.haze.g, T(-0.95), T(0.95));
+    V3<T> din = r.dir;
+    r.beta = r.beta * C.haze.albedo;
+    if (C.p.nee != 0 && !last) {
+        T u0[4], u1[4];
+        rng.next4(u0); rng.next4(u1);
+        V3<T> L = env_sample_dir_m(C.env, u0[0], u1[0], u1[1]);
+        T pL = env_pdf_m(C.env, L);
+        if (pL > T(0)) {
+            T ph = hg_eval(dot(din, L), g);
+            T w = mis_weight(pL, ph);
+            V3<T> le = C.env.radiance(L);
+            V3<T> contrib = r.beta * le * (ph * w / pL);
+            if (max3(contrib) > T(1e-7)) {
+                T R = T(C.d.env_radius);
+                T tr = C.haze.transmittance(r.pos, L, T(2) * R + length(r.pos), R);   // haze.js:472-485 hazeShadow
+                if (occlude(C, r.pos, L, r.n, st)) deposit(fr, r.pix, contrib * tr, st);
+            }
+        }
+    }
+    T u2[4]; rng.next4(u2);
+    V3<T> dout = hg_sample(din, g, u2[0], u2[1]);
+    r.dir = dout;
+    bool misOut = C.p.nee != 0 && !last;
+    if (misOut) {
+        T pB = hg_eval(dot(din, dout), g);
+        T pL = env_pdf_m(C.env, dout);
+        r.sunmis = pL <= T(0) ? T(1) : mis_weight(pB, pL);
+    } else {
+        r.sunmis = T(1);
+    }
+    if (r.bounces > C.p.maxbounce) r.state = RAY_TERMINATED;
+}
+
+template <class T>
+void trace_path(const Ctx<T>& C, U4 sseed, uint32_t tile, const st_view& v, uint32_t W, uint32_t H,
+                Frame<T>& fr, Stats& st) {
+    // genrays (genrays.js:26-97): the tile grid, one jittered ray through the tile
+    Rng rng0 = path_rng(sseed, tile, 0);
+    const double N = double(W) * double(H);
+    uint32_t tilesX = std::max<uint32_t>(1, (uint32_t)std::llround(std::sqrt(N * (double(W) / std::max<double>(1, H)))));
+    uint32_t tilesY = std::max<uint32_t>(1, (uint32_t)std::ceil(N / tilesX));
+    T invTX = T(float(1.0 / tilesX)), invTY = T(float(1.0 / tilesY));
+    T cx = T(tile % tilesX), cy = T(tile / tilesX);
+    T uv0x = (cx + T(0.5)) * invTX, uv0y = (cy + T(0.5)) * invTY;
+    T rnd[4]; rng0.next4(rnd);
+    T ux = clampT(uv0x + (rnd[0] - T(0.5)) * invTX, T(0), T(1));
+    T uy = clampT(uv0y + (rnd[1] - T(0.5)) * invTY, T(0), T(1));
+    T xx = ux * T(2) - T(1), yy = uy * T(2) - T(1);
+    V3<T> right(T(v.right[0]), T(v.right[1]), T(v.right[2])), up(T(v.up[0]), T(v.up[1]), T(v.up[2])),
+        fwd(T(v.fwd[0]), T(v.fwd[1]), T(v.fwd[2])), cam(T(v.cam_pos[0]), T(v.cam_pos[1]), T(v.cam_pos[2]));
+    Ray<T> r;
+    if (v.camtype == 0) {
+        V3<T> dc(xx * T(v.fx), yy * T(v.fy), T(-1));
+        r.dir = normalize(right * dc.x + up * dc.y + fwd * dc.z);
+        r.pos = cam;
+    } else {
+        r.pos = cam + right * (xx * T(v.fx)) + up * (yy * T(v.fy));
+        r.dir = -fwd;
+    }
+    r.dir = normalize(r.dir);                                                      // newRay (tracebasics.js:479-499)
+    r.beta = V3<T>(1); r.rad = V3<T>(0);
+    r.ltot = 0; r.n = 1; r.sunmis = 1; r.tmax = 0; r.absLtot = 0;
+    r.bounces = 0; r.steps = 0; r.state = RAY_ACTIVE;
+    T px = clampT(ux * T(W), T(0), T(W) - T(1)), py = clampT(uy * T(H), T(0), T(H) - T(1));
+    r.pix = (uint32_t)px + (uint32_t)py * W;
+
+    for (uint32_t it = 0; it < C.budget; it++) {
+        bool last = it + 1 == C.budget;
+        bool use_haze = C.haze.on;
+        if (use_haze && r.tmax == T(0)) {                                          // haze.js:255-273 hazeDraw
+            // from where the leg starts: the vertex, before the step off it (absLtot is the ltot on arrival there)
+            V3<T> A = r.pos - r.dir * (std::max(r.ltot - r.absLtot, T(0)) / std::max(r.n, T(1e-4)));
+            Rng hr = path_rng(sseed, tile, SEED_SALT_HAZE + it);
+            r.tmax = C.haze.draw(A, r.dir, r.absLtot, r.n, T(C.d.env_radius), hr);
+        }
+        T dh = march(C, r, st, use_haze);
+        st.segments++;
+        if (r.state == RAY_ESCAPED) {                                              // wavefront.js:1303-1320
+            r.rad += r.beta * C.env.radiance(r.dir) * r.sunmis;
+            break;
+        }
+        if (r.state != RAY_ACTIVE && r.state != RAY_SCATTER) break;                // out of steps or length
+        Rng rng = path_rng(sseed, tile, 1 + it);
+        r.absLtot = r.ltot;                                                        // absorbAlong on arrival
+        if (r.state == RAY_SCATTER) {
+            medium_vertex(C, r, rng, last, fr, st);
+        } else {
+            shade_hit(C, r, dh, rng, last, fr, st);
+        }
+        if (r.state != RAY_ACTIVE) break;
+        r.tmax = T(0);                                                             // a new leg (wavefront.js:1375-1380)
+        if (last) { r.state = RAY_MAXITER; st.flushed++; }                         // THE FLUSH (wavefront.js:949-968)
+    }
+    // THE PATH IS OVER (wavefront.js:1400-1425): its radiance into the frame, and it counts once
+    deposit(fr, r.pix, r.rad, st);
+#pragma omp atomic
+    fr.cnt[r.pix] += 1;
+    st.paths++;
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------------------------------------------------
+// extern "C"
+// ------------------------------------------------------------------------------------------------------------
+static MfTables g_tb_f, g_tb_d;
+static bool g_tb_f_ok = false, g_tb_d_ok = false;
+
+template <class T> static const MfTables* tables();
+template <> const MfTables* tables<float>() {
+    if (!g_tb_f_ok) { g_tb_f = build_mf_tables<float>(); g_tb_f_ok = true; }
+    return &g_tb_f;
+}
+template <> const MfTables* tables<double>() {
+    if (!g_tb_d_ok) { g_tb_d = build_mf_tables<double>(); g_tb_d_ok = true; }
+    return &g_tb_d;
+}
+
+template <class T>
+static int render_impl(const st_scene_desc* s, const st_params* p, const st_view* v, uint32_t sample0,
+                       uint32_t nsamples, double* acc_rgb, double* mV, double* mS, uint32_t* acc_cnt,
+                       uint64_t* counters, int threads, uint32_t path_first, uint32_t path_count) {
+    Ctx<T> C;
+    C.s = s; C.p = *p; C.d = derive(*p, *s);
+    C.env.init(*p, C.d);
+    C.tb = tables<T>();
+    C.tol = T(C.d.tol_setting);
+    C.envR2 = T(C.d.env_radius * C.d.env_radius);
+    C.stepscale = T(p->stepscale);
+    // THE ITERATION BUDGET IS THE WORST CASE (raytrace_main.js:1795-1815): a segment per bounce, and room for a
+    // path's steps-off-a-surface (a march chunk's worth each in the reference, ceil(maxiter / 32) of them)
+    C.budget = p->budget ? p->budget : std::max(2u, p->maxbounce + 1 + (p->maxiter + 31) / 32);
+    C.haze.init(*s);
+    const uint32_t W = p->width, H = p->height, P = W * H;
+    uint32_t pend = std::min(P, path_first + (path_count ? path_count : P));
+    Stats st;
+#ifdef _OPENMP
+    if (threads > 0) omp_set_num_threads(threads);
+#endif
+    Frame<T> fr;
+    fr.rgb.assign((size_t)P * 3, 0.0);
+    fr.cnt.assign(P, 0);
+    for (uint32_t si = 0; si < nsamples; si++) {
+        U4 sseed = sample_seed(p->seed, sample0 + si);
+        std::fill(fr.rgb.begin(), fr.rgb.end(), 0.0);
+        std::fill(fr.cnt.begin(), fr.cnt.end(), 0u);
+#pragma omp parallel for schedule(dynamic, 64)
+        for (long t = (long)path_first; t < (long)pend; t++) trace_path(C, sseed, (uint32_t)t, *v, W, H, fr, st);
+        // resolve (wavefront.js:414-494, measure.js:36-51) in double precision
+        for (uint32_t i = 0; i < P; i++) {
+            uint32_t n = fr.cnt[i];
+            if (n == 0) continue;
+            double s3[3] = {fr.rgb[i * 3] / n, fr.rgb[i * 3 + 1] / n, fr.rgb[i * 3 + 2] / n};
+            double prevn = p->maxaverages ? std::min<double>(acc_cnt[i], p->maxaverages) : double(acc_cnt[i]);
+            double cnt = prevn + 1;
+            acc_cnt[i] = (uint32_t)cnt;
+            double prev[3];
+            for (int c = 0; c < 3; c++) prev[c] = std::min(std::max(acc_rgb[i * 3 + c], -1e20), 1e20);
+            for (int c = 0; c < 3; c++) acc_rgb[i * 3 + c] = (prev[c] * prevn + s3[c]) / cnt;
+            double y = s3[0] * LUMA_R + s3[1] * LUMA_G + s3[2] * LUMA_B;
+            double w = 1.0 / cnt;
+            double d = prevn > 0 ? y - (prev[0] * LUMA_R + prev[1] * LUMA_G + prev[2] * LUMA_B) : 0.0;
+            double v0 = std::min(std::max(mV[i], 0.0), 1e300), s0 = std::min(std::max(mS[i], 0.0), 1.0);
+            mV[i] = (1 - w) * (v0 + w * d * d);
+            mS[i] = (1 - w) * (1 - w) * s0 + w * w;
+        }
+    }
+    if (counters) {
+        counters[0] += st.paths; counters[1] += st.segments; counters[2] += st.march_steps;
+        counters[3] += st.shadow_rays; counters[4] += st.shadow_steps; counters[5] += st.nonfinite;
+        counters[6] += st.flushed; counters[7] += st.shadowcut;
+    }
+    return 0;
+}
+
+extern "C" {
+
+// Render nsamples samples from sample0 on, folding each into the FP64 accumulation (caller-owned, continued across
+// calls). fp64: 0 the reference-equivalent f32 arithmetic, 1 the accuracy oracle. path_first/path_count restrict the
+// traced paths (a crop, for the CPU baseline's bounded sample); 0/0 = all.
+int sto_render(const st_scene_desc* s, const st_params* p, const st_view* v, uint32_t sample0, uint32_t nsamples,
+               int fp64, double* acc_rgb, double* mV, double* mS, uint32_t* acc_cnt, uint64_t* counters, int threads,
+               uint32_t path_first, uint32_t path_count) {
+    if (!s || !p || !v || !acc_rgb || !mV || !mS || !acc_cnt) return -1;
+    if (s->n_materials == 0 || s->n_prims == 0) return -1;
+    if (fp64)
+        return render_impl<double>(s, p, v, sample0, nsamples, acc_rgb, mV, mS, acc_cnt, counters, threads, path_first, path_count);
+    return render_impl<float>(s, p, v, sample0, nsamples, acc_rgb, mV, mS, acc_cnt, counters, threads, path_first, path_count);
+}
+
+int sto_mf_tables(int fp64, float* ec, float* ecavg, float* e1) {
+    const MfTables* t = fp64 ? tables<double>() : tables<float>();
+    std::memcpy(ec, t->ec.data(), t->ec.size() * 4);
+    std::memcpy(ecavg, t->ecavg.data(), t->ecavg.size() * 4);
+    std::memcpy(e1, t->e1.data(), t->e1.size() * 4);
+    return 0;
+}
+
+int sto_scene_sdf(const st_scene_desc* s, const float* pts, uint32_t n, float* d, uint32_t* mat, uint32_t* med) {
+    for (uint32_t i = 0; i < n; i++) {
+        SceneHit<double> h = scene_eval(*s, V3<double>(pts[3 * i], pts[3 * i + 1], pts[3 * i + 2]));
+        d[i] = (float)h.d;
+        if (mat) mat[i] = h.m;
+        if (med) med[i] = h.a;
+    }
+    return 0;
+}
+
+void sto_pcg4d(const uint32_t* in, uint32_t* out) {
+    U4 v = {in[0], in[1], in[2], in[3]};
+    v = pcg4d(v);
+    out[0] = v.x; out[1] = v.y; out[2] = v.z; out[3] = v.w;
+}
+
+// n draws of PRNG() after SEED_uvec4(seed4) and SEED_u32 of each of the k words (tracebasics.js:335-380)
+void sto_prng(const uint32_t* seed4, const uint32_t* words, int k, int n, float* out) {
+    Rng r; r.h = {seed4[0], seed4[1], seed4[2], seed4[3]};
+    for (int i = 0; i < k; i++) r.seed_u32(words[i]);
+    for (int i = 0; i < n; i++) r.next4(out + 4 * i);
+}
+
+void sto_sample_seed(uint32_t base, uint32_t sample, uint32_t* out) {
+    U4 s = sample_seed(base, sample);
+    out[0] = s.x; out[1] = s.y; out[2] = s.z; out[3] = s.w;
+}
+
+void sto_derive(const st_params* p, const st_scene_desc* s, double* out) {
+    Derived d = derive(*p, *s);
+    out[0] = d.sun_half; out[1] = d.sun_omc; out[2] = d.sun_sin2; out[3] = d.sun_omega; out[4] = d.disc_lum;
+    out[5] = d.sun_on; out[6] = d.nee_sun_pick; out[7] = d.tol_setting; out[8] = d.env_radius;
+    out[9] = d.sun_tint[0]; out[10] = d.sun_tint[1]; out[11] = d.sun_tint[2];
+}
+
+double sto_fresnel_dielectric(double cosI, double eta) { return fresnel_dielectric<double>(cosI, eta); }
+
+// lobesEval / lobesPdf of a material at normal (0,0,1) for view v and light l (double precision), for the tests
+void sto_lobes(const st_material* m, const double* v, const double* l, double eta, double* f, double* pdf) {
+    const MfTables* tb = tables<double>();
+    Lobes<double> lb = make_lobes(V3<double>(0, 0, 1), V3<double>(v[0], v[1], v[2]), *m, eta, tb);
+    V3<double> fv = lobes_eval(lb, V3<double>(l[0], l[1], l[2]), 0.0);
+    f[0] = fv.x; f[1] = fv.y; f[2] = fv.z;
+    *pdf = lobes_pdf(lb, V3<double>(l[0], l[1], l[2]));
+}
+
+// n draws of lobesSample for a material at normal (0,0,1), view v: directions (3n) and weights (3n)
+void sto_lobes_sample(const st_material* m, const double* v, double eta, uint32_t seed, int n, double* dirs, double* w) {
+    const MfTables* tb = tables<double>();
+    Lobes<double> lb = make_lobes(V3<double>(0, 0, 1), V3<double>(v[0], v[1], v[2]), *m, eta, tb);
+    Rng r; r.h = sample_seed(seed, 0);
+    for (int i = 0; i < n; i++) {
+        double u[4]; r.next4(u);
+        LobeSample<double> s = lobes_sample(lb, u);
+        dirs[3 * i] = s.dir.x; dirs[3 * i + 1] = s.dir.y; dirs[3 * i + 2] = s.dir.z;
+        w[3 * i] = s.w.x; w[3 * i + 1] = s.w.y; w[3 * i + 2] = s.w.z;
+    }
+}
+
+}  // extern "C"

@@ -1,0 +1,546 @@
+// TEST INFRASTRUCTURE ONLY -- the oracle's path tracer: scene SDF fold, environment, GGX/Fresnel lobes, next-event
+// estimation with MIS, march, occlusion, resolve. Restates the reference (lampmaker/ShadyTracer v0.88.0) file:line
+// by file:line; the product never includes or links this.
+#pragma once
+#include "st_oracle_core.h"
+#include "../include/shadytracer.h"
+
+namespace sto {
+
+// ------------------------------------------------------------------------------------------------------------
+// DERIVED UNIFORMS in double precision -- core/photometry.js:55-73 sunCone/discLuminance, :182-237 derive
+// ------------------------------------------------------------------------------------------------------------
+struct Derived {
+    double sun_half, sun_omc, sun_sin2, sun_omega, disc_lum;
+    double sun_tint[3];
+    double sun_dir[3];
+    int sun_on;
+    double nee_sun_pick;
+    double tol_setting;        // tolSetting(): eps, else the scene's
+    double env_radius;
+};
+inline Derived derive(const st_params& p, const st_scene_desc& s) {
+    Derived d;
+    double half = std::max((double)p.sun_diameter, 1e-3) * PI_D / 360.0;         // photometry.js:56
+    double sh = std::sin(half / 2);
+    d.sun_half = half;
+    d.sun_omc = 2 * sh * sh;                                                       // 1 - cos via 2 sin^2(h/2)
+    d.sun_sin2 = std::sin(half) * std::sin(half);
+    d.sun_omega = 2 * PI_D * d.sun_omc;
+    d.disc_lum = (double)p.sun_illuminance / (PI_D * std::sin(half) * std::sin(half));   // photometry.js:73
+    const double raw[3] = {1.0, 0.96, 0.9};                                        // photometry.js:43-44 SUN_TINT
+    double y = raw[0] * LUMA_R + raw[1] * LUMA_G + raw[2] * LUMA_B;
+    for (int i = 0; i < 3; i++) d.sun_tint[i] = raw[i] / y;
+    bool furnace = p.env_uniform > 0;
+    d.sun_on = (p.sun_hint != 0 && p.sun_elevation * PI_D / 180.0 + half > 0 && !furnace) ? 1 : 0;   // photometry.js:194
+    d.nee_sun_pick = (d.sun_on && p.env_sun_gain > 0) ? p.nee_sun_pick : 0.0;                        // photometry.js:226
+    d.tol_setting = p.eps > 0 ? p.eps : (s.tolerance > 0 ? s.tolerance : 1e-3);                     // photometry.js:141-150
+    d.env_radius = s.env_radius > 0 ? s.env_radius : 400.0;                                          // photometry.js:158
+    double e = p.sun_elevation * PI_D / 180.0, a = p.sun_azimuth * PI_D / 180.0;                      // sdf.js:74-78
+    d.sun_dir[0] = std::cos(e) * std::sin(a); d.sun_dir[1] = std::cos(e) * std::cos(a); d.sun_dir[2] = std::sin(e);
+    return d;
+}
+
+// ------------------------------------------------------------------------------------------------------------
+// THE TOLERANCE -- core/tolerances.js:27-37 marchTol; tracebasics.js:164-165 normalTol, offsetTol
+// ------------------------------------------------------------------------------------------------------------
+template <class T> inline T march_tol(const V3<T>& p, T setting) {
+    T f = T(128.0) * T(1.1920928955078125e-7) * std::max(std::fabs(p.x), std::max(std::fabs(p.y), std::fabs(p.z)));
+    return std::max(std::max(setting, T(1e-9)), f);
+}
+
+// ------------------------------------------------------------------------------------------------------------
+// PRIMITIVES -- core/sdf.js:214-256, :602 Ntorus; core/shapes.js:266-287 prism, :621-660 aspheric lens, :717 extrude
+// ------------------------------------------------------------------------------------------------------------
+template <class T> inline T sd_box(const V3<T>& p, const V3<T>& b) {
+    V3<T> q(std::fabs(p.x) - b.x, std::fabs(p.y) - b.y, std::fabs(p.z) - b.z);
+    return length(vmax(q, T(0))) + std::min(std::max(q.x, std::max(q.y, q.z)), T(0));
+}
+// g2RegularPolygon (shapes.js:266-283): the signed distance in the plane; only .z (the distance) is used here
+template <class T> inline T g2_regular_polygon(T qx, T qy, T sides, T R0) {
+    const T PI = T(PI_D);
+    T n = clampT(std::nearbyint(sides), T(3), T(64));
+    T R = std::max(R0, T(0));
+    T an = PI / n;
+    T a = R * std::cos(an), he = R * std::sin(an);
+    T k = std::nearbyint((std::atan2(qy, qx) + T(0.5) * PI) / (T(2) * an));
+    T phi = T(-0.5) * PI + T(2) * an * k;
+    T nkx = std::cos(phi), nky = std::sin(phi);
+    T tkx = -nky, tky = nkx;
+    T u = qx * nkx + qy * nky, v = qx * tkx + qy * tky;
+    if (u <= a) return u - a;
+    T ex = u - a, ey = v - clampT(v, -he, he);
+    return std::sqrt(ex * ex + ey * ey);
+}
+// g2Extrude's distance (shapes.js:717-726)
+template <class T> inline T g2_extrude(T pz, T gz, T h) {
+    T wz = std::fabs(pz) - h;
+    if (gz > T(0) && wz > T(0)) return std::sqrt(gz * gz + wz * wz);
+    if (gz > wz) return gz;
+    return wz;
+}
+// the aspheric lens (shapes.js:629-660), its distance bound
+template <class T> inline void asph_sag(T r, T c, T k, T a4, T a6, T& sag, T& slope) {
+    T r2 = r * r;
+    T w = T(1) - (T(1) + k) * c * c * r2;
+    T u = std::sqrt(std::max(w, T(1e-4)));
+    T poly = r2 * r2 * (a4 + r2 * a6);
+    T dpoly = r * r2 * (T(4) * a4 + r2 * (T(6) * a6));
+    sag = c * r2 / (T(1) + u) + poly;
+    slope = (w >= T(1e-4) ? c * r / u : T(2) * c * r / (T(1) + u)) + dpoly;
+}
+template <class T> inline T asph_slope_max(T rho, T c, T k, T a4, T a6) {
+    T r2 = rho * rho;
+    T u = std::sqrt(std::max(T(1) - (T(1) + k) * c * c * r2, T(1e-4)));
+    T poly = rho * r2 * (T(4) * std::fabs(a4) + r2 * (T(6) * std::fabs(a6)));
+    return std::fabs(c) * rho / u + poly;
+}
+template <class T> inline T asph_face(const V3<T>& p, T l, T rho, T ht, T R, T k, T a4, T a6, T s) {
+    T c = std::fabs(R) > T(1e-9) ? T(1) / R : T(0);
+    T sag, slope;
+    asph_sag(std::min(l, rho), c, k, a4, a6, sag, slope);
+    T m = asph_slope_max(rho, c, k, a4, a6);
+    return (s * p.z - ht + sag) / std::sqrt(T(1) + m * m);
+}
+template <class T> inline T sd_asphere(const V3<T>& p, const float* q) {
+    T rho = std::max(T(0.5) * T(q[0]), T(1e-6));
+    T l = std::sqrt(p.x * p.x + p.y * p.y);
+    T d = l - rho;
+    T top = asph_face(p, l, rho, T(0.5) * T(q[1]), T(q[2]), T(q[3]), T(q[4]), T(q[5]), T(1));
+    if (top > d) d = top;
+    T bot = asph_face(p, l, rho, T(0.5) * T(q[1]), T(q[6]), T(q[7]), T(q[8]), T(q[9]), T(-1));
+    if (bot > d) d = bot;
+    return d;
+}
+
+template <class T> inline T prim_sdf(const st_prim& pr, const V3<T>& pw) {
+    V3<T> d = pw - V3<T>(T(pr.pos[0]), T(pr.pos[1]), T(pr.pos[2]));
+    V3<T> q(T(pr.rot[0]) * d.x + T(pr.rot[1]) * d.y + T(pr.rot[2]) * d.z,
+            T(pr.rot[3]) * d.x + T(pr.rot[4]) * d.y + T(pr.rot[5]) * d.z,
+            T(pr.rot[6]) * d.x + T(pr.rot[7]) * d.y + T(pr.rot[8]) * d.z);
+    const float* p = pr.p;
+    switch (pr.type) {
+        case ST_PRIM_PLANE: return q.z;
+        case ST_PRIM_SPHERE: return length(q) - T(p[0]);                                            // sdf.js:217
+        case ST_PRIM_BOX: return sd_box(q, V3<T>(T(p[0]), T(p[1]), T(p[2])));                       // sdf.js:220
+        case ST_PRIM_ROUNDBOX: return sd_box(q, V3<T>(T(p[0]), T(p[1]), T(p[2]))) - T(p[3]);       // sdf.js:224
+        case ST_PRIM_TORUS: {                                                                        // sdf.js:602
+            T lxy = std::sqrt(q.x * q.x + q.y * q.y);
+            T a = lxy - T(p[0]);
+            return std::sqrt(a * a + q.z * q.z) - T(p[1]);
+        }
+        case ST_PRIM_PRISM: {                                                                        // shapes.js:285
+            T g = g2_regular_polygon(q.x, q.y, T(p[0]), T(p[1]));
+            return g2_extrude(q.z, g, std::max(T(0.5) * T(p[2]), T(0))) - T(p[3]);
+        }
+        case ST_PRIM_ASPHERE: return sd_asphere(q, p);                                               // shapes.js:651
+        case ST_PRIM_CYLINDER: {                                                                     // sdf.js:228
+            T lx = std::sqrt(q.x * q.x + q.y * q.y) - T(p[1]);
+            T lz = std::fabs(q.z) - T(p[0]);
+            T ox = std::max(lx, T(0)), oz = std::max(lz, T(0));
+            return std::min(std::max(lx, lz), T(0)) + std::sqrt(ox * ox + oz * oz);
+        }
+    }
+    return T(1e7);
+}
+
+// opSmoothUnion (sdf.js:252-256)
+template <class T> inline T smooth_union(T d1, T d2, T k) {
+    if (!(k > T(0))) return std::min(d1, d2);
+    T h = clampT(T(0.5) + T(0.5) * (d2 - d1) / k, T(0), T(1));
+    return mixT(d2, d1, h) - k * h * (T(1) - h);
+}
+
+// THE FOLD (core/scene_api.js:28-80 add_new / fold; emptyHit :93): the surface is the item of least |d|, the
+// medium the item the point is least deep inside (material 0 -- the air -- when none).
+template <class T> struct SceneHit { T d; uint32_t m; uint32_t a; T insideW; };
+template <class T> inline SceneHit<T> scene_eval(const st_scene_desc& s, const V3<T>& p) {
+    SceneHit<T> H{T(1e7), 0u, 0u, T(-1e7)};
+    uint32_t i = 0;
+    while (i < s.n_prims) {
+        const st_prim& pi = s.prims[i];
+        T di = prim_sdf(pi, p);
+        uint32_t mat = pi.material;
+        T near = std::fabs(di);
+        uint32_t j = i + 1;
+        while (j < s.n_prims && s.prims[j].op != ST_OP_ITEM) {
+            const st_prim& pj = s.prims[j];
+            T dj = prim_sdf(pj, p);
+            if (pj.op == ST_OP_SMOOTH) di = smooth_union(di, dj, T(pj.k));
+            else if (pj.op == ST_OP_UNION) di = std::min(di, dj);
+            else di = std::max(di, -dj);
+            if (pj.op != ST_OP_SUB && std::fabs(dj) < near) { near = std::fabs(dj); mat = pj.material; }
+            j++;
+        }
+        if (di < T(0) && di > H.insideW) { H.insideW = di; H.a = mat; }
+        if (std::fabs(di) < std::fabs(H.d)) { H.d = di; H.m = mat; }
+        i = j;
+    }
+    return H;
+}
+
+// ------------------------------------------------------------------------------------------------------------
+// THE ENVIRONMENT -- core/sdf.js:70-160 (inSunDisc, envBase, skyRadiance, sampleSunCone, envRadiance,
+// skyLuminance). The environment's code (core/environment.js: "THE ENVIRONMENT IS CODE") is the scene's: here a
+// sun disc of the set illuminance (photometry.js discLuminance, SUN_TINT) over a uniform sky above the horizon and
+// a uniform ground below it; env_uniform > 0 is the white-furnace environment (sdf.js:124-127).
+// ------------------------------------------------------------------------------------------------------------
+template <class T> struct Env {
+    V3<T> sun_dir; T sun_sin2, sun_omc, sun_omega; int sun_on; T pick;
+    V3<T> disc; T sky, ground, uniform, sun_gain, sky_gain;
+    void init(const st_params& p, const Derived& d) {
+        sun_dir = V3<T>(T(d.sun_dir[0]), T(d.sun_dir[1]), T(d.sun_dir[2]));
+        sun_sin2 = T(d.sun_sin2); sun_omc = T(d.sun_omc); sun_omega = T(d.sun_omega); sun_on = d.sun_on;
+        pick = T(d.nee_sun_pick);
+        disc = V3<T>(T(d.disc_lum * d.sun_tint[0]), T(d.disc_lum * d.sun_tint[1]), T(d.disc_lum * d.sun_tint[2]));
+        sky = T(p.sky_luminance); ground = T(p.ground_luminance); uniform = T(p.env_uniform);
+        sun_gain = T(std::max(0.f, p.env_sun_gain)); sky_gain = T(std::max(0.f, p.env_sky_gain));
+    }
+    bool in_sun_disc(const V3<T>& dir) const {                       // sdf.js:91-96
+        V3<T> L = normalize(dir);
+        V3<T> c = cross(L, sun_dir);
+        return dot(L, sun_dir) > T(0) && dot(c, c) <= sun_sin2;
+    }
+    bool in_sun_cone(const V3<T>& dir) const { return sun_on && in_sun_disc(dir); }
+    V3<T> background(const V3<T>& dir) const {
+        if (in_sun_disc(dir)) return disc;
+        return V3<T>(dir.z > T(0) ? sky : ground);
+    }
+    V3<T> base(const V3<T>& dir) const {                             // sdf.js:121-130 envBase
+        if (uniform > T(0)) return V3<T>(uniform);
+        V3<T> c = background(normalize(dir));
+        return vmax(c, T(0));
+    }
+    V3<T> radiance(const V3<T>& dir) const {                         // sdf.js:180-182 envRadiance
+        return base(dir) * (in_sun_cone(dir) ? sun_gain : sky_gain);
+    }
+    V3<T> sample_sun_cone(T u0, T u1) const {                        // sdf.js:149-160
+        const V3<T>& sd = sun_dir;
+        T omc = u0 * sun_omc;
+        T cosT = T(1) - omc;
+        T sinT = std::sqrt(std::max(T(0), omc * (T(2) - omc)));
+        T phi = T(2) * T(PI_D) * u1;
+        V3<T> t = std::fabs(sd.x) > T(0.9) ? V3<T>(0, 1, 0) : V3<T>(1, 0, 0);
+        V3<T> b1 = normalize(cross(t, sd));
+        V3<T> b2 = cross(sd, b1);
+        return normalize(b1 * (std::cos(phi) * sinT) + b2 * (std::sin(phi) * sinT) + sd * cosT);
+    }
+};
+// sampleCosineHemi (tracebasics.js:655-665)
+template <class T> inline V3<T> sample_cosine_hemi(const V3<T>& n, T u0, T u1) {
+    T r = std::sqrt(u0);
+    T phi = T(2) * T(PI_D) * u1;
+    V3<T> t = std::fabs(n.x) > T(0.9) ? V3<T>(0, 1, 0) : V3<T>(1, 0, 0);
+    V3<T> b1 = normalize(cross(t, n));
+    V3<T> b2 = cross(n, b1);
+    return normalize(b1 * (r * std::cos(phi)) + b2 * (r * std::sin(phi)) + n * std::sqrt(std::max(T(0), T(1) - u0)));
+}
+// envSampleDir / envPdf (tracebasics.js:670-692), no environment map (envMapShare 0)
+template <class T> inline V3<T> env_sample_dir(const Env<T>& e, const V3<T>& n, T pick, T u0, T u1) {
+    if (pick < e.pick) return e.sample_sun_cone(u0, u1);
+    return sample_cosine_hemi(n, u0, u1);
+}
+template <class T> inline T env_pdf(const Env<T>& e, const V3<T>& L, const V3<T>& n) {
+    T pSun = e.in_sun_disc(L) ? T(1) / e.sun_omega : T(0);
+    T pCos = std::max(dot(L, n), T(0)) / T(PI_D);
+    return e.pick * pSun + (T(1) - e.pick) * pCos;
+}
+// power heuristic (tracebasics.js:695-699)
+template <class T> inline T mis_weight(T a, T b) { T a2 = a * a, b2 = b * b; return a2 / std::max(a2 + b2, T(1e-20)); }
+
+// ------------------------------------------------------------------------------------------------------------
+// MICROFACET -- core/microfacet.js:72-140 (GGX, Smith, VNDF by spherical caps, exact Fresnel, Schlick) and the
+// albedo tables, :143-330 (prog_mf_lut, prog_mf_lut_avg, the isotropic Ec / Ec_avg / E1 and their reads)
+// ------------------------------------------------------------------------------------------------------------
+const int MF_NMU = 32, MF_NR = 32, MF_NIOR = 16, MF_SQRT_SAMPLES = 32;
+const double ALPHA_MIN = 1e-3;
+template <class T> inline T mf_lambda(const V3<T>& w, T a) {
+    T z2 = std::max(w.z * w.z, T(1e-12));
+    T t2 = (a * a * w.x * w.x + a * a * w.y * w.y) / z2;
+    return T(0.5) * (T(-1) + std::sqrt(T(1) + t2));
+}
+template <class T> inline T mf_g1(const V3<T>& w, T a) { return T(1) / (T(1) + mf_lambda(w, a)); }
+template <class T> inline T mf_g2(const V3<T>& o, const V3<T>& i, T a) { return T(1) / (T(1) + mf_lambda(o, a) + mf_lambda(i, a)); }
+template <class T> inline T mf_d(const V3<T>& h, T a) {
+    if (h.z <= T(0)) return T(0);
+    T t = (h.x * h.x) / (a * a) + (h.y * h.y) / (a * a) + h.z * h.z;
+    return T(1) / (T(PI_D) * a * a * t * t);
+}
+template <class T> inline V3<T> mf_sample_vndf(const V3<T>& o, T a, T u0, T u1) {
+    V3<T> os = normalize(V3<T>(o.x * a, o.y * a, o.z));
+    T phi = T(2) * T(PI_D) * u0;
+    T z = (T(1) - u1) * (T(1) + os.z) - os.z;
+    T sinT = std::sqrt(clampT(T(1) - z * z, T(0), T(1)));
+    V3<T> c(sinT * std::cos(phi), sinT * std::sin(phi), z);
+    V3<T> hs = c + os;
+    return normalize(V3<T>(hs.x * a, hs.y * a, std::max(hs.z, T(1e-7))));
+}
+template <class T> inline T mf_pdf_reflect(const V3<T>& o, const V3<T>& i, T a) {
+    if (o.z <= T(0) || i.z <= T(0)) return T(0);
+    V3<T> h = normalize(o + i);
+    return mf_g1(o, a) * mf_d(h, a) / (T(4) * o.z);
+}
+template <class T> inline T fresnel_dielectric(T cosI_in, T eta) {
+    T cosI = clampT(cosI_in, T(0), T(1));
+    T sin2T = eta * eta * (T(1) - cosI * cosI);
+    if (sin2T >= T(1)) return T(1);
+    T cosT = std::sqrt(T(1) - sin2T);
+    T rs = (eta * cosI - cosT) / (eta * cosI + cosT);
+    T rp = (cosI - eta * cosT) / (cosI + eta * cosT);
+    return T(0.5) * (rs * rs + rp * rp);
+}
+template <class T> inline V3<T> fresnel_schlick3(T cosI, const V3<T>& f0) {
+    T m = T(1) - clampT(cosI, T(0), T(1));
+    T m5 = m * m * m * m * m;
+    return f0 + (V3<T>(1) - f0) * m5;
+}
+
+struct MfTables {
+    std::vector<float> ec, ecavg, e1;   // [ior][r][mu], [ior][r], [r][mu]
+};
+// prog_mf_lut / prog_mf_lut_avg (microfacet.js:245-330), isotropic part, one entry at a time in T precision
+template <class T> inline MfTables build_mf_tables() {
+    MfTables t;
+    t.ec.resize(MF_NIOR * MF_NR * MF_NMU); t.ecavg.resize(MF_NIOR * MF_NR); t.e1.resize(MF_NR * MF_NMU);
+    auto entry = [](T ior, int k, int j, bool isE1) -> T {
+        T r = T(k) / T(MF_NR - 1);
+        T mu = (T(j) + T(0.5)) / T(MF_NMU);
+        T st = std::sqrt(std::max(T(0), T(1) - mu * mu));
+        T a = std::max(r * r, T(ALPHA_MIN));
+        V3<T> o(st, 0, mu);
+        T acc = 0;
+        for (int sy = 0; sy < MF_SQRT_SAMPLES; sy++)
+            for (int sx = 0; sx < MF_SQRT_SAMPLES; sx++) {
+                T vx = (T(sx) + T(0.5)) / T(MF_SQRT_SAMPLES), vy = (T(sy) + T(0.5)) / T(MF_SQRT_SAMPLES);
+                T ux = vx, uy = T(1) - (T(1) - vy) * (T(1) - vy);
+                V3<T> h = mf_sample_vndf(o, a, ux, uy);
+                V3<T> i3 = reflectv(-o, h);
+                if (i3.z > T(0)) {
+                    T fr = isE1 ? T(1) : fresnel_dielectric(dot(o, h), T(1) / ior);
+                    acc += T(2) * (T(1) - vy) * fr * mf_g2(o, i3, a) / mf_g1(o, a);
+                }
+            }
+        return acc / T(MF_SQRT_SAMPLES * MF_SQRT_SAMPLES);
+    };
+    for (int e = 0; e < MF_NIOR * MF_NR * MF_NMU; e++) {
+        T ior = T(1) + T(2) * T(e / (MF_NR * MF_NMU)) / T(MF_NIOR - 1);
+        t.ec[e] = (float)entry(ior, (e / MF_NMU) % MF_NR, e % MF_NMU, false);
+    }
+    for (int e = 0; e < MF_NR * MF_NMU; e++) t.e1[e] = (float)entry(T(1), e / MF_NMU, e % MF_NMU, true);
+    for (int e = 0; e < MF_NIOR * MF_NR; e++) {
+        T acc = 0;
+        for (int j = 0; j < MF_NMU; j++) {
+            T mu = (T(j) + T(0.5)) / T(MF_NMU);
+            acc += T(2) * T(t.ec[e * MF_NMU + j]) * mu / T(MF_NMU);
+        }
+        t.ecavg[e] = (float)acc;
+    }
+    return t;
+}
+// the reads (microfacet.js:152-240): linear in every axis, clamped at the ends
+template <class T> inline void mf_axis(T x, int n, T& i0, T& f) {
+    T c = clampT(x, T(0), T(n - 1));
+    i0 = std::min(std::floor(c), T(n - 2));
+    f = c - i0;
+}
+template <class T> inline T mf_ec(const MfTables& tb, T mu, T r, T n) {
+    T m0, mf, r0, rf, n0, nf;
+    mf_axis(mu * T(MF_NMU) - T(0.5), MF_NMU, m0, mf);
+    mf_axis(r * T(MF_NR - 1), MF_NR, r0, rf);
+    mf_axis((n - T(1)) * T(MF_NIOR - 1) / T(2), MF_NIOR, n0, nf);
+    T acc = 0;
+    for (int c = 0; c < 8; c++) {
+        int di = c & 1, dk = (c >> 1) & 1, dj = (c >> 2) & 1;
+        T w = (di ? nf : T(1) - nf) * (dk ? rf : T(1) - rf) * (dj ? mf : T(1) - mf);
+        int idx = (((int)n0 + di) * MF_NR + (int)r0 + dk) * MF_NMU + (int)m0 + dj;
+        acc += w * T(tb.ec[idx]);
+    }
+    return acc;
+}
+template <class T> inline T mf_ecavg(const MfTables& tb, T r, T n) {
+    T r0, rf, n0, nf;
+    mf_axis(r * T(MF_NR - 1), MF_NR, r0, rf);
+    mf_axis((n - T(1)) * T(MF_NIOR - 1) / T(2), MF_NIOR, n0, nf);
+    T acc = 0;
+    for (int c = 0; c < 4; c++) {
+        int di = c & 1, dk = (c >> 1) & 1;
+        T w = (di ? nf : T(1) - nf) * (dk ? rf : T(1) - rf);
+        acc += w * T(tb.ecavg[((int)n0 + di) * MF_NR + (int)r0 + dk]);
+    }
+    return acc;
+}
+template <class T> inline T mf_e1(const MfTables& tb, T mu, T r) {
+    T m0, mf, r0, rf;
+    mf_axis(mu * T(MF_NMU) - T(0.5), MF_NMU, m0, mf);
+    mf_axis(r * T(MF_NR - 1), MF_NR, r0, rf);
+    T acc = 0;
+    for (int c = 0; c < 4; c++) {
+        int dk = c & 1, dj = (c >> 1) & 1;
+        T w = (dk ? rf : T(1) - rf) * (dj ? mf : T(1) - mf);
+        acc += w * T(tb.e1[((int)r0 + dk) * MF_NMU + (int)m0 + dj]);
+    }
+    return acc;
+}
+
+// ------------------------------------------------------------------------------------------------------------
+// THE LOBES -- core/materials_pbr.js:164-275 makeLobes, :296-350 lobesEval/lobesPdf, :352-358 interfaceReflectP,
+// :450-596 lobesSample; isotropic, uncoated, no haze share (transl 0): what the hot path's materials use.
+// ------------------------------------------------------------------------------------------------------------
+const uint32_t EV_NONE = 0, EV_DELTA = 1, EV_EVAL = 2, EV_OTHER = 3;
+const double LT_MIN_ALPHA = 0.05;
+template <class T> struct Lobes {
+    V3<T> tX, tY, nZ, o, base, transTint, coatK, cm, ecO, ecAvg;
+    T a, aMin, r, metallic, trans, eta, etaT, nrel, ps;
+    bool isDelta;
+    const MfTables* tb;
+    V3<T> to_local(const V3<T>& w) const { return V3<T>(dot(w, tX), dot(w, tY), dot(w, nZ)); }
+    V3<T> to_world(const V3<T>& w) const { return normalize(tX * w.x + tY * w.y + nZ * w.z); }
+    V3<T> coat_fresnel(T cosI) const { return vmin(coatK * fresnel_dielectric(cosI, eta), T(1)); }
+    V3<T> metal_fresnel(T cosI) const { return fresnel_schlick3(cosI, base); }
+    V3<T> coat_albedo(const V3<T>& w) const { return vmin(coatK * mf_ec(*tb, w.z, r, nrel), T(1)); }
+};
+template <class T> inline T refract_share(const st_material& m) { return sat(T(m.transmission)); }
+template <class T> inline Lobes<T> make_lobes(const V3<T>& n, const V3<T>& v, const st_material& m, T eta,
+                                              const MfTables* tb, T transmission_override = T(-1), T specular_override = T(-1)) {
+    Lobes<T> lb;
+    lb.tb = tb;
+    // mtlOrthonormalBasis (materials_pbr.js:13-19)
+    V3<T> s = std::fabs(n.z) < T(0.999) ? normalize(cross(n, V3<T>(0, 0, 1))) : normalize(cross(n, V3<T>(0, 1, 0)));
+    V3<T> t = cross(s, n);
+    lb.tX = s; lb.tY = t; lb.nZ = n;
+    lb.o = V3<T>(dot(v, lb.tX), dot(v, lb.tY), std::max(dot(v, n), T(1e-4)));
+    lb.r = clampT(T(m.roughness), T(0), T(1));
+    T aIso = lb.r * lb.r;
+    lb.isDelta = aIso < T(ALPHA_MIN);
+    lb.aMin = aIso;
+    lb.a = clampT(aIso, T(ALPHA_MIN), T(1));
+    lb.metallic = sat(T(m.metallic));
+    T transm = transmission_override >= T(0) ? transmission_override : T(m.transmission);
+    T spec = specular_override >= T(0) ? specular_override : T(m.specular);
+    lb.trans = sat(transm);
+    lb.base = V3<T>(T(m.base[0]), T(m.base[1]), T(m.base[2]));
+    lb.transTint = m.attenuation > 0 ? V3<T>(1) : lb.base;
+    T lum = max3(lb.base);
+    V3<T> tint = lum > T(0) ? lb.base / std::max(lum, T(1e-6)) : V3<T>(1);
+    T st = T(m.specular_tint);
+    V3<T> tintMix = V3<T>(1) * (T(1) - st) + tint * st;
+    lb.coatK = tintMix * mixT(T(2) * spec, T(1), lb.trans);
+    lb.eta = eta; lb.etaT = eta;
+    lb.nrel = clampT(T(1) / eta, T(1), T(3));
+    // coatPs (materials_pbr.js:275-279)
+    T fo = max3(lb.coat_fresnel(lb.o.z));
+    lb.ps = std::min(fo, fresnel_dielectric(lb.o.z, lb.eta) >= T(1) ? T(1) : T(0.999));
+    lb.ecO = lb.coat_albedo(lb.o);
+    T e1 = lb.metallic > T(0) ? mf_e1(*tb, lb.o.z, lb.r) : T(1);
+    T eAvg = mf_ecavg(*tb, lb.r, lb.nrel);
+    lb.ecAvg = vmin(lb.coatK * eAvg, T(1));
+    lb.cm = V3<T>(1) + lb.base * (T(1) / std::max(e1, T(1e-3)) - T(1));
+    return lb;
+}
+template <class T> inline V3<T> lobes_eval(const Lobes<T>& lb, const V3<T>& l, T minAlpha) {
+    V3<T> i = lb.to_local(l);
+    if (i.z <= T(0)) return V3<T>(0);
+    V3<T> f(0);
+    if (!lb.isDelta && lb.aMin >= minAlpha) {
+        V3<T> h = normalize(lb.o + i);
+        T spec = mf_d(h, lb.a) * mf_g2(lb.o, i, lb.a) / (T(4) * lb.o.z * i.z);
+        T oh = dot(lb.o, h);
+        f += lb.cm * lb.metal_fresnel(oh) * (lb.metallic * spec);
+        f += lb.coat_fresnel(oh) * ((T(1) - lb.metallic) * spec);
+    }
+    T wDiff = (T(1) - lb.metallic) * (T(1) - lb.trans);
+    if (wDiff > T(0)) {
+        V3<T> ecI = lb.coat_albedo(i);
+        V3<T> den = vmax(V3<T>(1) - lb.ecAvg, T(1e-4)) * T(PI_D);
+        f += lb.base * (V3<T>(1) - lb.ecO) * (V3<T>(1) - ecI) / den * wDiff;
+    }
+    return f;
+}
+template <class T> inline T interface_reflect_p(const Lobes<T>& lb, T oh) {
+    T fh = max3(lb.coat_fresnel(oh));
+    T den = fh + (T(1) - fh) * lb.trans;
+    return den > T(1e-6) ? fh / den : T(1);
+}
+template <class T> inline T lobes_pdf(const Lobes<T>& lb, const V3<T>& l) {
+    V3<T> i = lb.to_local(l);
+    if (i.z <= T(0)) return T(0);
+    T wd = T(1) - lb.metallic;
+    T pd = (T(1) - lb.ps) * (T(1) - lb.trans);
+    T p = wd * pd * i.z / T(PI_D);
+    if (!lb.isDelta) {
+        T pr = mf_pdf_reflect(lb.o, i, lb.a);
+        p += (lb.metallic + wd * (T(1) - pd) * interface_reflect_p(lb, dot(lb.o, normalize(lb.o + i)))) * pr;
+    }
+    return p;
+}
+// lobesNone (materials_pbr.js:325-328)
+template <class T> inline bool lobes_none(const st_material& m, T transmission) {
+    T r = clampT(T(m.roughness), T(0), T(1));
+    return r * r < T(ALPHA_MIN) && (T(1) - sat(T(m.metallic))) * (T(1) - sat(transmission)) <= T(0);
+}
+template <class T> struct LobeSample { V3<T> dir, w; uint32_t ev; bool isDelta, transmitted; };
+template <class T> inline LobeSample<T> lobes_sample(const Lobes<T>& lb, const T rnd[4]) {
+    LobeSample<T> s;
+    s.w = V3<T>(0); s.ev = EV_OTHER; s.isDelta = false; s.transmitted = false;
+    V3<T> i(0, 0, 1);
+    uint32_t glossyEv = lb.aMin >= T(LT_MIN_ALPHA) ? EV_EVAL : EV_OTHER;
+    T wd = T(1) - lb.metallic;
+    T pick = rnd[0];
+    if (pick < lb.metallic) {                                                  // metal
+        if (lb.isDelta) {
+            i = V3<T>(-lb.o.x, -lb.o.y, lb.o.z);
+            s.w = lb.metal_fresnel(lb.o.z) * lb.cm;
+            s.ev = EV_DELTA; s.isDelta = true;
+        } else {
+            V3<T> h = mf_sample_vndf(lb.o, lb.a, rnd[1], rnd[2]);
+            i = reflectv(-lb.o, h);
+            if (i.z > T(0)) s.w = lb.cm * lb.metal_fresnel(dot(lb.o, h)) * (mf_g2(lb.o, i, lb.a) / mf_g1(lb.o, lb.a));
+            s.ev = glossyEv;
+        }
+    } else {
+        pick = (pick - lb.metallic) / std::max(wd, T(1e-6));
+        T pd = (T(1) - lb.ps) * (T(1) - lb.trans);
+        if (pick < T(1) - pd) {
+            T sub = pick / std::max(T(1) - pd, T(1e-6));
+            if (lb.isDelta) {
+                if (sub < lb.ps / std::max(T(1) - pd, T(1e-6))) {                    // mirror coat
+                    i = V3<T>(-lb.o.x, -lb.o.y, lb.o.z);
+                    s.w = lb.coat_fresnel(lb.o.z) / lb.ps;
+                } else {                                                             // clear refraction
+                    s.transmitted = true;
+                    i = refractv(-lb.o, V3<T>(0, 0, 1), lb.etaT);
+                    if (i.z < T(0)) s.w = (V3<T>(1) - lb.coat_fresnel(lb.o.z)) * lb.transTint / (T(1) - lb.ps);
+                }
+                s.ev = EV_DELTA; s.isDelta = true;
+            } else {
+                V3<T> h = mf_sample_vndf(lb.o, lb.a, rnd[1], rnd[2]);
+                T oh = dot(lb.o, h);
+                V3<T> fc = lb.coat_fresnel(oh);
+                T r = interface_reflect_p(lb, oh);
+                if (sub < r) {                                                       // glossy coat
+                    i = reflectv(-lb.o, h);
+                    if (i.z > T(0)) s.w = fc * (mf_g2(lb.o, i, lb.a) / mf_g1(lb.o, lb.a) / ((T(1) - pd) * r));
+                    s.ev = glossyEv;
+                } else {                                                             // rough refraction
+                    s.transmitted = true;
+                    i = refractv(-lb.o, h, lb.etaT);
+                    if (i.z < T(0))
+                        s.w = (V3<T>(1) - fc) * lb.transTint *
+                              (lb.trans * mf_g2(lb.o, i, lb.a) / mf_g1(lb.o, lb.a) / ((T(1) - pd) * (T(1) - r)));
+                    s.ev = lb.aMin >= T(LT_MIN_ALPHA) ? EV_EVAL : EV_OTHER;
+                }
+            }
+        } else {                                                                     // diffuse base
+            T r = std::sqrt(rnd[1]);
+            T phi = T(2) * T(PI_D) * rnd[2];
+            i = V3<T>(r * std::cos(phi), r * std::sin(phi), std::sqrt(std::max(T(0), T(1) - rnd[1])));
+            V3<T> ecI = lb.coat_albedo(i);
+            s.w = lb.base * (V3<T>(1) - lb.ecO) * (V3<T>(1) - ecI) / vmax(V3<T>(1) - lb.ecAvg, T(1e-4)) / (T(1) - lb.ps);
+            s.ev = EV_EVAL;
+        }
+    }
+    s.dir = lb.to_world(i);
+    return s;
+}
+
+}  // namespace sto

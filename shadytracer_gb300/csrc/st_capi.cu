@@ -1,0 +1,625 @@
+// st_capi.cu -- the C ABI of libshadytracer.so (include/shadytracer.h): the context, the scene / settings / camera,
+// the wave's device buffers, and the per-sample launch chain.
+//
+// A SAMPLE, AS THE HOST RUNS IT (the reference's R.trace, core/raytrace_main.js:1574-2300): genrays, then `budget`
+// wavefront iterations of march -> shade -> occlude, then resolve. Nothing is read back inside it; every kernel
+// sizes itself from the device counters, so the chain is recorded once into a CUDA graph per (scene, settings,
+// wave size) and replayed per wave -- the sample index the kernels seed from lives in device memory and resolve
+// advances it. A WAVE holds several samples of a small picture at once (samples_per_wave), so a 256 x 256 image
+// still puts two million paths in flight; a 1080p one runs one sample a wave.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "st_internal.h"
+#include "st_ext.h"
+
+using namespace st;
+
+namespace {
+struct KTimeAcc { std::string name; uint32_t launches = 0; double ms = 0; };
+struct PendingEvent { int idx; cudaEvent_t a, b; };
+const double PI_D = 3.14159265358979323846;
+}  // namespace
+
+struct st_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    int sms = 1;
+    std::string err;
+    // the scene
+    std::vector<st_prim> prims;
+    std::vector<st_material> mats;
+    st_scene_desc desc{};
+    bool has_scene = false, has_params = false, has_view = false;
+    st_prim* d_prims = nullptr;
+    st_material* d_mats = nullptr;
+    st_params params{};
+    st_view view{};
+    // the albedo tables
+    float *d_ec = nullptr, *d_ecavg = nullptr, *d_e1 = nullptr;
+    // the wave
+    uint32_t W = 0, H = 0, P = 0, spw = 0, slot_cap = 0;
+    PathBuf pb{};
+    Queues q{};
+    DevCtr* d_ctr = nullptr;
+    float4* d_frame = nullptr;
+    Acc4* d_acc = nullptr;
+    double2* d_mom = nullptr;
+    uint32_t samples = 0;
+    bool in_flight = false;
+    // the launch chain as a graph, per wave size
+    cudaGraphExec_t graph = nullptr;
+    uint32_t graph_w = 0;
+    bool graph_ok = true;
+    // per-kernel timing (core/kerneltime.js's role): CUDA events on this stream around each launch, when on
+    bool timing = false;
+    std::vector<KTimeAcc> ktimes;
+    std::vector<PendingEvent> pending;
+    std::vector<cudaEvent_t> event_pool;
+    StExt ext;   // the photon map's and the optics bench's state (st_sppm.cu, st_optics.cu)
+};
+
+static int fail(st_ctx* c, int code, const std::string& msg) {
+    if (c) c->err = msg;
+    return code;
+}
+static int cuda_fail(st_ctx* c, cudaError_t e, const char* what) {
+    return fail(c, e == cudaErrorMemoryAllocation ? ST_ERR_OOM : ST_ERR_CUDA,
+                std::string(what) + ": " + cudaGetErrorString(e));
+}
+#define CK(call, what)                                         \
+    do {                                                       \
+        cudaError_t e_ = (call);                               \
+        if (e_ != cudaSuccess) return cuda_fail(ctx, e_, what); \
+    } while (0)
+
+static void free_wave(st_ctx* ctx) {
+    void* ptrs[] = {ctx->pb.pos, ctx->pb.dir, ctx->pb.beta, ctx->pb.rad, ctx->pb.meta, ctx->q.ray[0], ctx->q.ray[1],
+                    ctx->q.hit, ctx->q.hitd, ctx->q.s_org, ctx->q.s_dir, ctx->q.s_rad, ctx->d_frame,
+                    ctx->d_acc, ctx->d_mom};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    ctx->pb = PathBuf{};
+    ctx->q = Queues{};
+    ctx->d_frame = nullptr;
+    ctx->d_acc = nullptr;
+    ctx->d_mom = nullptr;
+    ctx->slot_cap = 0;
+    if (ctx->graph) { cudaGraphExecDestroy(ctx->graph); ctx->graph = nullptr; ctx->graph_w = 0; }
+}
+
+static int time_index(st_ctx* ctx, const char* name) {
+    for (size_t i = 0; i < ctx->ktimes.size(); i++)
+        if (ctx->ktimes[i].name == name) return (int)i;
+    ctx->ktimes.push_back(KTimeAcc{name, 0, 0});
+    return (int)ctx->ktimes.size() - 1;
+}
+static cudaEvent_t take_event(st_ctx* ctx) {
+    if (!ctx->event_pool.empty()) {
+        cudaEvent_t e = ctx->event_pool.back();
+        ctx->event_pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    return e;
+}
+static void collect_times(st_ctx* ctx) {
+    for (auto& p : ctx->pending) {
+        float ms = 0;
+        if (cudaEventElapsedTime(&ms, p.a, p.b) == cudaSuccess) {
+            ctx->ktimes[p.idx].ms += ms;
+            ctx->ktimes[p.idx].launches++;
+        }
+        ctx->event_pool.push_back(p.a);
+        ctx->event_pool.push_back(p.b);
+    }
+    ctx->pending.clear();
+}
+
+// ------------------------------------------------------------------------------------------------------------
+// the uniforms, derived on the host in double precision (core/photometry.js:55-73 sunCone / discLuminance,
+// :182-237 derive), then rounded once
+// ------------------------------------------------------------------------------------------------------------
+static Uni make_uni(const st_ctx* ctx) {
+    const st_params& p = ctx->params;
+    const st_scene_desc& s = ctx->desc;
+    const st_view& v = ctx->view;
+    Uni u{};
+    u.W = p.width; u.H = p.height; u.P = p.width * p.height;
+    const double N = double(u.W) * double(u.H);
+    u.tilesX = std::max<uint32_t>(1, (uint32_t)std::llround(std::sqrt(N * (double(u.W) / std::max<double>(1, u.H)))));
+    u.tilesY = std::max<uint32_t>(1, (uint32_t)std::ceil(N / u.tilesX));
+    u.invTX = float(1.0 / u.tilesX);
+    u.invTY = float(1.0 / u.tilesY);
+    u.maxbounce = p.maxbounce; u.maxiter = p.maxiter; u.nee = p.nee; u.rr = p.rr;
+    // THE ITERATION BUDGET IS THE WORST CASE (core/raytrace_main.js:1795-1815): maxbounce + 1 + ceil(maxiter / 32)
+    u.budget = p.budget ? p.budget : std::max(2u, p.maxbounce + 1 + (p.maxiter + 31) / 32);
+    u.stepscale = p.stepscale;
+    double tol = p.eps > 0 ? p.eps : (s.tolerance > 0 ? s.tolerance : 1e-3);
+    double R = s.env_radius > 0 ? s.env_radius : 400.0;
+    u.tol = (float)tol;
+    u.envR = (float)R;
+    u.envR2 = (float)(R * R);
+    u.cam = mk(v.cam_pos[0], v.cam_pos[1], v.cam_pos[2]);
+    u.right = mk(v.right[0], v.right[1], v.right[2]);
+    u.up = mk(v.up[0], v.up[1], v.up[2]);
+    u.fwd = mk(v.fwd[0], v.fwd[1], v.fwd[2]);
+    u.fx = v.fx; u.fy = v.fy; u.camtype = v.camtype;
+    double half = std::max((double)p.sun_diameter, 1e-3) * PI_D / 360.0;
+    double sh = std::sin(half / 2);
+    double omc = 2 * sh * sh;
+    double sin2 = std::sin(half) * std::sin(half);
+    double disc = (double)p.sun_illuminance / (PI_D * sin2);
+    const double raw[3] = {1.0, 0.96, 0.9};
+    double y = raw[0] * 0.2126 + raw[1] * 0.7152 + raw[2] * 0.0722;
+    bool furnace = p.env_uniform > 0;
+    int sun_on = (p.sun_hint != 0 && p.sun_elevation * PI_D / 180.0 + half > 0 && !furnace) ? 1 : 0;
+    double e = p.sun_elevation * PI_D / 180.0, az = p.sun_azimuth * PI_D / 180.0;
+    u.sun_dir = mk((float)(std::cos(e) * std::sin(az)), (float)(std::cos(e) * std::cos(az)), (float)std::sin(e));
+    u.sun_sin2 = (float)sin2;
+    u.sun_omc = (float)omc;
+    u.sun_omega = (float)(2 * PI_D * omc);
+    u.pick = (float)((sun_on && p.env_sun_gain > 0) ? p.nee_sun_pick : 0.0);
+    u.sun_on = sun_on;
+    u.disc = mk((float)(disc * raw[0] / y), (float)(disc * raw[1] / y), (float)(disc * raw[2] / y));
+    u.sky = p.sky_luminance; u.ground = p.ground_luminance; u.uniform = p.env_uniform;
+    u.sun_gain = std::max(0.f, p.env_sun_gain); u.sky_gain = std::max(0.f, p.env_sky_gain);
+    u.haze_on = s.haze_sigma_t > 0 ? 1 : 0;
+    u.hc = mk(s.haze_centre[0], s.haze_centre[1], s.haze_centre[2]);
+    u.hu = mk(s.haze_axes[0], s.haze_axes[1], s.haze_axes[2]);
+    u.hv = mk(s.haze_axes[3], s.haze_axes[4], s.haze_axes[5]);
+    u.hw = mk(s.haze_axes[6], s.haze_axes[7], s.haze_axes[8]);
+    u.hhu = s.haze_half[0]; u.hhv = s.haze_half[1]; u.hhw = s.haze_half[2];
+    u.hsig = s.haze_sigma_t;
+    auto sat01 = [](float x) { return std::min(std::max(x, 0.f), 1.f); };
+    u.halb = mk(sat01(s.haze_albedo[0]), sat01(s.haze_albedo[1]), sat01(s.haze_albedo[2]));
+    u.hg = std::min(std::max(s.haze_g, -0.95f), 0.95f);
+    u.seed = p.seed; u.maxaverages = p.maxaverages;
+    u.n_prims = (uint32_t)ctx->prims.size();
+    u.n_mats = (uint32_t)ctx->mats.size();
+    return u;
+}
+
+static uint32_t samples_per_wave(const st_ctx* ctx) {
+    if (ctx->params.samples_per_wave) return ctx->params.samples_per_wave;
+    const uint32_t target = 2u << 20;   // about two million paths in flight fill 152 SMs several times over
+    uint32_t s = (target + ctx->P - 1) / ctx->P;
+    return std::max(1u, std::min(s, 64u));
+}
+
+static int ensure_wave(st_ctx* ctx) {
+    uint32_t spw = samples_per_wave(ctx);
+    uint32_t cap = spw * ctx->P;
+    bool pixels_changed = !ctx->d_acc;
+    if (ctx->slot_cap == cap && ctx->spw == spw && !pixels_changed) return ST_OK;
+    free_wave(ctx);
+    ctx->spw = spw;
+    size_t S = cap;
+    CK(cudaMalloc(&ctx->pb.pos, S * sizeof(float4)), "cudaMalloc path state");
+    CK(cudaMalloc(&ctx->pb.dir, S * sizeof(float4)), "cudaMalloc path state");
+    CK(cudaMalloc(&ctx->pb.beta, S * sizeof(float4)), "cudaMalloc path state");
+    CK(cudaMalloc(&ctx->pb.rad, S * sizeof(float4)), "cudaMalloc path state");
+    CK(cudaMalloc(&ctx->pb.meta, S * sizeof(uint4)), "cudaMalloc path state");
+    CK(cudaMalloc(&ctx->q.ray[0], S * 4), "cudaMalloc queues");
+    CK(cudaMalloc(&ctx->q.ray[1], S * 4), "cudaMalloc queues");
+    CK(cudaMalloc(&ctx->q.hit, S * 4), "cudaMalloc queues");
+    CK(cudaMalloc(&ctx->q.hitd, S * 4), "cudaMalloc queues");
+    CK(cudaMalloc(&ctx->q.s_org, S * sizeof(float4)), "cudaMalloc shadow queue");
+    CK(cudaMalloc(&ctx->q.s_dir, S * sizeof(float4)), "cudaMalloc shadow queue");
+    CK(cudaMalloc(&ctx->q.s_rad, S * sizeof(float4)), "cudaMalloc shadow queue");
+    CK(cudaMalloc(&ctx->d_frame, S * sizeof(float4)), "cudaMalloc frame");
+    CK(cudaMalloc(&ctx->d_acc, (size_t)ctx->P * sizeof(Acc4)), "cudaMalloc accumulation");
+    CK(cudaMalloc(&ctx->d_mom, (size_t)ctx->P * sizeof(double2)), "cudaMalloc moments");
+    ctx->q.cap = cap;
+    ctx->slot_cap = cap;
+    CK(cudaMemsetAsync(ctx->d_frame, 0, S * sizeof(float4), ctx->stream), "memset");
+    CK(cudaMemsetAsync(ctx->d_acc, 0, (size_t)ctx->P * sizeof(Acc4), ctx->stream), "memset");
+    CK(cudaMemsetAsync(ctx->d_mom, 0, (size_t)ctx->P * sizeof(double2), ctx->stream), "memset");
+    CK(cudaMemsetAsync(ctx->d_ctr, 0, sizeof(DevCtr), ctx->stream), "memset");
+    ctx->samples = 0;
+    return ST_OK;
+}
+
+static WaveArgs wave_args(st_ctx* ctx, uint32_t w) {
+    WaveArgs a;
+    a.u = make_uni(ctx);
+    a.prims = ctx->d_prims;
+    a.mats = ctx->d_mats;
+    a.tab = MfTab{ctx->d_ec, ctx->d_ecavg, ctx->d_e1};
+    a.pb = ctx->pb;
+    a.q = ctx->q;
+    a.ctr = ctx->d_ctr;
+    a.frame = ctx->d_frame;
+    a.acc = ctx->d_acc;
+    a.mom = ctx->d_mom;
+    a.spw = w;
+    a.slots = w * ctx->P;
+    return a;
+}
+
+// one wave's launch chain, onto the stream (recorded into a graph, or run directly when timing)
+static cudaError_t record_wave(st_ctx* ctx, const WaveArgs& a) {
+    cudaStream_t s = ctx->stream;
+    const bool T = ctx->timing;
+    auto timed = [&](const char* name, auto&& launch) -> cudaError_t {
+        if (!T) return launch();
+        PendingEvent pe{time_index(ctx, name), take_event(ctx), take_event(ctx)};
+        cudaEventRecord(pe.a, s);
+        cudaError_t e = launch();
+        cudaEventRecord(pe.b, s);
+        ctx->pending.push_back(pe);
+        return e;
+    };
+    cudaError_t e;
+    if ((e = launch_iter_begin(a, 1, 1, s))) return e;
+    if ((e = timed("genrays", [&] { return launch_genrays(a, ctx->sms, s); }))) return e;
+    int cur = 0;
+    for (uint32_t it = 0; it < a.u.budget; it++) {
+        int nxt = cur ^ 1;
+        int last = it + 1 == a.u.budget;
+        if (it > 0 && (e = launch_iter_begin(a, nxt, 0, s))) return e;
+        if ((e = timed("march", [&] { return launch_march(a, cur, (int)it, ctx->sms, s); }))) return e;
+        if ((e = timed("shade", [&] { return launch_shade(a, nxt, (int)it, last, ctx->sms, s); }))) return e;
+        if ((e = timed("occlude", [&] { return launch_occlude(a, ctx->sms, s); }))) return e;
+        cur = nxt;
+    }
+    return timed("resolve", [&] { return launch_resolve(a, s); });
+}
+
+static int run_wave(st_ctx* ctx, uint32_t w) {
+    WaveArgs a = wave_args(ctx, w);
+    if (ctx->timing || !ctx->graph_ok) {
+        CK(record_wave(ctx, a), "launch");
+    } else {
+        if (!ctx->graph || ctx->graph_w != w) {
+            if (ctx->graph) { cudaGraphExecDestroy(ctx->graph); ctx->graph = nullptr; }
+            cudaGraph_t g;
+            CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal), "capture");
+            cudaError_t e = record_wave(ctx, a);
+            cudaError_t e2 = cudaStreamEndCapture(ctx->stream, &g);
+            if (e != cudaSuccess || e2 != cudaSuccess) {
+                cudaGetLastError();
+                ctx->graph_ok = false;                       // fall back to direct launches, still on the GPU
+                CK(record_wave(ctx, a), "launch");
+                ctx->samples += w;
+                return ST_OK;
+            }
+            CK(cudaGraphInstantiate(&ctx->graph, g, 0), "graph instantiate");
+            cudaGraphDestroy(g);
+            ctx->graph_w = w;
+        }
+        CK(cudaGraphLaunch(ctx->graph, ctx->stream), "graph launch");
+    }
+    ctx->samples += w;
+    return ST_OK;
+}
+
+static void invalidate_graph(st_ctx* ctx) {
+    if (ctx->graph) { cudaGraphExecDestroy(ctx->graph); ctx->graph = nullptr; ctx->graph_w = 0; }
+}
+
+extern "C" {
+
+int st_abi_version(void) { return ST_ABI_VERSION; }
+
+const char* st_last_error(const st_ctx* ctx) { return ctx ? ctx->err.c_str() : "no context"; }
+
+int st_create(int device, st_ctx** out) {
+    if (!out) return ST_ERR_ARG;
+    *out = nullptr;
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) return ST_ERR_CUDA;
+    if (device < 0 || device >= n) return ST_ERR_ARG;
+    st_ctx* ctx = new st_ctx();
+    ctx->device = device;
+    cudaError_t e = cudaSetDevice(device);
+    if (e != cudaSuccess) { delete ctx; return ST_ERR_CUDA; }
+    cudaDeviceGetAttribute(&ctx->sms, cudaDevAttrMultiProcessorCount, device);
+    if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) { delete ctx; return ST_ERR_CUDA; }
+    const size_t NEC = 16 * 32 * 32, NAVG = 16 * 32, NE1 = 32 * 32;
+    if (cudaMalloc(&ctx->d_ec, NEC * 4) || cudaMalloc(&ctx->d_ecavg, NAVG * 4) || cudaMalloc(&ctx->d_e1, NE1 * 4) ||
+        cudaMalloc(&ctx->d_ctr, sizeof(DevCtr))) {
+        st_destroy(ctx);
+        return ST_ERR_OOM;
+    }
+    cudaMemsetAsync(ctx->d_ctr, 0, sizeof(DevCtr), ctx->stream);
+    if (launch_mf_tables(ctx->d_ec, ctx->d_ecavg, ctx->d_e1, ctx->stream) != cudaSuccess ||
+        cudaStreamSynchronize(ctx->stream) != cudaSuccess) {
+        st_destroy(ctx);
+        return ST_ERR_CUDA;
+    }
+    *out = ctx;
+    return ST_OK;
+}
+
+int st_destroy(st_ctx* ctx) {
+    if (!ctx) return ST_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    free_wave(ctx);
+    ext_free(ctx->ext);
+    for (void* p : {(void*)ctx->d_prims, (void*)ctx->d_mats, (void*)ctx->d_ec, (void*)ctx->d_ecavg,
+                    (void*)ctx->d_e1, (void*)ctx->d_ctr})
+        if (p) cudaFree(p);
+    for (auto& pe : ctx->pending) { cudaEventDestroy(pe.a); cudaEventDestroy(pe.b); }
+    for (auto e : ctx->event_pool) cudaEventDestroy(e);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return ST_OK;
+}
+
+int st_set_scene(st_ctx* ctx, const char* cuda_src, const st_scene_desc* d, char* errbuf, size_t errlen) {
+    if (!ctx) return ST_ERR_ARG;
+    auto refuse = [&](int code, const std::string& m) {
+        if (errbuf && errlen) { std::snprintf(errbuf, errlen, "%s", m.c_str()); }
+        return fail(ctx, code, m);
+    };
+    if (ctx->in_flight) return refuse(ST_ERR_BUSY, "a trace is in flight: st_sync first");
+    if (cuda_src) return refuse(ST_ERR_COMPILE, "this build takes scenes as primitive tables (cuda_src must be NULL)");
+    if (!d || !d->prims || !d->materials) return refuse(ST_ERR_ARG, "no scene table");
+    if (d->n_prims == 0 || d->n_prims > ST_MAX_PRIMS) return refuse(ST_ERR_ARG, "n_prims out of range (1..256)");
+    if (d->n_materials == 0 || d->n_materials > ST_MAX_MATERIALS) return refuse(ST_ERR_ARG, "n_materials out of range (1..256)");
+    if (d->prims[0].op != ST_OP_ITEM) return refuse(ST_ERR_ARG, "the first primitive must start an item (ST_OP_ITEM)");
+    for (uint32_t i = 0; i < d->n_prims; i++) {
+        if (d->prims[i].type > ST_PRIM_CYLINDER) return refuse(ST_ERR_ARG, "primitive " + std::to_string(i) + ": unknown type");
+        if (d->prims[i].op > ST_OP_SUB) return refuse(ST_ERR_ARG, "primitive " + std::to_string(i) + ": unknown op");
+        if (d->prims[i].material >= d->n_materials)
+            return refuse(ST_ERR_ARG, "primitive " + std::to_string(i) + ": material out of range");
+    }
+    if (!(d->env_radius >= 0) || !(d->tolerance >= 0)) return refuse(ST_ERR_ARG, "negative radius or tolerance");
+    cudaSetDevice(ctx->device);
+    std::vector<st_prim> prims(d->prims, d->prims + d->n_prims);
+    std::vector<st_material> mats(d->materials, d->materials + d->n_materials);
+    if (prims.size() > ctx->prims.size() || !ctx->d_prims) {
+        if (ctx->d_prims) cudaFree(ctx->d_prims);
+        ctx->d_prims = nullptr;
+        CK(cudaMalloc(&ctx->d_prims, ST_MAX_PRIMS * sizeof(st_prim)), "cudaMalloc scene");
+    }
+    if (!ctx->d_mats) CK(cudaMalloc(&ctx->d_mats, ST_MAX_MATERIALS * sizeof(st_material)), "cudaMalloc materials");
+    CK(cudaMemcpyAsync(ctx->d_prims, prims.data(), prims.size() * sizeof(st_prim), cudaMemcpyHostToDevice, ctx->stream), "scene upload");
+    CK(cudaMemcpyAsync(ctx->d_mats, mats.data(), mats.size() * sizeof(st_material), cudaMemcpyHostToDevice, ctx->stream), "scene upload");
+    CK(cudaStreamSynchronize(ctx->stream), "scene upload");
+    ctx->prims = std::move(prims);
+    ctx->mats = std::move(mats);
+    ctx->desc = *d;
+    ctx->desc.prims = nullptr;
+    ctx->desc.materials = nullptr;
+    ctx->has_scene = true;
+    invalidate_graph(ctx);
+    return st_invalidate(ctx);
+}
+
+int st_set_params(st_ctx* ctx, const st_params* p, uint64_t* unknown_mask) {
+    if (!ctx || !p) return ST_ERR_ARG;
+    if (ctx->in_flight) return fail(ctx, ST_ERR_BUSY, "a trace is in flight: st_sync first");
+    if (unknown_mask) *unknown_mask = 0;
+    if (p->width == 0 || p->height == 0 || (uint64_t)p->width * p->height > (1u << 26))
+        return fail(ctx, ST_ERR_ARG, "picture size out of range");
+    if (p->maxbounce == 0 || p->maxbounce > 64) return fail(ctx, ST_ERR_ARG, "maxbounce out of range (1..64)");
+    if (p->maxiter == 0 || p->maxiter > 65535) return fail(ctx, ST_ERR_ARG, "maxiter out of range (1..65535)");
+    if (!(p->stepscale > 0 && p->stepscale <= 1)) return fail(ctx, ST_ERR_ARG, "stepscale out of range (0, 1]");
+    if (p->budget > 256) return fail(ctx, ST_ERR_ARG, "budget out of range (0..256)");
+    if (p->samples_per_wave > 1024) return fail(ctx, ST_ERR_ARG, "samples_per_wave out of range (0..1024)");
+    cudaSetDevice(ctx->device);
+    bool resize = p->width != ctx->params.width || p->height != ctx->params.height ||
+                  p->samples_per_wave != ctx->params.samples_per_wave || !ctx->has_params;
+    ctx->params = *p;
+    ctx->has_params = true;
+    ctx->W = p->width; ctx->H = p->height; ctx->P = p->width * p->height;
+    invalidate_graph(ctx);
+    if (resize) {
+        free_wave(ctx);
+        int rc = ensure_wave(ctx);
+        if (rc) return rc;
+    }
+    return st_invalidate(ctx);
+}
+
+int st_set_view(st_ctx* ctx, const st_view* v) {
+    if (!ctx || !v) return ST_ERR_ARG;
+    if (ctx->in_flight) return fail(ctx, ST_ERR_BUSY, "a trace is in flight: st_sync first");
+    ctx->view = *v;
+    ctx->has_view = true;
+    invalidate_graph(ctx);
+    return st_invalidate(ctx);
+}
+
+int st_invalidate(st_ctx* ctx) {
+    if (!ctx) return ST_ERR_ARG;
+    if (ctx->in_flight) return fail(ctx, ST_ERR_BUSY, "a trace is in flight: st_sync first");
+    if (!ctx->d_acc) return ST_OK;
+    cudaSetDevice(ctx->device);
+    CK(cudaMemsetAsync(ctx->d_acc, 0, (size_t)ctx->P * sizeof(Acc4), ctx->stream), "memset");
+    CK(cudaMemsetAsync(ctx->d_mom, 0, (size_t)ctx->P * sizeof(double2), ctx->stream), "memset");
+    CK(cudaMemsetAsync(ctx->d_frame, 0, (size_t)ctx->slot_cap * sizeof(float4), ctx->stream), "memset");
+    CK(cudaMemsetAsync(ctx->d_ctr, 0, sizeof(DevCtr), ctx->stream), "memset");
+    CK(cudaStreamSynchronize(ctx->stream), "invalidate");
+    ctx->samples = 0;
+    return ST_OK;
+}
+
+int st_step_async(st_ctx* ctx, int n) {
+    if (!ctx || n < 0) return ST_ERR_ARG;
+    if (!ctx->has_scene || !ctx->has_params || !ctx->has_view)
+        return fail(ctx, ST_ERR_STATE, "set a scene, the settings and the view first");
+    cudaSetDevice(ctx->device);
+    int rc = ensure_wave(ctx);
+    if (rc) return rc;
+    uint32_t left = (uint32_t)n;
+    while (left > 0) {
+        uint32_t w = std::min(left, ctx->spw);
+        rc = run_wave(ctx, w);
+        if (rc) return rc;
+        left -= w;
+    }
+    ctx->in_flight = n > 0;
+    return ST_OK;
+}
+
+int st_sync(st_ctx* ctx, int timeout_ms) {
+    if (!ctx) return ST_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    auto t0 = std::chrono::steady_clock::now();
+    for (;;) {
+        cudaError_t e = cudaStreamQuery(ctx->stream);
+        if (e == cudaSuccess) break;
+        if (e != cudaErrorNotReady) { ctx->in_flight = false; return cuda_fail(ctx, e, "trace"); }
+        if (timeout_ms >= 0) {
+            double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+            if (ms > timeout_ms) return fail(ctx, ST_ERR_TIMEOUT, "the trace did not finish in time");
+        }
+        std::this_thread::sleep_for(std::chrono::microseconds(50));
+    }
+    ctx->in_flight = false;
+    if (ctx->timing) collect_times(ctx);
+    DevCtr c;
+    CK(cudaMemcpy(&c, ctx->d_ctr, sizeof(DevCtr), cudaMemcpyDeviceToHost), "counters");
+    if (c.pad0) return fail(ctx, ST_ERR_TIMEOUT, "a kernel's wait for its scene table ran out of iterations");
+    return ST_OK;
+}
+
+int st_step(st_ctx* ctx, int n) {
+    int rc = st_step_async(ctx, n);
+    if (rc) return rc;
+    return st_sync(ctx, -1);
+}
+
+int st_read_accum(st_ctx* ctx, double* rgb, double* V, double* S, uint32_t* count) {
+    if (!ctx) return ST_ERR_ARG;
+    if (!ctx->d_acc) return fail(ctx, ST_ERR_STATE, "nothing rendered yet");
+    if (ctx->in_flight) { int rc = st_sync(ctx, -1); if (rc) return rc; }
+    cudaSetDevice(ctx->device);
+    std::vector<Acc4> acc(ctx->P);
+    std::vector<double2> mom(ctx->P);
+    CK(cudaMemcpyAsync(acc.data(), ctx->d_acc, acc.size() * sizeof(Acc4), cudaMemcpyDeviceToHost, ctx->stream), "readback");
+    CK(cudaMemcpyAsync(mom.data(), ctx->d_mom, mom.size() * sizeof(double2), cudaMemcpyDeviceToHost, ctx->stream), "readback");
+    CK(cudaStreamSynchronize(ctx->stream), "readback");
+    for (uint32_t i = 0; i < ctx->P; i++) {
+        if (rgb) { rgb[3 * i] = acc[i].x; rgb[3 * i + 1] = acc[i].y; rgb[3 * i + 2] = acc[i].z; }
+        if (count) count[i] = (uint32_t)acc[i].w;
+        if (V) V[i] = mom[i].x;
+        if (S) S[i] = mom[i].y;
+    }
+    return ST_OK;
+}
+
+int st_image_stats(st_ctx* ctx, st_image_stats_t* out) {
+    if (!ctx || !out) return ST_ERR_ARG;
+    std::vector<double> rgb(3 * (size_t)ctx->P), V(ctx->P), S(ctx->P);
+    std::vector<uint32_t> cnt(ctx->P);
+    int rc = st_read_accum(ctx, rgb.data(), V.data(), S.data(), cnt.data());
+    if (rc) return rc;
+    std::vector<double> L;
+    double sum = 0, rel = 0;
+    uint32_t nrel = 0;
+    for (uint32_t i = 0; i < ctx->P; i++) {
+        if (!cnt[i]) continue;
+        double y = rgb[3 * i] * 0.2126 + rgb[3 * i + 1] * 0.7152 + rgb[3 * i + 2] * 0.0722;
+        L.push_back(y);
+        sum += y;
+        if (y > 0 && S[i] > 0 && S[i] < 1) { rel += std::sqrt(S[i] * V[i] / (1 - S[i])) / y; nrel++; }
+    }
+    *out = st_image_stats_t{};
+    out->sampled = (uint32_t)L.size();
+    out->samples = ctx->samples;
+    if (L.empty()) return ST_OK;
+    out->mean_luma = sum / L.size();
+    std::sort(L.begin(), L.end());
+    out->median_luma = L[L.size() / 2];
+    size_t cut = L.size() / 100, a = cut, b = L.size() - cut;
+    double ts = 0;
+    for (size_t i = a; i < b; i++) ts += L[i];
+    out->trimmed_mean_luma = b > a ? ts / (b - a) : out->mean_luma;
+    out->mean_rel_se = nrel ? rel / nrel : 0;
+    return ST_OK;
+}
+
+int st_read_counters(st_ctx* ctx, st_counters_t* out) {
+    if (!ctx || !out) return ST_ERR_ARG;
+    if (ctx->in_flight) { int rc = st_sync(ctx, -1); if (rc) return rc; }
+    cudaSetDevice(ctx->device);
+    DevCtr c;
+    CK(cudaMemcpy(&c, ctx->d_ctr, sizeof(DevCtr), cudaMemcpyDeviceToHost), "counters");
+    out->paths = c.paths; out->segments = c.segments; out->march_steps = c.march_steps;
+    out->shadow_rays = c.shadow_rays; out->shadow_steps = c.shadow_steps;
+    out->nonfinite = c.nonfinite; out->flushed = c.flushed; out->shadowcut = c.shadowcut;
+    out->samples = ctx->samples;
+    return ST_OK;
+}
+
+int st_enable_kernel_times(st_ctx* ctx, int on) {
+    if (!ctx) return ST_ERR_ARG;
+    ctx->timing = on != 0;
+    return ST_OK;
+}
+
+int st_kernel_times(st_ctx* ctx, st_kernel_time* out, int max, int* n_out) {
+    if (!ctx || (!out && max > 0)) return ST_ERR_ARG;
+    if (ctx->in_flight) { int rc = st_sync(ctx, -1); if (rc) return rc; }
+    collect_times(ctx);
+    int n = std::min<int>(max, (int)ctx->ktimes.size());
+    for (int i = 0; i < n; i++) {
+        std::memset(out[i].name, 0, sizeof(out[i].name));
+        std::snprintf(out[i].name, sizeof(out[i].name), "%s", ctx->ktimes[i].name.c_str());
+        out[i].launches = ctx->ktimes[i].launches;
+        out[i].ms = ctx->ktimes[i].ms;
+    }
+    if (n_out) *n_out = (int)ctx->ktimes.size();
+    return ST_OK;
+}
+
+int st_reset_kernel_times(st_ctx* ctx) {
+    if (!ctx) return ST_ERR_ARG;
+    if (ctx->in_flight) { int rc = st_sync(ctx, -1); if (rc) return rc; }
+    collect_times(ctx);
+    ctx->ktimes.clear();
+    return ST_OK;
+}
+
+int st_mf_tables(st_ctx* ctx, float* ec, float* ecavg, float* e1) {
+    if (!ctx || !ec || !ecavg || !e1) return ST_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    CK(cudaMemcpy(ec, ctx->d_ec, 16 * 32 * 32 * 4, cudaMemcpyDeviceToHost), "tables");
+    CK(cudaMemcpy(ecavg, ctx->d_ecavg, 16 * 32 * 4, cudaMemcpyDeviceToHost), "tables");
+    CK(cudaMemcpy(e1, ctx->d_e1, 32 * 32 * 4, cudaMemcpyDeviceToHost), "tables");
+    return ST_OK;
+}
+
+// the struct sizes this library was built with, for the host's bindings to check theirs against
+int st_struct_sizes(uint32_t* out, int max) {
+    const uint32_t s[] = {(uint32_t)sizeof(st_prim), (uint32_t)sizeof(st_material), (uint32_t)sizeof(st_scene_desc),
+                          (uint32_t)sizeof(st_params), (uint32_t)sizeof(st_view), (uint32_t)sizeof(st_counters_t),
+                          (uint32_t)sizeof(st_image_stats_t), (uint32_t)sizeof(st_kernel_time),
+                          (uint32_t)sizeof(st_sppm_stats), (uint32_t)sizeof(st_optics_source),
+                          (uint32_t)sizeof(st_optics_far), (uint32_t)sizeof(st_optics_batch),
+                          (uint32_t)sizeof(st_optics_totals)};
+    int n = (int)(sizeof(s) / sizeof(s[0]));
+    for (int i = 0; i < n && i < max; i++) out[i] = s[i];
+    return n;
+}
+
+// the context's stream, for a host that times or orders its own work against the library's (cudaStream_t)
+void* st_stream(st_ctx* ctx) { return ctx ? (void*)ctx->stream : nullptr; }
+
+}  // extern "C"
+
+// the extension units' access to the context (st_ext.h)
+StExt& ctx_ext(st_ctx* ctx) { return ctx->ext; }
+cudaStream_t ctx_stream(st_ctx* ctx) { return ctx->stream; }
+int ctx_device(st_ctx* ctx) { return ctx->device; }
+int ctx_sms(st_ctx* ctx) { return ctx->sms; }
+void ctx_set_error(st_ctx* ctx, const std::string& m) { ctx->err = m; }
+const st_prim* ctx_d_prims(st_ctx* ctx) { return ctx->d_prims; }
+const st_material* ctx_d_mats(st_ctx* ctx) { return ctx->d_mats; }
+uint32_t ctx_n_prims(st_ctx* ctx) { return (uint32_t)ctx->prims.size(); }
+uint32_t ctx_n_mats(st_ctx* ctx) { return (uint32_t)ctx->mats.size(); }
+const st_scene_desc& ctx_desc(st_ctx* ctx) { return ctx->desc; }
+bool ctx_has_scene(st_ctx* ctx) { return ctx->has_scene; }
+MfTab ctx_tab(st_ctx* ctx) { return MfTab{ctx->d_ec, ctx->d_ecavg, ctx->d_e1}; }

@@ -1,0 +1,632 @@
+// st_device.cuh -- device-side arithmetic of the rendering hot path for sm_103a: vectors, the PCG4D generator, the
+// surface tolerance, the scene table's SDF fold, the environment, the GGX lobes and their albedo tables.
+//
+// Each function restates the reference (lampmaker/ShadyTracer v0.88.0) at the file:line given; the kernels that
+// use them are in st_render.cu. Everything is f32 with f32 accumulation, as the reference's WGSL computes.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+#include "../../include/shadytracer.h"
+
+#define ST_PI 3.14159265358979f
+
+namespace st {
+
+// ------------------------------------------------------------------------------------------------------------
+// vectors
+// ------------------------------------------------------------------------------------------------------------
+struct f3 { float x, y, z; };
+__host__ __device__ __forceinline__ f3 mk(float x, float y, float z) { return f3{x, y, z}; }
+__host__ __device__ __forceinline__ f3 mk(float a) { return f3{a, a, a}; }
+__device__ __forceinline__ f3 operator+(f3 a, f3 b) { return f3{a.x + b.x, a.y + b.y, a.z + b.z}; }
+__device__ __forceinline__ f3 operator-(f3 a, f3 b) { return f3{a.x - b.x, a.y - b.y, a.z - b.z}; }
+__device__ __forceinline__ f3 operator*(f3 a, f3 b) { return f3{a.x * b.x, a.y * b.y, a.z * b.z}; }
+__device__ __forceinline__ f3 operator/(f3 a, f3 b) { return f3{a.x / b.x, a.y / b.y, a.z / b.z}; }
+__device__ __forceinline__ f3 operator*(f3 a, float s) { return f3{a.x * s, a.y * s, a.z * s}; }
+__device__ __forceinline__ f3 operator/(f3 a, float s) { return f3{a.x / s, a.y / s, a.z / s}; }
+__device__ __forceinline__ f3 operator-(f3 a) { return f3{-a.x, -a.y, -a.z}; }
+__device__ __forceinline__ float dot(f3 a, f3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ f3 cross(f3 a, f3 b) { return f3{a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x}; }
+__device__ __forceinline__ float length(f3 a) { return sqrtf(dot(a, a)); }
+__device__ __forceinline__ f3 normalize(f3 a) { return a / length(a); }
+__device__ __forceinline__ float max3(f3 a) { return fmaxf(a.x, fmaxf(a.y, a.z)); }
+__device__ __forceinline__ f3 vmin(f3 a, float s) { return f3{fminf(a.x, s), fminf(a.y, s), fminf(a.z, s)}; }
+__device__ __forceinline__ f3 vmax(f3 a, float s) { return f3{fmaxf(a.x, s), fmaxf(a.y, s), fmaxf(a.z, s)}; }
+__device__ __forceinline__ float clampf(float x, float lo, float hi) { return fminf(fmaxf(x, lo), hi); }
+__device__ __forceinline__ float sat(float x) { return clampf(x, 0.f, 1.f); }
+__device__ __forceinline__ float mixf(float a, float b, float t) { return a * (1.f - t) + b * t; }
+__device__ __forceinline__ float luma(f3 c) { return c.x * 0.2126f + c.y * 0.7152f + c.z * 0.0722f; }
+__device__ __forceinline__ f3 reflectv(f3 I, f3 N) { return I - N * (2.f * dot(N, I)); }
+__device__ __forceinline__ f3 refractv(f3 I, f3 N, float eta) {
+    float d = dot(N, I);
+    float k = 1.f - eta * eta * (1.f - d * d);
+    if (k < 0.f) return mk(0.f);
+    return I * eta - N * (eta * d + sqrtf(k));
+}
+__device__ __forceinline__ f3 xyz(float4 v) { return f3{v.x, v.y, v.z}; }
+__device__ __forceinline__ float4 f4(f3 a, float w) { return make_float4(a.x, a.y, a.z, w); }
+
+// ------------------------------------------------------------------------------------------------------------
+// PCG4D (core/tracebasics.js:330-380): SEED_u32, pcg4d, PRNG -- the top 24 bits of each lane
+// ------------------------------------------------------------------------------------------------------------
+struct Rng {
+    uint4 h;
+    __device__ __forceinline__ static uint4 pcg4d(uint4 v) {
+        v.x = v.x * 1664525u + 1013904223u; v.y = v.y * 1664525u + 1013904223u;
+        v.z = v.z * 1664525u + 1013904223u; v.w = v.w * 1664525u + 1013904223u;
+        v.x += v.y * v.w; v.y += v.z * v.x; v.z += v.x * v.y; v.w += v.y * v.z;
+        v.x ^= v.x >> 16; v.y ^= v.y >> 16; v.z ^= v.z >> 16; v.w ^= v.w >> 16;
+        v.x += v.y * v.w; v.y += v.z * v.x; v.z += v.x * v.y; v.w += v.y * v.z;
+        return v;
+    }
+    __device__ __forceinline__ void seed(uint32_t v) {
+        uint4 o = h;
+        h.x = (o.y ^ v) * 2313257647u; h.y = (o.z ^ v) * 2700274807u;
+        h.z = (o.w ^ v) * 3152041561u; h.w = (o.x ^ v) * 3679390633u;
+    }
+    __device__ __forceinline__ float4 next() {
+        h = pcg4d(h);
+        const float s = 1.0f / 16777216.0f;
+        return make_float4(float(h.x >> 8) * s, float(h.y >> 8) * s, float(h.z >> 8) * s, float(h.w >> 8) * s);
+    }
+};
+// the sample's seed from the base seed, and a path's generator at an event (0 the camera ray, 1 + i the shade of its
+// i-th segment): seeded by the path, as the reference's optics shade seeds by the ray (optics/kernels.js:598-606)
+__host__ __device__ __forceinline__ uint4 sample_seed(uint32_t base, uint32_t sample) {
+    uint4 v = make_uint4(base, sample, 0xA53B3F17u, 0xC0FFEE42u);
+    for (int r = 0; r < 2; r++) {
+        v.x = v.x * 1664525u + 1013904223u; v.y = v.y * 1664525u + 1013904223u;
+        v.z = v.z * 1664525u + 1013904223u; v.w = v.w * 1664525u + 1013904223u;
+        v.x += v.y * v.w; v.y += v.z * v.x; v.z += v.x * v.y; v.w += v.y * v.z;
+        v.x ^= v.x >> 16; v.y ^= v.y >> 16; v.z ^= v.z >> 16; v.w ^= v.w >> 16;
+        v.x += v.y * v.w; v.y += v.z * v.x; v.z += v.x * v.y; v.w += v.y * v.z;
+    }
+    return v;
+}
+__device__ __forceinline__ Rng path_rng(uint4 sseed, uint32_t path, uint32_t event) {
+    Rng r; r.h = sseed; r.seed(path); r.seed(event); return r;
+}
+#define ST_SALT_HAZE 0x48410000u
+
+// ------------------------------------------------------------------------------------------------------------
+// The uniforms a launch reads: the settings and their host-derived values (core/photometry.js:182-237, in double
+// on the host, rounded once to f32 here), passed by value in the kernel's parameter bank.
+// ------------------------------------------------------------------------------------------------------------
+struct Uni {
+    uint32_t W, H, P;            // picture, paths per sample (P = W * H)
+    uint32_t tilesX, tilesY;
+    float invTX, invTY;
+    uint32_t maxbounce, maxiter, nee, rr, budget;
+    float stepscale, tol, envR2, envR;
+    // camera (genrays.js:65-92)
+    f3 cam, right, up, fwd; float fx, fy; uint32_t camtype;
+    // environment (sdf.js:70-160)
+    f3 sun_dir; float sun_sin2, sun_omc, sun_omega, pick; int sun_on;
+    f3 disc; float sky, ground, uniform, sun_gain, sky_gain;
+    // haze box (haze.js:64-80)
+    int haze_on; f3 hc, hu, hv, hw, halb; float hhu, hhv, hhw, hsig, hg;
+    // the sample sequence
+    uint32_t seed, maxaverages, n_prims, n_mats;
+};
+
+// ------------------------------------------------------------------------------------------------------------
+// THE TOLERANCE (core/tolerances.js:27-37 marchTol); offsetTol = 10 marchTol (tracebasics.js:165)
+// ------------------------------------------------------------------------------------------------------------
+__device__ __forceinline__ float march_tol(f3 p, float setting) {
+    float f = 128.0f * 1.1920928955078125e-7f * fmaxf(fabsf(p.x), fmaxf(fabsf(p.y), fabsf(p.z)));
+    return fmaxf(fmaxf(setting, 1e-9f), f);
+}
+
+// ------------------------------------------------------------------------------------------------------------
+// THE SCENE TABLE'S SDF (core/scene_api.js:28-80 fold; sdf.js:214-256, :602; shapes.js:266-287, :621-726)
+// The table sits in shared memory (st_render.cu stages it with a bulk copy); every thread of a warp reads the
+// same record at the same time, a broadcast.
+// ------------------------------------------------------------------------------------------------------------
+__device__ __forceinline__ float sd_box(f3 p, f3 b) {
+    f3 q = mk(fabsf(p.x) - b.x, fabsf(p.y) - b.y, fabsf(p.z) - b.z);
+    return length(vmax(q, 0.f)) + fminf(fmaxf(q.x, fmaxf(q.y, q.z)), 0.f);
+}
+__device__ __forceinline__ float g2_regular_polygon(float qx, float qy, float sides, float R0) {
+    float n = clampf(rintf(sides), 3.f, 64.f);
+    float R = fmaxf(R0, 0.f);
+    float an = ST_PI / n;
+    float san, can;
+    sincosf(an, &san, &can);
+    float a = R * can, he = R * san;
+    float k = rintf((atan2f(qy, qx) + 0.5f * ST_PI) / (2.f * an));
+    float phi = -0.5f * ST_PI + 2.f * an * k;
+    float nky, nkx;
+    sincosf(phi, &nky, &nkx);
+    float tkx = -nky, tky = nkx;
+    float u = qx * nkx + qy * nky, v = qx * tkx + qy * tky;
+    if (u <= a) return u - a;
+    float ex = u - a, ey = v - clampf(v, -he, he);
+    return sqrtf(ex * ex + ey * ey);
+}
+__device__ __forceinline__ float g2_extrude(float pz, float gz, float h) {
+    float wz = fabsf(pz) - h;
+    if (gz > 0.f && wz > 0.f) return sqrtf(gz * gz + wz * wz);
+    if (gz > wz) return gz;
+    return wz;
+}
+__device__ __forceinline__ void asph_sag(float r, float c, float k, float a4, float a6, float& sag, float& slope) {
+    float r2 = r * r;
+    float w = 1.f - (1.f + k) * c * c * r2;
+    float u = sqrtf(fmaxf(w, 1e-4f));
+    float poly = r2 * r2 * (a4 + r2 * a6);
+    float dpoly = r * r2 * (4.f * a4 + r2 * (6.f * a6));
+    sag = c * r2 / (1.f + u) + poly;
+    slope = (w >= 1e-4f ? c * r / u : 2.f * c * r / (1.f + u)) + dpoly;
+}
+__device__ __forceinline__ float asph_face(f3 p, float l, float rho, float ht, float R, float k, float a4, float a6, float s) {
+    float c = fabsf(R) > 1e-9f ? 1.f / R : 0.f;
+    float sag, slope;
+    asph_sag(fminf(l, rho), c, k, a4, a6, sag, slope);
+    float r2 = rho * rho;
+    float u = sqrtf(fmaxf(1.f - (1.f + k) * c * c * r2, 1e-4f));
+    float poly = rho * r2 * (4.f * fabsf(a4) + r2 * (6.f * fabsf(a6)));
+    float m = fabsf(c) * rho / u + poly;
+    return (s * p.z - ht + sag) / sqrtf(1.f + m * m);
+}
+
+// one primitive, world point in; the record's float4 words: [1] pos,k [2] rot r0 [3] rot r1,(r2.x) ...
+__device__ __forceinline__ float prim_sdf(const st_prim& pr, f3 pw) {
+    f3 d = pw - mk(pr.pos[0], pr.pos[1], pr.pos[2]);
+    f3 q = mk(pr.rot[0] * d.x + pr.rot[1] * d.y + pr.rot[2] * d.z,
+              pr.rot[3] * d.x + pr.rot[4] * d.y + pr.rot[5] * d.z,
+              pr.rot[6] * d.x + pr.rot[7] * d.y + pr.rot[8] * d.z);
+    const float* p = pr.p;
+    switch (pr.type) {
+        case ST_PRIM_PLANE: return q.z;
+        case ST_PRIM_SPHERE: return length(q) - p[0];
+        case ST_PRIM_BOX: return sd_box(q, mk(p[0], p[1], p[2]));
+        case ST_PRIM_ROUNDBOX: return sd_box(q, mk(p[0], p[1], p[2])) - p[3];
+        case ST_PRIM_TORUS: {
+            float lxy = sqrtf(q.x * q.x + q.y * q.y);
+            float a = lxy - p[0];
+            return sqrtf(a * a + q.z * q.z) - p[1];
+        }
+        case ST_PRIM_PRISM: {
+            float g = g2_regular_polygon(q.x, q.y, p[0], p[1]);
+            return g2_extrude(q.z, g, fmaxf(0.5f * p[2], 0.f)) - p[3];
+        }
+        case ST_PRIM_ASPHERE: {
+            float rho = fmaxf(0.5f * p[0], 1e-6f);
+            float l = sqrtf(q.x * q.x + q.y * q.y);
+            float dd = l - rho;
+            float top = asph_face(q, l, rho, 0.5f * p[1], p[2], p[3], p[4], p[5], 1.f);
+            if (top > dd) dd = top;
+            float bot = asph_face(q, l, rho, 0.5f * p[1], p[6], p[7], p[8], p[9], -1.f);
+            if (bot > dd) dd = bot;
+            return dd;
+        }
+        case ST_PRIM_CYLINDER: {
+            float lx = sqrtf(q.x * q.x + q.y * q.y) - p[1];
+            float lz = fabsf(q.z) - p[0];
+            float ox = fmaxf(lx, 0.f), oz = fmaxf(lz, 0.f);
+            return fminf(fmaxf(lx, lz), 0.f) + sqrtf(ox * ox + oz * oz);
+        }
+    }
+    return 1e7f;
+}
+__device__ __forceinline__ float smooth_union(float d1, float d2, float k) {          // sdf.js:252-256
+    if (!(k > 0.f)) return fminf(d1, d2);
+    float h = clampf(0.5f + 0.5f * (d2 - d1) / k, 0.f, 1.f);
+    return mixf(d2, d1, h) - k * h * (1.f - h);
+}
+
+struct SceneHit { float d; uint32_t m, a; };
+// distance only (scene_api.js FOLD_DIST): the march's and the shadow rays' question
+__device__ __forceinline__ float scene_dist(const st_prim* __restrict__ pr, uint32_t n, f3 p) {
+    float best = 1e7f;
+    uint32_t i = 0;
+    while (i < n) {
+        float di = prim_sdf(pr[i], p);
+        uint32_t j = i + 1;
+        while (j < n && pr[j].op != ST_OP_ITEM) {
+            float dj = prim_sdf(pr[j], p);
+            uint32_t op = pr[j].op;
+            if (op == ST_OP_SMOOTH) di = smooth_union(di, dj, pr[j].k);
+            else if (op == ST_OP_UNION) di = fminf(di, dj);
+            else di = fmaxf(di, -dj);
+            j++;
+        }
+        if (fabsf(di) < fabsf(best)) best = di;
+        i = j;
+    }
+    return best;
+}
+// the whole answer (FOLD_FULL): the surface's material and the medium (the least-deep item the point is in)
+__device__ __forceinline__ SceneHit scene_full(const st_prim* __restrict__ pr, uint32_t n, f3 p) {
+    SceneHit H{1e7f, 0u, 0u};
+    float insideW = -1e7f;
+    uint32_t i = 0;
+    while (i < n) {
+        float di = prim_sdf(pr[i], p);
+        uint32_t mat = pr[i].material;
+        float nearv = fabsf(di);
+        uint32_t j = i + 1;
+        while (j < n && pr[j].op != ST_OP_ITEM) {
+            float dj = prim_sdf(pr[j], p);
+            uint32_t op = pr[j].op;
+            if (op == ST_OP_SMOOTH) di = smooth_union(di, dj, pr[j].k);
+            else if (op == ST_OP_UNION) di = fminf(di, dj);
+            else di = fmaxf(di, -dj);
+            if (op != ST_OP_SUB && fabsf(dj) < nearv) { nearv = fabsf(dj); mat = pr[j].material; }
+            j++;
+        }
+        if (di < 0.f && di > insideW) { insideW = di; H.a = mat; }
+        if (fabsf(di) < fabsf(H.d)) { H.d = di; H.m = mat; }
+        i = j;
+    }
+    return H;
+}
+
+// ------------------------------------------------------------------------------------------------------------
+// THE ENVIRONMENT (sdf.js:70-182; tracebasics.js:655-699)
+// ------------------------------------------------------------------------------------------------------------
+__device__ __forceinline__ bool in_sun_disc(const Uni& u, f3 dir) {
+    f3 L = normalize(dir);
+    f3 c = cross(L, u.sun_dir);
+    return dot(L, u.sun_dir) > 0.f && dot(c, c) <= u.sun_sin2;
+}
+__device__ __forceinline__ f3 env_base(const Uni& u, f3 dir) {
+    if (u.uniform > 0.f) return mk(u.uniform);
+    f3 d = normalize(dir);
+    if (in_sun_disc(u, d)) return u.disc;
+    return mk(d.z > 0.f ? u.sky : u.ground);
+}
+__device__ __forceinline__ f3 env_radiance(const Uni& u, f3 dir) {
+    bool cone = u.sun_on && in_sun_disc(u, dir);
+    return env_base(u, dir) * (cone ? u.sun_gain : u.sky_gain);
+}
+__device__ __forceinline__ f3 sample_sun_cone(const Uni& u, float u0, float u1) {
+    f3 sd = u.sun_dir;
+    float omc = u0 * u.sun_omc;
+    float cosT = 1.f - omc;
+    float sinT = sqrtf(fmaxf(0.f, omc * (2.f - omc)));
+    float sp, cp;
+    sincosf(2.f * ST_PI * u1, &sp, &cp);
+    f3 t = fabsf(sd.x) > 0.9f ? mk(0, 1, 0) : mk(1, 0, 0);
+    f3 b1 = normalize(cross(t, sd));
+    f3 b2 = cross(sd, b1);
+    return normalize(b1 * (cp * sinT) + b2 * (sp * sinT) + sd * cosT);
+}
+__device__ __forceinline__ f3 sample_cosine_hemi(f3 n, float u0, float u1) {
+    float r = sqrtf(u0);
+    float sp, cp;
+    sincosf(2.f * ST_PI * u1, &sp, &cp);
+    f3 t = fabsf(n.x) > 0.9f ? mk(0, 1, 0) : mk(1, 0, 0);
+    f3 b1 = normalize(cross(t, n));
+    f3 b2 = cross(n, b1);
+    return normalize(b1 * (r * cp) + b2 * (r * sp) + n * sqrtf(fmaxf(0.f, 1.f - u0)));
+}
+__device__ __forceinline__ f3 env_sample_dir(const Uni& u, f3 n, float pick, float u0, float u1) {
+    if (pick < u.pick) return sample_sun_cone(u, u0, u1);
+    return sample_cosine_hemi(n, u0, u1);
+}
+__device__ __forceinline__ float env_pdf(const Uni& u, f3 L, f3 n) {
+    float pSun = in_sun_disc(u, L) ? 1.f / u.sun_omega : 0.f;
+    float pCos = fmaxf(dot(L, n), 0.f) / ST_PI;
+    return u.pick * pSun + (1.f - u.pick) * pCos;
+}
+__device__ __forceinline__ float mis_weight(float a, float b) {
+    float a2 = a * a, b2 = b * b;
+    return a2 / fmaxf(a2 + b2, 1e-20f);
+}
+// the environment from a point in the air (haze.js:296-310)
+__device__ __forceinline__ f3 env_sample_dir_m(const Uni& u, float pick, float u0, float u1) {
+    if (pick < u.pick) return sample_sun_cone(u, u0, u1);
+    float z = 1.f - 2.f * u0;
+    float s = sqrtf(fmaxf(0.f, 1.f - z * z));
+    float sp, cp;
+    sincosf(2.f * ST_PI * u1, &sp, &cp);
+    return mk(s * cp, s * sp, z);
+}
+__device__ __forceinline__ float env_pdf_m(const Uni& u, f3 L) {
+    float pSun = in_sun_disc(u, L) ? 1.f / u.sun_omega : 0.f;
+    return u.pick * pSun + (1.f - u.pick) / (4.f * ST_PI);
+}
+
+// ------------------------------------------------------------------------------------------------------------
+// HAZE (haze.js:191-288): Henyey-Greenstein, the box's span and transmittance, the leg's collision
+// ------------------------------------------------------------------------------------------------------------
+__device__ __forceinline__ float hg_eval(float cosT, float g) {
+    float d = 1.f + g * g - 2.f * g * cosT;
+    return (1.f - g * g) / (4.f * ST_PI * powf(fmaxf(d, 1e-12f), 1.5f));
+}
+__device__ __forceinline__ f3 hg_sample(f3 d, float g, float u0, float u1) {
+    float c = 1.f - 2.f * u0;
+    if (fabsf(g) >= 1e-3f) {
+        float s = (1.f - g * g) / (1.f - g + 2.f * g * u0);
+        c = clampf((1.f + g * g - s * s) / (2.f * g), -1.f, 1.f);
+    }
+    float sn = sqrtf(fmaxf(0.f, 1.f - c * c));
+    float sp, cp;
+    sincosf(2.f * ST_PI * u1, &sp, &cp);
+    f3 t = fabsf(d.x) > 0.9f ? mk(0, 1, 0) : mk(1, 0, 0);
+    f3 b1 = normalize(cross(t, d));
+    f3 b2 = cross(d, b1);
+    return normalize(b1 * (cp * sn) + b2 * (sp * sn) + d * c);
+}
+__device__ __forceinline__ void haze_slab(float o, float dd, float h, float& t0, float& t1) {
+    if (fabsf(dd) < 1e-12f) { if (fabsf(o) > h) { t0 = 1.f; t1 = 0.f; } return; }
+    float a = (-h - o) / dd, b = (h - o) / dd;
+    t0 = fmaxf(t0, fminf(a, b));
+    t1 = fminf(t1, fmaxf(a, b));
+}
+__device__ __forceinline__ void haze_span(const Uni& u, f3 A, f3 d, float len, float& t0, float& t1) {
+    f3 o = A - u.hc;
+    t0 = 0.f; t1 = len;
+    haze_slab(dot(o, u.hu), dot(d, u.hu), u.hhu, t0, t1);
+    haze_slab(dot(o, u.hv), dot(d, u.hv), u.hhv, t0, t1);
+    haze_slab(dot(o, u.hw), dot(d, u.hw), u.hhw, t0, t1);
+    float b = dot(A, d);
+    float disc = b * b - (dot(A, A) - u.envR * u.envR);
+    if (disc <= 0.f) { t0 = 1.f; t1 = 0.f; return; }
+    float s = sqrtf(disc);
+    t0 = fmaxf(t0, -b - s);
+    t1 = fminf(t1, -b + s);
+}
+__device__ __forceinline__ float haze_tr(const Uni& u, f3 A, f3 d, float len) {
+    if (!u.haze_on) return 1.f;
+    float t0, t1;
+    haze_span(u, A, d, len, t0, t1);
+    if (t1 <= t0) return 1.f;
+    return expf(-u.hsig * (t1 - t0));
+}
+
+// ------------------------------------------------------------------------------------------------------------
+// MICROFACET (microfacet.js:72-240): GGX, Smith, the VNDF sampler, Fresnel, the isotropic albedo tables' reads
+// ------------------------------------------------------------------------------------------------------------
+#define MF_NMU 32
+#define MF_NR 32
+#define MF_NIOR 16
+#define MF_ALPHA_MIN 1e-3f
+struct MfTab { const float* __restrict__ ec; const float* __restrict__ ecavg; const float* __restrict__ e1; };
+
+__device__ __forceinline__ float mf_lambda(f3 w, float a) {
+    float z2 = fmaxf(w.z * w.z, 1e-12f);
+    float t2 = (a * a * w.x * w.x + a * a * w.y * w.y) / z2;
+    return 0.5f * (-1.f + sqrtf(1.f + t2));
+}
+__device__ __forceinline__ float mf_g1(f3 w, float a) { return 1.f / (1.f + mf_lambda(w, a)); }
+__device__ __forceinline__ float mf_g2(f3 o, f3 i, float a) { return 1.f / (1.f + mf_lambda(o, a) + mf_lambda(i, a)); }
+__device__ __forceinline__ float mf_d(f3 h, float a) {
+    if (h.z <= 0.f) return 0.f;
+    float t = (h.x * h.x) / (a * a) + (h.y * h.y) / (a * a) + h.z * h.z;
+    return 1.f / (ST_PI * a * a * t * t);
+}
+__device__ __forceinline__ f3 mf_sample_vndf(f3 o, float a, float u0, float u1) {
+    f3 os = normalize(mk(o.x * a, o.y * a, o.z));
+    float z = (1.f - u1) * (1.f + os.z) - os.z;
+    float sinT = sqrtf(clampf(1.f - z * z, 0.f, 1.f));
+    float sp, cp;
+    sincosf(2.f * ST_PI * u0, &sp, &cp);
+    f3 c = mk(sinT * cp, sinT * sp, z);
+    f3 hs = c + os;
+    return normalize(mk(hs.x * a, hs.y * a, fmaxf(hs.z, 1e-7f)));
+}
+__device__ __forceinline__ float mf_pdf_reflect(f3 o, f3 i, float a) {
+    if (o.z <= 0.f || i.z <= 0.f) return 0.f;
+    f3 h = normalize(o + i);
+    return mf_g1(o, a) * mf_d(h, a) / (4.f * o.z);
+}
+__device__ __forceinline__ float fresnel_dielectric(float cosI_in, float eta) {
+    float cosI = clampf(cosI_in, 0.f, 1.f);
+    float sin2T = eta * eta * (1.f - cosI * cosI);
+    if (sin2T >= 1.f) return 1.f;
+    float cosT = sqrtf(1.f - sin2T);
+    float rs = (eta * cosI - cosT) / (eta * cosI + cosT);
+    float rp = (cosI - eta * cosT) / (cosI + eta * cosT);
+    return 0.5f * (rs * rs + rp * rp);
+}
+__device__ __forceinline__ f3 fresnel_schlick3(float cosI, f3 f0) {
+    float m = 1.f - clampf(cosI, 0.f, 1.f);
+    float m5 = m * m * m * m * m;
+    return f0 + (mk(1.f) - f0) * m5;
+}
+__device__ __forceinline__ void mf_axis(float x, int n, float& i0, float& f) {
+    float c = clampf(x, 0.f, float(n - 1));
+    i0 = fminf(floorf(c), float(n - 2));
+    f = c - i0;
+}
+__device__ __forceinline__ float mf_ec(const MfTab& t, float mu, float r, float n) {
+    float m0, mf, r0, rf, n0, nf;
+    mf_axis(mu * float(MF_NMU) - 0.5f, MF_NMU, m0, mf);
+    mf_axis(r * float(MF_NR - 1), MF_NR, r0, rf);
+    mf_axis((n - 1.f) * float(MF_NIOR - 1) / 2.f, MF_NIOR, n0, nf);
+    float acc = 0.f;
+#pragma unroll
+    for (int c = 0; c < 8; c++) {
+        int di = c & 1, dk = (c >> 1) & 1, dj = (c >> 2) & 1;
+        float w = (di ? nf : 1.f - nf) * (dk ? rf : 1.f - rf) * (dj ? mf : 1.f - mf);
+        int idx = (((int)n0 + di) * MF_NR + (int)r0 + dk) * MF_NMU + (int)m0 + dj;
+        acc += w * __ldg(t.ec + idx);
+    }
+    return acc;
+}
+__device__ __forceinline__ float mf_ecavg(const MfTab& t, float r, float n) {
+    float r0, rf, n0, nf;
+    mf_axis(r * float(MF_NR - 1), MF_NR, r0, rf);
+    mf_axis((n - 1.f) * float(MF_NIOR - 1) / 2.f, MF_NIOR, n0, nf);
+    float acc = 0.f;
+#pragma unroll
+    for (int c = 0; c < 4; c++) {
+        int di = c & 1, dk = (c >> 1) & 1;
+        float w = (di ? nf : 1.f - nf) * (dk ? rf : 1.f - rf);
+        acc += w * __ldg(t.ecavg + ((int)n0 + di) * MF_NR + (int)r0 + dk);
+    }
+    return acc;
+}
+__device__ __forceinline__ float mf_e1(const MfTab& t, float mu, float r) {
+    float m0, mf, r0, rf;
+    mf_axis(mu * float(MF_NMU) - 0.5f, MF_NMU, m0, mf);
+    mf_axis(r * float(MF_NR - 1), MF_NR, r0, rf);
+    float acc = 0.f;
+#pragma unroll
+    for (int c = 0; c < 4; c++) {
+        int dk = c & 1, dj = (c >> 1) & 1;
+        float w = (dk ? rf : 1.f - rf) * (dj ? mf : 1.f - mf);
+        acc += w * __ldg(t.e1 + ((int)r0 + dk) * MF_NMU + (int)m0 + dj);
+    }
+    return acc;
+}
+
+// ------------------------------------------------------------------------------------------------------------
+// THE LOBES (materials_pbr.js:164-596): isotropic, uncoated, no haze share -- the hot path's materials
+// ------------------------------------------------------------------------------------------------------------
+#define EV_NONE 0u
+#define EV_DELTA 1u
+#define EV_EVAL 2u
+#define EV_OTHER 3u
+struct Lobes {
+    f3 tX, tY, nZ, o, base, transTint, coatK, cm, ecO, ecAvg;
+    float a, aMin, r, metallic, trans, eta, etaT, nrel, ps;
+    bool isDelta;
+    __device__ __forceinline__ f3 to_local(f3 w) const { return mk(dot(w, tX), dot(w, tY), dot(w, nZ)); }
+    __device__ __forceinline__ f3 to_world(f3 w) const { return normalize(tX * w.x + tY * w.y + nZ * w.z); }
+    __device__ __forceinline__ f3 coat_fresnel(float cosI) const { return vmin(coatK * fresnel_dielectric(cosI, eta), 1.f); }
+    __device__ __forceinline__ f3 metal_fresnel(float cosI) const { return fresnel_schlick3(cosI, base); }
+};
+__device__ __forceinline__ f3 coat_albedo(const Lobes& lb, const MfTab& t, f3 w) {
+    return vmin(lb.coatK * mf_ec(t, w.z, lb.r, lb.nrel), 1.f);
+}
+__device__ __forceinline__ Lobes make_lobes(f3 n, f3 v, const st_material& m, float eta, const MfTab& t,
+                                            float transm, float spec) {
+    Lobes lb;
+    f3 s = fabsf(n.z) < 0.999f ? normalize(cross(n, mk(0, 0, 1))) : normalize(cross(n, mk(0, 1, 0)));
+    lb.tX = s; lb.tY = cross(s, n); lb.nZ = n;
+    lb.o = mk(dot(v, lb.tX), dot(v, lb.tY), fmaxf(dot(v, n), 1e-4f));
+    lb.r = clampf(m.roughness, 0.f, 1.f);
+    float aIso = lb.r * lb.r;
+    lb.isDelta = aIso < MF_ALPHA_MIN;
+    lb.aMin = aIso;
+    lb.a = clampf(aIso, MF_ALPHA_MIN, 1.f);
+    lb.metallic = sat(m.metallic);
+    lb.trans = sat(transm);
+    lb.base = mk(m.base[0], m.base[1], m.base[2]);
+    lb.transTint = m.attenuation > 0.f ? mk(1.f) : lb.base;
+    float lum = max3(lb.base);
+    f3 tint = lum > 0.f ? lb.base / fmaxf(lum, 1e-6f) : mk(1.f);
+    float st = m.specular_tint;
+    f3 tintMix = mk(1.f) * (1.f - st) + tint * st;
+    lb.coatK = tintMix * mixf(2.f * spec, 1.f, lb.trans);
+    lb.eta = eta; lb.etaT = eta;
+    lb.nrel = clampf(1.f / eta, 1.f, 3.f);
+    float fo = max3(lb.coat_fresnel(lb.o.z));
+    lb.ps = fminf(fo, fresnel_dielectric(lb.o.z, lb.eta) >= 1.f ? 1.f : 0.999f);
+    lb.ecO = coat_albedo(lb, t, lb.o);
+    float e1 = lb.metallic > 0.f ? mf_e1(t, lb.o.z, lb.r) : 1.f;
+    float eAvg = mf_ecavg(t, lb.r, lb.nrel);
+    lb.ecAvg = vmin(lb.coatK * eAvg, 1.f);
+    lb.cm = mk(1.f) + lb.base * (1.f / fmaxf(e1, 1e-3f) - 1.f);
+    return lb;
+}
+__device__ __forceinline__ f3 lobes_eval(const Lobes& lb, const MfTab& t, f3 l, float minAlpha) {
+    f3 i = lb.to_local(l);
+    if (i.z <= 0.f) return mk(0.f);
+    f3 f = mk(0.f);
+    if (!lb.isDelta && lb.aMin >= minAlpha) {
+        f3 h = normalize(lb.o + i);
+        float spec = mf_d(h, lb.a) * mf_g2(lb.o, i, lb.a) / (4.f * lb.o.z * i.z);
+        float oh = dot(lb.o, h);
+        f = f + lb.cm * lb.metal_fresnel(oh) * (lb.metallic * spec);
+        f = f + lb.coat_fresnel(oh) * ((1.f - lb.metallic) * spec);
+    }
+    float wDiff = (1.f - lb.metallic) * (1.f - lb.trans);
+    if (wDiff > 0.f) {
+        f3 ecI = coat_albedo(lb, t, i);
+        f3 den = vmax(mk(1.f) - lb.ecAvg, 1e-4f) * ST_PI;
+        f = f + lb.base * (mk(1.f) - lb.ecO) * (mk(1.f) - ecI) / den * wDiff;
+    }
+    return f;
+}
+__device__ __forceinline__ float interface_reflect_p(const Lobes& lb, float oh) {
+    float fh = max3(lb.coat_fresnel(oh));
+    float den = fh + (1.f - fh) * lb.trans;
+    return den > 1e-6f ? fh / den : 1.f;
+}
+__device__ __forceinline__ float lobes_pdf(const Lobes& lb, f3 l) {
+    f3 i = lb.to_local(l);
+    if (i.z <= 0.f) return 0.f;
+    float wd = 1.f - lb.metallic;
+    float pd = (1.f - lb.ps) * (1.f - lb.trans);
+    float p = wd * pd * i.z / ST_PI;
+    if (!lb.isDelta) {
+        float pr = mf_pdf_reflect(lb.o, i, lb.a);
+        p += (lb.metallic + wd * (1.f - pd) * interface_reflect_p(lb, dot(lb.o, normalize(lb.o + i)))) * pr;
+    }
+    return p;
+}
+__device__ __forceinline__ bool lobes_none(const st_material& m, float transmission) {
+    float r = clampf(m.roughness, 0.f, 1.f);
+    return r * r < MF_ALPHA_MIN && (1.f - sat(m.metallic)) * (1.f - sat(transmission)) <= 0.f;
+}
+struct LobeSample { f3 dir, w; uint32_t ev; bool isDelta, transmitted; };
+__device__ __forceinline__ LobeSample lobes_sample(const Lobes& lb, const MfTab& t, float4 rnd) {
+    LobeSample s;
+    s.w = mk(0.f); s.ev = EV_OTHER; s.isDelta = false; s.transmitted = false;
+    f3 i = mk(0, 0, 1);
+    uint32_t glossyEv = lb.aMin >= 0.05f ? EV_EVAL : EV_OTHER;
+    float wd = 1.f - lb.metallic;
+    float pick = rnd.x;
+    if (pick < lb.metallic) {
+        if (lb.isDelta) {
+            i = mk(-lb.o.x, -lb.o.y, lb.o.z);
+            s.w = lb.metal_fresnel(lb.o.z) * lb.cm;
+            s.ev = EV_DELTA; s.isDelta = true;
+        } else {
+            f3 h = mf_sample_vndf(lb.o, lb.a, rnd.y, rnd.z);
+            i = reflectv(-lb.o, h);
+            if (i.z > 0.f) s.w = lb.cm * lb.metal_fresnel(dot(lb.o, h)) * (mf_g2(lb.o, i, lb.a) / mf_g1(lb.o, lb.a));
+            s.ev = glossyEv;
+        }
+    } else {
+        pick = (pick - lb.metallic) / fmaxf(wd, 1e-6f);
+        float pd = (1.f - lb.ps) * (1.f - lb.trans);
+        if (pick < 1.f - pd) {
+            float sub = pick / fmaxf(1.f - pd, 1e-6f);
+            if (lb.isDelta) {
+                if (sub < lb.ps / fmaxf(1.f - pd, 1e-6f)) {
+                    i = mk(-lb.o.x, -lb.o.y, lb.o.z);
+                    s.w = lb.coat_fresnel(lb.o.z) / lb.ps;
+                } else {
+                    s.transmitted = true;
+                    i = refractv(-lb.o, mk(0, 0, 1), lb.etaT);
+                    if (i.z < 0.f) s.w = (mk(1.f) - lb.coat_fresnel(lb.o.z)) * lb.transTint / (1.f - lb.ps);
+                }
+                s.ev = EV_DELTA; s.isDelta = true;
+            } else {
+                f3 h = mf_sample_vndf(lb.o, lb.a, rnd.y, rnd.z);
+                float oh = dot(lb.o, h);
+                f3 fc = lb.coat_fresnel(oh);
+                float r = interface_reflect_p(lb, oh);
+                if (sub < r) {
+                    i = reflectv(-lb.o, h);
+                    if (i.z > 0.f) s.w = fc * (mf_g2(lb.o, i, lb.a) / mf_g1(lb.o, lb.a) / ((1.f - pd) * r));
+                    s.ev = glossyEv;
+                } else {
+                    s.transmitted = true;
+                    i = refractv(-lb.o, h, lb.etaT);
+                    if (i.z < 0.f)
+                        s.w = (mk(1.f) - fc) * lb.transTint *
+                              (lb.trans * mf_g2(lb.o, i, lb.a) / mf_g1(lb.o, lb.a) / ((1.f - pd) * (1.f - r)));
+                    s.ev = lb.aMin >= 0.05f ? EV_EVAL : EV_OTHER;
+                }
+            }
+        } else {
+            float r = sqrtf(rnd.y);
+            float sp, cp;
+            sincosf(2.f * ST_PI * rnd.z, &sp, &cp);
+            i = mk(r * cp, r * sp, sqrtf(fmaxf(0.f, 1.f - rnd.y)));
+            f3 ecI = coat_albedo(lb, t, i);
+            s.w = lb.base * (mk(1.f) - lb.ecO) * (mk(1.f) - ecI) / vmax(mk(1.f) - lb.ecAvg, 1e-4f) / (1.f - lb.ps);
+            s.ev = EV_EVAL;
+        }
+    }
+    s.dir = lb.to_world(i);
+    return s;
+}
+
+}  // namespace st

@@ -1,0 +1,11 @@
+// st_ext.cu -- freeing the photon map's and the optics bench's device state with the context.
+#include "st_ext.h"
+
+void ext_free(StExt& e) {
+    SppmState& s = e.sppm;
+    void* ps[] = {s.pos, s.power, s.dir_oct, s.nrm_oct, s.flags, s.key, s.order, s.cell_count, s.cell_start,
+                  s.scan_part, s.spos, s.spow, s.sdir, s.snrm, s.sflags, s.stats, e.optics.scratch};
+    for (void* p : ps)
+        if (p) cudaFree(p);
+    e = StExt{};
+}

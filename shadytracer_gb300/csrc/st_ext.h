@@ -1,0 +1,60 @@
+// st_ext.h -- the photon map's and the optics bench's state inside a context, and the context accessors their
+// translation units (st_sppm.cu, st_optics.cu) use.
+#pragma once
+#include <cstdint>
+#include <string>
+#include <vector>
+#include <cuda_runtime.h>
+#include "st_device.cuh"
+
+struct st_ctx;
+
+struct SppmState {
+    uint32_t n = 0, cap = 0;
+    float cell = 0;
+    // records, structure of arrays (core/sppm.js:350-423: point, power, incoming direction, normal, flags)
+    float4* pos = nullptr;       // xyz point, w unused
+    float4* power = nullptr;     // xyz power, w unused
+    uint32_t* dir_oct = nullptr;
+    uint32_t* nrm_oct = nullptr;
+    uint32_t* flags = nullptr;   // bounce (low 16) | sub-list << 16 | SPPM_ALL / SPPM_VOL bits
+    uint32_t* key = nullptr;     // each record's cell hash
+    uint32_t* order = nullptr;   // the records in cell order (the counting sort's output)
+    uint32_t* cell_count = nullptr;   // 2^20
+    uint32_t* cell_start = nullptr;   // 2^20 (+1)
+    uint32_t* scan_part = nullptr;    // the scan's block partials
+    float4* spos = nullptr;      // the records' point and power, permuted into cell order
+    float4* spow = nullptr;
+    uint32_t* sdir = nullptr;
+    uint32_t* snrm = nullptr;
+    uint32_t* sflags = nullptr;
+    uint32_t* stats = nullptr;   // gathers, cut, visits_max, visits lo, visits hi
+};
+
+struct OpticsState {
+    std::vector<st_optics_source> sources;
+    st_optics_far far{};
+    bool has_far = false;
+    void* scratch = nullptr;     // device work space, grown as needed
+    size_t scratch_bytes = 0;
+};
+
+struct StExt {
+    SppmState sppm;
+    OpticsState optics;
+};
+
+void ext_free(StExt& e);
+
+StExt& ctx_ext(st_ctx* ctx);
+cudaStream_t ctx_stream(st_ctx* ctx);
+int ctx_device(st_ctx* ctx);
+int ctx_sms(st_ctx* ctx);
+void ctx_set_error(st_ctx* ctx, const std::string& m);
+const st_prim* ctx_d_prims(st_ctx* ctx);
+const st_material* ctx_d_mats(st_ctx* ctx);
+uint32_t ctx_n_prims(st_ctx* ctx);
+uint32_t ctx_n_mats(st_ctx* ctx);
+const st_scene_desc& ctx_desc(st_ctx* ctx);
+bool ctx_has_scene(st_ctx* ctx);
+st::MfTab ctx_tab(st_ctx* ctx);

@@ -1,0 +1,73 @@
+// st_internal.h -- what the host side of libshadytracer (st_capi.cu) and the kernels (st_render.cu, st_sppm.cu,
+// st_optics.cu) share: the device buffers of a wave, the device counters, and the launch wrappers.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+#include "st_device.cuh"
+
+namespace st {
+
+// Ray states (core/tracebasics.js:101-111; haze.js RAY_SCATTER)
+#define RAY_ACTIVE 0u
+#define RAY_ABSORBED 1u
+#define RAY_ESCAPED 2u
+#define RAY_MAXITER 4u
+#define RAY_SOURCE 5u
+#define RAY_TERMINATED 8u
+#define RAY_SCATTER 9u
+
+// THE WAVE'S PATH STATE, structure of arrays indexed by the path's slot (slot = sample-in-wave * P + tile): the
+// reference's 112-byte Ray (tracebasics.js:400-460) cut to what the hot path carries, as four float4 and one uint4
+// so every access is one 128-bit load or store.
+struct PathBuf {
+    float4* pos;    // xyz position, w ltot (optical length travelled)
+    float4* dir;    // xyz direction, w n (index of the medium it is in)
+    float4* beta;   // xyz throughput, w sunmis (the environment's MIS weight on escape)
+    float4* rad;    // xyz radiance collected, w tmax (the haze's collision, as ltot)
+    uint4* meta;    // x pix, y bounces | state << 16, z march steps over the path, w absLtot (f32 bits)
+};
+// THE QUEUES: indices into the path state, appended by warp-aggregated atomics (one per warp)
+struct Queues {
+    uint32_t* ray[2];   // the march's input, ping-pong
+    uint32_t* hit;      // the shade queue: slot
+    float* hitd;        // ...and the signed distance at the hit
+    float4* s_org;      // shadow rays: xyz origin, w n
+    float4* s_dir;      // xyz direction, w pix (u32 bits)
+    float4* s_rad;      // xyz what it deposits if it reaches, w unused
+    uint32_t cap;       // slots in a wave: every queue holds at most this many
+};
+// THE COUNTERS (wavefront.js:150 Counters), on the device
+struct DevCtr {
+    uint32_t rayCount[2], hitCount, shadowCount;
+    uint32_t marchHead, occHead, shadeHead, pad0;
+    uint32_t nonfinite, flushed, shadowcut, sample;   // sample: the first sample of the wave in flight
+    unsigned long long paths, segments, march_steps, shadow_rays, shadow_steps;
+};
+
+struct __align__(32) Acc4 { double x, y, z, w; };   // FP64 mean rgb + the sample count
+
+struct WaveArgs {
+    Uni u;
+    const st_prim* prims;
+    const st_material* mats;
+    MfTab tab;
+    PathBuf pb;
+    Queues q;
+    DevCtr* ctr;
+    float4* frame;      // spw * P: this wave's deposits, rgb + count
+    Acc4* acc;         // P: FP64 mean rgb + count
+    double2* mom;       // P: FP64 V, S (the error bar's moments)
+    uint32_t spw;       // samples in this wave
+    uint32_t slots;     // spw * P
+};
+
+// launch wrappers (st_render.cu)
+cudaError_t launch_mf_tables(float* ec, float* ecavg, float* e1, cudaStream_t s);
+cudaError_t launch_genrays(const WaveArgs& a, int sms, cudaStream_t s);
+cudaError_t launch_iter_begin(const WaveArgs& a, int nxt, int first, cudaStream_t s);
+cudaError_t launch_march(const WaveArgs& a, int cur, int it, int sms, cudaStream_t s);
+cudaError_t launch_shade(const WaveArgs& a, int nxt, int it, int last, int sms, cudaStream_t s);
+cudaError_t launch_occlude(const WaveArgs& a, int sms, cudaStream_t s);
+cudaError_t launch_resolve(const WaveArgs& a, cudaStream_t s);
+
+}  // namespace st

@@ -1,0 +1,712 @@
+// st_render.cu -- the wavefront kernels of the rendering hot path, for sm_103a.
+//
+//   k_mf_lut, k_mf_avg   the GGX albedo tables, once at init            core/microfacet.js:245-330
+//   k_genrays            one camera ray per path of the wave             core/genrays.js:36-107
+//   k_iter_begin         a wavefront iteration's counters                core/wavefront.js:333-387 (prog_flip)
+//   k_march              sphere tracing, persistent with refill          core/wavefront.js:834-1005 (prog_march)
+//   k_shade              surface answers + BSDF + light sample + deposit core/wavefront.js:1037-1147 (prog_surface),
+//                                                                        :1244-1442 (prog_shade)
+//   k_occlude            shadow rays, persistent with refill             core/wavefront.js:1481-1692 (prog_occlude)
+//   k_resolve            the sample into the FP64 mean and error bar     core/wavefront.js:414-494 (prog_resolve)
+//
+// GB300 shape of it. The path state lives in HBM by slot as structure-of-arrays float4s; the queues hold slots,
+// appended with one atomic per warp (ballot + popc). The march and the occlusion pass are persistent: a grid of a
+// few CTAs per SM whose warps claim the queue 64 entries at a time and refill a lane the moment its ray ends, so a
+// warp keeps 32 rays in flight however uneven their step counts. The scene's primitive table is staged into
+// shared memory by one bulk copy (cp.async.bulk + mbarrier) per CTA and read as broadcasts. Nothing is read back
+// by the host inside a sample: every kernel sizes itself from the device counters.
+#include "st_internal.h"
+
+namespace st {
+
+#define FULL_MASK 0xffffffffu
+#define INVALID_SLOT 0xffffffffu
+#define CLAIM 64u
+#define WAIT_LIMIT (1u << 24)
+
+__device__ __forceinline__ uint32_t lanemask_lt() {
+    uint32_t m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+
+// ------------------------------------------------------------------------------------------------------------
+// A TABLE INTO SHARED MEMORY BY ONE BULK COPY: thread 0 arms an mbarrier with the byte count and issues
+// cp.async.bulk; every thread waits on the barrier's phase, a bounded number of times. bytes is a multiple of 16,
+// both addresses 16-byte aligned (st_prim is 128 bytes, st_material 64, cudaMalloc 256-aligned). Returns false
+// (and flags the counters) if the copy did not land within the limit.
+// ------------------------------------------------------------------------------------------------------------
+__device__ __forceinline__ bool stage_table(void* sdst, const void* gsrc, uint32_t bytes, uint64_t* mbar,
+                                            DevCtr* ctr) {
+    uint32_t mb = (uint32_t)__cvta_generic_to_shared(mbar);
+    uint32_t dst = (uint32_t)__cvta_generic_to_shared(sdst);
+    if (threadIdx.x == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mb) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mb), "r"(bytes) : "memory");
+        asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                     ::"r"(dst), "l"(gsrc), "r"(bytes), "r"(mb) : "memory");
+    }
+    uint32_t done = 0;
+    for (uint32_t k = 0; k < WAIT_LIMIT && !done; k++) {
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(done) : "r"(mb) : "memory");
+    }
+    // one decision for the whole CTA, so no thread leaves while another still waits at a barrier
+    if (__syncthreads_or(!done)) {
+        if (threadIdx.x == 0) atomicExch(&ctr->pad0, 1u);
+        return false;
+    }
+    return true;
+}
+
+// ------------------------------------------------------------------------------------------------------------
+// THE ALBEDO TABLES (microfacet.js:245-330), the isotropic part: one thread per entry, a 32 x 32 stratified grid
+// warped toward the visible cap's rim.
+// ------------------------------------------------------------------------------------------------------------
+__global__ void k_mf_lut(float* ec, float* e1) {
+    uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t NEC = MF_NIOR * MF_NR * MF_NMU, NE1 = MF_NR * MF_NMU;
+    if (e >= NEC + NE1) return;
+    float ior = 1.f;
+    uint32_t k, j;
+    bool isE1 = false;
+    if (e < NEC) {
+        ior = 1.f + 2.f * float(e / (MF_NR * MF_NMU)) / float(MF_NIOR - 1);
+        k = (e / MF_NMU) % MF_NR; j = e % MF_NMU;
+    } else {
+        uint32_t t = e - NEC;
+        isE1 = true; k = t / MF_NMU; j = t % MF_NMU;
+    }
+    float r = float(k) / float(MF_NR - 1);
+    float mu = (float(j) + 0.5f) / float(MF_NMU);
+    float st = sqrtf(fmaxf(0.f, 1.f - mu * mu));
+    float a = fmaxf(r * r, MF_ALPHA_MIN);
+    f3 o = mk(st, 0.f, mu);
+    float acc = 0.f;
+    for (int sy = 0; sy < 32; sy++)
+        for (int sx = 0; sx < 32; sx++) {
+            float vx = (float(sx) + 0.5f) / 32.f, vy = (float(sy) + 0.5f) / 32.f;
+            float ux = vx, uy = 1.f - (1.f - vy) * (1.f - vy);
+            f3 h = mf_sample_vndf(o, a, ux, uy);
+            f3 i3 = reflectv(-o, h);
+            if (i3.z > 0.f) {
+                float fr = isE1 ? 1.f : fresnel_dielectric(dot(o, h), 1.f / ior);
+                acc += 2.f * (1.f - vy) * fr * mf_g2(o, i3, a) / mf_g1(o, a);
+            }
+        }
+    acc = acc / 1024.f;
+    if (e < NEC) ec[e] = acc; else e1[e - NEC] = acc;
+}
+__global__ void k_mf_avg(const float* ec, float* ecavg) {
+    uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= MF_NIOR * MF_NR) return;
+    float acc = 0.f;
+    for (int j = 0; j < MF_NMU; j++) {
+        float mu = (float(j) + 0.5f) / float(MF_NMU);
+        acc += 2.f * ec[e * MF_NMU + j] * mu / float(MF_NMU);
+    }
+    ecavg[e] = acc;
+}
+
+// ------------------------------------------------------------------------------------------------------------
+// GENRAYS (genrays.js:36-107): slot i is path (tile = i mod P) of sample (first + i / P)
+// ------------------------------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_genrays(WaveArgs a) {
+    const Uni& u = a.u;
+    const uint32_t first = a.ctr->sample;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < a.slots; i += gridDim.x * blockDim.x) {
+        uint32_t tile = i % u.P, j = i / u.P;
+        Rng rng = path_rng(sample_seed(u.seed, first + j), tile, 0);
+        float cx = float(tile % u.tilesX), cy = float(tile / u.tilesX);
+        float uv0x = (cx + 0.5f) * u.invTX, uv0y = (cy + 0.5f) * u.invTY;
+        float4 rnd = rng.next();
+        float ux = clampf(uv0x + (rnd.x - 0.5f) * u.invTX, 0.f, 1.f);
+        float uy = clampf(uv0y + (rnd.y - 0.5f) * u.invTY, 0.f, 1.f);
+        float xx = ux * 2.f - 1.f, yy = uy * 2.f - 1.f;
+        f3 pos, dir;
+        if (u.camtype == 0) {
+            f3 dc = mk(xx * u.fx, yy * u.fy, -1.f);
+            dir = normalize(u.right * dc.x + u.up * dc.y + u.fwd * dc.z);
+            pos = u.cam;
+        } else {
+            pos = u.cam + u.right * (xx * u.fx) + u.up * (yy * u.fy);
+            dir = -u.fwd;
+        }
+        dir = normalize(dir);
+        float px = clampf(ux * float(u.W), 0.f, float(u.W) - 1.f), py = clampf(uy * float(u.H), 0.f, float(u.H) - 1.f);
+        uint32_t pix = (uint32_t)px + (uint32_t)py * u.W;
+        a.pb.pos[i] = make_float4(pos.x, pos.y, pos.z, 0.f);
+        a.pb.dir[i] = make_float4(dir.x, dir.y, dir.z, 1.f);
+        a.pb.beta[i] = make_float4(1.f, 1.f, 1.f, 1.f);
+        a.pb.rad[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+        a.pb.meta[i] = make_uint4(pix, RAY_ACTIVE << 16, 0u, __float_as_uint(0.f));
+        a.q.ray[0][i] = i;
+    }
+}
+
+// a wavefront iteration's start: the queues it fills emptied (prog_flip)
+__global__ void k_iter_begin(DevCtr* ctr, int nxt, uint32_t slots, int first) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        if (first) ctr->rayCount[0] = slots;
+        ctr->rayCount[nxt] = 0u;
+        ctr->hitCount = 0u;
+        ctr->shadowCount = 0u;
+        ctr->marchHead = 0u;
+        ctr->occHead = 0u;
+        ctr->shadeHead = 0u;
+    }
+}
+
+// warp-aggregated append: one atomic per warp for every lane with want set; returns this lane's position
+__device__ __forceinline__ uint32_t warp_append(uint32_t* counter, bool want) {
+    uint32_t m = __ballot_sync(FULL_MASK, want);
+    uint32_t base = 0;
+    int lane = threadIdx.x & 31;
+    int leader = m ? __ffs(m) - 1 : 0;
+    if (m && lane == leader) base = atomicAdd(counter, (uint32_t)__popc(m));
+    base = __shfl_sync(FULL_MASK, base, leader);
+    return base + __popc(m & lanemask_lt());
+}
+
+// ------------------------------------------------------------------------------------------------------------
+// THE MARCH (wavefront.js:866-947), persistent. Each warp claims CLAIM queue entries at a time; a lane whose ray
+// ended takes the next one at once. A step: the scene's distance, the hit test against marchTol, lmax and
+// maxiter, the escape test; then the step of ea * stepscale. On the haze's collision (haze.js:280-288) the ray is
+// moved back to it and handed to shade as RAY_SCATTER.
+// ------------------------------------------------------------------------------------------------------------
+template <bool HAZE>
+__global__ void __launch_bounds__(256) k_march(WaveArgs a, int cur, int it) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    __shared__ __align__(8) uint64_t mbar;
+    st_prim* sp = reinterpret_cast<st_prim*>(smem);
+    const Uni& u = a.u;
+    if (!stage_table(sp, a.prims, u.n_prims * (uint32_t)sizeof(st_prim), &mbar, a.ctr)) return;
+    const uint32_t count = a.ctr->rayCount[cur];
+    const uint32_t* __restrict__ inq = a.q.ray[cur];
+    const int lane = threadIdx.x & 31;
+
+    uint32_t slot = INVALID_SLOT;
+    f3 pos = mk(0.f), dir = mk(0.f);
+    float ltot = 0.f, n = 1.f, tmax = 0.f;
+    uint32_t steps = 0;
+    uint32_t wpos = 0, wend = 0;
+    bool exhausted = false;
+    unsigned long long evals = 0;
+
+    for (;;) {
+        // ---- refill: idle lanes take the warp's next claimed entries ----
+        uint32_t idle = __ballot_sync(FULL_MASK, slot == INVALID_SLOT);
+        if (idle && !exhausted) {
+            if (wpos >= wend) {
+                uint32_t b = 0;
+                if (lane == 0) b = atomicAdd(&a.ctr->marchHead, CLAIM);
+                b = __shfl_sync(FULL_MASK, b, 0);
+                if (b >= count) exhausted = true;
+                else { wpos = b; wend = min(b + CLAIM, count); }
+            }
+            if (!exhausted) {
+                uint32_t avail = wend - wpos;
+                uint32_t rank = __popc(idle & lanemask_lt());
+                if (slot == INVALID_SLOT && rank < avail) {
+                    slot = inq[wpos + rank];
+                    float4 p4 = a.pb.pos[slot], d4 = a.pb.dir[slot];
+                    pos = xyz(p4); ltot = p4.w; dir = xyz(d4); n = d4.w;
+                    steps = a.pb.meta[slot].z;
+                    tmax = HAZE ? a.pb.rad[slot].w : 0.f;
+                    if (HAZE && tmax == 0.f) {
+                        // THE LEG'S COLLISION, drawn as it starts (haze.js:255-273 hazeDraw)
+                        tmax = -1.f;
+                        if (fabsf(n - 1.f) <= 1e-3f) {
+                            float absL = __uint_as_float(a.pb.meta[slot].w);
+                            f3 A = pos - dir * (fmaxf(ltot - absL, 0.f) / fmaxf(n, 1e-4f));
+                            float t0, t1;
+                            haze_span(u, A, dir, 1e30f, t0, t1);
+                            if (t1 > t0) {
+                                uint32_t tile = slot % u.P, j = slot / u.P;
+                                Rng hr = path_rng(sample_seed(u.seed, a.ctr->sample + j), tile, ST_SALT_HAZE + it);
+                                float4 r4 = hr.next();
+                                float t = t0 - logf(1.f - r4.x) / u.hsig;
+                                if (t < t1) tmax = fmaxf(absL + t * n, 1e-30f);
+                            }
+                        }
+                    }
+                }
+                wpos += min((uint32_t)__popc(idle), avail);
+            }
+        }
+        if (__ballot_sync(FULL_MASK, slot != INVALID_SLOT) == 0) break;
+
+        // ---- one step ----
+        bool fin = false;
+        uint32_t state = RAY_ACTIVE;
+        float dh = 0.f;
+        if (slot != INVALID_SLOT) {
+            if (HAZE && tmax > 0.f && ltot >= tmax) {
+                pos = pos - dir * ((ltot - tmax) / fmaxf(n, 1e-4f));
+                ltot = tmax;
+                state = RAY_SCATTER;
+                fin = true;
+            } else {
+                float d = scene_dist(sp, u.n_prims, pos);
+                evals++;
+                float ea = fabsf(d);
+                float eps = march_tol(pos, u.tol);
+                if (ltot > 1000.f || steps > u.maxiter) state = RAY_MAXITER;
+                if (dot(pos, dir) > 0.f && dot(pos, pos) > u.envR2) state = RAY_ESCAPED;
+                if (ea < eps || state != RAY_ACTIVE) {
+                    fin = true;
+                    dh = d;
+                } else {
+                    steps += 1;
+                    f3 off = dir * (ea * u.stepscale);
+                    pos = pos + off;
+                    ltot += length(off) * n;
+                }
+            }
+        }
+        uint32_t qp = warp_append(&a.ctr->hitCount, fin);
+        if (fin) {
+            a.pb.pos[slot] = make_float4(pos.x, pos.y, pos.z, ltot);
+            uint4 m = a.pb.meta[slot];
+            m.y = (m.y & 0xffffu) | (state << 16);
+            m.z = steps;
+            a.pb.meta[slot] = m;
+            if (HAZE) a.pb.rad[slot].w = tmax;
+            a.q.hit[qp] = slot;
+            a.q.hitd[qp] = dh;
+            slot = INVALID_SLOT;
+        }
+    }
+    // the steps taken, one atomic per warp
+    for (int o = 16; o > 0; o >>= 1) evals += __shfl_down_sync(FULL_MASK, evals, o);
+    if (lane == 0 && evals) atomicAdd(&a.ctr->march_steps, evals);
+}
+
+// ------------------------------------------------------------------------------------------------------------
+// THE DEPOSIT (wavefront.js:162-245): refused if a channel is NaN or inf or the luminance negative
+// ------------------------------------------------------------------------------------------------------------
+__device__ __forceinline__ bool bad_deposit(f3 c) {
+    return !isfinite(c.x) || !isfinite(c.y) || !isfinite(c.z) || luma(c) < 0.f;
+}
+__device__ __forceinline__ void deposit(float4* frame, uint32_t pix, f3 c, DevCtr* ctr) {
+    if (bad_deposit(c)) { atomicAdd(&ctr->nonfinite, 1u); return; }
+    float* f = reinterpret_cast<float*>(frame + pix);
+    if (c.x != 0.f) atomicAdd(f + 0, c.x);
+    if (c.y != 0.f) atomicAdd(f + 1, c.y);
+    if (c.z != 0.f) atomicAdd(f + 2, c.z);
+}
+
+// ------------------------------------------------------------------------------------------------------------
+// SHADE: what prog_surface asks the scene (the normal by three forward differences at normalTol, the material, the
+// medium beyond) and what prog_shade does with it (pathBegin..pathEnd, processMaterial_advanced's light sample and
+// lobe draw, the MIS weights, the bounce cap and roulette); an escaped ray's environment; a point in the haze
+// (haze.js:493-596 mediumVertex); the deposit of a path that ends. One thread per shade-queue entry.
+// ------------------------------------------------------------------------------------------------------------
+struct ShadowOut { bool valid; f3 org, dir, rad; float n; };
+
+__device__ __forceinline__ void shade_surface(const WaveArgs& a, const st_prim* sp, const st_material* sm,
+                                              f3& pos, f3& dir, float& ltot, float& n, f3& beta, float& sunmis,
+                                              f3& rad, uint32_t& bounces, uint32_t& state, float dh, Rng& rng,
+                                              bool last, ShadowOut& sh) {
+    const Uni& u = a.u;
+    float eps = march_tol(pos, u.tol);
+    float gx = scene_dist(sp, u.n_prims, mk(pos.x + eps, pos.y, pos.z)) - dh;
+    float gy = scene_dist(sp, u.n_prims, mk(pos.x, pos.y + eps, pos.z)) - dh;
+    float gz = scene_dist(sp, u.n_prims, mk(pos.x, pos.y, pos.z + eps)) - dh;
+    f3 nn = normalize(mk(gx, gy, gz));
+    bool inside = dh < 0.f;
+    f3 nrm = inside ? -nn : nn;                                       // pathFacing (scene_api.js:127-135)
+    float otol = 10.f * eps;                                          // offsetTol
+    if (dot(-dir, nrm) < 0.f) {                                       // leaving: moved on along its way, no bounce
+        f3 off = dir * otol;
+        pos = pos + off; ltot += length(off) * n;
+        return;
+    }
+    bounces += 1;
+    SceneHit h = scene_full(sp, u.n_prims, pos);
+    const st_material& m = sm[min(h.m, u.n_mats - 1)];
+    f3 emis = mk(m.emissive[0], m.emissive[1], m.emissive[2]);
+    if (max3(emis) > 0.f) {                                           // emitterHit (materials_pbr.js:1014-1075)
+        rad = rad + beta * emis;
+        state = RAY_SOURCE;
+        f3 off = dir * (otol * 2.f);
+        pos = pos + off; ltot += length(off) * n;
+        return;
+    }
+    float n0 = n;
+    float n1 = fmaxf(m.ior, n0);                                      // ownMedium
+    if (m.transmission > 0.f && m.metallic < 1.f) {                   // asksMedium -> mediumBeyond
+        SceneHit mb = scene_full(sp, u.n_prims, pos + (-nrm) * (otol * 2.f));
+        n1 = sm[min(mb.a, u.n_mats - 1)].ior;
+    }
+    float pG = sat(m.transmission);
+    float trans = m.transmission, specv = m.specular;
+    bool diffFace = false;
+    if (inside && pG > 0.f && pG < 1.f) {                             // materials_pbr.js:1150-1165
+        float k = mixf(2.f * m.specular, 1.f, pG);
+        float4 r4 = rng.next();
+        if (r4.x < pG) trans = 1.f;
+        else { trans = 0.f; specv = 0.5f * k; diffFace = true; }
+    }
+    float etaFace = diffFace ? fminf(n0, n1) / fmaxf(n0, n1) : n0 / n1;
+    Lobes lb = make_lobes(nrm, -dir, m, etaFace, a.tab, trans, specv);
+    lb.etaT = n0 / n1;
+    if (u.nee != 0u && !last) {                                       // light sampling (materials_pbr.js:1196-1330)
+        float4 u0 = rng.next();
+        float4 u1 = rng.next();
+        if (!lobes_none(m, trans)) {
+            f3 L = env_sample_dir(u, nrm, u0.x, u1.x, u1.y);
+            float NoL = dot(nrm, L);
+            float pL = env_pdf(u, L, nrm);
+            if (NoL > 0.f && pL > 0.f) {
+                f3 le = env_radiance(u, L);
+                f3 f = lobes_eval(lb, a.tab, L, 0.f);
+                float pB = lobes_pdf(lb, L);
+                float w = mis_weight(pL, pB);
+                f3 contrib = beta * f * le * (fabsf(NoL) * (w / pL));
+                if (max3(contrib) > 1e-7f) {
+                    float tr = 1.f;
+                    if (u.haze_on && fabsf(n - 1.f) <= 1e-3f) tr = haze_tr(u, pos, L, 2.f * u.envR + length(pos));
+                    sh.valid = true;
+                    sh.org = pos + nrm * (otol * 2.f);
+                    sh.dir = L;
+                    sh.rad = contrib * tr;
+                    sh.n = n;
+                }
+            }
+        }
+    }
+    LobeSample smp = lobes_sample(lb, a.tab, rng.next());           // the bounce
+    dir = smp.dir;
+    beta = beta * smp.w;
+    if (smp.transmitted) n = n1;
+    if (max3(smp.w) <= 0.f) state = RAY_ABSORBED;
+    if (u.nee != 0u && !last) {                                       // the other half of MIS (:1370-1395)
+        bool above = dot(nrm, dir) > 0.f && !smp.isDelta;
+        float pOut = smp.isDelta ? 0.f : lobes_pdf(lb, smp.dir);
+        float pLout = above ? env_pdf(u, dir, nrm) : 0.f;
+        sunmis = pLout <= 0.f ? 1.f : mis_weight(pOut, pLout);
+    } else {
+        sunmis = 1.f;
+    }
+    f3 off = dir * otol;
+    pos = pos + off; ltot += length(off) * n;
+    if (bounces > u.maxbounce) state = RAY_TERMINATED;                // pathEnd's tail (tracebasics.js:1040-1103)
+    if (u.rr != 0u && bounces >= 3u && state == RAY_ACTIVE) {
+        float p = clampf(max3(beta), 0.1f, 0.95f);
+        float4 r4 = rng.next();
+        if (r4.x > p) state = RAY_TERMINATED;
+        else beta = beta / p;
+    }
+}
+
+__device__ __forceinline__ void shade_medium(const WaveArgs& a, f3& pos, f3& dir, f3& beta, float& sunmis,
+                                             uint32_t& bounces, uint32_t& state, float n, Rng& rng, bool last,
+                                             ShadowOut& sh) {
+    const Uni& u = a.u;
+    state = RAY_ACTIVE;
+    bounces += 1;
+    float g = clampf(u.hg, -0.95f, 0.95f);
+    f3 din = dir;
+    beta = beta * u.halb;
+    if (u.nee != 0u && !last) {                                       // mediumNee (haze.js:318-405)
+        float4 u0 = rng.next();
+        float4 u1 = rng.next();
+        f3 L = env_sample_dir_m(u, u0.x, u1.x, u1.y);
+        float pL = env_pdf_m(u, L);
+        if (pL > 0.f) {
+            float ph = hg_eval(dot(din, L), g);
+            float w = mis_weight(pL, ph);
+            f3 le = env_radiance(u, L);
+            f3 contrib = beta * le * (ph * w / pL);
+            if (max3(contrib) > 1e-7f) {
+                float tr = haze_tr(u, pos, L, 2.f * u.envR + length(pos));
+                sh.valid = true; sh.org = pos; sh.dir = L; sh.rad = contrib * tr; sh.n = n;
+            }
+        }
+    }
+    float4 r2 = rng.next();
+    f3 dout = hg_sample(din, g, r2.x, r2.y);
+    dir = dout;
+    if (u.nee != 0u && !last) {
+        float pB = hg_eval(dot(din, dout), g);
+        float pL = env_pdf_m(u, dout);
+        sunmis = pL <= 0.f ? 1.f : mis_weight(pB, pL);
+    } else {
+        sunmis = 1.f;
+    }
+    if (bounces > u.maxbounce) state = RAY_TERMINATED;
+}
+
+__global__ void __launch_bounds__(256) k_shade(WaveArgs a, int nxt, int it, int last) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    __shared__ __align__(8) uint64_t mbar;
+    __shared__ __align__(8) uint64_t mbar2;
+    const Uni& u = a.u;
+    st_prim* sp = reinterpret_cast<st_prim*>(smem);
+    st_material* sm = reinterpret_cast<st_material*>(smem + u.n_prims * sizeof(st_prim));
+    if (!stage_table(sp, a.prims, u.n_prims * (uint32_t)sizeof(st_prim), &mbar, a.ctr)) return;
+    if (!stage_table(sm, a.mats, u.n_mats * (uint32_t)sizeof(st_material), &mbar2, a.ctr)) return;
+    const uint32_t count = a.ctr->hitCount;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    const uint32_t nrounds = (count + stride - 1) / stride;
+    unsigned long long paths = 0;
+    uint32_t flushed = 0;
+    for (uint32_t r = 0; r < nrounds; r++) {
+        uint32_t q = r * stride + blockIdx.x * blockDim.x + threadIdx.x;
+        bool valid = q < count;
+        bool cont = false;
+        ShadowOut sh; sh.valid = false;
+        uint32_t slot = 0, pix = 0, gpix = 0;
+        f3 pos, dir, beta, rad;
+        float ltot = 0.f, n = 1.f, sunmis = 1.f, tmax = 0.f;
+        uint4 m4 = make_uint4(0, 0, 0, 0);
+        uint32_t bounces = 0, state = RAY_TERMINATED;
+        if (valid) {
+            slot = a.q.hit[q];
+            float dh = a.q.hitd[q];
+            float4 p4 = a.pb.pos[slot], d4 = a.pb.dir[slot], b4 = a.pb.beta[slot], r4 = a.pb.rad[slot];
+            m4 = a.pb.meta[slot];
+            pos = xyz(p4); ltot = p4.w; dir = xyz(d4); n = d4.w; beta = xyz(b4); sunmis = b4.w;
+            rad = xyz(r4); tmax = r4.w;
+            pix = m4.x; bounces = m4.y & 0xffffu; state = m4.y >> 16;
+            gpix = (slot / u.P) * u.P + pix;                          // the pixel in the wave's frames
+            if (state == RAY_ESCAPED) {
+                rad = rad + beta * env_radiance(u, dir) * sunmis;     // wavefront.js:1303-1320
+            } else if (state == RAY_ACTIVE || state == RAY_SCATTER) {
+                uint32_t tile = slot % u.P, j = slot / u.P;
+                Rng rng = path_rng(sample_seed(u.seed, a.ctr->sample + j), tile, 1u + (uint32_t)it);
+                m4.w = __float_as_uint(ltot);                         // absorbAlong: absLtot on arrival
+                if (state == RAY_SCATTER)
+                    shade_medium(a, pos, dir, beta, sunmis, bounces, state, n, rng, last != 0, sh);
+                else
+                    shade_surface(a, sp, sm, pos, dir, ltot, n, beta, sunmis, rad, bounces, state, dh, rng,
+                                  last != 0, sh);
+                if (state == RAY_ACTIVE) {
+                    tmax = 0.f;                                       // a new leg
+                    if (last) { state = RAY_MAXITER; flushed++; }     // THE FLUSH
+                    else cont = true;
+                }
+            }
+        }
+        // the shadow ray, the ray on, the path's end: one append per warp each
+        uint32_t sq = warp_append(&a.ctr->shadowCount, sh.valid);
+        if (sh.valid) {
+            a.q.s_org[sq] = f4(sh.org, sh.n);
+            a.q.s_dir[sq] = f4(sh.dir, __uint_as_float(gpix));
+            a.q.s_rad[sq] = f4(sh.rad, 0.f);
+        }
+        uint32_t rq = warp_append(&a.ctr->rayCount[nxt], cont);
+        if (cont) {
+            a.pb.pos[slot] = f4(pos, ltot);
+            a.pb.dir[slot] = f4(dir, n);
+            a.pb.beta[slot] = f4(beta, sunmis);
+            a.pb.rad[slot] = f4(rad, tmax);
+            m4.y = bounces | (RAY_ACTIVE << 16);
+            a.pb.meta[slot] = m4;
+            a.q.ray[nxt][rq] = slot;
+        } else if (valid) {
+            // THE PATH IS OVER (wavefront.js:1400-1425): its radiance into this sample's frame, counted once
+            uint32_t j = slot / u.P;
+            float4* fr = a.frame + (size_t)j * u.P;
+            deposit(fr, pix, rad, a.ctr);
+            atomicAdd(&fr[pix].w, 1.f);
+            paths++;
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        paths += __shfl_down_sync(FULL_MASK, paths, o);
+        flushed += __shfl_down_sync(FULL_MASK, flushed, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        if (paths) atomicAdd(&a.ctr->paths, paths);
+        if (flushed) atomicAdd(&a.ctr->flushed, flushed);
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&a.ctr->segments, (unsigned long long)count);
+}
+
+// ------------------------------------------------------------------------------------------------------------
+// THE OCCLUSION PASS (wavefront.js:1481-1692), distance only, persistent with refill like the march: any surface
+// blocks; leaving the scene, lmax or maxiter reaches (maxiter counted in shadowcut); a ray that reaches deposits.
+// ------------------------------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_occlude(WaveArgs a) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    __shared__ __align__(8) uint64_t mbar;
+    st_prim* sp = reinterpret_cast<st_prim*>(smem);
+    const Uni& u = a.u;
+    if (!stage_table(sp, a.prims, u.n_prims * (uint32_t)sizeof(st_prim), &mbar, a.ctr)) return;
+    const uint32_t count = a.ctr->shadowCount;
+    const int lane = threadIdx.x & 31;
+    uint32_t idx = INVALID_SLOT;
+    f3 pos = mk(0.f), dir = mk(0.f);
+    float ltot = 0.f, n = 1.f;
+    uint32_t steps = 0;
+    uint32_t wpos = 0, wend = 0;
+    bool exhausted = false;
+    unsigned long long evals = 0, rays = 0;
+    uint32_t cuts = 0;
+    for (;;) {
+        uint32_t idle = __ballot_sync(FULL_MASK, idx == INVALID_SLOT);
+        if (idle && !exhausted) {
+            if (wpos >= wend) {
+                uint32_t b = 0;
+                if (lane == 0) b = atomicAdd(&a.ctr->occHead, CLAIM);
+                b = __shfl_sync(FULL_MASK, b, 0);
+                if (b >= count) exhausted = true;
+                else { wpos = b; wend = min(b + CLAIM, count); }
+            }
+            if (!exhausted) {
+                uint32_t avail = wend - wpos;
+                uint32_t rank = __popc(idle & lanemask_lt());
+                if (idx == INVALID_SLOT && rank < avail) {
+                    idx = wpos + rank;
+                    float4 o4 = a.q.s_org[idx], d4 = a.q.s_dir[idx];
+                    pos = xyz(o4); n = o4.w; dir = xyz(d4);
+                    ltot = 0.f; steps = 0;
+                    rays++;
+                }
+                wpos += min((uint32_t)__popc(idle), avail);
+            }
+        }
+        if (__ballot_sync(FULL_MASK, idx != INVALID_SLOT) == 0) break;
+        if (idx != INVALID_SLOT) {
+            float d = scene_dist(sp, u.n_prims, pos);
+            evals++;
+            float ea = fabsf(d);
+            float eps = march_tol(pos, u.tol);
+            bool blocked = false, reached = false;
+            if (ea < eps) blocked = true;
+            else if (dot(pos, dir) > 0.f && dot(pos, pos) > u.envR2) reached = true;
+            else {
+                steps += 1;
+                if (ltot > 1000.f || steps > u.maxiter) {
+                    reached = true;
+                    if (steps > u.maxiter) cuts++;
+                } else {
+                    f3 off = dir * (ea * u.stepscale);
+                    pos = pos + off;
+                    ltot += length(off) * n;
+                }
+            }
+            if (reached) {
+                float4 r4 = a.q.s_rad[idx];
+                float4 d4 = a.q.s_dir[idx];
+                uint32_t pix = __float_as_uint(d4.w);
+                // the pixel in the wave's frames: sample-in-wave * P + pixel (k_shade packs it)
+                deposit(a.frame, pix, xyz(r4), a.ctr);
+            }
+            if (blocked || reached) idx = INVALID_SLOT;
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        evals += __shfl_down_sync(FULL_MASK, evals, o);
+        rays += __shfl_down_sync(FULL_MASK, rays, o);
+        cuts += __shfl_down_sync(FULL_MASK, cuts, o);
+    }
+    if (lane == 0) {
+        if (evals) atomicAdd(&a.ctr->shadow_steps, evals);
+        if (rays) atomicAdd(&a.ctr->shadow_rays, rays);
+        if (cuts) atomicAdd(&a.ctr->shadowcut, cuts);
+    }
+}
+
+// ------------------------------------------------------------------------------------------------------------
+// RESOLVE (wavefront.js:414-494; measure.js:36-51), in FP64: each sample of the wave in order folded into the mean
+// and the error bar's moments, the frame taken and cleared in the same pass.
+// ------------------------------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_resolve(WaveArgs a) {
+    const Uni& u = a.u;
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i == 0) atomicAdd(&a.ctr->sample, a.spw);
+    if (i >= u.P) return;
+    Acc4 acc = a.acc[i];
+    double2 mo = a.mom[i];
+    for (uint32_t j = 0; j < a.spw; j++) {
+        float4 f = a.frame[(size_t)j * u.P + i];
+        a.frame[(size_t)j * u.P + i] = make_float4(0.f, 0.f, 0.f, 0.f);
+        uint32_t n = (uint32_t)f.w;
+        if (n == 0u) continue;
+        double sx = double(f.x) / n, sy = double(f.y) / n, sz = double(f.z) / n;
+        double prevn = u.maxaverages ? fmin(acc.w, double(u.maxaverages)) : acc.w;
+        double cnt = prevn + 1.0;
+        double px = fmin(fmax(acc.x, -1e20), 1e20), py = fmin(fmax(acc.y, -1e20), 1e20), pz = fmin(fmax(acc.z, -1e20), 1e20);
+        acc.x = (px * prevn + sx) / cnt;
+        acc.y = (py * prevn + sy) / cnt;
+        acc.z = (pz * prevn + sz) / cnt;
+        acc.w = cnt;
+        double y = sx * 0.2126 + sy * 0.7152 + sz * 0.0722;
+        double w = 1.0 / cnt;
+        double d = prevn > 0 ? y - (px * 0.2126 + py * 0.7152 + pz * 0.0722) : 0.0;
+        double v0 = fmin(fmax(mo.x, 0.0), 1e300), s0 = fmin(fmax(mo.y, 0.0), 1.0);
+        mo.x = (1 - w) * (v0 + w * d * d);
+        mo.y = (1 - w) * (1 - w) * s0 + w * w;
+    }
+    a.acc[i] = acc;
+    a.mom[i] = mo;
+}
+
+// ------------------------------------------------------------------------------------------------------------
+// launch wrappers
+// ------------------------------------------------------------------------------------------------------------
+static int g_occ_march = 0, g_occ_occl = 0, g_occ_shade = 0;
+
+cudaError_t launch_mf_tables(float* ec, float* ecavg, float* e1, cudaStream_t s) {
+    const uint32_t N = MF_NIOR * MF_NR * MF_NMU + MF_NR * MF_NMU;
+    k_mf_lut<<<(N + 127) / 128, 128, 0, s>>>(ec, e1);
+    k_mf_avg<<<(MF_NIOR * MF_NR + 127) / 128, 128, 0, s>>>(ec, ecavg);
+    return cudaGetLastError();
+}
+cudaError_t launch_genrays(const WaveArgs& a, int sms, cudaStream_t s) {
+    uint32_t blocks = min((a.slots + 255) / 256, (uint32_t)sms * 8u);
+    k_genrays<<<blocks, 256, 0, s>>>(a);
+    return cudaGetLastError();
+}
+cudaError_t launch_iter_begin(const WaveArgs& a, int nxt, int first, cudaStream_t s) {
+    k_iter_begin<<<1, 32, 0, s>>>(a.ctr, nxt, a.slots, first);
+    return cudaGetLastError();
+}
+static int occupancy(const void* fn, size_t smem) {
+    int nb = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, 256, smem);
+    return nb > 0 ? nb : 1;
+}
+cudaError_t launch_march(const WaveArgs& a, int cur, int it, int sms, cudaStream_t s) {
+    size_t smem = a.u.n_prims * sizeof(st_prim);
+    if (a.u.haze_on) {
+        if (smem > 48 * 1024) cudaFuncSetAttribute(k_march<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        int nb = occupancy((const void*)k_march<true>, smem);
+        k_march<true><<<sms * nb, 256, smem, s>>>(a, cur, it);
+    } else {
+        if (smem > 48 * 1024) cudaFuncSetAttribute(k_march<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (!g_occ_march) g_occ_march = occupancy((const void*)k_march<false>, 32 * 1024);
+        k_march<false><<<sms * g_occ_march, 256, smem, s>>>(a, cur, it);
+    }
+    return cudaGetLastError();
+}
+cudaError_t launch_shade(const WaveArgs& a, int nxt, int it, int last, int sms, cudaStream_t s) {
+    size_t smem = a.u.n_prims * sizeof(st_prim) + a.u.n_mats * sizeof(st_material);
+    if (smem > 48 * 1024) cudaFuncSetAttribute(k_shade, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (!g_occ_shade) g_occ_shade = occupancy((const void*)k_shade, 48 * 1024);
+    k_shade<<<sms * g_occ_shade, 256, smem, s>>>(a, nxt, it, last);
+    return cudaGetLastError();
+}
+cudaError_t launch_occlude(const WaveArgs& a, int sms, cudaStream_t s) {
+    size_t smem = a.u.n_prims * sizeof(st_prim);
+    if (smem > 48 * 1024) cudaFuncSetAttribute(k_occlude, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (!g_occ_occl) g_occ_occl = occupancy((const void*)k_occlude, 32 * 1024);
+    k_occlude<<<sms * g_occ_occl, 256, smem, s>>>(a);
+    return cudaGetLastError();
+}
+cudaError_t launch_resolve(const WaveArgs& a, cudaStream_t s) {
+    k_resolve<<<(a.u.P + 255) / 256, 256, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+}  // namespace st

@@ -1,0 +1,162 @@
+"""The renderer facade: the reference's createPathTracer / RT (lib/pathtracer/index.js:90, contract in
+lib/pathtracer/README.md:38-124), over the C ABI of libshadytracer.so.
+
+    rt = create_path_tracer(scene)     # createPathTracer({scene, ...}); RT.init()
+    rt.set(maxbounce=8)                # RT.set(values) -> the keys it did not recognise
+    rt.step(16)                        # RT.step(n): returns when the GPU has finished
+    rt.image_stats()                   # RT.imageStats()
+    rt.measure(x, y)                   # RT.measure: the pixel's luminance and its standard error
+    rt.set_scene(other)                # RT.setScene(s): on a failed build the old scene is kept
+    rt.invalidate()                    # RT.invalidate()
+
+Errors are exceptions (StError), as the reference's are (core/raytrace_main.js:1580-1581). Everything runs on the
+GPU through the library; a missing library or GPU raises.
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import st_types as T
+from ._lib import load, check, StError  # noqa: F401
+
+PARAM_KEYS = [f for f, _ in T.StParams._fields_]
+
+
+class PathTracer:
+    def __init__(self, scene=None, device=0):
+        self.L = load()
+        self.ctx = C.c_void_p()
+        check(self.L.st_create(device, C.byref(self.ctx)), None, "st_create (no GPU, or no device %d)" % device)
+        self.params = None
+        self.view = None
+        self.scene = None
+        if scene is not None:
+            self.set_scene(scene)
+            self.set_params(scene.params)
+            self.set_view(scene.view)
+
+    # ---- life cycle ----
+    def close(self):
+        if self.ctx:
+            self.L.st_destroy(self.ctx)
+            self.ctx = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # ---- the scene, the settings, the camera ----
+    def set_scene(self, scene):
+        err = C.create_string_buffer(512)
+        rc = self.L.st_set_scene(self.ctx, None, C.byref(scene.desc), err, 512)
+        if rc != 0:
+            raise StError(rc, "setScene: " + err.value.decode(errors="replace"))
+        self.scene = scene
+
+    def set_params(self, p):
+        check(self.L.st_set_params(self.ctx, C.byref(p), None), self.ctx, "st_set_params")
+        self.params = T.StParams.from_buffer_copy(p)
+
+    def set_view(self, v):
+        check(self.L.st_set_view(self.ctx, C.byref(v)), self.ctx, "st_set_view")
+        self.view = v
+
+    def set(self, reset=True, **values):
+        """RT.set(values): applies the settings it knows, returns the names it does not (README.md:56)."""
+        p = T.StParams.from_buffer_copy(self.params) if self.params else T.default_params()
+        unknown = []
+        for k, v in values.items():
+            if k in PARAM_KEYS:
+                setattr(p, k, v)
+            else:
+                unknown.append(k)
+        self.set_params(p)
+        return unknown
+
+    def get(self):
+        return {k: getattr(self.params, k) for k in PARAM_KEYS} if self.params else {}
+
+    def invalidate(self):
+        check(self.L.st_invalidate(self.ctx), self.ctx, "st_invalidate")
+
+    # ---- tracing ----
+    def step(self, n=1):
+        check(self.L.st_step(self.ctx, int(n)), self.ctx, "st_step")
+
+    def step_async(self, n=1):
+        check(self.L.st_step_async(self.ctx, int(n)), self.ctx, "st_step_async")
+
+    def sync(self, timeout_ms=-1):
+        check(self.L.st_sync(self.ctx, int(timeout_ms)), self.ctx, "st_sync")
+
+    # ---- readings ----
+    def read_accum(self):
+        """(rgb HxWx3, V HxW, S HxW, count HxW): the FP64 mean, the error bar's moments, the samples per pixel."""
+        W, H = self.params.width, self.params.height
+        rgb = np.zeros((H, W, 3), np.float64)
+        V = np.zeros((H, W), np.float64)
+        S = np.zeros((H, W), np.float64)
+        cnt = np.zeros((H, W), np.uint32)
+        P = C.c_void_p
+        check(self.L.st_read_accum(self.ctx, rgb.ctypes.data_as(P), V.ctypes.data_as(P), S.ctypes.data_as(P),
+                                   cnt.ctypes.data_as(P)), self.ctx, "st_read_accum")
+        return rgb, V, S, cnt
+
+    def image_stats(self):
+        s = T.StImageStats()
+        check(self.L.st_image_stats(self.ctx, C.byref(s)), self.ctx, "st_image_stats")
+        return {f: getattr(s, f) for f, _ in T.StImageStats._fields_}
+
+    def counters(self):
+        c = T.StCounters()
+        check(self.L.st_read_counters(self.ctx, C.byref(c)), self.ctx, "st_read_counters")
+        return {f: getattr(c, f) for f, _ in T.StCounters._fields_}
+
+    def measure(self, x, y):
+        """The reading at pixel (x, y), row 0 the bottom (core/measure.js:56-66 reading): L, se, nEff, count."""
+        rgb, V, S, cnt = self.read_accum()
+        c = int(cnt[y, x])
+        if not c:
+            return None
+        L = float(rgb[y, x] @ np.array([0.2126, 0.7152, 0.0722]))
+        s, v = float(S[y, x]), float(V[y, x])
+        se = float(np.sqrt(s * v / (1 - s))) if 0 < s < 1 and v >= 0 else None
+        return {"L": L, "se": se, "nEff": 1.0 / s if s > 0 else None, "count": c, "rgb": rgb[y, x].tolist()}
+
+    def mf_tables(self):
+        ec = np.zeros(16 * 32 * 32, np.float32)
+        ecavg = np.zeros(16 * 32, np.float32)
+        e1 = np.zeros(32 * 32, np.float32)
+        P = C.c_void_p
+        check(self.L.st_mf_tables(self.ctx, ec.ctypes.data_as(P), ecavg.ctypes.data_as(P), e1.ctypes.data_as(P)),
+              self.ctx, "st_mf_tables")
+        return ec, ecavg, e1
+
+    # ---- kernel times (core/kerneltime.js) ----
+    def enable_kernel_times(self, on=True):
+        check(self.L.st_enable_kernel_times(self.ctx, 1 if on else 0), self.ctx, "st_enable_kernel_times")
+
+    def kernel_times(self):
+        buf = (T.StKernelTime * 32)()
+        n = C.c_int()
+        check(self.L.st_kernel_times(self.ctx, buf, 32, C.byref(n)), self.ctx, "st_kernel_times")
+        return {buf[i].name.decode(): (buf[i].launches, buf[i].ms) for i in range(min(n.value, 32))}
+
+    def reset_kernel_times(self):
+        check(self.L.st_reset_kernel_times(self.ctx), self.ctx, "st_reset_kernel_times")
+
+    def stream(self):
+        return self.L.st_stream(self.ctx)
+
+
+def create_path_tracer(scene=None, device=0):
+    """createPathTracer (lib/pathtracer/index.js:90) + RT.init: a context on `device` with `scene` loaded."""
+    return PathTracer(scene, device)

@@ -1,0 +1,246 @@
+"""The workloads, as scene tables: the scene-as-data form of the reference's scene contract.
+
+A scene here is what the reference's builder generates (builder/codegen.js:974-1060 generate -> an SDF and a
+getMaterial2) written as data: a table of primitives folded the way core/scene_api.js:28-80 folds them, and a
+material table (core/materials.js:12-60 Material2, the fields the hot path reads). Material 0 is the air.
+
+Each builder returns a `Scene` holding the ctypes arrays (kept alive here) and the st_scene_desc that points
+at them, plus the st_params and st_view of its workload.
+"""
+import ctypes as C
+import math
+
+from .st_types import (StPrim, StMaterial, StSceneDesc, StView, default_params,
+                       ST_PRIM_PLANE, ST_PRIM_SPHERE, ST_PRIM_BOX, ST_PRIM_ROUNDBOX, ST_PRIM_TORUS,
+                       ST_PRIM_PRISM, ST_PRIM_ASPHERE, ST_PRIM_CYLINDER,
+                       ST_OP_ITEM, ST_OP_SMOOTH, ST_OP_UNION, ST_OP_SUB)
+
+IDENTITY = (1.0, 0.0, 0.0, 0.0, 1.0, 0.0, 0.0, 0.0, 1.0)
+
+
+class Scene:
+    def __init__(self, prims, materials, env_radius=400.0, tolerance=0.0, haze=None, name="scene"):
+        self.name = name
+        self.prim_list = list(prims)
+        self.material_list = list(materials)
+        self.prims = (StPrim * len(prims))(*prims)
+        self.materials = (StMaterial * len(materials))(*materials)
+        d = StSceneDesc()
+        d.prims = C.cast(self.prims, C.POINTER(StPrim))
+        d.n_prims = len(prims)
+        d.materials = C.cast(self.materials, C.POINTER(StMaterial))
+        d.n_materials = len(materials)
+        d.env_radius = env_radius
+        d.tolerance = tolerance
+        for i in range(9):
+            d.haze_axes[i] = IDENTITY[i]
+        if haze:
+            for i in range(3):
+                d.haze_centre[i] = haze["centre"][i]
+                d.haze_half[i] = haze["half"][i]
+                d.haze_albedo[i] = haze.get("albedo", (1.0, 1.0, 1.0))[i]
+            d.haze_sigma_t = haze["sigma_t"]
+            d.haze_g = haze.get("g", 0.0)
+            if "axes" in haze:
+                for i in range(9):
+                    d.haze_axes[i] = haze["axes"][i]
+        self.desc = d
+        self.params = None
+        self.view = None
+        self.info = {}
+
+
+def prim(type_, pos=(0, 0, 0), params=(), material=1, op=ST_OP_ITEM, k=0.0, rot=IDENTITY, flags=0):
+    p = StPrim()
+    p.type, p.op, p.material, p.flags = type_, op, material, flags
+    for i in range(3):
+        p.pos[i] = pos[i]
+    p.k = k
+    for i in range(9):
+        p.rot[i] = rot[i]
+    for i, v in enumerate(params):
+        p.p[i] = v
+    return p
+
+
+def material(base=(0.8, 0.8, 0.8), metallic=0.0, roughness=0.5, specular=0.5, specular_tint=0.0,
+             transmission=0.0, ior=1.0, abbe=0.0, attenuation=0.0, detector=0.0, emissive=(0, 0, 0)):
+    """makeDefaultMaterial's defaults (core/materials.js:170-191), then the fields given."""
+    m = StMaterial()
+    for i in range(3):
+        m.base[i] = base[i]
+        m.emissive[i] = emissive[i]
+    m.metallic, m.roughness, m.specular, m.specular_tint = metallic, roughness, specular, specular_tint
+    m.transmission, m.ior, m.abbe, m.attenuation, m.detector = transmission, ior, abbe, attenuation, detector
+    return m
+
+
+def air():
+    return material(base=(1, 1, 1), specular=0.0, ior=1.0)
+
+
+def diffuse(c, roughness=1.0):
+    """makeDiffuse (core/materials.js:197-207): a Lambertian of albedo c exactly, no coat."""
+    return material(base=c, metallic=0.0, roughness=roughness, specular=0.0, transmission=0.0, ior=1.5)
+
+
+def plastic(c, roughness, specular=0.5):
+    """makePlastic (core/materials.js:220-229)."""
+    return material(base=c, metallic=0.0, roughness=roughness, specular=specular, transmission=0.0, ior=1.5)
+
+
+def metal(c, roughness):
+    """makeMetal (core/materials.js:231-239)."""
+    return material(base=c, metallic=1.0, roughness=roughness, specular=1.0, transmission=0.0)
+
+
+def glass(c=(1, 1, 1), ior=1.5, roughness=0.0, abbe=0.0):
+    """makeGlassSmooth / makeGlassRough (core/materials.js:241-256)."""
+    return material(base=c, metallic=0.0, roughness=roughness, specular=0.5, transmission=1.0, ior=max(ior, 1.0),
+                    abbe=abbe)
+
+
+def look_at(eye, target, vfov_deg, aspect, up=(0.0, 0.0, 1.0)):
+    """The camera as genrays reads it (core/genrays.js:65-92): right, up and fwd (target -> camera) from the
+    view, fx = tan(fov/2) * aspect, fy = tan(fov/2)."""
+    d = [target[i] - eye[i] for i in range(3)]
+    ln = math.sqrt(sum(x * x for x in d))
+    d = [x / ln for x in d]
+    r = [d[1] * up[2] - d[2] * up[1], d[2] * up[0] - d[0] * up[2], d[0] * up[1] - d[1] * up[0]]
+    ln = math.sqrt(sum(x * x for x in r))
+    r = [x / ln for x in r]
+    u = [r[1] * d[2] - r[2] * d[1], r[2] * d[0] - r[0] * d[2], r[0] * d[1] - r[1] * d[0]]
+    v = StView()
+    for i in range(3):
+        v.cam_pos[i] = eye[i]
+        v.right[i] = r[i]
+        v.up[i] = u[i]
+        v.fwd[i] = -d[i]
+    fy = math.tan(math.radians(vfov_deg) / 2)
+    v.fy = fy
+    v.fx = fy * aspect
+    v.camtype = 0
+    return v
+
+
+def rot_from_quat(q):
+    """World -> local rotation (row major) of the unit quaternion q = (w, x, y, z): the transpose of its matrix."""
+    w, x, y, z = q
+    m = [1 - 2 * (y * y + z * z), 2 * (x * y - w * z), 2 * (x * z + w * y),
+         2 * (x * y + w * z), 1 - 2 * (x * x + z * z), 2 * (y * z - w * x),
+         2 * (x * z - w * y), 2 * (y * z + w * x), 1 - 2 * (x * x + y * y)]
+    return (m[0], m[3], m[6], m[1], m[4], m[7], m[2], m[5], m[8])
+
+
+class Pcg32:
+    """PCG32 (O'Neill 2014, XSH RR 64/32), the seeded generator the room's primitives are drawn from."""
+
+    def __init__(self, seed, seq=54):
+        self.state = 0
+        self.inc = ((seq << 1) | 1) & 0xFFFFFFFFFFFFFFFF
+        self.next_u32()
+        self.state = (self.state + seed) & 0xFFFFFFFFFFFFFFFF
+        self.next_u32()
+
+    def next_u32(self):
+        old = self.state
+        self.state = (old * 6364136223846793005 + self.inc) & 0xFFFFFFFFFFFFFFFF
+        xs = (((old >> 18) ^ old) >> 27) & 0xFFFFFFFF
+        rot = old >> 59
+        return ((xs >> rot) | (xs << ((-rot) & 31))) & 0xFFFFFFFF
+
+    def uniform(self, lo=0.0, hi=1.0):
+        return lo + (hi - lo) * (self.next_u32() / 4294967296.0)
+
+
+# ---------------------------------------------------------------------------------------------------------------
+# Config 1: the photometry row (lib/pathtracer/tests.js:447-509): a white floor under a uniform environment.
+# ---------------------------------------------------------------------------------------------------------------
+def floor_furnace(width=256, height=256, spp=16, albedo=0.8, sky=1000.0, maxbounce=4, seed=1):
+    """An infinite Lambertian floor (reflectance `albedo`, the plane z = 0) under a uniform environment of `sky`
+    cd/m^2, a pinhole camera 1 m above it looking 30 degrees down (vertical field 70 degrees). Closed form: every
+    floor pixel is albedo * sky, every sky pixel sky."""
+    s = Scene([prim(ST_PRIM_PLANE, material=1)], [air(), diffuse((albedo, albedo, albedo))], name="floor")
+    s.params = default_params(width=width, height=height, maxbounce=maxbounce, env_uniform=sky, sun_hint=0,
+                              seed=seed)
+    pitch = math.radians(30.0)
+    eye = (0.0, 0.0, 1.0)
+    target = (0.0, math.cos(pitch), 1.0 - math.sin(pitch))
+    s.view = look_at(eye, target, 70.0, width / height)
+    s.info = {"spp": spp, "closed_form_floor": albedo * sky, "closed_form_sky": sky, "workload": "floor-256"}
+    return s
+
+
+# ---------------------------------------------------------------------------------------------------------------
+# Config 2: the path-traced SDF room.
+# ---------------------------------------------------------------------------------------------------------------
+ROOM_HALF = (3.0, 2.0, 1.5)          # a 6 x 4 x 3 m room, floor at z = 0
+ROOM_WALL = 0.1
+
+
+def sdf_room(width=1920, height=1080, spp=64, maxbounce=8, seed=1, n_prims=24, prim_seed=2):
+    """A 6 x 4 x 3 m room (its walls a hollow box 0.1 m thick, a 2 x 1.5 m window in the +y wall) holding
+    `n_prims` primitives drawn from PCG32(prim_seed): types uniform over {box, sphere, torus, rounded prism}, sizes
+    0.15-0.4 m, placed uniformly in the room, randomly turned, smooth-unioned in order with radii U(0.02, 0.1) m.
+    Materials: roughness U(0.05, 1), albedo U(0.2, 0.9) per channel, 20 % metallic (the rest plastic). Lit by a
+    100 klx sun (0.53 degrees, 35 degrees up) and a uniform sky of 10 klx on the level (3183 cd/m^2) through the
+    window. March tolerance 1e-4 m."""
+    rng = Pcg32(prim_seed)
+    mats = [air(), diffuse((0.75, 0.73, 0.70))]
+    hx, hy, hz = ROOM_HALF
+    t = ROOM_WALL
+    prims = [
+        prim(ST_PRIM_BOX, pos=(0, 0, hz), params=(hx + t, hy + t, hz + t), material=1, op=ST_OP_ITEM),
+        prim(ST_PRIM_BOX, pos=(0, 0, hz), params=(hx, hy, hz), material=1, op=ST_OP_SUB),
+        prim(ST_PRIM_BOX, pos=(0.0, hy + t / 2, 1.65), params=(1.0, t, 0.75), material=1, op=ST_OP_SUB),
+    ]
+    kinds = [ST_PRIM_BOX, ST_PRIM_SPHERE, ST_PRIM_TORUS, ST_PRIM_PRISM]
+    for i in range(n_prims):
+        kind = kinds[min(3, int(rng.uniform() * 4))]
+        size = rng.uniform(0.15, 0.4)
+        pos = (rng.uniform(-hx + 0.5, hx - 0.5), rng.uniform(-hy + 0.5, hy - 0.5), rng.uniform(0.3, 2 * hz - 0.5))
+        # a uniformly random rotation (Shoemake's quaternion from three uniforms)
+        u1, u2, u3 = rng.uniform(), rng.uniform(), rng.uniform()
+        q = (math.sqrt(1 - u1) * math.sin(2 * math.pi * u2), math.sqrt(1 - u1) * math.cos(2 * math.pi * u2),
+             math.sqrt(u1) * math.sin(2 * math.pi * u3), math.sqrt(u1) * math.cos(2 * math.pi * u3))
+        k = rng.uniform(0.02, 0.1)
+        rough = rng.uniform(0.05, 1.0)
+        albedo = (rng.uniform(0.2, 0.9), rng.uniform(0.2, 0.9), rng.uniform(0.2, 0.9))
+        is_metal = rng.uniform() < 0.2
+        mats.append(metal(albedo, rough) if is_metal else plastic(albedo, rough))
+        if kind == ST_PRIM_BOX:
+            params = (size, size * rng.uniform(0.5, 1.0), size * rng.uniform(0.5, 1.0))
+        elif kind == ST_PRIM_SPHERE:
+            params = (size,)
+        elif kind == ST_PRIM_TORUS:
+            params = (size, size * rng.uniform(0.2, 0.45))
+        else:
+            params = (float(3 + int(rng.uniform() * 4)), size, size * rng.uniform(0.8, 2.0), 0.02)
+        prims.append(prim(kind, pos=pos, params=params, material=len(mats) - 1,
+                          op=ST_OP_ITEM if i == 0 else ST_OP_SMOOTH, k=k, rot=rot_from_quat(q)))
+    s = Scene(prims, mats, env_radius=20.0, name="room24")
+    s.params = default_params(width=width, height=height, maxbounce=maxbounce, sun_elevation=35.0, sun_azimuth=20.0,
+                              sun_illuminance=100000.0, sky_luminance=10000.0 / math.pi, ground_luminance=1000.0,
+                              eps=1e-4, seed=seed)
+    eye = (-2.6, -1.6, 1.7)
+    target = (0.8, 0.9, 1.1)
+    s.view = look_at(eye, target, 60.0, width / height)
+    s.info = {"spp": spp, "workload": "room24-1080p", "paths": width * height * spp}
+    return s
+
+
+# ---------------------------------------------------------------------------------------------------------------
+# Config 4: the haze box (lib/pathtracer/tests.js:1818-1866 'haze' row; core/haze.js).
+# ---------------------------------------------------------------------------------------------------------------
+def haze_furnace(width=64, height=64, sigma_t=0.2, g=0.0, albedo=1.0, sky=1000.0, maxbounce=32, seed=1):
+    """The haze row's furnace: an albedo-1 haze box (2 x 2 x 4 m) in a uniform environment with nothing else in
+    it but a far-away dark plane the camera never sees -- every pixel must read `sky` exactly, whatever sigma_t and
+    g (energy conservation: what the dust scatters out of a camera ray it scatters back in)."""
+    s = Scene([prim(ST_PRIM_PLANE, pos=(0, 0, -50.0), material=1)], [air(), diffuse((1.0, 1.0, 1.0))],
+              env_radius=40.0,
+              haze={"centre": (0.0, 0.0, 2.0), "half": (1.0, 1.0, 2.0), "sigma_t": sigma_t, "g": g,
+                    "albedo": (albedo, albedo, albedo)}, name="haze-furnace")
+    s.params = default_params(width=width, height=height, maxbounce=maxbounce, env_uniform=sky, sun_hint=0, seed=seed)
+    s.view = look_at((0.0, -6.0, 2.0), (0.0, 0.0, 2.0), 50.0, width / height)
+    s.info = {"closed_form": sky}
+    return s

@@ -1,0 +1,140 @@
+"""ctypes mirrors of the C ABI's structs (include/shadytracer.h), field for field.
+
+The host side (renderer.py, optics.py) fills these and passes pointers across the boundary; nothing here
+computes. A struct whose size drifts from the header's is caught by tests/test_capi.py, which compares
+ctypes.sizeof against the sizes the library itself reports.
+"""
+import ctypes as C
+
+ST_OK = 0
+ST_ERR_ARG = -1
+ST_ERR_OOM = -2
+ST_ERR_CUDA = -3
+ST_ERR_TIMEOUT = -4
+ST_ERR_BUSY = -5
+ST_ERR_COMPILE = -6
+ST_ERR_STATE = -7
+
+ST_PRIM_PLANE, ST_PRIM_SPHERE, ST_PRIM_BOX, ST_PRIM_ROUNDBOX, ST_PRIM_TORUS, ST_PRIM_PRISM, \
+    ST_PRIM_ASPHERE, ST_PRIM_CYLINDER = range(8)
+ST_OP_ITEM, ST_OP_SMOOTH, ST_OP_UNION, ST_OP_SUB = range(4)
+ST_MAX_PRIMS = 256
+ST_MAX_MATERIALS = 256
+
+
+class StPrim(C.Structure):
+    _fields_ = [("type", C.c_uint32), ("op", C.c_uint32), ("material", C.c_uint32), ("flags", C.c_uint32),
+                ("pos", C.c_float * 3), ("k", C.c_float),
+                ("rot", C.c_float * 9), ("pad0", C.c_float * 3),
+                ("p", C.c_float * 12)]
+
+
+class StMaterial(C.Structure):
+    _fields_ = [("base", C.c_float * 3), ("metallic", C.c_float),
+                ("roughness", C.c_float), ("specular", C.c_float), ("specular_tint", C.c_float),
+                ("transmission", C.c_float), ("ior", C.c_float), ("abbe", C.c_float),
+                ("attenuation", C.c_float), ("detector", C.c_float),
+                ("emissive", C.c_float * 3), ("pad", C.c_float)]
+
+
+class StSceneDesc(C.Structure):
+    _fields_ = [("prims", C.POINTER(StPrim)), ("n_prims", C.c_uint32),
+                ("materials", C.POINTER(StMaterial)), ("n_materials", C.c_uint32),
+                ("env_radius", C.c_float), ("tolerance", C.c_float),
+                ("haze_centre", C.c_float * 3), ("haze_sigma_t", C.c_float),
+                ("haze_axes", C.c_float * 9), ("haze_half", C.c_float * 3),
+                ("haze_albedo", C.c_float * 3), ("haze_g", C.c_float)]
+
+
+class StParams(C.Structure):
+    _fields_ = [("width", C.c_uint32), ("height", C.c_uint32),
+                ("maxbounce", C.c_uint32), ("maxiter", C.c_uint32), ("stepscale", C.c_float),
+                ("nee", C.c_uint32), ("rr", C.c_uint32), ("nee_sun_pick", C.c_float),
+                ("sun_elevation", C.c_float), ("sun_azimuth", C.c_float), ("sun_diameter", C.c_float),
+                ("sun_illuminance", C.c_float), ("sky_luminance", C.c_float), ("ground_luminance", C.c_float),
+                ("env_uniform", C.c_float), ("env_sun_gain", C.c_float), ("env_sky_gain", C.c_float),
+                ("sun_hint", C.c_uint32), ("seed", C.c_uint32), ("maxaverages", C.c_uint32),
+                ("eps", C.c_float), ("budget", C.c_uint32), ("samples_per_wave", C.c_uint32)]
+
+
+class StView(C.Structure):
+    _fields_ = [("cam_pos", C.c_float * 3), ("right", C.c_float * 3), ("up", C.c_float * 3),
+                ("fwd", C.c_float * 3), ("fx", C.c_float), ("fy", C.c_float), ("camtype", C.c_uint32)]
+
+
+class StCounters(C.Structure):
+    _fields_ = [("paths", C.c_uint64), ("segments", C.c_uint64), ("march_steps", C.c_uint64),
+                ("shadow_rays", C.c_uint64), ("shadow_steps", C.c_uint64),
+                ("nonfinite", C.c_uint32), ("flushed", C.c_uint32), ("shadowcut", C.c_uint32),
+                ("samples", C.c_uint32)]
+
+
+class StImageStats(C.Structure):
+    _fields_ = [("mean_luma", C.c_double), ("median_luma", C.c_double), ("trimmed_mean_luma", C.c_double),
+                ("mean_rel_se", C.c_double), ("sampled", C.c_uint32), ("samples", C.c_uint32)]
+
+
+class StKernelTime(C.Structure):
+    _fields_ = [("name", C.c_char * 24), ("launches", C.c_uint32), ("ms", C.c_double)]
+
+
+class StSppmStats(C.Structure):
+    _fields_ = [("stored", C.c_uint32), ("gathers", C.c_uint32), ("cut", C.c_uint32),
+                ("visits_max", C.c_uint32), ("visits", C.c_uint64)]
+
+
+class StOpticsSource(C.Structure):
+    _fields_ = [("centre", C.c_float * 3), ("flux", C.c_float),
+                ("axis", C.c_float * 3), ("shape", C.c_uint32),
+                ("tangent", C.c_float * 3), ("size_x", C.c_float),
+                ("size_y", C.c_float), ("dist", C.c_uint32), ("cos_half", C.c_float), ("n_exp", C.c_float),
+                ("emit_n", C.c_float), ("two_sided", C.c_uint32), ("on_surface", C.c_uint32),
+                ("instance", C.c_uint32)]
+
+
+class StOpticsFar(C.Structure):
+    _fields_ = [("nC", C.c_uint32), ("nG", C.c_uint32), ("axis", C.c_float * 3), ("c0", C.c_float * 3)]
+
+
+class StOpticsBatch(C.Structure):
+    _fields_ = [("n_instances", C.c_uint32), ("ray_count", C.POINTER(C.c_uint32)),
+                ("lux_cells", C.c_uint32), ("lux_half", C.c_float), ("lux_height", C.c_float),
+                ("maxbounce", C.c_uint32), ("seed", C.c_uint32)]
+
+
+class StOpticsTotals(C.Structure):
+    _fields_ = [("emitted", C.c_double), ("escaped", C.c_double), ("lost", C.c_double),
+                ("detected", C.c_double), ("absorbed", C.c_double),
+                ("interactions", C.c_uint64), ("rays", C.c_uint64)]
+
+
+def default_params(**kw):
+    """The reference's defaults for the settings the hot path reads (core/uniforms.schema.js UniformSpec)."""
+    p = StParams()
+    p.width, p.height = 256, 256
+    p.maxbounce = 10
+    p.maxiter = 400
+    p.stepscale = 0.9
+    p.nee = 1
+    p.rr = 0
+    p.nee_sun_pick = 0.5
+    p.sun_elevation = 45.0
+    p.sun_azimuth = 0.0
+    p.sun_diameter = 0.53
+    p.sun_illuminance = 100000.0
+    p.sky_luminance = 0.0
+    p.ground_luminance = 0.0
+    p.env_uniform = 0.0
+    p.env_sun_gain = 1.0
+    p.env_sky_gain = 1.0
+    p.sun_hint = 1
+    p.seed = 1
+    p.maxaverages = 0
+    p.eps = 0.0
+    p.budget = 0
+    p.samples_per_wave = 0
+    for k, v in kw.items():
+        if not hasattr(p, k):
+            raise KeyError(k)
+        setattr(p, k, v)
+    return p
