@@ -14,6 +14,8 @@
 // segment here too; the last iteration takes no light sample (UB.lastpass) and ends what is left (THE FLUSH).
 #include "st_oracle_render.h"
 #include "st_oracle_extra.h"
+#include "st_oracle_optics.h"
+#include "st_oracle_sppm.h"
 #ifdef _OPENMP
 #include <omp.h>
 #endif
@@ -23,6 +25,8 @@ using namespace sto;
 
 namespace {
 
+// the most SDF evaluations a ray takes in one iteration's march (the product's MARCH_CHUNK)
+const uint32_t MARCH_CHUNK = 48;
 const uint32_t RAY_ACTIVE = 0, RAY_ABSORBED = 1, RAY_ESCAPED = 2, RAY_MAXITER = 4, RAY_SOURCE = 5,
                RAY_TERMINATED = 8, RAY_SCATTER = 9;
 
@@ -74,7 +78,7 @@ template <class T> inline void deposit(Frame<T>& f, uint32_t pix, const V3<T>& c
 }
 
 // the march (wavefront.js:866-947): to the surface, the sky, lmax or maxiter
-template <class T> inline T march(const Ctx<T>& C, Ray<T>& r, Stats& st, bool use_haze) {
+template <class T> inline T march(const Ctx<T>& C, Ray<T>& r, Stats& st, bool use_haze, uint32_t& evals_out) {
     uint64_t steps = 0;
     T dh = T(1e7);
     for (;;) {
@@ -96,6 +100,7 @@ template <class T> inline T march(const Ctx<T>& C, Ray<T>& r, Stats& st, bool us
         move_by(r, r.dir * d);
     }
     st.march_steps += steps;
+    evals_out = (uint32_t)steps;
     return dh;
 }
 
@@ -231,6 +236,48 @@ inline void shade_hit(const Ctx<T>& C, Ray<T>& r, T dhit, Rng& rng, bool last, F
     }
 }
 
+// A PHOTON'S HIT (an optics ray, TAG_PHOTON | TAG_OPTIC): pathBegin..pathEnd without light sampling -- a photon
+// carries flux, it samples no light (materials_pbr.js:1196-1201) -- and without the photon's end at a scatter,
+// since an optics ray walks through every event (tracebasics.js:1008-1022); the bounce cap stays.
+template <class T>
+inline void shade_photon(const Ctx<T>& C, Ray<T>& r, T dhit, Rng& rng) {
+    V3<T> n = hit_normal(C, r.pos, dhit);
+    bool inside = dhit < T(0);
+    V3<T> nrm = inside ? -n : n;
+    T otol = T(10) * march_tol(r.pos, C.tol);
+    if (dot(-r.dir, nrm) < T(0)) { move_by(r, r.dir * otol); return; }
+    r.bounces += 1;
+    SceneHit<T> h = scene_eval(*C.s, r.pos);
+    const st_material& m = C.s->materials[std::min(h.m, C.s->n_materials - 1)];
+    T n0 = r.n;
+    T n1 = std::max(T(m.ior), n0);
+    if (m.transmission > 0 && m.metallic < 1) {
+        SceneHit<T> mb = scene_eval(*C.s, r.pos + (-nrm) * (otol * T(2)));
+        n1 = T(C.s->materials[std::min(mb.a, C.s->n_materials - 1)].ior);
+    }
+    T pG = refract_share<T>(m);
+    T trans = T(m.transmission), specv = T(m.specular);
+    bool diffFace = false;
+    if (inside && pG > T(0) && pG < T(1)) {
+        T k = mixT(T(2) * T(m.specular), T(1), pG);
+        T u4[4]; rng.next4(u4);
+        if (u4[0] < pG) trans = T(1);
+        else { trans = T(0); specv = T(0.5) * k; diffFace = true; }
+    }
+    T etaFace = diffFace ? std::min(n0, n1) / std::max(n0, n1) : n0 / n1;
+    Lobes<T> lb = make_lobes(nrm, -r.dir, m, etaFace, C.tb, trans, specv);
+    lb.etaT = n0 / n1;
+    T ur[4]; rng.next4(ur);
+    LobeSample<T> smp = lobes_sample(lb, ur);
+    r.dir = smp.dir;
+    r.beta *= smp.w;
+    if (smp.transmitted) r.n = n1;
+    if (max3(smp.w) <= T(0)) r.state = RAY_ABSORBED;
+    r.sunmis = T(1);
+    move_by(r, r.dir * otol);
+    if (r.bounces > C.p.maxbounce) r.state = RAY_TERMINATED;
+}
+
 // ------------------------------------------------------------------------------------------------------------
 // THE MEDIUM VERTEX -- core/haze.js:493-596 mediumVertex, mediumNee: a point in the dust, its light sample
 // (sun's cone or the uniform sphere, power heuristic against the phase function) and its phase-function draw
@@ -306,23 +353,31 @@ void trace_path(const Ctx<T>& C, U4 sseed, uint32_t tile, const st_view& v, uint
     T px = clampT(ux * T(W), T(0), T(W) - T(1)), py = clampT(uy * T(H), T(0), T(H) - T(1));
     r.pix = (uint32_t)px + (uint32_t)py * W;
 
-    for (uint32_t it = 0; it < C.budget; it++) {
-        bool last = it + 1 == C.budget;
+    // The wavefront's iterations, as they pass this path: a segment is marched MARCH_CHUNK evaluations an iteration
+    // (the reference's 32-step dispatches, wavefront.js:870; the last iteration marches to the end), then shaded in
+    // the iteration its march ended. Its random numbers are seeded by how many times it has been shaded (seg).
+    uint32_t it = 0, seg = 0;
+    while (it < C.budget) {
         bool use_haze = C.haze.on;
         if (use_haze && r.tmax == T(0)) {                                          // haze.js:255-273 hazeDraw
             // from where the leg starts: the vertex, before the step off it (absLtot is the ltot on arrival there)
             V3<T> A = r.pos - r.dir * (std::max(r.ltot - r.absLtot, T(0)) / std::max(r.n, T(1e-4)));
-            Rng hr = path_rng(sseed, tile, SEED_SALT_HAZE + it);
+            Rng hr = path_rng(sseed, tile, SEED_SALT_HAZE + seg);
             r.tmax = C.haze.draw(A, r.dir, r.absLtot, r.n, T(C.d.env_radius), hr);
         }
-        T dh = march(C, r, st, use_haze);
+        uint32_t evals = 0;
+        T dh = march(C, r, st, use_haze, evals);
+        uint32_t chunks = std::max(1u, (evals + MARCH_CHUNK - 1) / MARCH_CHUNK);
+        it = std::min(it + chunks - 1, C.budget - 1);
+        bool last = it + 1 == C.budget;
         st.segments++;
         if (r.state == RAY_ESCAPED) {                                              // wavefront.js:1303-1320
             r.rad += r.beta * C.env.radiance(r.dir) * r.sunmis;
             break;
         }
         if (r.state != RAY_ACTIVE && r.state != RAY_SCATTER) break;                // out of steps or length
-        Rng rng = path_rng(sseed, tile, 1 + it);
+        Rng rng = path_rng(sseed, tile, 1 + seg);
+        seg++;
         r.absLtot = r.ltot;                                                        // absorbAlong on arrival
         if (r.state == RAY_SCATTER) {
             medium_vertex(C, r, rng, last, fr, st);
@@ -331,7 +386,8 @@ void trace_path(const Ctx<T>& C, U4 sseed, uint32_t tile, const st_view& v, uint
         }
         if (r.state != RAY_ACTIVE) break;
         r.tmax = T(0);                                                             // a new leg (wavefront.js:1375-1380)
-        if (last) { r.state = RAY_MAXITER; st.flushed++; }                         // THE FLUSH (wavefront.js:949-968)
+        if (last) { r.state = RAY_MAXITER; st.flushed++; break; }                  // THE FLUSH (wavefront.js:949-968)
+        it++;
     }
     // THE PATH IS OVER (wavefront.js:1400-1425): its radiance into the frame, and it counts once
     deposit(fr, r.pix, r.rad, st);
@@ -340,6 +396,91 @@ void trace_path(const Ctx<T>& C, U4 sseed, uint32_t tile, const st_view& v, uint
     st.paths++;
 }
 
+// ------------------------------------------------------------------------------------------------------------
+// THE OPTICS TRACE, one ray (optics/kernels.js:429-438 the generator, :571-699 the shade): a photon that walks
+// through every event (TAG_OPTIC) -- no light sampling, no end at a diffuse bounce -- until it escapes, is absorbed,
+// is stopped by a detector or runs out of bounces or steps; what it carries, as luminance (optWeight), tallied per
+// interaction. Seeded by its id at the source and by its id and bounces at each shade (kernels.js:602-606).
+// ------------------------------------------------------------------------------------------------------------
+struct OptTally {
+    double escaped = 0, lost = 0, detected = 0, absorbed = 0, emitted = 0;
+    uint64_t interactions = 0;
+    std::vector<double> far, lux;
+};
+struct OptFrame {
+    float axis[3], c0[3], c90[3], origin[3];
+    uint32_t nC, nG, cells;
+    float half, height;
+};
+
+template <class T>
+void optics_ray(const Ctx<T>& C, U4 bseed, uint32_t id, const st_optics_source* src, const float* cdf, uint32_t nsrc,
+                const OptFrame& F, uint32_t maxbounce, OptTally& tl) {
+    Rng r0; r0.h = bseed; r0.seed_u32(id); r0.seed_u32(0x9E3779B9u);
+    V3<T> org, dir;
+    uint32_t which;
+    source_ray(src, cdf, nsrc, r0, C.tol, org, dir, which);
+    Ray<T> r;
+    r.pos = org; r.dir = dir;
+    r.beta = V3<T>(1); r.rad = V3<T>(1);
+    r.ltot = 0; r.n = T(std::max(1.f, src[which].emit_n)); r.sunmis = 1; r.tmax = 0; r.absLtot = 0;
+    r.bounces = 0; r.steps = 0; r.state = RAY_ACTIVE; r.pix = id;
+    tl.emitted += (double)luma(r.beta * r.rad);
+    Stats st;
+    for (;;) {
+        uint32_t evals = 0;
+        T dh = march(C, r, st, false, evals);
+        T wIn = luma(r.beta * r.rad);
+        if (r.state == RAY_ESCAPED) {                                             // kernels.js:609-625
+            tl.escaped += (double)wIn;
+            float d[3] = {(float)r.dir.x, (float)r.dir.y, (float)r.dir.z};
+            tl.far[far_bin(d, F.axis, F.c0, F.nC, F.nG)] += (double)wIn;
+            // the lux plane: the escaping ray's line met at `height` along the axis (it crosses nothing more)
+            T dn = r.dir.x * T(F.axis[0]) + r.dir.y * T(F.axis[1]) + r.dir.z * T(F.axis[2]);
+            if (F.cells && dn > T(0)) {
+                V3<T> rel = r.pos - V3<T>(T(F.origin[0]), T(F.origin[1]), T(F.origin[2]));
+                T z = rel.x * T(F.axis[0]) + rel.y * T(F.axis[1]) + rel.z * T(F.axis[2]);
+                T t = (T(F.height) - z) / dn;
+                V3<T> h = rel + r.dir * t;
+                T a = h.x * T(F.c0[0]) + h.y * T(F.c0[1]) + h.z * T(F.c0[2]);
+                T b = h.x * T(F.c90[0]) + h.y * T(F.c90[1]) + h.z * T(F.c90[2]);
+                T cell = T(2) * T(F.half) / T(F.cells);
+                if (t >= T(0) && std::fabs(a) < T(F.half) && std::fabs(b) < T(F.half)) {
+                    uint32_t ix = std::min((uint32_t)((a + T(F.half)) / cell), F.cells - 1);
+                    uint32_t iy = std::min((uint32_t)((b + T(F.half)) / cell), F.cells - 1);
+                    tl.lux[(size_t)iy * F.cells + ix] += (double)wIn;
+                }
+            }
+            return;
+        }
+        if (r.state != RAY_ACTIVE) { tl.lost += (double)wIn; return; }           // out of steps or length
+        SceneHit<T> h = scene_eval(*C.s, r.pos);
+        const st_material& m = C.s->materials[std::min(h.m, C.s->n_materials - 1)];
+        V3<T> nn = hit_normal(C, r.pos, dh);
+        bool inside = dh < T(0);
+        V3<T> nrm = inside ? -nn : nn;
+        if (m.detector > 0.5f && dot(-r.dir, nrm) >= T(0)) {                      // kernels.js:660-672
+            tl.detected += (double)wIn;
+            tl.interactions++;
+            return;
+        }
+        uint32_t b0 = r.bounces;
+        Rng rng; rng.h = bseed; rng.seed_u32(id); rng.seed_u32(r.bounces);
+        shade_photon(C, r, dh, rng);
+        if (r.bounces == b0) {                                                   // declined: not an interaction
+            if (r.state == RAY_ACTIVE) continue;
+            tl.lost += (double)wIn;
+            return;
+        }
+        tl.interactions++;
+        bool goesOn = r.state == RAY_ACTIVE || r.state == RAY_TERMINATED;
+        T wOut = goesOn ? luma(r.beta * r.rad) : T(0);
+        tl.absorbed += (double)(wIn - wOut);
+        if (r.state == RAY_TERMINATED) { tl.lost += (double)wOut; return; }       // the bounce cap
+        if (r.state != RAY_ACTIVE) return;
+        (void)maxbounce;
+    }
+}
 }  // namespace
 
 // ------------------------------------------------------------------------------------------------------------
@@ -495,6 +636,76 @@ void sto_lobes_sample(const st_material* m, const double* v, double eta, uint32_
         dirs[3 * i] = s.dir.x; dirs[3 * i + 1] = s.dir.y; dirs[3 * i + 2] = s.dir.z;
         w[3 * i] = s.w.x; w[3 * i + 1] = s.w.y; w[3 * i + 2] = s.w.z;
     }
+}
+
+// Trace an optics batch (config: the scene, its settings for the march; sources with their instance; per instance its
+// ray count, far-field frame, lux plane). Tallies per instance into far (n_inst * nG * nC), lux (n_inst * cells^2),
+// totals (n_inst * 6: emitted, escaped, lost, detected, absorbed, interactions).
+int sto_optics_run(const st_scene_desc* const* scenes, const st_params* p, const st_optics_source* src, uint32_t nsrc,
+                   const uint32_t* ray_count, uint32_t n_inst, const float* frames, uint32_t nC, uint32_t nG,
+                   uint32_t cells, float half, float height, uint32_t maxbounce, uint32_t seed, int fp64,
+                   double* far, double* lux, double* totals, int threads) {
+#ifdef _OPENMP
+    if (threads > 0) omp_set_num_threads(threads);
+#endif
+    for (uint32_t inst = 0; inst < n_inst; inst++) {
+        std::vector<st_optics_source> mine;
+        for (uint32_t i = 0; i < nsrc; i++) if (src[i].instance == inst) mine.push_back(src[i]);
+        if (mine.empty() || !ray_count[inst]) continue;
+        double tot = 0;
+        for (auto& s : mine) tot += s.flux;
+        std::vector<float> cdf(mine.size());
+        double acc = 0;
+        for (size_t i = 0; i < mine.size(); i++) { acc += mine[i].flux; cdf[i] = (float)(acc / tot); }
+        cdf.back() = 1.f;
+        OptFrame F;
+        const float* fr = frames + inst * 12;
+        for (int k = 0; k < 3; k++) { F.origin[k] = fr[k]; F.axis[k] = fr[3 + k]; F.c0[k] = fr[6 + k]; }
+        F.c90[0] = F.axis[1] * F.c0[2] - F.axis[2] * F.c0[1];
+        F.c90[1] = F.axis[2] * F.c0[0] - F.axis[0] * F.c0[2];
+        F.c90[2] = F.axis[0] * F.c0[1] - F.axis[1] * F.c0[0];
+        F.nC = nC; F.nG = nG; F.cells = cells; F.half = half; F.height = height;
+        U4 bseed = sample_seed(seed, inst);
+        auto run = [&](auto zero) {
+            using T = decltype(zero);
+            Ctx<T> C;
+            st_params pp = *p;
+            pp.maxbounce = maxbounce;
+            C.s = scenes[inst]; C.p = pp; C.d = derive(pp, *scenes[inst]);
+            C.env.init(pp, C.d);
+            C.tb = tables<T>();
+            C.tol = T(C.d.tol_setting);
+            C.envR2 = T(C.d.env_radius * C.d.env_radius);
+            C.stepscale = T(pp.stepscale);
+            C.budget = 0;
+            C.haze.init(*scenes[inst]);
+            int nt = 1;
+#ifdef _OPENMP
+            nt = omp_get_max_threads();
+#endif
+            std::vector<OptTally> tls(nt);
+            for (auto& t : tls) { t.far.assign((size_t)nC * nG, 0.0); t.lux.assign((size_t)cells * cells, 0.0); }
+#pragma omp parallel for schedule(dynamic, 256)
+            for (long id = 0; id < (long)ray_count[inst]; id++) {
+                int tid = 0;
+#ifdef _OPENMP
+                tid = omp_get_thread_num();
+#endif
+                optics_ray(C, bseed, (uint32_t)id, mine.data(), cdf.data(), (uint32_t)mine.size(), F, maxbounce, tls[tid]);
+            }
+            double* fo = far + (size_t)inst * nC * nG;
+            double* lo = lux + (size_t)inst * cells * cells;
+            double* to = totals + (size_t)inst * 6;
+            for (auto& t : tls) {
+                for (size_t i = 0; i < t.far.size(); i++) fo[i] += t.far[i];
+                for (size_t i = 0; i < t.lux.size(); i++) lo[i] += t.lux[i];
+                to[0] += t.emitted; to[1] += t.escaped; to[2] += t.lost; to[3] += t.detected; to[4] += t.absorbed;
+                to[5] += (double)t.interactions;
+            }
+        };
+        if (fp64) run(0.0); else run(0.0f);
+    }
+    return 0;
 }
 
 }  // extern "C"

@@ -37,7 +37,7 @@ struct st_ctx {
     std::vector<st_material> mats;
     st_scene_desc desc{};
     bool has_scene = false, has_params = false, has_view = false;
-    st_prim* d_prims = nullptr;
+    DPrim* d_prims = nullptr;
     st_material* d_mats = nullptr;
     st_params params{};
     st_view view{};
@@ -81,7 +81,8 @@ static int cuda_fail(st_ctx* c, cudaError_t e, const char* what) {
 
 static void free_wave(st_ctx* ctx) {
     void* ptrs[] = {ctx->pb.pos, ctx->pb.dir, ctx->pb.beta, ctx->pb.rad, ctx->pb.meta, ctx->q.ray[0], ctx->q.ray[1],
-                    ctx->q.hit, ctx->q.hitd, ctx->q.s_org, ctx->q.s_dir, ctx->q.s_rad, ctx->d_frame,
+                    ctx->q.hit, ctx->q.hitd, ctx->q.s_org[0], ctx->q.s_dir[0], ctx->q.s_rad[0], ctx->q.s_steps[0],
+                    ctx->q.s_org[1], ctx->q.s_dir[1], ctx->q.s_rad[1], ctx->q.s_steps[1], ctx->d_frame,
                     ctx->d_acc, ctx->d_mom};
     for (void* p : ptrs)
         if (p) cudaFree(p);
@@ -187,9 +188,46 @@ static Uni make_uni(const st_ctx* ctx) {
     return u;
 }
 
+// ------------------------------------------------------------------------------------------------------------
+// A PRIMITIVE AS THE KERNELS READ IT (st_device.cuh DPrim): its fields in 16-byte words, the radius of a sphere
+// about its centre that holds it -- inflated by 0.1 % + 10 um so the f32 test never passes a primitive whose own f32
+// distance is nearer -- and a prism's edge constants (shapes.js:266-283), in double here. +inf where the distance is
+// not an exact one (the aspheric lens's is a bound, shapes.js:621-640) or the shape is unbounded (the plane).
+// ------------------------------------------------------------------------------------------------------------
+static DPrim pack_prim(const st_prim& p) {
+    DPrim d{};
+    const float* q = p.p;
+    double R = INFINITY;
+    switch (p.type) {
+        case ST_PRIM_SPHERE: R = std::fabs(q[0]); break;
+        case ST_PRIM_BOX: R = std::sqrt(double(q[0]) * q[0] + double(q[1]) * q[1] + double(q[2]) * q[2]); break;
+        case ST_PRIM_ROUNDBOX:
+            R = std::sqrt(double(q[0]) * q[0] + double(q[1]) * q[1] + double(q[2]) * q[2]) + std::fabs(q[3]);
+            break;
+        case ST_PRIM_TORUS: R = std::fabs(q[0]) + std::fabs(q[1]); break;
+        case ST_PRIM_PRISM: R = std::sqrt(double(q[1]) * q[1] + 0.25 * double(q[2]) * q[2]) + std::fabs(q[3]); break;
+        case ST_PRIM_CYLINDER: R = std::sqrt(double(q[0]) * q[0] + double(q[1]) * q[1]); break;
+        default: R = INFINITY;
+    }
+    float Rf = std::isfinite(R) ? (float)(R * 1.001 + 1e-5) : INFINITY;
+    d.a = make_float4(p.pos[0], p.pos[1], p.pos[2], Rf);
+    d.r0 = make_float4(p.rot[0], p.rot[1], p.rot[2], p.k);
+    d.r1 = make_float4(p.rot[3], p.rot[4], p.rot[5], q[0]);
+    d.r2 = make_float4(p.rot[6], p.rot[7], p.rot[8], q[1]);
+    d.e = make_float4(q[2], q[3], q[4], q[5]);
+    d.f = make_float4(q[6], q[7], q[8], q[9]);
+    if (p.type == ST_PRIM_PRISM) {
+        double n = std::min(std::max(std::nearbyint((double)q[0]), 3.0), 64.0);
+        double an = PI_D / n, Rp = std::max((double)q[1], 0.0);
+        d.g = make_float4((float)(Rp * std::cos(an)), (float)(Rp * std::sin(an)), (float)(2 * an), (float)n);
+    }
+    d.h = make_uint4(p.type, p.op, p.material, p.flags);
+    return d;
+}
+
 static uint32_t samples_per_wave(const st_ctx* ctx) {
     if (ctx->params.samples_per_wave) return ctx->params.samples_per_wave;
-    const uint32_t target = 2u << 20;   // about two million paths in flight fill 152 SMs several times over
+    const uint32_t target = 4u << 20;   // about four million paths a wave: twenty a lane of a full persistent grid
     uint32_t s = (target + ctx->P - 1) / ctx->P;
     return std::max(1u, std::min(s, 64u));
 }
@@ -211,9 +249,15 @@ static int ensure_wave(st_ctx* ctx) {
     CK(cudaMalloc(&ctx->q.ray[1], S * 4), "cudaMalloc queues");
     CK(cudaMalloc(&ctx->q.hit, S * 4), "cudaMalloc queues");
     CK(cudaMalloc(&ctx->q.hitd, S * 4), "cudaMalloc queues");
-    CK(cudaMalloc(&ctx->q.s_org, S * sizeof(float4)), "cudaMalloc shadow queue");
-    CK(cudaMalloc(&ctx->q.s_dir, S * sizeof(float4)), "cudaMalloc shadow queue");
-    CK(cudaMalloc(&ctx->q.s_rad, S * sizeof(float4)), "cudaMalloc shadow queue");
+    // each shadow side holds this iteration's new rays (at most one a path) and the last one's continuations
+    size_t SS = 2 * S;
+    for (int k = 0; k < 2; k++) {
+        CK(cudaMalloc(&ctx->q.s_org[k], SS * sizeof(float4)), "cudaMalloc shadow queue");
+        CK(cudaMalloc(&ctx->q.s_dir[k], SS * sizeof(float4)), "cudaMalloc shadow queue");
+        CK(cudaMalloc(&ctx->q.s_rad[k], SS * sizeof(float4)), "cudaMalloc shadow queue");
+        CK(cudaMalloc(&ctx->q.s_steps[k], SS * sizeof(uint32_t)), "cudaMalloc shadow queue");
+    }
+    ctx->q.scap = (uint32_t)SS;
     CK(cudaMalloc(&ctx->d_frame, S * sizeof(float4)), "cudaMalloc frame");
     CK(cudaMalloc(&ctx->d_acc, (size_t)ctx->P * sizeof(Acc4)), "cudaMalloc accumulation");
     CK(cudaMalloc(&ctx->d_mom, (size_t)ctx->P * sizeof(double2)), "cudaMalloc moments");
@@ -258,16 +302,17 @@ static cudaError_t record_wave(st_ctx* ctx, const WaveArgs& a) {
         return e;
     };
     cudaError_t e;
-    if ((e = launch_iter_begin(a, 1, 1, s))) return e;
+    if ((e = launch_iter_begin(a, 0, 1, 1, s))) return e;
     if ((e = timed("genrays", [&] { return launch_genrays(a, ctx->sms, s); }))) return e;
     int cur = 0;
     for (uint32_t it = 0; it < a.u.budget; it++) {
         int nxt = cur ^ 1;
         int last = it + 1 == a.u.budget;
-        if (it > 0 && (e = launch_iter_begin(a, nxt, 0, s))) return e;
-        if ((e = timed("march", [&] { return launch_march(a, cur, (int)it, ctx->sms, s); }))) return e;
-        if ((e = timed("shade", [&] { return launch_shade(a, nxt, (int)it, last, ctx->sms, s); }))) return e;
-        if ((e = timed("occlude", [&] { return launch_occlude(a, ctx->sms, s); }))) return e;
+        int side = (int)(it & 1u);
+        if (it > 0 && (e = launch_iter_begin(a, (int)it, nxt, 0, s))) return e;
+        if ((e = timed("march", [&] { return launch_march(a, cur, nxt, last, ctx->sms, s); }))) return e;
+        if ((e = timed("shade", [&] { return launch_shade(a, nxt, side, last, ctx->sms, s); }))) return e;
+        if ((e = timed("occlude", [&] { return launch_occlude(a, side, last, ctx->sms, s); }))) return e;
         cur = nxt;
     }
     return timed("resolve", [&] { return launch_resolve(a, s); });
@@ -380,10 +425,12 @@ int st_set_scene(st_ctx* ctx, const char* cuda_src, const st_scene_desc* d, char
     if (prims.size() > ctx->prims.size() || !ctx->d_prims) {
         if (ctx->d_prims) cudaFree(ctx->d_prims);
         ctx->d_prims = nullptr;
-        CK(cudaMalloc(&ctx->d_prims, ST_MAX_PRIMS * sizeof(st_prim)), "cudaMalloc scene");
+        CK(cudaMalloc(&ctx->d_prims, ST_MAX_PRIMS * sizeof(DPrim)), "cudaMalloc scene");
     }
     if (!ctx->d_mats) CK(cudaMalloc(&ctx->d_mats, ST_MAX_MATERIALS * sizeof(st_material)), "cudaMalloc materials");
-    CK(cudaMemcpyAsync(ctx->d_prims, prims.data(), prims.size() * sizeof(st_prim), cudaMemcpyHostToDevice, ctx->stream), "scene upload");
+    std::vector<DPrim> packed(prims.size());
+    for (size_t i = 0; i < prims.size(); i++) packed[i] = pack_prim(prims[i]);
+    CK(cudaMemcpyAsync(ctx->d_prims, packed.data(), packed.size() * sizeof(DPrim), cudaMemcpyHostToDevice, ctx->stream), "scene upload");
     CK(cudaMemcpyAsync(ctx->d_mats, mats.data(), mats.size() * sizeof(st_material), cudaMemcpyHostToDevice, ctx->stream), "scene upload");
     CK(cudaStreamSynchronize(ctx->stream), "scene upload");
     ctx->prims = std::move(prims);
@@ -433,14 +480,14 @@ int st_set_view(st_ctx* ctx, const st_view* v) {
 
 int st_invalidate(st_ctx* ctx) {
     if (!ctx) return ST_ERR_ARG;
-    if (ctx->in_flight) return fail(ctx, ST_ERR_BUSY, "a trace is in flight: st_sync first");
     if (!ctx->d_acc) return ST_OK;
     cudaSetDevice(ctx->device);
+    // stream-ordered: it takes effect after whatever is queued, so it needs no st_sync (RT.invalidate may be called
+    // between queued samples); the sample index restarts, the statistics keep accumulating
     CK(cudaMemsetAsync(ctx->d_acc, 0, (size_t)ctx->P * sizeof(Acc4), ctx->stream), "memset");
     CK(cudaMemsetAsync(ctx->d_mom, 0, (size_t)ctx->P * sizeof(double2), ctx->stream), "memset");
     CK(cudaMemsetAsync(ctx->d_frame, 0, (size_t)ctx->slot_cap * sizeof(float4), ctx->stream), "memset");
-    CK(cudaMemsetAsync(ctx->d_ctr, 0, sizeof(DevCtr), ctx->stream), "memset");
-    CK(cudaStreamSynchronize(ctx->stream), "invalidate");
+    CK(cudaMemsetAsync(&ctx->d_ctr->sample, 0, sizeof(uint32_t), ctx->stream), "memset");
     ctx->samples = 0;
     return ST_OK;
 }
@@ -481,7 +528,7 @@ int st_sync(st_ctx* ctx, int timeout_ms) {
     if (ctx->timing) collect_times(ctx);
     DevCtr c;
     CK(cudaMemcpy(&c, ctx->d_ctr, sizeof(DevCtr), cudaMemcpyDeviceToHost), "counters");
-    if (c.pad0) return fail(ctx, ST_ERR_TIMEOUT, "a kernel's wait for its scene table ran out of iterations");
+    if (c.errflag) return fail(ctx, ST_ERR_TIMEOUT, "a kernel's wait for its scene table ran out of iterations");
     return ST_OK;
 }
 
@@ -616,7 +663,7 @@ cudaStream_t ctx_stream(st_ctx* ctx) { return ctx->stream; }
 int ctx_device(st_ctx* ctx) { return ctx->device; }
 int ctx_sms(st_ctx* ctx) { return ctx->sms; }
 void ctx_set_error(st_ctx* ctx, const std::string& m) { ctx->err = m; }
-const st_prim* ctx_d_prims(st_ctx* ctx) { return ctx->d_prims; }
+const DPrim* ctx_d_prims(st_ctx* ctx) { return ctx->d_prims; }
 const st_material* ctx_d_mats(st_ctx* ctx) { return ctx->d_mats; }
 uint32_t ctx_n_prims(st_ctx* ctx) { return (uint32_t)ctx->prims.size(); }
 uint32_t ctx_n_mats(st_ctx* ctx) { return (uint32_t)ctx->mats.size(); }

@@ -126,23 +126,6 @@ __device__ __forceinline__ float sd_box(f3 p, f3 b) {
     f3 q = mk(fabsf(p.x) - b.x, fabsf(p.y) - b.y, fabsf(p.z) - b.z);
     return length(vmax(q, 0.f)) + fminf(fmaxf(q.x, fmaxf(q.y, q.z)), 0.f);
 }
-__device__ __forceinline__ float g2_regular_polygon(float qx, float qy, float sides, float R0) {
-    float n = clampf(rintf(sides), 3.f, 64.f);
-    float R = fmaxf(R0, 0.f);
-    float an = ST_PI / n;
-    float san, can;
-    sincosf(an, &san, &can);
-    float a = R * can, he = R * san;
-    float k = rintf((atan2f(qy, qx) + 0.5f * ST_PI) / (2.f * an));
-    float phi = -0.5f * ST_PI + 2.f * an * k;
-    float nky, nkx;
-    sincosf(phi, &nky, &nkx);
-    float tkx = -nky, tky = nkx;
-    float u = qx * nkx + qy * nky, v = qx * tkx + qy * tky;
-    if (u <= a) return u - a;
-    float ex = u - a, ey = v - clampf(v, -he, he);
-    return sqrtf(ex * ex + ey * ey);
-}
 __device__ __forceinline__ float g2_extrude(float pz, float gz, float h) {
     float wz = fabsf(pz) - h;
     if (gz > 0.f && wz > 0.f) return sqrtf(gz * gz + wz * wz);
@@ -169,40 +152,66 @@ __device__ __forceinline__ float asph_face(f3 p, float l, float rho, float ht, f
     return (s * p.z - ht + sag) / sqrtf(1.f + m * m);
 }
 
-// one primitive, world point in; the record's float4 words: [1] pos,k [2] rot r0 [3] rot r1,(r2.x) ...
-__device__ __forceinline__ float prim_sdf(const st_prim& pr, f3 pw) {
-    f3 d = pw - mk(pr.pos[0], pr.pos[1], pr.pos[2]);
-    f3 q = mk(pr.rot[0] * d.x + pr.rot[1] * d.y + pr.rot[2] * d.z,
-              pr.rot[3] * d.x + pr.rot[4] * d.y + pr.rot[5] * d.z,
-              pr.rot[6] * d.x + pr.rot[7] * d.y + pr.rot[8] * d.z);
-    const float* p = pr.p;
-    switch (pr.type) {
+// THE TABLE AS THE KERNELS READ IT: each st_prim repacked on the host (st_capi.cu pack_prims) into eight 16-byte
+// words, so a record is read with 128-bit shared-memory loads and carries what the host could work out once: the
+// radius of a sphere about its centre that holds it (its BOUND, +inf where none is valid) and a prism's edge
+// constants. 128 bytes, as st_prim.
+struct __align__(16) DPrim {
+    float4 a;    // centre xyz, bound radius (inflated; +inf: never culled)
+    float4 r0;   // rotation row 0, smooth-union radius k
+    float4 r1;   // rotation row 1, p0
+    float4 r2;   // rotation row 2, p1
+    float4 e;    // p2..p5
+    float4 f;    // p6..p9
+    float4 g;    // prism: distance to an edge's middle, half an edge, 2 pi / sides, sides
+    uint4 h;     // type, op, material, flags
+};
+
+__device__ __forceinline__ float prim_sdf(const DPrim& pr, f3 pw) {
+    const float4 A = pr.a, R0 = pr.r0, R1 = pr.r1, R2 = pr.r2;
+    f3 d = pw - mk(A.x, A.y, A.z);
+    f3 q = mk(R0.x * d.x + R0.y * d.y + R0.z * d.z,
+              R1.x * d.x + R1.y * d.y + R1.z * d.z,
+              R2.x * d.x + R2.y * d.y + R2.z * d.z);
+    const float p0 = R1.w, p1 = R2.w;
+    switch (pr.h.x) {
         case ST_PRIM_PLANE: return q.z;
-        case ST_PRIM_SPHERE: return length(q) - p[0];
-        case ST_PRIM_BOX: return sd_box(q, mk(p[0], p[1], p[2]));
-        case ST_PRIM_ROUNDBOX: return sd_box(q, mk(p[0], p[1], p[2])) - p[3];
+        case ST_PRIM_SPHERE: return length(q) - p0;
+        case ST_PRIM_BOX: return sd_box(q, mk(p0, p1, pr.e.x));
+        case ST_PRIM_ROUNDBOX: { float4 E = pr.e; return sd_box(q, mk(p0, p1, E.x)) - E.y; }
         case ST_PRIM_TORUS: {
             float lxy = sqrtf(q.x * q.x + q.y * q.y);
-            float a = lxy - p[0];
-            return sqrtf(a * a + q.z * q.z) - p[1];
+            float t = lxy - p0;
+            return sqrtf(t * t + q.z * q.z) - p1;
         }
         case ST_PRIM_PRISM: {
-            float g = g2_regular_polygon(q.x, q.y, p[0], p[1]);
-            return g2_extrude(q.z, g, fmaxf(0.5f * p[2], 0.f)) - p[3];
+            // g2RegularPolygon (shapes.js:266-283) with its per-shape constants from the host; the edge normal's
+            // angle -pi/2 + 2 pi k / n as sin / cos of pi (2k / n), which need no argument reduction
+            const float4 G = pr.g, E = pr.e;
+            float k = rintf((atan2f(q.y, q.x) + 0.5f * ST_PI) / G.z);
+            float sp, cp;
+            sincospif(2.f * k / G.w, &sp, &cp);
+            float nkx = sp, nky = -cp;
+            float u = q.x * nkx + q.y * nky, v = -q.x * nky + q.y * nkx;
+            float gz;
+            if (u <= G.x) gz = u - G.x;
+            else { float ex = u - G.x, ey = v - clampf(v, -G.y, G.y); gz = sqrtf(ex * ex + ey * ey); }
+            return g2_extrude(q.z, gz, fmaxf(0.5f * E.x, 0.f)) - E.y;
         }
         case ST_PRIM_ASPHERE: {
-            float rho = fmaxf(0.5f * p[0], 1e-6f);
+            const float4 E = pr.e, F = pr.f;
+            float rho = fmaxf(0.5f * p0, 1e-6f);
             float l = sqrtf(q.x * q.x + q.y * q.y);
             float dd = l - rho;
-            float top = asph_face(q, l, rho, 0.5f * p[1], p[2], p[3], p[4], p[5], 1.f);
+            float top = asph_face(q, l, rho, 0.5f * p1, E.x, E.y, E.z, E.w, 1.f);
             if (top > dd) dd = top;
-            float bot = asph_face(q, l, rho, 0.5f * p[1], p[6], p[7], p[8], p[9], -1.f);
+            float bot = asph_face(q, l, rho, 0.5f * p1, F.x, F.y, F.z, F.w, -1.f);
             if (bot > dd) dd = bot;
             return dd;
         }
         case ST_PRIM_CYLINDER: {
-            float lx = sqrtf(q.x * q.x + q.y * q.y) - p[1];
-            float lz = fabsf(q.z) - p[0];
+            float lx = sqrtf(q.x * q.x + q.y * q.y) - p1;
+            float lz = fabsf(q.z) - p0;
             float ox = fmaxf(lx, 0.f), oz = fmaxf(lz, 0.f);
             return fminf(fmaxf(lx, lz), 0.f) + sqrtf(ox * ox + oz * oz);
         }
@@ -214,21 +223,42 @@ __device__ __forceinline__ float smooth_union(float d1, float d2, float k) {    
     float h = clampf(0.5f + 0.5f * (d2 - d1) / k, 0.f, 1.f);
     return mixf(d2, d1, h) - k * h * (1.f - h);
 }
+// THE CULL: whether the primitive's distance at p is at least t, from its bounding sphere alone (|p - c| - R <= d,
+// true of every exact distance the table holds; the host gives +inf R where it is not). Exact by construction: a
+// culled primitive is one whose fold or union would have left the running value as it was.
+__device__ __forceinline__ bool beyond(const DPrim& pr, f3 p, float t) {
+    const float4 A = pr.a;
+    float s = t + A.w;
+    if (!(s < 3.0e38f)) return false;                                 // no bound (+inf)
+    if (s < 0.f) return true;
+    f3 d = p - mk(A.x, A.y, A.z);
+    return dot(d, d) >= s * s;
+}
+#define CULL_REL 1.001f
+#define CULL_ABS 1e-6f
 
 struct SceneHit { float d; uint32_t m, a; };
-// distance only (scene_api.js FOLD_DIST): the march's and the shadow rays' question
-__device__ __forceinline__ float scene_dist(const st_prim* __restrict__ pr, uint32_t n, f3 p) {
+// distance only (scene_api.js FOLD_DIST): the march's and the shadow rays' question. Within an item's CSG chain a
+// primitive is evaluated only where it could change the running value: a smooth union of radius k leaves acc alone
+// where d_j >= acc + k (sdf.js opSmoothUnion's h is then 1), a union where d_j >= acc, a subtraction where
+// d_j >= -acc -- the same number, bit for bit, as evaluating it.
+__device__ __forceinline__ float scene_dist(const DPrim* __restrict__ pr, uint32_t n, f3 p) {
     float best = 1e7f;
     uint32_t i = 0;
     while (i < n) {
         float di = prim_sdf(pr[i], p);
         uint32_t j = i + 1;
-        while (j < n && pr[j].op != ST_OP_ITEM) {
-            float dj = prim_sdf(pr[j], p);
-            uint32_t op = pr[j].op;
-            if (op == ST_OP_SMOOTH) di = smooth_union(di, dj, pr[j].k);
-            else if (op == ST_OP_UNION) di = fminf(di, dj);
-            else di = fmaxf(di, -dj);
+        while (j < n) {
+            const uint32_t op = pr[j].h.y;
+            if (op == ST_OP_ITEM) break;
+            if (op == ST_OP_SMOOTH) {
+                float k = pr[j].r0.w;
+                if (!beyond(pr[j], p, di + k * CULL_REL + CULL_ABS)) di = smooth_union(di, prim_sdf(pr[j], p), k);
+            } else if (op == ST_OP_UNION) {
+                if (!beyond(pr[j], p, di + CULL_ABS)) di = fminf(di, prim_sdf(pr[j], p));
+            } else {
+                if (!beyond(pr[j], p, -di + CULL_ABS)) di = fmaxf(di, -prim_sdf(pr[j], p));
+            }
             j++;
         }
         if (fabsf(di) < fabsf(best)) best = di;
@@ -236,23 +266,37 @@ __device__ __forceinline__ float scene_dist(const st_prim* __restrict__ pr, uint
     }
     return best;
 }
-// the whole answer (FOLD_FULL): the surface's material and the medium (the least-deep item the point is in)
-__device__ __forceinline__ SceneHit scene_full(const st_prim* __restrict__ pr, uint32_t n, f3 p) {
+// the whole answer (FOLD_FULL): the surface's material (the chain's primitive of least |d|) and the medium (the
+// least-deep item the point is in). A primitive is culled only where it could change neither the running value
+// nor the nearest primitive.
+__device__ __forceinline__ SceneHit scene_full(const DPrim* __restrict__ pr, uint32_t n, f3 p) {
     SceneHit H{1e7f, 0u, 0u};
     float insideW = -1e7f;
     uint32_t i = 0;
     while (i < n) {
         float di = prim_sdf(pr[i], p);
-        uint32_t mat = pr[i].material;
+        uint32_t mat = pr[i].h.z;
         float nearv = fabsf(di);
         uint32_t j = i + 1;
-        while (j < n && pr[j].op != ST_OP_ITEM) {
-            float dj = prim_sdf(pr[j], p);
-            uint32_t op = pr[j].op;
-            if (op == ST_OP_SMOOTH) di = smooth_union(di, dj, pr[j].k);
-            else if (op == ST_OP_UNION) di = fminf(di, dj);
-            else di = fmaxf(di, -dj);
-            if (op != ST_OP_SUB && fabsf(dj) < nearv) { nearv = fabsf(dj); mat = pr[j].material; }
+        while (j < n) {
+            const uint32_t op = pr[j].h.y;
+            if (op == ST_OP_ITEM) break;
+            if (op == ST_OP_SMOOTH) {
+                float k = pr[j].r0.w;
+                if (!beyond(pr[j], p, fmaxf(di + k * CULL_REL, nearv) + CULL_ABS)) {
+                    float dj = prim_sdf(pr[j], p);
+                    di = smooth_union(di, dj, k);
+                    if (fabsf(dj) < nearv) { nearv = fabsf(dj); mat = pr[j].h.z; }
+                }
+            } else if (op == ST_OP_UNION) {
+                if (!beyond(pr[j], p, fmaxf(di, nearv) + CULL_ABS)) {
+                    float dj = prim_sdf(pr[j], p);
+                    di = fminf(di, dj);
+                    if (fabsf(dj) < nearv) { nearv = fabsf(dj); mat = pr[j].h.z; }
+                }
+            } else {
+                if (!beyond(pr[j], p, -di + CULL_ABS)) di = fmaxf(di, -prim_sdf(pr[j], p));
+            }
             j++;
         }
         if (di < 0.f && di > insideW) { insideW = di; H.a = mat; }

@@ -51,7 +51,7 @@ cudaStream_t ctx_stream(st_ctx* ctx);
 int ctx_device(st_ctx* ctx);
 int ctx_sms(st_ctx* ctx);
 void ctx_set_error(st_ctx* ctx, const std::string& m);
-const st_prim* ctx_d_prims(st_ctx* ctx);
+const st::DPrim* ctx_d_prims(st_ctx* ctx);
 const st_material* ctx_d_mats(st_ctx* ctx);
 uint32_t ctx_n_prims(st_ctx* ctx);
 uint32_t ctx_n_mats(st_ctx* ctx);

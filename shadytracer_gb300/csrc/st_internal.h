@@ -16,6 +16,17 @@ namespace st {
 #define RAY_TERMINATED 8u
 #define RAY_SCATTER 9u
 
+// A MARCH CHUNK: the most SDF evaluations a ray takes in one launch of the march or the occlusion pass before it is
+// handed to the next iteration (the reference's MARCH_STEPS, wavefront.js:870, is 32); the last iteration's launches
+// march to the end. It bounds the tail a persistent launch spends on its longest rays.
+#define MARCH_CHUNK 48u
+
+// meta.y: the bounces (bits 0-7), the path's segment -- its shades so far, which its random numbers are seeded by
+// (bits 8-15) -- and the state (bits 16-23)
+__host__ __device__ __forceinline__ uint32_t meta_y(uint32_t bounces, uint32_t seg, uint32_t state) {
+    return (bounces & 0xffu) | ((seg & 0xffu) << 8) | (state << 16);
+}
+
 // THE WAVE'S PATH STATE, structure of arrays indexed by the path's slot (slot = sample-in-wave * P + tile): the
 // reference's 112-byte Ray (tracebasics.js:400-460) cut to what the hot path carries, as four float4 and one uint4
 // so every access is one 128-bit load or store.
@@ -24,23 +35,27 @@ struct PathBuf {
     float4* dir;    // xyz direction, w n (index of the medium it is in)
     float4* beta;   // xyz throughput, w sunmis (the environment's MIS weight on escape)
     float4* rad;    // xyz radiance collected, w tmax (the haze's collision, as ltot)
-    uint4* meta;    // x pix, y bounces | state << 16, z march steps over the path, w absLtot (f32 bits)
+    uint4* meta;    // x pix, y bounces | segment << 8 | state << 16, z march steps over the path, w absLtot (f32)
 };
-// THE QUEUES: indices into the path state, appended by warp-aggregated atomics (one per warp)
+// THE QUEUES: indices into the path state, appended with one atomic per warp (ballot + popc)
 struct Queues {
-    uint32_t* ray[2];   // the march's input, ping-pong
-    uint32_t* hit;      // the shade queue: slot
-    float* hitd;        // ...and the signed distance at the hit
-    float4* s_org;      // shadow rays: xyz origin, w n
-    float4* s_dir;      // xyz direction, w pix (u32 bits)
-    float4* s_rad;      // xyz what it deposits if it reaches, w unused
-    uint32_t cap;       // slots in a wave: every queue holds at most this many
+    uint32_t* ray[2];    // the march's input, ping-pong: new segments and march continuations
+    uint32_t* hit;       // the shade queue: slot
+    float* hitd;         // ...and the signed distance at the hit
+    // shadow rays, ping-pong (side it & 1 read by the occlusion pass of iteration it, continuations to the other)
+    float4* s_org[2];    // xyz where it is, w ltot
+    float4* s_dir[2];    // xyz direction, w pix in the wave's frames (u32 bits)
+    float4* s_rad[2];    // xyz what it deposits if it reaches, w n
+    uint32_t* s_steps[2];
+    uint32_t cap;        // slots in a wave: the path queues hold at most this many
+    uint32_t scap;       // each shadow side's room; appends past it are dropped and counted
 };
-// THE COUNTERS (wavefront.js:150 Counters), on the device
+// THE COUNTERS (wavefront.js:150 Counters), on the device. The statistics accumulate from the context's creation.
 struct DevCtr {
-    uint32_t rayCount[2], hitCount, shadowCount;
-    uint32_t marchHead, occHead, shadeHead, pad0;
+    uint32_t rayCount[2], hitCount, shadowCount[2];
+    uint32_t marchHead, occHead, errflag;
     uint32_t nonfinite, flushed, shadowcut, sample;   // sample: the first sample of the wave in flight
+    uint32_t shadowdrop, pad1, pad2, pad3;
     unsigned long long paths, segments, march_steps, shadow_rays, shadow_steps;
 };
 
@@ -48,7 +63,7 @@ struct __align__(32) Acc4 { double x, y, z, w; };   // FP64 mean rgb + the sampl
 
 struct WaveArgs {
     Uni u;
-    const st_prim* prims;
+    const DPrim* prims;
     const st_material* mats;
     MfTab tab;
     PathBuf pb;
@@ -64,10 +79,10 @@ struct WaveArgs {
 // launch wrappers (st_render.cu)
 cudaError_t launch_mf_tables(float* ec, float* ecavg, float* e1, cudaStream_t s);
 cudaError_t launch_genrays(const WaveArgs& a, int sms, cudaStream_t s);
-cudaError_t launch_iter_begin(const WaveArgs& a, int nxt, int first, cudaStream_t s);
-cudaError_t launch_march(const WaveArgs& a, int cur, int it, int sms, cudaStream_t s);
-cudaError_t launch_shade(const WaveArgs& a, int nxt, int it, int last, int sms, cudaStream_t s);
-cudaError_t launch_occlude(const WaveArgs& a, int sms, cudaStream_t s);
+cudaError_t launch_iter_begin(const WaveArgs& a, int it, int nxt, int first, cudaStream_t s);
+cudaError_t launch_march(const WaveArgs& a, int cur, int nxt, int last, int sms, cudaStream_t s);
+cudaError_t launch_shade(const WaveArgs& a, int nxt, int side, int last, int sms, cudaStream_t s);
+cudaError_t launch_occlude(const WaveArgs& a, int side, int last, int sms, cudaStream_t s);
 cudaError_t launch_resolve(const WaveArgs& a, cudaStream_t s);
 
 }  // namespace st

@@ -33,7 +33,7 @@ __device__ __forceinline__ uint32_t lanemask_lt() {
 // ------------------------------------------------------------------------------------------------------------
 // A TABLE INTO SHARED MEMORY BY ONE BULK COPY: thread 0 arms an mbarrier with the byte count and issues
 // cp.async.bulk; every thread waits on the barrier's phase, a bounded number of times. bytes is a multiple of 16,
-// both addresses 16-byte aligned (st_prim is 128 bytes, st_material 64, cudaMalloc 256-aligned). Returns false
+// both addresses 16-byte aligned (DPrim is 128 bytes, st_material 64, cudaMalloc 256-aligned). Returns false
 // (and flags the counters) if the copy did not land within the limit.
 // ------------------------------------------------------------------------------------------------------------
 __device__ __forceinline__ bool stage_table(void* sdst, const void* gsrc, uint32_t bytes, uint64_t* mbar,
@@ -60,7 +60,7 @@ __device__ __forceinline__ bool stage_table(void* sdst, const void* gsrc, uint32
     }
     // one decision for the whole CTA, so no thread leaves while another still waits at a barrier
     if (__syncthreads_or(!done)) {
-        if (threadIdx.x == 0) atomicExch(&ctr->pad0, 1u);
+        if (threadIdx.x == 0) atomicExch(&ctr->errflag, 1u);
         return false;
     }
     return true;
@@ -151,16 +151,15 @@ __global__ void __launch_bounds__(256) k_genrays(WaveArgs a) {
     }
 }
 
-// a wavefront iteration's start: the queues it fills emptied (prog_flip)
-__global__ void k_iter_begin(DevCtr* ctr, int nxt, uint32_t slots, int first) {
+// a wavefront iteration's start: the queues it fills emptied (prog_flip, wavefront.js:368-387)
+__global__ void k_iter_begin(DevCtr* ctr, int it, int nxt, uint32_t slots, int first) {
     if (threadIdx.x == 0 && blockIdx.x == 0) {
-        if (first) ctr->rayCount[0] = slots;
+        if (first) { ctr->rayCount[0] = slots; ctr->shadowCount[0] = 0u; }
         ctr->rayCount[nxt] = 0u;
         ctr->hitCount = 0u;
-        ctr->shadowCount = 0u;
+        ctr->shadowCount[(it + 1) & 1] = 0u;
         ctr->marchHead = 0u;
         ctr->occHead = 0u;
-        ctr->shadeHead = 0u;
     }
 }
 
@@ -179,23 +178,30 @@ __device__ __forceinline__ uint32_t warp_append(uint32_t* counter, bool want) {
 // THE MARCH (wavefront.js:866-947), persistent. Each warp claims CLAIM queue entries at a time; a lane whose ray
 // ended takes the next one at once. A step: the scene's distance, the hit test against marchTol, lmax and
 // maxiter, the escape test; then the step of ea * stepscale. On the haze's collision (haze.js:280-288) the ray is
-// moved back to it and handed to shade as RAY_SCATTER.
+// moved back to it and handed to shade as RAY_SCATTER. A ray still marching after MARCH_CHUNK evaluations goes on
+// in the next iteration (the reference's 32-step dispatches, wavefront.js:870); the last iteration's launch
+// marches every ray to its end.
 // ------------------------------------------------------------------------------------------------------------
 template <bool HAZE>
-__global__ void __launch_bounds__(256) k_march(WaveArgs a, int cur, int it) {
+__global__ void __launch_bounds__(256, 3) k_march(WaveArgs a, int cur, int nxt, int last) {
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ __align__(8) uint64_t mbar;
-    st_prim* sp = reinterpret_cast<st_prim*>(smem);
-    const Uni& u = a.u;
-    if (!stage_table(sp, a.prims, u.n_prims * (uint32_t)sizeof(st_prim), &mbar, a.ctr)) return;
+    DPrim* sp = reinterpret_cast<DPrim*>(smem);
+    const uint32_t n_prims = a.u.n_prims;
+    if (!stage_table(sp, a.prims, n_prims * (uint32_t)sizeof(DPrim), &mbar, a.ctr)) return;
     const uint32_t count = a.ctr->rayCount[cur];
-    const uint32_t* __restrict__ inq = a.q.ray[cur];
+    const uint32_t* __restrict__ inq = cur ? a.q.ray[1] : a.q.ray[0];
+    uint32_t* __restrict__ outq = nxt ? a.q.ray[1] : a.q.ray[0];
+    uint32_t* outc = nxt ? &a.ctr->rayCount[1] : &a.ctr->rayCount[0];
+    const float tol = a.u.tol, stepscale = a.u.stepscale, envR2 = a.u.envR2;
+    const uint32_t maxiter = a.u.maxiter;
+    const uint32_t chunk = last ? 0xffffffffu : MARCH_CHUNK;
     const int lane = threadIdx.x & 31;
 
     uint32_t slot = INVALID_SLOT;
     f3 pos = mk(0.f), dir = mk(0.f);
     float ltot = 0.f, n = 1.f, tmax = 0.f;
-    uint32_t steps = 0;
+    uint32_t steps = 0, evals_here = 0;
     uint32_t wpos = 0, wend = 0;
     bool exhausted = false;
     unsigned long long evals = 0;
@@ -218,19 +224,22 @@ __global__ void __launch_bounds__(256) k_march(WaveArgs a, int cur, int it) {
                     slot = inq[wpos + rank];
                     float4 p4 = a.pb.pos[slot], d4 = a.pb.dir[slot];
                     pos = xyz(p4); ltot = p4.w; dir = xyz(d4); n = d4.w;
-                    steps = a.pb.meta[slot].z;
+                    uint4 m4 = a.pb.meta[slot];
+                    steps = m4.z;
+                    evals_here = 0;
                     tmax = HAZE ? a.pb.rad[slot].w : 0.f;
                     if (HAZE && tmax == 0.f) {
                         // THE LEG'S COLLISION, drawn as it starts (haze.js:255-273 hazeDraw)
+                        const Uni& u = a.u;
                         tmax = -1.f;
                         if (fabsf(n - 1.f) <= 1e-3f) {
-                            float absL = __uint_as_float(a.pb.meta[slot].w);
+                            float absL = __uint_as_float(m4.w);
                             f3 A = pos - dir * (fmaxf(ltot - absL, 0.f) / fmaxf(n, 1e-4f));
                             float t0, t1;
                             haze_span(u, A, dir, 1e30f, t0, t1);
                             if (t1 > t0) {
-                                uint32_t tile = slot % u.P, j = slot / u.P;
-                                Rng hr = path_rng(sample_seed(u.seed, a.ctr->sample + j), tile, ST_SALT_HAZE + it);
+                                uint32_t tile = slot % u.P, j = slot / u.P, seg = (m4.y >> 8) & 0xffu;
+                                Rng hr = path_rng(sample_seed(u.seed, a.ctr->sample + j), tile, ST_SALT_HAZE + seg);
                                 float4 r4 = hr.next();
                                 float t = t0 - logf(1.f - r4.x) / u.hsig;
                                 if (t < t1) tmax = fmaxf(absL + t * n, 1e-30f);
@@ -244,43 +253,49 @@ __global__ void __launch_bounds__(256) k_march(WaveArgs a, int cur, int it) {
         if (__ballot_sync(FULL_MASK, slot != INVALID_SLOT) == 0) break;
 
         // ---- one step ----
-        bool fin = false;
+        bool fin = false, more = false;
         uint32_t state = RAY_ACTIVE;
         float dh = 0.f;
         if (slot != INVALID_SLOT) {
             if (HAZE && tmax > 0.f && ltot >= tmax) {
-                pos = pos - dir * ((ltot - tmax) / fmaxf(n, 1e-4f));
-                ltot = tmax;
                 state = RAY_SCATTER;
                 fin = true;
             } else {
-                float d = scene_dist(sp, u.n_prims, pos);
+                float d = scene_dist(sp, n_prims, pos);
                 evals++;
+                evals_here++;
                 float ea = fabsf(d);
-                float eps = march_tol(pos, u.tol);
-                if (ltot > 1000.f || steps > u.maxiter) state = RAY_MAXITER;
-                if (dot(pos, dir) > 0.f && dot(pos, pos) > u.envR2) state = RAY_ESCAPED;
+                float eps = march_tol(pos, tol);
+                if (ltot > 1000.f || steps > maxiter) state = RAY_MAXITER;
+                if (dot(pos, dir) > 0.f && dot(pos, pos) > envR2) state = RAY_ESCAPED;
                 if (ea < eps || state != RAY_ACTIVE) {
                     fin = true;
                     dh = d;
                 } else {
                     steps += 1;
-                    f3 off = dir * (ea * u.stepscale);
+                    f3 off = dir * (ea * stepscale);
                     pos = pos + off;
                     ltot += length(off) * n;
+                    if (HAZE && tmax > 0.f && ltot >= tmax) { state = RAY_SCATTER; fin = true; }
+                    else if (evals_here >= chunk) more = true;
                 }
+            }
+            if (state == RAY_SCATTER) {                                 // hazeAt: back to the collision
+                pos = pos - dir * ((ltot - tmax) / fmaxf(n, 1e-4f));
+                ltot = tmax;
             }
         }
         uint32_t qp = warp_append(&a.ctr->hitCount, fin);
-        if (fin) {
+        uint32_t cp = warp_append(outc, more);
+        if (fin || more) {
             a.pb.pos[slot] = make_float4(pos.x, pos.y, pos.z, ltot);
             uint4 m = a.pb.meta[slot];
             m.y = (m.y & 0xffffu) | (state << 16);
             m.z = steps;
             a.pb.meta[slot] = m;
             if (HAZE) a.pb.rad[slot].w = tmax;
-            a.q.hit[qp] = slot;
-            a.q.hitd[qp] = dh;
+            if (fin) { a.q.hit[qp] = slot; a.q.hitd[qp] = dh; }
+            else outq[cp] = slot;
             slot = INVALID_SLOT;
         }
     }
@@ -311,7 +326,7 @@ __device__ __forceinline__ void deposit(float4* frame, uint32_t pix, f3 c, DevCt
 // ------------------------------------------------------------------------------------------------------------
 struct ShadowOut { bool valid; f3 org, dir, rad; float n; };
 
-__device__ __forceinline__ void shade_surface(const WaveArgs& a, const st_prim* sp, const st_material* sm,
+__device__ __forceinline__ void shade_surface(const WaveArgs& a, const DPrim* sp, const st_material* sm,
                                               f3& pos, f3& dir, float& ltot, float& n, f3& beta, float& sunmis,
                                               f3& rad, uint32_t& bounces, uint32_t& state, float dh, Rng& rng,
                                               bool last, ShadowOut& sh) {
@@ -445,20 +460,27 @@ __device__ __forceinline__ void shade_medium(const WaveArgs& a, f3& pos, f3& dir
     if (bounces > u.maxbounce) state = RAY_TERMINATED;
 }
 
-__global__ void __launch_bounds__(256) k_shade(WaveArgs a, int nxt, int it, int last) {
+__global__ void __launch_bounds__(256) k_shade(WaveArgs a, int nxt, int side, int last) {
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ __align__(8) uint64_t mbar;
     __shared__ __align__(8) uint64_t mbar2;
     const Uni& u = a.u;
-    st_prim* sp = reinterpret_cast<st_prim*>(smem);
-    st_material* sm = reinterpret_cast<st_material*>(smem + u.n_prims * sizeof(st_prim));
-    if (!stage_table(sp, a.prims, u.n_prims * (uint32_t)sizeof(st_prim), &mbar, a.ctr)) return;
+    DPrim* sp = reinterpret_cast<DPrim*>(smem);
+    st_material* sm = reinterpret_cast<st_material*>(smem + u.n_prims * sizeof(DPrim));
+    if (!stage_table(sp, a.prims, u.n_prims * (uint32_t)sizeof(DPrim), &mbar, a.ctr)) return;
     if (!stage_table(sm, a.mats, u.n_mats * (uint32_t)sizeof(st_material), &mbar2, a.ctr)) return;
     const uint32_t count = a.ctr->hitCount;
     const uint32_t stride = gridDim.x * blockDim.x;
     const uint32_t nrounds = (count + stride - 1) / stride;
+    uint32_t* __restrict__ outq = nxt ? a.q.ray[1] : a.q.ray[0];
+    uint32_t* outc = nxt ? &a.ctr->rayCount[1] : &a.ctr->rayCount[0];
+    float4* s_org = side ? a.q.s_org[1] : a.q.s_org[0];
+    float4* s_dir = side ? a.q.s_dir[1] : a.q.s_dir[0];
+    float4* s_rad = side ? a.q.s_rad[1] : a.q.s_rad[0];
+    uint32_t* s_steps = side ? a.q.s_steps[1] : a.q.s_steps[0];
+    uint32_t* s_cnt = side ? &a.ctr->shadowCount[1] : &a.ctr->shadowCount[0];
     unsigned long long paths = 0;
-    uint32_t flushed = 0;
+    uint32_t flushed = 0, dropped = 0;
     for (uint32_t r = 0; r < nrounds; r++) {
         uint32_t q = r * stride + blockIdx.x * blockDim.x + threadIdx.x;
         bool valid = q < count;
@@ -468,7 +490,7 @@ __global__ void __launch_bounds__(256) k_shade(WaveArgs a, int nxt, int it, int 
         f3 pos, dir, beta, rad;
         float ltot = 0.f, n = 1.f, sunmis = 1.f, tmax = 0.f;
         uint4 m4 = make_uint4(0, 0, 0, 0);
-        uint32_t bounces = 0, state = RAY_TERMINATED;
+        uint32_t bounces = 0, seg = 0, state = RAY_TERMINATED;
         if (valid) {
             slot = a.q.hit[q];
             float dh = a.q.hitd[q];
@@ -476,13 +498,14 @@ __global__ void __launch_bounds__(256) k_shade(WaveArgs a, int nxt, int it, int 
             m4 = a.pb.meta[slot];
             pos = xyz(p4); ltot = p4.w; dir = xyz(d4); n = d4.w; beta = xyz(b4); sunmis = b4.w;
             rad = xyz(r4); tmax = r4.w;
-            pix = m4.x; bounces = m4.y & 0xffffu; state = m4.y >> 16;
+            pix = m4.x; bounces = m4.y & 0xffu; seg = (m4.y >> 8) & 0xffu; state = m4.y >> 16;
             gpix = (slot / u.P) * u.P + pix;                          // the pixel in the wave's frames
             if (state == RAY_ESCAPED) {
                 rad = rad + beta * env_radiance(u, dir) * sunmis;     // wavefront.js:1303-1320
             } else if (state == RAY_ACTIVE || state == RAY_SCATTER) {
                 uint32_t tile = slot % u.P, j = slot / u.P;
-                Rng rng = path_rng(sample_seed(u.seed, a.ctr->sample + j), tile, 1u + (uint32_t)it);
+                Rng rng = path_rng(sample_seed(u.seed, a.ctr->sample + j), tile, 1u + seg);
+                seg += 1;
                 m4.w = __float_as_uint(ltot);                         // absorbAlong: absLtot on arrival
                 if (state == RAY_SCATTER)
                     shade_medium(a, pos, dir, beta, sunmis, bounces, state, n, rng, last != 0, sh);
@@ -497,21 +520,26 @@ __global__ void __launch_bounds__(256) k_shade(WaveArgs a, int nxt, int it, int 
             }
         }
         // the shadow ray, the ray on, the path's end: one append per warp each
-        uint32_t sq = warp_append(&a.ctr->shadowCount, sh.valid);
+        uint32_t sq = warp_append(s_cnt, sh.valid);
         if (sh.valid) {
-            a.q.s_org[sq] = f4(sh.org, sh.n);
-            a.q.s_dir[sq] = f4(sh.dir, __uint_as_float(gpix));
-            a.q.s_rad[sq] = f4(sh.rad, 0.f);
+            if (sq < a.q.scap) {
+                s_org[sq] = f4(sh.org, 0.f);
+                s_dir[sq] = f4(sh.dir, __uint_as_float(gpix));
+                s_rad[sq] = f4(sh.rad, sh.n);
+                s_steps[sq] = 0u;
+            } else {
+                dropped++;
+            }
         }
-        uint32_t rq = warp_append(&a.ctr->rayCount[nxt], cont);
+        uint32_t rq = warp_append(outc, cont);
         if (cont) {
             a.pb.pos[slot] = f4(pos, ltot);
             a.pb.dir[slot] = f4(dir, n);
             a.pb.beta[slot] = f4(beta, sunmis);
             a.pb.rad[slot] = f4(rad, tmax);
-            m4.y = bounces | (RAY_ACTIVE << 16);
+            m4.y = meta_y(bounces, seg, RAY_ACTIVE);
             a.pb.meta[slot] = m4;
-            a.q.ray[nxt][rq] = slot;
+            outq[rq] = slot;
         } else if (valid) {
             // THE PATH IS OVER (wavefront.js:1400-1425): its radiance into this sample's frame, counted once
             uint32_t j = slot / u.P;
@@ -524,10 +552,12 @@ __global__ void __launch_bounds__(256) k_shade(WaveArgs a, int nxt, int it, int 
     for (int o = 16; o > 0; o >>= 1) {
         paths += __shfl_down_sync(FULL_MASK, paths, o);
         flushed += __shfl_down_sync(FULL_MASK, flushed, o);
+        dropped += __shfl_down_sync(FULL_MASK, dropped, o);
     }
     if ((threadIdx.x & 31) == 0) {
         if (paths) atomicAdd(&a.ctr->paths, paths);
         if (flushed) atomicAdd(&a.ctr->flushed, flushed);
+        if (dropped) atomicAdd(&a.ctr->shadowdrop, dropped);
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&a.ctr->segments, (unsigned long long)count);
 }
@@ -535,23 +565,38 @@ __global__ void __launch_bounds__(256) k_shade(WaveArgs a, int nxt, int it, int 
 // ------------------------------------------------------------------------------------------------------------
 // THE OCCLUSION PASS (wavefront.js:1481-1692), distance only, persistent with refill like the march: any surface
 // blocks; leaving the scene, lmax or maxiter reaches (maxiter counted in shadowcut); a ray that reaches deposits.
+// A ray still going after MARCH_CHUNK evaluations is queued for the next iteration's pass on the other side; the
+// last iteration's pass runs every ray to its end (the reference's extra rounds on the last pass,
+// raytrace_main.js THE LAST PASS'S SHADOW ROUNDS).
 // ------------------------------------------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) k_occlude(WaveArgs a) {
+__global__ void __launch_bounds__(256, 3) k_occlude(WaveArgs a, int side, int last) {
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ __align__(8) uint64_t mbar;
-    st_prim* sp = reinterpret_cast<st_prim*>(smem);
-    const Uni& u = a.u;
-    if (!stage_table(sp, a.prims, u.n_prims * (uint32_t)sizeof(st_prim), &mbar, a.ctr)) return;
-    const uint32_t count = a.ctr->shadowCount;
+    DPrim* sp = reinterpret_cast<DPrim*>(smem);
+    const uint32_t n_prims = a.u.n_prims;
+    if (!stage_table(sp, a.prims, n_prims * (uint32_t)sizeof(DPrim), &mbar, a.ctr)) return;
+    const uint32_t count = min(side ? a.ctr->shadowCount[1] : a.ctr->shadowCount[0], a.q.scap);
+    const float4* __restrict__ i_org = side ? a.q.s_org[1] : a.q.s_org[0];
+    const float4* __restrict__ i_dir = side ? a.q.s_dir[1] : a.q.s_dir[0];
+    const float4* __restrict__ i_rad = side ? a.q.s_rad[1] : a.q.s_rad[0];
+    const uint32_t* __restrict__ i_steps = side ? a.q.s_steps[1] : a.q.s_steps[0];
+    float4* o_org = side ? a.q.s_org[0] : a.q.s_org[1];
+    float4* o_dir = side ? a.q.s_dir[0] : a.q.s_dir[1];
+    float4* o_rad = side ? a.q.s_rad[0] : a.q.s_rad[1];
+    uint32_t* o_steps = side ? a.q.s_steps[0] : a.q.s_steps[1];
+    uint32_t* o_cnt = side ? &a.ctr->shadowCount[0] : &a.ctr->shadowCount[1];
+    const float tol = a.u.tol, stepscale = a.u.stepscale, envR2 = a.u.envR2;
+    const uint32_t maxiter = a.u.maxiter;
+    const uint32_t chunk = last ? 0xffffffffu : MARCH_CHUNK;
     const int lane = threadIdx.x & 31;
     uint32_t idx = INVALID_SLOT;
     f3 pos = mk(0.f), dir = mk(0.f);
     float ltot = 0.f, n = 1.f;
-    uint32_t steps = 0;
+    uint32_t steps = 0, evals_here = 0;
     uint32_t wpos = 0, wend = 0;
     bool exhausted = false;
     unsigned long long evals = 0, rays = 0;
-    uint32_t cuts = 0;
+    uint32_t cuts = 0, dropped = 0;
     for (;;) {
         uint32_t idle = __ballot_sync(FULL_MASK, idx == INVALID_SLOT);
         if (idle && !exhausted) {
@@ -567,53 +612,67 @@ __global__ void __launch_bounds__(256) k_occlude(WaveArgs a) {
                 uint32_t rank = __popc(idle & lanemask_lt());
                 if (idx == INVALID_SLOT && rank < avail) {
                     idx = wpos + rank;
-                    float4 o4 = a.q.s_org[idx], d4 = a.q.s_dir[idx];
-                    pos = xyz(o4); n = o4.w; dir = xyz(d4);
-                    ltot = 0.f; steps = 0;
-                    rays++;
+                    float4 o4 = i_org[idx], d4 = i_dir[idx];
+                    pos = xyz(o4); ltot = o4.w; dir = xyz(d4); n = i_rad[idx].w;
+                    steps = i_steps[idx];
+                    evals_here = 0;
+                    if (steps == 0u) rays++;
                 }
                 wpos += min((uint32_t)__popc(idle), avail);
             }
         }
         if (__ballot_sync(FULL_MASK, idx != INVALID_SLOT) == 0) break;
+        bool reached = false, done = false, more = false;
         if (idx != INVALID_SLOT) {
-            float d = scene_dist(sp, u.n_prims, pos);
+            float d = scene_dist(sp, n_prims, pos);
             evals++;
+            evals_here++;
             float ea = fabsf(d);
-            float eps = march_tol(pos, u.tol);
-            bool blocked = false, reached = false;
-            if (ea < eps) blocked = true;
-            else if (dot(pos, dir) > 0.f && dot(pos, pos) > u.envR2) reached = true;
+            float eps = march_tol(pos, tol);
+            if (ea < eps) done = true;                                // blocked
+            else if (dot(pos, dir) > 0.f && dot(pos, pos) > envR2) { reached = true; done = true; }
             else {
                 steps += 1;
-                if (ltot > 1000.f || steps > u.maxiter) {
-                    reached = true;
-                    if (steps > u.maxiter) cuts++;
+                if (ltot > 1000.f || steps > maxiter) {
+                    reached = true; done = true;
+                    if (steps > maxiter) cuts++;
                 } else {
-                    f3 off = dir * (ea * u.stepscale);
+                    f3 off = dir * (ea * stepscale);
                     pos = pos + off;
                     ltot += length(off) * n;
+                    if (evals_here >= chunk) more = true;
                 }
             }
-            if (reached) {
-                float4 r4 = a.q.s_rad[idx];
-                float4 d4 = a.q.s_dir[idx];
-                uint32_t pix = __float_as_uint(d4.w);
-                // the pixel in the wave's frames: sample-in-wave * P + pixel (k_shade packs it)
-                deposit(a.frame, pix, xyz(r4), a.ctr);
-            }
-            if (blocked || reached) idx = INVALID_SLOT;
         }
+        uint32_t cp = warp_append(o_cnt, more);
+        if (reached) {
+            float4 r4 = i_rad[idx];
+            uint32_t gpix = __float_as_uint(i_dir[idx].w);          // the pixel in the wave's frames
+            deposit(a.frame, gpix, xyz(r4), a.ctr);
+        }
+        if (more) {
+            if (cp < a.q.scap) {
+                o_org[cp] = f4(pos, ltot);
+                o_dir[cp] = i_dir[idx];
+                o_rad[cp] = i_rad[idx];
+                o_steps[cp] = steps;
+            } else {
+                dropped++;
+            }
+        }
+        if (done || more) idx = INVALID_SLOT;
     }
     for (int o = 16; o > 0; o >>= 1) {
         evals += __shfl_down_sync(FULL_MASK, evals, o);
         rays += __shfl_down_sync(FULL_MASK, rays, o);
         cuts += __shfl_down_sync(FULL_MASK, cuts, o);
+        dropped += __shfl_down_sync(FULL_MASK, dropped, o);
     }
     if (lane == 0) {
         if (evals) atomicAdd(&a.ctr->shadow_steps, evals);
         if (rays) atomicAdd(&a.ctr->shadow_rays, rays);
         if (cuts) atomicAdd(&a.ctr->shadowcut, cuts);
+        if (dropped) atomicAdd(&a.ctr->shadowdrop, dropped);
     }
 }
 
@@ -668,8 +727,8 @@ cudaError_t launch_genrays(const WaveArgs& a, int sms, cudaStream_t s) {
     k_genrays<<<blocks, 256, 0, s>>>(a);
     return cudaGetLastError();
 }
-cudaError_t launch_iter_begin(const WaveArgs& a, int nxt, int first, cudaStream_t s) {
-    k_iter_begin<<<1, 32, 0, s>>>(a.ctr, nxt, a.slots, first);
+cudaError_t launch_iter_begin(const WaveArgs& a, int it, int nxt, int first, cudaStream_t s) {
+    k_iter_begin<<<1, 32, 0, s>>>(a.ctr, it, nxt, a.slots, first);
     return cudaGetLastError();
 }
 static int occupancy(const void* fn, size_t smem) {
@@ -677,31 +736,31 @@ static int occupancy(const void* fn, size_t smem) {
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, 256, smem);
     return nb > 0 ? nb : 1;
 }
-cudaError_t launch_march(const WaveArgs& a, int cur, int it, int sms, cudaStream_t s) {
-    size_t smem = a.u.n_prims * sizeof(st_prim);
+cudaError_t launch_march(const WaveArgs& a, int cur, int nxt, int last, int sms, cudaStream_t s) {
+    size_t smem = a.u.n_prims * sizeof(DPrim);
     if (a.u.haze_on) {
         if (smem > 48 * 1024) cudaFuncSetAttribute(k_march<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         int nb = occupancy((const void*)k_march<true>, smem);
-        k_march<true><<<sms * nb, 256, smem, s>>>(a, cur, it);
+        k_march<true><<<sms * nb, 256, smem, s>>>(a, cur, nxt, last);
     } else {
         if (smem > 48 * 1024) cudaFuncSetAttribute(k_march<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (!g_occ_march) g_occ_march = occupancy((const void*)k_march<false>, 32 * 1024);
-        k_march<false><<<sms * g_occ_march, 256, smem, s>>>(a, cur, it);
+        k_march<false><<<sms * g_occ_march, 256, smem, s>>>(a, cur, nxt, last);
     }
     return cudaGetLastError();
 }
-cudaError_t launch_shade(const WaveArgs& a, int nxt, int it, int last, int sms, cudaStream_t s) {
-    size_t smem = a.u.n_prims * sizeof(st_prim) + a.u.n_mats * sizeof(st_material);
+cudaError_t launch_shade(const WaveArgs& a, int nxt, int side, int last, int sms, cudaStream_t s) {
+    size_t smem = a.u.n_prims * sizeof(DPrim) + a.u.n_mats * sizeof(st_material);
     if (smem > 48 * 1024) cudaFuncSetAttribute(k_shade, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (!g_occ_shade) g_occ_shade = occupancy((const void*)k_shade, 48 * 1024);
-    k_shade<<<sms * g_occ_shade, 256, smem, s>>>(a, nxt, it, last);
+    k_shade<<<sms * g_occ_shade, 256, smem, s>>>(a, nxt, side, last);
     return cudaGetLastError();
 }
-cudaError_t launch_occlude(const WaveArgs& a, int sms, cudaStream_t s) {
-    size_t smem = a.u.n_prims * sizeof(st_prim);
+cudaError_t launch_occlude(const WaveArgs& a, int side, int last, int sms, cudaStream_t s) {
+    size_t smem = a.u.n_prims * sizeof(DPrim);
     if (smem > 48 * 1024) cudaFuncSetAttribute(k_occlude, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (!g_occ_occl) g_occ_occl = occupancy((const void*)k_occlude, 32 * 1024);
-    k_occlude<<<sms * g_occ_occl, 256, smem, s>>>(a);
+    k_occlude<<<sms * g_occ_occl, 256, smem, s>>>(a, side, last);
     return cudaGetLastError();
 }
 cudaError_t launch_resolve(const WaveArgs& a, cudaStream_t s) {
