@@ -243,12 +243,13 @@ int  st_sppm_build(st_ctx* ctx, const float* pos, const float* power, const uint
                    const uint32_t* nrm_oct, const uint32_t* flags, uint32_t n, float cell);
 int  st_sppm_read_grid(st_ctx* ctx, uint32_t* key, uint32_t* cell_count, uint32_t* cell_start,
                        uint32_t* order);
-/* gather at m query points: pos (3m), normal (3m), radius, the surface's albedo (Lambertian f =
- * albedo/pi) and bounce of each query; out (3m) = sum f * power within r on a facing surface
- * (core/sppm.js:305-346,475-494, budget 0 = unlimited). */
+/* gather at m query points: pos (3m), normal (3m), the surface's albedo (3m; Lambertian f = albedo/pi) and the
+ * camera path's bounces at each; out (3m, FP64) = sum f * power over the records within `radius` (at most half the
+ * cell) on a facing surface inside the bounce cap (core/sppm.js:305-346,475-494); budget: records a gather may walk
+ * (0 = unlimited; past a cell's share of it, sub-lists), seed: the sub-lists' draws. */
 int  st_sppm_gather(st_ctx* ctx, const float* qpos, const float* qnrm, const float* qalbedo,
                     const uint32_t* qbounce, uint32_t m, float radius, uint32_t maxbounce,
-                    uint32_t budget, uint32_t seed, float* out);
+                    uint32_t budget, uint32_t seed, double* out);
 int  st_sppm_stats_read(st_ctx* ctx, st_sppm_stats* out);
 
 /* ---- the optics bench (optics/index.js, optics/kernels.js) ---- */

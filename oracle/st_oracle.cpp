@@ -708,4 +708,51 @@ int sto_optics_run(const st_scene_desc* const* scenes, const st_params* p, const
     return 0;
 }
 
+// ---- the photon map (st_oracle_sppm.h) ----
+static SppmGrid g_grid;
+uint32_t sto_sppm_hash(int32_t i, int32_t j, int32_t k) { return sppm_hash(i, j, k); }
+double sto_sppm_radius(double r1, int k, double alpha) { return sppm_radius(r1, k, alpha); }
+double sto_sppm_keep(double capacity, double demand) { return sppm_keep(capacity, demand); }
+uint32_t sto_sppm_subs_of(uint32_t count, uint32_t share) { return sppm_subs_of(count, share); }
+uint32_t sto_sppm_oct(const float* v) { return sppm_oct(v); }
+void sto_sppm_unoct(uint32_t w, float* out) { sppm_unoct(w, out); }
+int sto_sppm_build(const float* pos, const float* power, const uint32_t* nrm, const uint32_t* flags, uint32_t n,
+                   float cell, uint32_t* key, uint32_t* cell_count) {
+    sppm_build(g_grid, pos, power, nrm, flags, n, cell);
+    if (key) for (uint32_t i = 0; i < n; i++) key[i] = g_grid.key[i];
+    if (cell_count) for (uint32_t h = 0; h < SPPM_HEADS; h++) cell_count[h] = (uint32_t)g_grid.lists[h].size();
+    return 0;
+}
+int sto_sppm_gather(const float* qpos, const float* qnrm, const float* qalb, const uint32_t* qb, uint32_t m, float radius,
+                    uint32_t maxbounce, uint32_t budget, uint32_t seed, double* out, uint32_t* visits, uint32_t* cuts) {
+    U4 ss = sample_seed(seed, 0);
+#pragma omp parallel for schedule(dynamic, 64)
+    for (long i = 0; i < (long)m; i++) {
+        Rng r; r.h = ss; r.seed_u32((uint32_t)i); r.seed_u32(0x53505000u);
+        uint32_t v = 0; bool cut = false;
+        sppm_gather(g_grid, &qpos[3 * i], &qnrm[3 * i], &qalb[3 * i], qb[i], radius, maxbounce, budget, r, &out[3 * i], v, cut);
+        if (visits) visits[i] = v;
+        if (cuts) cuts[i] = cut ? 1 : 0;
+    }
+    return 0;
+}
+
+// ---- haze (st_oracle_extra.h) and the far field (st_oracle_optics.h), for the tests ----
+void sto_haze_span(const st_scene_desc* s, const double* A, const double* d, double len, double R, double* t) {
+    HazeBox<double> h; h.init(*s);
+    h.span(V3<double>(A[0], A[1], A[2]), V3<double>(d[0], d[1], d[2]), len, R, t[0], t[1]);
+}
+double sto_hg_eval(double c, double g) { return hg_eval(c, g); }
+void sto_hg_sample(double g, const double* d, uint32_t seed, int n, double* out) {
+    Rng r; r.h = sample_seed(seed, 1);
+    for (int i = 0; i < n; i++) {
+        double u[4]; r.next4(u);
+        V3<double> v = hg_sample(V3<double>(d[0], d[1], d[2]), g, u[0], u[1]);
+        out[3 * i] = v.x; out[3 * i + 1] = v.y; out[3 * i + 2] = v.z;
+    }
+}
+uint32_t sto_far_bin(const float* d, const float* ax, const float* c0, uint32_t nC, uint32_t nG) { return far_bin(d, ax, c0, nC, nG); }
+void sto_far_geometry(uint32_t nC, uint32_t nG, double* omega) { far_geometry(nC, nG, omega); }
+void sto_far_intensity(const double* flux, uint32_t nC, uint32_t nG, double* I) { far_intensity(flux, nC, nG, I); }
+
 }  // extern "C"
