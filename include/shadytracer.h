@@ -303,6 +303,22 @@ int  st_optics_set_far(st_ctx* ctx, const st_optics_far* far);
 int  st_optics_run(st_ctx* ctx, const st_optics_batch* batch, double* far, double* lux,
                    st_optics_totals* totals);
 
+/* ---- a render that allocates nothing ----
+ * No counterpart in the reference: an entry point for hosts that may not allocate device memory when they want a
+ * picture -- one held to a memory budget fixed at start-up, one on a real-time thread, one whose allocations would
+ * land inside a stream capture it does not own. It renders `nsamples` samples of a picture of at most 128 x 128
+ * pixels (ST_NOALLOC_MAX_PIXELS) into the caller's host buffers (width*height entries each; NULL skips one), using
+ * only a scratch array compiled into the library: 8 MiB (ST_NOALLOC_SCRATCH_BYTES) of device memory on every GPU that
+ * loads the library, held until exit. No cudaMalloc, no cudaFree, no allocating library call. A larger picture, or
+ * more than 256 primitives or materials, returns ST_ERR_ARG. Each call clears the accumulation and counters it keeps
+ * in the shared array and runs on the device's legacy default stream; calls that overlap on one GPU race, so a host
+ * serialises them. The first call on a device does the set-up (the array's address, the albedo tables) and should
+ * come before any stream capture. The result equals st_step's for the same inputs. */
+#define ST_NOALLOC_MAX_PIXELS (128u * 128u)
+#define ST_NOALLOC_SCRATCH_BYTES (8u << 20)
+int  st_render_noalloc(int device, const st_scene_desc* desc, const st_params* p, const st_view* v, int nsamples,
+                       double* rgb, double* V, double* S, uint32_t* count);
+
 /* ---- the binding's checks ---- */
 /* The sizes of the structs above as this library was built (st_prim, st_material, st_scene_desc, st_params,
  * st_view, st_counters_t, st_image_stats_t, st_kernel_time, st_sppm_stats, st_optics_source, st_optics_far,
