@@ -277,8 +277,8 @@ typedef struct st_optics_far {
 } st_optics_far;
 
 /* A batch of independent instances traced in one launch chain: instance i owns rays
- * [ray_first[i], ray_first[i] + ray_count[i]) and the scene items whose st_prim.flags >> 8 == i
- * (0xFFFFFF: shared by all). */
+ * [ray_first[i], ray_first[i] + ray_count[i]) and the scene items whose st_prim.flags >> 8 == i, which
+ * must be contiguous in the table; an item naming an instance past the batch is an error. */
 typedef struct st_optics_batch {
     uint32_t n_instances;
     const uint32_t* ray_count;    /* rays per instance                                             */

@@ -175,3 +175,176 @@ def lobes_sample(mat, v, eta, seed, n):
     w = np.zeros((n, 3), np.float64)
     lib().sto_lobes_sample(C.byref(mat), ptr(np.asarray(v, np.float64)), eta, seed, n, ptr(d), ptr(w))
     return d, w
+
+
+# ---- the photon map (st_oracle_sppm.h) ----
+def _declare_extra(L):
+    P = C.c_void_p
+    sig = {
+        "sto_sppm_hash": ([C.c_int32, C.c_int32, C.c_int32], C.c_uint32),
+        "sto_sppm_radius": ([C.c_double, C.c_int, C.c_double], C.c_double),
+        "sto_sppm_keep": ([C.c_double, C.c_double], C.c_double),
+        "sto_sppm_subs_of": ([C.c_uint32, C.c_uint32], C.c_uint32),
+        "sto_sppm_oct": ([P], C.c_uint32),
+        "sto_sppm_unoct": ([C.c_uint32, P], None),
+        "sto_sppm_build": ([P, P, P, P, C.c_uint32, C.c_float, P, P], C.c_int),
+        "sto_sppm_gather": ([P, P, P, P, C.c_uint32, C.c_float, C.c_uint32, C.c_uint32, C.c_uint32, P, P, P], C.c_int),
+        "sto_haze_span": ([P, P, P, C.c_double, C.c_double, P], None),
+        "sto_hg_eval": ([C.c_double, C.c_double], C.c_double),
+        "sto_hg_sample": ([C.c_double, P, C.c_uint32, C.c_int, P], None),
+        "sto_far_bin": ([P, P, P, C.c_uint32, C.c_uint32], C.c_uint32),
+        "sto_far_geometry": ([C.c_uint32, C.c_uint32, P], None),
+        "sto_far_intensity": ([P, C.c_uint32, C.c_uint32, P], None),
+        "sto_step_moments": ([P, C.c_double, C.c_double], None),
+        "sto_optics_run": ([P, P, P, C.c_uint32, P, C.c_uint32, P, C.c_uint32, C.c_uint32, C.c_uint32, C.c_float,
+                            C.c_float, C.c_uint32, C.c_uint32, C.c_int, P, P, P, C.c_int], C.c_int),
+    }
+    for name, (args, res) in sig.items():
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = res
+
+
+_extra_done = False
+
+
+def xlib():
+    global _extra_done
+    L = lib()
+    if not _extra_done:
+        _declare_extra(L)
+        _extra_done = True
+    return L
+
+
+def sppm_hash(i, j, k):
+    return xlib().sto_sppm_hash(i, j, k)
+
+
+def sppm_radius(r1, k, alpha=2.0 / 3.0):
+    return xlib().sto_sppm_radius(r1, k, alpha)
+
+
+def sppm_keep(capacity, demand):
+    return xlib().sto_sppm_keep(capacity, demand)
+
+
+def sppm_subs_of(count, share):
+    return xlib().sto_sppm_subs_of(count, share)
+
+
+def sppm_oct(v):
+    return xlib().sto_sppm_oct(ptr(np.asarray(v, np.float32)))
+
+
+def sppm_unoct(w):
+    o = np.zeros(3, np.float32)
+    xlib().sto_sppm_unoct(w, ptr(o))
+    return o
+
+
+def sppm_build(pos, power, nrm_oct, flags, cell):
+    pos = np.ascontiguousarray(pos, np.float32)
+    power = np.ascontiguousarray(power, np.float32)
+    nrm_oct = np.ascontiguousarray(nrm_oct, np.uint32)
+    flags = np.ascontiguousarray(flags, np.uint32)
+    n = len(flags)
+    key = np.zeros(n, np.uint32)
+    cnt = np.zeros(1 << 20, np.uint32)
+    xlib().sto_sppm_build(ptr(pos), ptr(power), ptr(nrm_oct), ptr(flags), n, cell, ptr(key), ptr(cnt))
+    return key, cnt
+
+
+def sppm_gather(qpos, qnrm, qalb, qb, radius, maxbounce, budget, seed):
+    qpos = np.ascontiguousarray(qpos, np.float32)
+    qnrm = np.ascontiguousarray(qnrm, np.float32)
+    qalb = np.ascontiguousarray(qalb, np.float32)
+    qb = np.ascontiguousarray(qb, np.uint32)
+    m = len(qb)
+    out = np.zeros((m, 3), np.float64)
+    vis = np.zeros(m, np.uint32)
+    cut = np.zeros(m, np.uint32)
+    xlib().sto_sppm_gather(ptr(qpos), ptr(qnrm), ptr(qalb), ptr(qb), m, radius, maxbounce, budget, seed, ptr(out),
+                           ptr(vis), ptr(cut))
+    return out, vis, cut
+
+
+def step_moments(state, x, window=float("inf")):
+    """One resolve step of a pixel's luminance moments; state = [Y, V, S, cnt] (numpy float64, updated in place)."""
+    xlib().sto_step_moments(ptr(state), x, window)
+    return state
+
+
+def standard_error(V, S):
+    """sqrt(S V / (1 - S)), None where it is unknown (measure.js:46-51)."""
+    if not (0 < S < 1) or V < 0:
+        return None
+    return float(np.sqrt(S * V / (1 - S)))
+
+
+# ---- haze and the far field ----
+def haze_span(scene, A, d, length, R):
+    t = np.zeros(2, np.float64)
+    xlib().sto_haze_span(C.byref(scene.desc), ptr(np.asarray(A, np.float64)), ptr(np.asarray(d, np.float64)),
+                         length, R, ptr(t))
+    return t
+
+
+def hg_eval(c, g):
+    return xlib().sto_hg_eval(c, g)
+
+
+def hg_sample(g, d, seed, n):
+    out = np.zeros((n, 3), np.float64)
+    xlib().sto_hg_sample(g, ptr(np.asarray(d, np.float64)), seed, n, ptr(out))
+    return out
+
+
+def far_bin(d, axis, c0, nC, nG):
+    f = lambda v: ptr(np.asarray(v, np.float32))
+    return xlib().sto_far_bin(f(d), f(axis), f(c0), nC, nG)
+
+
+def far_geometry(nC, nG):
+    o = np.zeros(nG, np.float64)
+    xlib().sto_far_geometry(nC, nG, ptr(o))
+    return o
+
+
+def far_intensity(flux, nC, nG):
+    flux = np.ascontiguousarray(flux, np.float64).reshape(-1)
+    I = np.zeros(nG * nC, np.float64)
+    xlib().sto_far_intensity(ptr(flux), nC, nG, ptr(I))
+    return I.reshape(nG, nC)
+
+
+def optics_run(bench, ray_counts, nC=360, nG=181, cells=0, half=1.0, height=1.0, maxbounce=32, seed=1, fp64=False,
+               threads=0, axis=(0, 0, 1), c0=(1, 0, 0)):
+    """The optics trace on the CPU: `bench` a scenes.optics_bench scene; each instance traced against its own
+    primitives (flags >> 8), its rays seeded as the GPU's are."""
+    from shadytracer_gb300 import scenes as S
+    n = len(ray_counts)
+    per = []
+    for i in range(n):
+        prims = [p for p in bench.prim_list if (p.flags >> 8) == i]
+        per.append(S.Scene(prims, bench.material_list, env_radius=bench.desc.env_radius,
+                           tolerance=bench.desc.tolerance, name="instance"))
+    ptrs = (C.c_void_p * n)(*[C.cast(C.byref(s.desc), C.c_void_p) for s in per])
+    srcs = bench.info["sources"]
+    from shadytracer_gb300.st_types import StOpticsSource
+    sarr = (StOpticsSource * len(srcs))(*srcs)
+    rc = np.ascontiguousarray(ray_counts, np.uint32)
+    frames = np.zeros((n, 12), np.float32)
+    for i in range(n):
+        s0 = [s for s in srcs if s.instance == i][0]
+        frames[i, 0:3] = list(s0.centre)
+        frames[i, 3:6] = axis
+        frames[i, 6:9] = c0
+    far = np.zeros((n, nG, nC), np.float64)
+    lux = np.zeros((n, max(cells, 1), max(cells, 1)), np.float64)
+    tot = np.zeros((n, 6), np.float64)
+    xlib().sto_optics_run(ptrs, C.byref(bench.params), C.cast(sarr, C.c_void_p), len(srcs), ptr(rc), n, ptr(frames),
+                          nC, nG, cells, half, height, maxbounce, seed, 1 if fp64 else 0, ptr(far), ptr(lux), ptr(tot),
+                          threads)
+    keys = ["emitted", "escaped", "lost", "detected", "absorbed", "interactions"]
+    return {"far": far, "lux": lux, "totals": [dict(zip(keys, t.tolist())) for t in tot], "scenes": per}

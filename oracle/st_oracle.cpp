@@ -484,6 +484,18 @@ void optics_ray(const Ctx<T>& C, U4 bseed, uint32_t id, const st_optics_source* 
 }  // namespace
 
 // ------------------------------------------------------------------------------------------------------------
+// ONE RESOLVE STEP of a pixel's luminance moments (measure.js:36-51 stepMoments): the new sample y joins prevn
+// earlier ones (their count capped at the EMA window) at weight w = 1 / (prevn + 1); V is the weighted spread of the
+// deviations from the previous mean, S the sum of the squared weights (S = 1/n for a true mean of n, 1/(2N+1) at an
+// EMA window N). A first sample (prevn 0) leaves V = 0, S = 1.
+inline void step_moments(double prevn, double y, double prev_y, double& V, double& S) {
+    double w = 1.0 / (prevn + 1);
+    double d = prevn > 0 ? y - prev_y : 0.0;
+    double v0 = std::min(std::max(V, 0.0), 1e300), s0 = std::min(std::max(S, 0.0), 1.0);
+    V = (1 - w) * (v0 + w * d * d);
+    S = (1 - w) * (1 - w) * s0 + w * w;
+}
+
 // extern "C"
 // ------------------------------------------------------------------------------------------------------------
 static MfTables g_tb_f, g_tb_d;
@@ -541,11 +553,7 @@ static int render_impl(const st_scene_desc* s, const st_params* p, const st_view
             for (int c = 0; c < 3; c++) prev[c] = std::min(std::max(acc_rgb[i * 3 + c], -1e20), 1e20);
             for (int c = 0; c < 3; c++) acc_rgb[i * 3 + c] = (prev[c] * prevn + s3[c]) / cnt;
             double y = s3[0] * LUMA_R + s3[1] * LUMA_G + s3[2] * LUMA_B;
-            double w = 1.0 / cnt;
-            double d = prevn > 0 ? y - (prev[0] * LUMA_R + prev[1] * LUMA_G + prev[2] * LUMA_B) : 0.0;
-            double v0 = std::min(std::max(mV[i], 0.0), 1e300), s0 = std::min(std::max(mS[i], 0.0), 1.0);
-            mV[i] = (1 - w) * (v0 + w * d * d);
-            mS[i] = (1 - w) * (1 - w) * s0 + w * w;
+            step_moments(prevn, y, prev[0] * LUMA_R + prev[1] * LUMA_G + prev[2] * LUMA_B, mV[i], mS[i]);
         }
     }
     if (counters) {
@@ -710,6 +718,14 @@ int sto_optics_run(const st_scene_desc* const* scenes, const st_params* p, const
 
 // ---- the photon map (st_oracle_sppm.h) ----
 static SppmGrid g_grid;
+// state = {Y, V, S, cnt}; window: the EMA cap on the earlier samples' count (infinity: a true mean; 0: a reset)
+void sto_step_moments(double* state, double x, double window) {
+    double prevn = std::min(state[3], window);
+    double prevY = state[0];
+    state[0] = (prevY * prevn + x) / (prevn + 1);
+    step_moments(prevn, x, prevY, state[1], state[2]);
+    state[3] = prevn + 1;
+}
 uint32_t sto_sppm_hash(int32_t i, int32_t j, int32_t k) { return sppm_hash(i, j, k); }
 double sto_sppm_radius(double r1, int k, double alpha) { return sppm_radius(r1, k, alpha); }
 double sto_sppm_keep(double capacity, double demand) { return sppm_keep(capacity, demand); }

@@ -40,6 +40,8 @@ SIGNATURES = {
     "st_optics_set_sources": ([P, C.POINTER(T.StOpticsSource), C.c_uint32], C.c_int),
     "st_optics_set_far": ([P, C.POINTER(T.StOpticsFar)], C.c_int),
     "st_optics_run": ([P, C.POINTER(T.StOpticsBatch), P, P, C.POINTER(T.StOpticsTotals)], C.c_int),
+    "st_render_noalloc": ([C.c_int, C.POINTER(T.StSceneDesc), C.POINTER(T.StParams), C.POINTER(T.StView), C.c_int,
+                           P, P, P, P], C.c_int),
     "st_struct_sizes": ([P, C.c_int], C.c_int),
     "st_stream": ([P], C.c_void_p),
 }

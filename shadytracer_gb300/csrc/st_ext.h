@@ -35,8 +35,7 @@ struct OpticsState {
     std::vector<st_optics_source> sources;
     st_optics_far far{};
     bool has_far = false;
-    void* scratch = nullptr;     // device work space, grown as needed
-    size_t scratch_bytes = 0;
+    void* scratch = nullptr;     // the run's device buffers (st_optics.cu OptBuf), grown as needed
 };
 
 struct StExt {
@@ -45,6 +44,7 @@ struct StExt {
 };
 
 void ext_free(StExt& e);
+void optics_free(OpticsState& os);
 
 StExt& ctx_ext(st_ctx* ctx);
 cudaStream_t ctx_stream(st_ctx* ctx);

@@ -74,6 +74,8 @@ struct WaveArgs {
     double2* mom;       // P: FP64 V, S (the error bar's moments)
     uint32_t spw;       // samples in this wave
     uint32_t slots;     // spw * P
+    const uint2* inst_range = nullptr;   // a batch of instances (the optics bench): each one's [first, count) of the
+                                         // table, the instance in meta.w; null for a picture
 };
 
 // launch wrappers (st_render.cu)

@@ -1,0 +1,514 @@
+// st_optics.cu -- the optics bench (optics/kernels.js, optics/index.js) for sm_103a: many emitter + lens instances
+// traced in one launch chain, with FP64 tallies.
+//
+// THE REFERENCE traces one luminaire at a time: prog_opt_gen (kernels.js:429) draws rays from the sources, the
+// renderer's march moves them, prog_opt_shade (kernels.js:571-699) walks each through every event -- a photon that is
+// never ended by a scatter (TAG_OPTIC) -- and tallies, per interaction, what escaped, was lost, was absorbed or reached
+// a detector, and the far field by direction, in u64 fixed point. The host turns the far field into candela
+// (farfield.js) and a lux plane (illum.js).
+//
+// HERE a BATCH of instances -- each its own table range of primitives and its own sources, with its own ray count --
+// runs as one wave chain: k_opt_gen fills the wave with the rays of every instance (each instance's rays split evenly
+// over the waves, photons.js planBatches), the renderer's persistent march (k_march<INST>) moves each ray through its
+// own instance's primitives only, and k_opt_shade shades and tallies. The tallies are FP64: per instance the totals
+// (shared-memory atomics per CTA, one global add each at the end), the far field on a (C, gamma) grid and the lux map
+// on a plane at a set height along the axis (global FP64 atomics, spread over their bins).
+#include <algorithm>
+#include <cmath>
+#include <string>
+#include <vector>
+
+#include "st_ext.h"
+#include "st_kernels.cuh"
+
+using namespace st;
+
+#define OPT_MAX_INST 256u
+#define OPT_TOT 8u          // per instance: emitted, escaped, lost, detected, absorbed, interactions, rays, unused
+#define OPT_WAVE (4u << 20)
+
+namespace {
+
+struct OptArgs {
+    WaveArgs w;
+    const st_optics_source* src;    // sorted by instance
+    const float* cdf;               // each source's cumulative share within its instance
+    const uint2* src_range;         // per instance [first, count) of src
+    const float4* origin;           // per instance: where its axis starts (its first source's centre)
+    const uint32_t* wave_first;     // per instance: the first ray id of this wave
+    const uint32_t* wave_prefix;    // per instance: the wave's slots before it (n_inst + 1 entries)
+    uint32_t n_inst;
+    uint32_t seed;
+    f3 axis, c0, c90;
+    uint32_t nC, nG, cells;
+    float half, height;
+    double* far;                    // n_inst * nG * nC
+    double* lux;                    // n_inst * cells * cells
+    double* tot;                    // n_inst * OPT_TOT
+};
+
+// the far field's bin (kernels.js:251-272 optFarAdd), in f32 as the kernel bins it
+__device__ __forceinline__ uint32_t far_bin(const OptArgs& o, f3 d) {
+    f3 dn = normalize(d);
+    float g = acosf(clampf(dot(dn, o.axis), -1.f, 1.f));
+    float c = atan2f(dot(dn, o.c90), dot(dn, o.c0));
+    if (c < 0.f) c += 6.28318530718f;
+    uint32_t ig = min((uint32_t)(g / 3.14159265359f * (float)(o.nG - 1) + 0.5f), o.nG - 1);
+    uint32_t ic = (uint32_t)(c / 6.28318530718f * (float)o.nC + 0.5f) % o.nC;
+    return ig * o.nC + ic;
+}
+
+// A SOURCE'S RAY (kernels.js:299-408 optSourceRay): the source by flux, a point on it, the side, the direction from
+// its distribution, two march tolerances off the sheet when it is geometry
+__device__ __forceinline__ void source_ray(const OptArgs& o, uint32_t inst, Rng& rng, f3& org, f3& dir, float& en) {
+    const uint2 rg = o.src_range[inst];
+    float4 pick = rng.next();
+    uint32_t k = rg.x;
+    for (uint32_t i = 0; i < rg.y; i++) { k = rg.x + i; if (pick.x <= o.cdf[rg.x + i]) break; }
+    const st_optics_source& s = o.src[k];
+    f3 front = normalize(mk(s.axis[0], s.axis[1], s.axis[2]));
+    f3 t0 = mk(s.tangent[0], s.tangent[1], s.tangent[2]);
+    f3 tu = normalize(t0 - front * dot(t0, front));
+    f3 tv = cross(front, tu);
+    float4 u = rng.next();
+    f3 p = mk(s.centre[0], s.centre[1], s.centre[2]);
+    if (s.shape == 1u) {
+        float r = s.size_x * sqrtf(u.x);
+        float sp, cp;
+        sincosf(6.28318530718f * u.y, &sp, &cp);
+        p = p + (tu * cp + tv * sp) * r;
+    } else if (s.shape == 2u) {
+        p = p + tu * ((2.f * u.x - 1.f) * s.size_x) + tv * ((2.f * u.y - 1.f) * s.size_y);
+    }
+    f3 ax = front;
+    if (s.two_sided && pick.y < 0.5f) ax = -front;
+    float4 u2 = rng.next();
+    float c = 1.f;
+    if (s.dist == 1u) c = 1.f - u2.x * (1.f - s.cos_half);
+    else if (s.dist == 2u) {
+        float e = s.n_exp + 1.f;
+        float lo = powf(fmaxf(s.cos_half, 0.f), e);
+        c = powf(1.f - u2.x * (1.f - lo), 1.f / e);
+    }
+    float sn = sqrtf(fmaxf(0.f, 1.f - c * c));
+    float sp2, cp2;
+    sincosf(6.28318530718f * u2.y, &sp2, &cp2);
+    dir = normalize(tu * (sn * cp2) + tv * (sn * sp2) + ax * c);
+    float off = s.on_surface ? 2.f * march_tol(p, o.w.u.tol) : 0.f;
+    org = p + ax * off;
+    en = fmaxf(1.f, s.emit_n);
+}
+
+__global__ void __launch_bounds__(256) k_opt_gen(OptArgs o) {
+    __shared__ uint32_t pre[OPT_MAX_INST + 1];
+    for (uint32_t i = threadIdx.x; i <= o.n_inst; i += blockDim.x) pre[i] = o.wave_prefix[i];
+    __syncthreads();
+    const WaveArgs& a = o.w;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < a.slots; i += gridDim.x * blockDim.x) {
+        // the instance whose slots hold i: the first j in [1, n] with pre[j] > i, less one
+        uint32_t lo = 1, hi = o.n_inst;
+        while (lo < hi) { uint32_t mid = (lo + hi) >> 1; if (pre[mid] > i) hi = mid; else lo = mid + 1; }
+        const uint32_t inst = lo - 1;
+        uint32_t id = o.wave_first[inst] + (i - pre[inst]);
+        Rng rng;
+        rng.h = sample_seed(o.seed, inst);
+        rng.seed(id);
+        rng.seed(0x9E3779B9u);
+        f3 org, dir;
+        float en;
+        source_ray(o, inst, rng, org, dir, en);
+        a.pb.pos[i] = make_float4(org.x, org.y, org.z, 0.f);
+        a.pb.dir[i] = make_float4(dir.x, dir.y, dir.z, en);
+        a.pb.beta[i] = make_float4(1.f, 1.f, 1.f, 1.f);
+        a.pb.rad[i] = make_float4(1.f, 1.f, 1.f, 0.f);          // a photon's radiance field is its flux: weight 1
+        a.pb.meta[i] = make_uint4(id, meta_y(0, 0, RAY_ACTIVE), 0u, inst);
+        a.q.ray[0][i] = i;
+    }
+}
+
+// THE SHADE (kernels.js:571-699): escaped, lost, a detector's, or an interaction -- pathBegin..pathEnd with a
+// photon's rules: no light sampling, no end at a scatter, the bounce cap -- each tallied in FP64
+__global__ void __launch_bounds__(256) k_opt_shade(OptArgs o, int nxt, int last) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    __shared__ __align__(8) uint64_t mbar;
+    __shared__ __align__(8) uint64_t mbar2;
+    const WaveArgs& a = o.w;
+    const Uni& u = a.u;
+    DPrim* sp = reinterpret_cast<DPrim*>(smem);
+    st_material* sm = reinterpret_cast<st_material*>(smem + u.n_prims * sizeof(DPrim));
+    double* stot = reinterpret_cast<double*>(smem + u.n_prims * sizeof(DPrim) + u.n_mats * sizeof(st_material));
+    for (uint32_t i = threadIdx.x; i < o.n_inst * OPT_TOT; i += blockDim.x) stot[i] = 0.0;
+    if (!stage_table(sp, a.prims, u.n_prims * (uint32_t)sizeof(DPrim), &mbar, a.ctr)) return;
+    if (!stage_table(sm, a.mats, u.n_mats * (uint32_t)sizeof(st_material), &mbar2, a.ctr)) return;
+    const uint32_t count = a.ctr->hitCount;
+    uint32_t* __restrict__ outq = nxt ? a.q.ray[1] : a.q.ray[0];
+    uint32_t* outc = nxt ? &a.ctr->rayCount[1] : &a.ctr->rayCount[0];
+    const uint32_t stride = gridDim.x * blockDim.x;
+    const uint32_t nrounds = (count + stride - 1) / stride;
+    for (uint32_t r = 0; r < nrounds; r++) {
+        uint32_t q = r * stride + blockIdx.x * blockDim.x + threadIdx.x;
+        bool cont = false;
+        uint32_t slot = 0;
+        f3 pos, dir, beta;
+        float ltot = 0.f, n = 1.f;
+        uint4 m4 = make_uint4(0, 0, 0, 0);
+        if (q < count) {
+            slot = a.q.hit[q];
+            const float dh = a.q.hitd[q];
+            float4 p4 = a.pb.pos[slot], d4 = a.pb.dir[slot], b4 = a.pb.beta[slot];
+            m4 = a.pb.meta[slot];
+            pos = xyz(p4); ltot = p4.w; dir = xyz(d4); n = d4.w; beta = xyz(b4);
+            const uint32_t inst = m4.w, id = m4.x;
+            uint32_t bounces = m4.y & 0xffu, state = m4.y >> 16;
+            double* T = stot + inst * OPT_TOT;
+            const float wIn = luma(beta);                             // optWeight: beta x radiance (1), as luminance
+            if (state == RAY_ESCAPED) {                               // kernels.js:609-625
+                atomicAdd(&T[1], (double)wIn);
+                atomicAdd(&o.far[(size_t)inst * o.nG * o.nC + far_bin(o, dir)], (double)wIn);
+                // the lux plane: the escaping ray's line at `height` along the axis (nothing lies beyond the scene)
+                float dn = dot(dir, o.axis);
+                if (o.cells && dn > 0.f) {
+                    float4 og = o.origin[inst];
+                    f3 rel = pos - xyz(og);
+                    float t = (o.height - dot(rel, o.axis)) / dn;
+                    f3 hp = rel + dir * t;
+                    float ha = dot(hp, o.c0), hb = dot(hp, o.c90);
+                    float cell = 2.f * o.half / (float)o.cells;
+                    if (t >= 0.f && fabsf(ha) < o.half && fabsf(hb) < o.half) {
+                        uint32_t ix = min((uint32_t)((ha + o.half) / cell), o.cells - 1);
+                        uint32_t iy = min((uint32_t)((hb + o.half) / cell), o.cells - 1);
+                        atomicAdd(&o.lux[(size_t)inst * o.cells * o.cells + (size_t)iy * o.cells + ix], (double)wIn);
+                    }
+                }
+            } else if (state != RAY_ACTIVE) {
+                atomicAdd(&T[2], (double)wIn);                        // out of steps or length: lost
+            } else {
+                const uint2 rg = o.w.inst_range[inst];
+                const DPrim* ip = sp + rg.x;
+                const uint32_t np = rg.y;
+                float eps = march_tol(pos, u.tol);
+                float gx = scene_dist(ip, np, mk(pos.x + eps, pos.y, pos.z)) - dh;
+                float gy = scene_dist(ip, np, mk(pos.x, pos.y + eps, pos.z)) - dh;
+                float gz = scene_dist(ip, np, mk(pos.x, pos.y, pos.z + eps)) - dh;
+                f3 nn = normalize(mk(gx, gy, gz));
+                bool inside = dh < 0.f;
+                f3 nrm = inside ? -nn : nn;
+                float otol = 10.f * eps;
+                SceneHit h = scene_full(ip, np, pos);
+                const st_material& m = sm[min(h.m, u.n_mats - 1)];
+                if (m.detector > 0.5f && dot(-dir, nrm) >= 0.f) {     // kernels.js:660-672: a detector stops it
+                    atomicAdd(&T[3], (double)wIn);
+                    atomicAdd(&T[5], 1.0);
+                } else if (dot(-dir, nrm) < 0.f) {                    // seen from behind: moved on, no interaction
+                    f3 off = dir * otol;
+                    pos = pos + off; ltot += length(off) * n;
+                    if (last) atomicAdd(&T[2], (double)wIn);
+                    else cont = true;
+                } else {
+                    Rng rng;
+                    rng.h = sample_seed(o.seed, inst);
+                    rng.seed(id);
+                    rng.seed(bounces);
+                    bounces += 1;
+                    float n0 = n, n1 = fmaxf(m.ior, n0);
+                    if (m.transmission > 0.f && m.metallic < 1.f) {
+                        SceneHit mb = scene_full(ip, np, pos + (-nrm) * (otol * 2.f));
+                        n1 = sm[min(mb.a, u.n_mats - 1)].ior;
+                    }
+                    float pG = sat(m.transmission), trans = m.transmission, specv = m.specular;
+                    bool diffFace = false;
+                    if (inside && pG > 0.f && pG < 1.f) {
+                        float k = mixf(2.f * m.specular, 1.f, pG);
+                        float4 r4 = rng.next();
+                        if (r4.x < pG) trans = 1.f;
+                        else { trans = 0.f; specv = 0.5f * k; diffFace = true; }
+                    }
+                    float etaFace = diffFace ? fminf(n0, n1) / fmaxf(n0, n1) : n0 / n1;
+                    Lobes lb = make_lobes(nrm, -dir, m, etaFace, a.tab, trans, specv);
+                    lb.etaT = n0 / n1;
+                    LobeSample smp = lobes_sample(lb, a.tab, rng.next());
+                    dir = smp.dir;
+                    beta = beta * smp.w;
+                    if (smp.transmitted) n = n1;
+                    uint32_t st = RAY_ACTIVE;
+                    if (max3(smp.w) <= 0.f) st = RAY_ABSORBED;
+                    f3 off = dir * otol;
+                    pos = pos + off; ltot += length(off) * n;
+                    if (bounces > u.maxbounce) st = RAY_TERMINATED;
+                    atomicAdd(&T[5], 1.0);
+                    bool goesOn = st == RAY_ACTIVE || st == RAY_TERMINATED;
+                    float wOut = goesOn ? luma(beta) : 0.f;
+                    atomicAdd(&T[4], (double)(wIn - wOut));
+                    if (st == RAY_TERMINATED || (st == RAY_ACTIVE && last)) atomicAdd(&T[2], (double)wOut);
+                    else if (st == RAY_ACTIVE) cont = true;
+                    m4.y = meta_y(bounces, (m4.y >> 8) & 0xffu, RAY_ACTIVE);
+                }
+            }
+        }
+        uint32_t rq = warp_append(outc, cont);
+        if (cont) {
+            a.pb.pos[slot] = f4(pos, ltot);
+            a.pb.dir[slot] = f4(dir, n);
+            a.pb.beta[slot] = f4(beta, 1.f);
+            m4.y = (m4.y & 0xffffu) | (RAY_ACTIVE << 16);
+            a.pb.meta[slot] = m4;
+            outq[rq] = slot;
+        }
+    }
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < o.n_inst * OPT_TOT; i += blockDim.x)
+        if (stot[i] != 0.0) atomicAdd(&o.tot[i], stot[i]);
+}
+
+f3 normalize_host(f3 a) {
+    float l = std::sqrt(a.x * a.x + a.y * a.y + a.z * a.z);
+    return mk(a.x / l, a.y / l, a.z / l);
+}
+
+template <class X>
+cudaError_t grow(X*& p, size_t& have, size_t want) {
+    if (have >= want && p) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr;
+    have = 0;
+    cudaError_t e = cudaMalloc(&p, want * sizeof(X));
+    if (e == cudaSuccess) have = want;
+    return e;
+}
+
+// the optics run's device buffers, kept in the context between runs
+struct OptBuf {
+    float4 *pos = nullptr, *dir = nullptr, *beta = nullptr, *rad = nullptr;
+    uint4* meta = nullptr;
+    uint32_t *ray0 = nullptr, *ray1 = nullptr, *hit = nullptr;
+    float* hitd = nullptr;
+    size_t cap = 0, c1 = 0, c2 = 0, c3 = 0, c4 = 0, c5 = 0, c6 = 0, c7 = 0, c8 = 0, c9 = 0;
+    double *far = nullptr, *lux = nullptr, *tot = nullptr;
+    size_t nfar = 0, nlux = 0, ntot = 0;
+    st_optics_source* src = nullptr; size_t nsrc = 0;
+    float* cdf = nullptr; size_t ncdf = 0;
+    uint2 *range = nullptr, *srange = nullptr; size_t nrange = 0, nsrange = 0;
+    float4* origin = nullptr; size_t norigin = 0;
+    uint32_t *wfirst = nullptr, *wpre = nullptr; size_t nwfirst = 0, nwpre = 0;
+    DevCtr* ctr = nullptr; size_t nctr = 0;
+};
+
+}  // namespace
+
+void optics_free(OpticsState& os) {
+    if (!os.scratch) return;
+    OptBuf* B = static_cast<OptBuf*>(os.scratch);
+    void* ps[] = {B->pos, B->dir, B->beta, B->rad, B->meta, B->ray0, B->ray1, B->hit, B->hitd, B->far, B->lux, B->tot,
+                  B->src, B->cdf, B->range, B->srange, B->origin, B->wfirst, B->wpre, B->ctr};
+    for (void* p : ps)
+        if (p) cudaFree(p);
+    delete B;
+    os.scratch = nullptr;
+}
+
+extern "C" {
+
+int st_optics_set_sources(st_ctx* ctx, const st_optics_source* src, uint32_t n) {
+    if (!ctx || (n && !src)) return ST_ERR_ARG;
+    for (uint32_t i = 0; i < n; i++)
+        if (src[i].shape > 2 || src[i].dist > 2 || !(src[i].flux >= 0) || src[i].instance >= OPT_MAX_INST) {
+            ctx_set_error(ctx, "source " + std::to_string(i) + ": shape, distribution, flux or instance out of range");
+            return ST_ERR_ARG;
+        }
+    ctx_ext(ctx).optics.sources.assign(src, src + n);
+    return ST_OK;
+}
+
+int st_optics_set_far(st_ctx* ctx, const st_optics_far* far) {
+    if (!ctx || !far) return ST_ERR_ARG;
+    if (far->nC == 0 || far->nG < 2 || (uint64_t)far->nC * far->nG > (1u << 24)) {
+        ctx_set_error(ctx, "far field grid out of range");
+        return ST_ERR_ARG;
+    }
+    ctx_ext(ctx).optics.far = *far;
+    ctx_ext(ctx).optics.has_far = true;
+    return ST_OK;
+}
+
+int st_optics_run(st_ctx* ctx, const st_optics_batch* b, double* far_out, double* lux_out, st_optics_totals* totals) {
+    if (!ctx || !b || !b->ray_count || b->n_instances == 0 || b->n_instances > OPT_MAX_INST) return ST_ERR_ARG;
+    OpticsState& os = ctx_ext(ctx).optics;
+    if (!ctx_has_scene(ctx)) { ctx_set_error(ctx, "set a scene first"); return ST_ERR_STATE; }
+    if (!os.has_far) { ctx_set_error(ctx, "set the far field first (st_optics_set_far)"); return ST_ERR_STATE; }
+    if (b->lux_cells > 4096) { ctx_set_error(ctx, "lux map over 4096 cells a side"); return ST_ERR_ARG; }
+    if (b->maxbounce > 250) { ctx_set_error(ctx, "maxbounce over 250 (a ray's bounces are counted in 8 bits)"); return ST_ERR_ARG; }
+    const uint32_t NI = b->n_instances;
+    if ((uint64_t)NI * b->lux_cells * b->lux_cells > (1ull << 28) ||
+        (uint64_t)NI * os.far.nC * os.far.nG > (1ull << 28)) {
+        ctx_set_error(ctx, "the batch's far fields or lux maps hold over 2^28 bins");
+        return ST_ERR_ARG;
+    }
+    cudaSetDevice(ctx_device(ctx));
+    cudaStream_t st = ctx_stream(ctx);
+    if (!os.scratch) os.scratch = new OptBuf();
+    OptBuf& B = *static_cast<OptBuf*>(os.scratch);
+    auto fail = [&](cudaError_t e, const char* what) {
+        ctx_set_error(ctx, std::string(what) + ": " + cudaGetErrorString(e));
+        return e == cudaErrorMemoryAllocation ? ST_ERR_OOM : ST_ERR_CUDA;
+    };
+
+    // each instance's table range: the primitives whose flags >> 8 name it, contiguous (st_optics_batch)
+    const uint32_t np = ctx_n_prims(ctx);
+    std::vector<st_prim> prims(np);
+    {
+        std::vector<DPrim> dp(np);
+        cudaMemcpy(dp.data(), ctx_d_prims(ctx), np * sizeof(DPrim), cudaMemcpyDeviceToHost);
+        for (uint32_t i = 0; i < np; i++) prims[i].flags = dp[i].h.w;
+    }
+    std::vector<uint2> range(NI, make_uint2(0, 0));
+    for (uint32_t i = 0; i < np; i++) {
+        uint32_t inst = prims[i].flags >> 8;
+        if (inst >= NI) { ctx_set_error(ctx, "primitive " + std::to_string(i) + " names an instance past the batch"); return ST_ERR_ARG; }
+        if (range[inst].y == 0) range[inst] = make_uint2(i, 1);
+        else if (range[inst].x + range[inst].y == i) range[inst].y++;
+        else { ctx_set_error(ctx, "instance " + std::to_string(inst) + "'s primitives are not contiguous"); return ST_ERR_ARG; }
+    }
+    // sources by instance, their cumulative shares, each instance's axis origin
+    std::vector<st_optics_source> src;
+    std::vector<float> cdf;
+    std::vector<uint2> srange(NI, make_uint2(0, 0));
+    std::vector<float4> origin(NI, make_float4(0, 0, 0, 0));
+    for (uint32_t inst = 0; inst < NI; inst++) {
+        srange[inst].x = (uint32_t)src.size();
+        double tot = 0;
+        for (auto& s : os.sources) if (s.instance == inst) { src.push_back(s); tot += s.flux; }
+        srange[inst].y = (uint32_t)src.size() - srange[inst].x;
+        if (b->ray_count[inst] && (!srange[inst].y || range[inst].y == 0)) {
+            ctx_set_error(ctx, "instance " + std::to_string(inst) + " has rays but no source or no geometry");
+            return ST_ERR_ARG;
+        }
+        double acc = 0;
+        for (uint32_t k = 0; k < srange[inst].y; k++) {
+            acc += src[srange[inst].x + k].flux;
+            cdf.push_back(tot > 0 ? (float)(acc / tot) : (float)(k + 1) / srange[inst].y);
+        }
+        if (srange[inst].y) {
+            cdf.back() = 1.f;
+            const st_optics_source& s0 = src[srange[inst].x];
+            origin[inst] = make_float4(s0.centre[0], s0.centre[1], s0.centre[2], 0.f);
+        }
+    }
+    const st_optics_far& F = os.far;
+    const size_t nfar = (size_t)NI * F.nG * F.nC, nlux = (size_t)NI * b->lux_cells * b->lux_cells;
+    uint64_t total = 0;
+    for (uint32_t i = 0; i < NI; i++) total += b->ray_count[i];
+    const uint32_t K = (uint32_t)std::max<uint64_t>(1, (total + OPT_WAVE - 1) / OPT_WAVE);   // planBatches
+    const size_t W = (size_t)std::min<uint64_t>(OPT_WAVE + NI, total + NI);
+    cudaError_t e;
+    if ((e = grow(B.pos, B.cap, W)) || (e = grow(B.dir, B.c1, W)) || (e = grow(B.beta, B.c2, W)) || (e = grow(B.rad, B.c3, W)) ||
+        (e = grow(B.meta, B.c4, W)) || (e = grow(B.ray0, B.c5, W)) || (e = grow(B.ray1, B.c6, W)) || (e = grow(B.hit, B.c7, W)) ||
+        (e = grow(B.hitd, B.c8, W)) || (e = grow(B.far, B.nfar, std::max<size_t>(nfar, 1))) ||
+        (e = grow(B.lux, B.nlux, std::max<size_t>(nlux, 1))) || (e = grow(B.tot, B.ntot, (size_t)NI * OPT_TOT)) ||
+        (e = grow(B.src, B.nsrc, std::max<size_t>(src.size(), 1))) || (e = grow(B.cdf, B.ncdf, std::max<size_t>(cdf.size(), 1))) ||
+        (e = grow(B.range, B.nrange, (size_t)NI)) || (e = grow(B.srange, B.nsrange, (size_t)NI)) ||
+        (e = grow(B.origin, B.norigin, (size_t)NI)) || (e = grow(B.wfirst, B.nwfirst, (size_t)NI)) ||
+        (e = grow(B.wpre, B.nwpre, (size_t)NI + 1)) || (e = grow(B.ctr, B.nctr, (size_t)1)))
+        return fail(e, "cudaMalloc optics buffers");
+    if ((e = cudaMemcpyAsync(B.src, src.data(), src.size() * sizeof(st_optics_source), cudaMemcpyHostToDevice, st)) ||
+        (e = cudaMemcpyAsync(B.cdf, cdf.data(), cdf.size() * 4, cudaMemcpyHostToDevice, st)) ||
+        (e = cudaMemcpyAsync(B.range, range.data(), NI * sizeof(uint2), cudaMemcpyHostToDevice, st)) ||
+        (e = cudaMemcpyAsync(B.srange, srange.data(), NI * sizeof(uint2), cudaMemcpyHostToDevice, st)) ||
+        (e = cudaMemcpyAsync(B.origin, origin.data(), NI * sizeof(float4), cudaMemcpyHostToDevice, st)) ||
+        (e = cudaMemsetAsync(B.far, 0, std::max<size_t>(nfar, 1) * 8, st)) ||
+        (e = cudaMemsetAsync(B.lux, 0, std::max<size_t>(nlux, 1) * 8, st)) ||
+        (e = cudaMemsetAsync(B.tot, 0, (size_t)NI * OPT_TOT * 8, st)) ||
+        (e = cudaMemsetAsync(B.ctr, 0, sizeof(DevCtr), st)))
+        return fail(e, "optics upload");
+
+    // the uniforms the march and the shade read: the scene's tolerance and radius, the settings' march controls
+    const st_scene_desc& sd = ctx_desc(ctx);
+    OptArgs o;
+    Uni& u = o.w.u;
+    u = Uni{};
+    u.maxbounce = b->maxbounce ? b->maxbounce : 32;
+    u.maxiter = 400;
+    u.nee = 0; u.rr = 0;
+    u.stepscale = 0.9f;
+    u.budget = u.maxbounce + 1 + (u.maxiter + MARCH_CHUNK - 1) / MARCH_CHUNK + 4;
+    double tol = sd.tolerance > 0 ? sd.tolerance : 1e-3;
+    double R = sd.env_radius > 0 ? sd.env_radius : 400.0;
+    u.tol = (float)tol; u.envR = (float)R; u.envR2 = (float)(R * R);
+    u.n_prims = np; u.n_mats = ctx_n_mats(ctx);
+    u.P = 1;
+    o.w.prims = ctx_d_prims(ctx);
+    o.w.mats = ctx_d_mats(ctx);
+    o.w.tab = ctx_tab(ctx);
+    o.w.pb = PathBuf{B.pos, B.dir, B.beta, B.rad, B.meta};
+    o.w.q = Queues{};
+    o.w.q.ray[0] = B.ray0; o.w.q.ray[1] = B.ray1; o.w.q.hit = B.hit; o.w.q.hitd = B.hitd;
+    o.w.q.cap = (uint32_t)W;
+    o.w.ctr = B.ctr;
+    o.w.frame = nullptr; o.w.acc = nullptr; o.w.mom = nullptr;
+    o.w.spw = 1;
+    o.w.inst_range = B.range;
+    o.src = B.src; o.cdf = B.cdf; o.src_range = B.srange; o.origin = B.origin;
+    o.wave_first = B.wfirst; o.wave_prefix = B.wpre;
+    o.n_inst = NI;
+    o.seed = b->seed;
+    f3 ax = normalize_host(mk(F.axis[0], F.axis[1], F.axis[2]));
+    f3 c0 = normalize_host(mk(F.c0[0], F.c0[1], F.c0[2]));
+    o.axis = ax; o.c0 = c0;
+    o.c90 = mk(ax.y * c0.z - ax.z * c0.y, ax.z * c0.x - ax.x * c0.z, ax.x * c0.y - ax.y * c0.x);
+    o.nC = F.nC; o.nG = F.nG; o.cells = b->lux_cells;
+    o.half = b->lux_half; o.height = b->lux_height;
+    o.far = B.far; o.lux = B.lux; o.tot = B.tot;
+    const int sms = ctx_sms(ctx);
+    const size_t shade_smem = np * sizeof(DPrim) + u.n_mats * sizeof(st_material) + (size_t)NI * OPT_TOT * 8;
+    cudaFuncSetAttribute(k_opt_shade, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shade_smem);
+    int shade_blocks = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&shade_blocks, k_opt_shade, 256, shade_smem);
+    shade_blocks = std::max(1, shade_blocks) * sms;
+
+    // the waves: each instance's rays split evenly over K of them (photons.js:31-62 splitPart)
+    for (uint32_t k = 0; k < K; k++) {
+        std::vector<uint32_t> wf(NI), wp(NI + 1, 0);
+        for (uint32_t i = 0; i < NI; i++) {
+            uint64_t n = b->ray_count[i];
+            uint64_t f0 = n * k / K, f1 = n * (k + 1) / K;
+            wf[i] = (uint32_t)f0;
+            wp[i + 1] = wp[i] + (uint32_t)(f1 - f0);
+        }
+        const uint32_t slots = wp[NI];
+        if (!slots) continue;
+        if ((e = cudaMemcpyAsync(B.wfirst, wf.data(), NI * 4, cudaMemcpyHostToDevice, st)) ||
+            (e = cudaMemcpyAsync(B.wpre, wp.data(), (NI + 1) * 4, cudaMemcpyHostToDevice, st)))
+            return fail(e, "optics upload");
+        o.w.slots = slots;
+        if ((e = launch_iter_begin(o.w, 0, 1, 1, st))) return fail(e, "optics launch");
+        k_opt_gen<<<std::min((slots + 255) / 256, (uint32_t)sms * 8u), 256, 0, st>>>(o);
+        int cur = 0;
+        for (uint32_t it = 0; it < u.budget; it++) {
+            int nxt = cur ^ 1, last = it + 1 == u.budget;
+            if (it > 0 && (e = launch_iter_begin(o.w, (int)it, nxt, 0, st))) return fail(e, "optics launch");
+            if ((e = launch_march(o.w, cur, nxt, last, sms, st))) return fail(e, "optics march");
+            k_opt_shade<<<shade_blocks, 256, shade_smem, st>>>(o, nxt, last);
+            cur = nxt;
+        }
+        if ((e = cudaGetLastError())) return fail(e, "optics launch");
+    }
+    std::vector<double> tot((size_t)NI * OPT_TOT);
+    if ((e = cudaMemcpyAsync(tot.data(), B.tot, tot.size() * 8, cudaMemcpyDeviceToHost, st)) ||
+        (far_out && nfar && (e = cudaMemcpyAsync(far_out, B.far, nfar * 8, cudaMemcpyDeviceToHost, st))) ||
+        (lux_out && nlux && (e = cudaMemcpyAsync(lux_out, B.lux, nlux * 8, cudaMemcpyDeviceToHost, st))) ||
+        (e = cudaStreamSynchronize(st)))
+        return fail(e, "optics readback");
+    DevCtr c;
+    cudaMemcpy(&c, B.ctr, sizeof(DevCtr), cudaMemcpyDeviceToHost);
+    if (c.errflag) { ctx_set_error(ctx, "a kernel's wait for its scene table ran out of iterations"); return ST_ERR_TIMEOUT; }
+    if (totals)
+        for (uint32_t i = 0; i < NI; i++) {
+            const double* T = &tot[(size_t)i * OPT_TOT];
+            totals[i].emitted = (double)b->ray_count[i];
+            totals[i].escaped = T[1]; totals[i].lost = T[2]; totals[i].detected = T[3]; totals[i].absorbed = T[4];
+            totals[i].interactions = (uint64_t)T[5];
+            totals[i].rays = b->ray_count[i];
+        }
+    return ST_OK;
+}
+
+}  // extern "C"

@@ -15,56 +15,10 @@
 // warp keeps 32 rays in flight however uneven their step counts. The scene's primitive table is staged into
 // shared memory by one bulk copy (cp.async.bulk + mbarrier) per CTA and read as broadcasts. Nothing is read back
 // by the host inside a sample: every kernel sizes itself from the device counters.
-#include "st_internal.h"
+#include "st_kernels.cuh"
 
 namespace st {
 
-#define FULL_MASK 0xffffffffu
-#define INVALID_SLOT 0xffffffffu
-#define CLAIM 64u
-#define WAIT_LIMIT (1u << 24)
-
-__device__ __forceinline__ uint32_t lanemask_lt() {
-    uint32_t m;
-    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
-    return m;
-}
-
-// ------------------------------------------------------------------------------------------------------------
-// A TABLE INTO SHARED MEMORY BY ONE BULK COPY: thread 0 arms an mbarrier with the byte count and issues
-// cp.async.bulk; every thread waits on the barrier's phase, a bounded number of times. bytes is a multiple of 16,
-// both addresses 16-byte aligned (DPrim is 128 bytes, st_material 64, cudaMalloc 256-aligned). Returns false
-// (and flags the counters) if the copy did not land within the limit.
-// ------------------------------------------------------------------------------------------------------------
-__device__ __forceinline__ bool stage_table(void* sdst, const void* gsrc, uint32_t bytes, uint64_t* mbar,
-                                            DevCtr* ctr) {
-    uint32_t mb = (uint32_t)__cvta_generic_to_shared(mbar);
-    uint32_t dst = (uint32_t)__cvta_generic_to_shared(sdst);
-    if (threadIdx.x == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mb) : "memory");
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mb), "r"(bytes) : "memory");
-        asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
-                     ::"r"(dst), "l"(gsrc), "r"(bytes), "r"(mb) : "memory");
-    }
-    uint32_t done = 0;
-    for (uint32_t k = 0; k < WAIT_LIMIT && !done; k++) {
-        asm volatile(
-            "{\n\t.reg .pred p;\n\t"
-            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\n\t"
-            "selp.u32 %0, 1, 0, p;\n\t}"
-            : "=r"(done) : "r"(mb) : "memory");
-    }
-    // one decision for the whole CTA, so no thread leaves while another still waits at a barrier
-    if (__syncthreads_or(!done)) {
-        if (threadIdx.x == 0) atomicExch(&ctr->errflag, 1u);
-        return false;
-    }
-    return true;
-}
 
 // ------------------------------------------------------------------------------------------------------------
 // THE ALBEDO TABLES (microfacet.js:245-330), the isotropic part: one thread per entry, a 32 x 32 stratified grid
@@ -163,17 +117,6 @@ __global__ void k_iter_begin(DevCtr* ctr, int it, int nxt, uint32_t slots, int f
     }
 }
 
-// warp-aggregated append: one atomic per warp for every lane with want set; returns this lane's position
-__device__ __forceinline__ uint32_t warp_append(uint32_t* counter, bool want) {
-    uint32_t m = __ballot_sync(FULL_MASK, want);
-    uint32_t base = 0;
-    int lane = threadIdx.x & 31;
-    int leader = m ? __ffs(m) - 1 : 0;
-    if (m && lane == leader) base = atomicAdd(counter, (uint32_t)__popc(m));
-    base = __shfl_sync(FULL_MASK, base, leader);
-    return base + __popc(m & lanemask_lt());
-}
-
 // ------------------------------------------------------------------------------------------------------------
 // THE MARCH (wavefront.js:866-947), persistent. Each warp claims CLAIM queue entries at a time; a lane whose ray
 // ended takes the next one at once. A step: the scene's distance, the hit test against marchTol, lmax and
@@ -182,7 +125,7 @@ __device__ __forceinline__ uint32_t warp_append(uint32_t* counter, bool want) {
 // in the next iteration (the reference's 32-step dispatches, wavefront.js:870); the last iteration's launch
 // marches every ray to its end.
 // ------------------------------------------------------------------------------------------------------------
-template <bool HAZE>
+template <bool HAZE, bool INST>
 __global__ void __launch_bounds__(256, 3) k_march(WaveArgs a, int cur, int nxt, int last) {
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ __align__(8) uint64_t mbar;
@@ -205,6 +148,7 @@ __global__ void __launch_bounds__(256, 3) k_march(WaveArgs a, int cur, int nxt, 
     uint32_t wpos = 0, wend = 0;
     bool exhausted = false;
     unsigned long long evals = 0;
+    uint32_t pfirst = 0, pcount = n_prims;          // the primitives this ray sees: its instance's, in a batch
 
     for (;;) {
         // ---- refill: idle lanes take the warp's next claimed entries ----
@@ -227,6 +171,7 @@ __global__ void __launch_bounds__(256, 3) k_march(WaveArgs a, int cur, int nxt, 
                     uint4 m4 = a.pb.meta[slot];
                     steps = m4.z;
                     evals_here = 0;
+                    if (INST) { uint2 rg = a.inst_range[m4.w]; pfirst = rg.x; pcount = rg.y; }
                     tmax = HAZE ? a.pb.rad[slot].w : 0.f;
                     if (HAZE && tmax == 0.f) {
                         // THE LEG'S COLLISION, drawn as it starts (haze.js:255-273 hazeDraw)
@@ -261,7 +206,7 @@ __global__ void __launch_bounds__(256, 3) k_march(WaveArgs a, int cur, int nxt, 
                 state = RAY_SCATTER;
                 fin = true;
             } else {
-                float d = scene_dist(sp, n_prims, pos);
+                float d = scene_dist(sp + pfirst, pcount, pos);
                 evals++;
                 evals_here++;
                 float ea = fabsf(d);
@@ -302,20 +247,6 @@ __global__ void __launch_bounds__(256, 3) k_march(WaveArgs a, int cur, int nxt, 
     // the steps taken, one atomic per warp
     for (int o = 16; o > 0; o >>= 1) evals += __shfl_down_sync(FULL_MASK, evals, o);
     if (lane == 0 && evals) atomicAdd(&a.ctr->march_steps, evals);
-}
-
-// ------------------------------------------------------------------------------------------------------------
-// THE DEPOSIT (wavefront.js:162-245): refused if a channel is NaN or inf or the luminance negative
-// ------------------------------------------------------------------------------------------------------------
-__device__ __forceinline__ bool bad_deposit(f3 c) {
-    return !isfinite(c.x) || !isfinite(c.y) || !isfinite(c.z) || luma(c) < 0.f;
-}
-__device__ __forceinline__ void deposit(float4* frame, uint32_t pix, f3 c, DevCtr* ctr) {
-    if (bad_deposit(c)) { atomicAdd(&ctr->nonfinite, 1u); return; }
-    float* f = reinterpret_cast<float*>(frame + pix);
-    if (c.x != 0.f) atomicAdd(f + 0, c.x);
-    if (c.y != 0.f) atomicAdd(f + 1, c.y);
-    if (c.z != 0.f) atomicAdd(f + 2, c.z);
 }
 
 // ------------------------------------------------------------------------------------------------------------
@@ -738,14 +669,18 @@ static int occupancy(const void* fn, size_t smem) {
 }
 cudaError_t launch_march(const WaveArgs& a, int cur, int nxt, int last, int sms, cudaStream_t s) {
     size_t smem = a.u.n_prims * sizeof(DPrim);
-    if (a.u.haze_on) {
-        if (smem > 48 * 1024) cudaFuncSetAttribute(k_march<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        int nb = occupancy((const void*)k_march<true>, smem);
-        k_march<true><<<sms * nb, 256, smem, s>>>(a, cur, nxt, last);
+    if (a.inst_range) {
+        if (smem > 48 * 1024) cudaFuncSetAttribute(k_march<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        int nb = occupancy((const void*)k_march<false, true>, 32 * 1024);
+        k_march<false, true><<<sms * nb, 256, smem, s>>>(a, cur, nxt, last);
+    } else if (a.u.haze_on) {
+        if (smem > 48 * 1024) cudaFuncSetAttribute(k_march<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        int nb = occupancy((const void*)k_march<true, false>, smem);
+        k_march<true, false><<<sms * nb, 256, smem, s>>>(a, cur, nxt, last);
     } else {
-        if (smem > 48 * 1024) cudaFuncSetAttribute(k_march<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (!g_occ_march) g_occ_march = occupancy((const void*)k_march<false>, 32 * 1024);
-        k_march<false><<<sms * g_occ_march, 256, smem, s>>>(a, cur, nxt, last);
+        if (smem > 48 * 1024) cudaFuncSetAttribute(k_march<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (!g_occ_march) g_occ_march = occupancy((const void*)k_march<false, false>, 32 * 1024);
+        k_march<false, false><<<sms * g_occ_march, 256, smem, s>>>(a, cur, nxt, last);
     }
     return cudaGetLastError();
 }

@@ -244,3 +244,68 @@ def haze_furnace(width=64, height=64, sigma_t=0.2, g=0.0, albedo=1.0, sky=1000.0
     s.view = look_at((0.0, -6.0, 2.0), (0.0, 0.0, 2.0), 50.0, width / height)
     s.info = {"closed_form": sky}
     return s
+
+
+# ---------------------------------------------------------------------------------------------------------------
+# Config 5: the batched optics bench (optics/index.js; the reference's aspheric condenser, scenes/aspheric-condenser.json)
+# ---------------------------------------------------------------------------------------------------------------
+MM = 1e-3
+
+
+def led_lens_instance(inst, k1, a4_mm, a6_mm, mats_ids=(1, 2), ior=1.49):
+    """One emitter + lens: a 1 x 1 x 0.2 mm die (its top face at z = 0) under a plano-convex aspheric lens (6 mm
+    across, 2.5 mm thick, front radius 3.2 mm, conic k1, 4th/6th coefficients a4, a6 given in mm^-3, mm^-5), its flat
+    back 0.5 mm above the die. Primitives flagged with the instance (flags >> 8)."""
+    die = prim(ST_PRIM_BOX, pos=(0, 0, -0.1 * MM), params=(0.5 * MM, 0.5 * MM, 0.1 * MM), material=mats_ids[0],
+               flags=inst << 8)
+    t, D, R1 = 2.5 * MM, 6.0 * MM, 3.2 * MM
+    lens = prim(ST_PRIM_ASPHERE, pos=(0, 0, 0.5 * MM + t / 2),
+                params=(D, t, R1, k1, a4_mm * 1e9, a6_mm * 1e15, 0.0, 0.0, 0.0, 0.0), material=mats_ids[1],
+                flags=inst << 8)
+    return [die, lens]
+
+
+def led_source(inst, flux=1.0):
+    """The die's top face as a Lambertian source (cos^1 over the hemisphere), 1 x 1 mm, stepped off its sheet."""
+    s = __import__("shadytracer_gb300.st_types", fromlist=["StOpticsSource"]).StOpticsSource()
+    for i, v in enumerate((0.0, 0.0, 0.0)):
+        s.centre[i] = v
+    s.flux = flux
+    for i, v in enumerate((0.0, 0.0, 1.0)):
+        s.axis[i] = v
+    for i, v in enumerate((1.0, 0.0, 0.0)):
+        s.tangent[i] = v
+    s.shape = 2
+    s.size_x = s.size_y = 0.5 * MM
+    s.dist = 2
+    s.cos_half = 0.0
+    s.n_exp = 1.0
+    s.emit_n = 1.0
+    s.two_sided = 0
+    s.on_surface = 1
+    s.instance = inst
+    return s
+
+
+def optics_bench(n_instances=64, seed=5, ray_min=1e5, ray_max=1e7, ray_scale=1.0):
+    """The batched optics bench: n instances of led_lens_instance with k1 ~ U(-1.5, 0), a4, a6 ~ U(-1e-3, 1e-3)
+    (mm units) and IOR 1.49, each with its die's source and a ray count log-uniform in [ray_min, ray_max] (times
+    ray_scale), all drawn from PCG32(seed). Far field 1 x 1 degree (360 x 181 bins), lux 512 x 512 at 1 m."""
+    rng = Pcg32(seed)
+    mats = [air(), diffuse((0.5, 0.5, 0.5)), glass((1, 1, 1), ior=1.49)]
+    prims, srcs, rays, lenses = [], [], [], []
+    for i in range(n_instances):
+        k1 = rng.uniform(-1.5, 0.0)
+        a4 = rng.uniform(-1e-3, 1e-3)
+        a6 = rng.uniform(-1e-3, 1e-3)
+        n = math.exp(rng.uniform(math.log(ray_min), math.log(ray_max)))
+        prims += led_lens_instance(i, k1, a4, a6)
+        srcs.append(led_source(i))
+        rays.append(max(1, int(n * ray_scale)))
+        lenses.append({"k1": k1, "a4_mm": a4, "a6_mm": a6})
+    s = Scene(prims, mats, env_radius=0.02, tolerance=1e-6, name="optics-bench")
+    s.params = default_params(width=16, height=16, maxbounce=32)
+    s.view = look_at((0, -0.05, 0.01), (0, 0, 0.002), 30.0, 1.0)
+    s.info = {"sources": srcs, "rays": rays, "lenses": lenses, "nC": 360, "nG": 181, "lux_cells": 512,
+              "lux_half": 1.0, "lux_height": 1.0, "workload": "optics-bench-%d" % n_instances}
+    return s

@@ -1,0 +1,63 @@
+"""The oracle's render against closed forms, on the CPU (the reference's own on-GPU answers, lib/pathtracer/tests.js:
+the photometry floor and the haze furnace, restated here for the CPU restatement the GPU path is held to).
+
+A Lambertian floor of albedo a under a uniform sky L reads a L wherever it is seen (every path that leaves it sees the
+sky); an albedo-1 haze box in a uniform sky reads L everywhere (what it scatters out of a ray it scatters back in).
+The microfacet albedo tables and the scene distance function are checked for their defining properties.
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle
+from shadytracer_gb300 import scenes
+
+
+def test_floor_closed_form():
+    s = scenes.floor_furnace(width=64, height=64, maxbounce=4)
+    a = oracle.render(s, 2)
+    L = a.luma()
+    # the rows that meet the floor steeply read 800 in every sample; nearer the horizon a bounce so shallow that its
+    # march steps run out (maxiter) ends dark, as the reference's does
+    floor = L[:20]
+    assert abs(floor.mean() / 800.0 - 1) < 1e-3, floor.mean()
+    assert np.mean(np.abs(floor - 800.0) < 0.08) > 0.99
+    assert np.allclose(L[-3:], 1000.0, rtol=1e-6)
+
+
+def test_haze_furnace_closed_form():
+    s = scenes.haze_furnace(width=24, height=24, sigma_t=0.5, g=0.3)
+    a = oracle.render(s, 4)
+    assert abs(a.luma().mean() - 1000.0) < 1000.0 * 2e-3
+
+
+def test_counts_and_moments():
+    s = scenes.floor_furnace(width=16, height=16, maxbounce=4)
+    a = oracle.render(s, 3)
+    assert np.all(a.count == 3)
+    assert np.allclose(a.S, 1.0 / 3.0)
+    a = oracle.render(s, 1, accum=a)
+    assert np.all(a.count == 4) and a.next_sample == 4
+
+
+def test_microfacet_tables():
+    ec, ecavg, e1 = oracle.mf_tables()
+    assert np.all(ec >= 0) and np.all(ec <= 1.0 + 1e-5)
+    assert np.all(e1 >= 0) and np.all(e1 <= 1.0 + 1e-5)
+    e1 = e1.reshape(32, 32)                 # rows: roughness, smoothest first
+    assert np.all(e1[0] > 0.99)             # the smoothest lobe reflects next to everything in one bounce
+    assert np.all(np.diff(e1[:, -1]) <= 1e-3) and e1[-1, -1] < 0.5     # rougher loses more to multiple scattering
+    ec64, ecavg64, e164 = oracle.mf_tables(fp64=True)
+    assert np.abs(e164 - e1.reshape(-1)).max() < 2e-3 and np.abs(ec64 - ec).max() < 2e-3
+
+
+def test_scene_distance_is_a_distance():
+    s = scenes.sdf_room(width=32, height=18, n_prims=24)
+    rng = np.random.default_rng(0)
+    p = rng.uniform([-3, -2, 0], [3, 2, 3], (2000, 3)).astype(np.float32)
+    d, m, _ = oracle.scene_sdf(s, p)
+    # 1-Lipschitz (up to the smooth unions' slack): no two points' distances differ by more than their separation
+    q = p + rng.normal(scale=0.05, size=p.shape).astype(np.float32)
+    dq, _, _ = oracle.scene_sdf(s, q)
+    sep = np.linalg.norm(p - q, axis=1)
+    assert np.all(np.abs(d - dq) <= sep * 1.05 + 1e-5)
+    assert np.any(d < 0) and np.any(d > 0)
