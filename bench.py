@@ -5,7 +5,7 @@ Workload (the second of the reference's benchmark configurations): a 6 x 4 x 3 m
 window; 1920 x 1080, 64 samples per pixel, max depth 8, march tolerance 1e-4 m, FP64 pixel tallies. One STEP is
 the whole render -- 64 samples of every pixel, 132.7 M camera paths -- folded into the FP64 accumulation.
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference] [--small]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference] [--small] [--spp S]
 
 value: paths / s with the scene resident on the GPU (graph replays; the timed region brackets K renders with a
        synchronize). e2e: the same through the C ABI as a host calls it -- scene, settings and camera uploaded from
@@ -44,6 +44,7 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--small", action="store_true", help="a 480 x 270, 4-spp render (profiling runs)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
+    ap.add_argument("--spp", type=int, default=0, help="samples per pixel a step (profiling runs; default: 64)")
     return ap.parse_args()
 
 
@@ -54,12 +55,12 @@ def dist_env():
     return rank, world, local
 
 
-def workload(small):
+def workload(small, spp=0):
     from shadytracer_gb300 import scenes
     if small:
-        s = scenes.sdf_room(width=480, height=270, spp=4, maxbounce=8)
+        s = scenes.sdf_room(width=480, height=270, spp=spp or 4, maxbounce=8)
     else:
-        s = scenes.sdf_room(width=1920, height=1080, spp=64, maxbounce=8)
+        s = scenes.sdf_room(width=1920, height=1080, spp=spp or 64, maxbounce=8)
     return s
 
 
@@ -142,25 +143,30 @@ def cpu_baseline(s, budget_s=15.0):
     p = s.params
     P = p.width * p.height
     acc = oracle.Accum(p.width, p.height)
-    probe = min(P, 8192)
+    # bands of consecutive paths from the middle of the picture outwards, one sample each, until the budget is spent
+    band = min(P, 16384)
+    oracle.render(s, 1, acc, fp64=False, threads=threads, sample0=0, path_first=P // 2, path_count=band)  # warm
+    first0 = P // 2
+    n, k = 0, 0
     t = time.perf_counter()
-    oracle.render(s, 1, acc, fp64=False, threads=threads, sample0=0, path_first=P // 2, path_count=probe)
-    rate = probe / max(time.perf_counter() - t, 1e-6)
-    n = int(min(P, max(probe, rate * budget_s)))
-    first = max(0, P // 2 - n // 2)
-    t = time.perf_counter()
-    oracle.render(s, 1, acc, fp64=False, threads=threads, sample0=1, path_first=first, path_count=n)
-    dt = time.perf_counter() - t
+    while True:
+        first = (first0 + k * band) % max(P - band, 1)
+        oracle.render(s, 1, acc, fp64=False, threads=threads, sample0=1, path_first=first, path_count=band)
+        n += band
+        k += 1
+        dt = time.perf_counter() - t
+        if dt >= budget_s or k * band >= P:
+            break
     return {"value": n / dt / 1e6, "unit": "Mpaths/s", "cores": threads, "kind": "port",
-            "sample": "1 sample of %d consecutive paths (rows %d-%d of %dx%d), %.1f s" % (
-                n, first // p.width, (first + n) // p.width, p.width, p.height, dt)}
+            "sample": "%d paths of sample 1 (%d bands of %d consecutive paths from row %d on, %dx%d), %.1f s" % (
+                n, k, band, first0 // p.width, p.width, p.height, dt)}
 
 
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
         return 0
-    s = workload(args.small)
+    s = workload(args.small, args.spp)
     metric = "Mpaths/s"
     for _ in range(max(args.warmup, 0)):
         cpu_baseline(s, budget_s=3.0)
@@ -196,7 +202,7 @@ def run_ours(args):
         dist.init_process_group("nccl", device_id=torch.device("cuda", dev))
     from shadytracer_gb300 import flops
     from shadytracer_gb300.renderer import create_path_tracer
-    s = workload(args.small)
+    s = workload(args.small, args.spp)
     spp = s.info["spp"]
     p = s.params
     P = p.width * p.height
@@ -219,6 +225,7 @@ def run_ours(args):
         one_step()
         rt.sync()
     # ---- timed: value (device-resident scene; graph replays) ----
+    launches0 = rt.counters()["launches"]
     barrier()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with Clocks(dev) as clk:
@@ -231,6 +238,7 @@ def run_ours(args):
     ms = e0.elapsed_time(e1) / args.steps
     clocks = clk.summary()
     c = rt.counters()
+    launches = c["launches"] - launches0          # the library's kernels (graph nodes) in the timed region
     if dist:
         t = torch.tensor([ms], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
@@ -289,14 +297,13 @@ def run_ours(args):
     else:
         peak = sms * 128 * 2 * 2070e6 / 1e12
         peak_src = "FP32 FMA peak at the nominal 2070 MHz (fallback)"
-    launches_per_sample = 2 + 4 * (p.budget or (p.maxbounce + 1 + (p.maxiter + 31) // 32))
     line = {"metric": "Mpaths/s", "value": value, "unit": "Mpaths/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32 (FP64 pixel tallies)", "data": "synthetic (seeded scene)",
             "config": dict(config_of(s), parallelism="replicas" if world > 1 else "1 GPU"),
             "e2e": {"value": world * paths_per_step / e2e_s / 1e6, "unit": "Mpaths/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
-            "gpu_launches": launches_per_sample * spp * args.steps,
+            "gpu_launches": launches,
             "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                          "frac": achieved / peak if peak else None, "traffic": None,
                          "kernel": "k_march", "flops_per_eval": f_eval, "sfu_per_eval": sfu_eval,

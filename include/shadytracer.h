@@ -175,6 +175,7 @@ typedef struct st_counters_t {
     uint32_t flushed;             /* paths the last iteration had to end                           */
     uint32_t shadowcut;           /* shadow rays out of steps                                      */
     uint32_t samples;             /* samples folded since the last invalidate                      */
+    uint64_t launches;            /* kernels the wave chains ran (graph nodes counted) since st_create */
 } st_counters_t;
 
 typedef struct st_image_stats_t {

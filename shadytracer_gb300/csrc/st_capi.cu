@@ -57,6 +57,9 @@ struct st_ctx {
     cudaGraphExec_t graph = nullptr;
     uint32_t graph_w = 0;
     bool graph_ok = true;
+    uint32_t rec_launches = 0;            // kernels in the last recorded wave chain
+    uint32_t graph_launches = 0;          // ...and in the graph's (its kernel nodes)
+    uint64_t launches = 0;                // kernels run by the wave chains since the context was made
     // per-kernel timing (core/kerneltime.js's role): CUDA events on this stream around each launch, when on
     bool timing = false;
     std::vector<KTimeAcc> ktimes;
@@ -81,7 +84,7 @@ static int cuda_fail(st_ctx* c, cudaError_t e, const char* what) {
 
 static void free_wave(st_ctx* ctx) {
     void* ptrs[] = {ctx->pb.pos, ctx->pb.dir, ctx->pb.beta, ctx->pb.rad, ctx->pb.meta, ctx->q.ray[0], ctx->q.ray[1],
-                    ctx->q.hit, ctx->q.hitd, ctx->q.s_org[0], ctx->q.s_dir[0], ctx->q.s_rad[0], ctx->q.s_steps[0],
+                    ctx->q.hit, ctx->q.hitd, ctx->q.hsurf, ctx->q.s_org[0], ctx->q.s_dir[0], ctx->q.s_rad[0], ctx->q.s_steps[0],
                     ctx->q.s_org[1], ctx->q.s_dir[1], ctx->q.s_rad[1], ctx->q.s_steps[1], ctx->d_frame,
                     ctx->d_acc, ctx->d_mom};
     for (void* p : ptrs)
@@ -249,6 +252,7 @@ static int ensure_wave(st_ctx* ctx) {
     CK(cudaMalloc(&ctx->q.ray[1], S * 4), "cudaMalloc queues");
     CK(cudaMalloc(&ctx->q.hit, S * 4), "cudaMalloc queues");
     CK(cudaMalloc(&ctx->q.hitd, S * 4), "cudaMalloc queues");
+    CK(cudaMalloc(&ctx->q.hsurf, S * sizeof(float4)), "cudaMalloc queues");
     // each shadow side holds this iteration's new rays (at most one a path) and the last one's continuations
     size_t SS = 2 * S;
     for (int k = 0; k < 2; k++) {
@@ -292,7 +296,9 @@ static WaveArgs wave_args(st_ctx* ctx, uint32_t w) {
 static cudaError_t record_wave(st_ctx* ctx, const WaveArgs& a) {
     cudaStream_t s = ctx->stream;
     const bool T = ctx->timing;
+    ctx->rec_launches = 0;
     auto timed = [&](const char* name, auto&& launch) -> cudaError_t {
+        ctx->rec_launches++;
         if (!T) return launch();
         PendingEvent pe{time_index(ctx, name), take_event(ctx), take_event(ctx)};
         cudaEventRecord(pe.a, s);
@@ -302,6 +308,7 @@ static cudaError_t record_wave(st_ctx* ctx, const WaveArgs& a) {
         return e;
     };
     cudaError_t e;
+    ctx->rec_launches++;
     if ((e = launch_iter_begin(a, 0, 1, 1, s))) return e;
     if ((e = timed("genrays", [&] { return launch_genrays(a, ctx->sms, s); }))) return e;
     int cur = 0;
@@ -309,8 +316,9 @@ static cudaError_t record_wave(st_ctx* ctx, const WaveArgs& a) {
         int nxt = cur ^ 1;
         int last = it + 1 == a.u.budget;
         int side = (int)(it & 1u);
-        if (it > 0 && (e = launch_iter_begin(a, (int)it, nxt, 0, s))) return e;
+        if (it > 0 && (++ctx->rec_launches, e = launch_iter_begin(a, (int)it, nxt, 0, s))) return e;
         if ((e = timed("march", [&] { return launch_march(a, cur, nxt, last, ctx->sms, s); }))) return e;
+        if ((e = timed("surface", [&] { return launch_surface(a, ctx->sms, s); }))) return e;
         if ((e = timed("shade", [&] { return launch_shade(a, nxt, side, last, ctx->sms, s); }))) return e;
         if ((e = timed("occlude", [&] { return launch_occlude(a, side, last, ctx->sms, s); }))) return e;
         cur = nxt;
@@ -322,6 +330,7 @@ static int run_wave(st_ctx* ctx, uint32_t w) {
     WaveArgs a = wave_args(ctx, w);
     if (ctx->timing || !ctx->graph_ok) {
         CK(record_wave(ctx, a), "launch");
+        ctx->launches += ctx->rec_launches;
     } else {
         if (!ctx->graph || ctx->graph_w != w) {
             if (ctx->graph) { cudaGraphExecDestroy(ctx->graph); ctx->graph = nullptr; }
@@ -333,14 +342,17 @@ static int run_wave(st_ctx* ctx, uint32_t w) {
                 cudaGetLastError();
                 ctx->graph_ok = false;                       // fall back to direct launches, still on the GPU
                 CK(record_wave(ctx, a), "launch");
+                ctx->launches += ctx->rec_launches;
                 ctx->samples += w;
                 return ST_OK;
             }
             CK(cudaGraphInstantiate(&ctx->graph, g, 0), "graph instantiate");
             cudaGraphDestroy(g);
             ctx->graph_w = w;
+            ctx->graph_launches = ctx->rec_launches;
         }
         CK(cudaGraphLaunch(ctx->graph, ctx->stream), "graph launch");
+        ctx->launches += ctx->graph_launches;
     }
     ctx->samples += w;
     return ST_OK;
@@ -598,6 +610,7 @@ int st_read_counters(st_ctx* ctx, st_counters_t* out) {
     out->shadow_rays = c.shadow_rays; out->shadow_steps = c.shadow_steps;
     out->nonfinite = c.nonfinite; out->flushed = c.flushed; out->shadowcut = c.shadowcut;
     out->samples = ctx->samples;
+    out->launches = ctx->launches;
     return ST_OK;
 }
 

@@ -19,6 +19,8 @@ namespace st {
 // A MARCH CHUNK: the most SDF evaluations a ray takes in one launch of the march or the occlusion pass before it is
 // handed to the next iteration (the reference's MARCH_STEPS, wavefront.js:870, is 32); the last iteration's launches
 // march to the end. It bounds the tail a persistent launch spends on its longest rays.
+#define SURF_NONE 0xffffu                 // hsurf: no medium asked (n1 is the material's own index of refraction)
+#define SURF_LEAVING 0xffffffffu          // hsurf: the surface seen from behind, the ray moved on
 #define MARCH_CHUNK 48u
 
 // meta.y: the bounces (bits 0-7), the path's segment -- its shades so far, which its random numbers are seeded by
@@ -42,6 +44,9 @@ struct Queues {
     uint32_t* ray[2];    // the march's input, ping-pong: new segments and march continuations
     uint32_t* hit;       // the shade queue: slot
     float* hitd;         // ...and the signed distance at the hit
+    float4* hsurf;       // ...and what k_surface found there: the outward normal (xyz, before facing) and, as bits in
+                         // w, the material | the medium beyond << 16 (SURF_NONE: none asked; SURF_LEAVING in both:
+                         // seen from behind)
     // shadow rays, ping-pong (side it & 1 read by the occlusion pass of iteration it, continuations to the other)
     float4* s_org[2];    // xyz where it is, w ltot
     float4* s_dir[2];    // xyz direction, w pix in the wave's frames (u32 bits)
@@ -82,6 +87,7 @@ struct WaveArgs {
 cudaError_t launch_mf_tables(float* ec, float* ecavg, float* e1, cudaStream_t s);
 cudaError_t launch_genrays(const WaveArgs& a, int sms, cudaStream_t s);
 cudaError_t launch_iter_begin(const WaveArgs& a, int it, int nxt, int first, cudaStream_t s);
+cudaError_t launch_surface(const WaveArgs& a, int sms, cudaStream_t s);
 cudaError_t launch_march(const WaveArgs& a, int cur, int nxt, int last, int sms, cudaStream_t s);
 cudaError_t launch_shade(const WaveArgs& a, int nxt, int side, int last, int sms, cudaStream_t s);
 cudaError_t launch_occlude(const WaveArgs& a, int side, int last, int sms, cudaStream_t s);

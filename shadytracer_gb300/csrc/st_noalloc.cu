@@ -36,7 +36,7 @@ namespace {
 const double PI_D = 3.14159265358979323846;
 
 struct Layout {
-    size_t pos, dir, beta, rad, meta, ray0, ray1, hit, hitd, so[2], sd[2], sr[2], ss[2], frame, acc, mom, cnt, ctr,
+    size_t pos, dir, beta, rad, meta, ray0, ray1, hit, hitd, hsurf, so[2], sd[2], sr[2], ss[2], frame, acc, mom, cnt, ctr,
         ec, ecavg, e1, prims, mats, end;
 };
 // the array carved for P paths a wave (one sample), each buffer 256-byte aligned: first what does not depend on the
@@ -51,6 +51,7 @@ Layout layout(size_t P) {
     const size_t SS = 2 * P;                                   // a shadow side: new rays and continuations
     L.pos = take(P * 16); L.dir = take(P * 16); L.beta = take(P * 16); L.rad = take(P * 16); L.meta = take(P * 16);
     L.ray0 = take(P * 4); L.ray1 = take(P * 4); L.hit = take(P * 4); L.hitd = take(P * 4);
+    L.hsurf = take(P * 16);
     for (int k = 0; k < 2; k++) {
         L.so[k] = take(SS * 16); L.sd[k] = take(SS * 16); L.sr[k] = take(SS * 16); L.ss[k] = take(SS * 4);
     }
@@ -215,6 +216,7 @@ extern "C" int st_render_noalloc(int device, const st_scene_desc* desc, const st
     a.q.ray[1] = (uint32_t*)(base + L.ray1);
     a.q.hit = (uint32_t*)(base + L.hit);
     a.q.hitd = (float*)(base + L.hitd);
+    a.q.hsurf = (float4*)(base + L.hsurf);
     for (int k = 0; k < 2; k++) {
         a.q.s_org[k] = (float4*)(base + L.so[k]);
         a.q.s_dir[k] = (float4*)(base + L.sd[k]);
@@ -241,6 +243,7 @@ extern "C" int st_render_noalloc(int device, const st_scene_desc* desc, const st
             int nxt = cur ^ 1, last = it + 1 == a.u.budget, side = (int)(it & 1u);
             if (it > 0 && launch_iter_begin(a, (int)it, nxt, 0, s) != cudaSuccess) return ST_ERR_CUDA;
             if (launch_march(a, cur, nxt, last, sms, s) != cudaSuccess ||
+                launch_surface(a, sms, s) != cudaSuccess ||
                 launch_shade(a, nxt, side, last, sms, s) != cudaSuccess ||
                 launch_occlude(a, side, last, sms, s) != cudaSuccess)
                 return ST_ERR_CUDA;

@@ -255,29 +255,70 @@ __global__ void __launch_bounds__(256, 3) k_march(WaveArgs a, int cur, int nxt, 
 // lobe draw, the MIS weights, the bounce cap and roulette); an escaped ray's environment; a point in the haze
 // (haze.js:493-596 mediumVertex); the deposit of a path that ends. One thread per shade-queue entry.
 // ------------------------------------------------------------------------------------------------------------
+// THE SURFACE: the geometric half of prog_surface (wavefront.js:1037-1147) -- what a hit asks the scene: the
+// normal by three forward differences at normalTol (tracebasics.js:164-165), whether the ray meets it from behind
+// (pathFacing, scene_api.js:127-135), the material there and, for a transmissive one, the medium beyond it
+// (mediumBeyond, two offset tolerances inside). One thread per shade-queue entry, written to hsurf for k_shade,
+// so the shading kernel carries no distance function and the distance work runs at the march's occupancy.
+__global__ void __launch_bounds__(256, 3) k_surface(WaveArgs a) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    __shared__ __align__(8) uint64_t mbar;
+    __shared__ __align__(8) uint64_t mbar2;
+    const Uni& u = a.u;
+    DPrim* sp = reinterpret_cast<DPrim*>(smem);
+    st_material* sm = reinterpret_cast<st_material*>(smem + u.n_prims * sizeof(DPrim));
+    if (!stage_table(sp, a.prims, u.n_prims * (uint32_t)sizeof(DPrim), &mbar, a.ctr)) return;
+    if (!stage_table(sm, a.mats, u.n_mats * (uint32_t)sizeof(st_material), &mbar2, a.ctr)) return;
+    const uint32_t count = a.ctr->hitCount;
+    for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < count; q += gridDim.x * blockDim.x) {
+        const uint32_t slot = a.q.hit[q];
+        const uint4 m4 = a.pb.meta[slot];
+        if ((m4.y >> 16) != RAY_ACTIVE) continue;                     // escaped, out of steps, a haze collision
+        const float dh = a.q.hitd[q];
+        const f3 pos = xyz(a.pb.pos[slot]);
+        const f3 dir = xyz(a.pb.dir[slot]);
+        float eps = march_tol(pos, u.tol);
+        float gx = scene_dist(sp, u.n_prims, mk(pos.x + eps, pos.y, pos.z)) - dh;
+        float gy = scene_dist(sp, u.n_prims, mk(pos.x, pos.y + eps, pos.z)) - dh;
+        float gz = scene_dist(sp, u.n_prims, mk(pos.x, pos.y, pos.z + eps)) - dh;
+        f3 nn = normalize(mk(gx, gy, gz));
+        f3 nrm = dh < 0.f ? -nn : nn;
+        uint32_t ids = SURF_LEAVING;
+        if (!(dot(-dir, nrm) < 0.f)) {
+            SceneHit h = scene_full(sp, u.n_prims, pos);
+            const uint32_t mi = min(h.m, u.n_mats - 1);
+            const st_material& m = sm[mi];
+            uint32_t med = SURF_NONE;
+            if (m.transmission > 0.f && m.metallic < 1.f) {
+                SceneHit mb = scene_full(sp, u.n_prims, pos + (-nrm) * (10.f * eps * 2.f));
+                med = min(mb.a, u.n_mats - 1);
+            }
+            ids = mi | (med << 16);
+        }
+        a.q.hsurf[q] = make_float4(nn.x, nn.y, nn.z, __uint_as_float(ids));
+    }
+}
+
 struct ShadowOut { bool valid; f3 org, dir, rad; float n; };
 
-__device__ __forceinline__ void shade_surface(const WaveArgs& a, const DPrim* sp, const st_material* sm,
+__device__ __forceinline__ void shade_surface(const WaveArgs& a, const st_material* sm, float4 surf,
                                               f3& pos, f3& dir, float& ltot, float& n, f3& beta, float& sunmis,
                                               f3& rad, uint32_t& bounces, uint32_t& state, float dh, Rng& rng,
                                               bool last, ShadowOut& sh) {
     const Uni& u = a.u;
     float eps = march_tol(pos, u.tol);
-    float gx = scene_dist(sp, u.n_prims, mk(pos.x + eps, pos.y, pos.z)) - dh;
-    float gy = scene_dist(sp, u.n_prims, mk(pos.x, pos.y + eps, pos.z)) - dh;
-    float gz = scene_dist(sp, u.n_prims, mk(pos.x, pos.y, pos.z + eps)) - dh;
-    f3 nn = normalize(mk(gx, gy, gz));
+    const uint32_t ids = __float_as_uint(surf.w);
+    f3 nn = xyz(surf);                                                // k_surface: the normal, the material
     bool inside = dh < 0.f;
     f3 nrm = inside ? -nn : nn;                                       // pathFacing (scene_api.js:127-135)
     float otol = 10.f * eps;                                          // offsetTol
-    if (dot(-dir, nrm) < 0.f) {                                       // leaving: moved on along its way, no bounce
+    if (ids == SURF_LEAVING) {                                        // leaving: moved on along its way, no bounce
         f3 off = dir * otol;
         pos = pos + off; ltot += length(off) * n;
         return;
     }
     bounces += 1;
-    SceneHit h = scene_full(sp, u.n_prims, pos);
-    const st_material& m = sm[min(h.m, u.n_mats - 1)];
+    const st_material& m = sm[ids & 0xffffu];
     f3 emis = mk(m.emissive[0], m.emissive[1], m.emissive[2]);
     if (max3(emis) > 0.f) {                                           // emitterHit (materials_pbr.js:1014-1075)
         rad = rad + beta * emis;
@@ -288,10 +329,7 @@ __device__ __forceinline__ void shade_surface(const WaveArgs& a, const DPrim* sp
     }
     float n0 = n;
     float n1 = fmaxf(m.ior, n0);                                      // ownMedium
-    if (m.transmission > 0.f && m.metallic < 1.f) {                   // asksMedium -> mediumBeyond
-        SceneHit mb = scene_full(sp, u.n_prims, pos + (-nrm) * (otol * 2.f));
-        n1 = sm[min(mb.a, u.n_mats - 1)].ior;
-    }
+    if ((ids >> 16) != SURF_NONE) n1 = sm[ids >> 16].ior;             // asksMedium -> mediumBeyond
     float pG = sat(m.transmission);
     float trans = m.transmission, specv = m.specular;
     bool diffFace = false;
@@ -394,12 +432,9 @@ __device__ __forceinline__ void shade_medium(const WaveArgs& a, f3& pos, f3& dir
 __global__ void __launch_bounds__(256) k_shade(WaveArgs a, int nxt, int side, int last) {
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ __align__(8) uint64_t mbar;
-    __shared__ __align__(8) uint64_t mbar2;
     const Uni& u = a.u;
-    DPrim* sp = reinterpret_cast<DPrim*>(smem);
-    st_material* sm = reinterpret_cast<st_material*>(smem + u.n_prims * sizeof(DPrim));
-    if (!stage_table(sp, a.prims, u.n_prims * (uint32_t)sizeof(DPrim), &mbar, a.ctr)) return;
-    if (!stage_table(sm, a.mats, u.n_mats * (uint32_t)sizeof(st_material), &mbar2, a.ctr)) return;
+    st_material* sm = reinterpret_cast<st_material*>(smem);
+    if (!stage_table(sm, a.mats, u.n_mats * (uint32_t)sizeof(st_material), &mbar, a.ctr)) return;
     const uint32_t count = a.ctr->hitCount;
     const uint32_t stride = gridDim.x * blockDim.x;
     const uint32_t nrounds = (count + stride - 1) / stride;
@@ -441,8 +476,8 @@ __global__ void __launch_bounds__(256) k_shade(WaveArgs a, int nxt, int side, in
                 if (state == RAY_SCATTER)
                     shade_medium(a, pos, dir, beta, sunmis, bounces, state, n, rng, last != 0, sh);
                 else
-                    shade_surface(a, sp, sm, pos, dir, ltot, n, beta, sunmis, rad, bounces, state, dh, rng,
-                                  last != 0, sh);
+                    shade_surface(a, sm, a.q.hsurf[q], pos, dir, ltot, n, beta, sunmis, rad, bounces, state, dh,
+                                  rng, last != 0, sh);
                 if (state == RAY_ACTIVE) {
                     tmax = 0.f;                                       // a new leg
                     if (last) { state = RAY_MAXITER; flushed++; }     // THE FLUSH
@@ -645,7 +680,7 @@ __global__ void __launch_bounds__(256) k_resolve(WaveArgs a) {
 // ------------------------------------------------------------------------------------------------------------
 // launch wrappers
 // ------------------------------------------------------------------------------------------------------------
-static int g_occ_march = 0, g_occ_occl = 0, g_occ_shade = 0;
+static int g_occ_march = 0, g_occ_occl = 0, g_occ_shade = 0, g_occ_surf = 0;
 
 cudaError_t launch_mf_tables(float* ec, float* ecavg, float* e1, cudaStream_t s) {
     const uint32_t N = MF_NIOR * MF_NR * MF_NMU + MF_NR * MF_NMU;
@@ -684,10 +719,17 @@ cudaError_t launch_march(const WaveArgs& a, int cur, int nxt, int last, int sms,
     }
     return cudaGetLastError();
 }
-cudaError_t launch_shade(const WaveArgs& a, int nxt, int side, int last, int sms, cudaStream_t s) {
+cudaError_t launch_surface(const WaveArgs& a, int sms, cudaStream_t s) {
     size_t smem = a.u.n_prims * sizeof(DPrim) + a.u.n_mats * sizeof(st_material);
+    if (smem > 48 * 1024) cudaFuncSetAttribute(k_surface, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (!g_occ_surf) g_occ_surf = occupancy((const void*)k_surface, smem);
+    k_surface<<<sms * g_occ_surf, 256, smem, s>>>(a);
+    return cudaGetLastError();
+}
+cudaError_t launch_shade(const WaveArgs& a, int nxt, int side, int last, int sms, cudaStream_t s) {
+    size_t smem = a.u.n_mats * sizeof(st_material);
     if (smem > 48 * 1024) cudaFuncSetAttribute(k_shade, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (!g_occ_shade) g_occ_shade = occupancy((const void*)k_shade, 48 * 1024);
+    if (!g_occ_shade) g_occ_shade = occupancy((const void*)k_shade, smem);
     k_shade<<<sms * g_occ_shade, 256, smem, s>>>(a, nxt, side, last);
     return cudaGetLastError();
 }

@@ -66,7 +66,7 @@ class StCounters(C.Structure):
     _fields_ = [("paths", C.c_uint64), ("segments", C.c_uint64), ("march_steps", C.c_uint64),
                 ("shadow_rays", C.c_uint64), ("shadow_steps", C.c_uint64),
                 ("nonfinite", C.c_uint32), ("flushed", C.c_uint32), ("shadowcut", C.c_uint32),
-                ("samples", C.c_uint32)]
+                ("samples", C.c_uint32), ("launches", C.c_uint64)]
 
 
 class StImageStats(C.Structure):
