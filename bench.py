@@ -10,9 +10,11 @@ the whole render -- 64 samples of every pixel, 132.7 M camera paths -- folded in
 value: paths / s with the scene resident on the GPU (graph replays; the timed region brackets K renders with a
        synchronize). e2e: the same through the C ABI as a host calls it -- scene, settings and camera uploaded from
        host memory, the render, and the FP64 picture and its error bar read back to host memory, every step.
-roofline: the march kernel (the dominant one), FP32 arithmetic: evaluations counted on the device x the FLOPs of
-       one evaluation counted from the scene table (shadytracer_gb300/flops.py) / its CUDA-event time on its own
-       stream, in a second pass over the same K renders with per-kernel events on.
+roofline: the march kernel (the dominant one), FP32 arithmetic: the fold's work counted on the device in a counting
+       pass (evaluations by primitive type and fold operation, bounding-sphere tests, steps; one more render of the
+       same seeds through an instrumented march), weighed by FP32 operations (shadytracer_gb300/flops.py), per
+       launch, over the plain kernel's average CUDA-event time on the library's stream (a second pass over the same
+       K renders with per-kernel events on).
 cpu_baseline: the oracle (oracle/, the CPU restatement of the reference's path) in f32 on every host core, over a
        bounded band of the same picture's paths.
 --impl reference: the reference's own implementation cannot run here (JavaScript + WGSL through WebGPU); its CPU
@@ -282,12 +284,25 @@ def run_ours(args):
     c1 = rt.counters()
     rt.enable_kernel_times(False)
     evals = c1["march_steps"] - c0["march_steps"]
-    if c1["samples"] < c0["samples"]:
-        evals = c1["march_steps"]
-    f_eval, sfu_eval = flops.march_step_flops(s)
     m_launches, m_ms = kt.get("march", (0, 0.0))
     tot_ms = sum(v[1] for v in kt.values()) or 1.0
-    achieved = (evals * f_eval) / (m_ms / 1e3) / 1e12 if m_ms > 0 else 0.0   # TFLOP/s over the march's time
+
+    # ---- a counting pass: one render with an instrumented march, its fold's work counted on the device ----
+    rt.enable_kernel_times(True, count_work=True)
+    w0 = rt.counters()
+    one_step()
+    rt.sync()
+    w1 = rt.counters()
+    rt.enable_kernel_times(False)
+    dw = {k: [b - a for a, b in zip(w0[k], w1[k])] for k in ("prim_evals", "prim_warp_evals", "op_evals")}
+    for k in ("bound_tests", "bound_warp_tests", "march_steps"):
+        dw[k] = w1[k] - w0[k]
+    f_render, sfu_render = flops.counted_flops(dw, dw["march_steps"])
+    f_table, _ = flops.march_step_flops(s)                   # the whole table, every step: the uncull'd worst case
+    per_launch_flops = f_render / max(m_launches / max(args.steps, 1), 1)
+    avg_launch_s = m_ms / max(m_launches, 1) / 1e3
+    achieved = per_launch_flops / avg_launch_s / 1e12 if avg_launch_s > 0 else 0.0   # TFLOP/s per march launch
+    simd = sum(dw["prim_evals"]) / max(32 * sum(dw["prim_warp_evals"]), 1)
     pk = peaks()
     sms = torch.cuda.get_device_properties(dev).multi_processor_count
     if pk and pk.get("sm_max_mhz"):
@@ -306,9 +321,18 @@ def run_ours(args):
             "gpu_launches": launches,
             "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                          "frac": achieved / peak if peak else None, "traffic": None,
-                         "kernel": "k_march", "flops_per_eval": f_eval, "sfu_per_eval": sfu_eval,
+                         "kernel": "k_march", "flops_per_launch": per_launch_flops,
+                         "flops_per_eval": f_render / max(dw["march_steps"], 1),
+                         "flops_per_eval_whole_table": f_table,
+                         "sfu_per_eval": sfu_render / max(dw["march_steps"], 1),
                          "evals_per_launch": evals / max(m_launches, 1),
-                         "avg_launch_ms": m_ms / max(m_launches, 1), "peak_source": peak_src},
+                         "prims_evaluated_per_eval": sum(dw["prim_evals"]) / max(dw["march_steps"], 1),
+                         "fold_simd_efficiency": simd,
+                         "avg_launch_ms": m_ms / max(m_launches, 1), "peak_source": peak_src,
+                         "work": "counted on the device in a counting pass (an instrumented march over one more "
+                                 "render of the same seeds): evaluations by primitive type and fold operation, "
+                                 "bounding-sphere tests, steps, each weighed by its FP32 operations "
+                                 "(shadytracer_gb300/flops.py)"},
             "kernel_share": {k: round(v[1] / tot_ms, 4) for k, v in kt.items()},
             "clocks": clocks,
             "stats": {"mean_luma": Lmean, "segments_per_path": c["segments"] / max(c["paths"], 1),

@@ -176,6 +176,14 @@ typedef struct st_counters_t {
     uint32_t shadowcut;           /* shadow rays out of steps                                      */
     uint32_t samples;             /* samples folded since the last invalidate                      */
     uint64_t launches;            /* kernels the wave chains ran (graph nodes counted) since st_create */
+    /* the march's fold, counted only in a counting pass (st_enable_kernel_times(ctx, 2)): primitive
+     * evaluations by type (ST_PRIM_*) and the warp instructions that issued them; bounding-sphere tests
+     * and their warp issues. Their ratios are the fold's SIMD efficiency. */
+    uint64_t prim_evals[8];
+    uint64_t prim_warp_evals[8];
+    uint64_t bound_tests;
+    uint64_t bound_warp_tests;
+    uint64_t op_evals[4];         /* the evaluations by how they fold in (ST_OP_*; ITEM: a chain's head) */
 } st_counters_t;
 
 typedef struct st_image_stats_t {
@@ -219,7 +227,8 @@ int  st_read_accum(st_ctx* ctx, double* rgb, double* V, double* S, uint32_t* cou
 int  st_image_stats(st_ctx* ctx, st_image_stats_t* out);
 int  st_read_counters(st_ctx* ctx, st_counters_t* out);
 /* Per-kernel GPU time, CUDA events on the context's stream around every launch while enabled (launches then
- * run directly rather than as a replayed graph). */
+ * run directly rather than as a replayed graph). on = 2 also counts the march's fold work into the counters
+ * (a counting pass: an instrumented march, so its times are not the plain kernel's). */
 int  st_enable_kernel_times(st_ctx* ctx, int on);
 int  st_kernel_times(st_ctx* ctx, st_kernel_time* out, int max, int* n_out);
 int  st_reset_kernel_times(st_ctx* ctx);

@@ -62,6 +62,9 @@ struct st_ctx {
     uint64_t launches = 0;                // kernels run by the wave chains since the context was made
     // per-kernel timing (core/kerneltime.js's role): CUDA events on this stream around each launch, when on
     bool timing = false;
+    bool count_work = false;              // a counting pass: the march counts its fold's work
+    bool grid_ok = false;                 // the bounded primitives' box, for the march queue's space order
+    float grid_lo[3] = {0, 0, 0}, grid_hi[3] = {1, 1, 1};
     std::vector<KTimeAcc> ktimes;
     std::vector<PendingEvent> pending;
     std::vector<cudaEvent_t> event_pool;
@@ -84,7 +87,8 @@ static int cuda_fail(st_ctx* c, cudaError_t e, const char* what) {
 
 static void free_wave(st_ctx* ctx) {
     void* ptrs[] = {ctx->pb.pos, ctx->pb.dir, ctx->pb.beta, ctx->pb.rad, ctx->pb.meta, ctx->q.ray[0], ctx->q.ray[1],
-                    ctx->q.hit, ctx->q.hitd, ctx->q.hsurf, ctx->q.s_org[0], ctx->q.s_dir[0], ctx->q.s_rad[0], ctx->q.s_steps[0],
+                    ctx->q.hit, ctx->q.hitd, ctx->q.hsurf, ctx->q.sorted, ctx->q.skey, ctx->q.srank, ctx->q.bcnt,
+                    ctx->q.boff, ctx->q.ssorted, ctx->q.sskey, ctx->q.ssrank, ctx->q.s_org[0], ctx->q.s_dir[0], ctx->q.s_rad[0], ctx->q.s_steps[0],
                     ctx->q.s_org[1], ctx->q.s_dir[1], ctx->q.s_rad[1], ctx->q.s_steps[1], ctx->d_frame,
                     ctx->d_acc, ctx->d_mom};
     for (void* p : ptrs)
@@ -188,6 +192,11 @@ static Uni make_uni(const st_ctx* ctx) {
     u.seed = p.seed; u.maxaverages = p.maxaverages;
     u.n_prims = (uint32_t)ctx->prims.size();
     u.n_mats = (uint32_t)ctx->mats.size();
+    // the march queue's space order: a grid over the bounded primitives' spheres (none bounded: no sort)
+    u.sort_on = ctx->grid_ok && ctx->q.sorted ? 1u : 0u;
+    u.glo = mk(ctx->grid_lo[0], ctx->grid_lo[1], ctx->grid_lo[2]);
+    u.ginv = mk(SORT_G / (ctx->grid_hi[0] - ctx->grid_lo[0]), SORT_G / (ctx->grid_hi[1] - ctx->grid_lo[1]),
+                SORT_G / (ctx->grid_hi[2] - ctx->grid_lo[2]));
     return u;
 }
 
@@ -253,6 +262,15 @@ static int ensure_wave(st_ctx* ctx) {
     CK(cudaMalloc(&ctx->q.hit, S * 4), "cudaMalloc queues");
     CK(cudaMalloc(&ctx->q.hitd, S * 4), "cudaMalloc queues");
     CK(cudaMalloc(&ctx->q.hsurf, S * sizeof(float4)), "cudaMalloc queues");
+    CK(cudaMalloc(&ctx->q.sorted, S * 4), "cudaMalloc queues");
+    CK(cudaMalloc(&ctx->q.skey, S * 4), "cudaMalloc queues");
+    CK(cudaMalloc(&ctx->q.srank, S * 4), "cudaMalloc queues");
+    CK(cudaMalloc(&ctx->q.ssorted, 2 * S * 4), "cudaMalloc queues");
+    CK(cudaMalloc(&ctx->q.sskey, 2 * S * 4), "cudaMalloc queues");
+    CK(cudaMalloc(&ctx->q.ssrank, 2 * S * 4), "cudaMalloc queues");
+    CK(cudaMalloc(&ctx->q.bcnt, SORT_BUCKETS * 4), "cudaMalloc queues");
+    CK(cudaMalloc(&ctx->q.boff, SORT_BUCKETS * 4), "cudaMalloc queues");
+    CK(cudaMemset(ctx->q.bcnt, 0, SORT_BUCKETS * 4), "memset queues");
     // each shadow side holds this iteration's new rays (at most one a path) and the last one's continuations
     size_t SS = 2 * S;
     for (int k = 0; k < 2; k++) {
@@ -278,6 +296,7 @@ static int ensure_wave(st_ctx* ctx) {
 static WaveArgs wave_args(st_ctx* ctx, uint32_t w) {
     WaveArgs a;
     a.u = make_uni(ctx);
+    a.u.count_work = ctx->count_work ? 1u : 0u;
     a.prims = ctx->d_prims;
     a.mats = ctx->d_mats;
     a.tab = MfTab{ctx->d_ec, ctx->d_ecavg, ctx->d_e1};
@@ -317,9 +336,17 @@ static cudaError_t record_wave(st_ctx* ctx, const WaveArgs& a) {
         int last = it + 1 == a.u.budget;
         int side = (int)(it & 1u);
         if (it > 0 && (++ctx->rec_launches, e = launch_iter_begin(a, (int)it, nxt, 0, s))) return e;
+        if (a.u.sort_on) {
+            if ((e = timed("sort", [&] { return launch_sort(a, cur, ctx->sms, s); }))) return e;
+            ctx->rec_launches += 2;                                  // key, scan, scatter
+        }
         if ((e = timed("march", [&] { return launch_march(a, cur, nxt, last, ctx->sms, s); }))) return e;
         if ((e = timed("surface", [&] { return launch_surface(a, ctx->sms, s); }))) return e;
         if ((e = timed("shade", [&] { return launch_shade(a, nxt, side, last, ctx->sms, s); }))) return e;
+        if (a.u.sort_on) {
+            if ((e = timed("sort", [&] { return launch_sort_shadow(a, side, ctx->sms, s); }))) return e;
+            ctx->rec_launches += 2;
+        }
         if ((e = timed("occlude", [&] { return launch_occlude(a, side, last, ctx->sms, s); }))) return e;
         cur = nxt;
     }
@@ -442,6 +469,22 @@ int st_set_scene(st_ctx* ctx, const char* cuda_src, const st_scene_desc* d, char
     if (!ctx->d_mats) CK(cudaMalloc(&ctx->d_mats, ST_MAX_MATERIALS * sizeof(st_material)), "cudaMalloc materials");
     std::vector<DPrim> packed(prims.size());
     for (size_t i = 0; i < prims.size(); i++) packed[i] = pack_prim(prims[i]);
+    {
+        double lo[3] = {1e30, 1e30, 1e30}, hi[3] = {-1e30, -1e30, -1e30};
+        bool any = false;
+        for (const DPrim& q : packed) {
+            if (!(q.a.w < 1e30f)) continue;                   // unbounded (a plane) or a bound-only distance
+            const double c[3] = {q.a.x, q.a.y, q.a.z};
+            for (int k = 0; k < 3; k++) { lo[k] = std::min(lo[k], c[k] - q.a.w); hi[k] = std::max(hi[k], c[k] + q.a.w); }
+            any = true;
+        }
+        ctx->grid_ok = any;
+        for (int k = 0; k < 3; k++) {
+            double pad = 1e-3 * (hi[k] - lo[k]) + 1e-6;
+            ctx->grid_lo[k] = any ? (float)(lo[k] - pad) : 0.f;
+            ctx->grid_hi[k] = any ? (float)(hi[k] + pad) : 1.f;
+        }
+    }
     CK(cudaMemcpyAsync(ctx->d_prims, packed.data(), packed.size() * sizeof(DPrim), cudaMemcpyHostToDevice, ctx->stream), "scene upload");
     CK(cudaMemcpyAsync(ctx->d_mats, mats.data(), mats.size() * sizeof(st_material), cudaMemcpyHostToDevice, ctx->stream), "scene upload");
     CK(cudaStreamSynchronize(ctx->stream), "scene upload");
@@ -611,12 +654,17 @@ int st_read_counters(st_ctx* ctx, st_counters_t* out) {
     out->nonfinite = c.nonfinite; out->flushed = c.flushed; out->shadowcut = c.shadowcut;
     out->samples = ctx->samples;
     out->launches = ctx->launches;
+    for (int k = 0; k < 8; k++) { out->prim_evals[k] = c.work[WC_EVAL + k]; out->prim_warp_evals[k] = c.work[WC_WEVAL + k]; }
+    out->bound_tests = c.work[WC_TEST];
+    out->bound_warp_tests = c.work[WC_WTEST];
+    for (int k = 0; k < 4; k++) out->op_evals[k] = c.work[WC_OP + k];
     return ST_OK;
 }
 
 int st_enable_kernel_times(st_ctx* ctx, int on) {
     if (!ctx) return ST_ERR_ARG;
     ctx->timing = on != 0;
+    ctx->count_work = (on & 2) != 0;
     return ST_OK;
 }
 

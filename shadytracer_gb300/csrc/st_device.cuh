@@ -107,6 +107,9 @@ struct Uni {
     int haze_on; f3 hc, hu, hv, hw, halb; float hhu, hhv, hhw, hsig, hg;
     // the sample sequence
     uint32_t seed, maxaverages, n_prims, n_mats;
+    uint32_t count_work;         // a counting pass: the march counts its fold's work (WC_*)
+    // the march queue's space order (st_render.cu k_sort_*): a SORT_G^3 grid over the primitives' bounds
+    uint32_t sort_on; f3 glo, ginv;
 };
 
 // ------------------------------------------------------------------------------------------------------------
@@ -237,27 +240,69 @@ __device__ __forceinline__ bool beyond(const DPrim& pr, f3 p, float t) {
 #define CULL_REL 1.001f
 #define CULL_ABS 1e-6f
 
+// WORK COUNTS, for a counting pass only (the COUNT instantiations): shared-memory counters a block flushes at its
+// end -- per primitive type the evaluations made (threads) and the warp issues that made them, and the same for the
+// bounding-sphere tests. Their ratio is the SIMD efficiency of the fold; their sum, weighted by each type's
+// operations, the algorithmic work a launch did.
+#define WC_EVAL 0u      // [0, 8): evaluations by primitive type
+#define WC_WEVAL 8u     // [8, 16): warp issues of those evaluations
+#define WC_TEST 16u     // bounding-sphere tests
+#define WC_WTEST 17u    // ...their warp issues
+#define WC_OP 18u       // [18, 22): evaluations by how they fold in (ST_OP_ITEM: a chain's head, SMOOTH, UNION, SUB)
+#define WC_N 22u
+// one more of counter k (threads) and of its warp-issue counter wk, from the warp's lowest active lane
+template <bool COUNT>
+__device__ __forceinline__ void wc_add(uint32_t* c, uint32_t k, uint32_t wk) {
+    if (COUNT) {
+        const uint32_t m = __activemask();
+        if ((threadIdx.x & 31u) == (uint32_t)(__ffs(m) - 1)) {
+            atomicAdd(&c[k], (uint32_t)__popc(m));
+            atomicAdd(&c[wk], 1u);
+        }
+    }
+}
+template <bool COUNT>
+__device__ __forceinline__ void wc_eval(uint32_t* c, const DPrim& pr, uint32_t op) {
+    if (COUNT) {
+        wc_add<COUNT>(c, WC_EVAL + (pr.h.x & 7u), WC_WEVAL + (pr.h.x & 7u));
+        const uint32_t m = __activemask();
+        if ((threadIdx.x & 31u) == (uint32_t)(__ffs(m) - 1)) atomicAdd(&c[WC_OP + (op & 3u)], (uint32_t)__popc(m));
+    }
+}
+
 struct SceneHit { float d; uint32_t m, a; };
 // distance only (scene_api.js FOLD_DIST): the march's and the shadow rays' question. Within an item's CSG chain a
 // primitive is evaluated only where it could change the running value: a smooth union of radius k leaves acc alone
 // where d_j >= acc + k (sdf.js opSmoothUnion's h is then 1), a union where d_j >= acc, a subtraction where
 // d_j >= -acc -- the same number, bit for bit, as evaluating it.
-__device__ __forceinline__ float scene_dist(const DPrim* __restrict__ pr, uint32_t n, f3 p) {
+template <bool COUNT = false>
+__device__ __forceinline__ float scene_dist(const DPrim* __restrict__ pr, uint32_t n, f3 p, uint32_t* wc = nullptr) {
     float best = 1e7f;
     uint32_t i = 0;
     while (i < n) {
+        wc_eval<COUNT>(wc, pr[i], ST_OP_ITEM);
         float di = prim_sdf(pr[i], p);
         uint32_t j = i + 1;
         while (j < n) {
             const uint32_t op = pr[j].h.y;
             if (op == ST_OP_ITEM) break;
+            wc_add<COUNT>(wc, WC_TEST, WC_WTEST);
             if (op == ST_OP_SMOOTH) {
                 float k = pr[j].r0.w;
-                if (!beyond(pr[j], p, di + k * CULL_REL + CULL_ABS)) di = smooth_union(di, prim_sdf(pr[j], p), k);
+                if (!beyond(pr[j], p, di + k * CULL_REL + CULL_ABS)) {
+                    wc_eval<COUNT>(wc, pr[j], op);
+                    di = smooth_union(di, prim_sdf(pr[j], p), k);
+                }
             } else if (op == ST_OP_UNION) {
-                if (!beyond(pr[j], p, di + CULL_ABS)) di = fminf(di, prim_sdf(pr[j], p));
+                if (!beyond(pr[j], p, di + CULL_ABS)) {
+                    wc_eval<COUNT>(wc, pr[j], op);
+                    di = fminf(di, prim_sdf(pr[j], p));
+                }
             } else {
-                if (!beyond(pr[j], p, -di + CULL_ABS)) di = fmaxf(di, -prim_sdf(pr[j], p));
+                if (!beyond(pr[j], p, -di + CULL_ABS)) {
+                    wc_eval<COUNT>(wc, pr[j], op);
+                    di = fmaxf(di, -prim_sdf(pr[j], p));
+                }
             }
             j++;
         }

@@ -21,6 +21,8 @@ namespace st {
 // march to the end. It bounds the tail a persistent launch spends on its longest rays.
 #define SURF_NONE 0xffffu                 // hsurf: no medium asked (n1 is the material's own index of refraction)
 #define SURF_LEAVING 0xffffffffu          // hsurf: the surface seen from behind, the ray moved on
+#define SORT_G 16u                        // the march queue's space order: SORT_G^3 cells ...
+#define SORT_BUCKETS (SORT_G * SORT_G * SORT_G * 8u)   // ... x 8 direction octants
 #define MARCH_CHUNK 48u
 
 // meta.y: the bounces (bits 0-7), the path's segment -- its shades so far, which its random numbers are seeded by
@@ -44,6 +46,14 @@ struct Queues {
     uint32_t* ray[2];    // the march's input, ping-pong: new segments and march continuations
     uint32_t* hit;       // the shade queue: slot
     float* hitd;         // ...and the signed distance at the hit
+    uint32_t* sorted;    // the march queue of this iteration in space order (cell, octant), when sort_on
+    uint32_t* skey;      // ...each entry's bucket and its rank in it
+    uint32_t* srank;
+    uint32_t* ssorted;   // the shadow queue of this iteration in space order: positions into its side's arrays
+    uint32_t* sskey;     // ...each entry's bucket and its rank in it
+    uint32_t* ssrank;
+    uint32_t* bcnt;      // SORT_BUCKETS counts (zero between sorts) and their exclusive offsets
+    uint32_t* boff;
     float4* hsurf;       // ...and what k_surface found there: the outward normal (xyz, before facing) and, as bits in
                          // w, the material | the medium beyond << 16 (SURF_NONE: none asked; SURF_LEAVING in both:
                          // seen from behind)
@@ -62,6 +72,7 @@ struct DevCtr {
     uint32_t nonfinite, flushed, shadowcut, sample;   // sample: the first sample of the wave in flight
     uint32_t shadowdrop, pad1, pad2, pad3;
     unsigned long long paths, segments, march_steps, shadow_rays, shadow_steps;
+    unsigned long long work[WC_N];     // the march's fold, counted in a counting pass (WC_* in st_device.cuh)
 };
 
 struct __align__(32) Acc4 { double x, y, z, w; };   // FP64 mean rgb + the sample count
@@ -88,6 +99,8 @@ cudaError_t launch_mf_tables(float* ec, float* ecavg, float* e1, cudaStream_t s)
 cudaError_t launch_genrays(const WaveArgs& a, int sms, cudaStream_t s);
 cudaError_t launch_iter_begin(const WaveArgs& a, int it, int nxt, int first, cudaStream_t s);
 cudaError_t launch_surface(const WaveArgs& a, int sms, cudaStream_t s);
+cudaError_t launch_sort(const WaveArgs& a, int cur, int sms, cudaStream_t s);
+cudaError_t launch_sort_shadow(const WaveArgs& a, int side, int sms, cudaStream_t s);
 cudaError_t launch_march(const WaveArgs& a, int cur, int nxt, int last, int sms, cudaStream_t s);
 cudaError_t launch_shade(const WaveArgs& a, int nxt, int side, int last, int sms, cudaStream_t s);
 cudaError_t launch_occlude(const WaveArgs& a, int side, int last, int sms, cudaStream_t s);

@@ -205,7 +205,7 @@ extern "C" int st_render_noalloc(int device, const st_scene_desc* desc, const st
         cudaMemsetAsync(base + L.ctr, 0, sizeof(DevCtr), s) != cudaSuccess)
         return ST_ERR_CUDA;
 
-    WaveArgs a;
+    WaveArgs a{};
     a.u = uniforms(*desc, *p, *v, desc->n_prims, desc->n_materials);
     a.prims = reinterpret_cast<const DPrim*>(base + L.prims);
     a.mats = reinterpret_cast<const st_material*>(base + L.mats);

@@ -125,15 +125,99 @@ __global__ void k_iter_begin(DevCtr* ctr, int it, int nxt, uint32_t slots, int f
 // in the next iteration (the reference's 32-step dispatches, wavefront.js:870); the last iteration's launch
 // marches every ray to its end.
 // ------------------------------------------------------------------------------------------------------------
-template <bool HAZE, bool INST>
+// ------------------------------------------------------------------------------------------------------------
+// THE MARCH QUEUE IN SPACE ORDER. The fold skips a primitive by its bounding sphere per lane, but a warp issues a
+// primitive's evaluation whenever any of its 32 rays needs it, so rays far apart in one warp pay for the union of
+// their neighbourhoods. Before each march the queue is put in the order of a counting sort on (cell of a
+// SORT_G^3 grid over the primitives' bounds, direction octant): one atomic per ray for its rank in its bucket, a
+// one-block scan of the buckets, a scatter. Each ray's answer is its own (its random numbers come from its path),
+// so the order changes only which rays share a warp.
+// ------------------------------------------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t sort_bucket(f3 glo, f3 ginv, f3 p, f3 d) {
+    const float fx = (p.x - glo.x) * ginv.x, fy = (p.y - glo.y) * ginv.y, fz = (p.z - glo.z) * ginv.z;
+    const uint32_t ix = (uint32_t)fminf(fmaxf(fx, 0.f), (float)(SORT_G - 1));
+    const uint32_t iy = (uint32_t)fminf(fmaxf(fy, 0.f), (float)(SORT_G - 1));
+    const uint32_t iz = (uint32_t)fminf(fmaxf(fz, 0.f), (float)(SORT_G - 1));
+    const uint32_t oct = (d.x < 0.f ? 1u : 0u) | (d.y < 0.f ? 2u : 0u) | (d.z < 0.f ? 4u : 0u);
+    return ((iz * SORT_G + iy) * SORT_G + ix) * 8u + oct;
+}
+// each entry's bucket and rank: entry i is the ray at pos / dir [inq ? inq[i] : i]
+__global__ void __launch_bounds__(256) k_sort_key(const uint32_t* __restrict__ countp, uint32_t cap,
+                                                  const uint32_t* __restrict__ inq, const float4* __restrict__ pos,
+                                                  const float4* __restrict__ dir, f3 glo, f3 ginv,
+                                                  uint32_t* __restrict__ key, uint32_t* __restrict__ rank,
+                                                  uint32_t* __restrict__ bcnt) {
+    const uint32_t count = min(*countp, cap);
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
+        const uint32_t at = inq ? inq[i] : i;
+        const uint32_t b = sort_bucket(glo, ginv, xyz(pos[at]), xyz(dir[at]));
+        key[i] = b;
+        rank[i] = atomicAdd(&bcnt[b], 1u);
+    }
+}
+__global__ void __launch_bounds__(1024) k_sort_scan(uint32_t* __restrict__ cnt, uint32_t* __restrict__ off) {
+    constexpr uint32_t PER = SORT_BUCKETS / 1024u;
+    __shared__ uint32_t wsum[32];
+    uint32_t v[PER];
+    uint4* c4 = reinterpret_cast<uint4*>(cnt + threadIdx.x * PER);
+    uint32_t t = 0;
+#pragma unroll
+    for (uint32_t k = 0; k < PER / 4; k++) {
+        uint4 q = c4[k];
+        v[4 * k] = q.x; v[4 * k + 1] = q.y; v[4 * k + 2] = q.z; v[4 * k + 3] = q.w;
+        t += q.x + q.y + q.z + q.w;
+        c4[k] = make_uint4(0u, 0u, 0u, 0u);
+    }
+    const uint32_t lane = threadIdx.x & 31u, w = threadIdx.x >> 5;
+    uint32_t incl = t;
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t y = __shfl_up_sync(FULL_MASK, incl, o);
+        if (lane >= (uint32_t)o) incl += y;
+    }
+    if (lane == 31u) wsum[w] = incl;
+    __syncthreads();
+    if (w == 0) {
+        uint32_t x = wsum[lane], xi = x;
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t y = __shfl_up_sync(FULL_MASK, xi, o);
+            if (lane >= (uint32_t)o) xi += y;
+        }
+        wsum[lane] = xi - x;
+    }
+    __syncthreads();
+    uint32_t run = wsum[w] + incl - t;
+    uint4* o4 = reinterpret_cast<uint4*>(off + threadIdx.x * PER);
+#pragma unroll
+    for (uint32_t k = 0; k < PER / 4; k++) {
+        uint4 q;
+        q.x = run; run += v[4 * k];
+        q.y = run; run += v[4 * k + 1];
+        q.z = run; run += v[4 * k + 2];
+        q.w = run; run += v[4 * k + 3];
+        o4[k] = q;
+    }
+}
+__global__ void __launch_bounds__(256) k_sort_scatter(const uint32_t* __restrict__ countp, uint32_t cap,
+                                                      const uint32_t* __restrict__ inq,
+                                                      const uint32_t* __restrict__ key, const uint32_t* __restrict__ rank,
+                                                      const uint32_t* __restrict__ boff, uint32_t* __restrict__ out) {
+    const uint32_t count = min(*countp, cap);
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x)
+        out[boff[key[i]] + rank[i]] = inq ? inq[i] : i;
+}
+
+template <bool HAZE, bool INST, bool COUNT>
 __global__ void __launch_bounds__(256, 3) k_march(WaveArgs a, int cur, int nxt, int last) {
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ __align__(8) uint64_t mbar;
+    __shared__ uint32_t wc[COUNT ? WC_N : 1];
     DPrim* sp = reinterpret_cast<DPrim*>(smem);
     const uint32_t n_prims = a.u.n_prims;
+    if (COUNT)
+        for (uint32_t k = threadIdx.x; k < WC_N; k += blockDim.x) wc[k] = 0u;
     if (!stage_table(sp, a.prims, n_prims * (uint32_t)sizeof(DPrim), &mbar, a.ctr)) return;
     const uint32_t count = a.ctr->rayCount[cur];
-    const uint32_t* __restrict__ inq = cur ? a.q.ray[1] : a.q.ray[0];
+    const uint32_t* __restrict__ inq = a.u.sort_on ? a.q.sorted : (cur ? a.q.ray[1] : a.q.ray[0]);
     uint32_t* __restrict__ outq = nxt ? a.q.ray[1] : a.q.ray[0];
     uint32_t* outc = nxt ? &a.ctr->rayCount[1] : &a.ctr->rayCount[0];
     const float tol = a.u.tol, stepscale = a.u.stepscale, envR2 = a.u.envR2;
@@ -206,7 +290,7 @@ __global__ void __launch_bounds__(256, 3) k_march(WaveArgs a, int cur, int nxt, 
                 state = RAY_SCATTER;
                 fin = true;
             } else {
-                float d = scene_dist(sp + pfirst, pcount, pos);
+                float d = scene_dist<COUNT>(sp + pfirst, pcount, pos, wc);
                 evals++;
                 evals_here++;
                 float ea = fabsf(d);
@@ -247,6 +331,11 @@ __global__ void __launch_bounds__(256, 3) k_march(WaveArgs a, int cur, int nxt, 
     // the steps taken, one atomic per warp
     for (int o = 16; o > 0; o >>= 1) evals += __shfl_down_sync(FULL_MASK, evals, o);
     if (lane == 0 && evals) atomicAdd(&a.ctr->march_steps, evals);
+    if (COUNT) {
+        __syncthreads();
+        for (uint32_t k = threadIdx.x; k < WC_N; k += blockDim.x)
+            if (wc[k]) atomicAdd(&a.ctr->work[k], (unsigned long long)wc[k]);
+    }
 }
 
 // ------------------------------------------------------------------------------------------------------------
@@ -577,7 +666,7 @@ __global__ void __launch_bounds__(256, 3) k_occlude(WaveArgs a, int side, int la
                 uint32_t avail = wend - wpos;
                 uint32_t rank = __popc(idle & lanemask_lt());
                 if (idx == INVALID_SLOT && rank < avail) {
-                    idx = wpos + rank;
+                    idx = a.u.sort_on ? a.q.ssorted[wpos + rank] : wpos + rank;
                     float4 o4 = i_org[idx], d4 = i_dir[idx];
                     pos = xyz(o4); ltot = o4.w; dir = xyz(d4); n = i_rad[idx].w;
                     steps = i_steps[idx];
@@ -702,21 +791,40 @@ static int occupancy(const void* fn, size_t smem) {
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, 256, smem);
     return nb > 0 ? nb : 1;
 }
-cudaError_t launch_march(const WaveArgs& a, int cur, int nxt, int last, int sms, cudaStream_t s) {
+template <bool HAZE, bool INST, bool COUNT>
+static void march_variant(const WaveArgs& a, int cur, int nxt, int last, int sms, cudaStream_t s, int* occ_cache) {
     size_t smem = a.u.n_prims * sizeof(DPrim);
-    if (a.inst_range) {
-        if (smem > 48 * 1024) cudaFuncSetAttribute(k_march<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        int nb = occupancy((const void*)k_march<false, true>, 32 * 1024);
-        k_march<false, true><<<sms * nb, 256, smem, s>>>(a, cur, nxt, last);
-    } else if (a.u.haze_on) {
-        if (smem > 48 * 1024) cudaFuncSetAttribute(k_march<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        int nb = occupancy((const void*)k_march<true, false>, smem);
-        k_march<true, false><<<sms * nb, 256, smem, s>>>(a, cur, nxt, last);
-    } else {
-        if (smem > 48 * 1024) cudaFuncSetAttribute(k_march<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (!g_occ_march) g_occ_march = occupancy((const void*)k_march<false, false>, 32 * 1024);
-        k_march<false, false><<<sms * g_occ_march, 256, smem, s>>>(a, cur, nxt, last);
-    }
+    auto fn = k_march<HAZE, INST, COUNT>;
+    if (smem > 48 * 1024) cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    int nb = occ_cache && *occ_cache ? *occ_cache : occupancy((const void*)fn, smem);
+    if (occ_cache) *occ_cache = nb;
+    fn<<<sms * nb, 256, smem, s>>>(a, cur, nxt, last);
+}
+cudaError_t launch_march(const WaveArgs& a, int cur, int nxt, int last, int sms, cudaStream_t s) {
+    if (a.inst_range) march_variant<false, true, false>(a, cur, nxt, last, sms, s, nullptr);
+    else if (a.u.count_work && a.u.haze_on) march_variant<true, false, true>(a, cur, nxt, last, sms, s, nullptr);
+    else if (a.u.count_work) march_variant<false, false, true>(a, cur, nxt, last, sms, s, nullptr);
+    else if (a.u.haze_on) march_variant<true, false, false>(a, cur, nxt, last, sms, s, nullptr);
+    else march_variant<false, false, false>(a, cur, nxt, last, sms, s, &g_occ_march);
+    return cudaGetLastError();
+}
+cudaError_t launch_sort(const WaveArgs& a, int cur, int sms, cudaStream_t s) {
+    if (!a.u.sort_on) return cudaSuccess;
+    const uint32_t* cnt = &a.ctr->rayCount[cur];
+    const uint32_t* inq = cur ? a.q.ray[1] : a.q.ray[0];
+    k_sort_key<<<sms * 8, 256, 0, s>>>(cnt, a.q.cap, inq, a.pb.pos, a.pb.dir, a.u.glo, a.u.ginv, a.q.skey, a.q.srank,
+                                       a.q.bcnt);
+    k_sort_scan<<<1, 1024, 0, s>>>(a.q.bcnt, a.q.boff);
+    k_sort_scatter<<<sms * 8, 256, 0, s>>>(cnt, a.q.cap, inq, a.q.skey, a.q.srank, a.q.boff, a.q.sorted);
+    return cudaGetLastError();
+}
+cudaError_t launch_sort_shadow(const WaveArgs& a, int side, int sms, cudaStream_t s) {
+    if (!a.u.sort_on) return cudaSuccess;
+    const uint32_t* cnt = &a.ctr->shadowCount[side];
+    k_sort_key<<<sms * 8, 256, 0, s>>>(cnt, a.q.scap, nullptr, a.q.s_org[side], a.q.s_dir[side], a.u.glo, a.u.ginv,
+                                       a.q.sskey, a.q.ssrank, a.q.bcnt);
+    k_sort_scan<<<1, 1024, 0, s>>>(a.q.bcnt, a.q.boff);
+    k_sort_scatter<<<sms * 8, 256, 0, s>>>(cnt, a.q.scap, nullptr, a.q.sskey, a.q.ssrank, a.q.boff, a.q.ssorted);
     return cudaGetLastError();
 }
 cudaError_t launch_surface(const WaveArgs& a, int sms, cudaStream_t s) {

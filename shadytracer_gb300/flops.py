@@ -6,6 +6,10 @@ way the kernels (csrc/st_device.cuh prim_sdf / scene_dist, csrc/st_render.cu k_m
 multiply, a min/max/abs, a compare are 1; a fused multiply-add is 2; sqrt, reciprocal, divide and the
 transcendentals run on the special-function unit and are counted apart (`sfu`). The achieved FLOP/s a roofline
 reports is (evaluations counted on the device) x (this count) / (the kernel's time).
+
+The fold skips primitives by their bounding spheres, so a step evaluates fewer than the whole table: `counted_flops`
+weighs the work a counting pass of the march counted on the device (evaluations by primitive type and by fold
+operation, bounding-sphere tests, steps) -- the work the kernel did, not the table's worst case.
 """
 from .st_types import (ST_PRIM_PLANE, ST_PRIM_SPHERE, ST_PRIM_BOX, ST_PRIM_ROUNDBOX, ST_PRIM_TORUS, ST_PRIM_PRISM,
                        ST_PRIM_ASPHERE, ST_PRIM_CYLINDER, ST_OP_ITEM, ST_OP_SMOOTH, ST_OP_UNION, ST_OP_SUB)
@@ -47,3 +51,24 @@ def march_step_flops(scene):
     """(flops, sfu) of one march step: the SDF and the step."""
     f, s = sdf_flops(scene)
     return f + STEP[0], s + STEP[1]
+
+
+BOUND_TEST = (10, 0)        # |p - c|^2 against (t + R)^2: 3 subtracts, a multiply and 2 FMAs, an add, a multiply, 2 compares
+
+
+def counted_flops(c, n_steps):
+    """(flops, sfu) of the march's fold as a counting pass counted it: `c` the counters' differences (prim_evals by
+    type, op_evals by fold operation, bound_tests), `n_steps` the evaluations (march steps)."""
+    f = s = 0
+    for t, n in enumerate(c["prim_evals"]):
+        a, b = PRIM.get(t, (0, 0))
+        f += n * (TRANSFORM[0] + a)
+        s += n * (TRANSFORM[1] + b)
+    for op, n in enumerate(c["op_evals"]):
+        o = OP.get(op, (0, 0))
+        f += n * (o[0] + (FOLD[0] if op == ST_OP_ITEM else 0))
+        s += n * o[1]
+    f += c["bound_tests"] * BOUND_TEST[0]
+    f += n_steps * STEP[0]
+    s += n_steps * STEP[1]
+    return f, s

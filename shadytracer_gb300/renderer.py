@@ -118,7 +118,11 @@ class PathTracer:
     def counters(self):
         c = T.StCounters()
         check(self.L.st_read_counters(self.ctx, C.byref(c)), self.ctx, "st_read_counters")
-        return {f: getattr(c, f) for f, _ in T.StCounters._fields_}
+        out = {}
+        for f, _ in T.StCounters._fields_:
+            v = getattr(c, f)
+            out[f] = list(v) if hasattr(v, "__len__") else v
+        return out
 
     def measure(self, x, y):
         """The reading at pixel (x, y), row 0 the bottom (core/measure.js:56-66 reading): L, se, nEff, count."""
@@ -141,8 +145,9 @@ class PathTracer:
         return ec, ecavg, e1
 
     # ---- kernel times (core/kerneltime.js) ----
-    def enable_kernel_times(self, on=True):
-        check(self.L.st_enable_kernel_times(self.ctx, 1 if on else 0), self.ctx, "st_enable_kernel_times")
+    def enable_kernel_times(self, on=True, count_work=False):
+        mode = (2 if count_work else 1) if on else 0
+        check(self.L.st_enable_kernel_times(self.ctx, mode), self.ctx, "st_enable_kernel_times")
 
     def kernel_times(self):
         buf = (T.StKernelTime * 32)()

@@ -66,7 +66,9 @@ class StCounters(C.Structure):
     _fields_ = [("paths", C.c_uint64), ("segments", C.c_uint64), ("march_steps", C.c_uint64),
                 ("shadow_rays", C.c_uint64), ("shadow_steps", C.c_uint64),
                 ("nonfinite", C.c_uint32), ("flushed", C.c_uint32), ("shadowcut", C.c_uint32),
-                ("samples", C.c_uint32), ("launches", C.c_uint64)]
+                ("samples", C.c_uint32), ("launches", C.c_uint64), ("prim_evals", C.c_uint64 * 8),
+                ("prim_warp_evals", C.c_uint64 * 8), ("bound_tests", C.c_uint64), ("bound_warp_tests", C.c_uint64),
+                ("op_evals", C.c_uint64 * 4)]
 
 
 class StImageStats(C.Structure):
