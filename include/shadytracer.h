@@ -226,6 +226,9 @@ int  st_sync(st_ctx* ctx, int timeout_ms);    /* wait for the queued samples; <0
 int  st_read_accum(st_ctx* ctx, double* rgb, double* V, double* S, uint32_t* count);
 int  st_image_stats(st_ctx* ctx, st_image_stats_t* out);
 int  st_read_counters(st_ctx* ctx, st_counters_t* out);
+/* The scene's signed distance at n points (3n floats, metres) into out (n floats), as the march folds the table
+ * (scene_api.js FOLD_DIST, each primitive behind its bounding-sphere test). */
+int  st_eval_sdf(st_ctx* ctx, const float* pts, uint32_t n, float* out);
 /* Per-kernel GPU time, CUDA events on the context's stream around every launch while enabled (launches then
  * run directly rather than as a replayed graph). on = 2 also counts the march's fold work into the counters
  * (a counting pass: an instrumented march, so its times are not the plain kernel's). */

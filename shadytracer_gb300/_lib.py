@@ -42,6 +42,7 @@ SIGNATURES = {
     "st_optics_run": ([P, C.POINTER(T.StOpticsBatch), P, P, C.POINTER(T.StOpticsTotals)], C.c_int),
     "st_render_noalloc": ([C.c_int, C.POINTER(T.StSceneDesc), C.POINTER(T.StParams), C.POINTER(T.StView), C.c_int,
                            P, P, P, P], C.c_int),
+    "st_eval_sdf": ([P, P, C.c_uint32, P], C.c_int),
     "st_struct_sizes": ([P, C.c_int], C.c_int),
     "st_stream": ([P], C.c_void_p),
 }

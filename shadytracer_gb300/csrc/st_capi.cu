@@ -661,6 +661,23 @@ int st_read_counters(st_ctx* ctx, st_counters_t* out) {
     return ST_OK;
 }
 
+int st_eval_sdf(st_ctx* ctx, const float* pts, uint32_t n, float* out) {
+    if (!ctx || (n && (!pts || !out))) return ST_ERR_ARG;
+    if (!ctx->has_scene) return fail(ctx, ST_ERR_STATE, "set a scene first");
+    if (ctx->in_flight) { int rc = st_sync(ctx, -1); if (rc) return rc; }
+    if (n == 0) return ST_OK;
+    cudaSetDevice(ctx->device);
+    float* dp = nullptr;
+    CK(cudaMalloc(&dp, (size_t)n * 16), "cudaMalloc points");
+    cudaError_t e = cudaMemcpyAsync(dp, pts, (size_t)n * 12, cudaMemcpyHostToDevice, ctx->stream);
+    if (!e) e = launch_eval_sdf(ctx->d_prims, (uint32_t)ctx->prims.size(), dp, n, dp + 3 * (size_t)n, ctx->stream);
+    if (!e) e = cudaMemcpyAsync(out, dp + 3 * (size_t)n, (size_t)n * 4, cudaMemcpyDeviceToHost, ctx->stream);
+    if (!e) e = cudaStreamSynchronize(ctx->stream);
+    cudaFree(dp);
+    CK(e, "scene distance");
+    return ST_OK;
+}
+
 int st_enable_kernel_times(st_ctx* ctx, int on) {
     if (!ctx) return ST_ERR_ARG;
     ctx->timing = on != 0;

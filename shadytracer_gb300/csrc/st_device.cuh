@@ -289,7 +289,7 @@ __device__ __forceinline__ float scene_dist(const DPrim* __restrict__ pr, uint32
             wc_add<COUNT>(wc, WC_TEST, WC_WTEST);
             if (op == ST_OP_SMOOTH) {
                 float k = pr[j].r0.w;
-                if (!beyond(pr[j], p, di + k * CULL_REL + CULL_ABS)) {
+                if (!beyond(pr[j], p, di + fmaxf(k, 0.f) * CULL_REL + CULL_ABS)) {
                     wc_eval<COUNT>(wc, pr[j], op);
                     di = smooth_union(di, prim_sdf(pr[j], p), k);
                 }
@@ -328,7 +328,7 @@ __device__ __forceinline__ SceneHit scene_full(const DPrim* __restrict__ pr, uin
             if (op == ST_OP_ITEM) break;
             if (op == ST_OP_SMOOTH) {
                 float k = pr[j].r0.w;
-                if (!beyond(pr[j], p, fmaxf(di + k * CULL_REL, nearv) + CULL_ABS)) {
+                if (!beyond(pr[j], p, fmaxf(di + fmaxf(k, 0.f) * CULL_REL, nearv) + CULL_ABS)) {
                     float dj = prim_sdf(pr[j], p);
                     di = smooth_union(di, dj, k);
                     if (fabsf(dj) < nearv) { nearv = fabsf(dj); mat = pr[j].h.z; }

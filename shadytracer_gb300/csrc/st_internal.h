@@ -100,6 +100,8 @@ cudaError_t launch_genrays(const WaveArgs& a, int sms, cudaStream_t s);
 cudaError_t launch_iter_begin(const WaveArgs& a, int it, int nxt, int first, cudaStream_t s);
 cudaError_t launch_surface(const WaveArgs& a, int sms, cudaStream_t s);
 cudaError_t launch_sort(const WaveArgs& a, int cur, int sms, cudaStream_t s);
+cudaError_t launch_eval_sdf(const DPrim* prims, uint32_t n_prims, const float* pts, uint32_t n, float* out,
+                            cudaStream_t s);
 cudaError_t launch_sort_shadow(const WaveArgs& a, int side, int sms, cudaStream_t s);
 cudaError_t launch_march(const WaveArgs& a, int cur, int nxt, int last, int sms, cudaStream_t s);
 cudaError_t launch_shade(const WaveArgs& a, int nxt, int side, int last, int sms, cudaStream_t s);

@@ -207,7 +207,7 @@ __global__ void __launch_bounds__(256) k_sort_scatter(const uint32_t* __restrict
 }
 
 template <bool HAZE, bool INST, bool COUNT>
-__global__ void __launch_bounds__(256, 3) k_march(WaveArgs a, int cur, int nxt, int last) {
+__global__ void __launch_bounds__(256, 4) k_march(WaveArgs a, int cur, int nxt, int last) {
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ __align__(8) uint64_t mbar;
     __shared__ uint32_t wc[COUNT ? WC_N : 1];
@@ -624,7 +624,9 @@ __global__ void __launch_bounds__(256) k_shade(WaveArgs a, int nxt, int side, in
 // last iteration's pass runs every ray to its end (the reference's extra rounds on the last pass,
 // raytrace_main.js THE LAST PASS'S SHADOW ROUNDS).
 // ------------------------------------------------------------------------------------------------------------
-__global__ void __launch_bounds__(256, 3) k_occlude(WaveArgs a, int side, int last) {
+template <int SIDE>
+__global__ void __launch_bounds__(256, 4) k_occlude(WaveArgs a, int last) {
+    constexpr int side = SIDE;
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ __align__(8) uint64_t mbar;
     DPrim* sp = reinterpret_cast<DPrim*>(smem);
@@ -808,6 +810,17 @@ cudaError_t launch_march(const WaveArgs& a, int cur, int nxt, int last, int sms,
     else march_variant<false, false, false>(a, cur, nxt, last, sms, s, &g_occ_march);
     return cudaGetLastError();
 }
+// the scene's distance at given points, as the march folds the table (st_eval_sdf)
+__global__ void __launch_bounds__(256) k_eval_sdf(const DPrim* __restrict__ pr, uint32_t n_prims,
+                                                  const float* __restrict__ pts, uint32_t n, float* __restrict__ out) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        out[i] = scene_dist(pr, n_prims, mk(pts[3 * i], pts[3 * i + 1], pts[3 * i + 2]));
+}
+cudaError_t launch_eval_sdf(const DPrim* prims, uint32_t n_prims, const float* pts, uint32_t n, float* out,
+                            cudaStream_t s) {
+    k_eval_sdf<<<std::min((n + 255u) / 256u, 4096u), 256, 0, s>>>(prims, n_prims, pts, n, out);
+    return cudaGetLastError();
+}
 cudaError_t launch_sort(const WaveArgs& a, int cur, int sms, cudaStream_t s) {
     if (!a.u.sort_on) return cudaSuccess;
     const uint32_t* cnt = &a.ctr->rayCount[cur];
@@ -841,11 +854,16 @@ cudaError_t launch_shade(const WaveArgs& a, int nxt, int side, int last, int sms
     k_shade<<<sms * g_occ_shade, 256, smem, s>>>(a, nxt, side, last);
     return cudaGetLastError();
 }
-cudaError_t launch_occlude(const WaveArgs& a, int side, int last, int sms, cudaStream_t s) {
+template <int SIDE>
+static void occlude_side(const WaveArgs& a, int last, int sms, cudaStream_t s) {
     size_t smem = a.u.n_prims * sizeof(DPrim);
-    if (smem > 48 * 1024) cudaFuncSetAttribute(k_occlude, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (!g_occ_occl) g_occ_occl = occupancy((const void*)k_occlude, 32 * 1024);
-    k_occlude<<<sms * g_occ_occl, 256, smem, s>>>(a, side, last);
+    if (smem > 48 * 1024) cudaFuncSetAttribute(k_occlude<SIDE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (!g_occ_occl) g_occ_occl = occupancy((const void*)k_occlude<SIDE>, smem);
+    k_occlude<SIDE><<<sms * g_occ_occl, 256, smem, s>>>(a, last);
+}
+cudaError_t launch_occlude(const WaveArgs& a, int side, int last, int sms, cudaStream_t s) {
+    if (side) occlude_side<1>(a, last, sms, s);
+    else occlude_side<0>(a, last, sms, s);
     return cudaGetLastError();
 }
 cudaError_t launch_resolve(const WaveArgs& a, cudaStream_t s) {
