@@ -328,6 +328,11 @@ def run_ours(args):
                          "evals_per_launch": evals / max(m_launches, 1),
                          "prims_evaluated_per_eval": sum(dw["prim_evals"]) / max(dw["march_steps"], 1),
                          "fold_simd_efficiency": simd,
+                         "evals_by_type": {flops.TYPE_NAMES.get(t, str(t)): {
+                             "per_step": n / max(dw["march_steps"], 1),
+                             "simd_efficiency": n / max(32 * w, 1)}
+                             for t, (n, w) in enumerate(zip(dw["prim_evals"], dw["prim_warp_evals"])) if n},
+                         "bound_tests_per_step": dw["bound_tests"] / max(dw["march_steps"], 1),
                          "avg_launch_ms": m_ms / max(m_launches, 1), "peak_source": peak_src,
                          "work": "counted on the device in a counting pass (an instrumented march over one more "
                                  "render of the same seeds): evaluations by primitive type and fold operation, "

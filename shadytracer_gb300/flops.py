@@ -27,6 +27,8 @@ PRIM = {
     ST_PRIM_ASPHERE: (2 * 40 + 6, 8),            # two faces (sag, slope bound), the rim
     ST_PRIM_CYLINDER: (2 + 1 + 1 + 1 + 2 + 2 + 1 + 2 + 1, 2),
 }
+TYPE_NAMES = {ST_PRIM_PLANE: "plane", ST_PRIM_SPHERE: "sphere", ST_PRIM_BOX: "box", ST_PRIM_ROUNDBOX: "roundbox",
+              ST_PRIM_TORUS: "torus", ST_PRIM_PRISM: "prism", ST_PRIM_ASPHERE: "asphere", ST_PRIM_CYLINDER: "cylinder"}
 OP = {ST_OP_SMOOTH: (9, 1), ST_OP_UNION: (1, 0), ST_OP_SUB: (2, 0), ST_OP_ITEM: (0, 0)}
 FOLD = (3, 0)                                      # |d| compare and select per item
 STEP = (30, 1)                                     # marchTol, the escape and hit tests, the step and its length
