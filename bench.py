@@ -19,6 +19,8 @@ cpu_baseline: the oracle (oracle/, the CPU restatement of the reference's path) 
        bounded band of the same picture's paths.
 --impl reference: the reference's own implementation cannot run here (JavaScript + WGSL through WebGPU); its CPU
        restatement, the oracle, is timed instead on the host's cores, on the same workload and metric.
+optics: the batched optics bench (64 emitter + aspheric-lens instances, 120.2 M rays, FP64 far-field and lux
+       tallies) in rays/s, with the tallies on the device (`value`) and read back every run (`e2e`).
 Multi-GPU (torchrun): replicas -- each rank renders the whole workload on its own GPU; value sums the ranks' paths
        over the slowest rank's time (weak scaling). There is no data exchange in the path tracer.
 """
@@ -46,6 +48,7 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--small", action="store_true", help="a 480 x 270, 4-spp render (profiling runs)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
+    ap.add_argument("--no-optics", action="store_true", help="skip the optics bench's rays/s leg")
     ap.add_argument("--spp", type=int, default=0, help="samples per pixel a step (profiling runs; default: 64)")
     return ap.parse_args()
 
@@ -191,6 +194,74 @@ def run_reference(args):
                     "path is timed through the oracle, its CPU restatement, on every host core"}
     print(json.dumps(line), flush=True)
     return 0
+
+
+def optics_leg(args, dev, with_cpu):
+    """The batched optics bench (64 emitter + aspheric-lens instances, log-uniform ray counts from PCG32(5): 120.2 M
+    rays; far field 1 x 1 degree, lux 512 x 512 at 1 m, FP64 tallies) in rays/s: `value` with the tallies left on
+    the device, `e2e` with every instance's far field and lux map read back to host memory each run."""
+    import torch
+    from shadytracer_gb300 import scenes
+    from shadytracer_gb300.optics import Optics
+    from shadytracer_gb300.renderer import create_path_tracer
+    b = scenes.optics_bench(n_instances=8 if args.small else 64, seed=5, ray_scale=0.01 if args.small else 1.0)
+    rays = b.info["rays"]
+    total = int(sum(rays))
+    rt = create_path_tracer(b, device=dev)
+    O = Optics(rt)
+    O.set_sources(b.info["sources"])
+    O.set_far(nC=360, nG=181)
+    L = rt.L
+    n = len(rays)
+    rc = (C.c_uint32 * n)(*rays)
+    from shadytracer_gb300 import st_types as T
+    batch = T.StOpticsBatch()
+    batch.n_instances, batch.ray_count = n, C.cast(rc, C.POINTER(C.c_uint32))
+    batch.lux_cells, batch.lux_half, batch.lux_height, batch.maxbounce, batch.seed = 512, 1.0, 1.0, 32, 1
+    tot = (T.StOpticsTotals * n)()
+    far = np.zeros((n, 181, 360))
+    lux = np.zeros((n, 512, 512))
+
+    def run(out):
+        f = far.ctypes.data_as(C.c_void_p) if out else None
+        x = lux.ctypes.data_as(C.c_void_p) if out else None
+        r = L.st_optics_run(rt.ctx, C.byref(batch), f, x, tot)
+        if r != 0:
+            raise RuntimeError(L.st_last_error(rt.ctx))
+
+    for _ in range(max(args.warmup, 3)):
+        run(False)
+    K = max(args.steps, 1)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(K):
+        run(False)
+    torch.cuda.synchronize()
+    dev_s = (time.perf_counter() - t0) / K
+    t0 = time.perf_counter()
+    for _ in range(K):
+        run(True)
+    e2e_s = (time.perf_counter() - t0) / K
+    emitted = sum(tot[i].emitted for i in range(n))
+    escaped = sum(tot[i].escaped for i in range(n))
+    out = {"workload": "optics bench: %d LED die + aspheric lens instances, %d rays (log-uniform per instance), far "
+                       "field 360 x 181, lux 512 x 512 at 1 m, FP64 tallies" % (n, total),
+           "metric": "rays/s", "value": total / dev_s, "unit": "rays/s", "ms_per_run": 1e3 * dev_s,
+           "e2e": {"value": total / e2e_s, "unit": "rays/s", "h2d_bytes_per_step": 4 * n + C.sizeof(batch),
+                   "d2h_bytes_per_step": int(far.nbytes + lux.nbytes + C.sizeof(tot))},
+           "interactions_per_ray": sum(tot[i].interactions for i in range(n)) / max(total, 1),
+           "escaped_share": escaped / max(emitted, 1)}
+    rt.close()
+    if with_cpu:
+        from oracle import oracle
+        import os as _os
+        sub = [2000000] * 4
+        o_t = time.perf_counter()
+        oracle.optics_run(b, sub, nC=360, nG=181, cells=0, maxbounce=32, seed=1, threads=_os.cpu_count() or 1)
+        dt = time.perf_counter() - o_t
+        out["cpu_baseline"] = {"value": sum(sub) / dt, "unit": "rays/s", "cores": _os.cpu_count(), "kind": "port",
+                               "sample": "instances 0-3 of the same batch, 2 M rays each, far field only, %.1f s" % dt}
+    return out
 
 
 def run_ours(args):
@@ -348,6 +419,10 @@ def run_ours(args):
         line["cpu_baseline"] = cpu_baseline(s)
     elif rank == 0:
         line["cpu_baseline"] = None
+    if not args.no_optics:
+        line["optics"] = optics_leg(args, dev, rank == 0 and world == 1 and not args.no_cpu)
+        if world > 1:
+            line["optics"]["note"] = "per rank (each rank runs the whole batch)"
     if rank == 0:
         print(json.dumps(line), flush=True)
     rt.close()
