@@ -14,7 +14,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "liboracle.so")
 SOURCES = ["st_oracle.cpp", "st_oracle_core.h", "st_oracle_render.h", "st_oracle_extra.h", "st_oracle_sppm.h",
-           "st_oracle_optics.h", "st_oracle_api2.cpp", "../include/shadytracer.h"]
+           "st_oracle_optics.h", "st_oracle_spectral.h", "../include/shadytracer.h"]
 
 _lib = None
 
@@ -27,7 +27,7 @@ def build(force=False):
         t = os.path.getmtime(LIB)
         if all(os.path.getmtime(s) <= t for s in srcs):
             return LIB
-    cpp = [os.path.join(HERE, s) for s in ("st_oracle.cpp", "st_oracle_api2.cpp") if os.path.exists(os.path.join(HERE, s))]
+    cpp = [os.path.join(HERE, "st_oracle.cpp")]
     tmp = LIB + ".tmp%d" % os.getpid()
     cmd = ["g++", "-O2", "-std=c++17", "-fopenmp", "-fPIC", "-shared", "-fno-fast-math", "-ffp-contract=off",
            "-o", tmp] + cpp
@@ -196,6 +196,11 @@ def _declare_extra(L):
         "sto_far_geometry": ([C.c_uint32, C.c_uint32, P], None),
         "sto_far_intensity": ([P, C.c_uint32, C.c_uint32, P], None),
         "sto_step_moments": ([P, C.c_double, C.c_double], None),
+        "sto_cauchy_n": ([C.c_double, C.c_double, C.c_double], C.c_double),
+        "sto_lambda_code": ([C.c_double], C.c_uint32),
+        "sto_lambda_of": ([C.c_uint32], C.c_double),
+        "sto_spec_table": ([P, P], None),
+        "sto_spec_draw": ([C.c_double, P], C.c_double),
         "sto_optics_run": ([P, P, P, C.c_uint32, P, C.c_uint32, P, C.c_uint32, C.c_uint32, C.c_uint32, C.c_float,
                             C.c_float, C.c_uint32, C.c_uint32, C.c_int, P, P, P, C.c_int], C.c_int),
     }
@@ -280,6 +285,32 @@ def standard_error(V, S):
     if not (0 < S < 1) or V < 0:
         return None
     return float(np.sqrt(S * V / (1 - S)))
+
+
+# ---- dispersion (st_oracle_spectral.h) ----
+def cauchy_n(nd, vd, lam):
+    return xlib().sto_cauchy_n(nd, vd, lam)
+
+
+def lambda_code(lam):
+    return xlib().sto_lambda_code(lam)
+
+
+def lambda_of(code):
+    return xlib().sto_lambda_of(code)
+
+
+def spec_table():
+    cdf = np.zeros(400, np.float32)
+    col = np.zeros((400, 3), np.float32)
+    xlib().sto_spec_table(ptr(cdf), ptr(col))
+    return cdf, col
+
+
+def spec_draw(u):
+    w = np.zeros(3, np.float64)
+    lam = xlib().sto_spec_draw(u, ptr(w))
+    return lam, w
 
 
 # ---- haze and the far field ----

@@ -16,6 +16,7 @@
 #include "st_oracle_extra.h"
 #include "st_oracle_optics.h"
 #include "st_oracle_sppm.h"
+#include "st_oracle_spectral.h"
 #ifdef _OPENMP
 #include <omp.h>
 #endif
@@ -49,6 +50,7 @@ template <class T> struct Ctx {
 template <class T> struct Ray {
     V3<T> pos, dir, beta, rad;
     T ltot, n, sunmis, tmax, absLtot;
+    T lam = T(0);                           // the wavelength a dispersive refraction gave it (nm, as coded), 0 none
     uint32_t bounces, steps, state, pix;
 };
 
@@ -162,10 +164,25 @@ inline void shade_hit(const Ctx<T>& C, Ray<T>& r, T dhit, Rng& rng, bool last, F
         return;
     }
     T n0 = r.n;
-    T n1 = std::max(T(m.ior), n0);                                                 // ownMedium (materials_pbr.js:1080)
+    T n1d = std::max(T(m.ior), n0);                                                // ownMedium (materials_pbr.js:1080)
+    T v1 = T(0);
     if (m.transmission > 0 && m.metallic < 1) {                                    // asksMedium (materials.js:114)
         SceneHit<T> mb = scene_eval(*C.s, r.pos + (-nrm) * (otol * T(2)));         // mediumBeyond (tracebasics.js:1332)
-        n1 = T(C.s->materials[std::min(mb.a, C.s->n_materials - 1)].ior);
+        const st_material& mm = C.s->materials[std::min(mb.a, C.s->n_materials - 1)];
+        n1d = T(mm.ior);
+        v1 = T(mm.abbe);
+    }
+    // DISPERSION (materials_pbr.js:1116-1139): the medium beyond at the ray's own wavelength, if it has one; a ray
+    // without one, at a dispersive medium beyond, draws one, used only if it refracts
+    const T lam0 = r.lam;
+    const T n1 = lam0 > T(0) ? cauchy_n(n1d, v1, lam0) : n1d;
+    const bool draw = v1 > T(0) && lam0 == T(0);
+    T nT = n1, lamD = T(0);
+    V3<T> specW(T(1), T(1), T(1));
+    if (draw) {
+        T ul[4]; rng.next4(ul);
+        lamD = lambda_coded(spec_draw(ul[0], specW));
+        nT = cauchy_n(n1d, v1, lamD);
     }
     // A FACE THAT BOTH REFRACTS AND DIFFUSES, SEEN FROM INSIDE (materials_pbr.js:1150-1165): one part drawn
     T pG = refract_share<T>(m);
@@ -179,7 +196,7 @@ inline void shade_hit(const Ctx<T>& C, Ray<T>& r, T dhit, Rng& rng, bool last, F
     }
     T etaFace = diffFace ? std::min(n0, n1) / std::max(n0, n1) : n0 / n1;
     Lobes<T> lb = make_lobes(nrm, -r.dir, m, etaFace, C.tb, trans, specv);
-    lb.etaT = n0 / n1;
+    lb.etaT = n0 / nT;
 
     // LIGHT SAMPLING (materials_pbr.js:1196-1330): the environment only (no faces, no discovered emitters)
     if (C.p.nee != 0 && !last) {
@@ -214,7 +231,10 @@ inline void shade_hit(const Ctx<T>& C, Ray<T>& r, T dhit, Rng& rng, bool last, F
     LobeSample<T> smp = lobes_sample(lb, ur);
     r.dir = smp.dir;
     r.beta *= smp.w;
-    if (smp.transmitted) r.n = n1;
+    if (smp.transmitted) {
+        r.n = nT;                                                                  // n(lambda) where it has one
+        if (draw) { r.beta *= specW; r.lam = lamD; }
+    }
     if (max3(smp.w) <= T(0)) r.state = RAY_ABSORBED;
     bool misOut = C.p.nee != 0 && !last;
     if (misOut) {                                                                  // materials_pbr.js:1370-1395
@@ -725,6 +745,19 @@ void sto_step_moments(double* state, double x, double window) {
     state[0] = (prevY * prevn + x) / (prevn + 1);
     step_moments(prevn, x, prevY, state[1], state[2]);
     state[3] = prevn + 1;
+}
+double sto_cauchy_n(double nd, double vd, double lam) { return cauchy_n<double>(nd, vd, lam); }
+uint32_t sto_lambda_code(double l) { return lambda_code(l); }
+double sto_lambda_of(uint32_t c) { return lambda_of(c); }
+void sto_spec_table(float* cdf, float* col) {
+    const SpecTable& t = spec_table();
+    for (int i = 0; i < SPEC_N; i++) { cdf[i] = t.cdf[i]; for (int c = 0; c < 3; c++) col[3 * i + c] = t.col[i][c]; }
+}
+double sto_spec_draw(double u, double* w) {
+    V3<double> v;
+    double l = spec_draw<double>(u, v);
+    w[0] = v.x; w[1] = v.y; w[2] = v.z;
+    return l;
 }
 uint32_t sto_sppm_hash(int32_t i, int32_t j, int32_t k) { return sppm_hash(i, j, k); }
 double sto_sppm_radius(double r1, int k, double alpha) { return sppm_radius(r1, k, alpha); }

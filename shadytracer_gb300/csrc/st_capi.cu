@@ -18,6 +18,7 @@
 
 #include "st_internal.h"
 #include "st_ext.h"
+#include "st_spectral.h"
 
 using namespace st;
 
@@ -43,6 +44,7 @@ struct st_ctx {
     st_view view{};
     // the albedo tables
     float *d_ec = nullptr, *d_ecavg = nullptr, *d_e1 = nullptr;
+    float4* d_spec = nullptr;             // the camera's wavelength table (st_spectral.h), SPEC_CELLS float4s
     // the wave
     uint32_t W = 0, H = 0, P = 0, spw = 0, slot_cap = 0;
     PathBuf pb{};
@@ -86,7 +88,7 @@ static int cuda_fail(st_ctx* c, cudaError_t e, const char* what) {
     } while (0)
 
 static void free_wave(st_ctx* ctx) {
-    void* ptrs[] = {ctx->pb.pos, ctx->pb.dir, ctx->pb.beta, ctx->pb.rad, ctx->pb.meta, ctx->q.ray[0], ctx->q.ray[1],
+    void* ptrs[] = {ctx->pb.pos, ctx->pb.dir, ctx->pb.beta, ctx->pb.rad, ctx->pb.meta, ctx->pb.lam, ctx->q.ray[0], ctx->q.ray[1],
                     ctx->q.hit, ctx->q.hitd, ctx->q.hsurf, ctx->q.sorted, ctx->q.skey, ctx->q.srank, ctx->q.bcnt,
                     ctx->q.boff, ctx->q.ssorted, ctx->q.sskey, ctx->q.ssrank, ctx->q.s_org[0], ctx->q.s_dir[0], ctx->q.s_rad[0], ctx->q.s_steps[0],
                     ctx->q.s_org[1], ctx->q.s_dir[1], ctx->q.s_rad[1], ctx->q.s_steps[1], ctx->d_frame,
@@ -257,6 +259,7 @@ static int ensure_wave(st_ctx* ctx) {
     CK(cudaMalloc(&ctx->pb.beta, S * sizeof(float4)), "cudaMalloc path state");
     CK(cudaMalloc(&ctx->pb.rad, S * sizeof(float4)), "cudaMalloc path state");
     CK(cudaMalloc(&ctx->pb.meta, S * sizeof(uint4)), "cudaMalloc path state");
+    CK(cudaMalloc(&ctx->pb.lam, S * sizeof(float)), "cudaMalloc path state");
     CK(cudaMalloc(&ctx->q.ray[0], S * 4), "cudaMalloc queues");
     CK(cudaMalloc(&ctx->q.ray[1], S * 4), "cudaMalloc queues");
     CK(cudaMalloc(&ctx->q.hit, S * 4), "cudaMalloc queues");
@@ -300,6 +303,7 @@ static WaveArgs wave_args(st_ctx* ctx, uint32_t w) {
     a.prims = ctx->d_prims;
     a.mats = ctx->d_mats;
     a.tab = MfTab{ctx->d_ec, ctx->d_ecavg, ctx->d_e1};
+    a.spec = ctx->d_spec;
     a.pb = ctx->pb;
     a.q = ctx->q;
     a.ctr = ctx->d_ctr;
@@ -409,11 +413,21 @@ int st_create(int device, st_ctx** out) {
     if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) { delete ctx; return ST_ERR_CUDA; }
     const size_t NEC = 16 * 32 * 32, NAVG = 16 * 32, NE1 = 32 * 32;
     if (cudaMalloc(&ctx->d_ec, NEC * 4) || cudaMalloc(&ctx->d_ecavg, NAVG * 4) || cudaMalloc(&ctx->d_e1, NE1 * 4) ||
-        cudaMalloc(&ctx->d_ctr, sizeof(DevCtr))) {
+        cudaMalloc(&ctx->d_ctr, sizeof(DevCtr)) || cudaMalloc(&ctx->d_spec, SPEC_CELLS * sizeof(float4))) {
         st_destroy(ctx);
         return ST_ERR_OOM;
     }
     cudaMemsetAsync(ctx->d_ctr, 0, sizeof(DevCtr), ctx->stream);
+    {
+        const std::vector<double> t = spectral_table();
+        std::vector<float4> f(SPEC_CELLS);
+        for (int i = 0; i < SPEC_CELLS; i++)
+            f[i] = make_float4((float)t[4 * i], (float)t[4 * i + 1], (float)t[4 * i + 2], (float)t[4 * i + 3]);
+        if (cudaMemcpy(ctx->d_spec, f.data(), SPEC_CELLS * sizeof(float4), cudaMemcpyHostToDevice) != cudaSuccess) {
+            st_destroy(ctx);
+            return ST_ERR_CUDA;
+        }
+    }
     if (launch_mf_tables(ctx->d_ec, ctx->d_ecavg, ctx->d_e1, ctx->stream) != cudaSuccess ||
         cudaStreamSynchronize(ctx->stream) != cudaSuccess) {
         st_destroy(ctx);
@@ -430,7 +444,7 @@ int st_destroy(st_ctx* ctx) {
     free_wave(ctx);
     ext_free(ctx->ext);
     for (void* p : {(void*)ctx->d_prims, (void*)ctx->d_mats, (void*)ctx->d_ec, (void*)ctx->d_ecavg,
-                    (void*)ctx->d_e1, (void*)ctx->d_ctr})
+                    (void*)ctx->d_e1, (void*)ctx->d_ctr, (void*)ctx->d_spec})
         if (p) cudaFree(p);
     for (auto& pe : ctx->pending) { cudaEventDestroy(pe.a); cudaEventDestroy(pe.b); }
     for (auto e : ctx->event_pool) cudaEventDestroy(e);

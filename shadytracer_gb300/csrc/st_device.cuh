@@ -113,6 +113,41 @@ struct Uni {
 };
 
 // ------------------------------------------------------------------------------------------------------------
+// DISPERSION (spectral.js:121-128 cauchyN, :136-137 lambdaCode; lightspectra.js specDraw): Cauchy's index through a
+// glass's n_d and Abbe number, the wavelength as the reference's 15-bit code keeps it, and the camera's draw of a
+// wavelength from the 1 nm table (csrc/st_spectral.h builds it on the host: per cell the CDF and its colour).
+// ------------------------------------------------------------------------------------------------------------
+#define SPEC_NCELLS 400
+__device__ __forceinline__ float cauchy_n(float nd, float vd, float lam) {
+    if (!(vd > 0.f)) return nd;
+    const float FC = (float)(1.0 / (486.13 * 486.13) - 1.0 / (656.27 * 656.27));   // 1/lambda_F^2 - 1/lambda_C^2
+    const float LD2 = (float)(587.56 * 587.56);
+    const float B = (nd - 1.f) / (vd * FC);
+    return nd + B * (1.f / (lam * lam) - 1.f / LD2);
+}
+__device__ __forceinline__ float lambda_coded(float lam) {
+    const float c = 1.f + rintf(fminf(fmaxf((lam - 380.f) / 400.f, 0.f), 1.f) * 32766.f);
+    return 380.f + (c - 1.f) * (400.f / 32766.f);
+}
+struct SpecDraw { float lam; f3 w; };
+__device__ __forceinline__ SpecDraw spec_draw(const float4* __restrict__ tab, float u) {
+    uint32_t lo = 0, hi = SPEC_NCELLS - 1;
+    while (lo < hi) {                                                  // the first cell whose CDF passes u
+        const uint32_t mid = (lo + hi) >> 1;
+        if (__ldg(&tab[mid].x) > u) hi = mid;
+        else lo = mid + 1;
+    }
+    const float c0 = lo ? __ldg(&tab[lo - 1].x) : 0.f;
+    const float4 t = __ldg(&tab[lo]);
+    const float q = t.x - c0;
+    const float f = q > 0.f ? fminf(fmaxf((u - c0) / q, 0.f), 1.f) : 0.5f;
+    SpecDraw d;
+    d.lam = 380.f + (float)lo + f;
+    d.w = mk(t.y, t.z, t.w);
+    return d;
+}
+
+// ------------------------------------------------------------------------------------------------------------
 // THE TOLERANCE (core/tolerances.js:27-37 marchTol); offsetTol = 10 marchTol (tracebasics.js:165)
 // ------------------------------------------------------------------------------------------------------------
 __device__ __forceinline__ float march_tol(f3 p, float setting) {

@@ -40,6 +40,7 @@ struct PathBuf {
     float4* beta;   // xyz throughput, w sunmis (the environment's MIS weight on escape)
     float4* rad;    // xyz radiance collected, w tmax (the haze's collision, as ltot)
     uint4* meta;    // x pix, y bounces | segment << 8 | state << 16, z march steps over the path, w absLtot (f32)
+    float* lam = nullptr;   // the wavelength a dispersive refraction gave the path (nm, as coded), 0 none
 };
 // THE QUEUES: indices into the path state, appended with one atomic per warp (ballot + popc)
 struct Queues {
@@ -90,6 +91,7 @@ struct WaveArgs {
     double2* mom;       // P: FP64 V, S (the error bar's moments)
     uint32_t spw;       // samples in this wave
     uint32_t slots;     // spw * P
+    const float4* spec = nullptr;         // the camera's wavelength table (SPEC_NCELLS cells: CDF, colour rgb)
     const uint2* inst_range = nullptr;   // a batch of instances (the optics bench): each one's [first, count) of the
                                          // table, the instance in meta.w; null for a picture
 };

@@ -24,6 +24,7 @@
 #include <cstring>
 #include <mutex>
 
+#include "st_spectral.h"
 #include "st_internal.h"
 
 using namespace st;
@@ -37,7 +38,7 @@ const double PI_D = 3.14159265358979323846;
 
 struct Layout {
     size_t pos, dir, beta, rad, meta, ray0, ray1, hit, hitd, hsurf, so[2], sd[2], sr[2], ss[2], frame, acc, mom, cnt, ctr,
-        ec, ecavg, e1, prims, mats, end;
+        ec, ecavg, e1, spec, lam, prims, mats, end;
 };
 // the array carved for P paths a wave (one sample), each buffer 256-byte aligned: first what does not depend on the
 // picture's size (the albedo tables, built once, the scene's tables, the counters), then the wave's buffers
@@ -46,10 +47,12 @@ Layout layout(size_t P) {
     size_t o = 0;
     auto take = [&](size_t bytes) { size_t at = o; o += (bytes + 255) & ~size_t(255); return at; };
     L.ec = take(16 * 32 * 32 * 4); L.ecavg = take(16 * 32 * 4); L.e1 = take(32 * 32 * 4);
+    L.spec = take(SPEC_CELLS * sizeof(float4));
     L.prims = take(ST_MAX_PRIMS * sizeof(DPrim)); L.mats = take(ST_MAX_MATERIALS * sizeof(st_material));
     L.ctr = take(sizeof(DevCtr));
     const size_t SS = 2 * P;                                   // a shadow side: new rays and continuations
     L.pos = take(P * 16); L.dir = take(P * 16); L.beta = take(P * 16); L.rad = take(P * 16); L.meta = take(P * 16);
+    L.lam = take(P * 4);
     L.ray0 = take(P * 4); L.ray1 = take(P * 4); L.hit = take(P * 4); L.hitd = take(P * 4);
     L.hsurf = take(P * 16);
     for (int k = 0; k < 2; k++) {
@@ -187,6 +190,11 @@ extern "C" int st_render_noalloc(int device, const st_scene_desc* desc, const st
             if (launch_mf_tables((float*)(b + L.ec), (float*)(b + L.ecavg), (float*)(b + L.e1), s) != cudaSuccess ||
                 cudaStreamSynchronize(s) != cudaSuccess)
                 return ST_ERR_CUDA;
+            const std::vector<double> t = spectral_table();             // the camera's wavelength table
+            float4 f[SPEC_CELLS];
+            for (int i = 0; i < SPEC_CELLS; i++)
+                f[i] = make_float4((float)t[4 * i], (float)t[4 * i + 1], (float)t[4 * i + 2], (float)t[4 * i + 3]);
+            if (cudaMemcpy(b + L.spec, f, sizeof(f), cudaMemcpyHostToDevice) != cudaSuccess) return ST_ERR_CUDA;
             g_base[device] = b;
         }
         base = g_base[device];
@@ -210,8 +218,10 @@ extern "C" int st_render_noalloc(int device, const st_scene_desc* desc, const st
     a.prims = reinterpret_cast<const DPrim*>(base + L.prims);
     a.mats = reinterpret_cast<const st_material*>(base + L.mats);
     a.tab = MfTab{(const float*)(base + L.ec), (const float*)(base + L.ecavg), (const float*)(base + L.e1)};
+    a.spec = (const float4*)(base + L.spec);
     a.pb = PathBuf{(float4*)(base + L.pos), (float4*)(base + L.dir), (float4*)(base + L.beta), (float4*)(base + L.rad),
                    (uint4*)(base + L.meta)};
+    a.pb.lam = (float*)(base + L.lam);
     a.q.ray[0] = (uint32_t*)(base + L.ray0);
     a.q.ray[1] = (uint32_t*)(base + L.ray1);
     a.q.hit = (uint32_t*)(base + L.hit);

@@ -101,6 +101,7 @@ __global__ void __launch_bounds__(256) k_genrays(WaveArgs a) {
         a.pb.beta[i] = make_float4(1.f, 1.f, 1.f, 1.f);
         a.pb.rad[i] = make_float4(0.f, 0.f, 0.f, 0.f);
         a.pb.meta[i] = make_uint4(pix, RAY_ACTIVE << 16, 0u, __float_as_uint(0.f));
+        a.pb.lam[i] = 0.f;
         a.q.ray[0][i] = i;
     }
 }
@@ -392,8 +393,8 @@ struct ShadowOut { bool valid; f3 org, dir, rad; float n; };
 
 __device__ __forceinline__ void shade_surface(const WaveArgs& a, const st_material* sm, float4 surf,
                                               f3& pos, f3& dir, float& ltot, float& n, f3& beta, float& sunmis,
-                                              f3& rad, uint32_t& bounces, uint32_t& state, float dh, Rng& rng,
-                                              bool last, ShadowOut& sh) {
+                                              f3& rad, uint32_t& bounces, uint32_t& state, float& lam, float dh,
+                                              Rng& rng, bool last, ShadowOut& sh) {
     const Uni& u = a.u;
     float eps = march_tol(pos, u.tol);
     const uint32_t ids = __float_as_uint(surf.w);
@@ -417,8 +418,25 @@ __device__ __forceinline__ void shade_surface(const WaveArgs& a, const st_materi
         return;
     }
     float n0 = n;
-    float n1 = fmaxf(m.ior, n0);                                      // ownMedium
-    if ((ids >> 16) != SURF_NONE) n1 = sm[ids >> 16].ior;             // asksMedium -> mediumBeyond
+    float n1d = fmaxf(m.ior, n0), v1 = 0.f;                           // ownMedium
+    if ((ids >> 16) != SURF_NONE) {                                   // asksMedium -> mediumBeyond: index, Abbe
+        n1d = sm[ids >> 16].ior;
+        v1 = sm[ids >> 16].abbe;
+    }
+    // DISPERSION (materials_pbr.js:1116-1139): a ray with a wavelength meets the medium beyond at n(its wavelength);
+    // one without, at a dispersive medium, draws one (the camera's table), used only if it refracts -- the reflect-
+    // or-refract pick and its Fresnel stay the d line's
+    const float lam0 = lam;
+    const float n1 = lam0 > 0.f ? cauchy_n(n1d, v1, lam0) : n1d;
+    const bool draw = v1 > 0.f && lam0 == 0.f;
+    SpecDraw spec;
+    float nT = n1;
+    if (draw) {
+        float4 r4 = rng.next();
+        spec = spec_draw(a.spec, r4.x);
+        spec.lam = lambda_coded(spec.lam);
+        nT = cauchy_n(n1d, v1, spec.lam);
+    }
     float pG = sat(m.transmission);
     float trans = m.transmission, specv = m.specular;
     bool diffFace = false;
@@ -430,7 +448,7 @@ __device__ __forceinline__ void shade_surface(const WaveArgs& a, const st_materi
     }
     float etaFace = diffFace ? fminf(n0, n1) / fmaxf(n0, n1) : n0 / n1;
     Lobes lb = make_lobes(nrm, -dir, m, etaFace, a.tab, trans, specv);
-    lb.etaT = n0 / n1;
+    lb.etaT = n0 / nT;
     if (u.nee != 0u && !last) {                                       // light sampling (materials_pbr.js:1196-1330)
         float4 u0 = rng.next();
         float4 u1 = rng.next();
@@ -459,7 +477,10 @@ __device__ __forceinline__ void shade_surface(const WaveArgs& a, const st_materi
     LobeSample smp = lobes_sample(lb, a.tab, rng.next());           // the bounce
     dir = smp.dir;
     beta = beta * smp.w;
-    if (smp.transmitted) n = n1;
+    if (smp.transmitted) {
+        n = nT;                                                       // n(lambda) where the ray has a wavelength
+        if (draw) { beta = beta * spec.w; lam = spec.lam; }           // ...and the one it was refracted at, kept
+    }
     if (max3(smp.w) <= 0.f) state = RAY_ABSORBED;
     if (u.nee != 0u && !last) {                                       // the other half of MIS (:1370-1395)
         bool above = dot(nrm, dir) > 0.f && !smp.isDelta;
@@ -546,6 +567,7 @@ __global__ void __launch_bounds__(256) k_shade(WaveArgs a, int nxt, int side, in
         float ltot = 0.f, n = 1.f, sunmis = 1.f, tmax = 0.f;
         uint4 m4 = make_uint4(0, 0, 0, 0);
         uint32_t bounces = 0, seg = 0, state = RAY_TERMINATED;
+        float lam = 0.f;
         if (valid) {
             slot = a.q.hit[q];
             float dh = a.q.hitd[q];
@@ -565,8 +587,11 @@ __global__ void __launch_bounds__(256) k_shade(WaveArgs a, int nxt, int side, in
                 if (state == RAY_SCATTER)
                     shade_medium(a, pos, dir, beta, sunmis, bounces, state, n, rng, last != 0, sh);
                 else
-                    shade_surface(a, sm, a.q.hsurf[q], pos, dir, ltot, n, beta, sunmis, rad, bounces, state, dh,
-                                  rng, last != 0, sh);
+                {
+                    lam = a.pb.lam[slot];
+                    shade_surface(a, sm, a.q.hsurf[q], pos, dir, ltot, n, beta, sunmis, rad, bounces, state, lam,
+                                  dh, rng, last != 0, sh);
+                }
                 if (state == RAY_ACTIVE) {
                     tmax = 0.f;                                       // a new leg
                     if (last) { state = RAY_MAXITER; flushed++; }     // THE FLUSH
@@ -592,6 +617,7 @@ __global__ void __launch_bounds__(256) k_shade(WaveArgs a, int nxt, int side, in
             a.pb.dir[slot] = f4(dir, n);
             a.pb.beta[slot] = f4(beta, sunmis);
             a.pb.rad[slot] = f4(rad, tmax);
+            if (lam != 0.f) a.pb.lam[slot] = lam;
             m4.y = meta_y(bounces, seg, RAY_ACTIVE);
             a.pb.meta[slot] = m4;
             outq[rq] = slot;

@@ -230,6 +230,25 @@ def sdf_room(width=1920, height=1080, spp=64, maxbounce=8, seed=1, n_prims=24, p
 
 
 # ---------------------------------------------------------------------------------------------------------------
+# Dispersion (spectral.js cauchyN, lightspectra.js specDraw): the glass of config 3's caustic.
+# ---------------------------------------------------------------------------------------------------------------
+def dispersive_furnace(width=64, height=64, ior=1.5168, abbe=40.0, sky=1000.0, maxbounce=16, seed=1, floor=False):
+    """A clear glass sphere (r 0.3 m) of index `ior` at the d line and Abbe number `abbe` in a uniform environment of
+    `sky` cd/m^2 (with `floor`, on a white Lambertian floor, albedo 0.7). Without the floor every pixel must read `sky`
+    on average: the glass absorbs nothing, and the wavelength a refraction draws weighs each channel by 1 on average
+    (spectral.js / lightspectra.js: the draw's colour over its chance)."""
+    mats = [air(), glass((1.0, 1.0, 1.0), ior=ior, abbe=abbe), diffuse((0.7, 0.7, 0.7))]
+    prims = [prim(ST_PRIM_SPHERE, pos=(0.0, 0.0, 0.3 if floor else 1.0), params=(0.3,), material=1)]
+    if floor:
+        prims.append(prim(ST_PRIM_PLANE, material=2))
+    s = Scene(prims, mats, env_radius=40.0, name="dispersive-furnace")
+    s.params = default_params(width=width, height=height, maxbounce=maxbounce, env_uniform=sky, sun_hint=0, seed=seed)
+    s.view = look_at((0.0, -1.6, 1.2 if floor else 1.0), (0.0, 0.0, 0.3 if floor else 1.0), 40.0, width / height)
+    s.info = {"closed_form": None if floor else sky}
+    return s
+
+
+# ---------------------------------------------------------------------------------------------------------------
 # Config 4: the haze box (lib/pathtracer/tests.js:1818-1866 'haze' row; core/haze.js).
 # ---------------------------------------------------------------------------------------------------------------
 def haze_furnace(width=64, height=64, sigma_t=0.2, g=0.0, albedo=1.0, sky=1000.0, maxbounce=32, seed=1):

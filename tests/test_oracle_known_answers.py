@@ -280,3 +280,47 @@ def test_far_bins():
     assert oracle.far_bin((1, 0, 0), ax, c0, 360, 181) == 90 * 360
     assert oracle.far_bin((0, 1, 0), ax, c0, 360, 181) == 90 * 360 + 90
     assert oracle.far_bin((0, -1, 0), ax, c0, 360, 181) == 90 * 360 + 270
+
+
+# ---- dispersion (core/test/spectral.test.mjs:138-151, lightspectra.js's table) ----
+def test_cauchy_index():
+    LD, LF, LC = 587.56, 486.13, 656.27
+    assert oracle.cauchy_n(1.5168, 64.17, LD) == pytest.approx(1.5168, abs=1e-15)
+    assert (1.75 - 1) / (oracle.cauchy_n(1.75, 28, LF) - oracle.cauchy_n(1.75, 28, LC)) == pytest.approx(28, abs=1e-9)
+    assert oracle.cauchy_n(1.5168, 64.17, LF) == pytest.approx(1.52238, abs=1e-4)          # Schott N-BK7
+    assert oracle.cauchy_n(1.5168, 64.17, LC) == pytest.approx(1.51432, abs=1e-4)
+    ns = [oracle.cauchy_n(1.6, 40, l) for l in (400, 450, 500, 600, 700, 780)]
+    assert all(b < a for a, b in zip(ns, ns[1:]))                                      # blue bends more
+    assert all(oracle.cauchy_n(1.5, 0, l) == 1.5 for l in (380, 587.56, 780))            # Abbe 0: no dispersion
+
+
+def test_lambda_code():
+    for l in (380, 412.345, 550, 699.999, 780):
+        assert abs(oracle.lambda_of(oracle.lambda_code(l)) - l) <= 400 / 32766 / 2 + 1e-9
+    assert oracle.lambda_of(0) == 0
+    assert oracle.lambda_code(380) == 1 and oracle.lambda_code(780) == 32767
+    assert oracle.lambda_code(200) == 1 and oracle.lambda_code(900) == 32767
+
+
+def test_camera_wavelength_table():
+    cdf, col = oracle.spec_table()
+    q = np.diff(np.concatenate([[0.0], cdf.astype(np.float64)]))
+    assert np.all(q >= 0) and cdf[-1] == 1.0
+    assert np.allclose((q[:, None] * col).sum(0), 1.0, atol=1e-5)       # each channel's mean weight is 1
+    assert col.max() <= 3.0 + 1e-6 and col.min() >= 0
+    # a draw lands in its cell, uniform inside it, its colour the cell's
+    for u in (0.0, 0.1, 0.5, 0.9, 0.999999):
+        lam, w = oracle.spec_draw(u)
+        i = int(np.searchsorted(cdf, u, side="right"))
+        assert 380 + i <= lam <= 381 + i
+        assert np.allclose(w, col[i])
+    # blue early, red late
+    assert oracle.spec_draw(0.05)[1][2] > oracle.spec_draw(0.05)[1][0]
+    assert oracle.spec_draw(0.95)[1][0] > oracle.spec_draw(0.95)[1][2]
+
+
+def test_dispersive_furnace_on_the_oracle():
+    s = scenes.dispersive_furnace(width=24, height=24)
+    a = oracle.render(s, 8)
+    L = a.luma()
+    assert abs(L.mean() / 1000.0 - 1) < 0.02
