@@ -152,6 +152,14 @@ typedef struct st_params {
     uint32_t budget;              /* wavefront iterations a sample runs; 0 = the worst case,
                                      maxbounce + 1 + ceil(maxiter / 32) (raytrace_main.js:1815)   */
     uint32_t samples_per_wave;    /* 0 = automatic                                                 */
+    /* the photon map (core/sppm.js): sun photons traced through glass and mirrors before each sample's
+     * camera rays, stored where they first land on an evaluable surface, gathered by camera rays that
+     * have seen only glass and mirrors since the eye; one sample a wave while it runs */
+    uint32_t sppm;                /* 1 on                                                           */
+    uint32_t sppm_photons;        /* photons a sample (0: one a pixel)                              */
+    float    sppm_r1;             /* the first sample's radius, metres (0: 5 mm)                    */
+    float    sppm_alpha;          /* the radius schedule's alpha (0: 2/3)                           */
+    float    sppm_half;           /* the sun photons' square, half width, metres (0: min(15, radius)) */
 } st_params;
 
 /* The camera, as genrays reads it (core/genrays.js:65-92): the basis from invView's columns and the
@@ -247,7 +255,7 @@ int  st_mf_tables(st_ctx* ctx, float* ec, float* ecavg, float* e1);
 typedef struct st_sppm_stats {
     uint32_t stored;              /* records in the grid                                           */
     uint32_t gathers;             /* gathers run                                                   */
-    uint32_t cut;                 /* gathers that reached the hard cap                             */
+    uint32_t cut;                 /* gathers that reached the hard cap (the wavefront's map: records dropped) */
     uint32_t visits_max;          /* most records one gather looked at                              */
     uint64_t visits;              /* records looked at in all                                      */
 } st_sppm_stats;

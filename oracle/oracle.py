@@ -197,6 +197,7 @@ def _declare_extra(L):
         "sto_far_intensity": ([P, C.c_uint32, C.c_uint32, P], None),
         "sto_step_moments": ([P, C.c_double, C.c_double], None),
         "sto_cauchy_n": ([C.c_double, C.c_double, C.c_double], C.c_double),
+        "sto_sppm_photons": ([P, P, C.c_uint32, P, P, P], C.c_int),
         "sto_lambda_code": ([C.c_double], C.c_uint32),
         "sto_lambda_of": ([C.c_uint32], C.c_double),
         "sto_spec_table": ([P, P], None),
@@ -285,6 +286,14 @@ def standard_error(V, S):
     if not (0 < S < 1) or V < 0:
         return None
     return float(np.sqrt(S * V / (1 - S)))
+
+
+def sppm_photons(scene, sample=0, lo=(-1e9, -1e9, -1e9), hi=(1e9, 1e9, 1e9)):
+    """One sample's photon pass alone: (records stored, their power summed over the box lo..hi)."""
+    out = np.zeros(4, np.float64)
+    xlib().sto_sppm_photons(C.byref(scene.desc), C.byref(scene.params), sample, ptr(np.asarray(lo, np.float32)),
+                            ptr(np.asarray(hi, np.float32)), ptr(out))
+    return int(out[0]), out[1:]
 
 
 # ---- dispersion (st_oracle_spectral.h) ----

@@ -45,12 +45,22 @@ template <class T> struct Ctx {
     T tol, envR2, stepscale;
     uint32_t budget;
     HazeBox<T> haze;
+    // the photon map of the sample being traced (sppm.js): on, its grid, radius, cell, 1 / (pi r^2), the photons'
+    // square, the gather's budget
+    bool sppm = false;
+    const SppmGrid* grid = nullptr;
+    float sp_r2 = 0, sp_cell = 0, sp_half = 0;
+    double sp_inv_area = 0;
+    uint32_t sp_budget = 512;
 };
 
 template <class T> struct Ray {
     V3<T> pos, dir, beta, rad;
     T ltot, n, sunmis, tmax, absLtot;
     T lam = T(0);                           // the wavelength a dispersive refraction gave it (nm, as coded), 0 none
+    uint32_t lens = 0;                      // a camera path's lens field (materials_pbr.js lensField): 1 delta only
+                                            // since the eye, 2 at its D, 3 delta only since its D
+    bool passed = false;                    // a photon that has passed a delta event (TAG_PASSED)
     uint32_t bounces, steps, state, pix;
 };
 
@@ -141,10 +151,108 @@ template <class T> inline V3<T> hit_normal(const Ctx<T>& C, const V3<T>& p, T d)
     return normalize(V3<T>(gx, gy, gz));
 }
 
+const uint32_t SPPM_STORE_SALT = 0x53505031u;   // a store's and a gather's own stream (wavefront.js:1186)
+const uint32_t PHOTON_SEED_SALT = 0x50484F54u;  // the photons' sample seed: the picture's seed xor this
+const uint32_t PHOTON_GEN_SALT = 0x5A17u;       // their draw at the source (wavefront.js:594)
+
+// sppmEvaluable (wavefront.js prog_sppm): a diffuse base, or gloss rough enough (LT_MIN_ALPHA 0.05 for a photon's
+// store, ALPHA_MIN 1e-3 for a camera's gather)
+inline bool sppm_evaluable(const st_material& m, bool all) {
+    float r = std::min(std::max(m.roughness, 0.f), 1.f);
+    float rs = std::min(std::max(m.transmission, 0.f), 1.f);
+    return (1.f - m.metallic) * (1.f - rs) > 0.f || r * r >= (all ? 1e-3f : 0.05f);
+}
+// THE GATHER at a camera vertex (sppm.js:475-494 sppmGather through sppmWalk): the eight cells, each cell's whole list
+// within its share of the budget, else m of its sub-lists from a drawn start, each record weighing SUBS / m; records of
+// another cell, past r, facing away or past the bounce cap passed by; f over the evaluable lobes (from LT_MIN_ALPHA)
+template <class T>
+inline V3<T> sppm_gather_lobes(const Ctx<T>& C, const V3<T>& X, const V3<T>& nrm, const Lobes<T>& lb, uint32_t bc,
+                               Rng& rng) {
+    const SppmGrid& g = *C.grid;
+    const float csz = g.cell;
+    const float x[3] = {(float)X.x, (float)X.y, (float)X.z};
+    const float nq[3] = {(float)nrm.x, (float)nrm.y, (float)nrm.z};
+    float gx[3] = {x[0] / csz, x[1] / csz, x[2] / csz};
+    int32_t c0[3], side[3];
+    for (int a = 0; a < 3; a++) {
+        c0[a] = (int32_t)std::floor(gx[a]);
+        side[a] = (gx[a] - std::floor(gx[a]) >= 0.5f) ? 1 : -1;
+    }
+    const uint32_t share = std::max(1u, C.sp_budget / 8);
+    const uint64_t hard = (uint64_t)SPPM_VISIT_HARD * C.sp_budget;
+    uint64_t visits = 0;
+    bool cut = false;
+    V3<T> sum(T(0));
+    for (uint32_t k = 0; k < 8 && !cut; k++) {
+        int32_t cell[3] = {c0[0] + ((k & 1) ? side[0] : 0), c0[1] + ((k & 2) ? side[1] : 0), c0[2] + ((k & 4) ? side[2] : 0)};
+        uint32_t h = sppm_hash(cell[0], cell[1], cell[2]);
+        const std::vector<uint32_t>& L = g.lists[h];
+        uint32_t count = (uint32_t)L.size();
+        bool whole = count <= share;
+        uint32_t subs = whole ? 1 : std::max(1u, (SPPM_SUBS * share) / std::max(count, 1u));
+        T w = whole ? T(1) : T(SPPM_SUBS) / T(subs);
+        float u4[4];
+        rng.next4(u4);
+        uint32_t start = std::min((uint32_t)(u4[0] * (float)SPPM_SUBS), SPPM_SUBS - 1);
+        for (uint32_t j = 0; j < subs && !cut; j++) {
+            uint32_t s = (start + j) % SPPM_SUBS;
+            for (uint32_t idx : L) {
+                uint32_t b = g.flags[idx];
+                if (!whole && ((b >> SPPM_SUB_SHIFT) & (SPPM_SUBS - 1)) != s) continue;
+                if (visits >= hard) { cut = true; break; }
+                visits++;
+                const float* p = &g.pos[3 * idx];
+                int32_t pc[3];
+                sppm_cell(p, csz, pc);
+                if (pc[0] != cell[0] || pc[1] != cell[1] || pc[2] != cell[2]) continue;
+                float d[3] = {p[0] - x[0], p[1] - x[1], p[2] - x[2]};
+                float dd = d[0] * d[0] + d[1] * d[1];
+                dd = dd + d[2] * d[2];
+                if (dd > C.sp_r2) continue;
+                if (bc + (b & SPPM_B_MASK) > C.p.maxbounce + 1) continue;
+                float pn[3];
+                sppm_unoct(g.nrm[idx], pn);
+                float nd = pn[0] * nq[0] + pn[1] * nq[1];
+                nd = nd + pn[2] * nq[2];
+                if (nd < SPPM_NORMAL_DOT) continue;
+                float l[3];
+                sppm_unoct(g.dir[idx], l);
+                V3<T> f = lobes_eval(lb, V3<T>(T(l[0]), T(l[1]), T(l[2])), T(0.05));
+                sum += f * V3<T>(T(g.power[3 * idx]), T(g.power[3 * idx + 1]), T(g.power[3 * idx + 2])) * w;
+            }
+        }
+    }
+    return sum;
+}
+// lensStep (materials_pbr.js:862-873), a camera path's: at its first surface 1 for a delta event, else 0; 1 stays
+// 1 through a delta and goes to 2 at an evaluable event; 2 or 3 go to 3 through a delta; anything else to 0
+inline uint32_t lens_step(uint32_t lens, uint32_t bounces, uint32_t ev) {
+    const bool delta = ev == EV_DELTA;
+    if (bounces == 1) return delta ? 1u : 0u;
+    if (lens == 1) return delta ? 1u : (ev == EV_EVAL ? 2u : 0u);
+    return ((lens == 2 || lens == 3) && delta) ? 3u : 0u;
+}
+// sdf.js ltCovers: whether the sun's photons were drawn along this line (it crosses their square)
+template <class T> inline void sun_frame(const Env<T>& e, V3<T>& b1, V3<T>& b2) {
+    const V3<T> s = e.sun_dir;
+    const V3<T> t = std::fabs(s.x) > T(0.9) ? V3<T>(0, 1, 0) : V3<T>(1, 0, 0);
+    b1 = normalize(cross(t, s));
+    b2 = cross(s, b1);
+}
+template <class T> inline bool sppm_covers(const Ctx<T>& C, const V3<T>& p, const V3<T>& d) {
+    const V3<T> s = C.env.sun_dir;
+    const T ds = dot(d, s);
+    if (!(ds > T(0))) return false;
+    const V3<T> x = p - d * (dot(p, s) / ds);
+    V3<T> b1, b2;
+    sun_frame(C.env, b1, b2);
+    return std::fabs(dot(x, b1)) <= T(C.sp_half) && std::fabs(dot(x, b2)) <= T(C.sp_half);
+}
+
 // a path's hit, shaded: pathBegin..pathEnd (tracebasics.js:834-1100) with processMaterial_advanced
 // (materials_pbr.js:1110-1440). The light sample's shadow ray is traced here and its deposit made at once.
 template <class T>
-inline void shade_hit(const Ctx<T>& C, Ray<T>& r, T dhit, Rng& rng, bool last, Frame<T>& fr, Stats& st) {
+inline void shade_hit(const Ctx<T>& C, Ray<T>& r, T dhit, Rng& rng, Rng& grng, bool last, Frame<T>& fr, Stats& st) {
     V3<T> n = hit_normal(C, r.pos, dhit);
     bool inside = dhit < T(0);
     V3<T> nrm = inside ? -n : n;                                                   // scene_api.js:127-135 pathFacing
@@ -153,10 +261,18 @@ inline void shade_hit(const Ctx<T>& C, Ray<T>& r, T dhit, Rng& rng, bool last, F
         move_by(r, r.dir * otol);
         return;
     }
-    r.bounces += 1;
     SceneHit<T> h = scene_eval(*C.s, r.pos);
     const st_material& m = C.s->materials[std::min(h.m, C.s->n_materials - 1)];
     V3<T> emis(T(m.emissive[0]), T(m.emissive[1]), T(m.emissive[2]));
+    // THE PHOTON MAP'S GATHER (wavefront.js:1196-1212), before the shading: a camera ray with delta events only since
+    // the eye, on an evaluable surface, takes sum f Phi / (pi r^2) / n^2 into its radiance
+    if (C.sppm && r.lens == 1 && !(max3(emis) > T(0)) && sppm_evaluable(m, true)) {
+        T n0g = r.n;
+        Lobes<T> lg = make_lobes(nrm, -r.dir, m, n0g / std::max(T(m.ior), n0g), C.tb, T(m.transmission), T(m.specular));
+        V3<T> L = sppm_gather_lobes(C, r.pos, nrm, lg, r.bounces + 1, grng) * T(C.sp_inv_area / ((double)n0g * n0g));
+        r.rad += r.beta * L;
+    }
+    r.bounces += 1;
     if (max3(emis) > T(0)) {                                                       // materials_pbr.js:1014-1075 emitterHit
         r.rad += r.beta * emis;
         r.state = RAY_SOURCE;
@@ -235,6 +351,7 @@ inline void shade_hit(const Ctx<T>& C, Ray<T>& r, T dhit, Rng& rng, bool last, F
         r.n = nT;                                                                  // n(lambda) where it has one
         if (draw) { r.beta *= specW; r.lam = lamD; }
     }
+    if (C.sppm) r.lens = lens_step(r.lens, r.bounces, smp.ev);
     if (max3(smp.w) <= T(0)) r.state = RAY_ABSORBED;
     bool misOut = C.p.nee != 0 && !last;
     if (misOut) {                                                                  // materials_pbr.js:1370-1395
@@ -391,18 +508,22 @@ void trace_path(const Ctx<T>& C, U4 sseed, uint32_t tile, const st_view& v, uint
         it = std::min(it + chunks - 1, C.budget - 1);
         bool last = it + 1 == C.budget;
         st.segments++;
-        if (r.state == RAY_ESCAPED) {                                              // wavefront.js:1303-1320
-            r.rad += r.beta * C.env.radiance(r.dir) * r.sunmis;
+        if (r.state == RAY_ESCAPED) {                                              // wavefront.js:1292-1310
+            // a path the photon map owns (lens field 3) takes the sky but not the disc where the photons were drawn
+            bool owned = C.sppm && r.lens == 3 && sppm_covers(C, r.pos, r.dir);
+            r.rad += r.beta * (owned ? C.env.sky_only(r.dir) : C.env.radiance(r.dir)) * r.sunmis;
             break;
         }
         if (r.state != RAY_ACTIVE && r.state != RAY_SCATTER) break;                // out of steps or length
         Rng rng = path_rng(sseed, tile, 1 + seg);
+        Rng grng = path_rng(sseed, tile, SPPM_STORE_SALT + seg);                   // the gather's own stream
         seg++;
         r.absLtot = r.ltot;                                                        // absorbAlong on arrival
         if (r.state == RAY_SCATTER) {
             medium_vertex(C, r, rng, last, fr, st);
+            r.lens = 0;                                                            // haze.js:539
         } else {
-            shade_hit(C, r, dh, rng, last, fr, st);
+            shade_hit(C, r, dh, rng, grng, last, fr, st);
         }
         if (r.state != RAY_ACTIVE) break;
         r.tmax = T(0);                                                             // a new leg (wavefront.js:1375-1380)
@@ -531,6 +652,125 @@ template <> const MfTables* tables<double>() {
     return &g_tb_d;
 }
 
+// ONE SUN PHOTON (wavefront.js:596-626 prog_genphotons, then the wavefront's iterations with prog_sppm's store and a
+// photon's shade): a direction in the sun's cone, a point uniform over the square of half width sp_half across the
+// sun, flux L_disc cos Omega / (N pdf_area); at each hit stored where it has passed delta events only, at least one,
+// on an evaluable surface within the cap, else bounced -- a delta lobe keeps it, anything else ends it
+struct PhotonRec { float pos[3], power[3]; uint32_t dir, nrm, flags; };
+template <class T>
+void trace_photon(const Ctx<T>& C, U4 ps, uint32_t id, uint32_t N, std::vector<PhotonRec>& out, Stats& st) {
+    Rng r0 = path_rng(ps, id, PHOTON_GEN_SALT);
+    T u[4]; r0.next4(u);
+    V3<T> w = C.env.sample_sun_cone(u[0], u[1]);
+    const V3<T> sdir = C.env.sun_dir;
+    V3<T> b1, b2;
+    sun_frame(C.env, b1, b2);
+    const T R = T(C.sp_half);
+    const T x = -R + T(2) * R * u[2], y = -R + T(2) * R * u[3];
+    const T cosW = std::max(dot(w, sdir), T(1e-4));
+    const V3<T> q = b1 * x + b2 * y;
+    const T envR = T(C.d.env_radius);
+    Ray<T> r;
+    r.pos = q + w * ((envR - dot(q, sdir)) / cosW);
+    r.dir = -w;
+    r.beta = V3<T>(1);
+    V3<T> disc = C.env.sun_on ? C.env.radiance(w) : V3<T>(0);
+    r.rad = disc * (cosW * C.env.sun_omega * (T(4) * R * R) / T(N));
+    r.ltot = 0; r.n = 1; r.sunmis = 1; r.tmax = 0; r.absLtot = 0;
+    r.bounces = 0; r.steps = 0; r.state = RAY_ACTIVE; r.pix = id;
+    uint32_t it = 0, seg = 0;
+    while (it < C.budget) {
+        uint32_t evals = 0;
+        T dh = march(C, r, st, false, evals);
+        uint32_t chunks = std::max(1u, (evals + MARCH_CHUNK - 1) / MARCH_CHUNK);
+        it = std::min(it + chunks - 1, C.budget - 1);
+        bool last = it + 1 == C.budget;
+        if (r.state != RAY_ACTIVE) break;
+        V3<T> nn = hit_normal(C, r.pos, dh);
+        bool inside = dh < T(0);
+        V3<T> nrm = inside ? -nn : nn;
+        T otol = T(10) * march_tol(r.pos, C.tol);
+        if (dot(-r.dir, nrm) < T(0)) {                                             // leaving: moved on, no event
+            move_by(r, r.dir * otol);
+            if (last) break;
+            it++;
+            continue;
+        }
+        SceneHit<T> h = scene_eval(*C.s, r.pos);
+        const st_material& m = C.s->materials[std::min(h.m, C.s->n_materials - 1)];
+        if (std::max(std::max(m.emissive[0], m.emissive[1]), m.emissive[2]) > 0.f) break;
+        if (r.passed && sppm_evaluable(m, false)) {
+            V3<T> pw = r.rad * r.beta;
+            if (r.bounces + 2 <= C.p.maxbounce && luma(pw) > T(0)) {                 // sppm.js sppmStores / sppmStore
+                Rng rs = path_rng(ps, id, SPPM_STORE_SALT);
+                float us[4]; rs.next4(us);
+                uint32_t sub = std::min((uint32_t)(us[1] * (float)SPPM_SUBS), SPPM_SUBS - 1);
+                PhotonRec rec;
+                rec.pos[0] = (float)r.pos.x; rec.pos[1] = (float)r.pos.y; rec.pos[2] = (float)r.pos.z;
+                rec.power[0] = (float)pw.x; rec.power[1] = (float)pw.y; rec.power[2] = (float)pw.z;
+                float dv[3] = {(float)-r.dir.x, (float)-r.dir.y, (float)-r.dir.z};
+                float nv[3] = {(float)nrm.x, (float)nrm.y, (float)nrm.z};
+                rec.dir = sppm_oct(dv);
+                rec.nrm = sppm_oct(nv);
+                rec.flags = (r.bounces + 1) | (sub << SPPM_SUB_SHIFT);
+                out.push_back(rec);
+            }
+            break;
+        }
+        r.bounces += 1;
+        Rng rng = path_rng(ps, id, 1 + seg);
+        seg++;
+        T n0 = r.n, n1d = std::max(T(m.ior), n0), v1 = T(0);
+        if (m.transmission > 0 && m.metallic < 1) {
+            SceneHit<T> mb = scene_eval(*C.s, r.pos + (-nrm) * (otol * T(2)));
+            const st_material& mm = C.s->materials[std::min(mb.a, C.s->n_materials - 1)];
+            n1d = T(mm.ior);
+            v1 = T(mm.abbe);
+        }
+        const T lam0 = r.lam;
+        const T n1 = lam0 > T(0) ? cauchy_n(n1d, v1, lam0) : n1d;
+        const bool draw = v1 > T(0) && lam0 == T(0);
+        T nT = n1, lamD = T(0);
+        V3<T> specW(T(1), T(1), T(1));
+        if (draw) {
+            T ul[4]; rng.next4(ul);
+            lamD = lambda_coded(spec_draw(ul[0], specW));
+            nT = cauchy_n(n1d, v1, lamD);
+        }
+        T pG = refract_share<T>(m);
+        T trans = T(m.transmission), specv = T(m.specular);
+        bool diffFace = false;
+        if (inside && pG > T(0) && pG < T(1)) {
+            T k = mixT(T(2) * T(m.specular), T(1), pG);
+            T u4[4]; rng.next4(u4);
+            if (u4[0] < pG) trans = T(1);
+            else { trans = T(0); specv = T(0.5) * k; diffFace = true; }
+        }
+        T etaFace = diffFace ? std::min(n0, n1) / std::max(n0, n1) : n0 / n1;
+        Lobes<T> lb = make_lobes(nrm, -r.dir, m, etaFace, C.tb, trans, specv);
+        lb.etaT = n0 / nT;
+        T ur[4]; rng.next4(ur);
+        LobeSample<T> smp = lobes_sample(lb, ur);
+        r.dir = smp.dir;
+        r.beta *= smp.w;
+        if (smp.transmitted) {
+            r.n = nT;
+            if (draw) { r.beta *= specW; r.lam = lamD; }
+        }
+        move_by(r, r.dir * otol);
+        bool alive = max3(smp.w) > T(0) && smp.ev == EV_DELTA && r.bounces <= C.p.maxbounce;
+        if (alive && C.p.rr != 0 && r.bounces >= 3) {
+            T p = clampT(max3(r.beta), T(0.1), T(0.95));
+            T uu[4]; rng.next4(uu);
+            if (uu[0] > p) alive = false;
+            else r.beta = r.beta / p;
+        }
+        r.passed = true;
+        if (!alive || last) break;
+        it++;
+    }
+}
+
 template <class T>
 static int render_impl(const st_scene_desc* s, const st_params* p, const st_view* v, uint32_t sample0,
                        uint32_t nsamples, double* acc_rgb, double* mV, double* mS, uint32_t* acc_cnt,
@@ -555,10 +795,51 @@ static int render_impl(const st_scene_desc* s, const st_params* p, const st_view
     Frame<T> fr;
     fr.rgb.assign((size_t)P * 3, 0.0);
     fr.cnt.assign(P, 0);
+    // the photon map runs while it is set and the sun shines (its photons are the sun's)
+    const bool sppm_on = p->sppm != 0 && C.env.sun_on && p->env_uniform <= 0.f;
+    const uint32_t NPH = p->sppm_photons ? p->sppm_photons : P;
+    SppmGrid grid;
+    if (sppm_on) {
+        C.sppm = true;
+        C.grid = &grid;
+        C.sp_half = p->sppm_half > 0.f ? p->sppm_half : std::min(15.f, (float)C.d.env_radius);
+        C.sp_budget = 512;
+    }
     for (uint32_t si = 0; si < nsamples; si++) {
         U4 sseed = sample_seed(p->seed, sample0 + si);
         std::fill(fr.rgb.begin(), fr.rgb.end(), 0.0);
         std::fill(fr.cnt.begin(), fr.cnt.end(), 0u);
+        if (sppm_on) {
+            // THE SAMPLE'S PHOTONS FIRST: the radius r_k (k = the sample's number from 1), the photons traced and
+            // stored, the grid of cell 2 r_k built
+            const double r1 = p->sppm_r1 > 0.f ? p->sppm_r1 : 0.005, al = p->sppm_alpha > 0.f ? p->sppm_alpha : 2.0 / 3.0;
+            const double rk = sppm_radius(r1, (int)(sample0 + si + 1), al);
+            C.sp_r2 = (float)rk * (float)rk;
+            C.sp_cell = (float)(2.0 * rk);
+            C.sp_inv_area = 1.0 / (PI_D * rk * rk);
+            const U4 ps = sample_seed(p->seed ^ PHOTON_SEED_SALT, sample0 + si);
+            std::vector<std::vector<PhotonRec>> recs(1);
+#ifdef _OPENMP
+            recs.resize(omp_get_max_threads());
+#endif
+#pragma omp parallel for schedule(dynamic, 256)
+            for (long i = 0; i < (long)NPH; i++) {
+                int tid = 0;
+#ifdef _OPENMP
+                tid = omp_get_thread_num();
+#endif
+                trace_photon(C, ps, (uint32_t)i, NPH, recs[tid], st);
+            }
+            std::vector<float> pos, pw;
+            std::vector<uint32_t> dirs, nrms, flags;
+            for (auto& v : recs)
+                for (auto& rr : v) {
+                    for (int k = 0; k < 3; k++) { pos.push_back(rr.pos[k]); pw.push_back(rr.power[k]); }
+                    dirs.push_back(rr.dir); nrms.push_back(rr.nrm); flags.push_back(rr.flags);
+                }
+            sppm_build(grid, pos.data(), pw.data(), nrms.data(), flags.data(), (uint32_t)flags.size(), C.sp_cell);
+            grid.dir = dirs;
+        }
 #pragma omp parallel for schedule(dynamic, 64)
         for (long t = (long)path_first; t < (long)pend; t++) trace_path(C, sseed, (uint32_t)t, *v, W, H, fr, st);
         // resolve (wavefront.js:414-494, measure.js:36-51) in double precision
@@ -745,6 +1026,34 @@ void sto_step_moments(double* state, double x, double window) {
     state[0] = (prevY * prevn + x) / (prevn + 1);
     step_moments(prevn, x, prevY, state[1], state[2]);
     state[3] = prevn + 1;
+}
+// the photon pass of one sample alone (tests): the records' count, and their power summed over a box (lo, hi)
+int sto_sppm_photons(const st_scene_desc* s, const st_params* p, uint32_t sample, const float* lo, const float* hi,
+                     double* out) {
+    Ctx<float> C;
+    C.s = s; C.p = *p; C.d = derive(*p, *s);
+    C.env.init(*p, C.d);
+    C.tb = tables<float>();
+    C.tol = float(C.d.tol_setting);
+    C.envR2 = float(C.d.env_radius * C.d.env_radius);
+    C.stepscale = p->stepscale;
+    C.budget = p->budget ? p->budget : std::max(2u, p->maxbounce + 1 + (p->maxiter + 31) / 32);
+    C.haze.init(*s);
+    C.sppm = true;
+    C.sp_half = p->sppm_half > 0.f ? p->sppm_half : std::min(15.f, (float)C.d.env_radius);
+    const uint32_t N = p->sppm_photons ? p->sppm_photons : p->width * p->height;
+    const U4 ps = sample_seed(p->seed ^ PHOTON_SEED_SALT, sample);
+    Stats st;
+    std::vector<PhotonRec> recs;
+    for (uint32_t i = 0; i < N; i++) trace_photon(C, ps, i, N, recs, st);
+    double sum[3] = {0, 0, 0};
+    for (auto& r : recs) {
+        bool in = true;
+        for (int k = 0; k < 3; k++) in = in && r.pos[k] >= lo[k] && r.pos[k] <= hi[k];
+        if (in) for (int k = 0; k < 3; k++) sum[k] += r.power[k];
+    }
+    out[0] = (double)recs.size(); out[1] = sum[0]; out[2] = sum[1]; out[3] = sum[2];
+    return 0;
 }
 double sto_cauchy_n(double nd, double vd, double lam) { return cauchy_n<double>(nd, vd, lam); }
 uint32_t sto_lambda_code(double l) { return lambda_code(l); }

@@ -196,6 +196,11 @@ template <class T> struct Env {
         sky = T(p.sky_luminance); ground = T(p.ground_luminance); uniform = T(p.env_uniform);
         sun_gain = T(std::max(0.f, p.env_sun_gain)); sky_gain = T(std::max(0.f, p.env_sky_gain));
     }
+    V3<T> sky_only(const V3<T>& dir) const {                        // sdf.js skyRadiance: no disc
+        bool cone = sun_on && in_sun_disc(dir);
+        V3<T> b = uniform > T(0) ? V3<T>(uniform) : V3<T>(normalize(dir).z > T(0) ? sky : ground);
+        return b * (cone ? sun_gain : sky_gain);
+    }
     bool in_sun_disc(const V3<T>& dir) const {                       // sdf.js:91-96
         V3<T> L = normalize(dir);
         V3<T> c = cross(L, sun_dir);

@@ -79,7 +79,7 @@ inline void sppm_unoct(uint32_t w, float* out) {
 struct SppmGrid {
     float cell;
     std::vector<float> pos, power;
-    std::vector<uint32_t> nrm, flags, key;
+    std::vector<uint32_t> nrm, flags, key, dir;
     std::vector<std::vector<uint32_t>> lists;   // per hash: record indices, ascending
 };
 inline void sppm_build(SppmGrid& g, const float* pos, const float* power, const uint32_t* nrm, const uint32_t* flags,

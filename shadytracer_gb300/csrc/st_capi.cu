@@ -20,6 +20,8 @@
 #include "st_ext.h"
 #include "st_spectral.h"
 
+#define SPPM_WAVE_BUDGET 512u                 // records a gather walks before it subsamples (sppm.js SPPM_VISIT)
+
 using namespace st;
 
 namespace {
@@ -239,7 +241,10 @@ static DPrim pack_prim(const st_prim& p) {
     return d;
 }
 
+static bool sppm_runs(const st_ctx* ctx);
+static uint32_t sppm_photons(const st_ctx* ctx);
 static uint32_t samples_per_wave(const st_ctx* ctx) {
+    if (sppm_runs(ctx)) return 1;            // the photon map: each sample its own photons, radius and grid
     if (ctx->params.samples_per_wave) return ctx->params.samples_per_wave;
     const uint32_t target = 4u << 20;   // about four million paths a wave: twenty a lane of a full persistent grid
     uint32_t s = (target + ctx->P - 1) / ctx->P;
@@ -247,6 +252,11 @@ static uint32_t samples_per_wave(const st_ctx* ctx) {
 }
 
 static int ensure_wave(st_ctx* ctx) {
+    if (sppm_runs(ctx)) {
+        int rc = sppm_ensure(ctx, sppm_photons(ctx));
+        if (rc) return rc;
+        ctx_ext(ctx).sppm.wave = true;
+    }
     uint32_t spw = samples_per_wave(ctx);
     uint32_t cap = spw * ctx->P;
     bool pixels_changed = !ctx->d_acc;
@@ -296,6 +306,16 @@ static int ensure_wave(st_ctx* ctx) {
     return ST_OK;
 }
 
+// the photon map runs while it is set and the sun shines (its photons are the sun's)
+static bool sppm_runs(const st_ctx* ctx) {
+    if (!ctx->has_params || !ctx->params.sppm) return false;
+    const Uni u = make_uni(ctx);
+    return u.sun_on != 0 && ctx->params.env_uniform <= 0.f;
+}
+static uint32_t sppm_photons(const st_ctx* ctx) {
+    return ctx->params.sppm_photons ? ctx->params.sppm_photons : ctx->P;
+}
+
 static WaveArgs wave_args(st_ctx* ctx, uint32_t w) {
     WaveArgs a;
     a.u = make_uni(ctx);
@@ -312,6 +332,15 @@ static WaveArgs wave_args(st_ctx* ctx, uint32_t w) {
     a.mom = ctx->d_mom;
     a.spw = w;
     a.slots = w * ctx->P;
+    if (sppm_runs(ctx)) {
+        a.u.sppm_on = 1u;
+        a.u.sppm_n = sppm_photons(ctx);
+        a.u.sppm_budget = SPPM_WAVE_BUDGET;
+        a.u.sppm_half = ctx->params.sppm_half > 0.f ? ctx->params.sppm_half : std::min(15.f, a.u.envR);
+        a.u.sppm_r1 = ctx->params.sppm_r1 > 0.f ? ctx->params.sppm_r1 : 0.005f;
+        a.u.sppm_alpha = ctx->params.sppm_alpha > 0.f ? ctx->params.sppm_alpha : (float)(2.0 / 3.0);
+        a.sp = sppm_bufs(ctx_ext(ctx).sppm);
+    }
     return a;
 }
 
@@ -331,6 +360,36 @@ static cudaError_t record_wave(st_ctx* ctx, const WaveArgs& a) {
         return e;
     };
     cudaError_t e;
+    if (a.u.sppm_on) {
+        // THE SAMPLE'S PHOTONS FIRST (photons.js planBatches's `first`): in chunks of the wave's slots, each through
+        // the march, the surface kernel and the photon's shade; then the grid
+        ctx->rec_launches++;
+        if ((e = launch_sppm_begin(a, s))) return e;
+        const uint32_t N = a.u.sppm_n, C = a.slots;
+        for (uint32_t first = 0; first < N; first += C) {
+            WaveArgs pa = a;
+            pa.slots = std::min(C, N - first);
+            pa.u.haze_on = 0;                    // the map's photons cross the haze unscattered (no volume map)
+            ctx->rec_launches++;
+            if ((e = launch_iter_begin(pa, 0, 1, 1, s))) return e;
+            if ((e = timed("photons", [&] { return launch_genphotons(pa, first, pa.slots, ctx->sms, s); }))) return e;
+            int pc = 0;
+            for (uint32_t it = 0; it < pa.u.budget; it++) {
+                int nxt = pc ^ 1, last = it + 1 == pa.u.budget;
+                if (it > 0 && (++ctx->rec_launches, e = launch_iter_begin(pa, (int)it, nxt, 0, s))) return e;
+                if (pa.u.sort_on) {
+                    if ((e = timed("photon_sort", [&] { return launch_sort(pa, pc, ctx->sms, s); }))) return e;
+                    ctx->rec_launches += 2;
+                }
+                if ((e = timed("photon_march", [&] { return launch_march(pa, pc, nxt, last, ctx->sms, s); }))) return e;
+                if ((e = timed("photon_surface", [&] { return launch_surface(pa, ctx->sms, s); }))) return e;
+                if ((e = timed("photon_shade", [&] { return launch_photon_shade(pa, nxt, last, ctx->sms, s); }))) return e;
+                pc = nxt;
+            }
+        }
+        if ((e = timed("grid", [&] { return sppm_grid_launch(ctx_ext(ctx).sppm, ctx->sms, s); }))) return e;
+        ctx->rec_launches += 5;                                      // key, three scan phases, scatter
+    }
     ctx->rec_launches++;
     if ((e = launch_iter_begin(a, 0, 1, 1, s))) return e;
     if ((e = timed("genrays", [&] { return launch_genrays(a, ctx->sms, s); }))) return e;
@@ -346,6 +405,7 @@ static cudaError_t record_wave(st_ctx* ctx, const WaveArgs& a) {
         }
         if ((e = timed("march", [&] { return launch_march(a, cur, nxt, last, ctx->sms, s); }))) return e;
         if ((e = timed("surface", [&] { return launch_surface(a, ctx->sms, s); }))) return e;
+        if (a.u.sppm_on && (e = timed("gather", [&] { return launch_gather(a, ctx->sms, s); }))) return e;
         if ((e = timed("shade", [&] { return launch_shade(a, nxt, side, last, ctx->sms, s); }))) return e;
         if (a.u.sort_on) {
             if ((e = timed("sort", [&] { return launch_sort_shadow(a, side, ctx->sms, s); }))) return e;

@@ -110,6 +110,8 @@ struct Uni {
     uint32_t count_work;         // a counting pass: the march counts its fold's work (WC_*)
     // the march queue's space order (st_render.cu k_sort_*): a SORT_G^3 grid over the primitives' bounds
     uint32_t sort_on; f3 glo, ginv;
+    // the photon map (st_photons.cu): photons a sample, the sun photons' square, the radius schedule, the budget
+    uint32_t sppm_on, sppm_n, sppm_budget, sppm_seed; float sppm_half, sppm_r1, sppm_alpha;
 };
 
 // ------------------------------------------------------------------------------------------------------------
@@ -403,6 +405,24 @@ __device__ __forceinline__ f3 env_base(const Uni& u, f3 dir) {
 __device__ __forceinline__ f3 env_radiance(const Uni& u, f3 dir) {
     bool cone = u.sun_on && in_sun_disc(u, dir);
     return env_base(u, dir) * (cone ? u.sun_gain : u.sky_gain);
+}
+// the environment without the sun's disc (sdf.js skyRadiance): what a path the photon map owns finds there
+__device__ __forceinline__ f3 env_sky(const Uni& u, f3 dir) {
+    bool cone = u.sun_on && in_sun_disc(u, dir);
+    f3 base = u.uniform > 0.f ? mk(u.uniform) : mk(normalize(dir).z > 0.f ? u.sky : u.ground);
+    return base * (cone ? u.sun_gain : u.sky_gain);
+}
+// whether the sun's photons were drawn along this line (sdf.js ltCovers): it crosses the square of half width
+// sppm_half across the sun's direction through the origin
+__device__ __forceinline__ bool sppm_covers(const Uni& u, f3 p, f3 d) {
+    const f3 s = u.sun_dir;
+    const float ds = dot(d, s);
+    if (!(ds > 0.f)) return false;
+    const f3 x = p - d * (dot(p, s) / ds);
+    const f3 t = fabsf(s.x) > 0.9f ? mk(0, 1, 0) : mk(1, 0, 0);
+    const f3 b1 = normalize(cross(t, s));
+    const f3 b2 = cross(s, b1);
+    return fabsf(dot(x, b1)) <= u.sppm_half && fabsf(dot(x, b2)) <= u.sppm_half;
 }
 __device__ __forceinline__ f3 sample_sun_cone(const Uni& u, float u0, float u1) {
     f3 sd = u.sun_dir;

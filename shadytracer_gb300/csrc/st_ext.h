@@ -6,6 +6,7 @@
 #include <vector>
 #include <cuda_runtime.h>
 #include "st_device.cuh"
+#include "st_internal.h"
 
 struct st_ctx;
 
@@ -29,7 +30,14 @@ struct SppmState {
     uint32_t* snrm = nullptr;
     uint32_t* sflags = nullptr;
     uint32_t* stats = nullptr;   // gathers, cut, visits_max, visits lo, visits hi
+    uint32_t* bucket = nullptr;  // the sort's scratch: each record's bucket and rank in it
+    uint32_t* rank = nullptr;
+    st::SppmDev* dev = nullptr;  // the count, the capacity, the radius and cell on the device
+    bool wave = false;           // the wavefront's map ran last (st_sppm_stats_read reads its device state)
 };
+int sppm_ensure(st_ctx* ctx, uint32_t n);
+cudaError_t sppm_grid_launch(SppmState& s, int sms, cudaStream_t st);
+st::SppmBufs sppm_bufs(const SppmState& s);
 
 struct OpticsState {
     std::vector<st_optics_source> sources;

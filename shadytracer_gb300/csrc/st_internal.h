@@ -19,6 +19,11 @@ namespace st {
 // A MARCH CHUNK: the most SDF evaluations a ray takes in one launch of the march or the occlusion pass before it is
 // handed to the next iteration (the reference's MARCH_STEPS, wavefront.js:870, is 32); the last iteration's launches
 // march to the end. It bounds the tail a persistent launch spends on its longest rays.
+// meta.y's upper byte: the photon map's classes (materials_pbr.js lensField / TAG_PASSED)
+#define META_PASSED (1u << 24)            // a photon that has passed a delta event
+#define META_LENS_SHIFT 25u               // a camera path's lens field (2 bits): 1 delta events only since the eye,
+                                          // 2 at its D, 3 delta events since its D (the map owns the sun it reaches)
+#define META_LOW 0x00ffffffu
 #define SURF_NONE 0xffffu                 // hsurf: no medium asked (n1 is the material's own index of refraction)
 #define SURF_LEAVING 0xffffffffu          // hsurf: the surface seen from behind, the ray moved on
 #define SORT_G 16u                        // the march queue's space order: SORT_G^3 cells ...
@@ -76,6 +81,23 @@ struct DevCtr {
     unsigned long long work[WC_N];     // the march's fold, counted in a counting pass (WC_* in st_device.cuh)
 };
 
+// THE PHOTON MAP ON THE DEVICE (st_sppm.cu builds its grid, st_photons.cu stores and gathers): the sample's radius
+// and the records' count, then the records as stored and in cell order
+struct SppmDev {
+    uint32_t count, cap, dropped, gathers;   // records stored (may pass cap: the rest are dropped), capacity
+    float r, cell, inv_area, r2;              // this sample's radius, the grid's cell (2r), 1 / (pi r^2), r^2
+    unsigned long long visits, stores;
+};
+struct SppmBufs {
+    SppmDev* dev = nullptr;
+    uint32_t cap = 0;                         // the records' capacity
+    float4 *pos = nullptr, *power = nullptr;  // as stored: point, power
+    uint32_t *dir_oct = nullptr, *nrm_oct = nullptr, *flags = nullptr;
+    const uint32_t* start = nullptr;          // per (cell hash, sub-list) bucket: its first record in cell order
+    const float4 *spos = nullptr, *spow = nullptr;
+    const uint32_t *sdir = nullptr, *snrm = nullptr, *sflags = nullptr;
+};
+
 struct __align__(32) Acc4 { double x, y, z, w; };   // FP64 mean rgb + the sample count
 
 struct WaveArgs {
@@ -92,6 +114,7 @@ struct WaveArgs {
     uint32_t spw;       // samples in this wave
     uint32_t slots;     // spw * P
     const float4* spec = nullptr;         // the camera's wavelength table (SPEC_NCELLS cells: CDF, colour rgb)
+    SppmBufs sp;                          // the photon map, while it runs
     const uint2* inst_range = nullptr;   // a batch of instances (the optics bench): each one's [first, count) of the
                                          // table, the instance in meta.w; null for a picture
 };
@@ -102,6 +125,11 @@ cudaError_t launch_genrays(const WaveArgs& a, int sms, cudaStream_t s);
 cudaError_t launch_iter_begin(const WaveArgs& a, int it, int nxt, int first, cudaStream_t s);
 cudaError_t launch_surface(const WaveArgs& a, int sms, cudaStream_t s);
 cudaError_t launch_sort(const WaveArgs& a, int cur, int sms, cudaStream_t s);
+// the photon map in the wavefront (st_photons.cu)
+cudaError_t launch_sppm_begin(const WaveArgs& a, cudaStream_t s);
+cudaError_t launch_genphotons(const WaveArgs& a, uint32_t first, uint32_t n, int sms, cudaStream_t s);
+cudaError_t launch_photon_shade(const WaveArgs& a, int nxt, int last, int sms, cudaStream_t s);
+cudaError_t launch_gather(const WaveArgs& a, int sms, cudaStream_t s);
 cudaError_t launch_eval_sdf(const DPrim* prims, uint32_t n_prims, const float* pts, uint32_t n, float* out,
                             cudaStream_t s);
 cudaError_t launch_sort_shadow(const WaveArgs& a, int side, int sms, cudaStream_t s);

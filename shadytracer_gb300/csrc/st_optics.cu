@@ -159,7 +159,7 @@ __global__ void __launch_bounds__(256) k_opt_shade(OptArgs o, int nxt, int last)
             m4 = a.pb.meta[slot];
             pos = xyz(p4); ltot = p4.w; dir = xyz(d4); n = d4.w; beta = xyz(b4);
             const uint32_t inst = m4.w, id = m4.x;
-            uint32_t bounces = m4.y & 0xffu, state = m4.y >> 16;
+            uint32_t bounces = m4.y & 0xffu, state = (m4.y >> 16) & 0xffu;
             double* T = stot + inst * OPT_TOT;
             const float wIn = luma(beta);                             // optWeight: beta x radiance (1), as luminance
             if (state == RAY_ESCAPED) {                               // kernels.js:609-625

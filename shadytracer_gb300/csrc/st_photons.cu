@@ -1,0 +1,332 @@
+// st_photons.cu -- the photon map inside the wavefront (core/sppm.js, core/wavefront.js:519-626 prog_genphotons,
+// :1150-1235 prog_sppm) for sm_103a.
+//
+// THE REFERENCE runs a sample's photons before its camera rays through the same wavefront: sun photons are drawn
+// over a square across the sun's direction, marched, and at each hit either STORED -- a photon that has passed
+// delta events only (glass, mirrors), at least one, landing on a surface a camera connection can evaluate -- or
+// bounced; the sample's camera rays that have seen only delta events since the eye then GATHER the stored photons
+// where they land (sum f Phi / (pi r^2), over the evaluable lobes), the radius shrinking from sample to sample, and a
+// camera path that reaches the sun through delta events after its D leaves the disc's light to the map.
+//
+// HERE the same order inside one graph a sample: k_sppm_begin (the sample's radius, the count cleared), per chunk of
+// photons k_genphotons then the march / surface / k_photon_shade iterations (a photon that is stored, or scatters
+// off anything but a delta lobe, is done: it can never be stored again), the grid built by a counting sort
+// (st_sppm.cu sppm_grid_launch), then the camera's iterations with k_gather between the surface kernel and shade.
+// The photons' random numbers come from their own sample seed, the photon's id and its shade count; the gather's
+// from the path's own stream with a salt of its own, so the shading draws are the same with the map on or off.
+#include <algorithm>
+#include <cmath>
+
+#include "st_internal.h"
+#include "st_kernels.cuh"
+#include "st_sppm_dev.cuh"
+
+namespace st {
+
+#define PHOTON_SEED_SALT 0x50484F54u       // the photons' sample seed: the picture's seed xor this
+#define PHOTON_GEN_SALT 0x5A17u            // their draw at the source (wavefront.js:594 SEED_u32(0x5A17))
+#define SPPM_STORE_SALT 0x53505031u        // a store's and a gather's own stream (wavefront.js:1186)
+
+__device__ __forceinline__ uint4 photon_seed(const Uni& u, uint32_t sample) {
+    return sample_seed(u.seed ^ PHOTON_SEED_SALT, sample);
+}
+// sppmEvaluable (wavefront.js prog_sppm, sppm.js:441-444): a diffuse base, or gloss rough enough to evaluate
+__device__ __forceinline__ bool sppm_evaluable(const st_material& m, bool all) {
+    const float r = clampf(m.roughness, 0.f, 1.f);
+    return (1.f - m.metallic) * (1.f - sat(m.transmission)) > 0.f || r * r >= (all ? 1e-3f : LT_MIN_ALPHA);
+}
+
+// THE SAMPLE'S RADIUS (sppm.js:177-181): r_k^2 = r_1^2 prod_{i<k} (i + alpha) / (i + 1), k the sample's number from
+// 1; the grid's cell is 2 r; the count of records cleared
+__global__ void k_sppm_begin(SppmDev* __restrict__ d, const DevCtr* __restrict__ ctr, float r1, float alpha, uint32_t cap) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const uint32_t k = ctr->sample + 1u;
+    double s = 1.0;
+    for (uint32_t i = 1; i < k; i++) s *= (i + (double)alpha) / (i + 1.0);
+    const double r = (double)r1 * sqrt(s);
+    d->r = (float)r;
+    d->r2 = (float)r * (float)r;
+    d->cell = (float)(2.0 * r);
+    d->inv_area = (float)(1.0 / (3.14159265358979323846 * r * r));
+    d->count = 0u;
+    d->cap = cap;
+    d->dropped = 0u;
+}
+
+// THE SUN'S PHOTONS (wavefront.js:596-626): a direction in the sun's cone, a point uniform over the square of half
+// width sppm_half across the sun's direction (the reference's learned 128^2 map at its uniform start), the photon
+// started back along its line at the scene's radius, its flux L_disc cos Omega / (N pdf_area)
+__global__ void __launch_bounds__(256) k_genphotons(WaveArgs a, uint32_t first, uint32_t n) {
+    const Uni& u = a.u;
+    const uint4 ps = photon_seed(u, a.ctr->sample);
+    const f3 s = u.sun_dir;
+    const f3 t = fabsf(s.x) > 0.9f ? mk(0, 1, 0) : mk(1, 0, 0);
+    const f3 b1 = normalize(cross(t, s));
+    const f3 b2 = cross(s, b1);
+    const float R = u.sppm_half;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t id = first + i;
+        Rng rng = path_rng(ps, id, PHOTON_GEN_SALT);
+        const float4 r0 = rng.next();
+        const f3 w = sample_sun_cone(u, r0.x, r0.y);
+        const float x = -R + 2.f * R * r0.z, y = -R + 2.f * R * r0.w;      // the square, uniform
+        const float cosW = fmaxf(dot(w, s), 1e-4f);
+        const f3 q = b1 * x + b2 * y;
+        const f3 org = q + w * ((u.envR - dot(q, s)) / cosW);
+        const f3 disc = u.sun_on ? env_radiance(u, w) : mk(0.f);
+        const f3 flux = disc * (cosW * u.sun_omega * (4.f * R * R) / (float)u.sppm_n);
+        a.pb.pos[i] = make_float4(org.x, org.y, org.z, 0.f);
+        a.pb.dir[i] = make_float4(-w.x, -w.y, -w.z, 1.f);
+        a.pb.beta[i] = make_float4(1.f, 1.f, 1.f, 1.f);
+        a.pb.rad[i] = make_float4(flux.x, flux.y, flux.z, 0.f);          // a photon's radiance field is its flux
+        a.pb.meta[i] = make_uint4(id, meta_y(0, 0, RAY_ACTIVE), 0u, 0u);
+        a.pb.lam[i] = 0.f;
+        a.q.ray[0][i] = i;
+    }
+}
+
+// A PHOTON'S HIT (prog_sppm's store, then pathBegin..pathEnd for a photon): stored where it may be, else bounced --
+// no light sampling; a delta lobe keeps it in the map's class, anything else ends it
+__global__ void __launch_bounds__(256) k_photon_shade(WaveArgs a, int nxt, int last) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    __shared__ __align__(8) uint64_t mbar;
+    const Uni& u = a.u;
+    st_material* sm = reinterpret_cast<st_material*>(smem);
+    if (!stage_table(sm, a.mats, u.n_mats * (uint32_t)sizeof(st_material), &mbar, a.ctr)) return;
+    const uint32_t count = a.ctr->hitCount;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    const uint32_t nrounds = (count + stride - 1) / stride;
+    uint32_t* __restrict__ outq = nxt ? a.q.ray[1] : a.q.ray[0];
+    uint32_t* outc = nxt ? &a.ctr->rayCount[1] : &a.ctr->rayCount[0];
+    const uint4 ps = photon_seed(u, a.ctr->sample);
+    SppmDev* d = a.sp.dev;
+    for (uint32_t r = 0; r < nrounds; r++) {
+        const uint32_t q = r * stride + blockIdx.x * blockDim.x + threadIdx.x;
+        bool cont = false, store = false;
+        uint32_t slot = 0;
+        f3 pos = mk(0.f), dir = mk(0.f), beta = mk(0.f), rad = mk(0.f), nrm = mk(0.f);
+        float ltot = 0.f, n = 1.f, lam = 0.f;
+        uint4 m4 = make_uint4(0, 0, 0, 0);
+        uint32_t bounces = 0, sub = 0;
+        if (q < count) {
+            slot = a.q.hit[q];
+            const float dh = a.q.hitd[q];
+            const float4 p4 = a.pb.pos[slot], d4 = a.pb.dir[slot], b4 = a.pb.beta[slot], r4 = a.pb.rad[slot];
+            m4 = a.pb.meta[slot];
+            pos = xyz(p4); ltot = p4.w; dir = xyz(d4); n = d4.w; beta = xyz(b4); rad = xyz(r4);
+            bounces = m4.y & 0xffu;
+            const uint32_t state = (m4.y >> 16) & 0xffu;
+            if (state == RAY_ACTIVE) {
+                const float4 sf = a.q.hsurf[q];
+                const uint32_t ids = __float_as_uint(sf.w);
+                const f3 nn = xyz(sf);
+                nrm = dh < 0.f ? -nn : nn;
+                const float eps = march_tol(pos, u.tol), otol = 10.f * eps;
+                if (ids == SURF_LEAVING) {                            // seen from behind: moved on, no event
+                    const f3 off = dir * otol;
+                    pos = pos + off; ltot += length(off) * n;
+                    cont = !last;
+                } else {
+                    const st_material& m = sm[ids & 0xffffu];
+                    const bool emissive = fmaxf(fmaxf(m.emissive[0], m.emissive[1]), m.emissive[2]) > 0.f;
+                    const bool passed = (m4.y & META_PASSED) != 0u;
+                    if (emissive) {
+                    } else if (passed && sppm_evaluable(m, false)) {
+                        // STORED (sppm.js sppmStores / sppmStore): within the cap a gather can accept
+                        if (bounces + 2u <= u.maxbounce && luma(rad * beta) > 0.f) {
+                            Rng rs = path_rng(ps, m4.x, SPPM_STORE_SALT);
+                            const float4 us = rs.next();
+                            sub = min((uint32_t)(us.y * (float)SPPM_SUBS), SPPM_SUBS - 1u);
+                            store = true;
+                        }
+                    } else {
+                        lam = a.pb.lam[slot];
+                        bounces += 1;
+                        uint32_t seg = (m4.y >> 8) & 0xffu;
+                        Rng rng = path_rng(ps, m4.x, 1u + seg);
+                        seg += 1;
+                        const bool inside = dh < 0.f;
+                        float n0 = n, n1d = fmaxf(m.ior, n0), v1 = 0.f;
+                        if ((ids >> 16) != SURF_NONE) { n1d = sm[ids >> 16].ior; v1 = sm[ids >> 16].abbe; }
+                        const float lam0 = lam;
+                        const float n1 = lam0 > 0.f ? cauchy_n(n1d, v1, lam0) : n1d;
+                        const bool draw = v1 > 0.f && lam0 == 0.f;
+                        SpecDraw spec;
+                        float nT = n1;
+                        if (draw) {
+                            const float4 rl = rng.next();
+                            spec = spec_draw(a.spec, rl.x);
+                            spec.lam = lambda_coded(spec.lam);
+                            nT = cauchy_n(n1d, v1, spec.lam);
+                        }
+                        const float pG = sat(m.transmission);
+                        float trans = m.transmission, specv = m.specular;
+                        bool diffFace = false;
+                        if (inside && pG > 0.f && pG < 1.f) {
+                            const float k = mixf(2.f * m.specular, 1.f, pG);
+                            const float4 rp = rng.next();
+                            if (rp.x < pG) trans = 1.f;
+                            else { trans = 0.f; specv = 0.5f * k; diffFace = true; }
+                        }
+                        const float etaFace = diffFace ? fminf(n0, n1) / fmaxf(n0, n1) : n0 / n1;
+                        Lobes lb = make_lobes(nrm, -dir, m, etaFace, a.tab, trans, specv);
+                        lb.etaT = n0 / nT;
+                        const LobeSample smp = lobes_sample(lb, a.tab, rng.next());
+                        dir = smp.dir;
+                        beta = beta * smp.w;
+                        if (smp.transmitted) {
+                            n = nT;
+                            if (draw) { beta = beta * spec.w; lam = spec.lam; }
+                        }
+                        const f3 off = dir * otol;
+                        pos = pos + off; ltot += length(off) * n;
+                        // a delta event keeps it in the class (TAG_PASSED); anything else is its D: nothing more
+                        // can store it, so it ends here (the reference's photon goes on for light tracing only)
+                        bool alive = max3(smp.w) > 0.f && smp.ev == EV_DELTA && bounces <= u.maxbounce;
+                        if (alive && u.rr != 0u && bounces >= 3u) {
+                            const float p = clampf(max3(beta), 0.1f, 0.95f);
+                            const float4 rr = rng.next();
+                            if (rr.x > p) alive = false;
+                            else beta = beta / p;
+                        }
+                        m4.y = meta_y(bounces, seg, RAY_ACTIVE) | (m4.y & ~META_LOW) | META_PASSED;
+                        cont = alive && !last;
+                    }
+                }
+            }
+        }
+        const uint32_t at = warp_append(&d->count, store);
+        if (store) {
+            if (at < d->cap) {
+                const f3 pw = rad * beta;
+                a.sp.pos[at] = make_float4(pos.x, pos.y, pos.z, 0.f);
+                a.sp.power[at] = make_float4(pw.x, pw.y, pw.z, 0.f);
+                a.sp.dir_oct[at] = oct_word(-dir);
+                a.sp.nrm_oct[at] = oct_word(nrm);
+                a.sp.flags[at] = (bounces + 1u) | (sub << SPPM_SUB_SHIFT);
+            } else {
+                atomicAdd(&d->dropped, 1u);
+            }
+        }
+        const uint32_t rq = warp_append(outc, cont);
+        if (cont) {
+            a.pb.pos[slot] = f4(pos, ltot);
+            a.pb.dir[slot] = f4(dir, n);
+            a.pb.beta[slot] = make_float4(beta.x, beta.y, beta.z, 1.f);
+            a.pb.meta[slot] = m4;
+            if (lam != 0.f) a.pb.lam[slot] = lam;
+            outq[rq] = slot;
+        }
+    }
+}
+
+// THE GATHER (sppm.js:475-494 sppmGather, wavefront.js:1196-1212): a camera ray with delta events only since the
+// eye, at least one (its lens field 1), on an evaluable surface facing it, takes sum f(l_p -> v) Phi_p / (pi r^2)
+// over the records within r on a facing surface inside the bounce cap, over n^2, times its throughput, into its
+// radiance; the eight cells, each cell's records whole within its share of the budget, else m of its sub-lists
+__global__ void __launch_bounds__(256) k_gather(WaveArgs a) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    __shared__ __align__(8) uint64_t mbar;
+    const Uni& u = a.u;
+    st_material* sm = reinterpret_cast<st_material*>(smem);
+    if (!stage_table(sm, a.mats, u.n_mats * (uint32_t)sizeof(st_material), &mbar, a.ctr)) return;
+    const uint32_t count = a.ctr->hitCount;
+    const SppmDev* d = a.sp.dev;
+    const float cellsz = d->cell, r2 = d->r2, inv_area = d->inv_area;
+    const uint32_t nrec = min(d->count, d->cap);
+    if (nrec == 0u) return;
+    unsigned long long walked = 0;
+    for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < count; q += gridDim.x * blockDim.x) {
+        const uint32_t slot = a.q.hit[q];
+        const uint4 m4 = a.pb.meta[slot];
+        if (((m4.y >> 16) & 0xffu) != RAY_ACTIVE || ((m4.y >> META_LENS_SHIFT) & 3u) != 1u) continue;
+        const float4 sf = a.q.hsurf[q];
+        const uint32_t ids = __float_as_uint(sf.w);
+        if (ids == SURF_LEAVING) continue;
+        const st_material& m = sm[ids & 0xffffu];
+        if (fmaxf(fmaxf(m.emissive[0], m.emissive[1]), m.emissive[2]) > 0.f || !sppm_evaluable(m, true)) continue;
+        const float dh = a.q.hitd[q];
+        const f3 nrm = dh < 0.f ? -xyz(sf) : xyz(sf);
+        const float4 p4 = a.pb.pos[slot], d4 = a.pb.dir[slot];
+        const f3 x = xyz(p4), dir = xyz(d4);
+        const float n0 = d4.w;
+        const Lobes lb = make_lobes(nrm, -dir, m, n0 / fmaxf(m.ior, n0), a.tab, m.transmission, m.specular);
+        const uint32_t tile = slot % u.P, j = slot / u.P, seg = (m4.y >> 8) & 0xffu;
+        Rng rng = path_rng(sample_seed(u.seed, a.ctr->sample + j), tile, SPPM_STORE_SALT + seg);
+        int32_t c0[3], side[3];
+        const float gx[3] = {__fdiv_rn(x.x, cellsz), __fdiv_rn(x.y, cellsz), __fdiv_rn(x.z, cellsz)};
+        for (int k = 0; k < 3; k++) {
+            c0[k] = (int32_t)floorf(gx[k]);
+            side[k] = (__fsub_rn(gx[k], floorf(gx[k])) >= 0.5f) ? 1 : -1;
+        }
+        const uint32_t bc = (m4.y & 0xffu) + 1u;
+        const uint32_t share = max(1u, u.sppm_budget / 8u);
+        const unsigned long long hard = (unsigned long long)SPPM_VISIT_HARD * u.sppm_budget;
+        f3 sum = mk(0.f);
+        unsigned long long visits = 0;
+        bool cut = false;
+        for (uint32_t k = 0; k < 8 && !cut; k++) {
+            const int32_t cx = c0[0] + ((k & 1) ? side[0] : 0), cy = c0[1] + ((k & 2) ? side[1] : 0),
+                          cz = c0[2] + ((k & 4) ? side[2] : 0);
+            const uint32_t h = sppm_hash(cx, cy, cz);
+            const uint32_t a0 = a.sp.start[h * SPPM_SUBS], a1 = a.sp.start[(h + 1) * SPPM_SUBS];
+            const uint32_t cnt = a1 - a0;
+            const bool whole = cnt <= share;
+            const uint32_t subs = whole ? 1u : max(1u, (SPPM_SUBS * share) / max(cnt, 1u));
+            const float w = whole ? 1.f : (float)SPPM_SUBS / (float)subs;
+            const float4 rk = rng.next();
+            const uint32_t st0 = min((uint32_t)(rk.x * (float)SPPM_SUBS), SPPM_SUBS - 1);
+            for (uint32_t jj = 0; jj < subs && !cut; jj++) {
+                uint32_t lo, hi;
+                if (whole) { lo = a0; hi = a1; }
+                else { const uint32_t s = (st0 + jj) % SPPM_SUBS; lo = a.sp.start[h * SPPM_SUBS + s]; hi = a.sp.start[h * SPPM_SUBS + s + 1]; }
+                for (uint32_t rec = lo; rec < hi; rec++) {
+                    if (visits >= hard) { cut = true; break; }
+                    visits++;
+                    const float4 pp = a.sp.spos[rec];
+                    if (cell_of(pp.x, cellsz) != cx || cell_of(pp.y, cellsz) != cy || cell_of(pp.z, cellsz) != cz) continue;
+                    const float dx = __fsub_rn(pp.x, x.x), dy = __fsub_rn(pp.y, x.y), dz = __fsub_rn(pp.z, x.z);
+                    const float dd = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+                    if (dd > r2) continue;
+                    const uint32_t b = a.sp.sflags[rec];
+                    if (bc + (b & SPPM_B_MASK) > u.maxbounce + 1u) continue;
+                    const f3 pn = unoct(a.sp.snrm[rec]);
+                    const float nd = __fadd_rn(__fadd_rn(__fmul_rn(pn.x, nrm.x), __fmul_rn(pn.y, nrm.y)), __fmul_rn(pn.z, nrm.z));
+                    if (nd < SPPM_NORMAL_DOT) continue;
+                    const f3 f = lobes_eval(lb, a.tab, unoct(a.sp.sdir[rec]), LT_MIN_ALPHA);
+                    sum = sum + f * xyz(a.sp.spow[rec]) * w;
+                }
+            }
+        }
+        const f3 L = sum * (inv_area / (n0 * n0));
+        if (luma(L) != 0.f) {
+            const float4 r4 = a.pb.rad[slot];
+            const f3 b = xyz(a.pb.beta[slot]);
+            a.pb.rad[slot] = make_float4(r4.x + b.x * L.x, r4.y + b.y * L.y, r4.z + b.z * L.z, r4.w);
+        }
+        walked += visits;
+    }
+    for (int o = 16; o > 0; o >>= 1) walked += __shfl_down_sync(FULL_MASK, walked, o);
+    if ((threadIdx.x & 31u) == 0u && walked) atomicAdd(&a.sp.dev->visits, walked);
+}
+
+cudaError_t launch_sppm_begin(const WaveArgs& a, cudaStream_t s) {
+    k_sppm_begin<<<1, 32, 0, s>>>(a.sp.dev, a.ctr, a.u.sppm_r1, a.u.sppm_alpha, a.sp.cap);
+    return cudaGetLastError();
+}
+cudaError_t launch_genphotons(const WaveArgs& a, uint32_t first, uint32_t n, int sms, cudaStream_t s) {
+    k_genphotons<<<std::min((n + 255u) / 256u, (uint32_t)sms * 8u), 256, 0, s>>>(a, first, n);
+    return cudaGetLastError();
+}
+cudaError_t launch_photon_shade(const WaveArgs& a, int nxt, int last, int sms, cudaStream_t s) {
+    const size_t smem = a.u.n_mats * sizeof(st_material);
+    k_photon_shade<<<sms * 4, 256, smem, s>>>(a, nxt, last);
+    return cudaGetLastError();
+}
+cudaError_t launch_gather(const WaveArgs& a, int sms, cudaStream_t s) {
+    const size_t smem = a.u.n_mats * sizeof(st_material);
+    k_gather<<<sms * 4, 256, smem, s>>>(a);
+    return cudaGetLastError();
+}
+
+}  // namespace st

@@ -320,7 +320,7 @@ __global__ void __launch_bounds__(256, 4) k_march(WaveArgs a, int cur, int nxt, 
         if (fin || more) {
             a.pb.pos[slot] = make_float4(pos.x, pos.y, pos.z, ltot);
             uint4 m = a.pb.meta[slot];
-            m.y = (m.y & 0xffffu) | (state << 16);
+            m.y = (m.y & ~0x00ff0000u) | (state << 16);               // the classes above it kept
             m.z = steps;
             a.pb.meta[slot] = m;
             if (HAZE) a.pb.rad[slot].w = tmax;
@@ -363,7 +363,7 @@ __global__ void __launch_bounds__(256, 3) k_surface(WaveArgs a) {
     for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < count; q += gridDim.x * blockDim.x) {
         const uint32_t slot = a.q.hit[q];
         const uint4 m4 = a.pb.meta[slot];
-        if ((m4.y >> 16) != RAY_ACTIVE) continue;                     // escaped, out of steps, a haze collision
+        if (((m4.y >> 16) & 0xffu) != RAY_ACTIVE) continue;          // escaped, out of steps, a haze collision
         const float dh = a.q.hitd[q];
         const f3 pos = xyz(a.pb.pos[slot]);
         const f3 dir = xyz(a.pb.dir[slot]);
@@ -393,8 +393,8 @@ struct ShadowOut { bool valid; f3 org, dir, rad; float n; };
 
 __device__ __forceinline__ void shade_surface(const WaveArgs& a, const st_material* sm, float4 surf,
                                               f3& pos, f3& dir, float& ltot, float& n, f3& beta, float& sunmis,
-                                              f3& rad, uint32_t& bounces, uint32_t& state, float& lam, float dh,
-                                              Rng& rng, bool last, ShadowOut& sh) {
+                                              f3& rad, uint32_t& bounces, uint32_t& state, float& lam,
+                                              uint32_t& lens, float dh, Rng& rng, bool last, ShadowOut& sh) {
     const Uni& u = a.u;
     float eps = march_tol(pos, u.tol);
     const uint32_t ids = __float_as_uint(surf.w);
@@ -480,6 +480,12 @@ __device__ __forceinline__ void shade_surface(const WaveArgs& a, const st_materi
     if (smp.transmitted) {
         n = nT;                                                       // n(lambda) where the ray has a wavelength
         if (draw) { beta = beta * spec.w; lam = spec.lam; }           // ...and the one it was refracted at, kept
+    }
+    if (u.sppm_on) {                                                  // materials_pbr.js:862-873 lensStep
+        const bool delta = smp.ev == EV_DELTA;
+        if (bounces == 1u) lens = delta ? 1u : 0u;
+        else if (lens == 1u) lens = delta ? 1u : (smp.ev == EV_EVAL ? 2u : 0u);
+        else lens = ((lens == 2u || lens == 3u) && delta) ? 3u : 0u;
     }
     if (max3(smp.w) <= 0.f) state = RAY_ABSORBED;
     if (u.nee != 0u && !last) {                                       // the other half of MIS (:1370-1395)
@@ -575,22 +581,29 @@ __global__ void __launch_bounds__(256) k_shade(WaveArgs a, int nxt, int side, in
             m4 = a.pb.meta[slot];
             pos = xyz(p4); ltot = p4.w; dir = xyz(d4); n = d4.w; beta = xyz(b4); sunmis = b4.w;
             rad = xyz(r4); tmax = r4.w;
-            pix = m4.x; bounces = m4.y & 0xffu; seg = (m4.y >> 8) & 0xffu; state = m4.y >> 16;
+            pix = m4.x; bounces = m4.y & 0xffu; seg = (m4.y >> 8) & 0xffu; state = (m4.y >> 16) & 0xffu;
             gpix = (slot / u.P) * u.P + pix;                          // the pixel in the wave's frames
             if (state == RAY_ESCAPED) {
-                rad = rad + beta * env_radiance(u, dir) * sunmis;     // wavefront.js:1303-1320
+                // wavefront.js:1292-1310: a path the photon map owns (its lens field 3: delta events only since
+                // its D) takes the sky but not the disc, where the sun's photons were drawn along its line
+                const bool owned = u.sppm_on && ((m4.y >> META_LENS_SHIFT) & 3u) == 3u && sppm_covers(u, pos, dir);
+                rad = rad + beta * (owned ? env_sky(u, dir) : env_radiance(u, dir)) * sunmis;
             } else if (state == RAY_ACTIVE || state == RAY_SCATTER) {
                 uint32_t tile = slot % u.P, j = slot / u.P;
                 Rng rng = path_rng(sample_seed(u.seed, a.ctr->sample + j), tile, 1u + seg);
                 seg += 1;
                 m4.w = __float_as_uint(ltot);                         // absorbAlong: absLtot on arrival
-                if (state == RAY_SCATTER)
+                if (state == RAY_SCATTER) {
                     shade_medium(a, pos, dir, beta, sunmis, bounces, state, n, rng, last != 0, sh);
+                    m4.y &= ~(3u << META_LENS_SHIFT);                 // haze.js:539: the air is no delta event
+                }
                 else
                 {
                     lam = a.pb.lam[slot];
+                    uint32_t lens = (m4.y >> META_LENS_SHIFT) & 3u;
                     shade_surface(a, sm, a.q.hsurf[q], pos, dir, ltot, n, beta, sunmis, rad, bounces, state, lam,
-                                  dh, rng, last != 0, sh);
+                                  lens, dh, rng, last != 0, sh);
+                    m4.y = (m4.y & ~(3u << META_LENS_SHIFT)) | (lens << META_LENS_SHIFT);
                 }
                 if (state == RAY_ACTIVE) {
                     tmax = 0.f;                                       // a new leg
@@ -618,7 +631,7 @@ __global__ void __launch_bounds__(256) k_shade(WaveArgs a, int nxt, int side, in
             a.pb.beta[slot] = f4(beta, sunmis);
             a.pb.rad[slot] = f4(rad, tmax);
             if (lam != 0.f) a.pb.lam[slot] = lam;
-            m4.y = meta_y(bounces, seg, RAY_ACTIVE);
+            m4.y = meta_y(bounces, seg, RAY_ACTIVE) | (m4.y & ~META_LOW);
             a.pb.meta[slot] = m4;
             outq[rq] = slot;
         } else if (valid) {

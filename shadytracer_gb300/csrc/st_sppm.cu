@@ -19,15 +19,10 @@
 
 #include "st_ext.h"
 #include "st_internal.h"
+#include "st_sppm_dev.cuh"
 
 using namespace st;
 
-#define SPPM_HEADS (1u << 20)
-#define SPPM_SUBS 32u
-#define SPPM_BUCKETS (SPPM_HEADS * SPPM_SUBS)
-#define SPPM_VISIT_HARD 8u
-#define SPPM_SUB_SHIFT 16u
-#define SPPM_B_MASK 0xFFFFu
 #define SCAN_THREADS 256u
 #define SCAN_ITEMS 16u
 #define SCAN_TILE (SCAN_THREADS * SCAN_ITEMS)
@@ -36,34 +31,14 @@ using namespace st;
 
 namespace {
 
-// the cell's hash (sppm.js:383-386 sppmHash): 32-bit wrapping multiplies of the cell's coordinates
-__device__ __forceinline__ uint32_t sppm_hash(int32_t x, int32_t y, int32_t z) {
-    return (((uint32_t)x * 73856093u) ^ ((uint32_t)y * 19349663u) ^ ((uint32_t)z * 83492791u)) & (SPPM_HEADS - 1);
-}
-__device__ __forceinline__ int32_t cell_of(float p, float c) { return (int32_t)floorf(__fdiv_rn(p, c)); }
-
-// a direction from 32 bits (sppm.js:372-379 sppmUnoct): two 16-bit snorms, octahedral
-__device__ __forceinline__ float unsnorm16(uint32_t w) {
-    int16_t q = (int16_t)(uint16_t)(w & 0xFFFFu);
-    return fmaxf(__fdiv_rn((float)q, 32767.f), -1.f);
-}
-__device__ __forceinline__ f3 unoct(uint32_t w) {
-    float ex = unsnorm16(w), ey = unsnorm16(w >> 16);
-    float vx = ex, vy = ey, vz = __fsub_rn(__fsub_rn(1.f, fabsf(ex)), fabsf(ey));
-    if (vz < 0.f) {
-        float nx = __fmul_rn(__fsub_rn(1.f, fabsf(vy)), vx >= 0.f ? 1.f : -1.f);
-        float ny = __fmul_rn(__fsub_rn(1.f, fabsf(vx)), vy >= 0.f ? 1.f : -1.f);
-        vx = nx; vy = ny;
-    }
-    float l = __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(vx, vx), __fmul_rn(vy, vy)), __fmul_rn(vz, vz)));
-    return mk(__fdiv_rn(vx, l), __fdiv_rn(vy, l), __fdiv_rn(vz, l));
-}
-
 // THE KEYS: each record's cell hash, its bucket (hash, sub-list), its rank in the bucket
+// (the count and the cell are the device's: the wavefront's photons stored them there, or st_sppm_build)
 __global__ void __launch_bounds__(256) k_sppm_key(const float4* __restrict__ pos, const uint32_t* __restrict__ flags,
-                                                  uint32_t n, float cell, uint32_t* __restrict__ key,
+                                                  const SppmDev* __restrict__ d, uint32_t* __restrict__ key,
                                                   uint32_t* __restrict__ bucket, uint32_t* __restrict__ rank,
                                                   uint32_t* __restrict__ counts) {
+    const uint32_t n = min(d->count, d->cap);
+    const float cell = d->cell;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         float4 p = pos[i];
         uint32_t h = sppm_hash(cell_of(p.x, cell), cell_of(p.y, cell), cell_of(p.z, cell));
@@ -145,17 +120,20 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_apply(uint32_t* __restric
 
 // THE SCATTER: each record into its bucket's range at its rank, the records themselves permuted with it
 __global__ void __launch_bounds__(256) k_sppm_scatter(const uint32_t* __restrict__ bucket, const uint32_t* __restrict__ rank,
-                                                      const uint32_t* __restrict__ start, uint32_t n,
+                                                      const uint32_t* __restrict__ start, const SppmDev* __restrict__ d,
                                                       const float4* __restrict__ pos, const float4* __restrict__ pow,
-                                                      const uint32_t* __restrict__ nrm, const uint32_t* __restrict__ flags,
-                                                      uint32_t* __restrict__ order, float4* __restrict__ spos,
-                                                      float4* __restrict__ spow, uint32_t* __restrict__ snrm,
+                                                      const uint32_t* __restrict__ dir, const uint32_t* __restrict__ nrm,
+                                                      const uint32_t* __restrict__ flags, uint32_t* __restrict__ order,
+                                                      float4* __restrict__ spos, float4* __restrict__ spow,
+                                                      uint32_t* __restrict__ sdir, uint32_t* __restrict__ snrm,
                                                       uint32_t* __restrict__ sflags) {
+    const uint32_t n = min(d->count, d->cap);
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         uint32_t at = start[bucket[i]] + rank[i];
         order[at] = i;
         spos[at] = pos[i];
         spow[at] = pow[i];
+        sdir[at] = dir[i];
         snrm[at] = nrm[i];
         sflags[at] = flags[i];
     }
@@ -246,10 +224,15 @@ __global__ void __launch_bounds__(128) k_sppm_gather(const float* __restrict__ q
     atomicAdd(reinterpret_cast<unsigned long long*>(&stats[4]), visits);
 }
 
-int ensure(st_ctx* ctx, uint32_t n) {
+}  // namespace
+
+// the map's buffers for n records (kept, grown as needed)
+int sppm_ensure(st_ctx* ctx, uint32_t n) {
     SppmState& s = ctx_ext(ctx).sppm;
     auto fail = [&](const char* what) { ctx_set_error(ctx, what); return ST_ERR_OOM; };
     if (!s.cell_start) {
+        if (cudaMalloc(&s.dev, sizeof(SppmDev)) != cudaSuccess) return fail("cudaMalloc photon grid");
+        if (cudaMemset(s.dev, 0, sizeof(SppmDev)) != cudaSuccess) return fail("memset photon grid");
         if (cudaMalloc(&s.cell_start, (size_t)(SPPM_BUCKETS + SCAN_TILE) * 4) != cudaSuccess) return fail("cudaMalloc photon grid");
         if (cudaMalloc(&s.scan_part, (size_t)(SCAN_BLOCKS + 8) * 4) != cudaSuccess) return fail("cudaMalloc photon grid");
         if (cudaMalloc(&s.cell_count, (size_t)SPPM_HEADS * 4 * 2) != cudaSuccess) return fail("cudaMalloc photon grid");
@@ -257,22 +240,45 @@ int ensure(st_ctx* ctx, uint32_t n) {
     }
     if (n > s.cap) {
         void* ps[] = {s.pos, s.power, s.dir_oct, s.nrm_oct, s.flags, s.key, s.order, s.spos, s.spow, s.sdir,
-                      s.snrm, s.sflags};
+                      s.snrm, s.sflags, s.bucket, s.rank};
         for (void* p : ps) if (p) cudaFree(p);
         uint32_t cap = std::max(n, 1024u);
         bool ok = cudaMalloc(&s.pos, (size_t)cap * 16) == cudaSuccess && cudaMalloc(&s.power, (size_t)cap * 16) == cudaSuccess &&
                   cudaMalloc(&s.dir_oct, (size_t)cap * 4) == cudaSuccess && cudaMalloc(&s.nrm_oct, (size_t)cap * 4) == cudaSuccess &&
                   cudaMalloc(&s.flags, (size_t)cap * 4) == cudaSuccess && cudaMalloc(&s.key, (size_t)cap * 4) == cudaSuccess &&
                   cudaMalloc(&s.order, (size_t)cap * 4) == cudaSuccess && cudaMalloc(&s.spos, (size_t)cap * 16) == cudaSuccess &&
-                  cudaMalloc(&s.spow, (size_t)cap * 16) == cudaSuccess && cudaMalloc(&s.sdir, (size_t)cap * 4 * 2) == cudaSuccess &&
-                  cudaMalloc(&s.snrm, (size_t)cap * 4) == cudaSuccess && cudaMalloc(&s.sflags, (size_t)cap * 4) == cudaSuccess;
+                  cudaMalloc(&s.spow, (size_t)cap * 16) == cudaSuccess && cudaMalloc(&s.sdir, (size_t)cap * 4) == cudaSuccess &&
+                  cudaMalloc(&s.snrm, (size_t)cap * 4) == cudaSuccess && cudaMalloc(&s.sflags, (size_t)cap * 4) == cudaSuccess &&
+                  cudaMalloc(&s.bucket, (size_t)cap * 4) == cudaSuccess && cudaMalloc(&s.rank, (size_t)cap * 4) == cudaSuccess;
         if (!ok) { s.cap = 0; return fail("cudaMalloc photon records"); }
         s.cap = cap;
     }
     return ST_OK;
 }
 
-}  // namespace
+// THE GRID'S BUILD from the records the device holds (count and cell in s.dev): the buckets zeroed, the keys and
+// ranks, the three-phase scan, the scatter into cell order -- a fixed launch shape, so a graph can hold it
+cudaError_t sppm_grid_launch(SppmState& s, int sms, cudaStream_t st) {
+    cudaError_t e = cudaMemsetAsync(s.cell_start, 0, (size_t)(SPPM_BUCKETS + SCAN_TILE) * 4, st);
+    if (e) return e;
+    k_sppm_key<<<(uint32_t)sms * 16u, 256, 0, st>>>(s.pos, s.flags, s.dev, s.key, s.bucket, s.rank, s.cell_start);
+    k_scan_sums<<<SCAN_BLOCKS, SCAN_THREADS, 0, st>>>(s.cell_start, s.scan_part);
+    k_scan_partials<<<1, 1024, 0, st>>>(s.scan_part, SCAN_BLOCKS, s.cell_start + SPPM_BUCKETS);
+    k_scan_apply<<<SCAN_BLOCKS, SCAN_THREADS, 0, st>>>(s.cell_start, s.scan_part);
+    // the sentinel: the total, past the last bucket (k_scan_apply's last tile covers [SPPM_BUCKETS - SCAN_TILE, SPPM_BUCKETS))
+    k_sppm_scatter<<<(uint32_t)sms * 16u, 256, 0, st>>>(s.bucket, s.rank, s.cell_start, s.dev, s.pos, s.power, s.dir_oct,
+                                                       s.nrm_oct, s.flags, s.order, s.spos, s.spow, s.sdir, s.snrm,
+                                                       s.sflags);
+    return cudaGetLastError();
+}
+SppmBufs sppm_bufs(const SppmState& s) {
+    SppmBufs b;
+    b.dev = s.dev;
+    b.cap = s.cap;
+    b.pos = s.pos; b.power = s.power; b.dir_oct = s.dir_oct; b.nrm_oct = s.nrm_oct; b.flags = s.flags;
+    b.start = s.cell_start; b.spos = s.spos; b.spow = s.spow; b.sdir = s.sdir; b.snrm = s.snrm; b.sflags = s.sflags;
+    return b;
+}
 
 extern "C" {
 
@@ -281,7 +287,7 @@ int st_sppm_build(st_ctx* ctx, const float* pos, const float* power, const uint3
     if (!ctx || (n && (!pos || !power || !nrm_oct || !flags)) || !(cell > 0)) return ST_ERR_ARG;
     if (n > (1u << 28)) { ctx_set_error(ctx, "more than 2^28 photon records"); return ST_ERR_ARG; }
     cudaSetDevice(ctx_device(ctx));
-    int rc = ensure(ctx, n);
+    int rc = sppm_ensure(ctx, n);
     if (rc) return rc;
     SppmState& s = ctx_ext(ctx).sppm;
     cudaStream_t st = ctx_stream(ctx);
@@ -295,26 +301,20 @@ int st_sppm_build(st_ctx* ctx, const float* pos, const float* power, const uint3
         p4[i] = make_float4(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2], 0.f);
         w4[i] = make_float4(power[3 * i], power[3 * i + 1], power[3 * i + 2], 0.f);
     }
-    uint32_t* bucket = s.sdir;            // scratch: the bucket and the rank of each record
-    uint32_t* rank = s.sdir + s.cap;
-    if (!ck(cudaMemcpyAsync(s.pos, p4.data(), (size_t)n * 16, cudaMemcpyHostToDevice, st), "photon upload") ||
+    s.wave = false;
+    SppmDev hd{};
+    hd.count = n; hd.cap = s.cap; hd.cell = cell;
+    if (!ck(cudaMemcpyAsync(s.dev, &hd, sizeof(hd), cudaMemcpyHostToDevice, st), "photon upload") || !ck(cudaMemcpyAsync(s.pos, p4.data(), (size_t)n * 16, cudaMemcpyHostToDevice, st), "photon upload") ||
         !ck(cudaMemcpyAsync(s.power, w4.data(), (size_t)n * 16, cudaMemcpyHostToDevice, st), "photon upload") ||
         !ck(cudaMemcpyAsync(s.nrm_oct, nrm_oct, (size_t)n * 4, cudaMemcpyHostToDevice, st), "photon upload") ||
         !ck(cudaMemcpyAsync(s.flags, flags, (size_t)n * 4, cudaMemcpyHostToDevice, st), "photon upload") ||
-        !ck(cudaMemsetAsync(s.cell_start, 0, (size_t)(SPPM_BUCKETS + SCAN_TILE) * 4, st), "memset") ||
         !ck(cudaMemsetAsync(s.stats, 0, 8 * 4, st), "memset"))
         return ST_ERR_CUDA;
-    if (dir_oct && !ck(cudaMemcpyAsync(s.dir_oct, dir_oct, (size_t)n * 4, cudaMemcpyHostToDevice, st), "photon upload"))
+    if (!ck(dir_oct ? cudaMemcpyAsync(s.dir_oct, dir_oct, (size_t)n * 4, cudaMemcpyHostToDevice, st)
+                    : cudaMemsetAsync(s.dir_oct, 0, (size_t)n * 4, st), "photon upload"))
         return ST_ERR_CUDA;
-    const int sms = ctx_sms(ctx);
-    if (n) k_sppm_key<<<std::min((n + 255) / 256, (uint32_t)sms * 16u), 256, 0, st>>>(s.pos, s.flags, n, cell, s.key, bucket, rank, s.cell_start);
-    k_scan_sums<<<SCAN_BLOCKS, SCAN_THREADS, 0, st>>>(s.cell_start, s.scan_part);
-    k_scan_partials<<<1, 1024, 0, st>>>(s.scan_part, SCAN_BLOCKS, s.cell_start + SPPM_BUCKETS);
-    k_scan_apply<<<SCAN_BLOCKS, SCAN_THREADS, 0, st>>>(s.cell_start, s.scan_part);
-    // the sentinel: the total, past the last bucket (k_scan_apply's last tile covers [SPPM_BUCKETS - SCAN_TILE, SPPM_BUCKETS))
-    if (n) k_sppm_scatter<<<std::min((n + 255) / 256, (uint32_t)sms * 16u), 256, 0, st>>>(
-        bucket, rank, s.cell_start, n, s.pos, s.power, s.nrm_oct, s.flags, s.order, s.spos, s.spow, s.snrm, s.sflags);
-    if (!ck(cudaGetLastError(), "photon grid launch") || !ck(cudaStreamSynchronize(st), "photon grid")) return ST_ERR_CUDA;
+    if (!ck(sppm_grid_launch(s, ctx_sms(ctx), st), "photon grid launch") || !ck(cudaStreamSynchronize(st), "photon grid"))
+        return ST_ERR_CUDA;
     s.n = n;
     s.cell = cell;
     return ST_OK;
@@ -381,6 +381,17 @@ int st_sppm_stats_read(st_ctx* ctx, st_sppm_stats* out) {
     SppmState& s = ctx_ext(ctx).sppm;
     if (!s.stats) { *out = st_sppm_stats{}; return ST_OK; }
     cudaSetDevice(ctx_device(ctx));
+    if (s.wave) {                              // the wavefront's map: its last sample's records and walks
+        SppmDev d;
+        if (cudaStreamSynchronize(ctx_stream(ctx)) != cudaSuccess ||
+            cudaMemcpy(&d, s.dev, sizeof(d), cudaMemcpyDeviceToHost) != cudaSuccess)
+            return ST_ERR_CUDA;
+        *out = st_sppm_stats{};
+        out->stored = std::min(d.count, d.cap);
+        out->cut = d.dropped;
+        out->visits = d.visits;
+        return ST_OK;
+    }
     uint32_t h[8];
     if (cudaMemcpy(h, s.stats, 32, cudaMemcpyDeviceToHost) != cudaSuccess) return ST_ERR_CUDA;
     out->stored = s.n;

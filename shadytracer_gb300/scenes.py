@@ -249,6 +249,56 @@ def dispersive_furnace(width=64, height=64, ior=1.5168, abbe=40.0, sky=1000.0, m
 
 
 # ---------------------------------------------------------------------------------------------------------------
+# Config 3: the photon map (core/sppm.js) -- a caustic under glass, and its closed form through a pane.
+# ---------------------------------------------------------------------------------------------------------------
+def cauchy_glass(a=1.50, b_um2=0.0042):
+    """n(lambda) = a + b / lambda^2 (lambda in um) as the reference's materials take it: n_d and the Abbe number V_d
+    (spectral.js cauchyN goes through both)."""
+    ld, lf, lc = 0.58756, 0.48613, 0.65627
+    nd = a + b_um2 / ld ** 2
+    vd = (nd - 1.0) / (b_um2 * (1 / lf ** 2 - 1 / lc ** 2))
+    return nd, vd
+
+
+def sppm_caustic(width=1024, height=1024, photons=4_000_000, r1=0.005, alpha=0.7, maxbounce=8, seed=1,
+                 sun_elevation=50.0, sun_illuminance=100000.0, sky=3000.0, dispersion=True):
+    """Config 3: a glass sphere (r 0.3 m, n(lambda) = 1.50 + 0.0042 / lambda^2 um) on a diffuse floor (albedo 0.7) under
+    the sun and a sky; the photon map on: `photons` sun photons a sample over a 0.5 m square, first radius r1, alpha."""
+    nd, vd = cauchy_glass()
+    mats = [air(), glass((1.0, 1.0, 1.0), ior=nd, abbe=vd if dispersion else 0.0), diffuse((0.7, 0.7, 0.7))]
+    prims = [prim(ST_PRIM_SPHERE, pos=(0.0, 0.0, 0.3), params=(0.3,), material=1), prim(ST_PRIM_PLANE, material=2)]
+    s = Scene(prims, mats, env_radius=20.0, name="sppm-caustic")
+    s.params = default_params(width=width, height=height, maxbounce=maxbounce, seed=seed, sun_elevation=sun_elevation,
+                              sun_azimuth=200.0, sun_illuminance=sun_illuminance, sky_luminance=sky,
+                              ground_luminance=0.0, sppm=1, sppm_photons=photons, sppm_r1=r1, sppm_alpha=alpha,
+                              sppm_half=0.5)
+    s.view = look_at((1.2, -1.4, 1.3), (0.15, 0.3, 0.1), 45.0, width / height)
+    s.info = {"workload": "sppm-caustic-%dx%d" % (width, height), "photons": photons}
+    return s
+
+
+def sppm_pane(width=48, height=48, photons=400_000, r1=0.02, alpha=0.7, sun_elevation=60.0, ior=1.5, seed=1):
+    """The photon map's closed form: a clear pane (2 x 2 m, 2 cm thick, index `ior`) 0.5 m over a white-ish floor
+    (albedo 0.7) under the sun alone, seen from straight above through the pane's middle. The floor is a slab cut to
+    the pane's shadow (the sun at 60 degrees from +y puts it at y in [-1.29, 0.71]), so it is lit only through the
+    glass -- the map's light:
+        L = T(view) rho / pi * E_sun sin(elevation) T(sun),  T = (1 - F) / (1 + F) for a slab (every inner
+    reflection summed), F the dielectric Fresnel reflectance at the face's angle. (The light a floor inter-reflection
+    through the pane's underside brings is neither side's: the map stores a photon at its first D only, and light
+    sampling from the floor is blocked by the glass -- as in the reference.)"""
+    mats = [air(), glass((1.0, 1.0, 1.0), ior=ior), diffuse((0.7, 0.7, 0.7))]
+    prims = [prim(ST_PRIM_BOX, pos=(0.0, 0.0, 0.5), params=(1.0, 1.0, 0.01), material=1),
+             prim(ST_PRIM_BOX, pos=(0.0, -0.15, -0.05), params=(1.0, 0.85, 0.05), material=2)]
+    s = Scene(prims, mats, env_radius=20.0, name="sppm-pane")
+    s.params = default_params(width=width, height=height, maxbounce=8, seed=seed, sun_elevation=sun_elevation,
+                              sun_azimuth=0.0, sun_illuminance=100000.0, sky_luminance=0.0, ground_luminance=0.0,
+                              sppm=1, sppm_photons=photons, sppm_r1=r1, sppm_alpha=alpha, sppm_half=1.6)
+    s.view = look_at((0.0, 0.0, 3.0), (0.0, 0.0, 0.0), 12.0, width / height, up=(0.0, 1.0, 0.0))
+    s.info = {"ior": ior, "albedo": 0.7, "sun_elevation": sun_elevation, "E_sun": 100000.0}
+    return s
+
+
+# ---------------------------------------------------------------------------------------------------------------
 # Config 4: the haze box (lib/pathtracer/tests.js:1818-1866 'haze' row; core/haze.js).
 # ---------------------------------------------------------------------------------------------------------------
 def haze_furnace(width=64, height=64, sigma_t=0.2, g=0.0, albedo=1.0, sky=1000.0, maxbounce=32, seed=1):

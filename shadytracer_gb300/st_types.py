@@ -54,7 +54,9 @@ class StParams(C.Structure):
                 ("sun_illuminance", C.c_float), ("sky_luminance", C.c_float), ("ground_luminance", C.c_float),
                 ("env_uniform", C.c_float), ("env_sun_gain", C.c_float), ("env_sky_gain", C.c_float),
                 ("sun_hint", C.c_uint32), ("seed", C.c_uint32), ("maxaverages", C.c_uint32),
-                ("eps", C.c_float), ("budget", C.c_uint32), ("samples_per_wave", C.c_uint32)]
+                ("eps", C.c_float), ("budget", C.c_uint32), ("samples_per_wave", C.c_uint32),
+                ("sppm", C.c_uint32), ("sppm_photons", C.c_uint32), ("sppm_r1", C.c_float),
+                ("sppm_alpha", C.c_float), ("sppm_half", C.c_float)]
 
 
 class StView(C.Structure):
@@ -135,6 +137,11 @@ def default_params(**kw):
     p.eps = 0.0
     p.budget = 0
     p.samples_per_wave = 0
+    p.sppm = 0
+    p.sppm_photons = 0
+    p.sppm_r1 = 0.0
+    p.sppm_alpha = 0.0
+    p.sppm_half = 0.0
     for k, v in kw.items():
         if not hasattr(p, k):
             raise KeyError(k)

@@ -61,3 +61,19 @@ def test_scene_distance_is_a_distance():
     sep = np.linalg.norm(p - q, axis=1)
     assert np.all(np.abs(d - dq) <= sep * 1.05 + 1e-5)
     assert np.any(d < 0) and np.any(d > 0)
+
+
+def test_photon_map_pane_closed_form():
+    """The oracle's photon map (per sample: sun photons, stores past glass, the grid, the camera's gather) against the
+    pane's closed form T(view) rho / pi E_sun sin(elevation) T(sun)."""
+    import math
+    s = scenes.sppm_pane(width=32, height=32, photons=400_000, r1=0.03)
+    a = oracle.render(s, 4)
+    Fv = oracle.fresnel_dielectric(1.0, 1 / 1.5)
+    Fs = oracle.fresnel_dielectric(math.cos(math.radians(30)), 1 / 1.5)
+    cf = (1 - Fv) / (1 + Fv) * 0.7 / math.pi * 1e5 * math.sin(math.radians(60)) * (1 - Fs) / (1 + Fs)
+    assert abs(a.luma().mean() / cf - 1) < 0.03
+    # the stored photons' power over a patch of the floor is the slab's transmitted irradiance
+    n, pw = oracle.sppm_photons(s, 0, lo=(-0.3, -0.3, -0.01), hi=(0.3, 0.3, 0.01))
+    E = (pw @ np.array([0.2126, 0.7152, 0.0722])) / 0.36
+    assert abs(E / (1e5 * math.sin(math.radians(60)) * (1 - Fs) / (1 + Fs)) - 1) < 0.01
