@@ -19,6 +19,8 @@ cpu_baseline: the oracle (oracle/, the CPU restatement of the reference's path) 
        bounded band of the same picture's paths.
 --impl reference: the reference's own implementation cannot run here (JavaScript + WGSL through WebGPU); its CPU
        restatement, the oracle, is timed instead on the host's cores, on the same workload and metric.
+sppm: config 3, the photon map's caustic (1024^2, 4 M sun photons a pass, 64 passes): photons/s over the photon
+       pass's kernels, and the render's paths/s with the map on.
 optics: the batched optics bench (64 emitter + aspheric-lens instances, 120.2 M rays, FP64 far-field and lux
        tallies) in rays/s, with the tallies on the device (`value`) and read back every run (`e2e`).
 Multi-GPU (torchrun): replicas -- each rank renders the whole workload on its own GPU; value sums the ranks' paths
@@ -49,6 +51,7 @@ def parse():
     ap.add_argument("--small", action="store_true", help="a 480 x 270, 4-spp render (profiling runs)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
     ap.add_argument("--no-optics", action="store_true", help="skip the optics bench's rays/s leg")
+    ap.add_argument("--no-sppm", action="store_true", help="skip the photon map's photons/s leg")
     ap.add_argument("--spp", type=int, default=0, help="samples per pixel a step (profiling runs; default: 64)")
     return ap.parse_args()
 
@@ -264,6 +267,70 @@ def optics_leg(args, dev, with_cpu):
     return out
 
 
+def sppm_leg(args, dev, with_cpu):
+    """Config 3, the photon map: a dispersive glass sphere on a floor under the sun, 1024 x 1024, 4 M sun photons a
+    pass, r1 5 mm, alpha 0.7, 64 passes a render. `value`: photons/s over the photon pass's kernels (their CUDA-event
+    time: generation, sort, march, surface, store); `render`: the whole render's camera paths/s with the map on."""
+    import torch
+    from shadytracer_gb300 import scenes
+    from shadytracer_gb300.renderer import create_path_tracer
+    small = args.small
+    W = 256 if small else 1024
+    N = 250_000 if small else 4_000_000
+    passes = 8 if small else 64
+    s = scenes.sppm_caustic(width=W, height=W, photons=N, r1=0.005, alpha=0.7)
+    rt = create_path_tracer(s, device=dev)
+    stream = torch.cuda.ExternalStream(rt.stream(), device=torch.device("cuda", dev))
+    for _ in range(max(args.warmup, 3)):
+        rt.invalidate()
+        rt.step_async(2)
+        rt.sync()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    rt.invalidate()
+    e0.record(stream)
+    rt.step_async(passes)
+    e1.record(stream)
+    rt.sync()
+    render_ms = e0.elapsed_time(e1)
+    Lmean = float((rt.read_accum()[0] @ np.array([0.2126, 0.7152, 0.0722])).mean())
+    # the photon pass's own kernels, from per-kernel events over a few passes
+    rt.enable_kernel_times(True)
+    rt.reset_kernel_times()
+    rt.invalidate()
+    kp = 4
+    rt.step(kp)
+    kt = rt.kernel_times()
+    rt.enable_kernel_times(False)
+    ph_keys = ("photons", "photon_sort", "photon_march", "photon_surface", "photon_shade")
+    ph_ms = sum(kt.get(k, (0, 0.0))[1] for k in ph_keys)
+    tot_ms = sum(v[1] for v in kt.values()) or 1.0
+    import ctypes as _C
+    from shadytracer_gb300.st_types import StSppmStats
+    stt = StSppmStats()
+    rt.L.st_sppm_stats_read(rt.ctx, _C.byref(stt))
+    rt.close()
+    out = {"workload": "sppm caustic: glass sphere r 0.3 m (Cauchy 1.50 + 0.0042/um^2) on a floor (albedo 0.7) under "
+                       "the sun, %dx%d, %d sun photons a pass, r1 5 mm, alpha 0.7, %d passes" % (W, W, N, passes),
+           "metric": "photons/s", "value": N * kp / (ph_ms / 1e3) if ph_ms > 0 else None, "unit": "photons/s",
+           "photon_pass_share": ph_ms / tot_ms,
+           "render": {"metric": "Mpaths/s (with the photon pass)", "value": W * W * passes / (render_ms / 1e3) / 1e6,
+                      "ms_per_render": render_ms, "passes": passes, "photons_per_s_whole": N * passes / (render_ms / 1e3)},
+           "stored_per_pass": stt.stored, "dropped": stt.cut, "mean_luma": Lmean,
+           "kernel_share": {k: round(v[1] / tot_ms, 4) for k, v in kt.items()}}
+    if with_cpu:
+        from oracle import oracle
+        import os as _os
+        sc = scenes.sppm_caustic(width=W, height=W, photons=200_000, r1=0.005, alpha=0.7)
+        t0 = time.perf_counter()
+        n, _ = oracle.sppm_photons(sc, 0)
+        dt = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": 200_000 / dt, "unit": "photons/s", "cores": 1, "kind": "port",
+                               "sample": "one pass of 200000 sun photons of the same scene, single-threaded, %.1f s "
+                                         "(%d stored)" % (dt, n)}
+    return out
+
+
 def run_ours(args):
     rank, world, local = dist_env()
     import torch
@@ -419,6 +486,8 @@ def run_ours(args):
         line["cpu_baseline"] = cpu_baseline(s)
     elif rank == 0:
         line["cpu_baseline"] = None
+    if not args.no_sppm:
+        line["sppm"] = sppm_leg(args, dev, rank == 0 and world == 1 and not args.no_cpu)
     if not args.no_optics:
         line["optics"] = optics_leg(args, dev, rank == 0 and world == 1 and not args.no_cpu)
         if world > 1:

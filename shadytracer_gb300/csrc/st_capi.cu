@@ -370,6 +370,7 @@ static cudaError_t record_wave(st_ctx* ctx, const WaveArgs& a) {
             WaveArgs pa = a;
             pa.slots = std::min(C, N - first);
             pa.u.haze_on = 0;                    // the map's photons cross the haze unscattered (no volume map)
+            pa.u.sort_on = 0;                    // the sun's photons start in order already (parallel, on a square)
             ctx->rec_launches++;
             if ((e = launch_iter_begin(pa, 0, 1, 1, s))) return e;
             if ((e = timed("photons", [&] { return launch_genphotons(pa, first, pa.slots, ctx->sms, s); }))) return e;
