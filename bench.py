@@ -21,6 +21,8 @@ cpu_baseline: the oracle (oracle/, the CPU restatement of the reference's path) 
        restatement, the oracle, is timed instead on the host's cores, on the same workload and metric.
 sppm: config 3, the photon map's caustic (1024^2, 4 M sun photons a pass, 64 passes): photons/s over the photon
        pass's kernels, and the render's paths/s with the map on.
+time_to_rmse: seconds to 1 % relative RMSE against a closed form, the photon map guided by the learned emission map
+       vs plain.
 optics: the batched optics bench (64 emitter + aspheric-lens instances, 120.2 M rays, FP64 far-field and lux
        tallies) in rays/s, with the tallies on the device (`value`) and read back every run (`e2e`).
 Multi-GPU (torchrun): replicas -- each rank renders the whole workload on its own GPU; value sums the ranks' paths
@@ -331,6 +333,55 @@ def sppm_leg(args, dev, with_cpu):
     return out
 
 
+def rmse_leg(args, dev):
+    """Time to 1 % relative RMSE against the closed form, guided vs plain: the photon map's pane (a 0.5 m glass pane
+    over a floor lit only through it, the sun's photons drawn over a 4 m square), plain -- the photons uniform over the
+    square -- against guided -- drawn from the learned emission map (rebuilt every 4 passes from each cell's stores per
+    photon). RMSE over the picture's pixels of (L - closed form) / closed form; GPU time of the passes (CUDA events),
+    checked every 8 passes (every 64 past 512), up to 12288 passes."""
+    import torch
+    from oracle import oracle as _o        # the closed form's Fresnel term only (the checker's), not the path
+    from shadytracer_gb300 import scenes
+    from shadytracer_gb300.renderer import create_path_tracer
+    W = 64 if args.small else 128
+    N = 1_000_000 if args.small else 4_000_000
+    out = {"metric": "seconds to 1% relative RMSE vs the closed form", "unit": "s", "higher_is_better": False,
+           "workload": "sppm pane: 0.5 m pane 0.5 m over a floor lit only through it, sun at 75 deg, %dx%d, %d sun "
+                       "photons a pass over a 4 m square, r1 5 mm, alpha 0.7" % (W, W, N)}
+    for name, learn in (("plain", 0), ("guided", 1)):
+        s = scenes.sppm_pane(width=W, height=W, photons=N, r1=0.005, alpha=0.7, sun_elevation=75.0, pane_half=0.25,
+                             photon_half=2.0, vfov=3.5)
+        s.params.sppm_learn = learn
+        cf = scenes.sppm_pane_closed_form(s, _o.fresnel_dielectric)
+        rt = create_path_tracer(s, device=dev)
+        stream = torch.cuda.ExternalStream(rt.stream(), device=torch.device("cuda", dev))
+        rt.step(1)                                    # the graph captured
+        rt.invalidate()
+        ms, passes, rm, hit = 0.0, 0, None, None
+        curve = []
+        while passes < 12288:
+            k = 8 if passes < 512 else 64
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            rt.step_async(k)
+            e1.record(stream)
+            rt.sync()
+            ms += e0.elapsed_time(e1)
+            passes += k
+            L = rt.read_accum()[0] @ np.array([0.2126, 0.7152, 0.0722])
+            rm = float(np.sqrt(np.mean((L - cf) ** 2)) / cf)
+            if passes in (8, 32, 128, 512, 2048, 8192) or rm <= 0.01:
+                curve.append([passes, round(ms / 1e3, 3), round(rm, 4)])
+            if rm <= 0.01:
+                hit = ms / 1e3
+                break
+        rt.close()
+        out[name] = {"seconds": hit, "passes": passes, "rmse": rm, "curve": curve}
+    if out["plain"]["seconds"] and out["guided"]["seconds"]:
+        out["speedup"] = out["plain"]["seconds"] / out["guided"]["seconds"]
+    return out
+
+
 def run_ours(args):
     rank, world, local = dist_env()
     import torch
@@ -488,6 +539,7 @@ def run_ours(args):
         line["cpu_baseline"] = None
     if not args.no_sppm:
         line["sppm"] = sppm_leg(args, dev, rank == 0 and world == 1 and not args.no_cpu)
+        line["time_to_rmse"] = rmse_leg(args, dev)
     if not args.no_optics:
         line["optics"] = optics_leg(args, dev, rank == 0 and world == 1 and not args.no_cpu)
         if world > 1:

@@ -160,6 +160,9 @@ typedef struct st_params {
     float    sppm_r1;             /* the first sample's radius, metres (0: 5 mm)                    */
     float    sppm_alpha;          /* the radius schedule's alpha (0: 2/3)                           */
     float    sppm_half;           /* the sun photons' square, half width, metres (0: min(15, radius)) */
+    uint32_t sppm_learn;          /* 1: the sun's photons drawn from the learned 128^2 emission map
+                                   * (wavefront.js:628-711), rebuilt every 4 samples from each cell's
+                                   * stores per photon sent, mixed with a 20 % uniform floor; 0: uniform */
 } st_params;
 
 /* The camera, as genrays reads it (core/genrays.js:65-92): the basis from invView's columns and the

@@ -52,7 +52,61 @@ template <class T> struct Ctx {
     float sp_r2 = 0, sp_cell = 0, sp_half = 0;
     double sp_inv_area = 0;
     uint32_t sp_budget = 512;
+    // the learned emission map (wavefront.js:628-711): on, the photons sent and stored per cell, the CDF
+    bool sp_learn = false;
+    uint32_t* lt_emit = nullptr;
+    uint32_t* lt_hit = nullptr;
+    const float* lt_cdf = nullptr;
 };
+const uint32_t LT_G = 128, LT_N = LT_G * LT_G;
+const float LT_FLOOR_F = 0.2f;
+// ltSearch / ltMass (wavefront.js:520-536)
+inline uint32_t lt_search(const float* cdf, float u) {
+    uint32_t lo = 0, hi = LT_G - 1;
+    while (lo < hi) { uint32_t mid = (lo + hi) / 2; if (u < cdf[mid]) hi = mid; else lo = mid + 1; }
+    return lo;
+}
+inline float lt_mass(const float* cdf, uint32_t i) { return std::max(cdf[i] - (i ? cdf[i - 1] : 0.f), 0.f); }
+// prog_lt_build (wavefront.js:628-711): worth = stores / sent per cell, both halved; the floor mixed in; row CDF and
+// per-row conditional CDFs, in f32 as the kernel sums them
+inline void lt_build(uint32_t* emit, uint32_t* hit, float* cdf) {
+    std::vector<float> rowW(LT_G), rowP(LT_G);
+    for (uint32_t r = 0; r < LT_G; r++) {
+        float sum = 0.f;
+        for (uint32_t c = 0; c < LT_G; c++) {
+            uint32_t e = emit[r * LT_G + c], h = hit[r * LT_G + c];
+            float w = e > 0 ? (float)h / (float)e : 0.f;
+            cdf[r * LT_G + c] = w;
+            sum += w;
+            emit[r * LT_G + c] = e / 2;
+            hit[r * LT_G + c] = h / 2;
+        }
+        rowW[r] = sum;
+    }
+    float T = 0.f;
+    for (uint32_t r = 0; r < LT_G; r++) T += rowW[r];
+    const bool learned = T > 0.f;
+    for (uint32_t r = 0; r < LT_G; r++) {
+        float rp = learned ? (1.f - LT_FLOOR_F) * rowW[r] / std::max(T, 1e-30f) + LT_FLOOR_F / (float)LT_G : 1.f / (float)LT_G;
+        rowP[r] = rp;
+        float acc = 0.f;
+        for (uint32_t c = 0; c < LT_G; c++) {
+            float p = learned ? (1.f - LT_FLOOR_F) * cdf[r * LT_G + c] / std::max(T, 1e-30f) + LT_FLOOR_F / (float)LT_N
+                              : 1.f / (float)LT_N;
+            acc += p;
+            cdf[r * LT_G + c] = acc / rp;
+        }
+        cdf[r * LT_G + LT_G - 1] = 1.f;
+    }
+    float racc = 0.f;
+    for (uint32_t r = 0; r < LT_G; r++) { racc += rowP[r]; cdf[LT_N + r] = racc; }
+    cdf[LT_N + LT_G - 1] = 1.f;
+}
+inline void lt_uniform(float* cdf) {
+    for (uint32_t r = 0; r < LT_G; r++)
+        for (uint32_t c = 0; c < LT_G; c++) cdf[r * LT_G + c] = c + 1 == LT_G ? 1.f : (float)(c + 1) / LT_G;
+    for (uint32_t r = 0; r < LT_G; r++) cdf[LT_N + r] = r + 1 == LT_G ? 1.f : (float)(r + 1) / LT_G;
+}
 
 template <class T> struct Ray {
     V3<T> pos, dir, beta, rad;
@@ -224,11 +278,13 @@ inline V3<T> sppm_gather_lobes(const Ctx<T>& C, const V3<T>& X, const V3<T>& nrm
     }
     return sum;
 }
-// lensStep (materials_pbr.js:862-873), a camera path's: at its first surface 1 for a delta event, else 0; 1 stays
-// 1 through a delta and goes to 2 at an evaluable event; 2 or 3 go to 3 through a delta; anything else to 0
+// lensStep (materials_pbr.js:862-873), a camera path's: at its first surface 1 for a delta event, 2 for an
+// evaluable one (the map gathers there: light -> delta+ -> D -> eye, the reference's light tracer's class, is the
+// map's in this build), else 0; 1 stays 1 through a delta and goes to 2 at an evaluable event; 2 or 3 go to 3
+// through a delta; anything else to 0
 inline uint32_t lens_step(uint32_t lens, uint32_t bounces, uint32_t ev) {
     const bool delta = ev == EV_DELTA;
-    if (bounces == 1) return delta ? 1u : 0u;
+    if (bounces == 1) return delta ? 1u : (ev == EV_EVAL ? 2u : 0u);     // a D at the eye's first surface: gathered
     if (lens == 1) return delta ? 1u : (ev == EV_EVAL ? 2u : 0u);
     return ((lens == 2 || lens == 3) && delta) ? 3u : 0u;
 }
@@ -266,7 +322,7 @@ inline void shade_hit(const Ctx<T>& C, Ray<T>& r, T dhit, Rng& rng, Rng& grng, b
     V3<T> emis(T(m.emissive[0]), T(m.emissive[1]), T(m.emissive[2]));
     // THE PHOTON MAP'S GATHER (wavefront.js:1196-1212), before the shading: a camera ray with delta events only since
     // the eye, on an evaluable surface, takes sum f Phi / (pi r^2) / n^2 into its radiance
-    if (C.sppm && r.lens == 1 && !(max3(emis) > T(0)) && sppm_evaluable(m, true)) {
+    if (C.sppm && (r.bounces == 0 || r.lens == 1) && !(max3(emis) > T(0)) && sppm_evaluable(m, true)) {
         T n0g = r.n;
         Lobes<T> lg = make_lobes(nrm, -r.dir, m, n0g / std::max(T(m.ior), n0g), C.tb, T(m.transmission), T(m.specular));
         V3<T> L = sppm_gather_lobes(C, r.pos, nrm, lg, r.bounces + 1, grng) * T(C.sp_inv_area / ((double)n0g * n0g));
@@ -666,7 +722,25 @@ void trace_photon(const Ctx<T>& C, U4 ps, uint32_t id, uint32_t N, std::vector<P
     V3<T> b1, b2;
     sun_frame(C.env, b1, b2);
     const T R = T(C.sp_half);
-    const T x = -R + T(2) * R * u[2], y = -R + T(2) * R * u[3];
+    T x, y, area;
+    uint32_t cell = 0xffffffffu;
+    if (C.sp_learn) {                                                              // a cell by the map, a point in it
+        T u2[4]; r0.next4(u2);
+        const uint32_t row = lt_search(C.lt_cdf + LT_N, (float)u[2]);
+        const uint32_t col = lt_search(C.lt_cdf + row * LT_G, (float)u[3]);
+        const float pCell = lt_mass(C.lt_cdf + LT_N, row) * lt_mass(C.lt_cdf + row * LT_G, col);
+        const T csz = T(2) * R / T(LT_G);
+        x = -R + (T(col) + u2[0]) * csz;
+        y = -R + (T(row) + u2[1]) * csz;
+        area = csz * csz / T(std::max(pCell, 1e-30f));
+        cell = row * LT_G + col;
+#pragma omp atomic
+        C.lt_emit[cell]++;
+    } else {
+        x = -R + T(2) * R * u[2];
+        y = -R + T(2) * R * u[3];
+        area = T(4) * R * R;
+    }
     const T cosW = std::max(dot(w, sdir), T(1e-4));
     const V3<T> q = b1 * x + b2 * y;
     const T envR = T(C.d.env_radius);
@@ -675,7 +749,7 @@ void trace_photon(const Ctx<T>& C, U4 ps, uint32_t id, uint32_t N, std::vector<P
     r.dir = -w;
     r.beta = V3<T>(1);
     V3<T> disc = C.env.sun_on ? C.env.radiance(w) : V3<T>(0);
-    r.rad = disc * (cosW * C.env.sun_omega * (T(4) * R * R) / T(N));
+    r.rad = disc * (cosW * C.env.sun_omega * area / T(N));
     r.ltot = 0; r.n = 1; r.sunmis = 1; r.tmax = 0; r.absLtot = 0;
     r.bounces = 0; r.steps = 0; r.state = RAY_ACTIVE; r.pix = id;
     uint32_t it = 0, seg = 0;
@@ -714,6 +788,10 @@ void trace_photon(const Ctx<T>& C, U4 ps, uint32_t id, uint32_t N, std::vector<P
                 rec.nrm = sppm_oct(nv);
                 rec.flags = (r.bounces + 1) | (sub << SPPM_SUB_SHIFT);
                 out.push_back(rec);
+                if (cell < LT_N) {
+#pragma omp atomic
+                    C.lt_hit[cell]++;
+                }
             }
             break;
         }
@@ -805,6 +883,11 @@ static int render_impl(const st_scene_desc* s, const st_params* p, const st_view
         C.sp_half = p->sppm_half > 0.f ? p->sppm_half : std::min(15.f, (float)C.d.env_radius);
         C.sp_budget = 512;
     }
+    std::vector<uint32_t> lt_emit(LT_N, 0), lt_hit(LT_N, 0);
+    std::vector<float> lt_cdf(LT_N + LT_G);
+    lt_uniform(lt_cdf.data());
+    C.sp_learn = sppm_on && p->sppm_learn != 0;
+    C.lt_emit = lt_emit.data(); C.lt_hit = lt_hit.data(); C.lt_cdf = lt_cdf.data();
     for (uint32_t si = 0; si < nsamples; si++) {
         U4 sseed = sample_seed(p->seed, sample0 + si);
         std::fill(fr.rgb.begin(), fr.rgb.end(), 0.0);
@@ -818,6 +901,8 @@ static int render_impl(const st_scene_desc* s, const st_params* p, const st_view
             C.sp_cell = (float)(2.0 * rk);
             C.sp_inv_area = 1.0 / (PI_D * rk * rk);
             const U4 ps = sample_seed(p->seed ^ PHOTON_SEED_SALT, sample0 + si);
+            const uint32_t kk = sample0 + si;
+            if (C.sp_learn && kk > 0 && (kk & 3u) == 0) lt_build(lt_emit.data(), lt_hit.data(), lt_cdf.data());
             std::vector<std::vector<PhotonRec>> recs(1);
 #ifdef _OPENMP
             recs.resize(omp_get_max_threads());

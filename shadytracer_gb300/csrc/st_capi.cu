@@ -259,6 +259,8 @@ static int ensure_wave(st_ctx* ctx) {
     }
     uint32_t spw = samples_per_wave(ctx);
     uint32_t cap = spw * ctx->P;
+    // the photon map's photons run in chunks of the wave's slots: give them room for up to four million at once
+    if (sppm_runs(ctx)) cap = std::max(cap, std::min(sppm_photons(ctx), 4u << 20));
     bool pixels_changed = !ctx->d_acc;
     if (ctx->slot_cap == cap && ctx->spw == spw && !pixels_changed) return ST_OK;
     free_wave(ctx);
@@ -339,6 +341,7 @@ static WaveArgs wave_args(st_ctx* ctx, uint32_t w) {
         a.u.sppm_half = ctx->params.sppm_half > 0.f ? ctx->params.sppm_half : std::min(15.f, a.u.envR);
         a.u.sppm_r1 = ctx->params.sppm_r1 > 0.f ? ctx->params.sppm_r1 : 0.005f;
         a.u.sppm_alpha = ctx->params.sppm_alpha > 0.f ? ctx->params.sppm_alpha : (float)(2.0 / 3.0);
+        a.u.sppm_learn = ctx->params.sppm_learn ? 1u : 0u;
         a.sp = sppm_bufs(ctx_ext(ctx).sppm);
     }
     return a;
@@ -365,7 +368,8 @@ static cudaError_t record_wave(st_ctx* ctx, const WaveArgs& a) {
         // the march, the surface kernel and the photon's shade; then the grid
         ctx->rec_launches++;
         if ((e = launch_sppm_begin(a, s))) return e;
-        const uint32_t N = a.u.sppm_n, C = a.slots;
+        if (a.u.sppm_learn && (e = timed("lt_build", [&] { return launch_lt_build(a, s); }))) return e;
+        const uint32_t N = a.u.sppm_n, C = ctx->slot_cap;          // the slots the path state holds
         for (uint32_t first = 0; first < N; first += C) {
             WaveArgs pa = a;
             pa.slots = std::min(C, N - first);
@@ -618,6 +622,7 @@ int st_invalidate(st_ctx* ctx) {
     CK(cudaMemsetAsync(ctx->d_mom, 0, (size_t)ctx->P * sizeof(double2), ctx->stream), "memset");
     CK(cudaMemsetAsync(ctx->d_frame, 0, (size_t)ctx->slot_cap * sizeof(float4), ctx->stream), "memset");
     CK(cudaMemsetAsync(&ctx->d_ctr->sample, 0, sizeof(uint32_t), ctx->stream), "memset");
+    CK(sppm_lt_reset(ctx_ext(ctx).sppm, ctx->stream), "memset");     // the emission map starts over uniform
     ctx->samples = 0;
     return ST_OK;
 }

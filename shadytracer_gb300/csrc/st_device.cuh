@@ -111,7 +111,7 @@ struct Uni {
     // the march queue's space order (st_render.cu k_sort_*): a SORT_G^3 grid over the primitives' bounds
     uint32_t sort_on; f3 glo, ginv;
     // the photon map (st_photons.cu): photons a sample, the sun photons' square, the radius schedule, the budget
-    uint32_t sppm_on, sppm_n, sppm_budget, sppm_seed; float sppm_half, sppm_r1, sppm_alpha;
+    uint32_t sppm_on, sppm_n, sppm_budget, sppm_learn; float sppm_half, sppm_r1, sppm_alpha;
 };
 
 // ------------------------------------------------------------------------------------------------------------

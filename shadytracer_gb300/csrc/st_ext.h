@@ -34,8 +34,13 @@ struct SppmState {
     uint32_t* rank = nullptr;
     st::SppmDev* dev = nullptr;  // the count, the capacity, the radius and cell on the device
     bool wave = false;           // the wavefront's map ran last (st_sppm_stats_read reads its device state)
+    uint32_t* lt_emit = nullptr; // the learned emission map: photons sent, photons stored, the CDF
+    uint32_t* lt_hit = nullptr;
+    float* lt_cdf = nullptr;
+    std::vector<float> lt_uniform;   // the uniform CDF the map starts from (and returns to at an invalidate)
 };
 int sppm_ensure(st_ctx* ctx, uint32_t n);
+cudaError_t sppm_lt_reset(SppmState& s, cudaStream_t st);
 cudaError_t sppm_grid_launch(SppmState& s, int sms, cudaStream_t st);
 st::SppmBufs sppm_bufs(const SppmState& s);
 

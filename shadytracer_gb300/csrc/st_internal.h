@@ -96,7 +96,14 @@ struct SppmBufs {
     const uint32_t* start = nullptr;          // per (cell hash, sub-list) bucket: its first record in cell order
     const float4 *spos = nullptr, *spow = nullptr;
     const uint32_t *sdir = nullptr, *snrm = nullptr, *sflags = nullptr;
+    // the learned emission map (wavefront.js:628-711): per cell of the LT_GRID^2 square the photons sent and those
+    // stored, and the CDF the sun's photons are drawn from (LT_CELLS conditional row entries, then LT_GRID rows)
+    uint32_t *lt_emit = nullptr, *lt_hit = nullptr;
+    float* lt_cdf = nullptr;
 };
+#define LT_GRID 128u
+#define LT_CELLS (LT_GRID * LT_GRID)
+#define LT_FLOOR 0.2f
 
 struct __align__(32) Acc4 { double x, y, z, w; };   // FP64 mean rgb + the sample count
 
@@ -127,6 +134,7 @@ cudaError_t launch_surface(const WaveArgs& a, int sms, cudaStream_t s);
 cudaError_t launch_sort(const WaveArgs& a, int cur, int sms, cudaStream_t s);
 // the photon map in the wavefront (st_photons.cu)
 cudaError_t launch_sppm_begin(const WaveArgs& a, cudaStream_t s);
+cudaError_t launch_lt_build(const WaveArgs& a, cudaStream_t s);
 cudaError_t launch_genphotons(const WaveArgs& a, uint32_t first, uint32_t n, int sms, cudaStream_t s);
 cudaError_t launch_photon_shade(const WaveArgs& a, int nxt, int last, int sms, cudaStream_t s);
 cudaError_t launch_gather(const WaveArgs& a, int sms, cudaStream_t s);

@@ -53,6 +53,69 @@ __global__ void k_sppm_begin(SppmDev* __restrict__ d, const DevCtr* __restrict__
     d->dropped = 0u;
 }
 
+// THE LEARNED EMISSION MAP (wavefront.js:520-536 ltSearch / ltMass, :628-711 prog_lt_build). A cell's worth is its
+// stores per photon it sent (the reference's camera connections per photon; this build has no connections to the
+// camera, and a stored photon is what the map's camera rays use); both counts halve at every rebuild, so the map
+// forgets; the density is (1 - LT_FLOOR) worth / total + LT_FLOOR uniform, as a row CDF and per-row conditional
+// CDFs. One block of LT_GRID threads, a row each; run at a sample's start, every fourth sample from the fourth.
+__device__ __forceinline__ uint32_t lt_search(const float* __restrict__ cdf, float u) {
+    uint32_t lo = 0, hi = LT_GRID - 1u;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (u < cdf[mid]) hi = mid;
+        else lo = mid + 1;
+    }
+    return lo;
+}
+__device__ __forceinline__ float lt_mass(const float* __restrict__ cdf, uint32_t i) {
+    return fmaxf(cdf[i] - (i ? cdf[i - 1] : 0.f), 0.f);
+}
+__global__ void __launch_bounds__(LT_GRID) k_lt_build(SppmBufs b, const DevCtr* __restrict__ ctr) {
+    __shared__ float rowW[LT_GRID], rowP[LT_GRID];
+    __shared__ float total;
+    const uint32_t k = ctr->sample;
+    if (k == 0u || (k & 3u) != 0u) return;                           // every fourth sample
+    const uint32_t r = threadIdx.x, base = r * LT_GRID;
+    float sum = 0.f;
+    for (uint32_t c = 0; c < LT_GRID; c++) {
+        const uint32_t e = b.lt_emit[base + c], h = b.lt_hit[base + c];
+        const float w = e > 0u ? (float)h / (float)e : 0.f;
+        b.lt_cdf[base + c] = w;                                      // scratch: the raw worth
+        sum += w;
+        b.lt_emit[base + c] = e / 2u;                                // forget half
+        b.lt_hit[base + c] = h / 2u;
+    }
+    rowW[r] = sum;
+    __syncthreads();
+    if (r == 0) {
+        float t = 0.f;
+        for (uint32_t q = 0; q < LT_GRID; q++) t += rowW[q];
+        total = t;
+    }
+    __syncthreads();
+    const float T = total;
+    const bool learned = T > 0.f;
+    const float n = (float)LT_CELLS;
+    const float rp = learned ? (1.f - LT_FLOOR) * rowW[r] / fmaxf(T, 1e-30f) + LT_FLOOR / (float)LT_GRID : 1.f / (float)LT_GRID;
+    rowP[r] = rp;
+    float acc = 0.f;
+    for (uint32_t c = 0; c < LT_GRID; c++) {
+        const float p = learned ? (1.f - LT_FLOOR) * b.lt_cdf[base + c] / fmaxf(T, 1e-30f) + LT_FLOOR / n : 1.f / n;
+        acc += p;
+        b.lt_cdf[base + c] = acc / rp;                                // conditional on the row
+    }
+    b.lt_cdf[base + LT_GRID - 1u] = 1.f;
+    __syncthreads();
+    if (r == 0) {
+        float racc = 0.f;
+        for (uint32_t q = 0; q < LT_GRID; q++) {
+            racc += rowP[q];
+            b.lt_cdf[LT_CELLS + q] = racc;
+        }
+        b.lt_cdf[LT_CELLS + LT_GRID - 1u] = 1.f;
+    }
+}
+
 // THE SUN'S PHOTONS (wavefront.js:596-626): a direction in the sun's cone, a point uniform over the square of half
 // width sppm_half across the sun's direction (the reference's learned 128^2 map at its uniform start), the photon
 // started back along its line at the scene's radius, its flux L_disc cos Omega / (N pdf_area)
@@ -69,17 +132,34 @@ __global__ void __launch_bounds__(256) k_genphotons(WaveArgs a, uint32_t first, 
         Rng rng = path_rng(ps, id, PHOTON_GEN_SALT);
         const float4 r0 = rng.next();
         const f3 w = sample_sun_cone(u, r0.x, r0.y);
-        const float x = -R + 2.f * R * r0.z, y = -R + 2.f * R * r0.w;      // the square, uniform
+        float x, y, area;                                                // the point, and 1 / its density
+        uint32_t cell = 0xffffffffu;
+        if (u.sppm_learn) {                                              // a cell by the map, a point in it
+            const float4 r1 = rng.next();
+            const uint32_t row = lt_search(a.sp.lt_cdf + LT_CELLS, r0.z);
+            const uint32_t col = lt_search(a.sp.lt_cdf + row * LT_GRID, r0.w);
+            const float pCell = lt_mass(a.sp.lt_cdf + LT_CELLS, row) * lt_mass(a.sp.lt_cdf + row * LT_GRID, col);
+            const float csz = 2.f * R / (float)LT_GRID;
+            x = -R + ((float)col + r1.x) * csz;
+            y = -R + ((float)row + r1.y) * csz;
+            area = csz * csz / fmaxf(pCell, 1e-30f);
+            cell = row * LT_GRID + col;
+            atomicAdd(&a.sp.lt_emit[cell], 1u);
+        } else {                                                         // the square, uniform
+            x = -R + 2.f * R * r0.z;
+            y = -R + 2.f * R * r0.w;
+            area = 4.f * R * R;
+        }
         const float cosW = fmaxf(dot(w, s), 1e-4f);
         const f3 q = b1 * x + b2 * y;
         const f3 org = q + w * ((u.envR - dot(q, s)) / cosW);
         const f3 disc = u.sun_on ? env_radiance(u, w) : mk(0.f);
-        const f3 flux = disc * (cosW * u.sun_omega * (4.f * R * R) / (float)u.sppm_n);
+        const f3 flux = disc * (cosW * u.sun_omega * area / (float)u.sppm_n);
         a.pb.pos[i] = make_float4(org.x, org.y, org.z, 0.f);
         a.pb.dir[i] = make_float4(-w.x, -w.y, -w.z, 1.f);
         a.pb.beta[i] = make_float4(1.f, 1.f, 1.f, 1.f);
         a.pb.rad[i] = make_float4(flux.x, flux.y, flux.z, 0.f);          // a photon's radiance field is its flux
-        a.pb.meta[i] = make_uint4(id, meta_y(0, 0, RAY_ACTIVE), 0u, 0u);
+        a.pb.meta[i] = make_uint4(id, meta_y(0, 0, RAY_ACTIVE), 0u, cell);   // w: its emission cell
         a.pb.lam[i] = 0.f;
         a.q.ray[0][i] = i;
     }
@@ -204,6 +284,7 @@ __global__ void __launch_bounds__(256) k_photon_shade(WaveArgs a, int nxt, int l
                 a.sp.dir_oct[at] = oct_word(-dir);
                 a.sp.nrm_oct[at] = oct_word(nrm);
                 a.sp.flags[at] = (bounces + 1u) | (sub << SPPM_SUB_SHIFT);
+                if (m4.w < LT_CELLS) atomicAdd(&a.sp.lt_hit[m4.w], 1u);     // teach the map: this cell paid
             } else {
                 atomicAdd(&d->dropped, 1u);
             }
@@ -221,7 +302,9 @@ __global__ void __launch_bounds__(256) k_photon_shade(WaveArgs a, int nxt, int l
 }
 
 // THE GATHER (sppm.js:475-494 sppmGather, wavefront.js:1196-1212): a camera ray with delta events only since the
-// eye, at least one (its lens field 1), on an evaluable surface facing it, takes sum f(l_p -> v) Phi_p / (pi r^2)
+// eye (its lens field 1) -- or at the eye's first surface: the class light -> delta+ -> D -> eye, which the
+// reference hands to its light tracer (CLS_CAND | CLS_SPEC) and this build, which has none, to the map -- on an
+// evaluable surface facing it, takes sum f(l_p -> v) Phi_p / (pi r^2)
 // over the records within r on a facing surface inside the bounce cap, over n^2, times its throughput, into its
 // radiance; the eight cells, each cell's records whole within its share of the budget, else m of its sub-lists
 __global__ void __launch_bounds__(256) k_gather(WaveArgs a) {
@@ -239,7 +322,9 @@ __global__ void __launch_bounds__(256) k_gather(WaveArgs a) {
     for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < count; q += gridDim.x * blockDim.x) {
         const uint32_t slot = a.q.hit[q];
         const uint4 m4 = a.pb.meta[slot];
-        if (((m4.y >> 16) & 0xffu) != RAY_ACTIVE || ((m4.y >> META_LENS_SHIFT) & 3u) != 1u) continue;
+        // the eye's first surface, or delta events only since the eye (lens field 1)
+        if (((m4.y >> 16) & 0xffu) != RAY_ACTIVE) continue;
+        if ((m4.y & 0xffu) != 0u && ((m4.y >> META_LENS_SHIFT) & 3u) != 1u) continue;
         const float4 sf = a.q.hsurf[q];
         const uint32_t ids = __float_as_uint(sf.w);
         if (ids == SURF_LEAVING) continue;
@@ -312,6 +397,10 @@ __global__ void __launch_bounds__(256) k_gather(WaveArgs a) {
 
 cudaError_t launch_sppm_begin(const WaveArgs& a, cudaStream_t s) {
     k_sppm_begin<<<1, 32, 0, s>>>(a.sp.dev, a.ctr, a.u.sppm_r1, a.u.sppm_alpha, a.sp.cap);
+    return cudaGetLastError();
+}
+cudaError_t launch_lt_build(const WaveArgs& a, cudaStream_t s) {
+    k_lt_build<<<1, LT_GRID, 0, s>>>(a.sp, a.ctr);
     return cudaGetLastError();
 }
 cudaError_t launch_genphotons(const WaveArgs& a, uint32_t first, uint32_t n, int sms, cudaStream_t s) {

@@ -483,7 +483,8 @@ __device__ __forceinline__ void shade_surface(const WaveArgs& a, const st_materi
     }
     if (u.sppm_on) {                                                  // materials_pbr.js:862-873 lensStep
         const bool delta = smp.ev == EV_DELTA;
-        if (bounces == 1u) lens = delta ? 1u : 0u;
+        // the first surface: 1 through a delta; a D there was gathered, so 2 (the reference's light tracer's class)
+        if (bounces == 1u) lens = delta ? 1u : (smp.ev == EV_EVAL ? 2u : 0u);
         else if (lens == 1u) lens = delta ? 1u : (smp.ev == EV_EVAL ? 2u : 0u);
         else lens = ((lens == 2u || lens == 3u) && delta) ? 3u : 0u;
     }

@@ -237,6 +237,16 @@ int sppm_ensure(st_ctx* ctx, uint32_t n) {
         if (cudaMalloc(&s.scan_part, (size_t)(SCAN_BLOCKS + 8) * 4) != cudaSuccess) return fail("cudaMalloc photon grid");
         if (cudaMalloc(&s.cell_count, (size_t)SPPM_HEADS * 4 * 2) != cudaSuccess) return fail("cudaMalloc photon grid");
         if (cudaMalloc(&s.stats, 8 * 4) != cudaSuccess) return fail("cudaMalloc photon grid");
+        if (cudaMalloc(&s.lt_emit, LT_CELLS * 4) != cudaSuccess || cudaMalloc(&s.lt_hit, LT_CELLS * 4) != cudaSuccess ||
+            cudaMalloc(&s.lt_cdf, (LT_CELLS + LT_GRID) * 4) != cudaSuccess)
+            return fail("cudaMalloc emission map");
+        // the uniform map: each row's conditional CDF (c + 1) / G, the rows' CDF likewise
+        s.lt_uniform.assign(LT_CELLS + LT_GRID, 0.f);
+        for (uint32_t r = 0; r < LT_GRID; r++)
+            for (uint32_t c = 0; c < LT_GRID; c++) s.lt_uniform[r * LT_GRID + c] = c + 1 == LT_GRID ? 1.f : (float)(c + 1) / LT_GRID;
+        for (uint32_t r = 0; r < LT_GRID; r++) s.lt_uniform[LT_CELLS + r] = r + 1 == LT_GRID ? 1.f : (float)(r + 1) / LT_GRID;
+        if (sppm_lt_reset(s, ctx_stream(ctx)) != cudaSuccess || cudaStreamSynchronize(ctx_stream(ctx)) != cudaSuccess)
+            return fail("emission map reset");
     }
     if (n > s.cap) {
         void* ps[] = {s.pos, s.power, s.dir_oct, s.nrm_oct, s.flags, s.key, s.order, s.spos, s.spow, s.sdir,
@@ -271,11 +281,20 @@ cudaError_t sppm_grid_launch(SppmState& s, int sms, cudaStream_t st) {
                                                        s.sflags);
     return cudaGetLastError();
 }
+// the emission map back to uniform, its counts cleared (raytrace_main.js:347, a reset)
+cudaError_t sppm_lt_reset(SppmState& s, cudaStream_t st) {
+    if (!s.lt_cdf) return cudaSuccess;
+    cudaError_t e = cudaMemsetAsync(s.lt_emit, 0, LT_CELLS * 4, st);
+    if (!e) e = cudaMemsetAsync(s.lt_hit, 0, LT_CELLS * 4, st);
+    if (!e) e = cudaMemcpyAsync(s.lt_cdf, s.lt_uniform.data(), (LT_CELLS + LT_GRID) * 4, cudaMemcpyHostToDevice, st);
+    return e;
+}
 SppmBufs sppm_bufs(const SppmState& s) {
     SppmBufs b;
     b.dev = s.dev;
     b.cap = s.cap;
     b.pos = s.pos; b.power = s.power; b.dir_oct = s.dir_oct; b.nrm_oct = s.nrm_oct; b.flags = s.flags;
+    b.lt_emit = s.lt_emit; b.lt_hit = s.lt_hit; b.lt_cdf = s.lt_cdf;
     b.start = s.cell_start; b.spos = s.spos; b.spow = s.spow; b.sdir = s.sdir; b.snrm = s.snrm; b.sflags = s.sflags;
     return b;
 }

@@ -277,7 +277,8 @@ def sppm_caustic(width=1024, height=1024, photons=4_000_000, r1=0.005, alpha=0.7
     return s
 
 
-def sppm_pane(width=48, height=48, photons=400_000, r1=0.02, alpha=0.7, sun_elevation=60.0, ior=1.5, seed=1):
+def sppm_pane(width=48, height=48, photons=400_000, r1=0.02, alpha=0.7, sun_elevation=60.0, ior=1.5, seed=1,
+              pane_half=1.0, photon_half=1.6, vfov=12.0):
     """The photon map's closed form: a clear pane (2 x 2 m, 2 cm thick, index `ior`) 0.5 m over a white-ish floor
     (albedo 0.7) under the sun alone, seen from straight above through the pane's middle. The floor is a slab cut to
     the pane's shadow (the sun at 60 degrees from +y puts it at y in [-1.29, 0.71]), so it is lit only through the
@@ -287,15 +288,29 @@ def sppm_pane(width=48, height=48, photons=400_000, r1=0.02, alpha=0.7, sun_elev
     through the pane's underside brings is neither side's: the map stores a photon at its first D only, and light
     sampling from the floor is blocked by the glass -- as in the reference.)"""
     mats = [air(), glass((1.0, 1.0, 1.0), ior=ior), diffuse((0.7, 0.7, 0.7))]
-    prims = [prim(ST_PRIM_BOX, pos=(0.0, 0.0, 0.5), params=(1.0, 1.0, 0.01), material=1),
-             prim(ST_PRIM_BOX, pos=(0.0, -0.15, -0.05), params=(1.0, 0.85, 0.05), material=2)]
+    h = pane_half
+    off = 0.5 / math.tan(math.radians(sun_elevation))        # the shadow's shift away from the sun (+y)
+    prims = [prim(ST_PRIM_BOX, pos=(0.0, 0.0, 0.5), params=(h, h, 0.01), material=1),
+             prim(ST_PRIM_BOX, pos=(0.0, -off, -0.05), params=(h, h, 0.05), material=2)]
     s = Scene(prims, mats, env_radius=20.0, name="sppm-pane")
-    s.params = default_params(width=width, height=height, maxbounce=8, seed=seed, sun_elevation=sun_elevation,
+    # depth 5: the pane's two faces, the floor, the pane again -- no second floor vertex, so the floor-pane-floor
+    # inter-reflection (light nobody's closed form counts, and a path tracer's rare hit of the sun) is cut
+    s.params = default_params(width=width, height=height, maxbounce=5, seed=seed, sun_elevation=sun_elevation,
                               sun_azimuth=0.0, sun_illuminance=100000.0, sky_luminance=0.0, ground_luminance=0.0,
-                              sppm=1, sppm_photons=photons, sppm_r1=r1, sppm_alpha=alpha, sppm_half=1.6)
-    s.view = look_at((0.0, 0.0, 3.0), (0.0, 0.0, 0.0), 12.0, width / height, up=(0.0, 1.0, 0.0))
+                              sppm=1, sppm_photons=photons, sppm_r1=r1, sppm_alpha=alpha, sppm_half=photon_half)
+    s.view = look_at((0.0, 0.0, 3.0), (0.0, 0.0, 0.0), vfov, width / height, up=(0.0, 1.0, 0.0))
     s.info = {"ior": ior, "albedo": 0.7, "sun_elevation": sun_elevation, "E_sun": 100000.0}
     return s
+
+
+def sppm_pane_closed_form(scene, fresnel):
+    """The pane's radiance, T(view) rho / pi E_sun sin(elevation) T(sun); `fresnel(cos_i, eta)` the dielectric
+    Fresnel reflectance (the caller's: the oracle's, in the tests)."""
+    i = scene.info
+    ior, el = i["ior"], i["sun_elevation"]
+    Fv = fresnel(1.0, 1.0 / ior)
+    Fs = fresnel(math.cos(math.radians(90.0 - el)), 1.0 / ior)
+    return (1 - Fv) / (1 + Fv) * i["albedo"] / math.pi * i["E_sun"] * math.sin(math.radians(el)) * (1 - Fs) / (1 + Fs)
 
 
 # ---------------------------------------------------------------------------------------------------------------

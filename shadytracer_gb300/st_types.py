@@ -56,7 +56,7 @@ class StParams(C.Structure):
                 ("sun_hint", C.c_uint32), ("seed", C.c_uint32), ("maxaverages", C.c_uint32),
                 ("eps", C.c_float), ("budget", C.c_uint32), ("samples_per_wave", C.c_uint32),
                 ("sppm", C.c_uint32), ("sppm_photons", C.c_uint32), ("sppm_r1", C.c_float),
-                ("sppm_alpha", C.c_float), ("sppm_half", C.c_float)]
+                ("sppm_alpha", C.c_float), ("sppm_half", C.c_float), ("sppm_learn", C.c_uint32)]
 
 
 class StView(C.Structure):
@@ -142,6 +142,7 @@ def default_params(**kw):
     p.sppm_r1 = 0.0
     p.sppm_alpha = 0.0
     p.sppm_half = 0.0
+    p.sppm_learn = 0
     for k, v in kw.items():
         if not hasattr(p, k):
             raise KeyError(k)
