@@ -4,7 +4,7 @@
 void ext_free(StExt& e) {
     SppmState& s = e.sppm;
     void* ps[] = {s.pos, s.power, s.dir_oct, s.nrm_oct, s.flags, s.key, s.order, s.cell_count, s.cell_start,
-                  s.scan_part, s.spos, s.spow, s.sdir, s.snrm, s.sflags, s.stats, s.bucket, s.rank, (void*)s.dev,
+                  s.heads, s.scan_part, s.spos, s.spow, s.sdir, s.snrm, s.sflags, s.stats, s.bucket, s.rank, (void*)s.dev,
                   s.lt_emit, s.lt_hit, s.lt_cdf};
     for (void* p : ps)
         if (p) cudaFree(p);

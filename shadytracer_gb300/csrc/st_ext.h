@@ -22,7 +22,8 @@ struct SppmState {
     uint32_t* key = nullptr;     // each record's cell hash
     uint32_t* order = nullptr;   // the records in cell order (the counting sort's output)
     uint32_t* cell_count = nullptr;   // 2^20
-    uint32_t* cell_start = nullptr;   // 2^20 (+1)
+    uint32_t* cell_start = nullptr;   // per (hash, sub-list) bucket: its first record, 2^25 (+1)
+    uint32_t* heads = nullptr;        // per hash: its first record, 2^20 (+1) -- the gathers' cell ranges, 4 MB
     uint32_t* scan_part = nullptr;    // the scan's block partials
     float4* spos = nullptr;      // the records' point and power, permuted into cell order
     float4* spow = nullptr;

@@ -94,6 +94,7 @@ struct SppmBufs {
     float4 *pos = nullptr, *power = nullptr;  // as stored: point, power
     uint32_t *dir_oct = nullptr, *nrm_oct = nullptr, *flags = nullptr;
     const uint32_t* start = nullptr;          // per (cell hash, sub-list) bucket: its first record in cell order
+    const uint32_t* heads = nullptr;          // per cell hash: its first record (start at the hash's sub-list 0)
     const float4 *spos = nullptr, *spow = nullptr;
     const uint32_t *sdir = nullptr, *snrm = nullptr, *sflags = nullptr;
     // the learned emission map (wavefront.js:628-711): per cell of the LT_GRID^2 square the photons sent and those

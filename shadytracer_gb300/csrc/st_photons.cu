@@ -51,6 +51,8 @@ __global__ void k_sppm_begin(SppmDev* __restrict__ d, const DevCtr* __restrict__
     d->count = 0u;
     d->cap = cap;
     d->dropped = 0u;
+    d->gathers = 0u;
+    d->visits = 0ull;
 }
 
 // THE LEARNED EMISSION MAP (wavefront.js:520-536 ltSearch / ltMass, :628-711 prog_lt_build). A cell's worth is its
@@ -304,95 +306,241 @@ __global__ void __launch_bounds__(256) k_photon_shade(WaveArgs a, int nxt, int l
 // THE GATHER (sppm.js:475-494 sppmGather, wavefront.js:1196-1212): a camera ray with delta events only since the
 // eye (its lens field 1) -- or at the eye's first surface: the class light -> delta+ -> D -> eye, which the
 // reference hands to its light tracer (CLS_CAND | CLS_SPEC) and this build, which has none, to the map -- on an
-// evaluable surface facing it, takes sum f(l_p -> v) Phi_p / (pi r^2)
-// over the records within r on a facing surface inside the bounce cap, over n^2, times its throughput, into its
-// radiance; the eight cells, each cell's records whole within its share of the budget, else m of its sub-lists
-__global__ void __launch_bounds__(256) k_gather(WaveArgs a) {
+// evaluable surface facing it, takes sum f(l_p -> v) Phi_p / (pi r^2) over the records within r on a facing surface
+// inside the bounce cap, over n^2, times its throughput, into its radiance; the eight cells, each cell's records
+// whole within its share of the budget, else m of its sub-lists from a drawn start, each record found weighing 32 / m;
+// a gather stops at the hard cap, counting the records in walk order.
+//
+// A query walks 9 to 10 records on average (up to the cap at a caustic's focus), so its time is memory latency: the
+// eight cells' ranges, then the records. Here each lane sets up one query (its lobes, its cell coordinates) and loads
+// its eight cells' ranges at once from the per-hash heads (4 MB, resident in L2); the warp then walks the records of
+// all its queries whose cells are whole and within the cap as one list, 32 records a pass, each lane finding its
+// record's query and cell in shared memory, the sums segmented by query across the lanes (in a fixed order, so a
+// render repeats to the bit). A query with a cell past its share (sub-lists drawn, the cap possible) is walked by
+// the whole warp in the reference's order, 32 records of a range at a time.
+struct GatherQuery {
+    Lobes lb;
+    f3 x, nrm;
+    float scale;          // 1 / (pi r^2 n^2)
+    uint32_t slot, my;    // the path's slot and meta word
+    int32_t c0[3];
+    uint32_t side;        // bit k: the neighbour along axis k is on the + side
+    uint32_t a0[8];       // each cell's first record
+    uint32_t pre[9];      // the records of the cells before each; pre[8] their total
+    uint32_t pad;
+};
+// an odd number of words, so lanes reading one field of 32 different queries meet 32 different banks
+static_assert(sizeof(GatherQuery) % 8 == 4, "GatherQuery: an odd word stride");
+
+__device__ __forceinline__ void gather_cell(const GatherQuery& g, uint32_t k, int32_t& cx, int32_t& cy, int32_t& cz) {
+    cx = g.c0[0] + ((k & 1) ? ((g.side & 1) ? 1 : -1) : 0);
+    cy = g.c0[1] + ((k & 2) ? ((g.side & 2) ? 1 : -1) : 0);
+    cz = g.c0[2] + ((k & 4) ? ((g.side & 4) ? 1 : -1) : 0);
+}
+// one record's share f(l_p -> v) Phi_p, or 0 where it is of another cell with the hash, past r, past the bounce cap,
+// or on a surface facing away (the radius and normal tests in IEEE f32, unfused, as the reference's)
+__device__ __forceinline__ f3 gather_record(const WaveArgs& a, const GatherQuery& g, uint32_t rec, int32_t cx,
+                                            int32_t cy, int32_t cz, float cellsz, float r2) {
+    const float4 pp = a.sp.spos[rec];
+    if (cell_of(pp.x, cellsz) != cx || cell_of(pp.y, cellsz) != cy || cell_of(pp.z, cellsz) != cz) return mk(0.f);
+    const float dx = __fsub_rn(pp.x, g.x.x), dy = __fsub_rn(pp.y, g.x.y), dz = __fsub_rn(pp.z, g.x.z);
+    const float dd = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+    if (dd > r2) return mk(0.f);
+    const uint32_t b = a.sp.sflags[rec];
+    if ((g.my & 0xffu) + 1u + (b & SPPM_B_MASK) > a.u.maxbounce + 1u) return mk(0.f);
+    const f3 pn = unoct(a.sp.snrm[rec]);
+    const float nd = __fadd_rn(__fadd_rn(__fmul_rn(pn.x, g.nrm.x), __fmul_rn(pn.y, g.nrm.y)), __fmul_rn(pn.z, g.nrm.z));
+    if (nd < SPPM_NORMAL_DOT) return mk(0.f);
+    return lobes_eval(g.lb, a.tab, unoct(a.sp.sdir[rec]), LT_MIN_ALPHA) * xyz(a.sp.spow[rec]);
+}
+__device__ __forceinline__ void gather_add(const WaveArgs& a, uint32_t slot, f3 L) {
+    if (luma(L) == 0.f) return;
+    const float4 r4 = a.pb.rad[slot];
+    const f3 b = xyz(a.pb.beta[slot]);
+    a.pb.rad[slot] = make_float4(r4.x + b.x * L.x, r4.y + b.y * L.y, r4.z + b.z * L.z, r4.w);
+}
+
+__global__ void __launch_bounds__(256, 2) k_gather(WaveArgs a) {
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ __align__(8) uint64_t mbar;
+    __shared__ uint32_t qpre_all[8][33];
+    __shared__ float acc_all[8][32][3];
     const Uni& u = a.u;
     st_material* sm = reinterpret_cast<st_material*>(smem);
-    if (!stage_table(sm, a.mats, u.n_mats * (uint32_t)sizeof(st_material), &mbar, a.ctr)) return;
+    const uint32_t mat_bytes = u.n_mats * (uint32_t)sizeof(st_material);
+    if (!stage_table(sm, a.mats, mat_bytes, &mbar, a.ctr)) return;
+    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+    GatherQuery* gq = reinterpret_cast<GatherQuery*>(smem + ((mat_bytes + 15u) & ~15u)) + warp * 32u;
+    uint32_t* qpre = qpre_all[warp];
+    float(*acc)[3] = acc_all[warp];
     const uint32_t count = a.ctr->hitCount;
     const SppmDev* d = a.sp.dev;
     const float cellsz = d->cell, r2 = d->r2, inv_area = d->inv_area;
     const uint32_t nrec = min(d->count, d->cap);
     if (nrec == 0u) return;
+    const uint32_t share = max(1u, u.sppm_budget / 8u);
+    const uint32_t hard = SPPM_VISIT_HARD * u.sppm_budget;
+    const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
     unsigned long long walked = 0;
-    for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < count; q += gridDim.x * blockDim.x) {
-        const uint32_t slot = a.q.hit[q];
-        const uint4 m4 = a.pb.meta[slot];
-        // the eye's first surface, or delta events only since the eye (lens field 1)
-        if (((m4.y >> 16) & 0xffu) != RAY_ACTIVE) continue;
-        if ((m4.y & 0xffu) != 0u && ((m4.y >> META_LENS_SHIFT) & 3u) != 1u) continue;
-        const float4 sf = a.q.hsurf[q];
-        const uint32_t ids = __float_as_uint(sf.w);
-        if (ids == SURF_LEAVING) continue;
-        const st_material& m = sm[ids & 0xffffu];
-        if (fmaxf(fmaxf(m.emissive[0], m.emissive[1]), m.emissive[2]) > 0.f || !sppm_evaluable(m, true)) continue;
-        const float dh = a.q.hitd[q];
-        const f3 nrm = dh < 0.f ? -xyz(sf) : xyz(sf);
-        const float4 p4 = a.pb.pos[slot], d4 = a.pb.dir[slot];
-        const f3 x = xyz(p4), dir = xyz(d4);
-        const float n0 = d4.w;
-        const Lobes lb = make_lobes(nrm, -dir, m, n0 / fmaxf(m.ior, n0), a.tab, m.transmission, m.specular);
-        const uint32_t tile = slot % u.P, j = slot / u.P, seg = (m4.y >> 8) & 0xffu;
-        Rng rng = path_rng(sample_seed(u.seed, a.ctr->sample + j), tile, SPPM_STORE_SALT + seg);
-        int32_t c0[3], side[3];
-        const float gx[3] = {__fdiv_rn(x.x, cellsz), __fdiv_rn(x.y, cellsz), __fdiv_rn(x.z, cellsz)};
-        for (int k = 0; k < 3; k++) {
-            c0[k] = (int32_t)floorf(gx[k]);
-            side[k] = (__fsub_rn(gx[k], floorf(gx[k])) >= 0.5f) ? 1 : -1;
-        }
-        const uint32_t bc = (m4.y & 0xffu) + 1u;
-        const uint32_t share = max(1u, u.sppm_budget / 8u);
-        const unsigned long long hard = (unsigned long long)SPPM_VISIT_HARD * u.sppm_budget;
-        f3 sum = mk(0.f);
-        unsigned long long visits = 0;
-        bool cut = false;
-        for (uint32_t k = 0; k < 8 && !cut; k++) {
-            const int32_t cx = c0[0] + ((k & 1) ? side[0] : 0), cy = c0[1] + ((k & 2) ? side[1] : 0),
-                          cz = c0[2] + ((k & 4) ? side[2] : 0);
-            const uint32_t h = sppm_hash(cx, cy, cz);
-            const uint32_t a0 = a.sp.start[h * SPPM_SUBS], a1 = a.sp.start[(h + 1) * SPPM_SUBS];
-            const uint32_t cnt = a1 - a0;
-            const bool whole = cnt <= share;
-            const uint32_t subs = whole ? 1u : max(1u, (SPPM_SUBS * share) / max(cnt, 1u));
-            const float w = whole ? 1.f : (float)SPPM_SUBS / (float)subs;
-            const float4 rk = rng.next();
-            const uint32_t st0 = min((uint32_t)(rk.x * (float)SPPM_SUBS), SPPM_SUBS - 1);
-            for (uint32_t jj = 0; jj < subs && !cut; jj++) {
-                uint32_t lo, hi;
-                if (whole) { lo = a0; hi = a1; }
-                else { const uint32_t s = (st0 + jj) % SPPM_SUBS; lo = a.sp.start[h * SPPM_SUBS + s]; hi = a.sp.start[h * SPPM_SUBS + s + 1]; }
-                for (uint32_t rec = lo; rec < hi; rec++) {
-                    if (visits >= hard) { cut = true; break; }
-                    visits++;
-                    const float4 pp = a.sp.spos[rec];
-                    if (cell_of(pp.x, cellsz) != cx || cell_of(pp.y, cellsz) != cy || cell_of(pp.z, cellsz) != cz) continue;
-                    const float dx = __fsub_rn(pp.x, x.x), dy = __fsub_rn(pp.y, x.y), dz = __fsub_rn(pp.z, x.z);
-                    const float dd = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
-                    if (dd > r2) continue;
-                    const uint32_t b = a.sp.sflags[rec];
-                    if (bc + (b & SPPM_B_MASK) > u.maxbounce + 1u) continue;
-                    const f3 pn = unoct(a.sp.snrm[rec]);
-                    const float nd = __fadd_rn(__fadd_rn(__fmul_rn(pn.x, nrm.x), __fmul_rn(pn.y, nrm.y)), __fmul_rn(pn.z, nrm.z));
-                    if (nd < SPPM_NORMAL_DOT) continue;
-                    const f3 f = lobes_eval(lb, a.tab, unoct(a.sp.sdir[rec]), LT_MIN_ALPHA);
-                    sum = sum + f * xyz(a.sp.spow[rec]) * w;
+    uint32_t gathers = 0;
+    for (uint32_t q0 = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32u; q0 < count; q0 += nwarps * 32u) {
+        // 1. each lane's query: the eye's first surface, or delta events only since the eye (lens field 1), on an
+        // evaluable surface that does not emit; its setup and its cells' ranges into shared memory
+        const uint32_t q = q0 + lane;
+        bool take = false, fast = false;
+        uint32_t T = 0;
+        if (q < count) {
+            const uint32_t slot = a.q.hit[q];
+            const uint32_t my = a.pb.meta[slot].y;
+            const float4 sf = a.q.hsurf[q];
+            const uint32_t ids = __float_as_uint(sf.w);
+            if (((my >> 16) & 0xffu) == RAY_ACTIVE && ((my & 0xffu) == 0u || ((my >> META_LENS_SHIFT) & 3u) == 1u) &&
+                ids != SURF_LEAVING) {
+                const st_material& m = sm[ids & 0xffffu];
+                take = fmaxf(fmaxf(m.emissive[0], m.emissive[1]), m.emissive[2]) <= 0.f && sppm_evaluable(m, true);
+                if (take) {
+                    GatherQuery& g = gq[lane];
+                    const float dh = a.q.hitd[q];
+                    const f3 nrm = dh < 0.f ? -xyz(sf) : xyz(sf);
+                    const float4 p4 = a.pb.pos[slot], d4 = a.pb.dir[slot];
+                    const f3 x = xyz(p4);
+                    const float n0 = d4.w;
+                    g.lb = make_lobes(nrm, -xyz(d4), m, n0 / fmaxf(m.ior, n0), a.tab, m.transmission, m.specular);
+                    g.x = x;
+                    g.nrm = nrm;
+                    g.scale = inv_area / (n0 * n0);
+                    g.slot = slot;
+                    g.my = my;
+                    const float gx[3] = {__fdiv_rn(x.x, cellsz), __fdiv_rn(x.y, cellsz), __fdiv_rn(x.z, cellsz)};
+                    uint32_t side = 0;
+                    int32_t c0[3];
+                    for (int k = 0; k < 3; k++) {
+                        c0[k] = (int32_t)floorf(gx[k]);
+                        g.c0[k] = c0[k];
+                        if (__fsub_rn(gx[k], floorf(gx[k])) >= 0.5f) side |= 1u << k;
+                    }
+                    g.side = side;
+                    uint32_t a0[8], a1[8];
+#pragma unroll
+                    for (uint32_t k = 0; k < 8; k++) {
+                        const int32_t cx = c0[0] + ((k & 1) ? ((side & 1) ? 1 : -1) : 0),
+                                      cy = c0[1] + ((k & 2) ? ((side & 2) ? 1 : -1) : 0),
+                                      cz = c0[2] + ((k & 4) ? ((side & 4) ? 1 : -1) : 0);
+                        const uint32_t h = sppm_hash(cx, cy, cz);
+                        a0[k] = __ldg(&a.sp.heads[h]);
+                        a1[k] = __ldg(&a.sp.heads[h + 1]);
+                    }
+                    bool whole = true;
+#pragma unroll
+                    for (uint32_t k = 0; k < 8; k++) {
+                        g.a0[k] = a0[k];
+                        g.pre[k] = T;
+                        whole = whole && a1[k] - a0[k] <= share;
+                        T += a1[k] - a0[k];
+                    }
+                    g.pre[8] = T;
+                    fast = whole && T <= hard;
                 }
             }
         }
-        const f3 L = sum * (inv_area / (n0 * n0));
-        if (luma(L) != 0.f) {
-            const float4 r4 = a.pb.rad[slot];
-            const f3 b = xyz(a.pb.beta[slot]);
-            a.pb.rad[slot] = make_float4(r4.x + b.x * L.x, r4.y + b.y * L.y, r4.z + b.z * L.z, r4.w);
+        const uint32_t taken = __ballot_sync(FULL_MASK, take);
+        const uint32_t slow = __ballot_sync(FULL_MASK, take && !fast);
+        gathers += __popc(taken);
+        // 2. the whole-cell queries' records as one list over the lanes: each query's first item, their total
+        const uint32_t t = fast ? T : 0u;
+        uint32_t incl = t;
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t v = __shfl_up_sync(FULL_MASK, incl, o);
+            if ((int)lane >= o) incl += v;
         }
-        walked += visits;
+        qpre[lane] = incl - t;
+        if (lane == 31u) qpre[32] = incl;
+        acc[lane][0] = acc[lane][1] = acc[lane][2] = 0.f;
+        walked += t;
+        __syncwarp();
+        const uint32_t total = qpre[32];
+        for (uint32_t base = 0; base < total; base += 32u) {
+            const uint32_t i = base + lane;
+            uint32_t s = 32u;                                   // no query: past the list's end
+            f3 v = mk(0.f);
+            if (i < total) {
+                // the item's query: the last whose first item is at or before it (the ones with none are passed)
+                s = 0;
+#pragma unroll
+                for (uint32_t st = 16; st > 0; st >>= 1)
+                    if (qpre[s + st] <= i) s += st;
+                const GatherQuery& g = gq[s];
+                const uint32_t r = i - qpre[s];
+                uint32_t k = 0;
+#pragma unroll
+                for (uint32_t st = 4; st > 0; st >>= 1)
+                    if (g.pre[k + st] <= r) k += st;
+                int32_t cx, cy, cz;
+                gather_cell(g, k, cx, cy, cz);
+                v = gather_record(a, g, g.a0[k] + (r - g.pre[k]), cx, cy, cz, cellsz, r2);
+            }
+            // the sums segmented by query (the items lie in query order), each segment's added by its last lane
+            for (int o = 1; o < 32; o <<= 1) {
+                const float vx = __shfl_up_sync(FULL_MASK, v.x, o), vy = __shfl_up_sync(FULL_MASK, v.y, o),
+                            vz = __shfl_up_sync(FULL_MASK, v.z, o);
+                const uint32_t so = __shfl_up_sync(FULL_MASK, s, o);
+                if ((int)lane >= o && so == s) { v.x += vx; v.y += vy; v.z += vz; }
+            }
+            const uint32_t sn = __shfl_down_sync(FULL_MASK, s, 1);
+            if (s < 32u && (lane == 31u || sn != s)) {
+                acc[s][0] += v.x;
+                acc[s][1] += v.y;
+                acc[s][2] += v.z;
+            }
+            __syncwarp();
+        }
+        if (fast && T > 0u) gather_add(a, gq[lane].slot, mk(acc[lane][0], acc[lane][1], acc[lane][2]) * gq[lane].scale);
+        // 3. the others, one at a time by the whole warp, in the reference's order
+        for (uint32_t todo = slow; todo != 0u; todo &= todo - 1u) {
+            const GatherQuery& g = gq[__ffs(todo) - 1];
+            const uint32_t tile = g.slot % u.P, j = g.slot / u.P, seg = (g.my >> 8) & 0xffu;
+            Rng rng = path_rng(sample_seed(u.seed, a.ctr->sample + j), tile, SPPM_STORE_SALT + seg);
+            f3 sum = mk(0.f);
+            uint32_t visits = 0;
+            bool cut = false;
+            for (uint32_t k = 0; k < 8 && !cut; k++) {
+                int32_t cx, cy, cz;
+                gather_cell(g, k, cx, cy, cz);
+                const uint32_t h = sppm_hash(cx, cy, cz);
+                const uint32_t a0 = g.a0[k], cnt = g.pre[k + 1] - g.pre[k];
+                const bool whole = cnt <= share;
+                const uint32_t subs = whole ? 1u : max(1u, (SPPM_SUBS * share) / max(cnt, 1u));
+                const float w = whole ? 1.f : (float)SPPM_SUBS / (float)subs;
+                const float4 rk = rng.next();
+                const uint32_t st0 = min((uint32_t)(rk.x * (float)SPPM_SUBS), SPPM_SUBS - 1);
+                for (uint32_t jj = 0; jj < subs && !cut; jj++) {
+                    uint32_t lo = a0, hi = a0 + cnt;
+                    if (!whole) {
+                        const uint32_t sl = (st0 + jj) % SPPM_SUBS;
+                        lo = __ldg(&a.sp.start[h * SPPM_SUBS + sl]);
+                        hi = __ldg(&a.sp.start[h * SPPM_SUBS + sl + 1]);
+                    }
+                    if (visits + (hi - lo) > hard) { hi = lo + (hard - visits); cut = true; }
+                    visits += hi - lo;
+                    for (uint32_t rec = lo + lane; rec < hi; rec += 32u)
+                        sum = sum + gather_record(a, g, rec, cx, cy, cz, cellsz, r2) * w;
+                }
+            }
+            for (int o = 16; o > 0; o >>= 1) {
+                sum.x += __shfl_xor_sync(FULL_MASK, sum.x, o);
+                sum.y += __shfl_xor_sync(FULL_MASK, sum.y, o);
+                sum.z += __shfl_xor_sync(FULL_MASK, sum.z, o);
+            }
+            if (lane == 0u) {
+                gather_add(a, g.slot, sum * g.scale);
+                walked += visits;
+            }
+        }
+        __syncwarp();
     }
     for (int o = 16; o > 0; o >>= 1) walked += __shfl_down_sync(FULL_MASK, walked, o);
-    if ((threadIdx.x & 31u) == 0u && walked) atomicAdd(&a.sp.dev->visits, walked);
+    if (lane == 0u && walked) atomicAdd(&a.sp.dev->visits, walked);
+    if (lane == 0u && gathers) atomicAdd(&a.sp.dev->gathers, gathers);
 }
 
 cudaError_t launch_sppm_begin(const WaveArgs& a, cudaStream_t s) {
@@ -413,8 +561,11 @@ cudaError_t launch_photon_shade(const WaveArgs& a, int nxt, int last, int sms, c
     return cudaGetLastError();
 }
 cudaError_t launch_gather(const WaveArgs& a, int sms, cudaStream_t s) {
-    const size_t smem = a.u.n_mats * sizeof(st_material);
-    k_gather<<<sms * 4, 256, smem, s>>>(a);
+    const size_t smem = ((a.u.n_mats * sizeof(st_material) + 15) & ~(size_t)15) + 256 * sizeof(GatherQuery);
+    cudaFuncSetAttribute(k_gather, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    int nb = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_gather, 256, smem);
+    k_gather<<<sms * (nb > 0 ? nb : 1), 256, smem, s>>>(a);
     return cudaGetLastError();
 }
 

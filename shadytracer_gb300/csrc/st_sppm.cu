@@ -70,7 +70,8 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_sums(const uint32_t* __re
         part[blockIdx.x] = t;
     }
 }
-__global__ void __launch_bounds__(1024) k_scan_partials(uint32_t* part, uint32_t nblocks, uint32_t* total) {
+__global__ void __launch_bounds__(1024) k_scan_partials(uint32_t* part, uint32_t nblocks, uint32_t* total,
+                                                        uint32_t* total2) {
     __shared__ uint32_t sh[1024];
     const uint32_t per = (nblocks + 1023) / 1024;
     uint32_t lo = threadIdx.x * per, hi = min(lo + per, nblocks), s = 0;
@@ -85,9 +86,12 @@ __global__ void __launch_bounds__(1024) k_scan_partials(uint32_t* part, uint32_t
     }
     uint32_t run = threadIdx.x ? sh[threadIdx.x - 1] : 0u;
     for (uint32_t i = lo; i < hi; i++) { uint32_t v = part[i]; part[i] = run; run += v; }
-    if (threadIdx.x == 1023) *total = sh[1023];
+    if (threadIdx.x == 1023) { *total = sh[1023]; *total2 = sh[1023]; }
 }
-__global__ void __launch_bounds__(SCAN_THREADS) k_scan_apply(uint32_t* __restrict__ c, const uint32_t* __restrict__ part) {
+// Each hash's first record (its sub-list 0's start) is also written to heads, so that a gather reads its eight cells'
+// ranges from 4 MB rather than from the 128 MB of buckets.
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_apply(uint32_t* __restrict__ c, const uint32_t* __restrict__ part,
+                                                            uint32_t* __restrict__ heads) {
     __shared__ uint32_t wsum[SCAN_THREADS / 32];
     const uint32_t base = blockIdx.x * SCAN_TILE + threadIdx.x * SCAN_ITEMS;
     uint32_t v[SCAN_ITEMS];
@@ -116,6 +120,8 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_apply(uint32_t* __restric
     for (uint32_t k = 0; k < SCAN_ITEMS; k++) { uint32_t t = v[k]; v[k] = run; run += t; }
 #pragma unroll
     for (uint32_t k = 0; k < SCAN_ITEMS / 4; k++) c4[k] = make_uint4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]);
+    static_assert(SPPM_SUBS % SCAN_ITEMS == 0, "a hash's buckets start on a thread's first item");
+    if (base % SPPM_SUBS == 0u) heads[base / SPPM_SUBS] = v[0];
 }
 
 // THE SCATTER: each record into its bucket's range at its rank, the records themselves permuted with it
@@ -140,9 +146,9 @@ __global__ void __launch_bounds__(256) k_sppm_scatter(const uint32_t* __restrict
 }
 
 // a hash's count and start, for the host's reading of the grid (the reference's per-cell counts, sppm.js:415)
-__global__ void k_sppm_cells(const uint32_t* __restrict__ start, uint32_t* __restrict__ cnt, uint32_t* __restrict__ cst) {
+__global__ void k_sppm_cells(const uint32_t* __restrict__ heads, uint32_t* __restrict__ cnt, uint32_t* __restrict__ cst) {
     for (uint32_t h = blockIdx.x * blockDim.x + threadIdx.x; h < SPPM_HEADS; h += gridDim.x * blockDim.x) {
-        uint32_t a = start[h * SPPM_SUBS], b = start[(h + 1) * SPPM_SUBS];
+        uint32_t a = heads[h], b = heads[h + 1];
         cnt[h] = b - a;
         cst[h] = a;
     }
@@ -157,7 +163,7 @@ __global__ void __launch_bounds__(128) k_sppm_gather(const float* __restrict__ q
                                                      const float* __restrict__ qalb, const uint32_t* __restrict__ qb,
                                                      uint32_t m, float radius, float cell, uint32_t maxbounce,
                                                      uint32_t budget, uint4 sseed, const uint32_t* __restrict__ start,
-                                                     const float4* __restrict__ spos, const float4* __restrict__ spow,
+                                                     const uint32_t* __restrict__ heads, const float4* __restrict__ spos, const float4* __restrict__ spow,
                                                      const uint32_t* __restrict__ snrm,
                                                      const uint32_t* __restrict__ sflags, double* __restrict__ out,
                                                      uint32_t* __restrict__ stats) {
@@ -186,7 +192,7 @@ __global__ void __launch_bounds__(128) k_sppm_gather(const float* __restrict__ q
         const int32_t cx = c0[0] + ((k & 1) ? side[0] : 0), cy = c0[1] + ((k & 2) ? side[1] : 0),
                       cz = c0[2] + ((k & 4) ? side[2] : 0);
         const uint32_t h = sppm_hash(cx, cy, cz);
-        const uint32_t a0 = start[h * SPPM_SUBS], a1 = start[(h + 1) * SPPM_SUBS];
+        const uint32_t a0 = heads[h], a1 = heads[h + 1];
         const uint32_t count = a1 - a0;
         const bool whole = count <= share;
         const uint32_t subs = whole ? 1u : max(1u, (SPPM_SUBS * share) / max(count, 1u));
@@ -235,6 +241,7 @@ int sppm_ensure(st_ctx* ctx, uint32_t n) {
         if (cudaMemset(s.dev, 0, sizeof(SppmDev)) != cudaSuccess) return fail("memset photon grid");
         if (cudaMalloc(&s.cell_start, (size_t)(SPPM_BUCKETS + SCAN_TILE) * 4) != cudaSuccess) return fail("cudaMalloc photon grid");
         if (cudaMalloc(&s.scan_part, (size_t)(SCAN_BLOCKS + 8) * 4) != cudaSuccess) return fail("cudaMalloc photon grid");
+        if (cudaMalloc(&s.heads, (size_t)(SPPM_HEADS + 32) * 4) != cudaSuccess) return fail("cudaMalloc photon grid");
         if (cudaMalloc(&s.cell_count, (size_t)SPPM_HEADS * 4 * 2) != cudaSuccess) return fail("cudaMalloc photon grid");
         if (cudaMalloc(&s.stats, 8 * 4) != cudaSuccess) return fail("cudaMalloc photon grid");
         if (cudaMalloc(&s.lt_emit, LT_CELLS * 4) != cudaSuccess || cudaMalloc(&s.lt_hit, LT_CELLS * 4) != cudaSuccess ||
@@ -273,8 +280,8 @@ cudaError_t sppm_grid_launch(SppmState& s, int sms, cudaStream_t st) {
     if (e) return e;
     k_sppm_key<<<(uint32_t)sms * 16u, 256, 0, st>>>(s.pos, s.flags, s.dev, s.key, s.bucket, s.rank, s.cell_start);
     k_scan_sums<<<SCAN_BLOCKS, SCAN_THREADS, 0, st>>>(s.cell_start, s.scan_part);
-    k_scan_partials<<<1, 1024, 0, st>>>(s.scan_part, SCAN_BLOCKS, s.cell_start + SPPM_BUCKETS);
-    k_scan_apply<<<SCAN_BLOCKS, SCAN_THREADS, 0, st>>>(s.cell_start, s.scan_part);
+    k_scan_partials<<<1, 1024, 0, st>>>(s.scan_part, SCAN_BLOCKS, s.cell_start + SPPM_BUCKETS, s.heads + SPPM_HEADS);
+    k_scan_apply<<<SCAN_BLOCKS, SCAN_THREADS, 0, st>>>(s.cell_start, s.scan_part, s.heads);
     // the sentinel: the total, past the last bucket (k_scan_apply's last tile covers [SPPM_BUCKETS - SCAN_TILE, SPPM_BUCKETS))
     k_sppm_scatter<<<(uint32_t)sms * 16u, 256, 0, st>>>(s.bucket, s.rank, s.cell_start, s.dev, s.pos, s.power, s.dir_oct,
                                                        s.nrm_oct, s.flags, s.order, s.spos, s.spow, s.sdir, s.snrm,
@@ -295,7 +302,7 @@ SppmBufs sppm_bufs(const SppmState& s) {
     b.cap = s.cap;
     b.pos = s.pos; b.power = s.power; b.dir_oct = s.dir_oct; b.nrm_oct = s.nrm_oct; b.flags = s.flags;
     b.lt_emit = s.lt_emit; b.lt_hit = s.lt_hit; b.lt_cdf = s.lt_cdf;
-    b.start = s.cell_start; b.spos = s.spos; b.spow = s.spow; b.sdir = s.sdir; b.snrm = s.snrm; b.sflags = s.sflags;
+    b.start = s.cell_start; b.heads = s.heads; b.spos = s.spos; b.spow = s.spow; b.sdir = s.sdir; b.snrm = s.snrm; b.sflags = s.sflags;
     return b;
 }
 
@@ -347,7 +354,7 @@ int st_sppm_read_grid(st_ctx* ctx, uint32_t* key, uint32_t* cell_count, uint32_t
     cudaStream_t st = ctx_stream(ctx);
     uint32_t* cnt = s.cell_count;
     uint32_t* cst = s.cell_count + SPPM_HEADS;
-    k_sppm_cells<<<1024, 256, 0, st>>>(s.cell_start, cnt, cst);
+    k_sppm_cells<<<1024, 256, 0, st>>>(s.heads, cnt, cst);
     cudaError_t e = cudaGetLastError();
     if (!e && key && s.n) e = cudaMemcpyAsync(key, s.key, (size_t)s.n * 4, cudaMemcpyDeviceToHost, st);
     if (!e && order && s.n) e = cudaMemcpyAsync(order, s.order, (size_t)s.n * 4, cudaMemcpyDeviceToHost, st);
@@ -383,7 +390,7 @@ int st_sppm_gather(st_ctx* ctx, const float* qpos, const float* qnrm, const floa
     if (!e) {
         k_sppm_gather<<<(m + 127) / 128, 128, 0, st>>>(dq, dq + 3 * (size_t)m, dq + 6 * (size_t)m, db, m, radius,
                                                       s.cell, maxbounce, budget, sample_seed(seed, 0), s.cell_start,
-                                                      s.spos, s.spow, s.snrm, s.sflags, dout, s.stats);
+                                                      s.heads, s.spos, s.spow, s.snrm, s.sflags, dout, s.stats);
         e = cudaGetLastError();
     }
     if (!e) e = cudaMemcpyAsync(out, dout, (size_t)m * 24, cudaMemcpyDeviceToHost, st);
@@ -400,7 +407,7 @@ int st_sppm_stats_read(st_ctx* ctx, st_sppm_stats* out) {
     SppmState& s = ctx_ext(ctx).sppm;
     if (!s.stats) { *out = st_sppm_stats{}; return ST_OK; }
     cudaSetDevice(ctx_device(ctx));
-    if (s.wave) {                              // the wavefront's map: its last sample's records and walks
+    if (s.wave) {                              // the wavefront's map: its last sample's records, gathers and walks
         SppmDev d;
         if (cudaStreamSynchronize(ctx_stream(ctx)) != cudaSuccess ||
             cudaMemcpy(&d, s.dev, sizeof(d), cudaMemcpyDeviceToHost) != cudaSuccess)
@@ -408,6 +415,7 @@ int st_sppm_stats_read(st_ctx* ctx, st_sppm_stats* out) {
         *out = st_sppm_stats{};
         out->stored = std::min(d.count, d.cap);
         out->cut = d.dropped;
+        out->gathers = d.gathers;
         out->visits = d.visits;
         return ST_OK;
     }
