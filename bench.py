@@ -6,6 +6,7 @@ window; 1920 x 1080, 64 samples per pixel, max depth 8, march tolerance 1e-4 m, 
 the whole render -- 64 samples of every pixel, 132.7 M camera paths -- folded into the FP64 accumulation.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference] [--small] [--spp S]
+                    [--leg sppm|rmse|optics]     # one leg alone, its JSON printed (for profiling runs)
 
 value: paths / s with the scene resident on the GPU (graph replays; the timed region brackets K renders with a
        synchronize). e2e: the same through the C ABI as a host calls it -- scene, settings and camera uploaded from
@@ -55,6 +56,8 @@ def parse():
     ap.add_argument("--no-optics", action="store_true", help="skip the optics bench's rays/s leg")
     ap.add_argument("--no-sppm", action="store_true", help="skip the photon map's photons/s leg")
     ap.add_argument("--spp", type=int, default=0, help="samples per pixel a step (profiling runs; default: 64)")
+    ap.add_argument("--leg", default="all", choices=["all", "sppm", "rmse", "optics"],
+                    help="run one leg alone and print its JSON (profiling runs of the photon map or the optics bench)")
     return ap.parse_args()
 
 
@@ -209,7 +212,8 @@ def optics_leg(args, dev, with_cpu):
     from shadytracer_gb300 import scenes
     from shadytracer_gb300.optics import Optics
     from shadytracer_gb300.renderer import create_path_tracer
-    b = scenes.optics_bench(n_instances=8 if args.small else 64, seed=5, ray_scale=0.01 if args.small else 1.0)
+    # --small: the same 64 instances at a tenth of the rays (12 M), a profiling case still larger than L2
+    b = scenes.optics_bench(n_instances=64, seed=5, ray_scale=0.1 if args.small else 1.0)
     rays = b.info["rays"]
     total = int(sum(rays))
     rt = create_path_tracer(b, device=dev)
@@ -387,6 +391,13 @@ def run_ours(args):
     import torch
     dev = local if world > 1 else 0
     torch.cuda.set_device(dev)
+    if args.leg != "all":
+        with_cpu = rank == 0 and world == 1 and not args.no_cpu
+        out = {"sppm": lambda: sppm_leg(args, dev, with_cpu), "rmse": lambda: rmse_leg(args, dev),
+               "optics": lambda: optics_leg(args, dev, with_cpu)}[args.leg]()
+        if rank == 0:
+            print(json.dumps(out), flush=True)
+        return 0
     dist = None
     if world > 1:
         import torch.distributed as dist

@@ -399,16 +399,21 @@ static cudaError_t record_wave(st_ctx* ctx, const WaveArgs& a) {
     if ((e = launch_iter_begin(a, 0, 1, 1, s))) return e;
     if ((e = timed("genrays", [&] { return launch_genrays(a, ctx->sms, s); }))) return e;
     int cur = 0;
+    // the camera's rays march unsorted: they leave one point in pixel-tile order, already coherent, where the space
+    // order would only split them by octant
+    WaveArgs a_eye = a;
+    a_eye.u.sort_on = 0;
     for (uint32_t it = 0; it < a.u.budget; it++) {
         int nxt = cur ^ 1;
         int last = it + 1 == a.u.budget;
         int side = (int)(it & 1u);
         if (it > 0 && (++ctx->rec_launches, e = launch_iter_begin(a, (int)it, nxt, 0, s))) return e;
-        if (a.u.sort_on) {
+        if (a.u.sort_on && it > 0) {
             if ((e = timed("sort", [&] { return launch_sort(a, cur, ctx->sms, s); }))) return e;
             ctx->rec_launches += 2;                                  // key, scan, scatter
         }
-        if ((e = timed("march", [&] { return launch_march(a, cur, nxt, last, ctx->sms, s); }))) return e;
+        const WaveArgs& am = it == 0 ? a_eye : a;
+        if ((e = timed("march", [&] { return launch_march(am, cur, nxt, last, ctx->sms, s); }))) return e;
         if ((e = timed("surface", [&] { return launch_surface(a, ctx->sms, s); }))) return e;
         if (a.u.sppm_on && (e = timed("gather", [&] { return launch_gather(a, ctx->sms, s); }))) return e;
         if ((e = timed("shade", [&] { return launch_shade(a, nxt, side, last, ctx->sms, s); }))) return e;

@@ -315,9 +315,9 @@ __global__ void __launch_bounds__(256) k_photon_shade(WaveArgs a, int nxt, int l
 // eight cells' ranges, then the records. Here each lane sets up one query (its lobes, its cell coordinates) and loads
 // its eight cells' ranges at once from the per-hash heads (4 MB, resident in L2); the warp then walks the records of
 // all its queries whose cells are whole and within the cap as one list, 32 records a pass, each lane finding its
-// record's query and cell in shared memory, the sums segmented by query across the lanes (in a fixed order, so a
-// render repeats to the bit). A query with a cell past its share (sub-lists drawn, the cap possible) is walked by
-// the whole warp in the reference's order, 32 records of a range at a time.
+// record's query and cell in shared memory, the sums segmented by query across the lanes in a fixed order. A query
+// with a cell past its share (sub-lists drawn, the cap possible) is walked by the whole warp in the reference's
+// order, cell by cell: the cell's drawn sub-lists' ranges loaded at once, one a lane, and walked as one list.
 struct GatherQuery {
     Lobes lb;
     f3 x, nrm;
@@ -495,15 +495,15 @@ __global__ void __launch_bounds__(256, 2) k_gather(WaveArgs a) {
             __syncwarp();
         }
         if (fast && T > 0u) gather_add(a, gq[lane].slot, mk(acc[lane][0], acc[lane][1], acc[lane][2]) * gq[lane].scale);
-        // 3. the others, one at a time by the whole warp, in the reference's order
+        // 3. the others, one at a time by the whole warp, in the reference's order: per cell, its whole range on lane
+        // 0 or its drawn sub-lists' ranges on lanes 0..m-1 (loaded at once), walked as one list 32 records a pass
         for (uint32_t todo = slow; todo != 0u; todo &= todo - 1u) {
             const GatherQuery& g = gq[__ffs(todo) - 1];
             const uint32_t tile = g.slot % u.P, j = g.slot / u.P, seg = (g.my >> 8) & 0xffu;
             Rng rng = path_rng(sample_seed(u.seed, a.ctr->sample + j), tile, SPPM_STORE_SALT + seg);
             f3 sum = mk(0.f);
             uint32_t visits = 0;
-            bool cut = false;
-            for (uint32_t k = 0; k < 8 && !cut; k++) {
+            for (uint32_t k = 0; k < 8; k++) {
                 int32_t cx, cy, cz;
                 gather_cell(g, k, cx, cy, cz);
                 const uint32_t h = sppm_hash(cx, cy, cz);
@@ -513,18 +513,36 @@ __global__ void __launch_bounds__(256, 2) k_gather(WaveArgs a) {
                 const float w = whole ? 1.f : (float)SPPM_SUBS / (float)subs;
                 const float4 rk = rng.next();
                 const uint32_t st0 = min((uint32_t)(rk.x * (float)SPPM_SUBS), SPPM_SUBS - 1);
-                for (uint32_t jj = 0; jj < subs && !cut; jj++) {
-                    uint32_t lo = a0, hi = a0 + cnt;
-                    if (!whole) {
-                        const uint32_t sl = (st0 + jj) % SPPM_SUBS;
-                        lo = __ldg(&a.sp.start[h * SPPM_SUBS + sl]);
-                        hi = __ldg(&a.sp.start[h * SPPM_SUBS + sl + 1]);
-                    }
-                    if (visits + (hi - lo) > hard) { hi = lo + (hard - visits); cut = true; }
-                    visits += hi - lo;
-                    for (uint32_t rec = lo + lane; rec < hi; rec += 32u)
-                        sum = sum + gather_record(a, g, rec, cx, cy, cz, cellsz, r2) * w;
+                uint32_t lo = 0, len = 0;
+                if (whole) {
+                    if (lane == 0u) { lo = a0; len = cnt; }
+                } else if (lane < subs) {
+                    const uint32_t sl = (st0 + lane) % SPPM_SUBS;
+                    lo = __ldg(&a.sp.start[h * SPPM_SUBS + sl]);
+                    len = __ldg(&a.sp.start[h * SPPM_SUBS + sl + 1]) - lo;
                 }
+                uint32_t incl = len;
+                for (int o = 1; o < 32; o <<= 1) {
+                    const uint32_t v = __shfl_up_sync(FULL_MASK, incl, o);
+                    if ((int)lane >= o) incl += v;
+                }
+                const uint32_t off = incl - len;
+                uint32_t n = __shfl_sync(FULL_MASK, incl, 31);
+                // the hard cap, in walk order: the records past it are not met, nor the cells after
+                const bool cut = visits + n > hard;
+                if (cut) n = hard - visits;
+                visits += n;
+                for (uint32_t base = 0; base < n; base += 32u) {
+                    const uint32_t i = base + lane;
+                    // the lane whose range holds item i: the last whose offset is at or before it
+                    uint32_t src = 0;
+#pragma unroll
+                    for (uint32_t st = 16; st > 0; st >>= 1)
+                        if (__shfl_sync(FULL_MASK, off, src + st) <= i) src += st;
+                    const uint32_t lo_s = __shfl_sync(FULL_MASK, lo, src), off_s = __shfl_sync(FULL_MASK, off, src);
+                    if (i < n) sum = sum + gather_record(a, g, lo_s + (i - off_s), cx, cy, cz, cellsz, r2) * w;
+                }
+                if (cut) break;
             }
             for (int o = 16; o > 0; o >>= 1) {
                 sum.x += __shfl_xor_sync(FULL_MASK, sum.x, o);

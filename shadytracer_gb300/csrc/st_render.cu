@@ -142,18 +142,31 @@ __device__ __forceinline__ uint32_t sort_bucket(f3 glo, f3 ginv, f3 p, f3 d) {
     const uint32_t oct = (d.x < 0.f ? 1u : 0u) | (d.y < 0.f ? 2u : 0u) | (d.z < 0.f ? 4u : 0u);
     return ((iz * SORT_G + iy) * SORT_G + ix) * 8u + oct;
 }
-// each entry's bucket and rank: entry i is the ray at pos / dir [inq ? inq[i] : i]
+// each entry's bucket and rank: entry i is the ray at pos / dir [inq ? inq[i] : i]. The lanes of a warp that share
+// a bucket take their ranks with one atomic (coherent rays share buckets, and one counter taking a million atomics
+// one at a time serialises the launch), in lane order, so the queue's order survives within a bucket.
 __global__ void __launch_bounds__(256) k_sort_key(const uint32_t* __restrict__ countp, uint32_t cap,
                                                   const uint32_t* __restrict__ inq, const float4* __restrict__ pos,
                                                   const float4* __restrict__ dir, f3 glo, f3 ginv,
                                                   uint32_t* __restrict__ key, uint32_t* __restrict__ rank,
                                                   uint32_t* __restrict__ bcnt) {
     const uint32_t count = min(*countp, cap);
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
-        const uint32_t at = inq ? inq[i] : i;
-        const uint32_t b = sort_bucket(glo, ginv, xyz(pos[at]), xyz(dir[at]));
-        key[i] = b;
-        rank[i] = atomicAdd(&bcnt[b], 1u);
+    const uint32_t lane = threadIdx.x & 31u;
+    for (uint32_t i0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); i0 < count; i0 += gridDim.x * blockDim.x) {
+        const uint32_t i = i0 + lane;
+        const bool ok = i < count;
+        uint32_t b = 0xffffffffu;
+        if (ok) {
+            const uint32_t at = inq ? inq[i] : i;
+            b = sort_bucket(glo, ginv, xyz(pos[at]), xyz(dir[at]));
+            key[i] = b;
+        }
+        const uint32_t peers = __match_any_sync(FULL_MASK, b);
+        const uint32_t leader = (uint32_t)__ffs(peers) - 1u;
+        uint32_t base = 0;
+        if (ok && lane == leader) base = atomicAdd(&bcnt[b], (uint32_t)__popc(peers));
+        base = __shfl_sync(FULL_MASK, base, leader);
+        if (ok) rank[i] = base + (uint32_t)__popc(peers & ((1u << lane) - 1u));
     }
 }
 __global__ void __launch_bounds__(1024) k_sort_scan(uint32_t* __restrict__ cnt, uint32_t* __restrict__ off) {
