@@ -163,6 +163,15 @@ typedef struct st_params {
     uint32_t sppm_learn;          /* 1: the sun's photons drawn from the learned 128^2 emission map
                                    * (wavefront.js:628-711), rebuilt every 4 samples from each cell's
                                    * stores per photon sent, mixed with a 20 % uniform floor; 0: uniform */
+    /* the learned proposal (no counterpart in the reference, which removed its path guiding): a network of the
+     * surface point (hash-grid position, harmonics of the normal; 3 x 64 hidden, BF16 on the tensor cores) gives a
+     * mixture of 8 von Mises-Fisher lobes that a camera path's BSDF sampling is mixed with under one-sample MIS at its
+     * evaluable opaque vertices; trained online on the incident light the paths find, between waves */
+    uint32_t guide;               /* 1 on                                                           */
+    float    guide_alpha;         /* the mixture's share of the one-sample MIS (0: 0.5)             */
+    float    guide_lr;            /* Adam's learning rate (0: 0.005)                                 */
+    uint32_t guide_train;         /* 1: train after every wave; 0: the weights as they are          */
+    uint32_t guide_seed;          /* the initial weights' seed (a change draws them afresh)          */
 } st_params;
 
 /* The camera, as genrays reads it (core/genrays.js:65-92): the basis from invView's columns and the
@@ -327,6 +336,32 @@ int  st_optics_set_far(st_ctx* ctx, const st_optics_far* far);
 int  st_optics_run(st_ctx* ctx, const st_optics_batch* batch, double* far, double* lux,
                    st_optics_totals* totals);
 
+/* ---- the learned proposal (st_params.guide) ----
+ * The parameters, FP32, in one array of ST_MLP_PARAMS: W1 (64 x 48), W2 (64 x 64), W3 (64 x 64), W4 (40 x 64), each
+ * [out][in] row-major, then the hash grid's features (16 levels x 2^15 entries x 2). Inputs: 2 features a level of a
+ * trilinear blend over the box's cells (level l has floor(8 * 128^(l/15)) cells across the box's longest side), then
+ * the 16 real spherical harmonics of degree <= 3 of the normal; outputs: 8 lobes x (mean direction, unnormalised;
+ * log kappa, clamped to [-1, 8]; mixture logit). */
+#define ST_MLP_PARAMS (13824u + 1048576u)
+typedef struct st_mlp_stats {
+    uint32_t steps;               /* Adam steps since the weights were set                          */
+    uint32_t samples;             /* training samples in the last wave's batch                      */
+    float    loss;                /* the last wave's loss a sample                                  */
+    float    mean_weight;         /* the last batch's mean weight (incident luminance / pdf)        */
+    float    box_lo[3];           /* the hash grid's box: its low corner, metres                     */
+    float    box_inv_ext;         /* ... and 1 / its longest side                                    */
+} st_mlp_stats;
+int  st_mlp_get_weights(st_ctx* ctx, float* out, size_t n);
+int  st_mlp_set_weights(st_ctx* ctx, const float* in, size_t n);
+/* the network at n points (pos, nrm: 3n): raw (40n) its outputs; mix (40n) each lobe's mean direction, kappa and
+ * weight as the sampler reads them (quantised: the mean direction in 2 x 16 bits, kappa and the weight as halves) */
+int  st_mlp_eval(st_ctx* ctx, const float* pos, const float* nrm, uint32_t n, float* raw, float* mix);
+/* the gradient (ST_MLP_PARAMS) of sum_i -(w_i / mean w) log q(dir_i | pos_i, nrm_i), each normalised weight capped
+ * at 20, with respect to every parameter, at 1 to 16384 samples, without a step; loss: the sum */
+int  st_mlp_grad(st_ctx* ctx, const float* pos, const float* nrm, const float* dir, const float* weight, uint32_t n,
+                 float* grad, float* loss);
+int  st_mlp_stats_read(st_ctx* ctx, st_mlp_stats* out);
+
 /* ---- a render that allocates nothing ----
  * No counterpart in the reference: an entry point for hosts that may not allocate device memory when they want a
  * picture -- one held to a memory budget fixed at start-up, one on a real-time thread, one whose allocations would
@@ -346,7 +381,7 @@ int  st_render_noalloc(int device, const st_scene_desc* desc, const st_params* p
 /* ---- the binding's checks ---- */
 /* The sizes of the structs above as this library was built (st_prim, st_material, st_scene_desc, st_params,
  * st_view, st_counters_t, st_image_stats_t, st_kernel_time, st_sppm_stats, st_optics_source, st_optics_far,
- * st_optics_batch, st_optics_totals, in that order); returns how many it has. */
+ * st_optics_batch, st_optics_totals, st_mlp_stats, in that order); returns how many it has. */
 int  st_struct_sizes(uint32_t* out, int max);
 /* The context's CUDA stream (a cudaStream_t), for a host that orders or times its own work against it. */
 void* st_stream(st_ctx* ctx);

@@ -14,7 +14,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "liboracle.so")
 SOURCES = ["st_oracle.cpp", "st_oracle_core.h", "st_oracle_render.h", "st_oracle_extra.h", "st_oracle_sppm.h",
-           "st_oracle_optics.h", "st_oracle_spectral.h", "../include/shadytracer.h"]
+           "st_oracle_optics.h", "st_oracle_spectral.h", "st_oracle_guide.h", "../include/shadytracer.h"]
 
 _lib = None
 
@@ -204,6 +204,13 @@ def _declare_extra(L):
         "sto_spec_draw": ([C.c_double, P], C.c_double),
         "sto_optics_run": ([P, P, P, C.c_uint32, P, C.c_uint32, P, C.c_uint32, C.c_uint32, C.c_uint32, C.c_float,
                             C.c_float, C.c_uint32, C.c_uint32, C.c_int, P, P, P, C.c_int], C.c_int),
+        "sto_guide_forward": ([P, C.c_uint32, P, P, P, C.c_float, C.c_int, P], None),
+        "sto_guide_decode": ([P, C.c_uint32, P], None),
+        "sto_guide_grad": ([P, C.c_uint32, P, P, P, P, P, C.c_float, C.c_int, P], C.c_double),
+        "sto_guide_loss": ([P, C.c_uint32, P, P, P, P, P, C.c_float], C.c_double),
+        "sto_guide_mix_pdf": ([P, P], C.c_double),
+        "sto_guide_mix_sample": ([P, P, C.c_uint32, P], None),
+        "sto_bf16": ([C.c_float], C.c_float),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -388,3 +395,66 @@ def optics_run(bench, ray_counts, nC=360, nG=181, cells=0, half=1.0, height=1.0,
                           threads)
     keys = ["emitted", "escaped", "lost", "detected", "absorbed", "interactions"]
     return {"far": far, "lux": lux, "totals": [dict(zip(keys, t.tolist())) for t in tot], "scenes": per}
+
+
+# ---- the learned proposal (st_oracle_guide.h) ----
+GUIDE_NW = 13824
+GUIDE_NPARAM = 13824 + 1048576
+
+
+def _f32(a, shape=None):
+    a = np.ascontiguousarray(a, np.float32)
+    return a if shape is None else a.reshape(shape)
+
+
+def guide_forward(params, pos, nrm, box_lo, inv_ext, bf16=True):
+    """The network's 40 outputs at n points (double), with BF16 rounding where the tensor cores take BF16 (bf16=True)
+    or exact."""
+    L = xlib()
+    params, pos, nrm, lo = _f32(params), _f32(pos), _f32(nrm), _f32(box_lo)
+    n = len(pos)
+    raw = np.zeros((n, 40), np.float64)
+    L.sto_guide_forward(ptr(params), n, ptr(pos), ptr(nrm), ptr(lo), inv_ext, int(bf16), ptr(raw))
+    return raw
+
+
+def guide_decode(raw):
+    """Each point's mixture: 8 lobes x (mean direction xyz, kappa, weight), exact."""
+    raw = np.ascontiguousarray(raw, np.float64)
+    out = np.zeros((len(raw), 8, 5), np.float64)
+    xlib().sto_guide_decode(ptr(raw), len(raw), ptr(out))
+    return out
+
+
+def guide_grad(params, pos, nrm, dirs, weight, box_lo, inv_ext, bf16=True):
+    """(gradient of every parameter, summed loss) of the training loss at a batch."""
+    L = xlib()
+    a = [_f32(x) for x in (params, pos, nrm, dirs, weight, box_lo)]
+    G = np.zeros(GUIDE_NPARAM, np.float64)
+    loss = L.sto_guide_grad(ptr(a[0]), len(a[1]), ptr(a[1]), ptr(a[2]), ptr(a[3]), ptr(a[4]), ptr(a[5]), inv_ext,
+                            int(bf16), ptr(G))
+    return G, loss
+
+
+def guide_loss(params, pos, nrm, dirs, weight, box_lo, inv_ext):
+    L = xlib()
+    a = [_f32(x) for x in (params, pos, nrm, dirs, weight, box_lo)]
+    return L.sto_guide_loss(ptr(a[0]), len(a[1]), ptr(a[1]), ptr(a[2]), ptr(a[3]), ptr(a[4]), ptr(a[5]), inv_ext)
+
+
+def guide_mix_pdf(mix, d):
+    mix = np.ascontiguousarray(mix, np.float64)
+    d = np.ascontiguousarray(d, np.float64)
+    return xlib().sto_guide_mix_pdf(ptr(mix), ptr(d))
+
+
+def guide_mix_sample(mix, u):
+    mix = np.ascontiguousarray(mix, np.float64)
+    u = np.ascontiguousarray(u, np.float64)
+    d = np.zeros((len(u), 3), np.float64)
+    xlib().sto_guide_mix_sample(ptr(mix), ptr(u), len(u), ptr(d))
+    return d
+
+
+def bf16(x):
+    return xlib().sto_bf16(float(x))

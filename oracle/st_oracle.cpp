@@ -17,6 +17,7 @@
 #include "st_oracle_optics.h"
 #include "st_oracle_sppm.h"
 #include "st_oracle_spectral.h"
+#include "st_oracle_guide.h"
 #ifdef _OPENMP
 #include <omp.h>
 #endif
@@ -1197,5 +1198,42 @@ void sto_hg_sample(double g, const double* d, uint32_t seed, int n, double* out)
 uint32_t sto_far_bin(const float* d, const float* ax, const float* c0, uint32_t nC, uint32_t nG) { return far_bin(d, ax, c0, nC, nG); }
 void sto_far_geometry(uint32_t nC, uint32_t nG, double* omega) { far_geometry(nC, nG, omega); }
 void sto_far_intensity(const double* flux, uint32_t nC, uint32_t nG, double* I) { far_intensity(flux, nC, nG, I); }
+
+}  // extern "C"
+
+// ---- the learned proposal (st_oracle_guide.h) ----
+extern "C" {
+
+void sto_guide_forward(const float* P, uint32_t n, const float* pos, const float* nrm, const float* lo, float inv_ext,
+                       int bf, double* raw) {
+    guide::Fwd f;
+    for (uint32_t i = 0; i < n; i++) {
+        if (bf) guide::forward<true>(P, pos + 3 * i, nrm + 3 * i, lo, inv_ext, f);
+        else guide::forward<false>(P, pos + 3 * i, nrm + 3 * i, lo, inv_ext, f);
+        for (int o = 0; o < guide::OUT; o++) raw[(size_t)i * guide::OUT + o] = f.y[o];
+    }
+}
+void sto_guide_decode(const double* raw, uint32_t n, double* mix) {
+    for (uint32_t i = 0; i < n; i++)
+        guide::decode(raw + (size_t)i * guide::OUT, reinterpret_cast<double(*)[5]>(mix + (size_t)i * 40));
+}
+double sto_guide_grad(const float* P, uint32_t n, const float* pos, const float* nrm, const float* dir, const float* wt,
+                      const float* lo, float inv_ext, int bf, double* G) {
+    return bf ? guide::batch_grad<true>(P, (int)n, pos, nrm, dir, wt, lo, inv_ext, G)
+              : guide::batch_grad<false>(P, (int)n, pos, nrm, dir, wt, lo, inv_ext, G);
+}
+double sto_guide_loss(const float* P, uint32_t n, const float* pos, const float* nrm, const float* dir, const float* wt,
+                      const float* lo, float inv_ext) {
+    std::vector<double> G(guide::NPARAM, 0.0);
+    return guide::batch_grad<false>(P, (int)n, pos, nrm, dir, wt, lo, inv_ext, G.data());
+}
+double sto_guide_mix_pdf(const double* mix, const double* d) {
+    return guide::mix_pdf(reinterpret_cast<const double(*)[5]>(mix), d);
+}
+void sto_guide_mix_sample(const double* mix, const double* u, uint32_t n, double* d) {
+    for (uint32_t i = 0; i < n; i++)
+        guide::mix_sample(reinterpret_cast<const double(*)[5]>(mix), u[3 * i], u[3 * i + 1], u[3 * i + 2], d + 3 * i);
+}
+float sto_bf16(float x) { return guide::bf16(x); }
 
 }  // extern "C"

@@ -43,12 +43,18 @@ SIGNATURES = {
     "st_render_noalloc": ([C.c_int, C.POINTER(T.StSceneDesc), C.POINTER(T.StParams), C.POINTER(T.StView), C.c_int,
                            P, P, P, P], C.c_int),
     "st_eval_sdf": ([P, P, C.c_uint32, P], C.c_int),
+    "st_mlp_get_weights": ([P, P, C.c_size_t], C.c_int),
+    "st_mlp_set_weights": ([P, P, C.c_size_t], C.c_int),
+    "st_mlp_eval": ([P, P, P, C.c_uint32, P, P], C.c_int),
+    "st_mlp_grad": ([P, P, P, P, P, C.c_uint32, P, P], C.c_int),
+    "st_mlp_stats_read": ([P, C.POINTER(T.StMlpStats)], C.c_int),
     "st_struct_sizes": ([P, C.c_int], C.c_int),
     "st_stream": ([P], C.c_void_p),
 }
 
 STRUCT_ORDER = [T.StPrim, T.StMaterial, T.StSceneDesc, T.StParams, T.StView, T.StCounters, T.StImageStats,
-                T.StKernelTime, T.StSppmStats, T.StOpticsSource, T.StOpticsFar, T.StOpticsBatch, T.StOpticsTotals]
+                T.StKernelTime, T.StSppmStats, T.StOpticsSource, T.StOpticsFar, T.StOpticsBatch, T.StOpticsTotals,
+                T.StMlpStats]
 
 
 def load(path=None):

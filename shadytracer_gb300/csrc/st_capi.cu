@@ -257,6 +257,13 @@ static int ensure_wave(st_ctx* ctx) {
         if (rc) return rc;
         ctx_ext(ctx).sppm.wave = true;
     }
+    if (ctx->params.guide) {
+        const uint32_t spw_g = samples_per_wave(ctx);
+        uint32_t cap_g = spw_g * ctx->P;
+        if (sppm_runs(ctx)) cap_g = std::max(cap_g, std::min(sppm_photons(ctx), 4u << 20));
+        int rc = guide_ensure(ctx, cap_g, spw_g * ctx->P, ctx->params.guide_seed);
+        if (rc) return rc;
+    }
     uint32_t spw = samples_per_wave(ctx);
     uint32_t cap = spw * ctx->P;
     // the photon map's photons run in chunks of the wave's slots: give them room for up to four million at once
@@ -344,6 +351,9 @@ static WaveArgs wave_args(st_ctx* ctx, uint32_t w) {
         a.u.sppm_learn = ctx->params.sppm_learn ? 1u : 0u;
         a.sp = sppm_bufs(ctx_ext(ctx).sppm);
     }
+    if (ctx->params.guide)
+        a.gd = guide_bufs(ctx, 1u, ctx->params.guide_train ? 1u : 0u,
+                          ctx->params.guide_alpha > 0.f ? std::min(ctx->params.guide_alpha, 1.f) : 0.5f, a.slots);
     return a;
 }
 
@@ -396,6 +406,7 @@ static cudaError_t record_wave(st_ctx* ctx, const WaveArgs& a) {
         ctx->rec_launches += 5;                                      // key, three scan phases, scatter
     }
     ctx->rec_launches++;
+    if (a.gd.train && (e = guide_wave_begin(ctx, a.slots, s))) return e;
     if ((e = launch_iter_begin(a, 0, 1, 1, s))) return e;
     if ((e = timed("genrays", [&] { return launch_genrays(a, ctx->sms, s); }))) return e;
     int cur = 0;
@@ -416,6 +427,7 @@ static cudaError_t record_wave(st_ctx* ctx, const WaveArgs& a) {
         if ((e = timed("march", [&] { return launch_march(am, cur, nxt, last, ctx->sms, s); }))) return e;
         if ((e = timed("surface", [&] { return launch_surface(a, ctx->sms, s); }))) return e;
         if (a.u.sppm_on && (e = timed("gather", [&] { return launch_gather(a, ctx->sms, s); }))) return e;
+        if (a.gd.on && !last && (e = timed("guide", [&] { return launch_guide_infer(a, ctx->sms, s); }))) return e;
         if ((e = timed("shade", [&] { return launch_shade(a, nxt, side, last, ctx->sms, s); }))) return e;
         if (a.u.sort_on) {
             if ((e = timed("sort", [&] { return launch_sort_shadow(a, side, ctx->sms, s); }))) return e;
@@ -423,6 +435,13 @@ static cudaError_t record_wave(st_ctx* ctx, const WaveArgs& a) {
         }
         if ((e = timed("occlude", [&] { return launch_occlude(a, side, last, ctx->sms, s); }))) return e;
         cur = nxt;
+    }
+    if (a.gd.train) {   // the records into a batch, then the training steps
+        if ((e = timed("guide_collect", [&] { return launch_guide_collect(a, ctx->sms, s); }))) return e;
+        const float lr = ctx->params.guide_lr > 0.f ? ctx->params.guide_lr : 0.005f;
+        int n = 0;
+        if ((e = timed("guide_train", [&] { return guide_train_launch(ctx, lr, ctx->sms, s, &n); }))) return e;
+        ctx->rec_launches += n - 1;
     }
     return timed("resolve", [&] { return launch_resolve(a, s); });
 }
@@ -809,7 +828,7 @@ int st_struct_sizes(uint32_t* out, int max) {
                           (uint32_t)sizeof(st_image_stats_t), (uint32_t)sizeof(st_kernel_time),
                           (uint32_t)sizeof(st_sppm_stats), (uint32_t)sizeof(st_optics_source),
                           (uint32_t)sizeof(st_optics_far), (uint32_t)sizeof(st_optics_batch),
-                          (uint32_t)sizeof(st_optics_totals)};
+                          (uint32_t)sizeof(st_optics_totals), (uint32_t)sizeof(st_mlp_stats)};
     int n = (int)(sizeof(s) / sizeof(s[0]));
     for (int i = 0; i < n && i < max; i++) out[i] = s[i];
     return n;
@@ -822,6 +841,15 @@ void* st_stream(st_ctx* ctx) { return ctx ? (void*)ctx->stream : nullptr; }
 
 // the extension units' access to the context (st_ext.h)
 StExt& ctx_ext(st_ctx* ctx) { return ctx->ext; }
+// the learned proposal's hash-grid box: the primitives' bounds as the space sort has them, a cube of their longest
+// side from their low corner; a scene of unbounded primitives only, a 50 m cube about the origin
+void guide_box(st_ctx* ctx, f3& lo, float& inv_ext) {
+    if (!ctx->grid_ok) { lo = mk(-25.f); inv_ext = 1.f / 50.f; return; }
+    lo = mk(ctx->grid_lo[0], ctx->grid_lo[1], ctx->grid_lo[2]);
+    const float ext = std::max(ctx->grid_hi[0] - ctx->grid_lo[0],
+                               std::max(ctx->grid_hi[1] - ctx->grid_lo[1], ctx->grid_hi[2] - ctx->grid_lo[2]));
+    inv_ext = 1.f / std::max(ext, 1e-6f);
+}
 cudaStream_t ctx_stream(st_ctx* ctx) { return ctx->stream; }
 int ctx_device(st_ctx* ctx) { return ctx->device; }
 int ctx_sms(st_ctx* ctx) { return ctx->sms; }

@@ -8,6 +8,10 @@ void ext_free(StExt& e) {
                   s.lt_emit, s.lt_hit, s.lt_cdf};
     for (void* p : ps)
         if (p) cudaFree(p);
+    GuideState& g = e.guide;
+    void* gs[] = {g.param, g.grad, g.m1, g.m2, g.wbf, (void*)g.dev, (void*)g.samp, g.act, g.mix, (void*)g.rec, g.acc};
+    for (void* p : gs)
+        if (p) cudaFree(p);
     optics_free(e.optics);
     e = StExt{};
 }

@@ -52,9 +52,40 @@ struct OpticsState {
     void* scratch = nullptr;     // the run's device buffers (st_optics.cu OptBuf), grown as needed
 };
 
+// THE LEARNED PROPOSAL (st_guide.cu): FP32 weights and features with their gradients and Adam moments, the BF16
+// copy the kernels read, the batch and a mini-batch's activations, the per-queue mixtures and per-path records
+struct GuideState {
+    float* param = nullptr;          // GUIDE_NPARAM: W1 W2 W3 W4 (GUIDE_NW), then the hash grid's features
+    float* grad = nullptr;
+    float* m1 = nullptr;
+    float* m2 = nullptr;
+    uint16_t* wbf = nullptr;
+    st::GuideDev* dev = nullptr;
+    st::GuideSample* samp = nullptr;
+    uint16_t* act = nullptr;
+    uint2* mix = nullptr;
+    uint32_t mix_cap = 0;
+    st::GuideRec* rec = nullptr;
+    float* acc = nullptr;
+    uint32_t rec_cap = 0;
+    uint32_t seed = 0;               // the seed the weights were drawn from
+};
+int guide_ensure(st_ctx* ctx, uint32_t queue_cap, uint32_t slots, uint32_t seed);
+int guide_upload(st_ctx* ctx, const float* h);
+st::GuideBufs guide_bufs(st_ctx* ctx, uint32_t on, uint32_t train, float alpha, uint32_t slots);
+cudaError_t guide_wave_begin(st_ctx* ctx, uint32_t slots, cudaStream_t st);
+cudaError_t guide_train_launch(st_ctx* ctx, float lr, int sms, cudaStream_t st, int* launches);
+cudaError_t guide_eval_launch(st_ctx* ctx, uint32_t n, float* d_raw, uint2* d_mix, cudaStream_t st);
+int guide_eval(st_ctx* ctx, const float* pos, const float* nrm, uint32_t n, float* raw, float* mix);
+int guide_grad(st_ctx* ctx, const float* pos, const float* nrm, const float* dir, const float* weight, uint32_t n,
+               float* grad, float* loss);
+void guide_unpack_host(uint2 v, float* out);
+void guide_box(st_ctx* ctx, st::f3& lo, float& inv_ext);     // the hash grid's box (st_capi.cu)
+
 struct StExt {
     SppmState sppm;
     OpticsState optics;
+    GuideState guide;
 };
 
 void ext_free(StExt& e);

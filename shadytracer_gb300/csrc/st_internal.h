@@ -23,6 +23,7 @@ namespace st {
 #define META_PASSED (1u << 24)            // a photon that has passed a delta event
 #define META_LENS_SHIFT 25u               // a camera path's lens field (2 bits): 1 delta events only since the eye,
                                           // 2 at its D, 3 delta events since its D (the map owns the sun it reaches)
+#define META_TRAIN (1u << 27)             // a camera path that holds a training record for the learned proposal
 #define META_LOW 0x00ffffffu
 #define SURF_NONE 0xffffu                 // hsurf: no medium asked (n1 is the material's own index of refraction)
 #define SURF_LEAVING 0xffffffffu          // hsurf: the surface seen from behind, the ray moved on
@@ -108,6 +109,32 @@ struct SppmBufs {
 
 struct __align__(32) Acc4 { double x, y, z, w; };   // FP64 mean rgb + the sample count
 
+// THE LEARNED PROPOSAL (st_guide.cu, st_guide.cuh): per hit-queue entry the mixture its vertex samples from; per path
+// (its pixel in the wave's frames) the training record of its first guided vertex and the light found after it; the
+// batch those records make at the wave's end; the weights the kernels read.
+struct GuideRec { float4 a, b; };         // a: position, pdf of the direction; b: normal, direction (oct16 bits),
+                                          // throughput luminance after the bounce, radiance luminance before it
+struct GuideSample { float4 a, b, c; };   // a: position, weight (incident luminance / pdf); b: normal; c: direction
+struct GuideDev {
+    uint32_t count, step, pad0, pad1;     // samples in the batch; Adam steps taken
+    float wsum, loss, loss_n, pad2;       // the batch's summed weight; the last step's summed loss and samples
+};
+struct GuideBufs {
+    uint32_t on = 0, train = 0;           // guided sampling; records and training
+    float alpha = 0.5f;                   // the guide's share of one-sample MIS
+    f3 lo = {0.f, 0.f, 0.f};              // the hash grid's box: its low corner and 1 / its longest side
+    float inv_ext = 1.f;
+    const float2* table = nullptr;        // hash-grid features, FP32
+    const uint16_t* wbf = nullptr;        // the network's weights, BF16 bits, [out][in] row-major, W1 W2 W3 W4
+    uint2* mix = nullptr;                 // 8 packed lobes a hit-queue entry
+    GuideRec* rec = nullptr;              // a path's record (by its pixel in the wave's frames)
+    float* acc = nullptr;                 // ...and the luminance found after its vertex
+    GuideSample* samp = nullptr;          // the training batch
+    GuideDev* dev = nullptr;
+    uint32_t cap = 0;                     // the batch's room
+    uint32_t keep = 0;                    // a record joins the batch when its hash is below this (of 2^32)
+};
+
 struct WaveArgs {
     Uni u;
     const DPrim* prims;
@@ -125,6 +152,7 @@ struct WaveArgs {
     SppmBufs sp;                          // the photon map, while it runs
     const uint2* inst_range = nullptr;   // a batch of instances (the optics bench): each one's [first, count) of the
                                          // table, the instance in meta.w; null for a picture
+    GuideBufs gd;                         // the learned proposal, while it runs
 };
 
 // launch wrappers (st_render.cu)
@@ -146,5 +174,8 @@ cudaError_t launch_march(const WaveArgs& a, int cur, int nxt, int last, int sms,
 cudaError_t launch_shade(const WaveArgs& a, int nxt, int side, int last, int sms, cudaStream_t s);
 cudaError_t launch_occlude(const WaveArgs& a, int side, int last, int sms, cudaStream_t s);
 cudaError_t launch_resolve(const WaveArgs& a, cudaStream_t s);
+// the learned proposal (st_guide.cu)
+cudaError_t launch_guide_infer(const WaveArgs& a, int sms, cudaStream_t s);
+cudaError_t launch_guide_collect(const WaveArgs& a, int sms, cudaStream_t s);
 
 }  // namespace st

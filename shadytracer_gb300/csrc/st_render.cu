@@ -15,6 +15,7 @@
 // warp keeps 32 rays in flight however uneven their step counts. The scene's primitive table is staged into
 // shared memory by one bulk copy (cp.async.bulk + mbarrier) per CTA and read as broadcasts. Nothing is read back
 // by the host inside a sample: every kernel sizes itself from the device counters.
+#include "st_guide.cuh"
 #include "st_kernels.cuh"
 
 namespace st {
@@ -404,10 +405,12 @@ __global__ void __launch_bounds__(256, 3) k_surface(WaveArgs a) {
 
 struct ShadowOut { bool valid; f3 org, dir, rad; float n; };
 
+template <bool GUIDE>
 __device__ __forceinline__ void shade_surface(const WaveArgs& a, const st_material* sm, float4 surf,
                                               f3& pos, f3& dir, float& ltot, float& n, f3& beta, float& sunmis,
                                               f3& rad, uint32_t& bounces, uint32_t& state, float& lam,
-                                              uint32_t& lens, float dh, Rng& rng, bool last, ShadowOut& sh) {
+                                              uint32_t& lens, float dh, Rng& rng, bool last, ShadowOut& sh,
+                                              uint32_t q, uint32_t& my, uint32_t gpix) {
     const Uni& u = a.u;
     float eps = march_tol(pos, u.tol);
     const uint32_t ids = __float_as_uint(surf.w);
@@ -462,6 +465,13 @@ __device__ __forceinline__ void shade_surface(const WaveArgs& a, const st_materi
     float etaFace = diffFace ? fminf(n0, n1) / fmaxf(n0, n1) : n0 / n1;
     Lobes lb = make_lobes(nrm, -dir, m, etaFace, a.tab, trans, specv);
     lb.etaT = n0 / nT;
+    // THE LEARNED PROPOSAL (st_guide.cuh): at an evaluable opaque vertex met from outside, the direction is drawn from
+    // the network's mixture with probability alpha, else from the BSDF, and weighed by f cos / (alpha q + (1 - alpha)
+    // p_bsdf) -- one-sample MIS, so the estimator stays unbiased whatever the network says; the environment's MIS
+    // weights take the same combined density on both sides
+    const bool guided = GUIDE && a.gd.on != 0u && !last && !inside && guide_vertex(m);
+    const uint2* __restrict__ gmix = a.gd.mix + (size_t)q * GUIDE_LOBES;
+    const float galpha = guided ? a.gd.alpha : 0.f;
     if (u.nee != 0u && !last) {                                       // light sampling (materials_pbr.js:1196-1330)
         float4 u0 = rng.next();
         float4 u1 = rng.next();
@@ -473,6 +483,7 @@ __device__ __forceinline__ void shade_surface(const WaveArgs& a, const st_materi
                 f3 le = env_radiance(u, L);
                 f3 f = lobes_eval(lb, a.tab, L, 0.f);
                 float pB = lobes_pdf(lb, L);
+                if (guided) pB = galpha * guide_pdf(gmix, L) + (1.f - galpha) * pB;
                 float w = mis_weight(pL, pB);
                 f3 contrib = beta * f * le * (fabsf(NoL) * (w / pL));
                 if (max3(contrib) > 1e-7f) {
@@ -487,7 +498,34 @@ __device__ __forceinline__ void shade_surface(const WaveArgs& a, const st_materi
             }
         }
     }
-    LobeSample smp = lobes_sample(lb, a.tab, rng.next());           // the bounce
+    LobeSample smp;                                                   // the bounce
+    float pGuided = 0.f;
+    if (guided) {
+        const float4 rg = rng.next();
+        if (rg.x < galpha) {
+            smp.dir = guide_sample(gmix, rg.y, rg.z, rg.w);
+        } else {
+            smp = lobes_sample(lb, a.tab, rng.next());
+        }
+        const float c = dot(nrm, smp.dir);
+        pGuided = galpha * guide_pdf(gmix, smp.dir) + (1.f - galpha) * lobes_pdf(lb, smp.dir);
+        smp.w = (c > 0.f && pGuided > 0.f) ? lobes_eval(lb, a.tab, smp.dir, 0.f) * (c / pGuided) : mk(0.f);
+        smp.ev = EV_EVAL;
+        smp.isDelta = false;
+        smp.transmitted = false;
+        // the path's first guided vertex keeps a training record: where, the direction and its density, the
+        // throughput after the bounce and the radiance before it (the light found after it is summed into acc)
+        if (GUIDE && a.gd.train && !(my & META_TRAIN) && max3(smp.w) > 0.f) {
+            GuideRec rc;
+            rc.a = make_float4(pos.x, pos.y, pos.z, pGuided);
+            rc.b = make_float4(__uint_as_float(guide_oct16(nrm)), __uint_as_float(guide_oct16(smp.dir)),
+                               luma(beta * smp.w), luma(rad));
+            a.gd.rec[gpix] = rc;
+            my |= META_TRAIN;
+        }
+    } else {
+        smp = lobes_sample(lb, a.tab, rng.next());
+    }
     dir = smp.dir;
     beta = beta * smp.w;
     if (smp.transmitted) {
@@ -504,7 +542,7 @@ __device__ __forceinline__ void shade_surface(const WaveArgs& a, const st_materi
     if (max3(smp.w) <= 0.f) state = RAY_ABSORBED;
     if (u.nee != 0u && !last) {                                       // the other half of MIS (:1370-1395)
         bool above = dot(nrm, dir) > 0.f && !smp.isDelta;
-        float pOut = smp.isDelta ? 0.f : lobes_pdf(lb, smp.dir);
+        float pOut = smp.isDelta ? 0.f : (guided ? pGuided : lobes_pdf(lb, smp.dir));
         float pLout = above ? env_pdf(u, dir, nrm) : 0.f;
         sunmis = pLout <= 0.f ? 1.f : mis_weight(pOut, pLout);
     } else {
@@ -559,6 +597,9 @@ __device__ __forceinline__ void shade_medium(const WaveArgs& a, f3& pos, f3& dir
     if (bounces > u.maxbounce) state = RAY_TERMINATED;
 }
 
+// GUIDE: the variant with the learned proposal (its sampling, records and their light), kept apart so the plain
+// kernel's registers stay as they were
+template <bool GUIDE>
 __global__ void __launch_bounds__(256) k_shade(WaveArgs a, int nxt, int side, int last) {
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ __align__(8) uint64_t mbar;
@@ -588,6 +629,7 @@ __global__ void __launch_bounds__(256) k_shade(WaveArgs a, int nxt, int side, in
         uint4 m4 = make_uint4(0, 0, 0, 0);
         uint32_t bounces = 0, seg = 0, state = RAY_TERMINATED;
         float lam = 0.f;
+        bool train_nee = false;
         if (valid) {
             slot = a.q.hit[q];
             float dh = a.q.hitd[q];
@@ -603,6 +645,7 @@ __global__ void __launch_bounds__(256) k_shade(WaveArgs a, int nxt, int side, in
                 const bool owned = u.sppm_on && ((m4.y >> META_LENS_SHIFT) & 3u) == 3u && sppm_covers(u, pos, dir);
                 rad = rad + beta * (owned ? env_sky(u, dir) : env_radiance(u, dir)) * sunmis;
             } else if (state == RAY_ACTIVE || state == RAY_SCATTER) {
+                train_nee = GUIDE && (m4.y & META_TRAIN) != 0u;       // light found past a record's vertex counts
                 uint32_t tile = slot % u.P, j = slot / u.P;
                 Rng rng = path_rng(sample_seed(u.seed, a.ctr->sample + j), tile, 1u + seg);
                 seg += 1;
@@ -615,8 +658,8 @@ __global__ void __launch_bounds__(256) k_shade(WaveArgs a, int nxt, int side, in
                 {
                     lam = a.pb.lam[slot];
                     uint32_t lens = (m4.y >> META_LENS_SHIFT) & 3u;
-                    shade_surface(a, sm, a.q.hsurf[q], pos, dir, ltot, n, beta, sunmis, rad, bounces, state, lam,
-                                  lens, dh, rng, last != 0, sh);
+                    shade_surface<GUIDE>(a, sm, a.q.hsurf[q], pos, dir, ltot, n, beta, sunmis, rad, bounces, state,
+                                         lam, lens, dh, rng, last != 0, sh, q, m4.y, gpix);
                     m4.y = (m4.y & ~(3u << META_LENS_SHIFT)) | (lens << META_LENS_SHIFT);
                 }
                 if (state == RAY_ACTIVE) {
@@ -632,7 +675,7 @@ __global__ void __launch_bounds__(256) k_shade(WaveArgs a, int nxt, int side, in
             if (sq < a.q.scap) {
                 s_org[sq] = f4(sh.org, 0.f);
                 s_dir[sq] = f4(sh.dir, __uint_as_float(gpix));
-                s_rad[sq] = f4(sh.rad, sh.n);
+                s_rad[sq] = f4(sh.rad, train_nee ? -sh.n : sh.n);    // a negative index: counted for a record
                 s_steps[sq] = 0u;
             } else {
                 dropped++;
@@ -655,6 +698,8 @@ __global__ void __launch_bounds__(256) k_shade(WaveArgs a, int nxt, int side, in
             deposit(fr, pix, rad, a.ctr);
             atomicAdd(&fr[pix].w, 1.f);
             paths++;
+            if (GUIDE && a.gd.train && (m4.y & META_TRAIN))
+                atomicAdd(&a.gd.acc[gpix], luma(rad) - a.gd.rec[gpix].b.w);
         }
     }
     for (int o = 16; o > 0; o >>= 1) {
@@ -723,7 +768,7 @@ __global__ void __launch_bounds__(256, 4) k_occlude(WaveArgs a, int last) {
                 if (idx == INVALID_SLOT && rank < avail) {
                     idx = a.u.sort_on ? a.q.ssorted[wpos + rank] : wpos + rank;
                     float4 o4 = i_org[idx], d4 = i_dir[idx];
-                    pos = xyz(o4); ltot = o4.w; dir = xyz(d4); n = i_rad[idx].w;
+                    pos = xyz(o4); ltot = o4.w; dir = xyz(d4); n = fabsf(i_rad[idx].w);
                     steps = i_steps[idx];
                     evals_here = 0;
                     if (steps == 0u) rays++;
@@ -759,6 +804,7 @@ __global__ void __launch_bounds__(256, 4) k_occlude(WaveArgs a, int last) {
             float4 r4 = i_rad[idx];
             uint32_t gpix = __float_as_uint(i_dir[idx].w);          // the pixel in the wave's frames
             deposit(a.frame, gpix, xyz(r4), a.ctr);
+            if (r4.w < 0.f && a.gd.train) atomicAdd(&a.gd.acc[gpix], luma(xyz(r4)));
         }
         if (more) {
             if (cp < a.q.scap) {
@@ -824,7 +870,7 @@ __global__ void __launch_bounds__(256) k_resolve(WaveArgs a) {
 // ------------------------------------------------------------------------------------------------------------
 // launch wrappers
 // ------------------------------------------------------------------------------------------------------------
-static int g_occ_march = 0, g_occ_occl = 0, g_occ_shade = 0, g_occ_surf = 0;
+static int g_occ_march = 0, g_occ_occl = 0, g_occ_shade = 0, g_occ_shade_g = 0, g_occ_surf = 0;
 
 cudaError_t launch_mf_tables(float* ec, float* ecavg, float* e1, cudaStream_t s) {
     const uint32_t N = MF_NIOR * MF_NR * MF_NMU + MF_NR * MF_NMU;
@@ -902,9 +948,15 @@ cudaError_t launch_surface(const WaveArgs& a, int sms, cudaStream_t s) {
 }
 cudaError_t launch_shade(const WaveArgs& a, int nxt, int side, int last, int sms, cudaStream_t s) {
     size_t smem = a.u.n_mats * sizeof(st_material);
-    if (smem > 48 * 1024) cudaFuncSetAttribute(k_shade, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (!g_occ_shade) g_occ_shade = occupancy((const void*)k_shade, smem);
-    k_shade<<<sms * g_occ_shade, 256, smem, s>>>(a, nxt, side, last);
+    if (a.gd.on) {
+        if (smem > 48 * 1024) cudaFuncSetAttribute(k_shade<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (!g_occ_shade_g) g_occ_shade_g = occupancy((const void*)k_shade<true>, smem);
+        k_shade<true><<<sms * g_occ_shade_g, 256, smem, s>>>(a, nxt, side, last);
+        return cudaGetLastError();
+    }
+    if (smem > 48 * 1024) cudaFuncSetAttribute(k_shade<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (!g_occ_shade) g_occ_shade = occupancy((const void*)k_shade<false>, smem);
+    k_shade<false><<<sms * g_occ_shade, 256, smem, s>>>(a, nxt, side, last);
     return cudaGetLastError();
 }
 template <int SIDE>

@@ -161,6 +161,45 @@ class PathTracer:
     def stream(self):
         return self.L.st_stream(self.ctx)
 
+    # ---- the learned proposal (st_params.guide; include/shadytracer.h st_mlp_*) ----
+    def mlp_weights(self):
+        """Every parameter, FP32: W1 (64x48), W2, W3 (64x64), W4 (40x64), then the hash grid's features."""
+        w = np.zeros(T.MLP_PARAMS, np.float32)
+        check(self.L.st_mlp_get_weights(self.ctx, w.ctypes.data_as(C.c_void_p), w.size), self.ctx, "st_mlp_get_weights")
+        return w
+
+    def set_mlp_weights(self, w):
+        w = np.ascontiguousarray(w, np.float32)
+        check(self.L.st_mlp_set_weights(self.ctx, w.ctypes.data_as(C.c_void_p), w.size), self.ctx, "st_mlp_set_weights")
+
+    def mlp_eval(self, pos, nrm):
+        """The network at n points: (raw outputs n x 40, mixture n x 8 x [mean xyz, kappa, weight] as sampled)."""
+        pos = np.ascontiguousarray(pos, np.float32)
+        nrm = np.ascontiguousarray(nrm, np.float32)
+        n = len(pos)
+        raw = np.zeros((n, 40), np.float32)
+        mix = np.zeros((n, 8, 5), np.float32)
+        P = C.c_void_p
+        check(self.L.st_mlp_eval(self.ctx, pos.ctypes.data_as(P), nrm.ctypes.data_as(P), n, raw.ctypes.data_as(P),
+                                 mix.ctypes.data_as(P)), self.ctx, "st_mlp_eval")
+        return raw, mix
+
+    def mlp_grad(self, pos, nrm, dirs, weight):
+        """The gradient of the training loss at a batch (no step): (gradient of every parameter, summed loss)."""
+        arrs = [np.ascontiguousarray(a, np.float32) for a in (pos, nrm, dirs, weight)]
+        g = np.zeros(T.MLP_PARAMS, np.float32)
+        loss = C.c_float()
+        P = C.c_void_p
+        check(self.L.st_mlp_grad(self.ctx, *[a.ctypes.data_as(P) for a in arrs], len(arrs[0]), g.ctypes.data_as(P),
+                                 C.byref(loss)), self.ctx, "st_mlp_grad")
+        return g, loss.value
+
+    def mlp_stats(self):
+        s = T.StMlpStats()
+        check(self.L.st_mlp_stats_read(self.ctx, C.byref(s)), self.ctx, "st_mlp_stats_read")
+        return {"steps": s.steps, "samples": s.samples, "loss": s.loss, "mean_weight": s.mean_weight,
+                "box_lo": list(s.box_lo), "box_inv_ext": s.box_inv_ext}
+
 
 def create_path_tracer(scene=None, device=0):
     """createPathTracer (lib/pathtracer/index.js:90) + RT.init: a context on `device` with `scene` loaded."""

@@ -56,7 +56,9 @@ class StParams(C.Structure):
                 ("sun_hint", C.c_uint32), ("seed", C.c_uint32), ("maxaverages", C.c_uint32),
                 ("eps", C.c_float), ("budget", C.c_uint32), ("samples_per_wave", C.c_uint32),
                 ("sppm", C.c_uint32), ("sppm_photons", C.c_uint32), ("sppm_r1", C.c_float),
-                ("sppm_alpha", C.c_float), ("sppm_half", C.c_float), ("sppm_learn", C.c_uint32)]
+                ("sppm_alpha", C.c_float), ("sppm_half", C.c_float), ("sppm_learn", C.c_uint32),
+                ("guide", C.c_uint32), ("guide_alpha", C.c_float), ("guide_lr", C.c_float),
+                ("guide_train", C.c_uint32), ("guide_seed", C.c_uint32)]
 
 
 class StView(C.Structure):
@@ -85,6 +87,14 @@ class StKernelTime(C.Structure):
 class StSppmStats(C.Structure):
     _fields_ = [("stored", C.c_uint32), ("gathers", C.c_uint32), ("cut", C.c_uint32),
                 ("visits_max", C.c_uint32), ("visits", C.c_uint64)]
+
+
+class StMlpStats(C.Structure):
+    _fields_ = [("steps", C.c_uint32), ("samples", C.c_uint32), ("loss", C.c_float), ("mean_weight", C.c_float),
+                ("box_lo", C.c_float * 3), ("box_inv_ext", C.c_float)]
+
+
+MLP_PARAMS = 13824 + 1048576        # ST_MLP_PARAMS: W1 W2 W3 W4 then the hash grid's features
 
 
 class StOpticsSource(C.Structure):
@@ -143,6 +153,11 @@ def default_params(**kw):
     p.sppm_alpha = 0.0
     p.sppm_half = 0.0
     p.sppm_learn = 0
+    p.guide = 0
+    p.guide_alpha = 0.0
+    p.guide_lr = 0.0
+    p.guide_train = 1
+    p.guide_seed = 0
     for k, v in kw.items():
         if not hasattr(p, k):
             raise KeyError(k)
