@@ -338,16 +338,16 @@ int  st_optics_run(st_ctx* ctx, const st_optics_batch* batch, double* far, doubl
 
 /* ---- the learned proposal (st_params.guide) ----
  * The parameters, FP32, in one array of ST_MLP_PARAMS: W1 (64 x 48), W2 (64 x 64), W3 (64 x 64), W4 (40 x 64), each
- * [out][in] row-major, then the hash grid's features (16 levels x 2^15 entries x 2). Inputs: 2 features a level of a
- * trilinear blend over the box's cells (level l has floor(8 * 128^(l/15)) cells across the box's longest side), then
+ * [out][in] row-major, then the hash grid's features (16 levels x 2^12 entries x 2). Inputs: 2 features a level of a
+ * trilinear blend over the box's cells (level l has floor(2 * 16^(l/15)) cells across the box's longest side), then
  * the 16 real spherical harmonics of degree <= 3 of the normal; outputs: 8 lobes x (mean direction, unnormalised;
- * log kappa, clamped to [-1, 8]; mixture logit). */
-#define ST_MLP_PARAMS (13824u + 1048576u)
+ * log kappa, clamped to [-1, 6]; mixture logit). */
+#define ST_MLP_PARAMS (13824u + 131072u)
 typedef struct st_mlp_stats {
     uint32_t steps;               /* Adam steps since the weights were set                          */
     uint32_t samples;             /* training samples in the last wave's batch                      */
     float    loss;                /* the last wave's loss a sample                                  */
-    float    mean_weight;         /* the last batch's mean weight (incident luminance / pdf)        */
+    float    mean_weight;         /* the last batch's mean weight (f cos L_in / pdf at the vertex)   */
     float    box_lo[3];           /* the hash grid's box: its low corner, metres                     */
     float    box_inv_ext;         /* ... and 1 / its longest side                                    */
 } st_mlp_stats;
@@ -360,7 +360,13 @@ int  st_mlp_eval(st_ctx* ctx, const float* pos, const float* nrm, uint32_t n, fl
  * at 20, with respect to every parameter, at 1 to 16384 samples, without a step; loss: the sum */
 int  st_mlp_grad(st_ctx* ctx, const float* pos, const float* nrm, const float* dir, const float* weight, uint32_t n,
                  float* grad, float* loss);
+/* `steps` training steps (Adam, learning rate lr; 0: 0.005) on the given batch of 1 to 131072 samples, mini-batches of
+ * 16384 in turn: what a wave's end does with the records its paths made */
+int  st_mlp_train(st_ctx* ctx, const float* pos, const float* nrm, const float* dir, const float* weight, uint32_t n,
+                  uint32_t steps, float lr);
 int  st_mlp_stats_read(st_ctx* ctx, st_mlp_stats* out);
+/* the last wave's training batch, at most max_n samples of 10 floats (position, normal, direction, weight) */
+int  st_mlp_read_batch(st_ctx* ctx, float* out, uint32_t max_n, uint32_t* n);
 
 /* ---- a render that allocates nothing ----
  * No counterpart in the reference: an entry point for hosts that may not allocate device memory when they want a

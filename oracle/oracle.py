@@ -399,7 +399,7 @@ def optics_run(bench, ray_counts, nC=360, nG=181, cells=0, half=1.0, height=1.0,
 
 # ---- the learned proposal (st_oracle_guide.h) ----
 GUIDE_NW = 13824
-GUIDE_NPARAM = 13824 + 1048576
+GUIDE_NPARAM = 13824 + 131072
 
 
 def _f32(a, shape=None):

@@ -15,11 +15,11 @@
 namespace sto {
 namespace guide {
 
-const int LEVELS = 16, T = 1 << 15, IN = 48, H = 64, OUT = 40, LOBES = 8;
+const int LEVELS = 16, T = 1 << 12, IN = 48, H = 64, OUT = 40, LOBES = 8;
 const int W1 = 0, W2 = W1 + H * IN, W3 = W2 + H * H, W4 = W3 + H * H, NW = W4 + OUT * H;
 const int NHASH = LEVELS * T * 2, NPARAM = NW + NHASH;
-const double KLO = -1.0, KHI = 8.0, WCAP = 20.0;
-const float RES[LEVELS] = {8, 11, 15, 21, 29, 40, 55, 76, 106, 147, 203, 280, 388, 536, 741, 1024};
+const double KLO = -1.0, KHI = 6.0, WCAP = 1000.0;
+const float RES[LEVELS] = {2, 2, 2, 3, 4, 5, 6, 7, 8, 10, 12, 15, 18, 22, 26, 32};
 
 // round to the nearest BF16, ties to even (the finite values the network meets)
 inline float bf16(float x) {

@@ -47,7 +47,9 @@ SIGNATURES = {
     "st_mlp_set_weights": ([P, P, C.c_size_t], C.c_int),
     "st_mlp_eval": ([P, P, P, C.c_uint32, P, P], C.c_int),
     "st_mlp_grad": ([P, P, P, P, P, C.c_uint32, P, P], C.c_int),
+    "st_mlp_train": ([P, P, P, P, P, C.c_uint32, C.c_uint32, C.c_float], C.c_int),
     "st_mlp_stats_read": ([P, C.POINTER(T.StMlpStats)], C.c_int),
+    "st_mlp_read_batch": ([P, P, C.c_uint32, C.POINTER(C.c_uint32)], C.c_int),
     "st_struct_sizes": ([P, C.c_int], C.c_int),
     "st_stream": ([P], C.c_void_p),
 }

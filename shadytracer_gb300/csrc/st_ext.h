@@ -80,6 +80,8 @@ int guide_eval(st_ctx* ctx, const float* pos, const float* nrm, uint32_t n, floa
 int guide_grad(st_ctx* ctx, const float* pos, const float* nrm, const float* dir, const float* weight, uint32_t n,
                float* grad, float* loss);
 void guide_unpack_host(uint2 v, float* out);
+int guide_train_samples(st_ctx* ctx, const float* pos, const float* nrm, const float* dir, const float* weight,
+                        uint32_t n, uint32_t steps, float lr);
 void guide_box(st_ctx* ctx, st::f3& lo, float& inv_ext);     // the hash grid's box (st_capi.cu)
 
 struct StExt {

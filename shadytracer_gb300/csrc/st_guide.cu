@@ -3,16 +3,17 @@
 // tensor cores, the weight gradients as one GEMM over the batch, Adam), with the C ABI's st_mlp_* entry points.
 //
 //   k_guide_infer     after the surface kernel: each guided vertex's mixture (8 packed vMF lobes), 16 vertices a warp
-//   k_guide_collect   a wave's end: each path's record -> (position, normal, direction, incident luminance / pdf)
+//   k_guide_collect   a wave's end: each path's record -> (position, normal, direction, f cos L_in / pdf)
 //   k_guide_train     a mini-batch: forward, the loss's gradient at the 40 outputs, backward to the 48 inputs; the
 //                     activations and their gradients (BF16) for the weight GEMM; the hash grid's gradient by atomics
 //   k_guide_dw        dW_l = dZ_l^T A_l over the mini-batch (K = samples), split over the blocks, FP32 atomics
 //   k_guide_adam      Adam on the FP32 weights and features; the BF16 copy the kernels read
 //
-// THE LOSS. A record at vertex x, direction w drawn with density p, and the luminance L the path found along w
-// (everything it collected after the bounce, over the throughput the bounce gave it) is one Monte-Carlo sample of
-// the incident radiance; the network's mixture q is fitted to it by minimising E[-(L / p) log q(w)], the cross
-// entropy of q against the normalised incident radiance (the KL divergence up to a constant), with each weight L / p
+// THE LOSS. A record at vertex x, direction w drawn with density p, and the luminance the path collected after the
+// bounce over the throughput that reached x -- which is f(w) cos(w) L_in(w) / p(w), the integrand over the density
+// -- is one Monte-Carlo sample of the light the vertex reflects from w; the network's mixture q is fitted to that
+// integrand by minimising E[-(f cos L_in / p) log q(w)], the cross entropy of q against the normalised integrand
+// (the KL divergence up to a constant: the density that would make the vertex's estimate noise-free), each weight
 // over the batch's mean and capped at GUIDE_WCAP.
 #include <algorithm>
 #include <cmath>
@@ -28,9 +29,9 @@
 namespace st {
 
 #define GUIDE_MB 16384u                 // samples a training step
-#define GUIDE_STEPS 4u                  // training steps a wave
+#define GUIDE_STEPS 8u                  // training steps a wave
 #define GUIDE_CAP (GUIDE_MB * GUIDE_STEPS)
-#define GUIDE_WCAP 20.f
+#define GUIDE_WCAP 1000.f
 #define GUIDE_ACT 8u                    // activation arrays of a mini-batch: X H1 H2 H3 dY dH3 dH2 dH1
 #define GUIDE_ACT_LD 64u
 // the weights in shared memory: forward W1 [64][56], W2 [64][72], W3 [64][72], W4 [40][72]; the training kernel
@@ -122,7 +123,7 @@ __global__ void __launch_bounds__(256) k_guide_infer(WaveArgs a) {
             const uint32_t slot = a.q.hit[q];
             const uint32_t my = a.pb.meta[slot].y;
             const uint32_t ids = __float_as_uint(a.q.hsurf[q].w);
-            if (((my >> 16) & 0xffu) == RAY_ACTIVE && ids != SURF_LEAVING && a.q.hitd[q] >= 0.f)
+            if (((my >> 16) & 0xffu) == RAY_ACTIVE && (my & 0xffu) == 0u && ids != SURF_LEAVING && a.q.hitd[q] >= 0.f)
                 want = guide_vertex(sm[ids & 0xffffu]);
         }
         const uint32_t m = __ballot_sync(FULL_MASK, want);
@@ -182,8 +183,7 @@ __global__ void __launch_bounds__(256) k_guide_collect(WaveArgs a) {
         }
         const uint32_t at = warp_append(&a.gd.dev->count, take);
         if (take && at < a.gd.cap) {
-            const float L = a.gd.acc[i] / fmaxf(r.b.z, 1e-30f);
-            const float W = fmaxf(L, 0.f) / r.a.w;
+            const float W = fmaxf(a.gd.acc[i], 0.f) / fmaxf(r.b.z, 1e-30f);    // f cos L_in / p
             GuideSample s;
             s.a = make_float4(r.a.x, r.a.y, r.a.z, W);
             const f3 nn = guide_unoct16(__float_as_uint(r.b.x)), d = guide_unoct16(__float_as_uint(r.b.y));
@@ -717,6 +717,42 @@ int st_mlp_grad(st_ctx* ctx, const float* pos, const float* nrm, const float* di
     return guide_grad(ctx, pos, nrm, dir, weight, n, grad, loss);
 }
 
+// training steps on a given batch (up to GUIDE_CAP samples, mini-batches of GUIDE_MB in turn): the step a wave takes,
+// on samples the caller chose
+int st_mlp_train(st_ctx* ctx, const float* pos, const float* nrm, const float* dir, const float* weight, uint32_t n,
+                 uint32_t steps, float lr) {
+    if (!ctx || !pos || !nrm || !dir || !weight) return ST_ERR_ARG;
+    if (n == 0 || n > GUIDE_CAP) { ctx_set_error(ctx, "st_mlp_train: 1 to 131072 samples"); return ST_ERR_ARG; }
+    cudaSetDevice(ctx_device(ctx));
+    GuideState& g = ctx_ext(ctx).guide;
+    if (!g.param) { ctx_set_error(ctx, "the learned proposal has no weights"); return ST_ERR_STATE; }
+    return guide_train_samples(ctx, pos, nrm, dir, weight, n, steps, lr > 0.f ? lr : 0.005f);
+}
+
+// the last wave's training batch: per sample position, normal, direction, weight (10 floats); returns how many
+int st_mlp_read_batch(st_ctx* ctx, float* out, uint32_t max_n, uint32_t* n) {
+    if (!ctx || !out || !n) return ST_ERR_ARG;
+    cudaSetDevice(ctx_device(ctx));
+    GuideState& g = ctx_ext(ctx).guide;
+    *n = 0;
+    if (!g.dev) return ST_OK;
+    GuideDev d;
+    cudaStream_t st = ctx_stream(ctx);
+    if (cudaStreamSynchronize(st) || cudaMemcpy(&d, g.dev, sizeof(d), cudaMemcpyDeviceToHost)) return ST_ERR_CUDA;
+    const uint32_t m = std::min(std::min(d.count, GUIDE_CAP), max_n);
+    std::vector<GuideSample> hs(m);
+    if (m && cudaMemcpy(hs.data(), g.samp, m * sizeof(GuideSample), cudaMemcpyDeviceToHost)) return ST_ERR_CUDA;
+    for (uint32_t i = 0; i < m; i++) {
+        float* o = out + 10 * (size_t)i;
+        o[0] = hs[i].a.x; o[1] = hs[i].a.y; o[2] = hs[i].a.z;
+        o[3] = hs[i].b.x; o[4] = hs[i].b.y; o[5] = hs[i].b.z;
+        o[6] = hs[i].c.x; o[7] = hs[i].c.y; o[8] = hs[i].c.z;
+        o[9] = hs[i].a.w;
+    }
+    *n = m;
+    return ST_OK;
+}
+
 int st_mlp_stats_read(st_ctx* ctx, st_mlp_stats* out) {
     if (!ctx || !out) return ST_ERR_ARG;
     cudaSetDevice(ctx_device(ctx));
@@ -856,4 +892,52 @@ void guide_unpack_host(uint2 v, float* out) {
     out[0] = x / l; out[1] = y / l; out[2] = z / l;
     out[3] = half_to_float((uint16_t)(v.y & 0xffffu));
     out[4] = half_to_float((uint16_t)(v.y >> 16));
+}
+
+int guide_train_samples(st_ctx* ctx, const float* pos, const float* nrm, const float* dir, const float* weight,
+                        uint32_t n, uint32_t steps, float lr) {
+    GuideState& g = ctx_ext(ctx).guide;
+    cudaStream_t st = ctx_stream(ctx);
+    std::vector<GuideSample> hs(n);
+    double wsum = 0.0;
+    for (uint32_t i = 0; i < n; i++) {
+        hs[i].a = make_float4(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2], weight[i]);
+        hs[i].b = make_float4(nrm[3 * i], nrm[3 * i + 1], nrm[3 * i + 2], 0.f);
+        hs[i].c = make_float4(dir[3 * i], dir[3 * i + 1], dir[3 * i + 2], 0.f);
+        wsum += weight[i];
+    }
+    GuideDev d;
+    cudaError_t e = cudaMemcpyAsync(g.samp, hs.data(), n * sizeof(GuideSample), cudaMemcpyHostToDevice, st);
+    if (!e) e = cudaMemcpyAsync(&d, g.dev, sizeof(d), cudaMemcpyDeviceToHost, st);
+    if (!e) e = cudaStreamSynchronize(st);
+    if (e) { ctx_set_error(ctx, std::string("st_mlp_train: ") + cudaGetErrorString(e)); return ST_ERR_CUDA; }
+    d.count = n;
+    d.wsum = (float)wsum;
+    d.loss = 0.f;
+    d.loss_n = 0.f;
+    e = cudaMemcpyAsync(g.dev, &d, sizeof(d), cudaMemcpyHostToDevice, st);
+    GuideTrain tr;
+    tr.samp = g.samp;
+    tr.dev = g.dev;
+    guide_box(ctx, tr.lo, tr.inv_ext);
+    tr.table = reinterpret_cast<const float2*>(g.param + GUIDE_NW);
+    tr.gtable = reinterpret_cast<float2*>(g.grad + GUIDE_NW);
+    tr.wbf = g.wbf;
+    tr.act = g.act;
+    tr.gw = g.grad;
+    const size_t smem = (size_t)SW_ALL * 2;
+    if (!e) e = cudaFuncSetAttribute(k_guide_train, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    const uint32_t nmb = (n + GUIDE_MB - 1) / GUIDE_MB;
+    const int sms = ctx_sms(ctx);
+    for (uint32_t s = 0; s < steps && !e; s++) {
+        tr.first = (s % nmb) * GUIDE_MB;
+        k_guide_train<<<sms * 2, 256, smem, st>>>(tr);
+        k_guide_dw<<<sms * 2, 256, 0, st>>>(g.dev, tr.first, g.act, g.grad);
+        k_guide_step<<<1, 32, 0, st>>>(g.dev, tr.first);
+        k_guide_adam<<<sms * 4, 256, 0, st>>>(g.dev, tr.first, lr, g.param, g.grad, g.m1, g.m2, g.wbf);
+        e = cudaGetLastError();
+    }
+    if (!e) e = cudaStreamSynchronize(st);
+    if (e) { ctx_set_error(ctx, std::string("st_mlp_train: ") + cudaGetErrorString(e)); return ST_ERR_CUDA; }
+    return ST_OK;
 }

@@ -8,7 +8,7 @@
 // 2012).
 //
 // THE NETWORK. Input 48: 16 hash-grid levels x 2 features (a trilinear blend of the 8 corners' entries; level l's
-// resolution 8 * 128^(l/15) cells across the scene's bounding box, floored) and the 16 real
+// resolution 2 * 16^(l/15) cells across the scene's bounding box, floored) and the 16 real
 // spherical harmonics of degree <= 3 of the normal. Three hidden layers of 64, ReLU, no biases (the constant harmonic
 // is one); output 40 = 8 lobes x (mean direction m, 3, unnormalised; log kappa; mixture logit). BF16 operands, FP32
 // accumulation (mma.sync m16n8k16), weights [out][in] row-major.
@@ -21,7 +21,7 @@
 namespace st {
 
 #define GUIDE_LEVELS 16u
-#define GUIDE_T (1u << 15)                       // hash-table entries a level
+#define GUIDE_T (1u << 12)                       // hash-table entries a level
 #define GUIDE_IN 48u
 #define GUIDE_H 64u
 #define GUIDE_OUT 40u
@@ -31,18 +31,21 @@ namespace st {
 #define GUIDE_W3 (GUIDE_W2 + GUIDE_H * GUIDE_H)
 #define GUIDE_W4 (GUIDE_W3 + GUIDE_H * GUIDE_H)
 #define GUIDE_NW (GUIDE_W4 + GUIDE_OUT * GUIDE_H)               // 13 824 network weights
-#define GUIDE_NHASH (GUIDE_LEVELS * GUIDE_T * 2u)                // 1 048 576 hash-grid features
+#define GUIDE_NHASH (GUIDE_LEVELS * GUIDE_T * 2u)                // 131 072 hash-grid features
 #define GUIDE_NPARAM (GUIDE_NW + GUIDE_NHASH)
-#define GUIDE_KLO (-1.f)                          // log kappa's clamp: kappa in [e^-1, e^8]
-#define GUIDE_KHI 8.f
+#define GUIDE_KLO (-1.f)                          // log kappa's clamp: kappa in [e^-1, e^6]
+#define GUIDE_KHI 6.f
 // shared-memory rows of the weights, padded by 8 BF16 so the fragment loads of 8 rows meet 8 different bank groups
 #define GUIDE_LD_IN (GUIDE_IN + 8u)
 #define GUIDE_LD_H (GUIDE_H + 8u)
 
-// the resolution of level l (cells across the box's longest side): floor(8 * 128^(l/15)), 8 to 1024, as integers so
-// every side of the build (and the oracle) agrees on them exactly
-static __constant__ float c_guide_res[GUIDE_LEVELS] = {8, 11, 15, 21, 29, 40, 55, 76, 106, 147, 203, 280, 388, 536, 741, 1024};
-static const float h_guide_res[GUIDE_LEVELS] = {8, 11, 15, 21, 29, 40, 55, 76, 106, 147, 203, 280, 388, 536, 741, 1024};
+// the resolution of level l (cells across the box's longest side): floor(2 * 16^(l/15)), 2 to 32, as integers so
+// every side of the build (and the oracle) agrees on them exactly. The finest cell is the box over 32 (25 cm in a
+// room) and a level holds 4096 entries: the light a point receives changes slowly, and a finer or larger grid only
+// memorises the noise of single paths (held-out cross entropy on a wave's records: 1.52 here, 2.9 with 6 mm cells
+// and 32 768 entries a level, 1.66 for the cosine lobe alone).
+static __constant__ float c_guide_res[GUIDE_LEVELS] = {2, 2, 2, 3, 4, 5, 6, 7, 8, 10, 12, 15, 18, 22, 26, 32};
+static const float h_guide_res[GUIDE_LEVELS] = {2, 2, 2, 3, 4, 5, 6, 7, 8, 10, 12, 15, 18, 22, 26, 32};
 __host__ __device__ __forceinline__ float guide_res(uint32_t l) {
 #ifdef __CUDA_ARCH__
     return c_guide_res[l];
@@ -97,11 +100,19 @@ __host__ __device__ __forceinline__ f3 guide_unit(f3 p, f3 lo, float inv_ext) {
               fminf(fmaxf((p.z - lo.z) * inv_ext, 0.f), 1.f));
 }
 
-// the vertex a camera path's shade guides (met from outside): an opaque surface with no delta lobe, not emitting
+// the vertex a camera path's shade guides (met from outside): an opaque, mostly dielectric surface rough enough that
+// what it reflects hardly depends on the direction it is seen from (the network does not see that direction: at a
+// glossy vertex its one mixture for every view would fit none), not emitting
+#define GUIDE_MIN_ROUGHNESS 0.5f
 __device__ __forceinline__ bool guide_vertex(const st_material& m) {
-    const float r = clampf(m.roughness, 0.f, 1.f);
-    return m.transmission <= 0.f && r * r >= MF_ALPHA_MIN &&
+    return m.transmission <= 0.f && m.metallic < 0.5f && m.roughness >= GUIDE_MIN_ROUGHNESS &&
            fmaxf(fmaxf(m.emissive[0], m.emissive[1]), m.emissive[2]) <= 0.f;
+}
+// the guide's share of the one-sample MIS: ramped in over its first GUIDE_RAMP training steps (a network not yet
+// trained would only take samples from the BSDF); fixed within a wave, where the weights are
+#define GUIDE_RAMP 64.f
+__device__ __forceinline__ float guide_share(float alpha, const uint32_t* step, uint32_t train) {
+    return train ? alpha * fminf(1.f, (float)*step / GUIDE_RAMP) : alpha;
 }
 
 // ---------------------------------------------------------------------------------------------------------------

@@ -113,8 +113,8 @@ struct __align__(32) Acc4 { double x, y, z, w; };   // FP64 mean rgb + the sampl
 // (its pixel in the wave's frames) the training record of its first guided vertex and the light found after it; the
 // batch those records make at the wave's end; the weights the kernels read.
 struct GuideRec { float4 a, b; };         // a: position, pdf of the direction; b: normal, direction (oct16 bits),
-                                          // throughput luminance after the bounce, radiance luminance before it
-struct GuideSample { float4 a, b, c; };   // a: position, weight (incident luminance / pdf); b: normal; c: direction
+                                          // throughput luminance reaching the vertex, radiance luminance before it
+struct GuideSample { float4 a, b, c; };   // a: position, weight (f cos L_in / pdf); b: normal; c: direction
 struct GuideDev {
     uint32_t count, step, pad0, pad1;     // samples in the batch; Adam steps taken
     float wsum, loss, loss_n, pad2;       // the batch's summed weight; the last step's summed loss and samples

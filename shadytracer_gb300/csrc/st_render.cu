@@ -469,9 +469,9 @@ __device__ __forceinline__ void shade_surface(const WaveArgs& a, const st_materi
     // the network's mixture with probability alpha, else from the BSDF, and weighed by f cos / (alpha q + (1 - alpha)
     // p_bsdf) -- one-sample MIS, so the estimator stays unbiased whatever the network says; the environment's MIS
     // weights take the same combined density on both sides
-    const bool guided = GUIDE && a.gd.on != 0u && !last && !inside && guide_vertex(m);
+    const bool guided = GUIDE && a.gd.on != 0u && !last && !inside && bounces == 1u && guide_vertex(m);
     const uint2* __restrict__ gmix = a.gd.mix + (size_t)q * GUIDE_LOBES;
-    const float galpha = guided ? a.gd.alpha : 0.f;
+    const float galpha = guided ? guide_share(a.gd.alpha, &a.gd.dev->step, a.gd.train) : 0.f;
     if (u.nee != 0u && !last) {                                       // light sampling (materials_pbr.js:1196-1330)
         float4 u0 = rng.next();
         float4 u1 = rng.next();
@@ -514,12 +514,12 @@ __device__ __forceinline__ void shade_surface(const WaveArgs& a, const st_materi
         smp.isDelta = false;
         smp.transmitted = false;
         // the path's first guided vertex keeps a training record: where, the direction and its density, the
-        // throughput after the bounce and the radiance before it (the light found after it is summed into acc)
+        // throughput reaching the vertex and the radiance before it (the light found after it is summed into acc)
         if (GUIDE && a.gd.train && !(my & META_TRAIN) && max3(smp.w) > 0.f) {
             GuideRec rc;
             rc.a = make_float4(pos.x, pos.y, pos.z, pGuided);
             rc.b = make_float4(__uint_as_float(guide_oct16(nrm)), __uint_as_float(guide_oct16(smp.dir)),
-                               luma(beta * smp.w), luma(rad));
+                               luma(beta), luma(rad));
             a.gd.rec[gpix] = rc;
             my |= META_TRAIN;
         }

@@ -194,6 +194,22 @@ class PathTracer:
                                  C.byref(loss)), self.ctx, "st_mlp_grad")
         return g, loss.value
 
+    def mlp_train(self, pos, nrm, dirs, weight, steps, lr=0.0):
+        """`steps` Adam steps on a given batch (what a wave's end does with its paths' records)."""
+        arrs = [np.ascontiguousarray(a, np.float32) for a in (pos, nrm, dirs, weight)]
+        P = C.c_void_p
+        check(self.L.st_mlp_train(self.ctx, *[a.ctypes.data_as(P) for a in arrs], len(arrs[0]), int(steps), float(lr)),
+              self.ctx, "st_mlp_train")
+
+    def mlp_batch(self):
+        """The last wave's training batch: (n x 3 positions, normals, directions; n weights)."""
+        out = np.zeros((131072, 10), np.float32)
+        n = C.c_uint32()
+        check(self.L.st_mlp_read_batch(self.ctx, out.ctypes.data_as(C.c_void_p), 131072, C.byref(n)), self.ctx,
+              "st_mlp_read_batch")
+        b = out[:n.value]
+        return b[:, 0:3], b[:, 3:6], b[:, 6:9], b[:, 9]
+
     def mlp_stats(self):
         s = T.StMlpStats()
         check(self.L.st_mlp_stats_read(self.ctx, C.byref(s)), self.ctx, "st_mlp_stats_read")

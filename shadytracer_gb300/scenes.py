@@ -178,13 +178,17 @@ ROOM_HALF = (3.0, 2.0, 1.5)          # a 6 x 4 x 3 m room, floor at z = 0
 ROOM_WALL = 0.1
 
 
-def sdf_room(width=1920, height=1080, spp=64, maxbounce=8, seed=1, n_prims=24, prim_seed=2):
+def sdf_room(width=1920, height=1080, spp=64, maxbounce=8, seed=1, n_prims=24, prim_seed=2, finish="mixed",
+             sky_illuminance=10000.0, ground_luminance=1000.0):
     """A 6 x 4 x 3 m room (its walls a hollow box 0.1 m thick, a 2 x 1.5 m window in the +y wall) holding
     `n_prims` primitives drawn from PCG32(prim_seed): types uniform over {box, sphere, torus, rounded prism}, sizes
     0.15-0.4 m, placed uniformly in the room, randomly turned, smooth-unioned in order with radii U(0.02, 0.1) m.
     Materials: roughness U(0.05, 1), albedo U(0.2, 0.9) per channel, 20 % metallic (the rest plastic). Lit by a
     100 klx sun (0.53 degrees, 35 degrees up) and a uniform sky of 10 klx on the level (3183 cd/m^2) through the
-    window. March tolerance 1e-4 m."""
+    window. March tolerance 1e-4 m. finish="diffuse": every object Lambertian of its drawn albedo (the same draws, the
+    same geometry), so most of the room is lit by the light the sunlit floor and walls send on -- the learned
+    proposal's workload; sky_illuminance and ground_luminance near 0 leave the sun's patch on the floor the room's only
+    light after the sun itself."""
     rng = Pcg32(prim_seed)
     mats = [air(), diffuse((0.75, 0.73, 0.70))]
     hx, hy, hz = ROOM_HALF
@@ -207,7 +211,10 @@ def sdf_room(width=1920, height=1080, spp=64, maxbounce=8, seed=1, n_prims=24, p
         rough = rng.uniform(0.05, 1.0)
         albedo = (rng.uniform(0.2, 0.9), rng.uniform(0.2, 0.9), rng.uniform(0.2, 0.9))
         is_metal = rng.uniform() < 0.2
-        mats.append(metal(albedo, rough) if is_metal else plastic(albedo, rough))
+        if finish == "diffuse":
+            mats.append(diffuse(albedo))
+        else:
+            mats.append(metal(albedo, rough) if is_metal else plastic(albedo, rough))
         if kind == ST_PRIM_BOX:
             params = (size, size * rng.uniform(0.5, 1.0), size * rng.uniform(0.5, 1.0))
         elif kind == ST_PRIM_SPHERE:
@@ -218,9 +225,10 @@ def sdf_room(width=1920, height=1080, spp=64, maxbounce=8, seed=1, n_prims=24, p
             params = (float(3 + int(rng.uniform() * 4)), size, size * rng.uniform(0.8, 2.0), 0.02)
         prims.append(prim(kind, pos=pos, params=params, material=len(mats) - 1,
                           op=ST_OP_ITEM if i == 0 else ST_OP_SMOOTH, k=k, rot=rot_from_quat(q)))
-    s = Scene(prims, mats, env_radius=20.0, name="room24")
+    s = Scene(prims, mats, env_radius=20.0, name="room24" if finish == "mixed" else "room24-diffuse")
     s.params = default_params(width=width, height=height, maxbounce=maxbounce, sun_elevation=35.0, sun_azimuth=20.0,
-                              sun_illuminance=100000.0, sky_luminance=10000.0 / math.pi, ground_luminance=1000.0,
+                              sun_illuminance=100000.0, sky_luminance=sky_illuminance / math.pi,
+                              ground_luminance=ground_luminance,
                               eps=1e-4, seed=seed)
     eye = (-2.6, -1.6, 1.7)
     target = (0.8, 0.9, 1.1)

@@ -94,7 +94,7 @@ class StMlpStats(C.Structure):
                 ("box_lo", C.c_float * 3), ("box_inv_ext", C.c_float)]
 
 
-MLP_PARAMS = 13824 + 1048576        # ST_MLP_PARAMS: W1 W2 W3 W4 then the hash grid's features
+MLP_PARAMS = 13824 + 131072         # ST_MLP_PARAMS: W1 W2 W3 W4 then the hash grid's features
 
 
 class StOpticsSource(C.Structure):
