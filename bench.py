@@ -26,6 +26,8 @@ time_to_rmse: seconds to 1 % relative RMSE against a closed form, the photon map
        vs plain.
 optics: the batched optics bench (64 emitter + aspheric-lens instances, 120.2 M rays, FP64 far-field and lux
        tallies) in rays/s, with the tallies on the device (`value`) and read back every run (`e2e`).
+mlp: the learned proposal (a BF16 network guiding BSDF sampling): relative RMSE and GPU time, plain against guided,
+       on the diffuse room lit by the sun's patch; the network's inference and training flops a second.
 Multi-GPU (torchrun): replicas -- each rank renders the whole workload on its own GPU; value sums the ranks' paths
        over the slowest rank's time (weak scaling). There is no data exchange in the path tracer.
 """
@@ -56,7 +58,8 @@ def parse():
     ap.add_argument("--no-optics", action="store_true", help="skip the optics bench's rays/s leg")
     ap.add_argument("--no-sppm", action="store_true", help="skip the photon map's photons/s leg")
     ap.add_argument("--spp", type=int, default=0, help="samples per pixel a step (profiling runs; default: 64)")
-    ap.add_argument("--leg", default="all", choices=["all", "sppm", "rmse", "optics"],
+    ap.add_argument("--no-mlp", action="store_true", help="skip the learned proposal's leg")
+    ap.add_argument("--leg", default="all", choices=["all", "sppm", "rmse", "optics", "mlp"],
                     help="run one leg alone and print its JSON (profiling runs of the photon map or the optics bench)")
     return ap.parse_args()
 
@@ -337,6 +340,76 @@ def sppm_leg(args, dev, with_cpu):
     return out
 
 
+MLP_FWD_FLOPS = 2 * (48 * 64 + 64 * 64 + 64 * 64 + 40 * 64)     # 27 648 a vertex: 13 824 BF16 multiply-adds
+MLP_TRAIN_FLOPS = 3 * MLP_FWD_FLOPS                               # forward, backward to the inputs, weight GEMM
+
+
+def mlp_leg(args, dev):
+    """The learned proposal: the diffuse room lit by the sun's patch (sky almost black), 160 x 90, plain and guided
+    (trained online from the first wave) against a plain render of 8192 samples: relative RMSE and GPU time at 1024
+    samples; the network's inference (BF16 tensor-core flops a second at the vertices it ran at) and training."""
+    import torch
+    from shadytracer_gb300 import scenes
+    from shadytracer_gb300.renderer import create_path_tracer
+    W, H = (96, 54) if args.small else (160, 90)
+    ref_spp, spp = (1024, 256) if args.small else (8192, 1024)
+    luma = np.array([0.2126, 0.7152, 0.0722])
+
+    def scene(guide):
+        s = scenes.sdf_room(width=W, height=H, spp=spp, finish="diffuse", sky_illuminance=10.0, ground_luminance=1.0)
+        s.params.guide = guide
+        return s
+    rt = create_path_tracer(scene(0), device=dev)
+    left = ref_spp
+    while left > 0:
+        rt.step(min(512, left))
+        left -= 512
+    Lref = rt.read_accum()[0] @ luma
+    rt.close()
+    out = {"workload": "room24 diffuse, sun patch only (sky 10 lx), %dx%d, %d samples against a %d-sample plain render"
+                       % (W, H, spp, ref_spp), "metric": "relative RMSE at equal samples", "legs": {}}
+    for guide in (0, 1):
+        rt = create_path_tracer(scene(guide), device=dev)
+        stream = torch.cuda.ExternalStream(rt.stream(), device=torch.device("cuda", dev))
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        rt.invalidate()
+        e0.record(stream)
+        rt.step_async(spp)
+        e1.record(stream)
+        rt.sync()
+        L = rt.read_accum()[0] @ luma
+        leg = {"rmse": float(np.sqrt(np.mean((L - Lref) ** 2)) / Lref.mean()), "ms": e0.elapsed_time(e1)}
+        if guide:
+            st = rt.mlp_stats()
+            rt.enable_kernel_times(True)
+            rt.reset_kernel_times()
+            rt.step(64)
+            kt = rt.kernel_times()
+            st2 = rt.mlp_stats()
+            rt.enable_kernel_times(False)
+            n_i, ms_i = kt.get("guide", (0, 0.0))
+            n_t, ms_t = kt.get("guide_train", (0, 0.0))
+            waves = max(kt.get("resolve", (1, 0.0))[0], 1)
+            inferred = st2["inferred"] * waves              # the last wave's count, each wave alike
+            pk = peaks()
+            peak = pk.get("bf16_tflops") if pk else None
+            tf_i = MLP_FWD_FLOPS * inferred / (ms_i / 1e3) / 1e12 if ms_i > 0 else None
+            tf_t = MLP_TRAIN_FLOPS * st2["samples"] * waves / (ms_t / 1e3) / 1e12 if ms_t > 0 else None
+            leg.update({"train_steps": st["steps"], "loss": st["loss"],
+                        "infer": {"launches": n_i, "ms": ms_i, "vertices": inferred, "tflops": tf_i,
+                                  "frac_of_bf16_peak": tf_i / peak if (tf_i and peak) else None},
+                        "train": {"waves": waves, "ms": ms_t, "samples_per_wave": st2["samples"], "tflops": tf_t},
+                        "share_of_render": (ms_i + ms_t + kt.get("guide_collect", (0, 0.0))[1]) /
+                                           max(sum(v[1] for v in kt.values()), 1e-9)})
+        out["legs"]["guided" if guide else "plain"] = leg
+        rt.close()
+    out["rmse_ratio_guided_over_plain"] = out["legs"]["guided"]["rmse"] / out["legs"]["plain"]["rmse"]
+    out["time_ratio_guided_over_plain"] = out["legs"]["guided"]["ms"] / out["legs"]["plain"]["ms"]
+    # at equal time the guided render's RMSE would scale by sqrt(time ratio): the speed-up to equal error
+    out["speedup_to_equal_rmse"] = 1.0 / (out["rmse_ratio_guided_over_plain"] ** 2 * out["time_ratio_guided_over_plain"])
+    return out
+
+
 def rmse_leg(args, dev):
     """Time to 1 % relative RMSE against the closed form, guided vs plain: the photon map's pane (a 0.5 m glass pane
     over a floor lit only through it, the sun's photons drawn over a 4 m square), plain -- the photons uniform over the
@@ -394,7 +467,7 @@ def run_ours(args):
     if args.leg != "all":
         with_cpu = rank == 0 and world == 1 and not args.no_cpu
         out = {"sppm": lambda: sppm_leg(args, dev, with_cpu), "rmse": lambda: rmse_leg(args, dev),
-               "optics": lambda: optics_leg(args, dev, with_cpu)}[args.leg]()
+               "optics": lambda: optics_leg(args, dev, with_cpu), "mlp": lambda: mlp_leg(args, dev)}[args.leg]()
         if rank == 0:
             print(json.dumps(out), flush=True)
         return 0
@@ -551,6 +624,8 @@ def run_ours(args):
     if not args.no_sppm:
         line["sppm"] = sppm_leg(args, dev, rank == 0 and world == 1 and not args.no_cpu)
         line["time_to_rmse"] = rmse_leg(args, dev)
+    if not args.no_mlp:
+        line["mlp"] = mlp_leg(args, dev)
     if not args.no_optics:
         line["optics"] = optics_leg(args, dev, rank == 0 and world == 1 and not args.no_cpu)
         if world > 1:

@@ -350,6 +350,7 @@ typedef struct st_mlp_stats {
     float    mean_weight;         /* the last batch's mean weight (f cos L_in / pdf at the vertex)   */
     float    box_lo[3];           /* the hash grid's box: its low corner, metres                     */
     float    box_inv_ext;         /* ... and 1 / its longest side                                    */
+    uint32_t inferred;            /* vertices the network ran at in the last wave                   */
 } st_mlp_stats;
 int  st_mlp_get_weights(st_ctx* ctx, float* out, size_t n);
 int  st_mlp_set_weights(st_ctx* ctx, const float* in, size_t n);

@@ -132,6 +132,7 @@ __global__ void __launch_bounds__(256) k_guide_infer(WaveArgs a) {
         uint32_t off = 0, n = 0;
         for (uint32_t w = 0; w < 8u; w++) { if (w < warp) off += wcnt[w]; n += wcnt[w]; }
         if (want) list[off + __popc(m & lanemask_lt())] = q;
+        if (threadIdx.x == 0u && n) atomicAdd(&a.gd.dev->inferred, n);
         __syncthreads();
         for (uint32_t tile = warp; tile * 16u < n; tile += 8u) {
             const uint32_t e0 = tile * 16u + g, e1 = e0 + 8u;
@@ -643,6 +644,7 @@ cudaError_t guide_wave_begin(st_ctx* ctx, uint32_t slots, cudaStream_t st) {
     cudaError_t e = cudaMemsetAsync(g.rec, 0, (size_t)slots * sizeof(GuideRec), st);
     if (!e) e = cudaMemsetAsync(g.acc, 0, (size_t)slots * 4, st);
     if (!e) e = cudaMemsetAsync(g.dev, 0, 4, st);                         // count
+    if (!e) e = cudaMemsetAsync(reinterpret_cast<char*>(g.dev) + 8, 0, 4, st);     // inferred
     if (!e) e = cudaMemsetAsync(reinterpret_cast<char*>(g.dev) + 16, 0, 16, st);   // wsum, loss, loss_n
     return e;
 }
@@ -769,6 +771,7 @@ int st_mlp_stats_read(st_ctx* ctx, st_mlp_stats* out) {
     out->samples = std::min(d.count, GUIDE_CAP);
     out->loss = d.loss_n > 0.f ? d.loss / d.loss_n : 0.f;
     out->mean_weight = d.count ? d.wsum / (float)std::min(d.count, GUIDE_CAP) : 0.f;
+    out->inferred = d.inferred;
     return ST_OK;
 }
 

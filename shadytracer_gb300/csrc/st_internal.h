@@ -116,7 +116,7 @@ struct GuideRec { float4 a, b; };         // a: position, pdf of the direction; 
                                           // throughput luminance reaching the vertex, radiance luminance before it
 struct GuideSample { float4 a, b, c; };   // a: position, weight (f cos L_in / pdf); b: normal; c: direction
 struct GuideDev {
-    uint32_t count, step, pad0, pad1;     // samples in the batch; Adam steps taken
+    uint32_t count, step, inferred, pad1; // samples in the batch; Adam steps taken; vertices the network ran at
     float wsum, loss, loss_n, pad2;       // the batch's summed weight; the last step's summed loss and samples
 };
 struct GuideBufs {

@@ -214,7 +214,7 @@ class PathTracer:
         s = T.StMlpStats()
         check(self.L.st_mlp_stats_read(self.ctx, C.byref(s)), self.ctx, "st_mlp_stats_read")
         return {"steps": s.steps, "samples": s.samples, "loss": s.loss, "mean_weight": s.mean_weight,
-                "box_lo": list(s.box_lo), "box_inv_ext": s.box_inv_ext}
+                "box_lo": list(s.box_lo), "box_inv_ext": s.box_inv_ext, "inferred": s.inferred}
 
 
 def create_path_tracer(scene=None, device=0):

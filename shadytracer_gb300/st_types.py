@@ -91,7 +91,7 @@ class StSppmStats(C.Structure):
 
 class StMlpStats(C.Structure):
     _fields_ = [("steps", C.c_uint32), ("samples", C.c_uint32), ("loss", C.c_float), ("mean_weight", C.c_float),
-                ("box_lo", C.c_float * 3), ("box_inv_ext", C.c_float)]
+                ("box_lo", C.c_float * 3), ("box_inv_ext", C.c_float), ("inferred", C.c_uint32)]
 
 
 MLP_PARAMS = 13824 + 131072         # ST_MLP_PARAMS: W1 W2 W3 W4 then the hash grid's features
