@@ -197,7 +197,10 @@ static Uni make_uni(const st_ctx* ctx) {
     u.n_prims = (uint32_t)ctx->prims.size();
     u.n_mats = (uint32_t)ctx->mats.size();
     // the march queue's space order: a grid over the bounded primitives' spheres (none bounded: no sort)
-    u.sort_on = ctx->grid_ok && ctx->q.sorted ? 1u : 0u;
+    // the space order pays where a step is dear: a table of a few primitives marches fast in any order, and there the
+    // sort's three launches an iteration cost more than the coherence saves (the SDF room, 27 primitives: 19 % faster
+    // sorted; the photon map's caustic, 3: 2 % slower)
+    u.sort_on = ctx->grid_ok && ctx->q.sorted && ctx->prims.size() >= SORT_MIN_PRIMS ? 1u : 0u;
     u.glo = mk(ctx->grid_lo[0], ctx->grid_lo[1], ctx->grid_lo[2]);
     u.ginv = mk(SORT_G / (ctx->grid_hi[0] - ctx->grid_lo[0]), SORT_G / (ctx->grid_hi[1] - ctx->grid_lo[1]),
                 SORT_G / (ctx->grid_hi[2] - ctx->grid_lo[2]));

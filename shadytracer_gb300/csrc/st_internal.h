@@ -29,6 +29,7 @@ namespace st {
 #define SURF_LEAVING 0xffffffffu          // hsurf: the surface seen from behind, the ray moved on
 #define SORT_G 16u                        // the march queue's space order: SORT_G^3 cells ...
 #define SORT_BUCKETS (SORT_G * SORT_G * SORT_G * 8u)   // ... x 8 direction octants
+#define SORT_MIN_PRIMS 8u                 // scenes of fewer primitives march their queues unsorted
 #define MARCH_CHUNK 48u
 
 // meta.y: the bounces (bits 0-7), the path's segment -- its shades so far, which its random numbers are seeded by
