@@ -172,6 +172,13 @@ typedef struct st_params {
     float    guide_lr;            /* Adam's learning rate (0: 0.005)                                 */
     uint32_t guide_train;         /* 1: train after every wave; 0: the weights as they are          */
     uint32_t guide_seed;          /* the initial weights' seed (a change draws them afresh)          */
+    /* emissive surfaces (materials_pbr.js:887-960, wavefront.js:715-815): camera paths that meet an emitter
+     * discover it; every 2 samples the discovered emitters become a list of bounding spheres that light sampling
+     * aims at (under MIS with the BSDF's hits of them) */
+    float    emit_share;          /* the light samples' share aimed at the list once it holds any (0: 0.5; clamped
+                                   * to [0.05, 0.95]; the reference's neeEmitShare)                   */
+    float    emit_radius;         /* the discovery grid's half-size, metres (0: 15; capped at the scene's radius)  */
+    uint32_t emit_off;            /* 1: no light sampling of emitters (discovery goes on)            */
 } st_params;
 
 /* The camera, as genrays reads it (core/genrays.js:65-92): the basis from invView's columns and the
@@ -368,6 +375,11 @@ int  st_mlp_train(st_ctx* ctx, const float* pos, const float* nrm, const float* 
 int  st_mlp_stats_read(st_ctx* ctx, st_mlp_stats* out);
 /* the last wave's training batch, at most max_n samples of 10 floats (position, normal, direction, weight) */
 int  st_mlp_read_batch(st_ctx* ctx, float* out, uint32_t max_n, uint32_t* n);
+
+/* ---- emissive surfaces ----
+ * The list light sampling aims at, as the last build left it: per box its bounding sphere's centre and radius
+ * (metres), its probability and the running sum of the probabilities (6 floats a box, in the grid's voxel order). */
+int  st_emit_list(st_ctx* ctx, float* out, uint32_t max_n, uint32_t* n);
 
 /* ---- a render that allocates nothing ----
  * No counterpart in the reference: an entry point for hosts that may not allocate device memory when they want a

@@ -37,6 +37,26 @@ struct Stats {
     std::atomic<uint32_t> nonfinite{0}, flushed{0}, shadowcut{0};
 };
 
+// THE EMITTER LIST (wavefront.js:715-815 prog_emit_collect / publish; tracebasics.js:1148-1210 EMIT_LIST;
+// materials_pbr.js:887-905 emitDeposit): the discovery grid the camera paths' emitter hits go into (a copy a thread,
+// merged after each sample), and the list built from it between samples, every EMIT_EPOCH -- in voxel order, as the
+// product builds it
+const uint32_t EMIT_G = 16, EMIT_CELLS = EMIT_G * EMIT_G * EMIT_G, EMIT_MAX = 64, EMIT_EPOCH = 2;
+const float EMIT_Q = 16777215.f, EMIT_LUM_K = 209715.2f;
+const uint32_t EMIT_LUM_DECAY = 31877u;
+struct EmitList {
+    uint32_t count = 0, last = 0;
+    float box[EMIT_MAX][4];           // centre, radius
+    float pc[EMIT_MAX][2];            // probability, running sum
+};
+inline uint32_t emit_lum_code(float lum) {
+    return (uint32_t)(std::fmin(std::fmax(std::log2(std::fmax(lum, 1e-30f)) + 40.f, 0.f), 80.f) * EMIT_LUM_K) + 1u;
+}
+inline float emit_lum_decode(uint32_t q) { return q ? std::exp2((float)(q - 1u) / EMIT_LUM_K - 40.f) : 0.f; }
+inline void emit_grid_init(uint32_t* g) {
+    for (uint32_t i = 0; i < EMIT_CELLS * 8; i++) g[i] = (i & 7u) < 3u ? 0xFFFFFFFFu : 0u;
+}
+
 template <class T> struct Ctx {
     const st_scene_desc* s;
     st_params p;
@@ -58,6 +78,11 @@ template <class T> struct Ctx {
     uint32_t* lt_emit = nullptr;
     uint32_t* lt_hit = nullptr;
     const float* lt_cdf = nullptr;
+    // the emitter list: on in a scene with emitters; light sampling aims at it (nee) with this share; the grid's half
+    bool em_on = false, em_nee = false;
+    float em_share = 0.5f, em_half = 15.f;
+    const EmitList* em = nullptr;
+    std::vector<std::vector<uint32_t>>* em_grids = nullptr;     // a discovery grid a thread
 };
 const uint32_t LT_G = 128, LT_N = LT_G * LT_G;
 const float LT_FLOOR_F = 0.2f;
@@ -113,6 +138,7 @@ template <class T> struct Ray {
     V3<T> pos, dir, beta, rad;
     T ltot, n, sunmis, tmax, absLtot;
     T lam = T(0);                           // the wavelength a dispersive refraction gave it (nm, as coded), 0 none
+    T emw = T(1);                           // an emitter hit's MIS weight against the last vertex's light sample
     uint32_t lens = 0;                      // a camera path's lens field (materials_pbr.js lensField): 1 delta only
                                             // since the eye, 2 at its D, 3 delta only since its D
     bool passed = false;                    // a photon that has passed a delta event (TAG_PASSED)
@@ -172,7 +198,8 @@ template <class T> inline T march(const Ctx<T>& C, Ray<T>& r, Stats& st, bool us
 }
 
 // the occlusion pass (wavefront.js:1481-1692), distance only: true when the shadow ray reaches the light
-template <class T> inline bool occlude(const Ctx<T>& C, V3<T> pos, const V3<T>& dir, T n, Stats& st) {
+template <class T> inline bool occlude(const Ctx<T>& C, V3<T> pos, const V3<T>& dir, T n, Stats& st,
+                                      V3<T>* stop = nullptr, T* stop_ltot = nullptr) {
     T ltot = 0;
     uint32_t steps = 0;
     bool reached = false, cut = false;
@@ -194,7 +221,104 @@ template <class T> inline bool occlude(const Ctx<T>& C, V3<T> pos, const V3<T>& 
     st.shadow_rays++;
     st.shadow_steps += evals;
     if (cut) st.shadowcut++;
+    if (stop) *stop = pos;
+    if (stop_ltot) *stop_ltot = ltot;
     return reached;
+}
+
+// the list's questions (tracebasics.js:1148-1210): a box by its running sum, 1 - cos of a sphere's cone, the
+// mixture's density of a direction, a direction into a box's cone
+inline uint32_t emit_pick(const EmitList& L, float u) {
+    for (uint32_t b = 0; b < L.count; b++)
+        if (u < L.pc[b][1]) return b;
+    return L.count ? L.count - 1 : 0;
+}
+template <class T> inline T cone_omc(T r, T d2) {
+    const T s2 = r * r / d2;
+    return s2 / (T(1) + std::sqrt(std::max(T(0), T(1) - s2)));
+}
+template <class T> inline T emit_cone_pdf(const EmitList& L, const V3<T>& x, const V3<T>& w) {
+    T p = 0;
+    for (uint32_t b = 0; b < L.count; b++) {
+        const V3<T> dc(T(L.box[b][0]) - x.x, T(L.box[b][1]) - x.y, T(L.box[b][2]) - x.z);
+        const T d2 = dot(dc, dc), r = T(L.box[b][3]);
+        if (d2 <= r * r) continue;
+        const T omc = cone_omc(r, d2);
+        if (dot(w, dc) >= (T(1) - omc) * std::sqrt(d2)) p += T(L.pc[b][0]) / (T(2) * T(PI_D) * omc);
+    }
+    return p;
+}
+template <class T> inline bool emit_sample(const EmitList& L, uint32_t b, const V3<T>& x, T u1, T u2, V3<T>& w) {
+    const V3<T> dc(T(L.box[b][0]) - x.x, T(L.box[b][1]) - x.y, T(L.box[b][2]) - x.z);
+    const T d2 = dot(dc, dc), r = T(L.box[b][3]);
+    if (d2 <= r * r) return false;
+    const T d = std::sqrt(d2);
+    const V3<T> axis = dc * (T(1) / d);
+    const T omc = cone_omc(r, d2);
+    const T cosT = T(1) - u1 * omc;
+    const T sinT = std::sqrt(std::max(T(0), T(1) - cosT * cosT));
+    const T ph = T(2) * T(PI_D) * u2;
+    const V3<T> tt = std::fabs(axis.x) > T(0.9) ? V3<T>(0, 1, 0) : V3<T>(1, 0, 0);
+    const V3<T> b1 = normalize(cross(tt, axis));
+    const V3<T> b2 = cross(axis, b1);
+    w = normalize(b1 * (std::cos(ph) * sinT) + b2 * (std::sin(ph) * sinT) + axis * cosT);
+    return true;
+}
+// a camera path's emitter hit into this thread's grid (materials_pbr.js:887-905 emitDeposit)
+template <class T> inline void emit_deposit(const Ctx<T>& C, const V3<T>& p, const V3<T>& le) {
+    const float R = C.em_half;
+    const float ux = ((float)p.x + R) / (2.f * R), uy = ((float)p.y + R) / (2.f * R), uz = ((float)p.z + R) / (2.f * R);
+    if (ux < 0.f || uy < 0.f || uz < 0.f || ux >= 1.f || uy >= 1.f || uz >= 1.f) return;
+    int tid = 0;
+#ifdef _OPENMP
+    tid = omp_get_thread_num();
+#endif
+    uint32_t* g = (*C.em_grids)[tid].data() +
+                  8 * ((uint32_t)(ux * EMIT_G) + EMIT_G * ((uint32_t)(uy * EMIT_G) + EMIT_G * (uint32_t)(uz * EMIT_G)));
+    const uint32_t q[3] = {(uint32_t)(ux * EMIT_Q), (uint32_t)(uy * EMIT_Q), (uint32_t)(uz * EMIT_Q)};
+    for (int k = 0; k < 3; k++) { g[k] = std::min(g[k], q[k]); g[3 + k] = std::max(g[3 + k], q[k]); }
+    g[6] = std::max(g[6], emit_lum_code((float)luma(le)));
+    g[7] += 1;
+}
+// the list from the grid (prog_emit_collect + publish): each voxel with hits a box, its hits and brightness fading
+// by a tenth; at most EMIT_MAX, in voxel order; probabilities by brightness x size^2
+inline void emit_build(uint32_t* g, EmitList& L, float half, float tol_setting) {
+    const float R = half;
+    std::vector<float> score;
+    uint32_t K = 0;
+    for (uint32_t cell = 0; cell < EMIT_CELLS; cell++) {
+        uint32_t* v = g + 8 * cell;
+        const uint32_t w = v[6], n = v[7];
+        if (n == 0) continue;
+        const uint32_t n2 = n - n / 10u, w2 = std::max(w, EMIT_LUM_DECAY + 1u) - EMIT_LUM_DECAY;
+        v[6] = w2; v[7] = n2;
+        if (n2 == 0) { v[0] = v[1] = v[2] = 0xFFFFFFFFu; v[3] = v[4] = v[5] = 0; continue; }
+        float mn[3], mx[3], c[3];
+        for (int k = 0; k < 3; k++) {
+            mn[k] = (float)v[k] / EMIT_Q * (2.f * R) - R;
+            mx[k] = (float)v[3 + k] / EMIT_Q * (2.f * R) - R;
+            c[k] = (mn[k] + mx[k]) * 0.5f;
+        }
+        const float pad = 10.f * march_tol(V3<float>(c[0], c[1], c[2]), tol_setting);
+        const float dx = mx[0] - mn[0], dy = mx[1] - mn[1], dz = mx[2] - mn[2];
+        const float r = std::sqrt(dx * dx + dy * dy + dz * dz) * 0.5f * 1.05f + pad + 4.f * (2.f * R) / EMIT_Q;
+        if (K < EMIT_MAX) {
+            L.box[K][0] = c[0]; L.box[K][1] = c[1]; L.box[K][2] = c[2]; L.box[K][3] = r;
+            score.push_back(emit_lum_decode(w2) * r * r);
+        }
+        K++;
+    }
+    K = std::min(K, EMIT_MAX);
+    float tot = 0.f;
+    for (uint32_t b = 0; b < K; b++) tot += score[b];
+    float acc = 0.f;
+    for (uint32_t b = 0; b < K; b++) {
+        const float P = tot > 0.f ? score[b] / tot : 1.f / (float)K;
+        acc += P;
+        L.pc[b][0] = P;
+        L.pc[b][1] = b + 1 == K ? 1.f : acc;
+    }
+    L.count = K;
 }
 
 // the normal by three forward differences at normalTol (tracebasics.js:1310-1322 calcNormals_fast)
@@ -331,7 +455,8 @@ inline void shade_hit(const Ctx<T>& C, Ray<T>& r, T dhit, Rng& rng, Rng& grng, b
     }
     r.bounces += 1;
     if (max3(emis) > T(0)) {                                                       // materials_pbr.js:1014-1075 emitterHit
-        r.rad += r.beta * emis;
+        r.rad += r.beta * emis * r.emw;            // weighed against the last vertex's emitter light sample
+        if (C.em_on) emit_deposit(C, r.pos, emis);  // and discovered
         r.state = RAY_SOURCE;
         move_by(r, r.dir * (otol * T(2)));
         return;
@@ -371,30 +496,58 @@ inline void shade_hit(const Ctx<T>& C, Ray<T>& r, T dhit, Rng& rng, Rng& grng, b
     Lobes<T> lb = make_lobes(nrm, -r.dir, m, etaFace, C.tb, trans, specv);
     lb.etaT = n0 / nT;
 
-    // LIGHT SAMPLING (materials_pbr.js:1196-1330): the environment only (no faces, no discovered emitters)
+    // LIGHT SAMPLING (materials_pbr.js:1196-1330): the discovered emitters with their share of the samples (0 while
+    // nothing is listed, when the environment's draw is what it always was), else the environment; no light faces
+    const T es = (C.em_on && C.em_nee && C.p.nee != 0 && !last && C.em->count > 0)
+                     ? T(std::min(std::max(C.em_share, 0.05f), 0.95f)) : T(0);
     if (C.p.nee != 0 && !last) {
         T u0[4], u1[4];
         rng.next4(u0);                                                             // pick00
         rng.next4(u1);                                                             // uL
         if (!lobes_none<T>(m, trans)) {
-            T pick = u0[0];
-            V3<T> L = env_sample_dir(C.env, nrm, pick, u1[0], u1[1]);
+            V3<T> L(0, 0, 1);
+            T pS = 0;
+            bool toEmit = false;
+            if (u0[0] < es) {
+                const uint32_t b = emit_pick(*C.em, (float)(u0[0] / es));
+                if (emit_sample(*C.em, b, r.pos, u1[0], u1[1], L)) {
+                    pS = es * emit_cone_pdf(*C.em, r.pos, L);
+                    toEmit = true;
+                }
+            } else {
+                T pick = es > T(0) ? (u0[0] - es) / (T(1) - es) : u0[0];
+                L = env_sample_dir(C.env, nrm, pick, u1[0], u1[1]);
+                pS = (T(1) - es) * env_pdf(C.env, L, nrm);
+            }
             T NoL = dot(nrm, L);
-            T pL = env_pdf(C.env, L, nrm);
-            if (NoL > T(0) && pL > T(0)) {
-                V3<T> le = C.env.radiance(L);
+            if (NoL > T(0) && pS > T(0)) {
+                V3<T> le = toEmit ? V3<T>(1, 1, 1) : C.env.radiance(L);
                 V3<T> f = lobes_eval(lb, L, T(0));
                 T pB = lobes_pdf(lb, L);
-                T w = mis_weight(pL, pB);
-                V3<T> contrib = r.beta * f * le * (std::fabs(NoL) * (w / pL));
-                if (max3(contrib) > T(1e-7)) {
+                T w = mis_weight(pS, pB);
+                V3<T> contrib = r.beta * f * le * (std::fabs(NoL) * (w / pS));
+                if (max3(contrib) > (toEmit ? T(1e-9) : T(1e-7))) {
                     V3<T> o = r.pos + nrm * (otol * T(2));
                     T tr = T(1);
-                    if (C.haze.on && std::fabs(r.n - T(1)) <= T(1e-3)) {                   // haze.js:472-485 hazeShadow
-                        T R = T(C.d.env_radius);
-                        tr = C.haze.transmittance(r.pos, L, T(2) * R + length(r.pos), R);
+                    const bool air = C.haze.on && std::fabs(r.n - T(1)) <= T(1e-3);
+                    T R = T(C.d.env_radius);
+                    if (!toEmit) {
+                        if (air) tr = C.haze.transmittance(r.pos, L, T(2) * R + length(r.pos), R);   // haze.js:472-485
+                        if (occlude(C, o, L, r.n, st)) deposit(fr, r.pix, contrib * tr, st);
+                    } else {
+                        // an emitter's ray counts the emission of whatever it stops at (wavefront.js:1694-1749)
+                        V3<T> hp;
+                        T hl = 0;
+                        if (!occlude(C, o, L, r.n, st, &hp, &hl)) {
+                            SceneHit<T> hh = scene_eval(*C.s, hp);
+                            const st_material& me = C.s->materials[std::min(hh.m, C.s->n_materials - 1)];
+                            V3<T> ee(T(me.emissive[0]), T(me.emissive[1]), T(me.emissive[2]));
+                            if (max3(ee) > T(0)) {
+                                if (air) tr = C.haze.transmittance(o, L, std::max(hl, T(0)) / std::max(r.n, T(1e-4)), R);
+                                deposit(fr, r.pix, contrib * ee * tr, st);
+                            }
+                        }
                     }
-                    if (occlude(C, o, L, r.n, st)) deposit(fr, r.pix, contrib * tr, st);
                 }
             }
         }
@@ -414,10 +567,13 @@ inline void shade_hit(const Ctx<T>& C, Ray<T>& r, T dhit, Rng& rng, Rng& grng, b
     if (misOut) {                                                                  // materials_pbr.js:1370-1395
         bool above = dot(nrm, r.dir) > T(0) && !smp.isDelta;
         T pOut = smp.isDelta ? T(0) : lobes_pdf(lb, smp.dir);
-        T pLout = above ? env_pdf(C.env, r.dir, nrm) : T(0);
+        T pLout = above ? (T(1) - es) * env_pdf(C.env, r.dir, nrm) : T(0);
         r.sunmis = pLout <= T(0) ? T(1) : mis_weight(pOut, pLout);
+        const T pEout = (above && es > T(0)) ? es * emit_cone_pdf(*C.em, r.pos, r.dir) : T(0);
+        r.emw = pEout <= T(0) ? T(1) : mis_weight(pOut, pEout);
     } else {
         r.sunmis = T(1);
+        r.emw = T(1);
     }
     move_by(r, r.dir * otol);
     // pathEnd's tail (tracebasics.js:1040-1103): the bounce cap, Russian roulette
@@ -511,6 +667,7 @@ void medium_vertex(const Ctx<T>& C, Ray<T>& r, Rng& rng, bool last, Frame<T>& fr
     } else {
         r.sunmis = T(1);
     }
+    r.emw = T(1);                                  // no emitter light sample from the air
     if (r.bounces > C.p.maxbounce) r.state = RAY_TERMINATED;
 }
 
@@ -889,8 +1046,33 @@ static int render_impl(const st_scene_desc* s, const st_params* p, const st_view
     lt_uniform(lt_cdf.data());
     C.sp_learn = sppm_on && p->sppm_learn != 0;
     C.lt_emit = lt_emit.data(); C.lt_hit = lt_hit.data(); C.lt_cdf = lt_cdf.data();
+    // the emitter list, in a scene with an emissive material: a grid a thread, the merged grid, the list
+    EmitList elist;
+    std::vector<uint32_t> egrid(EMIT_CELLS * 8);
+    std::vector<std::vector<uint32_t>> egrids(1);
+#ifdef _OPENMP
+    egrids.resize(omp_get_max_threads());
+#endif
+    for (uint32_t i = 0; i < s->n_materials; i++)
+        if (std::max(s->materials[i].emissive[0], std::max(s->materials[i].emissive[1], s->materials[i].emissive[2])) > 0.f)
+            C.em_on = true;
+    if (C.em_on) {
+        C.em_nee = p->emit_off == 0;
+        C.em_share = p->emit_share > 0.f ? p->emit_share : 0.5f;
+        const float set = p->emit_radius > 0.f ? p->emit_radius : 15.f;     // photometry.js:147-148 photonHalf
+        C.em_half = std::max(std::min(std::max(set, 1e-3f), (float)C.d.env_radius), 1e-6f);
+        emit_grid_init(egrid.data());
+        for (auto& g : egrids) { g.resize(EMIT_CELLS * 8); emit_grid_init(g.data()); }
+        C.em = &elist;
+        C.em_grids = &egrids;
+    }
     for (uint32_t si = 0; si < nsamples; si++) {
         U4 sseed = sample_seed(p->seed, sample0 + si);
+        // the list rebuilt between samples, every EMIT_EPOCH (a wave a sample)
+        if (C.em_on && sample0 + si >= elist.last + EMIT_EPOCH) {
+            emit_build(egrid.data(), elist, C.em_half, (float)C.d.tol_setting);
+            elist.last = sample0 + si;
+        }
         std::fill(fr.rgb.begin(), fr.rgb.end(), 0.0);
         std::fill(fr.cnt.begin(), fr.cnt.end(), 0u);
         if (sppm_on) {
@@ -928,6 +1110,16 @@ static int render_impl(const st_scene_desc* s, const st_params* p, const st_view
         }
 #pragma omp parallel for schedule(dynamic, 64)
         for (long t = (long)path_first; t < (long)pend; t++) trace_path(C, sseed, (uint32_t)t, *v, W, H, fr, st);
+        if (C.em_on)                                               // the threads' discoveries into the grid
+            for (auto& g : egrids) {
+                for (uint32_t i = 0; i < EMIT_CELLS * 8; i++) {
+                    const uint32_t k = i & 7u;
+                    if (k < 3) egrid[i] = std::min(egrid[i], g[i]);
+                    else if (k < 7) egrid[i] = std::max(egrid[i], g[i]);
+                    else egrid[i] += g[i];
+                }
+                emit_grid_init(g.data());
+            }
         // resolve (wavefront.js:414-494, measure.js:36-51) in double precision
         for (uint32_t i = 0; i < P; i++) {
             uint32_t n = fr.cnt[i];

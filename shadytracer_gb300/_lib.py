@@ -50,6 +50,7 @@ SIGNATURES = {
     "st_mlp_train": ([P, P, P, P, P, C.c_uint32, C.c_uint32, C.c_float], C.c_int),
     "st_mlp_stats_read": ([P, C.POINTER(T.StMlpStats)], C.c_int),
     "st_mlp_read_batch": ([P, P, C.c_uint32, C.POINTER(C.c_uint32)], C.c_int),
+    "st_emit_list": ([P, P, C.c_uint32, C.POINTER(C.c_uint32)], C.c_int),
     "st_struct_sizes": ([P, C.c_int], C.c_int),
     "st_stream": ([P], C.c_void_p),
 }

@@ -58,8 +58,10 @@ struct st_ctx {
     uint32_t samples = 0;
     bool in_flight = false;
     // the launch chain as a graph, per wave size
-    cudaGraphExec_t graph = nullptr;
+    cudaGraphExec_t graph = nullptr;      // the wave chain of graph_w samples, captured
     uint32_t graph_w = 0;
+    cudaGraphExec_t graph2 = nullptr;     // ...and a second size's (an emitter scene's first, short waves)
+    uint32_t graph2_w = 0, graph2_launches = 0;
     bool graph_ok = true;
     uint32_t rec_launches = 0;            // kernels in the last recorded wave chain
     uint32_t graph_launches = 0;          // ...and in the graph's (its kernel nodes)
@@ -104,6 +106,7 @@ static void free_wave(st_ctx* ctx) {
     ctx->d_mom = nullptr;
     ctx->slot_cap = 0;
     if (ctx->graph) { cudaGraphExecDestroy(ctx->graph); ctx->graph = nullptr; ctx->graph_w = 0; }
+    if (ctx->graph2) { cudaGraphExecDestroy(ctx->graph2); ctx->graph2 = nullptr; ctx->graph2_w = 0; }
 }
 
 static int time_index(st_ctx* ctx, const char* name) {
@@ -254,6 +257,13 @@ static uint32_t samples_per_wave(const st_ctx* ctx) {
     return std::max(1u, std::min(s, 64u));
 }
 
+// a scene with an emissive material: the emitter list's discovery and light sampling run
+static bool has_emitters(const st_ctx* ctx) {
+    for (const st_material& m : ctx->mats)
+        if (std::max(m.emissive[0], std::max(m.emissive[1], m.emissive[2])) > 0.f) return true;
+    return false;
+}
+
 static int ensure_wave(st_ctx* ctx) {
     if (sppm_runs(ctx)) {
         int rc = sppm_ensure(ctx, sppm_photons(ctx));
@@ -271,6 +281,10 @@ static int ensure_wave(st_ctx* ctx) {
     uint32_t cap = spw * ctx->P;
     // the photon map's photons run in chunks of the wave's slots: give them room for up to four million at once
     if (sppm_runs(ctx)) cap = std::max(cap, std::min(sppm_photons(ctx), 4u << 20));
+    if (has_emitters(ctx)) {                   // the list's per-slot weights and its hit queue (a shadow side's room)
+        int rc = emit_ensure(ctx, cap, 2u * cap);
+        if (rc) return rc;
+    }
     bool pixels_changed = !ctx->d_acc;
     if (ctx->slot_cap == cap && ctx->spw == spw && !pixels_changed) return ST_OK;
     free_wave(ctx);
@@ -357,6 +371,13 @@ static WaveArgs wave_args(st_ctx* ctx, uint32_t w) {
     if (ctx->params.guide)
         a.gd = guide_bufs(ctx, 1u, ctx->params.guide_train ? 1u : 0u,
                           ctx->params.guide_alpha > 0.f ? std::min(ctx->params.guide_alpha, 1.f) : 0.5f, a.slots);
+    if (has_emitters(ctx) && ctx_ext(ctx).emit.grid) {
+        // the grid's half-size as the reference derives emitHalf (photometry.js:147-148 photonHalf, :223)
+        const float set = ctx->params.emit_radius > 0.f ? ctx->params.emit_radius : 15.f;
+        const float half = std::max(std::min(std::max(set, 1e-3f), a.u.envR), 1e-6f);
+        a.em = emit_bufs(ctx, (!ctx->params.emit_off && a.u.nee) ? 1u : 0u,
+                         ctx->params.emit_share > 0.f ? ctx->params.emit_share : 0.5f, half);
+    }
     return a;
 }
 
@@ -410,6 +431,8 @@ static cudaError_t record_wave(st_ctx* ctx, const WaveArgs& a) {
     }
     ctx->rec_launches++;
     if (a.gd.train && (e = guide_wave_begin(ctx, a.slots, s))) return e;
+    // the emitter list, from what the camera paths discovered: rebuilt between samples, every EMIT_EPOCH
+    if (a.em.on && (e = timed("emit_build", [&] { return launch_emit_build(a, 0.f, s); }))) return e;
     if ((e = launch_iter_begin(a, 0, 1, 1, s))) return e;
     if ((e = timed("genrays", [&] { return launch_genrays(a, ctx->sms, s); }))) return e;
     int cur = 0;
@@ -437,6 +460,7 @@ static cudaError_t record_wave(st_ctx* ctx, const WaveArgs& a) {
             ctx->rec_launches += 2;
         }
         if ((e = timed("occlude", [&] { return launch_occlude(a, side, last, ctx->sms, s); }))) return e;
+        if (a.em.on && (e = timed("emit_resolve", [&] { return launch_emit_resolve(a, ctx->sms, s); }))) return e;
         cur = nxt;
     }
     if (a.gd.train) {   // the records into a batch, then the training steps
@@ -455,6 +479,18 @@ static int run_wave(st_ctx* ctx, uint32_t w) {
         CK(record_wave(ctx, a), "launch");
         ctx->launches += ctx->rec_launches;
     } else {
+        if (ctx->graph2 && ctx->graph2_w == w) {                // the other size's graph: swap the two
+            std::swap(ctx->graph, ctx->graph2);
+            std::swap(ctx->graph_w, ctx->graph2_w);
+            std::swap(ctx->graph_launches, ctx->graph2_launches);
+        } else if (ctx->graph && ctx->graph_w != w) {           // keep this one as the other size's
+            if (ctx->graph2) cudaGraphExecDestroy(ctx->graph2);
+            ctx->graph2 = ctx->graph;
+            ctx->graph2_w = ctx->graph_w;
+            ctx->graph2_launches = ctx->graph_launches;
+            ctx->graph = nullptr;
+            ctx->graph_w = 0;
+        }
         if (!ctx->graph || ctx->graph_w != w) {
             if (ctx->graph) { cudaGraphExecDestroy(ctx->graph); ctx->graph = nullptr; }
             cudaGraph_t g;
@@ -483,6 +519,7 @@ static int run_wave(st_ctx* ctx, uint32_t w) {
 
 static void invalidate_graph(st_ctx* ctx) {
     if (ctx->graph) { cudaGraphExecDestroy(ctx->graph); ctx->graph = nullptr; ctx->graph_w = 0; }
+    if (ctx->graph2) { cudaGraphExecDestroy(ctx->graph2); ctx->graph2 = nullptr; ctx->graph2_w = 0; }
 }
 
 extern "C" {
@@ -650,6 +687,7 @@ int st_invalidate(st_ctx* ctx) {
     CK(cudaMemsetAsync(ctx->d_frame, 0, (size_t)ctx->slot_cap * sizeof(float4), ctx->stream), "memset");
     CK(cudaMemsetAsync(&ctx->d_ctr->sample, 0, sizeof(uint32_t), ctx->stream), "memset");
     CK(sppm_lt_reset(ctx_ext(ctx).sppm, ctx->stream), "memset");     // the emission map starts over uniform
+    CK(emit_reset(ctx), "emitter list reset");                         // and the emitters' discovery
     ctx->samples = 0;
     return ST_OK;
 }
@@ -662,8 +700,12 @@ int st_step_async(st_ctx* ctx, int n) {
     int rc = ensure_wave(ctx);
     if (rc) return rc;
     uint32_t left = (uint32_t)n;
+    const bool emitters = has_emitters(ctx);
     while (left > 0) {
         uint32_t w = std::min(left, ctx->spw);
+        // an emitter scene's first two waves are EMIT_EPOCH samples each: the list is built between waves (samples
+        // in a wave run together), so it is found after the first and aimed at from the second on
+        if (emitters && ctx->samples < 2 * EMIT_EPOCH) w = std::min(w, EMIT_EPOCH);
         rc = run_wave(ctx, w);
         if (rc) return rc;
         left -= w;

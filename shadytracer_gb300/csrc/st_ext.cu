@@ -12,6 +12,10 @@ void ext_free(StExt& e) {
     void* gs[] = {g.param, g.grad, g.m1, g.m2, g.wbf, (void*)g.dev, (void*)g.samp, g.act, g.mix, (void*)g.rec, g.acc};
     for (void* p : gs)
         if (p) cudaFree(p);
+    EmitState& m = e.emit;
+    void* ms[] = {m.grid, (void*)m.dev, m.w, m.hpos, m.hdir, m.hrad};
+    for (void* p : ms)
+        if (p) cudaFree(p);
     optics_free(e.optics);
     e = StExt{};
 }

@@ -84,10 +84,24 @@ int guide_train_samples(st_ctx* ctx, const float* pos, const float* nrm, const f
                         uint32_t n, uint32_t steps, float lr);
 void guide_box(st_ctx* ctx, st::f3& lo, float& inv_ext);     // the hash grid's box (st_capi.cu)
 
+// THE EMITTER LIST (st_emit.cu): the discovery grid and the list, the per-slot MIS weights, the hit queue
+struct EmitState {
+    uint32_t* grid = nullptr;
+    st::EmitDev* dev = nullptr;
+    float* w = nullptr;
+    uint32_t w_cap = 0;
+    float4 *hpos = nullptr, *hdir = nullptr, *hrad = nullptr;
+    uint32_t h_cap = 0;
+};
+int emit_ensure(st_ctx* ctx, uint32_t slots, uint32_t scap);
+st::EmitBufs emit_bufs(st_ctx* ctx, uint32_t nee, float share, float half);
+cudaError_t emit_reset(st_ctx* ctx);
+
 struct StExt {
     SppmState sppm;
     OpticsState optics;
     GuideState guide;
+    EmitState emit;
 };
 
 void ext_free(StExt& e);

@@ -78,7 +78,8 @@ struct DevCtr {
     uint32_t rayCount[2], hitCount, shadowCount[2];
     uint32_t marchHead, occHead, errflag;
     uint32_t nonfinite, flushed, shadowcut, sample;   // sample: the first sample of the wave in flight
-    uint32_t shadowdrop, pad1, pad2, pad3;
+    uint32_t shadowdrop, emitHits, pad2, pad3;        // emitHits: this iteration's shadow rays that met something
+                                                      // while aiming at an emitter
     unsigned long long paths, segments, march_steps, shadow_rays, shadow_steps;
     unsigned long long work[WC_N];     // the march's fold, counted in a counting pass (WC_* in st_device.cuh)
 };
@@ -136,6 +137,32 @@ struct GuideBufs {
     uint32_t keep = 0;                    // a record joins the batch when its hash is below this (of 2^32)
 };
 
+// THE EMITTER LIST (core/tracebasics.js:1140-1210 EMIT_LIST; wavefront.js:715-815 prog_emit_collect / publish;
+// materials_pbr.js:887-905 emitDeposit): what the camera paths that hit emissive surfaces found, in a grid of
+// EMIT_G^3 voxels over +-half, turned every EMIT_EPOCH samples into at most EMIT_MAX bounding spheres that light
+// sampling aims at (st_emit.cu, st_emit.cuh)
+#define EMIT_G 16u
+#define EMIT_CELLS (EMIT_G * EMIT_G * EMIT_G)
+#define EMIT_MAX 64u
+#define EMIT_EPOCH 2u
+#define SHADOW_EMIT 0x80000000u           // a shadow side's steps word: the ray aims at an emitter (TAG_EMIT)
+struct EmitDev {
+    uint32_t count, last, pad0, pad1;     // boxes listed; the sample the list was last built before
+    float4 box[EMIT_MAX];                 // centre, radius: each box's bounding sphere
+    float4 pc[EMIT_MAX];                  // its probability, the cumulative probability, 0, 0
+};
+struct EmitBufs {
+    uint32_t on = 0;                      // the scene has emissive materials: discovery, the list, the MIS weights
+    uint32_t nee = 0;                     // light sampling aims at the list's boxes
+    float share = 0.5f;                   // ...with this share of the light samples once anything is listed
+    float half = 15.f;                    // the grid's half-size, metres
+    uint32_t* grid = nullptr;             // EMIT_CELLS x 8 words: min q xyz, max q xyz, brightness code, hits
+    EmitDev* dev = nullptr;
+    float* w = nullptr;                   // per slot: an emitter hit's MIS weight against the last vertex's light sample
+    float4 *hpos = nullptr, *hdir = nullptr, *hrad = nullptr;   // shadow rays that met something: where, dir | pixel,
+                                                                // contribution | n (resolved by k_emit_resolve)
+};
+
 struct WaveArgs {
     Uni u;
     const DPrim* prims;
@@ -154,6 +181,7 @@ struct WaveArgs {
     const uint2* inst_range = nullptr;   // a batch of instances (the optics bench): each one's [first, count) of the
                                          // table, the instance in meta.w; null for a picture
     GuideBufs gd;                         // the learned proposal, while it runs
+    EmitBufs em;                          // the emitter list, in a scene with emitters
 };
 
 // launch wrappers (st_render.cu)
@@ -175,6 +203,10 @@ cudaError_t launch_march(const WaveArgs& a, int cur, int nxt, int last, int sms,
 cudaError_t launch_shade(const WaveArgs& a, int nxt, int side, int last, int sms, cudaStream_t s);
 cudaError_t launch_occlude(const WaveArgs& a, int side, int last, int sms, cudaStream_t s);
 cudaError_t launch_resolve(const WaveArgs& a, cudaStream_t s);
+// the emitter list (st_emit.cu)
+cudaError_t launch_emit_build(const WaveArgs& a, float margin, cudaStream_t s);
+cudaError_t launch_emit_resolve(const WaveArgs& a, int sms, cudaStream_t s);
+cudaError_t launch_emit_reset(const EmitBufs& em, cudaStream_t s);
 // the learned proposal (st_guide.cu)
 cudaError_t launch_guide_infer(const WaveArgs& a, int sms, cudaStream_t s);
 cudaError_t launch_guide_collect(const WaveArgs& a, int sms, cudaStream_t s);

@@ -15,6 +15,7 @@
 // warp keeps 32 rays in flight however uneven their step counts. The scene's primitive table is staged into
 // shared memory by one bulk copy (cp.async.bulk + mbarrier) per CTA and read as broadcasts. Nothing is read back
 // by the host inside a sample: every kernel sizes itself from the device counters.
+#include "st_emit.cuh"
 #include "st_guide.cuh"
 #include "st_kernels.cuh"
 
@@ -103,6 +104,7 @@ __global__ void __launch_bounds__(256) k_genrays(WaveArgs a) {
         a.pb.rad[i] = make_float4(0.f, 0.f, 0.f, 0.f);
         a.pb.meta[i] = make_uint4(pix, RAY_ACTIVE << 16, 0u, __float_as_uint(0.f));
         a.pb.lam[i] = 0.f;
+        if (a.em.w) a.em.w[i] = 1.f;                                  // a camera ray: no light sample to weigh against
         a.q.ray[0][i] = i;
     }
 }
@@ -116,6 +118,7 @@ __global__ void k_iter_begin(DevCtr* ctr, int it, int nxt, uint32_t slots, int f
         ctr->shadowCount[(it + 1) & 1] = 0u;
         ctr->marchHead = 0u;
         ctr->occHead = 0u;
+        ctr->emitHits = 0u;
     }
 }
 
@@ -403,14 +406,14 @@ __global__ void __launch_bounds__(256, 3) k_surface(WaveArgs a) {
     }
 }
 
-struct ShadowOut { bool valid; f3 org, dir, rad; float n; };
+struct ShadowOut { bool valid, emit; f3 org, dir, rad; float n; };
 
 template <bool GUIDE>
 __device__ __forceinline__ void shade_surface(const WaveArgs& a, const st_material* sm, float4 surf,
                                               f3& pos, f3& dir, float& ltot, float& n, f3& beta, float& sunmis,
                                               f3& rad, uint32_t& bounces, uint32_t& state, float& lam,
                                               uint32_t& lens, float dh, Rng& rng, bool last, ShadowOut& sh,
-                                              uint32_t q, uint32_t& my, uint32_t gpix) {
+                                              uint32_t q, uint32_t& my, uint32_t gpix, float& emw) {
     const Uni& u = a.u;
     float eps = march_tol(pos, u.tol);
     const uint32_t ids = __float_as_uint(surf.w);
@@ -427,7 +430,10 @@ __device__ __forceinline__ void shade_surface(const WaveArgs& a, const st_materi
     const st_material& m = sm[ids & 0xffffu];
     f3 emis = mk(m.emissive[0], m.emissive[1], m.emissive[2]);
     if (max3(emis) > 0.f) {                                           // emitterHit (materials_pbr.js:1014-1075)
-        rad = rad + beta * emis;
+        // weighed against the light sample the last vertex could have drawn this direction with (emw, set there),
+        // and discovered: its place and brightness into the emitter grid
+        rad = rad + beta * emis * emw;
+        if (a.em.on) emit_deposit(a.em, pos, emis);
         state = RAY_SOURCE;
         f3 off = dir * (otol * 2.f);
         pos = pos + off; ltot += length(off) * n;
@@ -472,24 +478,41 @@ __device__ __forceinline__ void shade_surface(const WaveArgs& a, const st_materi
     const bool guided = GUIDE && a.gd.on != 0u && !last && !inside && bounces == 1u && guide_vertex(m);
     const uint2* __restrict__ gmix = a.gd.mix + (size_t)q * GUIDE_LOBES;
     const float galpha = guided ? guide_share(a.gd.alpha, &a.gd.dev->step, a.gd.train) : 0.f;
+    // the discovered emitters' share of the light samples (materials_pbr.js:1216-1330): 0 while nothing is listed,
+    // when the environment's draw is the one it always was
+    const float es = (a.em.on && u.nee != 0u && !last) ? emit_share(a.em) : 0.f;
     if (u.nee != 0u && !last) {                                       // light sampling (materials_pbr.js:1196-1330)
         float4 u0 = rng.next();
         float4 u1 = rng.next();
         if (!lobes_none(m, trans)) {
-            f3 L = env_sample_dir(u, nrm, u0.x, u1.x, u1.y);
+            f3 L = mk(0.f, 0.f, 1.f);
+            float pS = 0.f;
+            bool toEmit = false;
+            if (u0.x < es) {                                          // an emitter: a box, a direction into its cone
+                const uint32_t b = emit_pick(a.em.dev, u0.x / es);
+                if (emit_sample(a.em.dev, b, pos, u1.x, u1.y, L)) {
+                    pS = es * emit_cone_pdf(a.em.dev, pos, L);        // the whole mixture's density, not the box's
+                    toEmit = true;
+                }
+            } else {                                                  // the environment: sun disc or sky
+                L = env_sample_dir(u, nrm, es > 0.f ? (u0.x - es) / (1.f - es) : u0.x, u1.x, u1.y);
+                pS = (1.f - es) * env_pdf(u, L, nrm);
+            }
             float NoL = dot(nrm, L);
-            float pL = env_pdf(u, L, nrm);
-            if (NoL > 0.f && pL > 0.f) {
-                f3 le = env_radiance(u, L);
+            if (NoL > 0.f && pS > 0.f) {
+                // an emitter's radiance is the occlusion pass's to multiply in, where its ray stops
+                f3 le = toEmit ? mk(1.f) : env_radiance(u, L);
                 f3 f = lobes_eval(lb, a.tab, L, 0.f);
                 float pB = lobes_pdf(lb, L);
                 if (guided) pB = galpha * guide_pdf(gmix, L) + (1.f - galpha) * pB;
-                float w = mis_weight(pL, pB);
-                f3 contrib = beta * f * le * (fabsf(NoL) * (w / pL));
-                if (max3(contrib) > 1e-7f) {
+                float w = mis_weight(pS, pB);
+                f3 contrib = beta * f * le * (fabsf(NoL) * (w / pS));
+                if (max3(contrib) > (toEmit ? 1e-9f : 1e-7f)) {
                     float tr = 1.f;
-                    if (u.haze_on && fabsf(n - 1.f) <= 1e-3f) tr = haze_tr(u, pos, L, 2.f * u.envR + length(pos));
+                    if (!toEmit && u.haze_on && fabsf(n - 1.f) <= 1e-3f)
+                        tr = haze_tr(u, pos, L, 2.f * u.envR + length(pos));
                     sh.valid = true;
+                    sh.emit = toEmit;
                     sh.org = pos + nrm * (otol * 2.f);
                     sh.dir = L;
                     sh.rad = contrib * tr;
@@ -543,10 +566,14 @@ __device__ __forceinline__ void shade_surface(const WaveArgs& a, const st_materi
     if (u.nee != 0u && !last) {                                       // the other half of MIS (:1370-1395)
         bool above = dot(nrm, dir) > 0.f && !smp.isDelta;
         float pOut = smp.isDelta ? 0.f : (guided ? pGuided : lobes_pdf(lb, smp.dir));
-        float pLout = above ? env_pdf(u, dir, nrm) : 0.f;
+        float pLout = above ? (1.f - es) * env_pdf(u, dir, nrm) : 0.f;
         sunmis = pLout <= 0.f ? 1.f : mis_weight(pOut, pLout);
+        // an emitter this bounce meets is weighed against the list's density for the direction, from here
+        const float pEout = (above && es > 0.f) ? es * emit_cone_pdf(a.em.dev, pos, dir) : 0.f;
+        emw = pEout <= 0.f ? 1.f : mis_weight(pOut, pEout);
     } else {
         sunmis = 1.f;
+        emw = 1.f;
     }
     f3 off = dir * otol;
     pos = pos + off; ltot += length(off) * n;
@@ -622,13 +649,13 @@ __global__ void __launch_bounds__(256) k_shade(WaveArgs a, int nxt, int side, in
         uint32_t q = r * stride + blockIdx.x * blockDim.x + threadIdx.x;
         bool valid = q < count;
         bool cont = false;
-        ShadowOut sh; sh.valid = false;
+        ShadowOut sh; sh.valid = false; sh.emit = false;
         uint32_t slot = 0, pix = 0, gpix = 0;
         f3 pos, dir, beta, rad;
         float ltot = 0.f, n = 1.f, sunmis = 1.f, tmax = 0.f;
         uint4 m4 = make_uint4(0, 0, 0, 0);
         uint32_t bounces = 0, seg = 0, state = RAY_TERMINATED;
-        float lam = 0.f;
+        float lam = 0.f, emw = 1.f;
         bool train_nee = false;
         if (valid) {
             slot = a.q.hit[q];
@@ -646,12 +673,14 @@ __global__ void __launch_bounds__(256) k_shade(WaveArgs a, int nxt, int side, in
                 rad = rad + beta * (owned ? env_sky(u, dir) : env_radiance(u, dir)) * sunmis;
             } else if (state == RAY_ACTIVE || state == RAY_SCATTER) {
                 train_nee = GUIDE && (m4.y & META_TRAIN) != 0u;       // light found past a record's vertex counts
+                if (a.em.on) emw = a.em.w[slot];
                 uint32_t tile = slot % u.P, j = slot / u.P;
                 Rng rng = path_rng(sample_seed(u.seed, a.ctr->sample + j), tile, 1u + seg);
                 seg += 1;
                 m4.w = __float_as_uint(ltot);                         // absorbAlong: absLtot on arrival
                 if (state == RAY_SCATTER) {
                     shade_medium(a, pos, dir, beta, sunmis, bounces, state, n, rng, last != 0, sh);
+                    emw = 1.f;                                        // no emitter light sample from the air
                     m4.y &= ~(3u << META_LENS_SHIFT);                 // haze.js:539: the air is no delta event
                 }
                 else
@@ -659,7 +688,7 @@ __global__ void __launch_bounds__(256) k_shade(WaveArgs a, int nxt, int side, in
                     lam = a.pb.lam[slot];
                     uint32_t lens = (m4.y >> META_LENS_SHIFT) & 3u;
                     shade_surface<GUIDE>(a, sm, a.q.hsurf[q], pos, dir, ltot, n, beta, sunmis, rad, bounces, state,
-                                         lam, lens, dh, rng, last != 0, sh, q, m4.y, gpix);
+                                         lam, lens, dh, rng, last != 0, sh, q, m4.y, gpix, emw);
                     m4.y = (m4.y & ~(3u << META_LENS_SHIFT)) | (lens << META_LENS_SHIFT);
                 }
                 if (state == RAY_ACTIVE) {
@@ -676,7 +705,7 @@ __global__ void __launch_bounds__(256) k_shade(WaveArgs a, int nxt, int side, in
                 s_org[sq] = f4(sh.org, 0.f);
                 s_dir[sq] = f4(sh.dir, __uint_as_float(gpix));
                 s_rad[sq] = f4(sh.rad, train_nee ? -sh.n : sh.n);    // a negative index: counted for a record
-                s_steps[sq] = 0u;
+                s_steps[sq] = sh.emit ? SHADOW_EMIT : 0u;
             } else {
                 dropped++;
             }
@@ -688,6 +717,7 @@ __global__ void __launch_bounds__(256) k_shade(WaveArgs a, int nxt, int side, in
             a.pb.beta[slot] = f4(beta, sunmis);
             a.pb.rad[slot] = f4(rad, tmax);
             if (lam != 0.f) a.pb.lam[slot] = lam;
+            if (a.em.on) a.em.w[slot] = emw;
             m4.y = meta_y(bounces, seg, RAY_ACTIVE) | (m4.y & ~META_LOW);
             a.pb.meta[slot] = m4;
             outq[rq] = slot;
@@ -747,7 +777,7 @@ __global__ void __launch_bounds__(256, 4) k_occlude(WaveArgs a, int last) {
     uint32_t idx = INVALID_SLOT;
     f3 pos = mk(0.f), dir = mk(0.f);
     float ltot = 0.f, n = 1.f;
-    uint32_t steps = 0, evals_here = 0;
+    uint32_t steps = 0, evals_here = 0, sflag = 0;
     uint32_t wpos = 0, wend = 0;
     bool exhausted = false;
     unsigned long long evals = 0, rays = 0;
@@ -770,6 +800,8 @@ __global__ void __launch_bounds__(256, 4) k_occlude(WaveArgs a, int last) {
                     float4 o4 = i_org[idx], d4 = i_dir[idx];
                     pos = xyz(o4); ltot = o4.w; dir = xyz(d4); n = fabsf(i_rad[idx].w);
                     steps = i_steps[idx];
+                    sflag = steps & SHADOW_EMIT;                      // aimed at an emitter (TAG_EMIT)
+                    steps &= ~SHADOW_EMIT;
                     evals_here = 0;
                     if (steps == 0u) rays++;
                 }
@@ -800,7 +832,16 @@ __global__ void __launch_bounds__(256, 4) k_occlude(WaveArgs a, int last) {
             }
         }
         uint32_t cp = warp_append(o_cnt, more);
-        if (reached) {
+        // an emitter's ray asks what it stopped at (wavefront.js:1694-1749): handed to k_emit_resolve; it finds
+        // nothing where it leaves the scene
+        const bool met = done && !reached && sflag != 0u;
+        const uint32_t ep = a.em.on ? warp_append(&a.ctr->emitHits, met) : 0u;
+        if (met && ep < a.q.scap) {
+            a.em.hpos[ep] = f4(pos, ltot);
+            a.em.hdir[ep] = i_dir[idx];
+            a.em.hrad[ep] = i_rad[idx];
+        }
+        if (reached && sflag == 0u) {
             float4 r4 = i_rad[idx];
             uint32_t gpix = __float_as_uint(i_dir[idx].w);          // the pixel in the wave's frames
             deposit(a.frame, gpix, xyz(r4), a.ctr);
@@ -811,7 +852,7 @@ __global__ void __launch_bounds__(256, 4) k_occlude(WaveArgs a, int last) {
                 o_org[cp] = f4(pos, ltot);
                 o_dir[cp] = i_dir[idx];
                 o_rad[cp] = i_rad[idx];
-                o_steps[cp] = steps;
+                o_steps[cp] = steps | sflag;
             } else {
                 dropped++;
             }

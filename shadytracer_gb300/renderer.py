@@ -161,6 +161,14 @@ class PathTracer:
     def stream(self):
         return self.L.st_stream(self.ctx)
 
+    # ---- emissive surfaces ----
+    def emit_list(self):
+        """The emitter list light sampling aims at: n x [centre xyz, radius, probability, running sum]."""
+        out = np.zeros((64, 6), np.float32)
+        n = C.c_uint32()
+        check(self.L.st_emit_list(self.ctx, out.ctypes.data_as(C.c_void_p), 64, C.byref(n)), self.ctx, "st_emit_list")
+        return out[:n.value]
+
     # ---- the learned proposal (st_params.guide; include/shadytracer.h st_mlp_*) ----
     def mlp_weights(self):
         """Every parameter, FP32: W1 (64x48), W2, W3 (64x64), W4 (40x64), then the hash grid's features."""

@@ -171,6 +171,40 @@ def floor_furnace(width=256, height=256, spp=16, albedo=0.8, sky=1000.0, maxboun
     return s
 
 
+def emitter(le):
+    """makeEmissive (core/materials.js:263-268): emitted luminance `le` (cd/m^2, rgb), air beyond."""
+    return material(base=(0, 0, 0), specular=0.0, ior=1.0, emissive=le)
+
+
+def lamp_floor(width=96, height=64, spp=64, radius=0.1, lamp_height=1.0, le=1000.0, albedo=0.8, maxbounce=2,
+               seed=1):
+    """An emissive sphere of `radius` and luminance `le` (cd/m^2) at `lamp_height` over an infinite Lambertian floor
+    (reflectance `albedo`) in a black environment. A sphere of uniform luminance lights a point it is wholly above as a
+    point source of intensity pi a^2 Le at its centre, so a floor pixel's closed form is albedo Le a^2 h / D^3, D the
+    distance to the centre (h = lamp_height); the floor cannot see itself, so any bounce cap of 1 or more keeps it."""
+    s = Scene([prim(ST_PRIM_PLANE, material=1), prim(ST_PRIM_SPHERE, pos=(0.0, 0.0, lamp_height), params=(radius,),
+                                                      material=2)],
+              [air(), diffuse((albedo, albedo, albedo)), emitter((le, le, le))], env_radius=20.0, name="lamp-floor")
+    # a march tolerance of 1e-4 m: a ray meets the lamp within the tolerance of its surface, so the lamp lights the
+    # floor as a sphere that much larger (the scene's default, from its 20 m radius, would add 4 %)
+    s.params = default_params(width=width, height=height, maxbounce=maxbounce, sun_hint=0, sun_illuminance=0.0,
+                              sky_luminance=0.0, ground_luminance=0.0, seed=seed, eps=1e-4)
+    eye = (0.0, -2.5, 2.0)
+    target = (0.0, 0.6, 0.0)
+    s.view = look_at(eye, target, 55.0, width / height)
+    s.info = {"spp": spp, "workload": "lamp-floor", "lamp": (0.0, 0.0, lamp_height, radius, le), "albedo": albedo}
+    return s
+
+
+def lamp_floor_closed_form(scene, points):
+    """The floor's luminance at floor points (n x 3, z = 0): albedo Le a^2 h / D^3."""
+    import numpy as np
+    cx, cy, cz, a, le = scene.info["lamp"]
+    d = np.asarray(points, np.float64) - np.array([cx, cy, cz])
+    D = np.linalg.norm(d, axis=-1)
+    return scene.info["albedo"] * le * a * a * cz / D ** 3
+
+
 # ---------------------------------------------------------------------------------------------------------------
 # Config 2: the path-traced SDF room.
 # ---------------------------------------------------------------------------------------------------------------

@@ -58,7 +58,8 @@ class StParams(C.Structure):
                 ("sppm", C.c_uint32), ("sppm_photons", C.c_uint32), ("sppm_r1", C.c_float),
                 ("sppm_alpha", C.c_float), ("sppm_half", C.c_float), ("sppm_learn", C.c_uint32),
                 ("guide", C.c_uint32), ("guide_alpha", C.c_float), ("guide_lr", C.c_float),
-                ("guide_train", C.c_uint32), ("guide_seed", C.c_uint32)]
+                ("guide_train", C.c_uint32), ("guide_seed", C.c_uint32),
+                ("emit_share", C.c_float), ("emit_radius", C.c_float), ("emit_off", C.c_uint32)]
 
 
 class StView(C.Structure):
@@ -158,6 +159,9 @@ def default_params(**kw):
     p.guide_lr = 0.0
     p.guide_train = 1
     p.guide_seed = 0
+    p.emit_share = 0.0
+    p.emit_radius = 0.0
+    p.emit_off = 0
     for k, v in kw.items():
         if not hasattr(p, k):
             raise KeyError(k)

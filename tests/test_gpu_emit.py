@@ -1,0 +1,99 @@
+"""Emissive surfaces on the GPU (csrc/st_emit.cu, st_emit.cuh; st_render.cu's light sample and emitter hits; the
+occlusion pass's hand-off), through the C ABI: the lamp over a floor against its closed form and against the oracle
+(oracle/st_oracle.cpp's restatement of discovery, the list and the emitter light sample), the list the discovery
+builds, and the light sample's gain over finding the lamp by the BSDF alone.
+"""
+import numpy as np
+import pytest
+
+from shadytracer_gb300 import scenes
+from oracle import oracle
+
+pytestmark = pytest.mark.gpu
+
+LUMA = np.array([0.2126, 0.7152, 0.0722])
+
+
+def se_of(V, S):
+    ok = (S > 0) & (S < 1)
+    out = np.zeros_like(V)
+    out[ok] = np.sqrt(S[ok] * V[ok] / (1 - S[ok]))
+    return out
+
+
+def floor_pixels(s):
+    """Each pixel's centre ray's floor point and closed form, and which pixels see the floor (not the lamp)."""
+    W, H = s.params.width, s.params.height
+    v = s.view
+    fwd, right, up, eye = [np.array(list(x), np.float64) for x in (v.fwd, v.right, v.up, v.cam_pos)]
+    X, Y = np.meshgrid((np.arange(W) + 0.5) / W * 2 - 1, (np.arange(H) + 0.5) / H * 2 - 1)
+    d = -fwd + right * (X[..., None] * v.fx) + up * (Y[..., None] * v.fy)
+    d /= np.linalg.norm(d, axis=-1, keepdims=True)
+    t = -eye[2] / d[..., 2]
+    pts = eye + d * t[..., None]
+    cx, cy, cz, a, le = s.info["lamp"]
+    oc = eye - np.array([cx, cy, cz])
+    b = np.sum(d * oc, -1)
+    near_lamp = (b * b - (oc @ oc - (1.5 * a) ** 2)) > 0
+    # the floor within 8 m: beyond the scene's radius (20 m) a ray leaves the scene before it meets the floor
+    near = np.linalg.norm(pts[..., :2], axis=-1) < 8.0
+    return scenes.lamp_floor_closed_form(s, pts), (t > 0) & ~near_lamp & near
+
+
+def render(s, n):
+    from shadytracer_gb300.renderer import create_path_tracer
+    with create_path_tracer(s, device=0) as r:
+        r.step(n)
+        rgb, V, S, cnt = r.read_accum()
+        lst = r.emit_list()
+    return rgb @ LUMA, se_of(V, S), lst
+
+
+def test_lamp_floor_closed_form():
+    """The floor under a sphere lamp in the dark reads albedo Le a^2 h / D^3 (the sphere as a point source), with the
+    lamp found by the camera paths and light sampling aimed at it from the third sample on."""
+    s = scenes.lamp_floor(width=96, height=64)
+    L, se, lst = render(s, 512)
+    cf, ok = floor_pixels(s)
+    r = L[ok] / cf[ok]
+    assert abs(np.median(r) - 1) < 0.01 and abs(L[ok].sum() / cf[ok].sum() - 1) < 0.01, (np.median(r), L[ok].sum() / cf[ok].sum())
+    # the pixels' footprints average L over about 4 cm of floor: second order, well under the error bars' share
+    z = (L - cf)[ok] / np.maximum(se[ok], 1e-3 * cf[ok])
+    assert np.mean(np.abs(z) < 4) > 0.97, np.mean(np.abs(z) < 4)
+    # the list: the lamp sits on a corner of four voxels (the grid's 1.875 m cells meet at x = y = 0), so four boxes,
+    # each the bounding sphere of its quarter of the lamp, a quarter of the probability each
+    assert len(lst) == 4
+    assert np.all(np.linalg.norm(lst[:, :3] - np.array([0.0, 0.0, 1.0]), axis=1) < 0.1)
+    assert np.all((lst[:, 3] > 0.07) & (lst[:, 3] < 0.15))
+    assert np.allclose(lst[:, 4], 0.25, atol=0.01) and abs(lst[-1, 5] - 1) < 1e-6
+
+
+def test_lamp_floor_matches_the_oracle():
+    s = scenes.lamp_floor(width=48, height=32)
+    s.params.samples_per_wave = 1                # a list built between every two samples, as the oracle's
+    L, se, _ = render(s, 64)
+    ref = oracle.render(s, 64)
+    Lr = ref.luma()
+    ser = se_of(ref.V, ref.S)
+    sd = np.hypot(se, ser)
+    ok = sd > 0
+    z = (L - Lr)[ok] / sd[ok]
+    assert np.mean(np.abs(z) < 4) > 0.98, np.mean(np.abs(z) < 4)
+    zm = (L - Lr)[ok].mean() / (np.sqrt(np.sum(sd[ok] ** 2)) / ok.sum())
+    assert abs(zm) < 5, zm
+
+
+def test_light_sampling_the_lamp_is_unbiased_and_pays():
+    """With the emitter light sample off, the floor is lit only by the BSDF's hits of the lamp: the same mean, a far
+    larger error against the closed form."""
+    out = {}
+    for off in (0, 1):
+        s = scenes.lamp_floor(width=96, height=64)
+        s.params.emit_off = off
+        L, se, _ = render(s, 256)
+        cf, ok = floor_pixels(s)
+        out[off] = (L[ok].mean(), np.sqrt(np.sum(se[ok] ** 2)) / ok.sum(),
+                    float(np.sqrt(np.mean((L[ok] - cf[ok]) ** 2)) / cf[ok].mean()))
+    (m0, s0, e0), (m1, s1, e1) = out[0], out[1]
+    assert abs(m0 - m1) < 5 * np.hypot(s0, s1) + 0.01 * m0, out
+    assert e1 > 4 * e0, out                       # relative RMSE: the BSDF alone over with the light sample

@@ -77,3 +77,25 @@ def test_photon_map_pane_closed_form():
     n, pw = oracle.sppm_photons(s, 0, lo=(-0.3, -0.3, -0.01), hi=(0.3, 0.3, 0.01))
     E = (pw @ np.array([0.2126, 0.7152, 0.0722])) / 0.36
     assert abs(E / (1e5 * math.sin(math.radians(60)) * (1 - Fs) / (1 + Fs)) - 1) < 0.01
+
+
+def test_lamp_floor_closed_form():
+    """The oracle's emitter discovery, list and light sample (materials_pbr.js:887-960, wavefront.js:715-815): the
+    floor under a sphere lamp in the dark reads albedo Le a^2 h / D^3, and the list is the lamp's voxels."""
+    s = scenes.lamp_floor(width=48, height=32)
+    ref = oracle.render(s, 256)
+    L = ref.luma()
+    W, H = s.params.width, s.params.height
+    v = s.view
+    fwd, right, up, eye = [np.array(list(x), np.float64) for x in (v.fwd, v.right, v.up, v.cam_pos)]
+    X, Y = np.meshgrid((np.arange(W) + 0.5) / W * 2 - 1, (np.arange(H) + 0.5) / H * 2 - 1)
+    d = -fwd + right * (X[..., None] * v.fx) + up * (Y[..., None] * v.fy)
+    d /= np.linalg.norm(d, axis=-1, keepdims=True)
+    t = -eye[2] / d[..., 2]
+    pts = eye + d * t[..., None]
+    oc = eye - np.array([0.0, 0.0, 1.0])
+    b = np.sum(d * oc, -1)
+    ok = (t > 0) & ((b * b - (oc @ oc - 0.15 ** 2)) <= 0) & (np.linalg.norm(pts[..., :2], axis=-1) < 8.0)
+    cf = scenes.lamp_floor_closed_form(s, pts)
+    assert abs(L[ok].sum() / cf[ok].sum() - 1) < 0.02, L[ok].sum() / cf[ok].sum()
+    assert abs(np.median(L[ok] / cf[ok]) - 1) < 0.02
