@@ -28,6 +28,8 @@ optics: the batched optics bench (64 emitter + aspheric-lens instances, 120.2 M 
        tallies) in rays/s, with the tallies on the device (`value`) and read back every run (`e2e`).
 mlp: the learned proposal (a BF16 network guiding BSDF sampling): relative RMSE and GPU time, plain against guided,
        on the diffuse room lit by the sun's patch; the network's inference and training flops a second.
+emit: emissive surfaces: a sphere lamp over a floor (its closed form): Mpaths/s with the discovered lamp light-sampled,
+       and the relative RMSE with and without that light sample at equal samples.
 Multi-GPU (torchrun): replicas -- each rank renders the whole workload on its own GPU; value sums the ranks' paths
        over the slowest rank's time (weak scaling). There is no data exchange in the path tracer.
 """
@@ -59,7 +61,8 @@ def parse():
     ap.add_argument("--no-sppm", action="store_true", help="skip the photon map's photons/s leg")
     ap.add_argument("--spp", type=int, default=0, help="samples per pixel a step (profiling runs; default: 64)")
     ap.add_argument("--no-mlp", action="store_true", help="skip the learned proposal's leg")
-    ap.add_argument("--leg", default="all", choices=["all", "sppm", "rmse", "optics", "mlp"],
+    ap.add_argument("--no-emit", action="store_true", help="skip the emissive surfaces' leg")
+    ap.add_argument("--leg", default="all", choices=["all", "sppm", "rmse", "optics", "mlp", "emit"],
                     help="run one leg alone and print its JSON (profiling runs of the photon map or the optics bench)")
     return ap.parse_args()
 
@@ -410,6 +413,46 @@ def mlp_leg(args, dev):
     return out
 
 
+def emit_leg(args, dev):
+    """Emissive surfaces: a sphere lamp over a floor in the dark (its closed form, albedo Le a^2 h / D^3), 480 x 320,
+    256 samples: camera paths a second with the discovered lamp light-sampled, and the relative RMSE against the closed
+    form with the light sample and with the BSDF's hits alone, at equal samples and their GPU times."""
+    import torch
+    from shadytracer_gb300 import scenes
+    from shadytracer_gb300.renderer import create_path_tracer
+    W, H = (192, 128) if args.small else (480, 320)
+    spp = 64 if args.small else 256
+    out = {"workload": "lamp-floor: a 0.1 m sphere of 1000 cd/m^2 at 1 m over a 0.8 floor, black environment, %dx%d, "
+                       "%d samples" % (W, H, spp), "metric": "Mpaths/s", "legs": {}}
+    luma = np.array([0.2126, 0.7152, 0.0722])
+    for off in (0, 1):
+        s = scenes.lamp_floor(width=W, height=H, spp=spp)
+        s.params.emit_off = off
+        cf, ok = scenes.lamp_floor_pixels(s)
+        rt = create_path_tracer(s, device=dev)
+        stream = torch.cuda.ExternalStream(rt.stream(), device=torch.device("cuda", dev))
+        for _ in range(max(args.warmup, 3)):
+            rt.invalidate()
+            rt.step(spp)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        rt.invalidate()
+        e0.record(stream)
+        rt.step_async(spp)
+        e1.record(stream)
+        rt.sync()
+        ms = e0.elapsed_time(e1)
+        L = rt.read_accum()[0] @ luma
+        out["legs"]["bsdf_only" if off else "light_sampled"] = {
+            "ms": ms, "Mpaths_per_s": W * H * spp / (ms / 1e3) / 1e6,
+            "rmse": float(np.sqrt(np.mean((L[ok] - cf[ok]) ** 2)) / cf[ok].mean()),
+            "mean_over_closed_form": float(L[ok].sum() / cf[ok].sum()), "listed": int(len(rt.emit_list()))}
+        rt.close()
+    a, b = out["legs"]["light_sampled"], out["legs"]["bsdf_only"]
+    out["value"] = a["Mpaths_per_s"]
+    out["speedup_to_equal_rmse"] = (b["rmse"] / a["rmse"]) ** 2 * (b["ms"] / a["ms"])
+    return out
+
+
 def rmse_leg(args, dev):
     """Time to 1 % relative RMSE against the closed form, guided vs plain: the photon map's pane (a 0.5 m glass pane
     over a floor lit only through it, the sun's photons drawn over a 4 m square), plain -- the photons uniform over the
@@ -467,7 +510,8 @@ def run_ours(args):
     if args.leg != "all":
         with_cpu = rank == 0 and world == 1 and not args.no_cpu
         out = {"sppm": lambda: sppm_leg(args, dev, with_cpu), "rmse": lambda: rmse_leg(args, dev),
-               "optics": lambda: optics_leg(args, dev, with_cpu), "mlp": lambda: mlp_leg(args, dev)}[args.leg]()
+               "optics": lambda: optics_leg(args, dev, with_cpu), "mlp": lambda: mlp_leg(args, dev),
+               "emit": lambda: emit_leg(args, dev)}[args.leg]()
         if rank == 0:
             print(json.dumps(out), flush=True)
         return 0
@@ -626,6 +670,8 @@ def run_ours(args):
         line["time_to_rmse"] = rmse_leg(args, dev)
     if not args.no_mlp:
         line["mlp"] = mlp_leg(args, dev)
+    if not args.no_emit:
+        line["emit"] = emit_leg(args, dev)
     if not args.no_optics:
         line["optics"] = optics_leg(args, dev, rank == 0 and world == 1 and not args.no_cpu)
         if world > 1:

@@ -205,6 +205,26 @@ def lamp_floor_closed_form(scene, points):
     return scene.info["albedo"] * le * a * a * cz / D ** 3
 
 
+def lamp_floor_pixels(scene):
+    """Each pixel's closed form at its centre ray's floor point, and which pixels it holds for: the ray meets the
+    floor within 8 m (a ray leaves the 20 m scene before it meets the floor farther out) and passes clear of the lamp."""
+    import numpy as np
+    W, H = scene.params.width, scene.params.height
+    v = scene.view
+    fwd, right, up, eye = [np.array(list(x), np.float64) for x in (v.fwd, v.right, v.up, v.cam_pos)]
+    X, Y = np.meshgrid((np.arange(W) + 0.5) / W * 2 - 1, (np.arange(H) + 0.5) / H * 2 - 1)
+    d = -fwd + right * (X[..., None] * v.fx) + up * (Y[..., None] * v.fy)
+    d /= np.linalg.norm(d, axis=-1, keepdims=True)
+    t = -eye[2] / d[..., 2]
+    pts = eye + d * t[..., None]
+    cx, cy, cz, a, le = scene.info["lamp"]
+    oc = eye - np.array([cx, cy, cz])
+    b = np.sum(d * oc, -1)
+    clear = (b * b - (oc @ oc - (1.5 * a) ** 2)) <= 0
+    near = np.linalg.norm(pts[..., :2], axis=-1) < 8.0
+    return lamp_floor_closed_form(scene, pts), (t > 0) & clear & near
+
+
 # ---------------------------------------------------------------------------------------------------------------
 # Config 2: the path-traced SDF room.
 # ---------------------------------------------------------------------------------------------------------------

@@ -22,22 +22,7 @@ def se_of(V, S):
 
 
 def floor_pixels(s):
-    """Each pixel's centre ray's floor point and closed form, and which pixels see the floor (not the lamp)."""
-    W, H = s.params.width, s.params.height
-    v = s.view
-    fwd, right, up, eye = [np.array(list(x), np.float64) for x in (v.fwd, v.right, v.up, v.cam_pos)]
-    X, Y = np.meshgrid((np.arange(W) + 0.5) / W * 2 - 1, (np.arange(H) + 0.5) / H * 2 - 1)
-    d = -fwd + right * (X[..., None] * v.fx) + up * (Y[..., None] * v.fy)
-    d /= np.linalg.norm(d, axis=-1, keepdims=True)
-    t = -eye[2] / d[..., 2]
-    pts = eye + d * t[..., None]
-    cx, cy, cz, a, le = s.info["lamp"]
-    oc = eye - np.array([cx, cy, cz])
-    b = np.sum(d * oc, -1)
-    near_lamp = (b * b - (oc @ oc - (1.5 * a) ** 2)) > 0
-    # the floor within 8 m: beyond the scene's radius (20 m) a ray leaves the scene before it meets the floor
-    near = np.linalg.norm(pts[..., :2], axis=-1) < 8.0
-    return scenes.lamp_floor_closed_form(s, pts), (t > 0) & ~near_lamp & near
+    return scenes.lamp_floor_pixels(s)
 
 
 def render(s, n):
