@@ -190,6 +190,8 @@ typedef struct st_view {
     float    fwd[3];              /* from the target to the camera: the view looks down -fwd         */
     float    fx, fy;              /* invProjection[0][0], [1][1]: tan(fov/2) * aspect, tan(fov/2)    */
     uint32_t camtype;             /* 0 perspective, 1 orthographic                                 */
+    float    lens_radius;         /* the thin lens's aperture radius, metres (camLens.x; 0: a pinhole) */
+    float    focus_distance;      /* the distance to the plane in focus along -fwd, metres (camLens.y) */
 } st_view;
 
 typedef struct st_counters_t {

@@ -693,6 +693,13 @@ void trace_path(const Ctx<T>& C, U4 sseed, uint32_t tile, const st_view& v, uint
         V3<T> dc(xx * T(v.fx), yy * T(v.fy), T(-1));
         r.dir = normalize(right * dc.x + up * dc.y + fwd * dc.z);
         r.pos = cam;
+        if (v.lens_radius > 0.f) {                                                 // genrays.js:80-87, lens.js lensDisc
+            const T rr = T(v.lens_radius) * std::sqrt(rnd[2]);
+            const T ph = T(6.28318530718) * rnd[3];
+            const V3<T> off = right * (rr * std::cos(ph)) + up * (rr * std::sin(ph));
+            r.pos = cam + off;
+            r.dir = normalize((right * dc.x + up * dc.y + fwd * dc.z) * T(v.focus_distance) - off);
+        }
     } else {
         r.pos = cam + right * (xx * T(v.fx)) + up * (yy * T(v.fy));
         r.dir = -fwd;

@@ -167,6 +167,8 @@ static Uni make_uni(const st_ctx* ctx) {
     u.up = mk(v.up[0], v.up[1], v.up[2]);
     u.fwd = mk(v.fwd[0], v.fwd[1], v.fwd[2]);
     u.fx = v.fx; u.fy = v.fy; u.camtype = v.camtype;
+    u.lens_r = v.lens_radius > 0.f ? v.lens_radius : 0.f;
+    u.lens_f = v.focus_distance;
     double half = std::max((double)p.sun_diameter, 1e-3) * PI_D / 360.0;
     double sh = std::sin(half / 2);
     double omc = 2 * sh * sh;

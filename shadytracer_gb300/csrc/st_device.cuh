@@ -100,6 +100,7 @@ struct Uni {
     float stepscale, tol, envR2, envR;
     // camera (genrays.js:65-92)
     f3 cam, right, up, fwd; float fx, fy; uint32_t camtype;
+    float lens_r, lens_f;        // the thin lens (lens.js): aperture radius and focus distance; 0 a pinhole
     // environment (sdf.js:70-160)
     f3 sun_dir; float sun_sin2, sun_omc, sun_omega, pick; int sun_on;
     f3 disc; float sky, ground, uniform, sun_gain, sky_gain;

@@ -124,6 +124,8 @@ Uni uniforms(const st_scene_desc& s, const st_params& p, const st_view& v, uint3
     u.up = mk(v.up[0], v.up[1], v.up[2]);
     u.fwd = mk(v.fwd[0], v.fwd[1], v.fwd[2]);
     u.fx = v.fx; u.fy = v.fy; u.camtype = v.camtype;
+    u.lens_r = v.lens_radius > 0.f ? v.lens_radius : 0.f;
+    u.lens_f = v.focus_distance;
     double half = std::max((double)p.sun_diameter, 1e-3) * PI_D / 360.0;
     double sh = std::sin(half / 2), omc = 2 * sh * sh, sin2 = std::sin(half) * std::sin(half);
     double disc = (double)p.sun_illuminance / (PI_D * sin2);

@@ -91,6 +91,16 @@ __global__ void __launch_bounds__(256) k_genrays(WaveArgs a) {
             f3 dc = mk(xx * u.fx, yy * u.fy, -1.f);
             dir = normalize(u.right * dc.x + u.up * dc.y + u.fwd * dc.z);
             pos = u.cam;
+            // THROUGH THE LENS (genrays.js:80-87, lens.js lensDisc): from a point of its disc (the same draw's zw),
+            // at the point the pinhole's ray meets the focus plane
+            if (u.lens_r > 0.f) {
+                const float r = u.lens_r * sqrtf(rnd.z);
+                float sp, cp;
+                sincosf(6.28318530718f * rnd.w, &sp, &cp);
+                const f3 off = u.right * (r * cp) + u.up * (r * sp);
+                pos = u.cam + off;
+                dir = normalize((u.right * dc.x + u.up * dc.y + u.fwd * dc.z) * u.lens_f - off);
+            }
         } else {
             pos = u.cam + u.right * (xx * u.fx) + u.up * (yy * u.fy);
             dir = -u.fwd;

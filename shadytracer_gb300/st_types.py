@@ -64,7 +64,8 @@ class StParams(C.Structure):
 
 class StView(C.Structure):
     _fields_ = [("cam_pos", C.c_float * 3), ("right", C.c_float * 3), ("up", C.c_float * 3),
-                ("fwd", C.c_float * 3), ("fx", C.c_float), ("fy", C.c_float), ("camtype", C.c_uint32)]
+                ("fwd", C.c_float * 3), ("fx", C.c_float), ("fy", C.c_float), ("camtype", C.c_uint32),
+                ("lens_radius", C.c_float), ("focus_distance", C.c_float)]
 
 
 class StCounters(C.Structure):

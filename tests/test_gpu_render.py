@@ -131,3 +131,25 @@ def test_invalidate_and_state(rt_factory):
     rt.step(1)
     assert rt.read_accum()[3].max() == 1
     assert rt.set(maxbounce=3, not_a_setting=1) == ["not_a_setting"]
+
+
+def test_thin_lens_matches_the_oracle(rt_factory):
+    """The thin lens (genrays.js:80-87, lens.js lensDisc): a 5 cm aperture focused at 2 m in the room -- the picture
+    GPU and oracle agree on, pixel by pixel within the error bars, and the lens blurs (a pinhole's picture differs)."""
+    s = scenes.sdf_room(width=64, height=36, spp=16)
+    s.view.lens_radius = 0.05
+    s.view.focus_distance = 2.0
+    rt = rt_factory(s)
+    rt.step(16)
+    rgb, V, S, cnt = rt.read_accum()
+    ref = oracle.render(s, 16)
+    L, Lr = rgb @ LUMA, ref.luma()
+    sd = np.hypot(se_of(V, S), se_of(ref.V, ref.S))
+    ok = sd > 0
+    z = (L - Lr)[ok] / sd[ok]
+    assert np.mean(np.abs(z) < 4) > 0.98, np.mean(np.abs(z) < 4)
+    close = np.abs(L - Lr) <= 1e-3 * np.maximum(Lr, 1.0)
+    assert close.mean() > 0.5, close.mean()          # most paths take the same numbers through the lens too
+    s.view.lens_radius = 0.0
+    pin = oracle.render(s, 16).luma()
+    assert np.mean(np.abs(pin - Lr) > 0.05 * np.maximum(Lr, 1.0)) > 0.2
