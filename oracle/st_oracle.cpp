@@ -639,20 +639,47 @@ void medium_vertex(const Ctx<T>& C, Ray<T>& r, Rng& rng, bool last, Frame<T>& fr
     T g = clampT(C.haze.g, T(-0.95), T(0.95));
     V3<T> din = r.dir;
     r.beta = r.beta * C.haze.albedo;
+    // the discovered emitters' share of the air's light samples (haze.js:324-370), as at a surface
+    const T es = (C.em_on && C.em_nee && C.p.nee != 0 && !last && C.em->count > 0)
+                     ? T(std::min(std::max(C.em_share, 0.05f), 0.95f)) : T(0);
     if (C.p.nee != 0 && !last) {
         T u0[4], u1[4];
         rng.next4(u0); rng.next4(u1);
-        V3<T> L = env_sample_dir_m(C.env, u0[0], u1[0], u1[1]);
-        T pL = env_pdf_m(C.env, L);
-        if (pL > T(0)) {
+        V3<T> L(0, 0, 1);
+        T pS = 0;
+        bool toEmit = false;
+        if (u0[0] < es) {
+            const uint32_t b = emit_pick(*C.em, (float)(u0[0] / es));
+            if (emit_sample(*C.em, b, r.pos, u1[0], u1[1], L)) { pS = es * emit_cone_pdf(*C.em, r.pos, L); toEmit = true; }
+        } else {
+            L = env_sample_dir_m(C.env, es > T(0) ? (u0[0] - es) / (T(1) - es) : u0[0], u1[0], u1[1]);
+            pS = (T(1) - es) * env_pdf_m(C.env, L);
+        }
+        if (pS > T(0)) {
             T ph = hg_eval(dot(din, L), g);
-            T w = mis_weight(pL, ph);
-            V3<T> le = C.env.radiance(L);
-            V3<T> contrib = r.beta * le * (ph * w / pL);
-            if (max3(contrib) > T(1e-7)) {
+            T w = mis_weight(pS, ph);
+            V3<T> le = toEmit ? V3<T>(1, 1, 1) : C.env.radiance(L);
+            V3<T> contrib = r.beta * le * (ph * w / pS);
+            if (max3(contrib) > (toEmit ? T(1e-9) : T(1e-7))) {
                 T R = T(C.d.env_radius);
-                T tr = C.haze.transmittance(r.pos, L, T(2) * R + length(r.pos), R);   // haze.js:472-485 hazeShadow
-                if (occlude(C, r.pos, L, r.n, st)) deposit(fr, r.pix, contrib * tr, st);
+                if (!toEmit) {
+                    T tr = C.haze.transmittance(r.pos, L, T(2) * R + length(r.pos), R);   // haze.js:472-485 hazeShadow
+                    if (occlude(C, r.pos, L, r.n, st)) deposit(fr, r.pix, contrib * tr, st);
+                } else {
+                    V3<T> hp;
+                    T hl = 0;
+                    if (!occlude(C, r.pos, L, r.n, st, &hp, &hl)) {
+                        SceneHit<T> hh = scene_eval(*C.s, hp);
+                        const st_material& me = C.s->materials[std::min(hh.m, C.s->n_materials - 1)];
+                        V3<T> ee(T(me.emissive[0]), T(me.emissive[1]), T(me.emissive[2]));
+                        if (max3(ee) > T(0)) {
+                            T tr = T(1);
+                            if (C.haze.on && std::fabs(r.n - T(1)) <= T(1e-3))
+                                tr = C.haze.transmittance(r.pos, L, std::max(hl, T(0)) / std::max(r.n, T(1e-4)), R);
+                            deposit(fr, r.pix, contrib * ee * tr, st);
+                        }
+                    }
+                }
             }
         }
     }
@@ -662,12 +689,14 @@ void medium_vertex(const Ctx<T>& C, Ray<T>& r, Rng& rng, bool last, Frame<T>& fr
     bool misOut = C.p.nee != 0 && !last;
     if (misOut) {
         T pB = hg_eval(dot(din, dout), g);
-        T pL = env_pdf_m(C.env, dout);
+        T pL = (T(1) - es) * env_pdf_m(C.env, dout);
         r.sunmis = pL <= T(0) ? T(1) : mis_weight(pB, pL);
+        const T pE = es > T(0) ? es * emit_cone_pdf(*C.em, r.pos, dout) : T(0);
+        r.emw = pE <= T(0) ? T(1) : mis_weight(pB, pE);
     } else {
         r.sunmis = T(1);
+        r.emw = T(1);
     }
-    r.emw = T(1);                                  // no emitter light sample from the air
     if (r.bounces > C.p.maxbounce) r.state = RAY_TERMINATED;
 }
 

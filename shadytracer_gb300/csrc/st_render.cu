@@ -598,26 +598,40 @@ __device__ __forceinline__ void shade_surface(const WaveArgs& a, const st_materi
 
 __device__ __forceinline__ void shade_medium(const WaveArgs& a, f3& pos, f3& dir, f3& beta, float& sunmis,
                                              uint32_t& bounces, uint32_t& state, float n, Rng& rng, bool last,
-                                             ShadowOut& sh) {
+                                             ShadowOut& sh, float& emw) {
     const Uni& u = a.u;
     state = RAY_ACTIVE;
     bounces += 1;
     float g = clampf(u.hg, -0.95f, 0.95f);
     f3 din = dir;
     beta = beta * u.halb;
+    // the discovered emitters' share of the air's light samples (haze.js:324-370), as at a surface
+    const float es = (a.em.on && u.nee != 0u && !last) ? emit_share(a.em) : 0.f;
     if (u.nee != 0u && !last) {                                       // mediumNee (haze.js:318-405)
         float4 u0 = rng.next();
         float4 u1 = rng.next();
-        f3 L = env_sample_dir_m(u, u0.x, u1.x, u1.y);
-        float pL = env_pdf_m(u, L);
-        if (pL > 0.f) {
+        f3 L = mk(0.f, 0.f, 1.f);
+        float pS = 0.f;
+        bool toEmit = false;
+        if (u0.x < es) {
+            const uint32_t b = emit_pick(a.em.dev, u0.x / es);
+            if (emit_sample(a.em.dev, b, pos, u1.x, u1.y, L)) {
+                pS = es * emit_cone_pdf(a.em.dev, pos, L);
+                toEmit = true;
+            }
+        } else {
+            L = env_sample_dir_m(u, es > 0.f ? (u0.x - es) / (1.f - es) : u0.x, u1.x, u1.y);
+            pS = (1.f - es) * env_pdf_m(u, L);
+        }
+        if (pS > 0.f) {
             float ph = hg_eval(dot(din, L), g);
-            float w = mis_weight(pL, ph);
-            f3 le = env_radiance(u, L);
-            f3 contrib = beta * le * (ph * w / pL);
-            if (max3(contrib) > 1e-7f) {
-                float tr = haze_tr(u, pos, L, 2.f * u.envR + length(pos));
-                sh.valid = true; sh.org = pos; sh.dir = L; sh.rad = contrib * tr; sh.n = n;
+            float w = mis_weight(pS, ph);
+            f3 le = toEmit ? mk(1.f) : env_radiance(u, L);
+            f3 contrib = beta * le * (ph * w / pS);
+            if (max3(contrib) > (toEmit ? 1e-9f : 1e-7f)) {
+                // an emitter's ray takes the haze from where it starts to where it stops, at its resolve
+                float tr = toEmit ? 1.f : haze_tr(u, pos, L, 2.f * u.envR + length(pos));
+                sh.valid = true; sh.emit = toEmit; sh.org = pos; sh.dir = L; sh.rad = contrib * tr; sh.n = n;
             }
         }
     }
@@ -626,10 +640,13 @@ __device__ __forceinline__ void shade_medium(const WaveArgs& a, f3& pos, f3& dir
     dir = dout;
     if (u.nee != 0u && !last) {
         float pB = hg_eval(dot(din, dout), g);
-        float pL = env_pdf_m(u, dout);
+        float pL = (1.f - es) * env_pdf_m(u, dout);
         sunmis = pL <= 0.f ? 1.f : mis_weight(pB, pL);
+        const float pE = es > 0.f ? es * emit_cone_pdf(a.em.dev, pos, dout) : 0.f;
+        emw = pE <= 0.f ? 1.f : mis_weight(pB, pE);
     } else {
         sunmis = 1.f;
+        emw = 1.f;
     }
     if (bounces > u.maxbounce) state = RAY_TERMINATED;
 }
@@ -689,8 +706,7 @@ __global__ void __launch_bounds__(256) k_shade(WaveArgs a, int nxt, int side, in
                 seg += 1;
                 m4.w = __float_as_uint(ltot);                         // absorbAlong: absLtot on arrival
                 if (state == RAY_SCATTER) {
-                    shade_medium(a, pos, dir, beta, sunmis, bounces, state, n, rng, last != 0, sh);
-                    emw = 1.f;                                        // no emitter light sample from the air
+                    shade_medium(a, pos, dir, beta, sunmis, bounces, state, n, rng, last != 0, sh, emw);
                     m4.y &= ~(3u << META_LENS_SHIFT);                 // haze.js:539: the air is no delta event
                 }
                 else

@@ -177,14 +177,17 @@ def emitter(le):
 
 
 def lamp_floor(width=96, height=64, spp=64, radius=0.1, lamp_height=1.0, le=1000.0, albedo=0.8, maxbounce=2,
-               seed=1):
+               seed=1, haze_sigma_t=0.0, haze_g=0.0):
     """An emissive sphere of `radius` and luminance `le` (cd/m^2) at `lamp_height` over an infinite Lambertian floor
     (reflectance `albedo`) in a black environment. A sphere of uniform luminance lights a point it is wholly above as a
     point source of intensity pi a^2 Le at its centre, so a floor pixel's closed form is albedo Le a^2 h / D^3, D the
-    distance to the centre (h = lamp_height); the floor cannot see itself, so any bounce cap of 1 or more keeps it."""
+    distance to the centre (h = lamp_height); the floor cannot see itself, so any bounce cap of 1 or more keeps it.
+    haze_sigma_t > 0 fills a 3 x 3 x 2 m box about the lamp with albedo-1 haze (no closed form then)."""
     s = Scene([prim(ST_PRIM_PLANE, material=1), prim(ST_PRIM_SPHERE, pos=(0.0, 0.0, lamp_height), params=(radius,),
                                                       material=2)],
-              [air(), diffuse((albedo, albedo, albedo)), emitter((le, le, le))], env_radius=20.0, name="lamp-floor")
+              [air(), diffuse((albedo, albedo, albedo)), emitter((le, le, le))], env_radius=20.0, name="lamp-floor",
+              haze=None if haze_sigma_t <= 0 else {"centre": (0.0, 0.0, 1.0), "half": (1.5, 1.5, 1.0),
+                                                   "sigma_t": haze_sigma_t, "g": haze_g, "albedo": (1.0, 1.0, 1.0)})
     # a march tolerance of 1e-4 m: a ray meets the lamp within the tolerance of its surface, so the lamp lights the
     # floor as a sphere that much larger (the scene's default, from its 20 m radius, would add 4 %)
     s.params = default_params(width=width, height=height, maxbounce=maxbounce, sun_hint=0, sun_illuminance=0.0,
