@@ -20,7 +20,7 @@ cpu_baseline: the oracle (oracle/, the CPU restatement of the reference's path) 
        bounded band of the same picture's paths.
 --impl reference: the reference's own implementation cannot run here (JavaScript + WGSL through WebGPU); its CPU
        restatement, the oracle, is timed instead on the host's cores, on the same workload and metric.
-sppm: config 3, the photon map's caustic (1024^2, 4 M sun photons a pass, 64 passes): photons/s over the photon
+sppm: the photon map's caustic (1024^2, 4 M sun photons a pass, 64 passes): photons/s over the photon
        pass's kernels, and the render's paths/s with the map on.
 time_to_rmse: seconds to 1 % relative RMSE against a closed form, the photon map guided by the learned emission map
        vs plain.
@@ -280,7 +280,7 @@ def optics_leg(args, dev, with_cpu):
 
 
 def sppm_leg(args, dev, with_cpu):
-    """Config 3, the photon map: a dispersive glass sphere on a floor under the sun, 1024 x 1024, 4 M sun photons a
+    """The photon map's caustic: a dispersive glass sphere on a floor under the sun, 1024 x 1024, 4 M sun photons a
     pass, r1 5 mm, alpha 0.7, 64 passes a render. `value`: photons/s over the photon pass's kernels (their CUDA-event
     time: generation, sort, march, surface, store); `render`: the whole render's camera paths/s with the map on."""
     import torch

@@ -102,7 +102,9 @@ typedef struct st_material {
     float attenuation;    /* attenuationDistance (m); 0 = tint at each crossing                    */
     float detector;       /* optics: > 0.5 stops and records a ray (optics/kernels.js optIsDetector)*/
     float emissive[3];    /* cd/m^2                                                               */
-    float pad;
+    float beam_cos;       /* an emitter's beam (builder/lights.js beamShape, the cone of a cosine light): > 0,
+                           * the cosine of its half angle -- the emission, emissive straight out, only within that
+                           * cone about the surface's outward normal; 0, a glowing surface, the same every way   */
 } st_material;
 
 typedef struct st_scene_desc {

@@ -455,7 +455,8 @@ inline void shade_hit(const Ctx<T>& C, Ray<T>& r, T dhit, Rng& rng, Rng& grng, b
     }
     r.bounces += 1;
     if (max3(emis) > T(0)) {                                                       // materials_pbr.js:1014-1075 emitterHit
-        r.rad += r.beta * emis * r.emw;            // weighed against the last vertex's emitter light sample
+        const T beam = m.beam_cos > 0.f ? (-dot(r.dir, n) >= T(m.beam_cos) ? T(1) : T(0)) : T(1);   // lights.js beamShape
+        r.rad += r.beta * emis * (r.emw * beam);   // weighed against the last vertex's emitter light sample
         if (C.em_on) emit_deposit(C, r.pos, emis);  // and discovered
         r.state = RAY_SOURCE;
         move_by(r, r.dir * (otol * T(2)));
@@ -542,6 +543,10 @@ inline void shade_hit(const Ctx<T>& C, Ray<T>& r, T dhit, Rng& rng, Rng& grng, b
                             SceneHit<T> hh = scene_eval(*C.s, hp);
                             const st_material& me = C.s->materials[std::min(hh.m, C.s->n_materials - 1)];
                             V3<T> ee(T(me.emissive[0]), T(me.emissive[1]), T(me.emissive[2]));
+                            if (me.beam_cos > 0.f && max3(ee) > T(0)) {                        // lights.js beamShape
+                                const V3<T> nh = hit_normal(C, hp, hh.d);
+                                if (!(-dot(L, nh) >= T(me.beam_cos))) ee = V3<T>(0, 0, 0);
+                            }
                             if (max3(ee) > T(0)) {
                                 if (air) tr = C.haze.transmittance(o, L, std::max(hl, T(0)) / std::max(r.n, T(1e-4)), R);
                                 deposit(fr, r.pix, contrib * ee * tr, st);
@@ -672,6 +677,10 @@ void medium_vertex(const Ctx<T>& C, Ray<T>& r, Rng& rng, bool last, Frame<T>& fr
                         SceneHit<T> hh = scene_eval(*C.s, hp);
                         const st_material& me = C.s->materials[std::min(hh.m, C.s->n_materials - 1)];
                         V3<T> ee(T(me.emissive[0]), T(me.emissive[1]), T(me.emissive[2]));
+                        if (me.beam_cos > 0.f && max3(ee) > T(0)) {                        // lights.js beamShape
+                            const V3<T> nh = hit_normal(C, hp, hh.d);
+                            if (!(-dot(L, nh) >= T(me.beam_cos))) ee = V3<T>(0, 0, 0);
+                        }
                         if (max3(ee) > T(0)) {
                             T tr = T(1);
                             if (C.haze.on && std::fabs(r.n - T(1)) <= T(1e-3))

@@ -132,6 +132,14 @@ __global__ void __launch_bounds__(256) k_emit_resolve(WaveArgs a) {
         const f3 le = mk(m.emissive[0], m.emissive[1], m.emissive[2]);
         if (max3(le) <= 0.f) continue;
         f3 c = xyz(r4) * le;
+        if (m.beam_cos > 0.f) {                       // a beam: the outward normal there (three differences)
+            const float eps = march_tol(p, a.u.tol);
+            const float dh = scene_dist(a.prims, a.u.n_prims, p);
+            const f3 nn = normalize(mk(scene_dist(a.prims, a.u.n_prims, mk(p.x + eps, p.y, p.z)) - dh,
+                                       scene_dist(a.prims, a.u.n_prims, mk(p.x, p.y + eps, p.z)) - dh,
+                                       scene_dist(a.prims, a.u.n_prims, mk(p.x, p.y, p.z + eps)) - dh));
+            c = c * emit_beam(m.beam_cos, -dot(xyz(d4), nn));
+        }
         const float n = fabsf(r4.w);
         if (a.u.haze_on && fabsf(n - 1.f) <= 1e-3f) {
             const float hl = fmaxf(p4.w, 0.f) / fmaxf(n, 1e-4f);

@@ -31,6 +31,12 @@ __device__ __forceinline__ void emit_deposit(const EmitBufs& em, f3 p, f3 le) {
     atomicMax(&g[6], emit_lum_code(luma(le)));
     atomicAdd(&g[7], 1u);
 }
+// an emitter's emission leaving it at cosT from its outward normal, over its luminance straight out
+// (builder/lights.js:221-228 beamShape, a cosine light, n = 1): within its beam's cone 1, else 0; a glowing surface
+// (no beam) 1 every way
+__host__ __device__ __forceinline__ float emit_beam(float beam_cos, float cosT) {
+    return beam_cos > 0.f ? (cosT >= beam_cos ? 1.f : 0.f) : 1.f;
+}
 // 1 - cos of the cone a sphere of radius r subtends at squared distance d2, as sin^2 / (1 + cos)
 __device__ __forceinline__ float cone_omc(float r, float d2) {
     const float s2 = r * r / d2;

@@ -442,7 +442,7 @@ __device__ __forceinline__ void shade_surface(const WaveArgs& a, const st_materi
     if (max3(emis) > 0.f) {                                           // emitterHit (materials_pbr.js:1014-1075)
         // weighed against the light sample the last vertex could have drawn this direction with (emw, set there),
         // and discovered: its place and brightness into the emitter grid
-        rad = rad + beta * emis * emw;
+        rad = rad + beta * emis * (emw * emit_beam(m.beam_cos, -dot(dir, nn)));
         if (a.em.on) emit_deposit(a.em, pos, emis);
         state = RAY_SOURCE;
         f3 off = dir * (otol * 2.f);

@@ -154,7 +154,7 @@ class Pcg32:
 
 
 # ---------------------------------------------------------------------------------------------------------------
-# Config 1: the photometry row (lib/pathtracer/tests.js:447-509): a white floor under a uniform environment.
+# The photometry row (lib/pathtracer/tests.js:447-509): a white floor under a uniform environment.
 # ---------------------------------------------------------------------------------------------------------------
 def floor_furnace(width=256, height=256, spp=16, albedo=0.8, sky=1000.0, maxbounce=4, seed=1):
     """An infinite Lambertian floor (reflectance `albedo`, the plane z = 0) under a uniform environment of `sky`
@@ -171,9 +171,80 @@ def floor_furnace(width=256, height=256, spp=16, albedo=0.8, sky=1000.0, maxboun
     return s
 
 
-def emitter(le):
-    """makeEmissive (core/materials.js:263-268): emitted luminance `le` (cd/m^2, rgb), air beyond."""
-    return material(base=(0, 0, 0), specular=0.0, ior=1.0, emissive=le)
+def emitter(le, beam_deg=0.0):
+    """makeEmissive (core/materials.js:263-268): emitted luminance `le` (cd/m^2, rgb), air beyond; beam_deg > 0
+    limits the emission to a cone of that half angle about the surface's outward normal (a cosine light's beam,
+    builder/lights.js beamShape)."""
+    m = material(base=(0, 0, 0), specular=0.0, ior=1.0, emissive=le)
+    m.beam_cos = math.cos(math.radians(beam_deg)) if beam_deg > 0 else 0.0
+    return m
+
+
+def spot_luminance(flux_lm, area_m2, half_deg):
+    """A face's luminance straight out for `flux_lm` lumens into a cone of `half_deg` (builder/lights.js fluxFactor, a
+    cosine light, n = 1: flux = L A pi sin^2(half))."""
+    return flux_lm / (area_m2 * math.pi * math.sin(math.radians(half_deg)) ** 2)
+
+
+def spot_rot(axis):
+    """The world -> local rotation (row major) of a thin lamp whose lower face (local -z) looks along `axis`: its rows
+    are the local axes in world coordinates, z = -axis."""
+    n = math.sqrt(sum(x * x for x in axis))
+    z = [-x / n for x in axis]
+    h = (0.0, 1.0, 0.0) if abs(z[1]) < 0.9 else (1.0, 0.0, 0.0)
+    x = [h[1] * z[2] - h[2] * z[1], h[2] * z[0] - h[0] * z[2], h[0] * z[1] - h[1] * z[0]]
+    n = math.sqrt(sum(c * c for c in x))
+    x = [c / n for c in x]
+    y = [z[1] * x[2] - z[2] * x[1], z[2] * x[0] - z[0] * x[2], z[0] * x[1] - z[1] * x[0]]
+    return tuple(x) + tuple(y) + tuple(z)
+
+
+def spot_floor(width=128, height=128, spp=64, flux=1000.0, half_deg=10.0, side=0.2, albedo=0.8, seed=1):
+    """A 10-degree spot of `flux` lumens -- a thin square lamp `side` x `side` m whose lower face emits into a cone of
+    `half_deg` about its normal -- at (-1, 0, 1) aimed at the origin, over an infinite Lambertian floor in a black
+    environment, seen straight down by an orthographic camera over 2 x 2 m about the origin. All the beam's flux lands
+    on the floor, so pi / albedo times the floor's luminance summed over its area is the flux (the lamp's other faces
+    light no floor in view). A lamp of 20 cm keeps the emitter list's first boxes -- bounds of the few points the
+    camera found on it -- from leaving most of it to the BSDF's rare hits."""
+    le = spot_luminance(flux, side * side, half_deg)
+    axis = (1.0, 0.0, -1.0)
+    lamp = prim(ST_PRIM_BOX, pos=(-1.0, 0.0, 1.0), params=(side / 2, side / 2, 0.0005), material=2,
+                rot=spot_rot(axis))
+    s = Scene([prim(ST_PRIM_PLANE, material=1), lamp],
+              [air(), diffuse((albedo, albedo, albedo)), emitter((le, le, le), beam_deg=half_deg)], env_radius=20.0,
+              name="spot-floor")
+    s.params = default_params(width=width, height=height, maxbounce=2, sun_hint=0, sun_illuminance=0.0,
+                              sky_luminance=0.0, ground_luminance=0.0, seed=seed, eps=1e-4)
+    v = StView()
+    for i, c in enumerate((0.0, 0.0, 3.0)):
+        v.cam_pos[i] = c
+    for i in range(3):
+        v.right[i] = (1.0, 0.0, 0.0)[i]
+        v.up[i] = (0.0, 1.0, 0.0)[i]
+        v.fwd[i] = (0.0, 0.0, 1.0)[i]
+    v.fx, v.fy, v.camtype = 1.0, 1.0, 1
+    s.view = v
+    s.info = {"spp": spp, "workload": "spot-floor", "flux": flux, "albedo": albedo, "pixel_area": 4.0 / (width * height)}
+    return s
+
+
+def haze_beam(width=1280, height=720, spp=256, sigma_s=0.2, g=0.7, flux=1000.0, half_deg=10.0, maxbounce=32, seed=1):
+    """The haze-box beam: a 2 x 2 x 4 m box of homogeneous haze (scattering sigma_s, absorbing nothing, HG g), crossed
+    along its length by a 10-degree spot of 1000 lm -- a 5 cm square lamp 0.5 m below the box aiming up its axis -- in a
+    black environment, seen from the side. The lamp is a thin box of one beam material: its other faces emit too, each
+    into its own 10-degree cone (the downward face into the black below, the 1 mm edges sideways)."""
+    side = 0.05
+    le = spot_luminance(flux, side * side, half_deg)
+    lamp = prim(ST_PRIM_BOX, pos=(0.0, 0.0, -0.5), params=(side / 2, side / 2, 0.0005), material=1,
+                rot=spot_rot((0.0, 0.0, 1.0)))
+    s = Scene([lamp], [air(), emitter((le, le, le), beam_deg=half_deg)], env_radius=40.0,
+              haze={"centre": (0.0, 0.0, 2.0), "half": (1.0, 1.0, 2.0), "sigma_t": sigma_s, "g": g,
+                    "albedo": (1.0, 1.0, 1.0)}, name="haze-beam")
+    s.params = default_params(width=width, height=height, maxbounce=maxbounce, sun_hint=0, sun_illuminance=0.0,
+                              sky_luminance=0.0, ground_luminance=0.0, seed=seed, eps=1e-4)
+    s.view = look_at((0.0, -7.0, 1.8), (0.0, 0.0, 1.8), 45.0, width / height)
+    s.info = {"spp": spp, "workload": "haze-beam", "paths": width * height * spp}
+    return s
 
 
 def lamp_floor(width=96, height=64, spp=64, radius=0.1, lamp_height=1.0, le=1000.0, albedo=0.8, maxbounce=2,
@@ -229,7 +300,7 @@ def lamp_floor_pixels(scene):
 
 
 # ---------------------------------------------------------------------------------------------------------------
-# Config 2: the path-traced SDF room.
+# The path-traced SDF room.
 # ---------------------------------------------------------------------------------------------------------------
 ROOM_HALF = (3.0, 2.0, 1.5)          # a 6 x 4 x 3 m room, floor at z = 0
 ROOM_WALL = 0.1
@@ -295,7 +366,7 @@ def sdf_room(width=1920, height=1080, spp=64, maxbounce=8, seed=1, n_prims=24, p
 
 
 # ---------------------------------------------------------------------------------------------------------------
-# Dispersion (spectral.js cauchyN, lightspectra.js specDraw): the glass of config 3's caustic.
+# Dispersion (spectral.js cauchyN, lightspectra.js specDraw): the glass of the photon map's caustic.
 # ---------------------------------------------------------------------------------------------------------------
 def dispersive_furnace(width=64, height=64, ior=1.5168, abbe=40.0, sky=1000.0, maxbounce=16, seed=1, floor=False):
     """A clear glass sphere (r 0.3 m) of index `ior` at the d line and Abbe number `abbe` in a uniform environment of
@@ -314,7 +385,7 @@ def dispersive_furnace(width=64, height=64, ior=1.5168, abbe=40.0, sky=1000.0, m
 
 
 # ---------------------------------------------------------------------------------------------------------------
-# Config 3: the photon map (core/sppm.js) -- a caustic under glass, and its closed form through a pane.
+# The photon map (core/sppm.js) -- a caustic under glass, and its closed form through a pane.
 # ---------------------------------------------------------------------------------------------------------------
 def cauchy_glass(a=1.50, b_um2=0.0042):
     """n(lambda) = a + b / lambda^2 (lambda in um) as the reference's materials take it: n_d and the Abbe number V_d
@@ -327,7 +398,7 @@ def cauchy_glass(a=1.50, b_um2=0.0042):
 
 def sppm_caustic(width=1024, height=1024, photons=4_000_000, r1=0.005, alpha=0.7, maxbounce=8, seed=1,
                  sun_elevation=50.0, sun_illuminance=100000.0, sky=3000.0, dispersion=True):
-    """Config 3: a glass sphere (r 0.3 m, n(lambda) = 1.50 + 0.0042 / lambda^2 um) on a diffuse floor (albedo 0.7) under
+    """The caustic: a glass sphere (r 0.3 m, n(lambda) = 1.50 + 0.0042 / lambda^2 um) on a diffuse floor (albedo 0.7) under
     the sun and a sky; the photon map on: `photons` sun photons a sample over a 0.5 m square, first radius r1, alpha."""
     nd, vd = cauchy_glass()
     mats = [air(), glass((1.0, 1.0, 1.0), ior=nd, abbe=vd if dispersion else 0.0), diffuse((0.7, 0.7, 0.7))]
@@ -379,7 +450,7 @@ def sppm_pane_closed_form(scene, fresnel):
 
 
 # ---------------------------------------------------------------------------------------------------------------
-# Config 4: the haze box (lib/pathtracer/tests.js:1818-1866 'haze' row; core/haze.js).
+# The haze box (lib/pathtracer/tests.js:1818-1866 'haze' row; core/haze.js).
 # ---------------------------------------------------------------------------------------------------------------
 def haze_furnace(width=64, height=64, sigma_t=0.2, g=0.0, albedo=1.0, sky=1000.0, maxbounce=32, seed=1):
     """The haze row's furnace: an albedo-1 haze box (2 x 2 x 4 m) in a uniform environment with nothing else in
@@ -396,7 +467,7 @@ def haze_furnace(width=64, height=64, sigma_t=0.2, g=0.0, albedo=1.0, sky=1000.0
 
 
 # ---------------------------------------------------------------------------------------------------------------
-# Config 5: the batched optics bench (optics/index.js; the reference's aspheric condenser, scenes/aspheric-condenser.json)
+# The batched optics bench (optics/index.js; the reference's aspheric condenser, scenes/aspheric-condenser.json)
 # ---------------------------------------------------------------------------------------------------------------
 MM = 1e-3
 

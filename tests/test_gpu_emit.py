@@ -102,3 +102,45 @@ def test_lamp_in_haze_matches_the_oracle():
     m0, m1 = L0.mean(), L1.mean()
     e0, e1 = np.sqrt(np.sum(se0 ** 2)) / se0.size, np.sqrt(np.sum(se1 ** 2)) / se1.size
     assert abs(m0 - m1) < 5 * np.hypot(e0, e1) + 0.01 * m0, (m0, m1, e0, e1)
+
+
+def spot_angles(s):
+    """Each pixel's floor point's angle (deg) off the spot's axis, from the centre of the lamp's lower face."""
+    W, H = s.params.width, s.params.height
+    X, Y = np.meshgrid((np.arange(W) + 0.5) / W * 2 - 1, (np.arange(H) + 0.5) / H * 2 - 1)
+    pts = np.stack([X, Y, np.zeros_like(X)], -1)
+    axis = np.array([1.0, 0.0, -1.0]) / np.sqrt(2.0)
+    d = pts - (np.array([-1.0, 0.0, 1.0]) + axis * 0.0005)
+    d /= np.linalg.norm(d, axis=-1, keepdims=True)
+    return np.degrees(np.arccos(np.clip(d @ axis, -1, 1)))
+
+
+def test_spot_floor_flux():
+    """A 10-degree spot of 1000 lm (a beam emitter: its faces emit only within 10 degrees of their normals) on a
+    Lambertian floor: pi / albedo times the floor's luminance summed over its area is the lamp's flux, to 1 %, and the
+    floor is dark outside the cone, at the BSDF's hits of the lamp and at the light sample's alike."""
+    s = scenes.spot_floor(width=128, height=128)
+    L, se, lst = render(s, 512)
+    k = s.info["pixel_area"] * np.pi / s.info["albedo"]
+    flux, err = L.sum() * k, np.sqrt(np.sum(se ** 2)) * k
+    assert abs(flux - s.info["flux"]) < max(5 * err, 0.01 * s.info["flux"]), (flux, err)
+    ang = spot_angles(s)
+    out = ang > 18.0
+    assert np.mean(L[out] == 0.0) > 0.99 and L[out].sum() < 0.005 * L.sum()
+    assert np.all(L[ang < 3.0] > 0.0)
+    assert len(lst) >= 1
+
+
+def test_spot_floor_matches_the_oracle():
+    s = scenes.spot_floor(width=48, height=48)
+    s.params.samples_per_wave = 1
+    L, se, _ = render(s, 128)
+    ref = oracle.render(s, 128)
+    sd = np.hypot(se, se_of(ref.V, ref.S))
+    ok = sd > 0
+    z = (L - ref.luma())[ok] / sd[ok]
+    assert np.mean(np.abs(z) < 4) > 0.98, np.mean(np.abs(z) < 4)
+    zm = (L - ref.luma())[ok].mean() / (np.sqrt(np.sum(sd[ok] ** 2)) / ok.sum())
+    assert abs(zm) < 5, zm
+    assert np.all(L[~ok] == 0.0) and np.all(ref.luma()[~ok] == 0.0)
+

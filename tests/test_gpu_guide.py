@@ -99,7 +99,7 @@ def test_gradient_matches_the_oracle(rt):
 
 
 def test_guided_floor_keeps_the_closed_form():
-    """Config 1's floor under the uniform sky, guided and training: every floor pixel's mean is still 800 cd/m^2."""
+    """The photometry floor under the uniform sky, guided and training: every floor pixel's mean is still 800 cd/m^2."""
     from shadytracer_gb300.renderer import create_path_tracer
     s = scenes.floor_furnace(width=128, height=128)
     s.params.guide = 1

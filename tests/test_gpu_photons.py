@@ -3,7 +3,7 @@ camera's gather; st_render.cu's lens field and the disc the map owns) against it
 
 The pane (scenes.sppm_pane): a floor lit only through a clear glass pane, seen through it; its radiance is
 T(view) rho / pi E_sun sin(elevation) T(sun), all of it the map's light (light sampling from the floor is blocked by
-the glass). The caustic (scenes.sppm_caustic, config 3 small): a dispersive glass sphere on a floor under the sun and
+the glass). The caustic (scenes.sppm_caustic, small): a dispersive glass sphere on a floor under the sun and
 a sky; the GPU's picture and the oracle's, photons and camera paths seeded alike, agree within the error bars.
 """
 import math

@@ -5,6 +5,8 @@ A Lambertian floor of albedo a under a uniform sky L reads a L wherever it is se
 sky); an albedo-1 haze box in a uniform sky reads L everywhere (what it scatters out of a ray it scatters back in).
 The microfacet albedo tables and the scene distance function are checked for their defining properties.
 """
+import math
+
 import numpy as np
 import pytest
 
@@ -99,3 +101,33 @@ def test_lamp_floor_closed_form():
     cf = scenes.lamp_floor_closed_form(s, pts)
     assert abs(L[ok].sum() / cf[ok].sum() - 1) < 0.02, L[ok].sum() / cf[ok].sum()
     assert abs(np.median(L[ok] / cf[ok]) - 1) < 0.02
+
+
+def spot_floor_points(s):
+    """The floor point under each pixel centre of the spot-floor's orthographic camera, and each point's angle (deg)
+    off the beam's axis, seen from the centre of the lamp's lower face."""
+    W, H = s.params.width, s.params.height
+    X, Y = np.meshgrid((np.arange(W) + 0.5) / W * 2 - 1, (np.arange(H) + 0.5) / H * 2 - 1)
+    pts = np.stack([X, Y, np.zeros_like(X)], -1)
+    axis = np.array([1.0, 0.0, -1.0]) / math.sqrt(2.0)
+    face = np.array([-1.0, 0.0, 1.0]) + axis * 0.0005
+    d = pts - face
+    d /= np.linalg.norm(d, axis=-1, keepdims=True)
+    return pts, np.degrees(np.arccos(np.clip(d @ axis, -1, 1)))
+
+
+def test_spot_floor_flux():
+    """A 10-degree spot of 1000 lm (a beam emitter: a thin lamp whose face emits only within 10 degrees of its normal)
+    on a Lambertian floor: pi / albedo times the floor's luminance summed over its area is the lamp's flux, and the
+    floor is dark outside the cone."""
+    s = scenes.spot_floor(width=64, height=64)
+    ref = oracle.render(s, 256)
+    L = ref.luma()
+    flux = L.sum() * s.info["pixel_area"] * math.pi / s.info["albedo"]
+    assert abs(flux / s.info["flux"] - 1) < 0.04, flux
+    # the 20 cm lamp blurs the cone's edge by about 7 degrees either way; past that only the rims of the lamp's faces,
+    # where the distance field's normal turns from one face to the next, send a little light
+    _, ang = spot_floor_points(s)
+    out = ang > 18.0
+    assert np.mean(L[out] == 0.0) > 0.99 and L[out].sum() < 0.005 * L.sum()
+    assert np.all(L[ang < 3.0] > 0.0)
