@@ -6,7 +6,7 @@ window; 1920 x 1080, 64 samples per pixel, max depth 8, march tolerance 1e-4 m, 
 the whole render -- 64 samples of every pixel, 132.7 M camera paths -- folded into the FP64 accumulation.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference] [--small] [--spp S]
-                    [--leg sppm|rmse|optics]     # one leg alone, its JSON printed (for profiling runs)
+                    [--leg sppm|rmse|optics|mlp|emit|haze]   # one leg alone, its JSON printed
 
 value: paths / s with the scene resident on the GPU (graph replays; the timed region brackets K renders with a
        synchronize). e2e: the same through the C ABI as a host calls it -- scene, settings and camera uploaded from
@@ -30,6 +30,8 @@ mlp: the learned proposal (a BF16 network guiding BSDF sampling): relative RMSE 
        on the diffuse room lit by the sun's patch; the network's inference and training flops a second.
 emit: emissive surfaces: a sphere lamp over a floor (its closed form): Mpaths/s with the discovered lamp light-sampled,
        and the relative RMSE with and without that light sample at equal samples.
+haze_beam: the haze-box beam (a 10-degree 1000 lm spot, a light face, through 2 x 2 x 4 m of albedo-1 haze;
+       1280 x 720, 256 samples, 32 bounces) at each of its nine (sigma_s, g) cells: Mpaths/s per cell and overall.
 Multi-GPU (torchrun): replicas -- each rank renders the whole workload on its own GPU; value sums the ranks' paths
        over the slowest rank's time (weak scaling). There is no data exchange in the path tracer.
 """
@@ -62,7 +64,8 @@ def parse():
     ap.add_argument("--spp", type=int, default=0, help="samples per pixel a step (profiling runs; default: 64)")
     ap.add_argument("--no-mlp", action="store_true", help="skip the learned proposal's leg")
     ap.add_argument("--no-emit", action="store_true", help="skip the emissive surfaces' leg")
-    ap.add_argument("--leg", default="all", choices=["all", "sppm", "rmse", "optics", "mlp", "emit"],
+    ap.add_argument("--no-haze", action="store_true", help="skip the haze-box beam's leg")
+    ap.add_argument("--leg", default="all", choices=["all", "sppm", "rmse", "optics", "mlp", "emit", "haze"],
                     help="run one leg alone and print its JSON (profiling runs of the photon map or the optics bench)")
     return ap.parse_args()
 
@@ -453,6 +456,43 @@ def emit_leg(args, dev):
     return out
 
 
+def haze_leg(args, dev):
+    """The haze-box beam: a 2 x 2 x 4 m box of albedo-1 haze crossed by a 10-degree, 1000 lm spot (a 5 cm light face
+    below it), 1280 x 720, 256 samples, 32 bounces, at each of the nine cells sigma_s in {0.05, 0.2, 1.0} per metre x
+    g in {0, 0.7, 0.9}: camera paths a second per cell (CUDA events around one render), and over the nine."""
+    import torch
+    from shadytracer_gb300 import scenes
+    from shadytracer_gb300.renderer import create_path_tracer
+    W, H = (320, 180) if args.small else (1280, 720)
+    spp = 16 if args.small else 256
+    out = {"workload": "haze-beam: 2x2x4 m albedo-1 haze, 10 deg 1000 lm spot (5 cm face), %dx%d, %d samples, "
+                       "32 bounces" % (W, H, spp), "metric": "Mpaths/s", "cells": {}}
+    tot_paths, tot_ms = 0, 0.0
+    for sig in (0.05, 0.2, 1.0):
+        for g in (0.0, 0.7, 0.9):
+            s = scenes.haze_beam(width=W, height=H, sigma_s=sig, g=g)
+            rt = create_path_tracer(s, device=dev)
+            stream = torch.cuda.ExternalStream(rt.stream(), device=torch.device("cuda", dev))
+            rt.step(4)                                # the wave's buffers and graphs
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            rt.invalidate()
+            e0.record(stream)
+            rt.step_async(spp)
+            e1.record(stream)
+            rt.sync()
+            ms = e0.elapsed_time(e1)
+            c = rt.counters()
+            L = rt.read_accum()[0] @ np.array([0.2126, 0.7152, 0.0722])
+            out["cells"]["sigma%g_g%g" % (sig, g)] = {
+                "ms": ms, "Mpaths_per_s": W * H * spp / (ms / 1e3) / 1e6, "mean_luminance": float(L.mean()),
+                "segments_per_path": c["segments"] / max(c["paths"], 1), "nonfinite": c["nonfinite"]}
+            tot_paths += W * H * spp
+            tot_ms += ms
+            rt.close()
+    out["value"] = tot_paths / (tot_ms / 1e3) / 1e6
+    return out
+
+
 def rmse_leg(args, dev):
     """Time to 1 % relative RMSE against the closed form, guided vs plain: the photon map's pane (a 0.5 m glass pane
     over a floor lit only through it, the sun's photons drawn over a 4 m square), plain -- the photons uniform over the
@@ -511,7 +551,7 @@ def run_ours(args):
         with_cpu = rank == 0 and world == 1 and not args.no_cpu
         out = {"sppm": lambda: sppm_leg(args, dev, with_cpu), "rmse": lambda: rmse_leg(args, dev),
                "optics": lambda: optics_leg(args, dev, with_cpu), "mlp": lambda: mlp_leg(args, dev),
-               "emit": lambda: emit_leg(args, dev)}[args.leg]()
+               "emit": lambda: emit_leg(args, dev), "haze": lambda: haze_leg(args, dev)}[args.leg]()
         if rank == 0:
             print(json.dumps(out), flush=True)
         return 0
@@ -672,6 +712,8 @@ def run_ours(args):
         line["mlp"] = mlp_leg(args, dev)
     if not args.no_emit:
         line["emit"] = emit_leg(args, dev)
+    if not args.no_haze:
+        line["haze_beam"] = haze_leg(args, dev)
     if not args.no_optics:
         line["optics"] = optics_leg(args, dev, rank == 0 and world == 1 and not args.no_cpu)
         if world > 1:

@@ -107,6 +107,31 @@ typedef struct st_material {
                            * cone about the surface's outward normal; 0, a glowing surface, the same every way   */
 } st_material;
 
+/* A LIGHT'S FACE (builder/lights.js, the builder's light object; core/scene_api.js:259-289 LightFace,
+ * lightFaceArea, lightFaceDensity): a one-sided rectangle or disc of luminance le straight out along
+ * n = u x v, in a beam (lights.js:209-228 beamOf / beamShape). The library draws it -- a sheet of its
+ * material appended to the primitives, as the builder's codegen draws a light -- and light sampling
+ * aims at a point uniform on it (materials_pbr.js:1244-1268; haze.js:324-350 from the air), half the
+ * light samples of a vertex going to the faces; a BSDF's hit of it is weighed against that density.
+ * A face is never discovered as an emitter. 80 bytes. */
+enum st_light_shape { ST_LIGHT_DISC = 1, ST_LIGHT_RECTANGLE = 2 };
+enum st_light_dist  { ST_LIGHT_COSINE = 0, ST_LIGHT_UNIFORM = 1 };
+typedef struct st_light {
+    float    centre[3];    /* metres                                                               */
+    uint32_t shape;        /* st_light_shape                                                       */
+    float    u[3];         /* the face's first axis (unit); a rectangle's width runs along it        */
+    float    half_w;       /* half the width, or the disc's radius, metres                          */
+    float    v[3];         /* the second axis (unit, at right angles to u); the face emits along u x v */
+    float    half_h;       /* half the height (a rectangle), metres                                */
+    float    le[3];        /* luminance straight out, cd/m^2 (lights.js fluxFactor: flux = le A k)   */
+    uint32_t material;     /* the face's material: what the march meets there (no emission of its own) */
+    uint32_t dist;         /* st_light_dist: cos^n intensity (radiance cos^(n-1)), or even intensity  */
+    float    n;            /* the cos^n exponent (1: Lambertian)                                    */
+    float    beam_cos;     /* the cosine of the beam's half angle (0: 90 degrees)                   */
+    uint32_t pad;
+} st_light;
+#define ST_MAX_LIGHTS 64
+
 typedef struct st_scene_desc {
     const st_prim*     prims;
     uint32_t           n_prims;        /* at most ST_MAX_PRIMS                                      */
@@ -121,6 +146,8 @@ typedef struct st_scene_desc {
     float              haze_half[3];
     float              haze_albedo[3];
     float              haze_g;         /* Henyey-Greenstein asymmetry, |g| <= 0.95                  */
+    const st_light*    lights;         /* the lights' faces, or NULL                                */
+    uint32_t           n_lights;       /* at most ST_MAX_LIGHTS; n_prims + n_lights <= ST_MAX_PRIMS */
 } st_scene_desc;
 
 #define ST_MAX_PRIMS      256
@@ -404,7 +431,7 @@ int  st_render_noalloc(int device, const st_scene_desc* desc, const st_params* p
 /* ---- the binding's checks ---- */
 /* The sizes of the structs above as this library was built (st_prim, st_material, st_scene_desc, st_params,
  * st_view, st_counters_t, st_image_stats_t, st_kernel_time, st_sppm_stats, st_optics_source, st_optics_far,
- * st_optics_batch, st_optics_totals, st_mlp_stats, in that order); returns how many it has. */
+ * st_optics_batch, st_optics_totals, st_mlp_stats, st_light, in that order); returns how many it has. */
 int  st_struct_sizes(uint32_t* out, int max);
 /* The context's CUDA stream (a cudaStream_t), for a host that orders or times its own work against it. */
 void* st_stream(st_ctx* ctx);

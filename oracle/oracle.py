@@ -14,7 +14,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "liboracle.so")
 SOURCES = ["st_oracle.cpp", "st_oracle_core.h", "st_oracle_render.h", "st_oracle_extra.h", "st_oracle_sppm.h",
-           "st_oracle_optics.h", "st_oracle_spectral.h", "st_oracle_guide.h", "../include/shadytracer.h"]
+           "st_oracle_optics.h", "st_oracle_spectral.h", "st_oracle_guide.h", "st_oracle_light.h",
+           "../include/shadytracer.h"]
 
 _lib = None
 

@@ -18,6 +18,7 @@
 #include "st_oracle_sppm.h"
 #include "st_oracle_spectral.h"
 #include "st_oracle_guide.h"
+#include "st_oracle_light.h"
 #ifdef _OPENMP
 #include <omp.h>
 #endif
@@ -83,6 +84,9 @@ template <class T> struct Ctx {
     float em_share = 0.5f, em_half = 15.f;
     const EmitList* em = nullptr;
     std::vector<std::vector<uint32_t>>* em_grids = nullptr;     // a discovery grid a thread
+    // the lights' faces and the material -> face map (its index + 1, 0 none)
+    const std::vector<OFace>* faces = nullptr;
+    uint8_t face_of[ST_MAX_MATERIALS] = {};
 };
 const uint32_t LT_G = 128, LT_N = LT_G * LT_G;
 const float LT_FLOOR_F = 0.2f;
@@ -139,6 +143,8 @@ template <class T> struct Ray {
     T ltot, n, sunmis, tmax, absLtot;
     T lam = T(0);                           // the wavelength a dispersive refraction gave it (nm, as coded), 0 none
     T emw = T(1);                           // an emitter hit's MIS weight against the last vertex's light sample
+    T lpx = T(-1), lpy = T(0);              // the last vertex's density for the direction sent (< 0: no weight
+                                            // against the faces) and ltot there (prevPdf, vtxLtot)
     uint32_t lens = 0;                      // a camera path's lens field (materials_pbr.js lensField): 1 delta only
                                             // since the eye, 2 at its D, 3 delta only since its D
     bool passed = false;                    // a photon that has passed a delta event (TAG_PASSED)
@@ -199,8 +205,8 @@ template <class T> inline T march(const Ctx<T>& C, Ray<T>& r, Stats& st, bool us
 
 // the occlusion pass (wavefront.js:1481-1692), distance only: true when the shadow ray reaches the light
 template <class T> inline bool occlude(const Ctx<T>& C, V3<T> pos, const V3<T>& dir, T n, Stats& st,
-                                      V3<T>* stop = nullptr, T* stop_ltot = nullptr) {
-    T ltot = 0;
+                                      V3<T>* stop = nullptr, T* stop_ltot = nullptr, bool face = false, T ltot0 = T(0)) {
+    T ltot = ltot0;                         // a face's ray: minus the way to it, less four offsets (TAG_FNEE)
     uint32_t steps = 0;
     bool reached = false, cut = false;
     uint64_t evals = 0;
@@ -209,6 +215,7 @@ template <class T> inline bool occlude(const Ctx<T>& C, V3<T> pos, const V3<T>& 
         evals++;
         T ea = std::fabs(h.d);
         T eps = march_tol(pos, C.tol);
+        if (face && ltot >= T(0)) { reached = true; break; }                           // at the face
         if (ea < eps) break;                                                           // blocked
         if (dot(pos, dir) > T(0) && dot(pos, pos) > C.envR2) { reached = true; break; }
         steps += 1;
@@ -454,6 +461,23 @@ inline void shade_hit(const Ctx<T>& C, Ray<T>& r, T dhit, Rng& rng, Rng& grng, b
         r.rad += r.beta * L;
     }
     r.bounces += 1;
+    const uint32_t fid = C.faces ? C.face_of[std::min(h.m, C.s->n_materials - 1)] : 0u;
+    if (fid) {                                                                     // a light's face (codegen.js:795-836)
+        const OFace& f = (*C.faces)[fid - 1];
+        const T cosY = -(r.dir.x * T(f.n[0]) + r.dir.y * T(f.n[1]) + r.dir.z * T(f.n[2]));
+        T w = T(1);
+        if (r.bounces >= 2 && r.lpx >= T(0)) {
+            const T pl = T(face_density(FACE_SHARE, C.faces->size(), f,
+                                        (double)(std::max(r.ltot - r.lpy, T(0)) / std::max(r.n, T(1e-4))), (double)cosY));
+            const T a2 = r.lpx * r.lpx;
+            w = a2 / std::max(a2 + pl * pl, T(1e-20));
+        }
+        r.rad += r.beta * V3<T>(T(f.le[0]), T(f.le[1]), T(f.le[2])) *
+                 (T(face_beam(f, (double)cosY)) / std::max(r.n * r.n, T(1)) * w);
+        r.state = RAY_SOURCE;
+        move_by(r, r.dir * (otol * T(2)));
+        return;
+    }
     if (max3(emis) > T(0)) {                                                       // materials_pbr.js:1014-1075 emitterHit
         const T beam = m.beam_cos > 0.f ? (-dot(r.dir, n) >= T(m.beam_cos) ? T(1) : T(0)) : T(1);   // lights.js beamShape
         r.rad += r.beta * emis * (r.emw * beam);   // weighed against the last vertex's emitter light sample
@@ -497,32 +521,52 @@ inline void shade_hit(const Ctx<T>& C, Ray<T>& r, T dhit, Rng& rng, Rng& grng, b
     Lobes<T> lb = make_lobes(nrm, -r.dir, m, etaFace, C.tb, trans, specv);
     lb.etaT = n0 / nT;
 
-    // LIGHT SAMPLING (materials_pbr.js:1196-1330): the discovered emitters with their share of the samples (0 while
-    // nothing is listed, when the environment's draw is what it always was), else the environment; no light faces
+    // LIGHT SAMPLING (materials_pbr.js:1196-1330): the lights' faces with their share (lightFaceShare), then of the
+    // rest the discovered emitters with theirs (0 while nothing is listed), else the environment -- with no face and
+    // nothing listed, the environment's draw is what it always was
     const T es = (C.em_on && C.em_nee && C.p.nee != 0 && !last && C.em->count > 0)
                      ? T(std::min(std::max(C.em_share, 0.05f), 0.95f)) : T(0);
+    const T fs = (C.faces && !C.faces->empty() && C.p.nee != 0 && !last) ? T(FACE_SHARE) : T(0);
+    const T rs = T(1) - fs;
     if (C.p.nee != 0 && !last) {
         T u0[4], u1[4];
         rng.next4(u0);                                                             // pick00
         rng.next4(u1);                                                             // uL
         if (!lobes_none<T>(m, trans)) {
             V3<T> L(0, 0, 1);
-            T pS = 0;
-            bool toEmit = false;
-            if (u0[0] < es) {
-                const uint32_t b = emit_pick(*C.em, (float)(u0[0] / es));
+            T pS = 0, fdist = 0;
+            bool toEmit = false, toFace = false;
+            V3<T> fle(0, 0, 0);
+            const T pick0 = (u0[0] - fs) / std::max(rs, T(1e-6));
+            if (u0[0] < fs) {                                                      // a face, a point uniform on it
+                const size_t nf = C.faces->size();
+                const OFace& f = (*C.faces)[std::min((size_t)(u0[1] * T(nf)), nf - 1)];
+                double y[3];
+                face_point(f, (double)u1[0], (double)u1[1], y);
+                const V3<T> dy = V3<T>(T(y[0]), T(y[1]), T(y[2])) - r.pos;
+                fdist = length(dy);
+                L = dy * (T(1) / std::max(fdist, T(1e-20)));
+                const T cosY = -(L.x * T(f.n[0]) + L.y * T(f.n[1]) + L.z * T(f.n[2]));
+                if (fdist > T(0) && cosY > T(1e-6)) {
+                    pS = T(face_density((double)fs, nf, f, (double)fdist, (double)cosY));
+                    fle = V3<T>(T(f.le[0]), T(f.le[1]), T(f.le[2])) *
+                          (T(face_beam(f, (double)cosY)) / std::max(r.n * r.n, T(1)));
+                    toFace = true;
+                }
+            } else if (pick0 < es) {
+                const uint32_t b = emit_pick(*C.em, (float)(pick0 / es));
                 if (emit_sample(*C.em, b, r.pos, u1[0], u1[1], L)) {
-                    pS = es * emit_cone_pdf(*C.em, r.pos, L);
+                    pS = rs * es * emit_cone_pdf(*C.em, r.pos, L);
                     toEmit = true;
                 }
             } else {
-                T pick = es > T(0) ? (u0[0] - es) / (T(1) - es) : u0[0];
+                T pick = es > T(0) ? (pick0 - es) / (T(1) - es) : pick0;
                 L = env_sample_dir(C.env, nrm, pick, u1[0], u1[1]);
-                pS = (T(1) - es) * env_pdf(C.env, L, nrm);
+                pS = rs * (T(1) - es) * env_pdf(C.env, L, nrm);
             }
             T NoL = dot(nrm, L);
             if (NoL > T(0) && pS > T(0)) {
-                V3<T> le = toEmit ? V3<T>(1, 1, 1) : C.env.radiance(L);
+                V3<T> le = toEmit ? V3<T>(1, 1, 1) : (toFace ? fle : C.env.radiance(L));
                 V3<T> f = lobes_eval(lb, L, T(0));
                 T pB = lobes_pdf(lb, L);
                 T w = mis_weight(pS, pB);
@@ -532,7 +576,12 @@ inline void shade_hit(const Ctx<T>& C, Ray<T>& r, T dhit, Rng& rng, Rng& grng, b
                     T tr = T(1);
                     const bool air = C.haze.on && std::fabs(r.n - T(1)) <= T(1e-3);
                     T R = T(C.d.env_radius);
-                    if (!toEmit) {
+                    if (toFace) {
+                        // the face's ray aims at the point and arrives just short of it (TAG_FNEE)
+                        if (air) tr = C.haze.transmittance(r.pos, L, fdist, R);
+                        const T l0 = -std::max(fdist - T(40) * march_tol(o, C.tol), T(0)) * r.n;
+                        if (occlude(C, o, L, r.n, st, (V3<T>*)nullptr, (T*)nullptr, true, l0)) deposit(fr, r.pix, contrib * tr, st);
+                    } else if (!toEmit) {
                         if (air) tr = C.haze.transmittance(r.pos, L, T(2) * R + length(r.pos), R);   // haze.js:472-485
                         if (occlude(C, o, L, r.n, st)) deposit(fr, r.pix, contrib * tr, st);
                     } else {
@@ -572,14 +621,17 @@ inline void shade_hit(const Ctx<T>& C, Ray<T>& r, T dhit, Rng& rng, Rng& grng, b
     if (misOut) {                                                                  // materials_pbr.js:1370-1395
         bool above = dot(nrm, r.dir) > T(0) && !smp.isDelta;
         T pOut = smp.isDelta ? T(0) : lobes_pdf(lb, smp.dir);
-        T pLout = above ? (T(1) - es) * env_pdf(C.env, r.dir, nrm) : T(0);
+        T pLout = above ? rs * (T(1) - es) * env_pdf(C.env, r.dir, nrm) : T(0);
         r.sunmis = pLout <= T(0) ? T(1) : mis_weight(pOut, pLout);
-        const T pEout = (above && es > T(0)) ? es * emit_cone_pdf(*C.em, r.pos, r.dir) : T(0);
+        const T pEout = (above && es > T(0)) ? rs * es * emit_cone_pdf(*C.em, r.pos, r.dir) : T(0);
         r.emw = pEout <= T(0) ? T(1) : mis_weight(pOut, pEout);
+        r.lpx = (above && fs > T(0) && !lobes_none<T>(m, trans)) ? pOut : T(-1);   // prevPdf, for a face it meets
     } else {
         r.sunmis = T(1);
         r.emw = T(1);
+        r.lpx = T(-1);
     }
+    r.lpy = r.ltot;                                                                // vtxLtot
     move_by(r, r.dir * otol);
     // pathEnd's tail (tracebasics.js:1040-1103): the bounce cap, Russian roulette
     if (r.bounces > C.p.maxbounce) r.state = RAY_TERMINATED;
@@ -647,27 +699,49 @@ void medium_vertex(const Ctx<T>& C, Ray<T>& r, Rng& rng, bool last, Frame<T>& fr
     // the discovered emitters' share of the air's light samples (haze.js:324-370), as at a surface
     const T es = (C.em_on && C.em_nee && C.p.nee != 0 && !last && C.em->count > 0)
                      ? T(std::min(std::max(C.em_share, 0.05f), 0.95f)) : T(0);
+    const T fs = (C.faces && !C.faces->empty() && C.p.nee != 0 && !last) ? T(FACE_SHARE) : T(0);   // haze.js:315-350
+    const T rs = T(1) - fs;
     if (C.p.nee != 0 && !last) {
         T u0[4], u1[4];
         rng.next4(u0); rng.next4(u1);
         V3<T> L(0, 0, 1);
-        T pS = 0;
-        bool toEmit = false;
-        if (u0[0] < es) {
-            const uint32_t b = emit_pick(*C.em, (float)(u0[0] / es));
-            if (emit_sample(*C.em, b, r.pos, u1[0], u1[1], L)) { pS = es * emit_cone_pdf(*C.em, r.pos, L); toEmit = true; }
+        T pS = 0, fdist = 0;
+        bool toEmit = false, toFace = false;
+        V3<T> fle(0, 0, 0);
+        const T pick0 = (u0[0] - fs) / std::max(rs, T(1e-6));
+        if (u0[0] < fs) {                                      // a face: no vertex normal, the face's own side
+            const size_t nf = C.faces->size();
+            const OFace& f = (*C.faces)[std::min((size_t)(u0[1] * T(nf)), nf - 1)];
+            double y[3];
+            face_point(f, (double)u1[0], (double)u1[1], y);
+            const V3<T> dy = V3<T>(T(y[0]), T(y[1]), T(y[2])) - r.pos;
+            fdist = length(dy);
+            L = dy * (T(1) / std::max(fdist, T(1e-20)));
+            const T cosY = -(L.x * T(f.n[0]) + L.y * T(f.n[1]) + L.z * T(f.n[2]));
+            if (fdist > T(0) && cosY > T(1e-6)) {
+                pS = T(face_density((double)fs, nf, f, (double)fdist, (double)cosY));
+                fle = V3<T>(T(f.le[0]), T(f.le[1]), T(f.le[2])) * T(face_beam(f, (double)cosY));   // in air
+                toFace = true;
+            }
+        } else if (pick0 < es) {
+            const uint32_t b = emit_pick(*C.em, (float)(pick0 / es));
+            if (emit_sample(*C.em, b, r.pos, u1[0], u1[1], L)) { pS = rs * es * emit_cone_pdf(*C.em, r.pos, L); toEmit = true; }
         } else {
-            L = env_sample_dir_m(C.env, es > T(0) ? (u0[0] - es) / (T(1) - es) : u0[0], u1[0], u1[1]);
-            pS = (T(1) - es) * env_pdf_m(C.env, L);
+            L = env_sample_dir_m(C.env, es > T(0) ? (pick0 - es) / (T(1) - es) : pick0, u1[0], u1[1]);
+            pS = rs * (T(1) - es) * env_pdf_m(C.env, L);
         }
         if (pS > T(0)) {
             T ph = hg_eval(dot(din, L), g);
             T w = mis_weight(pS, ph);
-            V3<T> le = toEmit ? V3<T>(1, 1, 1) : C.env.radiance(L);
+            V3<T> le = toEmit ? V3<T>(1, 1, 1) : (toFace ? fle : C.env.radiance(L));
             V3<T> contrib = r.beta * le * (ph * w / pS);
             if (max3(contrib) > (toEmit ? T(1e-9) : T(1e-7))) {
                 T R = T(C.d.env_radius);
-                if (!toEmit) {
+                if (toFace) {
+                    T tr = C.haze.transmittance(r.pos, L, fdist, R);
+                    const T l0 = -std::max(fdist - T(40) * march_tol(r.pos, C.tol), T(0)) * r.n;
+                    if (occlude(C, r.pos, L, r.n, st, (V3<T>*)nullptr, (T*)nullptr, true, l0)) deposit(fr, r.pix, contrib * tr, st);
+                } else if (!toEmit) {
                     T tr = C.haze.transmittance(r.pos, L, T(2) * R + length(r.pos), R);   // haze.js:472-485 hazeShadow
                     if (occlude(C, r.pos, L, r.n, st)) deposit(fr, r.pix, contrib * tr, st);
                 } else {
@@ -698,14 +772,17 @@ void medium_vertex(const Ctx<T>& C, Ray<T>& r, Rng& rng, bool last, Frame<T>& fr
     bool misOut = C.p.nee != 0 && !last;
     if (misOut) {
         T pB = hg_eval(dot(din, dout), g);
-        T pL = (T(1) - es) * env_pdf_m(C.env, dout);
+        T pL = rs * (T(1) - es) * env_pdf_m(C.env, dout);
         r.sunmis = pL <= T(0) ? T(1) : mis_weight(pB, pL);
-        const T pE = es > T(0) ? es * emit_cone_pdf(*C.em, r.pos, dout) : T(0);
+        const T pE = es > T(0) ? rs * es * emit_cone_pdf(*C.em, r.pos, dout) : T(0);
         r.emw = pE <= T(0) ? T(1) : mis_weight(pB, pE);
+        r.lpx = fs > T(0) ? pB : T(-1);
     } else {
         r.sunmis = T(1);
         r.emw = T(1);
+        r.lpx = T(-1);
     }
+    r.lpy = r.ltot;
     if (r.bounces > C.p.maxbounce) r.state = RAY_TERMINATED;
 }
 
@@ -1056,7 +1133,19 @@ template <class T>
 static int render_impl(const st_scene_desc* s, const st_params* p, const st_view* v, uint32_t sample0,
                        uint32_t nsamples, double* acc_rgb, double* mV, double* mS, uint32_t* acc_cnt,
                        uint64_t* counters, int threads, uint32_t path_first, uint32_t path_count) {
+    // the lights' faces, drawn as sheets appended to the primitives (the scene the rest of the oracle sees)
+    std::vector<st_prim> prims_x(s->prims, s->prims + s->n_prims);
+    std::vector<OFace> faces;
+    st_scene_desc sx = *s;
     Ctx<T> C;
+    {
+        std::string why;
+        if (!build_faces(*s, prims_x, faces, C.face_of, why)) return -1;
+        sx.prims = prims_x.data();
+        sx.n_prims = (uint32_t)prims_x.size();
+        if (!faces.empty()) C.faces = &faces;
+        s = &sx;
+    }
     C.s = s; C.p = *p; C.d = derive(*p, *s);
     C.env.init(*p, C.d);
     C.tb = tables<T>();

@@ -57,7 +57,7 @@ SIGNATURES = {
 
 STRUCT_ORDER = [T.StPrim, T.StMaterial, T.StSceneDesc, T.StParams, T.StView, T.StCounters, T.StImageStats,
                 T.StKernelTime, T.StSppmStats, T.StOpticsSource, T.StOpticsFar, T.StOpticsBatch, T.StOpticsTotals,
-                T.StMlpStats]
+                T.StMlpStats, T.StLight]
 
 
 def load(path=None):

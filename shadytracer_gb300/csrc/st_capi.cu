@@ -41,6 +41,8 @@ struct st_ctx {
     st_scene_desc desc{};
     bool has_scene = false, has_params = false, has_view = false;
     DPrim* d_prims = nullptr;
+    float4* d_faces = nullptr;            // the lights' faces (FACE_F4 float4s each), then the material -> face map
+    uint32_t n_faces = 0;
     st_material* d_mats = nullptr;
     st_params params{};
     st_view view{};
@@ -92,7 +94,8 @@ static int cuda_fail(st_ctx* c, cudaError_t e, const char* what) {
     } while (0)
 
 static void free_wave(st_ctx* ctx) {
-    void* ptrs[] = {ctx->pb.pos, ctx->pb.dir, ctx->pb.beta, ctx->pb.rad, ctx->pb.meta, ctx->pb.lam, ctx->q.ray[0], ctx->q.ray[1],
+    void* ptrs[] = {ctx->pb.pos, ctx->pb.dir, ctx->pb.beta, ctx->pb.rad, ctx->pb.meta, ctx->pb.lam, ctx->pb.lprev,
+                    ctx->q.ray[0], ctx->q.ray[1],
                     ctx->q.hit, ctx->q.hitd, ctx->q.hsurf, ctx->q.sorted, ctx->q.skey, ctx->q.srank, ctx->q.bcnt,
                     ctx->q.boff, ctx->q.ssorted, ctx->q.sskey, ctx->q.ssrank, ctx->q.s_org[0], ctx->q.s_dir[0], ctx->q.s_rad[0], ctx->q.s_steps[0],
                     ctx->q.s_org[1], ctx->q.s_dir[1], ctx->q.s_rad[1], ctx->q.s_steps[1], ctx->d_frame,
@@ -218,6 +221,59 @@ static Uni make_uni(const st_ctx* ctx) {
 // distance is nearer -- and a prism's edge constants (shapes.js:266-283), in double here. +inf where the distance is
 // not an exact one (the aspheric lens's is a bound, shapes.js:621-640) or the shape is unbounded (the plane).
 // ------------------------------------------------------------------------------------------------------------
+// THE LIGHTS' FACES (builder/lights.js; codegen.js:861-912 emitLightFaces): each checked, its frame made orthonormal
+// (u, v at right angles, n = u x v), drawn as a sheet of its material appended to the primitives (a rectangle a box
+// of no thickness, a disc a cylinder of none) and packed for the device, with the map from its material to it
+static bool light_faces(const st_scene_desc* d, std::vector<st_prim>& prims, std::vector<float4>& out,
+                        std::string& why) {
+    const uint32_t nl = d->lights ? d->n_lights : 0u;
+    if (nl > ST_MAX_LIGHTS) { why = "n_lights out of range (0..64)"; return false; }
+    if (prims.size() + nl > ST_MAX_PRIMS) { why = "n_prims + n_lights above 256"; return false; }
+    uint8_t* of = reinterpret_cast<uint8_t*>(out.data() + ST_MAX_LIGHTS * FACE_F4);
+    for (uint32_t i = 0; i < nl; i++) {
+        const st_light& L = d->lights[i];
+        const std::string at = "light " + std::to_string(i) + ": ";
+        if (L.shape != ST_LIGHT_DISC && L.shape != ST_LIGHT_RECTANGLE) { why = at + "unknown shape"; return false; }
+        if (L.material == 0 || L.material >= d->n_materials) { why = at + "material out of range (1..n_materials-1)"; return false; }
+        if (of[L.material]) { why = at + "its material draws another light (one material a light)"; return false; }
+        if (!(L.half_w > 0.f) || (L.shape == ST_LIGHT_RECTANGLE && !(L.half_h > 0.f))) { why = at + "no size"; return false; }
+        if (!(L.beam_cos >= 0.f && L.beam_cos < 1.f) || !(L.n >= 0.f) || L.dist > ST_LIGHT_UNIFORM) {
+            why = at + "beam out of range"; return false;
+        }
+        if (!(L.le[0] >= 0.f && L.le[1] >= 0.f && L.le[2] >= 0.f)) { why = at + "negative luminance"; return false; }
+        double u[3] = {L.u[0], L.u[1], L.u[2]}, v[3] = {L.v[0], L.v[1], L.v[2]};
+        const double lu = std::sqrt(u[0] * u[0] + u[1] * u[1] + u[2] * u[2]);
+        if (!(lu > 1e-12)) { why = at + "no u axis"; return false; }
+        for (double& c : u) c /= lu;
+        const double uv = u[0] * v[0] + u[1] * v[1] + u[2] * v[2];
+        for (int k = 0; k < 3; k++) v[k] -= uv * u[k];
+        const double lv = std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+        if (!(lv > 1e-12)) { why = at + "v along u"; return false; }
+        for (double& c : v) c /= lv;
+        const double n[3] = {u[1] * v[2] - u[2] * v[1], u[2] * v[0] - u[0] * v[2], u[0] * v[1] - u[1] * v[0]};
+        const float hh = L.shape == ST_LIGHT_DISC ? L.half_w : L.half_h;
+        float4* f = out.data() + (size_t)i * FACE_F4;
+        f[0] = make_float4(L.centre[0], L.centre[1], L.centre[2], L.half_w);
+        f[1] = make_float4((float)u[0], (float)u[1], (float)u[2], hh);
+        f[2] = make_float4((float)v[0], (float)v[1], (float)v[2], (float)L.shape);
+        f[3] = make_float4((float)n[0], (float)n[1], (float)n[2], L.beam_cos);
+        f[4] = make_float4(L.le[0], L.le[1], L.le[2], L.dist == ST_LIGHT_UNIFORM ? -1.f : L.n);
+        of[L.material] = (uint8_t)(i + 1);
+        st_prim p{};
+        p.type = L.shape == ST_LIGHT_DISC ? ST_PRIM_CYLINDER : ST_PRIM_BOX;
+        p.op = ST_OP_ITEM;
+        p.material = L.material;
+        for (int k = 0; k < 3; k++) {
+            p.pos[k] = L.centre[k];
+            p.rot[k] = (float)u[k]; p.rot[3 + k] = (float)v[k]; p.rot[6 + k] = (float)n[k];   // world -> local rows
+        }
+        if (L.shape == ST_LIGHT_DISC) { p.p[0] = 0.f; p.p[1] = L.half_w; }
+        else { p.p[0] = L.half_w; p.p[1] = L.half_h; p.p[2] = 0.f; }
+        prims.push_back(p);
+    }
+    return true;
+}
+
 static DPrim pack_prim(const st_prim& p) {
     DPrim d{};
     const float* q = p.p;
@@ -298,6 +354,7 @@ static int ensure_wave(st_ctx* ctx) {
     CK(cudaMalloc(&ctx->pb.rad, S * sizeof(float4)), "cudaMalloc path state");
     CK(cudaMalloc(&ctx->pb.meta, S * sizeof(uint4)), "cudaMalloc path state");
     CK(cudaMalloc(&ctx->pb.lam, S * sizeof(float)), "cudaMalloc path state");
+    CK(cudaMalloc(&ctx->pb.lprev, S * sizeof(float2)), "cudaMalloc path state");
     CK(cudaMalloc(&ctx->q.ray[0], S * 4), "cudaMalloc queues");
     CK(cudaMalloc(&ctx->q.ray[1], S * 4), "cudaMalloc queues");
     CK(cudaMalloc(&ctx->q.hit, S * 4), "cudaMalloc queues");
@@ -379,6 +436,11 @@ static WaveArgs wave_args(st_ctx* ctx, uint32_t w) {
         const float half = std::max(std::min(std::max(set, 1e-3f), a.u.envR), 1e-6f);
         a.em = emit_bufs(ctx, (!ctx->params.emit_off && a.u.nee) ? 1u : 0u,
                          ctx->params.emit_share > 0.f ? ctx->params.emit_share : 0.5f, half);
+    }
+    if (ctx->n_faces) {
+        a.lf.face = ctx->d_faces;
+        a.lf.of = reinterpret_cast<const uint8_t*>(ctx->d_faces + ST_MAX_LIGHTS * FACE_F4);
+        a.lf.n = ctx->n_faces;
     }
     return a;
 }
@@ -574,7 +636,7 @@ int st_destroy(st_ctx* ctx) {
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     free_wave(ctx);
     ext_free(ctx->ext);
-    for (void* p : {(void*)ctx->d_prims, (void*)ctx->d_mats, (void*)ctx->d_ec, (void*)ctx->d_ecavg,
+    for (void* p : {(void*)ctx->d_prims, (void*)ctx->d_faces, (void*)ctx->d_mats, (void*)ctx->d_ec, (void*)ctx->d_ecavg,
                     (void*)ctx->d_e1, (void*)ctx->d_ctr, (void*)ctx->d_spec})
         if (p) cudaFree(p);
     for (auto& pe : ctx->pending) { cudaEventDestroy(pe.a); cudaEventDestroy(pe.b); }
@@ -603,15 +665,21 @@ int st_set_scene(st_ctx* ctx, const char* cuda_src, const st_scene_desc* d, char
             return refuse(ST_ERR_ARG, "primitive " + std::to_string(i) + ": material out of range");
     }
     if (!(d->env_radius >= 0) || !(d->tolerance >= 0)) return refuse(ST_ERR_ARG, "negative radius or tolerance");
-    cudaSetDevice(ctx->device);
     std::vector<st_prim> prims(d->prims, d->prims + d->n_prims);
     std::vector<st_material> mats(d->materials, d->materials + d->n_materials);
+    std::vector<float4> faces(ST_MAX_LIGHTS * FACE_F4 + ST_MAX_MATERIALS / 16, make_float4(0.f, 0.f, 0.f, 0.f));
+    {
+        std::string why;
+        if (!light_faces(d, prims, faces, why)) return refuse(ST_ERR_ARG, why);
+    }
+    cudaSetDevice(ctx->device);
     if (prims.size() > ctx->prims.size() || !ctx->d_prims) {
         if (ctx->d_prims) cudaFree(ctx->d_prims);
         ctx->d_prims = nullptr;
         CK(cudaMalloc(&ctx->d_prims, ST_MAX_PRIMS * sizeof(DPrim)), "cudaMalloc scene");
     }
     if (!ctx->d_mats) CK(cudaMalloc(&ctx->d_mats, ST_MAX_MATERIALS * sizeof(st_material)), "cudaMalloc materials");
+    if (!ctx->d_faces) CK(cudaMalloc(&ctx->d_faces, faces.size() * sizeof(float4)), "cudaMalloc light faces");
     std::vector<DPrim> packed(prims.size());
     for (size_t i = 0; i < prims.size(); i++) packed[i] = pack_prim(prims[i]);
     {
@@ -632,12 +700,15 @@ int st_set_scene(st_ctx* ctx, const char* cuda_src, const st_scene_desc* d, char
     }
     CK(cudaMemcpyAsync(ctx->d_prims, packed.data(), packed.size() * sizeof(DPrim), cudaMemcpyHostToDevice, ctx->stream), "scene upload");
     CK(cudaMemcpyAsync(ctx->d_mats, mats.data(), mats.size() * sizeof(st_material), cudaMemcpyHostToDevice, ctx->stream), "scene upload");
+    CK(cudaMemcpyAsync(ctx->d_faces, faces.data(), faces.size() * sizeof(float4), cudaMemcpyHostToDevice, ctx->stream), "scene upload");
+    ctx->n_faces = d->lights ? d->n_lights : 0u;
     CK(cudaStreamSynchronize(ctx->stream), "scene upload");
     ctx->prims = std::move(prims);
     ctx->mats = std::move(mats);
     ctx->desc = *d;
     ctx->desc.prims = nullptr;
     ctx->desc.materials = nullptr;
+    ctx->desc.lights = nullptr;
     ctx->has_scene = true;
     invalidate_graph(ctx);
     return st_invalidate(ctx);
@@ -875,7 +946,8 @@ int st_struct_sizes(uint32_t* out, int max) {
                           (uint32_t)sizeof(st_image_stats_t), (uint32_t)sizeof(st_kernel_time),
                           (uint32_t)sizeof(st_sppm_stats), (uint32_t)sizeof(st_optics_source),
                           (uint32_t)sizeof(st_optics_far), (uint32_t)sizeof(st_optics_batch),
-                          (uint32_t)sizeof(st_optics_totals), (uint32_t)sizeof(st_mlp_stats)};
+                          (uint32_t)sizeof(st_optics_totals), (uint32_t)sizeof(st_mlp_stats),
+                          (uint32_t)sizeof(st_light)};
     int n = (int)(sizeof(s) / sizeof(s[0]));
     for (int i = 0; i < n && i < max; i++) out[i] = s[i];
     return n;

@@ -48,6 +48,8 @@ struct PathBuf {
     float4* rad;    // xyz radiance collected, w tmax (the haze's collision, as ltot)
     uint4* meta;    // x pix, y bounces | segment << 8 | state << 16, z march steps over the path, w absLtot (f32)
     float* lam = nullptr;   // the wavelength a dispersive refraction gave the path (nm, as coded), 0 none
+    float2* lprev = nullptr;  // x: the last vertex's density for the direction it sent the path on, the light
+                              // faces' share folded in (< 0: no weight against them); y: ltot at that vertex
 };
 // THE QUEUES: indices into the path state, appended with one atomic per warp (ballot + popc)
 struct Queues {
@@ -146,6 +148,16 @@ struct GuideBufs {
 #define EMIT_MAX 64u
 #define EMIT_EPOCH 2u
 #define SHADOW_EMIT 0x80000000u           // a shadow side's steps word: the ray aims at an emitter (TAG_EMIT)
+#define SHADOW_FACE 0x40000000u           // ...at a point of a light's face (TAG_FNEE): it arrives when ltot,
+                                          // started at minus the way there, reaches 0
+#define SHADOW_FLAGS (SHADOW_EMIT | SHADOW_FACE)
+// THE LIGHTS' FACES (st_light.cuh): FACE_F4 float4s a face, then a byte a material (its face + 1, 0 none)
+#define FACE_F4 5
+struct LightBufs {
+    const float4* face = nullptr;         // centre|half_w, u|half_h, v|shape, n|beam_cos, le|(n, or -1 even)
+    const uint8_t* of = nullptr;          // ST_MAX_MATERIALS: the face a material draws, plus 1
+    uint32_t n = 0;                       // faces; 0, none (the light samples go as they always went)
+};
 struct EmitDev {
     uint32_t count, last, pad0, pad1;     // boxes listed; the sample the list was last built before
     float4 box[EMIT_MAX];                 // centre, radius: each box's bounding sphere
@@ -182,6 +194,7 @@ struct WaveArgs {
                                          // table, the instance in meta.w; null for a picture
     GuideBufs gd;                         // the learned proposal, while it runs
     EmitBufs em;                          // the emitter list, in a scene with emitters
+    LightBufs lf;                         // the lights' faces
 };
 
 // launch wrappers (st_render.cu)

@@ -166,6 +166,10 @@ extern "C" int st_render_noalloc(int device, const st_scene_desc* desc, const st
                      p->width, p->height, ST_NOALLOC_MAX_PIXELS);
         return ST_ERR_ARG;
     }
+    if (desc->lights && desc->n_lights) {
+        std::fprintf(stderr, "st_render_noalloc: a scene with light faces takes the context path (st_set_scene)\n");
+        return ST_ERR_ARG;
+    }
     if (desc->n_prims == 0 || desc->n_prims > ST_MAX_PRIMS || desc->n_materials == 0 ||
         desc->n_materials > ST_MAX_MATERIALS || desc->prims[0].op != ST_OP_ITEM)
         return ST_ERR_ARG;

@@ -16,6 +16,7 @@
 // shared memory by one bulk copy (cp.async.bulk + mbarrier) per CTA and read as broadcasts. Nothing is read back
 // by the host inside a sample: every kernel sizes itself from the device counters.
 #include "st_emit.cuh"
+#include "st_light.cuh"
 #include "st_guide.cuh"
 #include "st_kernels.cuh"
 
@@ -416,14 +417,14 @@ __global__ void __launch_bounds__(256, 3) k_surface(WaveArgs a) {
     }
 }
 
-struct ShadowOut { bool valid, emit; f3 org, dir, rad; float n; };
+struct ShadowOut { bool valid, emit, face; f3 org, dir, rad; float n, dist; };
 
 template <bool GUIDE>
 __device__ __forceinline__ void shade_surface(const WaveArgs& a, const st_material* sm, float4 surf,
                                               f3& pos, f3& dir, float& ltot, float& n, f3& beta, float& sunmis,
                                               f3& rad, uint32_t& bounces, uint32_t& state, float& lam,
                                               uint32_t& lens, float dh, Rng& rng, bool last, ShadowOut& sh,
-                                              uint32_t q, uint32_t& my, uint32_t gpix, float& emw) {
+                                              uint32_t q, uint32_t& my, uint32_t gpix, float& emw, float2& lp) {
     const Uni& u = a.u;
     float eps = march_tol(pos, u.tol);
     const uint32_t ids = __float_as_uint(surf.w);
@@ -438,6 +439,24 @@ __device__ __forceinline__ void shade_surface(const WaveArgs& a, const st_materi
     }
     bounces += 1;
     const st_material& m = sm[ids & 0xffffu];
+    const uint32_t fid = a.lf.n ? (uint32_t)a.lf.of[ids & 0xffu] : 0u;
+    if (fid) {                                                        // a light's face (codegen LIGHTS)
+        // its luminance at this angle from its own normal over n^2 of the medium met in, weighed past the first
+        // surface against the faces' light sample the last vertex could have drawn this point with (:826-834)
+        const Face f = face_at(a.lf, fid - 1u);
+        const float cosY = -dot(dir, f.n);
+        float w = 1.f;
+        if (bounces >= 2u && lp.x >= 0.f) {
+            const float pl = face_density(FACE_SHARE, a.lf.n, f, fmaxf(ltot - lp.y, 0.f) / fmaxf(n, 1e-4f), cosY);
+            const float a2 = lp.x * lp.x;
+            w = a2 / fmaxf(a2 + pl * pl, 1e-20f);
+        }
+        rad = rad + beta * f.le * (face_beam(f, cosY) / fmaxf(n * n, 1.f) * w);
+        state = RAY_SOURCE;
+        f3 off = dir * (otol * 2.f);
+        pos = pos + off; ltot += length(off) * n;
+        return;
+    }
     f3 emis = mk(m.emissive[0], m.emissive[1], m.emissive[2]);
     if (max3(emis) > 0.f) {                                           // emitterHit (materials_pbr.js:1014-1075)
         // weighed against the light sample the last vertex could have drawn this direction with (emw, set there),
@@ -491,27 +510,43 @@ __device__ __forceinline__ void shade_surface(const WaveArgs& a, const st_materi
     // the discovered emitters' share of the light samples (materials_pbr.js:1216-1330): 0 while nothing is listed,
     // when the environment's draw is the one it always was
     const float es = (a.em.on && u.nee != 0u && !last) ? emit_share(a.em) : 0.f;
+    // ...and before them the lights' faces' (lightFaceShare): half the samples when there are faces
+    const float fs = (a.lf.n && u.nee != 0u && !last) ? FACE_SHARE : 0.f;
+    const float rs = 1.f - fs;                                        // the rest's: emitters, then the environment
     if (u.nee != 0u && !last) {                                       // light sampling (materials_pbr.js:1196-1330)
         float4 u0 = rng.next();
         float4 u1 = rng.next();
         if (!lobes_none(m, trans)) {
             f3 L = mk(0.f, 0.f, 1.f);
-            float pS = 0.f;
-            bool toEmit = false;
-            if (u0.x < es) {                                          // an emitter: a box, a direction into its cone
-                const uint32_t b = emit_pick(a.em.dev, u0.x / es);
+            float pS = 0.f, fdist = 0.f;
+            bool toEmit = false, toFace = false;
+            f3 fle = mk(0.f);
+            const float pick0 = (u0.x - fs) / fmaxf(rs, 1e-6f);      // the rest's own draw, when it is theirs
+            if (u0.x < fs) {                                          // a face: one of them, a point uniform on it
+                const Face f = face_at(a.lf, min((uint32_t)(u0.y * (float)a.lf.n), a.lf.n - 1u));
+                const f3 dy = face_point(f, u1.x, u1.y) - pos;
+                fdist = length(dy);
+                L = dy * (1.f / fmaxf(fdist, 1e-20f));
+                const float cosY = -dot(f.n, L);
+                if (fdist > 0.f && cosY > 1e-6f) {
+                    pS = face_density(fs, a.lf.n, f, fdist, cosY);
+                    fle = f.le * (face_beam(f, cosY) / fmaxf(n * n, 1.f));
+                    toFace = true;
+                }
+            } else if (pick0 < es) {                                  // an emitter: a box, a direction into its cone
+                const uint32_t b = emit_pick(a.em.dev, pick0 / es);
                 if (emit_sample(a.em.dev, b, pos, u1.x, u1.y, L)) {
-                    pS = es * emit_cone_pdf(a.em.dev, pos, L);        // the whole mixture's density, not the box's
+                    pS = rs * es * emit_cone_pdf(a.em.dev, pos, L);   // the whole mixture's density, not the box's
                     toEmit = true;
                 }
             } else {                                                  // the environment: sun disc or sky
-                L = env_sample_dir(u, nrm, es > 0.f ? (u0.x - es) / (1.f - es) : u0.x, u1.x, u1.y);
-                pS = (1.f - es) * env_pdf(u, L, nrm);
+                L = env_sample_dir(u, nrm, es > 0.f ? (pick0 - es) / (1.f - es) : pick0, u1.x, u1.y);
+                pS = rs * (1.f - es) * env_pdf(u, L, nrm);
             }
             float NoL = dot(nrm, L);
             if (NoL > 0.f && pS > 0.f) {
                 // an emitter's radiance is the occlusion pass's to multiply in, where its ray stops
-                f3 le = toEmit ? mk(1.f) : env_radiance(u, L);
+                f3 le = toEmit ? mk(1.f) : (toFace ? fle : env_radiance(u, L));
                 f3 f = lobes_eval(lb, a.tab, L, 0.f);
                 float pB = lobes_pdf(lb, L);
                 if (guided) pB = galpha * guide_pdf(gmix, L) + (1.f - galpha) * pB;
@@ -520,9 +555,11 @@ __device__ __forceinline__ void shade_surface(const WaveArgs& a, const st_materi
                 if (max3(contrib) > (toEmit ? 1e-9f : 1e-7f)) {
                     float tr = 1.f;
                     if (!toEmit && u.haze_on && fabsf(n - 1.f) <= 1e-3f)
-                        tr = haze_tr(u, pos, L, 2.f * u.envR + length(pos));
+                        tr = haze_tr(u, pos, L, toFace ? fdist : 2.f * u.envR + length(pos));
                     sh.valid = true;
                     sh.emit = toEmit;
+                    sh.face = toFace;
+                    sh.dist = fdist;
                     sh.org = pos + nrm * (otol * 2.f);
                     sh.dir = L;
                     sh.rad = contrib * tr;
@@ -576,14 +613,17 @@ __device__ __forceinline__ void shade_surface(const WaveArgs& a, const st_materi
     if (u.nee != 0u && !last) {                                       // the other half of MIS (:1370-1395)
         bool above = dot(nrm, dir) > 0.f && !smp.isDelta;
         float pOut = smp.isDelta ? 0.f : (guided ? pGuided : lobes_pdf(lb, smp.dir));
-        float pLout = above ? (1.f - es) * env_pdf(u, dir, nrm) : 0.f;
+        float pLout = above ? rs * (1.f - es) * env_pdf(u, dir, nrm) : 0.f;
         sunmis = pLout <= 0.f ? 1.f : mis_weight(pOut, pLout);
         // an emitter this bounce meets is weighed against the list's density for the direction, from here
-        const float pEout = (above && es > 0.f) ? es * emit_cone_pdf(a.em.dev, pos, dir) : 0.f;
+        const float pEout = (above && es > 0.f) ? rs * es * emit_cone_pdf(a.em.dev, pos, dir) : 0.f;
         emw = pEout <= 0.f ? 1.f : mis_weight(pOut, pEout);
+        // a face it meets, against the faces' density there (prevPdf, vtxLtot): only what light sampling could draw
+        lp = make_float2((above && fs > 0.f && !lobes_none(m, trans)) ? pOut : -1.f, ltot);
     } else {
         sunmis = 1.f;
         emw = 1.f;
+        lp = make_float2(-1.f, ltot);
     }
     f3 off = dir * otol;
     pos = pos + off; ltot += length(off) * n;
@@ -598,7 +638,7 @@ __device__ __forceinline__ void shade_surface(const WaveArgs& a, const st_materi
 
 __device__ __forceinline__ void shade_medium(const WaveArgs& a, f3& pos, f3& dir, f3& beta, float& sunmis,
                                              uint32_t& bounces, uint32_t& state, float n, Rng& rng, bool last,
-                                             ShadowOut& sh, float& emw) {
+                                             ShadowOut& sh, float& emw, float ltot, float2& lp) {
     const Uni& u = a.u;
     state = RAY_ACTIVE;
     bounces += 1;
@@ -607,31 +647,47 @@ __device__ __forceinline__ void shade_medium(const WaveArgs& a, f3& pos, f3& dir
     beta = beta * u.halb;
     // the discovered emitters' share of the air's light samples (haze.js:324-370), as at a surface
     const float es = (a.em.on && u.nee != 0u && !last) ? emit_share(a.em) : 0.f;
+    const float fs = (a.lf.n && u.nee != 0u && !last) ? FACE_SHARE : 0.f;   // the faces' share (haze.js:315-350)
+    const float rs = 1.f - fs;
     if (u.nee != 0u && !last) {                                       // mediumNee (haze.js:318-405)
         float4 u0 = rng.next();
         float4 u1 = rng.next();
         f3 L = mk(0.f, 0.f, 1.f);
-        float pS = 0.f;
-        bool toEmit = false;
-        if (u0.x < es) {
-            const uint32_t b = emit_pick(a.em.dev, u0.x / es);
+        float pS = 0.f, fdist = 0.f;
+        bool toEmit = false, toFace = false;
+        f3 fle = mk(0.f);
+        const float pick0 = (u0.x - fs) / fmaxf(rs, 1e-6f);
+        if (u0.x < fs) {                                              // a face: no vertex normal, the face's side
+            const Face f = face_at(a.lf, min((uint32_t)(u0.y * (float)a.lf.n), a.lf.n - 1u));
+            const f3 dy = face_point(f, u1.x, u1.y) - pos;
+            fdist = length(dy);
+            L = dy * (1.f / fmaxf(fdist, 1e-20f));
+            const float cosY = -dot(f.n, L);
+            if (fdist > 0.f && cosY > 1e-6f) {
+                pS = face_density(fs, a.lf.n, f, fdist, cosY);
+                fle = f.le * face_beam(f, cosY);                      // in air: over n^2 = 1
+                toFace = true;
+            }
+        } else if (pick0 < es) {
+            const uint32_t b = emit_pick(a.em.dev, pick0 / es);
             if (emit_sample(a.em.dev, b, pos, u1.x, u1.y, L)) {
-                pS = es * emit_cone_pdf(a.em.dev, pos, L);
+                pS = rs * es * emit_cone_pdf(a.em.dev, pos, L);
                 toEmit = true;
             }
         } else {
-            L = env_sample_dir_m(u, es > 0.f ? (u0.x - es) / (1.f - es) : u0.x, u1.x, u1.y);
-            pS = (1.f - es) * env_pdf_m(u, L);
+            L = env_sample_dir_m(u, es > 0.f ? (pick0 - es) / (1.f - es) : pick0, u1.x, u1.y);
+            pS = rs * (1.f - es) * env_pdf_m(u, L);
         }
         if (pS > 0.f) {
             float ph = hg_eval(dot(din, L), g);
             float w = mis_weight(pS, ph);
-            f3 le = toEmit ? mk(1.f) : env_radiance(u, L);
+            f3 le = toEmit ? mk(1.f) : (toFace ? fle : env_radiance(u, L));
             f3 contrib = beta * le * (ph * w / pS);
             if (max3(contrib) > (toEmit ? 1e-9f : 1e-7f)) {
                 // an emitter's ray takes the haze from where it starts to where it stops, at its resolve
-                float tr = toEmit ? 1.f : haze_tr(u, pos, L, 2.f * u.envR + length(pos));
-                sh.valid = true; sh.emit = toEmit; sh.org = pos; sh.dir = L; sh.rad = contrib * tr; sh.n = n;
+                float tr = toEmit ? 1.f : haze_tr(u, pos, L, toFace ? fdist : 2.f * u.envR + length(pos));
+                sh.valid = true; sh.emit = toEmit; sh.face = toFace; sh.dist = fdist;
+                sh.org = pos; sh.dir = L; sh.rad = contrib * tr; sh.n = n;
             }
         }
     }
@@ -640,13 +696,15 @@ __device__ __forceinline__ void shade_medium(const WaveArgs& a, f3& pos, f3& dir
     dir = dout;
     if (u.nee != 0u && !last) {
         float pB = hg_eval(dot(din, dout), g);
-        float pL = (1.f - es) * env_pdf_m(u, dout);
+        float pL = rs * (1.f - es) * env_pdf_m(u, dout);
         sunmis = pL <= 0.f ? 1.f : mis_weight(pB, pL);
-        const float pE = es > 0.f ? es * emit_cone_pdf(a.em.dev, pos, dout) : 0.f;
+        const float pE = es > 0.f ? rs * es * emit_cone_pdf(a.em.dev, pos, dout) : 0.f;
         emw = pE <= 0.f ? 1.f : mis_weight(pB, pE);
+        lp = make_float2(fs > 0.f ? pB : -1.f, ltot);
     } else {
         sunmis = 1.f;
         emw = 1.f;
+        lp = make_float2(-1.f, ltot);
     }
     if (bounces > u.maxbounce) state = RAY_TERMINATED;
 }
@@ -676,13 +734,14 @@ __global__ void __launch_bounds__(256) k_shade(WaveArgs a, int nxt, int side, in
         uint32_t q = r * stride + blockIdx.x * blockDim.x + threadIdx.x;
         bool valid = q < count;
         bool cont = false;
-        ShadowOut sh; sh.valid = false; sh.emit = false;
+        ShadowOut sh; sh.valid = false; sh.emit = false; sh.face = false; sh.dist = 0.f;
         uint32_t slot = 0, pix = 0, gpix = 0;
         f3 pos, dir, beta, rad;
         float ltot = 0.f, n = 1.f, sunmis = 1.f, tmax = 0.f;
         uint4 m4 = make_uint4(0, 0, 0, 0);
         uint32_t bounces = 0, seg = 0, state = RAY_TERMINATED;
         float lam = 0.f, emw = 1.f;
+        float2 lp = make_float2(-1.f, 0.f);
         bool train_nee = false;
         if (valid) {
             slot = a.q.hit[q];
@@ -701,12 +760,13 @@ __global__ void __launch_bounds__(256) k_shade(WaveArgs a, int nxt, int side, in
             } else if (state == RAY_ACTIVE || state == RAY_SCATTER) {
                 train_nee = GUIDE && (m4.y & META_TRAIN) != 0u;       // light found past a record's vertex counts
                 if (a.em.on) emw = a.em.w[slot];
+                if (a.lf.n) lp = a.pb.lprev[slot];
                 uint32_t tile = slot % u.P, j = slot / u.P;
                 Rng rng = path_rng(sample_seed(u.seed, a.ctr->sample + j), tile, 1u + seg);
                 seg += 1;
                 m4.w = __float_as_uint(ltot);                         // absorbAlong: absLtot on arrival
                 if (state == RAY_SCATTER) {
-                    shade_medium(a, pos, dir, beta, sunmis, bounces, state, n, rng, last != 0, sh, emw);
+                    shade_medium(a, pos, dir, beta, sunmis, bounces, state, n, rng, last != 0, sh, emw, ltot, lp);
                     m4.y &= ~(3u << META_LENS_SHIFT);                 // haze.js:539: the air is no delta event
                 }
                 else
@@ -714,7 +774,7 @@ __global__ void __launch_bounds__(256) k_shade(WaveArgs a, int nxt, int side, in
                     lam = a.pb.lam[slot];
                     uint32_t lens = (m4.y >> META_LENS_SHIFT) & 3u;
                     shade_surface<GUIDE>(a, sm, a.q.hsurf[q], pos, dir, ltot, n, beta, sunmis, rad, bounces, state,
-                                         lam, lens, dh, rng, last != 0, sh, q, m4.y, gpix, emw);
+                                         lam, lens, dh, rng, last != 0, sh, q, m4.y, gpix, emw, lp);
                     m4.y = (m4.y & ~(3u << META_LENS_SHIFT)) | (lens << META_LENS_SHIFT);
                 }
                 if (state == RAY_ACTIVE) {
@@ -728,10 +788,11 @@ __global__ void __launch_bounds__(256) k_shade(WaveArgs a, int nxt, int side, in
         uint32_t sq = warp_append(s_cnt, sh.valid);
         if (sh.valid) {
             if (sq < a.q.scap) {
-                s_org[sq] = f4(sh.org, 0.f);
+                // a face's ray starts at minus the way to the face, less four offsets: it arrives at ltot 0
+                s_org[sq] = f4(sh.org, sh.face ? -fmaxf(sh.dist - 40.f * march_tol(sh.org, u.tol), 0.f) * sh.n : 0.f);
                 s_dir[sq] = f4(sh.dir, __uint_as_float(gpix));
                 s_rad[sq] = f4(sh.rad, train_nee ? -sh.n : sh.n);    // a negative index: counted for a record
-                s_steps[sq] = sh.emit ? SHADOW_EMIT : 0u;
+                s_steps[sq] = sh.emit ? SHADOW_EMIT : (sh.face ? SHADOW_FACE : 0u);
             } else {
                 dropped++;
             }
@@ -744,6 +805,7 @@ __global__ void __launch_bounds__(256) k_shade(WaveArgs a, int nxt, int side, in
             a.pb.rad[slot] = f4(rad, tmax);
             if (lam != 0.f) a.pb.lam[slot] = lam;
             if (a.em.on) a.em.w[slot] = emw;
+            if (a.lf.n) a.pb.lprev[slot] = lp;
             m4.y = meta_y(bounces, seg, RAY_ACTIVE) | (m4.y & ~META_LOW);
             a.pb.meta[slot] = m4;
             outq[rq] = slot;
@@ -826,8 +888,8 @@ __global__ void __launch_bounds__(256, 4) k_occlude(WaveArgs a, int last) {
                     float4 o4 = i_org[idx], d4 = i_dir[idx];
                     pos = xyz(o4); ltot = o4.w; dir = xyz(d4); n = fabsf(i_rad[idx].w);
                     steps = i_steps[idx];
-                    sflag = steps & SHADOW_EMIT;                      // aimed at an emitter (TAG_EMIT)
-                    steps &= ~SHADOW_EMIT;
+                    sflag = steps & SHADOW_FLAGS;                     // aimed at an emitter (TAG_EMIT), a face
+                    steps &= ~SHADOW_FLAGS;
                     evals_here = 0;
                     if (steps == 0u) rays++;
                 }
@@ -842,7 +904,8 @@ __global__ void __launch_bounds__(256, 4) k_occlude(WaveArgs a, int last) {
             evals_here++;
             float ea = fabsf(d);
             float eps = march_tol(pos, tol);
-            if (ea < eps) done = true;                                // blocked
+            if ((sflag & SHADOW_FACE) && ltot >= 0.f) { reached = true; done = true; }   // at the face (TAG_FNEE)
+            else if (ea < eps) done = true;                           // blocked
             else if (dot(pos, dir) > 0.f && dot(pos, pos) > envR2) { reached = true; done = true; }
             else {
                 steps += 1;
@@ -860,14 +923,14 @@ __global__ void __launch_bounds__(256, 4) k_occlude(WaveArgs a, int last) {
         uint32_t cp = warp_append(o_cnt, more);
         // an emitter's ray asks what it stopped at (wavefront.js:1694-1749): handed to k_emit_resolve; it finds
         // nothing where it leaves the scene
-        const bool met = done && !reached && sflag != 0u;
+        const bool met = done && !reached && (sflag & SHADOW_EMIT) != 0u;
         const uint32_t ep = a.em.on ? warp_append(&a.ctr->emitHits, met) : 0u;
         if (met && ep < a.q.scap) {
             a.em.hpos[ep] = f4(pos, ltot);
             a.em.hdir[ep] = i_dir[idx];
             a.em.hrad[ep] = i_rad[idx];
         }
-        if (reached && sflag == 0u) {
+        if (reached && (sflag & SHADOW_EMIT) == 0u) {
             float4 r4 = i_rad[idx];
             uint32_t gpix = __float_as_uint(i_dir[idx].w);          // the pixel in the wave's frames
             deposit(a.frame, gpix, xyz(r4), a.ctr);

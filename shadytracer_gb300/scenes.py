@@ -10,7 +10,8 @@ at them, plus the st_params and st_view of its workload.
 import ctypes as C
 import math
 
-from .st_types import (StPrim, StMaterial, StSceneDesc, StView, default_params,
+from .st_types import (StPrim, StMaterial, StSceneDesc, StView, StLight, default_params,
+                       ST_LIGHT_DISC, ST_LIGHT_RECTANGLE, ST_LIGHT_COSINE, ST_LIGHT_UNIFORM,
                        ST_PRIM_PLANE, ST_PRIM_SPHERE, ST_PRIM_BOX, ST_PRIM_ROUNDBOX, ST_PRIM_TORUS,
                        ST_PRIM_PRISM, ST_PRIM_ASPHERE, ST_PRIM_CYLINDER,
                        ST_OP_ITEM, ST_OP_SMOOTH, ST_OP_UNION, ST_OP_SUB)
@@ -19,8 +20,9 @@ IDENTITY = (1.0, 0.0, 0.0, 0.0, 1.0, 0.0, 0.0, 0.0, 1.0)
 
 
 class Scene:
-    def __init__(self, prims, materials, env_radius=400.0, tolerance=0.0, haze=None, name="scene"):
+    def __init__(self, prims, materials, env_radius=400.0, tolerance=0.0, haze=None, name="scene", lights=()):
         self.name = name
+        self.light_list = list(lights)
         self.prim_list = list(prims)
         self.material_list = list(materials)
         self.prims = (StPrim * len(prims))(*prims)
@@ -44,10 +46,53 @@ class Scene:
             if "axes" in haze:
                 for i in range(9):
                     d.haze_axes[i] = haze["axes"][i]
+        if self.light_list:
+            self.lights = (StLight * len(self.light_list))(*self.light_list)
+            d.lights = C.cast(self.lights, C.POINTER(StLight))
+            d.n_lights = len(self.light_list)
         self.desc = d
         self.params = None
         self.view = None
         self.info = {}
+
+
+def flux_factor(dist=ST_LIGHT_COSINE, n=1.0, half_deg=90.0):
+    """builder/lights.js fluxFactor: a face's flux per unit luminance straight out and unit area -- the integral of
+    its beam's shape times cos over the cone: 2 pi (1 - c^(n+1)) / (n + 1) for cos^n, 2 pi (1 - c) for even
+    intensity (c the cosine of the half angle)."""
+    c = math.cos(math.radians(min(90.0, max(0.0, half_deg))))
+    if dist == ST_LIGHT_UNIFORM:
+        return 2 * math.pi * (1 - c)
+    n = max(0.0, n)
+    return 2 * math.pi * (1 - max(c, 0.0) ** (n + 1)) / (n + 1)
+
+
+def light_face(centre, u, v, half_w, half_h=None, flux=None, le=None, colour=(1.0, 1.0, 1.0), material=1,
+               dist=ST_LIGHT_COSINE, n=1.0, half_deg=90.0, shape=ST_LIGHT_RECTANGLE):
+    """A light's face (the builder's light object): a rectangle (half_w x half_h about centre along the unit axes u,
+    v) or a disc (radius half_w), emitting along u x v in a cos^n or even-intensity beam of half angle half_deg.
+    Its luminance straight out is `le` (cd/m^2), or what puts `flux` lumens through the face: flux / (A k), k the
+    beam's flux factor, coloured by `colour` at that luminance (lights.js, codegen's emissive / luminance)."""
+    L = StLight()
+    area = 4 * half_w * (half_h if half_h is not None else half_w) if shape == ST_LIGHT_RECTANGLE else math.pi * half_w ** 2
+    if le is None:
+        lum = flux / (area * flux_factor(dist, n, half_deg))
+        y = 0.2126 * colour[0] + 0.7152 * colour[1] + 0.0722 * colour[2]
+        le = [c / max(y, 1e-6) * lum for c in colour]
+    for i in range(3):
+        L.centre[i], L.u[i], L.v[i], L.le[i] = centre[i], u[i], v[i], le[i]
+    L.shape = shape
+    L.half_w = half_w
+    L.half_h = half_h if half_h is not None else half_w
+    L.material, L.dist, L.n = material, dist, n
+    L.beam_cos = math.cos(math.radians(half_deg)) if half_deg < 90.0 else 0.0
+    return L
+
+
+def face_axes(axis):
+    """Unit axes u, v of a face that emits along `axis` (u x v = axis)."""
+    R = spot_rot([-c for c in axis])                  # its rows: local x, y and z = axis
+    return R[0:3], R[3:6]
 
 
 def prim(type_, pos=(0, 0, 0), params=(), material=1, op=ST_OP_ITEM, k=0.0, rot=IDENTITY, flags=0):
@@ -199,20 +244,30 @@ def spot_rot(axis):
     return tuple(x) + tuple(y) + tuple(z)
 
 
-def spot_floor(width=128, height=128, spp=64, flux=1000.0, half_deg=10.0, side=0.2, albedo=0.8, seed=1):
+def spot_floor(width=128, height=128, spp=64, flux=1000.0, half_deg=10.0, side=0.2, albedo=0.8, seed=1,
+               light="emitter"):
     """A 10-degree spot of `flux` lumens -- a thin square lamp `side` x `side` m whose lower face emits into a cone of
     `half_deg` about its normal -- at (-1, 0, 1) aimed at the origin, over an infinite Lambertian floor in a black
     environment, seen straight down by an orthographic camera over 2 x 2 m about the origin. All the beam's flux lands
     on the floor, so pi / albedo times the floor's luminance summed over its area is the flux (the lamp's other faces
     light no floor in view). A lamp of 20 cm keeps the emitter list's first boxes -- bounds of the few points the
-    camera found on it -- from leaving most of it to the BSDF's rare hits."""
+    camera found on it -- from leaving most of it to the BSDF's rare hits.
+    light="face": the lamp is a light's face instead (one-sided, its flux set through fluxFactor), which light
+    sampling aims at from the start."""
     le = spot_luminance(flux, side * side, half_deg)
     axis = (1.0, 0.0, -1.0)
-    lamp = prim(ST_PRIM_BOX, pos=(-1.0, 0.0, 1.0), params=(side / 2, side / 2, 0.0005), material=2,
-                rot=spot_rot(axis))
-    s = Scene([prim(ST_PRIM_PLANE, material=1), lamp],
-              [air(), diffuse((albedo, albedo, albedo)), emitter((le, le, le), beam_deg=half_deg)], env_radius=20.0,
-              name="spot-floor")
+    if light == "face":
+        u, v = face_axes(axis)
+        s = Scene([prim(ST_PRIM_PLANE, material=1)], [air(), diffuse((albedo, albedo, albedo)), diffuse((0, 0, 0))],
+                  env_radius=20.0, name="spot-face-floor",
+                  lights=[light_face((-1.0, 0.0, 1.0), u, v, side / 2, side / 2, flux=flux, material=2,
+                                     half_deg=half_deg)])
+    else:
+        lamp = prim(ST_PRIM_BOX, pos=(-1.0, 0.0, 1.0), params=(side / 2, side / 2, 0.0005), material=2,
+                    rot=spot_rot(axis))
+        s = Scene([prim(ST_PRIM_PLANE, material=1), lamp],
+                  [air(), diffuse((albedo, albedo, albedo)), emitter((le, le, le), beam_deg=half_deg)],
+                  env_radius=20.0, name="spot-floor")
     s.params = default_params(width=width, height=height, maxbounce=2, sun_hint=0, sun_illuminance=0.0,
                               sky_luminance=0.0, ground_luminance=0.0, seed=seed, eps=1e-4)
     v = StView()
@@ -228,18 +283,27 @@ def spot_floor(width=128, height=128, spp=64, flux=1000.0, half_deg=10.0, side=0
     return s
 
 
-def haze_beam(width=1280, height=720, spp=256, sigma_s=0.2, g=0.7, flux=1000.0, half_deg=10.0, maxbounce=32, seed=1):
+def haze_beam(width=1280, height=720, spp=256, sigma_s=0.2, g=0.7, flux=1000.0, half_deg=10.0, maxbounce=32, seed=1,
+              light="face"):
     """The haze-box beam: a 2 x 2 x 4 m box of homogeneous haze (scattering sigma_s, absorbing nothing, HG g), crossed
     along its length by a 10-degree spot of 1000 lm -- a 5 cm square lamp 0.5 m below the box aiming up its axis -- in a
-    black environment, seen from the side. The lamp is a thin box of one beam material: its other faces emit too, each
-    into its own 10-degree cone (the downward face into the black below, the 1 mm edges sideways)."""
+    black environment, seen from the side. The lamp is a light's face (light="face"): one-sided, aimed at by light
+    sampling from the air. light="emitter": a thin box of one beam material instead, found by discovery, whose other
+    faces emit too, each into its own cone."""
     side = 0.05
     le = spot_luminance(flux, side * side, half_deg)
-    lamp = prim(ST_PRIM_BOX, pos=(0.0, 0.0, -0.5), params=(side / 2, side / 2, 0.0005), material=1,
-                rot=spot_rot((0.0, 0.0, 1.0)))
-    s = Scene([lamp], [air(), emitter((le, le, le), beam_deg=half_deg)], env_radius=40.0,
-              haze={"centre": (0.0, 0.0, 2.0), "half": (1.0, 1.0, 2.0), "sigma_t": sigma_s, "g": g,
-                    "albedo": (1.0, 1.0, 1.0)}, name="haze-beam")
+    haze = {"centre": (0.0, 0.0, 2.0), "half": (1.0, 1.0, 2.0), "sigma_t": sigma_s, "g": g, "albedo": (1.0, 1.0, 1.0)}
+    if light == "face":
+        # a far floor below keeps the table of primitives from being empty; nothing of it is in view or lit
+        s = Scene([prim(ST_PRIM_PLANE, pos=(0.0, 0.0, -100.0), material=2)], [air(), diffuse((0, 0, 0)),
+                  diffuse((0, 0, 0))], env_radius=40.0, haze=haze, name="haze-beam",
+                  lights=[light_face((0.0, 0.0, -0.5), (1.0, 0.0, 0.0), (0.0, 1.0, 0.0), side / 2, side / 2, flux=flux,
+                                     material=1, half_deg=half_deg)])
+    else:
+        lamp = prim(ST_PRIM_BOX, pos=(0.0, 0.0, -0.5), params=(side / 2, side / 2, 0.0005), material=1,
+                    rot=spot_rot((0.0, 0.0, 1.0)))
+        s = Scene([lamp], [air(), emitter((le, le, le), beam_deg=half_deg)], env_radius=40.0, haze=haze,
+                  name="haze-beam")
     s.params = default_params(width=width, height=height, maxbounce=maxbounce, sun_hint=0, sun_illuminance=0.0,
                               sky_luminance=0.0, ground_luminance=0.0, seed=seed, eps=1e-4)
     s.view = look_at((0.0, -7.0, 1.8), (0.0, 0.0, 1.8), 45.0, width / height)

@@ -37,13 +37,25 @@ class StMaterial(C.Structure):
                 ("emissive", C.c_float * 3), ("beam_cos", C.c_float)]
 
 
+ST_LIGHT_DISC, ST_LIGHT_RECTANGLE = 1, 2
+ST_LIGHT_COSINE, ST_LIGHT_UNIFORM = 0, 1
+ST_MAX_LIGHTS = 64
+
+
+class StLight(C.Structure):
+    _fields_ = [("centre", C.c_float * 3), ("shape", C.c_uint32), ("u", C.c_float * 3), ("half_w", C.c_float),
+                ("v", C.c_float * 3), ("half_h", C.c_float), ("le", C.c_float * 3), ("material", C.c_uint32),
+                ("dist", C.c_uint32), ("n", C.c_float), ("beam_cos", C.c_float), ("pad", C.c_uint32)]
+
+
 class StSceneDesc(C.Structure):
     _fields_ = [("prims", C.POINTER(StPrim)), ("n_prims", C.c_uint32),
                 ("materials", C.POINTER(StMaterial)), ("n_materials", C.c_uint32),
                 ("env_radius", C.c_float), ("tolerance", C.c_float),
                 ("haze_centre", C.c_float * 3), ("haze_sigma_t", C.c_float),
                 ("haze_axes", C.c_float * 9), ("haze_half", C.c_float * 3),
-                ("haze_albedo", C.c_float * 3), ("haze_g", C.c_float)]
+                ("haze_albedo", C.c_float * 3), ("haze_g", C.c_float),
+                ("lights", C.POINTER(StLight)), ("n_lights", C.c_uint32)]
 
 
 class StParams(C.Structure):

@@ -117,18 +117,24 @@ def test_haze_furnace_conserves_energy(rt_factory):
 @pytest.mark.parametrize("sigma_s", [0.05, 0.2, 1.0])
 def test_haze_box_grid_conserves_energy(rt_factory, sigma_s):
     """The haze box at every scattering coefficient and anisotropy of its grid: an albedo-1 box in a uniform
-    1000 cd/m^2 environment reads 1000 to 0.02 % (a collision's weight is exactly one: HG drawn exactly) with 64
-    bounces; with 32 the paths the cap ends (at sigma_s 1, isotropic, about 4 in 10^4) are all it loses."""
+    1000 cd/m^2 environment. Drawing the phase function alone, every path's weight is exactly one (HG drawn exactly),
+    so the picture reads 1000 to 0.02 % with 64 bounces -- what the cap ends is all it may lose. With the light sample
+    and its MIS weights (32 bounces), each sample is 1000 only on average: the mean within its error bar."""
     for g in (0.0, 0.7, 0.9):
-        for maxbounce, tol in ((64, 2e-4), (32, 1e-3)):
-            s = scenes.haze_furnace(width=64, height=64, sigma_t=sigma_s, g=g, maxbounce=maxbounce)
-            rt = rt_factory(s)
-            rt.step(16)
-            rgb, V, S, cnt = rt.read_accum()
-            L = rgb @ LUMA
-            assert abs(L.mean() / 1000.0 - 1) < tol, (sigma_s, g, maxbounce, L.mean())
-            assert L.mean() <= 1000.0 * (1 + 1e-6)
-            assert rt.counters()["nonfinite"] == 0
+        s = scenes.haze_furnace(width=64, height=64, sigma_t=sigma_s, g=g, maxbounce=64)
+        s.params.nee = 0
+        rt = rt_factory(s)
+        rt.step(16)
+        L = rt.read_accum()[0] @ LUMA
+        assert abs(L.mean() / 1000.0 - 1) < 2e-4 and L.max() <= 1000.0 * (1 + 1e-5), (sigma_s, g, L.mean(), L.max())
+        assert rt.counters()["nonfinite"] == 0
+        s = scenes.haze_furnace(width=64, height=64, sigma_t=sigma_s, g=g, maxbounce=32)
+        rt = rt_factory(s)
+        rt.step(16)
+        rgb, V, S, cnt = rt.read_accum()
+        L = rgb @ LUMA
+        se = np.sqrt(np.sum(se_of(V, S) ** 2)) / L.size
+        assert abs(L.mean() - 1000.0) < 5 * se + 0.05, (sigma_s, g, L.mean(), se)
 
 
 def test_invalidate_and_state(rt_factory):

@@ -131,3 +131,33 @@ def test_spot_floor_flux():
     out = ang > 18.0
     assert np.mean(L[out] == 0.0) > 0.99 and L[out].sum() < 0.005 * L.sum()
     assert np.all(L[ang < 3.0] > 0.0)
+
+
+@pytest.mark.parametrize("side", [0.2, 0.05])
+def test_spot_face_flux(side):
+    """The spot as a light's face (builder/lights.js: one-sided, 1000 lm through its beam by fluxFactor; light sampling
+    aims at a point of it, scene_api.js lightFaceDensity): pi / albedo times the floor's luminance summed over its area
+    is the flux, and nothing lands past the cone's blurred edge."""
+    s = scenes.spot_floor(width=64, height=64, side=side, light="face")
+    ref = oracle.render(s, 64)
+    L = ref.luma()
+    k = s.info["pixel_area"] * math.pi / s.info["albedo"]
+    flux, err = L.sum() * k, math.sqrt(np.sum(ref.V / 64)) * k
+    assert abs(flux - 1000.0) < max(5 * err, 10.0), (flux, err)
+    _, ang = spot_floor_points(s)
+    assert np.all(L[ang > 18.0] == 0.0)
+
+
+def test_face_light_sample_is_unbiased():
+    """A BSDF's hits of a face weighed against the face's light sample (codegen.js:826-834) and the light sample
+    itself: the floor lit through both agrees with the floor lit by the BSDF's hits alone (light sampling off)."""
+    s = scenes.spot_floor(width=32, height=32, side=0.4, light="face")
+    s.params.maxbounce = 2
+    on = oracle.render(s, 256)
+    s.params.nee = 0
+    off = oracle.render(s, 2048)
+    k = s.info["pixel_area"] * math.pi / s.info["albedo"]
+    f_on, f_off = on.luma().sum() * k, off.luma().sum() * k
+    e_on, e_off = math.sqrt(np.sum(on.V / 256)) * k, math.sqrt(np.sum(off.V / 2048)) * k
+    assert abs(f_on - f_off) < 5 * math.hypot(e_on, e_off), (f_on, e_on, f_off, e_off)
+    assert abs(f_on - 1000.0) < 5 * e_on + 10.0
