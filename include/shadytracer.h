@@ -208,6 +208,7 @@ typedef struct st_params {
                                    * to [0.05, 0.95]; the reference's neeEmitShare)                   */
     float    emit_radius;         /* the discovery grid's half-size, metres (0: 15; capped at the scene's radius)  */
     uint32_t emit_off;            /* 1: no light sampling of emitters (discovery goes on)            */
+    uint32_t env_map_off;         /* 1: light sampling does not draw from the environment image's map  */
 } st_params;
 
 /* The camera, as genrays reads it (core/genrays.js:65-92): the basis from invView's columns and the
@@ -273,6 +274,17 @@ int  st_set_scene(st_ctx* ctx, const char* cuda_src, const st_scene_desc* desc, 
  * settings resets the accumulation. */
 int  st_set_params(st_ctx* ctx, const st_params* p, uint64_t* unknown_mask);
 int  st_set_view(st_ctx* ctx, const st_view* v);
+/* THE ENVIRONMENT IMAGE (core/envimage.js, the image preset of core/environment.js; core/envmap.js the map light
+ * sampling draws from): an equirectangular panorama, w x h pixels of linear rgb floats, top row first, its middle
+ * column +x, running right as one turns right, turned turn_deg about z (anticlockwise from above); luminance is the
+ * cd/m^2 of a unit (0: 179, a Radiance file's efficacy). It becomes the whole environment -- no sun, sky or ground --
+ * and light sampling draws half its environment samples from a 512 x 256 equal-area map of it (envMapShare), baked on
+ * the GPU here. rgb NULL goes back to the sun and sky. Resets the accumulation. */
+int  st_set_env_image(st_ctx* ctx, const float* rgb, uint32_t w, uint32_t h, float luminance, float turn_deg);
+/* The map's tables from its texels' mean luminances (envmap.js:215-260 envSampling), host-only: lum 512 x 256 floats,
+ * rows from straight up; tex 512 x 256 x 4 floats (the CDF along the row at the texel's end, the density per
+ * steradian, the CDF down the rows at the row's end, 0). Returns 0, or ST_ERR_ARG. */
+int  st_env_map_tables(const float* lum, float* tex);
 int  st_invalidate(st_ctx* ctx);
 
 /* ---- tracing ---- */

@@ -59,6 +59,9 @@ def _declare(L):
     L.sto_fresnel_dielectric.restype = C.c_double
     L.sto_lobes.argtypes = [P, P, P, C.c_double, P, P]
     L.sto_lobes_sample.argtypes = [P, P, C.c_double, C.c_uint32, C.c_int, P, P]
+    L.sto_set_env_image.argtypes = [P, C.c_uint32, C.c_uint32, C.c_float, C.c_float]
+    L.sto_env_map_tables.argtypes = [P, P]
+    L.sto_env_radiance.argtypes = [P, P, P, C.c_uint32, P]
     for name, args, res in _EXTRA:
         if hasattr(L, name):
             f = getattr(L, name)
@@ -111,6 +114,32 @@ def render(scene, nsamples, accum=None, fp64=False, threads=0, sample0=None, pat
         raise RuntimeError("sto_render failed: %d" % rc)
     accum.next_sample = s0 + nsamples
     return accum
+
+
+def set_env_image(rgb=None, luminance=0.0, turn=0.0):
+    """The environment image for the renders that follow (H x W x 3 linear floats, top row first); None clears it."""
+    if rgb is None:
+        lib().sto_set_env_image(None, 0, 0, 0.0, 0.0)
+        return
+    img = np.ascontiguousarray(rgb, np.float32)
+    if lib().sto_set_env_image(ptr(img), img.shape[1], img.shape[0], luminance, turn) != 0:
+        raise ValueError("bad environment image")
+
+
+def env_map_tables(lum):
+    """The map's tables (512 x 256 x 4) from its texels' mean luminances (256 rows x 512)."""
+    lum = np.ascontiguousarray(lum, np.float32).reshape(-1)
+    tex = np.zeros(lum.size * 4, np.float32)
+    lib().sto_env_map_tables(ptr(lum), ptr(tex))
+    return tex.reshape(256, 512, 4)
+
+
+def env_radiance(scene, dirs):
+    """The environment's radiance (rgb) in the given directions, as the oracle has it for this scene's settings."""
+    d = np.ascontiguousarray(dirs, np.float64).reshape(-1, 3)
+    out = np.zeros_like(d)
+    lib().sto_env_radiance(C.byref(scene.params), C.byref(scene.desc), ptr(d), len(d), ptr(out))
+    return out
 
 
 def mf_tables(fp64=False):

@@ -1282,6 +1282,52 @@ extern "C" {
 // Render nsamples samples from sample0 on, folding each into the FP64 accumulation (caller-owned, continued across
 // calls). fp64: 0 the reference-equivalent f32 arithmetic, 1 the accuracy oracle. path_first/path_count restrict the
 // traced paths (a crop, for the CPU baseline's bounded sample); 0/0 = all.
+// the environment image for every render that follows (envimage.js; envmap.js the map, baked here in double at the
+// library's 2 x 2 points a texel and tabulated as the library tabulates it); rgb NULL: back to the sun and sky
+int sto_set_env_image(const float* rgb, uint32_t w, uint32_t h, float luminance, float turn_deg) {
+    EnvImage& im = env_image_state();
+    if (!rgb) { im = EnvImage(); return 0; }
+    if (w < 2 || h < 1) return -1;
+    im.rgb.assign(rgb, rgb + (size_t)w * h * 3);
+    for (float& c : im.rgb) if (!std::isfinite(c)) c = 0.f;
+    im.w = w; im.h = h;
+    im.lum = luminance > 0.f ? luminance : 179.0;
+    im.turn = turn_deg;
+    std::vector<double> lum((size_t)ENV_MW * ENV_MH);
+    for (int i = 0; i < ENV_MW * ENV_MH; i++) {
+        const int x = i % ENV_MW, y = i / ENV_MW;
+        double acc[3] = {0, 0, 0};
+        for (int sy = 0; sy < 2; sy++)
+            for (int sx = 0; sx < 2; sx++) {
+                const double ux = (x + (sx + 0.5) * 0.5) / ENV_MW, uy = (y + (sy + 0.5) * 0.5) / ENV_MH;
+                const double z = 1 - 2 * uy, sz = std::sqrt(std::max(0.0, 1 - z * z)), ph = 2 * PI_D * ux;
+                double c[3];
+                env_image_at(im, sz * std::cos(ph), sz * std::sin(ph), z, c);
+                for (int k = 0; k < 3; k++) acc[k] += c[k];
+            }
+        lum[i] = 0.25 * (0.2126 * acc[0] + 0.7152 * acc[1] + 0.0722 * acc[2]);
+    }
+    env_tables(lum, im.tex);
+    return 0;
+}
+// the map's tables from given texel luminances (the library's st_env_map_tables, restated)
+int sto_env_map_tables(const float* lum, float* tex) {
+    std::vector<double> l(lum, lum + ENV_MW * ENV_MH);
+    std::vector<float> t;
+    env_tables(l, t);
+    std::copy(t.begin(), t.end(), tex);
+    return 0;
+}
+// the environment's radiance as the oracle has it, in n given directions (rgb out)
+int sto_env_radiance(const st_params* p, const st_scene_desc* s, const double* dirs, uint32_t n, double* out) {
+    Env<double> e;
+    e.init(*p, derive(*p, *s));
+    for (uint32_t i = 0; i < n; i++) {
+        V3<double> c = e.radiance(V3<double>(dirs[3 * i], dirs[3 * i + 1], dirs[3 * i + 2]));
+        out[3 * i] = c.x; out[3 * i + 1] = c.y; out[3 * i + 2] = c.z;
+    }
+    return 0;
+}
 int sto_render(const st_scene_desc* s, const st_params* p, const st_view* v, uint32_t sample0, uint32_t nsamples,
                int fp64, double* acc_rgb, double* mV, double* mS, uint32_t* acc_cnt, uint64_t* counters, int threads,
                uint32_t path_first, uint32_t path_count) {

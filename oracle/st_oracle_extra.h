@@ -29,6 +29,7 @@ template <class T> inline V3<T> hg_sample(const V3<T>& d, T g, T u0, T u1) {
 // the environment from a point in the air (haze.js:296-310 envSampleDirM / envPdfM): the sun's cone, else the sphere
 template <class T> inline V3<T> env_sample_dir_m(const Env<T>& e, T pick, T u0, T u1) {
     if (pick < e.pick) return e.sample_sun_cone(u0, u1);
+    if (e.mshare > T(0) && (pick - e.pick) / std::max(T(1) - e.pick, T(1e-6)) < e.mshare) return e.map_sample(u0, u1);
     T z = T(1) - T(2) * u0;
     T s = std::sqrt(std::max(T(0), T(1) - z * z));
     T ph = T(2) * T(PI_D) * u1;
@@ -36,7 +37,8 @@ template <class T> inline V3<T> env_sample_dir_m(const Env<T>& e, T pick, T u0, 
 }
 template <class T> inline T env_pdf_m(const Env<T>& e, const V3<T>& L) {
     T pSun = e.in_sun_disc(L) ? T(1) / e.sun_omega : T(0);
-    return e.pick * pSun + (T(1) - e.pick) / (T(4) * T(PI_D));
+    const T pm = e.mshare > T(0) ? e.mshare * e.map_pdf(L) : T(0);
+    return e.pick * pSun + (T(1) - e.pick) * (pm + (T(1) - e.mshare) / (T(4) * T(PI_D)));
 }
 
 // THE BOX (haze.js:64-80 hazeUniforms, :222-252 hazeSlab / hazeSpan / hazeTr, :255-273 hazeDraw)

@@ -10,6 +10,60 @@ namespace sto {
 // ------------------------------------------------------------------------------------------------------------
 // DERIVED UNIFORMS in double precision -- core/photometry.js:55-73 sunCone/discLuminance, :182-237 derive
 // ------------------------------------------------------------------------------------------------------------
+// THE ENVIRONMENT IMAGE (envimage.js) and the map light sampling draws from (envmap.js), set for every render that
+// follows (sto_set_env_image): the pixels (rgb, top row first), the cd/m^2 of a unit, the turn, the map's tables
+const int ENV_MW = 512, ENV_MH = 256;
+struct EnvImage {
+    std::vector<float> rgb;
+    uint32_t w = 0, h = 0;
+    double lum = 179.0, turn = 0.0;
+    std::vector<float> tex;                 // ENV_MW x ENV_MH x 4, as the library's
+    bool on() const { return w > 0; }
+};
+inline EnvImage& env_image_state() { static EnvImage e; return e; }
+// envImage (envimage.js:33-52 and its JS twin envImageAt): bilinear, wrapping across the seam, clamped at the poles
+inline void env_image_at(const EnvImage& im, double dx, double dy, double dz, double* out) {
+    const double n = std::sqrt(dx * dx + dy * dy + dz * dz);
+    dx /= n; dy /= n; dz /= n;
+    const int w = (int)im.w, h = (int)im.h;
+    double a = 0.5 - std::atan2(dy, dx) / (2.0 * PI_D) + im.turn / 360.0;
+    a -= std::floor(a);
+    const double u = a * w - 0.5, v = std::acos(std::min(1.0, std::max(-1.0, dz))) / PI_D * h - 0.5;
+    const double x0 = std::floor(u), y0 = std::floor(v), fx = u - x0, fy = v - y0;
+    const int xa = (((int)x0 % w) + w) % w, xb = (xa + 1) % w;
+    const int ya = std::min(std::max((int)y0, 0), h - 1), yb = std::min(std::max((int)y0 + 1, 0), h - 1);
+    for (int c = 0; c < 3; c++) {
+        auto px = [&](int x, int y) { return (double)im.rgb[((size_t)y * w + x) * 3 + c]; };
+        const double top = px(xa, ya) * (1 - fx) + px(xb, ya) * fx, bot = px(xa, yb) * (1 - fx) + px(xb, yb) * fx;
+        out[c] = std::max(0.0, top * (1 - fy) + bot * fy) * im.lum;
+    }
+}
+// envSampling (envmap.js:215-260): the texels' weights (luminance plus a floor of 1e-3 of the mean), the CDFs
+inline void env_tables(const std::vector<double>& lum, std::vector<float>& tex) {
+    const int W = ENV_MW, H = ENV_MH, N = W * H;
+    double sum = 0;
+    for (int i = 0; i < N; i++) sum += (lum[i] > 0 && std::isfinite(lum[i])) ? lum[i] : 0.0;
+    const double mean = sum / N, fl = mean > 0 ? 1e-3 * mean : 1.0;
+    std::vector<double> w(N);
+    double total = 0;
+    for (int i = 0; i < N; i++) { w[i] = ((lum[i] > 0 && std::isfinite(lum[i])) ? lum[i] : 0.0) + fl; total += w[i]; }
+    tex.assign((size_t)N * 4, 0.f);
+    double below = 0;
+    for (int row = 0; row < H; row++) {
+        double rs = 0, along = 0;
+        for (int x = 0; x < W; x++) rs += w[row * W + x];
+        const double rc = row == H - 1 ? 1.0 : (below + rs) / total;
+        for (int x = 0; x < W; x++) {
+            const int i = row * W + x;
+            along += w[i];
+            tex[4 * i] = x == W - 1 ? 1.f : (float)(along / rs);
+            tex[4 * i + 1] = (float)(w[i] / total * (N / (4.0 * PI_D)));
+            tex[4 * i + 2] = (float)rc;
+        }
+        below += rs;
+    }
+}
+
 struct Derived {
     double sun_half, sun_omc, sun_sin2, sun_omega, disc_lum;
     double sun_tint[3];
@@ -32,7 +86,8 @@ inline Derived derive(const st_params& p, const st_scene_desc& s) {
     double y = raw[0] * LUMA_R + raw[1] * LUMA_G + raw[2] * LUMA_B;
     for (int i = 0; i < 3; i++) d.sun_tint[i] = raw[i] / y;
     bool furnace = p.env_uniform > 0;
-    d.sun_on = (p.sun_hint != 0 && p.sun_elevation * PI_D / 180.0 + half > 0 && !furnace) ? 1 : 0;   // photometry.js:194
+    d.sun_on = (p.sun_hint != 0 && p.sun_elevation * PI_D / 180.0 + half > 0 && !furnace &&          // photometry.js:194
+                !env_image_state().on()) ? 1 : 0;                                                 // an image: no sun
     d.nee_sun_pick = (d.sun_on && p.env_sun_gain > 0) ? p.nee_sun_pick : 0.0;                        // photometry.js:226
     d.tol_setting = p.eps > 0 ? p.eps : (s.tolerance > 0 ? s.tolerance : 1e-3);                     // photometry.js:141-150
     d.env_radius = s.env_radius > 0 ? s.env_radius : 400.0;                                          // photometry.js:158
@@ -188,7 +243,12 @@ template <class T> inline SceneHit<T> scene_eval(const st_scene_desc& s, const V
 template <class T> struct Env {
     V3<T> sun_dir; T sun_sin2, sun_omc, sun_omega; int sun_on; T pick;
     V3<T> disc; T sky, ground, uniform, sun_gain, sky_gain;
+    const EnvImage* img = nullptr;          // the environment image, and its map's share of the samples
+    T mshare = 0;
     void init(const st_params& p, const Derived& d) {
+        const EnvImage& im = env_image_state();
+        img = im.on() ? &im : nullptr;
+        mshare = (img && !p.env_map_off) ? T(0.5) : T(0);
         sun_dir = V3<T>(T(d.sun_dir[0]), T(d.sun_dir[1]), T(d.sun_dir[2]));
         sun_sin2 = T(d.sun_sin2); sun_omc = T(d.sun_omc); sun_omega = T(d.sun_omega); sun_on = d.sun_on;
         pick = T(d.nee_sun_pick);
@@ -198,7 +258,7 @@ template <class T> struct Env {
     }
     V3<T> sky_only(const V3<T>& dir) const {                        // sdf.js skyRadiance: no disc
         bool cone = sun_on && in_sun_disc(dir);
-        V3<T> b = uniform > T(0) ? V3<T>(uniform) : V3<T>(normalize(dir).z > T(0) ? sky : ground);
+        V3<T> b = img ? image(dir) : (uniform > T(0) ? V3<T>(uniform) : V3<T>(normalize(dir).z > T(0) ? sky : ground));
         return b * (cone ? sun_gain : sky_gain);
     }
     bool in_sun_disc(const V3<T>& dir) const {                       // sdf.js:91-96
@@ -211,7 +271,41 @@ template <class T> struct Env {
         if (in_sun_disc(dir)) return disc;
         return V3<T>(dir.z > T(0) ? sky : ground);
     }
+    V3<T> image(const V3<T>& dir) const {
+        double c[3];
+        env_image_at(*img, (double)dir.x, (double)dir.y, (double)dir.z, c);
+        return V3<T>(T(c[0]), T(c[1]), T(c[2]));
+    }
+    // envMapSample / envMapPdf (envmap.js:54-98): a row down column 0's CDF, a column along the row's, a point uniform
+    // in (azimuth, z) inside the texel
+    V3<T> map_sample(T ux, T uy) const {
+        const std::vector<float>& m = img->tex;
+        auto at = [&](int x, int y, int c) { return (T)m[4 * ((size_t)y * ENV_MW + x) + c]; };
+        int lo = 0, hi = ENV_MH - 1;
+        while (lo < hi) { int mid = (lo + hi) / 2; if (ux < at(0, mid, 2)) hi = mid; else lo = mid + 1; }
+        const int row = lo;
+        const T r0 = row > 0 ? at(0, row - 1, 2) : T(0), r1 = at(0, row, 2);
+        const T fy = std::min(std::max((ux - r0) / std::max(r1 - r0, T(1e-12)), T(0)), T(0.999999));
+        lo = 0; hi = ENV_MW - 1;
+        while (lo < hi) { int mid = (lo + hi) / 2; if (uy < at(mid, row, 0)) hi = mid; else lo = mid + 1; }
+        const int col = lo;
+        const T c0 = col > 0 ? at(col - 1, row, 0) : T(0), c1 = at(col, row, 0);
+        const T fx = std::min(std::max((uy - c0) / std::max(c1 - c0, T(1e-12)), T(0)), T(0.999999));
+        const T z = T(1) - T(2) * (T(row) + fy) / T(ENV_MH);
+        const T phi = T(2) * T(PI_D) * (T(col) + fx) / T(ENV_MW);
+        const T sz = std::sqrt(std::max(T(0), T(1) - z * z));
+        return V3<T>(sz * std::cos(phi), sz * std::sin(phi), z);
+    }
+    T map_pdf(const V3<T>& L) const {
+        const V3<T> d = normalize(L);
+        T a = std::atan2(d.y, d.x) / (T(2) * T(PI_D));
+        a -= std::floor(a);
+        const int col = std::min(std::max((int)(a * T(ENV_MW)), 0), ENV_MW - 1);
+        const int row = std::min(std::max((int)((T(1) - d.z) * T(0.5) * T(ENV_MH)), 0), ENV_MH - 1);
+        return (T)img->tex[4 * ((size_t)row * ENV_MW + col) + 1];
+    }
     V3<T> base(const V3<T>& dir) const {                             // sdf.js:121-130 envBase
+        if (img) return image(dir);
         if (uniform > T(0)) return V3<T>(uniform);
         V3<T> c = background(normalize(dir));
         return vmax(c, T(0));
@@ -243,12 +337,14 @@ template <class T> inline V3<T> sample_cosine_hemi(const V3<T>& n, T u0, T u1) {
 // envSampleDir / envPdf (tracebasics.js:670-692), no environment map (envMapShare 0)
 template <class T> inline V3<T> env_sample_dir(const Env<T>& e, const V3<T>& n, T pick, T u0, T u1) {
     if (pick < e.pick) return e.sample_sun_cone(u0, u1);
+    if (e.mshare > T(0) && (pick - e.pick) / std::max(T(1) - e.pick, T(1e-6)) < e.mshare) return e.map_sample(u0, u1);
     return sample_cosine_hemi(n, u0, u1);
 }
 template <class T> inline T env_pdf(const Env<T>& e, const V3<T>& L, const V3<T>& n) {
     T pSun = e.in_sun_disc(L) ? T(1) / e.sun_omega : T(0);
     T pCos = std::max(dot(L, n), T(0)) / T(PI_D);
-    return e.pick * pSun + (T(1) - e.pick) * pCos;
+    const T pm = e.mshare > T(0) ? e.mshare * e.map_pdf(L) : T(0);
+    return e.pick * pSun + (T(1) - e.pick) * (pm + (T(1) - e.mshare) * pCos);
 }
 // power heuristic (tracebasics.js:695-699)
 template <class T> inline T mis_weight(T a, T b) { T a2 = a * a, b2 = b * b; return a2 / std::max(a2 + b2, T(1e-20)); }

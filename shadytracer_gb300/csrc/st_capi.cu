@@ -43,6 +43,10 @@ struct st_ctx {
     DPrim* d_prims = nullptr;
     float4* d_faces = nullptr;            // the lights' faces (FACE_F4 float4s each), then the material -> face map
     uint32_t n_faces = 0;
+    float4* d_envimg = nullptr;           // the environment image (rgb, 0) and its map's tables; null, none
+    float4* d_envmap = nullptr;
+    uint32_t env_w = 0, env_h = 0;
+    float env_lum = 0.f, env_turn = 0.f;
     st_material* d_mats = nullptr;
     st_params params{};
     st_view view{};
@@ -180,7 +184,8 @@ static Uni make_uni(const st_ctx* ctx) {
     const double raw[3] = {1.0, 0.96, 0.9};
     double y = raw[0] * 0.2126 + raw[1] * 0.7152 + raw[2] * 0.0722;
     bool furnace = p.env_uniform > 0;
-    int sun_on = (p.sun_hint != 0 && p.sun_elevation * PI_D / 180.0 + half > 0 && !furnace) ? 1 : 0;
+    // an environment image is the whole environment, with no sun to aim at (envimage.js, the image preset)
+    int sun_on = (p.sun_hint != 0 && p.sun_elevation * PI_D / 180.0 + half > 0 && !furnace && !ctx->d_envimg) ? 1 : 0;
     double e = p.sun_elevation * PI_D / 180.0, az = p.sun_azimuth * PI_D / 180.0;
     u.sun_dir = mk((float)(std::cos(e) * std::sin(az)), (float)(std::cos(e) * std::cos(az)), (float)std::sin(e));
     u.sun_sin2 = (float)sin2;
@@ -191,6 +196,12 @@ static Uni make_uni(const st_ctx* ctx) {
     u.disc = mk((float)(disc * raw[0] / y), (float)(disc * raw[1] / y), (float)(disc * raw[2] / y));
     u.sky = p.sky_luminance; u.ground = p.ground_luminance; u.uniform = p.env_uniform;
     u.sun_gain = std::max(0.f, p.env_sun_gain); u.sky_gain = std::max(0.f, p.env_sky_gain);
+    if (ctx->d_envimg) {
+        u.env_img = ctx->d_envimg; u.env_w = ctx->env_w; u.env_h = ctx->env_h;
+        u.env_lum = ctx->env_lum; u.env_turn = ctx->env_turn;
+        u.env_map = ctx->d_envmap;
+        u.env_mshare = ctx->d_envmap && !p.env_map_off ? 0.5f : 0.f;    // ENV_MAP_SHARE
+    }
     u.haze_on = s.haze_sigma_t > 0 ? 1 : 0;
     u.hc = mk(s.haze_centre[0], s.haze_centre[1], s.haze_centre[2]);
     u.hu = mk(s.haze_axes[0], s.haze_axes[1], s.haze_axes[2]);
@@ -636,7 +647,7 @@ int st_destroy(st_ctx* ctx) {
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     free_wave(ctx);
     ext_free(ctx->ext);
-    for (void* p : {(void*)ctx->d_prims, (void*)ctx->d_faces, (void*)ctx->d_mats, (void*)ctx->d_ec, (void*)ctx->d_ecavg,
+    for (void* p : {(void*)ctx->d_prims, (void*)ctx->d_faces, (void*)ctx->d_envimg, (void*)ctx->d_envmap, (void*)ctx->d_mats, (void*)ctx->d_ec, (void*)ctx->d_ecavg,
                     (void*)ctx->d_e1, (void*)ctx->d_ctr, (void*)ctx->d_spec})
         if (p) cudaFree(p);
     for (auto& pe : ctx->pending) { cudaEventDestroy(pe.a); cudaEventDestroy(pe.b); }
@@ -738,6 +749,88 @@ int st_set_params(st_ctx* ctx, const st_params* p, uint64_t* unknown_mask) {
         if (rc) return rc;
     }
     return st_invalidate(ctx);
+}
+
+// envSampling (envmap.js:215-260): each texel's weight its luminance (non-finite or negative: 0) plus a floor of
+// 1e-3 of the mean (1 in a black environment: a uniform map), then the CDFs along each row and down the rows, and
+// each texel's density per steradian, its share of the total times the texels a steradian
+int st_env_map_tables(const float* lum, float* tex) {
+    if (!lum || !tex) return ST_ERR_ARG;
+    const int W = ENV_MW, H = ENV_MH, N = W * H;
+    auto ok = [](float x) { return (x > 0.f && std::isfinite(x)) ? (double)x : 0.0; };
+    double sum = 0.0;
+    for (int i = 0; i < N; i++) sum += ok(lum[i]);
+    const double mean = sum / N;
+    const double floor_w = mean > 0.0 ? 1e-3 * mean : 1.0;
+    std::vector<double> w(N);
+    double total = 0.0;
+    for (int i = 0; i < N; i++) { w[i] = ok(lum[i]) + floor_w; total += w[i]; }
+    const double density = N / (4.0 * PI_D);
+    double below = 0.0;
+    for (int row = 0; row < H; row++) {
+        double rowSum = 0.0;
+        for (int x = 0; x < W; x++) rowSum += w[row * W + x];
+        const double rowCdf = row == H - 1 ? 1.0 : (below + rowSum) / total;
+        double along = 0.0;
+        for (int x = 0; x < W; x++) {
+            const int i = row * W + x;
+            along += w[i];
+            tex[4 * i] = x == W - 1 ? 1.f : (float)(along / rowSum);
+            tex[4 * i + 1] = (float)(w[i] / total * density);
+            tex[4 * i + 2] = (float)rowCdf;
+            tex[4 * i + 3] = 0.f;
+        }
+        below += rowSum;
+    }
+    return ST_OK;
+}
+
+int st_set_env_image(st_ctx* ctx, const float* rgb, uint32_t w, uint32_t h, float luminance, float turn_deg) {
+    if (!ctx) return ST_ERR_ARG;
+    if (ctx->in_flight) return fail(ctx, ST_ERR_BUSY, "a trace is in flight: st_sync first");
+    cudaSetDevice(ctx->device);
+    if (!rgb) {                                           // back to the sun and sky
+        if (ctx->d_envimg) cudaFree(ctx->d_envimg);
+        if (ctx->d_envmap) cudaFree(ctx->d_envmap);
+        ctx->d_envimg = ctx->d_envmap = nullptr;
+        ctx->env_w = ctx->env_h = 0;
+        invalidate_graph(ctx);
+        return ctx->has_params ? st_invalidate(ctx) : ST_OK;
+    }
+    if (w < 2 || h < 1 || w > 16384 || h > 8192) return fail(ctx, ST_ERR_ARG, "environment image size out of range");
+    if (!(luminance >= 0.f) || !std::isfinite(turn_deg)) return fail(ctx, ST_ERR_ARG, "bad luminance or turn");
+    std::vector<float4> px((size_t)w * h);
+    for (size_t i = 0; i < px.size(); i++) {
+        float c[3];
+        for (int k = 0; k < 3; k++) c[k] = std::isfinite(rgb[3 * i + k]) ? rgb[3 * i + k] : 0.f;
+        px[i] = make_float4(c[0], c[1], c[2], 0.f);
+    }
+    if (ctx->d_envimg && (size_t)ctx->env_w * ctx->env_h < px.size()) { cudaFree(ctx->d_envimg); ctx->d_envimg = nullptr; }
+    if (!ctx->d_envimg) CK(cudaMalloc(&ctx->d_envimg, px.size() * sizeof(float4)), "cudaMalloc environment image");
+    CK(cudaMemcpyAsync(ctx->d_envimg, px.data(), px.size() * sizeof(float4), cudaMemcpyHostToDevice, ctx->stream),
+       "environment image upload");
+    ctx->env_w = w; ctx->env_h = h;
+    ctx->env_lum = luminance > 0.f ? luminance : 179.f;
+    ctx->env_turn = turn_deg;
+    if (ctx->d_envmap) { cudaFree(ctx->d_envmap); ctx->d_envmap = nullptr; }
+    // the map: baked on the GPU from the image as the environment returns it, tabulated here
+    Uni u = make_uni(ctx);
+    float* d_lum = nullptr;
+    CK(cudaMalloc(&d_lum, (size_t)ENV_MW * ENV_MH * sizeof(float)), "cudaMalloc environment bake");
+    std::vector<float> lum((size_t)ENV_MW * ENV_MH);
+    cudaError_t e = launch_env_bake(u, d_lum, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(lum.data(), d_lum, lum.size() * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    cudaFree(d_lum);
+    if (e != cudaSuccess) return fail(ctx, ST_ERR_CUDA, std::string("environment bake: ") + cudaGetErrorString(e));
+    std::vector<float> tex(lum.size() * 4);
+    st_env_map_tables(lum.data(), tex.data());
+    CK(cudaMalloc(&ctx->d_envmap, tex.size() * sizeof(float)), "cudaMalloc environment map");
+    CK(cudaMemcpyAsync(ctx->d_envmap, tex.data(), tex.size() * sizeof(float), cudaMemcpyHostToDevice, ctx->stream),
+       "environment map upload");
+    CK(cudaStreamSynchronize(ctx->stream), "environment map upload");
+    invalidate_graph(ctx);
+    return ctx->has_params ? st_invalidate(ctx) : ST_OK;
 }
 
 int st_set_view(st_ctx* ctx, const st_view* v) {

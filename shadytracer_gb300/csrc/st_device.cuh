@@ -104,6 +104,9 @@ struct Uni {
     // environment (sdf.js:70-160)
     f3 sun_dir; float sun_sin2, sun_omc, sun_omega, pick; int sun_on;
     f3 disc; float sky, ground, uniform, sun_gain, sky_gain;
+    // the environment image (envimage.js) and the map light sampling draws from (envmap.js); null, none
+    const float4* env_img; uint32_t env_w, env_h; float env_lum, env_turn;
+    const float4* env_map; float env_mshare;
     // haze box (haze.js:64-80)
     int haze_on; f3 hc, hu, hv, hw, halb; float hhu, hhv, hhw, hsig, hg;
     // the sample sequence
@@ -397,7 +400,28 @@ __device__ __forceinline__ bool in_sun_disc(const Uni& u, f3 dir) {
     f3 c = cross(L, u.sun_dir);
     return dot(L, u.sun_dir) > 0.f && dot(c, c) <= u.sun_sin2;
 }
+// THE ENVIRONMENT IMAGE in direction dir (envimage.js:33-52 envImage): equirectangular, its middle column +x running
+// right as one turns right, top row straight up, turned env_turn degrees about z; bilinear, wrapping across the seam,
+// clamped at the poles; its own numbers times env_lum (cd/m^2 a unit)
+__device__ __forceinline__ f3 env_image(const Uni& u, f3 dir) {
+    const f3 d = normalize(dir);
+    const int w = (int)u.env_w, h = (int)u.env_h;
+    float a = 0.5f - atan2f(d.y, d.x) * (0.5f / ST_PI) + u.env_turn * (1.f / 360.f);
+    a -= floorf(a);
+    const float uu = a * (float)w - 0.5f;
+    const float vv = acosf(clampf(d.z, -1.f, 1.f)) * (1.f / ST_PI) * (float)h - 0.5f;
+    const float x0 = floorf(uu), y0 = floorf(vv), fx = uu - x0, fy = vv - y0;
+    const int xa = (((int)x0 % w) + w) % w, xb = (xa + 1) % w;
+    const int ya = min(max((int)y0, 0), h - 1), yb = min(max((int)y0 + 1, 0), h - 1);
+    const float4 p00 = __ldg(&u.env_img[(size_t)ya * w + xa]), p01 = __ldg(&u.env_img[(size_t)ya * w + xb]);
+    const float4 p10 = __ldg(&u.env_img[(size_t)yb * w + xa]), p11 = __ldg(&u.env_img[(size_t)yb * w + xb]);
+    const f3 top = mk(p00.x, p00.y, p00.z) * (1.f - fx) + mk(p01.x, p01.y, p01.z) * fx;
+    const f3 bot = mk(p10.x, p10.y, p10.z) * (1.f - fx) + mk(p11.x, p11.y, p11.z) * fx;
+    const f3 c = top * (1.f - fy) + bot * fy;
+    return mk(fmaxf(c.x, 0.f), fmaxf(c.y, 0.f), fmaxf(c.z, 0.f)) * u.env_lum;
+}
 __device__ __forceinline__ f3 env_base(const Uni& u, f3 dir) {
+    if (u.env_img) return env_image(u, dir);
     if (u.uniform > 0.f) return mk(u.uniform);
     f3 d = normalize(dir);
     if (in_sun_disc(u, d)) return u.disc;
@@ -410,7 +434,7 @@ __device__ __forceinline__ f3 env_radiance(const Uni& u, f3 dir) {
 // the environment without the sun's disc (sdf.js skyRadiance): what a path the photon map owns finds there
 __device__ __forceinline__ f3 env_sky(const Uni& u, f3 dir) {
     bool cone = u.sun_on && in_sun_disc(u, dir);
-    f3 base = u.uniform > 0.f ? mk(u.uniform) : mk(normalize(dir).z > 0.f ? u.sky : u.ground);
+    f3 base = u.env_img ? env_image(u, dir) : (u.uniform > 0.f ? mk(u.uniform) : mk(normalize(dir).z > 0.f ? u.sky : u.ground));
     return base * (cone ? u.sun_gain : u.sky_gain);
 }
 // whether the sun's photons were drawn along this line (sdf.js ltCovers): it crosses the square of half width
@@ -446,14 +470,58 @@ __device__ __forceinline__ f3 sample_cosine_hemi(f3 n, float u0, float u1) {
     f3 b2 = cross(n, b1);
     return normalize(b1 * (r * cp) + b2 * (r * sp) + n * sqrtf(fmaxf(0.f, 1.f - u0)));
 }
+// THE MAP OF WHERE THE ENVIRONMENT IS BRIGHT (envmap.js:44-98): ENV_MW x ENV_MH texels of equal solid angle, columns
+// azimuth, rows equal steps of z from straight up; each a float4 of (the CDF along its row at its end, its density
+// per steradian, the CDF down the rows at its row's end, 0). A row by the CDF down column 0, a column by the row's own,
+// a point uniform in (azimuth, z) inside the texel: both numbers pick and then place, no more are drawn.
+#define ENV_MW 512
+#define ENV_MH 256
+__device__ __forceinline__ f3 env_map_sample(const Uni& u, float ux, float uy) {
+    const float4* __restrict__ m = u.env_map;
+    int lo = 0, hi = ENV_MH - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (ux < __ldg(&m[mid * ENV_MW]).z) hi = mid; else lo = mid + 1;
+    }
+    const int row = lo;
+    const float r0 = row > 0 ? __ldg(&m[(row - 1) * ENV_MW]).z : 0.f, r1 = __ldg(&m[row * ENV_MW]).z;
+    const float fy = clampf((ux - r0) / fmaxf(r1 - r0, 1e-12f), 0.f, 0.999999f);
+    lo = 0; hi = ENV_MW - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (uy < __ldg(&m[row * ENV_MW + mid]).x) hi = mid; else lo = mid + 1;
+    }
+    const int col = lo;
+    const float c0 = col > 0 ? __ldg(&m[row * ENV_MW + col - 1]).x : 0.f, c1 = __ldg(&m[row * ENV_MW + col]).x;
+    const float fx = clampf((uy - c0) / fmaxf(c1 - c0, 1e-12f), 0.f, 0.999999f);
+    const float z = 1.f - 2.f * ((float)row + fy) / (float)ENV_MH;
+    const float phi = 2.f * ST_PI * ((float)col + fx) / (float)ENV_MW;
+    const float sz = sqrtf(fmaxf(0.f, 1.f - z * z));
+    float sp, cp;
+    sincosf(phi, &sp, &cp);
+    return mk(sz * cp, sz * sp, z);
+}
+__device__ __forceinline__ float env_map_pdf(const Uni& u, f3 L) {
+    const f3 d = normalize(L);
+    float a = atan2f(d.y, d.x) * (0.5f / ST_PI);
+    a -= floorf(a);
+    const int col = min(max((int)(a * (float)ENV_MW), 0), ENV_MW - 1);
+    const int row = min(max((int)((1.f - d.z) * 0.5f * (float)ENV_MH), 0), ENV_MH - 1);
+    return __ldg(&u.env_map[row * ENV_MW + col]).y;
+}
+// the environment's three strategies (tracebasics.js:686-713): the sun's cone with its pick, of the rest the map with
+// its share (0 with no map), else the cosine lobe -- one number picks all three, rescaled within its step
 __device__ __forceinline__ f3 env_sample_dir(const Uni& u, f3 n, float pick, float u0, float u1) {
     if (pick < u.pick) return sample_sun_cone(u, u0, u1);
+    if (u.env_mshare > 0.f && (pick - u.pick) / fmaxf(1.f - u.pick, 1e-6f) < u.env_mshare) return env_map_sample(u, u0, u1);
     return sample_cosine_hemi(n, u0, u1);
 }
 __device__ __forceinline__ float env_pdf(const Uni& u, f3 L, f3 n) {
     float pSun = in_sun_disc(u, L) ? 1.f / u.sun_omega : 0.f;
     float pCos = fmaxf(dot(L, n), 0.f) / ST_PI;
-    return u.pick * pSun + (1.f - u.pick) * pCos;
+    const float m = u.env_mshare;
+    const float pm = m > 0.f ? m * env_map_pdf(u, L) : 0.f;
+    return u.pick * pSun + (1.f - u.pick) * (pm + (1.f - m) * pCos);
 }
 __device__ __forceinline__ float mis_weight(float a, float b) {
     float a2 = a * a, b2 = b * b;
@@ -462,6 +530,7 @@ __device__ __forceinline__ float mis_weight(float a, float b) {
 // the environment from a point in the air (haze.js:296-310)
 __device__ __forceinline__ f3 env_sample_dir_m(const Uni& u, float pick, float u0, float u1) {
     if (pick < u.pick) return sample_sun_cone(u, u0, u1);
+    if (u.env_mshare > 0.f && (pick - u.pick) / fmaxf(1.f - u.pick, 1e-6f) < u.env_mshare) return env_map_sample(u, u0, u1);
     float z = 1.f - 2.f * u0;
     float s = sqrtf(fmaxf(0.f, 1.f - z * z));
     float sp, cp;
@@ -470,7 +539,9 @@ __device__ __forceinline__ f3 env_sample_dir_m(const Uni& u, float pick, float u
 }
 __device__ __forceinline__ float env_pdf_m(const Uni& u, f3 L) {
     float pSun = in_sun_disc(u, L) ? 1.f / u.sun_omega : 0.f;
-    return u.pick * pSun + (1.f - u.pick) / (4.f * ST_PI);
+    const float m = u.env_mshare;
+    const float pm = m > 0.f ? m * env_map_pdf(u, L) : 0.f;
+    return u.pick * pSun + (1.f - u.pick) * (pm + (1.f - m) / (4.f * ST_PI));
 }
 
 // ------------------------------------------------------------------------------------------------------------

@@ -216,6 +216,7 @@ cudaError_t launch_march(const WaveArgs& a, int cur, int nxt, int last, int sms,
 cudaError_t launch_shade(const WaveArgs& a, int nxt, int side, int last, int sms, cudaStream_t s);
 cudaError_t launch_occlude(const WaveArgs& a, int side, int last, int sms, cudaStream_t s);
 cudaError_t launch_resolve(const WaveArgs& a, cudaStream_t s);
+cudaError_t launch_env_bake(const Uni& u, float* out, cudaStream_t s);
 // the emitter list (st_emit.cu)
 cudaError_t launch_emit_build(const WaveArgs& a, float margin, cudaStream_t s);
 cudaError_t launch_emit_resolve(const WaveArgs& a, int sms, cudaStream_t s);

@@ -1045,6 +1045,29 @@ __global__ void __launch_bounds__(256) k_eval_sdf(const DPrim* __restrict__ pr, 
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
         out[i] = scene_dist(pr, n_prims, mk(pts[3 * i], pts[3 * i + 1], pts[3 * i + 2]));
 }
+// THE MAP'S BAKE (envmap.js:100-150 prog_envbake): one thread a texel of the equal-area map, the environment's own
+// light (no gains) at 2 x 2 stratified points in it, the sun's cone left out where there is one; its mean luminance
+__global__ void __launch_bounds__(256) k_env_bake(Uni u, float* __restrict__ out) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (uint32_t)(ENV_MW * ENV_MH)) return;
+    const float x = (float)(i % ENV_MW), y = (float)(i / ENV_MW);
+    f3 acc = mk(0.f);
+    for (int sy = 0; sy < 2; sy++)
+        for (int sx = 0; sx < 2; sx++) {
+            const float ux = (x + ((float)sx + 0.5f) * 0.5f) / (float)ENV_MW;
+            const float uy = (y + ((float)sy + 0.5f) * 0.5f) / (float)ENV_MH;
+            const float z = 1.f - 2.f * uy, sz = sqrtf(fmaxf(0.f, 1.f - z * z));
+            float sp, cp;
+            sincosf(2.f * ST_PI * ux, &sp, &cp);
+            const f3 d = mk(sz * cp, sz * sp, z);
+            if (!(u.sun_on && in_sun_disc(u, d))) acc = acc + env_base(u, d);
+        }
+    out[i] = luma(acc * 0.25f);
+}
+cudaError_t launch_env_bake(const Uni& u, float* out, cudaStream_t s) {
+    k_env_bake<<<(ENV_MW * ENV_MH + 255) / 256, 256, 0, s>>>(u, out);
+    return cudaGetLastError();
+}
 cudaError_t launch_eval_sdf(const DPrim* prims, uint32_t n_prims, const float* pts, uint32_t n, float* out,
                             cudaStream_t s) {
     k_eval_sdf<<<std::min((n + 255u) / 256u, 4096u), 256, 0, s>>>(prims, n_prims, pts, n, out);

@@ -69,6 +69,21 @@ class PathTracer:
         check(self.L.st_set_view(self.ctx, C.byref(v)), self.ctx, "st_set_view")
         self.view = v
 
+    def set_env_image(self, rgb=None, luminance=0.0, turn=0.0):
+        """The environment as an equirectangular image (envimage.js): `rgb` H x W x 3 linear floats, top row first,
+        `luminance` cd/m^2 a unit (0: 179), turned `turn` degrees about z; None goes back to the sun and sky."""
+        if rgb is None:
+            check(self.L.st_set_env_image(self.ctx, None, 0, 0, 0.0, 0.0), self.ctx, "st_set_env_image")
+            self.env_image = None
+            return
+        img = np.ascontiguousarray(rgb, dtype=np.float32)
+        if img.ndim != 3 or img.shape[2] != 3:
+            raise ValueError("the environment image is H x W x 3")
+        h, w = img.shape[:2]
+        check(self.L.st_set_env_image(self.ctx, img.ctypes.data_as(C.c_void_p), w, h, luminance, turn), self.ctx,
+              "st_set_env_image")
+        self.env_image = (img, luminance, turn)
+
     def set(self, reset=True, **values):
         """RT.set(values): applies the settings it knows, returns the names it does not (README.md:56)."""
         p = T.StParams.from_buffer_copy(self.params) if self.params else T.default_params()

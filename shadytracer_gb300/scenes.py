@@ -593,3 +593,71 @@ def optics_bench(n_instances=64, seed=5, ray_min=1e5, ray_max=1e7, ray_scale=1.0
     s.info = {"sources": srcs, "rays": rays, "lenses": lenses, "nC": 360, "nG": 181, "lux_cells": 512,
               "lux_half": 1.0, "lux_height": 1.0, "workload": "optics-bench-%d" % n_instances}
     return s
+
+
+# ------------------------------------------------------------------------------------------------------------
+# An environment image (core/envimage.js) and the map light sampling draws from it (core/envmap.js).
+# ------------------------------------------------------------------------------------------------------------
+def env_image_lookup(img, dirs, luminance=179.0, turn=0.0):
+    """envImageAt (envimage.js:56-70) for many directions: the equirectangular image `img` (H x W x 3, top row first)
+    looked up bilinearly in each unit direction, wrapping across the seam, clamped at the poles, times `luminance`."""
+    import numpy as np
+    img = np.asarray(img, np.float64)
+    h, w = img.shape[:2]
+    d = np.asarray(dirs, np.float64)
+    d = d / np.linalg.norm(d, axis=-1, keepdims=True)
+    a = 0.5 - np.arctan2(d[..., 1], d[..., 0]) / (2 * np.pi) + turn / 360.0
+    a = a - np.floor(a)
+    u = a * w - 0.5
+    v = np.arccos(np.clip(d[..., 2], -1, 1)) / np.pi * h - 0.5
+    x0, y0 = np.floor(u), np.floor(v)
+    fx, fy = (u - x0)[..., None], (v - y0)[..., None]
+    xa = (x0.astype(np.int64) % w + w) % w
+    xb = (xa + 1) % w
+    ya = np.clip(y0.astype(np.int64), 0, h - 1)
+    yb = np.clip(y0.astype(np.int64) + 1, 0, h - 1)
+    top = img[ya, xa] * (1 - fx) + img[ya, xb] * fx
+    bot = img[yb, xa] * (1 - fx) + img[yb, xb] * fx
+    return np.maximum(top * (1 - fy) + bot * fy, 0.0) * luminance
+
+
+def env_patch_image(w=256, h=128, background=1.0, patch=2000.0, row=40, col=100, size=6):
+    """A dim uniform panorama with one bright square patch `size` pixels across, its top-left pixel at (row, col)."""
+    import numpy as np
+    img = np.full((h, w, 3), background, np.float32)
+    img[row:row + size, col:col + size] = patch
+    return img
+
+
+def env_level_illuminance(img, luminance=179.0, turn=0.0, n=2048):
+    """What the image puts on a level surface facing up: the integral of L cos over the upper hemisphere, by an
+    equal-area midpoint grid of n x n/2 cells over the sphere (rows of equal steps in z)."""
+    import numpy as np
+    W, H = n, n // 2
+    z = 1 - 2 * (np.arange(H) + 0.5) / H
+    phi = 2 * np.pi * (np.arange(W) + 0.5) / W
+    Z, PH = np.meshgrid(z[z > 0], phi, indexing="ij")
+    S = np.sqrt(1 - Z * Z)
+    d = np.stack([S * np.cos(PH), S * np.sin(PH), Z], -1)
+    L = env_image_lookup(img, d, luminance, turn) @ np.array([0.2126, 0.7152, 0.0722])
+    return float((L * Z).sum() * 4 * np.pi / (W * H))
+
+
+def env_floor(width=32, height=32, albedo=0.8, maxbounce=2, seed=1):
+    """A Lambertian floor (albedo 0.8) under whatever environment is set, seen straight down by an orthographic camera
+    over 2 x 2 m: every pixel reads albedo / pi times the illuminance the environment's upper half puts on it."""
+    s = Scene([prim(ST_PRIM_PLANE, material=1)], [air(), diffuse((albedo, albedo, albedo))], env_radius=20.0,
+              name="env-floor")
+    s.params = default_params(width=width, height=height, maxbounce=maxbounce, sun_hint=0, sun_illuminance=0.0,
+                              sky_luminance=0.0, ground_luminance=0.0, seed=seed)
+    v = StView()
+    for i, c in enumerate((0.0, 0.0, 3.0)):
+        v.cam_pos[i] = c
+    for i in range(3):
+        v.right[i] = (1.0, 0.0, 0.0)[i]
+        v.up[i] = (0.0, 1.0, 0.0)[i]
+        v.fwd[i] = (0.0, 0.0, 1.0)[i]
+    v.fx, v.fy, v.camtype = 1.0, 1.0, 1
+    s.view = v
+    s.info = {"workload": "env-floor", "albedo": albedo}
+    return s

@@ -71,7 +71,8 @@ class StParams(C.Structure):
                 ("sppm_alpha", C.c_float), ("sppm_half", C.c_float), ("sppm_learn", C.c_uint32),
                 ("guide", C.c_uint32), ("guide_alpha", C.c_float), ("guide_lr", C.c_float),
                 ("guide_train", C.c_uint32), ("guide_seed", C.c_uint32),
-                ("emit_share", C.c_float), ("emit_radius", C.c_float), ("emit_off", C.c_uint32)]
+                ("emit_share", C.c_float), ("emit_radius", C.c_float), ("emit_off", C.c_uint32),
+                ("env_map_off", C.c_uint32)]
 
 
 class StView(C.Structure):
