@@ -6,7 +6,7 @@ window; 1920 x 1080, 64 samples per pixel, max depth 8, march tolerance 1e-4 m, 
 the whole render -- 64 samples of every pixel, 132.7 M camera paths -- folded into the FP64 accumulation.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference] [--small] [--spp S]
-                    [--leg sppm|rmse|optics|mlp|emit|haze]   # one leg alone, its JSON printed
+                    [--leg sppm|rmse|optics|mlp|emit|haze|env]   # one leg alone, its JSON printed
 
 value: paths / s with the scene resident on the GPU (graph replays; the timed region brackets K renders with a
        synchronize). e2e: the same through the C ABI as a host calls it -- scene, settings and camera uploaded from
@@ -32,6 +32,8 @@ emit: emissive surfaces: a sphere lamp over a floor (its closed form): Mpaths/s 
        and the relative RMSE with and without that light sample at equal samples.
 haze_beam: the haze-box beam (a 10-degree 1000 lm spot, a light face, through 2 x 2 x 4 m of albedo-1 haze;
        1280 x 720, 256 samples, 32 bounces) at each of its nine (sigma_s, g) cells: Mpaths/s per cell and overall.
+env: the environment image's map: a floor under a panorama with one small bright patch (its closed form), the relative
+       RMSE with the map's light samples and with the cosine lobe's alone at equal samples.
 Multi-GPU (torchrun): replicas -- each rank renders the whole workload on its own GPU; value sums the ranks' paths
        over the slowest rank's time (weak scaling). There is no data exchange in the path tracer.
 """
@@ -65,7 +67,8 @@ def parse():
     ap.add_argument("--no-mlp", action="store_true", help="skip the learned proposal's leg")
     ap.add_argument("--no-emit", action="store_true", help="skip the emissive surfaces' leg")
     ap.add_argument("--no-haze", action="store_true", help="skip the haze-box beam's leg")
-    ap.add_argument("--leg", default="all", choices=["all", "sppm", "rmse", "optics", "mlp", "emit", "haze"],
+    ap.add_argument("--no-env", action="store_true", help="skip the environment image's leg")
+    ap.add_argument("--leg", default="all", choices=["all", "sppm", "rmse", "optics", "mlp", "emit", "haze", "env"],
                     help="run one leg alone and print its JSON (profiling runs of the photon map or the optics bench)")
     return ap.parse_args()
 
@@ -493,6 +496,47 @@ def haze_leg(args, dev):
     return out
 
 
+def env_leg(args, dev):
+    """The environment image's map: a Lambertian floor under a panorama that is dim but for one small bright patch
+    (its closed form, albedo / pi times the upper half's illuminance), 256 x 256, 128 samples: camera paths a second
+    and the relative RMSE against the closed form with the map's light samples and with the cosine lobe's alone, at
+    equal samples, and the speed-up to equal error."""
+    import torch
+    from shadytracer_gb300 import scenes
+    from shadytracer_gb300.renderer import create_path_tracer
+    W = 128 if args.small else 256
+    spp = 32 if args.small else 128
+    img = scenes.env_patch_image(patch=20000.0, size=3)
+    cf = 0.8 / np.pi * scenes.env_level_illuminance(img)
+    out = {"workload": "env-floor: 0.8 floor under a 256x128 panorama of 179 cd/m^2 with a 3x3-pixel patch of "
+                       "3.58 Mcd/m^2, %dx%d, %d samples" % (W, W, spp), "metric": "Mpaths/s", "legs": {}}
+    for off in (0, 1):
+        s = scenes.env_floor(width=W, height=W)
+        s.params.env_map_off = off
+        rt = create_path_tracer(s, device=dev)
+        rt.set_env_image(img)
+        stream = torch.cuda.ExternalStream(rt.stream(), device=torch.device("cuda", dev))
+        for _ in range(max(args.warmup, 3)):
+            rt.invalidate()
+            rt.step(spp)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        rt.invalidate()
+        e0.record(stream)
+        rt.step_async(spp)
+        e1.record(stream)
+        rt.sync()
+        ms = e0.elapsed_time(e1)
+        L = rt.read_accum()[0] @ np.array([0.2126, 0.7152, 0.0722])
+        out["legs"]["lobe_only" if off else "map"] = {
+            "ms": ms, "Mpaths_per_s": W * W * spp / (ms / 1e3) / 1e6,
+            "rmse": float(np.sqrt(np.mean((L - cf) ** 2)) / cf), "mean_over_closed_form": float(L.mean() / cf)}
+        rt.close()
+    a, b = out["legs"]["map"], out["legs"]["lobe_only"]
+    out["value"] = a["Mpaths_per_s"]
+    out["speedup_to_equal_rmse"] = (b["rmse"] / a["rmse"]) ** 2 * (b["ms"] / a["ms"])
+    return out
+
+
 def rmse_leg(args, dev):
     """Time to 1 % relative RMSE against the closed form, guided vs plain: the photon map's pane (a 0.5 m glass pane
     over a floor lit only through it, the sun's photons drawn over a 4 m square), plain -- the photons uniform over the
@@ -551,7 +595,8 @@ def run_ours(args):
         with_cpu = rank == 0 and world == 1 and not args.no_cpu
         out = {"sppm": lambda: sppm_leg(args, dev, with_cpu), "rmse": lambda: rmse_leg(args, dev),
                "optics": lambda: optics_leg(args, dev, with_cpu), "mlp": lambda: mlp_leg(args, dev),
-               "emit": lambda: emit_leg(args, dev), "haze": lambda: haze_leg(args, dev)}[args.leg]()
+               "emit": lambda: emit_leg(args, dev), "haze": lambda: haze_leg(args, dev),
+               "env": lambda: env_leg(args, dev)}[args.leg]()
         if rank == 0:
             print(json.dumps(out), flush=True)
         return 0
@@ -714,6 +759,8 @@ def run_ours(args):
         line["emit"] = emit_leg(args, dev)
     if not args.no_haze:
         line["haze_beam"] = haze_leg(args, dev)
+    if not args.no_env:
+        line["env"] = env_leg(args, dev)
     if not args.no_optics:
         line["optics"] = optics_leg(args, dev, rank == 0 and world == 1 and not args.no_cpu)
         if world > 1:
