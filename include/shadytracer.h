@@ -105,6 +105,9 @@ typedef struct st_material {
     float beam_cos;       /* an emitter's beam (builder/lights.js beamShape, the cone of a cosine light): > 0,
                            * the cosine of its half angle -- the emission, emissive straight out, only within that
                            * cone about the surface's outward normal; 0, a glowing surface, the same every way   */
+    float haze;           /* of what transmission passes, the share diffused through rather than refracted
+                           * (materials.js Material2.haze): 0 clear, 1 an opal face                              */
+    float pad[3];         /* 80 bytes                                                                 */
 } st_material;
 
 /* A LIGHT'S FACE (builder/lights.js, the builder's light object; core/scene_api.js:259-289 LightFace,

@@ -456,7 +456,8 @@ inline void shade_hit(const Ctx<T>& C, Ray<T>& r, T dhit, Rng& rng, Rng& grng, b
     // the eye, on an evaluable surface, takes sum f Phi / (pi r^2) / n^2 into its radiance
     if (C.sppm && (r.bounces == 0 || r.lens == 1) && !(max3(emis) > T(0)) && sppm_evaluable(m, true)) {
         T n0g = r.n;
-        Lobes<T> lg = make_lobes(nrm, -r.dir, m, n0g / std::max(T(m.ior), n0g), C.tb, T(m.transmission), T(m.specular));
+        Lobes<T> lg = make_lobes(nrm, -r.dir, m, n0g / std::max(T(m.ior), n0g), C.tb, T(m.transmission), T(m.specular),
+                                 T(m.haze));
         V3<T> L = sppm_gather_lobes(C, r.pos, nrm, lg, r.bounces + 1, grng) * T(C.sp_inv_area / ((double)n0g * n0g));
         r.rad += r.beta * L;
     }
@@ -509,17 +510,24 @@ inline void shade_hit(const Ctx<T>& C, Ray<T>& r, T dhit, Rng& rng, Rng& grng, b
     }
     // A FACE THAT BOTH REFRACTS AND DIFFUSES, SEEN FROM INSIDE (materials_pbr.js:1150-1165): one part drawn
     T pG = refract_share<T>(m);
-    T trans = T(m.transmission), specv = T(m.specular);
-    bool diffFace = false;
+    T trans = T(m.transmission), specv = T(m.specular), hz = T(m.haze);
+    bool diffFace = pG <= T(0) && m.transmission > 0.f;                          // haze 1: the diffuse face alone
     if (inside && pG > T(0) && pG < T(1)) {
         T k = mixT(T(2) * T(m.specular), T(1), pG);
         T u4[4]; rng.next4(u4);
-        if (u4[0] < pG) { trans = T(1); }
-        else { trans = T(0); specv = T(0.5) * k; diffFace = true; }
+        if (u4[0] < pG) { trans = T(1); hz = T(0); }
+        else {
+            trans = sat(sat(T(m.transmission)) * sat(T(m.haze)) / std::max(T(1) - pG, T(1e-6)));
+            hz = T(1); specv = T(0.5) * k; diffFace = true;
+        }
     }
     T etaFace = diffFace ? std::min(n0, n1) / std::max(n0, n1) : n0 / n1;
-    Lobes<T> lb = make_lobes(nrm, -r.dir, m, etaFace, C.tb, trans, specv);
+    Lobes<T> lb = make_lobes(nrm, -r.dir, m, etaFace, C.tb, trans, specv, hz);
     lb.etaT = n0 / nT;
+    // THE SIDE BEYOND, LIT (materials_pbr.js:1176-1190): through this face where the medium beyond is air
+    const bool throughLit = std::fabs(n1 - T(1)) <= T(1e-3) && through_evaluable<T>(m, trans, hz);
+    lb.through = throughLit;
+    const T qf = throughLit ? T(1) : T(0);
 
     // LIGHT SAMPLING (materials_pbr.js:1196-1330): the lights' faces with their share (lightFaceShare), then of the
     // rest the discovered emitters with theirs (0 while nothing is listed), else the environment -- with no face and
@@ -532,7 +540,7 @@ inline void shade_hit(const Ctx<T>& C, Ray<T>& r, T dhit, Rng& rng, Rng& grng, b
         T u0[4], u1[4];
         rng.next4(u0);                                                             // pick00
         rng.next4(u1);                                                             // uL
-        if (!lobes_none<T>(m, trans)) {
+        if (!lobes_none<T>(m, trans, hz)) {
             V3<T> L(0, 0, 1);
             T pS = 0, fdist = 0;
             bool toEmit = false, toFace = false;
@@ -549,8 +557,9 @@ inline void shade_hit(const Ctx<T>& C, Ray<T>& r, T dhit, Rng& rng, Rng& grng, b
                 const T cosY = -(L.x * T(f.n[0]) + L.y * T(f.n[1]) + L.z * T(f.n[2]));
                 if (fdist > T(0) && cosY > T(1e-6)) {
                     pS = T(face_density((double)fs, nf, f, (double)fdist, (double)cosY));
+                    const T nSide = dot(nrm, L) < T(0) ? n1 : r.n;                       // the far side's is air
                     fle = V3<T>(T(f.le[0]), T(f.le[1]), T(f.le[2])) *
-                          (T(face_beam(f, (double)cosY)) / std::max(r.n * r.n, T(1)));
+                          (T(face_beam(f, (double)cosY)) / std::max(nSide * nSide, T(1)));
                     toFace = true;
                 }
             } else if (pick0 < es) {
@@ -561,34 +570,35 @@ inline void shade_hit(const Ctx<T>& C, Ray<T>& r, T dhit, Rng& rng, Rng& grng, b
                 }
             } else {
                 T pick = es > T(0) ? (pick0 - es) / (T(1) - es) : pick0;
-                L = env_sample_dir(C.env, nrm, pick, u1[0], u1[1]);
-                pS = rs * (T(1) - es) * env_pdf(C.env, L, nrm);
+                L = env_sample_dir_q(C.env, nrm, pick, u1[0], u1[1], qf);
+                pS = rs * (T(1) - es) * env_pdf_q(C.env, L, nrm, qf);
             }
             T NoL = dot(nrm, L);
-            if (NoL > T(0) && pS > T(0)) {
+            if ((NoL > T(0) || (throughLit && NoL < T(0))) && pS > T(0)) {              // sideLit
                 V3<T> le = toEmit ? V3<T>(1, 1, 1) : (toFace ? fle : C.env.radiance(L));
                 V3<T> f = lobes_eval(lb, L, T(0));
                 T pB = lobes_pdf(lb, L);
                 T w = mis_weight(pS, pB);
                 V3<T> contrib = r.beta * f * le * (std::fabs(NoL) * (w / pS));
                 if (max3(contrib) > (toEmit ? T(1e-9) : T(1e-7))) {
-                    V3<T> o = r.pos + nrm * (otol * T(2));
+                    const T nS = NoL < T(0) ? n1 : r.n;                                // the medium the ray crosses
+                    V3<T> o = r.pos + nrm * (NoL < T(0) ? -otol * T(2) : otol * T(2));
                     T tr = T(1);
-                    const bool air = C.haze.on && std::fabs(r.n - T(1)) <= T(1e-3);
+                    const bool air = C.haze.on && std::fabs(nS - T(1)) <= T(1e-3);
                     T R = T(C.d.env_radius);
                     if (toFace) {
                         // the face's ray aims at the point and arrives just short of it (TAG_FNEE)
                         if (air) tr = C.haze.transmittance(r.pos, L, fdist, R);
-                        const T l0 = -std::max(fdist - T(40) * march_tol(o, C.tol), T(0)) * r.n;
-                        if (occlude(C, o, L, r.n, st, (V3<T>*)nullptr, (T*)nullptr, true, l0)) deposit(fr, r.pix, contrib * tr, st);
+                        const T l0 = -std::max(fdist - T(40) * march_tol(o, C.tol), T(0)) * nS;
+                        if (occlude(C, o, L, nS, st, (V3<T>*)nullptr, (T*)nullptr, true, l0)) deposit(fr, r.pix, contrib * tr, st);
                     } else if (!toEmit) {
                         if (air) tr = C.haze.transmittance(r.pos, L, T(2) * R + length(r.pos), R);   // haze.js:472-485
-                        if (occlude(C, o, L, r.n, st)) deposit(fr, r.pix, contrib * tr, st);
+                        if (occlude(C, o, L, nS, st)) deposit(fr, r.pix, contrib * tr, st);
                     } else {
                         // an emitter's ray counts the emission of whatever it stops at (wavefront.js:1694-1749)
                         V3<T> hp;
                         T hl = 0;
-                        if (!occlude(C, o, L, r.n, st, &hp, &hl)) {
+                        if (!occlude(C, o, L, nS, st, &hp, &hl)) {
                             SceneHit<T> hh = scene_eval(*C.s, hp);
                             const st_material& me = C.s->materials[std::min(hh.m, C.s->n_materials - 1)];
                             V3<T> ee(T(me.emissive[0]), T(me.emissive[1]), T(me.emissive[2]));
@@ -597,7 +607,7 @@ inline void shade_hit(const Ctx<T>& C, Ray<T>& r, T dhit, Rng& rng, Rng& grng, b
                                 if (!(-dot(L, nh) >= T(me.beam_cos))) ee = V3<T>(0, 0, 0);
                             }
                             if (max3(ee) > T(0)) {
-                                if (air) tr = C.haze.transmittance(o, L, std::max(hl, T(0)) / std::max(r.n, T(1e-4)), R);
+                                if (air) tr = C.haze.transmittance(o, L, std::max(hl, T(0)) / std::max(nS, T(1e-4)), R);
                                 deposit(fr, r.pix, contrib * ee * tr, st);
                             }
                         }
@@ -619,13 +629,14 @@ inline void shade_hit(const Ctx<T>& C, Ray<T>& r, T dhit, Rng& rng, Rng& grng, b
     if (max3(smp.w) <= T(0)) r.state = RAY_ABSORBED;
     bool misOut = C.p.nee != 0 && !last;
     if (misOut) {                                                                  // materials_pbr.js:1370-1395
-        bool above = dot(nrm, r.dir) > T(0) && !smp.isDelta;
+        const T cO = dot(nrm, r.dir);
+        bool above = (cO > T(0) || (throughLit && cO < T(0))) && !smp.isDelta;      // sideLit
         T pOut = smp.isDelta ? T(0) : lobes_pdf(lb, smp.dir);
-        T pLout = above ? rs * (T(1) - es) * env_pdf(C.env, r.dir, nrm) : T(0);
+        T pLout = above ? rs * (T(1) - es) * env_pdf_q(C.env, r.dir, nrm, qf) : T(0);
         r.sunmis = pLout <= T(0) ? T(1) : mis_weight(pOut, pLout);
         const T pEout = (above && es > T(0)) ? rs * es * emit_cone_pdf(*C.em, r.pos, r.dir) : T(0);
         r.emw = pEout <= T(0) ? T(1) : mis_weight(pOut, pEout);
-        r.lpx = (above && fs > T(0) && !lobes_none<T>(m, trans)) ? pOut : T(-1);   // prevPdf, for a face it meets
+        r.lpx = (above && fs > T(0) && !lobes_none<T>(m, trans, hz)) ? pOut : T(-1);   // prevPdf, for a face it meets
     } else {
         r.sunmis = T(1);
         r.emw = T(1);
@@ -663,16 +674,19 @@ inline void shade_photon(const Ctx<T>& C, Ray<T>& r, T dhit, Rng& rng) {
         n1 = T(C.s->materials[std::min(mb.a, C.s->n_materials - 1)].ior);
     }
     T pG = refract_share<T>(m);
-    T trans = T(m.transmission), specv = T(m.specular);
-    bool diffFace = false;
+    T trans = T(m.transmission), specv = T(m.specular), hz = T(m.haze);
+    bool diffFace = pG <= T(0) && m.transmission > 0.f;
     if (inside && pG > T(0) && pG < T(1)) {
         T k = mixT(T(2) * T(m.specular), T(1), pG);
         T u4[4]; rng.next4(u4);
-        if (u4[0] < pG) trans = T(1);
-        else { trans = T(0); specv = T(0.5) * k; diffFace = true; }
+        if (u4[0] < pG) { trans = T(1); hz = T(0); }
+        else {
+            trans = sat(sat(T(m.transmission)) * sat(T(m.haze)) / std::max(T(1) - pG, T(1e-6)));
+            hz = T(1); specv = T(0.5) * k; diffFace = true;
+        }
     }
     T etaFace = diffFace ? std::min(n0, n1) / std::max(n0, n1) : n0 / n1;
-    Lobes<T> lb = make_lobes(nrm, -r.dir, m, etaFace, C.tb, trans, specv);
+    Lobes<T> lb = make_lobes(nrm, -r.dir, m, etaFace, C.tb, trans, specv, hz);
     lb.etaT = n0 / n1;
     T ur[4]; rng.next4(ur);
     LobeSample<T> smp = lobes_sample(lb, ur);
@@ -1096,16 +1110,19 @@ void trace_photon(const Ctx<T>& C, U4 ps, uint32_t id, uint32_t N, std::vector<P
             nT = cauchy_n(n1d, v1, lamD);
         }
         T pG = refract_share<T>(m);
-        T trans = T(m.transmission), specv = T(m.specular);
-        bool diffFace = false;
+        T trans = T(m.transmission), specv = T(m.specular), hz = T(m.haze);
+        bool diffFace = pG <= T(0) && m.transmission > 0.f;
         if (inside && pG > T(0) && pG < T(1)) {
             T k = mixT(T(2) * T(m.specular), T(1), pG);
             T u4[4]; rng.next4(u4);
-            if (u4[0] < pG) trans = T(1);
-            else { trans = T(0); specv = T(0.5) * k; diffFace = true; }
+            if (u4[0] < pG) { trans = T(1); hz = T(0); }
+            else {
+                trans = sat(sat(T(m.transmission)) * sat(T(m.haze)) / std::max(T(1) - pG, T(1e-6)));
+                hz = T(1); specv = T(0.5) * k; diffFace = true;
+            }
         }
         T etaFace = diffFace ? std::min(n0, n1) / std::max(n0, n1) : n0 / n1;
-        Lobes<T> lb = make_lobes(nrm, -r.dir, m, etaFace, C.tb, trans, specv);
+        Lobes<T> lb = make_lobes(nrm, -r.dir, m, etaFace, C.tb, trans, specv, hz);
         lb.etaT = n0 / nT;
         T ur[4]; rng.next4(ur);
         LobeSample<T> smp = lobes_sample(lb, ur);

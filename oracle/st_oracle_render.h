@@ -346,6 +346,22 @@ template <class T> inline T env_pdf(const Env<T>& e, const V3<T>& L, const V3<T>
     const T pm = e.mshare > T(0) ? e.mshare * e.map_pdf(L) : T(0);
     return e.pick * pSun + (T(1) - e.pick) * (pm + (T(1) - e.mshare) * pCos);
 }
+// envSampleDirQ / envPdfQ (materials_pbr.js:1089-1105): a share q of the sky's cosine draw from the far hemisphere
+template <class T> inline V3<T> env_sample_dir_q(const Env<T>& e, const V3<T>& n, T pick, T u0, T u1, T q) {
+    if (q <= T(0) || pick < e.pick) return env_sample_dir(e, n, pick, u0, u1);
+    const T rest = (pick - e.pick) / std::max(T(1) - e.pick, T(1e-6));
+    if (rest < e.mshare) return e.map_sample(u0, u1);
+    const T pc = (rest - e.mshare) / std::max(T(1) - e.mshare, T(1e-6));
+    return sample_cosine_hemi(pc < q ? n * T(-1) : n, u0, u1);
+}
+template <class T> inline T env_pdf_q(const Env<T>& e, const V3<T>& L, const V3<T>& n, T q) {
+    if (q <= T(0)) return env_pdf(e, L, n);
+    const T pSun = e.in_sun_disc(L) ? T(1) / e.sun_omega : T(0);
+    const T c = dot(L, n);
+    const T pCos = ((T(1) - q) * std::max(c, T(0)) + q * std::max(-c, T(0))) / T(PI_D);
+    const T pm = e.mshare > T(0) ? e.mshare * e.map_pdf(L) : T(0);
+    return e.pick * pSun + (T(1) - e.pick) * (pm + (T(1) - e.mshare) * pCos);
+}
 // power heuristic (tracebasics.js:695-699)
 template <class T> inline T mis_weight(T a, T b) { T a2 = a * a, b2 = b * b; return a2 / std::max(a2 + b2, T(1e-20)); }
 
@@ -485,14 +501,16 @@ template <class T> inline T mf_e1(const MfTables& tb, T mu, T r) {
 
 // ------------------------------------------------------------------------------------------------------------
 // THE LOBES -- core/materials_pbr.js:164-275 makeLobes, :296-350 lobesEval/lobesPdf, :352-358 interfaceReflectP,
-// :450-596 lobesSample; isotropic, uncoated, no haze share (transl 0): what the hot path's materials use.
+// :450-596 lobesSample; :379-432 THE SIDE BEYOND (the translucent base, rough refraction's value and density below
+// the surface); isotropic, uncoated: what the hot path's materials use.
 // ------------------------------------------------------------------------------------------------------------
 const uint32_t EV_NONE = 0, EV_DELTA = 1, EV_EVAL = 2, EV_OTHER = 3;
 const double LT_MIN_ALPHA = 0.05;
 template <class T> struct Lobes {
     V3<T> tX, tY, nZ, o, base, transTint, coatK, cm, ecO, ecAvg;
-    T a, aMin, r, metallic, trans, eta, etaT, nrel, ps;
+    T a, aMin, r, metallic, trans, transl, eta, etaT, nrel, ps;
     bool isDelta;
+    bool through = false;                   // the side beyond lit: the lobes below the surface evaluated
     const MfTables* tb;
     V3<T> to_local(const V3<T>& w) const { return V3<T>(dot(w, tX), dot(w, tY), dot(w, nZ)); }
     V3<T> to_world(const V3<T>& w) const { return normalize(tX * w.x + tY * w.y + nZ * w.z); }
@@ -500,9 +518,12 @@ template <class T> struct Lobes {
     V3<T> metal_fresnel(T cosI) const { return fresnel_schlick3(cosI, base); }
     V3<T> coat_albedo(const V3<T>& w) const { return vmin(coatK * mf_ec(*tb, w.z, r, nrel), T(1)); }
 };
-template <class T> inline T refract_share(const st_material& m) { return sat(T(m.transmission)); }
+// refractShare (materials.js:123): T (1 - H)
+template <class T> inline T refract_share_of(T transmission, T haze) { return sat(transmission) * (T(1) - sat(haze)); }
+template <class T> inline T refract_share(const st_material& m) { return refract_share_of(T(m.transmission), T(m.haze)); }
 template <class T> inline Lobes<T> make_lobes(const V3<T>& n, const V3<T>& v, const st_material& m, T eta,
-                                              const MfTables* tb, T transmission_override = T(-1), T specular_override = T(-1)) {
+                                              const MfTables* tb, T transmission_override = T(-1), T specular_override = T(-1),
+                                              T haze_override = T(-1)) {
     Lobes<T> lb;
     lb.tb = tb;
     // mtlOrthonormalBasis (materials_pbr.js:13-19)
@@ -518,7 +539,9 @@ template <class T> inline Lobes<T> make_lobes(const V3<T>& n, const V3<T>& v, co
     lb.metallic = sat(T(m.metallic));
     T transm = transmission_override >= T(0) ? transmission_override : T(m.transmission);
     T spec = specular_override >= T(0) ? specular_override : T(m.specular);
-    lb.trans = sat(transm);
+    T hz = haze_override >= T(0) ? haze_override : T(m.haze);
+    lb.trans = refract_share_of(transm, hz);                                   // materials_pbr.js:196-204
+    lb.transl = T(1) - lb.trans > T(1e-6) ? sat(sat(transm) * sat(hz) / std::max(T(1) - lb.trans, T(1e-6))) : T(0);
     lb.base = V3<T>(T(m.base[0]), T(m.base[1]), T(m.base[2]));
     lb.transTint = m.attenuation > 0 ? V3<T>(1) : lb.base;
     T lum = max3(lb.base);
@@ -538,8 +561,10 @@ template <class T> inline Lobes<T> make_lobes(const V3<T>& n, const V3<T>& v, co
     lb.cm = V3<T>(1) + lb.base * (T(1) / std::max(e1, T(1e-3)) - T(1));
     return lb;
 }
+template <class T> inline V3<T> lobes_through_eval(const Lobes<T>& lb, const V3<T>& i, T minAlpha);
 template <class T> inline V3<T> lobes_eval(const Lobes<T>& lb, const V3<T>& l, T minAlpha) {
     V3<T> i = lb.to_local(l);
+    if (lb.through && i.z < T(0)) return lobes_through_eval(lb, i, minAlpha);
     if (i.z <= T(0)) return V3<T>(0);
     V3<T> f(0);
     if (!lb.isDelta && lb.aMin >= minAlpha) {
@@ -549,7 +574,7 @@ template <class T> inline V3<T> lobes_eval(const Lobes<T>& lb, const V3<T>& l, T
         f += lb.cm * lb.metal_fresnel(oh) * (lb.metallic * spec);
         f += lb.coat_fresnel(oh) * ((T(1) - lb.metallic) * spec);
     }
-    T wDiff = (T(1) - lb.metallic) * (T(1) - lb.trans);
+    T wDiff = (T(1) - lb.metallic) * (T(1) - lb.trans) * (T(1) - lb.transl);
     if (wDiff > T(0)) {
         V3<T> ecI = lb.coat_albedo(i);
         V3<T> den = vmax(V3<T>(1) - lb.ecAvg, T(1e-4)) * T(PI_D);
@@ -562,12 +587,50 @@ template <class T> inline T interface_reflect_p(const Lobes<T>& lb, T oh) {
     T den = fh + (T(1) - fh) * lb.trans;
     return den > T(1e-6) ? fh / den : T(1);
 }
+// throughHalf (materials_pbr.js:385-396): the refraction's generalised half vector, turned to the view's side
+template <class T> inline bool through_half(const Lobes<T>& lb, const V3<T>& i, V3<T>& h) {
+    h = (lb.o * lb.etaT + i) * T(-1);
+    const T hl = length(h);
+    if (hl < T(1e-12)) return false;
+    h = h * (T(1) / hl);
+    if (h.z < T(0)) h = h * T(-1);
+    return dot(lb.o, h) > T(0) && dot(i, h) < T(0);
+}
+// lobesThroughEval / lobesThroughPdf (materials_pbr.js:397-432)
+template <class T> inline V3<T> lobes_through_eval(const Lobes<T>& lb, const V3<T>& i, T minAlpha) {
+    const T wd = T(1) - lb.metallic;
+    V3<T> f(0);
+    const T wT = wd * (T(1) - lb.trans) * lb.transl;
+    if (wT > T(0)) {
+        const V3<T> ecI = lb.coat_albedo(V3<T>(i.x, i.y, -i.z));
+        f = lb.base * (V3<T>(1) - lb.ecO) * (V3<T>(1) - ecI) / (vmax(V3<T>(1) - lb.ecAvg, T(1e-4)) * T(PI_D)) * wT;
+    }
+    if (wd <= T(0) || lb.trans <= T(0) || lb.isDelta || lb.aMin < minAlpha) return f;
+    V3<T> h;
+    if (!through_half(lb, i, h)) return f;
+    const T oh = dot(lb.o, h), ih = dot(i, h), den = lb.etaT * oh + ih;
+    const V3<T> fc = lb.coat_fresnel(oh);
+    return f + (V3<T>(1) - fc) * lb.transTint *
+               (wd * lb.trans * mf_d(h, lb.a) * mf_g2(lb.o, i, lb.a) * oh * (-ih) / (lb.o.z * (-i.z) * std::max(den * den, T(1e-20))));
+}
+template <class T> inline T lobes_through_pdf(const Lobes<T>& lb, const V3<T>& i) {
+    const T wd = T(1) - lb.metallic;
+    const T pd = (T(1) - lb.ps) * (T(1) - lb.trans);
+    const T p = wd * pd * lb.transl * (-i.z) / T(PI_D);
+    if (wd <= T(0) || lb.trans <= T(0) || lb.isDelta) return p;
+    V3<T> h;
+    if (!through_half(lb, i, h)) return p;
+    const T oh = dot(lb.o, h), ih = dot(i, h), den = lb.etaT * oh + ih;
+    return p + wd * (T(1) - pd) * (T(1) - interface_reflect_p(lb, oh)) * mf_g1(lb.o, lb.a) * mf_d(h, lb.a) * oh / lb.o.z *
+                   (-ih) / std::max(den * den, T(1e-20));
+}
 template <class T> inline T lobes_pdf(const Lobes<T>& lb, const V3<T>& l) {
     V3<T> i = lb.to_local(l);
+    if (lb.through && i.z < T(0)) return lobes_through_pdf(lb, i);
     if (i.z <= T(0)) return T(0);
     T wd = T(1) - lb.metallic;
     T pd = (T(1) - lb.ps) * (T(1) - lb.trans);
-    T p = wd * pd * i.z / T(PI_D);
+    T p = wd * pd * (T(1) - lb.transl) * i.z / T(PI_D);
     if (!lb.isDelta) {
         T pr = mf_pdf_reflect(lb.o, i, lb.a);
         p += (lb.metallic + wd * (T(1) - pd) * interface_reflect_p(lb, dot(lb.o, normalize(lb.o + i)))) * pr;
@@ -575,9 +638,14 @@ template <class T> inline T lobes_pdf(const Lobes<T>& lb, const V3<T>& l) {
     return p;
 }
 // lobesNone (materials_pbr.js:325-328)
-template <class T> inline bool lobes_none(const st_material& m, T transmission) {
+template <class T> inline bool lobes_none(const st_material& m, T transmission, T haze) {
     T r = clampT(T(m.roughness), T(0), T(1));
-    return r * r < T(ALPHA_MIN) && (T(1) - sat(T(m.metallic))) * (T(1) - sat(transmission)) <= T(0);
+    return r * r < T(ALPHA_MIN) && (T(1) - sat(T(m.metallic))) * (T(1) - refract_share_of(transmission, haze)) <= T(0);
+}
+// throughEvaluable (materials_pbr.js:379-384)
+template <class T> inline bool through_evaluable(const st_material& m, T transmission, T haze) {
+    const T r = clampT(T(m.roughness), T(0), T(1)), wd = T(1) - sat(T(m.metallic));
+    return (wd * refract_share_of(transmission, haze) > T(0) && r * r >= T(ALPHA_MIN)) || wd * sat(transmission) * sat(haze) > T(0);
 }
 template <class T> struct LobeSample { V3<T> dir, w; uint32_t ev; bool isDelta, transmitted; };
 template <class T> inline LobeSample<T> lobes_sample(const Lobes<T>& lb, const T rnd[4]) {
@@ -634,10 +702,12 @@ template <class T> inline LobeSample<T> lobes_sample(const Lobes<T>& lb, const T
         } else {                                                                     // diffuse base
             T r = std::sqrt(rnd[1]);
             T phi = T(2) * T(PI_D) * rnd[2];
-            i = V3<T>(r * std::cos(phi), r * std::sin(phi), std::sqrt(std::max(T(0), T(1) - rnd[1])));
+            const T z = std::sqrt(std::max(T(0), T(1) - rnd[1]));
+            i = V3<T>(r * std::cos(phi), r * std::sin(phi), z);
             V3<T> ecI = lb.coat_albedo(i);
             s.w = lb.base * (V3<T>(1) - lb.ecO) * (V3<T>(1) - ecI) / vmax(V3<T>(1) - lb.ecAvg, T(1e-4)) / (T(1) - lb.ps);
             s.ev = EV_EVAL;
+            if (rnd[3] < lb.transl) { i.z = -z; s.transmitted = true; }              // the translucent base (B1)
         }
     }
     s.dir = lb.to_world(i);

@@ -523,6 +523,25 @@ __device__ __forceinline__ float env_pdf(const Uni& u, f3 L, f3 n) {
     const float pm = m > 0.f ? m * env_map_pdf(u, L) : 0.f;
     return u.pick * pSun + (1.f - u.pick) * (pm + (1.f - m) * pCos);
 }
+// ...and with a share q of the sky's cosine draw from the far hemisphere (materials_pbr.js:1089-1105 envSampleDirQ,
+// envPdfQ): at q 0 exactly env_sample_dir and env_pdf
+__device__ __forceinline__ f3 env_sample_dir_q(const Uni& u, f3 n, float pick, float u0, float u1, float q) {
+    if (q <= 0.f || pick < u.pick) return env_sample_dir(u, n, pick, u0, u1);
+    const float rest = (pick - u.pick) / fmaxf(1.f - u.pick, 1e-6f);
+    const float m = u.env_mshare;
+    if (rest < m) return env_map_sample(u, u0, u1);
+    const float pc = (rest - m) / fmaxf(1.f - m, 1e-6f);
+    return sample_cosine_hemi(pc < q ? n * -1.f : n, u0, u1);
+}
+__device__ __forceinline__ float env_pdf_q(const Uni& u, f3 L, f3 n, float q) {
+    if (q <= 0.f) return env_pdf(u, L, n);
+    const float pSun = in_sun_disc(u, L) ? 1.f / u.sun_omega : 0.f;
+    const float c = dot(L, n);
+    const float pCos = ((1.f - q) * fmaxf(c, 0.f) + q * fmaxf(-c, 0.f)) / ST_PI;
+    const float m = u.env_mshare;
+    const float pm = m > 0.f ? m * env_map_pdf(u, L) : 0.f;
+    return u.pick * pSun + (1.f - u.pick) * (pm + (1.f - m) * pCos);
+}
 __device__ __forceinline__ float mis_weight(float a, float b) {
     float a2 = a * a, b2 = b * b;
     return a2 / fmaxf(a2 + b2, 1e-20f);
@@ -696,10 +715,17 @@ __device__ __forceinline__ float mf_e1(const MfTab& t, float mu, float r) {
 #define EV_DELTA 1u
 #define EV_EVAL 2u
 #define EV_OTHER 3u
+// the share of a material's light that refracts (materials.js:123 refractShare): what passes, less what its haze
+// diffuses through instead
+__host__ __device__ __forceinline__ float refract_share_of(float transmission, float haze) {
+    const float t = fminf(fmaxf(transmission, 0.f), 1.f), h = fminf(fmaxf(haze, 0.f), 1.f);
+    return t * (1.f - h);
+}
 struct Lobes {
     f3 tX, tY, nZ, o, base, transTint, coatK, cm, ecO, ecAvg;
-    float a, aMin, r, metallic, trans, eta, etaT, nrel, ps;
+    float a, aMin, r, metallic, trans, transl, eta, etaT, nrel, ps;
     bool isDelta;
+    bool through;      // THE SIDE BEYOND lit (materials_pbr.js:1176-1190): the lobes below the surface evaluated
     __device__ __forceinline__ f3 to_local(f3 w) const { return mk(dot(w, tX), dot(w, tY), dot(w, nZ)); }
     __device__ __forceinline__ f3 to_world(f3 w) const { return normalize(tX * w.x + tY * w.y + nZ * w.z); }
     __device__ __forceinline__ f3 coat_fresnel(float cosI) const { return vmin(coatK * fresnel_dielectric(cosI, eta), 1.f); }
@@ -708,9 +734,11 @@ struct Lobes {
 __device__ __forceinline__ f3 coat_albedo(const Lobes& lb, const MfTab& t, f3 w) {
     return vmin(lb.coatK * mf_ec(t, w.z, lb.r, lb.nrel), 1.f);
 }
+// transm, spec and hz: the material's transmission, specular and haze, or the part of the face drawn from inside
 __device__ __forceinline__ Lobes make_lobes(f3 n, f3 v, const st_material& m, float eta, const MfTab& t,
-                                            float transm, float spec) {
+                                            float transm, float spec, float hz) {
     Lobes lb;
+    lb.through = false;
     f3 s = fabsf(n.z) < 0.999f ? normalize(cross(n, mk(0, 0, 1))) : normalize(cross(n, mk(0, 1, 0)));
     lb.tX = s; lb.tY = cross(s, n); lb.nZ = n;
     lb.o = mk(dot(v, lb.tX), dot(v, lb.tY), fmaxf(dot(v, n), 1e-4f));
@@ -720,7 +748,10 @@ __device__ __forceinline__ Lobes make_lobes(f3 n, f3 v, const st_material& m, fl
     lb.aMin = aIso;
     lb.a = clampf(aIso, MF_ALPHA_MIN, 1.f);
     lb.metallic = sat(m.metallic);
-    lb.trans = sat(transm);
+    // TRANSMISSION AND HAZE (materials_pbr.js:196-204): T (1 - H) refracts; of the diffuse base, the share transl
+    // passes through (T H of the whole)
+    lb.trans = refract_share_of(transm, hz);
+    lb.transl = 1.f - lb.trans > 1e-6f ? sat(sat(transm) * sat(hz) / fmaxf(1.f - lb.trans, 1e-6f)) : 0.f;
     lb.base = mk(m.base[0], m.base[1], m.base[2]);
     lb.transTint = m.attenuation > 0.f ? mk(1.f) : lb.base;
     float lum = max3(lb.base);
@@ -739,8 +770,10 @@ __device__ __forceinline__ Lobes make_lobes(f3 n, f3 v, const st_material& m, fl
     lb.cm = mk(1.f) + lb.base * (1.f / fmaxf(e1, 1e-3f) - 1.f);
     return lb;
 }
+__device__ __forceinline__ f3 lobes_through_eval(const Lobes& lb, const MfTab& t, f3 i, float minAlpha);
 __device__ __forceinline__ f3 lobes_eval(const Lobes& lb, const MfTab& t, f3 l, float minAlpha) {
     f3 i = lb.to_local(l);
+    if (lb.through && i.z < 0.f) return lobes_through_eval(lb, t, i, minAlpha);
     if (i.z <= 0.f) return mk(0.f);
     f3 f = mk(0.f);
     if (!lb.isDelta && lb.aMin >= minAlpha) {
@@ -750,7 +783,7 @@ __device__ __forceinline__ f3 lobes_eval(const Lobes& lb, const MfTab& t, f3 l, 
         f = f + lb.cm * lb.metal_fresnel(oh) * (lb.metallic * spec);
         f = f + lb.coat_fresnel(oh) * ((1.f - lb.metallic) * spec);
     }
-    float wDiff = (1.f - lb.metallic) * (1.f - lb.trans);
+    float wDiff = (1.f - lb.metallic) * (1.f - lb.trans) * (1.f - lb.transl);   // ...less what passes through
     if (wDiff > 0.f) {
         f3 ecI = coat_albedo(lb, t, i);
         f3 den = vmax(mk(1.f) - lb.ecAvg, 1e-4f) * ST_PI;
@@ -763,21 +796,69 @@ __device__ __forceinline__ float interface_reflect_p(const Lobes& lb, float oh) 
     float den = fh + (1.f - fh) * lb.trans;
     return den > 1e-6f ? fh / den : 1.f;
 }
+// THE SIDE BEYOND (materials_pbr.js:385-432): the refraction's generalised half vector turned to the view's side (w 0:
+// none), the translucent base's value below -- the reflected share's form, mirrored -- and rough refraction's, and the
+// sampler's density there
+__device__ __forceinline__ float4 through_half(const Lobes& lb, f3 i) {
+    f3 h = (lb.o * lb.etaT + i) * -1.f;
+    const float hl = length(h);
+    if (hl < 1e-12f) return make_float4(0.f, 0.f, 0.f, 0.f);
+    h = h * (1.f / hl);
+    if (h.z < 0.f) h = h * -1.f;
+    if (dot(lb.o, h) <= 0.f || dot(i, h) >= 0.f) return make_float4(0.f, 0.f, 0.f, 0.f);
+    return make_float4(h.x, h.y, h.z, 1.f);
+}
+__device__ __forceinline__ f3 lobes_through_eval(const Lobes& lb, const MfTab& t, f3 i, float minAlpha) {
+    const float wd = 1.f - lb.metallic;
+    f3 f = mk(0.f);
+    const float wT = wd * (1.f - lb.trans) * lb.transl;
+    if (wT > 0.f) {
+        const f3 ecI = coat_albedo(lb, t, mk(i.x, i.y, -i.z));
+        f = lb.base * (mk(1.f) - lb.ecO) * (mk(1.f) - ecI) / (vmax(mk(1.f) - lb.ecAvg, 1e-4f) * ST_PI) * wT;
+    }
+    if (wd <= 0.f || lb.trans <= 0.f || lb.isDelta || lb.aMin < minAlpha) return f;
+    const float4 hh = through_half(lb, i);
+    if (hh.w == 0.f) return f;
+    const f3 h = mk(hh.x, hh.y, hh.z);
+    const float oh = dot(lb.o, h), ih = dot(i, h), den = lb.etaT * oh + ih;
+    const f3 fc = lb.coat_fresnel(oh);
+    return f + (mk(1.f) - fc) * lb.transTint *
+               (wd * lb.trans * mf_d(h, lb.a) * mf_g2(lb.o, i, lb.a) * oh * (-ih) /
+                (lb.o.z * (-i.z) * fmaxf(den * den, 1e-20f)));
+}
+__device__ __forceinline__ float lobes_through_pdf(const Lobes& lb, f3 i) {
+    const float wd = 1.f - lb.metallic;
+    const float pd = (1.f - lb.ps) * (1.f - lb.trans);
+    const float p = wd * pd * lb.transl * (-i.z) / ST_PI;            // the translucent base's cosine draw
+    if (wd <= 0.f || lb.trans <= 0.f || lb.isDelta) return p;
+    const float4 hh = through_half(lb, i);
+    if (hh.w == 0.f) return p;
+    const f3 h = mk(hh.x, hh.y, hh.z);
+    const float oh = dot(lb.o, h), ih = dot(i, h), den = lb.etaT * oh + ih;
+    return p + wd * (1.f - pd) * (1.f - interface_reflect_p(lb, oh)) * mf_g1(lb.o, lb.a) * mf_d(h, lb.a) * oh / lb.o.z *
+                   (-ih) / fmaxf(den * den, 1e-20f);
+}
 __device__ __forceinline__ float lobes_pdf(const Lobes& lb, f3 l) {
     f3 i = lb.to_local(l);
+    if (lb.through && i.z < 0.f) return lobes_through_pdf(lb, i);
     if (i.z <= 0.f) return 0.f;
     float wd = 1.f - lb.metallic;
     float pd = (1.f - lb.ps) * (1.f - lb.trans);
-    float p = wd * pd * i.z / ST_PI;
+    float p = wd * pd * (1.f - lb.transl) * i.z / ST_PI;
     if (!lb.isDelta) {
         float pr = mf_pdf_reflect(lb.o, i, lb.a);
         p += (lb.metallic + wd * (1.f - pd) * interface_reflect_p(lb, dot(lb.o, normalize(lb.o + i)))) * pr;
     }
     return p;
 }
-__device__ __forceinline__ bool lobes_none(const st_material& m, float transmission) {
+__device__ __forceinline__ bool lobes_none(const st_material& m, float transmission, float hz) {
     float r = clampf(m.roughness, 0.f, 1.f);
-    return r * r < MF_ALPHA_MIN && (1.f - sat(m.metallic)) * (1.f - sat(transmission)) <= 0.f;
+    return r * r < MF_ALPHA_MIN && (1.f - sat(m.metallic)) * (1.f - refract_share_of(transmission, hz)) <= 0.f;
+}
+// a transmission lobe that can be evaluated, from the material (or the part drawn) alone (materials_pbr.js:379-384)
+__device__ __forceinline__ bool through_evaluable(const st_material& m, float transmission, float hz) {
+    const float r = clampf(m.roughness, 0.f, 1.f), wd = 1.f - sat(m.metallic);
+    return (wd * refract_share_of(transmission, hz) > 0.f && r * r >= MF_ALPHA_MIN) || wd * sat(transmission) * sat(hz) > 0.f;
 }
 struct LobeSample { f3 dir, w; uint32_t ev; bool isDelta, transmitted; };
 __device__ __forceinline__ LobeSample lobes_sample(const Lobes& lb, const MfTab& t, float4 rnd) {
@@ -832,13 +913,18 @@ __device__ __forceinline__ LobeSample lobes_sample(const Lobes& lb, const MfTab&
                 }
             }
         } else {
+            // the diffuse base: of it, transl passes through (materials_pbr.js:525-539), a cosine below weighed as the
+            // reflected share's draw is, into the medium beyond as a refraction
             float r = sqrtf(rnd.y);
             float sp, cp;
             sincosf(2.f * ST_PI * rnd.z, &sp, &cp);
-            i = mk(r * cp, r * sp, sqrtf(fmaxf(0.f, 1.f - rnd.y)));
+            const float z = sqrtf(fmaxf(0.f, 1.f - rnd.y));
+            const bool thru = rnd.w < lb.transl;
+            i = mk(r * cp, r * sp, z);
             f3 ecI = coat_albedo(lb, t, i);
             s.w = lb.base * (mk(1.f) - lb.ecO) * (mk(1.f) - ecI) / vmax(mk(1.f) - lb.ecAvg, 1e-4f) / (1.f - lb.ps);
             s.ev = EV_EVAL;
+            if (thru) { i.z = -z; s.transmitted = true; }
         }
     }
     s.dir = lb.to_world(i);

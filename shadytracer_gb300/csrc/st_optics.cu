@@ -215,16 +215,20 @@ __global__ void __launch_bounds__(256) k_opt_shade(OptArgs o, int nxt, int last)
                         SceneHit mb = scene_full(ip, np, pos + (-nrm) * (otol * 2.f));
                         n1 = sm[min(mb.a, u.n_mats - 1)].ior;
                     }
-                    float pG = sat(m.transmission), trans = m.transmission, specv = m.specular;
-                    bool diffFace = false;
+                    float pG = refract_share_of(m.transmission, m.haze), trans = m.transmission, specv = m.specular;
+                    float hz = m.haze;
+                    bool diffFace = pG <= 0.f && m.transmission > 0.f;
                     if (inside && pG > 0.f && pG < 1.f) {
                         float k = mixf(2.f * m.specular, 1.f, pG);
                         float4 r4 = rng.next();
-                        if (r4.x < pG) trans = 1.f;
-                        else { trans = 0.f; specv = 0.5f * k; diffFace = true; }
+                        if (r4.x < pG) { trans = 1.f; hz = 0.f; }
+                        else {
+                            trans = sat(sat(m.transmission) * sat(m.haze) / fmaxf(1.f - pG, 1e-6f));
+                            hz = 1.f; specv = 0.5f * k; diffFace = true;
+                        }
                     }
                     float etaFace = diffFace ? fminf(n0, n1) / fmaxf(n0, n1) : n0 / n1;
-                    Lobes lb = make_lobes(nrm, -dir, m, etaFace, a.tab, trans, specv);
+                    Lobes lb = make_lobes(nrm, -dir, m, etaFace, a.tab, trans, specv, hz);
                     lb.etaT = n0 / n1;
                     LobeSample smp = lobes_sample(lb, a.tab, rng.next());
                     dir = smp.dir;

@@ -241,17 +241,20 @@ __global__ void __launch_bounds__(256) k_photon_shade(WaveArgs a, int nxt, int l
                             spec.lam = lambda_coded(spec.lam);
                             nT = cauchy_n(n1d, v1, spec.lam);
                         }
-                        const float pG = sat(m.transmission);
-                        float trans = m.transmission, specv = m.specular;
-                        bool diffFace = false;
+                        const float pG = refract_share_of(m.transmission, m.haze);
+                        float trans = m.transmission, specv = m.specular, hz = m.haze;
+                        bool diffFace = pG <= 0.f && m.transmission > 0.f;
                         if (inside && pG > 0.f && pG < 1.f) {
                             const float k = mixf(2.f * m.specular, 1.f, pG);
                             const float4 rp = rng.next();
-                            if (rp.x < pG) trans = 1.f;
-                            else { trans = 0.f; specv = 0.5f * k; diffFace = true; }
+                            if (rp.x < pG) { trans = 1.f; hz = 0.f; }
+                            else {
+                                trans = sat(sat(m.transmission) * sat(m.haze) / fmaxf(1.f - pG, 1e-6f));
+                                hz = 1.f; specv = 0.5f * k; diffFace = true;
+                            }
                         }
                         const float etaFace = diffFace ? fminf(n0, n1) / fmaxf(n0, n1) : n0 / n1;
-                        Lobes lb = make_lobes(nrm, -dir, m, etaFace, a.tab, trans, specv);
+                        Lobes lb = make_lobes(nrm, -dir, m, etaFace, a.tab, trans, specv, hz);
                         lb.etaT = n0 / nT;
                         const LobeSample smp = lobes_sample(lb, a.tab, rng.next());
                         dir = smp.dir;
@@ -327,7 +330,6 @@ struct GatherQuery {
     uint32_t side;        // bit k: the neighbour along axis k is on the + side
     uint32_t a0[8];       // each cell's first record
     uint32_t pre[9];      // the records of the cells before each; pre[8] their total
-    uint32_t pad;
 };
 // an odd number of words, so lanes reading one field of 32 different queries meet 32 different banks
 static_assert(sizeof(GatherQuery) % 8 == 4, "GatherQuery: an odd word stride");
@@ -405,7 +407,8 @@ __global__ void __launch_bounds__(256, 2) k_gather(WaveArgs a) {
                     const float4 p4 = a.pb.pos[slot], d4 = a.pb.dir[slot];
                     const f3 x = xyz(p4);
                     const float n0 = d4.w;
-                    g.lb = make_lobes(nrm, -xyz(d4), m, n0 / fmaxf(m.ior, n0), a.tab, m.transmission, m.specular);
+                    g.lb = make_lobes(nrm, -xyz(d4), m, n0 / fmaxf(m.ior, n0), a.tab, m.transmission, m.specular,
+                                      m.haze);
                     g.x = x;
                     g.nrm = nrm;
                     g.scale = inv_area / (n0 * n0);

@@ -488,18 +488,25 @@ __device__ __forceinline__ void shade_surface(const WaveArgs& a, const st_materi
         spec.lam = lambda_coded(spec.lam);
         nT = cauchy_n(n1d, v1, spec.lam);
     }
-    float pG = sat(m.transmission);
-    float trans = m.transmission, specv = m.specular;
-    bool diffFace = false;
-    if (inside && pG > 0.f && pG < 1.f) {                             // materials_pbr.js:1150-1165
+    // a face that both refracts and diffuses, seen from inside (materials_pbr.js:1141-1165): the area mix, one part
+    // drawn -- clear glass with the share that refracts, else the diffuse face, the same surface from either side
+    const float pG = refract_share_of(m.transmission, m.haze);
+    float trans = m.transmission, specv = m.specular, hz = m.haze;
+    bool diffFace = pG <= 0.f && m.transmission > 0.f;               // haze 1: the diffuse face alone
+    if (inside && pG > 0.f && pG < 1.f) {
         float k = mixf(2.f * m.specular, 1.f, pG);
         float4 r4 = rng.next();
-        if (r4.x < pG) trans = 1.f;
-        else { trans = 0.f; specv = 0.5f * k; diffFace = true; }
+        if (r4.x < pG) { trans = 1.f; hz = 0.f; }
+        else { trans = sat(sat(m.transmission) * sat(m.haze) / fmaxf(1.f - pG, 1e-6f)); hz = 1.f; specv = 0.5f * k; diffFace = true; }
     }
     float etaFace = diffFace ? fminf(n0, n1) / fmaxf(n0, n1) : n0 / n1;
-    Lobes lb = make_lobes(nrm, -dir, m, etaFace, a.tab, trans, specv);
+    Lobes lb = make_lobes(nrm, -dir, m, etaFace, a.tab, trans, specv, hz);
     lb.etaT = n0 / nT;
+    // THE SIDE BEYOND, LIT (materials_pbr.js:1176-1190): light sampling may aim through this face where what it
+    // transmits by can be evaluated and the medium beyond is air; the sky's cosine draw then comes from the far side
+    const bool throughLit = fabsf(n1 - 1.f) <= 1e-3f && through_evaluable(m, trans, hz);
+    lb.through = throughLit;
+    const float qf = throughLit ? 1.f : 0.f;
     // THE LEARNED PROPOSAL (st_guide.cuh): at an evaluable opaque vertex met from outside, the direction is drawn from
     // the network's mixture with probability alpha, else from the BSDF, and weighed by f cos / (alpha q + (1 - alpha)
     // p_bsdf) -- one-sample MIS, so the estimator stays unbiased whatever the network says; the environment's MIS
@@ -516,7 +523,7 @@ __device__ __forceinline__ void shade_surface(const WaveArgs& a, const st_materi
     if (u.nee != 0u && !last) {                                       // light sampling (materials_pbr.js:1196-1330)
         float4 u0 = rng.next();
         float4 u1 = rng.next();
-        if (!lobes_none(m, trans)) {
+        if (!lobes_none(m, trans, hz)) {
             f3 L = mk(0.f, 0.f, 1.f);
             float pS = 0.f, fdist = 0.f;
             bool toEmit = false, toFace = false;
@@ -530,7 +537,8 @@ __device__ __forceinline__ void shade_surface(const WaveArgs& a, const st_materi
                 const float cosY = -dot(f.n, L);
                 if (fdist > 0.f && cosY > 1e-6f) {
                     pS = face_density(fs, a.lf.n, f, fdist, cosY);
-                    fle = f.le * (face_beam(f, cosY) / fmaxf(n * n, 1.f));
+                    const float nSide = dot(nrm, L) < 0.f ? n1 : n;   // the far side's is air
+                    fle = f.le * (face_beam(f, cosY) / fmaxf(nSide * nSide, 1.f));
                     toFace = true;
                 }
             } else if (pick0 < es) {                                  // an emitter: a box, a direction into its cone
@@ -540,11 +548,11 @@ __device__ __forceinline__ void shade_surface(const WaveArgs& a, const st_materi
                     toEmit = true;
                 }
             } else {                                                  // the environment: sun disc or sky
-                L = env_sample_dir(u, nrm, es > 0.f ? (pick0 - es) / (1.f - es) : pick0, u1.x, u1.y);
-                pS = rs * (1.f - es) * env_pdf(u, L, nrm);
+                L = env_sample_dir_q(u, nrm, es > 0.f ? (pick0 - es) / (1.f - es) : pick0, u1.x, u1.y, qf);
+                pS = rs * (1.f - es) * env_pdf_q(u, L, nrm, qf);
             }
             float NoL = dot(nrm, L);
-            if (NoL > 0.f && pS > 0.f) {
+            if ((NoL > 0.f || (throughLit && NoL < 0.f)) && pS > 0.f) {  // sideLit
                 // an emitter's radiance is the occlusion pass's to multiply in, where its ray stops
                 f3 le = toEmit ? mk(1.f) : (toFace ? fle : env_radiance(u, L));
                 f3 f = lobes_eval(lb, a.tab, L, 0.f);
@@ -553,17 +561,18 @@ __device__ __forceinline__ void shade_surface(const WaveArgs& a, const st_materi
                 float w = mis_weight(pS, pB);
                 f3 contrib = beta * f * le * (fabsf(NoL) * (w / pS));
                 if (max3(contrib) > (toEmit ? 1e-9f : 1e-7f)) {
+                    const float nS = NoL < 0.f ? n1 : n;                 // the medium the shadow ray crosses
                     float tr = 1.f;
-                    if (!toEmit && u.haze_on && fabsf(n - 1.f) <= 1e-3f)
+                    if (!toEmit && u.haze_on && fabsf(nS - 1.f) <= 1e-3f)
                         tr = haze_tr(u, pos, L, toFace ? fdist : 2.f * u.envR + length(pos));
                     sh.valid = true;
                     sh.emit = toEmit;
                     sh.face = toFace;
                     sh.dist = fdist;
-                    sh.org = pos + nrm * (otol * 2.f);
+                    sh.org = pos + nrm * (NoL < 0.f ? -otol * 2.f : otol * 2.f);
                     sh.dir = L;
                     sh.rad = contrib * tr;
-                    sh.n = n;
+                    sh.n = nS;
                 }
             }
         }
@@ -611,15 +620,16 @@ __device__ __forceinline__ void shade_surface(const WaveArgs& a, const st_materi
     }
     if (max3(smp.w) <= 0.f) state = RAY_ABSORBED;
     if (u.nee != 0u && !last) {                                       // the other half of MIS (:1370-1395)
-        bool above = dot(nrm, dir) > 0.f && !smp.isDelta;
+        const float cO = dot(nrm, dir);
+        bool above = (cO > 0.f || (throughLit && cO < 0.f)) && !smp.isDelta;   // sideLit: what light sampling draws
         float pOut = smp.isDelta ? 0.f : (guided ? pGuided : lobes_pdf(lb, smp.dir));
-        float pLout = above ? rs * (1.f - es) * env_pdf(u, dir, nrm) : 0.f;
+        float pLout = above ? rs * (1.f - es) * env_pdf_q(u, dir, nrm, qf) : 0.f;
         sunmis = pLout <= 0.f ? 1.f : mis_weight(pOut, pLout);
         // an emitter this bounce meets is weighed against the list's density for the direction, from here
         const float pEout = (above && es > 0.f) ? rs * es * emit_cone_pdf(a.em.dev, pos, dir) : 0.f;
         emw = pEout <= 0.f ? 1.f : mis_weight(pOut, pEout);
         // a face it meets, against the faces' density there (prevPdf, vtxLtot): only what light sampling could draw
-        lp = make_float2((above && fs > 0.f && !lobes_none(m, trans)) ? pOut : -1.f, ltot);
+        lp = make_float2((above && fs > 0.f && !lobes_none(m, trans, hz)) ? pOut : -1.f, ltot);
     } else {
         sunmis = 1.f;
         emw = 1.f;

@@ -661,3 +661,35 @@ def env_floor(width=32, height=32, albedo=0.8, maxbounce=2, seed=1):
     s.view = v
     s.info = {"workload": "env-floor", "albedo": albedo}
     return s
+
+
+def translucent_furnace(kind="opal", width=48, height=48, sky=1000.0, maxbounce=32, seed=1):
+    """The side beyond (materials_pbr.js THE SIDE BEYOND; transmission.js): a sphere in the uniform furnace, seen whole --
+    "opal" a white body that diffuses all it passes (transmission 1, haze 1), "hazy" clear glass with a veil
+    (transmission 1, haze 0.3), "rough" rough glass (roughness 0.5), "frosted" a white base passing half (transmission
+    0.5, haze 1, roughness 0.3). Light samples aim through its faces from inside wherever the medium beyond is air."""
+    mats = {"opal": material(base=(1, 1, 1), roughness=0.2, specular=0.5, transmission=1.0, ior=1.5),
+            "hazy": material(base=(1, 1, 1), roughness=0.0, specular=0.5, transmission=1.0, ior=1.5),
+            "rough": material(base=(1, 1, 1), roughness=0.5, specular=0.5, transmission=1.0, ior=1.5),
+            "frosted": material(base=(1, 1, 1), roughness=0.3, specular=0.5, transmission=0.5, ior=1.5)}
+    m = mats[kind]
+    m.haze = {"opal": 1.0, "hazy": 0.3, "rough": 0.0, "frosted": 1.0}[kind]
+    s = Scene([prim(ST_PRIM_SPHERE, pos=(0.0, 0.0, 0.0), params=(0.5,), material=1)], [air(), m], env_radius=20.0,
+              name="translucent-" + kind)
+    s.params = default_params(width=width, height=height, maxbounce=maxbounce, env_uniform=sky, sun_hint=0, seed=seed)
+    s.view = look_at((0.0, -3.0, 0.0), (0.0, 0.0, 0.0), 25.0, 1.0)
+    s.info = {"sky": sky}
+    return s
+
+
+def translucent_sun(kind="opal", width=64, height=48, maxbounce=12, seed=1):
+    """A translucent sphere (translucent_furnace's materials) half sunk in a grey floor under the sun and sky: what
+    light reaches the camera through it comes from light samples aimed through its faces from inside."""
+    f = translucent_furnace(kind)
+    m = f.material_list[1]
+    s = Scene([prim(ST_PRIM_PLANE, material=1), prim(ST_PRIM_SPHERE, pos=(0.0, 0.0, 0.2), params=(0.5,), material=2)],
+              [air(), diffuse((0.5, 0.5, 0.5)), m], env_radius=20.0, name="translucent-sun-" + kind)
+    s.params = default_params(width=width, height=height, maxbounce=maxbounce, sun_elevation=40.0, sun_azimuth=30.0,
+                              sun_illuminance=100000.0, sky_luminance=3000.0, ground_luminance=0.0, seed=seed)
+    s.view = look_at((0.0, -3.0, 1.2), (0.0, 0.0, 0.3), 35.0, width / height)
+    return s
