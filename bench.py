@@ -6,7 +6,7 @@ window; 1920 x 1080, 64 samples per pixel, max depth 8, march tolerance 1e-4 m, 
 the whole render -- 64 samples of every pixel, 132.7 M camera paths -- folded into the FP64 accumulation.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference] [--small] [--spp S]
-                    [--leg sppm|rmse|optics|mlp|emit|haze|env]   # one leg alone, its JSON printed
+                    [--leg sppm|rmse|optics|mlp|emit|haze|env|sc]   # one leg alone, its JSON printed
 
 value: paths / s with the scene resident on the GPU (graph replays; the timed region brackets K renders with a
        synchronize). e2e: the same through the C ABI as a host calls it -- scene, settings and camera uploaded from
@@ -34,6 +34,8 @@ haze_beam: the haze-box beam (a 10-degree 1000 lm spot, a light face, through 2 
        1280 x 720, 256 samples, 32 bounces) at each of its nine (sigma_s, g) cells: Mpaths/s per cell and overall.
 env: the environment image's map: a floor under a panorama with one small bright patch (its closed form), the relative
        RMSE with the map's light samples and with the cosine lobe's alone at equal samples.
+step_cache: the headline room with the reference's step cache off, on one cell and on three: Mpaths/s and the scene
+       distance evaluations a path.
 Multi-GPU (torchrun): replicas -- each rank renders the whole workload on its own GPU; value sums the ranks' paths
        over the slowest rank's time (weak scaling). There is no data exchange in the path tracer.
 """
@@ -68,7 +70,8 @@ def parse():
     ap.add_argument("--no-emit", action="store_true", help="skip the emissive surfaces' leg")
     ap.add_argument("--no-haze", action="store_true", help="skip the haze-box beam's leg")
     ap.add_argument("--no-env", action="store_true", help="skip the environment image's leg")
-    ap.add_argument("--leg", default="all", choices=["all", "sppm", "rmse", "optics", "mlp", "emit", "haze", "env"],
+    ap.add_argument("--no-sc", action="store_true", help="skip the step cache's leg")
+    ap.add_argument("--leg", default="all", choices=["all", "sppm", "rmse", "optics", "mlp", "emit", "haze", "env", "sc"],
                     help="run one leg alone and print its JSON (profiling runs of the photon map or the optics bench)")
     return ap.parse_args()
 
@@ -537,6 +540,42 @@ def env_leg(args, dev):
     return out
 
 
+def sc_leg(args, dev):
+    """The step cache (the reference's developer setting, wavefront.js:67-150): the headline room at its full size and
+    samples with the cache off, on its own cell (1) and on three cells (2) with the reference's default 4 M cells, and
+    on its own cell with its largest 16 M -- paths a second (CUDA events around one render after a warm-up render) and
+    the scene-distance evaluations a path."""
+    import torch
+    from shadytracer_gb300.renderer import create_path_tracer
+    s = workload(args.small, args.spp)
+    spp = s.info["spp"]
+    P = s.params.width * s.params.height
+    out = {"workload": "the headline room with the step cache over the bounded primitives' box",
+           "metric": "Mpaths/s", "modes": {}}
+    for mode, cells in ((0, 4.0), (1, 4.0), (2, 4.0), (1, 16.0)):
+        s.params.step_cache = mode
+        s.params.step_cache_cells = cells
+        rt = create_path_tracer(s, device=dev)
+        stream = torch.cuda.ExternalStream(rt.stream(), device=torch.device("cuda", dev))
+        rt.step(spp)
+        c0 = rt.counters()["march_steps"]
+        rt.invalidate()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        rt.step_async(spp)
+        e1.record(stream)
+        rt.sync()
+        ms = e0.elapsed_time(e1)
+        evals = rt.counters()["march_steps"] - c0
+        out["modes"]["off" if mode == 0 else "%d_%gM" % (mode, cells)] = {
+            "ms": ms, "Mpaths_per_s": P * spp / (ms / 1e3) / 1e6, "evals_per_path": evals / (P * spp)}
+        rt.close()
+    s.params.step_cache = 0
+    s.params.step_cache_cells = 0.0
+    out["value"] = max(v["Mpaths_per_s"] for v in out["modes"].values())
+    return out
+
+
 def rmse_leg(args, dev):
     """Time to 1 % relative RMSE against the closed form, guided vs plain: the photon map's pane (a 0.5 m glass pane
     over a floor lit only through it, the sun's photons drawn over a 4 m square), plain -- the photons uniform over the
@@ -596,7 +635,7 @@ def run_ours(args):
         out = {"sppm": lambda: sppm_leg(args, dev, with_cpu), "rmse": lambda: rmse_leg(args, dev),
                "optics": lambda: optics_leg(args, dev, with_cpu), "mlp": lambda: mlp_leg(args, dev),
                "emit": lambda: emit_leg(args, dev), "haze": lambda: haze_leg(args, dev),
-               "env": lambda: env_leg(args, dev)}[args.leg]()
+               "env": lambda: env_leg(args, dev), "sc": lambda: sc_leg(args, dev)}[args.leg]()
         if rank == 0:
             print(json.dumps(out), flush=True)
         return 0
@@ -761,6 +800,8 @@ def run_ours(args):
         line["haze_beam"] = haze_leg(args, dev)
     if not args.no_env:
         line["env"] = env_leg(args, dev)
+    if not args.no_sc:
+        line["step_cache"] = sc_leg(args, dev)
     if not args.no_optics:
         line["optics"] = optics_leg(args, dev, rank == 0 and world == 1 and not args.no_cpu)
         if world > 1:

@@ -212,6 +212,11 @@ typedef struct st_params {
     float    emit_radius;         /* the discovery grid's half-size, metres (0: 15; capped at the scene's radius)  */
     uint32_t emit_off;            /* 1: no light sampling of emitters (discovery goes on)            */
     uint32_t env_map_off;         /* 1: light sampling does not draw from the environment image's map  */
+    /* THE STEP CACHE (core/wavefront.js:67-150 stepCacheWGSL, prog_stepcache_fill): a grid over the bounded
+     * primitives' box, each cell the scene's distance at its centre -- a ball with no surface in it, which a ray
+     * inside it may cross to where it leaves with no distance evaluation, when that is at least a cell */
+    uint32_t step_cache;          /* 0 off, 1 the ray's own cell, 2 also the two cells ahead              */
+    float    step_cache_cells;    /* cells, millions (0.25..16; 0: 4)                                     */
 } st_params;
 
 /* The camera, as genrays reads it (core/genrays.js:65-92): the basis from invView's columns and the

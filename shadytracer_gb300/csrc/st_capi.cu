@@ -43,6 +43,12 @@ struct st_ctx {
     DPrim* d_prims = nullptr;
     float4* d_faces = nullptr;            // the lights' faces (FACE_F4 float4s each), then the material -> face map
     uint32_t n_faces = 0;
+    float* d_sc = nullptr;                // the step cache's cells, and the grid they were filled for
+    size_t sc_cap = 0;
+    bool sc_live = false;
+    uint64_t sc_scene = 0, scene_gen = 0;
+    float sc_lo[3] = {0, 0, 0}, sc_cs = 0.f, sc_cells = 0.f;
+    uint32_t sc_dims[3] = {0, 0, 0};
     float4* d_envimg = nullptr;           // the environment image (rgb, 0) and its map's tables; null, none
     float4* d_envmap = nullptr;
     uint32_t env_w = 0, env_h = 0;
@@ -201,6 +207,13 @@ static Uni make_uni(const st_ctx* ctx) {
         u.env_lum = ctx->env_lum; u.env_turn = ctx->env_turn;
         u.env_map = ctx->d_envmap;
         u.env_mshare = ctx->d_envmap && !p.env_map_off ? 0.5f : 0.f;    // ENV_MAP_SHARE
+    }
+    if (ctx->sc_live && p.step_cache) {
+        u.sc = ctx->d_sc;
+        u.sc_lo = mk(ctx->sc_lo[0], ctx->sc_lo[1], ctx->sc_lo[2]);
+        u.sc_cs = ctx->sc_cs;
+        u.sc_dx = ctx->sc_dims[0]; u.sc_dy = ctx->sc_dims[1]; u.sc_dz = ctx->sc_dims[2];
+        u.sc_looks = p.step_cache >= 2 ? 3u : 1u;
     }
     u.haze_on = s.haze_sigma_t > 0 ? 1 : 0;
     u.hc = mk(s.haze_centre[0], s.haze_centre[1], s.haze_centre[2]);
@@ -647,7 +660,8 @@ int st_destroy(st_ctx* ctx) {
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     free_wave(ctx);
     ext_free(ctx->ext);
-    for (void* p : {(void*)ctx->d_prims, (void*)ctx->d_faces, (void*)ctx->d_envimg, (void*)ctx->d_envmap, (void*)ctx->d_mats, (void*)ctx->d_ec, (void*)ctx->d_ecavg,
+    for (void* p : {(void*)ctx->d_prims, (void*)ctx->d_faces, (void*)ctx->d_envimg, (void*)ctx->d_envmap, (void*)ctx->d_sc,
+                    (void*)ctx->d_mats, (void*)ctx->d_ec, (void*)ctx->d_ecavg,
                     (void*)ctx->d_e1, (void*)ctx->d_ctr, (void*)ctx->d_spec})
         if (p) cudaFree(p);
     for (auto& pe : ctx->pending) { cudaEventDestroy(pe.a); cudaEventDestroy(pe.b); }
@@ -721,6 +735,7 @@ int st_set_scene(st_ctx* ctx, const char* cuda_src, const st_scene_desc* d, char
     ctx->desc.materials = nullptr;
     ctx->desc.lights = nullptr;
     ctx->has_scene = true;
+    ctx->scene_gen++;
     invalidate_graph(ctx);
     return st_invalidate(ctx);
 }
@@ -858,12 +873,51 @@ int st_invalidate(st_ctx* ctx) {
     return ST_OK;
 }
 
+// THE STEP CACHE'S GRID (raytrace_main.js:984-1004 setStepCacheBox, :1049-1080 the fill): the bounded primitives'
+// box cut into about step_cache_cells million cubes, filled on the stream when the scene or the cells change
+static int sc_ensure(st_ctx* ctx) {
+    const st_params& p = ctx->params;
+    if (!p.step_cache || !ctx->grid_ok) {
+        if (ctx->sc_live) { ctx->sc_live = false; invalidate_graph(ctx); }
+        return ST_OK;
+    }
+    const float cells = std::min(16.f, std::max(0.25f, p.step_cache_cells > 0.f ? p.step_cache_cells : 4.f)) * 1e6f;
+    if (ctx->sc_live && ctx->sc_scene == ctx->scene_gen && ctx->sc_cells == cells) return ST_OK;
+    double size[3], vol = 1.0;
+    for (int k = 0; k < 3; k++) { size[k] = std::max((double)ctx->grid_hi[k] - ctx->grid_lo[k], 1e-6); vol *= size[k]; }
+    const double cs = std::cbrt(vol / cells);
+    size_t n = 1;
+    for (int k = 0; k < 3; k++) {
+        ctx->sc_dims[k] = (uint32_t)std::max(1.0, std::ceil(size[k] / cs));
+        n *= ctx->sc_dims[k];
+        ctx->sc_lo[k] = ctx->grid_lo[k];
+    }
+    ctx->sc_cs = (float)cs;
+    if (n > ctx->sc_cap) {
+        if (ctx->d_sc) cudaFree(ctx->d_sc);
+        ctx->d_sc = nullptr;
+        ctx->sc_cap = 0;
+        CK(cudaMalloc(&ctx->d_sc, n * sizeof(float)), "cudaMalloc step cache");
+        ctx->sc_cap = n;
+    }
+    CK(launch_sc_fill(ctx->d_prims, (uint32_t)ctx->prims.size(), mk(ctx->sc_lo[0], ctx->sc_lo[1], ctx->sc_lo[2]),
+                      ctx->sc_cs, ctx->sc_dims[0], ctx->sc_dims[1], ctx->sc_dims[2], ctx->d_sc, ctx->sms, ctx->stream),
+       "step cache fill");
+    ctx->sc_live = true;
+    ctx->sc_scene = ctx->scene_gen;
+    ctx->sc_cells = cells;
+    invalidate_graph(ctx);
+    return ST_OK;
+}
+
 int st_step_async(st_ctx* ctx, int n) {
     if (!ctx || n < 0) return ST_ERR_ARG;
     if (!ctx->has_scene || !ctx->has_params || !ctx->has_view)
         return fail(ctx, ST_ERR_STATE, "set a scene, the settings and the view first");
     cudaSetDevice(ctx->device);
     int rc = ensure_wave(ctx);
+    if (rc) return rc;
+    rc = sc_ensure(ctx);
     if (rc) return rc;
     uint32_t left = (uint32_t)n;
     const bool emitters = has_emitters(ctx);

@@ -107,6 +107,8 @@ struct Uni {
     // the environment image (envimage.js) and the map light sampling draws from (envmap.js); null, none
     const float4* env_img; uint32_t env_w, env_h; float env_lum, env_turn;
     const float4* env_map; float env_mshare;
+    // the step cache (wavefront.js:67-118): the cells' distances, the grid's low corner and cell size, its cells, looks
+    const float* sc; f3 sc_lo; float sc_cs; uint32_t sc_dx, sc_dy, sc_dz, sc_looks;
     // haze box (haze.js:64-80)
     int haze_on; f3 hc, hu, hv, hw, halb; float hhu, hhv, hhw, hsig, hg;
     // the sample sequence
@@ -159,6 +161,28 @@ __device__ __forceinline__ SpecDraw spec_draw(const float4* __restrict__ tab, fl
 __device__ __forceinline__ float march_tol(f3 p, float setting) {
     float f = 128.0f * 1.1920928955078125e-7f * fmaxf(fabsf(p.x), fmaxf(fabsf(p.y), fabsf(p.z)));
     return fmaxf(fmaxf(setting, 1e-9f), f);
+}
+
+// THE STEP CACHE (wavefront.js:95-118 scStep): the step a ball allows from pos along dir -- the farthest exit of
+// the balls of the ray's own cell and, with two looks more, of the cells one and two cells ahead, the ray inside
+// them -- or -1 where none holds it as far as a cell
+__device__ __forceinline__ float sc_step(const Uni& u, f3 pos, f3 dir) {
+    const float cs = u.sc_cs;
+    float best = 0.f;
+    for (uint32_t k = 0; k < u.sc_looks; k++) {
+        const f3 g = (pos + dir * ((float)k * cs) - u.sc_lo) * (1.f / cs);
+        if (g.x < 0.f || g.y < 0.f || g.z < 0.f || g.x >= (float)u.sc_dx || g.y >= (float)u.sc_dy || g.z >= (float)u.sc_dz)
+            continue;
+        const uint32_t cx = min((uint32_t)g.x, u.sc_dx - 1u), cy = min((uint32_t)g.y, u.sc_dy - 1u),
+                       cz = min((uint32_t)g.z, u.sc_dz - 1u);
+        const float r = __ldg(&u.sc[cx + u.sc_dx * (cy + u.sc_dy * cz)]);
+        const f3 oc = pos - (u.sc_lo + mk((float)cx + 0.5f, (float)cy + 0.5f, (float)cz + 0.5f) * cs);
+        const float c2 = dot(oc, oc) - r * r;
+        if (c2 >= 0.f) continue;                                      // not inside this ball (an empty cell's is none)
+        const float b = dot(oc, dir);
+        best = fmaxf(best, -b + sqrtf(b * b - c2));                   // where the ray leaves it
+    }
+    return best >= cs ? best : -1.f;
 }
 
 // ------------------------------------------------------------------------------------------------------------

@@ -151,6 +151,7 @@ struct GuideBufs {
 #define SHADOW_FACE 0x40000000u           // ...at a point of a light's face (TAG_FNEE): it arrives when ltot,
                                           // started at minus the way there, reaches 0
 #define SHADOW_FLAGS (SHADOW_EMIT | SHADOW_FACE)
+#define SC_BURST 4u                       // step-cache balls a lane may cross in a row before it asks the scene
 // THE LIGHTS' FACES (st_light.cuh): FACE_F4 float4s a face, then a byte a material (its face + 1, 0 none)
 #define FACE_F4 5
 struct LightBufs {
@@ -217,6 +218,8 @@ cudaError_t launch_shade(const WaveArgs& a, int nxt, int side, int last, int sms
 cudaError_t launch_occlude(const WaveArgs& a, int side, int last, int sms, cudaStream_t s);
 cudaError_t launch_resolve(const WaveArgs& a, cudaStream_t s);
 cudaError_t launch_env_bake(const Uni& u, float* out, cudaStream_t s);
+cudaError_t launch_sc_fill(const DPrim* prims, uint32_t n_prims, f3 lo, float cs, uint32_t dx, uint32_t dy, uint32_t dz,
+                           float* out, int sms, cudaStream_t s);
 // the emitter list (st_emit.cu)
 cudaError_t launch_emit_build(const WaveArgs& a, float margin, cudaStream_t s);
 cudaError_t launch_emit_resolve(const WaveArgs& a, int sms, cudaStream_t s);

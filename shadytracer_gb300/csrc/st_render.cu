@@ -315,7 +315,27 @@ __global__ void __launch_bounds__(256, 4) k_march(WaveArgs a, int cur, int nxt, 
         uint32_t state = RAY_ACTIVE;
         float dh = 0.f;
         if (slot != INVALID_SLOT) {
-            if (HAZE && tmax > 0.f && ltot >= tmax) {
+            // THE STEP CACHE (wavefront.js:901-912): a ball that holds the ray far enough moves it with no distance;
+            // a step that carries it past its collision in the haze is taken back to it below, as a distance step's
+            // is. Up to SC_BURST balls in a row: a lane in empty space goes on while its warp's others ask the scene,
+            // then asks it too where no ball holds it, so the warp's distance pass is not spent waiting on it
+            uint32_t burst = 0;
+            if (!INST && a.u.sc_looks) {
+                while (burst < SC_BURST && !(HAZE && tmax > 0.f && ltot >= tmax)) {
+                    const float sc = sc_step(a.u, pos, dir);
+                    if (!(sc > 0.f)) break;
+                    steps += 1;
+                    f3 off = dir * (sc * stepscale);
+                    pos = pos + off;
+                    ltot += length(off) * n;
+                    burst++;
+                }
+                evals_here += burst;
+            }
+            if (burst == SC_BURST || (burst && evals_here >= chunk)) {
+                if (HAZE && tmax > 0.f && ltot >= tmax) { state = RAY_SCATTER; fin = true; }
+                else if (evals_here >= chunk) more = true;
+            } else if (HAZE && tmax > 0.f && ltot >= tmax) {
                 state = RAY_SCATTER;
                 fin = true;
             } else {
@@ -908,7 +928,24 @@ __global__ void __launch_bounds__(256, 4) k_occlude(WaveArgs a, int last) {
         }
         if (__ballot_sync(FULL_MASK, idx != INVALID_SLOT) == 0) break;
         bool reached = false, done = false, more = false;
-        if (idx != INVALID_SLOT) {
+        // the step cache (wavefront.js:1536-1546): balls that hold the ray far enough move it with no distance, up to
+        // SC_BURST in a row, then the distance where none does (as in the march)
+        uint32_t burst = 0;
+        if (idx != INVALID_SLOT && a.u.sc_looks) {
+            while (burst < SC_BURST && !((sflag & SHADOW_FACE) && ltot >= 0.f)) {
+                const float sc = sc_step(a.u, pos, dir);
+                if (!(sc > 0.f)) break;
+                steps += 1;
+                f3 off = dir * (sc * stepscale);
+                pos = pos + off;
+                ltot += length(off) * n;
+                burst++;
+            }
+            evals_here += burst;
+        }
+        if (burst == SC_BURST || (burst && evals_here >= chunk)) {
+            if (evals_here >= chunk) more = true;
+        } else if (idx != INVALID_SLOT) {
             float d = scene_dist(sp, n_prims, pos);
             evals++;
             evals_here++;
@@ -1073,6 +1110,22 @@ __global__ void __launch_bounds__(256) k_env_bake(Uni u, float* __restrict__ out
             if (!(u.sun_on && in_sun_disc(u, d))) acc = acc + env_base(u, d);
         }
     out[i] = luma(acc * 0.25f);
+}
+// THE STEP CACHE'S CELLS (wavefront.js:119-147 prog_stepcache_fill): one thread a cell, the scene's distance at its
+// centre, its magnitude held to [1e-6, 1e18]
+__global__ void __launch_bounds__(256) k_sc_fill(const DPrim* __restrict__ prims, uint32_t n_prims, f3 lo, float cs,
+                                                 uint32_t dx, uint32_t dy, uint32_t dz, float* __restrict__ out) {
+    const uint64_t n = (uint64_t)dx * dy * dz;
+    for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t x = (uint32_t)(k % dx), y = (uint32_t)((k / dx) % dy), z = (uint32_t)(k / ((uint64_t)dx * dy));
+        const f3 c = lo + mk((float)x + 0.5f, (float)y + 0.5f, (float)z + 0.5f) * cs;
+        out[k] = fminf(fmaxf(fabsf(scene_dist(prims, n_prims, c)), 1e-6f), 1e18f);
+    }
+}
+cudaError_t launch_sc_fill(const DPrim* prims, uint32_t n_prims, f3 lo, float cs, uint32_t dx, uint32_t dy, uint32_t dz,
+                           float* out, int sms, cudaStream_t s) {
+    k_sc_fill<<<sms * 8, 256, 0, s>>>(prims, n_prims, lo, cs, dx, dy, dz, out);
+    return cudaGetLastError();
 }
 cudaError_t launch_env_bake(const Uni& u, float* out, cudaStream_t s) {
     k_env_bake<<<(ENV_MW * ENV_MH + 255) / 256, 256, 0, s>>>(u, out);

@@ -176,3 +176,29 @@ def test_thin_lens_matches_the_oracle(rt_factory):
     s.view.lens_radius = 0.0
     pin = oracle.render(s, 16).luma()
     assert np.mean(np.abs(pin - Lr) > 0.05 * np.maximum(Lr, 1.0)) > 0.2
+
+
+@pytest.mark.parametrize("looks", [1, 2])
+def test_step_cache_keeps_the_picture(rt_factory, looks):
+    """The step cache (wavefront.js:67-150): balls with no surface in them, crossed with no distance evaluation. The
+    room with it on reads as the oracle, marching without it, reads, pixel by pixel within the error bars, and the
+    march evaluates the scene's distance fewer times."""
+    s = scenes.sdf_room(width=96, height=54, spp=4)
+    rt0 = rt_factory(s)
+    rt0.step(16)
+    steps0 = rt0.counters()["march_steps"]
+    s.params.step_cache = looks
+    rt = rt_factory(s)
+    rt.step(16)
+    rgb, V, S, cnt = rt.read_accum()
+    L = rgb @ LUMA
+    steps = rt.counters()["march_steps"]
+    ref = oracle.render(s, 16)
+    sd = np.hypot(se_of(V, S), se_of(ref.V, ref.S))
+    ok = sd > 0
+    z = (L - ref.luma())[ok] / sd[ok]
+    assert np.mean(np.abs(z) < 4) > 0.98, np.mean(np.abs(z) < 4)
+    zm = (L - ref.luma())[ok].mean() / (np.sqrt(np.sum(sd[ok] ** 2)) / ok.sum())
+    assert abs(zm) < 5, zm
+    assert steps < 0.9 * steps0, (steps, steps0)
+    assert rt.counters()["nonfinite"] == 0
