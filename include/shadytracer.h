@@ -348,7 +348,7 @@ typedef struct st_optics_source {
     float    centre[3];           /* metres                                                        */
     float    flux;                /* lm: its share of the rays follows it                          */
     float    axis[3];             /* emission axis, unit                                           */
-    uint32_t shape;               /* 0 point, 1 disc, 2 rectangle                                   */
+    uint32_t shape;               /* 0 point, 1 disc, 2 rectangle, 3 a ray set (st_optics_set_rays) */
     float    tangent[3];          /* first tangent                                                 */
     float    size_x;              /* disc radius / rectangle half width                            */
     float    size_y;              /* rectangle half height                                          */
@@ -359,6 +359,8 @@ typedef struct st_optics_source {
     uint32_t two_sided;
     uint32_t on_surface;          /* start 2 march tolerances off the sheet                          */
     uint32_t instance;            /* which instance of a batch it belongs to                        */
+    uint32_t ray_first, ray_count;/* a ray set's rays in the ray table: each traced ray takes one at
+                                     random, as it is, carrying its weight (kernels.js:320-336)       */
 } st_optics_source;
 
 typedef struct st_optics_far {
@@ -389,6 +391,10 @@ typedef struct st_optics_totals {
 
 int  st_optics_set_sources(st_ctx* ctx, const st_optics_source* src, uint32_t n);
 int  st_optics_set_far(st_ctx* ctx, const st_optics_far* far);
+/* THE RAY TABLE the ray sets read (optics/sources.js RAYSET_VEC4; a Zemax source file's rays placed by the host,
+ * optics/zemax.js): n rays of 8 floats -- position (metres, world), weight (its flux over its set's mean),
+ * direction (unit), wavelength (nm, 0 none). */
+int  st_optics_set_rays(st_ctx* ctx, const float* rays, uint32_t n);
 /* Traces every instance of the batch; far (n_instances*nG*nC) and lux (n_instances*cells^2) are the
  * FP64 tallies in ray weight (the host multiplies by flux / rays); totals per instance. */
 int  st_optics_run(st_ctx* ctx, const st_optics_batch* batch, double* far, double* lux,

@@ -232,6 +232,7 @@ def _declare_extra(L):
         "sto_lambda_of": ([C.c_uint32], C.c_double),
         "sto_spec_table": ([P, P], None),
         "sto_spec_draw": ([C.c_double, P], C.c_double),
+        "sto_optics_set_rays": ([P, C.c_uint32], C.c_int),
         "sto_optics_run": ([P, P, P, C.c_uint32, P, C.c_uint32, P, C.c_uint32, C.c_uint32, C.c_uint32, C.c_float,
                             C.c_float, C.c_uint32, C.c_uint32, C.c_int, P, P, P, C.c_int], C.c_int),
         "sto_guide_forward": ([P, C.c_uint32, P, P, P, C.c_float, C.c_int, P], None),
@@ -393,6 +394,15 @@ def far_intensity(flux, nC, nG):
     I = np.zeros(nG * nC, np.float64)
     xlib().sto_far_intensity(ptr(flux), nC, nG, ptr(I))
     return I.reshape(nG, nC)
+
+
+def optics_set_rays(rays):
+    """The ray table the ray-set sources of the oracle's optics runs that follow read (N x 8); None clears it."""
+    if rays is None:
+        xlib().sto_optics_set_rays(None, 0)
+        return
+    r = np.ascontiguousarray(rays, np.float32).reshape(-1, 8)
+    xlib().sto_optics_set_rays(ptr(r), len(r))
 
 
 def optics_run(bench, ray_counts, nC=360, nG=181, cells=0, half=1.0, height=1.0, maxbounce=32, seed=1, fp64=False,

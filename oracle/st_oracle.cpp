@@ -910,10 +910,11 @@ void optics_ray(const Ctx<T>& C, U4 bseed, uint32_t id, const st_optics_source* 
     Rng r0; r0.h = bseed; r0.seed_u32(id); r0.seed_u32(0x9E3779B9u);
     V3<T> org, dir;
     uint32_t which;
-    source_ray(src, cdf, nsrc, r0, C.tol, org, dir, which);
+    T w;
+    source_ray(src, cdf, nsrc, r0, C.tol, org, dir, which, w);
     Ray<T> r;
     r.pos = org; r.dir = dir;
-    r.beta = V3<T>(1); r.rad = V3<T>(1);
+    r.beta = V3<T>(w); r.rad = V3<T>(1);
     r.ltot = 0; r.n = T(std::max(1.f, src[which].emit_n)); r.sunmis = 1; r.tmax = 0; r.absLtot = 0;
     r.bounces = 0; r.steps = 0; r.state = RAY_ACTIVE; r.pix = id;
     tl.emitted += (double)luma(r.beta * r.rad);
@@ -1425,6 +1426,11 @@ void sto_lobes_sample(const st_material* m, const double* v, double eta, uint32_
 // Trace an optics batch (config: the scene, its settings for the march; sources with their instance; per instance its
 // ray count, far-field frame, lux plane). Tallies per instance into far (n_inst * nG * nC), lux (n_inst * cells^2),
 // totals (n_inst * 6: emitted, escaped, lost, detected, absorbed, interactions).
+// the ray table the ray sets of the runs that follow read (8 floats a ray); n 0 clears it
+int sto_optics_set_rays(const float* rays, uint32_t n) {
+    optics_rays().assign(rays, rays + (size_t)n * 8);
+    return 0;
+}
 int sto_optics_run(const st_scene_desc* const* scenes, const st_params* p, const st_optics_source* src, uint32_t nsrc,
                    const uint32_t* ray_count, uint32_t n_inst, const float* frames, uint32_t nC, uint32_t nG,
                    uint32_t cells, float half, float height, uint32_t maxbounce, uint32_t seed, int fp64,

@@ -51,14 +51,28 @@ inline void far_intensity(const double* flux, uint32_t nC, uint32_t nG, double* 
 // A SOURCE'S RAY (kernels.js:299-408 optSourceRay): the source by flux, a point on it, the side, the direction from
 // the distribution, stepped two march tolerances off the sheet when the source is geometry. `cdf` is each source's
 // cumulative share. Returns the ray's origin and direction.
+// the ray table a ray set reads (8 floats a ray: position, weight, direction, wavelength), for the runs that follow
+inline std::vector<float>& optics_rays() { static std::vector<float> r; return r; }
 template <class T>
 inline void source_ray(const st_optics_source* src, const float* cdf, uint32_t nsrc, Rng& rng, T tol,
-                       V3<T>& org, V3<T>& dir, uint32_t& which) {
+                       V3<T>& org, V3<T>& dir, uint32_t& which, T& w) {
     T pick[4]; rng.next4(pick);
     uint32_t k = 0;
     for (uint32_t i = 0; i < nsrc; i++) { k = i; if (pick[0] <= T(cdf[i])) break; }
     which = k;
     const st_optics_source& s = src[k];
+    w = T(1);
+    if (s.shape == 3) {                                     // a ray set (kernels.js:320-336): one of its rays, weighted
+        const std::vector<float>& R = optics_rays();
+        const uint32_t cnt = std::max(s.ray_count, 1u);
+        T u[4]; rng.next4(u);
+        const uint32_t j = s.ray_first + std::min((uint32_t)(float)(u[0] * T(cnt)), cnt - 1u);
+        const float* r = &R[(size_t)j * 8];
+        org = V3<T>(T(r[0]), T(r[1]), T(r[2]));
+        dir = normalize(V3<T>(T(r[4]), T(r[5]), T(r[6])));
+        w = T(r[3]);
+        return;
+    }
     V3<T> front = normalize(V3<T>(T(s.axis[0]), T(s.axis[1]), T(s.axis[2])));
     V3<T> t0(T(s.tangent[0]), T(s.tangent[1]), T(s.tangent[2]));
     V3<T> tu = normalize(t0 - front * dot(t0, front));

@@ -23,6 +23,7 @@ SIGNATURES = {
     "st_set_params": ([P, C.POINTER(T.StParams), C.POINTER(C.c_uint64)], C.c_int),
     "st_set_view": ([P, C.POINTER(T.StView)], C.c_int),
     "st_set_env_image": ([P, P, C.c_uint32, C.c_uint32, C.c_float, C.c_float], C.c_int),
+    "st_optics_set_rays": ([P, P, C.c_uint32], C.c_int),
     "st_env_map_tables": ([P, P], C.c_int),
     "st_invalidate": ([P], C.c_int),
     "st_step": ([P, C.c_int], C.c_int),

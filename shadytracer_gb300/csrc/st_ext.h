@@ -47,6 +47,8 @@ st::SppmBufs sppm_bufs(const SppmState& s);
 
 struct OpticsState {
     std::vector<st_optics_source> sources;
+    float4* rays = nullptr;      // the ray table: two float4s a ray (position | weight, direction | wavelength)
+    uint32_t n_rays = 0;
     st_optics_far far{};
     bool has_far = false;
     void* scratch = nullptr;     // the run's device buffers (st_optics.cu OptBuf), grown as needed

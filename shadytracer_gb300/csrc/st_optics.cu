@@ -34,6 +34,9 @@ struct OptArgs {
     const st_optics_source* src;    // sorted by instance
     const float* cdf;               // each source's cumulative share within its instance
     const uint2* src_range;         // per instance [first, count) of src
+    const float4* rays;             // the ray table (two float4s a ray), and its rays
+    uint32_t n_rays;
+    uint32_t has_sets;              // a ray set among the sources: the weights emitted are summed (tot[7])
     const float4* origin;           // per instance: where its axis starts (its first source's centre)
     const uint32_t* wave_first;     // per instance: the first ray id of this wave
     const uint32_t* wave_prefix;    // per instance: the wave's slots before it (n_inst + 1 entries)
@@ -60,12 +63,25 @@ __device__ __forceinline__ uint32_t far_bin(const OptArgs& o, f3 d) {
 
 // A SOURCE'S RAY (kernels.js:299-408 optSourceRay): the source by flux, a point on it, the side, the direction from
 // its distribution, two march tolerances off the sheet when it is geometry
-__device__ __forceinline__ void source_ray(const OptArgs& o, uint32_t inst, Rng& rng, f3& org, f3& dir, float& en) {
+__device__ __forceinline__ void source_ray(const OptArgs& o, uint32_t inst, Rng& rng, f3& org, f3& dir, float& en,
+                                           float& w) {
     const uint2 rg = o.src_range[inst];
     float4 pick = rng.next();
     uint32_t k = rg.x;
     for (uint32_t i = 0; i < rg.y; i++) { k = rg.x + i; if (pick.x <= o.cdf[rg.x + i]) break; }
     const st_optics_source& s = o.src[k];
+    w = 1.f;
+    if (s.shape == 3u) {                                              // A RAY SET: one of its rays, as it is, weighted
+        const uint32_t cnt = max(s.ray_count, 1u);
+        const float4 u = rng.next();
+        const uint32_t j = min(s.ray_first + min((uint32_t)(u.x * (float)cnt), cnt - 1u), o.n_rays - 1u);
+        const float4 a = o.rays[2u * j], d = o.rays[2u * j + 1u];
+        org = mk(a.x, a.y, a.z);
+        dir = normalize(mk(d.x, d.y, d.z));
+        w = a.w;
+        en = fmaxf(1.f, s.emit_n);
+        return;
+    }
     f3 front = normalize(mk(s.axis[0], s.axis[1], s.axis[2]));
     f3 t0 = mk(s.tangent[0], s.tangent[1], s.tangent[2]);
     f3 tu = normalize(t0 - front * dot(t0, front));
@@ -115,11 +131,12 @@ __global__ void __launch_bounds__(256) k_opt_gen(OptArgs o) {
         rng.seed(id);
         rng.seed(0x9E3779B9u);
         f3 org, dir;
-        float en;
-        source_ray(o, inst, rng, org, dir, en);
+        float en, w;
+        source_ray(o, inst, rng, org, dir, en, w);
         a.pb.pos[i] = make_float4(org.x, org.y, org.z, 0.f);
         a.pb.dir[i] = make_float4(dir.x, dir.y, dir.z, en);
-        a.pb.beta[i] = make_float4(1.f, 1.f, 1.f, 1.f);
+        a.pb.beta[i] = make_float4(w, w, w, 1.f);                       // a ray set's ray carries its weight
+        if (o.has_sets) atomicAdd(&o.tot[(size_t)inst * OPT_TOT + 7], (double)w);
         a.pb.rad[i] = make_float4(1.f, 1.f, 1.f, 0.f);          // a photon's radiance field is its flux: weight 1
         a.pb.meta[i] = make_uint4(id, meta_y(0, 0, RAY_ACTIVE), 0u, inst);
         a.q.ray[0][i] = i;
@@ -300,6 +317,7 @@ struct OptBuf {
 }  // namespace
 
 void optics_free(OpticsState& os) {
+    if (os.rays) { cudaFree(os.rays); os.rays = nullptr; os.n_rays = 0; }
     if (!os.scratch) return;
     OptBuf* B = static_cast<OptBuf*>(os.scratch);
     void* ps[] = {B->pos, B->dir, B->beta, B->rad, B->meta, B->ray0, B->ray1, B->hit, B->hitd, B->far, B->lux, B->tot,
@@ -315,11 +333,34 @@ extern "C" {
 int st_optics_set_sources(st_ctx* ctx, const st_optics_source* src, uint32_t n) {
     if (!ctx || (n && !src)) return ST_ERR_ARG;
     for (uint32_t i = 0; i < n; i++)
-        if (src[i].shape > 2 || src[i].dist > 2 || !(src[i].flux >= 0) || src[i].instance >= OPT_MAX_INST) {
+        if (src[i].shape > 3 || src[i].dist > 2 || !(src[i].flux >= 0) || src[i].instance >= OPT_MAX_INST) {
             ctx_set_error(ctx, "source " + std::to_string(i) + ": shape, distribution, flux or instance out of range");
             return ST_ERR_ARG;
         }
     ctx_ext(ctx).optics.sources.assign(src, src + n);
+    return ST_OK;
+}
+
+int st_optics_set_rays(st_ctx* ctx, const float* rays, uint32_t n) {
+    if (!ctx || (n && !rays)) return ST_ERR_ARG;
+    OpticsState& os = ctx_ext(ctx).optics;
+    if (os.rays) { cudaFree(os.rays); os.rays = nullptr; os.n_rays = 0; }
+    if (!n) return ST_OK;
+    std::vector<float4> h((size_t)n * 2);
+    for (uint32_t i = 0; i < n; i++) {
+        const float* r = rays + (size_t)i * 8;
+        h[2 * i] = make_float4(r[0], r[1], r[2], r[3]);
+        h[2 * i + 1] = make_float4(r[4], r[5], r[6], r[7]);
+    }
+    cudaError_t e = cudaMalloc(&os.rays, h.size() * sizeof(float4));
+    if (e == cudaSuccess) e = cudaMemcpy(os.rays, h.data(), h.size() * sizeof(float4), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        if (os.rays) cudaFree(os.rays);
+        os.rays = nullptr;
+        ctx_set_error(ctx, std::string("ray table: ") + cudaGetErrorString(e));
+        return ST_ERR_CUDA;
+    }
+    os.n_rays = n;
     return ST_OK;
 }
 
@@ -339,6 +380,11 @@ int st_optics_run(st_ctx* ctx, const st_optics_batch* b, double* far_out, double
     OpticsState& os = ctx_ext(ctx).optics;
     if (!ctx_has_scene(ctx)) { ctx_set_error(ctx, "set a scene first"); return ST_ERR_STATE; }
     if (!os.has_far) { ctx_set_error(ctx, "set the far field first (st_optics_set_far)"); return ST_ERR_STATE; }
+    for (const st_optics_source& q : os.sources)
+        if (q.shape == 3u && (q.ray_count == 0 || (uint64_t)q.ray_first + q.ray_count > os.n_rays)) {
+            ctx_set_error(ctx, "a ray set's rays are past the ray table (st_optics_set_rays)");
+            return ST_ERR_ARG;
+        }
     if (b->lux_cells > 4096) { ctx_set_error(ctx, "lux map over 4096 cells a side"); return ST_ERR_ARG; }
     if (b->maxbounce > 250) { ctx_set_error(ctx, "maxbounce over 250 (a ray's bounces are counted in 8 bits)"); return ST_ERR_ARG; }
     const uint32_t NI = b->n_instances;
@@ -451,6 +497,9 @@ int st_optics_run(st_ctx* ctx, const st_optics_batch* b, double* far_out, double
     o.w.spw = 1;
     o.w.inst_range = B.range;
     o.src = B.src; o.cdf = B.cdf; o.src_range = B.srange; o.origin = B.origin;
+    o.rays = os.rays; o.n_rays = os.n_rays;
+    o.has_sets = 0;
+    for (const st_optics_source& q : os.sources) if (q.shape == 3u) o.has_sets = 1;
     o.wave_first = B.wfirst; o.wave_prefix = B.wpre;
     o.n_inst = NI;
     o.seed = b->seed;
@@ -507,7 +556,7 @@ int st_optics_run(st_ctx* ctx, const st_optics_batch* b, double* far_out, double
     if (totals)
         for (uint32_t i = 0; i < NI; i++) {
             const double* T = &tot[(size_t)i * OPT_TOT];
-            totals[i].emitted = (double)b->ray_count[i];
+            totals[i].emitted = o.has_sets ? T[7] : (double)b->ray_count[i];   // a ray set's: its rays' weights
             totals[i].escaped = T[1]; totals[i].lost = T[2]; totals[i].detected = T[3]; totals[i].absorbed = T[4];
             totals[i].interactions = (uint64_t)T[5];
             totals[i].rays = b->ray_count[i];

@@ -32,6 +32,14 @@ class Optics:
         check(self.L.st_optics_set_sources(self.rt.ctx, arr, len(sources)), self.rt.ctx, "st_optics_set_sources")
         self.sources = list(sources)
 
+    def set_rays(self, rays):
+        """The ray table the ray-set sources (shape 3) read: N x 8 floats -- position (m), weight, direction, wavelength
+        (nm) -- as ray_set_rays gives them (optics/sources.js RAYSET_VEC4)."""
+        r = np.ascontiguousarray(rays, np.float32).reshape(-1, 8)
+        check(self.L.st_optics_set_rays(self.rt.ctx, r.ctypes.data_as(C.c_void_p), len(r)), self.rt.ctx,
+              "st_optics_set_rays")
+        self.rays = r
+
     def set_far(self, nC=360, nG=181, axis=(0.0, 0.0, 1.0), c0=(1.0, 0.0, 0.0)):
         f = T.StOpticsFar()
         f.nC, f.nG = nC, nG
@@ -108,3 +116,86 @@ def virtual_plane(I, nC, nG, h=1.0, half=1.0, cells=64):
     v = lambda j: I[j, i0] * (1 - tc) + I[j, i1] * tc
     Ig = v(j0) * (1 - tg) + v(j1) * tg
     return Ig * cg ** 3 / (h * h)
+
+
+# ------------------------------------------------------------------------------------------------------------
+# ZEMAX SOURCE FILES (optics/zemax.js): ray sets as LED makers publish them, and the rays a ray-set source draws.
+# ------------------------------------------------------------------------------------------------------------
+ZEMAX_HEADER_BYTES = 208
+ZEMAX_UNITS = {0: ("m", 1.0), 1: ("in", 0.0254), 2: ("cm", 0.01), 3: ("ft", 0.3048), 4: ("mm", 0.001)}
+
+
+def _rot_xyz(rx, ry, rz):
+    """Rotations about x, then y, then z (radians), as one matrix (zemax.js: the builder's own convention)."""
+    cx, sx, cy, sy, cz, sz = math.cos(rx), math.sin(rx), math.cos(ry), math.sin(ry), math.cos(rz), math.sin(rz)
+    Rx = np.array([[1, 0, 0], [0, cx, -sx], [0, sx, cx]])
+    Ry = np.array([[cy, 0, sy], [0, 1, 0], [-sy, 0, cy]])
+    Rz = np.array([[cz, -sz, 0], [sz, cz, 0], [0, 0, 1]])
+    return Rz @ Ry @ Rx
+
+
+def parse_zemax(data):
+    """A Zemax OpticStudio source file (zemax.js parseZemax): the 208-byte little-endian header -- identifier, count,
+    description, source and ray-set flux, wavelength, the angles, the length unit, the placement, the ray format (0
+    flux only: x y z l m n flux; 2 spectral: + wavelength), the flux unit -- then the rays. Returns (header, rays), rays
+    N x 8 float32 (x, y, z in metres with the file's own placement applied, flux, l, m, n unit, wavelength in nm or 0).
+    Raises ValueError, saying why, for a file it cannot read honestly (a length that disagrees with the header's count
+    and format, an unknown unit or format)."""
+    import struct
+    b = bytes(data)
+    if len(b) < ZEMAX_HEADER_BYTES:
+        raise ValueError("not a Zemax source file: %d bytes, the header alone is %d" % (len(b), ZEMAX_HEADER_BYTES))
+    identifier, count = struct.unpack_from("<iI", b, 0)
+    desc = b[8:108].split(b"\0", 1)[0].decode("latin-1")
+    source_flux, rayset_flux, wavelength, inc0, inc1, az0, az1 = struct.unpack_from("<7f", b, 108)
+    (units,) = struct.unpack_from("<i", b, 136)
+    loc = struct.unpack_from("<3f", b, 140)
+    rot = struct.unpack_from("<3f", b, 152)
+    fmt, flux_type = struct.unpack_from("<ii", b, 192)
+    if units not in ZEMAX_UNITS:
+        raise ValueError("unknown length unit %d" % units)
+    if fmt not in (0, 2):
+        raise ValueError("unknown ray format %d (0 flux only, 2 spectral)" % fmt)
+    nf = 7 if fmt == 0 else 8
+    if len(b) != ZEMAX_HEADER_BYTES + count * nf * 4:
+        raise ValueError("%d bytes for %d rays of %d floats: the file and its header disagree" % (len(b), count, nf))
+    raw = np.frombuffer(b, "<f4", count * nf, ZEMAX_HEADER_BYTES).reshape(count, nf).astype(np.float64)
+    m = ZEMAX_UNITS[units][1]
+    R = _rot_xyz(*rot)
+    pos = (raw[:, 0:3] @ R.T + np.array(loc)) * m
+    d = raw[:, 3:6] @ R.T
+    d /= np.maximum(np.linalg.norm(d, axis=1, keepdims=True), 1e-30)
+    rays = np.zeros((count, 8), np.float32)
+    rays[:, 0:3] = pos
+    rays[:, 3] = raw[:, 6]
+    rays[:, 4:7] = d
+    rays[:, 7] = raw[:, 7] * 1000.0 if fmt == 2 else (wavelength * 1000.0 if wavelength > 0 else 0.0)
+    header = {"identifier": identifier, "count": count, "description": desc, "source_flux": source_flux,
+              "rayset_flux": rayset_flux, "wavelength_um": wavelength, "units": ZEMAX_UNITS[units][0],
+              "loc": loc, "rot": rot, "rotated": any(abs(x) > 0 for x in rot), "format": fmt,
+              "flux_type": "lm" if flux_type == 1 else "W"}
+    return header, rays
+
+
+def ray_set_rays(rays, origin=(0.0, 0.0, 0.0), rot=None):
+    """A file's rays placed in the scene (sources.js placeRays): turned by `rot` (3 x 3, optional) and moved to
+    `origin`, each ray's weight its flux over the set's mean (sources.js RAYSET_VEC4)."""
+    r = np.array(rays, np.float64, copy=True)
+    if rot is not None:
+        R = np.asarray(rot, np.float64)
+        r[:, 0:3] = r[:, 0:3] @ R.T
+        r[:, 4:7] = r[:, 4:7] @ R.T
+    r[:, 0:3] += np.asarray(origin, np.float64)
+    mean = r[:, 3].mean() if len(r) else 1.0
+    r[:, 3] = r[:, 3] / (mean if mean > 0 else 1.0)
+    return r.astype(np.float32)
+
+
+def ray_set_source(first, count, flux, instance=0, emit_n=1.0):
+    """A ray-set source (shape 3) of `flux` lumens over rays [first, first + count) of the ray table."""
+    s = T.StOpticsSource()
+    s.shape, s.flux, s.instance, s.emit_n = 3, flux, instance, emit_n
+    s.axis[2] = 1.0
+    s.tangent[0] = 1.0
+    s.ray_first, s.ray_count = first, count
+    return s

@@ -118,7 +118,7 @@ class StOpticsSource(C.Structure):
                 ("tangent", C.c_float * 3), ("size_x", C.c_float),
                 ("size_y", C.c_float), ("dist", C.c_uint32), ("cos_half", C.c_float), ("n_exp", C.c_float),
                 ("emit_n", C.c_float), ("two_sided", C.c_uint32), ("on_surface", C.c_uint32),
-                ("instance", C.c_uint32)]
+                ("instance", C.c_uint32), ("ray_first", C.c_uint32), ("ray_count", C.c_uint32)]
 
 
 class StOpticsFar(C.Structure):
