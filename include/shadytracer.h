@@ -107,7 +107,9 @@ typedef struct st_material {
                            * cone about the surface's outward normal; 0, a glowing surface, the same every way   */
     float haze;           /* of what transmission passes, the share diffused through rather than refracted
                            * (materials.js Material2.haze): 0 clear, 1 an opal face                              */
-    float pad[3];         /* 80 bytes                                                                 */
+    float anisotropy;     /* stretches the gloss along the surface's first tangent: 0 round, 1 ten to one
+                           * (materials.js Material2.anisotropy; the frame the normal's own, no grain)           */
+    float pad[2];         /* 80 bytes                                                                 */
 } st_material;
 
 /* A LIGHT'S FACE (builder/lights.js, the builder's light object; core/scene_api.js:259-289 LightFace,

@@ -371,32 +371,40 @@ template <class T> inline T mis_weight(T a, T b) { T a2 = a * a, b2 = b * b; ret
 // ------------------------------------------------------------------------------------------------------------
 const int MF_NMU = 32, MF_NR = 32, MF_NIOR = 16, MF_SQRT_SAMPLES = 32;
 const double ALPHA_MIN = 1e-3;
-template <class T> inline T mf_lambda(const V3<T>& w, T a) {
+// the two alphas along the local x and y (microfacet.js mfAnisoAlpha); equal, the isotropic formulas exactly
+template <class T> struct A2 { T x, y; };
+template <class T> inline T mf_lambda(const V3<T>& w, A2<T> a) {
     T z2 = std::max(w.z * w.z, T(1e-12));
-    T t2 = (a * a * w.x * w.x + a * a * w.y * w.y) / z2;
+    T t2 = (a.x * a.x * w.x * w.x + a.y * a.y * w.y * w.y) / z2;
     return T(0.5) * (T(-1) + std::sqrt(T(1) + t2));
 }
-template <class T> inline T mf_g1(const V3<T>& w, T a) { return T(1) / (T(1) + mf_lambda(w, a)); }
-template <class T> inline T mf_g2(const V3<T>& o, const V3<T>& i, T a) { return T(1) / (T(1) + mf_lambda(o, a) + mf_lambda(i, a)); }
-template <class T> inline T mf_d(const V3<T>& h, T a) {
+template <class T> inline T mf_g1(const V3<T>& w, A2<T> a) { return T(1) / (T(1) + mf_lambda(w, a)); }
+template <class T> inline T mf_g2(const V3<T>& o, const V3<T>& i, A2<T> a) { return T(1) / (T(1) + mf_lambda(o, a) + mf_lambda(i, a)); }
+template <class T> inline T mf_d(const V3<T>& h, A2<T> a) {
     if (h.z <= T(0)) return T(0);
-    T t = (h.x * h.x) / (a * a) + (h.y * h.y) / (a * a) + h.z * h.z;
-    return T(1) / (T(PI_D) * a * a * t * t);
+    T t = (h.x * h.x) / (a.x * a.x) + (h.y * h.y) / (a.y * a.y) + h.z * h.z;
+    return T(1) / (T(PI_D) * a.x * a.y * t * t);
 }
-template <class T> inline V3<T> mf_sample_vndf(const V3<T>& o, T a, T u0, T u1) {
-    V3<T> os = normalize(V3<T>(o.x * a, o.y * a, o.z));
+template <class T> inline V3<T> mf_sample_vndf(const V3<T>& o, A2<T> a, T u0, T u1) {
+    V3<T> os = normalize(V3<T>(o.x * a.x, o.y * a.y, o.z));
     T phi = T(2) * T(PI_D) * u0;
     T z = (T(1) - u1) * (T(1) + os.z) - os.z;
     T sinT = std::sqrt(clampT(T(1) - z * z, T(0), T(1)));
     V3<T> c(sinT * std::cos(phi), sinT * std::sin(phi), z);
     V3<T> hs = c + os;
-    return normalize(V3<T>(hs.x * a, hs.y * a, std::max(hs.z, T(1e-7))));
+    return normalize(V3<T>(hs.x * a.x, hs.y * a.y, std::max(hs.z, T(1e-7))));
 }
-template <class T> inline T mf_pdf_reflect(const V3<T>& o, const V3<T>& i, T a) {
+template <class T> inline T mf_pdf_reflect(const V3<T>& o, const V3<T>& i, A2<T> a) {
     if (o.z <= T(0) || i.z <= T(0)) return T(0);
     V3<T> h = normalize(o + i);
     return mf_g1(o, a) * mf_d(h, a) / (T(4) * o.z);
 }
+template <class T> inline T mf_lambda(const V3<T>& w, T a) { return mf_lambda(w, A2<T>{a, a}); }
+template <class T> inline T mf_g1(const V3<T>& w, T a) { return mf_g1(w, A2<T>{a, a}); }
+template <class T> inline T mf_g2(const V3<T>& o, const V3<T>& i, T a) { return mf_g2(o, i, A2<T>{a, a}); }
+template <class T> inline T mf_d(const V3<T>& h, T a) { return mf_d(h, A2<T>{a, a}); }
+template <class T> inline V3<T> mf_sample_vndf(const V3<T>& o, T a, T u0, T u1) { return mf_sample_vndf(o, A2<T>{a, a}, u0, u1); }
+template <class T> inline T mf_pdf_reflect(const V3<T>& o, const V3<T>& i, T a) { return mf_pdf_reflect(o, i, A2<T>{a, a}); }
 template <class T> inline T fresnel_dielectric(T cosI_in, T eta) {
     T cosI = clampT(cosI_in, T(0), T(1));
     T sin2T = eta * eta * (T(1) - cosI * cosI);
@@ -508,10 +516,12 @@ const uint32_t EV_NONE = 0, EV_DELTA = 1, EV_EVAL = 2, EV_OTHER = 3;
 const double LT_MIN_ALPHA = 0.05;
 template <class T> struct Lobes {
     V3<T> tX, tY, nZ, o, base, transTint, coatK, cm, ecO, ecAvg;
-    T a, aMin, r, metallic, trans, transl, eta, etaT, nrel, ps;
+    T ax, ay;                               // the alphas along tX and tY (tX the rough axis)
+    T aMin, r, metallic, trans, transl, eta, etaT, nrel, ps;
     bool isDelta;
     bool through = false;                   // the side beyond lit: the lobes below the surface evaluated
     const MfTables* tb;
+    A2<T> al() const { return A2<T>{ax, ay}; }
     V3<T> to_local(const V3<T>& w) const { return V3<T>(dot(w, tX), dot(w, tY), dot(w, nZ)); }
     V3<T> to_world(const V3<T>& w) const { return normalize(tX * w.x + tY * w.y + nZ * w.z); }
     V3<T> coat_fresnel(T cosI) const { return vmin(coatK * fresnel_dielectric(cosI, eta), T(1)); }
@@ -534,8 +544,12 @@ template <class T> inline Lobes<T> make_lobes(const V3<T>& n, const V3<T>& v, co
     lb.r = clampT(T(m.roughness), T(0), T(1));
     T aIso = lb.r * lb.r;
     lb.isDelta = aIso < T(ALPHA_MIN);
-    lb.aMin = aIso;
-    lb.a = clampT(aIso, T(ALPHA_MIN), T(1));
+    // anisotropy without a grain (microfacet.js mfAnisoAlpha): x the rough axis, ratio 1 / (1 - 0.9 |anisotropy|)
+    const T sa = std::sqrt(T(1) - T(0.9) * std::min(std::fabs(T(m.anisotropy)), T(1)));
+    const T ax = aIso / sa, ay = aIso * sa;
+    lb.aMin = std::min(ax, ay);
+    lb.ax = clampT(ax, T(ALPHA_MIN), T(1));
+    lb.ay = clampT(ay, T(ALPHA_MIN), T(1));
     lb.metallic = sat(T(m.metallic));
     T transm = transmission_override >= T(0) ? transmission_override : T(m.transmission);
     T spec = specular_override >= T(0) ? specular_override : T(m.specular);
@@ -569,7 +583,7 @@ template <class T> inline V3<T> lobes_eval(const Lobes<T>& lb, const V3<T>& l, T
     V3<T> f(0);
     if (!lb.isDelta && lb.aMin >= minAlpha) {
         V3<T> h = normalize(lb.o + i);
-        T spec = mf_d(h, lb.a) * mf_g2(lb.o, i, lb.a) / (T(4) * lb.o.z * i.z);
+        T spec = mf_d(h, lb.al()) * mf_g2(lb.o, i, lb.al()) / (T(4) * lb.o.z * i.z);
         T oh = dot(lb.o, h);
         f += lb.cm * lb.metal_fresnel(oh) * (lb.metallic * spec);
         f += lb.coat_fresnel(oh) * ((T(1) - lb.metallic) * spec);
@@ -611,7 +625,7 @@ template <class T> inline V3<T> lobes_through_eval(const Lobes<T>& lb, const V3<
     const T oh = dot(lb.o, h), ih = dot(i, h), den = lb.etaT * oh + ih;
     const V3<T> fc = lb.coat_fresnel(oh);
     return f + (V3<T>(1) - fc) * lb.transTint *
-               (wd * lb.trans * mf_d(h, lb.a) * mf_g2(lb.o, i, lb.a) * oh * (-ih) / (lb.o.z * (-i.z) * std::max(den * den, T(1e-20))));
+               (wd * lb.trans * mf_d(h, lb.al()) * mf_g2(lb.o, i, lb.al()) * oh * (-ih) / (lb.o.z * (-i.z) * std::max(den * den, T(1e-20))));
 }
 template <class T> inline T lobes_through_pdf(const Lobes<T>& lb, const V3<T>& i) {
     const T wd = T(1) - lb.metallic;
@@ -621,7 +635,7 @@ template <class T> inline T lobes_through_pdf(const Lobes<T>& lb, const V3<T>& i
     V3<T> h;
     if (!through_half(lb, i, h)) return p;
     const T oh = dot(lb.o, h), ih = dot(i, h), den = lb.etaT * oh + ih;
-    return p + wd * (T(1) - pd) * (T(1) - interface_reflect_p(lb, oh)) * mf_g1(lb.o, lb.a) * mf_d(h, lb.a) * oh / lb.o.z *
+    return p + wd * (T(1) - pd) * (T(1) - interface_reflect_p(lb, oh)) * mf_g1(lb.o, lb.al()) * mf_d(h, lb.al()) * oh / lb.o.z *
                    (-ih) / std::max(den * den, T(1e-20));
 }
 template <class T> inline T lobes_pdf(const Lobes<T>& lb, const V3<T>& l) {
@@ -632,7 +646,7 @@ template <class T> inline T lobes_pdf(const Lobes<T>& lb, const V3<T>& l) {
     T pd = (T(1) - lb.ps) * (T(1) - lb.trans);
     T p = wd * pd * (T(1) - lb.transl) * i.z / T(PI_D);
     if (!lb.isDelta) {
-        T pr = mf_pdf_reflect(lb.o, i, lb.a);
+        T pr = mf_pdf_reflect(lb.o, i, lb.al());
         p += (lb.metallic + wd * (T(1) - pd) * interface_reflect_p(lb, dot(lb.o, normalize(lb.o + i)))) * pr;
     }
     return p;
@@ -661,9 +675,9 @@ template <class T> inline LobeSample<T> lobes_sample(const Lobes<T>& lb, const T
             s.w = lb.metal_fresnel(lb.o.z) * lb.cm;
             s.ev = EV_DELTA; s.isDelta = true;
         } else {
-            V3<T> h = mf_sample_vndf(lb.o, lb.a, rnd[1], rnd[2]);
+            V3<T> h = mf_sample_vndf(lb.o, lb.al(), rnd[1], rnd[2]);
             i = reflectv(-lb.o, h);
-            if (i.z > T(0)) s.w = lb.cm * lb.metal_fresnel(dot(lb.o, h)) * (mf_g2(lb.o, i, lb.a) / mf_g1(lb.o, lb.a));
+            if (i.z > T(0)) s.w = lb.cm * lb.metal_fresnel(dot(lb.o, h)) * (mf_g2(lb.o, i, lb.al()) / mf_g1(lb.o, lb.al()));
             s.ev = glossyEv;
         }
     } else {
@@ -682,20 +696,20 @@ template <class T> inline LobeSample<T> lobes_sample(const Lobes<T>& lb, const T
                 }
                 s.ev = EV_DELTA; s.isDelta = true;
             } else {
-                V3<T> h = mf_sample_vndf(lb.o, lb.a, rnd[1], rnd[2]);
+                V3<T> h = mf_sample_vndf(lb.o, lb.al(), rnd[1], rnd[2]);
                 T oh = dot(lb.o, h);
                 V3<T> fc = lb.coat_fresnel(oh);
                 T r = interface_reflect_p(lb, oh);
                 if (sub < r) {                                                       // glossy coat
                     i = reflectv(-lb.o, h);
-                    if (i.z > T(0)) s.w = fc * (mf_g2(lb.o, i, lb.a) / mf_g1(lb.o, lb.a) / ((T(1) - pd) * r));
+                    if (i.z > T(0)) s.w = fc * (mf_g2(lb.o, i, lb.al()) / mf_g1(lb.o, lb.al()) / ((T(1) - pd) * r));
                     s.ev = glossyEv;
                 } else {                                                             // rough refraction
                     s.transmitted = true;
                     i = refractv(-lb.o, h, lb.etaT);
                     if (i.z < T(0))
                         s.w = (V3<T>(1) - fc) * lb.transTint *
-                              (lb.trans * mf_g2(lb.o, i, lb.a) / mf_g1(lb.o, lb.a) / ((T(1) - pd) * (T(1) - r)));
+                              (lb.trans * mf_g2(lb.o, i, lb.al()) / mf_g1(lb.o, lb.al()) / ((T(1) - pd) * (T(1) - r)));
                     s.ev = lb.aMin >= T(LT_MIN_ALPHA) ? EV_EVAL : EV_OTHER;
                 }
             }

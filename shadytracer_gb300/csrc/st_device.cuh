@@ -644,29 +644,31 @@ __device__ __forceinline__ float haze_tr(const Uni& u, f3 A, f3 d, float len) {
 #define MF_ALPHA_MIN 1e-3f
 struct MfTab { const float* __restrict__ ec; const float* __restrict__ ecavg; const float* __restrict__ e1; };
 
-__device__ __forceinline__ float mf_lambda(f3 w, float a) {
+// the two alphas along the local x and y (microfacet.js mfAnisoAlpha); an isotropic lobe's are equal, and then every
+// number below is the one the isotropic formulas give
+__device__ __forceinline__ float mf_lambda(f3 w, float2 a) {
     float z2 = fmaxf(w.z * w.z, 1e-12f);
-    float t2 = (a * a * w.x * w.x + a * a * w.y * w.y) / z2;
+    float t2 = (a.x * a.x * w.x * w.x + a.y * a.y * w.y * w.y) / z2;
     return 0.5f * (-1.f + sqrtf(1.f + t2));
 }
-__device__ __forceinline__ float mf_g1(f3 w, float a) { return 1.f / (1.f + mf_lambda(w, a)); }
-__device__ __forceinline__ float mf_g2(f3 o, f3 i, float a) { return 1.f / (1.f + mf_lambda(o, a) + mf_lambda(i, a)); }
-__device__ __forceinline__ float mf_d(f3 h, float a) {
+__device__ __forceinline__ float mf_g1(f3 w, float2 a) { return 1.f / (1.f + mf_lambda(w, a)); }
+__device__ __forceinline__ float mf_g2(f3 o, f3 i, float2 a) { return 1.f / (1.f + mf_lambda(o, a) + mf_lambda(i, a)); }
+__device__ __forceinline__ float mf_d(f3 h, float2 a) {
     if (h.z <= 0.f) return 0.f;
-    float t = (h.x * h.x) / (a * a) + (h.y * h.y) / (a * a) + h.z * h.z;
-    return 1.f / (ST_PI * a * a * t * t);
+    float t = (h.x * h.x) / (a.x * a.x) + (h.y * h.y) / (a.y * a.y) + h.z * h.z;
+    return 1.f / (ST_PI * a.x * a.y * t * t);
 }
-__device__ __forceinline__ f3 mf_sample_vndf(f3 o, float a, float u0, float u1) {
-    f3 os = normalize(mk(o.x * a, o.y * a, o.z));
+__device__ __forceinline__ f3 mf_sample_vndf(f3 o, float2 a, float u0, float u1) {
+    f3 os = normalize(mk(o.x * a.x, o.y * a.y, o.z));
     float z = (1.f - u1) * (1.f + os.z) - os.z;
     float sinT = sqrtf(clampf(1.f - z * z, 0.f, 1.f));
     float sp, cp;
     sincosf(2.f * ST_PI * u0, &sp, &cp);
     f3 c = mk(sinT * cp, sinT * sp, z);
     f3 hs = c + os;
-    return normalize(mk(hs.x * a, hs.y * a, fmaxf(hs.z, 1e-7f)));
+    return normalize(mk(hs.x * a.x, hs.y * a.y, fmaxf(hs.z, 1e-7f)));
 }
-__device__ __forceinline__ float mf_pdf_reflect(f3 o, f3 i, float a) {
+__device__ __forceinline__ float mf_pdf_reflect(f3 o, f3 i, float2 a) {
     if (o.z <= 0.f || i.z <= 0.f) return 0.f;
     f3 h = normalize(o + i);
     return mf_g1(o, a) * mf_d(h, a) / (4.f * o.z);
@@ -680,6 +682,12 @@ __device__ __forceinline__ float fresnel_dielectric(float cosI_in, float eta) {
     float rp = (cosI - eta * cosT) / (cosI + eta * cosT);
     return 0.5f * (rs * rs + rp * rp);
 }
+__device__ __forceinline__ float mf_lambda(f3 w, float a) { return mf_lambda(w, make_float2(a, a)); }
+__device__ __forceinline__ float mf_g1(f3 w, float a) { return mf_g1(w, make_float2(a, a)); }
+__device__ __forceinline__ float mf_g2(f3 o, f3 i, float a) { return mf_g2(o, i, make_float2(a, a)); }
+__device__ __forceinline__ float mf_d(f3 h, float a) { return mf_d(h, make_float2(a, a)); }
+__device__ __forceinline__ f3 mf_sample_vndf(f3 o, float a, float u0, float u1) { return mf_sample_vndf(o, make_float2(a, a), u0, u1); }
+__device__ __forceinline__ float mf_pdf_reflect(f3 o, f3 i, float a) { return mf_pdf_reflect(o, i, make_float2(a, a)); }
 __device__ __forceinline__ f3 fresnel_schlick3(float cosI, f3 f0) {
     float m = 1.f - clampf(cosI, 0.f, 1.f);
     float m5 = m * m * m * m * m;
@@ -747,9 +755,11 @@ __host__ __device__ __forceinline__ float refract_share_of(float transmission, f
 }
 struct Lobes {
     f3 tX, tY, nZ, o, base, transTint, coatK, cm, ecO, ecAvg;
-    float a, aMin, r, metallic, trans, transl, eta, etaT, nrel, ps;
+    float ax, ay;      // the alphas along tX and tY (tX the rough axis of an anisotropic lobe)
+    float aMin, r, metallic, trans, transl, eta, etaT, nrel, ps;
     bool isDelta;
     bool through;      // THE SIDE BEYOND lit (materials_pbr.js:1176-1190): the lobes below the surface evaluated
+    __device__ __forceinline__ float2 al() const { return make_float2(ax, ay); }
     __device__ __forceinline__ f3 to_local(f3 w) const { return mk(dot(w, tX), dot(w, tY), dot(w, nZ)); }
     __device__ __forceinline__ f3 to_world(f3 w) const { return normalize(tX * w.x + tY * w.y + nZ * w.z); }
     __device__ __forceinline__ f3 coat_fresnel(float cosI) const { return vmin(coatK * fresnel_dielectric(cosI, eta), 1.f); }
@@ -769,8 +779,13 @@ __device__ __forceinline__ Lobes make_lobes(f3 n, f3 v, const st_material& m, fl
     lb.r = clampf(m.roughness, 0.f, 1.f);
     float aIso = lb.r * lb.r;
     lb.isDelta = aIso < MF_ALPHA_MIN;
-    lb.aMin = aIso;
-    lb.a = clampf(aIso, MF_ALPHA_MIN, 1.f);
+    // ANISOTROPY (microfacet.js mfAnisoAlpha; materials_pbr.js:185-194, without a grain): x the rough axis, the two
+    // alphas' geometric mean r^2, their ratio 1 / (1 - 0.9 |anisotropy|) -- at most 10
+    const float sa = sqrtf(1.f - 0.9f * fminf(fabsf(m.anisotropy), 1.f));
+    const float ax = aIso / sa, ay = aIso * sa;
+    lb.aMin = fminf(ax, ay);
+    lb.ax = clampf(ax, MF_ALPHA_MIN, 1.f);
+    lb.ay = clampf(ay, MF_ALPHA_MIN, 1.f);
     lb.metallic = sat(m.metallic);
     // TRANSMISSION AND HAZE (materials_pbr.js:196-204): T (1 - H) refracts; of the diffuse base, the share transl
     // passes through (T H of the whole)
@@ -802,7 +817,7 @@ __device__ __forceinline__ f3 lobes_eval(const Lobes& lb, const MfTab& t, f3 l, 
     f3 f = mk(0.f);
     if (!lb.isDelta && lb.aMin >= minAlpha) {
         f3 h = normalize(lb.o + i);
-        float spec = mf_d(h, lb.a) * mf_g2(lb.o, i, lb.a) / (4.f * lb.o.z * i.z);
+        float spec = mf_d(h, lb.al()) * mf_g2(lb.o, i, lb.al()) / (4.f * lb.o.z * i.z);
         float oh = dot(lb.o, h);
         f = f + lb.cm * lb.metal_fresnel(oh) * (lb.metallic * spec);
         f = f + lb.coat_fresnel(oh) * ((1.f - lb.metallic) * spec);
@@ -847,7 +862,7 @@ __device__ __forceinline__ f3 lobes_through_eval(const Lobes& lb, const MfTab& t
     const float oh = dot(lb.o, h), ih = dot(i, h), den = lb.etaT * oh + ih;
     const f3 fc = lb.coat_fresnel(oh);
     return f + (mk(1.f) - fc) * lb.transTint *
-               (wd * lb.trans * mf_d(h, lb.a) * mf_g2(lb.o, i, lb.a) * oh * (-ih) /
+               (wd * lb.trans * mf_d(h, lb.al()) * mf_g2(lb.o, i, lb.al()) * oh * (-ih) /
                 (lb.o.z * (-i.z) * fmaxf(den * den, 1e-20f)));
 }
 __device__ __forceinline__ float lobes_through_pdf(const Lobes& lb, f3 i) {
@@ -859,7 +874,7 @@ __device__ __forceinline__ float lobes_through_pdf(const Lobes& lb, f3 i) {
     if (hh.w == 0.f) return p;
     const f3 h = mk(hh.x, hh.y, hh.z);
     const float oh = dot(lb.o, h), ih = dot(i, h), den = lb.etaT * oh + ih;
-    return p + wd * (1.f - pd) * (1.f - interface_reflect_p(lb, oh)) * mf_g1(lb.o, lb.a) * mf_d(h, lb.a) * oh / lb.o.z *
+    return p + wd * (1.f - pd) * (1.f - interface_reflect_p(lb, oh)) * mf_g1(lb.o, lb.al()) * mf_d(h, lb.al()) * oh / lb.o.z *
                    (-ih) / fmaxf(den * den, 1e-20f);
 }
 __device__ __forceinline__ float lobes_pdf(const Lobes& lb, f3 l) {
@@ -870,7 +885,7 @@ __device__ __forceinline__ float lobes_pdf(const Lobes& lb, f3 l) {
     float pd = (1.f - lb.ps) * (1.f - lb.trans);
     float p = wd * pd * (1.f - lb.transl) * i.z / ST_PI;
     if (!lb.isDelta) {
-        float pr = mf_pdf_reflect(lb.o, i, lb.a);
+        float pr = mf_pdf_reflect(lb.o, i, lb.al());
         p += (lb.metallic + wd * (1.f - pd) * interface_reflect_p(lb, dot(lb.o, normalize(lb.o + i)))) * pr;
     }
     return p;
@@ -898,9 +913,9 @@ __device__ __forceinline__ LobeSample lobes_sample(const Lobes& lb, const MfTab&
             s.w = lb.metal_fresnel(lb.o.z) * lb.cm;
             s.ev = EV_DELTA; s.isDelta = true;
         } else {
-            f3 h = mf_sample_vndf(lb.o, lb.a, rnd.y, rnd.z);
+            f3 h = mf_sample_vndf(lb.o, lb.al(), rnd.y, rnd.z);
             i = reflectv(-lb.o, h);
-            if (i.z > 0.f) s.w = lb.cm * lb.metal_fresnel(dot(lb.o, h)) * (mf_g2(lb.o, i, lb.a) / mf_g1(lb.o, lb.a));
+            if (i.z > 0.f) s.w = lb.cm * lb.metal_fresnel(dot(lb.o, h)) * (mf_g2(lb.o, i, lb.al()) / mf_g1(lb.o, lb.al()));
             s.ev = glossyEv;
         }
     } else {
@@ -919,20 +934,20 @@ __device__ __forceinline__ LobeSample lobes_sample(const Lobes& lb, const MfTab&
                 }
                 s.ev = EV_DELTA; s.isDelta = true;
             } else {
-                f3 h = mf_sample_vndf(lb.o, lb.a, rnd.y, rnd.z);
+                f3 h = mf_sample_vndf(lb.o, lb.al(), rnd.y, rnd.z);
                 float oh = dot(lb.o, h);
                 f3 fc = lb.coat_fresnel(oh);
                 float r = interface_reflect_p(lb, oh);
                 if (sub < r) {
                     i = reflectv(-lb.o, h);
-                    if (i.z > 0.f) s.w = fc * (mf_g2(lb.o, i, lb.a) / mf_g1(lb.o, lb.a) / ((1.f - pd) * r));
+                    if (i.z > 0.f) s.w = fc * (mf_g2(lb.o, i, lb.al()) / mf_g1(lb.o, lb.al()) / ((1.f - pd) * r));
                     s.ev = glossyEv;
                 } else {
                     s.transmitted = true;
                     i = refractv(-lb.o, h, lb.etaT);
                     if (i.z < 0.f)
                         s.w = (mk(1.f) - fc) * lb.transTint *
-                              (lb.trans * mf_g2(lb.o, i, lb.a) / mf_g1(lb.o, lb.a) / ((1.f - pd) * (1.f - r)));
+                              (lb.trans * mf_g2(lb.o, i, lb.al()) / mf_g1(lb.o, lb.al()) / ((1.f - pd) * (1.f - r)));
                     s.ev = lb.aMin >= 0.05f ? EV_EVAL : EV_OTHER;
                 }
             }

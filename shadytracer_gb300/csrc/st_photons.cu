@@ -330,6 +330,7 @@ struct GatherQuery {
     uint32_t side;        // bit k: the neighbour along axis k is on the + side
     uint32_t a0[8];       // each cell's first record
     uint32_t pre[9];      // the records of the cells before each; pre[8] their total
+    uint32_t pad;         // to an odd number of words
 };
 // an odd number of words, so lanes reading one field of 32 different queries meet 32 different banks
 static_assert(sizeof(GatherQuery) % 8 == 4, "GatherQuery: an odd word stride");

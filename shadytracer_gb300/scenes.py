@@ -693,3 +693,25 @@ def translucent_sun(kind="opal", width=64, height=48, maxbounce=12, seed=1):
                               sun_illuminance=100000.0, sky_luminance=3000.0, ground_luminance=0.0, seed=seed)
     s.view = look_at((0.0, -3.0, 1.2), (0.0, 0.0, 0.3), 35.0, width / height)
     return s
+
+
+def aniso_spheres(anisotropy=0.8, width=64, height=48, maxbounce=8, seed=1, furnace=False):
+    """Anisotropic gloss (microfacet.js mfAnisoAlpha; materials_pbr.js:185-194): a rough gold-ish metal sphere and a
+    glossy plastic one whose lobes are stretched along their first tangent, on a grey floor under the sun and sky (or
+    in the white furnace)."""
+    m1 = metal((0.95, 0.8, 0.5), 0.5)
+    m2 = plastic((0.2, 0.4, 0.8), 0.4)
+    m1.anisotropy = anisotropy
+    m2.anisotropy = anisotropy
+    s = Scene([prim(ST_PRIM_PLANE, material=1), prim(ST_PRIM_SPHERE, pos=(-0.6, 0.0, 0.5), params=(0.5,), material=2),
+               prim(ST_PRIM_SPHERE, pos=(0.6, 0.0, 0.5), params=(0.5,), material=3)],
+              [air(), diffuse((0.5, 0.5, 0.5)), m1, m2], env_radius=20.0, name="aniso")
+    if furnace:
+        s.params = default_params(width=width, height=height, maxbounce=maxbounce, env_uniform=1000.0, sun_hint=0,
+                                  seed=seed)
+    else:
+        s.params = default_params(width=width, height=height, maxbounce=maxbounce, sun_elevation=35.0,
+                                  sun_azimuth=200.0, sun_illuminance=100000.0, sky_luminance=3000.0,
+                                  ground_luminance=0.0, seed=seed)
+    s.view = look_at((0.0, -3.5, 1.4), (0.0, 0.0, 0.45), 35.0, width / height)
+    return s

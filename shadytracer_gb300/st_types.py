@@ -34,7 +34,7 @@ class StMaterial(C.Structure):
                 ("roughness", C.c_float), ("specular", C.c_float), ("specular_tint", C.c_float),
                 ("transmission", C.c_float), ("ior", C.c_float), ("abbe", C.c_float),
                 ("attenuation", C.c_float), ("detector", C.c_float),
-                ("emissive", C.c_float * 3), ("beam_cos", C.c_float), ("haze", C.c_float), ("pad", C.c_float * 3)]
+                ("emissive", C.c_float * 3), ("beam_cos", C.c_float), ("haze", C.c_float), ("anisotropy", C.c_float), ("pad", C.c_float * 2)]
 
 
 ST_LIGHT_DISC, ST_LIGHT_RECTANGLE = 1, 2

@@ -73,3 +73,15 @@ def test_light_through_the_face_is_unbiased():
     (m1, e1), (m0, e0) = out[1], out[0]
     assert abs(m1 - m0) < 5 * math.hypot(e1, e0) + 1e-3 * m0, out
     assert e0 * math.sqrt(1024 / 128) > 2 * e1, out
+
+
+@pytest.mark.parametrize("furnace", [False, True])
+def test_anisotropic_gloss_matches_the_oracle(furnace):
+    """Anisotropic metal and plastic spheres (microfacet.js mfAnisoAlpha), under the sun and in the furnace: GPU
+    against the oracle's restatement, pixel by pixel."""
+    s = scenes.aniso_spheres(0.8, width=48, height=36, furnace=furnace)
+    L, se, ctr = render(s, 128)
+    ref = oracle.render(s, 128)
+    frac, zm = z_parity(L, se, ref)
+    assert frac > 0.98 and abs(zm) < 5, (frac, zm)
+    assert ctr["nonfinite"] == 0

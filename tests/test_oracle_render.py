@@ -182,3 +182,19 @@ def test_translucent_furnace(kind):
         assert abs(m0 / 1000.0 - 1) < 0.01 + 5 * e0 / 1000.0, out
     else:
         assert 0.8 < m0 / 1000.0 < 0.95, out
+
+
+def test_anisotropic_gloss_light_sampling_is_unbiased():
+    """Anisotropic lobes (microfacet.js mfAnisoAlpha): the light sample's MIS weights and the BSDF's draw agree on the
+    stretched lobes' density -- the same picture with light sampling on and off -- and the stretch changes it."""
+    out = []
+    for nee, n in ((1, 128), (0, 512)):
+        s = scenes.aniso_spheres(0.8, width=32, height=24)
+        s.params.nee = nee
+        r = oracle.render(s, n)
+        out.append((r.luma().mean(), math.sqrt(np.nansum(r.se() ** 2)) / r.luma().size))
+    (m1, e1), (m0, e0) = out
+    assert abs(m1 - m0) < 5 * math.hypot(e1, e0) + 1e-3 * m0, out
+    iso = oracle.render(scenes.aniso_spheres(0.0, width=32, height=24), 128).luma()
+    an = oracle.render(scenes.aniso_spheres(0.8, width=32, height=24), 128).luma()
+    assert np.abs(an - iso).max() > 0.05 * iso.max()
