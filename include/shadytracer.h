@@ -450,7 +450,8 @@ int  st_emit_list(st_ctx* ctx, float* out, uint32_t max_n, uint32_t* n);
  * more than 256 primitives or materials, returns ST_ERR_ARG. Each call clears the accumulation and counters it keeps
  * in the shared array and runs on the device's legacy default stream; calls that overlap on one GPU race, so a host
  * serialises them. The first call on a device does the set-up (the array's address, the albedo tables) and should
- * come before any stream capture. The result equals st_step's for the same inputs. */
+ * come before any stream capture. The result equals st_step's for the same inputs, the step cache off (this
+ * render marches without it) and no light faces (a scene with them is refused here). */
 #define ST_NOALLOC_MAX_PIXELS (128u * 128u)
 #define ST_NOALLOC_SCRATCH_BYTES (8u << 20)
 int  st_render_noalloc(int device, const st_scene_desc* desc, const st_params* p, const st_view* v, int nsamples,
