@@ -451,6 +451,18 @@ inline void shade_hit(const Ctx<T>& C, Ray<T>& r, T dhit, Rng& rng, Rng& grng, b
     }
     SceneHit<T> h = scene_eval(*C.s, r.pos);
     const st_material& m = C.s->materials[std::min(h.m, C.s->n_materials - 1)];
+    // ABSORPTION INSIDE (tracebasics.js absorbAlong; materials.js:125-133 mediumMu): met from inside, the ray crossed
+    // this material from its last arrival: exp(-mu d) a channel, mu = -ln(base) / attenuationDistance
+    if (inside && m.attenuation > 0.f) {
+        const T d = std::max(r.ltot - r.absLtot, T(0)) / std::max(r.n, T(1e-4));
+        const T ia = T(1) / T(m.attenuation);
+        V3<T> tr;
+        tr.x = std::exp(std::log(std::min(std::max(T(m.base[0]), T(1e-6)), T(1))) * ia * d);
+        tr.y = std::exp(std::log(std::min(std::max(T(m.base[1]), T(1e-6)), T(1))) * ia * d);
+        tr.z = std::exp(std::log(std::min(std::max(T(m.base[2]), T(1e-6)), T(1))) * ia * d);
+        r.beta = r.beta * tr;
+    }
+    r.absLtot = r.ltot;                                                            // absorbAlong: arrival here
     V3<T> emis(T(m.emissive[0]), T(m.emissive[1]), T(m.emissive[2]));
     // THE PHOTON MAP'S GATHER (wavefront.js:1196-1212), before the shading: a camera ray with delta events only since
     // the eye, on an evaluable surface, takes sum f Phi / (pi r^2) / n^2 into its radiance
@@ -868,8 +880,8 @@ void trace_path(const Ctx<T>& C, U4 sseed, uint32_t tile, const st_view& v, uint
         Rng rng = path_rng(sseed, tile, 1 + seg);
         Rng grng = path_rng(sseed, tile, SPPM_STORE_SALT + seg);                   // the gather's own stream
         seg++;
-        r.absLtot = r.ltot;                                                        // absorbAlong on arrival
         if (r.state == RAY_SCATTER) {
+            r.absLtot = r.ltot;                                                    // absorbAlong on arrival
             medium_vertex(C, r, rng, last, fr, st);
             r.lens = 0;                                                            // haze.js:539
         } else {

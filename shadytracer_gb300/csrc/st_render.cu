@@ -444,7 +444,8 @@ __device__ __forceinline__ void shade_surface(const WaveArgs& a, const st_materi
                                               f3& pos, f3& dir, float& ltot, float& n, f3& beta, float& sunmis,
                                               f3& rad, uint32_t& bounces, uint32_t& state, float& lam,
                                               uint32_t& lens, float dh, Rng& rng, bool last, ShadowOut& sh,
-                                              uint32_t q, uint32_t& my, uint32_t gpix, float& emw, float2& lp) {
+                                              uint32_t q, uint32_t& my, uint32_t gpix, float& emw, float2& lp,
+                                              float& absL) {
     const Uni& u = a.u;
     float eps = march_tol(pos, u.tol);
     const uint32_t ids = __float_as_uint(surf.w);
@@ -459,6 +460,16 @@ __device__ __forceinline__ void shade_surface(const WaveArgs& a, const st_materi
     }
     bounces += 1;
     const st_material& m = sm[ids & 0xffffu];
+    // ABSORPTION INSIDE (tracebasics.js absorbAlong; materials.js:125-133 mediumMu): a ray met from inside crossed this
+    // material's volume from where it arrived last (absL): exp(-mu d) a channel, mu = -ln(base) / attenuationDistance
+    if (inside && m.attenuation > 0.f) {
+        const float d = fmaxf(ltot - absL, 0.f) / fmaxf(n, 1e-4f);
+        const float ia = 1.f / m.attenuation;
+        beta = beta * mk(__expf(logf(fminf(fmaxf(m.base[0], 1e-6f), 1.f)) * ia * d),
+                         __expf(logf(fminf(fmaxf(m.base[1], 1e-6f), 1.f)) * ia * d),
+                         __expf(logf(fminf(fmaxf(m.base[2], 1e-6f), 1.f)) * ia * d));
+    }
+    absL = ltot;                                                      // absorbAlong: arrival here
     const uint32_t fid = a.lf.n ? (uint32_t)a.lf.of[ids & 0xffu] : 0u;
     if (fid) {                                                        // a light's face (codegen LIGHTS)
         // its luminance at this angle from its own normal over n^2 of the medium met in, weighed past the first
@@ -794,8 +805,9 @@ __global__ void __launch_bounds__(256) k_shade(WaveArgs a, int nxt, int side, in
                 uint32_t tile = slot % u.P, j = slot / u.P;
                 Rng rng = path_rng(sample_seed(u.seed, a.ctr->sample + j), tile, 1u + seg);
                 seg += 1;
-                m4.w = __float_as_uint(ltot);                         // absorbAlong: absLtot on arrival
+                float absL = __uint_as_float(m4.w);                   // absorbAlong: ltot on arrival at the last vertex
                 if (state == RAY_SCATTER) {
+                    m4.w = __float_as_uint(ltot);
                     shade_medium(a, pos, dir, beta, sunmis, bounces, state, n, rng, last != 0, sh, emw, ltot, lp);
                     m4.y &= ~(3u << META_LENS_SHIFT);                 // haze.js:539: the air is no delta event
                 }
@@ -804,7 +816,8 @@ __global__ void __launch_bounds__(256) k_shade(WaveArgs a, int nxt, int side, in
                     lam = a.pb.lam[slot];
                     uint32_t lens = (m4.y >> META_LENS_SHIFT) & 3u;
                     shade_surface<GUIDE>(a, sm, a.q.hsurf[q], pos, dir, ltot, n, beta, sunmis, rad, bounces, state,
-                                         lam, lens, dh, rng, last != 0, sh, q, m4.y, gpix, emw, lp);
+                                         lam, lens, dh, rng, last != 0, sh, q, m4.y, gpix, emw, lp, absL);
+                    m4.w = __float_as_uint(absL);                     // kept where a leaving face moved the ray on
                     m4.y = (m4.y & ~(3u << META_LENS_SHIFT)) | (lens << META_LENS_SHIFT);
                 }
                 if (state == RAY_ACTIVE) {

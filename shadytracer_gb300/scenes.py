@@ -715,3 +715,25 @@ def aniso_spheres(anisotropy=0.8, width=64, height=48, maxbounce=8, seed=1, furn
                                   ground_luminance=0.0, seed=seed)
     s.view = look_at((0.0, -3.5, 1.4), (0.0, 0.0, 0.45), 35.0, width / height)
     return s
+
+
+def absorbing_box(width=32, height=32, base=(0.5, 0.25, 0.8), attenuation=1.0, sky=1000.0, seed=1):
+    """Absorption inside (tracebasics.js absorbAlong; materials.js mediumMu): a 1 m cube of a clear material of index 1
+    (no reflection, no bending) that takes its colour `base` off light over `attenuation` metres, seen straight through
+    by an orthographic camera against the white furnace: every ray through it reads sky x base^(1 / attenuation)."""
+    m = material(base=base, roughness=0.0, specular=0.0, transmission=1.0, ior=1.0, attenuation=attenuation)
+    s = Scene([prim(ST_PRIM_BOX, pos=(0.0, 0.0, 0.0), params=(0.5, 0.5, 0.5), material=1)], [air(), m],
+              env_radius=20.0, name="absorbing-box")
+    # a fine march tolerance: the path inside is the cube's width less up to a tolerance at each face
+    s.params = default_params(width=width, height=height, maxbounce=8, env_uniform=sky, sun_hint=0, seed=seed, eps=1e-5)
+    v = StView()
+    for i, c in enumerate((0.0, -3.0, 0.0)):
+        v.cam_pos[i] = c
+    for i in range(3):
+        v.right[i] = (1.0, 0.0, 0.0)[i]
+        v.up[i] = (0.0, 0.0, 1.0)[i]
+        v.fwd[i] = (0.0, -1.0, 0.0)[i]
+    v.fx, v.fy, v.camtype = 0.4, 0.4, 1
+    s.view = v
+    s.info = {"expected": [sky * b ** (1.0 / attenuation) for b in base]}
+    return s

@@ -85,3 +85,14 @@ def test_anisotropic_gloss_matches_the_oracle(furnace):
     frac, zm = z_parity(L, se, ref)
     assert frac > 0.98 and abs(zm) < 5, (frac, zm)
     assert ctr["nonfinite"] == 0
+
+
+def test_absorption_inside_closed_form():
+    """Beer-Lambert inside a material (absorbAlong): every ray through the 1 m cube reads the sky times base^(1 / d),
+    each channel, on the GPU as in the oracle."""
+    from shadytracer_gb300.renderer import create_path_tracer
+    s = scenes.absorbing_box()
+    with create_path_tracer(s, device=0) as r:
+        r.step(4)
+        rgb = r.read_accum()[0]
+    assert np.allclose(rgb.reshape(-1, 3), s.info["expected"], rtol=5e-5)

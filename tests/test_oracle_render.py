@@ -198,3 +198,11 @@ def test_anisotropic_gloss_light_sampling_is_unbiased():
     iso = oracle.render(scenes.aniso_spheres(0.0, width=32, height=24), 128).luma()
     an = oracle.render(scenes.aniso_spheres(0.8, width=32, height=24), 128).luma()
     assert np.abs(an - iso).max() > 0.05 * iso.max()
+
+
+def test_absorption_inside_closed_form():
+    """Beer-Lambert inside a material (absorbAlong): every ray through the 1 m cube reads the sky times base^(1 / d)."""
+    s = scenes.absorbing_box()
+    r = oracle.render(s, 4)
+    # the march stops within its tolerance (1e-5 m) of each face
+    assert np.allclose(r.rgb.reshape(-1, 3), s.info["expected"], rtol=5e-5)
