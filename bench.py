@@ -216,7 +216,7 @@ def run_reference(args):
     line = {"impl": "reference", "metric": metric, "value": v, "unit": "Mpaths/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / max(args.steps, 1),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": config_of(s),
+            "config": dict(config_of(s), step_cache="off: the oracle marches the distance field at every step"),
             "cpu_baseline": {"value": v, "unit": "Mpaths/s", "cores": os.cpu_count(), "kind": "port",
                              "sample": "each step: " + samples[-1]},
             "e2e": {"value": v, "unit": "Mpaths/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
