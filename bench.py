@@ -83,6 +83,22 @@ def dist_env():
     return rank, world, local
 
 
+def reduce_max(x, dist=None, device="cpu"):
+    """The largest of every rank's x -- the slowest rank's time -- over the process group (x itself with none)."""
+    if not dist:
+        return float(x)
+    import torch
+    t = torch.tensor([float(x)], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_value(world, paths_per_step, ms):
+    """Replicas (weak scaling): every rank renders the whole workload, so the job's paths a second are the ranks'
+    paths over the slowest rank's time, in millions."""
+    return world * paths_per_step / (ms / 1e3) / 1e6
+
+
 def workload(small, spp=0):
     from shadytracer_gb300 import scenes
     if small:
@@ -689,11 +705,8 @@ def run_ours(args):
     clocks = clk.summary()
     c = rt.counters()
     launches = c["launches"] - launches0          # the library's kernels (graph nodes) in the timed region
-    if dist:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    value = world * paths_per_step / (ms / 1e3) / 1e6
+    ms = reduce_max(ms, dist, "cuda")
+    value = replica_value(world, paths_per_step, ms)
 
     # ---- e2e: through the C ABI from host memory, the picture read back every step ----
     rgb = np.zeros((p.height, p.width, 3), np.float64)
@@ -713,10 +726,7 @@ def run_ours(args):
                         cnt.ctypes.data_as(Pv))
     barrier()
     e2e_s = (time.perf_counter() - t0) / args.steps
-    if dist:
-        t = torch.tensor([e2e_s], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = reduce_max(e2e_s, dist, "cuda")
     h2d = (C.sizeof(type(s.prims)) + C.sizeof(type(s.materials)) + C.sizeof(p) + C.sizeof(s.view))
     d2h = P * (32 + 16)
     Lmean = float((rgb @ np.array([0.2126, 0.7152, 0.0722])).mean())
