@@ -273,6 +273,7 @@ typedef struct st_kernel_time {
 /* ---- life cycle ---- */
 int  st_create(int device, st_ctx** out);
 int  st_destroy(st_ctx* ctx);
+/* ctx NULL: why the calling thread's last st_render_noalloc was refused ("no context" if it was not) */
 const char* st_last_error(const st_ctx* ctx);
 int  st_abi_version(void);
 
@@ -301,6 +302,13 @@ int  st_invalidate(st_ctx* ctx);
 int  st_step(st_ctx* ctx, int n);             /* n samples; returns when the GPU has finished       */
 int  st_step_async(st_ctx* ctx, int n);       /* queue n samples                                    */
 int  st_sync(st_ctx* ctx, int timeout_ms);    /* wait for the queued samples; <0 waits forever      */
+/* THE DEVICE-SIDE WAITS (the guard the reference keeps on the host: core/wavefront.js:298-303 clamps an indirect
+ * dispatch that could run forever, core/raytrace_main.js:67 cuts a frame's submissions short): every kernel that stages
+ * a table into shared memory waits for its copy at most `iterations` times (0: the default, 2^24), then flags the
+ * error and returns; st_sync then reports ST_ERR_TIMEOUT once (the flag is cleared) and the context stays usable --
+ * st_invalidate before trusting the picture again. arm_only 1 is the test of that path: the waits are armed but no
+ * copy is issued, so each runs out at its limit with nothing in flight. Kept until changed. */
+int  st_set_wait_limit(st_ctx* ctx, uint32_t iterations, int arm_only);
 
 /* ---- readings (caller-owned buffers, width*height entries each; NULL skips one) ---- */
 int  st_read_accum(st_ctx* ctx, double* rgb, double* V, double* S, uint32_t* count);
@@ -344,6 +352,11 @@ int  st_sppm_gather(st_ctx* ctx, const float* qpos, const float* qnrm, const flo
                     const uint32_t* qbounce, uint32_t m, float radius, uint32_t maxbounce,
                     uint32_t budget, uint32_t seed, double* out);
 int  st_sppm_stats_read(st_ctx* ctx, st_sppm_stats* out);
+/* THE LEARNED EMISSION MAP (st_params.sppm_learn; core/wavefront.js:628-711 ltEmit / ltHit / ltCdf, prog_lt_build), as
+ * the last sample left it: per cell of the 128 x 128 square the sun's photons cross, the photons sent through it and
+ * those stored (128^2 each, halved at every rebuild), and the CDF they are drawn from (128^2 conditional row entries,
+ * then 128 rows). NULL skips one. ST_ERR_STATE before the photon map has run. */
+int  st_sppm_emission_map(st_ctx* ctx, uint32_t* sent, uint32_t* stored, float* cdf);
 
 /* ---- the optics bench (optics/index.js, optics/kernels.js) ---- */
 typedef struct st_optics_source {
@@ -450,8 +463,10 @@ int  st_emit_list(st_ctx* ctx, float* out, uint32_t max_n, uint32_t* n);
  * more than 256 primitives or materials, returns ST_ERR_ARG. Each call clears the accumulation and counters it keeps
  * in the shared array and runs on the device's legacy default stream; calls that overlap on one GPU race, so a host
  * serialises them. The first call on a device does the set-up (the array's address, the albedo tables) and should
- * come before any stream capture. The result equals st_step's for the same inputs, the step cache off (this
- * render marches without it) and no light faces (a scene with them is refused here). */
+ * come before any stream capture. The caller's current device is as it was when the call returns. The result equals
+ * st_step's for the same inputs. What this render does not carry is refused with ST_ERR_ARG, and
+ * st_last_error(NULL) says why: light faces, st_params.sppm, st_params.guide, st_params.step_cache, and an emissive
+ * material unless st_params.emit_off is set (then both paths render it by the BSDF's hits alone). */
 #define ST_NOALLOC_MAX_PIXELS (128u * 128u)
 #define ST_NOALLOC_SCRATCH_BYTES (8u << 20)
 int  st_render_noalloc(int device, const st_scene_desc* desc, const st_params* p, const st_view* v, int nsamples,

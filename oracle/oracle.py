@@ -242,6 +242,8 @@ def _declare_extra(L):
         "sto_guide_mix_pdf": ([P, P], C.c_double),
         "sto_guide_mix_sample": ([P, P, C.c_uint32, P], None),
         "sto_bf16": ([C.c_float], C.c_float),
+        "sto_lt_build": ([P, P, P], None),
+        "sto_last_lt": ([P, P, P], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -285,6 +287,30 @@ def sppm_unoct(w):
     o = np.zeros(3, np.float32)
     xlib().sto_sppm_unoct(w, ptr(o))
     return o
+
+
+LT_G = 128
+LT_N = LT_G * LT_G
+
+
+def lt_build(sent, stored):
+    """The learned emission map's rebuild (prog_lt_build, wavefront.js:628-711) on the given counts: (sent/2,
+    stored/2, the CDF: LT_N conditional row entries, then LT_G rows)."""
+    e = np.array(sent, np.uint32).copy()
+    h = np.array(stored, np.uint32).copy()
+    cdf = np.zeros(LT_N + LT_G, np.float32)
+    xlib().sto_lt_build(ptr(e), ptr(h), ptr(cdf))
+    return e, h, cdf
+
+
+def last_lt():
+    """The emission map as the last render with it on left it: (sent, stored, CDF)."""
+    e = np.zeros(LT_N, np.uint32)
+    h = np.zeros(LT_N, np.uint32)
+    cdf = np.zeros(LT_N + LT_G, np.float32)
+    if xlib().sto_last_lt(ptr(e), ptr(h), ptr(cdf)) != 0:
+        raise RuntimeError("no render with the learned emission map has run")
+    return e, h, cdf
 
 
 def sppm_build(pos, power, nrm_oct, flags, cell):

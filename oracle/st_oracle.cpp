@@ -132,6 +132,9 @@ inline void lt_build(uint32_t* emit, uint32_t* hit, float* cdf) {
     for (uint32_t r = 0; r < LT_G; r++) { racc += rowP[r]; cdf[LT_N + r] = racc; }
     cdf[LT_N + LT_G - 1] = 1.f;
 }
+// the last render's learned emission map as it ended (photons sent, stored, the CDF), for the tests to read
+std::vector<uint32_t> g_lt_emit, g_lt_hit;
+std::vector<float> g_lt_cdf;
 inline void lt_uniform(float* cdf) {
     for (uint32_t r = 0; r < LT_G; r++)
         for (uint32_t c = 0; c < LT_G; c++) cdf[r * LT_G + c] = c + 1 == LT_G ? 1.f : (float)(c + 1) / LT_G;
@@ -1304,6 +1307,7 @@ static int render_impl(const st_scene_desc* s, const st_params* p, const st_view
         counters[3] += st.shadow_rays; counters[4] += st.shadow_steps; counters[5] += st.nonfinite;
         counters[6] += st.flushed; counters[7] += st.shadowcut;
     }
+    if (C.sp_learn) { g_lt_emit = lt_emit; g_lt_hit = lt_hit; g_lt_cdf = lt_cdf; }
     return 0;
 }
 
@@ -1563,6 +1567,16 @@ double sto_spec_draw(double u, double* w) {
 }
 uint32_t sto_sppm_hash(int32_t i, int32_t j, int32_t k) { return sppm_hash(i, j, k); }
 double sto_sppm_radius(double r1, int k, double alpha) { return sppm_radius(r1, k, alpha); }
+// prog_lt_build on the given counts (halved in place) into cdf (LT_N + LT_G floats)
+void sto_lt_build(uint32_t* emit, uint32_t* hit, float* cdf) { lt_build(emit, hit, cdf); }
+// the last render's emission map (sent, stored: LT_N each; cdf LT_N + LT_G); 0, or -1 if none ran
+int sto_last_lt(uint32_t* emit, uint32_t* hit, float* cdf) {
+    if (g_lt_cdf.empty()) return -1;
+    std::copy(g_lt_emit.begin(), g_lt_emit.end(), emit);
+    std::copy(g_lt_hit.begin(), g_lt_hit.end(), hit);
+    std::copy(g_lt_cdf.begin(), g_lt_cdf.end(), cdf);
+    return 0;
+}
 double sto_sppm_keep(double capacity, double demand) { return sppm_keep(capacity, demand); }
 uint32_t sto_sppm_subs_of(uint32_t count, uint32_t share) { return sppm_subs_of(count, share); }
 uint32_t sto_sppm_oct(const float* v) { return sppm_oct(v); }

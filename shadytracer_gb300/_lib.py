@@ -29,6 +29,7 @@ SIGNATURES = {
     "st_step": ([P, C.c_int], C.c_int),
     "st_step_async": ([P, C.c_int], C.c_int),
     "st_sync": ([P, C.c_int], C.c_int),
+    "st_set_wait_limit": ([P, C.c_uint32, C.c_int], C.c_int),
     "st_read_accum": ([P, P, P, P, P], C.c_int),
     "st_image_stats": ([P, C.POINTER(T.StImageStats)], C.c_int),
     "st_read_counters": ([P, C.POINTER(T.StCounters)], C.c_int),
@@ -40,6 +41,7 @@ SIGNATURES = {
     "st_sppm_read_grid": ([P, P, P, P, P], C.c_int),
     "st_sppm_gather": ([P, P, P, P, P, C.c_uint32, C.c_float, C.c_uint32, C.c_uint32, C.c_uint32, P], C.c_int),
     "st_sppm_stats_read": ([P, C.POINTER(T.StSppmStats)], C.c_int),
+    "st_sppm_emission_map": ([P, P, P, P], C.c_int),
     "st_optics_set_sources": ([P, C.POINTER(T.StOpticsSource), C.c_uint32], C.c_int),
     "st_optics_set_far": ([P, C.POINTER(T.StOpticsFar)], C.c_int),
     "st_optics_run": ([P, C.POINTER(T.StOpticsBatch), P, P, C.POINTER(T.StOpticsTotals)], C.c_int),

@@ -78,6 +78,7 @@ struct st_ctx {
     uint32_t rec_launches = 0;            // kernels in the last recorded wave chain
     uint32_t graph_launches = 0;          // ...and in the graph's (its kernel nodes)
     uint64_t launches = 0;                // kernels run by the wave chains since the context was made
+    uint32_t wait_limit = 0, wait_arm_only = 0;   // the device-side waits (st_set_wait_limit), kept across resets
     // per-kernel timing (core/kerneltime.js's role): CUDA events on this stream around each launch, when on
     bool timing = false;
     bool count_work = false;              // a counting pass: the march counts its fold's work
@@ -102,6 +103,13 @@ static int cuda_fail(st_ctx* c, cudaError_t e, const char* what) {
         cudaError_t e_ = (call);                               \
         if (e_ != cudaSuccess) return cuda_fail(ctx, e_, what); \
     } while (0)
+
+// the device-side waits' settings into the counters, where the kernels read them (after any reset of the counters)
+static cudaError_t push_wait(st_ctx* ctx) {
+    const uint32_t w[2] = {ctx->wait_limit, ctx->wait_arm_only};
+    cudaError_t e = cudaMemcpyAsync(&ctx->d_ctr->wait_limit, w, sizeof(w), cudaMemcpyHostToDevice, ctx->stream);
+    return e == cudaSuccess ? cudaStreamSynchronize(ctx->stream) : e;
+}
 
 static void free_wave(st_ctx* ctx) {
     void* ptrs[] = {ctx->pb.pos, ctx->pb.dir, ctx->pb.beta, ctx->pb.rad, ctx->pb.meta, ctx->pb.lam, ctx->pb.lprev,
@@ -155,10 +163,10 @@ static void collect_times(st_ctx* ctx) {
 // the uniforms, derived on the host in double precision (core/photometry.js:55-73 sunCone / discLuminance,
 // :182-237 derive), then rounded once
 // ------------------------------------------------------------------------------------------------------------
-static Uni make_uni(const st_ctx* ctx) {
-    const st_params& p = ctx->params;
-    const st_scene_desc& s = ctx->desc;
-    const st_view& v = ctx->view;
+// what depends only on the scene's description, the settings and the camera (the render that allocates nothing,
+// st_noalloc.cu, takes its uniforms from here too); env_image: an environment image replaces the sun and sky
+Uni make_uni_base(const st_scene_desc& s, const st_params& p, const st_view& v, uint32_t n_prims, uint32_t n_mats,
+                  bool env_image) {
     Uni u{};
     u.W = p.width; u.H = p.height; u.P = p.width * p.height;
     const double N = double(u.W) * double(u.H);
@@ -191,7 +199,7 @@ static Uni make_uni(const st_ctx* ctx) {
     double y = raw[0] * 0.2126 + raw[1] * 0.7152 + raw[2] * 0.0722;
     bool furnace = p.env_uniform > 0;
     // an environment image is the whole environment, with no sun to aim at (envimage.js, the image preset)
-    int sun_on = (p.sun_hint != 0 && p.sun_elevation * PI_D / 180.0 + half > 0 && !furnace && !ctx->d_envimg) ? 1 : 0;
+    int sun_on = (p.sun_hint != 0 && p.sun_elevation * PI_D / 180.0 + half > 0 && !furnace && !env_image) ? 1 : 0;
     double e = p.sun_elevation * PI_D / 180.0, az = p.sun_azimuth * PI_D / 180.0;
     u.sun_dir = mk((float)(std::cos(e) * std::sin(az)), (float)(std::cos(e) * std::cos(az)), (float)std::sin(e));
     u.sun_sin2 = (float)sin2;
@@ -202,6 +210,26 @@ static Uni make_uni(const st_ctx* ctx) {
     u.disc = mk((float)(disc * raw[0] / y), (float)(disc * raw[1] / y), (float)(disc * raw[2] / y));
     u.sky = p.sky_luminance; u.ground = p.ground_luminance; u.uniform = p.env_uniform;
     u.sun_gain = std::max(0.f, p.env_sun_gain); u.sky_gain = std::max(0.f, p.env_sky_gain);
+    u.haze_on = s.haze_sigma_t > 0 ? 1 : 0;
+    u.hc = mk(s.haze_centre[0], s.haze_centre[1], s.haze_centre[2]);
+    u.hu = mk(s.haze_axes[0], s.haze_axes[1], s.haze_axes[2]);
+    u.hv = mk(s.haze_axes[3], s.haze_axes[4], s.haze_axes[5]);
+    u.hw = mk(s.haze_axes[6], s.haze_axes[7], s.haze_axes[8]);
+    u.hhu = s.haze_half[0]; u.hhv = s.haze_half[1]; u.hhw = s.haze_half[2];
+    u.hsig = s.haze_sigma_t;
+    auto sat01 = [](float x) { return std::min(std::max(x, 0.f), 1.f); };
+    u.halb = mk(sat01(s.haze_albedo[0]), sat01(s.haze_albedo[1]), sat01(s.haze_albedo[2]));
+    u.hg = std::min(std::max(s.haze_g, -0.95f), 0.95f);
+    u.seed = p.seed; u.maxaverages = p.maxaverages;
+    u.n_prims = n_prims;
+    u.n_mats = n_mats;
+    return u;
+}
+
+static Uni make_uni(const st_ctx* ctx) {
+    const st_params& p = ctx->params;
+    Uni u = make_uni_base(ctx->desc, p, ctx->view, (uint32_t)ctx->prims.size(), (uint32_t)ctx->mats.size(),
+                          ctx->d_envimg != nullptr);
     if (ctx->d_envimg) {
         u.env_img = ctx->d_envimg; u.env_w = ctx->env_w; u.env_h = ctx->env_h;
         u.env_lum = ctx->env_lum; u.env_turn = ctx->env_turn;
@@ -215,19 +243,6 @@ static Uni make_uni(const st_ctx* ctx) {
         u.sc_dx = ctx->sc_dims[0]; u.sc_dy = ctx->sc_dims[1]; u.sc_dz = ctx->sc_dims[2];
         u.sc_looks = p.step_cache >= 2 ? 3u : 1u;
     }
-    u.haze_on = s.haze_sigma_t > 0 ? 1 : 0;
-    u.hc = mk(s.haze_centre[0], s.haze_centre[1], s.haze_centre[2]);
-    u.hu = mk(s.haze_axes[0], s.haze_axes[1], s.haze_axes[2]);
-    u.hv = mk(s.haze_axes[3], s.haze_axes[4], s.haze_axes[5]);
-    u.hw = mk(s.haze_axes[6], s.haze_axes[7], s.haze_axes[8]);
-    u.hhu = s.haze_half[0]; u.hhv = s.haze_half[1]; u.hhw = s.haze_half[2];
-    u.hsig = s.haze_sigma_t;
-    auto sat01 = [](float x) { return std::min(std::max(x, 0.f), 1.f); };
-    u.halb = mk(sat01(s.haze_albedo[0]), sat01(s.haze_albedo[1]), sat01(s.haze_albedo[2]));
-    u.hg = std::min(std::max(s.haze_g, -0.95f), 0.95f);
-    u.seed = p.seed; u.maxaverages = p.maxaverages;
-    u.n_prims = (uint32_t)ctx->prims.size();
-    u.n_mats = (uint32_t)ctx->mats.size();
     // the march queue's space order: a grid over the bounded primitives' spheres (none bounded: no sort)
     // the space order pays where a step is dear: a table of a few primitives marches fast in any order, and there the
     // sort's three launches an iteration cost more than the coherence saves (the SDF room, 27 primitives: 19 % faster
@@ -298,7 +313,7 @@ static bool light_faces(const st_scene_desc* d, std::vector<st_prim>& prims, std
     return true;
 }
 
-static DPrim pack_prim(const st_prim& p) {
+DPrim pack_prim(const st_prim& p) {
     DPrim d{};
     const float* q = p.p;
     double R = INFINITY;
@@ -411,6 +426,7 @@ static int ensure_wave(st_ctx* ctx) {
     CK(cudaMemsetAsync(ctx->d_acc, 0, (size_t)ctx->P * sizeof(Acc4), ctx->stream), "memset");
     CK(cudaMemsetAsync(ctx->d_mom, 0, (size_t)ctx->P * sizeof(double2), ctx->stream), "memset");
     CK(cudaMemsetAsync(ctx->d_ctr, 0, sizeof(DevCtr), ctx->stream), "memset");
+    if (ctx->wait_limit || ctx->wait_arm_only) CK(push_wait(ctx), "wait limit");
     ctx->samples = 0;
     return ST_OK;
 }
@@ -614,7 +630,11 @@ extern "C" {
 
 int st_abi_version(void) { return ST_ABI_VERSION; }
 
-const char* st_last_error(const st_ctx* ctx) { return ctx ? ctx->err.c_str() : "no context"; }
+const char* st_last_error(const st_ctx* ctx) {
+    if (ctx) return ctx->err.c_str();
+    const char* m = noalloc_last_error();         // the calls with no context: st_render_noalloc's refusals
+    return *m ? m : "no context";
+}
 
 int st_create(int device, st_ctx** out) {
     if (!out) return ST_ERR_ARG;
@@ -952,7 +972,25 @@ int st_sync(st_ctx* ctx, int timeout_ms) {
     if (ctx->timing) collect_times(ctx);
     DevCtr c;
     CK(cudaMemcpy(&c, ctx->d_ctr, sizeof(DevCtr), cudaMemcpyDeviceToHost), "counters");
-    if (c.errflag) return fail(ctx, ST_ERR_TIMEOUT, "a kernel's wait for its scene table ran out of iterations");
+    if (c.errflag) {
+        // reported once: the flag is cleared, so the next trace that finishes its waits reports success
+        CK(cudaMemsetAsync(&ctx->d_ctr->errflag, 0, sizeof(uint32_t), ctx->stream), "counters");
+        CK(cudaStreamSynchronize(ctx->stream), "counters");
+        return fail(ctx, ST_ERR_TIMEOUT, "a kernel's wait for its scene table ran out of iterations");
+    }
+    return ST_OK;
+}
+
+// THE DEVICE-SIDE WAITS' LIMIT: every kernel that stages a table into shared memory waits for its copy at most this
+// many times (0: the default, 2^24) before it flags ST_ERR_TIMEOUT and returns; arm_only 1 arms the waits and issues
+// no copy, so each runs out at its limit with nothing in flight -- the failure path, exercised without a fault
+int st_set_wait_limit(st_ctx* ctx, uint32_t iterations, int arm_only) {
+    if (!ctx) return ST_ERR_ARG;
+    if (ctx->in_flight) return fail(ctx, ST_ERR_BUSY, "a trace is in flight: st_sync first");
+    cudaSetDevice(ctx->device);
+    ctx->wait_limit = iterations;
+    ctx->wait_arm_only = arm_only ? 1u : 0u;
+    CK(push_wait(ctx), "wait limit");
     return ST_OK;
 }
 

@@ -80,8 +80,10 @@ struct DevCtr {
     uint32_t rayCount[2], hitCount, shadowCount[2];
     uint32_t marchHead, occHead, errflag;
     uint32_t nonfinite, flushed, shadowcut, sample;   // sample: the first sample of the wave in flight
-    uint32_t shadowdrop, emitHits, pad2, pad3;        // emitHits: this iteration's shadow rays that met something
+    uint32_t shadowdrop, emitHits;                    // emitHits: this iteration's shadow rays that met something
                                                       // while aiming at an emitter
+    uint32_t wait_limit, wait_arm_only;               // the device-side waits' limit (0: WAIT_LIMIT) and the test of
+                                                      // their failure path (st_set_wait_limit)
     unsigned long long paths, segments, march_steps, shadow_rays, shadow_steps;
     unsigned long long work[WC_N];     // the march's fold, counted in a counting pass (WC_* in st_device.cuh)
 };
@@ -229,3 +231,13 @@ cudaError_t launch_guide_infer(const WaveArgs& a, int sms, cudaStream_t s);
 cudaError_t launch_guide_collect(const WaveArgs& a, int sms, cudaStream_t s);
 
 }  // namespace st
+
+// HOST HELPERS (st_capi.cu) that the context path and the render that allocates nothing (st_noalloc.cu) share, so
+// the two derive the same uniforms and pack the same table: the uniforms that depend only on the scene's
+// description, the settings and the camera (env_image: an environment image replaces the sun and sky), and a
+// primitive as the kernels read it
+st::Uni make_uni_base(const st_scene_desc& s, const st_params& p, const st_view& v, uint32_t n_prims, uint32_t n_mats,
+                      bool env_image);
+st::DPrim pack_prim(const st_prim& p);
+// why st_render_noalloc last refused a call on this thread ("" if it did not)
+const char* noalloc_last_error();

@@ -21,11 +21,30 @@ __device__ __forceinline__ uint32_t lanemask_lt() {
 // cp.async.bulk; every thread waits on the barrier's phase, a bounded number of times. bytes is a multiple of 16,
 // both addresses 16-byte aligned (DPrim is 128 bytes, st_material 64, cudaMalloc 256-aligned). Returns false
 // (and flags the counters) if the copy did not land within the limit.
+//
+// THE LIMIT is the counters' wait_limit (0: WAIT_LIMIT), so a host can make it short; with wait_arm_only set the
+// barrier is armed but no copy is issued -- a test of this failure path: the wait runs out at its limit with nothing
+// in flight, the CTA flags the error and returns, and the context stays usable. Where a real copy was issued and the
+// wait ran out, the CTA waits once more (bounded again) for that copy to land in its shared memory before it leaves.
+// The reference's own guards against a GPU that never finishes are host-side (core/wavefront.js:298-303 clamps the
+// indirect dispatch, core/raytrace_main.js:67 cuts a frame's submissions); a wait on the device has none there.
 // ------------------------------------------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t mbar_try(uint32_t mb) {
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(done) : "r"(mb) : "memory");
+    return done;
+}
 __device__ __forceinline__ bool stage_table(void* sdst, const void* gsrc, uint32_t bytes, uint64_t* mbar,
                                             DevCtr* ctr) {
     uint32_t mb = (uint32_t)__cvta_generic_to_shared(mbar);
     uint32_t dst = (uint32_t)__cvta_generic_to_shared(sdst);
+    const uint32_t wl = ctr->wait_limit;
+    const uint32_t limit = wl ? wl : WAIT_LIMIT;
+    const bool issue = ctr->wait_arm_only == 0u;
     if (threadIdx.x == 0) {
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mb) : "memory");
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -33,20 +52,18 @@ __device__ __forceinline__ bool stage_table(void* sdst, const void* gsrc, uint32
     __syncthreads();
     if (threadIdx.x == 0) {
         asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mb), "r"(bytes) : "memory");
-        asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
-                     ::"r"(dst), "l"(gsrc), "r"(bytes), "r"(mb) : "memory");
+        if (issue)
+            asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                         ::"r"(dst), "l"(gsrc), "r"(bytes), "r"(mb) : "memory");
     }
     uint32_t done = 0;
-    for (uint32_t k = 0; k < WAIT_LIMIT && !done; k++) {
-        asm volatile(
-            "{\n\t.reg .pred p;\n\t"
-            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\n\t"
-            "selp.u32 %0, 1, 0, p;\n\t}"
-            : "=r"(done) : "r"(mb) : "memory");
-    }
+    for (uint32_t k = 0; k < limit && !done; k++) done = mbar_try(mb);
     // one decision for the whole CTA, so no thread leaves while another still waits at a barrier
     if (__syncthreads_or(!done)) {
         if (threadIdx.x == 0) atomicExch(&ctr->errflag, 1u);
+        if (issue)                                   // the copy in flight: let it land before the CTA is gone
+            for (uint32_t k = 0; k < WAIT_LIMIT && !done; k++) done = mbar_try(mb);
+        __syncthreads();
         return false;
     }
     return true;

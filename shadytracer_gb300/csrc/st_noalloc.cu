@@ -16,13 +16,20 @@
 // start at zero (the accumulation, the moments, the frame, the counters) before it renders. Calls that overlap on
 // the GPU -- from two host threads at once, for one device -- race on the array and give wrong pictures; a caller
 // serialises them. The kernels are the regular path's own (st_render.cu), launched on the device's legacy default
-// stream, so the picture equals st_step's for the same scene, settings, camera and samples.
+// stream, with the uniforms and the packed table from the same host functions (st_capi.cu make_uni_base,
+// pack_prim), so the picture equals st_step's for the same scene, settings, camera and samples. What this render
+// does not carry -- light faces, the photon map, the learned proposal, the step cache, light sampling of emissive
+// materials -- is refused with ST_ERR_ARG and a message (st_last_error(NULL)), never silently left out.
+//
+// THE CALLER'S DEVICE. The call makes its device current while it runs and puts the caller's back before it returns.
 //
 // SET-UP. The first call on a device, with that device current, takes the array's device address with
 // cudaGetSymbolAddress and builds the albedo tables in it; make that first call before any stream capture.
+#include <cstdarg>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
+#include <string>
 
 #include "st_spectral.h"
 #include "st_internal.h"
@@ -34,8 +41,6 @@ using namespace st;
 static __device__ __align__(256) unsigned char g_noalloc_scratch[ST_NOALLOC_SCRATCH_BYTES];
 
 namespace {
-const double PI_D = 3.14159265358979323846;
-
 struct Layout {
     size_t pos, dir, beta, rad, meta, ray0, ray1, hit, hitd, hsurf, so[2], sd[2], sr[2], ss[2], frame, acc, mom, cnt, ctr,
         ec, ecavg, e1, spec, lam, prims, mats, end;
@@ -72,116 +77,64 @@ __global__ void k_counts(const Acc4* acc, uint32_t* cnt, uint32_t P) {
     if (i < P) cnt[i] = (uint32_t)acc[i].w;
 }
 
-// a primitive as the kernels read it: st_capi.cu's packing, restated here so this file changes nothing there
-DPrim pack(const st_prim& p) {
-    DPrim d{};
-    const float* q = p.p;
-    double R = INFINITY;
-    switch (p.type) {
-        case ST_PRIM_SPHERE: R = std::fabs(q[0]); break;
-        case ST_PRIM_BOX: R = std::sqrt(double(q[0]) * q[0] + double(q[1]) * q[1] + double(q[2]) * q[2]); break;
-        case ST_PRIM_ROUNDBOX:
-            R = std::sqrt(double(q[0]) * q[0] + double(q[1]) * q[1] + double(q[2]) * q[2]) + std::fabs(q[3]);
-            break;
-        case ST_PRIM_TORUS: R = std::fabs(q[0]) + std::fabs(q[1]); break;
-        case ST_PRIM_PRISM: R = std::sqrt(double(q[1]) * q[1] + 0.25 * double(q[2]) * q[2]) + std::fabs(q[3]); break;
-        case ST_PRIM_CYLINDER: R = std::sqrt(double(q[0]) * q[0] + double(q[1]) * q[1]); break;
-        default: R = INFINITY;
-    }
-    float Rf = std::isfinite(R) ? (float)(R * 1.001 + 1e-5) : INFINITY;
-    d.a = make_float4(p.pos[0], p.pos[1], p.pos[2], Rf);
-    d.r0 = make_float4(p.rot[0], p.rot[1], p.rot[2], p.k);
-    d.r1 = make_float4(p.rot[3], p.rot[4], p.rot[5], q[0]);
-    d.r2 = make_float4(p.rot[6], p.rot[7], p.rot[8], q[1]);
-    d.e = make_float4(q[2], q[3], q[4], q[5]);
-    d.f = make_float4(q[6], q[7], q[8], q[9]);
-    if (p.type == ST_PRIM_PRISM) {
-        double n = std::min(std::max(std::nearbyint((double)q[0]), 3.0), 64.0);
-        double an = PI_D / n, Rp = std::max((double)q[1], 0.0);
-        d.g = make_float4((float)(Rp * std::cos(an)), (float)(Rp * std::sin(an)), (float)(2 * an), (float)n);
-    }
-    d.h = make_uint4(p.type, p.op, p.material, p.flags);
-    return d;
-}
+thread_local std::string g_err;         // why the last call on this thread was refused (st_last_error(NULL))
 
-// the uniforms, derived on the host in double precision as st_capi.cu's make_uni does
-Uni uniforms(const st_scene_desc& s, const st_params& p, const st_view& v, uint32_t n_prims, uint32_t n_mats) {
-    Uni u{};
-    u.W = p.width; u.H = p.height; u.P = p.width * p.height;
-    const double N = double(u.W) * double(u.H);
-    u.tilesX = std::max<uint32_t>(1, (uint32_t)std::llround(std::sqrt(N * (double(u.W) / std::max<double>(1, u.H)))));
-    u.tilesY = std::max<uint32_t>(1, (uint32_t)std::ceil(N / u.tilesX));
-    u.invTX = float(1.0 / u.tilesX);
-    u.invTY = float(1.0 / u.tilesY);
-    u.maxbounce = p.maxbounce; u.maxiter = p.maxiter; u.nee = p.nee; u.rr = p.rr;
-    u.budget = p.budget ? p.budget : std::max(2u, p.maxbounce + 1 + (p.maxiter + 31) / 32);
-    u.stepscale = p.stepscale;
-    double tol = p.eps > 0 ? p.eps : (s.tolerance > 0 ? s.tolerance : 1e-3);
-    double R = s.env_radius > 0 ? s.env_radius : 400.0;
-    u.tol = (float)tol; u.envR = (float)R; u.envR2 = (float)(R * R);
-    u.cam = mk(v.cam_pos[0], v.cam_pos[1], v.cam_pos[2]);
-    u.right = mk(v.right[0], v.right[1], v.right[2]);
-    u.up = mk(v.up[0], v.up[1], v.up[2]);
-    u.fwd = mk(v.fwd[0], v.fwd[1], v.fwd[2]);
-    u.fx = v.fx; u.fy = v.fy; u.camtype = v.camtype;
-    u.lens_r = v.lens_radius > 0.f ? v.lens_radius : 0.f;
-    u.lens_f = v.focus_distance;
-    double half = std::max((double)p.sun_diameter, 1e-3) * PI_D / 360.0;
-    double sh = std::sin(half / 2), omc = 2 * sh * sh, sin2 = std::sin(half) * std::sin(half);
-    double disc = (double)p.sun_illuminance / (PI_D * sin2);
-    const double raw[3] = {1.0, 0.96, 0.9};
-    double y = raw[0] * 0.2126 + raw[1] * 0.7152 + raw[2] * 0.0722;
-    int sun_on = (p.sun_hint != 0 && p.sun_elevation * PI_D / 180.0 + half > 0 && !(p.env_uniform > 0)) ? 1 : 0;
-    double e = p.sun_elevation * PI_D / 180.0, az = p.sun_azimuth * PI_D / 180.0;
-    u.sun_dir = mk((float)(std::cos(e) * std::sin(az)), (float)(std::cos(e) * std::cos(az)), (float)std::sin(e));
-    u.sun_sin2 = (float)sin2; u.sun_omc = (float)omc; u.sun_omega = (float)(2 * PI_D * omc);
-    u.pick = (float)((sun_on && p.env_sun_gain > 0) ? p.nee_sun_pick : 0.0);
-    u.sun_on = sun_on;
-    u.disc = mk((float)(disc * raw[0] / y), (float)(disc * raw[1] / y), (float)(disc * raw[2] / y));
-    u.sky = p.sky_luminance; u.ground = p.ground_luminance; u.uniform = p.env_uniform;
-    u.sun_gain = std::max(0.f, p.env_sun_gain); u.sky_gain = std::max(0.f, p.env_sky_gain);
-    u.haze_on = s.haze_sigma_t > 0 ? 1 : 0;
-    u.hc = mk(s.haze_centre[0], s.haze_centre[1], s.haze_centre[2]);
-    u.hu = mk(s.haze_axes[0], s.haze_axes[1], s.haze_axes[2]);
-    u.hv = mk(s.haze_axes[3], s.haze_axes[4], s.haze_axes[5]);
-    u.hw = mk(s.haze_axes[6], s.haze_axes[7], s.haze_axes[8]);
-    u.hhu = s.haze_half[0]; u.hhv = s.haze_half[1]; u.hhw = s.haze_half[2];
-    u.hsig = s.haze_sigma_t;
-    auto sat01 = [](float x) { return std::min(std::max(x, 0.f), 1.f); };
-    u.halb = mk(sat01(s.haze_albedo[0]), sat01(s.haze_albedo[1]), sat01(s.haze_albedo[2]));
-    u.hg = std::min(std::max(s.haze_g, -0.95f), 0.95f);
-    u.seed = p.seed; u.maxaverages = p.maxaverages;
-    u.n_prims = n_prims; u.n_mats = n_mats;
-    return u;
+// the calling thread's current device, put back on every way out: a host that counts on its device staying put
+// finds it as it was
+struct DeviceGuard {
+    int prev = -1;
+    DeviceGuard() { if (cudaGetDevice(&prev) != cudaSuccess) prev = -1; }
+    ~DeviceGuard() { if (prev >= 0) cudaSetDevice(prev); }
+};
+
+int refuse(const char* fmt, ...) {
+    char buf[256];
+    va_list ap;
+    va_start(ap, fmt);
+    std::vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_err = std::string("st_render_noalloc: ") + buf;
+    std::fprintf(stderr, "%s\n", g_err.c_str());
+    return ST_ERR_ARG;
 }
 }  // namespace
 
+const char* noalloc_last_error() { return g_err.c_str(); }
+
 extern "C" int st_render_noalloc(int device, const st_scene_desc* desc, const st_params* p, const st_view* v,
                                  int nsamples, double* rgb, double* V, double* S, uint32_t* count) {
-    if (!desc || !p || !v || nsamples < 0 || !desc->prims || !desc->materials) return ST_ERR_ARG;
-    if (device < 0 || device >= ST_NOALLOC_MAX_DEVICES) return ST_ERR_ARG;
+    g_err.clear();
+    if (!desc || !p || !v || nsamples < 0 || !desc->prims || !desc->materials)
+        return refuse("a null scene, settings or camera, or a negative sample count");
+    if (device < 0 || device >= ST_NOALLOC_MAX_DEVICES) return refuse("device %d out of range", device);
     const size_t P = (size_t)p->width * p->height;
-    if (p->width == 0 || p->height == 0 || P > ST_NOALLOC_MAX_PIXELS) {
-        std::fprintf(stderr, "st_render_noalloc: %ux%u pixels is over its limit of %u pixels (128 x 128)\n",
-                     p->width, p->height, ST_NOALLOC_MAX_PIXELS);
-        return ST_ERR_ARG;
-    }
-    if (desc->lights && desc->n_lights) {
-        std::fprintf(stderr, "st_render_noalloc: a scene with light faces takes the context path (st_set_scene)\n");
-        return ST_ERR_ARG;
+    if (p->width == 0 || p->height == 0 || P > ST_NOALLOC_MAX_PIXELS)
+        return refuse("%ux%u pixels is over its limit of %u pixels (128 x 128)", p->width, p->height,
+                      ST_NOALLOC_MAX_PIXELS);
+    // what this render does not do, refused rather than left out: its picture would differ from st_step's
+    if (desc->lights && desc->n_lights) return refuse("a scene with light faces takes the context path (st_set_scene)");
+    if (p->sppm) return refuse("the photon map (st_params.sppm) takes the context path");
+    if (p->guide) return refuse("the learned proposal (st_params.guide) takes the context path");
+    if (p->step_cache) return refuse("the step cache (st_params.step_cache) takes the context path");
+    for (uint32_t i = 0; i < desc->n_materials && !p->emit_off; i++) {
+        const float* e = desc->materials[i].emissive;
+        if (e[0] > 0.f || e[1] > 0.f || e[2] > 0.f)
+            return refuse("material %u is emissive: its light sampling (the emitter list) takes the context path; "
+                          "set st_params.emit_off to render it by the BSDF's hits alone", i);
     }
     if (desc->n_prims == 0 || desc->n_prims > ST_MAX_PRIMS || desc->n_materials == 0 ||
         desc->n_materials > ST_MAX_MATERIALS || desc->prims[0].op != ST_OP_ITEM)
-        return ST_ERR_ARG;
+        return refuse("the table's size is out of range (1..256 primitives and materials) or it starts with no item");
     for (uint32_t i = 0; i < desc->n_prims; i++)
         if (desc->prims[i].type > ST_PRIM_CYLINDER || desc->prims[i].op > ST_OP_SUB ||
             desc->prims[i].material >= desc->n_materials)
-            return ST_ERR_ARG;
+            return refuse("primitive %u: unknown type or op, or material out of range", i);
     if (p->maxbounce == 0 || p->maxbounce > 64 || p->maxiter == 0 || p->maxiter > 65535 || !(p->stepscale > 0) ||
         p->stepscale > 1 || p->budget > 256)
-        return ST_ERR_ARG;
+        return refuse("maxbounce, maxiter, stepscale or budget out of range");
     const Layout L = layout(P);
-    if (L.end > ST_NOALLOC_SCRATCH_BYTES) return ST_ERR_ARG;
+    if (L.end > ST_NOALLOC_SCRATCH_BYTES) return refuse("the picture's buffers do not fit the scratch array");
+    DeviceGuard keep_device;
     if (cudaSetDevice(device) != cudaSuccess) return ST_ERR_CUDA;
     cudaStream_t s = 0;
 
@@ -207,7 +160,7 @@ extern "C" int st_render_noalloc(int device, const st_scene_desc* desc, const st
     }
     // the scene's tables
     DPrim packed[ST_MAX_PRIMS];
-    for (uint32_t i = 0; i < desc->n_prims; i++) packed[i] = pack(desc->prims[i]);
+    for (uint32_t i = 0; i < desc->n_prims; i++) packed[i] = pack_prim(desc->prims[i]);
     if (cudaMemcpyAsync(base + L.prims, packed, desc->n_prims * sizeof(DPrim), cudaMemcpyHostToDevice, s) != cudaSuccess ||
         cudaMemcpyAsync(base + L.mats, desc->materials, desc->n_materials * sizeof(st_material), cudaMemcpyHostToDevice,
                         s) != cudaSuccess)
@@ -220,7 +173,7 @@ extern "C" int st_render_noalloc(int device, const st_scene_desc* desc, const st
         return ST_ERR_CUDA;
 
     WaveArgs a{};
-    a.u = uniforms(*desc, *p, *v, desc->n_prims, desc->n_materials);
+    a.u = make_uni_base(*desc, *p, *v, desc->n_prims, desc->n_materials, false);
     a.prims = reinterpret_cast<const DPrim*>(base + L.prims);
     a.mats = reinterpret_cast<const st_material*>(base + L.mats);
     a.tab = MfTab{(const float*)(base + L.ec), (const float*)(base + L.ecavg), (const float*)(base + L.e1)};

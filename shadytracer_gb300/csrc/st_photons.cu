@@ -73,17 +73,20 @@ __device__ __forceinline__ float lt_mass(const float* __restrict__ cdf, uint32_t
     return fmaxf(cdf[i] - (i ? cdf[i - 1] : 0.f), 0.f);
 }
 __global__ void __launch_bounds__(LT_GRID) k_lt_build(SppmBufs b, const DevCtr* __restrict__ ctr) {
+    // every operation IEEE-rounded and none fused (the _rn intrinsics): the map is a function of the integer counts
+    // alone, the same bits as the oracle's sequential f32 build of them
     __shared__ float rowW[LT_GRID], rowP[LT_GRID];
     __shared__ float total;
     const uint32_t k = ctr->sample;
     if (k == 0u || (k & 3u) != 0u) return;                           // every fourth sample
     const uint32_t r = threadIdx.x, base = r * LT_GRID;
+    const float keep = 1.f - LT_FLOOR, rfloor = LT_FLOOR / (float)LT_GRID, cfloor = LT_FLOOR / (float)LT_CELLS;
     float sum = 0.f;
     for (uint32_t c = 0; c < LT_GRID; c++) {
         const uint32_t e = b.lt_emit[base + c], h = b.lt_hit[base + c];
-        const float w = e > 0u ? (float)h / (float)e : 0.f;
+        const float w = e > 0u ? __fdiv_rn((float)h, (float)e) : 0.f;
         b.lt_cdf[base + c] = w;                                      // scratch: the raw worth
-        sum += w;
+        sum = __fadd_rn(sum, w);
         b.lt_emit[base + c] = e / 2u;                                // forget half
         b.lt_hit[base + c] = h / 2u;
     }
@@ -91,27 +94,28 @@ __global__ void __launch_bounds__(LT_GRID) k_lt_build(SppmBufs b, const DevCtr* 
     __syncthreads();
     if (r == 0) {
         float t = 0.f;
-        for (uint32_t q = 0; q < LT_GRID; q++) t += rowW[q];
+        for (uint32_t q = 0; q < LT_GRID; q++) t = __fadd_rn(t, rowW[q]);
         total = t;
     }
     __syncthreads();
     const float T = total;
     const bool learned = T > 0.f;
-    const float n = (float)LT_CELLS;
-    const float rp = learned ? (1.f - LT_FLOOR) * rowW[r] / fmaxf(T, 1e-30f) + LT_FLOOR / (float)LT_GRID : 1.f / (float)LT_GRID;
+    const float Tm = fmaxf(T, 1e-30f);
+    const float rp = learned ? __fadd_rn(__fdiv_rn(__fmul_rn(keep, rowW[r]), Tm), rfloor) : 1.f / (float)LT_GRID;
     rowP[r] = rp;
     float acc = 0.f;
     for (uint32_t c = 0; c < LT_GRID; c++) {
-        const float p = learned ? (1.f - LT_FLOOR) * b.lt_cdf[base + c] / fmaxf(T, 1e-30f) + LT_FLOOR / n : 1.f / n;
-        acc += p;
-        b.lt_cdf[base + c] = acc / rp;                                // conditional on the row
+        const float p = learned ? __fadd_rn(__fdiv_rn(__fmul_rn(keep, b.lt_cdf[base + c]), Tm), cfloor)
+                                : 1.f / (float)LT_CELLS;
+        acc = __fadd_rn(acc, p);
+        b.lt_cdf[base + c] = __fdiv_rn(acc, rp);                      // conditional on the row
     }
     b.lt_cdf[base + LT_GRID - 1u] = 1.f;
     __syncthreads();
     if (r == 0) {
         float racc = 0.f;
         for (uint32_t q = 0; q < LT_GRID; q++) {
-            racc += rowP[q];
+            racc = __fadd_rn(racc, rowP[q]);
             b.lt_cdf[LT_CELLS + q] = racc;
         }
         b.lt_cdf[LT_CELLS + LT_GRID - 1u] = 1.f;

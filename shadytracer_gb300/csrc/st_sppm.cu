@@ -402,6 +402,21 @@ int st_sppm_gather(st_ctx* ctx, const float* qpos, const float* qnrm, const floa
     return ST_OK;
 }
 
+int st_sppm_emission_map(st_ctx* ctx, uint32_t* sent, uint32_t* stored, float* cdf) {
+    if (!ctx) return ST_ERR_ARG;
+    SppmState& s = ctx_ext(ctx).sppm;
+    if (!s.lt_cdf) { ctx_set_error(ctx, "no photon map has run"); return ST_ERR_STATE; }
+    cudaSetDevice(ctx_device(ctx));
+    cudaStream_t st = ctx_stream(ctx);
+    cudaError_t e = cudaStreamSynchronize(st);
+    if (!e && sent) e = cudaMemcpyAsync(sent, s.lt_emit, LT_CELLS * 4, cudaMemcpyDeviceToHost, st);
+    if (!e && stored) e = cudaMemcpyAsync(stored, s.lt_hit, LT_CELLS * 4, cudaMemcpyDeviceToHost, st);
+    if (!e && cdf) e = cudaMemcpyAsync(cdf, s.lt_cdf, (LT_CELLS + LT_GRID) * 4, cudaMemcpyDeviceToHost, st);
+    if (!e) e = cudaStreamSynchronize(st);
+    if (e) { ctx_set_error(ctx, std::string("emission map readback: ") + cudaGetErrorString(e)); return ST_ERR_CUDA; }
+    return ST_OK;
+}
+
 int st_sppm_stats_read(st_ctx* ctx, st_sppm_stats* out) {
     if (!ctx || !out) return ST_ERR_ARG;
     SppmState& s = ctx_ext(ctx).sppm;

@@ -54,9 +54,20 @@ def render_regular(s, n):
         rt.close()
 
 
+def lamp_by_hits():
+    s = scenes.lamp_floor(width=48, height=32, spp=4)
+    s.params.emit_off = 1          # the emitter rendered by the BSDF's hits alone, on both paths
+    return s
+
+
 @pytest.mark.parametrize("make, n", [
     (lambda: scenes.floor_furnace(width=64, height=64), 4),
     (lambda: scenes.sdf_room(width=64, height=36, maxbounce=8), 3),
+    (lambda: scenes.haze_furnace(width=32, height=32, sigma_t=0.5, g=0.7), 3),
+    (lambda: scenes.dispersive_furnace(width=32, height=32, floor=True), 3),
+    (lambda: scenes.absorbing_box(width=32, height=32), 3),
+    (lambda: scenes.aniso_spheres(width=32, height=24), 3),
+    (lamp_by_hits, 3),
 ])
 def test_noalloc_equals_the_regular_render_twice_in_a_row(make, n):
     f = noalloc_fn()
@@ -77,3 +88,28 @@ def test_noalloc_refuses_a_picture_over_its_limit():
     s = scenes.floor_furnace(width=129, height=128)
     rc, *_ = render_noalloc(f, s, 1)
     assert rc == T.ST_ERR_ARG
+
+
+def refused(make, setting=None):
+    f = noalloc_fn()
+    s = make()
+    if setting:
+        setattr(s.params, setting, 1)
+    rc, *_ = render_noalloc(f, s, 1)
+    from shadytracer_gb300._lib import load
+    return rc, load().st_last_error(None).decode()
+
+
+@pytest.mark.parametrize("make, setting, why", [
+    (lambda: scenes.spot_floor(width=32, height=32, light="face"), None, "light faces"),
+    (lambda: scenes.floor_furnace(width=32, height=32), "sppm", "photon map"),
+    (lambda: scenes.floor_furnace(width=32, height=32), "guide", "learned proposal"),
+    (lambda: scenes.floor_furnace(width=32, height=32), "step_cache", "step cache"),
+    (lambda: scenes.lamp_floor(width=32, height=32), None, "emissive"),
+])
+def test_noalloc_refuses_what_it_does_not_render(make, setting, why):
+    """Each setting this render does not carry is refused with ST_ERR_ARG and a reason, never silently dropped: its
+    picture would differ from st_step's."""
+    rc, msg = refused(make, setting)
+    assert rc == T.ST_ERR_ARG
+    assert why in msg, msg
