@@ -34,8 +34,10 @@
 #ifndef SHADYTRACER_H
 #define SHADYTRACER_H
 
+#ifndef __CUDACC_RTC__                 /* NVRTC (a scene's code, compiled at st_set_scene) has the types built in */
 #include <stddef.h>
 #include <stdint.h>
+#endif
 
 #ifdef __cplusplus
 extern "C" {
@@ -278,9 +280,27 @@ const char* st_last_error(const st_ctx* ctx);
 int  st_abi_version(void);
 
 /* ---- the scene, the settings, the camera ---- */
-/* cuda_src: NULL for a scene given as a primitive table (desc); the table is copied. On failure the
- * previous scene is kept and errbuf (if given) holds the reason. */
+/* THE SCENE, AS DATA OR AS CODE (the reference's scene contract, lib/pathtracer/README.md:126-145: its `wgsl` is the
+ * scene's SDF and material functions, builder/codegen.js:974-1060 generates them; setScene compiles them,
+ * core/raytrace_main.js:1145). cuda_src NULL: the scene is desc's primitive table, folded by a loop over it.
+ * cuda_src given: CUDA C++ that defines, at file scope over the library's device types,
+ *     __device__ float        st_scene_dist(st::f3 p);      the signed distance at p (FOLD_DIST)
+ *     __device__ st::SceneHit st_scene_full(st::f3 p);      distance, material of the nearest surface, medium (FOLD_FULL)
+ * (and, with #define ST_SCENE_COUNTS, __device__ float st_scene_dist_count(st::f3 p, uint32_t* wc), the distance
+ * tallying its work with st::wc_prim / st::wc_test for the counting pass); it is compiled by NVRTC for sm_103a with
+ * the kernels that ask the scene and loaded (a source compiled before in the process is taken from a cache). desc
+ * still gives the materials, the haze, the lights' faces and the radii; its primitives, which may then be none,
+ * bound the space sort and the step cache and are what the optics trace folds. shadytracer_gb300/codegen.py writes
+ * such code from a table or a node tree. On failure -- a bad table, or code that does not compile (ST_ERR_COMPILE;
+ * errbuf holds NVRTC's log, each error followed by the scene's line it names) -- the previous scene is kept. */
 int  st_set_scene(st_ctx* ctx, const char* cuda_src, const st_scene_desc* desc, char* errbuf, size_t errlen);
+/* the scene in force: is_code 1 when it was given as code; NVRTC's time for it (0 when it came from the cache) and its
+ * cubin's size */
+int  st_scene_code_info(st_ctx* ctx, int* is_code, double* compile_ms, uint64_t* cubin_bytes);
+/* a scene's code compiled for sm_103a into the process's cache, with no device or context (the builder's check that a
+ * scene compiles before it is set): ST_OK, or ST_ERR_COMPILE with NVRTC's log in errbuf as st_set_scene gives it;
+ * compile_ms NVRTC's time (0 when the source was compiled before). A later st_set_scene of the same source loads it. */
+int  st_compile_scene(const char* cuda_src, char* errbuf, size_t errlen, double* compile_ms);
 /* unknown_mask: reserved (0); the struct has no unknown keys. Changing the picture size or the
  * settings resets the accumulation. */
 int  st_set_params(st_ctx* ctx, const st_params* p, uint64_t* unknown_mask);

@@ -22,6 +22,8 @@ SIGNATURES = {
     "st_set_scene": ([P, C.c_char_p, C.POINTER(T.StSceneDesc), C.c_char_p, C.c_size_t], C.c_int),
     "st_set_params": ([P, C.POINTER(T.StParams), C.POINTER(C.c_uint64)], C.c_int),
     "st_set_view": ([P, C.POINTER(T.StView)], C.c_int),
+    "st_scene_code_info": ([P, C.POINTER(C.c_int), C.POINTER(C.c_double), C.POINTER(C.c_uint64)], C.c_int),
+    "st_compile_scene": ([C.c_char_p, C.c_char_p, C.c_size_t, C.POINTER(C.c_double)], C.c_int),
     "st_set_env_image": ([P, P, C.c_uint32, C.c_uint32, C.c_float, C.c_float], C.c_int),
     "st_optics_set_rays": ([P, P, C.c_uint32], C.c_int),
     "st_env_map_tables": ([P, P], C.c_int),

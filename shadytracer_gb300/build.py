@@ -33,6 +33,18 @@ def nvcc():
     return "nvcc"
 
 
+def cuda_lib_dir():
+    """The toolkit's library directory, beside the nvcc in use (lib64, or lib on some layouts)."""
+    import shutil
+    n = nvcc()
+    path = n if os.path.isabs(n) else (shutil.which(n) or "/usr/local/cuda/bin/nvcc")
+    root = os.path.dirname(os.path.dirname(os.path.realpath(path)))
+    for d in ("lib64", "lib"):
+        if os.path.exists(os.path.join(root, d, "libnvrtc.so")):
+            return os.path.join(root, d)
+    return os.path.join(root, "lib64")
+
+
 def _stale(target, deps):
     if not os.path.exists(target):
         return True
@@ -61,7 +73,11 @@ def build(verbose=False, force=False):
                 raise RuntimeError("nvcc failed: " + " ".join(cmd))
     if force or jobs or _stale(LIB, objs):
         tmp = LIB + ".tmp%d" % os.getpid()
-        cmd = [nvcc()] + ARCH + ["-shared", "-cudart", "static", "-o", tmp] + objs
+        # NVRTC (a scene given as code is compiled at st_set_scene): the toolkit's shared library, found at run time
+        # where it was at link time
+        lib = cuda_lib_dir()
+        cmd = [nvcc()] + ARCH + ["-shared", "-cudart", "static", "-o", tmp] + objs + \
+            ["-L" + lib, "-lnvrtc", "-Xlinker", "-rpath=" + lib]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode:
             sys.stderr.write(r.stdout + r.stderr)

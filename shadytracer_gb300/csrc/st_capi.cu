@@ -88,6 +88,8 @@ struct st_ctx {
     std::vector<PendingEvent> pending;
     std::vector<cudaEvent_t> event_pool;
     StExt ext;   // the photon map's and the optics bench's state (st_sppm.cu, st_optics.cu)
+    SceneCode code;                       // the scene as compiled code (st_scene_rtc.cu), when it was given as code
+    bool has_code = false;
 };
 
 static int fail(st_ctx* c, int code, const std::string& msg) {
@@ -457,6 +459,7 @@ static WaveArgs wave_args(st_ctx* ctx, uint32_t w) {
     a.mom = ctx->d_mom;
     a.spw = w;
     a.slots = w * ctx->P;
+    a.code = ctx->has_code ? &ctx->code : nullptr;
     if (sppm_runs(ctx)) {
         a.u.sppm_on = 1u;
         a.u.sppm_n = sppm_photons(ctx);
@@ -680,6 +683,7 @@ int st_destroy(st_ctx* ctx) {
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     free_wave(ctx);
     ext_free(ctx->ext);
+    if (ctx->has_code) scene_code_free(ctx->code);
     for (void* p : {(void*)ctx->d_prims, (void*)ctx->d_faces, (void*)ctx->d_envimg, (void*)ctx->d_envmap, (void*)ctx->d_sc,
                     (void*)ctx->d_mats, (void*)ctx->d_ec, (void*)ctx->d_ecavg,
                     (void*)ctx->d_e1, (void*)ctx->d_ctr, (void*)ctx->d_spec})
@@ -698,11 +702,13 @@ int st_set_scene(st_ctx* ctx, const char* cuda_src, const st_scene_desc* d, char
         return fail(ctx, code, m);
     };
     if (ctx->in_flight) return refuse(ST_ERR_BUSY, "a trace is in flight: st_sync first");
-    if (cuda_src) return refuse(ST_ERR_COMPILE, "this build takes scenes as primitive tables (cuda_src must be NULL)");
-    if (!d || !d->prims || !d->materials) return refuse(ST_ERR_ARG, "no scene table");
-    if (d->n_prims == 0 || d->n_prims > ST_MAX_PRIMS) return refuse(ST_ERR_ARG, "n_prims out of range (1..256)");
+    // a scene as code: the table may be empty (its primitives, when given, still bound the space sort and the step
+    // cache and are what the optics trace folds)
+    const uint32_t min_prims = cuda_src ? 0u : 1u;
+    if (!d || (!d->prims && d->n_prims) || !d->materials) return refuse(ST_ERR_ARG, "no scene table");
+    if (d->n_prims < min_prims || d->n_prims > ST_MAX_PRIMS) return refuse(ST_ERR_ARG, "n_prims out of range (1..256)");
     if (d->n_materials == 0 || d->n_materials > ST_MAX_MATERIALS) return refuse(ST_ERR_ARG, "n_materials out of range (1..256)");
-    if (d->prims[0].op != ST_OP_ITEM) return refuse(ST_ERR_ARG, "the first primitive must start an item (ST_OP_ITEM)");
+    if (d->n_prims && d->prims[0].op != ST_OP_ITEM) return refuse(ST_ERR_ARG, "the first primitive must start an item (ST_OP_ITEM)");
     for (uint32_t i = 0; i < d->n_prims; i++) {
         if (d->prims[i].type > ST_PRIM_CYLINDER) return refuse(ST_ERR_ARG, "primitive " + std::to_string(i) + ": unknown type");
         if (d->prims[i].op > ST_OP_SUB) return refuse(ST_ERR_ARG, "primitive " + std::to_string(i) + ": unknown op");
@@ -712,10 +718,20 @@ int st_set_scene(st_ctx* ctx, const char* cuda_src, const st_scene_desc* d, char
     if (!(d->env_radius >= 0) || !(d->tolerance >= 0)) return refuse(ST_ERR_ARG, "negative radius or tolerance");
     std::vector<st_prim> prims(d->prims, d->prims + d->n_prims);
     std::vector<st_material> mats(d->materials, d->materials + d->n_materials);
+    // THE SCENE'S CODE first: a source that does not compile leaves everything as it was (README.md:216-218)
+    SceneCode code;
+    if (cuda_src) {
+        cudaSetDevice(ctx->device);
+        std::string why;
+        if (!scene_code_build(cuda_src, code, why)) return refuse(ST_ERR_COMPILE, why);
+    }
     std::vector<float4> faces(ST_MAX_LIGHTS * FACE_F4 + ST_MAX_MATERIALS / 16, make_float4(0.f, 0.f, 0.f, 0.f));
     {
         std::string why;
-        if (!light_faces(d, prims, faces, why)) return refuse(ST_ERR_ARG, why);
+        if (!light_faces(d, prims, faces, why)) {
+            if (cuda_src) scene_code_free(code);
+            return refuse(ST_ERR_ARG, why);
+        }
     }
     cudaSetDevice(ctx->device);
     if (prims.size() > ctx->prims.size() || !ctx->d_prims) {
@@ -750,6 +766,9 @@ int st_set_scene(st_ctx* ctx, const char* cuda_src, const st_scene_desc* d, char
     CK(cudaStreamSynchronize(ctx->stream), "scene upload");
     ctx->prims = std::move(prims);
     ctx->mats = std::move(mats);
+    if (ctx->has_code) scene_code_free(ctx->code);
+    ctx->code = code;
+    ctx->has_code = cuda_src != nullptr;
     ctx->desc = *d;
     ctx->desc.prims = nullptr;
     ctx->desc.materials = nullptr;
@@ -921,7 +940,8 @@ static int sc_ensure(st_ctx* ctx) {
         ctx->sc_cap = n;
     }
     CK(launch_sc_fill(ctx->d_prims, (uint32_t)ctx->prims.size(), mk(ctx->sc_lo[0], ctx->sc_lo[1], ctx->sc_lo[2]),
-                      ctx->sc_cs, ctx->sc_dims[0], ctx->sc_dims[1], ctx->sc_dims[2], ctx->d_sc, ctx->sms, ctx->stream),
+                      ctx->sc_cs, ctx->sc_dims[0], ctx->sc_dims[1], ctx->sc_dims[2], ctx->d_sc, ctx->sms, ctx->stream,
+                      ctx->has_code ? &ctx->code : nullptr),
        "step cache fill");
     ctx->sc_live = true;
     ctx->sc_scene = ctx->scene_gen;
@@ -1077,7 +1097,8 @@ int st_eval_sdf(st_ctx* ctx, const float* pts, uint32_t n, float* out) {
     float* dp = nullptr;
     CK(cudaMalloc(&dp, (size_t)n * 16), "cudaMalloc points");
     cudaError_t e = cudaMemcpyAsync(dp, pts, (size_t)n * 12, cudaMemcpyHostToDevice, ctx->stream);
-    if (!e) e = launch_eval_sdf(ctx->d_prims, (uint32_t)ctx->prims.size(), dp, n, dp + 3 * (size_t)n, ctx->stream);
+    if (!e) e = launch_eval_sdf(ctx->d_prims, (uint32_t)ctx->prims.size(), dp, n, dp + 3 * (size_t)n, ctx->stream,
+                                ctx->has_code ? &ctx->code : nullptr);
     if (!e) e = cudaMemcpyAsync(out, dp + 3 * (size_t)n, (size_t)n * 4, cudaMemcpyDeviceToHost, ctx->stream);
     if (!e) e = cudaStreamSynchronize(ctx->stream);
     cudaFree(dp);
@@ -1125,6 +1146,14 @@ int st_mf_tables(st_ctx* ctx, float* ec, float* ecavg, float* e1) {
 }
 
 // the struct sizes this library was built with, for the host's bindings to check theirs against
+int st_scene_code_info(st_ctx* ctx, int* is_code, double* compile_ms, uint64_t* cubin_bytes) {
+    if (!ctx) return ST_ERR_ARG;
+    if (is_code) *is_code = ctx->has_code ? 1 : 0;
+    if (compile_ms) *compile_ms = ctx->has_code ? ctx->code.compile_ms : 0.0;
+    if (cubin_bytes) *cubin_bytes = ctx->has_code ? (uint64_t)ctx->code.cubin_bytes : 0u;
+    return ST_OK;
+}
+
 int st_struct_sizes(uint32_t* out, int max) {
     const uint32_t s[] = {(uint32_t)sizeof(st_prim), (uint32_t)sizeof(st_material), (uint32_t)sizeof(st_scene_desc),
                           (uint32_t)sizeof(st_params), (uint32_t)sizeof(st_view), (uint32_t)sizeof(st_counters_t),

@@ -4,8 +4,10 @@
 // Each function restates the reference (lampmaker/ShadyTracer v0.88.0) at the file:line given; the kernels that
 // use them are in st_render.cu. Everything is f32 with f32 accumulation, as the reference's WGSL computes.
 #pragma once
+#ifndef __CUDACC_RTC__                 // NVRTC (st_scene_rtc.cu) compiles this header too; it has the types built in
 #include <cstdint>
 #include <cuda_runtime.h>
+#endif
 #include "../../include/shadytracer.h"
 
 #define ST_PI 3.14159265358979f
@@ -334,6 +336,15 @@ __device__ __forceinline__ void wc_eval(uint32_t* c, const DPrim& pr, uint32_t o
         if ((threadIdx.x & 31u) == (uint32_t)(__ffs(m) - 1)) atomicAdd(&c[WC_OP + (op & 3u)], (uint32_t)__popc(m));
     }
 }
+
+// ...and the same tallies from a scene's generated code (st_scene_rtc.cu's st_scene_dist_count): one evaluation of a
+// primitive of type t folded in by op, one bounding-sphere test
+__device__ __forceinline__ void wc_prim(uint32_t* c, uint32_t t, uint32_t op) {
+    wc_add<true>(c, WC_EVAL + (t & 7u), WC_WEVAL + (t & 7u));
+    const uint32_t m = __activemask();
+    if ((threadIdx.x & 31u) == (uint32_t)(__ffs(m) - 1)) atomicAdd(&c[WC_OP + (op & 3u)], (uint32_t)__popc(m));
+}
+__device__ __forceinline__ void wc_test(uint32_t* c) { wc_add<true>(c, WC_TEST, WC_WTEST); }
 
 struct SceneHit { float d; uint32_t m, a; };
 // distance only (scene_api.js FOLD_DIST): the march's and the shadow rays' question. Within an item's CSG chain a

@@ -19,6 +19,7 @@
 #include "st_emit.cuh"
 #include "st_ext.h"
 #include "st_kernels.cuh"
+#include "st_scene_kernels.cuh"
 
 namespace st {
 
@@ -120,37 +121,6 @@ __global__ void __launch_bounds__(EMIT_BUILD_THREADS) k_emit_build(uint32_t* __r
     }
 }
 
-// THE EMITTER RAYS THAT MET SOMETHING (wavefront.js:1694-1749): the material where each stopped, its emission
-// times what the ray carries, into the pixel; through the haze in air from where the ray started
-__global__ void __launch_bounds__(256) k_emit_resolve(WaveArgs a) {
-    const uint32_t count = min(a.ctr->emitHits, a.q.scap);
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
-        const float4 p4 = a.em.hpos[i], d4 = a.em.hdir[i], r4 = a.em.hrad[i];
-        const f3 p = xyz(p4);
-        const SceneHit H = scene_full(a.prims, a.u.n_prims, p);
-        const st_material& m = a.mats[H.m];
-        const f3 le = mk(m.emissive[0], m.emissive[1], m.emissive[2]);
-        if (max3(le) <= 0.f) continue;
-        f3 c = xyz(r4) * le;
-        if (m.beam_cos > 0.f) {                       // a beam: the outward normal there (three differences)
-            const float eps = march_tol(p, a.u.tol);
-            const float dh = scene_dist(a.prims, a.u.n_prims, p);
-            const f3 nn = normalize(mk(scene_dist(a.prims, a.u.n_prims, mk(p.x + eps, p.y, p.z)) - dh,
-                                       scene_dist(a.prims, a.u.n_prims, mk(p.x, p.y + eps, p.z)) - dh,
-                                       scene_dist(a.prims, a.u.n_prims, mk(p.x, p.y, p.z + eps)) - dh));
-            c = c * emit_beam(m.beam_cos, -dot(xyz(d4), nn));
-        }
-        const float n = fabsf(r4.w);
-        if (a.u.haze_on && fabsf(n - 1.f) <= 1e-3f) {
-            const float hl = fmaxf(p4.w, 0.f) / fmaxf(n, 1e-4f);
-            c = c * haze_tr(a.u, p - xyz(d4) * hl, xyz(d4), hl);
-        }
-        const uint32_t gpix = __float_as_uint(d4.w);
-        deposit(a.frame, gpix, c, a.ctr);
-        if (r4.w < 0.f && a.gd.train) atomicAdd(&a.gd.acc[gpix], luma(c));
-    }
-}
-
 cudaError_t launch_emit_reset(const EmitBufs& em, cudaStream_t s) {
     k_emit_reset<<<32, 256, 0, s>>>(em.grid, em.dev);
     return cudaGetLastError();
@@ -160,7 +130,12 @@ cudaError_t launch_emit_build(const WaveArgs& a, float margin, cudaStream_t s) {
     return cudaGetLastError();
 }
 cudaError_t launch_emit_resolve(const WaveArgs& a, int sms, cudaStream_t s) {
-    k_emit_resolve<<<sms * 2, 256, 0, s>>>(a);
+    if (a.code) {
+        if (!a.code->emit_resolve) return cudaErrorInvalidDeviceFunction;
+        void* args[] = {(void*)&a};
+        return cudaLaunchKernel(a.code->emit_resolve, dim3((unsigned)sms * 2u), dim3(256), args, 0, s);
+    }
+    k_emit_resolve<TableScene><<<sms * 2, 256, 0, s>>>(a);
     return cudaGetLastError();
 }
 

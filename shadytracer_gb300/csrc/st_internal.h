@@ -1,8 +1,10 @@
 // st_internal.h -- what the host side of libshadytracer (st_capi.cu) and the kernels (st_render.cu, st_sppm.cu,
 // st_optics.cu) share: the device buffers of a wave, the device counters, and the launch wrappers.
 #pragma once
+#ifndef __CUDACC_RTC__
 #include <cstdint>
 #include <cuda_runtime.h>
+#endif
 #include "st_device.cuh"
 
 namespace st {
@@ -178,6 +180,23 @@ struct EmitBufs {
                                                                 // contribution | n (resolved by k_emit_resolve)
 };
 
+// A SCENE AS CODE, compiled (st_scene_rtc.cu): the scene-calling kernels of st_scene_kernels.cuh built by NVRTC for
+// sm_103a with the scene's own functions, loaded as a library; each kernel a cudaKernel_t (as the runtime's launch
+// calls take it), and the persistent kernels' occupancies, found once. Host-side only; the kernels never read it.
+struct SceneCode {
+    void* lib = nullptr;                          // cudaLibrary_t
+    const void* march[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};   // [haze][counting pass]
+    const void* surface = nullptr;
+    const void* occlude[2] = {nullptr, nullptr};  // by the shadow side read
+    const void* emit_resolve = nullptr;
+    const void* sc_fill = nullptr;
+    const void* eval_sdf = nullptr;
+    mutable int occ_march[2][2] = {{0, 0}, {0, 0}};   // found at the first launch
+    mutable int occ_surface = 0, occ_occlude = 0;
+    double compile_ms = 0.0;                      // NVRTC's time for it (0: taken from the cache)
+    size_t cubin_bytes = 0;
+};
+
 struct WaveArgs {
     Uni u;
     const DPrim* prims;
@@ -198,8 +217,10 @@ struct WaveArgs {
     GuideBufs gd;                         // the learned proposal, while it runs
     EmitBufs em;                          // the emitter list, in a scene with emitters
     LightBufs lf;                         // the lights' faces
+    const SceneCode* code = nullptr;      // the scene as compiled code (host-side: which kernels to launch); null, the table
 };
 
+#ifndef __CUDACC_RTC__                 // host-side: the launch wrappers and the host helpers
 // launch wrappers (st_render.cu)
 cudaError_t launch_mf_tables(float* ec, float* ecavg, float* e1, cudaStream_t s);
 cudaError_t launch_genrays(const WaveArgs& a, int sms, cudaStream_t s);
@@ -213,7 +234,7 @@ cudaError_t launch_genphotons(const WaveArgs& a, uint32_t first, uint32_t n, int
 cudaError_t launch_photon_shade(const WaveArgs& a, int nxt, int last, int sms, cudaStream_t s);
 cudaError_t launch_gather(const WaveArgs& a, int sms, cudaStream_t s);
 cudaError_t launch_eval_sdf(const DPrim* prims, uint32_t n_prims, const float* pts, uint32_t n, float* out,
-                            cudaStream_t s);
+                            cudaStream_t s, const SceneCode* code = nullptr);
 cudaError_t launch_sort_shadow(const WaveArgs& a, int side, int sms, cudaStream_t s);
 cudaError_t launch_march(const WaveArgs& a, int cur, int nxt, int last, int sms, cudaStream_t s);
 cudaError_t launch_shade(const WaveArgs& a, int nxt, int side, int last, int sms, cudaStream_t s);
@@ -221,7 +242,7 @@ cudaError_t launch_occlude(const WaveArgs& a, int side, int last, int sms, cudaS
 cudaError_t launch_resolve(const WaveArgs& a, cudaStream_t s);
 cudaError_t launch_env_bake(const Uni& u, float* out, cudaStream_t s);
 cudaError_t launch_sc_fill(const DPrim* prims, uint32_t n_prims, f3 lo, float cs, uint32_t dx, uint32_t dy, uint32_t dz,
-                           float* out, int sms, cudaStream_t s);
+                           float* out, int sms, cudaStream_t s, const SceneCode* code = nullptr);
 // the emitter list (st_emit.cu)
 cudaError_t launch_emit_build(const WaveArgs& a, float margin, cudaStream_t s);
 cudaError_t launch_emit_resolve(const WaveArgs& a, int sms, cudaStream_t s);
@@ -229,9 +250,11 @@ cudaError_t launch_emit_reset(const EmitBufs& em, cudaStream_t s);
 // the learned proposal (st_guide.cu)
 cudaError_t launch_guide_infer(const WaveArgs& a, int sms, cudaStream_t s);
 cudaError_t launch_guide_collect(const WaveArgs& a, int sms, cudaStream_t s);
+#endif  // __CUDACC_RTC__
 
 }  // namespace st
 
+#ifndef __CUDACC_RTC__
 // HOST HELPERS (st_capi.cu) that the context path and the render that allocates nothing (st_noalloc.cu) share, so
 // the two derive the same uniforms and pack the same table: the uniforms that depend only on the scene's
 // description, the settings and the camera (env_image: an environment image replaces the sun and sky), and a
@@ -241,3 +264,13 @@ st::Uni make_uni_base(const st_scene_desc& s, const st_params& p, const st_view&
 st::DPrim pack_prim(const st_prim& p);
 // why st_render_noalloc last refused a call on this thread ("" if it did not)
 const char* noalloc_last_error();
+#include <string>
+namespace st {
+// a scene given as code (st_scene_rtc.cu): compiled by NVRTC with the scene-calling kernels and loaded; on failure err
+// says why (with the scene's line) and nothing is kept
+bool scene_code_build(const char* user_src, SceneCode& out, std::string& err);
+bool scene_code_compile(const char* user_src, double& ms, std::string& err);
+void scene_code_free(SceneCode& c);
+}  // namespace st
+
+#endif  // __CUDACC_RTC__

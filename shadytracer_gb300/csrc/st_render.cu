@@ -19,6 +19,7 @@
 #include "st_light.cuh"
 #include "st_guide.cuh"
 #include "st_kernels.cuh"
+#include "st_scene_kernels.cuh"
 
 namespace st {
 
@@ -235,157 +236,6 @@ __global__ void __launch_bounds__(256) k_sort_scatter(const uint32_t* __restrict
         out[boff[key[i]] + rank[i]] = inq ? inq[i] : i;
 }
 
-template <bool HAZE, bool INST, bool COUNT>
-__global__ void __launch_bounds__(256, 4) k_march(WaveArgs a, int cur, int nxt, int last) {
-    extern __shared__ __align__(128) unsigned char smem[];
-    __shared__ __align__(8) uint64_t mbar;
-    __shared__ uint32_t wc[COUNT ? WC_N : 1];
-    DPrim* sp = reinterpret_cast<DPrim*>(smem);
-    const uint32_t n_prims = a.u.n_prims;
-    if (COUNT)
-        for (uint32_t k = threadIdx.x; k < WC_N; k += blockDim.x) wc[k] = 0u;
-    if (!stage_table(sp, a.prims, n_prims * (uint32_t)sizeof(DPrim), &mbar, a.ctr)) return;
-    const uint32_t count = a.ctr->rayCount[cur];
-    const uint32_t* __restrict__ inq = a.u.sort_on ? a.q.sorted : (cur ? a.q.ray[1] : a.q.ray[0]);
-    uint32_t* __restrict__ outq = nxt ? a.q.ray[1] : a.q.ray[0];
-    uint32_t* outc = nxt ? &a.ctr->rayCount[1] : &a.ctr->rayCount[0];
-    const float tol = a.u.tol, stepscale = a.u.stepscale, envR2 = a.u.envR2;
-    const uint32_t maxiter = a.u.maxiter;
-    const uint32_t chunk = last ? 0xffffffffu : MARCH_CHUNK;
-    const int lane = threadIdx.x & 31;
-
-    uint32_t slot = INVALID_SLOT;
-    f3 pos = mk(0.f), dir = mk(0.f);
-    float ltot = 0.f, n = 1.f, tmax = 0.f;
-    uint32_t steps = 0, evals_here = 0;
-    uint32_t wpos = 0, wend = 0;
-    bool exhausted = false;
-    unsigned long long evals = 0;
-    uint32_t pfirst = 0, pcount = n_prims;          // the primitives this ray sees: its instance's, in a batch
-
-    for (;;) {
-        // ---- refill: idle lanes take the warp's next claimed entries ----
-        uint32_t idle = __ballot_sync(FULL_MASK, slot == INVALID_SLOT);
-        if (idle && !exhausted) {
-            if (wpos >= wend) {
-                uint32_t b = 0;
-                if (lane == 0) b = atomicAdd(&a.ctr->marchHead, CLAIM);
-                b = __shfl_sync(FULL_MASK, b, 0);
-                if (b >= count) exhausted = true;
-                else { wpos = b; wend = min(b + CLAIM, count); }
-            }
-            if (!exhausted) {
-                uint32_t avail = wend - wpos;
-                uint32_t rank = __popc(idle & lanemask_lt());
-                if (slot == INVALID_SLOT && rank < avail) {
-                    slot = inq[wpos + rank];
-                    float4 p4 = a.pb.pos[slot], d4 = a.pb.dir[slot];
-                    pos = xyz(p4); ltot = p4.w; dir = xyz(d4); n = d4.w;
-                    uint4 m4 = a.pb.meta[slot];
-                    steps = m4.z;
-                    evals_here = 0;
-                    if (INST) { uint2 rg = a.inst_range[m4.w]; pfirst = rg.x; pcount = rg.y; }
-                    tmax = HAZE ? a.pb.rad[slot].w : 0.f;
-                    if (HAZE && tmax == 0.f) {
-                        // THE LEG'S COLLISION, drawn as it starts (haze.js:255-273 hazeDraw)
-                        const Uni& u = a.u;
-                        tmax = -1.f;
-                        if (fabsf(n - 1.f) <= 1e-3f) {
-                            float absL = __uint_as_float(m4.w);
-                            f3 A = pos - dir * (fmaxf(ltot - absL, 0.f) / fmaxf(n, 1e-4f));
-                            float t0, t1;
-                            haze_span(u, A, dir, 1e30f, t0, t1);
-                            if (t1 > t0) {
-                                uint32_t tile = slot % u.P, j = slot / u.P, seg = (m4.y >> 8) & 0xffu;
-                                Rng hr = path_rng(sample_seed(u.seed, a.ctr->sample + j), tile, ST_SALT_HAZE + seg);
-                                float4 r4 = hr.next();
-                                float t = t0 - logf(1.f - r4.x) / u.hsig;
-                                if (t < t1) tmax = fmaxf(absL + t * n, 1e-30f);
-                            }
-                        }
-                    }
-                }
-                wpos += min((uint32_t)__popc(idle), avail);
-            }
-        }
-        if (__ballot_sync(FULL_MASK, slot != INVALID_SLOT) == 0) break;
-
-        // ---- one step ----
-        bool fin = false, more = false;
-        uint32_t state = RAY_ACTIVE;
-        float dh = 0.f;
-        if (slot != INVALID_SLOT) {
-            // THE STEP CACHE (wavefront.js:901-912): a ball that holds the ray far enough moves it with no distance;
-            // a step that carries it past its collision in the haze is taken back to it below, as a distance step's
-            // is. Up to SC_BURST balls in a row: a lane in empty space goes on while its warp's others ask the scene,
-            // then asks it too where no ball holds it, so the warp's distance pass is not spent waiting on it
-            uint32_t burst = 0;
-            if (!INST && a.u.sc_looks) {
-                while (burst < SC_BURST && !(HAZE && tmax > 0.f && ltot >= tmax)) {
-                    const float sc = sc_step(a.u, pos, dir);
-                    if (!(sc > 0.f)) break;
-                    steps += 1;
-                    f3 off = dir * (sc * stepscale);
-                    pos = pos + off;
-                    ltot += length(off) * n;
-                    burst++;
-                }
-                evals_here += burst;
-            }
-            if (burst == SC_BURST || (burst && evals_here >= chunk)) {
-                if (HAZE && tmax > 0.f && ltot >= tmax) { state = RAY_SCATTER; fin = true; }
-                else if (evals_here >= chunk) more = true;
-            } else if (HAZE && tmax > 0.f && ltot >= tmax) {
-                state = RAY_SCATTER;
-                fin = true;
-            } else {
-                float d = scene_dist<COUNT>(sp + pfirst, pcount, pos, wc);
-                evals++;
-                evals_here++;
-                float ea = fabsf(d);
-                float eps = march_tol(pos, tol);
-                if (ltot > 1000.f || steps > maxiter) state = RAY_MAXITER;
-                if (dot(pos, dir) > 0.f && dot(pos, pos) > envR2) state = RAY_ESCAPED;
-                if (ea < eps || state != RAY_ACTIVE) {
-                    fin = true;
-                    dh = d;
-                } else {
-                    steps += 1;
-                    f3 off = dir * (ea * stepscale);
-                    pos = pos + off;
-                    ltot += length(off) * n;
-                    if (HAZE && tmax > 0.f && ltot >= tmax) { state = RAY_SCATTER; fin = true; }
-                    else if (evals_here >= chunk) more = true;
-                }
-            }
-            if (state == RAY_SCATTER) {                                 // hazeAt: back to the collision
-                pos = pos - dir * ((ltot - tmax) / fmaxf(n, 1e-4f));
-                ltot = tmax;
-            }
-        }
-        uint32_t qp = warp_append(&a.ctr->hitCount, fin);
-        uint32_t cp = warp_append(outc, more);
-        if (fin || more) {
-            a.pb.pos[slot] = make_float4(pos.x, pos.y, pos.z, ltot);
-            uint4 m = a.pb.meta[slot];
-            m.y = (m.y & ~0x00ff0000u) | (state << 16);               // the classes above it kept
-            m.z = steps;
-            a.pb.meta[slot] = m;
-            if (HAZE) a.pb.rad[slot].w = tmax;
-            if (fin) { a.q.hit[qp] = slot; a.q.hitd[qp] = dh; }
-            else outq[cp] = slot;
-            slot = INVALID_SLOT;
-        }
-    }
-    // the steps taken, one atomic per warp
-    for (int o = 16; o > 0; o >>= 1) evals += __shfl_down_sync(FULL_MASK, evals, o);
-    if (lane == 0 && evals) atomicAdd(&a.ctr->march_steps, evals);
-    if (COUNT) {
-        __syncthreads();
-        for (uint32_t k = threadIdx.x; k < WC_N; k += blockDim.x)
-            if (wc[k]) atomicAdd(&a.ctr->work[k], (unsigned long long)wc[k]);
-    }
-}
 
 // ------------------------------------------------------------------------------------------------------------
 // SHADE: what prog_surface asks the scene (the normal by three forward differences at normalTol, the material, the
@@ -393,50 +243,6 @@ __global__ void __launch_bounds__(256, 4) k_march(WaveArgs a, int cur, int nxt, 
 // lobe draw, the MIS weights, the bounce cap and roulette); an escaped ray's environment; a point in the haze
 // (haze.js:493-596 mediumVertex); the deposit of a path that ends. One thread per shade-queue entry.
 // ------------------------------------------------------------------------------------------------------------
-// THE SURFACE: the geometric half of prog_surface (wavefront.js:1037-1147) -- what a hit asks the scene: the
-// normal by three forward differences at normalTol (tracebasics.js:164-165), whether the ray meets it from behind
-// (pathFacing, scene_api.js:127-135), the material there and, for a transmissive one, the medium beyond it
-// (mediumBeyond, two offset tolerances inside). One thread per shade-queue entry, written to hsurf for k_shade,
-// so the shading kernel carries no distance function and the distance work runs at the march's occupancy.
-__global__ void __launch_bounds__(256, 3) k_surface(WaveArgs a) {
-    extern __shared__ __align__(128) unsigned char smem[];
-    __shared__ __align__(8) uint64_t mbar;
-    __shared__ __align__(8) uint64_t mbar2;
-    const Uni& u = a.u;
-    DPrim* sp = reinterpret_cast<DPrim*>(smem);
-    st_material* sm = reinterpret_cast<st_material*>(smem + u.n_prims * sizeof(DPrim));
-    if (!stage_table(sp, a.prims, u.n_prims * (uint32_t)sizeof(DPrim), &mbar, a.ctr)) return;
-    if (!stage_table(sm, a.mats, u.n_mats * (uint32_t)sizeof(st_material), &mbar2, a.ctr)) return;
-    const uint32_t count = a.ctr->hitCount;
-    for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < count; q += gridDim.x * blockDim.x) {
-        const uint32_t slot = a.q.hit[q];
-        const uint4 m4 = a.pb.meta[slot];
-        if (((m4.y >> 16) & 0xffu) != RAY_ACTIVE) continue;          // escaped, out of steps, a haze collision
-        const float dh = a.q.hitd[q];
-        const f3 pos = xyz(a.pb.pos[slot]);
-        const f3 dir = xyz(a.pb.dir[slot]);
-        float eps = march_tol(pos, u.tol);
-        float gx = scene_dist(sp, u.n_prims, mk(pos.x + eps, pos.y, pos.z)) - dh;
-        float gy = scene_dist(sp, u.n_prims, mk(pos.x, pos.y + eps, pos.z)) - dh;
-        float gz = scene_dist(sp, u.n_prims, mk(pos.x, pos.y, pos.z + eps)) - dh;
-        f3 nn = normalize(mk(gx, gy, gz));
-        f3 nrm = dh < 0.f ? -nn : nn;
-        uint32_t ids = SURF_LEAVING;
-        if (!(dot(-dir, nrm) < 0.f)) {
-            SceneHit h = scene_full(sp, u.n_prims, pos);
-            const uint32_t mi = min(h.m, u.n_mats - 1);
-            const st_material& m = sm[mi];
-            uint32_t med = SURF_NONE;
-            if (m.transmission > 0.f && m.metallic < 1.f) {
-                SceneHit mb = scene_full(sp, u.n_prims, pos + (-nrm) * (10.f * eps * 2.f));
-                med = min(mb.a, u.n_mats - 1);
-            }
-            ids = mi | (med << 16);
-        }
-        a.q.hsurf[q] = make_float4(nn.x, nn.y, nn.z, __uint_as_float(ids));
-    }
-}
-
 struct ShadowOut { bool valid, emit, face; f3 org, dir, rad; float n, dist; };
 
 template <bool GUIDE>
@@ -876,151 +682,6 @@ __global__ void __launch_bounds__(256) k_shade(WaveArgs a, int nxt, int side, in
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&a.ctr->segments, (unsigned long long)count);
 }
 
-// ------------------------------------------------------------------------------------------------------------
-// THE OCCLUSION PASS (wavefront.js:1481-1692), distance only, persistent with refill like the march: any surface
-// blocks; leaving the scene, lmax or maxiter reaches (maxiter counted in shadowcut); a ray that reaches deposits.
-// A ray still going after MARCH_CHUNK evaluations is queued for the next iteration's pass on the other side; the
-// last iteration's pass runs every ray to its end (the reference's extra rounds on the last pass,
-// raytrace_main.js THE LAST PASS'S SHADOW ROUNDS).
-// ------------------------------------------------------------------------------------------------------------
-template <int SIDE>
-__global__ void __launch_bounds__(256, 4) k_occlude(WaveArgs a, int last) {
-    constexpr int side = SIDE;
-    extern __shared__ __align__(128) unsigned char smem[];
-    __shared__ __align__(8) uint64_t mbar;
-    DPrim* sp = reinterpret_cast<DPrim*>(smem);
-    const uint32_t n_prims = a.u.n_prims;
-    if (!stage_table(sp, a.prims, n_prims * (uint32_t)sizeof(DPrim), &mbar, a.ctr)) return;
-    const uint32_t count = min(side ? a.ctr->shadowCount[1] : a.ctr->shadowCount[0], a.q.scap);
-    const float4* __restrict__ i_org = side ? a.q.s_org[1] : a.q.s_org[0];
-    const float4* __restrict__ i_dir = side ? a.q.s_dir[1] : a.q.s_dir[0];
-    const float4* __restrict__ i_rad = side ? a.q.s_rad[1] : a.q.s_rad[0];
-    const uint32_t* __restrict__ i_steps = side ? a.q.s_steps[1] : a.q.s_steps[0];
-    float4* o_org = side ? a.q.s_org[0] : a.q.s_org[1];
-    float4* o_dir = side ? a.q.s_dir[0] : a.q.s_dir[1];
-    float4* o_rad = side ? a.q.s_rad[0] : a.q.s_rad[1];
-    uint32_t* o_steps = side ? a.q.s_steps[0] : a.q.s_steps[1];
-    uint32_t* o_cnt = side ? &a.ctr->shadowCount[0] : &a.ctr->shadowCount[1];
-    const float tol = a.u.tol, stepscale = a.u.stepscale, envR2 = a.u.envR2;
-    const uint32_t maxiter = a.u.maxiter;
-    const uint32_t chunk = last ? 0xffffffffu : MARCH_CHUNK;
-    const int lane = threadIdx.x & 31;
-    uint32_t idx = INVALID_SLOT;
-    f3 pos = mk(0.f), dir = mk(0.f);
-    float ltot = 0.f, n = 1.f;
-    uint32_t steps = 0, evals_here = 0, sflag = 0;
-    uint32_t wpos = 0, wend = 0;
-    bool exhausted = false;
-    unsigned long long evals = 0, rays = 0;
-    uint32_t cuts = 0, dropped = 0;
-    for (;;) {
-        uint32_t idle = __ballot_sync(FULL_MASK, idx == INVALID_SLOT);
-        if (idle && !exhausted) {
-            if (wpos >= wend) {
-                uint32_t b = 0;
-                if (lane == 0) b = atomicAdd(&a.ctr->occHead, CLAIM);
-                b = __shfl_sync(FULL_MASK, b, 0);
-                if (b >= count) exhausted = true;
-                else { wpos = b; wend = min(b + CLAIM, count); }
-            }
-            if (!exhausted) {
-                uint32_t avail = wend - wpos;
-                uint32_t rank = __popc(idle & lanemask_lt());
-                if (idx == INVALID_SLOT && rank < avail) {
-                    idx = a.u.sort_on ? a.q.ssorted[wpos + rank] : wpos + rank;
-                    float4 o4 = i_org[idx], d4 = i_dir[idx];
-                    pos = xyz(o4); ltot = o4.w; dir = xyz(d4); n = fabsf(i_rad[idx].w);
-                    steps = i_steps[idx];
-                    sflag = steps & SHADOW_FLAGS;                     // aimed at an emitter (TAG_EMIT), a face
-                    steps &= ~SHADOW_FLAGS;
-                    evals_here = 0;
-                    if (steps == 0u) rays++;
-                }
-                wpos += min((uint32_t)__popc(idle), avail);
-            }
-        }
-        if (__ballot_sync(FULL_MASK, idx != INVALID_SLOT) == 0) break;
-        bool reached = false, done = false, more = false;
-        // the step cache (wavefront.js:1536-1546): balls that hold the ray far enough move it with no distance, up to
-        // SC_BURST in a row, then the distance where none does (as in the march)
-        uint32_t burst = 0;
-        if (idx != INVALID_SLOT && a.u.sc_looks) {
-            while (burst < SC_BURST && !((sflag & SHADOW_FACE) && ltot >= 0.f)) {
-                const float sc = sc_step(a.u, pos, dir);
-                if (!(sc > 0.f)) break;
-                steps += 1;
-                f3 off = dir * (sc * stepscale);
-                pos = pos + off;
-                ltot += length(off) * n;
-                burst++;
-            }
-            evals_here += burst;
-        }
-        if (burst == SC_BURST || (burst && evals_here >= chunk)) {
-            if (evals_here >= chunk) more = true;
-        } else if (idx != INVALID_SLOT) {
-            float d = scene_dist(sp, n_prims, pos);
-            evals++;
-            evals_here++;
-            float ea = fabsf(d);
-            float eps = march_tol(pos, tol);
-            if ((sflag & SHADOW_FACE) && ltot >= 0.f) { reached = true; done = true; }   // at the face (TAG_FNEE)
-            else if (ea < eps) done = true;                           // blocked
-            else if (dot(pos, dir) > 0.f && dot(pos, pos) > envR2) { reached = true; done = true; }
-            else {
-                steps += 1;
-                if (ltot > 1000.f || steps > maxiter) {
-                    reached = true; done = true;
-                    if (steps > maxiter) cuts++;
-                } else {
-                    f3 off = dir * (ea * stepscale);
-                    pos = pos + off;
-                    ltot += length(off) * n;
-                    if (evals_here >= chunk) more = true;
-                }
-            }
-        }
-        uint32_t cp = warp_append(o_cnt, more);
-        // an emitter's ray asks what it stopped at (wavefront.js:1694-1749): handed to k_emit_resolve; it finds
-        // nothing where it leaves the scene
-        const bool met = done && !reached && (sflag & SHADOW_EMIT) != 0u;
-        const uint32_t ep = a.em.on ? warp_append(&a.ctr->emitHits, met) : 0u;
-        if (met && ep < a.q.scap) {
-            a.em.hpos[ep] = f4(pos, ltot);
-            a.em.hdir[ep] = i_dir[idx];
-            a.em.hrad[ep] = i_rad[idx];
-        }
-        if (reached && (sflag & SHADOW_EMIT) == 0u) {
-            float4 r4 = i_rad[idx];
-            uint32_t gpix = __float_as_uint(i_dir[idx].w);          // the pixel in the wave's frames
-            deposit(a.frame, gpix, xyz(r4), a.ctr);
-            if (r4.w < 0.f && a.gd.train) atomicAdd(&a.gd.acc[gpix], luma(xyz(r4)));
-        }
-        if (more) {
-            if (cp < a.q.scap) {
-                o_org[cp] = f4(pos, ltot);
-                o_dir[cp] = i_dir[idx];
-                o_rad[cp] = i_rad[idx];
-                o_steps[cp] = steps | sflag;
-            } else {
-                dropped++;
-            }
-        }
-        if (done || more) idx = INVALID_SLOT;
-    }
-    for (int o = 16; o > 0; o >>= 1) {
-        evals += __shfl_down_sync(FULL_MASK, evals, o);
-        rays += __shfl_down_sync(FULL_MASK, rays, o);
-        cuts += __shfl_down_sync(FULL_MASK, cuts, o);
-        dropped += __shfl_down_sync(FULL_MASK, dropped, o);
-    }
-    if (lane == 0) {
-        if (evals) atomicAdd(&a.ctr->shadow_steps, evals);
-        if (rays) atomicAdd(&a.ctr->shadow_rays, rays);
-        if (cuts) atomicAdd(&a.ctr->shadowcut, cuts);
-        if (dropped) atomicAdd(&a.ctr->shadowdrop, dropped);
-    }
-}
 
 // ------------------------------------------------------------------------------------------------------------
 // RESOLVE (wavefront.js:414-494; measure.js:36-51), in FP64: each sample of the wave in order folded into the mean
@@ -1085,25 +746,37 @@ static int occupancy(const void* fn, size_t smem) {
 template <bool HAZE, bool INST, bool COUNT>
 static void march_variant(const WaveArgs& a, int cur, int nxt, int last, int sms, cudaStream_t s, int* occ_cache) {
     size_t smem = a.u.n_prims * sizeof(DPrim);
-    auto fn = k_march<HAZE, INST, COUNT>;
+    auto fn = k_march<TableScene, HAZE, INST, COUNT>;
     if (smem > 48 * 1024) cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     int nb = occ_cache && *occ_cache ? *occ_cache : occupancy((const void*)fn, smem);
     if (occ_cache) *occ_cache = nb;
     fn<<<sms * nb, 256, smem, s>>>(a, cur, nxt, last);
 }
+// a kernel of the scene's own compiled code (st_scene_rtc.cu): a persistent grid at its occupancy (occ non-null), or
+// grid_per_sm CTAs an SM
+static cudaError_t code_launch(const void* fn, int* occ, unsigned grid_per_sm, int sms, size_t smem, cudaStream_t s,
+                               void** args) {
+    if (!fn) return cudaErrorInvalidDeviceFunction;
+    if (smem > 48 * 1024) cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    unsigned per_sm = grid_per_sm;
+    if (occ) {
+        if (!*occ) *occ = occupancy(fn, smem);
+        per_sm = (unsigned)*occ;
+    }
+    return cudaLaunchKernel(fn, dim3((unsigned)sms * per_sm), dim3(256), args, smem, s);
+}
 cudaError_t launch_march(const WaveArgs& a, int cur, int nxt, int last, int sms, cudaStream_t s) {
+    if (a.code && !a.inst_range) {
+        const int haze = a.u.haze_on ? 1 : 0, count = a.u.count_work ? 1 : 0;
+        void* args[] = {(void*)&a, &cur, &nxt, &last};
+        return code_launch(a.code->march[haze][count], &a.code->occ_march[haze][count], 0, sms, 0, s, args);
+    }
     if (a.inst_range) march_variant<false, true, false>(a, cur, nxt, last, sms, s, nullptr);
     else if (a.u.count_work && a.u.haze_on) march_variant<true, false, true>(a, cur, nxt, last, sms, s, nullptr);
     else if (a.u.count_work) march_variant<false, false, true>(a, cur, nxt, last, sms, s, nullptr);
     else if (a.u.haze_on) march_variant<true, false, false>(a, cur, nxt, last, sms, s, nullptr);
     else march_variant<false, false, false>(a, cur, nxt, last, sms, s, &g_occ_march);
     return cudaGetLastError();
-}
-// the scene's distance at given points, as the march folds the table (st_eval_sdf)
-__global__ void __launch_bounds__(256) k_eval_sdf(const DPrim* __restrict__ pr, uint32_t n_prims,
-                                                  const float* __restrict__ pts, uint32_t n, float* __restrict__ out) {
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-        out[i] = scene_dist(pr, n_prims, mk(pts[3 * i], pts[3 * i + 1], pts[3 * i + 2]));
 }
 // THE MAP'S BAKE (envmap.js:100-150 prog_envbake): one thread a texel of the equal-area map, the environment's own
 // light (no gains) at 2 x 2 stratified points in it, the sun's cone left out where there is one; its mean luminance
@@ -1124,20 +797,13 @@ __global__ void __launch_bounds__(256) k_env_bake(Uni u, float* __restrict__ out
         }
     out[i] = luma(acc * 0.25f);
 }
-// THE STEP CACHE'S CELLS (wavefront.js:119-147 prog_stepcache_fill): one thread a cell, the scene's distance at its
-// centre, its magnitude held to [1e-6, 1e18]
-__global__ void __launch_bounds__(256) k_sc_fill(const DPrim* __restrict__ prims, uint32_t n_prims, f3 lo, float cs,
-                                                 uint32_t dx, uint32_t dy, uint32_t dz, float* __restrict__ out) {
-    const uint64_t n = (uint64_t)dx * dy * dz;
-    for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (uint64_t)gridDim.x * blockDim.x) {
-        const uint32_t x = (uint32_t)(k % dx), y = (uint32_t)((k / dx) % dy), z = (uint32_t)(k / ((uint64_t)dx * dy));
-        const f3 c = lo + mk((float)x + 0.5f, (float)y + 0.5f, (float)z + 0.5f) * cs;
-        out[k] = fminf(fmaxf(fabsf(scene_dist(prims, n_prims, c)), 1e-6f), 1e18f);
-    }
-}
 cudaError_t launch_sc_fill(const DPrim* prims, uint32_t n_prims, f3 lo, float cs, uint32_t dx, uint32_t dy, uint32_t dz,
-                           float* out, int sms, cudaStream_t s) {
-    k_sc_fill<<<sms * 8, 256, 0, s>>>(prims, n_prims, lo, cs, dx, dy, dz, out);
+                           float* out, int sms, cudaStream_t s, const SceneCode* code) {
+    if (code) {
+        void* args[] = {(void*)&prims, &n_prims, &lo, &cs, &dx, &dy, &dz, &out};
+        return code_launch(code->sc_fill, nullptr, 8, sms, 0, s, args);
+    }
+    k_sc_fill<TableScene><<<sms * 8, 256, 0, s>>>(prims, n_prims, lo, cs, dx, dy, dz, out);
     return cudaGetLastError();
 }
 cudaError_t launch_env_bake(const Uni& u, float* out, cudaStream_t s) {
@@ -1145,8 +811,14 @@ cudaError_t launch_env_bake(const Uni& u, float* out, cudaStream_t s) {
     return cudaGetLastError();
 }
 cudaError_t launch_eval_sdf(const DPrim* prims, uint32_t n_prims, const float* pts, uint32_t n, float* out,
-                            cudaStream_t s) {
-    k_eval_sdf<<<std::min((n + 255u) / 256u, 4096u), 256, 0, s>>>(prims, n_prims, pts, n, out);
+                            cudaStream_t s, const SceneCode* code) {
+    const unsigned blocks = std::min((n + 255u) / 256u, 4096u);
+    if (code) {
+        if (!code->eval_sdf) return cudaErrorInvalidDeviceFunction;
+        void* args[] = {(void*)&prims, &n_prims, (void*)&pts, &n, &out};
+        return cudaLaunchKernel(code->eval_sdf, dim3(blocks), dim3(256), args, 0, s);
+    }
+    k_eval_sdf<TableScene><<<blocks, 256, 0, s>>>(prims, n_prims, pts, n, out);
     return cudaGetLastError();
 }
 cudaError_t launch_sort(const WaveArgs& a, int cur, int sms, cudaStream_t s) {
@@ -1169,10 +841,16 @@ cudaError_t launch_sort_shadow(const WaveArgs& a, int side, int sms, cudaStream_
     return cudaGetLastError();
 }
 cudaError_t launch_surface(const WaveArgs& a, int sms, cudaStream_t s) {
+    if (a.code && !a.inst_range) {
+        const size_t smem = a.u.n_mats * sizeof(st_material);
+        void* args[] = {(void*)&a};
+        return code_launch(a.code->surface, &a.code->occ_surface, 0, sms, smem, s, args);
+    }
     size_t smem = a.u.n_prims * sizeof(DPrim) + a.u.n_mats * sizeof(st_material);
-    if (smem > 48 * 1024) cudaFuncSetAttribute(k_surface, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (!g_occ_surf) g_occ_surf = occupancy((const void*)k_surface, smem);
-    k_surface<<<sms * g_occ_surf, 256, smem, s>>>(a);
+    auto fn = k_surface<TableScene>;
+    if (smem > 48 * 1024) cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (!g_occ_surf) g_occ_surf = occupancy((const void*)fn, smem);
+    fn<<<sms * g_occ_surf, 256, smem, s>>>(a);
     return cudaGetLastError();
 }
 cudaError_t launch_shade(const WaveArgs& a, int nxt, int side, int last, int sms, cudaStream_t s) {
@@ -1191,11 +869,16 @@ cudaError_t launch_shade(const WaveArgs& a, int nxt, int side, int last, int sms
 template <int SIDE>
 static void occlude_side(const WaveArgs& a, int last, int sms, cudaStream_t s) {
     size_t smem = a.u.n_prims * sizeof(DPrim);
-    if (smem > 48 * 1024) cudaFuncSetAttribute(k_occlude<SIDE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (!g_occ_occl) g_occ_occl = occupancy((const void*)k_occlude<SIDE>, smem);
-    k_occlude<SIDE><<<sms * g_occ_occl, 256, smem, s>>>(a, last);
+    auto fn = k_occlude<TableScene, SIDE>;
+    if (smem > 48 * 1024) cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (!g_occ_occl) g_occ_occl = occupancy((const void*)fn, smem);
+    fn<<<sms * g_occ_occl, 256, smem, s>>>(a, last);
 }
 cudaError_t launch_occlude(const WaveArgs& a, int side, int last, int sms, cudaStream_t s) {
+    if (a.code && !a.inst_range) {
+        void* args[] = {(void*)&a, &last};
+        return code_launch(a.code->occlude[side ? 1 : 0], &a.code->occ_occlude, 0, sms, 0, s, args);
+    }
     if (side) occlude_side<1>(a, last, sms, s);
     else occlude_side<0>(a, last, sms, s);
     return cudaGetLastError();

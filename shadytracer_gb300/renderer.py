@@ -23,7 +23,7 @@ PARAM_KEYS = [f for f, _ in T.StParams._fields_]
 
 
 class PathTracer:
-    def __init__(self, scene=None, device=0):
+    def __init__(self, scene=None, device=0, code=None):
         self.L = load()
         self.ctx = C.c_void_p()
         check(self.L.st_create(device, C.byref(self.ctx)), None, "st_create (no GPU, or no device %d)" % device)
@@ -31,7 +31,7 @@ class PathTracer:
         self.view = None
         self.scene = None
         if scene is not None:
-            self.set_scene(scene)
+            self.set_scene(scene, code=code)
             self.set_params(scene.params)
             self.set_view(scene.view)
 
@@ -54,12 +54,28 @@ class PathTracer:
         self.close()
 
     # ---- the scene, the settings, the camera ----
-    def set_scene(self, scene):
-        err = C.create_string_buffer(512)
-        rc = self.L.st_set_scene(self.ctx, None, C.byref(scene.desc), err, 512)
+    def set_scene(self, scene, code=None):
+        """RT.setScene(s). code: None, the scene's primitive table (the scene as data); True, the table written as
+        code by codegen.generate and compiled for sm_103a; a string, that CUDA source (st_set_scene's contract).
+        Returns NVRTC's milliseconds for it (0 for a table or a source compiled before). On failure the old scene is
+        kept and StError says why."""
+        if code is True:
+            from .codegen import generate
+            code = generate(scene)
+        err = C.create_string_buffer(1 << 16)
+        src = code.encode() if isinstance(code, str) else None
+        rc = self.L.st_set_scene(self.ctx, src, C.byref(scene.desc), err, 1 << 16)
         if rc != 0:
             raise StError(rc, "setScene: " + err.value.decode(errors="replace"))
         self.scene = scene
+        self.code = code
+        return self.scene_code_info()["compile_ms"]
+
+    def scene_code_info(self):
+        is_code, ms, nbytes = C.c_int(), C.c_double(), C.c_uint64()
+        check(self.L.st_scene_code_info(self.ctx, C.byref(is_code), C.byref(ms), C.byref(nbytes)), self.ctx,
+              "st_scene_code_info")
+        return {"code": bool(is_code.value), "compile_ms": ms.value, "cubin_bytes": nbytes.value}
 
     def set_params(self, p):
         check(self.L.st_set_params(self.ctx, C.byref(p), None), self.ctx, "st_set_params")
@@ -240,6 +256,7 @@ class PathTracer:
                 "box_lo": list(s.box_lo), "box_inv_ext": s.box_inv_ext, "inferred": s.inferred}
 
 
-def create_path_tracer(scene=None, device=0):
-    """createPathTracer (lib/pathtracer/index.js:90) + RT.init: a context on `device` with `scene` loaded."""
-    return PathTracer(scene, device)
+def create_path_tracer(scene=None, device=0, code=None):
+    """createPathTracer (lib/pathtracer/index.js:90) + RT.init: a context on `device` with `scene` loaded (as code
+    compiled for sm_103a when `code` is True or a source; PathTracer.set_scene)."""
+    return PathTracer(scene, device, code=code)
