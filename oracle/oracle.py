@@ -100,14 +100,15 @@ class Accum:
         return out
 
 
-def render(scene, nsamples, accum=None, fp64=False, threads=0, sample0=None, path_first=0, path_count=0):
-    """Trace `nsamples` samples of `scene` (a shadytracer_gb300.scenes.Scene) into `accum` (made if None)."""
+def render(scene, nsamples, accum=None, fp64=False, threads=0, sample0=None, path_first=0, path_count=0, cull=False):
+    """Trace `nsamples` samples of `scene` (a shadytracer_gb300.scenes.Scene) into `accum` (made if None). cull: the
+    f32 arithmetic with the reference's bounding-box culling at the root (its generated code's work a step)."""
     L = lib()
     p = scene.params
     if accum is None:
         accum = Accum(p.width, p.height)
     s0 = accum.next_sample if sample0 is None else sample0
-    rc = L.sto_render(C.byref(scene.desc), C.byref(p), C.byref(scene.view), s0, nsamples, 1 if fp64 else 0,
+    rc = L.sto_render(C.byref(scene.desc), C.byref(p), C.byref(scene.view), s0, nsamples, 1 if fp64 else (2 if cull else 0),
                       ptr(accum.rgb), ptr(accum.V), ptr(accum.S), ptr(accum.count), ptr(accum.counters), threads,
                       path_first, path_count)
     if rc != 0:

@@ -87,7 +87,14 @@ template <class T> struct Ctx {
     // the lights' faces and the material -> face map (its index + 1, 0 none)
     const std::vector<OFace>* faces = nullptr;
     uint8_t face_of[ST_MAX_MATERIALS] = {};
+    // the reference's bounding-box culling at the root (a timing mode: the CPU baseline does the reference's work)
+    const std::vector<CullBox>* cull = nullptr;
 };
+// the march's and the shadow rays' distance: the fold, or the reference's culled render copy of it
+template <class T> inline T march_dist(const Ctx<T>& C, const V3<T>& p) {
+    if (C.cull) return scene_dist_culled(*C.s, *C.cull, p, T(10) * march_tol(p, C.tol));
+    return scene_eval(*C.s, p).d;
+}
 const uint32_t LT_G = 128, LT_N = LT_G * LT_G;
 const float LT_FLOOR_F = 0.2f;
 // ltSearch / ltMass (wavefront.js:520-536)
@@ -190,13 +197,13 @@ template <class T> inline T march(const Ctx<T>& C, Ray<T>& r, Stats& st, bool us
             r.state = RAY_SCATTER;
             break;
         }
-        SceneHit<T> h = scene_eval(*C.s, r.pos);
-        T ea = std::fabs(h.d);
+        const T hd = march_dist(C, r.pos);
+        T ea = std::fabs(hd);
         T eps = march_tol(r.pos, C.tol);
         steps++;
         if (r.ltot > T(1000) || r.steps > C.p.maxiter) r.state = RAY_MAXITER;
         if (dot(r.pos, r.dir) > T(0) && dot(r.pos, r.pos) > C.envR2) r.state = RAY_ESCAPED;
-        if (ea < eps || r.state != RAY_ACTIVE) { dh = h.d; break; }
+        if (ea < eps || r.state != RAY_ACTIVE) { dh = hd; break; }
         r.steps += 1;
         T d = ea * C.stepscale;
         move_by(r, r.dir * d);
@@ -214,9 +221,9 @@ template <class T> inline bool occlude(const Ctx<T>& C, V3<T> pos, const V3<T>& 
     bool reached = false, cut = false;
     uint64_t evals = 0;
     for (;;) {
-        SceneHit<T> h = scene_eval(*C.s, pos);
+        const T hd = march_dist(C, pos);
         evals++;
-        T ea = std::fabs(h.d);
+        T ea = std::fabs(hd);
         T eps = march_tol(pos, C.tol);
         if (face && ltot >= T(0)) { reached = true; break; }                           // at the face
         if (ea < eps) break;                                                           // blocked
@@ -1165,7 +1172,7 @@ void trace_photon(const Ctx<T>& C, U4 ps, uint32_t id, uint32_t N, std::vector<P
 template <class T>
 static int render_impl(const st_scene_desc* s, const st_params* p, const st_view* v, uint32_t sample0,
                        uint32_t nsamples, double* acc_rgb, double* mV, double* mS, uint32_t* acc_cnt,
-                       uint64_t* counters, int threads, uint32_t path_first, uint32_t path_count) {
+                       uint64_t* counters, int threads, uint32_t path_first, uint32_t path_count, bool cull = false) {
     // the lights' faces, drawn as sheets appended to the primitives (the scene the rest of the oracle sees)
     std::vector<st_prim> prims_x(s->prims, s->prims + s->n_prims);
     std::vector<OFace> faces;
@@ -1179,6 +1186,8 @@ static int render_impl(const st_scene_desc* s, const st_params* p, const st_view
         if (!faces.empty()) C.faces = &faces;
         s = &sx;
     }
+    std::vector<CullBox> boxes;
+    if (cull) { boxes = cull_boxes(*s); C.cull = &boxes; }
     C.s = s; C.p = *p; C.d = derive(*p, *s);
     C.env.init(*p, C.d);
     C.tb = tables<T>();
@@ -1314,7 +1323,8 @@ static int render_impl(const st_scene_desc* s, const st_params* p, const st_view
 extern "C" {
 
 // Render nsamples samples from sample0 on, folding each into the FP64 accumulation (caller-owned, continued across
-// calls). fp64: 0 the reference-equivalent f32 arithmetic, 1 the accuracy oracle. path_first/path_count restrict the
+// calls). fp64: 0 the reference-equivalent f32 arithmetic, 1 the accuracy oracle, 2 the f32 arithmetic with the
+// reference's bounding-box culling at the root (the work its generated code does a step). path_first/path_count restrict the
 // traced paths (a crop, for the CPU baseline's bounded sample); 0/0 = all.
 // the environment image for every render that follows (envimage.js; envmap.js the map, baked here in double at the
 // library's 2 x 2 points a texel and tabulated as the library tabulates it); rgb NULL: back to the sun and sky
@@ -1367,9 +1377,10 @@ int sto_render(const st_scene_desc* s, const st_params* p, const st_view* v, uin
                uint32_t path_first, uint32_t path_count) {
     if (!s || !p || !v || !acc_rgb || !mV || !mS || !acc_cnt) return -1;
     if (s->n_materials == 0 || s->n_prims == 0) return -1;
-    if (fp64)
+    if (fp64 == 1)
         return render_impl<double>(s, p, v, sample0, nsamples, acc_rgb, mV, mS, acc_cnt, counters, threads, path_first, path_count);
-    return render_impl<float>(s, p, v, sample0, nsamples, acc_rgb, mV, mS, acc_cnt, counters, threads, path_first, path_count);
+    return render_impl<float>(s, p, v, sample0, nsamples, acc_rgb, mV, mS, acc_cnt, counters, threads, path_first, path_count,
+                              fp64 == 2);
 }
 
 int sto_mf_tables(int fp64, float* ec, float* ecavg, float* e1) {

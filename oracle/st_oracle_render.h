@@ -234,6 +234,81 @@ template <class T> inline SceneHit<T> scene_eval(const st_scene_desc& s, const V
     return H;
 }
 
+// BOUNDING-BOX CULLING AT THE ROOT (builder/codegen.js:2141-2193, ONLY THE DEAR ONES; scene_api.js:288-305 cullDist,
+// cullMargin): each top-level node that is not one plain shape -- here an item with a CSG chain -- is first measured
+// against its box; farther than the margin (ten surface tolerances), the box's distance stands in for it as a lower
+// bound (CULL, the nearest skipped box) and it is not evaluated; the fold's |d| is then held to CULL
+// (codegen.js:2350). A plain shape (an item of one primitive) is never boxed: its box test costs what it does. The
+// box: the members' bounding spheres (a subtraction adds nothing), widened by the largest smooth-union radius / 4
+// (the most a polynomial smooth union bulges past its members); none where a member has no bound (a plane, a lens).
+struct CullBox { uint32_t first, end; bool boxed; double lo[3], hi[3]; };
+inline std::vector<CullBox> cull_boxes(const st_scene_desc& s) {
+    std::vector<CullBox> out;
+    uint32_t i = 0;
+    while (i < s.n_prims) {
+        CullBox b{i, i + 1, false, {1e300, 1e300, 1e300}, {-1e300, -1e300, -1e300}};
+        while (b.end < s.n_prims && s.prims[b.end].op != ST_OP_ITEM) b.end++;
+        bool bounded = true;
+        double kmax = 0.0;
+        for (uint32_t j = b.first; j < b.end; j++) {
+            const st_prim& q = s.prims[j];
+            if (j > b.first && q.op == ST_OP_SUB) continue;
+            if (q.op == ST_OP_SMOOTH) kmax = std::max(kmax, (double)q.k);
+            const float* r = q.p;
+            double R;
+            switch (q.type) {
+                case ST_PRIM_SPHERE: R = std::fabs(r[0]); break;
+                case ST_PRIM_BOX: R = std::sqrt(double(r[0]) * r[0] + double(r[1]) * r[1] + double(r[2]) * r[2]); break;
+                case ST_PRIM_ROUNDBOX:
+                    R = std::sqrt(double(r[0]) * r[0] + double(r[1]) * r[1] + double(r[2]) * r[2]) + std::fabs(r[3]);
+                    break;
+                case ST_PRIM_TORUS: R = std::fabs(r[0]) + std::fabs(r[1]); break;
+                case ST_PRIM_PRISM: R = std::sqrt(double(r[1]) * r[1] + 0.25 * double(r[2]) * r[2]) + std::fabs(r[3]); break;
+                case ST_PRIM_CYLINDER: R = std::sqrt(double(r[0]) * r[0] + double(r[1]) * r[1]); break;
+                default: R = -1.0;
+            }
+            if (R < 0.0) { bounded = false; break; }
+            for (int k = 0; k < 3; k++) {
+                b.lo[k] = std::min(b.lo[k], (double)q.pos[k] - R);
+                b.hi[k] = std::max(b.hi[k], (double)q.pos[k] + R);
+            }
+        }
+        b.boxed = bounded && b.end - b.first > 1;
+        for (int k = 0; k < 3; k++) { b.lo[k] -= 0.25 * kmax + 1e-6; b.hi[k] += 0.25 * kmax + 1e-6; }
+        out.push_back(b);
+        i = b.end;
+    }
+    return out;
+}
+// the distance alone, as the reference's culled render copy folds it (the march's and the shadow rays' question)
+template <class T> inline T scene_dist_culled(const st_scene_desc& s, const std::vector<CullBox>& boxes, const V3<T>& p,
+                                              T margin) {
+    T best = T(1e7), cull = T(1e7);
+    for (const CullBox& b : boxes) {
+        if (b.boxed) {                                                      // cullDist (scene_api.js:297-301)
+            const T cx = T(0.5) * (T(b.lo[0]) + T(b.hi[0])), cy = T(0.5) * (T(b.lo[1]) + T(b.hi[1]));
+            const T cz = T(0.5) * (T(b.lo[2]) + T(b.hi[2]));
+            const T dx = std::fabs(p.x - cx) - T(0.5) * (T(b.hi[0]) - T(b.lo[0]));
+            const T dy = std::fabs(p.y - cy) - T(0.5) * (T(b.hi[1]) - T(b.lo[1]));
+            const T dz = std::fabs(p.z - cz) - T(0.5) * (T(b.hi[2]) - T(b.lo[2]));
+            const T ox = std::max(dx, T(0)), oy = std::max(dy, T(0)), oz = std::max(dz, T(0));
+            const T bd = std::sqrt(ox * ox + oy * oy + oz * oz) + std::min(std::max(dx, std::max(dy, dz)), T(0));
+            if (bd > margin) { cull = std::min(cull, bd); continue; }
+        }
+        T di = prim_sdf(s.prims[b.first], p);
+        for (uint32_t j = b.first + 1; j < b.end; j++) {
+            const st_prim& pj = s.prims[j];
+            T dj = prim_sdf(pj, p);
+            if (pj.op == ST_OP_SMOOTH) di = smooth_union(di, dj, T(pj.k));
+            else if (pj.op == ST_OP_UNION) di = std::min(di, dj);
+            else di = std::max(di, -dj);
+        }
+        if (std::fabs(di) < std::fabs(best)) best = di;
+    }
+    if (cull < std::fabs(best)) best = cull;
+    return best;
+}
+
 // ------------------------------------------------------------------------------------------------------------
 // THE ENVIRONMENT -- core/sdf.js:70-160 (inSunDisc, envBase, skyRadiance, sampleSunCone, envRadiance,
 // skyLuminance). The environment's code (core/environment.js: "THE ENVIRONMENT IS CODE") is the scene's: here a

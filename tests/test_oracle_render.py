@@ -206,3 +206,37 @@ def test_absorption_inside_closed_form():
     r = oracle.render(s, 4)
     # the march stops within its tolerance (1e-5 m) of each face
     assert np.allclose(r.rgb.reshape(-1, 3), s.info["expected"], rtol=5e-5)
+
+
+def clusters_scene(width=48, height=32):
+    """Four separate smooth-unioned pairs over a floor: groups whose boxes the reference's root cull skips wherever a
+    point is farther from them than ten surface tolerances."""
+    from shadytracer_gb300.scenes import Scene, prim, air, diffuse, plastic, look_at, default_params
+    from shadytracer_gb300.st_types import ST_PRIM_PLANE, ST_PRIM_SPHERE, ST_PRIM_BOX, ST_OP_SMOOTH
+    mats = [air(), diffuse((0.7, 0.7, 0.7)), plastic((0.8, 0.3, 0.2), 0.3)]
+    prims = [prim(ST_PRIM_PLANE, material=1)]
+    for i, (x, y) in enumerate([(-1.5, -1.5), (1.5, -1.5), (-1.5, 1.5), (1.5, 1.5)]):
+        prims.append(prim(ST_PRIM_SPHERE, pos=(x, y, 0.4), params=(0.35,), material=2))
+        prims.append(prim(ST_PRIM_BOX, pos=(x + 0.3, y, 0.3), params=(0.25, 0.25, 0.3), material=2, op=ST_OP_SMOOTH,
+                          k=0.08))
+    s = Scene(prims, mats, env_radius=30.0, name="clusters")
+    s.params = default_params(width=width, height=height, maxbounce=4, sun_elevation=40.0, sun_azimuth=30.0,
+                              sun_illuminance=100000.0, sky_luminance=3000.0, ground_luminance=500.0, eps=1e-4, seed=3)
+    s.view = look_at((-4.0, -5.0, 3.0), (0.0, 0.0, 0.3), 50.0, width / height)
+    s.info = {"spp": 4}
+    return s
+
+
+@pytest.mark.parametrize("make", [clusters_scene, lambda: scenes.sdf_room(width=48, height=27)])
+def test_the_references_root_cull_keeps_the_picture(make):
+    """The oracle's timing mode with the reference's bounding-box culling at the root (builder/codegen.js:2141-2193,
+    scene_api.js cullDist): a culled group's box distance stands in for it, so the march takes different steps
+    but meets the same surfaces -- the picture within the error bars of the unculled one, most pixels equal."""
+    s = make()
+    a = oracle.render(s, 4)
+    b = oracle.render(make(), 4, cull=True)
+    La, Lb = a.luma(), b.luma()
+    sd = np.hypot(np.nan_to_num(a.se()), np.nan_to_num(b.se()))
+    ok = sd > 0
+    assert np.mean(np.abs((La - Lb)[ok]) <= 4 * sd[ok] + 1e-3 * np.maximum(La[ok], 1.0)) > 0.98
+    assert np.mean(np.abs(La - Lb) <= 1e-3 * np.maximum(La, 1.0)) > 0.5
