@@ -71,7 +71,8 @@ def parse():
     ap.add_argument("--no-haze", action="store_true", help="skip the haze-box beam's leg")
     ap.add_argument("--no-env", action="store_true", help="skip the environment image's leg")
     ap.add_argument("--no-sc", action="store_true", help="skip the step cache's leg")
-    ap.add_argument("--leg", default="all", choices=["all", "sppm", "rmse", "optics", "mlp", "emit", "haze", "env", "sc"],
+    ap.add_argument("--leg", default="all", choices=["all", "sppm", "rmse", "caustic_rmse", "optics", "mlp", "emit",
+                                                     "haze", "env", "sc"],
                     help="run one leg alone and print its JSON (profiling runs of the photon map or the optics bench)")
     return ap.parse_args()
 
@@ -100,17 +101,21 @@ def replica_value(world, paths_per_step, ms):
 
 
 def workload(small, spp=0):
+    """The room as the reference renders it by default: its scene as code (the builder's generated SDF, here
+    codegen.py's CUDA compiled by NVRTC for sm_103a at st_set_scene), the step cache off (the reference's developer
+    setting; the scene_forms leg measures it on)."""
     from shadytracer_gb300 import scenes
     if small:
         s = scenes.sdf_room(width=480, height=270, spp=spp or 4, maxbounce=8)
     else:
         s = scenes.sdf_room(width=1920, height=1080, spp=spp or 64, maxbounce=8)
-    # the reference's step cache (its developer setting, which its own bench builds measure filled once): one look,
-    # 16 M cells (64 MB, held in L2) over the primitives' box; filled once a scene, outside the timed renders and
-    # inside the end-to-end ones (each sets the scene again). The same picture, within the march tolerance.
-    s.params.step_cache = 1
-    s.params.step_cache_cells = 16.0
+    s.params.step_cache = 0
     return s
+
+
+def scene_code(s):
+    from shadytracer_gb300 import codegen
+    return codegen.generate(s)
 
 
 def config_of(s):
@@ -119,6 +124,7 @@ def config_of(s):
                                                                                      s.info["spp"], p.maxbounce),
             "width": p.width, "height": p.height, "spp": s.info["spp"], "maxbounce": p.maxbounce,
             "paths_per_step": p.width * p.height * s.info["spp"], "primitives": 24,
+            "scene": "code: codegen.py's CUDA for the room, compiled by NVRTC for sm_103a at st_set_scene",
             "step_cache": ("%d look%s, %g M cells" % (1 if p.step_cache == 1 else 3, "" if p.step_cache == 1 else "s",
                                                     p.step_cache_cells or 4.0)) if p.step_cache else "off",
             "l2": "working set above L2: path state + queues of 2.07 M paths are 300 MB a wave (> 129 MB L2)"}
@@ -189,6 +195,8 @@ def peaks():
 # the CPU baseline: the oracle in f32 over a band of the picture's paths, all host threads
 # ---------------------------------------------------------------------------------------------------------------
 def cpu_baseline(s, budget_s=15.0):
+    """The oracle in f32 with the reference's bounding-box culling at the root (the work the reference's generated
+    code does a step, builder/codegen.js:2141-2193), every host thread, bands of the picture's paths."""
     from oracle import oracle
     threads = os.cpu_count() or 1
     p = s.params
@@ -196,21 +204,22 @@ def cpu_baseline(s, budget_s=15.0):
     acc = oracle.Accum(p.width, p.height)
     # bands of consecutive paths from the middle of the picture outwards, one sample each, until the budget is spent
     band = min(P, 16384)
-    oracle.render(s, 1, acc, fp64=False, threads=threads, sample0=0, path_first=P // 2, path_count=band)  # warm
+    oracle.render(s, 1, acc, fp64=False, threads=threads, sample0=0, path_first=P // 2, path_count=band,
+                  cull=True)  # warm
     first0 = P // 2
     n, k = 0, 0
     t = time.perf_counter()
     while True:
         first = (first0 + k * band) % max(P - band, 1)
-        oracle.render(s, 1, acc, fp64=False, threads=threads, sample0=1, path_first=first, path_count=band)
+        oracle.render(s, 1, acc, fp64=False, threads=threads, sample0=1, path_first=first, path_count=band, cull=True)
         n += band
         k += 1
         dt = time.perf_counter() - t
         if dt >= budget_s or k * band >= P:
             break
     return {"value": n / dt / 1e6, "unit": "Mpaths/s", "cores": threads, "kind": "port",
-            "sample": "%d paths of sample 1 (%d bands of %d consecutive paths from row %d on, %dx%d), %.1f s" % (
-                n, k, band, first0 // p.width, p.width, p.height, dt)}
+            "sample": "%d paths of sample 1 (%d bands of %d consecutive paths from row %d on, %dx%d), %.1f s; f32, the "
+                      "reference's root bounding-box cull" % (n, k, band, first0 // p.width, p.width, p.height, dt)}
 
 
 def run_reference(args):
@@ -232,7 +241,8 @@ def run_reference(args):
     line = {"impl": "reference", "metric": metric, "value": v, "unit": "Mpaths/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / max(args.steps, 1),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": dict(config_of(s), step_cache="off: the oracle marches the distance field at every step"),
+            "config": dict(config_of(s), scene="the reference's fold: every top-level group culled by its box "
+                                              "where it is farther than ten tolerances (its generated code's work)"),
             "cpu_baseline": {"value": v, "unit": "Mpaths/s", "cores": os.cpu_count(), "kind": "port",
                              "sample": "each step: " + samples[-1]},
             "e2e": {"value": v, "unit": "Mpaths/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -323,7 +333,7 @@ def sppm_leg(args, dev, with_cpu):
     N = 250_000 if small else 4_000_000
     passes = 8 if small else 64
     s = scenes.sppm_caustic(width=W, height=W, photons=N, r1=0.005, alpha=0.7)
-    rt = create_path_tracer(s, device=dev)
+    rt = create_path_tracer(s, device=dev, code=True)
     stream = torch.cuda.ExternalStream(rt.stream(), device=torch.device("cuda", dev))
     for _ in range(max(args.warmup, 3)):
         rt.invalidate()
@@ -363,15 +373,29 @@ def sppm_leg(args, dev, with_cpu):
            "stored_per_pass": stt.stored, "dropped": stt.cut, "mean_luma": Lmean,
            "kernel_share": {k: round(v[1] / tot_ms, 4) for k, v in kt.items()}}
     if with_cpu:
+        # the oracle on every host thread over whole passes -- the sun's photons traced and stored, the grid built,
+        # the camera's paths traced and gathered -- against the GPU's whole-render photons a second
         from oracle import oracle
         import os as _os
-        sc = scenes.sppm_caustic(width=W, height=W, photons=200_000, r1=0.005, alpha=0.7)
+        Wc = 256
+        Nc = N * Wc * Wc // (W * W)              # the same photons a camera path as the GPU's render
+        sc = scenes.sppm_caustic(width=Wc, height=Wc, photons=Nc, r1=0.005, alpha=0.7)
+        threads = _os.cpu_count() or 1
+        oracle.render(sc, 1, threads=threads)                       # warm
         t0 = time.perf_counter()
-        n, _ = oracle.sppm_photons(sc, 0)
+        k = 0
+        while True:
+            oracle.render(scenes.sppm_caustic(width=Wc, height=Wc, photons=Nc, r1=0.005, alpha=0.7), 1,
+                          threads=threads, sample0=k)
+            k += 1
+            if time.perf_counter() - t0 > 10.0 or k >= 8:
+                break
         dt = time.perf_counter() - t0
-        out["cpu_baseline"] = {"value": 200_000 / dt, "unit": "photons/s", "cores": 1, "kind": "port",
-                               "sample": "one pass of 200000 sun photons of the same scene, single-threaded, %.1f s "
-                                         "(%d stored)" % (dt, n)}
+        out["cpu_baseline"] = {"value": Nc * k / dt, "unit": "photons/s (whole passes)", "cores": threads,
+                               "kind": "port", "compare_to": "render.photons_per_s_whole",
+                               "sample": "%d whole passes of the caustic at %dx%d with %d sun photons a pass (trace, "
+                                         "store, grid, camera paths, gather), every host thread, %.1f s"
+                                         % (k, Wc, Wc, Nc, dt)}
     return out
 
 
@@ -394,7 +418,7 @@ def mlp_leg(args, dev):
         s = scenes.sdf_room(width=W, height=H, spp=spp, finish="diffuse", sky_illuminance=10.0, ground_luminance=1.0)
         s.params.guide = guide
         return s
-    rt = create_path_tracer(scene(0), device=dev)
+    rt = create_path_tracer(scene(0), device=dev, code=True)
     left = ref_spp
     while left > 0:
         rt.step(min(512, left))
@@ -404,7 +428,7 @@ def mlp_leg(args, dev):
     out = {"workload": "room24 diffuse, sun patch only (sky 10 lx), %dx%d, %d samples against a %d-sample plain render"
                        % (W, H, spp, ref_spp), "metric": "relative RMSE at equal samples", "legs": {}}
     for guide in (0, 1):
-        rt = create_path_tracer(scene(guide), device=dev)
+        rt = create_path_tracer(scene(guide), device=dev, code=True)
         stream = torch.cuda.ExternalStream(rt.stream(), device=torch.device("cuda", dev))
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         rt.invalidate()
@@ -461,7 +485,7 @@ def emit_leg(args, dev):
         s = scenes.lamp_floor(width=W, height=H, spp=spp)
         s.params.emit_off = off
         cf, ok = scenes.lamp_floor_pixels(s)
-        rt = create_path_tracer(s, device=dev)
+        rt = create_path_tracer(s, device=dev, code=True)
         stream = torch.cuda.ExternalStream(rt.stream(), device=torch.device("cuda", dev))
         for _ in range(max(args.warmup, 3)):
             rt.invalidate()
@@ -500,7 +524,7 @@ def haze_leg(args, dev):
     for sig in (0.05, 0.2, 1.0):
         for g in (0.0, 0.7, 0.9):
             s = scenes.haze_beam(width=W, height=H, sigma_s=sig, g=g)
-            rt = create_path_tracer(s, device=dev)
+            rt = create_path_tracer(s, device=dev, code=True)
             stream = torch.cuda.ExternalStream(rt.stream(), device=torch.device("cuda", dev))
             rt.step(4)                                # the wave's buffers and graphs
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -539,7 +563,7 @@ def env_leg(args, dev):
     for off in (0, 1):
         s = scenes.env_floor(width=W, height=W)
         s.params.env_map_off = off
-        rt = create_path_tracer(s, device=dev)
+        rt = create_path_tracer(s, device=dev, code=True)
         rt.set_env_image(img)
         stream = torch.cuda.ExternalStream(rt.stream(), device=torch.device("cuda", dev))
         for _ in range(max(args.warmup, 3)):
@@ -564,38 +588,41 @@ def env_leg(args, dev):
 
 
 def sc_leg(args, dev):
-    """The step cache (the reference's developer setting, wavefront.js:67-150): the headline room at its full size and
-    samples with the cache off, on its own cell (1) and on three cells (2) with the reference's default 4 M cells, and
-    on its own cell with its largest 16 M -- paths a second (CUDA events around one render after a warm-up render) and
-    the scene-distance evaluations a path."""
+    """The scene's two forms and the step cache (the reference's developer setting, wavefront.js:67-150): the headline
+    room at its full size and samples as a primitive table (the scene as data, a loop over the table in shared memory)
+    and as code (codegen.py's CUDA, NVRTC), each with the cache off and on (one look, 16 M cells) -- paths a second
+    (CUDA events around one render after a warm-up render) and the scene-distance evaluations a path."""
     import torch
     from shadytracer_gb300.renderer import create_path_tracer
     s = workload(args.small, args.spp)
     spp = s.info["spp"]
     P = s.params.width * s.params.height
-    out = {"workload": "the headline room with the step cache over the bounded primitives' box",
+    out = {"workload": "the headline room as a table and as code, the step cache off and on",
            "metric": "Mpaths/s", "modes": {}}
-    for mode, cells in ((0, 4.0), (1, 4.0), (2, 4.0), (1, 16.0)):
-        s.params.step_cache = mode
-        s.params.step_cache_cells = cells
-        rt = create_path_tracer(s, device=dev)
-        stream = torch.cuda.ExternalStream(rt.stream(), device=torch.device("cuda", dev))
-        rt.step(spp)
-        c0 = rt.counters()["march_steps"]
-        rt.invalidate()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        rt.step_async(spp)
-        e1.record(stream)
-        rt.sync()
-        ms = e0.elapsed_time(e1)
-        evals = rt.counters()["march_steps"] - c0
-        out["modes"]["off" if mode == 0 else "%d_%gM" % (mode, cells)] = {
-            "ms": ms, "Mpaths_per_s": P * spp / (ms / 1e3) / 1e6, "evals_per_path": evals / (P * spp)}
-        rt.close()
+    for form in ("table", "code"):
+        for mode, cells in ((0, 4.0), (1, 16.0)):
+            s.params.step_cache = mode
+            s.params.step_cache_cells = cells
+            rt = create_path_tracer(s, device=dev, code=True if form == "code" else None)
+            stream = torch.cuda.ExternalStream(rt.stream(), device=torch.device("cuda", dev))
+            rt.step(spp)
+            c0 = rt.counters()["march_steps"]
+            rt.invalidate()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            rt.step_async(spp)
+            e1.record(stream)
+            rt.sync()
+            ms = e0.elapsed_time(e1)
+            evals = rt.counters()["march_steps"] - c0
+            out["modes"]["%s_%s" % (form, "cache_off" if mode == 0 else "cache_1look_16M")] = {
+                "ms": ms, "Mpaths_per_s": P * spp / (ms / 1e3) / 1e6, "evals_per_path": evals / (P * spp)}
+            rt.close()
     s.params.step_cache = 0
     s.params.step_cache_cells = 0.0
-    out["value"] = max(v["Mpaths_per_s"] for v in out["modes"].values())
+    m = out["modes"]
+    out["code_over_table"] = m["code_cache_off"]["Mpaths_per_s"] / m["table_cache_off"]["Mpaths_per_s"]
+    out["value"] = max(v["Mpaths_per_s"] for v in m.values())
     return out
 
 
@@ -619,7 +646,7 @@ def rmse_leg(args, dev):
                              photon_half=2.0, vfov=3.5)
         s.params.sppm_learn = learn
         cf = scenes.sppm_pane_closed_form(s, _o.fresnel_dielectric)
-        rt = create_path_tracer(s, device=dev)
+        rt = create_path_tracer(s, device=dev, code=True)
         stream = torch.cuda.ExternalStream(rt.stream(), device=torch.device("cuda", dev))
         rt.step(1)                                    # the graph captured
         rt.invalidate()
@@ -648,6 +675,79 @@ def rmse_leg(args, dev):
     return out
 
 
+# the march's DRAM traffic per scene evaluation, from one ncu capture of k_march on the 480 x 270 room at 4 samples
+# (dram__bytes_read.sum + dram__bytes_write.sum over the launch's evaluations), scaled by each launch's evaluations:
+# the path state a ray's refill and hand-off move, spread over its steps (the scene itself is code)
+MARCH_DRAM_BYTES_PER_EVAL = 7.4
+MARCH_DRAM_PROFILE = "profiles/k_march-room24-code-480x270.md"
+
+
+def caustic_rmse_leg(args, dev):
+    """Time to 1 % relative RMSE on the caustic as configured (1024^2, 4 M sun photons a pass, r1 5 mm, alpha 0.7):
+    plain (the sun's photons uniform over their square) against guided (drawn from the learned 128^2 emission map,
+    rebuilt every 4 passes), each against an FP64-accumulated render of 16 x 64 passes. The RMSE over the picture's
+    pixels of the luminance's difference, less the reference's own variance (its pixels' squared standard errors), over
+    the reference's mean; GPU time of the passes (CUDA events), checked every 8 passes up to 1024."""
+    import torch
+    from shadytracer_gb300 import scenes
+    from shadytracer_gb300.renderer import create_path_tracer
+    W = 256 if args.small else 1024
+    N = 250_000 if args.small else 4_000_000
+    ref_passes = 16 * (8 if args.small else 64)
+    cap = 256 if args.small else 1024
+    luma = np.array([0.2126, 0.7152, 0.0722])
+    mk = lambda: scenes.sppm_caustic(width=W, height=W, photons=N, r1=0.005, alpha=0.7)
+    rt = create_path_tracer(mk(), device=dev, code=True)
+    left = ref_passes
+    while left > 0:
+        rt.step(min(64, left))
+        left -= 64
+    rgb, V, S, cnt = rt.read_accum()
+    rt.close()
+    Lref = rgb @ luma
+    ok = (S > 0) & (S < 1)
+    se2 = np.zeros_like(V)
+    se2[ok] = S[ok] * V[ok] / (1 - S[ok])
+    # the sun's glints on the glass (camera paths that reach the disc, 1.6e9 cd/m^2) are a few pixels whose noise
+    # would be the whole RMSE: the metric is over the rest, the brightest 0.1 % of the reference's pixels left out
+    keep = Lref <= np.quantile(Lref, 0.999)
+    noise_ref = float(np.mean(se2[keep]))
+    mean_ref = float(Lref[keep].mean())
+    out = {"metric": "seconds to 1% relative RMSE vs an FP64 render at 16x the passes", "unit": "s",
+           "higher_is_better": False,
+           "workload": "sppm caustic %dx%d, %d sun photons a pass, r1 5 mm, alpha 0.7; reference %d passes (its own "
+                       "relative noise %.4f, taken out); the brightest 0.1 %% of pixels (the sun's glints) left out"
+                       % (W, W, N, ref_passes, np.sqrt(noise_ref) / mean_ref)}
+    for name, learn in (("plain", 0), ("guided", 1)):
+        s = mk()
+        s.params.sppm_learn = learn
+        rt = create_path_tracer(s, device=dev, code=True)
+        stream = torch.cuda.ExternalStream(rt.stream(), device=torch.device("cuda", dev))
+        rt.step(1)
+        rt.invalidate()
+        ms, passes, rm, hit, curve = 0.0, 0, None, None, []
+        while passes < cap:
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            rt.step_async(8)
+            e1.record(stream)
+            rt.sync()
+            ms += e0.elapsed_time(e1)
+            passes += 8
+            L = rt.read_accum()[0] @ luma
+            rm = float(np.sqrt(max(np.mean((L[keep] - Lref[keep]) ** 2) - noise_ref, 0.0)) / mean_ref)
+            if passes in (8, 64, 256, 1024) or rm <= 0.01:
+                curve.append([passes, round(ms / 1e3, 3), round(rm, 4)])
+            if rm <= 0.01:
+                hit = ms / 1e3
+                break
+        rt.close()
+        out[name] = {"seconds": hit, "passes": passes, "rmse": rm, "curve": curve, "ms_per_pass": ms / passes}
+    if out["plain"]["seconds"] and out["guided"]["seconds"]:
+        out["speedup"] = out["plain"]["seconds"] / out["guided"]["seconds"]
+    return out
+
+
 def run_ours(args):
     rank, world, local = dist_env()
     import torch
@@ -656,6 +756,7 @@ def run_ours(args):
     if args.leg != "all":
         with_cpu = rank == 0 and world == 1 and not args.no_cpu
         out = {"sppm": lambda: sppm_leg(args, dev, with_cpu), "rmse": lambda: rmse_leg(args, dev),
+               "caustic_rmse": lambda: caustic_rmse_leg(args, dev),
                "optics": lambda: optics_leg(args, dev, with_cpu), "mlp": lambda: mlp_leg(args, dev),
                "emit": lambda: emit_leg(args, dev), "haze": lambda: haze_leg(args, dev),
                "env": lambda: env_leg(args, dev), "sc": lambda: sc_leg(args, dev)}[args.leg]()
@@ -673,7 +774,9 @@ def run_ours(args):
     p = s.params
     P = p.width * p.height
     paths_per_step = P * spp
-    rt = create_path_tracer(s, device=dev)
+    src = scene_code(s)                     # the builder's step: the scene written as code, once
+    rt = create_path_tracer(s, device=dev, code=src)
+    compile_ms = rt.scene_code_info()["compile_ms"]
     stream = torch.cuda.ExternalStream(rt.stream(), device=torch.device("cuda", dev))
 
     def barrier():
@@ -718,7 +821,8 @@ def run_ours(args):
     barrier()
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        rt.set_scene(s)                     # scene table + materials, host -> device
+        rt.set_scene(s, code=src)           # the scene's code (its compiled library, from the process's cache) and
+                                            # its materials and table, host -> device
         rt.set_params(p)                    # the settings (resets the accumulation)
         rt.set_view(s.view)
         rt.step(spp)
@@ -727,7 +831,8 @@ def run_ours(args):
     barrier()
     e2e_s = (time.perf_counter() - t0) / args.steps
     e2e_s = reduce_max(e2e_s, dist, "cuda")
-    h2d = (C.sizeof(type(s.prims)) + C.sizeof(type(s.materials)) + C.sizeof(p) + C.sizeof(s.view))
+    h2d = (C.sizeof(type(s.prims)) + C.sizeof(type(s.materials)) + C.sizeof(p) + C.sizeof(s.view) +
+           len(src.encode()))
     d2h = P * (32 + 16)
     Lmean = float((rgb @ np.array([0.2126, 0.7152, 0.0722])).mean())
 
@@ -777,13 +882,19 @@ def run_ours(args):
             "e2e": {"value": world * paths_per_step / e2e_s / 1e6, "unit": "Mpaths/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
             "gpu_launches": launches,
+            "scene_compile_ms": compile_ms,
             "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                         "frac": achieved / peak if peak else None, "traffic": None,
+                         "frac": achieved / peak if peak else None,
+                         "traffic": MARCH_DRAM_BYTES_PER_EVAL * evals / max(m_launches, 1),
+                         "traffic_unit": "bytes of DRAM read + written per launch: ncu's dram__bytes per scene "
+                                         "evaluation on the 480x270 case (%s) times this launch's evaluations" %
+                                         MARCH_DRAM_PROFILE,
                          "kernel": "k_march", "flops_per_launch": per_launch_flops,
                          "flops_per_eval": f_render / max(dw["march_steps"], 1),
                          "flops_per_eval_whole_table": f_table,
                          "sfu_per_eval": sfu_render / max(dw["march_steps"], 1),
                          "evals_per_launch": evals / max(m_launches, 1),
+                         "evals_per_render": evals / max(args.steps, 1),
                          "prims_evaluated_per_eval": sum(dw["prim_evals"]) / max(dw["march_steps"], 1),
                          "fold_simd_efficiency": simd,
                          "evals_by_type": {flops.TYPE_NAMES.get(t, str(t)): {
@@ -808,7 +919,7 @@ def run_ours(args):
         line["cpu_baseline"] = None
     if not args.no_sppm:
         line["sppm"] = sppm_leg(args, dev, rank == 0 and world == 1 and not args.no_cpu)
-        line["time_to_rmse"] = rmse_leg(args, dev)
+        line["time_to_rmse"] = {"caustic": caustic_rmse_leg(args, dev), "pane": rmse_leg(args, dev)}
     if not args.no_mlp:
         line["mlp"] = mlp_leg(args, dev)
     if not args.no_emit:

@@ -422,7 +422,18 @@ typedef struct st_optics_totals {
     double   escaped, lost, detected, absorbed;   /* weight                                         */
     uint64_t interactions;
     uint64_t rays;
+    uint64_t n_escaped, n_lost, n_detected, n_absorbed;   /* rays (optics/kernels.js O_COUNT)     */
 } st_optics_totals;
+
+/* WHAT A RUN KEEPS BEYOND ITS TALLIES (optics/kernels.js:174-251): the detector hits (optRecordHit) up to det_cap, and
+ * the paths of each instance's first path_rays rays (optVertex) up to path_verts vertices each, an escaped ray's last
+ * esc_len (metres) past its last interaction. All 0: nothing kept (the default). */
+typedef struct st_optics_detail {
+    uint32_t det_cap;             /* detector hits kept a run (at most 2^24)                        */
+    uint32_t path_rays;           /* rays an instance whose paths are kept (at most 4096)          */
+    uint32_t path_verts;          /* vertices a kept path (at most 256)                            */
+    float    esc_len;             /* metres (0: 0.1)                                                */
+} st_optics_detail;
 
 int  st_optics_set_sources(st_ctx* ctx, const st_optics_source* src, uint32_t n);
 int  st_optics_set_far(st_ctx* ctx, const st_optics_far* far);
@@ -434,6 +445,18 @@ int  st_optics_set_rays(st_ctx* ctx, const float* rays, uint32_t n);
  * FP64 tallies in ray weight (the host multiplies by flux / rays); totals per instance. */
 int  st_optics_run(st_ctx* ctx, const st_optics_batch* batch, double* far, double* lux,
                    st_optics_totals* totals);
+int  st_optics_set_detail(st_ctx* ctx, const st_optics_detail* detail);
+/* THE LAST RUN'S TALLIES BY OBJECT AND BY MATERIAL (optics/kernels.js:651-681, O_TAG and O_MAT): per tag -- an item
+ * of the table, by its first primitive's index, 256 of them -- and per (instance, material) the weight incident, the
+ * weight leaving and the interactions, 3 doubles each; tags 256 x 3, mats n_instances x n_materials x 3 (NULL skips) */
+int  st_optics_tallies(st_ctx* ctx, double* tags, double* mats);
+/* THE LAST RUN'S DETECTOR HITS: n_out the hits that reached a detector (past det_cap only the first det_cap kept), up
+ * to max_n of them into hits, 12 floats each: position (metres), weight, direction, tag (the item's first primitive),
+ * instance, CIE X and Z of its colour (Y the weight), 0 */
+int  st_optics_hits(st_ctx* ctx, float* hits, uint32_t max_n, uint32_t* n_out);
+/* THE LAST RUN'S KEPT PATHS: counts (n_instances x path_rays) their vertices, verts (n_instances x path_rays x
+ * path_verts x 8 floats) each vertex's position, weight, optical length and hue rgb (the ray's colour at luminance 1) */
+int  st_optics_paths(st_ctx* ctx, float* verts, uint32_t* counts);
 
 /* ---- the learned proposal (st_params.guide) ----
  * The parameters, FP32, in one array of ST_MLP_PARAMS: W1 (64 x 48), W2 (64 x 64), W3 (64 x 64), W4 (40 x 64), each
@@ -495,7 +518,7 @@ int  st_render_noalloc(int device, const st_scene_desc* desc, const st_params* p
 /* ---- the binding's checks ---- */
 /* The sizes of the structs above as this library was built (st_prim, st_material, st_scene_desc, st_params,
  * st_view, st_counters_t, st_image_stats_t, st_kernel_time, st_sppm_stats, st_optics_source, st_optics_far,
- * st_optics_batch, st_optics_totals, st_mlp_stats, st_light, in that order); returns how many it has. */
+ * st_optics_batch, st_optics_totals, st_mlp_stats, st_light, st_optics_detail, in that order); returns how many it has. */
 int  st_struct_sizes(uint32_t* out, int max);
 /* The context's CUDA stream (a cudaStream_t), for a host that orders or times its own work against it. */
 void* st_stream(st_ctx* ctx);

@@ -244,6 +244,7 @@ def _declare_extra(L):
         "sto_guide_mix_sample": ([P, P, C.c_uint32, P], None),
         "sto_bf16": ([C.c_float], C.c_float),
         "sto_lt_build": ([P, P, P], None),
+        "sto_optics_detail": ([C.c_uint32, P, P, P, P, C.c_uint32, C.POINTER(C.c_uint32)], C.c_int),
         "sto_last_lt": ([P, P, P], C.c_int),
     }
     for name, (args, res) in sig.items():
@@ -461,7 +462,24 @@ def optics_run(bench, ray_counts, nC=360, nG=181, cells=0, half=1.0, height=1.0,
                           nC, nG, cells, half, height, maxbounce, seed, 1 if fp64 else 0, ptr(far), ptr(lux), ptr(tot),
                           threads)
     keys = ["emitted", "escaped", "lost", "detected", "absorbed", "interactions"]
-    return {"far": far, "lux": lux, "totals": [dict(zip(keys, t.tolist())) for t in tot], "scenes": per}
+    out = {"far": far, "lux": lux, "totals": [dict(zip(keys, t.tolist())) for t in tot], "scenes": per, "detail": []}
+    # per instance: the tallies by its own primitives' items (tag = the item's first primitive in the instance) and
+    # by material (incident, leaving, interactions), the ray counts, the detector hits
+    for i in range(n):
+        npr, nm = per[i].desc.n_prims, per[i].desc.n_materials
+        tag = np.zeros((npr, 3))
+        mat = np.zeros((nm, 3))
+        cnt = np.zeros(4, np.uint64)
+        nh = C.c_uint32()
+        if xlib().sto_optics_detail(i, ptr(tag), ptr(mat), ptr(cnt), None, 0, C.byref(nh)) != 0:
+            out["detail"].append(None)
+            continue
+        hits = np.zeros((nh.value, 12), np.float32)
+        xlib().sto_optics_detail(i, None, None, None, ptr(hits), nh.value, C.byref(nh))
+        out["detail"].append({"tag": tag, "mat": mat, "hits": hits,
+                              "counts": dict(zip(["n_escaped", "n_lost", "n_detected", "n_absorbed"],
+                                                 [int(c) for c in cnt]))})
+    return out
 
 
 # ---- the learned proposal (st_oracle_guide.h) ----

@@ -23,6 +23,7 @@
 #include <omp.h>
 #endif
 #include <atomic>
+#include <map>
 
 using namespace sto;
 
@@ -919,6 +920,12 @@ struct OptTally {
     double escaped = 0, lost = 0, detected = 0, absorbed = 0, emitted = 0;
     uint64_t interactions = 0;
     std::vector<double> far, lux;
+    // by object (the item's first primitive) and by material: weight incident, leaving, interactions
+    // (kernels.js:651-681 O_TAG / O_MAT); the rays escaped, lost, detected, absorbed (O_COUNT); the detector hits
+    // (optRecordHit: position, weight, direction, tag)
+    std::vector<double> tag, mat;
+    uint64_t n_escaped = 0, n_lost = 0, n_detected = 0, n_absorbed = 0;
+    std::vector<float> hits;
 };
 struct OptFrame {
     float axis[3], c0[3], c90[3], origin[3];
@@ -947,6 +954,7 @@ void optics_ray(const Ctx<T>& C, U4 bseed, uint32_t id, const st_optics_source* 
         T wIn = luma(r.beta * r.rad);
         if (r.state == RAY_ESCAPED) {                                             // kernels.js:609-625
             tl.escaped += (double)wIn;
+            tl.n_escaped++;
             float d[3] = {(float)r.dir.x, (float)r.dir.y, (float)r.dir.z};
             tl.far[far_bin(d, F.axis, F.c0, F.nC, F.nG)] += (double)wIn;
             // the lux plane: the escaping ray's line met at `height` along the axis (it crosses nothing more)
@@ -967,15 +975,22 @@ void optics_ray(const Ctx<T>& C, U4 bseed, uint32_t id, const st_optics_source* 
             }
             return;
         }
-        if (r.state != RAY_ACTIVE) { tl.lost += (double)wIn; return; }           // out of steps or length
+        if (r.state != RAY_ACTIVE) { tl.lost += (double)wIn; tl.n_lost++; return; }   // out of steps or length
         SceneHit<T> h = scene_eval(*C.s, r.pos);
-        const st_material& m = C.s->materials[std::min(h.m, C.s->n_materials - 1)];
+        const uint32_t mi = std::min(h.m, C.s->n_materials - 1);
+        const st_material& m = C.s->materials[mi];
         V3<T> nn = hit_normal(C, r.pos, dh);
         bool inside = dh < T(0);
         V3<T> nrm = inside ? -nn : nn;
         if (m.detector > 0.5f && dot(-r.dir, nrm) >= T(0)) {                      // kernels.js:660-672
             tl.detected += (double)wIn;
+            tl.n_detected++;
             tl.interactions++;
+            tl.tag[3 * h.item] += (double)wIn; tl.tag[3 * h.item + 2] += 1;
+            tl.mat[3 * mi] += (double)wIn; tl.mat[3 * mi + 2] += 1;
+            const float hit[12] = {(float)r.pos.x, (float)r.pos.y, (float)r.pos.z, (float)wIn, (float)r.dir.x,
+                                   (float)r.dir.y, (float)r.dir.z, (float)h.item, 0.f, 0.f, 0.f, 0.f};
+            tl.hits.insert(tl.hits.end(), hit, hit + 12);
             return;
         }
         uint32_t b0 = r.bounces;
@@ -984,13 +999,17 @@ void optics_ray(const Ctx<T>& C, U4 bseed, uint32_t id, const st_optics_source* 
         if (r.bounces == b0) {                                                   // declined: not an interaction
             if (r.state == RAY_ACTIVE) continue;
             tl.lost += (double)wIn;
+            tl.n_lost++;
             return;
         }
         tl.interactions++;
         bool goesOn = r.state == RAY_ACTIVE || r.state == RAY_TERMINATED;
         T wOut = goesOn ? luma(r.beta * r.rad) : T(0);
         tl.absorbed += (double)(wIn - wOut);
-        if (r.state == RAY_TERMINATED) { tl.lost += (double)wOut; return; }       // the bounce cap
+        if (!goesOn) tl.n_absorbed++;
+        tl.tag[3 * h.item] += (double)wIn; tl.tag[3 * h.item + 1] += (double)wOut; tl.tag[3 * h.item + 2] += 1;
+        tl.mat[3 * mi] += (double)wIn; tl.mat[3 * mi + 1] += (double)wOut; tl.mat[3 * mi + 2] += 1;
+        if (r.state == RAY_TERMINATED) { tl.lost += (double)wOut; tl.n_lost++; return; }   // the bounce cap
         if (r.state != RAY_ACTIVE) return;
         (void)maxbounce;
     }
@@ -1450,6 +1469,26 @@ void sto_lobes_sample(const st_material* m, const double* v, double eta, uint32_
     }
 }
 
+// the last optics run's tallies by object and material, counts and detector hits, per instance (for the tests)
+struct OptDetail { std::vector<double> tag, mat; uint64_t counts[4] = {0, 0, 0, 0}; std::vector<float> hits; };
+static std::map<uint32_t, OptDetail>& opt_detail() {
+    static std::map<uint32_t, OptDetail> d;
+    return d;
+}
+int sto_optics_detail(uint32_t inst, double* tag, double* mat, uint64_t* counts, float* hits, uint32_t max_hits,
+                      uint32_t* n_hits) {
+    auto it = opt_detail().find(inst);
+    if (it == opt_detail().end()) return -1;
+    const OptDetail& d = it->second;
+    if (tag) std::copy(d.tag.begin(), d.tag.end(), tag);
+    if (mat) std::copy(d.mat.begin(), d.mat.end(), mat);
+    if (counts) for (int k = 0; k < 4; k++) counts[k] = d.counts[k];
+    const uint32_t n = (uint32_t)(d.hits.size() / 12);
+    if (n_hits) *n_hits = n;
+    if (hits) std::copy(d.hits.begin(), d.hits.begin() + (size_t)std::min(n, max_hits) * 12, hits);
+    return 0;
+}
+
 // Trace an optics batch (config: the scene, its settings for the march; sources with their instance; per instance its
 // ray count, far-field frame, lux plane). Tallies per instance into far (n_inst * nG * nC), lux (n_inst * cells^2),
 // totals (n_inst * 6: emitted, escaped, lost, detected, absorbed, interactions).
@@ -1465,6 +1504,7 @@ int sto_optics_run(const st_scene_desc* const* scenes, const st_params* p, const
 #ifdef _OPENMP
     if (threads > 0) omp_set_num_threads(threads);
 #endif
+    opt_detail().clear();
     for (uint32_t inst = 0; inst < n_inst; inst++) {
         std::vector<st_optics_source> mine;
         for (uint32_t i = 0; i < nsrc; i++) if (src[i].instance == inst) mine.push_back(src[i]);
@@ -1501,7 +1541,11 @@ int sto_optics_run(const st_scene_desc* const* scenes, const st_params* p, const
             nt = omp_get_max_threads();
 #endif
             std::vector<OptTally> tls(nt);
-            for (auto& t : tls) { t.far.assign((size_t)nC * nG, 0.0); t.lux.assign((size_t)cells * cells, 0.0); }
+            for (auto& t : tls) {
+                t.far.assign((size_t)nC * nG, 0.0); t.lux.assign((size_t)cells * cells, 0.0);
+                t.tag.assign((size_t)scenes[inst]->n_prims * 3, 0.0);
+                t.mat.assign((size_t)scenes[inst]->n_materials * 3, 0.0);
+            }
 #pragma omp parallel for schedule(dynamic, 256)
             for (long id = 0; id < (long)ray_count[inst]; id++) {
                 int tid = 0;
@@ -1513,11 +1557,20 @@ int sto_optics_run(const st_scene_desc* const* scenes, const st_params* p, const
             double* fo = far + (size_t)inst * nC * nG;
             double* lo = lux + (size_t)inst * cells * cells;
             double* to = totals + (size_t)inst * 6;
+            OptDetail& dt = opt_detail()[inst];
+            dt = OptDetail{};
+            dt.tag.assign((size_t)scenes[inst]->n_prims * 3, 0.0);
+            dt.mat.assign((size_t)scenes[inst]->n_materials * 3, 0.0);
             for (auto& t : tls) {
                 for (size_t i = 0; i < t.far.size(); i++) fo[i] += t.far[i];
                 for (size_t i = 0; i < t.lux.size(); i++) lo[i] += t.lux[i];
                 to[0] += t.emitted; to[1] += t.escaped; to[2] += t.lost; to[3] += t.detected; to[4] += t.absorbed;
                 to[5] += (double)t.interactions;
+                for (size_t i = 0; i < t.tag.size(); i++) dt.tag[i] += t.tag[i];
+                for (size_t i = 0; i < t.mat.size(); i++) dt.mat[i] += t.mat[i];
+                dt.counts[0] += t.n_escaped; dt.counts[1] += t.n_lost; dt.counts[2] += t.n_detected;
+                dt.counts[3] += t.n_absorbed;
+                dt.hits.insert(dt.hits.end(), t.hits.begin(), t.hits.end());
             }
         };
         if (fp64) run(0.0); else run(0.0f);

@@ -208,9 +208,10 @@ template <class T> inline T smooth_union(T d1, T d2, T k) {
 
 // THE FOLD (core/scene_api.js:28-80 add_new / fold; emptyHit :93): the surface is the item of least |d|, the
 // medium the item the point is least deep inside (material 0 -- the air -- when none).
-template <class T> struct SceneHit { T d; uint32_t m; uint32_t a; T insideW; };
+template <class T> struct SceneHit { T d; uint32_t m; uint32_t a; T insideW; uint32_t item; };
+// item: the first primitive of the item the surface answered from (the object, the optics tallies' tag)
 template <class T> inline SceneHit<T> scene_eval(const st_scene_desc& s, const V3<T>& p) {
-    SceneHit<T> H{T(1e7), 0u, 0u, T(-1e7)};
+    SceneHit<T> H{T(1e7), 0u, 0u, T(-1e7), 0u};
     uint32_t i = 0;
     while (i < s.n_prims) {
         const st_prim& pi = s.prims[i];
@@ -228,7 +229,7 @@ template <class T> inline SceneHit<T> scene_eval(const st_scene_desc& s, const V
             j++;
         }
         if (di < T(0) && di > H.insideW) { H.insideW = di; H.a = mat; }
-        if (std::fabs(di) < std::fabs(H.d)) { H.d = di; H.m = mat; }
+        if (std::fabs(di) < std::fabs(H.d)) { H.d = di; H.m = mat; H.item = i; }
         i = j;
     }
     return H;

@@ -47,6 +47,10 @@ SIGNATURES = {
     "st_optics_set_sources": ([P, C.POINTER(T.StOpticsSource), C.c_uint32], C.c_int),
     "st_optics_set_far": ([P, C.POINTER(T.StOpticsFar)], C.c_int),
     "st_optics_run": ([P, C.POINTER(T.StOpticsBatch), P, P, C.POINTER(T.StOpticsTotals)], C.c_int),
+    "st_optics_set_detail": ([P, C.POINTER(T.StOpticsDetail)], C.c_int),
+    "st_optics_tallies": ([P, P, P], C.c_int),
+    "st_optics_hits": ([P, P, C.c_uint32, C.POINTER(C.c_uint32)], C.c_int),
+    "st_optics_paths": ([P, P, P], C.c_int),
     "st_render_noalloc": ([C.c_int, C.POINTER(T.StSceneDesc), C.POINTER(T.StParams), C.POINTER(T.StView), C.c_int,
                            P, P, P, P], C.c_int),
     "st_eval_sdf": ([P, P, C.c_uint32, P], C.c_int),
@@ -64,7 +68,7 @@ SIGNATURES = {
 
 STRUCT_ORDER = [T.StPrim, T.StMaterial, T.StSceneDesc, T.StParams, T.StView, T.StCounters, T.StImageStats,
                 T.StKernelTime, T.StSppmStats, T.StOpticsSource, T.StOpticsFar, T.StOpticsBatch, T.StOpticsTotals,
-                T.StMlpStats, T.StLight]
+                T.StMlpStats, T.StLight, T.StOpticsDetail]
 
 
 def load(path=None):

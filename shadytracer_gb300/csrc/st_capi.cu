@@ -1161,7 +1161,7 @@ int st_struct_sizes(uint32_t* out, int max) {
                           (uint32_t)sizeof(st_sppm_stats), (uint32_t)sizeof(st_optics_source),
                           (uint32_t)sizeof(st_optics_far), (uint32_t)sizeof(st_optics_batch),
                           (uint32_t)sizeof(st_optics_totals), (uint32_t)sizeof(st_mlp_stats),
-                          (uint32_t)sizeof(st_light)};
+                          (uint32_t)sizeof(st_light), (uint32_t)sizeof(st_optics_detail)};
     int n = (int)(sizeof(s) / sizeof(s[0]));
     for (int i = 0; i < n && i < max; i++) out[i] = s[i];
     return n;
@@ -1193,4 +1193,5 @@ uint32_t ctx_n_prims(st_ctx* ctx) { return (uint32_t)ctx->prims.size(); }
 uint32_t ctx_n_mats(st_ctx* ctx) { return (uint32_t)ctx->mats.size(); }
 const st_scene_desc& ctx_desc(st_ctx* ctx) { return ctx->desc; }
 bool ctx_has_scene(st_ctx* ctx) { return ctx->has_scene; }
+uint64_t ctx_scene_gen(st_ctx* ctx) { return ctx->scene_gen; }
 MfTab ctx_tab(st_ctx* ctx) { return MfTab{ctx->d_ec, ctx->d_ecavg, ctx->d_e1}; }

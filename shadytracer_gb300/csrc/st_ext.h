@@ -51,6 +51,9 @@ struct OpticsState {
     uint32_t n_rays = 0;
     st_optics_far far{};
     bool has_far = false;
+    st_optics_detail detail{};   // what a run keeps beyond its tallies (hits, paths)
+    uint64_t sources_gen = 0;    // the sources' and the ray table's changes (a batch's graph is recorded with them)
+    uint64_t launches = 0;       // kernels the batches' graphs ran
     void* scratch = nullptr;     // the run's device buffers (st_optics.cu OptBuf), grown as needed
 };
 
@@ -120,4 +123,5 @@ uint32_t ctx_n_prims(st_ctx* ctx);
 uint32_t ctx_n_mats(st_ctx* ctx);
 const st_scene_desc& ctx_desc(st_ctx* ctx);
 bool ctx_has_scene(st_ctx* ctx);
+uint64_t ctx_scene_gen(st_ctx* ctx);     // a count of the scenes set (a graph recorded with one is stale after)
 st::MfTab ctx_tab(st_ctx* ctx);

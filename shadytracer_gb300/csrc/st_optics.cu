@@ -15,6 +15,7 @@
 // on a plane at a set height along the axis (global FP64 atomics, spread over their bins).
 #include <algorithm>
 #include <cmath>
+#include <cstring>
 #include <string>
 #include <vector>
 
@@ -24,8 +25,27 @@
 using namespace st;
 
 #define OPT_MAX_INST 256u
-#define OPT_TOT 8u          // per instance: emitted, escaped, lost, detected, absorbed, interactions, rays, unused
+// per instance, in fixed point (OPT_FX a unit of weight) or counts: the weight emitted (a ray set's), escaped, lost,
+// detected, absorbed; the interactions; the rays escaped, lost, detected and absorbed
+#define OPT_TOT 16u
+#define T_EMIT 0u
+#define T_ESC 1u
+#define T_LOST 2u
+#define T_DET 3u
+#define T_ABS 4u
+#define T_INTER 5u
+#define T_NESC 6u
+#define T_NLOST 7u
+#define T_NDET 8u
+#define T_NABS 9u
 #define OPT_WAVE (4u << 20)
+// THE TALLIES IN FIXED POINT (the reference's optAdd, kernels.js:174-179, keeps u64 in lo/hi words at 2^20 a unit):
+// signed 64-bit integers at 2^24 a unit of weight, so every sum is exact and the same whatever order the atomics ran
+// in; FP64 only where the sums are read out (k_opt_flush)
+#define OPT_FX 16777216.0
+#define OPT_TAG_MAX 256u    // the tags: an item of the table, by its first primitive's index
+#define DET_F4 3u           // a detector hit: position | weight, direction | tag, colour X | Z | 0 | 0
+#define VERT_F4 2u          // a path vertex: position | weight, optical length | hue rgb
 
 namespace {
 
@@ -45,10 +65,98 @@ struct OptArgs {
     f3 axis, c0, c90;
     uint32_t nC, nG, cells;
     float half, height;
-    double* far;                    // n_inst * nG * nC
-    double* lux;                    // n_inst * cells * cells
-    double* tot;                    // n_inst * OPT_TOT
+    unsigned long long* far;        // n_inst * nG * nC, fixed point
+    unsigned long long* lux;        // n_inst * cells * cells, fixed point
+    unsigned long long* tot;        // n_inst * OPT_TOT
+    unsigned long long* tag;        // OPT_TAG_MAX * 3: incident, leaving (fixed point), interactions
+    unsigned long long* mat;        // n_inst * n_mats * 3: the same by material
+    // the detector hits recorded (optRecordHit, kernels.js:237-251) and the paths kept (optVertex, :193-206)
+    float4* det;                    // det_cap * DET_F4
+    uint32_t* det_n;                // hits reached (may pass det_cap: the rest were not kept)
+    uint32_t det_cap;
+    float4* verts;                  // n_inst * path_rays * path_verts * VERT_F4
+    uint32_t* vcount;               // n_inst * path_rays
+    uint32_t path_rays, path_verts;
+    float esc_len;                  // an escaped ray's last vertex, this far past its last interaction
 };
+
+__device__ __forceinline__ long long fx(float w) { return __double2ll_rn((double)w * OPT_FX); }
+
+// THE WARP'S TALLY: for every key the warp's lanes hold, the sums of their NV values over the lanes holding it, added
+// to base[key * stride + j] by one lane -- a few shuffles and one atomic a key instead of one a lane. Every lane of
+// the warp calls it; a lane with nothing to add passes has = false.
+template <int NV>
+__device__ __forceinline__ void warp_tally(bool has, uint32_t key, const long long (&v)[NV], unsigned long long* base,
+                                           uint32_t stride) {
+    uint32_t pending = __ballot_sync(FULL_MASK, has);
+    const uint32_t lane = threadIdx.x & 31u;
+    while (pending) {
+        const uint32_t leader = __ffs(pending) - 1;
+        const uint32_t k = __shfl_sync(FULL_MASK, key, leader);
+        const bool mine = has && key == k;
+#pragma unroll
+        for (int j = 0; j < NV; j++) {
+            long long x = mine ? v[j] : 0ll;
+            for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(FULL_MASK, x, o);
+            if (lane == leader && x != 0ll) atomicAdd(&base[(size_t)k * stride + j], (unsigned long long)x);
+        }
+        pending &= ~__ballot_sync(FULL_MASK, mine);
+    }
+}
+
+// scene_full with the item it answered from: the first primitive of the item whose surface is nearest (the tag the
+// reference's capture pass finds, scene_api.js tagCaptureBegin/End)
+__device__ __forceinline__ SceneHit scene_full_item(const DPrim* __restrict__ pr, uint32_t n, f3 p, uint32_t& item) {
+    SceneHit H{1e7f, 0u, 0u};
+    float insideW = -1e7f;
+    item = 0;
+    uint32_t i = 0;
+    while (i < n) {
+        float di = prim_sdf(pr[i], p);
+        uint32_t mat = pr[i].h.z;
+        float nearv = fabsf(di);
+        uint32_t j = i + 1;
+        while (j < n) {
+            const uint32_t op = pr[j].h.y;
+            if (op == ST_OP_ITEM) break;
+            if (op == ST_OP_SMOOTH) {
+                float k = pr[j].r0.w;
+                if (!beyond(pr[j], p, fmaxf(di + fmaxf(k, 0.f) * CULL_REL, nearv) + CULL_ABS)) {
+                    float dj = prim_sdf(pr[j], p);
+                    di = smooth_union(di, dj, k);
+                    if (fabsf(dj) < nearv) { nearv = fabsf(dj); mat = pr[j].h.z; }
+                }
+            } else if (op == ST_OP_UNION) {
+                if (!beyond(pr[j], p, fmaxf(di, nearv) + CULL_ABS)) {
+                    float dj = prim_sdf(pr[j], p);
+                    di = fminf(di, dj);
+                    if (fabsf(dj) < nearv) { nearv = fabsf(dj); mat = pr[j].h.z; }
+                }
+            } else {
+                if (!beyond(pr[j], p, -di + CULL_ABS)) di = fmaxf(di, -prim_sdf(pr[j], p));
+            }
+            j++;
+        }
+        if (di < 0.f && di > insideW) { insideW = di; H.a = mat; }
+        if (fabsf(di) < fabsf(H.d)) { H.d = di; H.m = mat; item = i; }
+        i = j;
+    }
+    return H;
+}
+
+// a kept path's next vertex (the reference's optVertex): one thread holds a ray at a time, so no atomics
+__device__ __forceinline__ void opt_vertex(const OptArgs& o, uint32_t inst, uint32_t id, f3 p, float w, float opl, f3 c) {
+    if (id >= o.path_rays) return;
+    const size_t r = (size_t)inst * o.path_rays + id;
+    const uint32_t k = o.vcount[r];
+    if (k >= o.path_verts) return;
+    const float y = luma(c);
+    const f3 hue = y > 0.f ? c / y : mk(1.f);
+    float4* v = o.verts + (r * o.path_verts + k) * VERT_F4;
+    v[0] = f4(p, w);
+    v[1] = make_float4(opl, hue.x, hue.y, hue.z);
+    o.vcount[r] = k + 1u;
+}
 
 // the far field's bin (kernels.js:251-272 optFarAdd), in f32 as the kernel bins it
 __device__ __forceinline__ uint32_t far_bin(const OptArgs& o, f3 d) {
@@ -136,7 +244,11 @@ __global__ void __launch_bounds__(256) k_opt_gen(OptArgs o) {
         a.pb.pos[i] = make_float4(org.x, org.y, org.z, 0.f);
         a.pb.dir[i] = make_float4(dir.x, dir.y, dir.z, en);
         a.pb.beta[i] = make_float4(w, w, w, 1.f);                       // a ray set's ray carries its weight
-        if (o.has_sets) atomicAdd(&o.tot[(size_t)inst * OPT_TOT + 7], (double)w);
+        if (o.has_sets) atomicAdd(&o.tot[(size_t)inst * OPT_TOT + T_EMIT], (unsigned long long)fx(w));
+        if (id < o.path_rays) {                                         // a kept path starts where the ray leaves
+            o.vcount[(size_t)inst * o.path_rays + id] = 0u;
+            opt_vertex(o, inst, id, org, w, 0.f, mk(w));
+        }
         a.pb.rad[i] = make_float4(1.f, 1.f, 1.f, 0.f);          // a photon's radiance field is its flux: weight 1
         a.pb.meta[i] = make_uint4(id, meta_y(0, 0, RAY_ACTIVE), 0u, inst);
         a.q.ray[0][i] = i;
@@ -144,7 +256,9 @@ __global__ void __launch_bounds__(256) k_opt_gen(OptArgs o) {
 }
 
 // THE SHADE (kernels.js:571-699): escaped, lost, a detector's, or an interaction -- pathBegin..pathEnd with a
-// photon's rules: no light sampling, no end at a scatter, the bounce cap -- each tallied in FP64
+// photon's rules: no light sampling, no end at a scatter, the bounce cap. Each lane works out what its ray adds to the
+// tallies; then the warp adds them, the instance's totals into the CTA's shared sums (flushed once at its end), the
+// object's and the material's incident / leaving / interactions into global sums, one atomic a key a warp.
 __global__ void __launch_bounds__(256) k_opt_shade(OptArgs o, int nxt, int last) {
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ __align__(8) uint64_t mbar;
@@ -153,8 +267,9 @@ __global__ void __launch_bounds__(256) k_opt_shade(OptArgs o, int nxt, int last)
     const Uni& u = a.u;
     DPrim* sp = reinterpret_cast<DPrim*>(smem);
     st_material* sm = reinterpret_cast<st_material*>(smem + u.n_prims * sizeof(DPrim));
-    double* stot = reinterpret_cast<double*>(smem + u.n_prims * sizeof(DPrim) + u.n_mats * sizeof(st_material));
-    for (uint32_t i = threadIdx.x; i < o.n_inst * OPT_TOT; i += blockDim.x) stot[i] = 0.0;
+    unsigned long long* stot =
+        reinterpret_cast<unsigned long long*>(smem + u.n_prims * sizeof(DPrim) + u.n_mats * sizeof(st_material));
+    for (uint32_t i = threadIdx.x; i < o.n_inst * OPT_TOT; i += blockDim.x) stot[i] = 0ull;
     if (!stage_table(sp, a.prims, u.n_prims * (uint32_t)sizeof(DPrim), &mbar, a.ctr)) return;
     if (!stage_table(sm, a.mats, u.n_mats * (uint32_t)sizeof(st_material), &mbar2, a.ctr)) return;
     const uint32_t count = a.ctr->hitCount;
@@ -165,23 +280,36 @@ __global__ void __launch_bounds__(256) k_opt_shade(OptArgs o, int nxt, int last)
     for (uint32_t r = 0; r < nrounds; r++) {
         uint32_t q = r * stride + blockIdx.x * blockDim.x + threadIdx.x;
         bool cont = false;
-        uint32_t slot = 0;
+        uint32_t slot = 0, inst = 0, tag = 0, mati = 0;
         f3 pos, dir, beta;
         float ltot = 0.f, n = 1.f;
         uint4 m4 = make_uint4(0, 0, 0, 0);
+        // this ray's part of the tallies
+        long long tv[OPT_TOT - 6] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};   // T_EMIT .. T_NABS
+        long long iv[3] = {0, 0, 0};                                 // incident, leaving, interactions (its object, material)
+        bool interacted = false;
         if (q < count) {
             slot = a.q.hit[q];
             const float dh = a.q.hitd[q];
             float4 p4 = a.pb.pos[slot], d4 = a.pb.dir[slot], b4 = a.pb.beta[slot];
             m4 = a.pb.meta[slot];
             pos = xyz(p4); ltot = p4.w; dir = xyz(d4); n = d4.w; beta = xyz(b4);
-            const uint32_t inst = m4.w, id = m4.x;
+            inst = m4.w;
+            const uint32_t id = m4.x;
             uint32_t bounces = m4.y & 0xffu, state = (m4.y >> 16) & 0xffu;
-            double* T = stot + inst * OPT_TOT;
             const float wIn = luma(beta);                             // optWeight: beta x radiance (1), as luminance
             if (state == RAY_ESCAPED) {                               // kernels.js:609-625
-                atomicAdd(&T[1], (double)wIn);
-                atomicAdd(&o.far[(size_t)inst * o.nG * o.nC + far_bin(o, dir)], (double)wIn);
+                tv[T_ESC] = fx(wIn);
+                tv[T_NESC] = 1;
+                atomicAdd(&o.far[(size_t)inst * o.nG * o.nC + far_bin(o, dir)], (unsigned long long)fx(wIn));
+                if (id < o.path_rays) {                               // drawn esc_len past its last vertex
+                    const size_t pr = (size_t)inst * o.path_rays + id;
+                    const uint32_t k = o.vcount[pr];
+                    if (k > 0u && k <= o.path_verts) {
+                        const float4* lv = o.verts + (pr * o.path_verts + (k - 1u)) * VERT_F4;
+                        opt_vertex(o, inst, id, xyz(lv[0]) + dir * o.esc_len, wIn, lv[1].x + o.esc_len * n, beta);
+                    }
+                }
                 // the lux plane: the escaping ray's line at `height` along the axis (nothing lies beyond the scene)
                 float dn = dot(dir, o.axis);
                 if (o.cells && dn > 0.f) {
@@ -194,11 +322,14 @@ __global__ void __launch_bounds__(256) k_opt_shade(OptArgs o, int nxt, int last)
                     if (t >= 0.f && fabsf(ha) < o.half && fabsf(hb) < o.half) {
                         uint32_t ix = min((uint32_t)((ha + o.half) / cell), o.cells - 1);
                         uint32_t iy = min((uint32_t)((hb + o.half) / cell), o.cells - 1);
-                        atomicAdd(&o.lux[(size_t)inst * o.cells * o.cells + (size_t)iy * o.cells + ix], (double)wIn);
+                        atomicAdd(&o.lux[(size_t)inst * o.cells * o.cells + (size_t)iy * o.cells + ix],
+                                  (unsigned long long)fx(wIn));
                     }
                 }
-            } else if (state != RAY_ACTIVE) {
-                atomicAdd(&T[2], (double)wIn);                        // out of steps or length: lost
+            } else if (state != RAY_ACTIVE) {                          // out of steps or length: lost
+                tv[T_LOST] = fx(wIn);
+                tv[T_NLOST] = 1;
+                opt_vertex(o, inst, id, pos, wIn, ltot, beta);
             } else {
                 const uint2 rg = o.w.inst_range[inst];
                 const DPrim* ip = sp + rg.x;
@@ -211,15 +342,32 @@ __global__ void __launch_bounds__(256) k_opt_shade(OptArgs o, int nxt, int last)
                 bool inside = dh < 0.f;
                 f3 nrm = inside ? -nn : nn;
                 float otol = 10.f * eps;
-                SceneHit h = scene_full(ip, np, pos);
-                const st_material& m = sm[min(h.m, u.n_mats - 1)];
+                uint32_t item = 0;
+                SceneHit h = scene_full_item(ip, np, pos, item);
+                tag = min(rg.x + item, OPT_TAG_MAX - 1u);
+                mati = min(h.m, u.n_mats - 1);
+                const st_material& m = sm[mati];
                 if (m.detector > 0.5f && dot(-dir, nrm) >= 0.f) {     // kernels.js:660-672: a detector stops it
-                    atomicAdd(&T[3], (double)wIn);
-                    atomicAdd(&T[5], 1.0);
+                    tv[T_DET] = fx(wIn);
+                    tv[T_NDET] = 1;
+                    tv[T_INTER] = 1;
+                    iv[0] = fx(wIn);
+                    iv[2] = 1;
+                    interacted = true;
+                    opt_vertex(o, inst, id, pos, wIn, ltot, beta);
+                    const uint32_t k = atomicAdd(o.det_n, 1u);        // optRecordHit
+                    if (k < o.det_cap) {
+                        float4* d = o.det + (size_t)k * DET_F4;
+                        d[0] = f4(pos, wIn);
+                        d[1] = make_float4(dir.x, dir.y, dir.z, __uint_as_float(tag | (inst << 16)));
+                        // the colour as CIE X and Z of its linear Rec.709 rgb (Y is the weight)
+                        d[2] = make_float4(0.4124f * beta.x + 0.3576f * beta.y + 0.1805f * beta.z,
+                                           0.0193f * beta.x + 0.1192f * beta.y + 0.9505f * beta.z, 0.f, 0.f);
+                    }
                 } else if (dot(-dir, nrm) < 0.f) {                    // seen from behind: moved on, no interaction
                     f3 off = dir * otol;
                     pos = pos + off; ltot += length(off) * n;
-                    if (last) atomicAdd(&T[2], (double)wIn);
+                    if (last) { tv[T_LOST] = fx(wIn); tv[T_NLOST] = 1; opt_vertex(o, inst, id, pos, wIn, ltot, beta); }
                     else cont = true;
                 } else {
                     Rng rng;
@@ -227,6 +375,8 @@ __global__ void __launch_bounds__(256) k_opt_shade(OptArgs o, int nxt, int last)
                     rng.seed(id);
                     rng.seed(bounces);
                     bounces += 1;
+                    const f3 hit_pos = pos, beta_in = beta;
+                    const float hit_ltot = ltot;
                     float n0 = n, n1 = fmaxf(m.ior, n0);
                     if (m.transmission > 0.f && m.metallic < 1.f) {
                         SceneHit mb = scene_full(ip, np, pos + (-nrm) * (otol * 2.f));
@@ -256,16 +406,26 @@ __global__ void __launch_bounds__(256) k_opt_shade(OptArgs o, int nxt, int last)
                     f3 off = dir * otol;
                     pos = pos + off; ltot += length(off) * n;
                     if (bounces > u.maxbounce) st = RAY_TERMINATED;
-                    atomicAdd(&T[5], 1.0);
                     bool goesOn = st == RAY_ACTIVE || st == RAY_TERMINATED;
                     float wOut = goesOn ? luma(beta) : 0.f;
-                    atomicAdd(&T[4], (double)(wIn - wOut));
-                    if (st == RAY_TERMINATED || (st == RAY_ACTIVE && last)) atomicAdd(&T[2], (double)wOut);
+                    tv[T_INTER] = 1;
+                    tv[T_ABS] = fx(wIn) - fx(wOut);
+                    if (!goesOn) tv[T_NABS] = 1;
+                    iv[0] = fx(wIn);
+                    iv[1] = fx(wOut);
+                    iv[2] = 1;
+                    interacted = true;
+                    opt_vertex(o, inst, id, hit_pos, wIn, hit_ltot, beta_in);
+                    if (st == RAY_TERMINATED || (st == RAY_ACTIVE && last)) { tv[T_LOST] = fx(wOut); tv[T_NLOST] = 1; }
                     else if (st == RAY_ACTIVE) cont = true;
                     m4.y = meta_y(bounces, (m4.y >> 8) & 0xffu, RAY_ACTIVE);
                 }
             }
         }
+        // the warp's tallies: the instances' totals into shared memory, the objects' and materials' into global
+        warp_tally<OPT_TOT - 6>(q < count, inst, tv, stot, OPT_TOT);
+        warp_tally<3>(interacted, tag, iv, o.tag, 3u);
+        warp_tally<3>(interacted, inst * u.n_mats + mati, iv, o.mat, 3u);
         uint32_t rq = warp_append(outc, cont);
         if (cont) {
             a.pb.pos[slot] = f4(pos, ltot);
@@ -278,7 +438,19 @@ __global__ void __launch_bounds__(256) k_opt_shade(OptArgs o, int nxt, int last)
     }
     __syncthreads();
     for (uint32_t i = threadIdx.x; i < o.n_inst * OPT_TOT; i += blockDim.x)
-        if (stot[i] != 0.0) atomicAdd(&o.tot[i], stot[i]);
+        if (stot[i] != 0ull) atomicAdd(&o.tot[i], stot[i]);
+}
+
+// THE FLUSH: the fixed-point sums as FP64 weight (counts stay counts), where they are read out
+__global__ void k_opt_flush(const unsigned long long* __restrict__ in, double* __restrict__ out, size_t n, int counts) {
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        out[i] = counts ? (double)in[i] : (double)(long long)in[i] / OPT_FX;
+}
+
+uint32_t __float_as_uint_host(float f) {
+    uint32_t u;
+    std::memcpy(&u, &f, 4);
+    return u;
 }
 
 f3 normalize_host(f3 a) {
@@ -304,14 +476,23 @@ struct OptBuf {
     uint32_t *ray0 = nullptr, *ray1 = nullptr, *hit = nullptr;
     float* hitd = nullptr;
     size_t cap = 0, c1 = 0, c2 = 0, c3 = 0, c4 = 0, c5 = 0, c6 = 0, c7 = 0, c8 = 0, c9 = 0;
-    double *far = nullptr, *lux = nullptr, *tot = nullptr;
-    size_t nfar = 0, nlux = 0, ntot = 0;
+    unsigned long long *far = nullptr, *lux = nullptr, *tot = nullptr, *tag = nullptr, *mat = nullptr;
+    size_t nfar = 0, nlux = 0, ntot = 0, ntag = 0, nmat = 0;
     st_optics_source* src = nullptr; size_t nsrc = 0;
     float* cdf = nullptr; size_t ncdf = 0;
     uint2 *range = nullptr, *srange = nullptr; size_t nrange = 0, nsrange = 0;
     float4* origin = nullptr; size_t norigin = 0;
     uint32_t *wfirst = nullptr, *wpre = nullptr; size_t nwfirst = 0, nwpre = 0;
     DevCtr* ctr = nullptr; size_t nctr = 0;
+    float4 *det = nullptr, *verts = nullptr; size_t ndet = 0, nverts = 0;
+    uint32_t *det_n = nullptr, *vcount = nullptr; size_t ndetn = 0, nvcount = 0;
+    // the last run, kept for the readings after it (st_optics_tallies / _hits / _paths)
+    uint32_t last_ni = 0, last_mats = 0, last_det_cap = 0, last_path_rays = 0, last_path_verts = 0;
+    // THE BATCH AS ONE CUDA GRAPH: its whole chain captured at its first run and replayed while nothing it was
+    // captured with changes (the key: the scene, the batch, the far field, the sources, the detail, the buffers)
+    cudaGraphExec_t graph = nullptr;
+    std::vector<uint64_t> graph_key;
+    uint32_t graph_launches = 0;
 };
 
 }  // namespace
@@ -321,9 +502,11 @@ void optics_free(OpticsState& os) {
     if (!os.scratch) return;
     OptBuf* B = static_cast<OptBuf*>(os.scratch);
     void* ps[] = {B->pos, B->dir, B->beta, B->rad, B->meta, B->ray0, B->ray1, B->hit, B->hitd, B->far, B->lux, B->tot,
-                  B->src, B->cdf, B->range, B->srange, B->origin, B->wfirst, B->wpre, B->ctr};
+                  B->tag, B->mat, B->src, B->cdf, B->range, B->srange, B->origin, B->wfirst, B->wpre, B->ctr, B->det,
+                  B->verts, B->det_n, B->vcount};
     for (void* p : ps)
         if (p) cudaFree(p);
+    if (B->graph) cudaGraphExecDestroy(B->graph);
     delete B;
     os.scratch = nullptr;
 }
@@ -338,6 +521,7 @@ int st_optics_set_sources(st_ctx* ctx, const st_optics_source* src, uint32_t n) 
             return ST_ERR_ARG;
         }
     ctx_ext(ctx).optics.sources.assign(src, src + n);
+    ctx_ext(ctx).optics.sources_gen++;
     return ST_OK;
 }
 
@@ -361,6 +545,7 @@ int st_optics_set_rays(st_ctx* ctx, const float* rays, uint32_t n) {
         return ST_ERR_CUDA;
     }
     os.n_rays = n;
+    os.sources_gen++;
     return ST_OK;
 }
 
@@ -444,30 +629,49 @@ int st_optics_run(st_ctx* ctx, const st_optics_batch* b, double* far_out, double
         }
     }
     const st_optics_far& F = os.far;
+    const st_optics_detail& D = os.detail;
     const size_t nfar = (size_t)NI * F.nG * F.nC, nlux = (size_t)NI * b->lux_cells * b->lux_cells;
+    const uint32_t NM = ctx_n_mats(ctx);
     uint64_t total = 0;
     for (uint32_t i = 0; i < NI; i++) total += b->ray_count[i];
     const uint32_t K = (uint32_t)std::max<uint64_t>(1, (total + OPT_WAVE - 1) / OPT_WAVE);   // planBatches
     const size_t W = (size_t)std::min<uint64_t>(OPT_WAVE + NI, total + NI);
+    const size_t nverts = (size_t)NI * D.path_rays * D.path_verts * VERT_F4;
     cudaError_t e;
     if ((e = grow(B.pos, B.cap, W)) || (e = grow(B.dir, B.c1, W)) || (e = grow(B.beta, B.c2, W)) || (e = grow(B.rad, B.c3, W)) ||
         (e = grow(B.meta, B.c4, W)) || (e = grow(B.ray0, B.c5, W)) || (e = grow(B.ray1, B.c6, W)) || (e = grow(B.hit, B.c7, W)) ||
         (e = grow(B.hitd, B.c8, W)) || (e = grow(B.far, B.nfar, std::max<size_t>(nfar, 1))) ||
         (e = grow(B.lux, B.nlux, std::max<size_t>(nlux, 1))) || (e = grow(B.tot, B.ntot, (size_t)NI * OPT_TOT)) ||
+        (e = grow(B.tag, B.ntag, (size_t)OPT_TAG_MAX * 3)) || (e = grow(B.mat, B.nmat, (size_t)NI * NM * 3)) ||
         (e = grow(B.src, B.nsrc, std::max<size_t>(src.size(), 1))) || (e = grow(B.cdf, B.ncdf, std::max<size_t>(cdf.size(), 1))) ||
         (e = grow(B.range, B.nrange, (size_t)NI)) || (e = grow(B.srange, B.nsrange, (size_t)NI)) ||
-        (e = grow(B.origin, B.norigin, (size_t)NI)) || (e = grow(B.wfirst, B.nwfirst, (size_t)NI)) ||
-        (e = grow(B.wpre, B.nwpre, (size_t)NI + 1)) || (e = grow(B.ctr, B.nctr, (size_t)1)))
+        (e = grow(B.origin, B.norigin, (size_t)NI)) || (e = grow(B.wfirst, B.nwfirst, (size_t)NI * K)) ||
+        (e = grow(B.wpre, B.nwpre, (size_t)(NI + 1) * K)) || (e = grow(B.ctr, B.nctr, (size_t)1)) ||
+        (e = grow(B.det, B.ndet, std::max<size_t>((size_t)D.det_cap * DET_F4, 1))) ||
+        (e = grow(B.det_n, B.ndetn, (size_t)1)) || (e = grow(B.verts, B.nverts, std::max<size_t>(nverts, 1))) ||
+        (e = grow(B.vcount, B.nvcount, std::max<size_t>((size_t)NI * D.path_rays, 1))))
         return fail(e, "cudaMalloc optics buffers");
+    // the waves: each instance's rays split evenly over K of them (photons.js:31-62 splitPart), all K tables at once
+    std::vector<uint32_t> wf((size_t)NI * K), wp((size_t)(NI + 1) * K, 0);
+    std::vector<uint32_t> wslots(K);
+    for (uint32_t k = 0; k < K; k++) {
+        uint32_t* pre = wp.data() + (size_t)k * (NI + 1);
+        for (uint32_t i = 0; i < NI; i++) {
+            uint64_t n = b->ray_count[i];
+            uint64_t f0 = n * k / K, f1 = n * (k + 1) / K;
+            wf[(size_t)k * NI + i] = (uint32_t)f0;
+            pre[i + 1] = pre[i] + (uint32_t)(f1 - f0);
+        }
+        wslots[k] = pre[NI];
+    }
     if ((e = cudaMemcpyAsync(B.src, src.data(), src.size() * sizeof(st_optics_source), cudaMemcpyHostToDevice, st)) ||
         (e = cudaMemcpyAsync(B.cdf, cdf.data(), cdf.size() * 4, cudaMemcpyHostToDevice, st)) ||
         (e = cudaMemcpyAsync(B.range, range.data(), NI * sizeof(uint2), cudaMemcpyHostToDevice, st)) ||
         (e = cudaMemcpyAsync(B.srange, srange.data(), NI * sizeof(uint2), cudaMemcpyHostToDevice, st)) ||
         (e = cudaMemcpyAsync(B.origin, origin.data(), NI * sizeof(float4), cudaMemcpyHostToDevice, st)) ||
-        (e = cudaMemsetAsync(B.far, 0, std::max<size_t>(nfar, 1) * 8, st)) ||
-        (e = cudaMemsetAsync(B.lux, 0, std::max<size_t>(nlux, 1) * 8, st)) ||
-        (e = cudaMemsetAsync(B.tot, 0, (size_t)NI * OPT_TOT * 8, st)) ||
-        (e = cudaMemsetAsync(B.ctr, 0, sizeof(DevCtr), st)))
+        (e = cudaMemcpyAsync(B.wfirst, wf.data(), wf.size() * 4, cudaMemcpyHostToDevice, st)) ||
+        (e = cudaMemcpyAsync(B.wpre, wp.data(), wp.size() * 4, cudaMemcpyHostToDevice, st)) ||
+        (e = cudaStreamSynchronize(st)))
         return fail(e, "optics upload");
 
     // the uniforms the march and the shade read: the scene's tolerance and radius, the settings' march controls
@@ -483,7 +687,7 @@ int st_optics_run(st_ctx* ctx, const st_optics_batch* b, double* far_out, double
     double tol = sd.tolerance > 0 ? sd.tolerance : 1e-3;
     double R = sd.env_radius > 0 ? sd.env_radius : 400.0;
     u.tol = (float)tol; u.envR = (float)R; u.envR2 = (float)(R * R);
-    u.n_prims = np; u.n_mats = ctx_n_mats(ctx);
+    u.n_prims = np; u.n_mats = NM;
     u.P = 1;
     o.w.prims = ctx_d_prims(ctx);
     o.w.mats = ctx_d_mats(ctx);
@@ -500,7 +704,6 @@ int st_optics_run(st_ctx* ctx, const st_optics_batch* b, double* far_out, double
     o.rays = os.rays; o.n_rays = os.n_rays;
     o.has_sets = 0;
     for (const st_optics_source& q : os.sources) if (q.shape == 3u) o.has_sets = 1;
-    o.wave_first = B.wfirst; o.wave_prefix = B.wpre;
     o.n_inst = NI;
     o.seed = b->seed;
     f3 ax = normalize_host(mk(F.axis[0], F.axis[1], F.axis[2]));
@@ -509,7 +712,10 @@ int st_optics_run(st_ctx* ctx, const st_optics_batch* b, double* far_out, double
     o.c90 = mk(ax.y * c0.z - ax.z * c0.y, ax.z * c0.x - ax.x * c0.z, ax.x * c0.y - ax.y * c0.x);
     o.nC = F.nC; o.nG = F.nG; o.cells = b->lux_cells;
     o.half = b->lux_half; o.height = b->lux_height;
-    o.far = B.far; o.lux = B.lux; o.tot = B.tot;
+    o.far = B.far; o.lux = B.lux; o.tot = B.tot; o.tag = B.tag; o.mat = B.mat;
+    o.det = B.det; o.det_n = B.det_n; o.det_cap = D.det_cap;
+    o.verts = B.verts; o.vcount = B.vcount; o.path_rays = D.path_rays; o.path_verts = D.path_verts;
+    o.esc_len = D.esc_len > 0.f ? D.esc_len : 0.1f;
     const int sms = ctx_sms(ctx);
     const size_t shade_smem = np * sizeof(DPrim) + u.n_mats * sizeof(st_material) + (size_t)NI * OPT_TOT * 8;
     cudaFuncSetAttribute(k_opt_shade, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shade_smem);
@@ -517,50 +723,172 @@ int st_optics_run(st_ctx* ctx, const st_optics_batch* b, double* far_out, double
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&shade_blocks, k_opt_shade, 256, shade_smem);
     shade_blocks = std::max(1, shade_blocks) * sms;
 
-    // the waves: each instance's rays split evenly over K of them (photons.js:31-62 splitPart)
-    for (uint32_t k = 0; k < K; k++) {
-        std::vector<uint32_t> wf(NI), wp(NI + 1, 0);
-        for (uint32_t i = 0; i < NI; i++) {
-            uint64_t n = b->ray_count[i];
-            uint64_t f0 = n * k / K, f1 = n * (k + 1) / K;
-            wf[i] = (uint32_t)f0;
-            wp[i + 1] = wp[i] + (uint32_t)(f1 - f0);
+    // THE CHAIN, every wave: the tallies cleared, then per wave its rays generated and traced to their ends
+    auto chain = [&](uint32_t& launches) -> cudaError_t {
+        cudaError_t r;
+        launches = 0;
+        if ((r = cudaMemsetAsync(B.far, 0, std::max<size_t>(nfar, 1) * 8, st)) ||
+            (r = cudaMemsetAsync(B.lux, 0, std::max<size_t>(nlux, 1) * 8, st)) ||
+            (r = cudaMemsetAsync(B.tot, 0, (size_t)NI * OPT_TOT * 8, st)) ||
+            (r = cudaMemsetAsync(B.tag, 0, (size_t)OPT_TAG_MAX * 3 * 8, st)) ||
+            (r = cudaMemsetAsync(B.mat, 0, (size_t)NI * NM * 3 * 8, st)) ||
+            (r = cudaMemsetAsync(B.det_n, 0, 4, st)) ||
+            (r = cudaMemsetAsync(B.ctr, 0, sizeof(DevCtr), st)))
+            return r;
+        for (uint32_t k = 0; k < K; k++) {
+            const uint32_t slots = wslots[k];
+            if (!slots) continue;
+            OptArgs ok = o;
+            ok.wave_first = B.wfirst + (size_t)k * NI;
+            ok.wave_prefix = B.wpre + (size_t)k * (NI + 1);
+            ok.w.slots = slots;
+            if ((r = launch_iter_begin(ok.w, 0, 1, 1, st))) return r;
+            k_opt_gen<<<std::min((slots + 255) / 256, (uint32_t)sms * 8u), 256, 0, st>>>(ok);
+            launches += 2;
+            int cur = 0;
+            for (uint32_t it = 0; it < u.budget; it++) {
+                int nxt = cur ^ 1, last = it + 1 == u.budget;
+                if (it > 0 && (r = launch_iter_begin(ok.w, (int)it, nxt, 0, st))) return r;
+                if ((r = launch_march(ok.w, cur, nxt, last, sms, st))) return r;
+                k_opt_shade<<<shade_blocks, 256, shade_smem, st>>>(ok, nxt, last);
+                launches += 3;
+                cur = nxt;
+            }
+            if ((r = cudaGetLastError())) return r;
         }
-        const uint32_t slots = wp[NI];
-        if (!slots) continue;
-        if ((e = cudaMemcpyAsync(B.wfirst, wf.data(), NI * 4, cudaMemcpyHostToDevice, st)) ||
-            (e = cudaMemcpyAsync(B.wpre, wp.data(), (NI + 1) * 4, cudaMemcpyHostToDevice, st)))
-            return fail(e, "optics upload");
-        o.w.slots = slots;
-        if ((e = launch_iter_begin(o.w, 0, 1, 1, st))) return fail(e, "optics launch");
-        k_opt_gen<<<std::min((slots + 255) / 256, (uint32_t)sms * 8u), 256, 0, st>>>(o);
-        int cur = 0;
-        for (uint32_t it = 0; it < u.budget; it++) {
-            int nxt = cur ^ 1, last = it + 1 == u.budget;
-            if (it > 0 && (e = launch_iter_begin(o.w, (int)it, nxt, 0, st))) return fail(e, "optics launch");
-            if ((e = launch_march(o.w, cur, nxt, last, sms, st))) return fail(e, "optics march");
-            k_opt_shade<<<shade_blocks, 256, shade_smem, st>>>(o, nxt, last);
-            cur = nxt;
-        }
-        if ((e = cudaGetLastError())) return fail(e, "optics launch");
+        return cudaSuccess;
+    };
+    // the graph's key: everything the chain was recorded with
+    std::vector<uint64_t> key = {ctx_scene_gen(ctx), NI, K, b->seed, b->lux_cells, b->maxbounce,
+                                 (uint64_t)(uintptr_t)B.pos, (uint64_t)(uintptr_t)B.far, (uint64_t)(uintptr_t)B.lux,
+                                 (uint64_t)(uintptr_t)B.det, (uint64_t)(uintptr_t)B.verts, (uint64_t)(uintptr_t)B.mat,
+                                 (uint64_t)(uintptr_t)B.wfirst, (uint64_t)(uintptr_t)B.src, os.sources_gen,
+                                 (uint64_t)(uintptr_t)os.rays, D.det_cap, D.path_rays, D.path_verts,
+                                 (uint64_t)__float_as_uint_host(o.esc_len), F.nC, F.nG,
+                                 (uint64_t)__float_as_uint_host(b->lux_half), (uint64_t)__float_as_uint_host(b->lux_height)};
+    for (int k = 0; k < 3; k++) {
+        key.push_back(__float_as_uint_host(F.axis[k]));
+        key.push_back(__float_as_uint_host(F.c0[k]));
     }
-    std::vector<double> tot((size_t)NI * OPT_TOT);
-    if ((e = cudaMemcpyAsync(tot.data(), B.tot, tot.size() * 8, cudaMemcpyDeviceToHost, st)) ||
-        (far_out && nfar && (e = cudaMemcpyAsync(far_out, B.far, nfar * 8, cudaMemcpyDeviceToHost, st))) ||
-        (lux_out && nlux && (e = cudaMemcpyAsync(lux_out, B.lux, nlux * 8, cudaMemcpyDeviceToHost, st))) ||
-        (e = cudaStreamSynchronize(st)))
-        return fail(e, "optics readback");
+    for (uint32_t i = 0; i < NI; i++) key.push_back(b->ray_count[i]);
+    if (!B.graph || key != B.graph_key) {
+        if (B.graph) { cudaGraphExecDestroy(B.graph); B.graph = nullptr; }
+        cudaGraph_t g;
+        uint32_t launches = 0;
+        if ((e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal))) return fail(e, "optics capture");
+        cudaError_t e1 = chain(launches);
+        cudaError_t e2 = cudaStreamEndCapture(st, &g);
+        if (e1 || e2) { cudaGetLastError(); return fail(e1 ? e1 : e2, "optics capture"); }
+        e = cudaGraphInstantiate(&B.graph, g, 0);
+        cudaGraphDestroy(g);
+        if (e) { B.graph = nullptr; return fail(e, "optics graph"); }
+        B.graph_key = key;
+        B.graph_launches = launches;
+    }
+    if ((e = cudaGraphLaunch(B.graph, st))) return fail(e, "optics graph launch");
+    os.launches += B.graph_launches;
+    // the readings: the totals as they are, the far field and the lux map flushed to FP64 in place, then read out
+    std::vector<unsigned long long> tot((size_t)NI * OPT_TOT);
+    if ((e = cudaMemcpyAsync(tot.data(), B.tot, tot.size() * 8, cudaMemcpyDeviceToHost, st))) return fail(e, "optics readback");
+    if (far_out && nfar) {
+        k_opt_flush<<<std::min<size_t>((nfar + 255) / 256, (size_t)sms * 16), 256, 0, st>>>(
+            B.far, reinterpret_cast<double*>(B.far), nfar, 0);
+        if ((e = cudaMemcpyAsync(far_out, B.far, nfar * 8, cudaMemcpyDeviceToHost, st))) return fail(e, "optics readback");
+    }
+    if (lux_out && nlux) {
+        k_opt_flush<<<std::min<size_t>((nlux + 255) / 256, (size_t)sms * 16), 256, 0, st>>>(
+            B.lux, reinterpret_cast<double*>(B.lux), nlux, 0);
+        if ((e = cudaMemcpyAsync(lux_out, B.lux, nlux * 8, cudaMemcpyDeviceToHost, st))) return fail(e, "optics readback");
+    }
+    if ((e = cudaStreamSynchronize(st))) return fail(e, "optics readback");
     DevCtr c;
     cudaMemcpy(&c, B.ctr, sizeof(DevCtr), cudaMemcpyDeviceToHost);
+    B.last_ni = NI; B.last_mats = NM; B.last_det_cap = D.det_cap;
+    B.last_path_rays = D.path_rays; B.last_path_verts = D.path_verts;
     if (c.errflag) { ctx_set_error(ctx, "a kernel's wait for its scene table ran out of iterations"); return ST_ERR_TIMEOUT; }
+    auto w = [&](uint32_t i, uint32_t j) { return (double)(long long)tot[(size_t)i * OPT_TOT + j] / OPT_FX; };
+    auto n = [&](uint32_t i, uint32_t j) { return (uint64_t)tot[(size_t)i * OPT_TOT + j]; };
     if (totals)
         for (uint32_t i = 0; i < NI; i++) {
-            const double* T = &tot[(size_t)i * OPT_TOT];
-            totals[i].emitted = o.has_sets ? T[7] : (double)b->ray_count[i];   // a ray set's: its rays' weights
-            totals[i].escaped = T[1]; totals[i].lost = T[2]; totals[i].detected = T[3]; totals[i].absorbed = T[4];
-            totals[i].interactions = (uint64_t)T[5];
+            totals[i].emitted = o.has_sets ? w(i, T_EMIT) : (double)b->ray_count[i];   // a ray set's: its rays' weights
+            totals[i].escaped = w(i, T_ESC); totals[i].lost = w(i, T_LOST); totals[i].detected = w(i, T_DET);
+            totals[i].absorbed = w(i, T_ABS);
+            totals[i].interactions = n(i, T_INTER);
             totals[i].rays = b->ray_count[i];
+            totals[i].n_escaped = n(i, T_NESC); totals[i].n_lost = n(i, T_NLOST);
+            totals[i].n_detected = n(i, T_NDET); totals[i].n_absorbed = n(i, T_NABS);
         }
+    return ST_OK;
+}
+
+int st_optics_set_detail(st_ctx* ctx, const st_optics_detail* d) {
+    if (!ctx || !d) return ST_ERR_ARG;
+    if (d->det_cap > (1u << 24) || d->path_rays > 4096 || d->path_verts > 256 || !(d->esc_len >= 0.f)) {
+        ctx_set_error(ctx, "optics detail out of range (det_cap <= 2^24, path_rays <= 4096, path_verts <= 256)");
+        return ST_ERR_ARG;
+    }
+    ctx_ext(ctx).optics.detail = *d;
+    return ST_OK;
+}
+
+static OptBuf* last_run(st_ctx* ctx) {
+    OpticsState& os = ctx_ext(ctx).optics;
+    OptBuf* B = static_cast<OptBuf*>(os.scratch);
+    if (!B || !B->last_ni) { ctx_set_error(ctx, "no optics run yet"); return nullptr; }
+    return B;
+}
+
+int st_optics_tallies(st_ctx* ctx, double* tags, double* mats) {
+    if (!ctx) return ST_ERR_ARG;
+    OptBuf* B = last_run(ctx);
+    if (!B) return ST_ERR_STATE;
+    cudaSetDevice(ctx_device(ctx));
+    auto out = [&](const unsigned long long* d, size_t n, double* h) -> bool {
+        std::vector<unsigned long long> v(n);
+        if (cudaMemcpy(v.data(), d, n * 8, cudaMemcpyDeviceToHost) != cudaSuccess) return false;
+        for (size_t i = 0; i < n; i++) h[i] = i % 3 == 2 ? (double)v[i] : (double)(long long)v[i] / OPT_FX;
+        return true;
+    };
+    if (tags && !out(B->tag, (size_t)OPT_TAG_MAX * 3, tags)) return ST_ERR_CUDA;
+    if (mats && !out(B->mat, (size_t)B->last_ni * B->last_mats * 3, mats)) return ST_ERR_CUDA;
+    return ST_OK;
+}
+
+int st_optics_hits(st_ctx* ctx, float* hits, uint32_t max_n, uint32_t* n_out) {
+    if (!ctx || (max_n && !hits)) return ST_ERR_ARG;
+    OptBuf* B = last_run(ctx);
+    if (!B) return ST_ERR_STATE;
+    cudaSetDevice(ctx_device(ctx));
+    uint32_t n = 0;
+    if (cudaMemcpy(&n, B->det_n, 4, cudaMemcpyDeviceToHost) != cudaSuccess) return ST_ERR_CUDA;
+    if (n_out) *n_out = n;
+    const uint32_t k = std::min(std::min(n, B->last_det_cap), max_n);
+    if (!k) return ST_OK;
+    std::vector<float4> v((size_t)k * DET_F4);
+    if (cudaMemcpy(v.data(), B->det, v.size() * sizeof(float4), cudaMemcpyDeviceToHost) != cudaSuccess) return ST_ERR_CUDA;
+    for (uint32_t i = 0; i < k; i++) {
+        const float4* d = &v[(size_t)i * DET_F4];
+        float* h = hits + (size_t)i * 12;
+        uint32_t t;
+        std::memcpy(&t, &d[1].w, 4);
+        h[0] = d[0].x; h[1] = d[0].y; h[2] = d[0].z; h[3] = d[0].w;          // position, weight
+        h[4] = d[1].x; h[5] = d[1].y; h[6] = d[1].z;                          // direction
+        h[7] = (float)(t & 0xffffu); h[8] = (float)(t >> 16);                  // tag, instance
+        h[9] = d[2].x; h[10] = d[2].y; h[11] = 0.f;                           // CIE X, Z
+    }
+    return ST_OK;
+}
+
+int st_optics_paths(st_ctx* ctx, float* verts, uint32_t* counts) {
+    if (!ctx) return ST_ERR_ARG;
+    OptBuf* B = last_run(ctx);
+    if (!B) return ST_ERR_STATE;
+    cudaSetDevice(ctx_device(ctx));
+    const size_t nr = (size_t)B->last_ni * B->last_path_rays;
+    if (counts && nr && cudaMemcpy(counts, B->vcount, nr * 4, cudaMemcpyDeviceToHost) != cudaSuccess) return ST_ERR_CUDA;
+    const size_t nv = nr * B->last_path_verts * VERT_F4;
+    if (verts && nv && cudaMemcpy(verts, B->verts, nv * sizeof(float4), cudaMemcpyDeviceToHost) != cudaSuccess)
+        return ST_ERR_CUDA;
     return ST_OK;
 }
 

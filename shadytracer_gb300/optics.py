@@ -26,6 +26,8 @@ class Optics:
         self.L = rt.L
         self.sources = []
         self.far = None
+        self.detail = T.StOpticsDetail()
+        self.n_instances = 0
 
     def set_sources(self, sources):
         arr = (T.StOpticsSource * max(1, len(sources)))(*sources)
@@ -65,7 +67,50 @@ class Optics:
         check(self.L.st_optics_run(self.rt.ctx, C.byref(b), far.ctypes.data_as(P), lux.ctypes.data_as(P), tot),
               self.rt.ctx, "st_optics_run")
         totals = [{f: getattr(tot[i], f) for f, _ in T.StOpticsTotals._fields_} for i in range(n)]
+        self.n_instances = n
         return {"far": far, "lux": lux, "totals": totals}
+
+    def set_detail(self, det_cap=0, path_rays=0, path_verts=0, esc_len=0.0):
+        """What a run keeps beyond its tallies (st_optics_set_detail): up to det_cap detector hits, and the paths of
+        each instance's first path_rays rays, path_verts vertices each, an escaped ray's last esc_len metres on."""
+        d = T.StOpticsDetail()
+        d.det_cap, d.path_rays, d.path_verts, d.esc_len = det_cap, path_rays, path_verts, esc_len
+        check(self.L.st_optics_set_detail(self.rt.ctx, C.byref(d)), self.rt.ctx, "st_optics_set_detail")
+        self.detail = d
+
+    def tallies(self):
+        """The last run's tallies by object and by material (kernels.js O_TAG / O_MAT): tags (256, 3) and mats
+        (instances, materials, 3), each row weight incident, weight leaving, interactions. A tag is an item of the
+        table, by its first primitive's index."""
+        nm = self.rt.scene.desc.n_materials
+        tags = np.zeros((256, 3))
+        mats = np.zeros((self.n_instances, nm, 3))
+        P = C.c_void_p
+        check(self.L.st_optics_tallies(self.rt.ctx, tags.ctypes.data_as(P), mats.ctypes.data_as(P)), self.rt.ctx,
+              "st_optics_tallies")
+        return tags, mats
+
+    def hits(self, max_n=None):
+        """The last run's detector hits (optRecordHit): an (n, 12) array -- position, weight, direction, tag, instance,
+        CIE X, Z, 0 -- and how many reached a detector in all (past det_cap they were not kept)."""
+        n = C.c_uint32()
+        check(self.L.st_optics_hits(self.rt.ctx, None, 0, C.byref(n)), self.rt.ctx, "st_optics_hits")
+        k = min(n.value, self.detail.det_cap if max_n is None else max_n)
+        out = np.zeros((k, 12), np.float32)
+        check(self.L.st_optics_hits(self.rt.ctx, out.ctypes.data_as(C.c_void_p), k, C.byref(n)), self.rt.ctx,
+              "st_optics_hits")
+        return out, n.value
+
+    def paths(self):
+        """The last run's kept paths (optVertex): counts (instances, path_rays) and verts (instances, path_rays,
+        path_verts, 8): position, weight, optical length, hue rgb."""
+        d = self.detail
+        counts = np.zeros((self.n_instances, d.path_rays), np.uint32)
+        verts = np.zeros((self.n_instances, d.path_rays, d.path_verts, 8), np.float32)
+        P = C.c_void_p
+        check(self.L.st_optics_paths(self.rt.ctx, verts.ctypes.data_as(P), counts.ctypes.data_as(P)), self.rt.ctx,
+              "st_optics_paths")
+        return verts, counts
 
 
 def far_geometry(nC, nG):
@@ -199,3 +244,134 @@ def ray_set_source(first, count, flux, instance=0, emit_n=1.0):
     s.tangent[0] = 1.0
     s.ray_first, s.ray_count = first, count
     return s
+
+
+# ---------------------------------------------------------------------------------------------------------------
+# THE DETECTOR MAP (optics/detmap.js:104-213 mapFrame / detectorMap / smoothMap): the recorded detector hits as an
+# illuminance map, in FP64 on the host. The plane is fitted to the hits (the principal axes of their positions; within
+# about a degree of a world axis, squared up to the other two); square cells over the hits' extent (`cells` along the
+# longer side); each cell the flux that landed in it over its area in square metres. Smoothing: 'none' (the
+# histogram), 'gauss' or 'epan' (kernel density estimates whose kernel is normalised over the cells each hit reaches,
+# so each hit deposits exactly its flux; bandwidth in cells), 'knn' (the photon-map estimate at each cell centre: the
+# k nearest hits' flux over the disc they fill, the reach capped at KNN_MAX_CELLS).
+# ---------------------------------------------------------------------------------------------------------------
+KNN_MAX_CELLS = 16
+
+
+def map_frame(pos, cells=64, rng=None):
+    """The plane of the hits and their in-plane coordinates: (centre, u, v, normal, ab, a0, a1, b0, b1, size, nx,
+    ny, flatness), or None for fewer than 3 hits."""
+    pos = np.asarray(pos, np.float64)
+    n = len(pos)
+    if n < 3:
+        return None
+    c = pos.mean(0)
+    d = pos - c
+    cov = d.T @ d / n
+    w, V = np.linalg.eigh(cov)                       # ascending: the normal is the direction they spread least along
+    order = np.argsort(w)[::-1]
+    w, V = w[order], V[:, order]
+    u, v, nrm = V[:, 0], V[:, 1], V[:, 2]
+    k = int(np.argmax(np.abs(nrm)))
+    if abs(nrm[k]) > 0.9998:                         # a floor, a wall: squared up to the world's axes
+        i, j = [q for q in range(3) if q != k]
+        u, v, nrm = np.eye(3)[i], np.eye(3)[j], np.eye(3)[k]
+    ab = np.stack([d @ u, d @ v], 1)
+    a0, a1 = ab[:, 0].min(), ab[:, 0].max()
+    b0, b1 = ab[:, 1].min(), ab[:, 1].max()
+    if rng is not None:
+        (a0, a1), (b0, b1) = rng
+    span = max(a1 - a0, b1 - b0) or 1e-9
+    size = span / max(1, int(cells))
+    nx = max(1, int(math.ceil((a1 - a0) / size - 1e-9)))
+    ny = max(1, int(math.ceil((b1 - b0) / size - 1e-9)))
+    return {"c": c, "u": u, "v": v, "normal": nrm, "ab": ab, "a0": a0, "a1": a1, "b0": b0, "b1": b1, "size": size,
+            "nx": nx, "ny": ny, "flatness": math.sqrt(max(w[2], 0.0)) / span}
+
+
+def detector_map(pos, flux, cells=64, metres_per_unit=1.0, smooth="none", bandwidth=1.5, k=32, rng=None):
+    """The illuminance map of hits at `pos` (n x 3) carrying `flux` (n, lm): a dict with E (ny x nx, lx), the hits'
+    count per cell, the frame, and the statistics detmap.js reports (total, max, meanLit, minLit, uniformity,
+    hitsPerLitCell, relNoise)."""
+    F = map_frame(pos, cells, rng)
+    if F is None:
+        return None
+    flux = np.asarray(flux, np.float64)
+    ab, a0, a1, b0, b1, size, nx, ny = F["ab"], F["a0"], F["a1"], F["b0"], F["b1"], F["size"], F["nx"], F["ny"]
+    inr = (ab[:, 0] >= a0) & (ab[:, 0] <= a1) & (ab[:, 1] >= b0) & (ab[:, 1] <= b1)
+    cx = np.minimum(nx - 1, np.floor((ab[:, 0] - a0) / size).astype(int))
+    cy = np.minimum(ny - 1, np.floor((ab[:, 1] - b0) / size).astype(int))
+    fl = np.zeros((ny, nx))
+    cnt = np.zeros((ny, nx), np.int64)
+    np.add.at(fl, (cy[inr], cx[inr]), flux[inr])
+    np.add.at(cnt, (cy[inr], cx[inr]), 1)
+    m2 = metres_per_unit * metres_per_unit
+    area = size * size * m2
+    h = max(0.1, float(bandwidth))
+    if smooth == "none":
+        E = fl / area
+    elif smooth in ("gauss", "epan"):
+        E = np.zeros((ny, nx))
+        hs = h * size
+        reach = 3 * h if smooth == "gauss" else h
+        R = int(math.ceil(reach)) + 1
+        for i in np.nonzero(inr)[0]:
+            a, b = ab[i]
+            x0, y0 = cx[i], cy[i]
+            ys = np.arange(max(0, y0 - R), min(ny - 1, y0 + R) + 1)
+            xs = np.arange(max(0, x0 - R), min(nx - 1, x0 + R) + 1)
+            db = (b0 + (ys + 0.5) * size - b) / hs
+            da = (a0 + (xs + 0.5) * size - a) / hs
+            r2 = db[:, None] ** 2 + da[None, :] ** 2
+            wk = np.where(r2 < 9, np.exp(-0.5 * r2), 0.0) if smooth == "gauss" else np.where(r2 < 1, 1 - r2, 0.0)
+            ws = wk.sum()
+            f = flux[i] / area
+            if not ws > 0:
+                E[y0, x0] += f
+            else:
+                E[np.ix_(ys, xs)] += f * wk / ws
+    elif smooth == "knn":
+        E = np.zeros((ny, nx))
+        kk = max(1, int(k))
+        bins = {}
+        for i in np.nonzero(inr)[0]:
+            bins.setdefault((cy[i], cx[i]), []).append(i)
+        for y in range(ny):
+            for x in range(nx):
+                ca, cb = a0 + (x + 0.5) * size, b0 + (y + 0.5) * size
+                r, got = 0, cnt[y, x]
+                while got < kk and r < KNN_MAX_CELLS:
+                    r += 1
+                    ring = 0
+                    for yy in range(y - r, y + r + 1):
+                        if yy < 0 or yy >= ny:
+                            continue
+                        for xx in (range(x - r, x + r + 1) if abs(yy - y) == r else (x - r, x + r)):
+                            if 0 <= xx < nx:
+                                ring += cnt[yy, xx]
+                    got += ring
+                if got < kk:
+                    continue
+                Rr = min(int(math.ceil((r + 0.5) * math.sqrt(2))), KNN_MAX_CELLS * 2)
+                idx = [i for yy in range(max(0, y - Rr), min(ny - 1, y + Rr) + 1)
+                       for xx in range(max(0, x - Rr), min(nx - 1, x + Rr) + 1) for i in bins.get((yy, xx), ())]
+                idx = np.array(idx)
+                d2 = (ab[idx, 0] - ca) ** 2 + (ab[idx, 1] - cb) ** 2
+                order = np.argsort(d2, kind="stable")[:kk]
+                rk2 = d2[order[-1]]
+                if rk2 > 0:
+                    E[y, x] = flux[idx[order]].sum() / (math.pi * rk2 * m2)
+    else:
+        raise ValueError("smooth: none, gauss, epan or knn")
+    lit = cnt > 0
+    inside = int(inr.sum())
+    hpc = inside / lit.sum() if lit.any() else 0.0
+    rel = None
+    if hpc:
+        rel = 1 / math.sqrt(kk) if smooth == "knn" else 1 / math.sqrt(
+            hpc * (4 * math.pi * h * h if smooth == "gauss" else 0.75 * math.pi * h * h if smooth == "epan" else 1))
+    meanLit = float(E[lit].mean()) if lit.any() else 0.0
+    minLit = float(E[lit].min()) if lit.any() else 0.0
+    return {"E": E, "count": cnt, "frame": F, "total": float(flux[inr].sum()), "max": float(E.max()),
+            "meanLit": meanLit, "minLit": minLit, "uniformity": minLit / meanLit if meanLit > 0 else None,
+            "litCells": int(lit.sum()), "hitsPerLitCell": hpc, "relNoise": rel, "cell_m": size * metres_per_unit}

@@ -595,6 +595,28 @@ def optics_bench(n_instances=64, seed=5, ray_min=1e5, ray_max=1e7, ray_scale=1.0
     return s
 
 
+def optics_detector_bench(n_instances=2, seed=5, height=0.02, radius=0.015, rays=200_000):
+    """The optics bench's emitter + lens instances, each with a detector above it (optics/kernels.js optIsDetector): a
+    thin disc of radius `radius` at `height` over the die, of a detector material, so the trace records the hits that
+    reach it (optRecordHit) and tallies them by object and by material."""
+    rng = Pcg32(seed)
+    det = material(base=(1, 1, 1), detector=1.0)
+    mats = [air(), diffuse((0.5, 0.5, 0.5)), glass((1, 1, 1), ior=1.49), det]
+    prims, srcs = [], []
+    for i in range(n_instances):
+        k1 = rng.uniform(-1.5, 0.0)
+        a4 = rng.uniform(-1e-3, 1e-3)
+        a6 = rng.uniform(-1e-3, 1e-3)
+        prims += led_lens_instance(i, k1, a4, a6)
+        prims.append(prim(ST_PRIM_CYLINDER, pos=(0, 0, height), params=(0.0005, radius), material=3, flags=i << 8))
+        srcs.append(led_source(i))
+    s = Scene(prims, mats, env_radius=0.1, tolerance=1e-6, name="optics-detector")
+    s.params = default_params(width=16, height=16, maxbounce=32)
+    s.view = look_at((0, -0.05, 0.01), (0, 0, 0.002), 30.0, 1.0)
+    s.info = {"sources": srcs, "rays": [rays] * n_instances, "workload": "optics-detector-%d" % n_instances}
+    return s
+
+
 # ------------------------------------------------------------------------------------------------------------
 # An environment image (core/envimage.js) and the map light sampling draws from it (core/envmap.js).
 # ------------------------------------------------------------------------------------------------------------

@@ -134,7 +134,14 @@ class StOpticsBatch(C.Structure):
 class StOpticsTotals(C.Structure):
     _fields_ = [("emitted", C.c_double), ("escaped", C.c_double), ("lost", C.c_double),
                 ("detected", C.c_double), ("absorbed", C.c_double),
-                ("interactions", C.c_uint64), ("rays", C.c_uint64)]
+                ("interactions", C.c_uint64), ("rays", C.c_uint64),
+                ("n_escaped", C.c_uint64), ("n_lost", C.c_uint64), ("n_detected", C.c_uint64),
+                ("n_absorbed", C.c_uint64)]
+
+
+class StOpticsDetail(C.Structure):
+    _fields_ = [("det_cap", C.c_uint32), ("path_rays", C.c_uint32), ("path_verts", C.c_uint32),
+                ("esc_len", C.c_float)]
 
 
 def default_params(**kw):

@@ -87,3 +87,109 @@ def test_far_field_and_lux_per_bin_at_a_million_rays():
         assert inside.all(), (key, np.count_nonzero(~inside), np.abs(F - R)[~inside][:5], bound[~inside][:5])
         moved = 0.5 * np.abs(F - R).sum() / max(R.sum(), 1.0)
         assert moved < 0.01, (key, moved)
+
+
+@pytest.fixture(scope="module")
+def detector_run():
+    from shadytracer_gb300.renderer import create_path_tracer
+    from shadytracer_gb300.optics import Optics
+    b = scenes.optics_detector_bench(n_instances=2, rays=300_000)
+    rays = b.info["rays"]
+    with create_path_tracer(b, device=0) as rt:
+        O = Optics(rt)
+        O.set_sources(b.info["sources"])
+        O.set_far(nC=90, nG=46)
+        O.set_detail(det_cap=1 << 20, path_rays=16, path_verts=16, esc_len=0.05)
+        g = O.run(rays, lux_cells=32, maxbounce=32, seed=3)
+        tags, mats = O.tallies()
+        hits, nhits = O.hits()
+        verts, counts = O.paths()
+        g2 = O.run(rays, lux_cells=32, maxbounce=32, seed=3)     # a replay of the batch's graph
+        tags2, mats2 = O.tallies()
+    o = oracle.optics_run(b, rays, nC=90, nG=46, cells=32, maxbounce=32, seed=3)
+    return b, rays, g, tags, mats, hits, nhits, verts, counts, g2, tags2, mats2, o
+
+
+def test_a_replayed_batch_is_the_same_to_the_bit(detector_run):
+    """The tallies are integers (fixed point) summed in any order: the batch's graph replayed gives the same bits."""
+    b, rays, g, tags, mats, hits, nhits, verts, counts, g2, tags2, mats2, o = detector_run
+    assert np.array_equal(g["far"], g2["far"]) and np.array_equal(g["lux"], g2["lux"])
+    assert np.array_equal(tags, tags2) and np.array_equal(mats, mats2)
+    assert g["totals"] == g2["totals"]
+
+
+def test_counts_and_tallies_by_object_and_material_match_the_oracle(detector_run):
+    b, rays, g, tags, mats, hits, nhits, verts, counts, g2, tags2, mats2, o = detector_run
+    first = [min(i for i, p in enumerate(b.prim_list) if (p.flags >> 8) == k) for k in range(len(rays))]
+    for k, n in enumerate(rays):
+        G, R, D = g["totals"][k], o["totals"][k], o["detail"][k]
+        assert G["n_escaped"] + G["n_lost"] + G["n_detected"] + G["n_absorbed"] <= n
+        for c in ("n_escaped", "n_detected", "n_lost"):
+            x, y = G[c], D["counts"][c]
+            assert abs(x - y) <= 4 * math.sqrt(max(y, 1)) + 0.003 * n, (k, c, x, y)
+        assert G["detected"] == pytest.approx(R["detected"], rel=0.01, abs=5)
+        # by material: incident, leaving and interactions of the die, the lens and the detector
+        for m in (1, 2, 3):
+            gi, ri = mats[k, m], D["mat"][m]
+            assert abs(gi[2] - ri[2]) <= 4 * math.sqrt(max(ri[2], 1)) + 0.003 * ri[2], (k, m, gi, ri)
+            assert gi[0] == pytest.approx(ri[0], rel=0.02, abs=5), (k, m, gi, ri)
+            assert gi[1] == pytest.approx(ri[1], rel=0.02, abs=5), (k, m, gi, ri)
+        # by object: the instance's items by their first primitive (the GPU's tags count from the batch's table)
+        for local in range(len(D["tag"])):
+            ri = D["tag"][local]
+            gi = tags[first[k] + local]
+            assert abs(gi[2] - ri[2]) <= 4 * math.sqrt(max(ri[2], 1)) + 0.003 * ri[2] + 1, (k, local, gi, ri)
+    # every interaction is some object's and some material's
+    assert tags[:, 2].sum() == sum(t["interactions"] for t in g["totals"])
+    assert mats[:, :, 2].sum() == sum(t["interactions"] for t in g["totals"])
+
+
+def test_detector_hits_match_the_oracle(detector_run):
+    b, rays, g, tags, mats, hits, nhits, verts, counts, g2, tags2, mats2, o = detector_run
+    assert nhits == len(hits) == sum(t["n_detected"] for t in g["totals"])
+    for k in range(len(rays)):
+        mine = hits[hits[:, 8] == k]
+        ref = o["detail"][k]["hits"]
+        assert abs(len(mine) - len(ref)) <= 4 * math.sqrt(len(ref)) + 0.003 * len(ref)
+        assert mine[:, 3].sum() == pytest.approx(g["totals"][k]["detected"], rel=1e-6)
+        # on the detector's plane, spread as the oracle's
+        assert np.allclose(mine[:, 2], 0.02 - 0.0005, atol=1e-4)
+        for c in (0, 1):
+            assert abs(mine[:, c].mean() - ref[:, c].mean()) < 4 * ref[:, c].std() / math.sqrt(len(ref)) + 1e-5
+            assert abs(mine[:, c].std() / ref[:, c].std() - 1) < 0.02
+        # its colour: a white source, X and Z of the weight's
+        assert np.allclose(mine[:, 9] / mine[:, 3], 0.9505, rtol=2e-3)
+
+
+def test_kept_paths_start_at_the_source_and_end_past_the_last_event(detector_run):
+    b, rays, g, tags, mats, hits, nhits, verts, counts, g2, tags2, mats2, o = detector_run
+    assert counts.shape == (2, 16) and counts.min() >= 2
+    start = verts[:, :, 0, :3]
+    assert np.all(np.abs(start[..., 2]) < 1e-5)                 # the die's face, z = 0
+    assert np.all(np.abs(start[..., :2]) <= 0.0005 + 1e-6)      # within its 1 x 1 mm
+    opl = np.array([[verts[i, r, :counts[i, r], 4] for r in range(16)] for i in range(2)], dtype=object)
+    for i in range(2):
+        for r in range(16):
+            o_ = verts[i, r, :counts[i, r], 4]
+            assert np.all(np.diff(o_) > 0), o_                   # optical length grows along the path
+
+
+def test_the_detector_map(detector_run):
+    """The recorded hits as an illuminance map (optics/detmap.js): the plane fitted to them is the detector's, the
+    histogram and the kernel estimates hold the hits' flux, the k-nearest estimate reads the same illuminance where
+    the hits are dense."""
+    from shadytracer_gb300.optics import detector_map
+    b, rays, g, tags, mats, hits, nhits, verts, counts, g2, tags2, mats2, o = detector_run
+    mine = hits[hits[:, 8] == 0]
+    m = detector_map(mine[:, :3], mine[:, 3], cells=32)
+    assert abs(abs(m["frame"]["normal"][2]) - 1) < 1e-9          # squared up to the world: a floor
+    assert m["total"] == pytest.approx(float(mine[:, 3].sum()), rel=1e-9)
+    cell_area = m["cell_m"] ** 2
+    assert (m["E"] * cell_area).sum() == pytest.approx(m["total"], rel=1e-9)
+    for sm in ("gauss", "epan"):
+        mk = detector_map(mine[:, :3], mine[:, 3], cells=32, smooth=sm, bandwidth=1.5)
+        assert (mk["E"] * cell_area).sum() == pytest.approx(m["total"], rel=1e-9)
+    mk = detector_map(mine[:, :3], mine[:, 3], cells=32, smooth="knn", k=64)
+    dense = m["count"] > 200
+    assert dense.any()
+    assert abs(np.median(mk["E"][dense] / m["E"][dense]) - 1) < 0.1
