@@ -1194,4 +1194,5 @@ uint32_t ctx_n_mats(st_ctx* ctx) { return (uint32_t)ctx->mats.size(); }
 const st_scene_desc& ctx_desc(st_ctx* ctx) { return ctx->desc; }
 bool ctx_has_scene(st_ctx* ctx) { return ctx->has_scene; }
 uint64_t ctx_scene_gen(st_ctx* ctx) { return ctx->scene_gen; }
+DevCtr* ctx_counters(st_ctx* ctx) { return ctx->d_ctr; }
 MfTab ctx_tab(st_ctx* ctx) { return MfTab{ctx->d_ec, ctx->d_ecavg, ctx->d_e1}; }

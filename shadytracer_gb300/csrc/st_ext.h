@@ -123,5 +123,6 @@ uint32_t ctx_n_prims(st_ctx* ctx);
 uint32_t ctx_n_mats(st_ctx* ctx);
 const st_scene_desc& ctx_desc(st_ctx* ctx);
 bool ctx_has_scene(st_ctx* ctx);
-uint64_t ctx_scene_gen(st_ctx* ctx);     // a count of the scenes set (a graph recorded with one is stale after)
+uint64_t ctx_scene_gen(st_ctx* ctx);
+st::DevCtr* ctx_counters(st_ctx* ctx);     // a count of the scenes set (a graph recorded with one is stale after)
 st::MfTab ctx_tab(st_ctx* ctx);

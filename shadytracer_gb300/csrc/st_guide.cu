@@ -97,76 +97,6 @@ __device__ __forceinline__ void store_out(const float (*o)[4], float* ws, uint32
 }
 
 // ---------------------------------------------------------------------------------------------------------------
-// INFERENCE over the hit queue: per round, the block's 256 entries whose vertex is guided, compacted, then 16 a warp
-// ---------------------------------------------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) k_guide_infer(WaveArgs a) {
-    extern __shared__ __align__(128) unsigned char smem[];
-    __shared__ __align__(8) uint64_t mbar;
-    __shared__ uint32_t list[256];
-    __shared__ uint32_t wcnt[8];
-    __shared__ float ws_all[8][16 * GUIDE_OUT];
-    const Uni& u = a.u;
-    st_material* sm = reinterpret_cast<st_material*>(smem);
-    const uint32_t mat_bytes = u.n_mats * (uint32_t)sizeof(st_material);
-    uint16_t* sw = reinterpret_cast<uint16_t*>(smem + ((mat_bytes + 15u) & ~15u));
-    if (!stage_table(sm, a.mats, mat_bytes, &mbar, a.ctr)) return;
-    guide_stage_weights(a.gd.wbf, sw, false);
-    __syncthreads();
-    const __nv_bfloat16* swb = reinterpret_cast<const __nv_bfloat16*>(sw);
-    const uint32_t count = a.ctr->hitCount;
-    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5, g = lane >> 2, t = lane & 3u;
-    float* ws = ws_all[warp];
-    for (uint32_t base = blockIdx.x * blockDim.x; base < count; base += gridDim.x * blockDim.x) {
-        const uint32_t q = base + threadIdx.x;
-        bool want = false;
-        if (q < count) {
-            const uint32_t slot = a.q.hit[q];
-            const uint32_t my = a.pb.meta[slot].y;
-            const uint32_t ids = __float_as_uint(a.q.hsurf[q].w);
-            if (((my >> 16) & 0xffu) == RAY_ACTIVE && (my & 0xffu) == 0u && ids != SURF_LEAVING && a.q.hitd[q] >= 0.f)
-                want = guide_vertex(sm[ids & 0xffffu]);
-        }
-        const uint32_t m = __ballot_sync(FULL_MASK, want);
-        if (lane == 0u) wcnt[warp] = __popc(m);
-        __syncthreads();
-        uint32_t off = 0, n = 0;
-        for (uint32_t w = 0; w < 8u; w++) { if (w < warp) off += wcnt[w]; n += wcnt[w]; }
-        if (want) list[off + __popc(m & lanemask_lt())] = q;
-        if (threadIdx.x == 0u && n) atomicAdd(&a.gd.dev->inferred, n);
-        __syncthreads();
-        for (uint32_t tile = warp; tile * 16u < n; tile += 8u) {
-            const uint32_t e0 = tile * 16u + g, e1 = e0 + 8u;
-            f3 u0 = mk(0.5f), u1 = mk(0.5f), n0 = mk(0.f, 0.f, 1.f), n1 = mk(0.f, 0.f, 1.f);
-            if (e0 < n) {
-                const uint32_t qq = list[e0];
-                u0 = guide_unit(xyz(a.pb.pos[a.q.hit[qq]]), a.gd.lo, a.gd.inv_ext);
-                n0 = xyz(a.q.hsurf[qq]);
-            }
-            if (e1 < n) {
-                const uint32_t qq = list[e1];
-                u1 = guide_unit(xyz(a.pb.pos[a.q.hit[qq]]), a.gd.lo, a.gd.inv_ext);
-                n1 = xyz(a.q.hsurf[qq]);
-            }
-            uint32_t a_in[3][4];
-            guide_input(a.gd.table, u0, n0, u1, n1, t, a_in);
-            GuideFwd f;
-            guide_forward(a_in, swb, g, t, f);
-            store_out(f.o, ws, g, t);
-            __syncwarp();
-            if (lane < 16u && tile * 16u + lane < n) {
-                uint2 out[GUIDE_LOBES];
-                guide_decode(ws + lane * GUIDE_OUT, out);
-                uint2* dst = a.gd.mix + (size_t)list[tile * 16u + lane] * GUIDE_LOBES;
-#pragma unroll
-                for (uint32_t k = 0; k < GUIDE_LOBES; k++) dst[k] = out[k];
-            }
-            __syncwarp();
-        }
-        __syncthreads();
-    }
-}
-
-// ---------------------------------------------------------------------------------------------------------------
 // THE BATCH: a wave's records, a hashed subsample of about GUIDE_CAP of them, each with the luminance found after it
 // ---------------------------------------------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) k_guide_collect(WaveArgs a) {
@@ -488,54 +418,6 @@ __global__ void k_guide_cast(const float* __restrict__ param, uint16_t* __restri
     }
 }
 
-// THE NETWORK AT GIVEN POINTS (st_mlp_eval): the batch's samples' positions and normals in, the 40 outputs and the
-// packed mixture out
-__global__ void __launch_bounds__(256) k_guide_eval(const GuideSample* __restrict__ samp, uint32_t n, f3 lo,
-                                                    float inv_ext, const float2* __restrict__ table,
-                                                    const uint16_t* __restrict__ wbf, float* __restrict__ raw,
-                                                    uint2* __restrict__ mix) {
-    extern __shared__ __align__(128) unsigned char smem[];
-    __shared__ float ws_all[8][16 * GUIDE_OUT];
-    uint16_t* sw = reinterpret_cast<uint16_t*>(smem);
-    guide_stage_weights(wbf, sw, false);
-    __syncthreads();
-    const __nv_bfloat16* swb = reinterpret_cast<const __nv_bfloat16*>(sw);
-    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5, g = lane >> 2, t = lane & 3u;
-    float* ws = ws_all[warp];
-    const uint32_t tiles = (n + 15u) / 16u, nwarps = (gridDim.x * blockDim.x) >> 5;
-    for (uint32_t tile = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; tile < tiles; tile += nwarps) {
-        const uint32_t r0 = tile * 16u + g, r1 = r0 + 8u;
-        f3 u0 = mk(0.5f), u1 = mk(0.5f), n0 = mk(0.f, 0.f, 1.f), n1 = mk(0.f, 0.f, 1.f);
-        if (r0 < n) { u0 = guide_unit(xyz(samp[r0].a), lo, inv_ext); n0 = xyz(samp[r0].b); }
-        if (r1 < n) { u1 = guide_unit(xyz(samp[r1].a), lo, inv_ext); n1 = xyz(samp[r1].b); }
-        uint32_t a_in[3][4];
-        guide_input(table, u0, n0, u1, n1, t, a_in);
-        GuideFwd f;
-        guide_forward(a_in, swb, g, t, f);
-        store_out(f.o, ws, g, t);
-        __syncwarp();
-        if (lane < 16u && tile * 16u + lane < n) {
-            const uint32_t r = tile * 16u + lane;
-            for (uint32_t k = 0; k < GUIDE_OUT; k++) raw[(size_t)r * GUIDE_OUT + k] = ws[lane * GUIDE_OUT + k];
-            uint2 out[GUIDE_LOBES];
-            guide_decode(ws + lane * GUIDE_OUT, out);
-            for (uint32_t k = 0; k < GUIDE_LOBES; k++) mix[(size_t)r * GUIDE_LOBES + k] = out[k];
-        }
-        __syncwarp();
-    }
-}
-
-static size_t infer_smem(uint32_t n_mats) {
-    return ((n_mats * sizeof(st_material) + 15) & ~(size_t)15) + (size_t)SW_FWD * 2;
-}
-cudaError_t launch_guide_infer(const WaveArgs& a, int sms, cudaStream_t s) {
-    const size_t smem = infer_smem(a.u.n_mats);
-    cudaFuncSetAttribute(k_guide_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    int nb = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_guide_infer, 256, smem);
-    k_guide_infer<<<sms * (nb > 0 ? nb : 1), 256, smem, s>>>(a);
-    return cudaGetLastError();
-}
 cudaError_t launch_guide_collect(const WaveArgs& a, int sms, cudaStream_t s) {
     k_guide_collect<<<sms * 8, 256, 0, s>>>(a);
     return cudaGetLastError();
@@ -815,11 +697,9 @@ cudaError_t guide_eval_launch(st_ctx* ctx, uint32_t n, float* d_raw, uint2* d_mi
     f3 lo;
     float inv_ext;
     guide_box(ctx, lo, inv_ext);
-    const size_t smem = (size_t)SW_FWD * 2;
-    cudaFuncSetAttribute(k_guide_eval, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    k_guide_eval<<<ctx_sms(ctx) * 2, 256, smem, st>>>(g.samp, n, lo, inv_ext, reinterpret_cast<const float2*>(g.param + GUIDE_NW),
-                                                     g.wbf, d_raw, d_mix);
-    return cudaGetLastError();
+    // the tensor cores' network (st_guide_tc.cu); the error word is the context's counters' (a wait that ran out)
+    return launch_guide_eval_tc(g.samp, n, lo, inv_ext, reinterpret_cast<const float2*>(g.param + GUIDE_NW), g.wbf,
+                                d_raw, d_mix, &ctx_counters(ctx)->errflag, ctx_sms(ctx), st);
 }
 
 int guide_grad(st_ctx* ctx, const float* pos, const float* nrm, const float* dir, const float* weight, uint32_t n,

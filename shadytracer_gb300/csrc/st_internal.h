@@ -250,6 +250,8 @@ cudaError_t launch_emit_reset(const EmitBufs& em, cudaStream_t s);
 // the learned proposal (st_guide.cu)
 cudaError_t launch_guide_infer(const WaveArgs& a, int sms, cudaStream_t s);
 cudaError_t launch_guide_collect(const WaveArgs& a, int sms, cudaStream_t s);
+cudaError_t launch_guide_eval_tc(const GuideSample* samp, uint32_t n, f3 lo, float inv_ext, const float2* table,
+                                 const uint16_t* wbf, float* raw, uint2* mix, uint32_t* err, int sms, cudaStream_t s);
 #endif  // __CUDACC_RTC__
 
 }  // namespace st

@@ -477,6 +477,35 @@ def sppm_caustic(width=1024, height=1024, photons=4_000_000, r1=0.005, alpha=0.7
     return s
 
 
+def caustic_mask(scene, centre=(0.0, 0.0, 0.3), radius=0.3, grow=1.25):
+    """The caustic's pixels: those whose centre's camera ray meets the floor (z = 0) before the sphere, at a point
+    whose line to the sun passes within grow x radius of the sphere's centre -- the sphere's shadow on the floor,
+    widened, where the glass focuses the sun. A boolean array of the picture's shape (row 0 the bottom)."""
+    import numpy as np
+    p, v = scene.params, scene.view
+    W, H = p.width, p.height
+    ux = (np.arange(W) + 0.5) / W
+    uy = (np.arange(H) + 0.5) / H
+    xx, yy = np.meshgrid(ux * 2 - 1, uy * 2 - 1)
+    R, U, F = (np.array(list(v.right)), np.array(list(v.up)), np.array(list(v.fwd)))
+    d = xx[..., None] * v.fx * R + yy[..., None] * v.fy * U - F
+    d /= np.linalg.norm(d, axis=-1, keepdims=True)
+    o = np.array(list(v.cam_pos))
+    c = np.array(centre)
+    t_floor = np.where(d[..., 2] < 0, -o[2] / np.minimum(d[..., 2], -1e-12), np.inf)
+    oc = o - c                                          # the sphere first?
+    b = (d * oc).sum(-1)
+    disc = b * b - (oc @ oc - radius * radius)
+    t_sph = np.where(disc > 0, -b - np.sqrt(np.maximum(disc, 0)), np.inf)
+    seen = np.isfinite(t_floor) & ((t_sph <= 0) | (t_floor < t_sph))
+    q = o + d * np.where(np.isfinite(t_floor), t_floor, 0)[..., None]
+    e, az = math.radians(p.sun_elevation), math.radians(p.sun_azimuth)
+    sun = np.array([math.cos(e) * math.sin(az), math.cos(e) * math.cos(az), math.sin(e)])
+    w = q - c                                           # the line q + t sun's nearest approach to the centre
+    dist2 = (w * w).sum(-1) - ((w * sun).sum(-1)) ** 2
+    return seen & (dist2 <= (grow * radius) ** 2)
+
+
 def sppm_pane(width=48, height=48, photons=400_000, r1=0.02, alpha=0.7, sun_elevation=60.0, ior=1.5, seed=1,
               pane_half=1.0, photon_half=1.6, vfov=12.0):
     """The photon map's closed form: a clear pane (2 x 2 m, 2 cm thick, index `ior`) 0.5 m over a white-ish floor

@@ -183,7 +183,7 @@ def test_the_detector_map(detector_run):
     mine = hits[hits[:, 8] == 0]
     m = detector_map(mine[:, :3], mine[:, 3], cells=32)
     assert abs(abs(m["frame"]["normal"][2]) - 1) < 1e-9          # squared up to the world: a floor
-    assert m["total"] == pytest.approx(float(mine[:, 3].sum()), rel=1e-9)
+    assert m["total"] == pytest.approx(float(mine[:, 3].astype(np.float64).sum()), rel=1e-9)
     cell_area = m["cell_m"] ** 2
     assert (m["E"] * cell_area).sum() == pytest.approx(m["total"], rel=1e-9)
     for sm in ("gauss", "epan"):
