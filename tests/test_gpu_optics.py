@@ -193,3 +193,27 @@ def test_the_detector_map(detector_run):
     dense = m["count"] > 200
     assert dense.any()
     assert abs(np.median(mk["E"][dense] / m["E"][dense]) - 1) < 0.1
+
+
+def test_the_plane_crossing_tally_is_the_far_fields_virtual_plane_for_a_small_luminaire():
+    """Two estimators of the lux plane: the trace's own (each escaping ray's line met at the plane, FP64 tally) and the
+    reference's (optics/illum.js virtualPlane: the far field's intensity, the luminaire a point, E = I cos^3 / h^2).
+    They agree where the luminaire is small against the distance -- a 6 mm lens at 1 m -- up to the far field's
+    binning and the noise of both."""
+    from shadytracer_gb300.renderer import create_path_tracer
+    from shadytracer_gb300.optics import Optics, intensity, virtual_plane, lux
+    b = scenes.optics_bench(n_instances=1, seed=9)
+    n = 4_000_000
+    with create_path_tracer(b, device=0) as rt:
+        O = Optics(rt)
+        O.set_sources(b.info["sources"])
+        O.set_far(nC=360, nG=181)
+        g = O.run([n], lux_cells=32, lux_half=1.0, lux_height=1.0, maxbounce=32, seed=2)
+    scale = 1.0 / n                                                   # a unit of weight: 1 lm over n rays (flux 1)
+    E_tally = lux(g["lux"][0], 32, 1.0, scale)
+    E_far = virtual_plane(intensity(g["far"][0], 360, 181, scale), 360, 181, h=1.0, half=1.0, cells=32)
+    lit = E_tally > 0.05 * E_tally.max()
+    assert lit.sum() > 50
+    ratio = E_far[lit] / E_tally[lit]
+    assert abs(np.median(ratio) - 1) < 0.03, np.median(ratio)
+    assert np.mean(np.abs(ratio - 1) < 0.15) > 0.9
