@@ -329,6 +329,19 @@ int  st_sync(st_ctx* ctx, int timeout_ms);    /* wait for the queued samples; <0
  * st_invalidate before trusting the picture again. arm_only 1 is the test of that path: the waits are armed but no
  * copy is issued, so each runs out at its limit with nothing in flight. Kept until changed. */
 int  st_set_wait_limit(st_ctx* ctx, uint32_t iterations, int arm_only);
+/* THE AUTOTUNER (the batching's tile sizes and march-step caps, picked on the workload itself): each pair of the march's
+ * and the occlusion pass's queue tile -- the entries a warp claims at a time, 32, 64 or 128 -- and march chunk -- the
+ * scene evaluations a ray takes a launch before it waits for the next iteration, 24 to 160 -- timed over `samples`
+ * samples of the scene, settings and view in force; the fastest is kept for the renders that follow and returned, with
+ * its time and the defaults' (64, 48). The accumulation is cleared. The picture does not depend on either. */
+typedef struct st_tune {
+    uint32_t claim;               /* queue entries a warp claims at a time (0: 64)                   */
+    uint32_t chunk;               /* evaluations a ray takes a launch (0: 48)                        */
+    float    ms;                  /* the pick's time for the tuning samples                           */
+    float    ms_default;          /* the defaults' time                                               */
+} st_tune;
+int  st_autotune(st_ctx* ctx, int samples, st_tune* out);
+int  st_set_tune(st_ctx* ctx, const st_tune* t);    /* set them (claim, chunk; 0 the defaults)       */
 
 /* ---- readings (caller-owned buffers, width*height entries each; NULL skips one) ---- */
 int  st_read_accum(st_ctx* ctx, double* rgb, double* V, double* S, uint32_t* count);
@@ -446,6 +459,9 @@ int  st_optics_set_rays(st_ctx* ctx, const float* rays, uint32_t n);
 int  st_optics_run(st_ctx* ctx, const st_optics_batch* batch, double* far, double* lux,
                    st_optics_totals* totals);
 int  st_optics_set_detail(st_ctx* ctx, const st_optics_detail* detail);
+/* the optics autotuner: the batch run with each queue tile and march chunk of st_autotune's candidates, the fastest
+ * kept for the runs that follow (st_tune as st_autotune returns it); the tallies are the last run's */
+int  st_optics_autotune(st_ctx* ctx, const st_optics_batch* batch, st_tune* out);
 /* THE LAST RUN'S TALLIES BY OBJECT AND BY MATERIAL (optics/kernels.js:651-681, O_TAG and O_MAT): per tag -- an item
  * of the table, by its first primitive's index, 256 of them -- and per (instance, material) the weight incident, the
  * weight leaving and the interactions, 3 doubles each; tags 256 x 3, mats n_instances x n_materials x 3 (NULL skips) */
@@ -518,7 +534,8 @@ int  st_render_noalloc(int device, const st_scene_desc* desc, const st_params* p
 /* ---- the binding's checks ---- */
 /* The sizes of the structs above as this library was built (st_prim, st_material, st_scene_desc, st_params,
  * st_view, st_counters_t, st_image_stats_t, st_kernel_time, st_sppm_stats, st_optics_source, st_optics_far,
- * st_optics_batch, st_optics_totals, st_mlp_stats, st_light, st_optics_detail, in that order); returns how many it has. */
+ * st_optics_batch, st_optics_totals, st_mlp_stats, st_light, st_optics_detail, st_tune, in that order); returns how many
+ * it has. */
 int  st_struct_sizes(uint32_t* out, int max);
 /* The context's CUDA stream (a cudaStream_t), for a host that orders or times its own work against it. */
 void* st_stream(st_ctx* ctx);

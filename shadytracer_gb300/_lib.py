@@ -32,6 +32,8 @@ SIGNATURES = {
     "st_step_async": ([P, C.c_int], C.c_int),
     "st_sync": ([P, C.c_int], C.c_int),
     "st_set_wait_limit": ([P, C.c_uint32, C.c_int], C.c_int),
+    "st_autotune": ([P, C.c_int, C.POINTER(T.StTune)], C.c_int),
+    "st_set_tune": ([P, C.POINTER(T.StTune)], C.c_int),
     "st_read_accum": ([P, P, P, P, P], C.c_int),
     "st_image_stats": ([P, C.POINTER(T.StImageStats)], C.c_int),
     "st_read_counters": ([P, C.POINTER(T.StCounters)], C.c_int),
@@ -48,6 +50,7 @@ SIGNATURES = {
     "st_optics_set_far": ([P, C.POINTER(T.StOpticsFar)], C.c_int),
     "st_optics_run": ([P, C.POINTER(T.StOpticsBatch), P, P, C.POINTER(T.StOpticsTotals)], C.c_int),
     "st_optics_set_detail": ([P, C.POINTER(T.StOpticsDetail)], C.c_int),
+    "st_optics_autotune": ([P, C.POINTER(T.StOpticsBatch), C.POINTER(T.StTune)], C.c_int),
     "st_optics_tallies": ([P, P, P], C.c_int),
     "st_optics_hits": ([P, P, C.c_uint32, C.POINTER(C.c_uint32)], C.c_int),
     "st_optics_paths": ([P, P, P], C.c_int),
@@ -68,7 +71,7 @@ SIGNATURES = {
 
 STRUCT_ORDER = [T.StPrim, T.StMaterial, T.StSceneDesc, T.StParams, T.StView, T.StCounters, T.StImageStats,
                 T.StKernelTime, T.StSppmStats, T.StOpticsSource, T.StOpticsFar, T.StOpticsBatch, T.StOpticsTotals,
-                T.StMlpStats, T.StLight, T.StOpticsDetail]
+                T.StMlpStats, T.StLight, T.StOpticsDetail, T.StTune]
 
 
 def load(path=None):

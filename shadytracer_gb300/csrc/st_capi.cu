@@ -90,6 +90,7 @@ struct st_ctx {
     StExt ext;   // the photon map's and the optics bench's state (st_sppm.cu, st_optics.cu)
     SceneCode code;                       // the scene as compiled code (st_scene_rtc.cu), when it was given as code
     bool has_code = false;
+    uint32_t tune_claim = 0, tune_chunk = 0;   // the autotuner's picks (st_autotune); 0, the defaults
 };
 
 static int fail(st_ctx* c, int code, const std::string& msg) {
@@ -232,6 +233,8 @@ static Uni make_uni(const st_ctx* ctx) {
     const st_params& p = ctx->params;
     Uni u = make_uni_base(ctx->desc, p, ctx->view, (uint32_t)ctx->prims.size(), (uint32_t)ctx->mats.size(),
                           ctx->d_envimg != nullptr);
+    u.claim = ctx->tune_claim;
+    u.chunk = ctx->tune_chunk;
     if (ctx->d_envimg) {
         u.env_img = ctx->d_envimg; u.env_w = ctx->env_w; u.env_h = ctx->env_h;
         u.env_lum = ctx->env_lum; u.env_turn = ctx->env_turn;
@@ -1146,6 +1149,61 @@ int st_mf_tables(st_ctx* ctx, float* ec, float* ecavg, float* e1) {
 }
 
 // the struct sizes this library was built with, for the host's bindings to check theirs against
+// THE AUTOTUNER: each (queue tile, march chunk) pair of the candidates timed over `samples` samples of the scene, view
+// and settings in force (CUDA events on the context's stream, each after one untimed sample that records its graph),
+// the fastest kept for the renders that follow; the accumulation is cleared after
+int st_autotune(st_ctx* ctx, int samples, st_tune* out) {
+    if (!ctx || samples <= 0) return ST_ERR_ARG;
+    if (!ctx->has_scene || !ctx->has_params || !ctx->has_view)
+        return fail(ctx, ST_ERR_STATE, "set a scene, the settings and the view first");
+    if (ctx->in_flight) return fail(ctx, ST_ERR_BUSY, "a trace is in flight: st_sync first");
+    static const uint32_t claims[] = {32u, 64u, 128u};
+    static const uint32_t chunks[] = {24u, 32u, 48u, 64u, 96u, 160u};
+    cudaSetDevice(ctx->device);
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0), "event");
+    CK(cudaEventCreate(&e1), "event");
+    float best = 1e30f, base = 0.f;
+    uint32_t bc = CLAIM, bk = MARCH_CHUNK;
+    int rc = ST_OK;
+    for (uint32_t cl : claims) {
+        for (uint32_t ch : chunks) {
+            ctx->tune_claim = cl;
+            ctx->tune_chunk = ch;
+            invalidate_graph(ctx);
+            if ((rc = st_step(ctx, 1))) break;               // the graph recorded, caches warm
+            cudaEventRecord(e0, ctx->stream);
+            if ((rc = st_step_async(ctx, samples))) break;
+            cudaEventRecord(e1, ctx->stream);
+            if ((rc = st_sync(ctx, -1))) break;
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, e0, e1);
+            if (cl == CLAIM && ch == MARCH_CHUNK) base = ms;
+            if (ms < best) { best = ms; bc = cl; bk = ch; }
+        }
+        if (rc) break;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    ctx->tune_claim = rc ? 0u : bc;
+    ctx->tune_chunk = rc ? 0u : bk;
+    invalidate_graph(ctx);
+    if (rc) return rc;
+    if (out) { out->claim = bc; out->chunk = bk; out->ms = best; out->ms_default = base; }
+    return st_invalidate(ctx);
+}
+
+int st_set_tune(st_ctx* ctx, const st_tune* t) {
+    if (!ctx || !t) return ST_ERR_ARG;
+    if (ctx->in_flight) return fail(ctx, ST_ERR_BUSY, "a trace is in flight: st_sync first");
+    if (t->claim > 1024u || (t->chunk && t->chunk < 4u) || t->chunk > 4096u)
+        return fail(ctx, ST_ERR_ARG, "tune out of range (claim <= 1024, chunk 4..4096, 0 the defaults)");
+    ctx->tune_claim = t->claim;
+    ctx->tune_chunk = t->chunk;
+    invalidate_graph(ctx);
+    return ST_OK;
+}
+
 int st_scene_code_info(st_ctx* ctx, int* is_code, double* compile_ms, uint64_t* cubin_bytes) {
     if (!ctx) return ST_ERR_ARG;
     if (is_code) *is_code = ctx->has_code ? 1 : 0;
@@ -1161,7 +1219,7 @@ int st_struct_sizes(uint32_t* out, int max) {
                           (uint32_t)sizeof(st_sppm_stats), (uint32_t)sizeof(st_optics_source),
                           (uint32_t)sizeof(st_optics_far), (uint32_t)sizeof(st_optics_batch),
                           (uint32_t)sizeof(st_optics_totals), (uint32_t)sizeof(st_mlp_stats),
-                          (uint32_t)sizeof(st_light), (uint32_t)sizeof(st_optics_detail)};
+                          (uint32_t)sizeof(st_light), (uint32_t)sizeof(st_optics_detail), (uint32_t)sizeof(st_tune)};
     int n = (int)(sizeof(s) / sizeof(s[0]));
     for (int i = 0; i < n && i < max; i++) out[i] = s[i];
     return n;

@@ -116,6 +116,9 @@ struct Uni {
     // the sample sequence
     uint32_t seed, maxaverages, n_prims, n_mats;
     uint32_t count_work;         // a counting pass: the march counts its fold's work (WC_*)
+    // the autotuner's picks (st_autotune): queue entries a warp claims at a time in the march and the occlusion pass,
+    // and the evaluations a ray takes a launch before it waits for the next iteration; 0, the defaults
+    uint32_t claim, chunk;
     // the march queue's space order (st_render.cu k_sort_*): a SORT_G^3 grid over the primitives' bounds
     uint32_t sort_on; f3 glo, ginv;
     // the photon map (st_photons.cu): photons a sample, the sun photons' square, the radius schedule, the budget

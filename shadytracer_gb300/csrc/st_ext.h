@@ -54,6 +54,7 @@ struct OpticsState {
     st_optics_detail detail{};   // what a run keeps beyond its tallies (hits, paths)
     uint64_t sources_gen = 0;    // the sources' and the ray table's changes (a batch's graph is recorded with them)
     uint64_t launches = 0;       // kernels the batches' graphs ran
+    uint32_t tune_claim = 0, tune_chunk = 0;   // the optics autotuner's picks (st_optics_autotune); 0, the defaults
     void* scratch = nullptr;     // the run's device buffers (st_optics.cu OptBuf), grown as needed
 };
 

@@ -33,6 +33,7 @@ namespace st {
 #define SORT_BUCKETS (SORT_G * SORT_G * SORT_G * 8u)   // ... x 8 direction octants
 #define SORT_MIN_PRIMS 8u                 // scenes of fewer primitives march their queues unsorted
 #define MARCH_CHUNK 48u
+#define CLAIM 64u                         // queue entries a warp of the march or the occlusion pass claims at a time
 
 // meta.y: the bounces (bits 0-7), the path's segment -- its shades so far, which its random numbers are seeded by
 // (bits 8-15) -- and the state (bits 16-23)

@@ -7,7 +7,6 @@ namespace st {
 
 #define FULL_MASK 0xffffffffu
 #define INVALID_SLOT 0xffffffffu
-#define CLAIM 64u
 #define WAIT_LIMIT (1u << 24)
 
 __device__ __forceinline__ uint32_t lanemask_lt() {

@@ -683,7 +683,10 @@ int st_optics_run(st_ctx* ctx, const st_optics_batch* b, double* far_out, double
     u.maxiter = 400;
     u.nee = 0; u.rr = 0;
     u.stepscale = 0.9f;
-    u.budget = u.maxbounce + 1 + (u.maxiter + MARCH_CHUNK - 1) / MARCH_CHUNK + 4;
+    u.claim = os.tune_claim;
+    u.chunk = os.tune_chunk;
+    const uint32_t chunk = u.chunk ? u.chunk : MARCH_CHUNK;
+    u.budget = u.maxbounce + 1 + (u.maxiter + chunk - 1) / chunk + 4;
     double tol = sd.tolerance > 0 ? sd.tolerance : 1e-3;
     double R = sd.env_radius > 0 ? sd.env_radius : 400.0;
     u.tol = (float)tol; u.envR = (float)R; u.envR2 = (float)(R * R);
@@ -765,7 +768,8 @@ int st_optics_run(st_ctx* ctx, const st_optics_batch* b, double* far_out, double
                                  (uint64_t)(uintptr_t)B.wfirst, (uint64_t)(uintptr_t)B.src, os.sources_gen,
                                  (uint64_t)(uintptr_t)os.rays, D.det_cap, D.path_rays, D.path_verts,
                                  (uint64_t)__float_as_uint_host(o.esc_len), F.nC, F.nG,
-                                 (uint64_t)__float_as_uint_host(b->lux_half), (uint64_t)__float_as_uint_host(b->lux_height)};
+                                 (uint64_t)__float_as_uint_host(b->lux_half), (uint64_t)__float_as_uint_host(b->lux_height),
+                                 u.claim, u.chunk};
     for (int k = 0; k < 3; k++) {
         key.push_back(__float_as_uint_host(F.axis[k]));
         key.push_back(__float_as_uint_host(F.c0[k]));
@@ -818,6 +822,45 @@ int st_optics_run(st_ctx* ctx, const st_optics_batch* b, double* far_out, double
             totals[i].n_escaped = n(i, T_NESC); totals[i].n_lost = n(i, T_NLOST);
             totals[i].n_detected = n(i, T_NDET); totals[i].n_absorbed = n(i, T_NABS);
         }
+    return ST_OK;
+}
+
+// THE OPTICS AUTOTUNER: the batch run with each (queue tile, march chunk) pair of the candidates (its graph recorded by
+// one untimed run, then one timed: CUDA events on the context's stream), the fastest kept for the runs that follow
+int st_optics_autotune(st_ctx* ctx, const st_optics_batch* b, st_tune* out) {
+    if (!ctx || !b) return ST_ERR_ARG;
+    OpticsState& os = ctx_ext(ctx).optics;
+    static const uint32_t claims[] = {32u, 64u, 128u};
+    static const uint32_t chunks[] = {24u, 32u, 48u, 64u, 96u, 160u};
+    cudaSetDevice(ctx_device(ctx));
+    cudaStream_t st = ctx_stream(ctx);
+    cudaEvent_t e0, e1;
+    if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) return ST_ERR_CUDA;
+    float best = 1e30f, base = 0.f;
+    uint32_t bc = CLAIM, bk = MARCH_CHUNK;
+    int rc = ST_OK;
+    for (uint32_t cl : claims) {
+        for (uint32_t ch : chunks) {
+            os.tune_claim = cl;
+            os.tune_chunk = ch;
+            if ((rc = st_optics_run(ctx, b, nullptr, nullptr, nullptr))) break;     // records the graph
+            cudaEventRecord(e0, st);
+            if ((rc = st_optics_run(ctx, b, nullptr, nullptr, nullptr))) break;
+            cudaEventRecord(e1, st);
+            cudaEventSynchronize(e1);
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, e0, e1);
+            if (cl == CLAIM && ch == MARCH_CHUNK) base = ms;
+            if (ms < best) { best = ms; bc = cl; bk = ch; }
+        }
+        if (rc) break;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    os.tune_claim = rc ? 0u : bc;
+    os.tune_chunk = rc ? 0u : bk;
+    if (rc) return rc;
+    if (out) { out->claim = bc; out->chunk = bk; out->ms = best; out->ms_default = base; }
     return ST_OK;
 }
 

@@ -36,7 +36,8 @@ struct TableScene {
 
 // ------------------------------------------------------------------------------------------------------------
 // THE MARCH (wavefront.js:834-1005): persistent -- a few CTAs an SM whose warps claim CLAIM queue entries at a time
-// and refill a lane the moment its ray ends; a ray marches at most MARCH_CHUNK evaluations a launch (the last
+// (the autotuner's claim) and refill a lane the moment its ray ends; a ray marches at most MARCH_CHUNK evaluations (the
+// autotuner's chunk) a launch (the last
 // iteration's launch to its end) and goes to the hit queue or the next iteration's march queue.
 // ------------------------------------------------------------------------------------------------------------
 template <class SC, bool HAZE, bool INST, bool COUNT>
@@ -55,7 +56,8 @@ __global__ void __launch_bounds__(256, 4) k_march(WaveArgs a, int cur, int nxt, 
     uint32_t* outc = nxt ? &a.ctr->rayCount[1] : &a.ctr->rayCount[0];
     const float tol = a.u.tol, stepscale = a.u.stepscale, envR2 = a.u.envR2;
     const uint32_t maxiter = a.u.maxiter;
-    const uint32_t chunk = last ? 0xffffffffu : MARCH_CHUNK;
+    const uint32_t chunk = last ? 0xffffffffu : (a.u.chunk ? a.u.chunk : MARCH_CHUNK);
+    const uint32_t claim = a.u.claim ? a.u.claim : CLAIM;
     const int lane = threadIdx.x & 31;
 
     uint32_t slot = INVALID_SLOT;
@@ -73,10 +75,10 @@ __global__ void __launch_bounds__(256, 4) k_march(WaveArgs a, int cur, int nxt, 
         if (idle && !exhausted) {
             if (wpos >= wend) {
                 uint32_t b = 0;
-                if (lane == 0) b = atomicAdd(&a.ctr->marchHead, CLAIM);
+                if (lane == 0) b = atomicAdd(&a.ctr->marchHead, claim);
                 b = __shfl_sync(FULL_MASK, b, 0);
                 if (b >= count) exhausted = true;
-                else { wpos = b; wend = min(b + CLAIM, count); }
+                else { wpos = b; wend = min(b + claim, count); }
             }
             if (!exhausted) {
                 uint32_t avail = wend - wpos;
@@ -263,7 +265,8 @@ __global__ void __launch_bounds__(256, 4) k_occlude(WaveArgs a, int last) {
     uint32_t* o_cnt = side ? &a.ctr->shadowCount[0] : &a.ctr->shadowCount[1];
     const float tol = a.u.tol, stepscale = a.u.stepscale, envR2 = a.u.envR2;
     const uint32_t maxiter = a.u.maxiter;
-    const uint32_t chunk = last ? 0xffffffffu : MARCH_CHUNK;
+    const uint32_t chunk = last ? 0xffffffffu : (a.u.chunk ? a.u.chunk : MARCH_CHUNK);
+    const uint32_t claim = a.u.claim ? a.u.claim : CLAIM;
     const int lane = threadIdx.x & 31;
     uint32_t idx = INVALID_SLOT;
     f3 pos = mk(0.f), dir = mk(0.f);
@@ -278,10 +281,10 @@ __global__ void __launch_bounds__(256, 4) k_occlude(WaveArgs a, int last) {
         if (idle && !exhausted) {
             if (wpos >= wend) {
                 uint32_t b = 0;
-                if (lane == 0) b = atomicAdd(&a.ctr->occHead, CLAIM);
+                if (lane == 0) b = atomicAdd(&a.ctr->occHead, claim);
                 b = __shfl_sync(FULL_MASK, b, 0);
                 if (b >= count) exhausted = true;
-                else { wpos = b; wend = min(b + CLAIM, count); }
+                else { wpos = b; wend = min(b + claim, count); }
             }
             if (!exhausted) {
                 uint32_t avail = wend - wpos;

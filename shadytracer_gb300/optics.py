@@ -70,6 +70,20 @@ class Optics:
         self.n_instances = n
         return {"far": far, "lux": lux, "totals": totals}
 
+    def autotune(self, ray_counts, lux_cells=512, lux_half=1.0, lux_height=1.0, maxbounce=32, seed=1):
+        """The optics autotuner (st_optics_autotune): the batch run with each queue tile and march chunk, the fastest
+        kept for the runs that follow. Returns {claim, chunk, ms, ms_default}."""
+        n = len(ray_counts)
+        rc = (C.c_uint32 * n)(*[int(x) for x in ray_counts])
+        b = T.StOpticsBatch()
+        b.n_instances = n
+        b.ray_count = C.cast(rc, C.POINTER(C.c_uint32))
+        b.lux_cells, b.lux_half, b.lux_height = lux_cells, lux_half, lux_height
+        b.maxbounce, b.seed = maxbounce, seed
+        t = T.StTune()
+        check(self.L.st_optics_autotune(self.rt.ctx, C.byref(b), C.byref(t)), self.rt.ctx, "st_optics_autotune")
+        return {f: getattr(t, f) for f, _ in T.StTune._fields_}
+
     def set_detail(self, det_cap=0, path_rays=0, path_verts=0, esc_len=0.0):
         """What a run keeps beyond its tallies (st_optics_set_detail): up to det_cap detector hits, and the paths of
         each instance's first path_rays rays, path_verts vertices each, an escaped ray's last esc_len metres on."""

@@ -71,6 +71,13 @@ class PathTracer:
         self.code = code
         return self.scene_code_info()["compile_ms"]
 
+    def autotune(self, samples=2):
+        """The autotuner (st_autotune): the queue tile and march chunk timed on this scene and view, the fastest kept.
+        Returns {claim, chunk, ms, ms_default}."""
+        t = T.StTune()
+        check(self.L.st_autotune(self.ctx, int(samples), C.byref(t)), self.ctx, "st_autotune")
+        return {f: getattr(t, f) for f, _ in T.StTune._fields_}
+
     def scene_code_info(self):
         is_code, ms, nbytes = C.c_int(), C.c_double(), C.c_uint64()
         check(self.L.st_scene_code_info(self.ctx, C.byref(is_code), C.byref(ms), C.byref(nbytes)), self.ctx,

@@ -139,6 +139,10 @@ class StOpticsTotals(C.Structure):
                 ("n_absorbed", C.c_uint64)]
 
 
+class StTune(C.Structure):
+    _fields_ = [("claim", C.c_uint32), ("chunk", C.c_uint32), ("ms", C.c_float), ("ms_default", C.c_float)]
+
+
 class StOpticsDetail(C.Structure):
     _fields_ = [("det_cap", C.c_uint32), ("path_rays", C.c_uint32), ("path_verts", C.c_uint32),
                 ("esc_len", C.c_float)]
