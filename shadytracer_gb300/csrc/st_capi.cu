@@ -235,6 +235,10 @@ static Uni make_uni(const st_ctx* ctx) {
                           ctx->d_envimg != nullptr);
     u.claim = ctx->tune_claim;
     u.chunk = ctx->tune_chunk;
+    // the worst case counted in chunks of at most 32 (the reference's dispatches): a tuned chunk below that gets the
+    // iterations its longer marches need
+    if (!p.budget && u.chunk && u.chunk < 32u)
+        u.budget = std::max(2u, p.maxbounce + 1 + (p.maxiter + u.chunk - 1) / u.chunk);
     if (ctx->d_envimg) {
         u.env_img = ctx->d_envimg; u.env_w = ctx->env_w; u.env_h = ctx->env_h;
         u.env_lum = ctx->env_lum; u.env_turn = ctx->env_turn;

@@ -1,7 +1,9 @@
 """The autotuner (st_autotune, st_optics_autotune): the march's and the occlusion pass's queue tile and march chunk,
 timed on the workload itself, the fastest kept. What it picks changes which rays share a warp and where a ray's march
-is cut between iterations -- never a ray's own path, which is seeded by the path -- so the picture and the tallies are
-the defaults' up to the order of f32 deposits."""
+is cut between iterations -- never a ray's own random numbers, which are seeded by the path. A path the wavefront's
+last iteration still finds going is ended there (the flush), and how many iterations a long march spends depends on
+the chunk, so a few paths end differently: the picture is the defaults' pixel for pixel on nearly every pixel and
+within the error bars on all. The optics tallies are integers and its rays run to their ends: the same bits."""
 import numpy as np
 import pytest
 
@@ -23,8 +25,24 @@ def test_the_tuned_render_is_the_defaults_picture():
         rt.step(4)
         got = rt.read_accum()
     assert np.array_equal(got[3], ref[3])
+    same_within_error(got, ref)
+
+
+def se_of(V, S):
+    ok = (S > 0) & (S < 1)
+    out = np.zeros_like(V)
+    out[ok] = np.sqrt(S[ok] * V[ok] / (1 - S[ok]))
+    return out
+
+
+def same_within_error(got, ref):
     L, Lr = got[0] @ LUMA, ref[0] @ LUMA
-    assert np.allclose(L, Lr, rtol=1e-4, atol=1e-6 * Lr.max())
+    exact = np.abs(L - Lr) <= 1e-4 * np.maximum(np.abs(Lr), 1.0)
+    assert exact.mean() > 0.98, exact.mean()
+    sd = np.hypot(se_of(got[1], got[2]), se_of(ref[1], ref[2]))
+    ok = sd > 0
+    assert np.mean(np.abs((L - Lr)[ok]) <= 4 * sd[ok] + 1e-4 * np.abs(Lr[ok])) > 0.995
+    assert abs(L.mean() / Lr.mean() - 1) < 0.01
 
 
 def test_a_set_tune_of_extremes_keeps_the_picture():
@@ -41,8 +59,7 @@ def test_a_set_tune_of_extremes_keeps_the_picture():
         rt.invalidate()
         rt.step(2)
         got = rt.read_accum()
-    L, Lr = got[0] @ LUMA, ref[0] @ LUMA
-    assert np.allclose(L, Lr, rtol=1e-4, atol=1e-6 * Lr.max())
+    same_within_error(got, ref)
 
 
 def test_the_tuned_optics_batch_keeps_its_tallies():
