@@ -71,6 +71,7 @@ def parse():
     ap.add_argument("--no-haze", action="store_true", help="skip the haze-box beam's leg")
     ap.add_argument("--no-env", action="store_true", help="skip the environment image's leg")
     ap.add_argument("--no-sc", action="store_true", help="skip the step cache's leg")
+    ap.add_argument("--tune", default="", help="CLAIM,CHUNK: set by hand, no autotuner (profiling runs)")
     ap.add_argument("--leg", default="all", choices=["all", "sppm", "rmse", "caustic_rmse", "optics", "mlp", "emit",
                                                      "haze", "env", "sc"],
                     help="run one leg alone and print its JSON (profiling runs of the photon map or the optics bench)")
@@ -811,7 +812,12 @@ def run_ours(args):
     rt = create_path_tracer(s, device=dev, code=src)
     compile_ms = rt.scene_code_info()["compile_ms"]
     # the autotuner picks the queue tile and the march chunk on this workload (2 samples each candidate, untimed)
-    tune = rt.autotune(2)
+    if args.tune:
+        claim, chunk = (int(x) for x in args.tune.split(","))
+        rt.set_tune(claim, chunk)
+        tune = {"claim": claim, "chunk": chunk, "ms": 0.0, "ms_default": 0.0}
+    else:
+        tune = rt.autotune(2)
     stream = torch.cuda.ExternalStream(rt.stream(), device=torch.device("cuda", dev))
 
     def barrier():

@@ -221,6 +221,16 @@ typedef struct st_params {
      * inside it may cross to where it leaves with no distance evaluation, when that is at least a cell */
     uint32_t step_cache;          /* 0 off, 1 the ray's own cell, 2 also the two cells ahead              */
     float    step_cache_cells;    /* cells, millions (0.25..16; 0: 4)                                     */
+    /* LIGHT TRACING TO THE CAMERA (materials_pbr.js:672-830 ltConnect, wavefront.js:1292-1310, :1649-1661): the
+     * sun's photons, traced through glass and mirrors, connect to the camera where they first land on a surface in air
+     * that a connection can evaluate -- a shadow ray to the camera (through the thin lens at a point of its disc), and
+     * what reaches it is added to its pixel as it is, not averaged with the pixel's paths. The camera's paths then
+     * leave the class light -> delta+ -> D -> eye to the photons (a first vertex drawn from an evaluable lobe, delta
+     * events after it, the sun's disc where the photons' square covers the line); with the photon map on too, the
+     * map gathers only past delta events from the eye, as the reference splits the two. One sample a wave. */
+    uint32_t lt;                  /* 1 on (the reference's photoncount > 0)                          */
+    uint32_t lt_photons;          /* photons a sample with the photon map off (0: one a pixel); with it on, its
+                                   * sppm_photons serve both, and sppm_half is the photons' square either way */
 } st_params;
 
 /* The camera, as genrays reads it (core/genrays.js:65-92): the basis from invView's columns and the
@@ -390,6 +400,10 @@ int  st_sppm_stats_read(st_ctx* ctx, st_sppm_stats* out);
  * those stored (128^2 each, halved at every rebuild), and the CDF they are drawn from (128^2 conditional row entries,
  * then 128 rows). NULL skips one. ST_ERR_STATE before the photon map has run. */
 int  st_sppm_emission_map(st_ctx* ctx, uint32_t* sent, uint32_t* stored, float* cdf);
+/* LIGHT TRACING'S MAP OF CONNECTIONS (st_params.lt; the splat buffer's fourth word, wavefront.js:1656-1660): per pixel
+ * (W x H) the photons' connections that reached the camera since the last invalidate -- where light tracing lights
+ * the picture, and how densely. ST_ERR_STATE before a wave has run. */
+int  st_lt_counts(st_ctx* ctx, uint32_t* counts);
 
 /* ---- the optics bench (optics/index.js, optics/kernels.js) ---- */
 typedef struct st_optics_source {
@@ -524,7 +538,7 @@ int  st_emit_list(st_ctx* ctx, float* out, uint32_t max_n, uint32_t* n);
  * serialises them. The first call on a device does the set-up (the array's address, the albedo tables) and should
  * come before any stream capture. The caller's current device is as it was when the call returns. The result equals
  * st_step's for the same inputs. What this render does not carry is refused with ST_ERR_ARG, and
- * st_last_error(NULL) says why: light faces, st_params.sppm, st_params.guide, st_params.step_cache, and an emissive
+ * st_last_error(NULL) says why: light faces, st_params.sppm, st_params.lt, st_params.guide, st_params.step_cache, and an emissive
  * material unless st_params.emit_off is set (then both paths render it by the BSDF's hits alone). */
 #define ST_NOALLOC_MAX_PIXELS (128u * 128u)
 #define ST_NOALLOC_SCRATCH_BYTES (8u << 20)

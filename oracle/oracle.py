@@ -246,6 +246,7 @@ def _declare_extra(L):
         "sto_lt_build": ([P, P, P], None),
         "sto_optics_detail": ([C.c_uint32, P, P, P, P, C.c_uint32, C.POINTER(C.c_uint32)], C.c_int),
         "sto_last_lt": ([P, P, P], C.c_int),
+        "sto_last_lt_counts": ([P, C.c_uint32], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -313,6 +314,14 @@ def last_lt():
     if xlib().sto_last_lt(ptr(e), ptr(h), ptr(cdf)) != 0:
         raise RuntimeError("no render with the learned emission map has run")
     return e, h, cdf
+
+
+def last_lt_counts(width, height):
+    """Light tracing's connections that reached each pixel over the last render call, (height, width)."""
+    out = np.zeros(width * height, np.uint32)
+    if xlib().sto_last_lt_counts(ptr(out), width * height) != 0:
+        raise RuntimeError("no render of this size has run")
+    return out.reshape(height, width)
 
 
 def sppm_build(pos, power, nrm_oct, flags, cell):

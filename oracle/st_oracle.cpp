@@ -90,6 +90,12 @@ template <class T> struct Ctx {
     uint8_t face_of[ST_MAX_MATERIALS] = {};
     // the reference's bounding-box culling at the root (a timing mode: the CPU baseline does the reference's work)
     const std::vector<CullBox>* cull = nullptr;
+    // light tracing to the camera (materials_pbr.js ltConnect): on, the camera, the sample's splat buffer (rgb a
+    // pixel, added to the pixel as it is) and the connections that reached each pixel
+    bool lt = false;
+    const st_view* view = nullptr;
+    std::vector<double>* splat = nullptr;
+    std::vector<uint32_t>* ltcount = nullptr;
 };
 // the march's and the shadow rays' distance: the fold, or the reference's culled render copy of it
 template <class T> inline T march_dist(const Ctx<T>& C, const V3<T>& p) {
@@ -142,6 +148,7 @@ inline void lt_build(uint32_t* emit, uint32_t* hit, float* cdf) {
 }
 // the last render's learned emission map as it ended (photons sent, stored, the CDF), for the tests to read
 std::vector<uint32_t> g_lt_emit, g_lt_hit;
+std::vector<uint32_t> g_lt_count;               // light tracing's connections per pixel, over the last render call
 std::vector<float> g_lt_cdf;
 inline void lt_uniform(float* cdf) {
     for (uint32_t r = 0; r < LT_G; r++)
@@ -159,6 +166,8 @@ template <class T> struct Ray {
     uint32_t lens = 0;                      // a camera path's lens field (materials_pbr.js lensField): 1 delta only
                                             // since the eye, 2 at its D, 3 delta only since its D
     bool passed = false;                    // a photon that has passed a delta event (TAG_PASSED)
+    uint32_t cls = 0;                       // light tracing's class (CLS_CAND 1, CLS_SPEC 2): a first vertex drawn
+                                            // from an evaluable lobe, then delta events only
     uint32_t bounces, steps, state, pix;
 };
 
@@ -425,9 +434,10 @@ inline V3<T> sppm_gather_lobes(const Ctx<T>& C, const V3<T>& X, const V3<T>& nrm
 // evaluable one (the map gathers there: light -> delta+ -> D -> eye, the reference's light tracer's class, is the
 // map's in this build), else 0; 1 stays 1 through a delta and goes to 2 at an evaluable event; 2 or 3 go to 3
 // through a delta; anything else to 0
-inline uint32_t lens_step(uint32_t lens, uint32_t bounces, uint32_t ev) {
+// (with light tracing on, a D at the first surface is its class, and the reference's 0)
+inline uint32_t lens_step(uint32_t lens, uint32_t bounces, uint32_t ev, bool lt) {
     const bool delta = ev == EV_DELTA;
-    if (bounces == 1) return delta ? 1u : (ev == EV_EVAL ? 2u : 0u);     // a D at the eye's first surface: gathered
+    if (bounces == 1) return delta ? 1u : ((ev == EV_EVAL && !lt) ? 2u : 0u);   // a D at the eye's first surface
     if (lens == 1) return delta ? 1u : (ev == EV_EVAL ? 2u : 0u);
     return ((lens == 2 || lens == 3) && delta) ? 3u : 0u;
 }
@@ -477,7 +487,7 @@ inline void shade_hit(const Ctx<T>& C, Ray<T>& r, T dhit, Rng& rng, Rng& grng, b
     V3<T> emis(T(m.emissive[0]), T(m.emissive[1]), T(m.emissive[2]));
     // THE PHOTON MAP'S GATHER (wavefront.js:1196-1212), before the shading: a camera ray with delta events only since
     // the eye, on an evaluable surface, takes sum f Phi / (pi r^2) / n^2 into its radiance
-    if (C.sppm && (r.bounces == 0 || r.lens == 1) && !(max3(emis) > T(0)) && sppm_evaluable(m, true)) {
+    if (C.sppm && ((r.bounces == 0 && !C.lt) || r.lens == 1) && !(max3(emis) > T(0)) && sppm_evaluable(m, true)) {
         T n0g = r.n;
         Lobes<T> lg = make_lobes(nrm, -r.dir, m, n0g / std::max(T(m.ior), n0g), C.tb, T(m.transmission), T(m.specular),
                                  T(m.haze));
@@ -648,7 +658,11 @@ inline void shade_hit(const Ctx<T>& C, Ray<T>& r, T dhit, Rng& rng, Rng& grng, b
         r.n = nT;                                                                  // n(lambda) where it has one
         if (draw) { r.beta *= specW; r.lam = lamD; }
     }
-    if (C.sppm) r.lens = lens_step(r.lens, r.bounces, smp.ev);
+    if (C.sppm) r.lens = lens_step(r.lens, r.bounces, smp.ev, C.lt);
+    if (C.lt) {                                                                    // tracebasics.js:995-1011
+        if (r.bounces == 1) r.cls = smp.ev == EV_EVAL ? 1u : 0u;
+        else if (r.cls & 1u) r.cls = smp.ev == EV_DELTA ? 3u : 0u;
+    }
     if (max3(smp.w) <= T(0)) r.state = RAY_ABSORBED;
     bool misOut = C.p.nee != 0 && !last;
     if (misOut) {                                                                  // materials_pbr.js:1370-1395
@@ -882,8 +896,9 @@ void trace_path(const Ctx<T>& C, U4 sseed, uint32_t tile, const st_view& v, uint
         bool last = it + 1 == C.budget;
         st.segments++;
         if (r.state == RAY_ESCAPED) {                                              // wavefront.js:1292-1310
-            // a path the photon map owns (lens field 3) takes the sky but not the disc where the photons were drawn
-            bool owned = C.sppm && r.lens == 3 && sppm_covers(C, r.pos, r.dir);
+            // a path the photon map owns (lens field 3), or light tracing (its class), takes the sky but not the disc
+            // where the photons were drawn
+            bool owned = ((C.sppm && r.lens == 3) || (C.lt && r.cls == 3u)) && sppm_covers(C, r.pos, r.dir);
             r.rad += r.beta * (owned ? C.env.sky_only(r.dir) : C.env.radiance(r.dir)) * r.sunmis;
             break;
         }
@@ -895,6 +910,7 @@ void trace_path(const Ctx<T>& C, U4 sseed, uint32_t tile, const st_view& v, uint
             r.absLtot = r.ltot;                                                    // absorbAlong on arrival
             medium_vertex(C, r, rng, last, fr, st);
             r.lens = 0;                                                            // haze.js:539
+            r.cls = 0;
         } else {
             shade_hit(C, r, dh, rng, grng, last, fr, st);
         }
@@ -1049,6 +1065,96 @@ template <> const MfTables* tables<double>() {
 // sun, flux L_disc cos Omega / (N pdf_area); at each hit stored where it has passed delta events only, at least one,
 // on an evaluable surface within the cap, else bounced -- a delta lobe keeps it, anything else ends it
 struct PhotonRec { float pos[3], power[3]; uint32_t dir, nrm, flags; };
+const uint32_t LT_LENS_SALT = 0x4C54434Eu;      // a connection's point of the lens, from the photon's own stream
+
+// A PHOTON'S CONNECTION TO THE CAMERA (materials_pbr.js:672-830 ltConnect, :598-612 camFootprint, lens.js lensDisc,
+// lensImage), traced and splatted: from P (in air, nrm turned to the photon, arriving along din with flux phi) to the
+// camera, or a point of its lens drawn from the photon's stream, through the evaluable lobes; phi f G / A_px to the
+// pixel the line lands on, if the shadow ray -- started on the line of sight as far along it as lifts it 2 offsets
+// off the surface (at most 4 such lengths at grazing views, the rest along the normal, re-aimed), stopped that height
+// short of the camera -- gets there
+template <class T>
+void lt_connect(const Ctx<T>& C, const st_material& m, const V3<T>& P, const V3<T>& nrm, const V3<T>& din,
+                const V3<T>& phi, U4 ps, uint32_t id, uint32_t cell, Stats& st) {
+    const st_view& vw = *C.view;
+    const V3<T> right(T(vw.right[0]), T(vw.right[1]), T(vw.right[2])), up(T(vw.up[0]), T(vw.up[1]), T(vw.up[2]));
+    const V3<T> fwd(T(vw.fwd[0]), T(vw.fwd[1]), T(vw.fwd[2])), cam0(T(vw.cam_pos[0]), T(vw.cam_pos[1]), T(vw.cam_pos[2]));
+    const T fx = T(vw.fx), fy = T(vw.fy), F = T(vw.focus_distance);
+    const uint32_t W = C.p.width, H = C.p.height;
+    V3<T> off(T(0));
+    const T R = vw.camtype == 0 ? T(vw.lens_radius) : T(0);
+    if (R > T(0)) {
+        Rng rl = path_rng(ps, id, LT_LENS_SALT);
+        T ul[4]; rl.next4(ul);
+        const T r = R * std::sqrt(ul[0]), ph = T(6.28318530718) * ul[1];
+        off = right * (r * std::cos(ph)) + up * (r * std::sin(ph));
+    }
+    if (lobes_none(m, T(m.transmission), T(m.haze))) return;
+    const V3<T> cam = cam0 + off, d = cam - P;
+    const T apx = T(4) * fx * fy / (T(W) * T(H));
+    V3<T> v;
+    T dist, xx, yy, G;
+    if (vw.camtype == 0) {
+        dist = length(d);
+        const T z = dot(d, fwd);
+        if (z <= T(1e-4) || dist <= T(1e-4)) return;
+        v = d / dist;
+        if (R > T(0)) {
+            const T c = dot(v, fwd);
+            const V3<T> Fp = off + (-v) * (F / std::max(c, T(1e-30)));
+            xx = dot(Fp, right) / (F * fx);
+            yy = dot(Fp, up) / (F * fy);
+        } else {
+            xx = -dot(d, right) / (z * fx);
+            yy = -dot(d, up) / (z * fy);
+        }
+        G = std::fabs(dot(nrm, v)) * dist / (z * z * z);
+    } else {
+        dist = dot(d, fwd);
+        if (dist <= T(1e-4)) return;
+        v = fwd;
+        xx = -dot(d, right) / fx;
+        yy = -dot(d, up) / fy;
+        G = std::fabs(dot(nrm, fwd));
+    }
+    if (std::fabs(xx) >= T(1) || std::fabs(yy) >= T(1)) return;
+    const T cv = dot(nrm, v);
+    if (cv <= T(0)) return;
+    Lobes<T> lb = make_lobes(nrm, v, m, T(1) / std::max(T(m.ior), T(1)), C.tb, T(m.transmission), T(m.specular), T(m.haze));
+    const V3<T> f = lobes_eval(lb, -din, T(0.05));
+    const V3<T> c = phi * f * (G / apx);
+    if (!(luma(c) > T(0))) return;
+    const T px = clampT((xx + T(1)) * T(0.5) * T(W), T(0), T(W) - T(1));
+    const T py = clampT((yy + T(1)) * T(0.5) * T(H), T(0), T(H) - T(1));
+    const uint32_t pix = (uint32_t)px + (uint32_t)py * W;
+    const T h = T(20) * march_tol(P, C.tol);
+    const bool grazing = cv < T(0.25);
+    const T sl = h / std::max(cv, T(0.25));
+    const T lift = grazing ? h - sl * cv : T(0);
+    V3<T> org = P + v * sl + nrm * lift, dir = v;
+    T len = dist - sl - cv * lift - h;
+    if (grazing && vw.camtype == 0) {
+        const V3<T> toCam = cam - org;
+        const T l = length(toCam);
+        dir = toCam / std::max(l, T(1e-30));
+        len = l - h;
+    }
+    if (!(len > T(0))) return;
+    if (C.sp_learn && cell < LT_N) {                                               // ltConnect's learn
+#pragma omp atomic
+        C.lt_hit[cell]++;
+    }
+    if (!occlude<T>(C, org, dir, T(1), st, nullptr, nullptr, true, -len)) return;
+    if (bad_deposit(c)) { st.nonfinite++; return; }
+#pragma omp atomic
+    (*C.splat)[pix * 3 + 0] += (double)c.x;
+#pragma omp atomic
+    (*C.splat)[pix * 3 + 1] += (double)c.y;
+#pragma omp atomic
+    (*C.splat)[pix * 3 + 2] += (double)c.z;
+#pragma omp atomic
+    (*C.ltcount)[pix]++;
+}
 template <class T>
 void trace_photon(const Ctx<T>& C, U4 ps, uint32_t id, uint32_t N, std::vector<PhotonRec>& out, Stats& st) {
     Rng r0 = path_rng(ps, id, PHOTON_GEN_SALT);
@@ -1109,9 +1215,12 @@ void trace_photon(const Ctx<T>& C, U4 ps, uint32_t id, uint32_t N, std::vector<P
         SceneHit<T> h = scene_eval(*C.s, r.pos);
         const st_material& m = C.s->materials[std::min(h.m, C.s->n_materials - 1)];
         if (std::max(std::max(m.emissive[0], m.emissive[1]), m.emissive[2]) > 0.f) break;
+        // light tracing: connected first, once it has passed a delta event, in air, within the bounce cap
+        if (C.lt && r.passed && std::fabs(r.n - T(1)) <= T(1e-3) && r.bounces + 1 <= C.p.maxbounce)
+            lt_connect(C, m, r.pos, nrm, r.dir, r.rad * r.beta, ps, id, cell, st);
         if (r.passed && sppm_evaluable(m, false)) {
             V3<T> pw = r.rad * r.beta;
-            if (r.bounces + 2 <= C.p.maxbounce && luma(pw) > T(0)) {                 // sppm.js sppmStores / sppmStore
+            if (C.sppm && r.bounces + 2 <= C.p.maxbounce && luma(pw) > T(0)) {       // sppm.js sppmStores / sppmStore
                 Rng rs = path_rng(ps, id, SPPM_STORE_SALT);
                 float us[4]; rs.next4(us);
                 uint32_t sub = std::min((uint32_t)(us[1] * (float)SPPM_SUBS), SPPM_SUBS - 1);
@@ -1124,7 +1233,7 @@ void trace_photon(const Ctx<T>& C, U4 ps, uint32_t id, uint32_t N, std::vector<P
                 rec.nrm = sppm_oct(nv);
                 rec.flags = (r.bounces + 1) | (sub << SPPM_SUB_SHIFT);
                 out.push_back(rec);
-                if (cell < LT_N) {
+                if (!C.lt && cell < LT_N) {                                        // (light tracing's connections teach it)
 #pragma omp atomic
                     C.lt_hit[cell]++;
                 }
@@ -1228,18 +1337,30 @@ static int render_impl(const st_scene_desc* s, const st_params* p, const st_view
     fr.cnt.assign(P, 0);
     // the photon map runs while it is set and the sun shines (its photons are the sun's)
     const bool sppm_on = p->sppm != 0 && C.env.sun_on && p->env_uniform <= 0.f;
-    const uint32_t NPH = p->sppm_photons ? p->sppm_photons : P;
+    // light tracing runs while it is set and the sun shines, with the same photons as the map's while it runs
+    const bool lt_on = p->lt != 0 && C.env.sun_on && p->env_uniform <= 0.f;
+    const uint32_t NPH = sppm_on ? (p->sppm_photons ? p->sppm_photons : P) : (p->lt_photons ? p->lt_photons : P);
     SppmGrid grid;
     if (sppm_on) {
         C.sppm = true;
         C.grid = &grid;
-        C.sp_half = p->sppm_half > 0.f ? p->sppm_half : std::min(15.f, (float)C.d.env_radius);
         C.sp_budget = 512;
+    }
+    if (sppm_on || lt_on) C.sp_half = p->sppm_half > 0.f ? p->sppm_half : std::min(15.f, (float)C.d.env_radius);
+    std::vector<double> splat;
+    std::vector<uint32_t>& ltcount = g_lt_count;
+    ltcount.assign(P, 0);
+    if (lt_on) {
+        C.lt = true;
+        C.view = v;
+        splat.assign((size_t)P * 3, 0.0);
+        C.splat = &splat;
+        C.ltcount = &ltcount;
     }
     std::vector<uint32_t> lt_emit(LT_N, 0), lt_hit(LT_N, 0);
     std::vector<float> lt_cdf(LT_N + LT_G);
     lt_uniform(lt_cdf.data());
-    C.sp_learn = sppm_on && p->sppm_learn != 0;
+    C.sp_learn = (sppm_on || lt_on) && p->sppm_learn != 0;
     C.lt_emit = lt_emit.data(); C.lt_hit = lt_hit.data(); C.lt_cdf = lt_cdf.data();
     // the emitter list, in a scene with an emissive material: a grid a thread, the merged grid, the list
     EmitList elist;
@@ -1270,9 +1391,11 @@ static int render_impl(const st_scene_desc* s, const st_params* p, const st_view
         }
         std::fill(fr.rgb.begin(), fr.rgb.end(), 0.0);
         std::fill(fr.cnt.begin(), fr.cnt.end(), 0u);
-        if (sppm_on) {
+        if (lt_on) std::fill(splat.begin(), splat.end(), 0.0);
+        if (sppm_on || lt_on) {
             // THE SAMPLE'S PHOTONS FIRST: the radius r_k (k = the sample's number from 1), the photons traced and
             // stored, the grid of cell 2 r_k built
+            // (light tracing alone: the photons and their connections, no records)
             const double r1 = p->sppm_r1 > 0.f ? p->sppm_r1 : 0.005, al = p->sppm_alpha > 0.f ? p->sppm_alpha : 2.0 / 3.0;
             const double rk = sppm_radius(r1, (int)(sample0 + si + 1), al);
             C.sp_r2 = (float)rk * (float)rk;
@@ -1300,8 +1423,10 @@ static int render_impl(const st_scene_desc* s, const st_params* p, const st_view
                     for (int k = 0; k < 3; k++) { pos.push_back(rr.pos[k]); pw.push_back(rr.power[k]); }
                     dirs.push_back(rr.dir); nrms.push_back(rr.nrm); flags.push_back(rr.flags);
                 }
-            sppm_build(grid, pos.data(), pw.data(), nrms.data(), flags.data(), (uint32_t)flags.size(), C.sp_cell);
-            grid.dir = dirs;
+            if (sppm_on) {
+                sppm_build(grid, pos.data(), pw.data(), nrms.data(), flags.data(), (uint32_t)flags.size(), C.sp_cell);
+                grid.dir = dirs;
+            }
         }
 #pragma omp parallel for schedule(dynamic, 64)
         for (long t = (long)path_first; t < (long)pend; t++) trace_path(C, sseed, (uint32_t)t, *v, W, H, fr, st);
@@ -1320,6 +1445,8 @@ static int render_impl(const st_scene_desc* s, const st_params* p, const st_view
             uint32_t n = fr.cnt[i];
             if (n == 0) continue;
             double s3[3] = {fr.rgb[i * 3] / n, fr.rgb[i * 3 + 1] / n, fr.rgb[i * 3 + 2] / n};
+            if (lt_on)                                 // light tracing's estimate, added as it is (wavefront.js:459-462)
+                for (int c = 0; c < 3; c++) s3[c] += splat[i * 3 + c];
             double prevn = p->maxaverages ? std::min<double>(acc_cnt[i], p->maxaverages) : double(acc_cnt[i]);
             double cnt = prevn + 1;
             acc_cnt[i] = (uint32_t)cnt;
@@ -1634,6 +1761,12 @@ double sto_sppm_radius(double r1, int k, double alpha) { return sppm_radius(r1, 
 // prog_lt_build on the given counts (halved in place) into cdf (LT_N + LT_G floats)
 void sto_lt_build(uint32_t* emit, uint32_t* hit, float* cdf) { lt_build(emit, hit, cdf); }
 // the last render's emission map (sent, stored: LT_N each; cdf LT_N + LT_G); 0, or -1 if none ran
+// light tracing's connections that reached each pixel over the last render call (n pixels)
+int sto_last_lt_counts(uint32_t* out, uint32_t n) {
+    if (g_lt_count.size() != n) return -1;
+    std::copy(g_lt_count.begin(), g_lt_count.end(), out);
+    return 0;
+}
 int sto_last_lt(uint32_t* emit, uint32_t* hit, float* cdf) {
     if (g_lt_cdf.empty()) return -1;
     std::copy(g_lt_emit.begin(), g_lt_emit.end(), emit);

@@ -46,6 +46,7 @@ SIGNATURES = {
     "st_sppm_gather": ([P, P, P, P, P, C.c_uint32, C.c_float, C.c_uint32, C.c_uint32, C.c_uint32, P], C.c_int),
     "st_sppm_stats_read": ([P, C.POINTER(T.StSppmStats)], C.c_int),
     "st_sppm_emission_map": ([P, P, P, P], C.c_int),
+    "st_lt_counts": ([P, P], C.c_int),
     "st_optics_set_sources": ([P, C.POINTER(T.StOpticsSource), C.c_uint32], C.c_int),
     "st_optics_set_far": ([P, C.POINTER(T.StOpticsFar)], C.c_int),
     "st_optics_run": ([P, C.POINTER(T.StOpticsBatch), P, P, C.POINTER(T.StOpticsTotals)], C.c_int),

@@ -65,6 +65,8 @@ struct st_ctx {
     Queues q{};
     DevCtr* d_ctr = nullptr;
     float4* d_frame = nullptr;
+    float4* d_splat = nullptr;            // light tracing's connections this sample, per pixel (rgb)
+    uint32_t* d_ltcount = nullptr;        // ...and the connections that reached each pixel since the last invalidate
     Acc4* d_acc = nullptr;
     double2* d_mom = nullptr;
     uint32_t samples = 0;
@@ -120,7 +122,7 @@ static void free_wave(st_ctx* ctx) {
                     ctx->q.hit, ctx->q.hitd, ctx->q.hsurf, ctx->q.sorted, ctx->q.skey, ctx->q.srank, ctx->q.bcnt,
                     ctx->q.boff, ctx->q.ssorted, ctx->q.sskey, ctx->q.ssrank, ctx->q.s_org[0], ctx->q.s_dir[0], ctx->q.s_rad[0], ctx->q.s_steps[0],
                     ctx->q.s_org[1], ctx->q.s_dir[1], ctx->q.s_rad[1], ctx->q.s_steps[1], ctx->d_frame,
-                    ctx->d_acc, ctx->d_mom};
+                    ctx->d_acc, ctx->d_mom, ctx->d_splat, ctx->d_ltcount};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     ctx->pb = PathBuf{};
@@ -128,6 +130,8 @@ static void free_wave(st_ctx* ctx) {
     ctx->d_frame = nullptr;
     ctx->d_acc = nullptr;
     ctx->d_mom = nullptr;
+    ctx->d_splat = nullptr;
+    ctx->d_ltcount = nullptr;
     ctx->slot_cap = 0;
     if (ctx->graph) { cudaGraphExecDestroy(ctx->graph); ctx->graph = nullptr; ctx->graph_w = 0; }
     if (ctx->graph2) { cudaGraphExecDestroy(ctx->graph2); ctx->graph2 = nullptr; ctx->graph2_w = 0; }
@@ -354,9 +358,11 @@ DPrim pack_prim(const st_prim& p) {
 }
 
 static bool sppm_runs(const st_ctx* ctx);
+static bool photons_run(const st_ctx* ctx);
 static uint32_t sppm_photons(const st_ctx* ctx);
 static uint32_t samples_per_wave(const st_ctx* ctx) {
-    if (sppm_runs(ctx)) return 1;            // the photon map: each sample its own photons, radius and grid
+    // the photon map or light tracing: each sample its own photons (and the map's radius and grid)
+    if (photons_run(ctx)) return 1;
     if (ctx->params.samples_per_wave) return ctx->params.samples_per_wave;
     const uint32_t target = 4u << 20;   // about four million paths a wave: twenty a lane of a full persistent grid
     uint32_t s = (target + ctx->P - 1) / ctx->P;
@@ -371,22 +377,23 @@ static bool has_emitters(const st_ctx* ctx) {
 }
 
 static int ensure_wave(st_ctx* ctx) {
-    if (sppm_runs(ctx)) {
-        int rc = sppm_ensure(ctx, sppm_photons(ctx));
+    if (photons_run(ctx)) {
+        // the map's records (light tracing alone stores none) and the emission map's counts
+        int rc = sppm_ensure(ctx, sppm_runs(ctx) ? sppm_photons(ctx) : 1024u);
         if (rc) return rc;
-        ctx_ext(ctx).sppm.wave = true;
+        if (sppm_runs(ctx)) ctx_ext(ctx).sppm.wave = true;
     }
     if (ctx->params.guide) {
         const uint32_t spw_g = samples_per_wave(ctx);
         uint32_t cap_g = spw_g * ctx->P;
-        if (sppm_runs(ctx)) cap_g = std::max(cap_g, std::min(sppm_photons(ctx), 4u << 20));
+        if (photons_run(ctx)) cap_g = std::max(cap_g, std::min(sppm_photons(ctx), 4u << 20));
         int rc = guide_ensure(ctx, cap_g, spw_g * ctx->P, ctx->params.guide_seed);
         if (rc) return rc;
     }
     uint32_t spw = samples_per_wave(ctx);
     uint32_t cap = spw * ctx->P;
-    // the photon map's photons run in chunks of the wave's slots: give them room for up to four million at once
-    if (sppm_runs(ctx)) cap = std::max(cap, std::min(sppm_photons(ctx), 4u << 20));
+    // the photons run in chunks of the wave's slots: give them room for up to four million at once
+    if (photons_run(ctx)) cap = std::max(cap, std::min(sppm_photons(ctx), 4u << 20));
     if (has_emitters(ctx)) {                   // the list's per-slot weights and its hit queue (a shadow side's room)
         int rc = emit_ensure(ctx, cap, 2u * cap);
         if (rc) return rc;
@@ -429,11 +436,15 @@ static int ensure_wave(st_ctx* ctx) {
     CK(cudaMalloc(&ctx->d_frame, S * sizeof(float4)), "cudaMalloc frame");
     CK(cudaMalloc(&ctx->d_acc, (size_t)ctx->P * sizeof(Acc4)), "cudaMalloc accumulation");
     CK(cudaMalloc(&ctx->d_mom, (size_t)ctx->P * sizeof(double2)), "cudaMalloc moments");
+    CK(cudaMalloc(&ctx->d_splat, (size_t)ctx->P * sizeof(float4)), "cudaMalloc splat");
+    CK(cudaMalloc(&ctx->d_ltcount, (size_t)ctx->P * sizeof(uint32_t)), "cudaMalloc splat");
     ctx->q.cap = cap;
     ctx->slot_cap = cap;
     CK(cudaMemsetAsync(ctx->d_frame, 0, S * sizeof(float4), ctx->stream), "memset");
     CK(cudaMemsetAsync(ctx->d_acc, 0, (size_t)ctx->P * sizeof(Acc4), ctx->stream), "memset");
     CK(cudaMemsetAsync(ctx->d_mom, 0, (size_t)ctx->P * sizeof(double2), ctx->stream), "memset");
+    CK(cudaMemsetAsync(ctx->d_splat, 0, (size_t)ctx->P * sizeof(float4), ctx->stream), "memset");
+    CK(cudaMemsetAsync(ctx->d_ltcount, 0, (size_t)ctx->P * sizeof(uint32_t), ctx->stream), "memset");
     CK(cudaMemsetAsync(ctx->d_ctr, 0, sizeof(DevCtr), ctx->stream), "memset");
     if (ctx->wait_limit || ctx->wait_arm_only) CK(push_wait(ctx), "wait limit");
     ctx->samples = 0;
@@ -446,8 +457,17 @@ static bool sppm_runs(const st_ctx* ctx) {
     const Uni u = make_uni(ctx);
     return u.sun_on != 0 && ctx->params.env_uniform <= 0.f;
 }
+// light tracing runs while it is set and the sun shines (its photons are the sun's)
+static bool lt_runs(const st_ctx* ctx) {
+    if (!ctx->has_params || !ctx->params.lt) return false;
+    const Uni u = make_uni(ctx);
+    return u.sun_on != 0 && ctx->params.env_uniform <= 0.f;
+}
+static bool photons_run(const st_ctx* ctx) { return sppm_runs(ctx) || lt_runs(ctx); }
+// the sun's photons a sample: the map's count while it runs (they serve both), else light tracing's
 static uint32_t sppm_photons(const st_ctx* ctx) {
-    return ctx->params.sppm_photons ? ctx->params.sppm_photons : ctx->P;
+    if (sppm_runs(ctx)) return ctx->params.sppm_photons ? ctx->params.sppm_photons : ctx->P;
+    return ctx->params.lt_photons ? ctx->params.lt_photons : ctx->P;
 }
 
 static WaveArgs wave_args(st_ctx* ctx, uint32_t w) {
@@ -462,13 +482,16 @@ static WaveArgs wave_args(st_ctx* ctx, uint32_t w) {
     a.q = ctx->q;
     a.ctr = ctx->d_ctr;
     a.frame = ctx->d_frame;
+    a.splat = ctx->d_splat;
+    a.ltcount = ctx->d_ltcount;
     a.acc = ctx->d_acc;
     a.mom = ctx->d_mom;
     a.spw = w;
     a.slots = w * ctx->P;
     a.code = ctx->has_code ? &ctx->code : nullptr;
-    if (sppm_runs(ctx)) {
-        a.u.sppm_on = 1u;
+    if (photons_run(ctx)) {
+        a.u.sppm_on = sppm_runs(ctx) ? 1u : 0u;
+        a.u.lt_on = lt_runs(ctx) ? 1u : 0u;
         a.u.sppm_n = sppm_photons(ctx);
         a.u.sppm_budget = SPPM_WAVE_BUDGET;
         a.u.sppm_half = ctx->params.sppm_half > 0.f ? ctx->params.sppm_half : std::min(15.f, a.u.envR);
@@ -511,11 +534,12 @@ static cudaError_t record_wave(st_ctx* ctx, const WaveArgs& a) {
         return e;
     };
     cudaError_t e;
-    if (a.u.sppm_on) {
+    if (a.u.sppm_on || a.u.lt_on) {
         // THE SAMPLE'S PHOTONS FIRST (photons.js planBatches's `first`): in chunks of the wave's slots, each through
-        // the march, the surface kernel and the photon's shade; then the grid
+        // the march, the surface kernel and the photon's shade (and, with light tracing, the occlusion pass of the
+        // connections it made); then the map's grid
         ctx->rec_launches++;
-        if ((e = launch_sppm_begin(a, s))) return e;
+        if (a.u.sppm_on && (e = launch_sppm_begin(a, s))) return e;
         if (a.u.sppm_learn && (e = timed("lt_build", [&] { return launch_lt_build(a, s); }))) return e;
         const uint32_t N = a.u.sppm_n, C = ctx->slot_cap;          // the slots the path state holds
         for (uint32_t first = 0; first < N; first += C) {
@@ -536,12 +560,18 @@ static cudaError_t record_wave(st_ctx* ctx, const WaveArgs& a) {
                 }
                 if ((e = timed("photon_march", [&] { return launch_march(pa, pc, nxt, last, ctx->sms, s); }))) return e;
                 if ((e = timed("photon_surface", [&] { return launch_surface(pa, ctx->sms, s); }))) return e;
-                if ((e = timed("photon_shade", [&] { return launch_photon_shade(pa, nxt, last, ctx->sms, s); }))) return e;
+                const int side = (int)(it & 1u);
+                if ((e = timed("photon_shade", [&] { return launch_photon_shade(pa, nxt, last, side, ctx->sms, s); })))
+                    return e;
+                if (pa.u.lt_on && (e = timed("photon_occlude", [&] { return launch_occlude(pa, side, last, ctx->sms, s); })))
+                    return e;
                 pc = nxt;
             }
         }
-        if ((e = timed("grid", [&] { return sppm_grid_launch(ctx_ext(ctx).sppm, ctx->sms, s); }))) return e;
-        ctx->rec_launches += 5;                                      // key, three scan phases, scatter
+        if (a.u.sppm_on) {
+            if ((e = timed("grid", [&] { return sppm_grid_launch(ctx_ext(ctx).sppm, ctx->sms, s); }))) return e;
+            ctx->rec_launches += 5;                                  // key, three scan phases, scatter
+        }
     }
     ctx->rec_launches++;
     if (a.gd.train && (e = guide_wave_begin(ctx, a.slots, s))) return e;
@@ -797,6 +827,7 @@ int st_set_params(st_ctx* ctx, const st_params* p, uint64_t* unknown_mask) {
     if (!(p->stepscale > 0 && p->stepscale <= 1)) return fail(ctx, ST_ERR_ARG, "stepscale out of range (0, 1]");
     if (p->budget > 256) return fail(ctx, ST_ERR_ARG, "budget out of range (0..256)");
     if (p->samples_per_wave > 1024) return fail(ctx, ST_ERR_ARG, "samples_per_wave out of range (0..1024)");
+    if (p->lt > 1) return fail(ctx, ST_ERR_ARG, "lt is 0 or 1");
     cudaSetDevice(ctx->device);
     bool resize = p->width != ctx->params.width || p->height != ctx->params.height ||
                   p->samples_per_wave != ctx->params.samples_per_wave || !ctx->has_params;
@@ -912,6 +943,8 @@ int st_invalidate(st_ctx* ctx) {
     CK(cudaMemsetAsync(ctx->d_acc, 0, (size_t)ctx->P * sizeof(Acc4), ctx->stream), "memset");
     CK(cudaMemsetAsync(ctx->d_mom, 0, (size_t)ctx->P * sizeof(double2), ctx->stream), "memset");
     CK(cudaMemsetAsync(ctx->d_frame, 0, (size_t)ctx->slot_cap * sizeof(float4), ctx->stream), "memset");
+    CK(cudaMemsetAsync(ctx->d_splat, 0, (size_t)ctx->P * sizeof(float4), ctx->stream), "memset");
+    CK(cudaMemsetAsync(ctx->d_ltcount, 0, (size_t)ctx->P * sizeof(uint32_t), ctx->stream), "memset");
     CK(cudaMemsetAsync(&ctx->d_ctr->sample, 0, sizeof(uint32_t), ctx->stream), "memset");
     CK(sppm_lt_reset(ctx_ext(ctx).sppm, ctx->stream), "memset");     // the emission map starts over uniform
     CK(emit_reset(ctx), "emitter list reset");                         // and the emitters' discovery
@@ -1043,6 +1076,18 @@ int st_read_accum(st_ctx* ctx, double* rgb, double* V, double* S, uint32_t* coun
         if (V) V[i] = mom[i].x;
         if (S) S[i] = mom[i].y;
     }
+    return ST_OK;
+}
+
+// light tracing's connections per pixel since the last invalidate (include/shadytracer.h st_lt_counts)
+int st_lt_counts(st_ctx* ctx, uint32_t* counts) {
+    if (!ctx || !counts) return ST_ERR_ARG;
+    if (!ctx->d_ltcount) return fail(ctx, ST_ERR_STATE, "nothing rendered yet");
+    if (ctx->in_flight) { int rc = st_sync(ctx, -1); if (rc) return rc; }
+    cudaSetDevice(ctx->device);
+    CK(cudaMemcpyAsync(counts, ctx->d_ltcount, (size_t)ctx->P * sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream),
+       "readback");
+    CK(cudaStreamSynchronize(ctx->stream), "readback");
     return ST_OK;
 }
 

@@ -123,6 +123,8 @@ struct Uni {
     uint32_t sort_on; f3 glo, ginv;
     // the photon map (st_photons.cu): photons a sample, the sun photons' square, the radius schedule, the budget
     uint32_t sppm_on, sppm_n, sppm_budget, sppm_learn; float sppm_half, sppm_r1, sppm_alpha;
+    // light tracing to the camera (st_photons.cu lt_connect): the photons above connect where they land
+    uint32_t lt_on;
 };
 
 // ------------------------------------------------------------------------------------------------------------

@@ -26,6 +26,8 @@ namespace st {
 #define META_LENS_SHIFT 25u               // a camera path's lens field (2 bits): 1 delta events only since the eye,
                                           // 2 at its D, 3 delta events since its D (the map owns the sun it reaches)
 #define META_TRAIN (1u << 27)             // a camera path that holds a training record for the learned proposal
+#define META_CAND (1u << 28)              // light tracing's class (tracebasics.js:195-196 CLS_CAND, CLS_SPEC): a camera
+#define META_SPEC (1u << 29)              // path whose first vertex drew an evaluable lobe; ...and delta events since
 #define META_LOW 0x00ffffffu
 #define SURF_NONE 0xffffu                 // hsurf: no medium asked (n1 is the material's own index of refraction)
 #define SURF_LEAVING 0xffffffffu          // hsurf: the surface seen from behind, the ray moved on
@@ -155,7 +157,9 @@ struct GuideBufs {
 #define SHADOW_EMIT 0x80000000u           // a shadow side's steps word: the ray aims at an emitter (TAG_EMIT)
 #define SHADOW_FACE 0x40000000u           // ...at a point of a light's face (TAG_FNEE): it arrives when ltot,
                                           // started at minus the way there, reaches 0
-#define SHADOW_FLAGS (SHADOW_EMIT | SHADOW_FACE)
+#define SHADOW_CONN 0x20000000u           // ...a photon's connection to the camera (TAG_CONN), a face's ray in its
+                                          // length; what arrives goes to the splat buffer
+#define SHADOW_FLAGS (SHADOW_EMIT | SHADOW_FACE | SHADOW_CONN)
 #define SC_BURST 4u                       // step-cache balls a lane may cross in a row before it asks the scene
 // THE LIGHTS' FACES (st_light.cuh): FACE_F4 float4s a face, then a byte a material (its face + 1, 0 none)
 #define FACE_F4 5
@@ -207,6 +211,8 @@ struct WaveArgs {
     Queues q;
     DevCtr* ctr;
     float4* frame;      // spw * P: this wave's deposits, rgb + count
+    float4* splat = nullptr;     // P: light tracing's connections this sample, rgb (wavefront.js splat_u32)
+    uint32_t* ltcount = nullptr; // P: the connections that reached each pixel since the last invalidate
     Acc4* acc;         // P: FP64 mean rgb + count
     double2* mom;       // P: FP64 V, S (the error bar's moments)
     uint32_t spw;       // samples in this wave
@@ -232,7 +238,7 @@ cudaError_t launch_sort(const WaveArgs& a, int cur, int sms, cudaStream_t s);
 cudaError_t launch_sppm_begin(const WaveArgs& a, cudaStream_t s);
 cudaError_t launch_lt_build(const WaveArgs& a, cudaStream_t s);
 cudaError_t launch_genphotons(const WaveArgs& a, uint32_t first, uint32_t n, int sms, cudaStream_t s);
-cudaError_t launch_photon_shade(const WaveArgs& a, int nxt, int last, int sms, cudaStream_t s);
+cudaError_t launch_photon_shade(const WaveArgs& a, int nxt, int last, int side, int sms, cudaStream_t s);
 cudaError_t launch_gather(const WaveArgs& a, int sms, cudaStream_t s);
 cudaError_t launch_eval_sdf(const DPrim* prims, uint32_t n_prims, const float* pts, uint32_t n, float* out,
                             cudaStream_t s, const SceneCode* code = nullptr);

@@ -26,6 +26,7 @@ namespace st {
 #define PHOTON_SEED_SALT 0x50484F54u       // the photons' sample seed: the picture's seed xor this
 #define PHOTON_GEN_SALT 0x5A17u            // their draw at the source (wavefront.js:594 SEED_u32(0x5A17))
 #define SPPM_STORE_SALT 0x53505031u        // a store's and a gather's own stream (wavefront.js:1186)
+#define LT_LENS_SALT 0x4C54434Eu           // a connection's point of the lens, from the photon's own stream
 
 __device__ __forceinline__ uint4 photon_seed(const Uni& u, uint32_t sample) {
     return sample_seed(u.seed ^ PHOTON_SEED_SALT, sample);
@@ -171,9 +172,90 @@ __global__ void __launch_bounds__(256) k_genphotons(WaveArgs a, uint32_t first, 
     }
 }
 
-// A PHOTON'S HIT (prog_sppm's store, then pathBegin..pathEnd for a photon): stored where it may be, else bounced --
-// no light sampling; a delta lobe keeps it in the map's class, anything else ends it
-__global__ void __launch_bounds__(256) k_photon_shade(WaveArgs a, int nxt, int last) {
+// A PHOTON'S CONNECTION TO THE CAMERA (materials_pbr.js:672-830 ltConnect, :598-612 camFootprint, lens.js lensDisc /
+// lensImage): from the point P it landed on (in air, the normal nrm turned to it, arriving along din with flux phi) to
+// the camera -- to a point of the thin lens's disc drawn uniformly from the photon's own stream, or the pinhole --
+// through the lobes a connection owns (the evaluable ones, glossy from LT_MIN_ALPHA up), for the pixel the line lands
+// on: phi f G / A_px, G = |n.v| dist / z^3 (perspective; |n.fwd| orthographic), A_px a pixel's area on the image plane
+// at unit distance. The shadow ray starts on the camera's line of sight to P, as far along it as lifts it 2 offsets off
+// the surface (at grazing views at most 4 such lengths, the rest along the normal, re-aimed at the camera), and stops
+// that height short of the camera. False where nothing connects: behind the camera, off the picture, the camera on
+// the surface's other side, no evaluable lobe, no light.
+struct LtConn { f3 org, dir, c; float len; uint32_t pix; };
+__device__ __forceinline__ bool lt_connect(const Uni& u, const st_material& m, const MfTab& tab, f3 P, f3 nrm, f3 din,
+                                           f3 phi, const uint4& ps, uint32_t id, LtConn& out) {
+    f3 off = mk(0.f);
+    const float R = u.camtype == 0u ? u.lens_r : 0.f;
+    if (R > 0.f) {
+        Rng rl = path_rng(ps, id, LT_LENS_SALT);
+        const float4 ul = rl.next();
+        const float r = R * sqrtf(ul.x);
+        float sp, cp;
+        sincosf(6.28318530718f * ul.y, &sp, &cp);
+        off = u.right * (r * cp) + u.up * (r * sp);
+    }
+    if (lobes_none(m, m.transmission, m.haze)) return false;
+    const f3 cam = u.cam + off;
+    const f3 d = cam - P;
+    const float apx = 4.f * u.fx * u.fy / ((float)u.W * (float)u.H);
+    f3 v;
+    float dist, xx, yy, G;
+    if (u.camtype == 0u) {
+        dist = length(d);
+        const float z = dot(d, u.fwd);                                // depth in front of the camera
+        if (z <= 1e-4f || dist <= 1e-4f) return false;
+        v = d * (1.f / dist);
+        if (R > 0.f) {                                                // where the lens point's ray meets the picture
+            const float c = dot(v, u.fwd);
+            const f3 F = off + (-v) * (u.lens_f / fmaxf(c, 1e-30f));
+            xx = dot(F, u.right) / (u.lens_f * u.fx);
+            yy = dot(F, u.up) / (u.lens_f * u.fy);
+        } else {
+            xx = -dot(d, u.right) / (z * u.fx);
+            yy = -dot(d, u.up) / (z * u.fy);
+        }
+        G = fabsf(dot(nrm, v)) * dist / (z * z * z);
+    } else {
+        dist = dot(d, u.fwd);                                          // to the camera plane along the view axis
+        if (dist <= 1e-4f) return false;
+        v = u.fwd;
+        xx = -dot(d, u.right) / u.fx;
+        yy = -dot(d, u.up) / u.fy;
+        G = fabsf(dot(nrm, u.fwd));
+    }
+    if (fabsf(xx) >= 1.f || fabsf(yy) >= 1.f) return false;           // off the picture
+    const float cv = dot(nrm, v);
+    if (cv <= 0.f) return false;                                      // the camera on the surface's other side
+    // the camera's own lobes at this vertex, seen along v, in air (the interface air to the material's index)
+    const Lobes lb = make_lobes(nrm, v, m, 1.f / fmaxf(m.ior, 1.f), tab, m.transmission, m.specular, m.haze);
+    const f3 f = lobes_eval(lb, tab, -din, LT_MIN_ALPHA);
+    const f3 c = phi * f * (G / apx);
+    if (!(luma(c) > 0.f)) return false;
+    const float px = clampf((xx + 1.f) * 0.5f * (float)u.W, 0.f, (float)u.W - 1.f);
+    const float py = clampf((yy + 1.f) * 0.5f * (float)u.H, 0.f, (float)u.H - 1.f);
+    out.pix = (uint32_t)px + (uint32_t)py * u.W;
+    const float h = 20.f * march_tol(P, u.tol);                       // offsetTol(P) * 2
+    const bool grazing = cv < 0.25f;
+    const float sl = h / fmaxf(cv, 0.25f);
+    const float lift = grazing ? h - sl * cv : 0.f;
+    out.org = P + v * sl + nrm * lift;
+    out.dir = v;
+    out.len = dist - sl - cv * lift - h;
+    if (grazing && u.camtype == 0u) {
+        const f3 toCam = cam - out.org;
+        const float l = length(toCam);
+        out.dir = toCam * (1.f / fmaxf(l, 1e-30f));
+        out.len = l - h;
+    }
+    out.c = c;
+    return out.len > 0.f;
+}
+
+// A PHOTON'S HIT (prog_sppm's store, then pathBegin..pathEnd for a photon): with light tracing on, connected to the
+// camera first (pathMiddle: once it has passed a delta event, in air, within the bounce cap); then stored where it
+// may be, else bounced -- no light sampling; a delta lobe keeps it in the class, anything else ends it. Connections go
+// to the shadow side `side`, which the occlusion pass after this kernel traces.
+__global__ void __launch_bounds__(256) k_photon_shade(WaveArgs a, int nxt, int last, int side) {
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ __align__(8) uint64_t mbar;
     const Uni& u = a.u;
@@ -194,6 +276,8 @@ __global__ void __launch_bounds__(256) k_photon_shade(WaveArgs a, int nxt, int l
         float ltot = 0.f, n = 1.f, lam = 0.f;
         uint4 m4 = make_uint4(0, 0, 0, 0);
         uint32_t bounces = 0, sub = 0;
+        bool conn = false;
+        LtConn lc;
         if (q < count) {
             slot = a.q.hit[q];
             const float dh = a.q.hitd[q];
@@ -216,10 +300,15 @@ __global__ void __launch_bounds__(256) k_photon_shade(WaveArgs a, int nxt, int l
                     const st_material& m = sm[ids & 0xffffu];
                     const bool emissive = fmaxf(fmaxf(m.emissive[0], m.emissive[1]), m.emissive[2]) > 0.f;
                     const bool passed = (m4.y & META_PASSED) != 0u;
+                    if (u.lt_on && !emissive && passed && fabsf(n - 1.f) <= 1e-3f && bounces + 1u <= u.maxbounce) {
+                        conn = lt_connect(u, m, a.tab, pos, nrm, dir, rad * beta, ps, m4.x, lc);
+                        // teach the emission map: this cell's photon reached the camera (ltConnect's learn)
+                        if (conn && u.sppm_learn && m4.w < LT_CELLS) atomicAdd(&a.sp.lt_hit[m4.w], 1u);
+                    }
                     if (emissive) {
                     } else if (passed && sppm_evaluable(m, false)) {
                         // STORED (sppm.js sppmStores / sppmStore): within the cap a gather can accept
-                        if (bounces + 2u <= u.maxbounce && luma(rad * beta) > 0.f) {
+                        if (u.sppm_on && bounces + 2u <= u.maxbounce && luma(rad * beta) > 0.f) {
                             Rng rs = path_rng(ps, m4.x, SPPM_STORE_SALT);
                             const float4 us = rs.next();
                             sub = min((uint32_t)(us.y * (float)SPPM_SUBS), SPPM_SUBS - 1u);
@@ -293,9 +382,24 @@ __global__ void __launch_bounds__(256) k_photon_shade(WaveArgs a, int nxt, int l
                 a.sp.dir_oct[at] = oct_word(-dir);
                 a.sp.nrm_oct[at] = oct_word(nrm);
                 a.sp.flags[at] = (bounces + 1u) | (sub << SPPM_SUB_SHIFT);
-                if (m4.w < LT_CELLS) atomicAdd(&a.sp.lt_hit[m4.w], 1u);     // teach the map: this cell paid
+                // teach the map: this cell paid (with light tracing on, its connections teach it instead)
+                if (!u.lt_on && m4.w < LT_CELLS) atomicAdd(&a.sp.lt_hit[m4.w], 1u);
             } else {
                 atomicAdd(&d->dropped, 1u);
+            }
+        }
+        if (u.lt_on) {
+            // the connection: a shadow ray of its length (it arrives when ltot, started at minus that, reaches 0)
+            const uint32_t cq = warp_append(&a.ctr->shadowCount[side], conn);
+            if (conn) {
+                if (cq < a.q.scap) {
+                    a.q.s_org[side][cq] = f4(lc.org, -lc.len);
+                    a.q.s_dir[side][cq] = make_float4(lc.dir.x, lc.dir.y, lc.dir.z, __uint_as_float(lc.pix));
+                    a.q.s_rad[side][cq] = make_float4(lc.c.x, lc.c.y, lc.c.z, 1.f);
+                    a.q.s_steps[side][cq] = SHADOW_FACE | SHADOW_CONN;
+                } else {
+                    atomicAdd(&a.ctr->shadowdrop, 1u);
+                }
             }
         }
         const uint32_t rq = warp_append(outc, cont);
@@ -401,7 +505,9 @@ __global__ void __launch_bounds__(256, 2) k_gather(WaveArgs a) {
             const uint32_t my = a.pb.meta[slot].y;
             const float4 sf = a.q.hsurf[q];
             const uint32_t ids = __float_as_uint(sf.w);
-            if (((my >> 16) & 0xffu) == RAY_ACTIVE && ((my & 0xffu) == 0u || ((my >> META_LENS_SHIFT) & 3u) == 1u) &&
+            // (at the eye's first surface too, unless light tracing runs: that class is its)
+            if (((my >> 16) & 0xffu) == RAY_ACTIVE &&
+                (((my & 0xffu) == 0u && !a.u.lt_on) || ((my >> META_LENS_SHIFT) & 3u) == 1u) &&
                 ids != SURF_LEAVING) {
                 const st_material& m = sm[ids & 0xffffu];
                 take = fmaxf(fmaxf(m.emissive[0], m.emissive[1]), m.emissive[2]) <= 0.f && sppm_evaluable(m, true);
@@ -581,9 +687,9 @@ cudaError_t launch_genphotons(const WaveArgs& a, uint32_t first, uint32_t n, int
     k_genphotons<<<std::min((n + 255u) / 256u, (uint32_t)sms * 8u), 256, 0, s>>>(a, first, n);
     return cudaGetLastError();
 }
-cudaError_t launch_photon_shade(const WaveArgs& a, int nxt, int last, int sms, cudaStream_t s) {
+cudaError_t launch_photon_shade(const WaveArgs& a, int nxt, int last, int side, int sms, cudaStream_t s) {
     const size_t smem = a.u.n_mats * sizeof(st_material);
-    k_photon_shade<<<sms * 4, 256, smem, s>>>(a, nxt, last);
+    k_photon_shade<<<sms * 4, 256, smem, s>>>(a, nxt, last, side);
     return cudaGetLastError();
 }
 cudaError_t launch_gather(const WaveArgs& a, int sms, cudaStream_t s) {

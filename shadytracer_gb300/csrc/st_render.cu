@@ -450,10 +450,17 @@ __device__ __forceinline__ void shade_surface(const WaveArgs& a, const st_materi
     }
     if (u.sppm_on) {                                                  // materials_pbr.js:862-873 lensStep
         const bool delta = smp.ev == EV_DELTA;
-        // the first surface: 1 through a delta; a D there was gathered, so 2 (the reference's light tracer's class)
-        if (bounces == 1u) lens = delta ? 1u : (smp.ev == EV_EVAL ? 2u : 0u);
+        // the first surface: 1 through a delta; a D there was gathered, so 2 -- unless light tracing runs, whose
+        // class that is (the reference's split: 0)
+        if (bounces == 1u) lens = delta ? 1u : ((smp.ev == EV_EVAL && !u.lt_on) ? 2u : 0u);
         else if (lens == 1u) lens = delta ? 1u : (smp.ev == EV_EVAL ? 2u : 0u);
         else lens = ((lens == 2u || lens == 3u) && delta) ? 3u : 0u;
+    }
+    if (u.lt_on) {
+        // LIGHT TRACING'S CLASS (tracebasics.js:995-1011): a first vertex drawn from an evaluable lobe, then delta
+        // events only; the first other event takes the path out for good
+        if (bounces == 1u) my = (my & ~(META_CAND | META_SPEC)) | (smp.ev == EV_EVAL ? META_CAND : 0u);
+        else if (my & META_CAND) my = smp.ev == EV_DELTA ? (my | META_SPEC) : (my & ~(META_CAND | META_SPEC));
     }
     if (max3(smp.w) <= 0.f) state = RAY_ABSORBED;
     if (u.nee != 0u && !last) {                                       // the other half of MIS (:1370-1395)
@@ -601,8 +608,11 @@ __global__ void __launch_bounds__(256) k_shade(WaveArgs a, int nxt, int side, in
             gpix = (slot / u.P) * u.P + pix;                          // the pixel in the wave's frames
             if (state == RAY_ESCAPED) {
                 // wavefront.js:1292-1310: a path the photon map owns (its lens field 3: delta events only since
-                // its D) takes the sky but not the disc, where the sun's photons were drawn along its line
-                const bool owned = u.sppm_on && ((m4.y >> META_LENS_SHIFT) & 3u) == 3u && sppm_covers(u, pos, dir);
+                // its D), or light tracing (its class: an evaluable first vertex, delta events since), takes the sky
+                // but not the disc, where the sun's photons were drawn along its line
+                const bool owned = ((u.sppm_on && ((m4.y >> META_LENS_SHIFT) & 3u) == 3u) ||
+                                    (u.lt_on && (m4.y & (META_CAND | META_SPEC)) == (META_CAND | META_SPEC))) &&
+                                   sppm_covers(u, pos, dir);
                 rad = rad + beta * (owned ? env_sky(u, dir) : env_radiance(u, dir)) * sunmis;
             } else if (state == RAY_ACTIVE || state == RAY_SCATTER) {
                 train_nee = GUIDE && (m4.y & META_TRAIN) != 0u;       // light found past a record's vertex counts
@@ -615,7 +625,8 @@ __global__ void __launch_bounds__(256) k_shade(WaveArgs a, int nxt, int side, in
                 if (state == RAY_SCATTER) {
                     m4.w = __float_as_uint(ltot);
                     shade_medium(a, pos, dir, beta, sunmis, bounces, state, n, rng, last != 0, sh, emw, ltot, lp);
-                    m4.y &= ~(3u << META_LENS_SHIFT);                 // haze.js:539: the air is no delta event
+                    // haze.js:539: the air is no delta event (out of the map's class and light tracing's)
+                    m4.y &= ~((3u << META_LENS_SHIFT) | META_CAND | META_SPEC);
                 }
                 else
                 {
@@ -694,12 +705,19 @@ __global__ void __launch_bounds__(256) k_resolve(WaveArgs a) {
     if (i >= u.P) return;
     Acc4 acc = a.acc[i];
     double2 mo = a.mom[i];
+    // light tracing's estimate for the pixel (one sample a wave while it runs), taken and cleared first: added as it
+    // is, not averaged with the pixel's paths (wavefront.js:425-433, :459-462)
+    float4 lt = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (u.lt_on) {
+        lt = a.splat[i];
+        a.splat[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
     for (uint32_t j = 0; j < a.spw; j++) {
         float4 f = a.frame[(size_t)j * u.P + i];
         a.frame[(size_t)j * u.P + i] = make_float4(0.f, 0.f, 0.f, 0.f);
         uint32_t n = (uint32_t)f.w;
         if (n == 0u) continue;
-        double sx = double(f.x) / n, sy = double(f.y) / n, sz = double(f.z) / n;
+        double sx = double(f.x) / n + lt.x, sy = double(f.y) / n + lt.y, sz = double(f.z) / n + lt.z;
         double prevn = u.maxaverages ? fmin(acc.w, double(u.maxaverages)) : acc.w;
         double cnt = prevn + 1.0;
         double px = fmin(fmax(acc.x, -1e20), 1e20), py = fmin(fmax(acc.y, -1e20), 1e20), pz = fmin(fmax(acc.z, -1e20), 1e20);

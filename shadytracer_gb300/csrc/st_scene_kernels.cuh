@@ -294,7 +294,8 @@ __global__ void __launch_bounds__(256, 4) k_occlude(WaveArgs a, int last) {
                     float4 o4 = i_org[idx], d4 = i_dir[idx];
                     pos = xyz(o4); ltot = o4.w; dir = xyz(d4); n = fabsf(i_rad[idx].w);
                     steps = i_steps[idx];
-                    sflag = steps & SHADOW_FLAGS;                     // aimed at an emitter (TAG_EMIT), a face
+                    sflag = steps & SHADOW_FLAGS;                     // aimed at an emitter (TAG_EMIT), a face,
+                                                                      // the camera (a photon's connection)
                     steps &= ~SHADOW_FLAGS;
                     evals_here = 0;
                     if (steps == 0u) rays++;
@@ -353,7 +354,13 @@ __global__ void __launch_bounds__(256, 4) k_occlude(WaveArgs a, int last) {
             a.em.hdir[ep] = i_dir[idx];
             a.em.hrad[ep] = i_rad[idx];
         }
-        if (reached && (sflag & SHADOW_EMIT) == 0u) {
+        if (reached && (sflag & SHADOW_CONN)) {
+            // a photon's connection (wavefront.js:1649-1661): to the splat buffer, added to its pixel as it is
+            // (resolve does not average it with the pixel's paths); the connections counted per pixel
+            const uint32_t pix = __float_as_uint(i_dir[idx].w);
+            deposit(a.splat, pix, xyz(i_rad[idx]), a.ctr);
+            atomicAdd(&a.ltcount[pix], 1u);
+        } else if (reached && (sflag & SHADOW_EMIT) == 0u) {
             float4 r4 = i_rad[idx];
             uint32_t gpix = __float_as_uint(i_dir[idx].w);          // the pixel in the wave's frames
             deposit(a.frame, gpix, xyz(r4), a.ctr);

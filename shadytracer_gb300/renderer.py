@@ -78,6 +78,11 @@ class PathTracer:
         check(self.L.st_autotune(self.ctx, int(samples), C.byref(t)), self.ctx, "st_autotune")
         return {f: getattr(t, f) for f, _ in T.StTune._fields_}
 
+    def set_tune(self, claim=0, chunk=0):
+        """The queue tile and march chunk set by hand (st_set_tune; 0 the defaults)."""
+        t = T.StTune(claim=int(claim), chunk=int(chunk))
+        check(self.L.st_set_tune(self.ctx, C.byref(t)), self.ctx, "st_set_tune")
+
     def scene_code_info(self):
         is_code, ms, nbytes = C.c_int(), C.c_double(), C.c_uint64()
         check(self.L.st_scene_code_info(self.ctx, C.byref(is_code), C.byref(ms), C.byref(nbytes)), self.ctx,
@@ -136,6 +141,13 @@ class PathTracer:
         check(self.L.st_sync(self.ctx, int(timeout_ms)), self.ctx, "st_sync")
 
     # ---- readings ----
+    def lt_counts(self):
+        """Light tracing's connections that reached each pixel since the last invalidate (st_lt_counts), HxW."""
+        W, H = self.params.width, self.params.height
+        out = np.zeros((H, W), np.uint32)
+        check(self.L.st_lt_counts(self.ctx, out.ctypes.data_as(C.c_void_p)), self.ctx, "st_lt_counts")
+        return out
+
     def read_accum(self):
         """(rgb HxWx3, V HxW, S HxW, count HxW): the FP64 mean, the error bar's moments, the samples per pixel."""
         W, H = self.params.width, self.params.height

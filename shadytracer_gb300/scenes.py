@@ -542,6 +542,61 @@ def sppm_pane_closed_form(scene, fresnel):
     return (1 - Fv) / (1 + Fv) * i["albedo"] / math.pi * i["E_sun"] * math.sin(math.radians(el)) * (1 - Fs) / (1 + Fs)
 
 
+def lt_pane(width=64, height=48, photons=400_000, sun_elevation=60.0, ior=1.5, seed=1, pane_z=1.0, photon_half=1.6,
+            lens_radius=0.0, sppm=0, vfov=40.0):
+    """Light tracing's closed form: the pane of sppm_pane (2 x 2 m, 2 cm thick), `pane_z` over a floor (albedo 0.7)
+    cut to its shadow under the sun alone, now seen DIRECTLY from the side, from under the pane: the class
+    light -> delta+ -> D -> eye, which light tracing owns. With the depth cap at 3 (the pane's two faces, the floor)
+    the photons that reach the floor have crossed each face once, so
+        L = rho / pi * E_sun sin(elevation) (1 - F)^2,  F the dielectric Fresnel reflectance at the sun's angle
+    (the camera's paths keep only the sky, which is black). `lens_radius` puts a thin lens focused on the floor's
+    middle in front of the camera."""
+    mats = [air(), glass((1.0, 1.0, 1.0), ior=ior), diffuse((0.7, 0.7, 0.7))]
+    off = pane_z / math.tan(math.radians(sun_elevation))      # the shadow's shift away from the sun (+y)
+    prims = [prim(ST_PRIM_BOX, pos=(0.0, 0.0, pane_z), params=(1.0, 1.0, 0.01), material=1),
+             prim(ST_PRIM_BOX, pos=(0.0, -off, -0.05), params=(1.0, 1.0, 0.05), material=2)]
+    s = Scene(prims, mats, env_radius=20.0, name="lt-pane")
+    s.params = default_params(width=width, height=height, maxbounce=3, seed=seed, sun_elevation=sun_elevation,
+                              sun_azimuth=0.0, sun_illuminance=100000.0, sky_luminance=0.0, ground_luminance=0.0,
+                              lt=1, lt_photons=photons, sppm=sppm, sppm_photons=photons, sppm_half=photon_half)
+    eye, target = (-2.0, -off, 0.8 * pane_z), (0.3, -off, 0.0)
+    s.view = look_at(eye, target, vfov, width / height)
+    if lens_radius > 0:
+        s.view.lens_radius = lens_radius
+        s.view.focus_distance = math.dist(eye, target)
+    s.info = {"ior": ior, "albedo": 0.7, "sun_elevation": sun_elevation, "E_sun": 100000.0, "eye": eye,
+              "floor": (-1.0, 1.0, -1.0 - off, 1.0 - off)}
+    return s
+
+
+def lt_pane_closed_form(scene, fresnel):
+    """The floor's radiance in lt_pane, rho / pi E_sun sin(elevation) (1 - F)^2; `fresnel(cos_i, eta)` the
+    caller's dielectric Fresnel reflectance."""
+    i = scene.info
+    el = i["sun_elevation"]
+    F = fresnel(math.cos(math.radians(90.0 - el)), 1.0 / i["ior"])
+    return i["albedo"] / math.pi * i["E_sun"] * math.sin(math.radians(el)) * (1 - F) ** 2
+
+
+def floor_mask(scene, margin=0.1):
+    """The pixels whose centre's ray meets the floor's top (z = 0) inside its rectangle, `margin` metres in."""
+    v, p = scene.view, scene.params
+    W, H = p.width, p.height
+    x0, x1, y0, y1 = scene.info["floor"]
+    cam = [v.cam_pos[i] for i in range(3)]
+    mask = [[False] * W for _ in range(H)]
+    for py in range(H):
+        for px in range(W):
+            xx, yy = (px + 0.5) / W * 2 - 1, (py + 0.5) / H * 2 - 1
+            d = [v.right[i] * xx * v.fx + v.up[i] * yy * v.fy - v.fwd[i] for i in range(3)]
+            if d[2] >= -1e-6:
+                continue
+            t = -cam[2] / d[2]
+            x, y = cam[0] + t * d[0], cam[1] + t * d[1]
+            mask[py][px] = x0 + margin < x < x1 - margin and y0 + margin < y < y1 - margin
+    return mask
+
+
 # ---------------------------------------------------------------------------------------------------------------
 # The haze box (lib/pathtracer/tests.js:1818-1866 'haze' row; core/haze.js).
 # ---------------------------------------------------------------------------------------------------------------

@@ -72,7 +72,8 @@ class StParams(C.Structure):
                 ("guide", C.c_uint32), ("guide_alpha", C.c_float), ("guide_lr", C.c_float),
                 ("guide_train", C.c_uint32), ("guide_seed", C.c_uint32),
                 ("emit_share", C.c_float), ("emit_radius", C.c_float), ("emit_off", C.c_uint32),
-                ("env_map_off", C.c_uint32), ("step_cache", C.c_uint32), ("step_cache_cells", C.c_float)]
+                ("env_map_off", C.c_uint32), ("step_cache", C.c_uint32), ("step_cache_cells", C.c_float),
+                ("lt", C.c_uint32), ("lt_photons", C.c_uint32)]
 
 
 class StView(C.Structure):

@@ -81,6 +81,24 @@ def test_photon_map_pane_closed_form():
     assert abs(E / (1e5 * math.sin(math.radians(60)) * (1 - Fs) / (1 + Fs)) - 1) < 0.01
 
 
+def test_light_tracing_pane_closed_form():
+    """The oracle's light tracing (materials_pbr.js ltConnect: the sun's photons past the pane connected to the camera
+    where they land on the floor, shadow-tested, splatted, added to the pixel as they are) against the floor seen
+    directly under the pane: rho / pi E_sun sin(elevation) (1 - F)^2; the connections reach every floor pixel."""
+    s = scenes.lt_pane(width=48, height=36, photons=300_000)
+    a = oracle.render(s, 8)
+    m = np.array(scenes.floor_mask(s))
+    cf = scenes.lt_pane_closed_form(s, oracle.fresnel_dielectric)
+    assert m.sum() > 300
+    assert abs(a.luma()[m].mean() / cf - 1) < 0.01, (a.luma()[m].mean(), cf)
+    counts = oracle.last_lt_counts(48, 36)
+    assert np.all(counts[m] > 0)
+    # off: the floor under the glass is dark (the class is light tracing's; the sun's disc through the pane is rare)
+    s.params.lt = 0
+    b = oracle.render(s, 2)
+    assert b.luma()[m].mean() < 0.05 * cf
+
+
 def test_lamp_floor_closed_form():
     """The oracle's emitter discovery, list and light sample (materials_pbr.js:887-960, wavefront.js:715-815): the
     floor under a sphere lamp in the dark reads albedo Le a^2 h / D^3, and the list is the lamp's voxels."""

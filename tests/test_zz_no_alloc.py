@@ -104,6 +104,7 @@ def refused(make, setting=None):
     (lambda: scenes.spot_floor(width=32, height=32, light="face"), None, "light faces"),
     (lambda: scenes.floor_furnace(width=32, height=32), "sppm", "photon map"),
     (lambda: scenes.floor_furnace(width=32, height=32), "guide", "learned proposal"),
+    (lambda: scenes.floor_furnace(width=32, height=32), "lt", "light tracing"),
     (lambda: scenes.floor_furnace(width=32, height=32), "step_cache", "step cache"),
     (lambda: scenes.lamp_floor(width=32, height=32), None, "emissive"),
 ])
