@@ -910,7 +910,7 @@ void trace_path(const Ctx<T>& C, U4 sseed, uint32_t tile, const st_view& v, uint
             r.absLtot = r.ltot;                                                    // absorbAlong on arrival
             medium_vertex(C, r, rng, last, fr, st);
             r.lens = 0;                                                            // haze.js:539
-            r.cls = 0;
+            r.cls = (C.lt && r.bounces == 1) ? 1u : 0u;                            // haze.js:550-553
         } else {
             shade_hit(C, r, dh, rng, grng, last, fr, st);
         }
@@ -1074,6 +1074,9 @@ const uint32_t LT_LENS_SALT = 0x4C54434Eu;      // a connection's point of the l
 // off the surface (at most 4 such lengths at grazing views, the rest along the normal, re-aimed), stopped that height
 // short of the camera -- gets there
 template <class T>
+void lt_splat(const Ctx<T>& C, const V3<T>& P, const V3<T>& org, const V3<T>& dir, T len, T h, V3<T> c, uint32_t pix,
+              uint32_t cell, Stats& st);
+template <class T>
 void lt_connect(const Ctx<T>& C, const st_material& m, const V3<T>& P, const V3<T>& nrm, const V3<T>& din,
                 const V3<T>& phi, U4 ps, uint32_t id, uint32_t cell, Stats& st) {
     const st_view& vw = *C.view;
@@ -1140,6 +1143,19 @@ void lt_connect(const Ctx<T>& C, const st_material& m, const V3<T>& P, const V3<
         len = l - h;
     }
     if (!(len > T(0))) return;
+    lt_splat(C, P, org, dir, len, h, c, pix, cell, st);
+}
+
+// the connection's end: the emission map taught, the haze on the true segment (haze.js:463-481 hazeShadow), the
+// shadow ray traced, what arrives splatted and counted
+template <class T>
+void lt_splat(const Ctx<T>& C, const V3<T>& P, const V3<T>& org, const V3<T>& dir, T len, T h, V3<T> c, uint32_t pix,
+              uint32_t cell, Stats& st) {
+    if (C.haze.on) {
+        const V3<T> e = org + dir * (len + h) - P;
+        const T el = length(e);
+        c = c * C.haze.transmittance(P, e / std::max(el, T(1e-30)), el, T(C.d.env_radius));
+    }
     if (C.sp_learn && cell < LT_N) {                                               // ltConnect's learn
 #pragma omp atomic
         C.lt_hit[cell]++;
@@ -1154,6 +1170,62 @@ void lt_connect(const Ctx<T>& C, const st_material& m, const V3<T>& P, const V3<
     (*C.splat)[pix * 3 + 2] += (double)c.z;
 #pragma omp atomic
     (*C.ltcount)[pix]++;
+}
+// A PHOTON SCATTERED IN THE HAZE, CONNECTED (haze.js:404-460 ltConnectMedium): the phase function for the lobes,
+// dist / z^3 for the footprint (1 orthographic), from the point itself to 2 offsets short of the camera
+template <class T>
+void lt_connect_medium(const Ctx<T>& C, const V3<T>& P, const V3<T>& din, const V3<T>& phi, U4 ps, uint32_t id,
+                       uint32_t cell, Stats& st) {
+    const st_view& vw = *C.view;
+    const V3<T> right(T(vw.right[0]), T(vw.right[1]), T(vw.right[2])), up(T(vw.up[0]), T(vw.up[1]), T(vw.up[2]));
+    const V3<T> fwd(T(vw.fwd[0]), T(vw.fwd[1]), T(vw.fwd[2])), cam0(T(vw.cam_pos[0]), T(vw.cam_pos[1]), T(vw.cam_pos[2]));
+    const T fx = T(vw.fx), fy = T(vw.fy), F = T(vw.focus_distance);
+    const uint32_t W = C.p.width, H = C.p.height;
+    V3<T> off(T(0));
+    const T R = vw.camtype == 0 ? T(vw.lens_radius) : T(0);
+    if (R > T(0)) {
+        Rng rl = path_rng(ps, id, LT_LENS_SALT);
+        T ul[4]; rl.next4(ul);
+        const T r = R * std::sqrt(ul[0]), ph = T(6.28318530718) * ul[1];
+        off = right * (r * std::cos(ph)) + up * (r * std::sin(ph));
+    }
+    const V3<T> cam = cam0 + off, d = cam - P;
+    V3<T> v;
+    T dist, xx, yy, gm;
+    if (vw.camtype == 0) {
+        dist = length(d);
+        const T z = dot(d, fwd);
+        if (z <= T(1e-4) || dist <= T(1e-4)) return;
+        v = d / dist;
+        if (R > T(0)) {
+            const T c = dot(v, fwd);
+            const V3<T> Fp = off + (-v) * (F / std::max(c, T(1e-30)));
+            xx = dot(Fp, right) / (F * fx);
+            yy = dot(Fp, up) / (F * fy);
+        } else {
+            xx = -dot(d, right) / (z * fx);
+            yy = -dot(d, up) / (z * fy);
+        }
+        gm = dist / (z * z * z);
+    } else {
+        dist = dot(d, fwd);
+        if (dist <= T(1e-4)) return;
+        v = fwd;
+        xx = -dot(d, right) / fx;
+        yy = -dot(d, up) / fy;
+        gm = T(1);
+    }
+    if (std::fabs(xx) >= T(1) || std::fabs(yy) >= T(1)) return;
+    const T apx = T(4) * fx * fy / (T(W) * T(H));
+    const V3<T> c = phi * (hg_eval(dot(din, v), clampT(C.haze.g, T(-0.95), T(0.95))) * gm / apx);
+    if (!(luma(c) > T(0))) return;
+    const T px = clampT((xx + T(1)) * T(0.5) * T(W), T(0), T(W) - T(1));
+    const T py = clampT((yy + T(1)) * T(0.5) * T(H), T(0), T(H) - T(1));
+    const uint32_t pix = (uint32_t)px + (uint32_t)py * W;
+    const T h = T(20) * march_tol(P, C.tol);
+    const T len = dist - h;
+    if (!(len > T(0))) return;
+    lt_splat(C, P, P, v, len, h, c, pix, cell, st);
 }
 template <class T>
 void trace_photon(const Ctx<T>& C, U4 ps, uint32_t id, uint32_t N, std::vector<PhotonRec>& out, Stats& st) {
@@ -1196,11 +1268,27 @@ void trace_photon(const Ctx<T>& C, U4 ps, uint32_t id, uint32_t N, std::vector<P
     r.bounces = 0; r.steps = 0; r.state = RAY_ACTIVE; r.pix = id;
     uint32_t it = 0, seg = 0;
     while (it < C.budget) {
+        // the haze: the leg's collision drawn as it starts, from the photon's own stream (haze.js:255-273 hazeDraw)
+        const bool use_haze = C.haze.on;
+        if (use_haze && r.tmax == T(0)) {
+            V3<T> A = r.pos - r.dir * (std::max(r.ltot - r.absLtot, T(0)) / std::max(r.n, T(1e-4)));
+            Rng hr = path_rng(ps, id, SEED_SALT_HAZE + seg);
+            r.tmax = C.haze.draw(A, r.dir, r.absLtot, r.n, T(C.d.env_radius), hr);
+        }
         uint32_t evals = 0;
-        T dh = march(C, r, st, false, evals);
+        T dh = march(C, r, st, use_haze, evals);
         uint32_t chunks = std::max(1u, (evals + MARCH_CHUNK - 1) / MARCH_CHUNK);
         it = std::min(it + chunks - 1, C.budget - 1);
         bool last = it + 1 == C.budget;
+        if (r.state == RAY_SCATTER) {
+            // a collision in the air (haze.js:491-545, a photon's): the albedo, the connection once past a delta
+            // event, its end
+            r.bounces += 1;
+            r.beta = r.beta * C.haze.albedo;
+            if (C.lt && r.passed && r.bounces <= C.p.maxbounce)
+                lt_connect_medium(C, r.pos, r.dir, r.rad * r.beta, ps, id, cell, st);
+            break;
+        }
         if (r.state != RAY_ACTIVE) break;
         V3<T> nn = hit_normal(C, r.pos, dh);
         bool inside = dh < T(0);
@@ -1241,6 +1329,8 @@ void trace_photon(const Ctx<T>& C, U4 ps, uint32_t id, uint32_t N, std::vector<P
             break;
         }
         r.bounces += 1;
+        r.absLtot = r.ltot;                                                        // the ltot on arrival here
+        r.tmax = T(0);                                                             // the next leg's collision: afresh
         Rng rng = path_rng(ps, id, 1 + seg);
         seg++;
         T n0 = r.n, n1d = std::max(T(m.ior), n0), v1 = T(0);

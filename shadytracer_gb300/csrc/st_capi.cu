@@ -545,7 +545,8 @@ static cudaError_t record_wave(st_ctx* ctx, const WaveArgs& a) {
         for (uint32_t first = 0; first < N; first += C) {
             WaveArgs pa = a;
             pa.slots = std::min(C, N - first);
-            pa.u.haze_on = 0;                    // the map's photons cross the haze unscattered (no volume map)
+            pa.u.photon_pass = 1u;               // photons: the haze's collisions drawn from their own streams; one ends
+                                                 // a photon (with light tracing, after its connection)
             pa.u.sort_on = 0;                    // the sun's photons start in order already (parallel, on a square)
             ctx->rec_launches++;
             if ((e = launch_iter_begin(pa, 0, 1, 1, s))) return e;

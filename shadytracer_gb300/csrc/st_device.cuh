@@ -74,6 +74,7 @@ struct Rng {
 };
 // the sample's seed from the base seed, and a path's generator at an event (0 the camera ray, 1 + i the shade of its
 // i-th segment): seeded by the path, as the reference's optics shade seeds by the ray (optics/kernels.js:598-606)
+#define PHOTON_SEED_SALT 0x50484F54u       // the photons' sample seed: the picture's seed xor this
 __host__ __device__ __forceinline__ uint4 sample_seed(uint32_t base, uint32_t sample) {
     uint4 v = make_uint4(base, sample, 0xA53B3F17u, 0xC0FFEE42u);
     for (int r = 0; r < 2; r++) {
@@ -84,6 +85,10 @@ __host__ __device__ __forceinline__ uint4 sample_seed(uint32_t base, uint32_t sa
         v.x += v.y * v.w; v.y += v.z * v.x; v.z += v.x * v.y; v.w += v.y * v.z;
     }
     return v;
+}
+// the photons' sample seed (their own streams: the photon's id, then its shade count)
+__host__ __device__ __forceinline__ uint4 photon_seed_of(uint32_t base, uint32_t sample) {
+    return sample_seed(base ^ PHOTON_SEED_SALT, sample);
 }
 __device__ __forceinline__ Rng path_rng(uint4 sseed, uint32_t path, uint32_t event) {
     Rng r; r.h = sseed; r.seed(path); r.seed(event); return r;
@@ -125,6 +130,7 @@ struct Uni {
     uint32_t sppm_on, sppm_n, sppm_budget, sppm_learn; float sppm_half, sppm_r1, sppm_alpha;
     // light tracing to the camera (st_photons.cu lt_connect): the photons above connect where they land
     uint32_t lt_on;
+    uint32_t photon_pass;        // the wave's photon pass: its rays are photons, seeded by the photon's own stream
 };
 
 // ------------------------------------------------------------------------------------------------------------

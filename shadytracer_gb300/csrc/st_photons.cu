@@ -23,14 +23,11 @@
 
 namespace st {
 
-#define PHOTON_SEED_SALT 0x50484F54u       // the photons' sample seed: the picture's seed xor this
 #define PHOTON_GEN_SALT 0x5A17u            // their draw at the source (wavefront.js:594 SEED_u32(0x5A17))
 #define SPPM_STORE_SALT 0x53505031u        // a store's and a gather's own stream (wavefront.js:1186)
 #define LT_LENS_SALT 0x4C54434Eu           // a connection's point of the lens, from the photon's own stream
 
-__device__ __forceinline__ uint4 photon_seed(const Uni& u, uint32_t sample) {
-    return sample_seed(u.seed ^ PHOTON_SEED_SALT, sample);
-}
+__device__ __forceinline__ uint4 photon_seed(const Uni& u, uint32_t sample) { return photon_seed_of(u.seed, sample); }
 // sppmEvaluable (wavefront.js prog_sppm, sppm.js:441-444): a diffuse base, or gloss rough enough to evaluate
 __device__ __forceinline__ bool sppm_evaluable(const st_material& m, bool all) {
     const float r = clampf(m.roughness, 0.f, 1.f);
@@ -166,24 +163,24 @@ __global__ void __launch_bounds__(256) k_genphotons(WaveArgs a, uint32_t first, 
         a.pb.dir[i] = make_float4(-w.x, -w.y, -w.z, 1.f);
         a.pb.beta[i] = make_float4(1.f, 1.f, 1.f, 1.f);
         a.pb.rad[i] = make_float4(flux.x, flux.y, flux.z, 0.f);          // a photon's radiance field is its flux
-        a.pb.meta[i] = make_uint4(id, meta_y(0, 0, RAY_ACTIVE), 0u, cell);   // w: its emission cell
+        a.pb.meta[i] = make_uint4(id, meta_y(0, 0, RAY_ACTIVE), 0u, __float_as_uint(0.f));   // w: absLtot (haze.js)
         a.pb.lam[i] = 0.f;
+        a.pb.lprev[i] = make_float2(__uint_as_float(cell), 0.f);        // its emission cell
         a.q.ray[0][i] = i;
     }
 }
 
 // A PHOTON'S CONNECTION TO THE CAMERA (materials_pbr.js:672-830 ltConnect, :598-612 camFootprint, lens.js lensDisc /
-// lensImage): from the point P it landed on (in air, the normal nrm turned to it, arriving along din with flux phi) to
-// the camera -- to a point of the thin lens's disc drawn uniformly from the photon's own stream, or the pinhole --
-// through the lobes a connection owns (the evaluable ones, glossy from LT_MIN_ALPHA up), for the pixel the line lands
-// on: phi f G / A_px, G = |n.v| dist / z^3 (perspective; |n.fwd| orthographic), A_px a pixel's area on the image plane
-// at unit distance. The shadow ray starts on the camera's line of sight to P, as far along it as lifts it 2 offsets off
-// the surface (at grazing views at most 4 such lengths, the rest along the normal, re-aimed at the camera), and stops
-// that height short of the camera. False where nothing connects: behind the camera, off the picture, the camera on
-// the surface's other side, no evaluable lobe, no light.
+// lensImage; haze.js:404-460 ltConnectMedium). From the point P to the camera -- to a point of the thin lens's disc
+// drawn uniformly from the photon's own stream, or the pinhole -- for the pixel the line lands on: phi f G / A_px, A_px
+// a pixel's area on the image plane at unit distance, f the camera's lobes evaluated for the photon's direction (the
+// evaluable ones, glossy from LT_MIN_ALPHA up) or, in the haze, the phase function; G = |n.v| dist / z^3 at a surface
+// and dist / z^3 in the air (perspective; |n.fwd| and 1 orthographic). False where nothing connects: behind the
+// camera, off the picture, the camera on the surface's other side, no evaluable lobe, no light. The haze the line
+// crosses is put on what it carries (haze.js:463-481 hazeShadow).
 struct LtConn { f3 org, dir, c; float len; uint32_t pix; };
-__device__ __forceinline__ bool lt_connect(const Uni& u, const st_material& m, const MfTab& tab, f3 P, f3 nrm, f3 din,
-                                           f3 phi, const uint4& ps, uint32_t id, LtConn& out) {
+struct LtView { f3 cam, v; float dist, gm; uint32_t pix; };
+__device__ __forceinline__ bool lt_view(const Uni& u, f3 P, const uint4& ps, uint32_t id, LtView& o) {
     f3 off = mk(0.f);
     const float R = u.camtype == 0u ? u.lens_r : 0.f;
     if (R > 0.f) {
@@ -194,60 +191,93 @@ __device__ __forceinline__ bool lt_connect(const Uni& u, const st_material& m, c
         sincosf(6.28318530718f * ul.y, &sp, &cp);
         off = u.right * (r * cp) + u.up * (r * sp);
     }
-    if (lobes_none(m, m.transmission, m.haze)) return false;
-    const f3 cam = u.cam + off;
-    const f3 d = cam - P;
-    const float apx = 4.f * u.fx * u.fy / ((float)u.W * (float)u.H);
-    f3 v;
-    float dist, xx, yy, G;
+    o.cam = u.cam + off;
+    const f3 d = o.cam - P;
+    float xx, yy;
     if (u.camtype == 0u) {
-        dist = length(d);
+        o.dist = length(d);
         const float z = dot(d, u.fwd);                                // depth in front of the camera
-        if (z <= 1e-4f || dist <= 1e-4f) return false;
-        v = d * (1.f / dist);
+        if (z <= 1e-4f || o.dist <= 1e-4f) return false;
+        o.v = d * (1.f / o.dist);
         if (R > 0.f) {                                                // where the lens point's ray meets the picture
-            const float c = dot(v, u.fwd);
-            const f3 F = off + (-v) * (u.lens_f / fmaxf(c, 1e-30f));
+            const float c = dot(o.v, u.fwd);
+            const f3 F = off + (-o.v) * (u.lens_f / fmaxf(c, 1e-30f));
             xx = dot(F, u.right) / (u.lens_f * u.fx);
             yy = dot(F, u.up) / (u.lens_f * u.fy);
         } else {
             xx = -dot(d, u.right) / (z * u.fx);
             yy = -dot(d, u.up) / (z * u.fy);
         }
-        G = fabsf(dot(nrm, v)) * dist / (z * z * z);
+        o.gm = o.dist / (z * z * z);
     } else {
-        dist = dot(d, u.fwd);                                          // to the camera plane along the view axis
-        if (dist <= 1e-4f) return false;
-        v = u.fwd;
+        o.dist = dot(d, u.fwd);                                       // to the camera plane along the view axis
+        if (o.dist <= 1e-4f) return false;
+        o.v = u.fwd;
         xx = -dot(d, u.right) / u.fx;
         yy = -dot(d, u.up) / u.fy;
-        G = fabsf(dot(nrm, u.fwd));
+        o.gm = 1.f;
     }
     if (fabsf(xx) >= 1.f || fabsf(yy) >= 1.f) return false;           // off the picture
+    const float px = clampf((xx + 1.f) * 0.5f * (float)u.W, 0.f, (float)u.W - 1.f);
+    const float py = clampf((yy + 1.f) * 0.5f * (float)u.H, 0.f, (float)u.H - 1.f);
+    o.pix = (uint32_t)px + (uint32_t)py * u.W;
+    return true;
+}
+__device__ __forceinline__ float lt_apx(const Uni& u) { return 4.f * u.fx * u.fy / ((float)u.W * (float)u.H); }
+__device__ __forceinline__ void lt_haze(const Uni& u, f3 P, float h, LtConn& out) {
+    if (!u.haze_on) return;
+    const f3 e = out.org + out.dir * (out.len + h) - P;               // the true segment, to the camera
+    const float el = length(e);
+    out.c = out.c * haze_tr(u, P, e * (1.f / fmaxf(el, 1e-30f)), el);
+}
+// at a surface (in air, nrm turned to the photon, which arrives along din with flux phi): the shadow ray starts on the
+// camera's line of sight to P, as far along it as lifts it 2 offsets off the surface (at grazing views at most 4 such
+// lengths, the rest along the normal, re-aimed at the camera), and stops that height short of the camera
+__device__ __forceinline__ bool lt_connect(const Uni& u, const st_material& m, const MfTab& tab, f3 P, f3 nrm, f3 din,
+                                           f3 phi, const uint4& ps, uint32_t id, LtConn& out) {
+    LtView w;
+    if (!lt_view(u, P, ps, id, w)) return false;
+    if (lobes_none(m, m.transmission, m.haze)) return false;
+    const f3 v = w.v;
     const float cv = dot(nrm, v);
     if (cv <= 0.f) return false;                                      // the camera on the surface's other side
     // the camera's own lobes at this vertex, seen along v, in air (the interface air to the material's index)
     const Lobes lb = make_lobes(nrm, v, m, 1.f / fmaxf(m.ior, 1.f), tab, m.transmission, m.specular, m.haze);
     const f3 f = lobes_eval(lb, tab, -din, LT_MIN_ALPHA);
-    const f3 c = phi * f * (G / apx);
-    if (!(luma(c) > 0.f)) return false;
-    const float px = clampf((xx + 1.f) * 0.5f * (float)u.W, 0.f, (float)u.W - 1.f);
-    const float py = clampf((yy + 1.f) * 0.5f * (float)u.H, 0.f, (float)u.H - 1.f);
-    out.pix = (uint32_t)px + (uint32_t)py * u.W;
+    out.c = phi * f * (cv * w.gm / lt_apx(u));
+    if (!(luma(out.c) > 0.f)) return false;
+    out.pix = w.pix;
     const float h = 20.f * march_tol(P, u.tol);                       // offsetTol(P) * 2
     const bool grazing = cv < 0.25f;
     const float sl = h / fmaxf(cv, 0.25f);
     const float lift = grazing ? h - sl * cv : 0.f;
     out.org = P + v * sl + nrm * lift;
     out.dir = v;
-    out.len = dist - sl - cv * lift - h;
+    out.len = w.dist - sl - cv * lift - h;
     if (grazing && u.camtype == 0u) {
-        const f3 toCam = cam - out.org;
+        const f3 toCam = w.cam - out.org;
         const float l = length(toCam);
         out.dir = toCam * (1.f / fmaxf(l, 1e-30f));
         out.len = l - h;
     }
-    out.c = c;
+    lt_haze(u, P, h, out);
+    return out.len > 0.f;
+}
+// in the haze (a collision; the photon arrives along din with flux phi, its albedo in it): no surface, so no side and
+// no lift -- the shadow ray starts at the point and stops 2 offsets short of the camera
+__device__ __forceinline__ bool lt_connect_medium(const Uni& u, f3 P, f3 din, f3 phi, const uint4& ps, uint32_t id,
+                                                  LtConn& out) {
+    LtView w;
+    if (!lt_view(u, P, ps, id, w)) return false;
+    const float ph = hg_eval(dot(din, w.v), clampf(u.hg, -0.95f, 0.95f));
+    out.c = phi * (ph * w.gm / lt_apx(u));
+    if (!(luma(out.c) > 0.f)) return false;
+    out.pix = w.pix;
+    const float h = 20.f * march_tol(P, u.tol);
+    out.org = P;
+    out.dir = w.v;
+    out.len = w.dist - h;
+    lt_haze(u, P, h, out);
     return out.len > 0.f;
 }
 
@@ -286,7 +316,17 @@ __global__ void __launch_bounds__(256) k_photon_shade(WaveArgs a, int nxt, int l
             pos = xyz(p4); ltot = p4.w; dir = xyz(d4); n = d4.w; beta = xyz(b4); rad = xyz(r4);
             bounces = m4.y & 0xffu;
             const uint32_t state = (m4.y >> 16) & 0xffu;
-            if (state == RAY_ACTIVE) {
+            const uint32_t cell = __float_as_uint(a.pb.lprev[slot].x);    // its emission cell
+            if (state == RAY_SCATTER) {
+                // A COLLISION IN THE AIR (haze.js:491-545 mediumVertex, a photon's): the albedo on its weight; once it
+                // has passed a delta event, its connection through the phase function (ltConnectMedium); then its end
+                bounces += 1;
+                beta = beta * u.halb;
+                if (u.lt_on && (m4.y & META_PASSED) != 0u && bounces <= u.maxbounce) {
+                    conn = lt_connect_medium(u, pos, dir, rad * beta, ps, m4.x, lc);
+                    if (conn && u.sppm_learn && cell < LT_CELLS) atomicAdd(&a.sp.lt_hit[cell], 1u);
+                }
+            } else if (state == RAY_ACTIVE) {
                 const float4 sf = a.q.hsurf[q];
                 const uint32_t ids = __float_as_uint(sf.w);
                 const f3 nn = xyz(sf);
@@ -303,7 +343,7 @@ __global__ void __launch_bounds__(256) k_photon_shade(WaveArgs a, int nxt, int l
                     if (u.lt_on && !emissive && passed && fabsf(n - 1.f) <= 1e-3f && bounces + 1u <= u.maxbounce) {
                         conn = lt_connect(u, m, a.tab, pos, nrm, dir, rad * beta, ps, m4.x, lc);
                         // teach the emission map: this cell's photon reached the camera (ltConnect's learn)
-                        if (conn && u.sppm_learn && m4.w < LT_CELLS) atomicAdd(&a.sp.lt_hit[m4.w], 1u);
+                        if (conn && u.sppm_learn && cell < LT_CELLS) atomicAdd(&a.sp.lt_hit[cell], 1u);
                     }
                     if (emissive) {
                     } else if (passed && sppm_evaluable(m, false)) {
@@ -317,6 +357,7 @@ __global__ void __launch_bounds__(256) k_photon_shade(WaveArgs a, int nxt, int l
                     } else {
                         lam = a.pb.lam[slot];
                         bounces += 1;
+                        m4.w = __float_as_uint(ltot);                        // absLtot: the ltot on arrival here
                         uint32_t seg = (m4.y >> 8) & 0xffu;
                         Rng rng = path_rng(ps, m4.x, 1u + seg);
                         seg += 1;
@@ -383,7 +424,8 @@ __global__ void __launch_bounds__(256) k_photon_shade(WaveArgs a, int nxt, int l
                 a.sp.nrm_oct[at] = oct_word(nrm);
                 a.sp.flags[at] = (bounces + 1u) | (sub << SPPM_SUB_SHIFT);
                 // teach the map: this cell paid (with light tracing on, its connections teach it instead)
-                if (!u.lt_on && m4.w < LT_CELLS) atomicAdd(&a.sp.lt_hit[m4.w], 1u);
+                const uint32_t cell = __float_as_uint(a.pb.lprev[slot].x);
+                if (!u.lt_on && cell < LT_CELLS) atomicAdd(&a.sp.lt_hit[cell], 1u);
             } else {
                 atomicAdd(&d->dropped, 1u);
             }
@@ -407,6 +449,7 @@ __global__ void __launch_bounds__(256) k_photon_shade(WaveArgs a, int nxt, int l
             a.pb.pos[slot] = f4(pos, ltot);
             a.pb.dir[slot] = f4(dir, n);
             a.pb.beta[slot] = make_float4(beta.x, beta.y, beta.z, 1.f);
+            if (u.haze_on) a.pb.rad[slot].w = 0.f;                     // a new leg: its collision drawn afresh
             a.pb.meta[slot] = m4;
             if (lam != 0.f) a.pb.lam[slot] = lam;
             outq[rq] = slot;

@@ -625,8 +625,10 @@ __global__ void __launch_bounds__(256) k_shade(WaveArgs a, int nxt, int side, in
                 if (state == RAY_SCATTER) {
                     m4.w = __float_as_uint(ltot);
                     shade_medium(a, pos, dir, beta, sunmis, bounces, state, n, rng, last != 0, sh, emw, ltot, lp);
-                    // haze.js:539: the air is no delta event (out of the map's class and light tracing's)
+                    // haze.js:539: the air is no delta event (out of the map's class); light tracing's class begins
+                    // at a first vertex in the air, as at an evaluable surface, and any later one ends it (:550-553)
                     m4.y &= ~((3u << META_LENS_SHIFT) | META_CAND | META_SPEC);
+                    if (u.lt_on && bounces == 1u) m4.y |= META_CAND;
                 }
                 else
                 {

@@ -103,7 +103,10 @@ __global__ void __launch_bounds__(256, 4) k_march(WaveArgs a, int cur, int nxt, 
                             haze_span(u, A, dir, 1e30f, t0, t1);
                             if (t1 > t0) {
                                 uint32_t tile = slot % u.P, j = slot / u.P, seg = (m4.y >> 8) & 0xffu;
-                                Rng hr = path_rng(sample_seed(u.seed, a.ctr->sample + j), tile, ST_SALT_HAZE + seg);
+                                // a photon's from its own stream (its id), a camera path's from its path's
+                                Rng hr = u.photon_pass
+                                             ? path_rng(photon_seed_of(u.seed, a.ctr->sample), m4.x, ST_SALT_HAZE + seg)
+                                             : path_rng(sample_seed(u.seed, a.ctr->sample + j), tile, ST_SALT_HAZE + seg);
                                 float4 r4 = hr.next();
                                 float t = t0 - logf(1.f - r4.x) / u.hsig;
                                 if (t < t1) tmax = fmaxf(absL + t * n, 1e-30f);

@@ -10,6 +10,8 @@ at them, plus the st_params and st_view of its workload.
 import ctypes as C
 import math
 
+import numpy as np
+
 from .st_types import (StPrim, StMaterial, StSceneDesc, StView, StLight, default_params,
                        ST_LIGHT_DISC, ST_LIGHT_RECTANGLE, ST_LIGHT_COSINE, ST_LIGHT_UNIFORM,
                        ST_PRIM_PLANE, ST_PRIM_SPHERE, ST_PRIM_BOX, ST_PRIM_ROUNDBOX, ST_PRIM_TORUS,
@@ -576,6 +578,72 @@ def lt_pane_closed_form(scene, fresnel):
     el = i["sun_elevation"]
     F = fresnel(math.cos(math.radians(90.0 - el)), 1.0 / i["ior"])
     return i["albedo"] / math.pi * i["E_sun"] * math.sin(math.radians(el)) * (1 - F) ** 2
+
+
+def lt_haze(width=48, height=36, photons=400_000, pane=True, sun_elevation=60.0, ior=1.5, sigma_t=0.3, g=0.5, seed=1,
+            photon_half=2.0):
+    """Light tracing in the haze (haze.js:404-460 ltConnectMedium): a box of haze (1 x 1 x 0.6 m, albedo 1, HG g)
+    under a clear pane (3 x 3 m, 2 cm thick, 1 m up) that the sun lights it through, seen from the side from under the
+    pane. A parallel slab turns no ray, so the haze is lit as without the pane times (1 - F)^2 (each face crossed once,
+    within a depth cap of 3: the faces, one collision): the single scattering light tracing's connections carry
+    (pane=True) is (1 - F)^2 that of the camera's light samples with the pane gone and a cap of 1 (pane=False). A
+    black sky, no floor: a far dark plane keeps the table from being empty."""
+    mats = [air(), glass((1.0, 1.0, 1.0), ior=ior), diffuse((0.0, 0.0, 0.0))]
+    off = 1.0 / math.tan(math.radians(sun_elevation))
+    prims = [prim(ST_PRIM_PLANE, pos=(0.0, 0.0, -50.0), material=2)]
+    if pane:
+        prims.append(prim(ST_PRIM_BOX, pos=(0.0, 0.0, 1.0), params=(1.5, 1.5, 0.01), material=1))
+    haze = {"centre": (0.0, -off * 0.6, 0.4), "half": (0.5, 0.5, 0.3), "sigma_t": sigma_t, "g": g,
+            "albedo": (1.0, 1.0, 1.0)}
+    s = Scene(prims, mats, env_radius=20.0, haze=haze, name="lt-haze")
+    s.params = default_params(width=width, height=height, maxbounce=3 if pane else 1, seed=seed,
+                              sun_elevation=sun_elevation, sun_azimuth=0.0, sun_illuminance=100000.0,
+                              sky_luminance=0.0, ground_luminance=0.0, lt=1 if pane else 0, lt_photons=photons,
+                              sppm_half=photon_half, eps=1e-4)
+    s.view = look_at((-2.5, -off * 0.6, 0.4), (0.0, -off * 0.6, 0.4), 30.0, width / height)
+    s.info = {"ior": ior, "sun_elevation": sun_elevation}
+    return s
+
+
+def lt_haze_single_scatter(scene, fresnel, n_t=4000):
+    """lt_haze's closed form, by quadrature along each pixel's centre ray: the sun's single-scattered light in the box,
+    sum over t of sigma_t p_HG(s . d) E_sun (1 - F)^2 exp(-sigma_t (t - t0)) exp(-sigma_t l_sun) dt (albedo 1), l_sun
+    the way out of the box toward the sun; (H, W), 0 where the ray misses the box."""
+    d, p, v = scene.desc, scene.params, scene.view
+    c = np.array([d.haze_centre[i] for i in range(3)])
+    h = np.array([d.haze_half[i] for i in range(3)])
+    sig, g = d.haze_sigma_t, d.haze_g
+    el, az = math.radians(p.sun_elevation), math.radians(p.sun_azimuth)
+    sun = np.array([math.sin(az) * math.cos(el), math.cos(az) * math.cos(el), math.sin(el)])
+    F = fresnel(math.cos(math.radians(90.0) - el), 1.0 / scene.info["ior"])
+    W, H = p.width, p.height
+    xx, yy = np.meshgrid((np.arange(W) + 0.5) / W * 2 - 1, (np.arange(H) + 0.5) / H * 2 - 1)
+    right, up, fwd = (np.array([getattr(v, k)[i] for i in range(3)]) for k in ("right", "up", "fwd"))
+    cam = np.array([v.cam_pos[i] for i in range(3)])
+    rd = right * (xx[..., None] * v.fx) + up * (yy[..., None] * v.fy) - fwd
+    rd /= np.linalg.norm(rd, axis=-1, keepdims=True)
+
+    def chord(o, dd):                                                 # the slab intersection [t0, t1] of o + dd t
+        with np.errstate(divide="ignore", invalid="ignore"):
+            a = (c - h - o) / dd
+            b = (c + h - o) / dd
+        t0 = np.nanmax(np.minimum(a, b), axis=-1)
+        t1 = np.nanmin(np.maximum(a, b), axis=-1)
+        return np.maximum(t0, 0.0), t1
+
+    t0, t1 = chord(cam, rd)
+    out = np.zeros((H, W))
+    hit = t1 > t0
+    cos = rd @ sun
+    ph = (1 - g * g) / (4 * math.pi * (1 + g * g - 2 * g * cos) ** 1.5)
+    for iy, ix in zip(*np.nonzero(hit)):
+        ts = np.linspace(t0[iy, ix], t1[iy, ix], n_t + 1)
+        tm = 0.5 * (ts[1:] + ts[:-1])
+        x = cam + rd[iy, ix] * tm[:, None]
+        _, ls = chord(x, np.broadcast_to(sun, x.shape))               # the way out toward the sun, from inside
+        integrand = sig * np.exp(-sig * (tm - t0[iy, ix])) * np.exp(-sig * ls)
+        out[iy, ix] = ph[iy, ix] * float(np.sum(integrand) * (ts[1] - ts[0]))
+    return out * p.sun_illuminance * (1 - F) ** 2
 
 
 def floor_mask(scene, margin=0.1):

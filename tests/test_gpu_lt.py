@@ -99,12 +99,12 @@ def test_caustic_with_the_map_matches_the_oracle():
 
 
 def test_caustic_light_tracing_agrees_with_the_map():
-    """The same caustic, seen directly, counted by the connections or by the map's gather at the eye's first surface
-    (the map's estimate biased by its radius, 5 mm here): the two pictures agree over the caustic."""
+    """The same caustic, seen directly, counted by the connections (with the map gathering only past delta events
+    from the eye) or by the map's gather at the eye's first surface too (its estimate biased by its radius, 5 mm
+    here): the two pictures agree, over the whole and over the caustic."""
     mk = lambda: scenes.sppm_caustic(width=96, height=96, photons=1_000_000, r1=0.005)
     a = mk()
     a.params.lt = 1
-    a.params.sppm = 0
     (rgb_a, Va, Sa, _), _, _ = render(a, 16)
     b = mk()
     (rgb_b, Vb, Sb, _), _, _ = render(b, 16)
@@ -112,6 +112,32 @@ def test_caustic_light_tracing_agrees_with_the_map():
     assert abs(La.mean() / Lb.mean() - 1) < 0.02, (La.mean(), Lb.mean())
     bright = Lb > np.quantile(Lb, 0.9)
     assert abs(La[bright].mean() / Lb[bright].mean() - 1) < 0.05, (La[bright].mean(), Lb[bright].mean())
+
+
+def inner_pixels(hit):
+    inner = hit.copy()
+    for dy in (-1, 0, 1):
+        for dx in (-1, 0, 1):
+            inner &= np.roll(np.roll(hit, dy, 0), dx, 1)
+    return inner
+
+
+def test_haze_closed_form_and_the_oracle():
+    """Photons through a pane scattered in a haze box, connected through the phase function (haze.js ltConnectMedium):
+    the single scattering by quadrature along each pixel's ray, and the oracle's picture pixel by pixel."""
+    s = scenes.lt_haze(width=64, height=48, photons=1_000_000)
+    gpu, counts, c = render(s, 32)
+    cf = scenes.lt_haze_single_scatter(s, oracle.fresnel_dielectric)
+    m = inner_pixels(cf > 0)
+    L = gpu[0] @ LUMA
+    assert m.sum() > 500 and c["nonfinite"] == 0
+    assert abs(L[m].sum() / cf[m].sum() - 1) < 0.01, L[m].sum() / cf[m].sum()
+    small = scenes.lt_haze(width=48, height=36, photons=300_000)
+    gpu, counts, _ = render(small, 8)
+    ref = oracle.render(scenes.lt_haze(width=48, height=36, photons=300_000), 8)
+    within_error_bars(gpu, ref)
+    ref_counts = oracle.last_lt_counts(48, 36)
+    assert abs(counts.sum() / ref_counts.sum() - 1) < 0.005, (counts.sum(), ref_counts.sum())
 
 
 def test_invalidate_clears_the_connections():

@@ -99,6 +99,25 @@ def test_light_tracing_pane_closed_form():
     assert b.luma()[m].mean() < 0.05 * cf
 
 
+def inner_pixels(hit):
+    inner = hit.copy()
+    for dy in (-1, 0, 1):
+        for dx in (-1, 0, 1):
+            inner &= np.roll(np.roll(hit, dy, 0), dx, 1)
+    return inner
+
+
+def test_light_tracing_in_the_haze_closed_form():
+    """The oracle's photons scattered in a haze box (haze.js ltConnectMedium: the phase function, dist / z^3, the haze
+    on the connection) against the sun's single scattering through a pane, by quadrature along each pixel's ray."""
+    s = scenes.lt_haze(width=48, height=36)
+    cf = scenes.lt_haze_single_scatter(s, oracle.fresnel_dielectric)
+    a = oracle.render(s, 32)
+    m = inner_pixels(cf > 0)
+    assert m.sum() > 300
+    assert abs(a.luma()[m].sum() / cf[m].sum() - 1) < 0.015, a.luma()[m].sum() / cf[m].sum()
+
+
 def test_lamp_floor_closed_form():
     """The oracle's emitter discovery, list and light sample (materials_pbr.js:887-960, wavefront.js:715-815): the
     floor under a sphere lamp in the dark reads albedo Le a^2 h / D^3, and the list is the lamp's voxels."""
