@@ -680,29 +680,42 @@ def rmse_leg(args, dev):
     return out
 
 
-# the march's DRAM traffic per scene evaluation, from one ncu capture of k_march on the 480 x 270 room at 4 samples
-# (dram__bytes_read.sum + dram__bytes_write.sum over the launch's evaluations), scaled by each launch's evaluations:
-# the path state a ray's refill and hand-off move, spread over its steps (the scene itself is code)
-MARCH_DRAM_BYTES_PER_EVAL = 7.4
-MARCH_DRAM_PROFILE = "profiles/k_march-room24-code-480x270.md"
+# the march's DRAM traffic per scene evaluation: ncu's dram__bytes_read.sum + dram__bytes_write.sum over the 26 march
+# launches of one render of the room at 1920 x 1080, 2 samples (claim 32, chunk 24), over that render's evaluations
+# as the counting pass finds them (15.54 GB / 1.127 G); scaled by each launch's evaluations: the path state a ray's
+# refill and hand-off move, spread over its steps (the scene itself is code)
+MARCH_DRAM_BYTES_PER_EVAL = 13.8
+MARCH_DRAM_PROFILE = "profiles/launches-room24-code-1920x1080-2spp.md"
 
 
 def caustic_rmse_leg(args, dev):
-    """Time to 1 % relative RMSE on the caustic as configured (1024^2, 4 M sun photons a pass, r1 5 mm, alpha 0.7):
-    plain (the sun's photons uniform over their square) against guided (drawn from the learned 128^2 emission map,
-    rebuilt every 4 passes), each against an FP64-accumulated render of 16 x 64 passes. The RMSE over the picture's
-    pixels of the luminance's difference, less the reference's own variance (its pixels' squared standard errors), over
-    the reference's mean; GPU time of the passes (CUDA events), checked every 8 passes up to 1024."""
+    """Time to 1 % relative RMSE on the caustic as configured (1024^2, 4 M sun photons a pass, r1 5 mm, alpha 0.7),
+    four ways: the photon map alone with the sun's photons uniform over their square ("plain") or drawn from the
+    learned 128^2 emission map ("guided"), and the reference's own split -- light tracing to the camera for the caustic
+    seen directly, the map past glass from the eye -- uniform ("lt") or guided ("lt_guided", the map then taught by
+    the connections, as the reference's is).
+
+    Against an FP64-accumulated render of 16 x the runs' passes of the split, on seeds of its own (no pass of it is a
+    pass of a run). The RMSE over the pixels of the luminance's difference, less the reference's own variance (its
+    pixels' squared standard errors), over the reference's mean; over the pixels the reference has converged on (its
+    standard error within 10 % of its value, and below its 99.9th percentile: a camera path that reaches the sun's disc
+    through glass along a line the photons' square does not cover is a single sample of ~1e9 cd/m^2 in a pixel, in any
+    of the four), the largest 0.1 % of each run's squared differences left out (the same rare paths of its own). The
+    passes are timed with CUDA events; past the first checks the error is the noise's, falling as passes^-1/2, so the
+    time to 1 % is the last check's time x (RMSE / 1 %)^2 -- and the ratio of two arms' is their efficiency's."""
     import torch
     from shadytracer_gb300 import scenes
     from shadytracer_gb300.renderer import create_path_tracer
     W = 256 if args.small else 1024
     N = 250_000 if args.small else 4_000_000
-    ref_passes = 16 * (8 if args.small else 64)
-    cap = 256 if args.small else 1024
+    run_passes = 64 if args.small else 256
+    ref_passes = 16 * run_passes
     luma = np.array([0.2126, 0.7152, 0.0722])
     mk = lambda: scenes.sppm_caustic(width=W, height=W, photons=N, r1=0.005, alpha=0.7)
-    rt = create_path_tracer(mk(), device=dev, code=True)
+    ref = mk()
+    ref.params.lt = 1
+    ref.params.seed = 7919                   # the reference's own streams: no pass of it is a pass of the runs
+    rt = create_path_tracer(ref, device=dev, code=True)
     left = ref_passes
     while left > 0:
         rt.step(min(64, left))
@@ -713,72 +726,58 @@ def caustic_rmse_leg(args, dev):
     ok = (S > 0) & (S < 1)
     se2 = np.zeros_like(V)
     se2[ok] = S[ok] * V[ok] / (1 - S[ok])
-    # the sun's glints on the glass (camera paths that reach the disc, 1.6e9 cd/m^2) are a few pixels whose noise
-    # would be the whole RMSE: the metric is over the rest, the brightest 0.1 % of the reference's pixels left out
-    keep = Lref <= np.quantile(Lref, 0.999)
-    noise_ref = float(np.mean(se2[keep]))
-    mean_ref = float(Lref[keep].mean())
-    # the caustic's own pixels (the sphere's shadow on the floor, where the glass focuses the sun): the photon map's
-    # part of the picture, where guiding the photons can change the error
-    cm = scenes.caustic_mask(mk()) & keep
-    noise_c = float(np.mean(se2[cm]))
-    mean_c = float(Lref[cm].mean())
+    keep = (Lref <= np.quantile(Lref, 0.999)) & (np.sqrt(se2) <= 0.1 * np.maximum(Lref, 1.0))
+    cm = scenes.caustic_mask(mk()) & keep           # the sphere's shadow on the floor, seen directly
+    regions = {"picture": (keep, float(np.mean(se2[keep])), float(Lref[keep].mean())),
+               "caustic": (cm, float(np.mean(se2[cm])), float(Lref[cm].mean()))}
+
+    def rmse(L, region):
+        mask, noise, mean = regions[region]
+        d2 = np.sort((L[mask] - Lref[mask]) ** 2)
+        d2 = d2[:max(1, int(len(d2) * 0.999))]
+        return float(np.sqrt(max(d2.mean() - noise, 0.0)) / mean)
+
     out = {"metric": "seconds to 1% relative RMSE vs an FP64 render at 16x the passes", "unit": "s",
            "higher_is_better": False,
-           "workload": "sppm caustic %dx%d, %d sun photons a pass, r1 5 mm, alpha 0.7; reference %d passes (its own "
-                       "relative noise %.4f, taken out); the brightest 0.1 %% of pixels (the sun's glints) left out"
-                       % (W, W, N, ref_passes, np.sqrt(noise_ref) / mean_ref)}
-    for name, learn in (("plain", 0), ("guided", 1)):
+           "workload": "sppm caustic %dx%d, %d sun photons a pass, r1 5 mm, alpha 0.7; %d passes a run, the reference "
+                       "%d passes of light tracing + the map on seeds of its own (its own relative noise %.4f, taken "
+                       "out); %.1f %% of the pixels converged in it" % (W, W, N, run_passes, ref_passes,
+                                                                      np.sqrt(regions["picture"][1]) / regions["picture"][2],
+                                                                      100 * keep.mean()),
+           "caustic_pixels": int(cm.sum())}
+    for name, learn, lt in (("plain", 0, 0), ("guided", 1, 0), ("lt", 0, 1), ("lt_guided", 1, 1)):
         s = mk()
         s.params.sppm_learn = learn
+        s.params.lt = lt
         rt = create_path_tracer(s, device=dev, code=True)
         stream = torch.cuda.ExternalStream(rt.stream(), device=torch.device("cuda", dev))
         rt.step(1)
         rt.invalidate()
-        ms, passes, rm, hit, curve = 0.0, 0, None, None, []
-        rc, hit_c, curve_c, noise64 = None, None, [], None
-        while passes < cap:
+        ms, passes, curve = 0.0, 0, []
+        while passes < run_passes:
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record(stream)
-            rt.step_async(8)
+            rt.step_async(run_passes // 4)
             e1.record(stream)
             rt.sync()
             ms += e0.elapsed_time(e1)
-            passes += 8
-            acc = rt.read_accum()
-            L = acc[0] @ luma
-            rm = float(np.sqrt(max(np.mean((L[keep] - Lref[keep]) ** 2) - noise_ref, 0.0)) / mean_ref)
-            rc = float(np.sqrt(max(np.mean((L[cm] - Lref[cm]) ** 2) - noise_c, 0.0)) / mean_c)
-            # the noise alone over the caustic: the pixels' own error bars (Finch moments), relative to the mean
-            okm = (acc[2] > 0) & (acc[2] < 1)
-            se2m = np.where(okm, acc[2] * acc[1] / np.where(okm, 1 - acc[2], 1.0), 0.0)
-            noise_now = float(np.sqrt(np.mean(se2m[cm])) / mean_c)
-            if passes in (8, 64, 256, 1024) or (rm <= 0.01 and hit is None) or (rc <= 0.01 and hit_c is None):
-                curve.append([passes, round(ms / 1e3, 3), round(rm, 4), round(rc, 4), round(noise_now, 5)])
-            if passes == 64:
-                noise64 = noise_now
-            if rm <= 0.01 and hit is None:
-                hit = ms / 1e3
-            if rc <= 0.01 and hit_c is None:
-                hit_c = ms / 1e3
-            if hit is not None and hit_c is not None:
-                break
+            passes += run_passes // 4
+            L = rt.read_accum()[0] @ luma
+            curve.append([passes, round(ms / 1e3, 3), round(rmse(L, "picture"), 5), round(rmse(L, "caustic"), 5)])
         rt.close()
-        out[name] = {"seconds": hit, "seconds_caustic": hit_c, "passes": passes, "rmse": rm, "rmse_caustic": rc,
-                     "curve (passes, s, rmse, rmse over the caustic, caustic noise)": curve, "ms_per_pass": ms / passes,
-                     "caustic_noise_at_64_passes": noise64}
-    if out["plain"]["seconds"] and out["guided"]["seconds"]:
-        out["speedup"] = out["plain"]["seconds"] / out["guided"]["seconds"]
-    if out["plain"]["seconds_caustic"] and out["guided"]["seconds_caustic"]:
-        out["speedup_caustic"] = out["plain"]["seconds_caustic"] / out["guided"]["seconds_caustic"]
-    out["caustic_pixels"] = int(cm.sum())
-    np_, ng_ = out["plain"]["caustic_noise_at_64_passes"], out["guided"]["caustic_noise_at_64_passes"]
-    if np_ and ng_:
-        # at equal time the noise's variance scales as 1 / passes: the speed-up to equal noise in the caustic
-        out["speedup_to_equal_caustic_noise"] = (np_ / ng_) ** 2 * out["plain"]["ms_per_pass"] / out["guided"]["ms_per_pass"]
-    out["note"] = ("the error against the reference falls as about 1 / passes alike for both: the progressive radius's bias "
-                   "dominates it at 4 M photons a pass, which guiding the emission does not change; the caustic's noise "
-                   "is what it changes")
+        _, t, rp, rc = curve[-1]
+        out[name] = {"seconds": t * (rp / 0.01) ** 2, "seconds_caustic": t * (rc / 0.01) ** 2, "passes": passes,
+                     "rmse": rp, "rmse_caustic": rc, "ms_per_pass": ms / passes,
+                     "curve (passes, s, rmse, rmse over the caustic)": curve}
+
+    def ratio(a, b, key):
+        return out[a][key] / out[b][key] if out[a][key] and out[b][key] else None
+    out["speedup"] = ratio("plain", "guided", "seconds")                 # guided emission, the map alone
+    out["speedup_caustic"] = ratio("plain", "guided", "seconds_caustic")
+    out["speedup_lt_over_plain"] = ratio("plain", "lt", "seconds")       # the reference's split over the map alone
+    out["speedup_lt_over_plain_caustic"] = ratio("plain", "lt", "seconds_caustic")
+    out["speedup_lt_guided_over_lt"] = ratio("lt", "lt_guided", "seconds")   # guided emission within the split
+    out["speedup_lt_guided_over_lt_caustic"] = ratio("lt", "lt_guided", "seconds_caustic")
     return out
 
 
@@ -930,8 +929,8 @@ def run_ours(args):
                          "frac": achieved / peak if peak else None,
                          "traffic": MARCH_DRAM_BYTES_PER_EVAL * evals / max(m_launches, 1),
                          "traffic_unit": "bytes of DRAM read + written per launch: ncu's dram__bytes per scene "
-                                         "evaluation on the 480x270 case (%s) times this launch's evaluations" %
-                                         MARCH_DRAM_PROFILE,
+                                         "evaluation over one render's march launches at 1920x1080, 2 samples (%s), "
+                                         "times this launch's evaluations" % MARCH_DRAM_PROFILE,
                          "kernel": "k_march", "flops_per_launch": per_launch_flops,
                          "flops_per_eval": f_render / max(dw["march_steps"], 1),
                          "flops_per_eval_whole_table": f_table,

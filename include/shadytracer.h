@@ -231,7 +231,24 @@ typedef struct st_params {
     uint32_t lt;                  /* 1 on (the reference's photoncount > 0)                          */
     uint32_t lt_photons;          /* photons a sample with the photon map off (0: one a pixel); with it on, its
                                    * sppm_photons serve both, and sppm_half is the photons' square either way */
+    /* THE ENVIRONMENT'S PRESETS (core/environment.js, the reference's environment as code with its presets' text):
+     * ST_ENV_ANALYTIC the disc of sun_illuminance in a uniform sky (sky_luminance above the horizon, ground_luminance
+     * below); ST_ENV_SUNSKY the sun and sky physically (SUNSKY_FN): sunlight of sun_outside lux above the atmosphere, a
+     * 5778 K white, through air (Rayleigh), aerosol (Mie, Henyey-Greenstein 0.7, albedo 0.9) and ozone in 16 bands of
+     * the spectrum, the disc what the air lets through and the sky that light scattered once toward the eye;
+     * ST_ENV_STUDIO an even light brighter above (STUDIO_FN), no sun. The two presets are baked into the map light
+     * sampling draws half its environment samples from, as an image is (an image, st_set_env_image, replaces all). */
+    uint32_t env_mode;
+    float    sun_outside;         /* ST_ENV_SUNSKY: lx above the atmosphere (0: 128 000)             */
+    float    sky_turbidity;       /* ST_ENV_SUNSKY: the aerosol's depth at 550 nm is 0.05 + 0.1 x this (0.7 a clear day) */
+    float    studio_illuminance;  /* ST_ENV_STUDIO: lx on a level surface facing up                   */
+    float    studio_top;          /* ST_ENV_STUDIO: 0 even, 1 none from straight below (L0 (1 + top z)) */
+    float    studio_color[3];     /* ST_ENV_STUDIO: its colour (normalised to luminance 1)             */
 } st_params;
+
+#define ST_ENV_ANALYTIC 0u
+#define ST_ENV_SUNSKY   1u
+#define ST_ENV_STUDIO   2u
 
 /* The camera, as genrays reads it (core/genrays.js:65-92): the basis from invView's columns and the
  * two diagonal entries of invProjection. */
@@ -538,7 +555,8 @@ int  st_emit_list(st_ctx* ctx, float* out, uint32_t max_n, uint32_t* n);
  * serialises them. The first call on a device does the set-up (the array's address, the albedo tables) and should
  * come before any stream capture. The caller's current device is as it was when the call returns. The result equals
  * st_step's for the same inputs. What this render does not carry is refused with ST_ERR_ARG, and
- * st_last_error(NULL) says why: light faces, st_params.sppm, st_params.lt, st_params.guide, st_params.step_cache, and an emissive
+ * st_last_error(NULL) says why: light faces, st_params.sppm, st_params.lt, st_params.guide, st_params.step_cache,
+ * st_params.env_mode other than ST_ENV_ANALYTIC, and an emissive
  * material unless st_params.emit_off is set (then both paths render it by the BSDF's hits alone). */
 #define ST_NOALLOC_MAX_PIXELS (128u * 128u)
 #define ST_NOALLOC_SCRATCH_BYTES (8u << 20)

@@ -1408,6 +1408,11 @@ static int render_impl(const st_scene_desc* s, const st_params* p, const st_view
     if (cull) { boxes = cull_boxes(*s); C.cull = &boxes; }
     C.s = s; C.p = *p; C.d = derive(*p, *s);
     C.env.init(*p, C.d);
+    std::vector<float> preset_tex;                  // a preset's map (the image's is its own)
+    if (C.env.mode != 0 && !C.env.img) {
+        preset_tex = preset_map(C.env);
+        C.env.init(*p, C.d, &preset_tex);
+    }
     C.tb = tables<T>();
     C.tol = T(C.d.tol_setting);
     C.envR2 = T(C.d.env_radius * C.d.env_radius);

@@ -64,11 +64,66 @@ inline void env_tables(const std::vector<double>& lum, std::vector<float>& tex) 
     }
 }
 
+// THE SUN AND SKY'S BANDS (environment.js SKY_BAND_TABLE), in double: 16 bands of 380-730 nm sampled at every
+// nanometre from each band's start, sunlight above the air (Planck, 5778 K) times the CIE 1931 functions (the
+// Wyman-Sloan-Shirley fit, as the spectral table's) to linear Rec.709, the sixteen scaled to luminance 1 together;
+// each band's middle (weighted by x + y + z), its Rayleigh depth there (Hansen & Travis 1974 eq. 2.29), Angstrom's
+// aerosol factor (l / 550)^-1.3 and the ozone's depth (the Chappuis band's 223 K cross-section, 300 Dobson units)
+struct SkyBand { double tauR, haze, ozone, nm, rgb[3]; };
+inline const std::vector<SkyBand>& sky_bands() {
+    static std::vector<SkyBand> bands;
+    if (!bands.empty()) return bands;
+    static const double sigma[16] = {6.2648e-24, 3.1169e-23, 1.0195e-22, 2.4886e-22, 5.4883e-22, 1.1517e-21, 2.0211e-21,
+                                     3.0497e-21, 4.2480e-21, 4.5252e-21, 4.7153e-21, 3.4726e-21, 2.3885e-21, 1.5936e-21,
+                                     9.8370e-22, 6.3061e-22};
+    auto lobe = [](double l, double mu, double lo, double hi) {
+        const double t = (l - mu) / (l < mu ? lo : hi);
+        return std::exp(-0.5 * t * t);
+    };
+    const double step = 350.0 / 16.0;
+    double tot[3] = {0, 0, 0};
+    for (int k = 0; k < 16; k++) {
+        double X = 0, Y = 0, Z = 0, wl = 0, ws = 0;
+        for (double l = 380.0 + k * step; l < 380.0 + (k + 1) * step; l += 1.0) {
+            const double li = std::round(l), m = l * 1e-9;
+            const double w = 1.0 / (std::pow(m, 5) * (std::exp(1.438776877e-2 / (m * 5778.0)) - 1.0));
+            const double x = 1.056 * lobe(li, 599.8, 37.9, 31.0) + 0.362 * lobe(li, 442.0, 16.0, 26.7) -
+                             0.065 * lobe(li, 501.1, 20.4, 26.2);
+            const double y = 0.821 * lobe(li, 568.8, 46.9, 40.5) + 0.286 * lobe(li, 530.9, 16.3, 31.1);
+            const double z = 1.217 * lobe(li, 437.0, 11.8, 36.0) + 0.681 * lobe(li, 459.0, 26.0, 13.8);
+            X += w * x; Y += w * y; Z += w * z;
+            wl += w * (x + y + z) * l; ws += w * (x + y + z);
+        }
+        SkyBand b;
+        b.nm = wl / ws;
+        const double um = b.nm / 1000.0;
+        b.tauR = 0.008569 * std::pow(um, -4.0) * (1 + 0.0113 * std::pow(um, -2.0) + 0.00013 * std::pow(um, -4.0));
+        b.haze = std::pow(b.nm / 550.0, -1.3);
+        b.ozone = sigma[k] * 300.0 * 2.6867e16;
+        b.rgb[0] = 3.2404542 * X - 1.5371385 * Y - 0.4985314 * Z;
+        b.rgb[1] = -0.9692660 * X + 1.8760108 * Y + 0.0415560 * Z;
+        b.rgb[2] = 0.0556434 * X - 0.2040259 * Y + 1.0572252 * Z;
+        for (int c = 0; c < 3; c++) tot[c] += b.rgb[c];
+        bands.push_back(b);
+    }
+    const double Yt = LUMA_R * tot[0] + LUMA_G * tot[1] + LUMA_B * tot[2];
+    for (auto& b : bands)
+        for (int c = 0; c < 3; c++) b.rgb[c] /= Yt;
+    return bands;
+}
+// Kasten-Young relative air mass (sdf.js:96-100)
+inline double air_mass(double cz) {
+    const double c = std::min(std::max(cz, 0.0), 1.0);
+    const double zdeg = std::acos(c) * 180.0 / PI_D;
+    return 1.0 / (c + 0.15 * std::pow(std::max(93.885 - zdeg, 0.1), -1.253));
+}
+
 struct Derived {
     double sun_half, sun_omc, sun_sin2, sun_omega, disc_lum;
     double sun_tint[3];
     double sun_dir[3];
     int sun_on;
+    uint32_t env_mode;
     double nee_sun_pick;
     double tol_setting;        // tolSetting(): eps, else the scene's
     double env_radius;
@@ -86,8 +141,10 @@ inline Derived derive(const st_params& p, const st_scene_desc& s) {
     double y = raw[0] * LUMA_R + raw[1] * LUMA_G + raw[2] * LUMA_B;
     for (int i = 0; i < 3; i++) d.sun_tint[i] = raw[i] / y;
     bool furnace = p.env_uniform > 0;
+    // the presets (environment.js): an image or the furnace replaces them; the studio has no sun to aim at
+    d.env_mode = (furnace || env_image_state().on() || p.env_mode > 2) ? 0u : p.env_mode;
     d.sun_on = (p.sun_hint != 0 && p.sun_elevation * PI_D / 180.0 + half > 0 && !furnace &&          // photometry.js:194
-                !env_image_state().on()) ? 1 : 0;                                                 // an image: no sun
+                !env_image_state().on() && d.env_mode != 2) ? 1 : 0;                              // an image: no sun
     d.nee_sun_pick = (d.sun_on && p.env_sun_gain > 0) ? p.nee_sun_pick : 0.0;                        // photometry.js:226
     d.tol_setting = p.eps > 0 ? p.eps : (s.tolerance > 0 ? s.tolerance : 1e-3);                     // photometry.js:141-150
     d.env_radius = s.env_radius > 0 ? s.env_radius : 400.0;                                          // photometry.js:158
@@ -320,11 +377,26 @@ template <class T> struct Env {
     V3<T> sun_dir; T sun_sin2, sun_omc, sun_omega; int sun_on; T pick;
     V3<T> disc; T sky, ground, uniform, sun_gain, sky_gain;
     const EnvImage* img = nullptr;          // the environment image, and its map's share of the samples
+    const std::vector<float>* tex = nullptr; // the map's tables: the image's, or a preset's
     T mshare = 0;
-    void init(const st_params& p, const Derived& d) {
+    // the presets: the mode, the sun and sky's light above the air and aerosol depth at 550 nm; the studio's L0, top
+    // and colour
+    uint32_t mode = 0;
+    double sun_outside = 128000.0, aerosol = 0.12, st_l0 = 0.0, st_top = 0.0, st_tint[3] = {1, 1, 1};
+    void init(const st_params& p, const Derived& d, const std::vector<float>* preset_tex = nullptr) {
         const EnvImage& im = env_image_state();
         img = im.on() ? &im : nullptr;
-        mshare = (img && !p.env_map_off) ? T(0.5) : T(0);
+        mode = d.env_mode;
+        sun_outside = p.sun_outside > 0.f ? p.sun_outside : 128000.0;
+        aerosol = 0.05 + 0.1 * std::max(0.0, (double)p.sky_turbidity);
+        st_top = std::min(std::max((double)p.studio_top, 0.0), 1.0);
+        double c[3] = {std::max(0.0, (double)p.studio_color[0]), std::max(0.0, (double)p.studio_color[1]),
+                       std::max(0.0, (double)p.studio_color[2])};
+        const double yc = std::max(c[0] * LUMA_R + c[1] * LUMA_G + c[2] * LUMA_B, 1e-6);
+        for (int k = 0; k < 3; k++) st_tint[k] = c[k] / yc;
+        st_l0 = std::max(0.0, (double)p.studio_illuminance) / (PI_D * (1.0 + 2.0 * st_top / 3.0));
+        tex = img ? &im.tex : (mode != 0 ? preset_tex : nullptr);
+        mshare = (tex && !p.env_map_off) ? T(0.5) : T(0);
         sun_dir = V3<T>(T(d.sun_dir[0]), T(d.sun_dir[1]), T(d.sun_dir[2]));
         sun_sin2 = T(d.sun_sin2); sun_omc = T(d.sun_omc); sun_omega = T(d.sun_omega); sun_on = d.sun_on;
         pick = T(d.nee_sun_pick);
@@ -332,10 +404,39 @@ template <class T> struct Env {
         sky = T(p.sky_luminance); ground = T(p.ground_luminance); uniform = T(p.env_uniform);
         sun_gain = T(std::max(0.f, p.env_sun_gain)); sky_gain = T(std::max(0.f, p.env_sky_gain));
     }
-    V3<T> sky_only(const V3<T>& dir) const {                        // sdf.js skyRadiance: no disc
-        bool cone = sun_on && in_sun_disc(dir);
-        V3<T> b = img ? image(dir) : (uniform > T(0) ? V3<T>(uniform) : V3<T>(normalize(dir).z > T(0) ? sky : ground));
-        return b * (cone ? sun_gain : sky_gain);
+    V3<T> sky_only(const V3<T>& dir) const {                        // sdf.js skyRadiance: nothing in the cone
+        if (sun_on && in_sun_disc(dir)) return V3<T>(0);
+        return base(dir) * sky_gain;
+    }
+    // THE SUN AND SKY, PHYSICALLY (environment.js SUNSKY_FN), in double
+    V3<T> sun_sky(const V3<T>& d) const {
+        const double sz = (double)sun_dir.z, dz = (double)d.z;
+        const double mv = air_mass(std::max(dz, 0.0)), ms = air_mass(std::max(sz, 0.0));
+        const bool disc_in = in_sun_disc(d) && sz > -std::sqrt((double)sun_sin2);
+        const double c = (double)dot(d, sun_dir), g = 0.7;
+        const double phR = 3.0 / (16.0 * PI_D) * (1.0 + c * c);
+        const double phM = (1.0 - g * g) / (4.0 * PI_D * std::pow(1.0 + g * g - 2.0 * g * c, 1.5));
+        const double up = std::min(std::max((sz + 0.05) / 0.05, 0.0), 1.0);
+        const double dm = mv - ms;
+        double L[3] = {0, 0, 0};
+        for (const SkyBand& b : sky_bands()) {
+            const double tr = b.tauR, ta = aerosol * b.haze, tau = tr + ta + b.ozone;
+            double v;
+            if (disc_in) v = std::exp(-tau * ms) / (PI_D * (double)sun_sin2);
+            else {
+                const double k1 = std::fabs(dm) < 1e-3 ? tau * mv * std::exp(-tau * mv)
+                                                       : mv * (std::exp(-tau * ms) - std::exp(-tau * mv)) / dm;
+                v = (tr * phR + 0.9 * ta * phM) / tau * k1 * up;
+            }
+            for (int k = 0; k < 3; k++) L[k] += b.rgb[k] * v;
+        }
+        return V3<T>(T(std::max(L[0], 0.0) * sun_outside), T(std::max(L[1], 0.0) * sun_outside),
+                     T(std::max(L[2], 0.0) * sun_outside));
+    }
+    // THE STUDIO (environment.js STUDIO_FN)
+    V3<T> studio(const V3<T>& d) const {
+        const double v = st_l0 * std::max(1.0 + st_top * (double)d.z, 0.0);
+        return V3<T>(T(st_tint[0] * v), T(st_tint[1] * v), T(st_tint[2] * v));
     }
     bool in_sun_disc(const V3<T>& dir) const {                       // sdf.js:91-96
         V3<T> L = normalize(dir);
@@ -355,7 +456,7 @@ template <class T> struct Env {
     // envMapSample / envMapPdf (envmap.js:54-98): a row down column 0's CDF, a column along the row's, a point uniform
     // in (azimuth, z) inside the texel
     V3<T> map_sample(T ux, T uy) const {
-        const std::vector<float>& m = img->tex;
+        const std::vector<float>& m = *tex;
         auto at = [&](int x, int y, int c) { return (T)m[4 * ((size_t)y * ENV_MW + x) + c]; };
         int lo = 0, hi = ENV_MH - 1;
         while (lo < hi) { int mid = (lo + hi) / 2; if (ux < at(0, mid, 2)) hi = mid; else lo = mid + 1; }
@@ -378,11 +479,13 @@ template <class T> struct Env {
         a -= std::floor(a);
         const int col = std::min(std::max((int)(a * T(ENV_MW)), 0), ENV_MW - 1);
         const int row = std::min(std::max((int)((T(1) - d.z) * T(0.5) * T(ENV_MH)), 0), ENV_MH - 1);
-        return (T)img->tex[4 * ((size_t)row * ENV_MW + col) + 1];
+        return (T)(*tex)[4 * ((size_t)row * ENV_MW + col) + 1];
     }
     V3<T> base(const V3<T>& dir) const {                             // sdf.js:121-130 envBase
         if (img) return image(dir);
         if (uniform > T(0)) return V3<T>(uniform);
+        if (mode == 1) return sun_sky(normalize(dir));
+        if (mode == 2) return studio(normalize(dir));
         V3<T> c = background(normalize(dir));
         return vmax(c, T(0));
     }
@@ -401,6 +504,29 @@ template <class T> struct Env {
         return normalize(b1 * (std::cos(phi) * sinT) + b2 * (std::sin(phi) * sinT) + sd * cosT);
     }
 };
+// A PRESET'S MAP (envmap.js:100-150 prog_envbake, as the library bakes it): per texel of the equal-area map the
+// environment's own light at 2 x 2 stratified points, the sun's cone left out where there is one, its mean luminance;
+// then the tables
+template <class T> inline std::vector<float> preset_map(const Env<T>& e) {
+    std::vector<double> lum((size_t)ENV_MW * ENV_MH);
+    for (int i = 0; i < ENV_MW * ENV_MH; i++) {
+        const int x = i % ENV_MW, y = i / ENV_MW;
+        double acc = 0;
+        for (int sy = 0; sy < 2; sy++)
+            for (int sx = 0; sx < 2; sx++) {
+                const double ux = (x + (sx + 0.5) * 0.5) / ENV_MW, uy = (y + (sy + 0.5) * 0.5) / ENV_MH;
+                const double z = 1 - 2 * uy, sz = std::sqrt(std::max(0.0, 1 - z * z)), ph = 2 * PI_D * ux;
+                const V3<T> d(T(sz * std::cos(ph)), T(sz * std::sin(ph)), T(z));
+                if (e.sun_on && e.in_sun_disc(d)) continue;
+                const V3<T> c = e.base(d);
+                acc += LUMA_R * (double)c.x + LUMA_G * (double)c.y + LUMA_B * (double)c.z;
+            }
+        lum[i] = 0.25 * acc;
+    }
+    std::vector<float> tex;
+    env_tables(lum, tex);
+    return tex;
+}
 // sampleCosineHemi (tracebasics.js:655-665)
 template <class T> inline V3<T> sample_cosine_hemi(const V3<T>& n, T u0, T u1) {
     T r = std::sqrt(u0);

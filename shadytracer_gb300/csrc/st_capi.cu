@@ -18,6 +18,7 @@
 
 #include "st_internal.h"
 #include "st_ext.h"
+#include "st_sky.h"
 #include "st_spectral.h"
 
 #define SPPM_WAVE_BUDGET 512u                 // records a gather walks before it subsamples (sppm.js SPPM_VISIT)
@@ -52,6 +53,8 @@ struct st_ctx {
     float4* d_envimg = nullptr;           // the environment image (rgb, 0) and its map's tables; null, none
     float4* d_envmap = nullptr;
     uint32_t env_w = 0, env_h = 0;
+    float4* d_skytab = nullptr;           // the sun and sky's 16 bands (st_sky.h), once a context
+    std::vector<float> env_key;           // what the preset's map was baked from (empty: no preset map)
     float env_lum = 0.f, env_turn = 0.f;
     st_material* d_mats = nullptr;
     st_params params{};
@@ -205,8 +208,11 @@ Uni make_uni_base(const st_scene_desc& s, const st_params& p, const st_view& v, 
     const double raw[3] = {1.0, 0.96, 0.9};
     double y = raw[0] * 0.2126 + raw[1] * 0.7152 + raw[2] * 0.0722;
     bool furnace = p.env_uniform > 0;
+    // the presets (environment.js): the image or the furnace replace them; the studio has no sun to aim at
+    const uint32_t env_mode = (furnace || env_image || p.env_mode > ST_ENV_STUDIO) ? 0u : p.env_mode;
     // an environment image is the whole environment, with no sun to aim at (envimage.js, the image preset)
-    int sun_on = (p.sun_hint != 0 && p.sun_elevation * PI_D / 180.0 + half > 0 && !furnace && !env_image) ? 1 : 0;
+    int sun_on = (p.sun_hint != 0 && p.sun_elevation * PI_D / 180.0 + half > 0 && !furnace && !env_image &&
+                  env_mode != ST_ENV_STUDIO) ? 1 : 0;
     double e = p.sun_elevation * PI_D / 180.0, az = p.sun_azimuth * PI_D / 180.0;
     u.sun_dir = mk((float)(std::cos(e) * std::sin(az)), (float)(std::cos(e) * std::cos(az)), (float)std::sin(e));
     u.sun_sin2 = (float)sin2;
@@ -217,6 +223,18 @@ Uni make_uni_base(const st_scene_desc& s, const st_params& p, const st_view& v, 
     u.disc = mk((float)(disc * raw[0] / y), (float)(disc * raw[1] / y), (float)(disc * raw[2] / y));
     u.sky = p.sky_luminance; u.ground = p.ground_luminance; u.uniform = p.env_uniform;
     u.sun_gain = std::max(0.f, p.env_sun_gain); u.sky_gain = std::max(0.f, p.env_sky_gain);
+    u.env_mode = env_mode;
+    u.sun_outside = p.sun_outside > 0.f ? p.sun_outside : 128000.f;              // environment.js: 128 klx
+    u.aerosol = (float)(0.05 + 0.1 * std::max(0.0, (double)p.sky_turbidity));
+    {
+        const double top = std::min(std::max((double)p.studio_top, 0.0), 1.0);
+        double c[3] = {std::max(0.0, (double)p.studio_color[0]), std::max(0.0, (double)p.studio_color[1]),
+                       std::max(0.0, (double)p.studio_color[2])};
+        const double y = std::max(c[0] * 0.2126 + c[1] * 0.7152 + c[2] * 0.0722, 1e-6);
+        u.studio_l0 = (float)(std::max(0.0, (double)p.studio_illuminance) / (PI_D * (1.0 + 2.0 * top / 3.0)));
+        u.studio_top = (float)top;
+        u.studio_tint = mk((float)(c[0] / y), (float)(c[1] / y), (float)(c[2] / y));
+    }
     u.haze_on = s.haze_sigma_t > 0 ? 1 : 0;
     u.hc = mk(s.haze_centre[0], s.haze_centre[1], s.haze_centre[2]);
     u.hu = mk(s.haze_axes[0], s.haze_axes[1], s.haze_axes[2]);
@@ -246,6 +264,10 @@ static Uni make_uni(const st_ctx* ctx) {
     if (ctx->d_envimg) {
         u.env_img = ctx->d_envimg; u.env_w = ctx->env_w; u.env_h = ctx->env_h;
         u.env_lum = ctx->env_lum; u.env_turn = ctx->env_turn;
+    }
+    u.sky_tab = ctx->d_skytab;
+    // the map light sampling draws from: an image's, or a preset's (envmap.js bakes one for every environment)
+    if (ctx->d_envimg || (u.env_mode != ST_ENV_ANALYTIC && !ctx->env_key.empty())) {
         u.env_map = ctx->d_envmap;
         u.env_mshare = ctx->d_envmap && !p.env_map_off ? 0.5f : 0.f;    // ENV_MAP_SHARE
     }
@@ -722,7 +744,7 @@ int st_destroy(st_ctx* ctx) {
     free_wave(ctx);
     ext_free(ctx->ext);
     if (ctx->has_code) scene_code_free(ctx->code);
-    for (void* p : {(void*)ctx->d_prims, (void*)ctx->d_faces, (void*)ctx->d_envimg, (void*)ctx->d_envmap, (void*)ctx->d_sc,
+    for (void* p : {(void*)ctx->d_prims, (void*)ctx->d_faces, (void*)ctx->d_envimg, (void*)ctx->d_envmap, (void*)ctx->d_skytab, (void*)ctx->d_sc,
                     (void*)ctx->d_mats, (void*)ctx->d_ec, (void*)ctx->d_ecavg,
                     (void*)ctx->d_e1, (void*)ctx->d_ctr, (void*)ctx->d_spec})
         if (p) cudaFree(p);
@@ -817,6 +839,7 @@ int st_set_scene(st_ctx* ctx, const char* cuda_src, const st_scene_desc* d, char
     return st_invalidate(ctx);
 }
 
+static int env_preset_ensure(st_ctx* ctx);
 int st_set_params(st_ctx* ctx, const st_params* p, uint64_t* unknown_mask) {
     if (!ctx || !p) return ST_ERR_ARG;
     if (ctx->in_flight) return fail(ctx, ST_ERR_BUSY, "a trace is in flight: st_sync first");
@@ -829,6 +852,7 @@ int st_set_params(st_ctx* ctx, const st_params* p, uint64_t* unknown_mask) {
     if (p->budget > 256) return fail(ctx, ST_ERR_ARG, "budget out of range (0..256)");
     if (p->samples_per_wave > 1024) return fail(ctx, ST_ERR_ARG, "samples_per_wave out of range (0..1024)");
     if (p->lt > 1) return fail(ctx, ST_ERR_ARG, "lt is 0 or 1");
+    if (p->env_mode > ST_ENV_STUDIO) return fail(ctx, ST_ERR_ARG, "env_mode out of range (ST_ENV_*)");
     cudaSetDevice(ctx->device);
     bool resize = p->width != ctx->params.width || p->height != ctx->params.height ||
                   p->samples_per_wave != ctx->params.samples_per_wave || !ctx->has_params;
@@ -836,6 +860,10 @@ int st_set_params(st_ctx* ctx, const st_params* p, uint64_t* unknown_mask) {
     ctx->has_params = true;
     ctx->W = p->width; ctx->H = p->height; ctx->P = p->width * p->height;
     invalidate_graph(ctx);
+    {
+        int rc = env_preset_ensure(ctx);
+        if (rc) return rc;
+    }
     if (resize) {
         free_wave(ctx);
         int rc = ensure_wave(ctx);
@@ -878,17 +906,65 @@ int st_env_map_tables(const float* lum, float* tex) {
     return ST_OK;
 }
 
+// THE MAP, baked on the GPU from the environment as it returns it (the image, or a preset), tabulated here
+static int env_map_bake(st_ctx* ctx) {
+    if (ctx->d_envmap) { cudaFree(ctx->d_envmap); ctx->d_envmap = nullptr; }
+    Uni u = make_uni(ctx);
+    float* d_lum = nullptr;
+    CK(cudaMalloc(&d_lum, (size_t)ENV_MW * ENV_MH * sizeof(float)), "cudaMalloc environment bake");
+    std::vector<float> lum((size_t)ENV_MW * ENV_MH);
+    cudaError_t e = launch_env_bake(u, d_lum, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(lum.data(), d_lum, lum.size() * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    cudaFree(d_lum);
+    if (e != cudaSuccess) return fail(ctx, ST_ERR_CUDA, std::string("environment bake: ") + cudaGetErrorString(e));
+    std::vector<float> tex(lum.size() * 4);
+    st_env_map_tables(lum.data(), tex.data());
+    CK(cudaMalloc(&ctx->d_envmap, tex.size() * sizeof(float)), "cudaMalloc environment map");
+    CK(cudaMemcpyAsync(ctx->d_envmap, tex.data(), tex.size() * sizeof(float), cudaMemcpyHostToDevice, ctx->stream),
+       "environment map upload");
+    CK(cudaStreamSynchronize(ctx->stream), "environment map upload");
+    return ST_OK;
+}
+// a preset's map, made again when what it is baked from changes (no image: an image's map is its own)
+static int env_preset_ensure(st_ctx* ctx) {
+    const st_params& p = ctx->params;
+    if (ctx->d_envimg) return ST_OK;
+    if (p.env_mode == ST_ENV_ANALYTIC || p.env_mode > ST_ENV_STUDIO || p.env_uniform > 0.f) {
+        if (!ctx->env_key.empty()) {
+            if (ctx->d_envmap) { cudaFree(ctx->d_envmap); ctx->d_envmap = nullptr; }
+            ctx->env_key.clear();
+        }
+        return ST_OK;
+    }
+    if (!ctx->d_skytab) {
+        const std::vector<double> t = sky_band_table();
+        std::vector<float> f(t.begin(), t.end());
+        CK(cudaMalloc(&ctx->d_skytab, f.size() * sizeof(float)), "cudaMalloc sky table");
+        CK(cudaMemcpy(ctx->d_skytab, f.data(), f.size() * sizeof(float), cudaMemcpyHostToDevice), "sky table upload");
+    }
+    const std::vector<float> key = {(float)p.env_mode, p.sun_elevation, p.sun_azimuth, p.sun_diameter, p.sun_outside,
+                                    p.sky_turbidity, p.studio_illuminance, p.studio_top, p.studio_color[0],
+                                    p.studio_color[1], p.studio_color[2], (float)p.sun_hint};
+    if (key == ctx->env_key && ctx->d_envmap) return ST_OK;
+    ctx->env_key = key;
+    return env_map_bake(ctx);
+}
+
 int st_set_env_image(st_ctx* ctx, const float* rgb, uint32_t w, uint32_t h, float luminance, float turn_deg) {
     if (!ctx) return ST_ERR_ARG;
     if (ctx->in_flight) return fail(ctx, ST_ERR_BUSY, "a trace is in flight: st_sync first");
     cudaSetDevice(ctx->device);
-    if (!rgb) {                                           // back to the sun and sky
+    if (!rgb) {                                           // back to the sun and sky (or the preset)
         if (ctx->d_envimg) cudaFree(ctx->d_envimg);
         if (ctx->d_envmap) cudaFree(ctx->d_envmap);
         ctx->d_envimg = ctx->d_envmap = nullptr;
         ctx->env_w = ctx->env_h = 0;
+        ctx->env_key.clear();
         invalidate_graph(ctx);
-        return ctx->has_params ? st_invalidate(ctx) : ST_OK;
+        if (!ctx->has_params) return ST_OK;
+        int rc = env_preset_ensure(ctx);
+        return rc ? rc : st_invalidate(ctx);
     }
     if (w < 2 || h < 1 || w > 16384 || h > 8192) return fail(ctx, ST_ERR_ARG, "environment image size out of range");
     if (!(luminance >= 0.f) || !std::isfinite(turn_deg)) return fail(ctx, ST_ERR_ARG, "bad luminance or turn");
@@ -905,23 +981,9 @@ int st_set_env_image(st_ctx* ctx, const float* rgb, uint32_t w, uint32_t h, floa
     ctx->env_w = w; ctx->env_h = h;
     ctx->env_lum = luminance > 0.f ? luminance : 179.f;
     ctx->env_turn = turn_deg;
-    if (ctx->d_envmap) { cudaFree(ctx->d_envmap); ctx->d_envmap = nullptr; }
-    // the map: baked on the GPU from the image as the environment returns it, tabulated here
-    Uni u = make_uni(ctx);
-    float* d_lum = nullptr;
-    CK(cudaMalloc(&d_lum, (size_t)ENV_MW * ENV_MH * sizeof(float)), "cudaMalloc environment bake");
-    std::vector<float> lum((size_t)ENV_MW * ENV_MH);
-    cudaError_t e = launch_env_bake(u, d_lum, ctx->stream);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(lum.data(), d_lum, lum.size() * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
-    cudaFree(d_lum);
-    if (e != cudaSuccess) return fail(ctx, ST_ERR_CUDA, std::string("environment bake: ") + cudaGetErrorString(e));
-    std::vector<float> tex(lum.size() * 4);
-    st_env_map_tables(lum.data(), tex.data());
-    CK(cudaMalloc(&ctx->d_envmap, tex.size() * sizeof(float)), "cudaMalloc environment map");
-    CK(cudaMemcpyAsync(ctx->d_envmap, tex.data(), tex.size() * sizeof(float), cudaMemcpyHostToDevice, ctx->stream),
-       "environment map upload");
-    CK(cudaStreamSynchronize(ctx->stream), "environment map upload");
+    ctx->env_key.clear();
+    int rc = env_map_bake(ctx);
+    if (rc) return rc;
     invalidate_graph(ctx);
     return ctx->has_params ? st_invalidate(ctx) : ST_OK;
 }

@@ -114,6 +114,11 @@ struct Uni {
     // the environment image (envimage.js) and the map light sampling draws from (envmap.js); null, none
     const float4* env_img; uint32_t env_w, env_h; float env_lum, env_turn;
     const float4* env_map; float env_mshare;
+    // the presets (environment.js): the mode, the sun and sky's light above the air, its aerosol depth at 550 nm and
+    // its 16 bands (st_sky.h: per band Rayleigh depth, aerosol factor, ozone depth, then its colour); the studio's L0,
+    // its top and its colour
+    uint32_t env_mode; float sun_outside, aerosol; const float4* sky_tab;
+    float studio_l0, studio_top; f3 studio_tint;
     // the step cache (wavefront.js:67-118): the cells' distances, the grid's low corner and cell size, its cells, looks
     const float* sc; f3 sc_lo; float sc_cs; uint32_t sc_dx, sc_dy, sc_dz, sc_looks;
     // haze box (haze.js:64-80)
@@ -466,10 +471,54 @@ __device__ __forceinline__ f3 env_image(const Uni& u, f3 dir) {
     const f3 c = top * (1.f - fy) + bot * fy;
     return mk(fmaxf(c.x, 0.f), fmaxf(c.y, 0.f), fmaxf(c.z, 0.f)) * u.env_lum;
 }
+// Kasten-Young relative air mass (sdf.js:96-100 airMass): 1 / cos(zenith) near the top, finite at the horizon
+__device__ __forceinline__ float air_mass(float cz) {
+    const float c = clampf(cz, 0.f, 1.f);
+    const float zdeg = acosf(c) * (180.f / ST_PI);
+    return 1.f / (c + 0.15f * powf(fmaxf(93.885f - zdeg, 0.1f), -1.253f));
+}
+// THE SUN AND SKY, PHYSICALLY (environment.js SUNSKY_FN): per band the disc -- the sunlight the air lets through,
+// exp(-tau m_s), spread over the disc, none once the sun has set -- or the sky, that light scattered once toward the
+// eye over the air's whole depth, E0 (tau_R P_R + 0.9 tau_A P_M) / tau  m_v (exp(-tau m_s) - exp(-tau m_v)) / (m_v - m_s)
+// (tau m_v exp(-tau m_v) where the two air masses meet), fading over the sun's last 3 degrees below the horizon; the
+// ozone in the extinction, not in what scatters; added up as colour, times the light above the air
+__device__ __forceinline__ f3 sun_sky(const Uni& u, f3 d) {
+    const f3 s = u.sun_dir;
+    const float mv = air_mass(fmaxf(d.z, 0.f)), ms = air_mass(fmaxf(s.z, 0.f));
+    const bool disc = in_sun_disc(u, d) && s.z > -sqrtf(u.sun_sin2);
+    const float c = dot(d, s), g = 0.7f;
+    const float phaseR = 3.f / (16.f * ST_PI) * (1.f + c * c);
+    const float phaseM = (1.f - g * g) / (4.f * ST_PI * powf(1.f + g * g - 2.f * g * c, 1.5f));
+    const float up = clampf((s.z + 0.05f) / 0.05f, 0.f, 1.f);
+    const float dm = mv - ms;
+    f3 L = mk(0.f);
+#pragma unroll 4
+    for (int k = 0; k < 16; k++) {
+        const float4 b = __ldg(&u.sky_tab[k]);
+        const float4 rgb = __ldg(&u.sky_tab[16 + k]);
+        const float tr = b.x, ta = u.aerosol * b.y, tau = tr + ta + b.z;
+        float v;
+        if (disc) {
+            v = expf(-tau * ms) / (ST_PI * u.sun_sin2);
+        } else {
+            const float k1 = fabsf(dm) < 1e-3f ? tau * mv * expf(-tau * mv) : mv * (expf(-tau * ms) - expf(-tau * mv)) / dm;
+            v = (tr * phaseR + 0.9f * ta * phaseM) / tau * k1 * up;
+        }
+        L = L + mk(rgb.x, rgb.y, rgb.z) * v;
+    }
+    return mk(fmaxf(L.x, 0.f), fmaxf(L.y, 0.f), fmaxf(L.z, 0.f)) * fmaxf(u.sun_outside, 0.f);
+}
+// THE STUDIO (environment.js STUDIO_FN): L0 (1 + top z) in its colour, L0 such that a level surface facing up receives
+// the set illuminance whatever top is
+__device__ __forceinline__ f3 studio_light(const Uni& u, f3 d) {
+    return u.studio_tint * (u.studio_l0 * fmaxf(1.f + u.studio_top * d.z, 0.f));
+}
 __device__ __forceinline__ f3 env_base(const Uni& u, f3 dir) {
     if (u.env_img) return env_image(u, dir);
     if (u.uniform > 0.f) return mk(u.uniform);
     f3 d = normalize(dir);
+    if (u.env_mode == 1u) return sun_sky(u, d);
+    if (u.env_mode == 2u) return studio_light(u, d);
     if (in_sun_disc(u, d)) return u.disc;
     return mk(d.z > 0.f ? u.sky : u.ground);
 }
@@ -477,11 +526,11 @@ __device__ __forceinline__ f3 env_radiance(const Uni& u, f3 dir) {
     bool cone = u.sun_on && in_sun_disc(u, dir);
     return env_base(u, dir) * (cone ? u.sun_gain : u.sky_gain);
 }
-// the environment without the sun's disc (sdf.js skyRadiance): what a path the photon map owns finds there
+// the environment outside the sun's cone (sdf.js skyRadiance): what a path the photons own finds there -- nothing in
+// the cone, whose light is theirs
 __device__ __forceinline__ f3 env_sky(const Uni& u, f3 dir) {
-    bool cone = u.sun_on && in_sun_disc(u, dir);
-    f3 base = u.env_img ? env_image(u, dir) : (u.uniform > 0.f ? mk(u.uniform) : mk(normalize(dir).z > 0.f ? u.sky : u.ground));
-    return base * (cone ? u.sun_gain : u.sky_gain);
+    if (u.sun_on && in_sun_disc(u, dir)) return mk(0.f);
+    return env_base(u, dir) * u.sky_gain;
 }
 // whether the sun's photons were drawn along this line (sdf.js ltCovers): it crosses the square of half width
 // sppm_half across the sun's direction through the origin

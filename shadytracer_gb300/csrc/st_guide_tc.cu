@@ -236,7 +236,10 @@ cudaError_t launch_guide_infer(const WaveArgs& a, int sms, cudaStream_t s) {
     cudaFuncSetAttribute(k_guide_infer_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     int nb = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_guide_infer_tc, 128, smem);
-    // at most 512 / TC_COLS CTAs an SM hold tensor memory at once (an allocation beyond that would wait)
+    // at least what the registers (128 threads x 128) and the shared memory allow, 4 CTAs an SM with a small table of
+    // materials; at most 512 / TC_COLS CTAs an SM hold tensor memory at once (an allocation beyond that would wait).
+    // A CTA's rounds are its own (by blockIdx), so a CTA that has to wait for room only starts later
+    nb = std::max(nb, std::min(4, (int)((228u << 10) / (smem + 1024u))));
     nb = std::min(std::max(nb, 1), (int)(512u / TC_COLS));
     k_guide_infer_tc<<<sms * nb, 128, smem, s>>>(a);
     return cudaGetLastError();

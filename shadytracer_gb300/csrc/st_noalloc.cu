@@ -116,6 +116,8 @@ extern "C" int st_render_noalloc(int device, const st_scene_desc* desc, const st
     if (p->sppm) return refuse("the photon map (st_params.sppm) takes the context path");
     if (p->guide) return refuse("the learned proposal (st_params.guide) takes the context path");
     if (p->lt) return refuse("light tracing (st_params.lt) takes the context path");
+    if (p->env_mode != ST_ENV_ANALYTIC && p->env_uniform <= 0.f)
+        return refuse("the environment's presets (st_params.env_mode: their tables and map) take the context path");
     if (p->step_cache) return refuse("the step cache (st_params.step_cache) takes the context path");
     for (uint32_t i = 0; i < desc->n_materials && !p->emit_off; i++) {
         const float* e = desc->materials[i].emissive;

@@ -218,6 +218,49 @@ def floor_furnace(width=256, height=256, spp=16, albedo=0.8, sky=1000.0, maxboun
     return s
 
 
+def floor_sky(width=64, height=64, env_mode=1, albedo=0.8, sun_elevation=45.0, sun_outside=128000.0, turbidity=0.7,
+              studio_illuminance=10000.0, studio_top=0.5, maxbounce=4, seed=1):
+    """The floor of floor_furnace under one of the environment's presets (environment.js): env_mode 1 the sun and sky
+    physically (sunlight of `sun_outside` lux above the air, `turbidity`), 2 the studio (`studio_illuminance` lux on a
+    level surface, brighter above by `studio_top`). The floor's closed form is albedo / pi times the illuminance the
+    environment puts on it: the studio's by its construction; the sun and sky's integrated from its radiance."""
+    s = floor_furnace(width=width, height=height, albedo=albedo, maxbounce=maxbounce, seed=seed)
+    s.params.env_uniform = 0.0
+    s.params.sun_hint = 1
+    s.params.env_mode = env_mode
+    s.params.sun_elevation = sun_elevation
+    s.params.sun_azimuth = 0.0
+    s.params.sun_outside = sun_outside
+    s.params.sky_turbidity = turbidity
+    s.params.studio_illuminance = studio_illuminance
+    s.params.studio_top = studio_top
+    for i in range(3):
+        s.params.studio_color[i] = 1.0
+    s.info = {"albedo": albedo, "workload": "floor-sky"}
+    return s
+
+
+def sky_illuminance(radiance, sun_elevation, sun_azimuth=0.0, sun_diameter=0.53, nz=400, nphi=800):
+    """What an environment puts on a level surface facing up, lux: its sun's disc at normal incidence times
+    sin(elevation), plus its sky over the upper hemisphere (midpoint rule in z and azimuth), the disc left out of that.
+    `radiance(dirs)` gives rgb at n x 3 unit directions. Returns (sun at normal incidence, sun on the level, sky)."""
+    luma = np.array([0.2126, 0.7152, 0.0722])
+    e, a = math.radians(sun_elevation), math.radians(sun_azimuth)
+    sun = np.array([math.cos(e) * math.sin(a), math.cos(e) * math.cos(a), math.sin(e)])
+    half = math.radians(sun_diameter / 2)
+    omega = 2 * math.pi * (1 - math.cos(half))
+    e_sun = float(radiance(sun[None])[0] @ luma) * omega
+    z = (np.arange(nz) + 0.5) / nz
+    ph = (np.arange(nphi) + 0.5) / nphi * 2 * math.pi
+    Z, PH = np.meshgrid(z, ph, indexing="ij")
+    R = np.sqrt(1 - Z * Z)
+    d = np.stack([R * np.cos(PH), R * np.sin(PH), Z], -1).reshape(-1, 3)
+    L = radiance(d) @ luma
+    L[(d @ sun) > math.cos(half)] = 0.0
+    e_sky = float((L * d[:, 2]).sum() / nz * (2 * math.pi / nphi))
+    return e_sun, e_sun * max(math.sin(e), 0.0), e_sky
+
+
 def emitter(le, beam_deg=0.0):
     """makeEmissive (core/materials.js:263-268): emitted luminance `le` (cd/m^2, rgb), air beyond; beam_deg > 0
     limits the emission to a cone of that half angle about the surface's outward normal (a cosine light's beam,

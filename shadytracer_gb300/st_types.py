@@ -18,6 +18,7 @@ ST_ERR_STATE = -7
 ST_PRIM_PLANE, ST_PRIM_SPHERE, ST_PRIM_BOX, ST_PRIM_ROUNDBOX, ST_PRIM_TORUS, ST_PRIM_PRISM, \
     ST_PRIM_ASPHERE, ST_PRIM_CYLINDER = range(8)
 ST_OP_ITEM, ST_OP_SMOOTH, ST_OP_UNION, ST_OP_SUB = range(4)
+ST_ENV_ANALYTIC, ST_ENV_SUNSKY, ST_ENV_STUDIO = range(3)
 ST_MAX_PRIMS = 256
 ST_MAX_MATERIALS = 256
 
@@ -73,7 +74,9 @@ class StParams(C.Structure):
                 ("guide_train", C.c_uint32), ("guide_seed", C.c_uint32),
                 ("emit_share", C.c_float), ("emit_radius", C.c_float), ("emit_off", C.c_uint32),
                 ("env_map_off", C.c_uint32), ("step_cache", C.c_uint32), ("step_cache_cells", C.c_float),
-                ("lt", C.c_uint32), ("lt_photons", C.c_uint32)]
+                ("lt", C.c_uint32), ("lt_photons", C.c_uint32),
+                ("env_mode", C.c_uint32), ("sun_outside", C.c_float), ("sky_turbidity", C.c_float),
+                ("studio_illuminance", C.c_float), ("studio_top", C.c_float), ("studio_color", C.c_float * 3)]
 
 
 class StView(C.Structure):

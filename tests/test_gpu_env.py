@@ -122,3 +122,45 @@ def test_clearing_goes_back_to_the_sky():
         lit = (r.read_accum()[0] @ LUMA)
     assert dark == 0.0
     assert abs(lit[:4].mean() / 800.0 - 1) < 0.01
+
+
+# ---- the presets (core/environment.js): the physical sun and sky, the studio ----
+def render_preset(s, n):
+    from shadytracer_gb300.renderer import create_path_tracer
+    with create_path_tracer(s, device=0) as r:
+        r.step(n)
+        rgb, V, S, cnt = r.read_accum()
+        ctr = r.counters()
+    return rgb, V, S, ctr
+
+
+@pytest.mark.parametrize("elevation, turbidity", [(45.0, 0.7), (12.0, 3.0)])
+def test_sun_and_sky_floor_closed_form_and_oracle(elevation, turbidity):
+    """The floor under the physical sun and sky: albedo / pi times the sun's and the sky's illuminance on it (the
+    oracle's radiance integrated), and the oracle's picture pixel by pixel; the sky seen above the horizon is the
+    oracle's radiance there."""
+    mk = lambda w: scenes.floor_sky(width=w, height=w, env_mode=1, sun_elevation=elevation, turbidity=turbidity)
+    s = mk(64)
+    rgb, V, S, ctr = render_preset(s, 64)
+    e_sun, e_sun_level, e_sky = scenes.sky_illuminance(lambda d: oracle.env_radiance(s, d), elevation)
+    L = rgb @ LUMA
+    cf = 0.8 / math.pi * (e_sun_level + e_sky)
+    assert abs(L[:24].mean() / cf - 1) < 0.01, (L[:24].mean(), cf)
+    assert ctr["nonfinite"] == 0
+    small = mk(32)
+    g = render_preset(small, 16)
+    ref = oracle.render(mk(32), 16)
+    Lg, Lr = g[0] @ LUMA, ref.luma()
+    se = np.sqrt(se_of(g[1], g[2]) ** 2 + np.nan_to_num(ref.se()) ** 2)
+    within = np.abs(Lg - Lr) <= 4 * se + 2e-3 * np.maximum(np.abs(Lr), 1.0)
+    assert within.mean() > 0.98, (~within).sum()
+
+
+def test_studio_floor_closed_form():
+    """The studio puts exactly studio_illuminance lux on a level surface, whatever its top: the floor reads
+    albedo / pi times it."""
+    for top in (0.0, 1.0):
+        s = scenes.floor_sky(width=48, height=48, env_mode=2, studio_illuminance=10000.0, studio_top=top)
+        rgb, V, S, ctr = render_preset(s, 32)
+        L = (rgb @ LUMA)[:18]
+        assert abs(L.mean() / (0.8 / math.pi * 10000.0) - 1) < 0.01, (top, L.mean())

@@ -105,6 +105,7 @@ def refused(make, setting=None):
     (lambda: scenes.floor_furnace(width=32, height=32), "sppm", "photon map"),
     (lambda: scenes.floor_furnace(width=32, height=32), "guide", "learned proposal"),
     (lambda: scenes.floor_furnace(width=32, height=32), "lt", "light tracing"),
+    (lambda: scenes.floor_sky(width=32, height=32, env_mode=1), None, "presets"),
     (lambda: scenes.floor_furnace(width=32, height=32), "step_cache", "step cache"),
     (lambda: scenes.lamp_floor(width=32, height=32), None, "emissive"),
 ])
