@@ -104,12 +104,13 @@ def replica_value(world, paths_per_step, ms):
 def workload(small, spp=0):
     """The room as the reference renders it by default: its scene as code (the builder's generated SDF, here
     codegen.py's CUDA compiled by NVRTC for sm_103a at st_set_scene), the step cache off (the reference's developer
-    setting; the scene_forms leg measures it on)."""
+    setting; the scene_forms leg measures it on), lit by the physical sun and sky (the reference's default
+    environment, environment.js; a 100 klx sun 35 degrees up)."""
     from shadytracer_gb300 import scenes
     if small:
-        s = scenes.sdf_room(width=480, height=270, spp=spp or 4, maxbounce=8)
+        s = scenes.sdf_room(width=480, height=270, spp=spp or 4, maxbounce=8, sky="physical")
     else:
-        s = scenes.sdf_room(width=1920, height=1080, spp=spp or 64, maxbounce=8)
+        s = scenes.sdf_room(width=1920, height=1080, spp=spp or 64, maxbounce=8, sky="physical")
     s.params.step_cache = 0
     return s
 
@@ -125,6 +126,7 @@ def config_of(s):
                                                                                      s.info["spp"], p.maxbounce),
             "width": p.width, "height": p.height, "spp": s.info["spp"], "maxbounce": p.maxbounce,
             "paths_per_step": p.width * p.height * s.info["spp"], "primitives": 24,
+            "environment": s.info.get("sky", "a 100 klx sun disc and a uniform sky of 10 klx on the level"),
             "scene": "code: codegen.py's CUDA for the room, compiled by NVRTC for sm_103a at st_set_scene",
             "step_cache": ("%d look%s, %g M cells" % (1 if p.step_cache == 1 else 3, "" if p.step_cache == 1 else "s",
                                                     p.step_cache_cells or 4.0)) if p.step_cache else "off",

@@ -12,7 +12,7 @@ import math
 
 import numpy as np
 
-from .st_types import (StPrim, StMaterial, StSceneDesc, StView, StLight, default_params,
+from .st_types import (StPrim, StMaterial, StSceneDesc, StView, StLight, default_params, ST_ENV_SUNSKY,
                        ST_LIGHT_DISC, ST_LIGHT_RECTANGLE, ST_LIGHT_COSINE, ST_LIGHT_UNIFORM,
                        ST_PRIM_PLANE, ST_PRIM_SPHERE, ST_PRIM_BOX, ST_PRIM_ROUNDBOX, ST_PRIM_TORUS,
                        ST_PRIM_PRISM, ST_PRIM_ASPHERE, ST_PRIM_CYLINDER,
@@ -416,7 +416,7 @@ ROOM_WALL = 0.1
 
 
 def sdf_room(width=1920, height=1080, spp=64, maxbounce=8, seed=1, n_prims=24, prim_seed=2, finish="mixed",
-             sky_illuminance=10000.0, ground_luminance=1000.0):
+             sky_illuminance=10000.0, ground_luminance=1000.0, sky="uniform"):
     """A 6 x 4 x 3 m room (its walls a hollow box 0.1 m thick, a 2 x 1.5 m window in the +y wall) holding
     `n_prims` primitives drawn from PCG32(prim_seed): types uniform over {box, sphere, torus, rounded prism}, sizes
     0.15-0.4 m, placed uniformly in the room, randomly turned, smooth-unioned in order with radii U(0.02, 0.1) m.
@@ -425,7 +425,8 @@ def sdf_room(width=1920, height=1080, spp=64, maxbounce=8, seed=1, n_prims=24, p
     window. March tolerance 1e-4 m. finish="diffuse": every object Lambertian of its drawn albedo (the same draws, the
     same geometry), so most of the room is lit by the light the sunlit floor and walls send on -- the learned
     proposal's workload; sky_illuminance and ground_luminance near 0 leave the sun's patch on the floor the room's only
-    light after the sun itself."""
+    light after the sun itself. sky="physical": the environment's physical sun and sky preset instead (environment.js
+    SUNSKY_FN, turbidity 0.7), its light above the air set so that the sun gives 100 klx at normal incidence."""
     rng = Pcg32(prim_seed)
     mats = [air(), diffuse((0.75, 0.73, 0.70))]
     hx, hy, hz = ROOM_HALF
@@ -471,7 +472,50 @@ def sdf_room(width=1920, height=1080, spp=64, maxbounce=8, seed=1, n_prims=24, p
     target = (0.8, 0.9, 1.1)
     s.view = look_at(eye, target, 60.0, width / height)
     s.info = {"spp": spp, "workload": "room24-1080p", "paths": width * height * spp}
+    if sky == "physical":
+        s.params.env_mode = ST_ENV_SUNSKY
+        s.params.sky_turbidity = 0.7
+        s.params.sun_outside = 100000.0 / sun_sky_transmittance(35.0, 0.7)
+        s.info["sky"] = "physical sun and sky, 100 klx sun, turbidity 0.7"
     return s
+
+
+def sun_sky_transmittance(elevation, turbidity):
+    """The share of the light above the air that reaches the ground as the sun's disc in the physical sun and sky
+    (environment.js SUNSKY_FN): sum over its 16 bands of each band's luminance share times exp(-tau m), m the
+    Kasten-Young air mass at the sun's elevation, tau the band's Rayleigh, aerosol (0.05 + 0.1 turbidity at 550 nm,
+    Angstrom 1.3) and ozone (300 DU) depths -- the bands as the library builds them (csrc/st_sky.h)."""
+    sigma = (6.2648e-24, 3.1169e-23, 1.0195e-22, 2.4886e-22, 5.4883e-22, 1.1517e-21, 2.0211e-21, 3.0497e-21, 4.2480e-21,
+             4.5252e-21, 4.7153e-21, 3.4726e-21, 2.3885e-21, 1.5936e-21, 9.8370e-22, 6.3061e-22)
+
+    def lobe(l, mu, lo, hi):
+        t = (l - mu) / (lo if l < mu else hi)
+        return math.exp(-0.5 * t * t)
+    c = math.sin(math.radians(elevation))
+    m = 1.0 / (c + 0.15 * max(93.885 - (90.0 - elevation), 0.1) ** -1.253)
+    aerosol = 0.05 + 0.1 * max(turbidity, 0.0)
+    step, lum, trans = 350.0 / 16, [], []
+    for k in range(16):
+        X = Y = Z = wl = ws = 0.0
+        l = 380.0 + k * step
+        while l < 380.0 + (k + 1) * step:
+            li, mm = round(l), l * 1e-9
+            w = 1.0 / (mm ** 5 * (math.exp(1.438776877e-2 / (mm * 5778.0)) - 1.0))
+            x = 1.056 * lobe(li, 599.8, 37.9, 31.0) + 0.362 * lobe(li, 442.0, 16.0, 26.7) - 0.065 * lobe(li, 501.1, 20.4, 26.2)
+            y = 0.821 * lobe(li, 568.8, 46.9, 40.5) + 0.286 * lobe(li, 530.9, 16.3, 31.1)
+            z = 1.217 * lobe(li, 437.0, 11.8, 36.0) + 0.681 * lobe(li, 459.0, 26.0, 13.8)
+            X, Y, Z, wl, ws = X + w * x, Y + w * y, Z + w * z, wl + w * (x + y + z) * l, ws + w * (x + y + z)
+            l += 1.0
+        nm = wl / ws
+        um = nm / 1000.0
+        tau = (0.008569 * um ** -4 * (1 + 0.0113 * um ** -2 + 0.00013 * um ** -4) + aerosol * (nm / 550.0) ** -1.3 +
+               sigma[k] * 300.0 * 2.6867e16)
+        r = 3.2404542 * X - 1.5371385 * Y - 0.4985314 * Z
+        g = -0.9692660 * X + 1.8760108 * Y + 0.0415560 * Z
+        b = 0.0556434 * X - 0.2040259 * Y + 1.0572252 * Z
+        lum.append(0.2126 * r + 0.7152 * g + 0.0722 * b)
+        trans.append(math.exp(-tau * m))
+    return sum(a * t for a, t in zip(lum, trans)) / sum(lum)
 
 
 # ---------------------------------------------------------------------------------------------------------------

@@ -57,7 +57,7 @@ def test_white_floor_at_its_stated_size():
 
 @pytest.fixture(scope="module")
 def room_1080p():
-    s = scenes.sdf_room(width=1920, height=1080, spp=8)
+    s = scenes.sdf_room(width=1920, height=1080, spp=8, sky="physical")      # the bench's room
     s.params.step_cache = 1
     s.params.step_cache_cells = 16.0
     with create_path_tracer(s) as rt:
@@ -74,7 +74,7 @@ def test_room_1080p_with_the_step_cache_matches_the_oracle_on_a_band(room_1080p,
     # a jittered ray lands in its own pixel but for f32 rounding at a pixel's very edge (1/1920 is inexact)
     assert (cnt == 8).mean() > 0.998
     W, rows = 1920, 24
-    s0 = scenes.sdf_room(width=1920, height=1080, spp=8)          # the oracle marches without the cache
+    s0 = scenes.sdf_room(width=1920, height=1080, spp=8, sky="physical")   # the oracle marches without the cache
     ref = oracle.render(s0, 8, path_first=row0 * W, path_count=rows * W)
     band = slice(row0, row0 + rows)
     L = (rgb @ LUMA)[band]
