@@ -244,6 +244,13 @@ typedef struct st_params {
     float    studio_illuminance;  /* ST_ENV_STUDIO: lx on a level surface facing up                   */
     float    studio_top;          /* ST_ENV_STUDIO: 0 even, 1 none from straight below (L0 (1 + top z)) */
     float    studio_color[3];     /* ST_ENV_STUDIO: its colour (normalised to luminance 1)             */
+    /* LIGHT TRACING'S EMITTER PHOTONS (wavefront.js:552-588 probes, tracebasics.js:726-831 THE PROBE): with light
+     * tracing on in a scene with emissive materials, this share of a sample's photons (all of them with the sun off)
+     * are probes -- a listed emitter box by its probability, a random line through its bounding sphere, followed from
+     * the far end back; at the first emissive surface seen from outside a probe becomes a photon leaving along the line,
+     * its flux the emission over the probes and the line density there (Crofton) -- which then connect and are stored
+     * as the sun's are; the camera's paths leave the emitters' light in light tracing's class to them */
+    float    lt_emit_share;       /* 0: 0.5; clamped to [0.05, 0.95] while the sun shines (the reference's ltEmitShare) */
 } st_params;
 
 #define ST_ENV_ANALYTIC 0u

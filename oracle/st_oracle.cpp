@@ -93,6 +93,7 @@ template <class T> struct Ctx {
     // light tracing to the camera (materials_pbr.js ltConnect): on, the camera, the sample's splat buffer (rgb a
     // pixel, added to the pixel as it is) and the connections that reached each pixel
     bool lt = false;
+    uint32_t lt_emit_n = 0;                 // of a sample's photons, the first this many are emitter probes
     const st_view* view = nullptr;
     std::vector<double>* splat = nullptr;
     std::vector<uint32_t>* ltcount = nullptr;
@@ -263,6 +264,14 @@ inline uint32_t emit_pick(const EmitList& L, float u) {
 template <class T> inline T cone_omc(T r, T d2) {
     const T s2 = r * r / d2;
     return s2 / (T(1) + std::sqrt(std::max(T(0), T(1) - s2)));
+}
+// tracebasics.js:1187-1195 emitCovers: inside a listed sphere
+template <class T> inline bool emit_covers(const EmitList& L, const V3<T>& y) {
+    for (uint32_t b = 0; b < L.count; b++) {
+        const V3<T> d(y.x - T(L.box[b][0]), y.y - T(L.box[b][1]), y.z - T(L.box[b][2]));
+        if (dot(d, d) < T(L.box[b][3]) * T(L.box[b][3])) return true;
+    }
+    return false;
 }
 template <class T> inline T emit_cone_pdf(const EmitList& L, const V3<T>& x, const V3<T>& w) {
     T p = 0;
@@ -514,7 +523,11 @@ inline void shade_hit(const Ctx<T>& C, Ray<T>& r, T dhit, Rng& rng, Rng& grng, b
     }
     if (max3(emis) > T(0)) {                                                       // materials_pbr.js:1014-1075 emitterHit
         const T beam = m.beam_cos > 0.f ? (-dot(r.dir, n) >= T(m.beam_cos) ? T(1) : T(0)) : T(1);   // lights.js beamShape
-        r.rad += r.beta * emis * (r.emw * beam);   // weighed against the last vertex's emitter light sample
+        // weighed against the last vertex's emitter light sample; left to the emitter photons by a path in light
+        // tracing's class (or the map's) where a probe could have started one (materials_pbr.js:1044-1047)
+        T w = r.emw;
+        if (C.lt_emit_n && (r.cls == 3u || (C.sppm && r.lens == 3)) && emit_covers(*C.em, r.pos)) w = T(0);
+        r.rad += r.beta * emis * (w * beam);
         if (C.em_on) emit_deposit(C, r.pos, emis);  // and discovered
         r.state = RAY_SOURCE;
         move_by(r, r.dir * (otol * T(2)));
@@ -1227,8 +1240,79 @@ void lt_connect_medium(const Ctx<T>& C, const V3<T>& P, const V3<T>& din, const 
     if (!(len > T(0))) return;
     lt_splat(C, P, P, v, len, h, c, pix, cell, st);
 }
+// AN EMITTER PROBE (wavefront.js:552-588; tracebasics.js:782-831 THE PROBE): a listed box by its probability, a line
+// uniformly random through its bounding sphere followed back from the far end, through everything but an emissive
+// surface seen from outside, where it becomes a photon leaving along the line, its flux the emission over the probes
+// and the line density there; false if it finds none (past its chord, out of the scene, out of steps or iterations)
+template <class T>
+bool probe_photon(const Ctx<T>& C, U4 ps, uint32_t id, Ray<T>& r, uint32_t& it, Stats& st) {
+    const EmitList& L = *C.em;
+    if (L.count == 0) return false;
+    Rng r0 = path_rng(ps, id, PHOTON_GEN_SALT);
+    T u[4], u2[4];
+    r0.next4(u); r0.next4(u2);
+    const uint32_t b = emit_pick(L, (float)u[0]);
+    const V3<T> c(T(L.box[b][0]), T(L.box[b][1]), T(L.box[b][2]));
+    const T rb = T(L.box[b][3]);
+    const T z = T(1) - T(2) * u[1], rz = std::sqrt(std::max(T(0), T(1) - z * z)), ph = T(2) * T(PI_D) * u[2];
+    const V3<T> w(rz * std::cos(ph), rz * std::sin(ph), z);
+    const V3<T> ta = std::fabs(w.x) > T(0.9) ? V3<T>(0, 1, 0) : V3<T>(1, 0, 0);
+    const V3<T> e1 = normalize(cross(ta, w)), e2 = cross(w, e1);
+    const T rho = rb * std::sqrt(u[3]), pd = T(2) * T(PI_D) * u2[0];
+    const V3<T> q = c + e1 * (rho * std::cos(pd)) + e2 * (rho * std::sin(pd));
+    const T hl = std::sqrt(std::max(rb * rb - rho * rho, T(0)));
+    r.pos = q + w * hl; r.dir = -w; r.beta = V3<T>(1); r.rad = V3<T>(0);
+    r.ltot = 0; r.n = 1; r.sunmis = 1; r.tmax = 0; r.absLtot = 0;
+    r.bounces = 0; r.steps = 0; r.state = RAY_ACTIVE; r.pix = id;
+    const T len = T(2) * hl;
+    while (it < C.budget) {
+        uint32_t evals = 0;
+        T dh = march(C, r, st, false, evals);
+        uint32_t chunks = std::max(1u, (evals + MARCH_CHUNK - 1) / MARCH_CHUNK);
+        it = std::min(it + chunks - 1, C.budget - 1);
+        const bool last = it + 1 == C.budget;
+        if (r.state != RAY_ACTIVE || r.ltot > len) return false;
+        const V3<T> nn = hit_normal(C, r.pos, dh);
+        const T otol = T(10) * march_tol(r.pos, C.tol);
+        const bool outside = dh >= T(0) && dot(nn, -r.dir) > T(0);
+        SceneHit<T> h = scene_eval(*C.s, r.pos);
+        const st_material& m = C.s->materials[std::min(h.m, C.s->n_materials - 1)];
+        const V3<T> le(T(m.emissive[0]), T(m.emissive[1]), T(m.emissive[2]));
+        if (outside && max3(le) > T(0)) {
+            T dens = 0;
+            for (uint32_t k = 0; k < L.count; k++) {
+                const V3<T> d = r.pos - V3<T>(T(L.box[k][0]), T(L.box[k][1]), T(L.box[k][2]));
+                const T rk = T(L.box[k][3]);
+                if (dot(d, d) < rk * rk) dens += T(L.pc[k][0]) / (T(4) * T(PI_D) * T(PI_D) * rk * rk);
+            }
+            if (!(dens > T(0))) return false;
+            r.pos = r.pos + nn * (T(2) * otol);
+            r.dir = -r.dir;
+            const T beam = m.beam_cos > 0.f ? (dot(r.dir, nn) >= T(m.beam_cos) ? T(1) : T(0)) : T(1);
+            r.rad = le * (beam / (T(C.lt_emit_n) * dens));
+            r.ltot = 0; r.n = 1; r.absLtot = 0; r.tmax = 0; r.bounces = 0;
+            if (last || !(luma(r.rad) > T(0))) return false;
+            it++;
+            return true;
+        }
+        move_by(r, r.dir * (T(2) * otol));                                        // through it, looking on
+        if (last) return false;
+        it++;
+    }
+    return false;
+}
+
+template <class T>
+void photon_walk(const Ctx<T>& C, U4 ps, uint32_t id, Ray<T>& r, uint32_t it, uint32_t cell, std::vector<PhotonRec>& out,
+                 Stats& st);
 template <class T>
 void trace_photon(const Ctx<T>& C, U4 ps, uint32_t id, uint32_t N, std::vector<PhotonRec>& out, Stats& st) {
+    if (id < C.lt_emit_n) {
+        Ray<T> r;
+        uint32_t it = 0;
+        if (probe_photon(C, ps, id, r, it, st)) photon_walk(C, ps, id, r, it, 0xffffffffu, out, st);
+        return;
+    }
     Rng r0 = path_rng(ps, id, PHOTON_GEN_SALT);
     T u[4]; r0.next4(u);
     V3<T> w = C.env.sample_sun_cone(u[0], u[1]);
@@ -1263,10 +1347,17 @@ void trace_photon(const Ctx<T>& C, U4 ps, uint32_t id, uint32_t N, std::vector<P
     r.dir = -w;
     r.beta = V3<T>(1);
     V3<T> disc = C.env.sun_on ? C.env.radiance(w) : V3<T>(0);
-    r.rad = disc * (cosW * C.env.sun_omega * area / T(N));
+    r.rad = disc * (cosW * C.env.sun_omega * area / T(std::max(N - C.lt_emit_n, 1u)));
     r.ltot = 0; r.n = 1; r.sunmis = 1; r.tmax = 0; r.absLtot = 0;
     r.bounces = 0; r.steps = 0; r.state = RAY_ACTIVE; r.pix = id;
-    uint32_t it = 0, seg = 0;
+    photon_walk(C, ps, id, r, 0u, cell, out, st);
+}
+
+// a photon's walk from where it leaves its source: connected and stored past delta events, bounced through them
+template <class T>
+void photon_walk(const Ctx<T>& C, U4 ps, uint32_t id, Ray<T>& r, uint32_t it, uint32_t cell, std::vector<PhotonRec>& out,
+                 Stats& st) {
+    uint32_t seg = 0;
     while (it < C.budget) {
         // the haze: the leg's collision drawn as it starts, from the photon's own stream (haze.js:255-273 hazeDraw)
         const bool use_haze = C.haze.on;
@@ -1432,8 +1523,14 @@ static int render_impl(const st_scene_desc* s, const st_params* p, const st_view
     fr.cnt.assign(P, 0);
     // the photon map runs while it is set and the sun shines (its photons are the sun's)
     const bool sppm_on = p->sppm != 0 && C.env.sun_on && p->env_uniform <= 0.f;
-    // light tracing runs while it is set and the sun shines, with the same photons as the map's while it runs
-    const bool lt_on = p->lt != 0 && C.env.sun_on && p->env_uniform <= 0.f;
+    // light tracing runs while it is set and there are photons (the sun's while it shines, the emitters' in a scene
+    // with emissive materials), the same photons as the map's while it runs
+    bool any_emit = false;
+    for (uint32_t i = 0; i < s->n_materials; i++)
+        if (std::max(s->materials[i].emissive[0], std::max(s->materials[i].emissive[1], s->materials[i].emissive[2])) > 0.f)
+            any_emit = true;
+    const bool sun_photons = C.env.sun_on && p->env_uniform <= 0.f;
+    const bool lt_on = p->lt != 0 && (sun_photons || any_emit);
     const uint32_t NPH = sppm_on ? (p->sppm_photons ? p->sppm_photons : P) : (p->lt_photons ? p->lt_photons : P);
     SppmGrid grid;
     if (sppm_on) {
@@ -1476,6 +1573,12 @@ static int render_impl(const st_scene_desc* s, const st_params* p, const st_view
         for (auto& g : egrids) { g.resize(EMIT_CELLS * 8); emit_grid_init(g.data()); }
         C.em = &elist;
         C.em_grids = &egrids;
+    }
+    // light tracing's emitter probes (raytrace_main.js:1634-1635): their share of the photons, all of them with no sun
+    if (lt_on && C.em_on) {
+        const float set = p->lt_emit_share > 0.f ? p->lt_emit_share : 0.5f;
+        const double share = sun_photons ? std::min(0.95, std::max(0.05, (double)set)) : 1.0;
+        C.lt_emit_n = (uint32_t)std::llround(share * (double)NPH);
     }
     for (uint32_t si = 0; si < nsamples; si++) {
         U4 sseed = sample_seed(p->seed, sample0 + si);

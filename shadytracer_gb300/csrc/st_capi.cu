@@ -479,11 +479,13 @@ static bool sppm_runs(const st_ctx* ctx) {
     const Uni u = make_uni(ctx);
     return u.sun_on != 0 && ctx->params.env_uniform <= 0.f;
 }
-// light tracing runs while it is set and the sun shines (its photons are the sun's)
+static bool has_emitters(const st_ctx* ctx);
+// light tracing runs while it is set and there are photons: the sun's while it shines, the emitters' in a scene with
+// emissive materials
 static bool lt_runs(const st_ctx* ctx) {
     if (!ctx->has_params || !ctx->params.lt) return false;
     const Uni u = make_uni(ctx);
-    return u.sun_on != 0 && ctx->params.env_uniform <= 0.f;
+    return (u.sun_on != 0 && ctx->params.env_uniform <= 0.f) || has_emitters(ctx);
 }
 static bool photons_run(const st_ctx* ctx) { return sppm_runs(ctx) || lt_runs(ctx); }
 // the sun's photons a sample: the map's count while it runs (they serve both), else light tracing's
@@ -532,6 +534,13 @@ static WaveArgs wave_args(st_ctx* ctx, uint32_t w) {
         a.em = emit_bufs(ctx, (!ctx->params.emit_off && a.u.nee) ? 1u : 0u,
                          ctx->params.emit_share > 0.f ? ctx->params.emit_share : 0.5f, half);
     }
+    // light tracing's emitter probes (raytrace_main.js:1634-1635): their share of the photons, all of them with no sun
+    if (a.u.lt_on && a.em.dev) {
+        const bool sun = a.u.sun_on != 0 && ctx->params.env_uniform <= 0.f;
+        const float set = ctx->params.lt_emit_share > 0.f ? ctx->params.lt_emit_share : 0.5f;
+        const double share = sun ? std::min(0.95, std::max(0.05, (double)set)) : 1.0;
+        a.u.lt_emit_n = (uint32_t)std::llround(share * (double)a.u.sppm_n);
+    }
     if (ctx->n_faces) {
         a.lf.face = ctx->d_faces;
         a.lf.of = reinterpret_cast<const uint8_t*>(ctx->d_faces + ST_MAX_LIGHTS * FACE_F4);
@@ -556,6 +565,9 @@ static cudaError_t record_wave(st_ctx* ctx, const WaveArgs& a) {
         return e;
     };
     cudaError_t e;
+    // the emitter list, from what the camera paths discovered: rebuilt between samples, every EMIT_EPOCH -- before the
+    // sample's photons, whose probes draw from the list the camera's paths then weigh against
+    if (a.em.on && (e = timed("emit_build", [&] { return launch_emit_build(a, 0.f, s); }))) return e;
     if (a.u.sppm_on || a.u.lt_on) {
         // THE SAMPLE'S PHOTONS FIRST (photons.js planBatches's `first`): in chunks of the wave's slots, each through
         // the march, the surface kernel and the photon's shade (and, with light tracing, the occlusion pass of the
@@ -598,8 +610,6 @@ static cudaError_t record_wave(st_ctx* ctx, const WaveArgs& a) {
     }
     ctx->rec_launches++;
     if (a.gd.train && (e = guide_wave_begin(ctx, a.slots, s))) return e;
-    // the emitter list, from what the camera paths discovered: rebuilt between samples, every EMIT_EPOCH
-    if (a.em.on && (e = timed("emit_build", [&] { return launch_emit_build(a, 0.f, s); }))) return e;
     if ((e = launch_iter_begin(a, 0, 1, 1, s))) return e;
     if ((e = timed("genrays", [&] { return launch_genrays(a, ctx->sms, s); }))) return e;
     int cur = 0;

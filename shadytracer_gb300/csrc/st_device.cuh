@@ -136,6 +136,7 @@ struct Uni {
     // light tracing to the camera (st_photons.cu lt_connect): the photons above connect where they land
     uint32_t lt_on;
     uint32_t photon_pass;        // the wave's photon pass: its rays are photons, seeded by the photon's own stream
+    uint32_t lt_emit_n;          // of the sample's sppm_n photons, the first this many are emitter probes (0: none)
 };
 
 // ------------------------------------------------------------------------------------------------------------

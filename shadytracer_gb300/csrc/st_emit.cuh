@@ -47,6 +47,16 @@ __device__ __forceinline__ float cone_omc(float r, float d2) {
 __device__ __forceinline__ float emit_share(const EmitBufs& em) {
     return (em.nee && em.dev->count > 0u) ? fminf(fmaxf(em.share, 0.05f), 0.95f) : 0.f;
 }
+// whether a probe could have started a photon at y (tracebasics.js:1187-1195 emitCovers): inside a listed sphere
+__device__ __forceinline__ bool emit_covers(const EmitDev* d, f3 y) {
+    const uint32_t K = min(d->count, EMIT_MAX);
+    for (uint32_t b = 0; b < K; b++) {
+        const float4 bx = d->box[b];
+        const f3 dc = mk(y.x - bx.x, y.y - bx.y, y.z - bx.z);
+        if (dot(dc, dc) < bx.w * bx.w) return true;
+    }
+    return false;
+}
 // a box by its cumulative probability (linear: at most EMIT_MAX)
 __device__ __forceinline__ uint32_t emit_pick(const EmitDev* d, float u) {
     const uint32_t K = min(d->count, EMIT_MAX);

@@ -28,6 +28,7 @@ namespace st {
 #define META_TRAIN (1u << 27)             // a camera path that holds a training record for the learned proposal
 #define META_CAND (1u << 28)              // light tracing's class (tracebasics.js:195-196 CLS_CAND, CLS_SPEC): a camera
 #define META_SPEC (1u << 29)              // path whose first vertex drew an evaluable lobe; ...and delta events since
+#define META_PROBE (1u << 30)             // an emitter photon's probe (TAG_PROBE): looking for where its photon starts
 #define META_LOW 0x00ffffffu
 #define SURF_NONE 0xffffu                 // hsurf: no medium asked (n1 is the material's own index of refraction)
 #define SURF_LEAVING 0xffffffffu          // hsurf: the surface seen from behind, the ray moved on

@@ -17,6 +17,7 @@
 #include <algorithm>
 #include <cmath>
 
+#include "st_emit.cuh"
 #include "st_internal.h"
 #include "st_kernels.cuh"
 #include "st_sppm_dev.cuh"
@@ -131,10 +132,50 @@ __global__ void __launch_bounds__(256) k_genphotons(WaveArgs a, uint32_t first, 
     const f3 b1 = normalize(cross(t, s));
     const f3 b2 = cross(s, b1);
     const float R = u.sppm_half;
+    const float n_sun = (float)max(u.sppm_n - u.lt_emit_n, 1u);
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const uint32_t id = first + i;
         Rng rng = path_rng(ps, id, PHOTON_GEN_SALT);
         const float4 r0 = rng.next();
+        if (id < u.lt_emit_n) {
+            // AN EMITTER PROBE (wavefront.js:552-588): a listed box by its probability, a direction w uniform on the
+            // sphere, a point uniform on the disc across the box's bounding sphere perpendicular to w -- a uniformly
+            // random line through the sphere -- started at the line's far end, heading back (-w), its chord its length;
+            // nothing listed yet: a probe that finds nothing
+            const EmitDev* ed = a.em.dev;
+            const uint32_t K = ed ? min(ed->count, EMIT_MAX) : 0u;
+            f3 org = mk(0.f), dir = mk(0.f, 0.f, 1.f);
+            float len = -1.f;
+            if (K > 0u) {
+                const float4 r1 = rng.next();
+                const uint32_t b = emit_pick(ed, r0.x);
+                const float4 bx = ed->box[b];
+                const float z = 1.f - 2.f * r0.y, rz = sqrtf(fmaxf(0.f, 1.f - z * z));
+                float sw, cw;
+                sincosf(2.f * ST_PI * r0.z, &sw, &cw);
+                const f3 w = mk(rz * cw, rz * sw, z);
+                const f3 ta = fabsf(w.x) > 0.9f ? mk(0.f, 1.f, 0.f) : mk(1.f, 0.f, 0.f);
+                const f3 e1 = normalize(cross(ta, w));
+                const f3 e2 = cross(w, e1);
+                const float rho = bx.w * sqrtf(r0.w);
+                float sd, cd;
+                sincosf(2.f * ST_PI * r1.x, &sd, &cd);
+                const f3 q = mk(bx.x, bx.y, bx.z) + e1 * (rho * cd) + e2 * (rho * sd);
+                const float hl = sqrtf(fmaxf(bx.w * bx.w - rho * rho, 0.f));
+                org = q + w * hl;
+                dir = -w;
+                len = 2.f * hl;
+            }
+            a.pb.pos[i] = make_float4(org.x, org.y, org.z, 0.f);
+            a.pb.dir[i] = make_float4(dir.x, dir.y, dir.z, 1.f);
+            a.pb.beta[i] = make_float4(1.f, 1.f, 1.f, 1.f);
+            a.pb.rad[i] = make_float4(0.f, 0.f, 0.f, len);                 // w: its length along the line
+            a.pb.meta[i] = make_uint4(id, meta_y(0, 0, RAY_ACTIVE) | META_PROBE, 0u, __float_as_uint(0.f));
+            a.pb.lam[i] = 0.f;
+            a.pb.lprev[i] = make_float2(__uint_as_float(0xffffffffu), 0.f);
+            a.q.ray[0][i] = i;
+            continue;
+        }
         const f3 w = sample_sun_cone(u, r0.x, r0.y);
         float x, y, area;                                                // the point, and 1 / its density
         uint32_t cell = 0xffffffffu;
@@ -158,7 +199,7 @@ __global__ void __launch_bounds__(256) k_genphotons(WaveArgs a, uint32_t first, 
         const f3 q = b1 * x + b2 * y;
         const f3 org = q + w * ((u.envR - dot(q, s)) / cosW);
         const f3 disc = u.sun_on ? env_radiance(u, w) : mk(0.f);
-        const f3 flux = disc * (cosW * u.sun_omega * area / (float)u.sppm_n);
+        const f3 flux = disc * (cosW * u.sun_omega * area / n_sun);
         a.pb.pos[i] = make_float4(org.x, org.y, org.z, 0.f);
         a.pb.dir[i] = make_float4(-w.x, -w.y, -w.z, 1.f);
         a.pb.beta[i] = make_float4(1.f, 1.f, 1.f, 1.f);
@@ -317,7 +358,49 @@ __global__ void __launch_bounds__(256) k_photon_shade(WaveArgs a, int nxt, int l
             bounces = m4.y & 0xffu;
             const uint32_t state = (m4.y >> 16) & 0xffu;
             const uint32_t cell = __float_as_uint(a.pb.lprev[slot].x);    // its emission cell
-            if (state == RAY_SCATTER) {
+            if (m4.y & META_PROBE) {
+                // THE PROBE (tracebasics.js:782-831): past its chord, out of the scene or out of steps it found
+                // nothing; an emissive surface seen from outside starts its photon, leaving along the line with the
+                // emission over the probes and the line density there (Crofton: |n.w| dA dw / (4 pi^2 r^2) a box, the
+                // Lambertian emission's own measure); anything else it passes through
+                const float4 r4 = a.pb.rad[slot];
+                if (state == RAY_ACTIVE && ltot <= r4.w) {
+                    const float4 sf = a.q.hsurf[q];
+                    const uint32_t ids = __float_as_uint(sf.w);
+                    const float otol = 10.f * march_tol(pos, u.tol);
+                    const st_material* m = ids != SURF_LEAVING ? &sm[ids & 0xffffu] : nullptr;
+                    const f3 nn = xyz(sf);
+                    const bool outside = m && dh >= 0.f && dot(nn, -dir) > 0.f;
+                    const f3 le = m ? mk(m->emissive[0], m->emissive[1], m->emissive[2]) : mk(0.f);
+                    if (outside && max3(le) > 0.f) {
+                        const EmitDev* ed = a.em.dev;
+                        const uint32_t K = min(ed->count, EMIT_MAX);
+                        float dens = 0.f;
+                        for (uint32_t b = 0; b < K; b++) {
+                            const float4 bx = ed->box[b];
+                            const f3 d = pos - mk(bx.x, bx.y, bx.z);
+                            if (dot(d, d) < bx.w * bx.w) dens += ed->pc[b].x / (4.f * ST_PI * ST_PI * bx.w * bx.w);
+                        }
+                        if (dens > 0.f) {
+                            pos = pos + nn * (2.f * otol);
+                            dir = -dir;
+                            rad = le * (emit_beam(m->beam_cos, dot(dir, nn)) / ((float)u.lt_emit_n * dens));
+                            beta = mk(1.f);
+                            ltot = 0.f;
+                            n = 1.f;
+                            bounces = 0;
+                            m4.y = meta_y(0, 0, RAY_ACTIVE);              // a photon now, its own flags clear
+                            m4.w = __float_as_uint(0.f);
+                            a.pb.rad[slot] = make_float4(rad.x, rad.y, rad.z, 0.f);
+                            cont = !last && luma(rad) > 0.f;
+                        }
+                    } else {
+                        const f3 off = dir * (2.f * otol);
+                        pos = pos + off; ltot += length(off);
+                        cont = !last;
+                    }
+                }
+            } else if (state == RAY_SCATTER) {
                 // A COLLISION IN THE AIR (haze.js:491-545 mediumVertex, a photon's): the albedo on its weight; once it
                 // has passed a delta event, its connection through the phase function (ltConnectMedium); then its end
                 bounces += 1;
@@ -449,7 +532,8 @@ __global__ void __launch_bounds__(256) k_photon_shade(WaveArgs a, int nxt, int l
             a.pb.pos[slot] = f4(pos, ltot);
             a.pb.dir[slot] = f4(dir, n);
             a.pb.beta[slot] = make_float4(beta.x, beta.y, beta.z, 1.f);
-            if (u.haze_on) a.pb.rad[slot].w = 0.f;                     // a new leg: its collision drawn afresh
+            // a new leg: its collision drawn afresh (a probe's is its chord, kept)
+            if (u.haze_on && !(m4.y & META_PROBE)) a.pb.rad[slot].w = 0.f;
             a.pb.meta[slot] = m4;
             if (lam != 0.f) a.pb.lam[slot] = lam;
             outq[rq] = slot;

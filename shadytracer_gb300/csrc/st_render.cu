@@ -297,8 +297,13 @@ __device__ __forceinline__ void shade_surface(const WaveArgs& a, const st_materi
     f3 emis = mk(m.emissive[0], m.emissive[1], m.emissive[2]);
     if (max3(emis) > 0.f) {                                           // emitterHit (materials_pbr.js:1014-1075)
         // weighed against the light sample the last vertex could have drawn this direction with (emw, set there),
-        // and discovered: its place and brightness into the emitter grid
-        rad = rad + beta * emis * (emw * emit_beam(m.beam_cos, -dot(dir, nn)));
+        // and discovered: its place and brightness into the emitter grid. A path in light tracing's class (or the
+        // map's) leaves it to the emitter photons where a probe could have started one (materials_pbr.js:1044-1047)
+        float w = emw;
+        if (u.lt_emit_n && ((my & (META_CAND | META_SPEC)) == (META_CAND | META_SPEC) || (u.sppm_on && lens == 3u)) &&
+            emit_covers(a.em.dev, pos))
+            w = 0.f;
+        rad = rad + beta * emis * (w * emit_beam(m.beam_cos, -dot(dir, nn)));
         if (a.em.on) emit_deposit(a.em, pos, emis);
         state = RAY_SOURCE;
         f3 off = dir * (otol * 2.f);

@@ -658,6 +658,46 @@ def lt_pane(width=64, height=48, photons=400_000, sun_elevation=60.0, ior=1.5, s
     return s
 
 
+def lt_lamp(width=64, height=48, photons=400_000, le=20000.0, radius=0.1, lamp_height=1.2, pane_z=0.8, ior=1.5,
+            albedo=0.7, seed=1):
+    """Light tracing's emitter photons: a glowing sphere (`radius`, luminance `le`) above a clear pane (3 x 3 m, 2 mm
+    thick, `pane_z` up) over a floor (albedo) in the dark, the floor seen from the side from under the pane. The
+    floor under the pane is lit only through the glass: the lamp's light sampling is blocked by it, and a camera path
+    that meets the lamp through it is in light tracing's class -- the emitter photons' (the probes' from the third
+    sample on, once the lamp is listed). A sphere of uniform luminance lights a point wholly below it as a point of
+    intensity pi a^2 Le at its centre, and a thin slab turns no ray, so within a depth cap of 3 (the faces, the floor)
+        L = albedo Le a^2 h / D^3 (1 - F)^2,  F at the line's angle to the pane."""
+    mats = [air(), glass((1.0, 1.0, 1.0), ior=ior), diffuse((albedo, albedo, albedo)), emitter((le, le, le))]
+    prims = [prim(ST_PRIM_PLANE, material=2),
+             prim(ST_PRIM_BOX, pos=(0.0, 0.0, pane_z), params=(1.5, 1.5, 0.001), material=1),
+             prim(ST_PRIM_SPHERE, pos=(0.0, 0.0, lamp_height), params=(radius,), material=3)]
+    s = Scene(prims, mats, env_radius=20.0, name="lt-lamp")
+    s.params = default_params(width=width, height=height, maxbounce=3, seed=seed, sun_hint=0, sun_illuminance=0.0,
+                              sky_luminance=0.0, ground_luminance=0.0, lt=1, lt_photons=photons, eps=1e-4)
+    s.view = look_at((-1.4, -0.2, 0.6), (0.2, 0.1, 0.0), 50.0, width / height)
+    s.info = {"ior": ior, "albedo": albedo, "le": le, "radius": radius, "lamp_height": lamp_height}
+    return s
+
+
+def lt_lamp_closed_form(scene, fresnel):
+    """lt_lamp's floor, per pixel (its centre's ray; 0 where it misses the floor under the pane, 1 m in)."""
+    v, p, i = scene.view, scene.params, scene.info
+    W, H = p.width, p.height
+    xx, yy = np.meshgrid((np.arange(W) + 0.5) / W * 2 - 1, (np.arange(H) + 0.5) / H * 2 - 1)
+    right, up, fwd = (np.array([getattr(v, k)[j] for j in range(3)]) for k in ("right", "up", "fwd"))
+    cam = np.array([v.cam_pos[j] for j in range(3)])
+    d = right * (xx[..., None] * v.fx) + up * (yy[..., None] * v.fy) - fwd
+    t = np.where(d[..., 2] < 0, -cam[2] / np.minimum(d[..., 2], -1e-12), np.inf)
+    x = cam + d * np.where(np.isfinite(t), t, 0.0)[..., None]
+    lamp = np.array([0.0, 0.0, i["lamp_height"]])
+    D = np.linalg.norm(lamp - x, axis=-1)
+    cos = i["lamp_height"] / D
+    F = np.vectorize(lambda c: fresnel(c, 1.0 / i["ior"]))(cos)
+    L = i["albedo"] * i["le"] * i["radius"] ** 2 * i["lamp_height"] / D ** 3 * (1 - F) ** 2
+    under = np.isfinite(t) & (np.abs(x[..., 0]) < 1.0) & (np.abs(x[..., 1]) < 1.0)
+    return np.where(under, L, 0.0)
+
+
 def lt_pane_closed_form(scene, fresnel):
     """The floor's radiance in lt_pane, rho / pi E_sun sin(elevation) (1 - F)^2; `fresnel(cos_i, eta)` the
     caller's dielectric Fresnel reflectance."""

@@ -76,7 +76,8 @@ class StParams(C.Structure):
                 ("env_map_off", C.c_uint32), ("step_cache", C.c_uint32), ("step_cache_cells", C.c_float),
                 ("lt", C.c_uint32), ("lt_photons", C.c_uint32),
                 ("env_mode", C.c_uint32), ("sun_outside", C.c_float), ("sky_turbidity", C.c_float),
-                ("studio_illuminance", C.c_float), ("studio_top", C.c_float), ("studio_color", C.c_float * 3)]
+                ("studio_illuminance", C.c_float), ("studio_top", C.c_float), ("studio_color", C.c_float * 3),
+                ("lt_emit_share", C.c_float)]
 
 
 class StView(C.Structure):

@@ -140,6 +140,30 @@ def test_haze_closed_form_and_the_oracle():
     assert abs(counts.sum() / ref_counts.sum() - 1) < 0.005, (counts.sum(), ref_counts.sum())
 
 
+def test_emitter_photons_closed_form_and_the_oracle():
+    """A lamp's light on a floor through a pane, the emitter photons' (the probes', from the third sample on, once the
+    lamp is listed; the first two samples taken out): albedo Le a^2 h / D^3 (1 - F)^2 over the floor, and the oracle's
+    picture pixel by pixel with its connections counted alike."""
+    s = scenes.lt_lamp(width=64, height=48, photons=1_000_000)
+    cf = scenes.lt_lamp_closed_form(s, oracle.fresnel_dielectric)
+    m = cf > 0.5 * np.median(cf[cf > 0])
+    with create_path_tracer(s, device=0) as rt:
+        rt.step(2)
+        L2 = rt.read_accum()[0] @ LUMA
+        rt.step(126)
+        L = rt.read_accum()[0] @ LUMA
+        c = rt.counters()
+    X = (128 * L - 2 * L2) / 126
+    assert m.sum() > 500 and c["nonfinite"] == 0
+    assert abs(X[m].mean() / cf[m].mean() - 1) < 0.025, X[m].mean() / cf[m].mean()
+    small = scenes.lt_lamp(width=48, height=36, photons=200_000)
+    gpu, counts, _ = render(small, 16)
+    ref = oracle.render(scenes.lt_lamp(width=48, height=36, photons=200_000), 16)
+    within_error_bars(gpu, ref, frac=0.97)
+    ref_counts = oracle.last_lt_counts(48, 36)
+    assert abs(counts.sum() / ref_counts.sum() - 1) < 0.01, (counts.sum(), ref_counts.sum())
+
+
 def test_invalidate_clears_the_connections():
     s = scenes.lt_pane(width=32, height=24, photons=100_000)
     with create_path_tracer(s, device=0) as rt:

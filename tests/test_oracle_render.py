@@ -99,6 +99,23 @@ def test_light_tracing_pane_closed_form():
     assert b.luma()[m].mean() < 0.05 * cf
 
 
+def test_light_tracing_emitter_photons_closed_form():
+    """The oracle's emitter photons (wavefront.js:552-588 probes; THE PROBE: a random line through a listed box's
+    sphere followed back to the first emissive surface seen from outside, the photon's flux the emission over the
+    probes and the line density there) connected to the camera: a lamp's light on a floor through a pane, which the
+    camera's paths leave to them once the lamp is listed (from the third sample on: the first two are taken out)."""
+    s = scenes.lt_lamp(width=48, height=36, photons=100_000)
+    cf = scenes.lt_lamp_closed_form(s, oracle.fresnel_dielectric)
+    m = cf > 0.5 * np.median(cf[cf > 0])
+    L2 = oracle.render(s, 2).luma()
+    L = oracle.render(s, 128).luma()
+    X = (128 * L - 2 * L2) / 126
+    assert m.sum() > 300
+    # (the camera's paths keep the lamp's points no listed sphere covers: their rare hits converge slowly)
+    assert abs(X[m].mean() / cf[m].mean() - 1) < 0.025, X[m].mean() / cf[m].mean()
+    assert oracle.last_lt_counts(48, 36)[m].min() > 0
+
+
 def inner_pixels(hit):
     inner = hit.copy()
     for dy in (-1, 0, 1):
