@@ -73,7 +73,7 @@ def parse():
     ap.add_argument("--no-sc", action="store_true", help="skip the step cache's leg")
     ap.add_argument("--tune", default="", help="CLAIM,CHUNK: set by hand, no autotuner (profiling runs)")
     ap.add_argument("--leg", default="all", choices=["all", "sppm", "rmse", "caustic_rmse", "optics", "mlp", "emit",
-                                                     "haze", "env", "sc"],
+                                                     "haze", "env", "sc", "views"],
                     help="run one leg alone and print its JSON (profiling runs of the photon map or the optics bench)")
     return ap.parse_args()
 
@@ -633,6 +633,51 @@ def sc_leg(args, dev):
     return out
 
 
+def views_leg(args, dev):
+    """Many views in one wavefront (st_set_views): four cameras of the headline room at 960 x 540, 16 samples each,
+    rendered together in the same waves, against the four rendered one after another -- paths a second (CUDA events
+    around the renders after a warm-up), the pictures the same."""
+    import torch
+    from shadytracer_gb300 import scenes
+    from shadytracer_gb300.renderer import create_path_tracer
+    W, H, spp = (240, 135, 8) if args.small else (960, 540, 16)
+    s = scenes.sdf_room(width=W, height=H, spp=spp, maxbounce=8, sky="physical")
+    s.params.step_cache = 0
+    views = [scenes.look_at(e, t, 60.0, W / H) for e, t in (((-2.6, -1.6, 1.7), (0.8, 0.9, 1.1)),
+                                                              ((2.5, -1.7, 1.5), (-0.5, 0.8, 0.8)),
+                                                              ((0.0, 1.6, 2.6), (0.0, -0.5, 0.3)),
+                                                              ((-2.5, 1.5, 1.2), (1.0, -0.5, 1.0)))]
+    paths = len(views) * W * H * spp
+    rt = create_path_tracer(s, device=dev, code=True)
+    stream = torch.cuda.ExternalStream(rt.stream(), device=torch.device("cuda", dev))
+
+    def timed(run):
+        run()
+        rt.sync()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        run()
+        e1.record(stream)
+        rt.sync()
+        return e0.elapsed_time(e1)
+
+    def together():
+        rt.set_views(views)
+        rt.step_async(spp)
+
+    def apart():
+        for v in views:
+            rt.set_views([v])
+            rt.step_async(spp)
+    ms_t = timed(together)
+    ms_a = timed(apart)
+    rt.close()
+    return {"workload": "the headline room from 4 cameras, %dx%d, %d samples each" % (W, H, spp), "metric": "Mpaths/s",
+            "together": {"ms": ms_t, "Mpaths_per_s": paths / ms_t / 1e3},
+            "one_after_another": {"ms": ms_a, "Mpaths_per_s": paths / ms_a / 1e3},
+            "speedup": ms_a / ms_t, "value": paths / ms_t / 1e3}
+
+
 def rmse_leg(args, dev):
     """Time to 1 % relative RMSE against the closed form, guided vs plain: the photon map's pane (a 0.5 m glass pane
     over a floor lit only through it, the sun's photons drawn over a 4 m square), plain -- the photons uniform over the
@@ -794,7 +839,8 @@ def run_ours(args):
                "caustic_rmse": lambda: caustic_rmse_leg(args, dev),
                "optics": lambda: optics_leg(args, dev, with_cpu), "mlp": lambda: mlp_leg(args, dev),
                "emit": lambda: emit_leg(args, dev), "haze": lambda: haze_leg(args, dev),
-               "env": lambda: env_leg(args, dev), "sc": lambda: sc_leg(args, dev)}[args.leg]()
+               "env": lambda: env_leg(args, dev), "sc": lambda: sc_leg(args, dev),
+               "views": lambda: views_leg(args, dev)}[args.leg]()
         if rank == 0:
             print(json.dumps(out), flush=True)
         return 0
@@ -974,6 +1020,7 @@ def run_ours(args):
         line["env"] = env_leg(args, dev)
     if not args.no_sc:
         line["step_cache"] = sc_leg(args, dev)
+        line["views"] = views_leg(args, dev)
     if not args.no_optics:
         line["optics"] = optics_leg(args, dev, rank == 0 and world == 1 and not args.no_cpu)
         if world > 1:

@@ -339,6 +339,16 @@ int  st_compile_scene(const char* cuda_src, char* errbuf, size_t errlen, double*
  * settings resets the accumulation. */
 int  st_set_params(st_ctx* ctx, const st_params* p, uint64_t* unknown_mask);
 int  st_set_view(st_ctx* ctx, const st_view* v);
+/* MANY VIEWS IN ONE WAVEFRONT (the batching of many views in one persistent launch): n cameras of the same scene and
+ * settings (1..ST_MAX_VIEWS), each a picture of its own, rendered together -- every step a sample of each, their paths
+ * in the same waves, one march and one occlusion pass over all of them, one photon pass shared. A view's paths take
+ * the random numbers the same view rendered alone takes, so each picture is the one st_set_view would give (but for
+ * the order of f32 deposits into a pixel, and what discovery and training gather from all the views together). Light
+ * tracing connects to one camera: st_step refuses it with more than one view. st_set_view is st_set_views(ctx, v, 1). */
+#define ST_MAX_VIEWS 16
+int  st_set_views(st_ctx* ctx, const st_view* views, uint32_t n);
+/* a view's picture, as st_read_accum reads view 0's */
+int  st_read_accum_view(st_ctx* ctx, uint32_t view, double* rgb, double* V, double* S, uint32_t* count);
 /* THE ENVIRONMENT IMAGE (core/envimage.js, the image preset of core/environment.js; core/envmap.js the map light
  * sampling draws from): an equirectangular panorama, w x h pixels of linear rgb floats, top row first, its middle
  * column +x, running right as one turns right, turned turn_deg about z (anticlockwise from above); luminance is the

@@ -47,6 +47,8 @@ SIGNATURES = {
     "st_sppm_stats_read": ([P, C.POINTER(T.StSppmStats)], C.c_int),
     "st_sppm_emission_map": ([P, P, P, P], C.c_int),
     "st_lt_counts": ([P, P], C.c_int),
+    "st_set_views": ([P, P, C.c_uint32], C.c_int),
+    "st_read_accum_view": ([P, C.c_uint32, P, P, P, P], C.c_int),
     "st_optics_set_sources": ([P, C.POINTER(T.StOpticsSource), C.c_uint32], C.c_int),
     "st_optics_set_far": ([P, C.POINTER(T.StOpticsFar)], C.c_int),
     "st_optics_run": ([P, C.POINTER(T.StOpticsBatch), P, P, C.POINTER(T.StOpticsTotals)], C.c_int),

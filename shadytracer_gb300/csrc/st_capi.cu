@@ -54,6 +54,12 @@ struct st_ctx {
     float4* d_envmap = nullptr;
     uint32_t env_w = 0, env_h = 0;
     float4* d_skytab = nullptr;           // the sun and sky's 16 bands (st_sky.h), once a context
+    // many views in one wave (st_set_views): their cameras and the table the kernels read them from (VIEW_F4 float4s a
+    // view; null with one); view 0 is `view`
+    std::vector<st_view> views;
+    uint32_t nv = 1;
+    uint32_t acc_views = 0;               // the views the accumulation holds
+    float4* d_views = nullptr;
     std::vector<float> env_key;           // what the preset's map was baked from (empty: no preset map)
     float env_lum = 0.f, env_turn = 0.f;
     st_material* d_mats = nullptr;
@@ -266,6 +272,8 @@ static Uni make_uni(const st_ctx* ctx) {
         u.env_lum = ctx->env_lum; u.env_turn = ctx->env_turn;
     }
     u.sky_tab = ctx->d_skytab;
+    u.nv = ctx->nv;
+    u.views = ctx->nv > 1 ? ctx->d_views : nullptr;
     // the map light sampling draws from: an image's, or a preset's (envmap.js bakes one for every environment)
     if (ctx->d_envimg || (u.env_mode != ST_ENV_ANALYTIC && !ctx->env_key.empty())) {
         u.env_map = ctx->d_envmap;
@@ -387,7 +395,8 @@ static uint32_t samples_per_wave(const st_ctx* ctx) {
     if (photons_run(ctx)) return 1;
     if (ctx->params.samples_per_wave) return ctx->params.samples_per_wave;
     const uint32_t target = 4u << 20;   // about four million paths a wave: twenty a lane of a full persistent grid
-    uint32_t s = (target + ctx->P - 1) / ctx->P;
+    const uint32_t per = ctx->P * ctx->nv;      // a sample of every view
+    uint32_t s = (target + per - 1) / per;
     return std::max(1u, std::min(s, 64u));
 }
 
@@ -407,20 +416,20 @@ static int ensure_wave(st_ctx* ctx) {
     }
     if (ctx->params.guide) {
         const uint32_t spw_g = samples_per_wave(ctx);
-        uint32_t cap_g = spw_g * ctx->P;
+        uint32_t cap_g = spw_g * ctx->nv * ctx->P;
         if (photons_run(ctx)) cap_g = std::max(cap_g, std::min(sppm_photons(ctx), 4u << 20));
-        int rc = guide_ensure(ctx, cap_g, spw_g * ctx->P, ctx->params.guide_seed);
+        int rc = guide_ensure(ctx, cap_g, spw_g * ctx->nv * ctx->P, ctx->params.guide_seed);
         if (rc) return rc;
     }
     uint32_t spw = samples_per_wave(ctx);
-    uint32_t cap = spw * ctx->P;
+    uint32_t cap = spw * ctx->nv * ctx->P;
     // the photons run in chunks of the wave's slots: give them room for up to four million at once
     if (photons_run(ctx)) cap = std::max(cap, std::min(sppm_photons(ctx), 4u << 20));
     if (has_emitters(ctx)) {                   // the list's per-slot weights and its hit queue (a shadow side's room)
         int rc = emit_ensure(ctx, cap, 2u * cap);
         if (rc) return rc;
     }
-    bool pixels_changed = !ctx->d_acc;
+    bool pixels_changed = !ctx->d_acc || ctx->acc_views != ctx->nv;
     if (ctx->slot_cap == cap && ctx->spw == spw && !pixels_changed) return ST_OK;
     free_wave(ctx);
     ctx->spw = spw;
@@ -456,15 +465,16 @@ static int ensure_wave(st_ctx* ctx) {
     }
     ctx->q.scap = (uint32_t)SS;
     CK(cudaMalloc(&ctx->d_frame, S * sizeof(float4)), "cudaMalloc frame");
-    CK(cudaMalloc(&ctx->d_acc, (size_t)ctx->P * sizeof(Acc4)), "cudaMalloc accumulation");
-    CK(cudaMalloc(&ctx->d_mom, (size_t)ctx->P * sizeof(double2)), "cudaMalloc moments");
+    CK(cudaMalloc(&ctx->d_acc, (size_t)ctx->nv * ctx->P * sizeof(Acc4)), "cudaMalloc accumulation");
+    CK(cudaMalloc(&ctx->d_mom, (size_t)ctx->nv * ctx->P * sizeof(double2)), "cudaMalloc moments");
+    ctx->acc_views = ctx->nv;
     CK(cudaMalloc(&ctx->d_splat, (size_t)ctx->P * sizeof(float4)), "cudaMalloc splat");
     CK(cudaMalloc(&ctx->d_ltcount, (size_t)ctx->P * sizeof(uint32_t)), "cudaMalloc splat");
     ctx->q.cap = cap;
     ctx->slot_cap = cap;
     CK(cudaMemsetAsync(ctx->d_frame, 0, S * sizeof(float4), ctx->stream), "memset");
-    CK(cudaMemsetAsync(ctx->d_acc, 0, (size_t)ctx->P * sizeof(Acc4), ctx->stream), "memset");
-    CK(cudaMemsetAsync(ctx->d_mom, 0, (size_t)ctx->P * sizeof(double2), ctx->stream), "memset");
+    CK(cudaMemsetAsync(ctx->d_acc, 0, (size_t)ctx->acc_views * ctx->P * sizeof(Acc4), ctx->stream), "memset");
+    CK(cudaMemsetAsync(ctx->d_mom, 0, (size_t)ctx->acc_views * ctx->P * sizeof(double2), ctx->stream), "memset");
     CK(cudaMemsetAsync(ctx->d_splat, 0, (size_t)ctx->P * sizeof(float4), ctx->stream), "memset");
     CK(cudaMemsetAsync(ctx->d_ltcount, 0, (size_t)ctx->P * sizeof(uint32_t), ctx->stream), "memset");
     CK(cudaMemsetAsync(ctx->d_ctr, 0, sizeof(DevCtr), ctx->stream), "memset");
@@ -511,7 +521,7 @@ static WaveArgs wave_args(st_ctx* ctx, uint32_t w) {
     a.acc = ctx->d_acc;
     a.mom = ctx->d_mom;
     a.spw = w;
-    a.slots = w * ctx->P;
+    a.slots = w * ctx->nv * ctx->P;
     a.code = ctx->has_code ? &ctx->code : nullptr;
     if (photons_run(ctx)) {
         a.u.sppm_on = sppm_runs(ctx) ? 1u : 0u;
@@ -754,7 +764,7 @@ int st_destroy(st_ctx* ctx) {
     free_wave(ctx);
     ext_free(ctx->ext);
     if (ctx->has_code) scene_code_free(ctx->code);
-    for (void* p : {(void*)ctx->d_prims, (void*)ctx->d_faces, (void*)ctx->d_envimg, (void*)ctx->d_envmap, (void*)ctx->d_skytab, (void*)ctx->d_sc,
+    for (void* p : {(void*)ctx->d_prims, (void*)ctx->d_faces, (void*)ctx->d_envimg, (void*)ctx->d_envmap, (void*)ctx->d_skytab, (void*)ctx->d_views, (void*)ctx->d_sc,
                     (void*)ctx->d_mats, (void*)ctx->d_ec, (void*)ctx->d_ecavg,
                     (void*)ctx->d_e1, (void*)ctx->d_ctr, (void*)ctx->d_spec})
         if (p) cudaFree(p);
@@ -998,11 +1008,40 @@ int st_set_env_image(st_ctx* ctx, const float* rgb, uint32_t w, uint32_t h, floa
     return ctx->has_params ? st_invalidate(ctx) : ST_OK;
 }
 
-int st_set_view(st_ctx* ctx, const st_view* v) {
-    if (!ctx || !v) return ST_ERR_ARG;
+int st_set_view(st_ctx* ctx, const st_view* v) { return st_set_views(ctx, v, 1); }
+
+// the views rendered together (include/shadytracer.h st_set_views): the table the kernels read, the accumulation of
+// each, the waves sized for all of them
+int st_set_views(st_ctx* ctx, const st_view* views, uint32_t n) {
+    if (!ctx || !views || n == 0 || n > ST_MAX_VIEWS) return ST_ERR_ARG;
     if (ctx->in_flight) return fail(ctx, ST_ERR_BUSY, "a trace is in flight: st_sync first");
-    ctx->view = *v;
+    cudaSetDevice(ctx->device);
+    ctx->views.assign(views, views + n);
+    ctx->view = views[0];
     ctx->has_view = true;
+    if (n > 1) {
+        std::vector<float4> t((size_t)n * VIEW_F4);
+        for (uint32_t i = 0; i < n; i++) {
+            const st_view& v = views[i];
+            float camtype;                                        // its bits, as the kernels read them back
+            std::memcpy(&camtype, &v.camtype, sizeof(float));
+            t[i * VIEW_F4 + 0] = make_float4(v.cam_pos[0], v.cam_pos[1], v.cam_pos[2], camtype);
+            t[i * VIEW_F4 + 1] = make_float4(v.right[0], v.right[1], v.right[2], v.fx);
+            t[i * VIEW_F4 + 2] = make_float4(v.up[0], v.up[1], v.up[2], v.fy);
+            t[i * VIEW_F4 + 3] = make_float4(v.fwd[0], v.fwd[1], v.fwd[2], v.lens_radius > 0.f ? v.lens_radius : 0.f);
+            t[i * VIEW_F4 + 4] = make_float4(v.focus_distance, 0.f, 0.f, 0.f);
+        }
+        if (!ctx->d_views) CK(cudaMalloc(&ctx->d_views, (size_t)ST_MAX_VIEWS * VIEW_F4 * sizeof(float4)), "cudaMalloc views");
+        CK(cudaMemcpy(ctx->d_views, t.data(), t.size() * sizeof(float4), cudaMemcpyHostToDevice), "views upload");
+    }
+    if (n != ctx->nv) {
+        ctx->nv = n;
+        if (ctx->has_params) {
+            free_wave(ctx);
+            int rc = ensure_wave(ctx);
+            if (rc) return rc;
+        }
+    }
     invalidate_graph(ctx);
     return st_invalidate(ctx);
 }
@@ -1013,8 +1052,8 @@ int st_invalidate(st_ctx* ctx) {
     cudaSetDevice(ctx->device);
     // stream-ordered: it takes effect after whatever is queued, so it needs no st_sync (RT.invalidate may be called
     // between queued samples); the sample index restarts, the statistics keep accumulating
-    CK(cudaMemsetAsync(ctx->d_acc, 0, (size_t)ctx->P * sizeof(Acc4), ctx->stream), "memset");
-    CK(cudaMemsetAsync(ctx->d_mom, 0, (size_t)ctx->P * sizeof(double2), ctx->stream), "memset");
+    CK(cudaMemsetAsync(ctx->d_acc, 0, (size_t)ctx->acc_views * ctx->P * sizeof(Acc4), ctx->stream), "memset");
+    CK(cudaMemsetAsync(ctx->d_mom, 0, (size_t)ctx->acc_views * ctx->P * sizeof(double2), ctx->stream), "memset");
     CK(cudaMemsetAsync(ctx->d_frame, 0, (size_t)ctx->slot_cap * sizeof(float4), ctx->stream), "memset");
     CK(cudaMemsetAsync(ctx->d_splat, 0, (size_t)ctx->P * sizeof(float4), ctx->stream), "memset");
     CK(cudaMemsetAsync(ctx->d_ltcount, 0, (size_t)ctx->P * sizeof(uint32_t), ctx->stream), "memset");
@@ -1067,6 +1106,8 @@ int st_step_async(st_ctx* ctx, int n) {
     if (!ctx || n < 0) return ST_ERR_ARG;
     if (!ctx->has_scene || !ctx->has_params || !ctx->has_view)
         return fail(ctx, ST_ERR_STATE, "set a scene, the settings and the view first");
+    if (ctx->nv > 1 && ctx->params.lt)
+        return fail(ctx, ST_ERR_ARG, "light tracing connects to one camera: one view with st_params.lt");
     cudaSetDevice(ctx->device);
     int rc = ensure_wave(ctx);
     if (rc) return rc;
@@ -1134,14 +1175,21 @@ int st_step(st_ctx* ctx, int n) {
 }
 
 int st_read_accum(st_ctx* ctx, double* rgb, double* V, double* S, uint32_t* count) {
+    return st_read_accum_view(ctx, 0, rgb, V, S, count);
+}
+int st_read_accum_view(st_ctx* ctx, uint32_t view, double* rgb, double* V, double* S, uint32_t* count) {
     if (!ctx) return ST_ERR_ARG;
     if (!ctx->d_acc) return fail(ctx, ST_ERR_STATE, "nothing rendered yet");
+    if (view >= ctx->acc_views) return fail(ctx, ST_ERR_ARG, "no such view");
     if (ctx->in_flight) { int rc = st_sync(ctx, -1); if (rc) return rc; }
     cudaSetDevice(ctx->device);
     std::vector<Acc4> acc(ctx->P);
     std::vector<double2> mom(ctx->P);
-    CK(cudaMemcpyAsync(acc.data(), ctx->d_acc, acc.size() * sizeof(Acc4), cudaMemcpyDeviceToHost, ctx->stream), "readback");
-    CK(cudaMemcpyAsync(mom.data(), ctx->d_mom, mom.size() * sizeof(double2), cudaMemcpyDeviceToHost, ctx->stream), "readback");
+    const size_t off = (size_t)view * ctx->P;
+    CK(cudaMemcpyAsync(acc.data(), ctx->d_acc + off, acc.size() * sizeof(Acc4), cudaMemcpyDeviceToHost, ctx->stream),
+       "readback");
+    CK(cudaMemcpyAsync(mom.data(), ctx->d_mom + off, mom.size() * sizeof(double2), cudaMemcpyDeviceToHost, ctx->stream),
+       "readback");
     CK(cudaStreamSynchronize(ctx->stream), "readback");
     for (uint32_t i = 0; i < ctx->P; i++) {
         if (rgb) { rgb[3 * i] = acc[i].x; rgb[3 * i + 1] = acc[i].y; rgb[3 * i + 2] = acc[i].z; }

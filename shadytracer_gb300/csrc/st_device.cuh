@@ -137,7 +137,14 @@ struct Uni {
     uint32_t lt_on;
     uint32_t photon_pass;        // the wave's photon pass: its rays are photons, seeded by the photon's own stream
     uint32_t lt_emit_n;          // of the sample's sppm_n photons, the first this many are emitter probes (0: none)
+    // many views in one wave (st_set_views): nv pictures of P pixels; a wave's frame k (slot / P) is sample k / nv of
+    // view k % nv; each view's camera in the table (VIEW_F4 float4s a view), null with one
+    uint32_t nv; const float4* views;
 };
+#define VIEW_F4 5
+// a slot's sample within its wave (what seeds its paths) and its view
+__device__ __forceinline__ uint32_t slot_sample(const Uni& u, uint32_t slot) { return (slot / u.P) / max(u.nv, 1u); }
+__device__ __forceinline__ uint32_t slot_view(const Uni& u, uint32_t slot) { return (slot / u.P) % max(u.nv, 1u); }
 
 // ------------------------------------------------------------------------------------------------------------
 // DISPERSION (spectral.js:121-128 cauchyN, :136-137 lambdaCode; lightspectra.js specDraw): Cauchy's index through a

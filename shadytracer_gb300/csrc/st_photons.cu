@@ -740,7 +740,7 @@ __global__ void __launch_bounds__(256, 2) k_gather(WaveArgs a) {
         // 0 or its drawn sub-lists' ranges on lanes 0..m-1 (loaded at once), walked as one list 32 records a pass
         for (uint32_t todo = slow; todo != 0u; todo &= todo - 1u) {
             const GatherQuery& g = gq[__ffs(todo) - 1];
-            const uint32_t tile = g.slot % u.P, j = g.slot / u.P, seg = (g.my >> 8) & 0xffu;
+            const uint32_t tile = g.slot % u.P, j = slot_sample(u, g.slot), seg = (g.my >> 8) & 0xffu;
             Rng rng = path_rng(sample_seed(u.seed, a.ctr->sample + j), tile, SPPM_STORE_SALT + seg);
             f3 sum = mk(0.f);
             uint32_t visits = 0;

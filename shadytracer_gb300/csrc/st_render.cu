@@ -80,7 +80,20 @@ __global__ void __launch_bounds__(256) k_genrays(WaveArgs a) {
     const Uni& u = a.u;
     const uint32_t first = a.ctr->sample;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < a.slots; i += gridDim.x * blockDim.x) {
-        uint32_t tile = i % u.P, j = i / u.P;
+        uint32_t tile = i % u.P, j = slot_sample(u, i);
+        // the slot's camera: its view's (many views in the wave), else the one
+        f3 ucam = u.cam, uright = u.right, uup = u.up, ufwd = u.fwd;
+        float ufx = u.fx, ufy = u.fy, ulens_r = u.lens_r, ulens_f = u.lens_f;
+        uint32_t ucamtype = u.camtype;
+        if (u.views) {
+            const float4* vw = u.views + (size_t)slot_view(u, i) * VIEW_F4;
+            const float4 v0 = vw[0], v1 = vw[1], v2 = vw[2], v3 = vw[3], v4 = vw[4];
+            ucam = xyz(v0); ucamtype = __float_as_uint(v0.w);
+            uright = xyz(v1); ufx = v1.w;
+            uup = xyz(v2); ufy = v2.w;
+            ufwd = xyz(v3); ulens_r = v3.w;
+            ulens_f = v4.x;
+        }
         Rng rng = path_rng(sample_seed(u.seed, first + j), tile, 0);
         float cx = float(tile % u.tilesX), cy = float(tile / u.tilesX);
         float uv0x = (cx + 0.5f) * u.invTX, uv0y = (cy + 0.5f) * u.invTY;
@@ -89,23 +102,23 @@ __global__ void __launch_bounds__(256) k_genrays(WaveArgs a) {
         float uy = clampf(uv0y + (rnd.y - 0.5f) * u.invTY, 0.f, 1.f);
         float xx = ux * 2.f - 1.f, yy = uy * 2.f - 1.f;
         f3 pos, dir;
-        if (u.camtype == 0) {
-            f3 dc = mk(xx * u.fx, yy * u.fy, -1.f);
-            dir = normalize(u.right * dc.x + u.up * dc.y + u.fwd * dc.z);
-            pos = u.cam;
+        if (ucamtype == 0) {
+            f3 dc = mk(xx * ufx, yy * ufy, -1.f);
+            dir = normalize(uright * dc.x + uup * dc.y + ufwd * dc.z);
+            pos = ucam;
             // THROUGH THE LENS (genrays.js:80-87, lens.js lensDisc): from a point of its disc (the same draw's zw),
             // at the point the pinhole's ray meets the focus plane
-            if (u.lens_r > 0.f) {
-                const float r = u.lens_r * sqrtf(rnd.z);
+            if (ulens_r > 0.f) {
+                const float r = ulens_r * sqrtf(rnd.z);
                 float sp, cp;
                 sincosf(6.28318530718f * rnd.w, &sp, &cp);
-                const f3 off = u.right * (r * cp) + u.up * (r * sp);
-                pos = u.cam + off;
-                dir = normalize((u.right * dc.x + u.up * dc.y + u.fwd * dc.z) * u.lens_f - off);
+                const f3 off = uright * (r * cp) + uup * (r * sp);
+                pos = ucam + off;
+                dir = normalize((uright * dc.x + uup * dc.y + ufwd * dc.z) * ulens_f - off);
             }
         } else {
-            pos = u.cam + u.right * (xx * u.fx) + u.up * (yy * u.fy);
-            dir = -u.fwd;
+            pos = ucam + uright * (xx * ufx) + uup * (yy * ufy);
+            dir = -ufwd;
         }
         dir = normalize(dir);
         float px = clampf(ux * float(u.W), 0.f, float(u.W) - 1.f), py = clampf(uy * float(u.H), 0.f, float(u.H) - 1.f);
@@ -623,7 +636,7 @@ __global__ void __launch_bounds__(256) k_shade(WaveArgs a, int nxt, int side, in
                 train_nee = GUIDE && (m4.y & META_TRAIN) != 0u;       // light found past a record's vertex counts
                 if (a.em.on) emw = a.em.w[slot];
                 if (a.lf.n) lp = a.pb.lprev[slot];
-                uint32_t tile = slot % u.P, j = slot / u.P;
+                uint32_t tile = slot % u.P, j = slot_sample(u, slot);
                 Rng rng = path_rng(sample_seed(u.seed, a.ctr->sample + j), tile, 1u + seg);
                 seg += 1;
                 float absL = __uint_as_float(m4.w);                   // absorbAlong: ltot on arrival at the last vertex
@@ -677,9 +690,9 @@ __global__ void __launch_bounds__(256) k_shade(WaveArgs a, int nxt, int side, in
             a.pb.meta[slot] = m4;
             outq[rq] = slot;
         } else if (valid) {
-            // THE PATH IS OVER (wavefront.js:1400-1425): its radiance into this sample's frame, counted once
-            uint32_t j = slot / u.P;
-            float4* fr = a.frame + (size_t)j * u.P;
+            // THE PATH IS OVER (wavefront.js:1400-1425): its radiance into this sample's (and view's) frame, once
+            uint32_t k = slot / u.P;
+            float4* fr = a.frame + (size_t)k * u.P;
             deposit(fr, pix, rad, a.ctr);
             atomicAdd(&fr[pix].w, 1.f);
             paths++;
@@ -707,21 +720,24 @@ __global__ void __launch_bounds__(256) k_shade(WaveArgs a, int nxt, int side, in
 // ------------------------------------------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) k_resolve(WaveArgs a) {
     const Uni& u = a.u;
-    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;                 // view i / P's pixel i % P
     if (i == 0) atomicAdd(&a.ctr->sample, a.spw);
-    if (i >= u.P) return;
+    const uint32_t nv = max(u.nv, 1u);
+    if (i >= nv * u.P) return;
+    const uint32_t view = i / u.P, pix = i % u.P;
     Acc4 acc = a.acc[i];
     double2 mo = a.mom[i];
     // light tracing's estimate for the pixel (one sample a wave while it runs), taken and cleared first: added as it
     // is, not averaged with the pixel's paths (wavefront.js:425-433, :459-462)
     float4 lt = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (u.lt_on) {
+    if (u.lt_on && view == 0u) {                                      // one view while light tracing runs
         lt = a.splat[i];
         a.splat[i] = make_float4(0.f, 0.f, 0.f, 0.f);
     }
     for (uint32_t j = 0; j < a.spw; j++) {
-        float4 f = a.frame[(size_t)j * u.P + i];
-        a.frame[(size_t)j * u.P + i] = make_float4(0.f, 0.f, 0.f, 0.f);
+        const size_t fi = (size_t)(j * nv + view) * u.P + pix;
+        float4 f = a.frame[fi];
+        a.frame[fi] = make_float4(0.f, 0.f, 0.f, 0.f);
         uint32_t n = (uint32_t)f.w;
         if (n == 0u) continue;
         double sx = double(f.x) / n + lt.x, sy = double(f.y) / n + lt.y, sz = double(f.z) / n + lt.z;
@@ -909,7 +925,7 @@ cudaError_t launch_occlude(const WaveArgs& a, int side, int last, int sms, cudaS
     return cudaGetLastError();
 }
 cudaError_t launch_resolve(const WaveArgs& a, cudaStream_t s) {
-    k_resolve<<<(a.u.P + 255) / 256, 256, 0, s>>>(a);
+    k_resolve<<<((a.u.nv ? a.u.nv : 1u) * a.u.P + 255) / 256, 256, 0, s>>>(a);
     return cudaGetLastError();
 }
 

@@ -102,7 +102,7 @@ __global__ void __launch_bounds__(256, 4) k_march(WaveArgs a, int cur, int nxt, 
                             float t0, t1;
                             haze_span(u, A, dir, 1e30f, t0, t1);
                             if (t1 > t0) {
-                                uint32_t tile = slot % u.P, j = slot / u.P, seg = (m4.y >> 8) & 0xffu;
+                                uint32_t tile = slot % u.P, j = slot_sample(u, slot), seg = (m4.y >> 8) & 0xffu;
                                 // a photon's from its own stream (its id), a camera path's from its path's
                                 Rng hr = u.photon_pass
                                              ? path_rng(photon_seed_of(u.seed, a.ctr->sample), m4.x, ST_SALT_HAZE + seg)

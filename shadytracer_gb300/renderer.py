@@ -97,6 +97,13 @@ class PathTracer:
         check(self.L.st_set_view(self.ctx, C.byref(v)), self.ctx, "st_set_view")
         self.view = v
 
+    def set_views(self, views):
+        """Many cameras of the scene rendered together (st_set_views): every step a sample of each, a picture each
+        (read_accum(view=i))."""
+        arr = (T.StView * len(views))(*views)
+        check(self.L.st_set_views(self.ctx, arr, len(views)), self.ctx, "st_set_views")
+        self.view = views[0]
+
     def set_env_image(self, rgb=None, luminance=0.0, turn=0.0):
         """The environment as an equirectangular image (envimage.js): `rgb` H x W x 3 linear floats, top row first,
         `luminance` cd/m^2 a unit (0: 179), turned `turn` degrees about z; None goes back to the sun and sky."""
@@ -148,16 +155,17 @@ class PathTracer:
         check(self.L.st_lt_counts(self.ctx, out.ctypes.data_as(C.c_void_p)), self.ctx, "st_lt_counts")
         return out
 
-    def read_accum(self):
-        """(rgb HxWx3, V HxW, S HxW, count HxW): the FP64 mean, the error bar's moments, the samples per pixel."""
+    def read_accum(self, view=0):
+        """(rgb HxWx3, V HxW, S HxW, count HxW): the FP64 mean, the error bar's moments, the samples per pixel (of
+        the view'th camera, with many)."""
         W, H = self.params.width, self.params.height
         rgb = np.zeros((H, W, 3), np.float64)
         V = np.zeros((H, W), np.float64)
         S = np.zeros((H, W), np.float64)
         cnt = np.zeros((H, W), np.uint32)
         P = C.c_void_p
-        check(self.L.st_read_accum(self.ctx, rgb.ctypes.data_as(P), V.ctypes.data_as(P), S.ctypes.data_as(P),
-                                   cnt.ctypes.data_as(P)), self.ctx, "st_read_accum")
+        check(self.L.st_read_accum_view(self.ctx, int(view), rgb.ctypes.data_as(P), V.ctypes.data_as(P),
+                                        S.ctypes.data_as(P), cnt.ctypes.data_as(P)), self.ctx, "st_read_accum_view")
         return rgb, V, S, cnt
 
     def image_stats(self):
