@@ -668,7 +668,7 @@ def views_leg(args, dev):
     def apart():
         for v in views:
             rt.set_views([v])
-            rt.step_async(spp)
+            rt.step(spp)                  # (a view's settings change only between traces)
     ms_t = timed(together)
     ms_a = timed(apart)
     rt.close()

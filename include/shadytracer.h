@@ -251,6 +251,12 @@ typedef struct st_params {
      * its flux the emission over the probes and the line density there (Crofton) -- which then connect and are stored
      * as the sun's are; the camera's paths leave the emitters' light in light tracing's class to them */
     float    lt_emit_share;       /* 0: 0.5; clamped to [0.05, 0.95] while the sun shines (the reference's ltEmitShare) */
+    /* THE ENVIRONMENT IN A TEXTURE (core/envmap.js, UniformSpec envCache / envCacheSize, on by default there): a
+     * preset's light baked once a change into an equirectangular env_cache_size x half texture (2 x 2 points a texel,
+     * the sun's cone left out), which every ray that leaves and every light sample reads bilinearly; in the sun's cone
+     * the preset itself is asked */
+    uint32_t env_cache;           /* 1 on                                                           */
+    uint32_t env_cache_size;      /* 1024, 2048 or 4096 (0: 2048)                                  */
 } st_params;
 
 #define ST_ENV_ANALYTIC 0u

@@ -1499,10 +1499,21 @@ static int render_impl(const st_scene_desc* s, const st_params* p, const st_view
     if (cull) { boxes = cull_boxes(*s); C.cull = &boxes; }
     C.s = s; C.p = *p; C.d = derive(*p, *s);
     C.env.init(*p, C.d);
-    std::vector<float> preset_tex;                  // a preset's map (the image's is its own)
+    std::vector<float> preset_tex, preset_cache;    // a preset's map (the image's is its own) and texture
     if (C.env.mode != 0 && !C.env.img) {
+        if (p->env_cache) {
+            const uint32_t tw = (p->env_cache_size == 1024u || p->env_cache_size == 4096u) ? p->env_cache_size : 2048u;
+            preset_cache = preset_texture(C.env, tw, tw / 2);
+            C.env.cache = &preset_cache;
+            C.env.cache_w = tw; C.env.cache_h = tw / 2;
+        }
         preset_tex = preset_map(C.env);
         C.env.init(*p, C.d, &preset_tex);
+        if (p->env_cache) {                          // init starts over: the texture back in
+            const uint32_t tw = (p->env_cache_size == 1024u || p->env_cache_size == 4096u) ? p->env_cache_size : 2048u;
+            C.env.cache = &preset_cache;
+            C.env.cache_w = tw; C.env.cache_h = tw / 2;
+        }
     }
     C.tb = tables<T>();
     C.tol = T(C.d.tol_setting);

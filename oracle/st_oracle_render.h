@@ -378,6 +378,8 @@ template <class T> struct Env {
     V3<T> disc; T sky, ground, uniform, sun_gain, sky_gain;
     const EnvImage* img = nullptr;          // the environment image, and its map's share of the samples
     const std::vector<float>* tex = nullptr; // the map's tables: the image's, or a preset's
+    const std::vector<float>* cache = nullptr;   // a preset in a texture (envCache): rgb, cache_w x cache_h
+    uint32_t cache_w = 0, cache_h = 0;
     T mshare = 0;
     // the presets: the mode, the sun and sky's light above the air and aerosol depth at 550 nm; the studio's L0, top
     // and colour
@@ -481,9 +483,26 @@ template <class T> struct Env {
         const int row = std::min(std::max((int)((T(1) - d.z) * T(0.5) * T(ENV_MH)), 0), ENV_MH - 1);
         return (T)(*tex)[4 * ((size_t)row * ENV_MW + col) + 1];
     }
+    // THE ENVIRONMENT FROM ITS TEXTURE (envmap.js:162-182 envCacheAt): bilinear, wrapping, clamped at the poles
+    V3<T> cache_at(const V3<T>& d) const {
+        const int w = (int)cache_w, h = (int)cache_h;
+        double a = std::atan2((double)d.y, (double)d.x) / (2.0 * PI_D);
+        a -= std::floor(a);
+        const double u = a * w - 0.5, v = std::acos(std::min(1.0, std::max(-1.0, (double)d.z))) / PI_D * h - 0.5;
+        const double x0 = std::floor(u), y0 = std::floor(v), fx = u - x0, fy = v - y0;
+        const int xa = (((int)x0 % w) + w) % w, xb = (xa + 1) % w;
+        const int ya = std::min(std::max((int)y0, 0), h - 1), yb = std::min(std::max((int)y0 + 1, 0), h - 1);
+        double c[3];
+        for (int k = 0; k < 3; k++) {
+            auto px = [&](int x, int y) { return (double)(*cache)[((size_t)y * w + x) * 3 + k]; };
+            c[k] = (px(xa, ya) * (1 - fx) + px(xb, ya) * fx) * (1 - fy) + (px(xa, yb) * (1 - fx) + px(xb, yb) * fx) * fy;
+        }
+        return V3<T>(T(c[0]), T(c[1]), T(c[2]));
+    }
     V3<T> base(const V3<T>& dir) const {                             // sdf.js:121-130 envBase
         if (img) return image(dir);
         if (uniform > T(0)) return V3<T>(uniform);
+        if (cache && !(sun_on && in_sun_disc(dir))) return cache_at(normalize(dir));
         if (mode == 1) return sun_sky(normalize(dir));
         if (mode == 2) return studio(normalize(dir));
         V3<T> c = background(normalize(dir));
@@ -507,6 +526,27 @@ template <class T> struct Env {
 // A PRESET'S MAP (envmap.js:100-150 prog_envbake, as the library bakes it): per texel of the equal-area map the
 // environment's own light at 2 x 2 stratified points, the sun's cone left out where there is one, its mean luminance;
 // then the tables
+// A PRESET'S TEXTURE (envmap.js:186-202 ENV_CACHE_MAIN): a texel the preset's light over 2 x 2 points even in azimuth
+// and angle, the sun's cone left out
+template <class T> inline std::vector<float> preset_texture(const Env<T>& e, uint32_t w, uint32_t h) {
+    std::vector<float> out((size_t)w * h * 3);
+#pragma omp parallel for schedule(static)
+    for (long i = 0; i < (long)w * h; i++) {
+        const double x = (double)(i % w), y = (double)(i / w);
+        double acc[3] = {0, 0, 0}, n = 0;
+        for (int sy = 0; sy < 2; sy++)
+            for (int sx = 0; sx < 2; sx++) {
+                const double u = (x + (sx + 0.5) * 0.5) / w, v = (y + (sy + 0.5) * 0.5) / h;
+                const double ph = 2 * PI_D * u, th = PI_D * v;
+                const V3<T> d(T(std::sin(th) * std::cos(ph)), T(std::sin(th) * std::sin(ph)), T(std::cos(th)));
+                if (e.sun_on && e.in_sun_disc(d)) continue;
+                const V3<T> c = e.base(d);
+                acc[0] += (double)c.x; acc[1] += (double)c.y; acc[2] += (double)c.z; n += 1;
+            }
+        for (int k = 0; k < 3; k++) out[(size_t)i * 3 + k] = (float)(acc[k] / std::max(n, 1.0));
+    }
+    return out;
+}
 template <class T> inline std::vector<float> preset_map(const Env<T>& e) {
     std::vector<double> lum((size_t)ENV_MW * ENV_MH);
     for (int i = 0; i < ENV_MW * ENV_MH; i++) {

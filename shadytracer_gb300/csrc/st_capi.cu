@@ -61,6 +61,8 @@ struct st_ctx {
     uint32_t acc_views = 0;               // the views the accumulation holds
     float4* d_views = nullptr;
     std::vector<float> env_key;           // what the preset's map was baked from (empty: no preset map)
+    float4* d_envtex = nullptr;           // the preset in a texture (envCache), env_tw x env_th; null, none
+    uint32_t env_tw = 0, env_th = 0;
     float env_lum = 0.f, env_turn = 0.f;
     st_material* d_mats = nullptr;
     st_params params{};
@@ -272,6 +274,9 @@ static Uni make_uni(const st_ctx* ctx) {
         u.env_lum = ctx->env_lum; u.env_turn = ctx->env_turn;
     }
     u.sky_tab = ctx->d_skytab;
+    if (ctx->d_envtex && u.env_mode != ST_ENV_ANALYTIC && !ctx->env_key.empty()) {
+        u.env_tex = ctx->d_envtex; u.env_tw = ctx->env_tw; u.env_th = ctx->env_th;
+    }
     u.nv = ctx->nv;
     u.views = ctx->nv > 1 ? ctx->d_views : nullptr;
     // the map light sampling draws from: an image's, or a preset's (envmap.js bakes one for every environment)
@@ -764,7 +769,7 @@ int st_destroy(st_ctx* ctx) {
     free_wave(ctx);
     ext_free(ctx->ext);
     if (ctx->has_code) scene_code_free(ctx->code);
-    for (void* p : {(void*)ctx->d_prims, (void*)ctx->d_faces, (void*)ctx->d_envimg, (void*)ctx->d_envmap, (void*)ctx->d_skytab, (void*)ctx->d_views, (void*)ctx->d_sc,
+    for (void* p : {(void*)ctx->d_prims, (void*)ctx->d_faces, (void*)ctx->d_envimg, (void*)ctx->d_envmap, (void*)ctx->d_skytab, (void*)ctx->d_views, (void*)ctx->d_envtex, (void*)ctx->d_sc,
                     (void*)ctx->d_mats, (void*)ctx->d_ec, (void*)ctx->d_ecavg,
                     (void*)ctx->d_e1, (void*)ctx->d_ctr, (void*)ctx->d_spec})
         if (p) cudaFree(p);
@@ -953,6 +958,7 @@ static int env_preset_ensure(st_ctx* ctx) {
     if (p.env_mode == ST_ENV_ANALYTIC || p.env_mode > ST_ENV_STUDIO || p.env_uniform > 0.f) {
         if (!ctx->env_key.empty()) {
             if (ctx->d_envmap) { cudaFree(ctx->d_envmap); ctx->d_envmap = nullptr; }
+            if (ctx->d_envtex) { cudaFree(ctx->d_envtex); ctx->d_envtex = nullptr; }
             ctx->env_key.clear();
         }
         return ST_OK;
@@ -963,10 +969,22 @@ static int env_preset_ensure(st_ctx* ctx) {
         CK(cudaMalloc(&ctx->d_skytab, f.size() * sizeof(float)), "cudaMalloc sky table");
         CK(cudaMemcpy(ctx->d_skytab, f.data(), f.size() * sizeof(float), cudaMemcpyHostToDevice), "sky table upload");
     }
+    const uint32_t tw = p.env_cache ? (p.env_cache_size == 1024u || p.env_cache_size == 4096u ? p.env_cache_size : 2048u)
+                                    : 0u;
     const std::vector<float> key = {(float)p.env_mode, p.sun_elevation, p.sun_azimuth, p.sun_diameter, p.sun_outside,
                                     p.sky_turbidity, p.studio_illuminance, p.studio_top, p.studio_color[0],
-                                    p.studio_color[1], p.studio_color[2], (float)p.sun_hint};
+                                    p.studio_color[1], p.studio_color[2], (float)p.sun_hint, (float)tw};
     if (key == ctx->env_key && ctx->d_envmap) return ST_OK;
+    // the texture (envmap.js THE ENVIRONMENT IN A TEXTURE), baked from the preset itself, then the map from either
+    if (ctx->d_envtex) { cudaFree(ctx->d_envtex); ctx->d_envtex = nullptr; }
+    ctx->env_key.clear();
+    if (tw) {
+        const uint32_t th = tw / 2;
+        CK(cudaMalloc(&ctx->d_envtex, (size_t)tw * th * sizeof(float4)), "cudaMalloc environment texture");
+        Uni u = make_uni(ctx);                                   // no texture yet: the preset itself
+        CK(launch_env_cache(u, ctx->d_envtex, tw, th, ctx->stream), "environment texture");
+        ctx->env_tw = tw; ctx->env_th = th;
+    }
     ctx->env_key = key;
     return env_map_bake(ctx);
 }

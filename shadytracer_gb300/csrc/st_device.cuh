@@ -118,6 +118,7 @@ struct Uni {
     // its 16 bands (st_sky.h: per band Rayleigh depth, aerosol factor, ozone depth, then its colour); the studio's L0,
     // its top and its colour
     uint32_t env_mode; float sun_outside, aerosol; const float4* sky_tab;
+    const float4* env_tex; uint32_t env_tw, env_th;   // the preset in a texture (envmap.js envCacheAt); null, none
     float studio_l0, studio_top; f3 studio_tint;
     // the step cache (wavefront.js:67-118): the cells' distances, the grid's low corner and cell size, its cells, looks
     const float* sc; f3 sc_lo; float sc_cs; uint32_t sc_dx, sc_dy, sc_dz, sc_looks;
@@ -521,10 +522,29 @@ __device__ __forceinline__ f3 sun_sky(const Uni& u, f3 d) {
 __device__ __forceinline__ f3 studio_light(const Uni& u, f3 d) {
     return u.studio_tint * (u.studio_l0 * fmaxf(1.f + u.studio_top * d.z, 0.f));
 }
+// THE ENVIRONMENT FROM ITS TEXTURE (envmap.js:162-182 envCacheAt): equirectangular, columns the azimuth from +x, rows
+// even in angle from straight up; bilinear, wrapping across the seam, clamped at the poles
+__device__ __forceinline__ f3 env_cache_at(const Uni& u, f3 d) {
+    const int w = (int)u.env_tw, h = (int)u.env_th;
+    float a = atan2f(d.y, d.x) * (0.5f / ST_PI);
+    a -= floorf(a);
+    const float uu = a * (float)w - 0.5f;
+    const float vv = acosf(clampf(d.z, -1.f, 1.f)) * (1.f / ST_PI) * (float)h - 0.5f;
+    const float x0 = floorf(uu), y0 = floorf(vv), fx = uu - x0, fy = vv - y0;
+    const int xa = (((int)x0 % w) + w) % w, xb = (xa + 1) % w;
+    const int ya = min(max((int)y0, 0), h - 1), yb = min(max((int)y0 + 1, 0), h - 1);
+    const float4 p00 = __ldg(&u.env_tex[(size_t)ya * w + xa]), p01 = __ldg(&u.env_tex[(size_t)ya * w + xb]);
+    const float4 p10 = __ldg(&u.env_tex[(size_t)yb * w + xa]), p11 = __ldg(&u.env_tex[(size_t)yb * w + xb]);
+    const f3 top = mk(p00.x, p00.y, p00.z) * (1.f - fx) + mk(p01.x, p01.y, p01.z) * fx;
+    const f3 bot = mk(p10.x, p10.y, p10.z) * (1.f - fx) + mk(p11.x, p11.y, p11.z) * fx;
+    return top * (1.f - fy) + bot * fy;
+}
 __device__ __forceinline__ f3 env_base(const Uni& u, f3 dir) {
     if (u.env_img) return env_image(u, dir);
     if (u.uniform > 0.f) return mk(u.uniform);
     f3 d = normalize(dir);
+    // a preset from its texture, outside the sun's cone (sdf.js envBase)
+    if (u.env_tex && !(u.sun_on && in_sun_disc(u, d))) return env_cache_at(u, d);
     if (u.env_mode == 1u) return sun_sky(u, d);
     if (u.env_mode == 2u) return studio_light(u, d);
     if (in_sun_disc(u, d)) return u.disc;

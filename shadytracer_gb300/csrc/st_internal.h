@@ -249,6 +249,7 @@ cudaError_t launch_shade(const WaveArgs& a, int nxt, int side, int last, int sms
 cudaError_t launch_occlude(const WaveArgs& a, int side, int last, int sms, cudaStream_t s);
 cudaError_t launch_resolve(const WaveArgs& a, cudaStream_t s);
 cudaError_t launch_env_bake(const Uni& u, float* out, cudaStream_t s);
+cudaError_t launch_env_cache(const Uni& u, float4* out, uint32_t w, uint32_t h, cudaStream_t s);
 cudaError_t launch_sc_fill(const DPrim* prims, uint32_t n_prims, f3 lo, float cs, uint32_t dx, uint32_t dy, uint32_t dz,
                            float* out, int sms, cudaStream_t s, const SceneCode* code = nullptr);
 // the emitter list (st_emit.cu)

@@ -847,6 +847,30 @@ cudaError_t launch_sc_fill(const DPrim* prims, uint32_t n_prims, f3 lo, float cs
     k_sc_fill<TableScene><<<sms * 8, 256, 0, s>>>(prims, n_prims, lo, cs, dx, dy, dz, out);
     return cudaGetLastError();
 }
+// THE ENVIRONMENT'S TEXTURE (envmap.js:186-202 ENV_CACHE_MAIN): a texel the preset's light averaged over 2 x 2 points
+// even in azimuth and angle, the sun's cone left out (there the preset itself is asked)
+__global__ void __launch_bounds__(256) k_env_cache(Uni u, float4* __restrict__ out, uint32_t w, uint32_t h) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= w * h) return;
+    const float x = (float)(i % w), y = (float)(i / w);
+    f3 acc = mk(0.f);
+    float n = 0.f;
+    for (int sy = 0; sy < 2; sy++)
+        for (int sx = 0; sx < 2; sx++) {
+            const float uu = (x + ((float)sx + 0.5f) * 0.5f) / (float)w, vv = (y + ((float)sy + 0.5f) * 0.5f) / (float)h;
+            float sp, cp, st, ct;
+            sincosf(2.f * ST_PI * uu, &sp, &cp);
+            sincosf(ST_PI * vv, &st, &ct);
+            const f3 d = mk(st * cp, st * sp, ct);
+            if (!(u.sun_on && in_sun_disc(u, d))) { acc = acc + env_base(u, d); n += 1.f; }
+        }
+    acc = acc * (1.f / fmaxf(n, 1.f));
+    out[i] = make_float4(acc.x, acc.y, acc.z, 1.f);
+}
+cudaError_t launch_env_cache(const Uni& u, float4* out, uint32_t w, uint32_t h, cudaStream_t s) {
+    k_env_cache<<<(w * h + 255) / 256, 256, 0, s>>>(u, out, w, h);
+    return cudaGetLastError();
+}
 cudaError_t launch_env_bake(const Uni& u, float* out, cudaStream_t s) {
     k_env_bake<<<(ENV_MW * ENV_MH + 255) / 256, 256, 0, s>>>(u, out);
     return cudaGetLastError();
