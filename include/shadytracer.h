@@ -111,7 +111,19 @@ typedef struct st_material {
                            * (materials.js Material2.haze): 0 clear, 1 an opal face                              */
     float anisotropy;     /* stretches the gloss along the surface's first tangent: 0 round, 1 ten to one
                            * (materials.js Material2.anisotropy; the frame the normal's own, no grain)           */
-    float pad[2];         /* 80 bytes                                                                 */
+    /* A COATING (materials.js:52-89 Material2.coat, coatR, coatEdge, coatWidth, coatIndex; :150-163 coatMaterial):
+     * a thin-film stack that is the interface instead of the bare Fresnel. R(lambda) runs from coat_lo below
+     * coat_edge (nm, at normal incidence) to coat_hi above it, a logistic of 10-90 % width coat_width (nm, 0 a step);
+     * the edge moves to shorter wavelengths with the angle through the stack's effective index coat_index. A
+     * channel's reflectance is R averaged over that channel's wavelengths. coat: where it is -- 0 none, 1 on the
+     * faces light enters by with the faces it leaves by anti-reflective, 2 entering with the leaving faces bare
+     * (the glass's Fresnel), 3 every face. On a metal the stack lies over it. specular and specular_tint do nothing
+     * where a coating is. coat_lo and coat_hi are held to [0, 1], coat_width to >= 0, coat_index to >= 1. */
+    uint32_t coat;
+    float coat_lo, coat_hi;
+    float coat_edge;      /* nm                                                                     */
+    float coat_width;     /* nm                                                                     */
+    float coat_index;     /* 96 bytes                                                               */
 } st_material;
 
 /* A LIGHT'S FACE (builder/lights.js, the builder's light object; core/scene_api.js:259-289 LightFace,

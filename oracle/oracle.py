@@ -59,6 +59,10 @@ def _declare(L):
     L.sto_fresnel_dielectric.restype = C.c_double
     L.sto_lobes.argtypes = [P, P, P, C.c_double, P, P]
     L.sto_lobes_sample.argtypes = [P, P, C.c_double, C.c_uint32, C.c_int, P, P]
+    L.sto_coat_rgb.argtypes = [C.c_double, C.c_double, C.c_double, C.c_double, P]
+    L.sto_coat_at_lambda.argtypes = [C.c_double] * 5
+    L.sto_coat_at_lambda.restype = C.c_double
+    L.sto_lobes_sample_coat.argtypes = [P, P, C.c_double, C.c_double, C.c_int, C.c_double, P, C.c_uint32, C.c_int, P, P]
     L.sto_set_env_image.argtypes = [P, C.c_uint32, C.c_uint32, C.c_float, C.c_float]
     L.sto_env_map_tables.argtypes = [P, P]
     L.sto_env_radiance.argtypes = [P, P, P, C.c_uint32, P]
@@ -205,6 +209,27 @@ def lobes_sample(mat, v, eta, seed, n):
     d = np.zeros((n, 3), np.float64)
     w = np.zeros((n, 3), np.float64)
     lib().sto_lobes_sample(C.byref(mat), ptr(np.asarray(v, np.float64)), eta, seed, n, ptr(d), ptr(w))
+    return d, w
+
+
+def coat_rgb(lo, hi, edge, width):
+    """A coating's reflectance per channel (spectral.js edgeRGB), as the oracle's lobes take it."""
+    out = np.zeros(3, np.float64)
+    lib().sto_coat_rgb(lo, hi, edge, width, ptr(out))
+    return out
+
+
+def coat_at_lambda(lo, hi, edge, width, lam):
+    return lib().sto_coat_at_lambda(lo, hi, edge, width, lam)
+
+
+def lobes_sample_coat(mat, v, eta, n0, inside, lam, beta, seed, n):
+    """n draws of a coated material's lobes at normal +z, view v, seen from medium n0 (inside or not), by a ray of
+    wavelength lam (0 none) carrying beta: directions and weights."""
+    d = np.zeros((n, 3), np.float64)
+    w = np.zeros((n, 3), np.float64)
+    lib().sto_lobes_sample_coat(C.byref(mat), ptr(np.asarray(v, np.float64)), eta, n0, int(inside), lam,
+                                ptr(np.asarray(beta, np.float64)), seed, n, ptr(d), ptr(w))
     return d, w
 
 

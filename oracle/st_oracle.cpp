@@ -499,7 +499,7 @@ inline void shade_hit(const Ctx<T>& C, Ray<T>& r, T dhit, Rng& rng, Rng& grng, b
     if (C.sppm && ((r.bounces == 0 && !C.lt) || r.lens == 1) && !(max3(emis) > T(0)) && sppm_evaluable(m, true)) {
         T n0g = r.n;
         Lobes<T> lg = make_lobes(nrm, -r.dir, m, n0g / std::max(T(m.ior), n0g), C.tb, T(m.transmission), T(m.specular),
-                                 T(m.haze));
+                                 T(m.haze), n0g, false, r.lam);
         V3<T> L = sppm_gather_lobes(C, r.pos, nrm, lg, r.bounces + 1, grng) * T(C.sp_inv_area / ((double)n0g * n0g));
         r.rad += r.beta * L;
     }
@@ -568,8 +568,9 @@ inline void shade_hit(const Ctx<T>& C, Ray<T>& r, T dhit, Rng& rng, Rng& grng, b
         }
     }
     T etaFace = diffFace ? std::min(n0, n1) / std::max(n0, n1) : n0 / n1;
-    Lobes<T> lb = make_lobes(nrm, -r.dir, m, etaFace, C.tb, trans, specv, hz);
+    Lobes<T> lb = make_lobes(nrm, -r.dir, m, etaFace, C.tb, trans, specv, hz, n0, inside, lam0);
     lb.etaT = n0 / nT;
+    coat_pick(lb, r.beta);
     // THE SIDE BEYOND, LIT (materials_pbr.js:1176-1190): through this face where the medium beyond is air
     const bool throughLit = std::fabs(n1 - T(1)) <= T(1e-3) && through_evaluable<T>(m, trans, hz);
     lb.through = throughLit;
@@ -736,8 +737,9 @@ inline void shade_photon(const Ctx<T>& C, Ray<T>& r, T dhit, Rng& rng) {
         }
     }
     T etaFace = diffFace ? std::min(n0, n1) / std::max(n0, n1) : n0 / n1;
-    Lobes<T> lb = make_lobes(nrm, -r.dir, m, etaFace, C.tb, trans, specv, hz);
+    Lobes<T> lb = make_lobes(nrm, -r.dir, m, etaFace, C.tb, trans, specv, hz, n0, inside, T(0));
     lb.etaT = n0 / n1;
+    coat_pick(lb, r.beta);
     T ur[4]; rng.next4(ur);
     LobeSample<T> smp = lobes_sample(lb, ur);
     r.dir = smp.dir;
@@ -1091,7 +1093,7 @@ void lt_splat(const Ctx<T>& C, const V3<T>& P, const V3<T>& org, const V3<T>& di
               uint32_t cell, Stats& st);
 template <class T>
 void lt_connect(const Ctx<T>& C, const st_material& m, const V3<T>& P, const V3<T>& nrm, const V3<T>& din,
-                const V3<T>& phi, U4 ps, uint32_t id, uint32_t cell, Stats& st) {
+                const V3<T>& phi, T lam, U4 ps, uint32_t id, uint32_t cell, Stats& st) {
     const st_view& vw = *C.view;
     const V3<T> right(T(vw.right[0]), T(vw.right[1]), T(vw.right[2])), up(T(vw.up[0]), T(vw.up[1]), T(vw.up[2]));
     const V3<T> fwd(T(vw.fwd[0]), T(vw.fwd[1]), T(vw.fwd[2])), cam0(T(vw.cam_pos[0]), T(vw.cam_pos[1]), T(vw.cam_pos[2]));
@@ -1136,7 +1138,9 @@ void lt_connect(const Ctx<T>& C, const st_material& m, const V3<T>& P, const V3<
     if (std::fabs(xx) >= T(1) || std::fabs(yy) >= T(1)) return;
     const T cv = dot(nrm, v);
     if (cv <= T(0)) return;
-    Lobes<T> lb = make_lobes(nrm, v, m, T(1) / std::max(T(m.ior), T(1)), C.tb, T(m.transmission), T(m.specular), T(m.haze));
+    // (a coating's pick keeps the even weights, the camera's first vertex's: its beta is white)
+    Lobes<T> lb = make_lobes(nrm, v, m, T(1) / std::max(T(m.ior), T(1)), C.tb, T(m.transmission), T(m.specular), T(m.haze),
+                             T(1), false, lam);
     const V3<T> f = lobes_eval(lb, -din, T(0.05));
     const V3<T> c = phi * f * (G / apx);
     if (!(luma(c) > T(0))) return;
@@ -1396,7 +1400,7 @@ void photon_walk(const Ctx<T>& C, U4 ps, uint32_t id, Ray<T>& r, uint32_t it, ui
         if (std::max(std::max(m.emissive[0], m.emissive[1]), m.emissive[2]) > 0.f) break;
         // light tracing: connected first, once it has passed a delta event, in air, within the bounce cap
         if (C.lt && r.passed && std::fabs(r.n - T(1)) <= T(1e-3) && r.bounces + 1 <= C.p.maxbounce)
-            lt_connect(C, m, r.pos, nrm, r.dir, r.rad * r.beta, ps, id, cell, st);
+            lt_connect(C, m, r.pos, nrm, r.dir, r.rad * r.beta, r.lam, ps, id, cell, st);
         if (r.passed && sppm_evaluable(m, false)) {
             V3<T> pw = r.rad * r.beta;
             if (C.sppm && r.bounces + 2 <= C.p.maxbounce && luma(pw) > T(0)) {       // sppm.js sppmStores / sppmStore
@@ -1454,8 +1458,9 @@ void photon_walk(const Ctx<T>& C, U4 ps, uint32_t id, Ray<T>& r, uint32_t it, ui
             }
         }
         T etaFace = diffFace ? std::min(n0, n1) / std::max(n0, n1) : n0 / n1;
-        Lobes<T> lb = make_lobes(nrm, -r.dir, m, etaFace, C.tb, trans, specv, hz);
+        Lobes<T> lb = make_lobes(nrm, -r.dir, m, etaFace, C.tb, trans, specv, hz, n0, inside, lam0);
         lb.etaT = n0 / nT;
+        coat_pick(lb, r.beta);
         T ur[4]; rng.next4(ur);
         LobeSample<T> smp = lobes_sample(lb, ur);
         r.dir = smp.dir;
@@ -1790,6 +1795,28 @@ void sto_lobes(const st_material* m, const double* v, const double* l, double et
     V3<double> fv = lobes_eval(lb, V3<double>(l[0], l[1], l[2]), 0.0);
     f[0] = fv.x; f[1] = fv.y; f[2] = fv.z;
     *pdf = lobes_pdf(lb, V3<double>(l[0], l[1], l[2]));
+}
+
+// a coating's reflectance per channel (spectral.js edgeRGB) and at one wavelength (edgeAt1), for the tests
+void sto_coat_rgb(double lo, double hi, double edge, double width, double* out) { coat_edge_rgb(lo, hi, edge, width, out); }
+double sto_coat_at_lambda(double lo, double hi, double edge, double width, double lam) {
+    return coat_edge_at_lambda(lo, hi, edge, width, lam);
+}
+// n draws of lobesSample for a coated material at normal (0,0,1), view v, seen from medium n0 (inside or not), a ray of
+// wavelength lam (0 none) carrying beta (coatPick): directions (3n) and weights (3n)
+void sto_lobes_sample_coat(const st_material* m, const double* v, double eta, double n0, int inside, double lam,
+                           const double* beta, uint32_t seed, int n, double* dirs, double* w) {
+    const MfTables* tb = tables<double>();
+    Lobes<double> lb = make_lobes(V3<double>(0, 0, 1), V3<double>(v[0], v[1], v[2]), *m, eta, tb, -1.0, -1.0, -1.0, n0,
+                                  inside != 0, lam);
+    coat_pick(lb, V3<double>(beta[0], beta[1], beta[2]));
+    Rng r; r.h = sample_seed(seed, 0);
+    for (int i = 0; i < n; i++) {
+        double u[4]; r.next4(u);
+        LobeSample<double> s = lobes_sample(lb, u);
+        dirs[3 * i] = s.dir.x; dirs[3 * i + 1] = s.dir.y; dirs[3 * i + 2] = s.dir.z;
+        w[3 * i] = s.w.x; w[3 * i + 1] = s.w.y; w[3 * i + 2] = s.w.z;
+    }
 }
 
 // n draws of lobesSample for a material at normal (0,0,1), view v: directions (3n) and weights (3n)

@@ -3,6 +3,7 @@
 // by file:line; the product never includes or links this.
 #pragma once
 #include "st_oracle_core.h"
+#include "st_oracle_spectral.h"
 #include "../include/shadytracer.h"
 
 namespace sto {
@@ -70,9 +71,8 @@ inline void env_tables(const std::vector<double>& lum, std::vector<float>& tex) 
 // each band's middle (weighted by x + y + z), its Rayleigh depth there (Hansen & Travis 1974 eq. 2.29), Angstrom's
 // aerosol factor (l / 550)^-1.3 and the ozone's depth (the Chappuis band's 223 K cross-section, 300 Dobson units)
 struct SkyBand { double tauR, haze, ozone, nm, rgb[3]; };
-inline const std::vector<SkyBand>& sky_bands() {
-    static std::vector<SkyBand> bands;
-    if (!bands.empty()) return bands;
+inline std::vector<SkyBand> sky_bands_build() {
+    std::vector<SkyBand> bands;
     static const double sigma[16] = {6.2648e-24, 3.1169e-23, 1.0195e-22, 2.4886e-22, 5.4883e-22, 1.1517e-21, 2.0211e-21,
                                      3.0497e-21, 4.2480e-21, 4.5252e-21, 4.7153e-21, 3.4726e-21, 2.3885e-21, 1.5936e-21,
                                      9.8370e-22, 6.3061e-22};
@@ -109,6 +109,12 @@ inline const std::vector<SkyBand>& sky_bands() {
     const double Yt = LUMA_R * tot[0] + LUMA_G * tot[1] + LUMA_B * tot[2];
     for (auto& b : bands)
         for (int c = 0; c < 3; c++) b.rgb[c] /= Yt;
+    return bands;
+}
+// built once, by whichever thread asks first (a function-local static is initialised exactly once, under a lock: the
+// presets' texture asks from many threads at once)
+inline const std::vector<SkyBand>& sky_bands() {
+    static const std::vector<SkyBand> bands = sky_bands_build();
     return bands;
 }
 // Kasten-Young relative air mass (sdf.js:96-100)
@@ -756,26 +762,62 @@ template <class T> inline T mf_e1(const MfTables& tb, T mu, T r) {
 // ------------------------------------------------------------------------------------------------------------
 const uint32_t EV_NONE = 0, EV_DELTA = 1, EV_EVAL = 2, EV_OTHER = 3;
 const double LT_MIN_ALPHA = 0.05;
+// a coating over a metal (materials_pbr.js:114-136 metalFresnel, coatOverMetal): the stack's R and the metal's F as
+// intensities, R + (1 - R)^2 F (1 + R F + (R F)^2 + ...) = 1 - (1 - R)(1 - F) / (1 - R F), F held to [0, 1]
+template <class T> inline V3<T> coat_over_metal(const V3<T>& r, const V3<T>& f) {
+    const V3<T> fc(sat(f.x), sat(f.y), sat(f.z));
+    const V3<T> one(1);
+    const V3<T> den = vmax(one - r * fc, T(1e-6));
+    return one - (one - r) * (one - fc) / den;
+}
 template <class T> struct Lobes {
     V3<T> tX, tY, nZ, o, base, transTint, coatK, cm, ecO, ecAvg;
+    V3<T> coatR{T(0)};                      // a coating's reflectance per channel at the view (0: anti-reflective)
+    V3<T> pw{T(1) / T(3)};                  // the channels' weights in a coated reflect-or-pass pick (coatPick)
     T ax, ay;                               // the alphas along tX and tY (tX the rough axis)
     T aMin, r, metallic, trans, transl, eta, etaT, nrel, ps;
     bool isDelta;
+    bool coated = false;                    // a coating is the interface: coatR, not coatK x the Fresnel
     bool through = false;                   // the side beyond lit: the lobes below the surface evaluated
     const MfTables* tb;
     A2<T> al() const { return A2<T>{ax, ay}; }
     V3<T> to_local(const V3<T>& w) const { return V3<T>(dot(w, tX), dot(w, tY), dot(w, nZ)); }
     V3<T> to_world(const V3<T>& w) const { return normalize(tX * w.x + tY * w.y + nZ * w.z); }
-    V3<T> coat_fresnel(T cosI) const { return vmin(coatK * fresnel_dielectric(cosI, eta), T(1)); }
-    V3<T> metal_fresnel(T cosI) const { return fresnel_schlick3(cosI, base); }
-    V3<T> coat_albedo(const V3<T>& w) const { return vmin(coatK * mf_ec(*tb, w.z, r, nrel), T(1)); }
+    // materials_pbr.js:106-113 coatFresnel: a coating's R at every facet, total past the critical angle
+    V3<T> coat_fresnel(T cosI) const {
+        const T f = fresnel_dielectric(cosI, eta);
+        if (coated) return f >= T(1) ? V3<T>(1) : coatR;
+        return vmin(coatK * f, T(1));
+    }
+    V3<T> metal_fresnel(T cosI) const {
+        const V3<T> f = fresnel_schlick3(cosI, base);
+        return coated ? coat_over_metal(coatR, f) : f;
+    }
+    // materials_pbr.js:137-142 reflectPick: the largest channel, or under a coating the channels weighed by the ray
+    T reflect_pick(const V3<T>& c) const { return coated ? dot(c, pw) : max3(c); }
+    V3<T> coat_albedo(const V3<T>& w) const {
+        if (coated) return coatR;           // materials_pbr.js:151-153: the coating's at the view, at every angle
+        return vmin(coatK * mf_ec(*tb, w.z, r, nrel), T(1));
+    }
+    // coatPs (materials_pbr.js:274-279)
+    T coat_ps() const {
+        return std::min(reflect_pick(coat_fresnel(o.z)), fresnel_dielectric(o.z, eta) >= T(1) ? T(1) : T(0.999));
+    }
 };
+// coatPick (materials_pbr.js:280-291): a coated lobe's pick weighed by the shares of |beta| the ray carries
+template <class T> inline void coat_pick(Lobes<T>& lb, const V3<T>& beta) {
+    if (!lb.coated) return;
+    const V3<T> a(std::fabs(beta.x), std::fabs(beta.y), std::fabs(beta.z));
+    const T t = a.x + a.y + a.z;
+    lb.pw = t > T(0) ? a * (T(1) / t) : V3<T>(T(1) / T(3));
+    lb.ps = lb.coat_ps();
+}
 // refractShare (materials.js:123): T (1 - H)
 template <class T> inline T refract_share_of(T transmission, T haze) { return sat(transmission) * (T(1) - sat(haze)); }
 template <class T> inline T refract_share(const st_material& m) { return refract_share_of(T(m.transmission), T(m.haze)); }
 template <class T> inline Lobes<T> make_lobes(const V3<T>& n, const V3<T>& v, const st_material& m, T eta,
                                               const MfTables* tb, T transmission_override = T(-1), T specular_override = T(-1),
-                                              T haze_override = T(-1)) {
+                                              T haze_override = T(-1), T n0 = T(1), bool inside = false, T lam = T(0)) {
     Lobes<T> lb;
     lb.tb = tb;
     // mtlOrthonormalBasis (materials_pbr.js:13-19)
@@ -807,14 +849,36 @@ template <class T> inline Lobes<T> make_lobes(const V3<T>& n, const V3<T>& v, co
     lb.coatK = tintMix * mixT(T(2) * spec, T(1), lb.trans);
     lb.eta = eta; lb.etaT = eta;
     lb.nrel = clampT(T(1) / eta, T(1), T(3));
-    // coatPs (materials_pbr.js:275-279)
-    T fo = max3(lb.coat_fresnel(lb.o.z));
-    lb.ps = std::min(fo, fresnel_dielectric(lb.o.z, lb.eta) >= T(1) ? T(1) : T(0.999));
+    // A COATING (materials_pbr.js:220-245): the interface on the faces light enters by; on the faces it leaves by,
+    // anti-reflective (coat 1), the bare interface (2) or the coating again (3); its R at the view's angle, the edge
+    // moved by the invariant n0 sin(theta0) through the stack's effective index; a ray with a wavelength takes R there
+    const uint32_t coat = std::min(m.coat, 3u);
+    if (coat != 0u) {
+        if (!inside || coat == 3u) {
+            const double sin0 = std::sqrt(std::max(0.0, 1.0 - (double)lb.o.z * (double)lb.o.z));
+            const double lo = std::min(std::max((double)m.coat_lo, 0.0), 1.0);
+            const double hi = std::min(std::max((double)m.coat_hi, 0.0), 1.0);
+            const double w = std::max((double)m.coat_width, 0.0);
+            const double edge = coat_edge_at((double)m.coat_edge, (double)n0 * sin0, std::max((double)m.coat_index, 1.0));
+            if (lam > T(0)) {
+                lb.coatR = V3<T>(T(coat_edge_at_lambda(lo, hi, edge, w, (double)lam)));
+            } else {
+                double c[3];
+                coat_edge_rgb(lo, hi, edge, w, c);
+                lb.coatR = V3<T>(T(c[0]), T(c[1]), T(c[2]));
+            }
+            lb.coated = true;
+        } else if (coat == 1u) {
+            lb.coated = true;
+        }
+    }
+    lb.ps = lb.coat_ps();
     lb.ecO = lb.coat_albedo(lb.o);
     T e1 = lb.metallic > T(0) ? mf_e1(*tb, lb.o.z, lb.r) : T(1);
-    T eAvg = mf_ecavg(*tb, lb.r, lb.nrel);
-    lb.ecAvg = vmin(lb.coatK * eAvg, T(1));
-    lb.cm = V3<T>(1) + lb.base * (T(1) / std::max(e1, T(1e-3)) - T(1));
+    lb.ecAvg = lb.coated ? lb.coatR : vmin(lb.coatK * mf_ecavg(*tb, lb.r, lb.nrel), T(1));
+    // Turquin's factor from F0: the metal's colour, or under a coating what the two reflect head-on
+    const V3<T> f0 = lb.coated ? coat_over_metal(lb.coatR, lb.base) : lb.base;
+    lb.cm = V3<T>(1) + f0 * (T(1) / std::max(e1, T(1e-3)) - T(1));
     return lb;
 }
 template <class T> inline V3<T> lobes_through_eval(const Lobes<T>& lb, const V3<T>& i, T minAlpha);
@@ -839,7 +903,7 @@ template <class T> inline V3<T> lobes_eval(const Lobes<T>& lb, const V3<T>& l, T
     return f;
 }
 template <class T> inline T interface_reflect_p(const Lobes<T>& lb, T oh) {
-    T fh = max3(lb.coat_fresnel(oh));
+    T fh = lb.reflect_pick(lb.coat_fresnel(oh));
     T den = fh + (T(1) - fh) * lb.trans;
     return den > T(1e-6) ? fh / den : T(1);
 }

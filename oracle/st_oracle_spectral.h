@@ -7,6 +7,7 @@
 // The colour-matching functions are the CIE 1931 observer's as fitted by Wyman, Sloan and Shirley (JCGT 2(2), 2013,
 // the multi-lobe piecewise Gaussian), where the reference integrates the tabulated functions (its cie1931.js).
 #pragma once
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
 
@@ -75,6 +76,65 @@ struct SpecTable {
 inline const SpecTable& spec_table() {
     static const SpecTable t;
     return t;
+}
+
+// A COATING (spectral.js:58-117, materials.js:150-163 coatMaterial). Its bins: 40 of 10 nm from 380 nm, per bin and
+// channel the clipped Rec.709 colour-matching function's mean over the bin by the midpoint rule at 0.1 nm (spectral.js
+// SPEC_WEIGHTS), each channel normalised to sum to 1.
+struct CoatBins {
+    double w[40][3];
+    CoatBins() {
+        auto lobe = [](double l, double mu, double lo, double hi) {
+            double t = (l - mu) / (l < mu ? lo : hi);
+            return std::exp(-0.5 * t * t);
+        };
+        double tot[3] = {0, 0, 0};
+        for (int k = 0; k < 40; k++) {
+            double a[3] = {0, 0, 0};
+            for (int j = 0; j < 100; j++) {
+                const double l = 380.0 + (k + (j + 0.5) / 100.0) * 10.0;
+                const double X = 1.056 * lobe(l, 599.8, 37.9, 31.0) + 0.362 * lobe(l, 442.0, 16.0, 26.7) -
+                                 0.065 * lobe(l, 501.1, 20.4, 26.2);
+                const double Y = 0.821 * lobe(l, 568.8, 46.9, 40.5) + 0.286 * lobe(l, 530.9, 16.3, 31.1);
+                const double Z = 1.217 * lobe(l, 437.0, 11.8, 36.0) + 0.681 * lobe(l, 459.0, 26.0, 13.8);
+                const double rgb[3] = {3.2404542 * X - 1.5371385 * Y - 0.4985314 * Z,
+                                       -0.9692660 * X + 1.8760108 * Y + 0.0415560 * Z,
+                                       0.0556434 * X - 0.2040259 * Y + 1.0572252 * Z};
+                for (int c = 0; c < 3; c++) a[c] += (rgb[c] > 0 ? rgb[c] : 0.0) / 100.0;
+            }
+            for (int c = 0; c < 3; c++) { w[k][c] = a[c]; tot[c] += a[c]; }
+        }
+        for (int k = 0; k < 40; k++)
+            for (int c = 0; c < 3; c++) w[k][c] /= tot[c];
+    }
+};
+inline const CoatBins& coat_bins() {
+    static const CoatBins b;
+    return b;
+}
+// the logistic's scale s for a 10-90 % width (nm): width / (2 ln 9), the width at least 0.01 nm
+inline double coat_scale(double width) { return std::max(width, 0.01) / (2.0 * std::log(9.0)); }
+inline double softplus(double x) { return std::max(x, 0.0) + std::log1p(std::exp(-std::fabs(x))); }
+// spectral.js edgeRGB: R(lambda) = lo + (hi - lo) / (1 + exp(-(lambda - edge) / s)) against each channel's bins, a bin's
+// mean of the logistic exactly: s (softplus((b1 - edge) / s) - softplus((b0 - edge) / s)) / 10
+inline void coat_edge_rgb(double lo, double hi, double edge, double width, double out[3]) {
+    const CoatBins& B = coat_bins();
+    const double s = coat_scale(width);
+    double acc[3] = {0, 0, 0};
+    for (int k = 0; k < 40; k++) {
+        const double m = s * (softplus((390.0 + 10.0 * k - edge) / s) - softplus((380.0 + 10.0 * k - edge) / s)) / 10.0;
+        for (int c = 0; c < 3; c++) acc[c] += B.w[k][c] * m;
+    }
+    for (int c = 0; c < 3; c++) out[c] = lo + (hi - lo) * acc[c];
+}
+// spectral.js edgeAt1: R at one wavelength
+inline double coat_edge_at_lambda(double lo, double hi, double edge, double width, double lam) {
+    return lo + (hi - lo) / (1.0 + std::exp(-(lam - edge) / coat_scale(width)));
+}
+// spectral.js edgeAt: the edge for light of invariant n0 sin(theta0) through a stack of effective index nEff
+inline double coat_edge_at(double edge0, double nSin, double nEff) {
+    const double q = nSin / std::max(nEff, 1e-6);
+    return edge0 * std::sqrt(std::max(0.0, 1.0 - q * q));
 }
 // the draw: the first cell whose CDF passes u, the wavelength uniform in it from the same u
 template <class T> inline T spec_draw(T u, V3<T>& w) {

@@ -69,6 +69,7 @@ struct st_ctx {
     st_view view{};
     // the albedo tables
     float *d_ec = nullptr, *d_ecavg = nullptr, *d_e1 = nullptr;
+    float4* d_coat = nullptr;             // a coating's 10 nm bins (st_spectral.h coat_bin_table), COAT_BINS float4s
     float4* d_spec = nullptr;             // the camera's wavelength table (st_spectral.h), SPEC_CELLS float4s
     // the wave
     uint32_t W = 0, H = 0, P = 0, spw = 0, slot_cap = 0;
@@ -515,7 +516,7 @@ static WaveArgs wave_args(st_ctx* ctx, uint32_t w) {
     a.u.count_work = ctx->count_work ? 1u : 0u;
     a.prims = ctx->d_prims;
     a.mats = ctx->d_mats;
-    a.tab = MfTab{ctx->d_ec, ctx->d_ecavg, ctx->d_e1};
+    a.tab = MfTab{ctx->d_ec, ctx->d_ecavg, ctx->d_e1, ctx->d_coat};
     a.spec = ctx->d_spec;
     a.pb = ctx->pb;
     a.q = ctx->q;
@@ -738,7 +739,8 @@ int st_create(int device, st_ctx** out) {
     if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) { delete ctx; return ST_ERR_CUDA; }
     const size_t NEC = 16 * 32 * 32, NAVG = 16 * 32, NE1 = 32 * 32;
     if (cudaMalloc(&ctx->d_ec, NEC * 4) || cudaMalloc(&ctx->d_ecavg, NAVG * 4) || cudaMalloc(&ctx->d_e1, NE1 * 4) ||
-        cudaMalloc(&ctx->d_ctr, sizeof(DevCtr)) || cudaMalloc(&ctx->d_spec, SPEC_CELLS * sizeof(float4))) {
+        cudaMalloc(&ctx->d_ctr, sizeof(DevCtr)) || cudaMalloc(&ctx->d_spec, SPEC_CELLS * sizeof(float4)) ||
+        cudaMalloc(&ctx->d_coat, COAT_BINS * sizeof(float4))) {
         st_destroy(ctx);
         return ST_ERR_OOM;
     }
@@ -748,7 +750,11 @@ int st_create(int device, st_ctx** out) {
         std::vector<float4> f(SPEC_CELLS);
         for (int i = 0; i < SPEC_CELLS; i++)
             f[i] = make_float4((float)t[4 * i], (float)t[4 * i + 1], (float)t[4 * i + 2], (float)t[4 * i + 3]);
-        if (cudaMemcpy(ctx->d_spec, f.data(), SPEC_CELLS * sizeof(float4), cudaMemcpyHostToDevice) != cudaSuccess) {
+        const std::vector<double> c = coat_bin_table();
+        float4 cb[COAT_BINS];
+        for (int k = 0; k < COAT_BINS; k++) cb[k] = make_float4((float)c[3 * k], (float)c[3 * k + 1], (float)c[3 * k + 2], 0.f);
+        if (cudaMemcpy(ctx->d_spec, f.data(), SPEC_CELLS * sizeof(float4), cudaMemcpyHostToDevice) != cudaSuccess ||
+            cudaMemcpy(ctx->d_coat, cb, sizeof(cb), cudaMemcpyHostToDevice) != cudaSuccess) {
             st_destroy(ctx);
             return ST_ERR_CUDA;
         }
@@ -771,7 +777,7 @@ int st_destroy(st_ctx* ctx) {
     if (ctx->has_code) scene_code_free(ctx->code);
     for (void* p : {(void*)ctx->d_prims, (void*)ctx->d_faces, (void*)ctx->d_envimg, (void*)ctx->d_envmap, (void*)ctx->d_skytab, (void*)ctx->d_views, (void*)ctx->d_envtex, (void*)ctx->d_sc,
                     (void*)ctx->d_mats, (void*)ctx->d_ec, (void*)ctx->d_ecavg,
-                    (void*)ctx->d_e1, (void*)ctx->d_ctr, (void*)ctx->d_spec})
+                    (void*)ctx->d_e1, (void*)ctx->d_ctr, (void*)ctx->d_spec, (void*)ctx->d_coat})
         if (p) cudaFree(p);
     for (auto& pe : ctx->pending) { cudaEventDestroy(pe.a); cudaEventDestroy(pe.b); }
     for (auto e : ctx->event_pool) cudaEventDestroy(e);
@@ -1441,4 +1447,4 @@ const st_scene_desc& ctx_desc(st_ctx* ctx) { return ctx->desc; }
 bool ctx_has_scene(st_ctx* ctx) { return ctx->has_scene; }
 uint64_t ctx_scene_gen(st_ctx* ctx) { return ctx->scene_gen; }
 DevCtr* ctx_counters(st_ctx* ctx) { return ctx->d_ctr; }
-MfTab ctx_tab(st_ctx* ctx) { return MfTab{ctx->d_ec, ctx->d_ecavg, ctx->d_e1}; }
+MfTab ctx_tab(st_ctx* ctx) { return MfTab{ctx->d_ec, ctx->d_ecavg, ctx->d_e1, ctx->d_coat}; }

@@ -741,7 +741,11 @@ __device__ __forceinline__ float haze_tr(const Uni& u, f3 A, f3 d, float len) {
 #define MF_NR 32
 #define MF_NIOR 16
 #define MF_ALPHA_MIN 1e-3f
-struct MfTab { const float* __restrict__ ec; const float* __restrict__ ecavg; const float* __restrict__ e1; };
+// the albedo tables, and a coating's 10 nm bins (st_spectral.h coat_bin_table: COAT_BINS rows of r, g, b, 0)
+struct MfTab {
+    const float* __restrict__ ec; const float* __restrict__ ecavg; const float* __restrict__ e1;
+    const float4* __restrict__ coat;
+};
 
 // the two alphas along the local x and y (microfacet.js mfAnisoAlpha); an isotropic lobe's are equal, and then every
 // number below is the one the isotropic formulas give
@@ -852,24 +856,93 @@ __host__ __device__ __forceinline__ float refract_share_of(float transmission, f
     const float t = fminf(fmaxf(transmission, 0.f), 1.f), h = fminf(fmaxf(haze, 0.f), 1.f);
     return t * (1.f - h);
 }
+// ------------------------------------------------------------------------------------------------------------
+// A COATING (materials.js:52-89 Material2.coat, :150-163 coatMaterial; spectral.js:80-117 edgeRGB, edgeAt, edgeAt1):
+// R(lambda) = lo + (hi - lo) / (1 + exp(-(lambda - edge) / s)), s the 10-90 % width over 2 ln 9, its edge moved to
+// shorter wavelengths by the light's invariant n0 sin(theta0) through the stack's effective index. A channel's
+// reflectance is R averaged against that channel's weights in 10 nm bins, each bin's mean of the logistic exact (a
+// softplus difference); a ray with a wavelength of its own takes R at it in every channel.
+// ------------------------------------------------------------------------------------------------------------
+#define COAT_NBINS 40
+#define COAT_W1090 4.39444915467244f     // the 10-90 % width of a logistic in units of its scale: 2 ln 9
+#define COAT_WIDTH_MIN 0.01f             // nm: a width of 0 asks for a step, and this is one to well under a bin
+__device__ __forceinline__ float coat_softplus(float x) { return fmaxf(x, 0.f) + log1pf(expf(-fabsf(x))); }
+__device__ __forceinline__ float coat_scale(float width) { return fmaxf(width, COAT_WIDTH_MIN) / COAT_W1090; }
+__device__ __forceinline__ f3 coat_edge_rgb(const float4* __restrict__ bins, float lo, float hi, float edge, float width) {
+    const float s = coat_scale(width);
+    f3 acc = mk(0.f);
+    float prev = coat_softplus((380.f - edge) / s);
+    for (int k = 0; k < COAT_NBINS; k++) {
+        const float next = coat_softplus((380.f + 10.f * (float)(k + 1) - edge) / s);
+        const float4 w = __ldg(&bins[k]);
+        acc = acc + mk(w.x, w.y, w.z) * (next - prev);
+        prev = next;
+    }
+    return mk(lo) + acc * ((hi - lo) * (s / 10.f));
+}
+__device__ __forceinline__ float coat_edge_at_lambda(float lo, float hi, float edge, float width, float lam) {
+    return lo + (hi - lo) / (1.f + expf(-(lam - edge) / coat_scale(width)));
+}
+__device__ __forceinline__ float coat_edge_at(float edge0, float nSin, float nEff) {
+    const float q = nSin / fmaxf(nEff, 1e-6f);
+    return edge0 * sqrtf(fmaxf(0.f, 1.f - q * q));
+}
+// a coating over a metal (materials_pbr.js:114-136 metalFresnel, coatOverMetal): the stack's R and the metal's F summed
+// as intensities, 1 - (1 - R)(1 - F) / (1 - R F), F held to [0, 1] first
+__device__ __forceinline__ f3 coat_over_metal(f3 r, f3 f) {
+    const f3 fc = mk(sat(f.x), sat(f.y), sat(f.z));
+    return mk(1.f) - (mk(1.f) - r) * (mk(1.f) - fc) / vmax(mk(1.f) - r * fc, 1e-6f);
+}
+
 struct Lobes {
     f3 tX, tY, nZ, o, base, transTint, coatK, cm, ecO, ecAvg;
+    f3 coatR;          // a coating's reflectance per channel at the view's angle (0 on an anti-reflective face)
+    f3 pw;             // ...and the channels' weights in a reflect-or-pass pick: the ray's own shares (coat_pick)
     float ax, ay;      // the alphas along tX and tY (tX the rough axis of an anisotropic lobe)
     float aMin, r, metallic, trans, transl, eta, etaT, nrel, ps;
     bool isDelta;
+    bool coated;       // a coating is the interface here: coatR, not coatK x the Fresnel (materials_pbr.js:106-112)
     bool through;      // THE SIDE BEYOND lit (materials_pbr.js:1176-1190): the lobes below the surface evaluated
     __device__ __forceinline__ float2 al() const { return make_float2(ax, ay); }
     __device__ __forceinline__ f3 to_local(f3 w) const { return mk(dot(w, tX), dot(w, tY), dot(w, nZ)); }
     __device__ __forceinline__ f3 to_world(f3 w) const { return normalize(tX * w.x + tY * w.y + nZ * w.z); }
-    __device__ __forceinline__ f3 coat_fresnel(float cosI) const { return vmin(coatK * fresnel_dielectric(cosI, eta), 1.f); }
-    __device__ __forceinline__ f3 metal_fresnel(float cosI) const { return fresnel_schlick3(cosI, base); }
+    // the interface's reflectance at cosI: a coating's at the view's angle for every facet, total past the critical
+    // angle, which no coating changes (materials_pbr.js:109-113 coatFresnel)
+    __device__ __forceinline__ f3 coat_fresnel(float cosI) const {
+        const float f = fresnel_dielectric(cosI, eta);
+        if (coated) return f >= 1.f ? mk(1.f) : coatR;
+        return vmin(coatK * f, 1.f);
+    }
+    __device__ __forceinline__ f3 metal_fresnel(float cosI) const {
+        const f3 f = fresnel_schlick3(cosI, base);
+        return coated ? coat_over_metal(coatR, f) : f;
+    }
+    // how likely a pick is to reflect, of a reflectance per channel (materials_pbr.js:137-142 reflectPick): the largest
+    // channel uncoated, the channels weighed by what the ray carries under a coating
+    __device__ __forceinline__ float reflect_pick(f3 c) const { return coated ? dot(c, pw) : max3(c); }
 };
 __device__ __forceinline__ f3 coat_albedo(const Lobes& lb, const MfTab& t, f3 w) {
+    if (lb.coated) return lb.coatR;                 // the coating's at the view, at every angle (materials_pbr.js:151-153)
     return vmin(lb.coatK * mf_ec(t, w.z, lb.r, lb.nrel), 1.f);
 }
+// the coat's pick probability at the view (materials_pbr.js:274-279 coatPs)
+__device__ __forceinline__ float coat_ps(const Lobes& lb) {
+    return fminf(lb.reflect_pick(lb.coat_fresnel(lb.o.z)), fresnel_dielectric(lb.o.z, lb.eta) >= 1.f ? 1.f : 0.999f);
+}
+// A COATING'S PICK WEIGHED BY THE RAY (materials_pbr.js:280-291 coatPick): the channels' shares of |beta|, or alike for a
+// ray carrying nothing; only where a ray scatters, so every density its MIS reads is this lobe's own
+__device__ __forceinline__ void coat_pick(Lobes& lb, f3 beta) {
+    if (!lb.coated) return;
+    const f3 a = mk(fabsf(beta.x), fabsf(beta.y), fabsf(beta.z));
+    const float t = a.x + a.y + a.z;
+    lb.pw = t > 0.f ? a * (1.f / t) : mk(1.f / 3.f);
+    lb.ps = coat_ps(lb);
+}
 // transm, spec and hz: the material's transmission, specular and haze, or the part of the face drawn from inside
+// n0 the index of the medium the view is in, inside whether it is seen from within (the normal turned), lam the
+// ray's own wavelength (0 none): a coating reads all three (materials_pbr.js:164 makeLobes)
 __device__ __forceinline__ Lobes make_lobes(f3 n, f3 v, const st_material& m, float eta, const MfTab& t,
-                                            float transm, float spec, float hz) {
+                                            float transm, float spec, float hz, float n0, bool inside, float lam) {
     Lobes lb;
     lb.through = false;
     f3 s = fabsf(n.z) < 0.999f ? normalize(cross(n, mk(0, 0, 1))) : normalize(cross(n, mk(0, 1, 0)));
@@ -899,13 +972,36 @@ __device__ __forceinline__ Lobes make_lobes(f3 n, f3 v, const st_material& m, fl
     lb.coatK = tintMix * mixf(2.f * spec, 1.f, lb.trans);
     lb.eta = eta; lb.etaT = eta;
     lb.nrel = clampf(1.f / eta, 1.f, 3.f);
-    float fo = max3(lb.coat_fresnel(lb.o.z));
-    lb.ps = fminf(fo, fresnel_dielectric(lb.o.z, lb.eta) >= 1.f ? 1.f : 0.999f);
+    // A COATING (materials_pbr.js:220-245) is the interface on every face the light enters by; on a face it leaves by,
+    // as the material says: anti-reflective (coat 1: nothing reflects but total internal reflection), the bare
+    // interface (2), or the coating again (3). Evaluated once, at the view: a smooth coating's angle exactly.
+    lb.coated = false;
+    lb.coatR = mk(0.f);
+    lb.pw = mk(1.f / 3.f);
+    const uint32_t coat = min(m.coat, 3u);
+    if (coat != 0u) {
+        if (!inside || coat == 3u) {
+            const float sin0 = sqrtf(fmaxf(0.f, 1.f - lb.o.z * lb.o.z));
+            const float lo = sat(m.coat_lo), hi = sat(m.coat_hi), w = fmaxf(m.coat_width, 0.f);
+            const float edge = coat_edge_at(m.coat_edge, n0 * sin0, fmaxf(m.coat_index, 1.f));
+            lb.coatR = lam > 0.f ? mk(coat_edge_at_lambda(lo, hi, edge, w, lam)) : coat_edge_rgb(t.coat, lo, hi, edge, w);
+            lb.coated = true;
+        } else if (coat == 1u) {
+            lb.coated = true;
+        }
+    }
+    lb.ps = coat_ps(lb);
     lb.ecO = coat_albedo(lb, t, lb.o);
     float e1 = lb.metallic > 0.f ? mf_e1(t, lb.o.z, lb.r) : 1.f;
-    float eAvg = mf_ecavg(t, lb.r, lb.nrel);
-    lb.ecAvg = vmin(lb.coatK * eAvg, 1.f);
-    lb.cm = mk(1.f) + lb.base * (1.f / fmaxf(e1, 1e-3f) - 1.f);
+    if (lb.coated) {
+        lb.ecAvg = lb.coatR;
+    } else {
+        float eAvg = mf_ecavg(t, lb.r, lb.nrel);
+        lb.ecAvg = vmin(lb.coatK * eAvg, 1.f);
+    }
+    // Turquin's factor from F0: the metal's colour, or under a coating what the two reflect head-on
+    const f3 f0 = lb.coated ? coat_over_metal(lb.coatR, lb.base) : lb.base;
+    lb.cm = mk(1.f) + f0 * (1.f / fmaxf(e1, 1e-3f) - 1.f);
     return lb;
 }
 __device__ __forceinline__ f3 lobes_through_eval(const Lobes& lb, const MfTab& t, f3 i, float minAlpha);
@@ -930,7 +1026,7 @@ __device__ __forceinline__ f3 lobes_eval(const Lobes& lb, const MfTab& t, f3 l, 
     return f;
 }
 __device__ __forceinline__ float interface_reflect_p(const Lobes& lb, float oh) {
-    float fh = max3(lb.coat_fresnel(oh));
+    float fh = lb.reflect_pick(lb.coat_fresnel(oh));
     float den = fh + (1.f - fh) * lb.trans;
     return den > 1e-6f ? fh / den : 1.f;
 }

@@ -43,7 +43,7 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[ST_NOALLOC_SCRA
 namespace {
 struct Layout {
     size_t pos, dir, beta, rad, meta, ray0, ray1, hit, hitd, hsurf, so[2], sd[2], sr[2], ss[2], frame, acc, mom, cnt, ctr,
-        ec, ecavg, e1, spec, lam, prims, mats, end;
+        ec, ecavg, e1, spec, coat, lam, prims, mats, end;
 };
 // the array carved for P paths a wave (one sample), each buffer 256-byte aligned: first what does not depend on the
 // picture's size (the albedo tables, built once, the scene's tables, the counters), then the wave's buffers
@@ -53,6 +53,7 @@ Layout layout(size_t P) {
     auto take = [&](size_t bytes) { size_t at = o; o += (bytes + 255) & ~size_t(255); return at; };
     L.ec = take(16 * 32 * 32 * 4); L.ecavg = take(16 * 32 * 4); L.e1 = take(32 * 32 * 4);
     L.spec = take(SPEC_CELLS * sizeof(float4));
+    L.coat = take(COAT_BINS * sizeof(float4));
     L.prims = take(ST_MAX_PRIMS * sizeof(DPrim)); L.mats = take(ST_MAX_MATERIALS * sizeof(st_material));
     L.ctr = take(sizeof(DevCtr));
     const size_t SS = 2 * P;                                   // a shadow side: new rays and continuations
@@ -156,7 +157,13 @@ extern "C" int st_render_noalloc(int device, const st_scene_desc* desc, const st
             float4 f[SPEC_CELLS];
             for (int i = 0; i < SPEC_CELLS; i++)
                 f[i] = make_float4((float)t[4 * i], (float)t[4 * i + 1], (float)t[4 * i + 2], (float)t[4 * i + 3]);
-            if (cudaMemcpy(b + L.spec, f, sizeof(f), cudaMemcpyHostToDevice) != cudaSuccess) return ST_ERR_CUDA;
+            const std::vector<double> c = coat_bin_table();                 // a coating's 10 nm bins
+            float4 cb[COAT_BINS];
+            for (int k = 0; k < COAT_BINS; k++)
+                cb[k] = make_float4((float)c[3 * k], (float)c[3 * k + 1], (float)c[3 * k + 2], 0.f);
+            if (cudaMemcpy(b + L.spec, f, sizeof(f), cudaMemcpyHostToDevice) != cudaSuccess ||
+                cudaMemcpy(b + L.coat, cb, sizeof(cb), cudaMemcpyHostToDevice) != cudaSuccess)
+                return ST_ERR_CUDA;
             g_base[device] = b;
         }
         base = g_base[device];
@@ -179,7 +186,8 @@ extern "C" int st_render_noalloc(int device, const st_scene_desc* desc, const st
     a.u = make_uni_base(*desc, *p, *v, desc->n_prims, desc->n_materials, false);
     a.prims = reinterpret_cast<const DPrim*>(base + L.prims);
     a.mats = reinterpret_cast<const st_material*>(base + L.mats);
-    a.tab = MfTab{(const float*)(base + L.ec), (const float*)(base + L.ecavg), (const float*)(base + L.e1)};
+    a.tab = MfTab{(const float*)(base + L.ec), (const float*)(base + L.ecavg), (const float*)(base + L.e1),
+                  (const float4*)(base + L.coat)};
     a.spec = (const float4*)(base + L.spec);
     a.pb = PathBuf{(float4*)(base + L.pos), (float4*)(base + L.dir), (float4*)(base + L.beta), (float4*)(base + L.rad),
                    (uint4*)(base + L.meta)};

@@ -395,8 +395,9 @@ __global__ void __launch_bounds__(256) k_opt_shade(OptArgs o, int nxt, int last)
                         }
                     }
                     float etaFace = diffFace ? fminf(n0, n1) / fmaxf(n0, n1) : n0 / n1;
-                    Lobes lb = make_lobes(nrm, -dir, m, etaFace, a.tab, trans, specv, hz);
+                    Lobes lb = make_lobes(nrm, -dir, m, etaFace, a.tab, trans, specv, hz, n0, inside, 0.f);
                     lb.etaT = n0 / n1;
+                    coat_pick(lb, beta);
                     LobeSample smp = lobes_sample(lb, a.tab, rng.next());
                     dir = smp.dir;
                     beta = beta * smp.w;

@@ -275,15 +275,17 @@ __device__ __forceinline__ void lt_haze(const Uni& u, f3 P, float h, LtConn& out
 // camera's line of sight to P, as far along it as lifts it 2 offsets off the surface (at grazing views at most 4 such
 // lengths, the rest along the normal, re-aimed at the camera), and stops that height short of the camera
 __device__ __forceinline__ bool lt_connect(const Uni& u, const st_material& m, const MfTab& tab, f3 P, f3 nrm, f3 din,
-                                           f3 phi, const uint4& ps, uint32_t id, LtConn& out) {
+                                           f3 phi, float lam, const uint4& ps, uint32_t id, LtConn& out) {
     LtView w;
     if (!lt_view(u, P, ps, id, w)) return false;
     if (lobes_none(m, m.transmission, m.haze)) return false;
     const f3 v = w.v;
     const float cv = dot(nrm, v);
     if (cv <= 0.f) return false;                                      // the camera on the surface's other side
-    // the camera's own lobes at this vertex, seen along v, in air (the interface air to the material's index)
-    const Lobes lb = make_lobes(nrm, v, m, 1.f / fmaxf(m.ior, 1.f), tab, m.transmission, m.specular, m.haze);
+    // the camera's own lobes at this vertex, seen along v, in air (the interface air to the material's index); a
+    // coating's pick keeps the even weights, the camera's first vertex's (its beta is white)
+    const Lobes lb = make_lobes(nrm, v, m, 1.f / fmaxf(m.ior, 1.f), tab, m.transmission, m.specular, m.haze, 1.f, false,
+                                lam);
     const f3 f = lobes_eval(lb, tab, -din, LT_MIN_ALPHA);
     out.c = phi * f * (cv * w.gm / lt_apx(u));
     if (!(luma(out.c) > 0.f)) return false;
@@ -424,7 +426,7 @@ __global__ void __launch_bounds__(256) k_photon_shade(WaveArgs a, int nxt, int l
                     const bool emissive = fmaxf(fmaxf(m.emissive[0], m.emissive[1]), m.emissive[2]) > 0.f;
                     const bool passed = (m4.y & META_PASSED) != 0u;
                     if (u.lt_on && !emissive && passed && fabsf(n - 1.f) <= 1e-3f && bounces + 1u <= u.maxbounce) {
-                        conn = lt_connect(u, m, a.tab, pos, nrm, dir, rad * beta, ps, m4.x, lc);
+                        conn = lt_connect(u, m, a.tab, pos, nrm, dir, rad * beta, a.pb.lam[slot], ps, m4.x, lc);
                         // teach the emission map: this cell's photon reached the camera (ltConnect's learn)
                         if (conn && u.sppm_learn && cell < LT_CELLS) atomicAdd(&a.sp.lt_hit[cell], 1u);
                     }
@@ -471,8 +473,9 @@ __global__ void __launch_bounds__(256) k_photon_shade(WaveArgs a, int nxt, int l
                             }
                         }
                         const float etaFace = diffFace ? fminf(n0, n1) / fmaxf(n0, n1) : n0 / n1;
-                        Lobes lb = make_lobes(nrm, -dir, m, etaFace, a.tab, trans, specv, hz);
+                        Lobes lb = make_lobes(nrm, -dir, m, etaFace, a.tab, trans, specv, hz, n0, inside, lam0);
                         lb.etaT = n0 / nT;
+                        coat_pick(lb, beta);
                         const LobeSample smp = lobes_sample(lb, a.tab, rng.next());
                         dir = smp.dir;
                         beta = beta * smp.w;
@@ -646,7 +649,7 @@ __global__ void __launch_bounds__(256, 2) k_gather(WaveArgs a) {
                     const f3 x = xyz(p4);
                     const float n0 = d4.w;
                     g.lb = make_lobes(nrm, -xyz(d4), m, n0 / fmaxf(m.ior, n0), a.tab, m.transmission, m.specular,
-                                      m.haze);
+                                      m.haze, n0, false, a.pb.lam[slot]);
                     g.x = x;
                     g.nrm = nrm;
                     g.scale = inv_area / (n0 * n0);

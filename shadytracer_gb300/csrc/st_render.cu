@@ -355,8 +355,9 @@ __device__ __forceinline__ void shade_surface(const WaveArgs& a, const st_materi
         else { trans = sat(sat(m.transmission) * sat(m.haze) / fmaxf(1.f - pG, 1e-6f)); hz = 1.f; specv = 0.5f * k; diffFace = true; }
     }
     float etaFace = diffFace ? fminf(n0, n1) / fmaxf(n0, n1) : n0 / n1;
-    Lobes lb = make_lobes(nrm, -dir, m, etaFace, a.tab, trans, specv, hz);
+    Lobes lb = make_lobes(nrm, -dir, m, etaFace, a.tab, trans, specv, hz, n0, inside, lam0);
     lb.etaT = n0 / nT;
+    coat_pick(lb, beta);
     // THE SIDE BEYOND, LIT (materials_pbr.js:1176-1190): light sampling may aim through this face where what it
     // transmits by can be evaluated and the medium beyond is air; the sky's cosine draw then comes from the far side
     const bool throughLit = fabsf(n1 - 1.f) <= 1e-3f && through_evaluable(m, trans, hz);

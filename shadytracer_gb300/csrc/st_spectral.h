@@ -66,4 +66,31 @@ inline std::vector<double> spectral_table() {
     return out;
 }
 
+// A COATING'S BINS (spectral.js SPEC_WEIGHTS, what coat_edge_rgb in st_device.cuh averages a coating's R(lambda)
+// against): COAT_BINS bins of 10 nm from 380 nm, per bin and channel the mean of the clipped Rec.709 colour-matching
+// function over the bin (the midpoint rule at 0.1 nm), each channel normalised to sum to 1 over the bins -- so a
+// constant R is that R in every channel exactly. Returned as COAT_BINS rows of (r, g, b).
+constexpr int COAT_BINS = 40;
+constexpr double COAT_STEP_NM = 10.0;
+inline std::vector<double> coat_bin_table() {
+    constexpr int SUB = 100;
+    std::vector<double> w(3 * COAT_BINS, 0.0);
+    double sum[3] = {0, 0, 0};
+    for (int k = 0; k < COAT_BINS; k++) {
+        for (int j = 0; j < SUB; j++) {
+            const double l = SPEC_LO_NM + (k + (j + 0.5) / SUB) * COAT_STEP_NM;
+            double X, Y, Z;
+            cie_xyz_fit(l, X, Y, Z);
+            const double c[3] = {3.2404542 * X - 1.5371385 * Y - 0.4985314 * Z,
+                                 -0.9692660 * X + 1.8760108 * Y + 0.0415560 * Z,
+                                 0.0556434 * X - 0.2040259 * Y + 1.0572252 * Z};
+            for (int i = 0; i < 3; i++) w[3 * k + i] += std::fmax(c[i], 0.0) / SUB;
+        }
+        for (int i = 0; i < 3; i++) sum[i] += w[3 * k + i];
+    }
+    for (int k = 0; k < COAT_BINS; k++)
+        for (int i = 0; i < 3; i++) w[3 * k + i] /= sum[i];
+    return w;
+}
+
 }  // namespace st

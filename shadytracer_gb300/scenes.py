@@ -119,6 +119,20 @@ def material(base=(0.8, 0.8, 0.8), metallic=0.0, roughness=0.5, specular=0.5, sp
         m.emissive[i] = emissive[i]
     m.metallic, m.roughness, m.specular, m.specular_tint = metallic, roughness, specular, specular_tint
     m.transmission, m.ior, m.abbe, m.attenuation, m.detector = transmission, ior, abbe, attenuation, detector
+    m.coat_edge, m.coat_width, m.coat_index = 550.0, 0.0, 1.8          # read only where coat != 0
+    return m
+
+
+COAT_NONE, COAT_AR_BACK, COAT_BARE_BACK, COAT_EVERY_FACE = 0, 1, 2, 3
+
+
+def coated(m, where=COAT_AR_BACK, lo=0.0, hi=0.0, edge=600.0, width=20.0, index=1.8):
+    """coatMaterial (core/materials.js:150-161): a coating put on material m -- R(lambda) from lo below `edge` (nm) to
+    hi above it, a logistic of 10-90 % width `width` (nm), its edge moving with the angle through the stack's effective
+    index; `where` the faces it is on (COAT_*). lo = hi is a beam splitter (no edge), 0 on every face a perfect AR."""
+    m.coat = min(int(where), 3)
+    m.coat_lo, m.coat_hi = min(max(lo, 0.0), 1.0), min(max(hi, 0.0), 1.0)
+    m.coat_edge, m.coat_width, m.coat_index = edge, max(width, 0.0), max(index, 1.0)
     return m
 
 
@@ -1037,4 +1051,110 @@ def absorbing_box(width=32, height=32, base=(0.5, 0.25, 0.8), attenuation=1.0, s
     v.fx, v.fy, v.camtype = 0.4, 0.4, 1
     s.view = v
     s.info = {"expected": [sky * b ** (1.0 / attenuation) for b in base]}
+    return s
+
+
+# ------------------------------------------------------------------------------------------------------------
+# A coating on a slab (core/materials.js coat; optics/fresnel.js coatedSlabT): the optics trace's collimated beam
+# through a clear coated slab onto a detector floor.
+# ------------------------------------------------------------------------------------------------------------
+def coated_slab(where=COAT_AR_BACK, lo=0.5, hi=0.5, edge=600.0, width=20.0, index=1.8, deg=0.0, ior=1.5,
+                rays=100_000):
+    """A clear smooth slab (n `ior`, white, 0.1 m thick, its middle at z 0.5, 8 m across) coated as `coated` says, over a
+    black detector floor at z 0; a collimated disc of radius 0.3 m at z 1 shining down, tilted `deg` degrees about y.
+    What reaches the floor is what the slab let through: the incoherent series (1 - R)(1 - Ri) / (1 - Ri^2), Ri what
+    each face reflects from within -- 0 with an AR back, the glass's Fresnel bare, R coated (coated_slab_t)."""
+    from .st_types import StOpticsSource
+    glass_m = coated(material(base=(1, 1, 1), roughness=0.0, specular=0.5, transmission=1.0, ior=ior), where, lo, hi,
+                     edge, width, index)
+    det = material(base=(0, 0, 0), specular=0.0, detector=1.0)
+    mats = [air(), glass_m, det]
+    prims = [prim(ST_PRIM_BOX, pos=(0, 0, 0.5), params=(4.0, 4.0, 0.05), material=1),
+             prim(ST_PRIM_BOX, pos=(0, 0, -0.05), params=(8.0, 8.0, 0.05), material=2)]
+    s = Scene(prims, mats, env_radius=20.0, tolerance=1e-5, name="coated-slab")
+    s.params = default_params(width=16, height=16, maxbounce=32)
+    s.view = look_at((0, -3, 2), (0, 0, 0.5), 40.0, 1.0)
+    a = math.radians(deg)
+    src = StOpticsSource()
+    for i, v in enumerate((0.0, 0.0, 1.0)):
+        src.centre[i] = v
+    for i, v in enumerate((math.sin(a), 0.0, -math.cos(a))):
+        src.axis[i] = v
+    for i, v in enumerate((0.0, 1.0, 0.0)):
+        src.tangent[i] = v
+    src.flux, src.shape, src.size_x, src.size_y = 1000.0, 1, 0.3, 0.3
+    src.dist, src.cos_half, src.n_exp, src.emit_n = 0, 1.0, 1.0, 1.0
+    s.info = {"sources": [src], "rays": [rays], "workload": "coated-slab"}
+    return s
+
+
+def coated_slab_t(deg, ior, R, where):
+    """optics/fresnel.js coatedSlabT: the slab's transmission for a coating of reflectance R on the faces light enters
+    by, the leaving faces as `where` says (Ri 0 with an AR back, the glass's unpolarised Fresnel bare, R coated)."""
+    if where == COAT_AR_BACK:
+        Ri = 0.0
+    elif where == COAT_BARE_BACK:
+        c = math.cos(math.radians(deg))
+        s2 = (1.0 / ior) ** 2 * (1.0 - c * c)                          # from outside: the Fresnel of the entry angle
+        ct = math.sqrt(1.0 - s2)
+        rs = ((c - ior * ct) / (c + ior * ct)) ** 2
+        rp = ((ct - ior * c) / (ct + ior * c)) ** 2
+        Ri = 0.5 * (rs + rp)
+    else:
+        Ri = R
+    return (1.0 - R) * (1.0 - Ri) / (1.0 - Ri * Ri)
+
+
+def coat_edge_rgb(lo, hi, edge, width):
+    """spectral.js edgeRGB, restated in numpy: a coating's reflectance per channel -- R(lambda) averaged against each
+    channel's 10 nm bin weights (the clipped Rec.709 colour-matching functions of the Wyman-Sloan-Shirley fit), each
+    bin's mean of the logistic exact (a softplus difference)."""
+    import numpy as np
+    l = 380.0 + (np.arange(4000) + 0.5) * 0.1
+    g = lambda x, mu, s1, s2: np.exp(-0.5 * ((x - mu) / np.where(x < mu, s1, s2)) ** 2)
+    X = 1.056 * g(l, 599.8, 37.9, 31.0) + 0.362 * g(l, 442.0, 16.0, 26.7) - 0.065 * g(l, 501.1, 20.4, 26.2)
+    Y = 0.821 * g(l, 568.8, 46.9, 40.5) + 0.286 * g(l, 530.9, 16.3, 31.1)
+    Z = 1.217 * g(l, 437.0, 11.8, 36.0) + 0.681 * g(l, 459.0, 26.0, 13.8)
+    M = np.array([[3.2404542, -1.5371385, -0.4985314], [-0.9692660, 1.8760108, 0.0415560],
+                  [0.0556434, -0.2040259, 1.0572252]])
+    rgb = np.maximum(M @ np.stack([X, Y, Z]), 0.0)                    # 3 x 4000
+    W = rgb.reshape(3, 40, 100).mean(axis=2)
+    W /= W.sum(axis=1, keepdims=True)
+    s = max(width, 0.01) / (2 * math.log(9))
+    sp = lambda x: np.maximum(x, 0) + np.log1p(np.exp(-np.abs(x)))
+    b = 380.0 + 10.0 * np.arange(41)
+    F = sp((b - edge) / s)
+    mean = s * np.diff(F) / 10.0
+    return lo + (hi - lo) * (W @ mean)
+
+
+def coat_edge_at(edge0, n_sin, n_eff):
+    """spectral.js edgeAt: the edge for light of invariant n0 sin(theta0) through a stack of effective index n_eff."""
+    return edge0 * math.sqrt(max(0.0, 1.0 - (n_sin / max(n_eff, 1e-6)) ** 2))
+
+
+def coated_spheres(width=64, height=48, maxbounce=12, seed=1, furnace=False, where=COAT_EVERY_FACE, abbe=30.0):
+    """Coatings in a render: a dichroic clear glass sphere (R 0 to 1 above 600 nm, 20 nm wide, coated as `where`
+    says), a rough gold-ish metal under a 30 % beam-splitter coating, and a dispersive glass sphere (Abbe `abbe`)
+    with the dichroic on every face -- its rays meet the inner faces with a wavelength of their own -- on a grey floor
+    under the sun and sky. `furnace`: the dichroic glass alone in a uniform environment, where a lossless coating
+    (R + T = 1 in every channel) must read the environment in every channel."""
+    dichroic = coated(glass((1, 1, 1), ior=1.5), where, 0.0, 1.0, 600.0, 20.0, 1.8)
+    if furnace:
+        s = Scene([prim(ST_PRIM_SPHERE, pos=(0.0, 0.0, 1.0), params=(0.3,), material=1)], [air(), dichroic],
+                  env_radius=40.0, name="coated-furnace")
+        s.params = default_params(width=width, height=height, maxbounce=maxbounce, env_uniform=1000.0, sun_hint=0,
+                                  seed=seed)
+        s.view = look_at((0.0, -1.6, 1.0), (0.0, 0.0, 1.0), 40.0, width / height)
+        s.info = {"closed_form": 1000.0}
+        return s
+    gold = coated(metal((0.95, 0.8, 0.5), 0.3), COAT_AR_BACK, 0.3, 0.3, 600.0, 20.0, 1.8)
+    disp = coated(glass((1, 1, 1), ior=1.6, abbe=abbe), COAT_EVERY_FACE, 0.0, 1.0, 560.0, 30.0, 1.8)
+    s = Scene([prim(ST_PRIM_PLANE, material=1), prim(ST_PRIM_SPHERE, pos=(-0.7, 0.0, 0.35), params=(0.35,), material=2),
+               prim(ST_PRIM_SPHERE, pos=(0.0, 0.3, 0.35), params=(0.35,), material=3),
+               prim(ST_PRIM_SPHERE, pos=(0.7, 0.0, 0.35), params=(0.35,), material=4)],
+              [air(), diffuse((0.6, 0.6, 0.6)), dichroic, gold, disp], env_radius=20.0, name="coated-spheres")
+    s.params = default_params(width=width, height=height, maxbounce=maxbounce, sun_elevation=40.0, sun_azimuth=30.0,
+                              sun_illuminance=100000.0, sky_luminance=3000.0, ground_luminance=0.0, seed=seed)
+    s.view = look_at((0.0, -3.0, 1.4), (0.0, 0.0, 0.3), 40.0, width / height)
     return s

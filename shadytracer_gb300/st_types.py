@@ -35,7 +35,9 @@ class StMaterial(C.Structure):
                 ("roughness", C.c_float), ("specular", C.c_float), ("specular_tint", C.c_float),
                 ("transmission", C.c_float), ("ior", C.c_float), ("abbe", C.c_float),
                 ("attenuation", C.c_float), ("detector", C.c_float),
-                ("emissive", C.c_float * 3), ("beam_cos", C.c_float), ("haze", C.c_float), ("anisotropy", C.c_float), ("pad", C.c_float * 2)]
+                ("emissive", C.c_float * 3), ("beam_cos", C.c_float), ("haze", C.c_float), ("anisotropy", C.c_float),
+                ("coat", C.c_uint32), ("coat_lo", C.c_float), ("coat_hi", C.c_float), ("coat_edge", C.c_float),
+                ("coat_width", C.c_float), ("coat_index", C.c_float)]
 
 
 ST_LIGHT_DISC, ST_LIGHT_RECTANGLE = 1, 2
