@@ -425,15 +425,26 @@ def mlp_leg(args, dev):
         s = scenes.sdf_room(width=W, height=H, spp=spp, finish="diffuse", sky_illuminance=10.0, ground_luminance=1.0)
         s.params.guide = guide
         return s
-    rt = create_path_tracer(scene(0), device=dev, code=True)
+    # the reference on seeds of its own: a plain run on the same seeds would share its first samples with it and read
+    # an error too small by the shared part (at 1024 of 8192 samples, a variance 0.875 of its true one against 1.125
+    # for any run on other numbers)
+    ref = scene(0)
+    ref.params.seed = 7919
+    rt = create_path_tracer(ref, device=dev, code=True)
     left = ref_spp
     while left > 0:
         rt.step(min(512, left))
         left -= 512
-    Lref = rt.read_accum()[0] @ luma
+    rgb, V, S, cnt = rt.read_accum()
+    Lref = rgb @ luma
+    ok = (S > 0) & (S < 1)
+    se2 = np.zeros_like(V)
+    se2[ok] = S[ok] * V[ok] / (1 - S[ok])
+    ref_noise = float(np.mean(se2))                 # the reference's own variance, taken out of each run's error
     rt.close()
-    out = {"workload": "room24 diffuse, sun patch only (sky 10 lx), %dx%d, %d samples against a %d-sample plain render"
-                       % (W, H, spp, ref_spp), "metric": "relative RMSE at equal samples", "legs": {}}
+    out = {"workload": "room24 diffuse, sun patch only (sky 10 lx), %dx%d, %d samples against a %d-sample plain render "
+                       "on seeds of its own (its own noise taken out)" % (W, H, spp, ref_spp),
+           "metric": "relative RMSE at equal samples", "legs": {}}
     for guide in (0, 1):
         rt = create_path_tracer(scene(guide), device=dev, code=True)
         stream = torch.cuda.ExternalStream(rt.stream(), device=torch.device("cuda", dev))
@@ -444,7 +455,8 @@ def mlp_leg(args, dev):
         e1.record(stream)
         rt.sync()
         L = rt.read_accum()[0] @ luma
-        leg = {"rmse": float(np.sqrt(np.mean((L - Lref) ** 2)) / Lref.mean()), "ms": e0.elapsed_time(e1)}
+        leg = {"rmse": float(np.sqrt(max(np.mean((L - Lref) ** 2) - ref_noise, 0.0)) / Lref.mean()),
+               "ms": e0.elapsed_time(e1)}
         if guide:
             st = rt.mlp_stats()
             rt.enable_kernel_times(True)

@@ -123,7 +123,15 @@ typedef struct st_material {
     float coat_lo, coat_hi;
     float coat_edge;      /* nm                                                                     */
     float coat_width;     /* nm                                                                     */
-    float coat_index;     /* 96 bytes                                                               */
+    float coat_index;
+    /* SCATTER INSIDE (materials.js:102-111 scatterDistance, scatterAnisotropy; haze.js:574-650 the medium's walk): the
+     * mean free path between scatterings in the material's volume (metres; 0 a clear volume) and the Henyey-Greenstein
+     * asymmetry of each scattering (held to +-0.95). A ray that refracts into the material walks it: free flights
+     * drawn from exp(-d / scatter_distance), each collision turning it by the phase function and weighing 1; the
+     * colour and the loss stay attenuation's, over the whole walk. */
+    float scatter_distance;
+    float scatter_g;
+    float pad[2];         /* 112 bytes                                                              */
 } st_material;
 
 /* A LIGHT'S FACE (builder/lights.js, the builder's light object; core/scene_api.js:259-289 LightFace,

@@ -68,6 +68,7 @@ template <class T> struct Ctx {
     T tol, envR2, stepscale;
     uint32_t budget;
     HazeBox<T> haze;
+    bool scatter_on = false;                // a material that scatters inside: the march walks it (haze.js:574-650)
     // the photon map of the sample being traced (sppm.js): on, its grid, radius, cell, 1 / (pi r^2), the photons'
     // square, the gather's budget
     bool sppm = false;
@@ -169,6 +170,7 @@ template <class T> struct Ray {
     bool passed = false;                    // a photon that has passed a delta event (TAG_PASSED)
     uint32_t cls = 0;                       // light tracing's class (CLS_CAND 1, CLS_SPEC 2): a first vertex drawn
                                             // from an evaluable lobe, then delta events only
+    uint32_t medium = 0;                    // the material whose volume holds the ray, 0 none (tracebasics.js md0-2)
     uint32_t bounces, steps, state, pix;
 };
 
@@ -197,12 +199,48 @@ template <class T> inline void deposit(Frame<T>& f, uint32_t pix, const V3<T>& c
     f.rgb[pix * 3 + 2] += (double)c.z;
 }
 
-// the march (wavefront.js:866-947): to the surface, the sky, lmax or maxiter
-template <class T> inline T march(const Ctx<T>& C, Ray<T>& r, Stats& st, bool use_haze, uint32_t& evals_out) {
+// the march (wavefront.js:866-947): to the surface, the sky, lmax or maxiter. With a walk's seed (wps: the path's
+// sample seed and its tile, or a photon's seed and id), a ray in a material that scatters inside walks it (haze.js:574-650
+// THE MEDIUM'S WALK): a free flight -ln(1 - u) / sigma drawn as its leg starts, from its vertex; at each collision
+// taken back to it, turned by Henyey-Greenstein, its next flight drawn, a march step; what it meets after that takes
+// its whole weight (prevPdf -1, sunmis 1). A collision counts as an evaluation in the chunks an iteration marches.
+const uint32_t SEED_SALT_WALK = 0x57410000u, SEED_SALT_WALK_HIT = 0x57480000u;
+// whether the ray is in a material that scatters inside (the haze's draw is then not its)
+template <class T> inline bool walks(const Ctx<T>& C, const Ray<T>& r) {
+    return C.scatter_on && r.medium != 0 && r.medium < C.s->n_materials && C.s->materials[r.medium].scatter_distance > 0.f;
+}
+template <class T> inline T march(const Ctx<T>& C, Ray<T>& r, Stats& st, bool use_haze, uint32_t& evals_out,
+                                  const U4* wps = nullptr, uint32_t wid = 0) {
     uint64_t steps = 0;
     T dh = T(1e7);
+    T wsig = T(0), wg = T(0);
+    if (wps && C.scatter_on && r.medium != 0 && r.medium < C.s->n_materials) {
+        const st_material& mm = C.s->materials[r.medium];
+        if (mm.scatter_distance > 0.f) {
+            wsig = T(1) / T(mm.scatter_distance);
+            wg = clampT(T(mm.scatter_g), T(-0.95), T(0.95));
+        }
+    }
+    if (wsig > T(0) && r.tmax == T(0)) {                                       // haze.js:598-618 mediumDraw
+        Rng wr = path_rng(*wps, wid, SEED_SALT_WALK + r.steps);
+        T u[4]; wr.next4(u);
+        r.tmax = std::max(std::min(r.absLtot, r.ltot) - std::log(T(1) - u[0]) / wsig * r.n, T(1e-30));
+    }
     for (;;) {
-        if (use_haze && haze_arrived(r.tmax, r.ltot)) {                       // haze.js:280-288 hazeArrived / hazeAt
+        if (wsig > T(0) && r.ltot >= r.tmax) {                                // haze.js:619-650 mediumCollide
+            r.pos = r.pos - r.dir * ((r.ltot - r.tmax) / std::max(r.n, T(1e-4)));
+            r.ltot = r.tmax;
+            Rng wr = path_rng(*wps, wid, SEED_SALT_WALK_HIT + r.steps);
+            T u[4]; wr.next4(u);
+            r.dir = hg_sample(r.dir, wg, u[0], u[1]);
+            r.tmax = std::max(r.ltot - std::log(T(1) - u[2]) / wsig * r.n, T(1e-30));
+            r.steps += 1;
+            steps++;
+            r.sunmis = T(1); r.emw = T(1); r.lpx = T(-1);
+            if (r.steps > C.p.maxiter) { r.state = RAY_MAXITER; break; }
+            continue;
+        }
+        if (use_haze && wsig == T(0) && haze_arrived(r.tmax, r.ltot)) {      // haze.js:280-288 hazeArrived / hazeAt
             r.pos = r.pos - r.dir * ((r.ltot - r.tmax) / std::max(r.n, T(1e-4)));
             r.ltot = r.tmax;
             r.state = RAY_SCATTER;
@@ -536,9 +574,11 @@ inline void shade_hit(const Ctx<T>& C, Ray<T>& r, T dhit, Rng& rng, Rng& grng, b
     T n0 = r.n;
     T n1d = std::max(T(m.ior), n0);                                                // ownMedium (materials_pbr.js:1080)
     T v1 = T(0);
+    uint32_t beyond = inside ? 0u : std::min(h.m, C.s->n_materials - 1);          // the medium a refraction enters
     if (m.transmission > 0 && m.metallic < 1) {                                    // asksMedium (materials.js:114)
         SceneHit<T> mb = scene_eval(*C.s, r.pos + (-nrm) * (otol * T(2)));         // mediumBeyond (tracebasics.js:1332)
-        const st_material& mm = C.s->materials[std::min(mb.a, C.s->n_materials - 1)];
+        beyond = std::min(mb.a, C.s->n_materials - 1);
+        const st_material& mm = C.s->materials[beyond];
         n1d = T(mm.ior);
         v1 = T(mm.abbe);
     }
@@ -671,6 +711,7 @@ inline void shade_hit(const Ctx<T>& C, Ray<T>& r, T dhit, Rng& rng, Rng& grng, b
     if (smp.transmitted) {
         r.n = nT;                                                                  // n(lambda) where it has one
         if (draw) { r.beta *= specW; r.lam = lamD; }
+        r.medium = beyond;                                                         // tracebasics.js:522-530 enterMedium
     }
     if (C.sppm) r.lens = lens_step(r.lens, r.bounces, smp.ev, C.lt);
     if (C.lt) {                                                                    // tracebasics.js:995-1011
@@ -898,14 +939,14 @@ void trace_path(const Ctx<T>& C, U4 sseed, uint32_t tile, const st_view& v, uint
     uint32_t it = 0, seg = 0;
     while (it < C.budget) {
         bool use_haze = C.haze.on;
-        if (use_haze && r.tmax == T(0)) {                                          // haze.js:255-273 hazeDraw
+        if (use_haze && r.tmax == T(0) && !walks(C, r)) {                          // haze.js:255-273 hazeDraw
             // from where the leg starts: the vertex, before the step off it (absLtot is the ltot on arrival there)
             V3<T> A = r.pos - r.dir * (std::max(r.ltot - r.absLtot, T(0)) / std::max(r.n, T(1e-4)));
             Rng hr = path_rng(sseed, tile, SEED_SALT_HAZE + seg);
             r.tmax = C.haze.draw(A, r.dir, r.absLtot, r.n, T(C.d.env_radius), hr);
         }
         uint32_t evals = 0;
-        T dh = march(C, r, st, use_haze, evals);
+        T dh = march(C, r, st, use_haze, evals, &sseed, tile);
         uint32_t chunks = std::max(1u, (evals + MARCH_CHUNK - 1) / MARCH_CHUNK);
         it = std::min(it + chunks - 1, C.budget - 1);
         bool last = it + 1 == C.budget;
@@ -1365,13 +1406,13 @@ void photon_walk(const Ctx<T>& C, U4 ps, uint32_t id, Ray<T>& r, uint32_t it, ui
     while (it < C.budget) {
         // the haze: the leg's collision drawn as it starts, from the photon's own stream (haze.js:255-273 hazeDraw)
         const bool use_haze = C.haze.on;
-        if (use_haze && r.tmax == T(0)) {
+        if (use_haze && r.tmax == T(0) && !walks(C, r)) {
             V3<T> A = r.pos - r.dir * (std::max(r.ltot - r.absLtot, T(0)) / std::max(r.n, T(1e-4)));
             Rng hr = path_rng(ps, id, SEED_SALT_HAZE + seg);
             r.tmax = C.haze.draw(A, r.dir, r.absLtot, r.n, T(C.d.env_radius), hr);
         }
         uint32_t evals = 0;
-        T dh = march(C, r, st, use_haze, evals);
+        T dh = march(C, r, st, use_haze, evals, &ps, id);
         uint32_t chunks = std::max(1u, (evals + MARCH_CHUNK - 1) / MARCH_CHUNK);
         it = std::min(it + chunks - 1, C.budget - 1);
         bool last = it + 1 == C.budget;
@@ -1429,9 +1470,11 @@ void photon_walk(const Ctx<T>& C, U4 ps, uint32_t id, Ray<T>& r, uint32_t it, ui
         Rng rng = path_rng(ps, id, 1 + seg);
         seg++;
         T n0 = r.n, n1d = std::max(T(m.ior), n0), v1 = T(0);
+        uint32_t beyond = inside ? 0u : std::min(h.m, C.s->n_materials - 1);
         if (m.transmission > 0 && m.metallic < 1) {
             SceneHit<T> mb = scene_eval(*C.s, r.pos + (-nrm) * (otol * T(2)));
-            const st_material& mm = C.s->materials[std::min(mb.a, C.s->n_materials - 1)];
+            beyond = std::min(mb.a, C.s->n_materials - 1);
+            const st_material& mm = C.s->materials[beyond];
             n1d = T(mm.ior);
             v1 = T(mm.abbe);
         }
@@ -1468,6 +1511,7 @@ void photon_walk(const Ctx<T>& C, U4 ps, uint32_t id, Ray<T>& r, uint32_t it, ui
         if (smp.transmitted) {
             r.n = nT;
             if (draw) { r.beta *= specW; r.lam = lamD; }
+            r.medium = beyond;
         }
         move_by(r, r.dir * otol);
         bool alive = max3(smp.w) > T(0) && smp.ev == EV_DELTA && r.bounces <= C.p.maxbounce;
@@ -1528,6 +1572,8 @@ static int render_impl(const st_scene_desc* s, const st_params* p, const st_view
     // path's steps-off-a-surface (a march chunk's worth each in the reference, ceil(maxiter / 32) of them)
     C.budget = p->budget ? p->budget : std::max(2u, p->maxbounce + 1 + (p->maxiter + 31) / 32);
     C.haze.init(*s);
+    for (uint32_t k = 0; k < s->n_materials; k++)
+        if (s->materials[k].scatter_distance > 0.f) C.scatter_on = true;
     const uint32_t W = p->width, H = p->height, P = W * H;
     uint32_t pend = std::min(P, path_first + (path_count ? path_count : P));
     Stats st;

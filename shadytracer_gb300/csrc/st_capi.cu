@@ -266,6 +266,8 @@ static Uni make_uni(const st_ctx* ctx) {
                           ctx->d_envimg != nullptr);
     u.claim = ctx->tune_claim;
     u.chunk = ctx->tune_chunk;
+    for (const st_material& m : ctx->mats)                     // the march walks the materials that scatter inside
+        if (m.scatter_distance > 0.f) u.scatter_on = 1u;
     // the worst case counted in chunks of at most 32 (the reference's dispatches): a tuned chunk below that gets the
     // iterations its longer marches need
     if (!p.budget && u.chunk && u.chunk < 32u)

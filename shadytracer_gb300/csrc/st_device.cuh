@@ -94,6 +94,8 @@ __device__ __forceinline__ Rng path_rng(uint4 sseed, uint32_t path, uint32_t eve
     Rng r; r.h = sseed; r.seed(path); r.seed(event); return r;
 }
 #define ST_SALT_HAZE 0x48410000u
+#define ST_SALT_WALK 0x57410000u          // a scattering material's walk: a leg's first flight (+ the path's steps)
+#define ST_SALT_WALK_HIT 0x57480000u      // ...a collision's turn and next flight (+ the path's steps)
 
 // ------------------------------------------------------------------------------------------------------------
 // The uniforms a launch reads: the settings and their host-derived values (core/photometry.js:182-237, in double
@@ -124,6 +126,7 @@ struct Uni {
     const float* sc; f3 sc_lo; float sc_cs; uint32_t sc_dx, sc_dy, sc_dz, sc_looks;
     // haze box (haze.js:64-80)
     int haze_on; f3 hc, hu, hv, hw, halb; float hhu, hhv, hhw, hsig, hg;
+    uint32_t scatter_on;         // a material that scatters inside (st_material.scatter_distance): the march walks it
     // the sample sequence
     uint32_t seed, maxaverages, n_prims, n_mats;
     uint32_t count_work;         // a counting pass: the march counts its fold's work (WC_*)

@@ -30,6 +30,10 @@ namespace st {
 #define META_SPEC (1u << 29)              // path whose first vertex drew an evaluable lobe; ...and delta events since
 #define META_PROBE (1u << 30)             // an emitter photon's probe (TAG_PROBE): looking for where its photon starts
 #define META_LOW 0x00ffffffu
+// meta.z: the march steps over the path (bits 0-23) and the medium it is in (bits 24-31): the material whose volume
+// holds it, 0 none -- what a scattering material's walk reads (materials.js:134-148 the medium a ray carries)
+#define META_STEPS 0x00ffffffu
+#define MEDIUM_SHIFT 24u
 #define SURF_NONE 0xffffu                 // hsurf: no medium asked (n1 is the material's own index of refraction)
 #define SURF_LEAVING 0xffffffffu          // hsurf: the surface seen from behind, the ray moved on
 #define SORT_G 16u                        // the march queue's space order: SORT_G^3 cells ...
@@ -191,7 +195,7 @@ struct EmitBufs {
 // calls take it), and the persistent kernels' occupancies, found once. Host-side only; the kernels never read it.
 struct SceneCode {
     void* lib = nullptr;                          // cudaLibrary_t
-    const void* march[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};   // [haze][counting pass]
+    const void* march[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};   // [media][counting pass]
     const void* surface = nullptr;
     const void* occlude[2] = {nullptr, nullptr};  // by the shadow side read
     const void* emit_resolve = nullptr;

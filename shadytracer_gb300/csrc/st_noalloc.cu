@@ -129,6 +129,9 @@ extern "C" int st_render_noalloc(int device, const st_scene_desc* desc, const st
     if (desc->n_prims == 0 || desc->n_prims > ST_MAX_PRIMS || desc->n_materials == 0 ||
         desc->n_materials > ST_MAX_MATERIALS || desc->prims[0].op != ST_OP_ITEM)
         return refuse("the table's size is out of range (1..256 primitives and materials) or it starts with no item");
+    for (uint32_t i = 0; i < desc->n_materials; i++)
+        if (desc->materials[i].scatter_distance > 0.f)
+            return refuse("material %u scatters inside (st_material.scatter_distance): its walk takes the context path", i);
     for (uint32_t i = 0; i < desc->n_prims; i++)
         if (desc->prims[i].type > ST_PRIM_CYLINDER || desc->prims[i].op > ST_OP_SUB ||
             desc->prims[i].material >= desc->n_materials)

@@ -482,6 +482,10 @@ __global__ void __launch_bounds__(256) k_photon_shade(WaveArgs a, int nxt, int l
                         if (smp.transmitted) {
                             n = nT;
                             if (draw) { beta = beta * spec.w; lam = spec.lam; }
+                            // the medium it is in now, the one beyond the face (tracebasics.js enterMedium)
+                            const uint32_t med = (ids >> 16) != SURF_NONE ? (ids >> 16)
+                                                                          : (inside ? 0u : (ids & 0xffffu));
+                            m4.z = (m4.z & META_STEPS) | (min(med, 255u) << MEDIUM_SHIFT);
                         }
                         const f3 off = dir * otol;
                         pos = pos + off; ltot += length(off) * n;
@@ -535,8 +539,8 @@ __global__ void __launch_bounds__(256) k_photon_shade(WaveArgs a, int nxt, int l
             a.pb.pos[slot] = f4(pos, ltot);
             a.pb.dir[slot] = f4(dir, n);
             a.pb.beta[slot] = make_float4(beta.x, beta.y, beta.z, 1.f);
-            // a new leg: its collision drawn afresh (a probe's is its chord, kept)
-            if (u.haze_on && !(m4.y & META_PROBE)) a.pb.rad[slot].w = 0.f;
+            // a new leg: its collision drawn afresh, in the haze or a scattering material (a probe's is its chord, kept)
+            if ((u.haze_on || u.scatter_on) && !(m4.y & META_PROBE)) a.pb.rad[slot].w = 0.f;
             a.pb.meta[slot] = m4;
             if (lam != 0.f) a.pb.lam[slot] = lam;
             outq[rq] = slot;

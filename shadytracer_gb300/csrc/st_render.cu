@@ -264,7 +264,7 @@ __device__ __forceinline__ void shade_surface(const WaveArgs& a, const st_materi
                                               f3& rad, uint32_t& bounces, uint32_t& state, float& lam,
                                               uint32_t& lens, float dh, Rng& rng, bool last, ShadowOut& sh,
                                               uint32_t q, uint32_t& my, uint32_t gpix, float& emw, float2& lp,
-                                              float& absL) {
+                                              float& absL, uint32_t& mz) {
     const Uni& u = a.u;
     float eps = march_tol(pos, u.tol);
     const uint32_t ids = __float_as_uint(surf.w);
@@ -466,6 +466,9 @@ __device__ __forceinline__ void shade_surface(const WaveArgs& a, const st_materi
     if (smp.transmitted) {
         n = nT;                                                       // n(lambda) where the ray has a wavelength
         if (draw) { beta = beta * spec.w; lam = spec.lam; }           // ...and the one it was refracted at, kept
+        // ...and the medium it is in now, the one beyond the face (tracebasics.js:522-530 enterMedium)
+        const uint32_t med = (ids >> 16) != SURF_NONE ? (ids >> 16) : (inside ? 0u : (ids & 0xffffu));
+        mz = (mz & META_STEPS) | (min(med, 255u) << MEDIUM_SHIFT);
     }
     if (u.sppm_on) {                                                  // materials_pbr.js:862-873 lensStep
         const bool delta = smp.ev == EV_DELTA;
@@ -654,7 +657,7 @@ __global__ void __launch_bounds__(256) k_shade(WaveArgs a, int nxt, int side, in
                     lam = a.pb.lam[slot];
                     uint32_t lens = (m4.y >> META_LENS_SHIFT) & 3u;
                     shade_surface<GUIDE>(a, sm, a.q.hsurf[q], pos, dir, ltot, n, beta, sunmis, rad, bounces, state,
-                                         lam, lens, dh, rng, last != 0, sh, q, m4.y, gpix, emw, lp, absL);
+                                         lam, lens, dh, rng, last != 0, sh, q, m4.y, gpix, emw, lp, absL, m4.z);
                     m4.w = __float_as_uint(absL);                     // kept where a leaving face moved the ray on
                     m4.y = (m4.y & ~(3u << META_LENS_SHIFT)) | (lens << META_LENS_SHIFT);
                 }
@@ -785,10 +788,10 @@ static int occupancy(const void* fn, size_t smem) {
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, 256, smem);
     return nb > 0 ? nb : 1;
 }
-template <bool HAZE, bool INST, bool COUNT>
+template <bool MEDIA, bool INST, bool COUNT>
 static void march_variant(const WaveArgs& a, int cur, int nxt, int last, int sms, cudaStream_t s, int* occ_cache) {
     size_t smem = a.u.n_prims * sizeof(DPrim);
-    auto fn = k_march<TableScene, HAZE, INST, COUNT>;
+    auto fn = k_march<TableScene, MEDIA, INST, COUNT>;
     if (smem > 48 * 1024) cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     int nb = occ_cache && *occ_cache ? *occ_cache : occupancy((const void*)fn, smem);
     if (occ_cache) *occ_cache = nb;
@@ -808,15 +811,16 @@ static cudaError_t code_launch(const void* fn, int* occ, unsigned grid_per_sm, i
     return cudaLaunchKernel(fn, dim3((unsigned)sms * per_sm), dim3(256), args, smem, s);
 }
 cudaError_t launch_march(const WaveArgs& a, int cur, int nxt, int last, int sms, cudaStream_t s) {
+    const bool media = a.u.haze_on || a.u.scatter_on;        // a haze box or a material that scatters inside
     if (a.code && !a.inst_range) {
-        const int haze = a.u.haze_on ? 1 : 0, count = a.u.count_work ? 1 : 0;
+        const int med = media ? 1 : 0, count = a.u.count_work ? 1 : 0;
         void* args[] = {(void*)&a, &cur, &nxt, &last};
-        return code_launch(a.code->march[haze][count], &a.code->occ_march[haze][count], 0, sms, 0, s, args);
+        return code_launch(a.code->march[med][count], &a.code->occ_march[med][count], 0, sms, 0, s, args);
     }
     if (a.inst_range) march_variant<false, true, false>(a, cur, nxt, last, sms, s, nullptr);
-    else if (a.u.count_work && a.u.haze_on) march_variant<true, false, true>(a, cur, nxt, last, sms, s, nullptr);
+    else if (a.u.count_work && media) march_variant<true, false, true>(a, cur, nxt, last, sms, s, nullptr);
     else if (a.u.count_work) march_variant<false, false, true>(a, cur, nxt, last, sms, s, nullptr);
-    else if (a.u.haze_on) march_variant<true, false, false>(a, cur, nxt, last, sms, s, nullptr);
+    else if (media) march_variant<true, false, false>(a, cur, nxt, last, sms, s, nullptr);
     else march_variant<false, false, false>(a, cur, nxt, last, sms, s, &g_occ_march);
     return cudaGetLastError();
 }

@@ -34,13 +34,25 @@ struct TableScene {
     __device__ static __forceinline__ SceneHit full(const DPrim* sp, uint32_t n, f3 p) { return scene_full(sp, n, p); }
 };
 
+// a scattering material's walk draws from the path's own streams (a photon's from its id), by the path's steps so far
+__device__ __forceinline__ Rng walk_rng(const WaveArgs& a, uint32_t slot, uint32_t id, uint32_t salt) {
+    const Uni& u = a.u;
+    return u.photon_pass ? path_rng(photon_seed_of(u.seed, a.ctr->sample), id, salt)
+                         : path_rng(sample_seed(u.seed, a.ctr->sample + slot_sample(u, slot)), slot % u.P, salt);
+}
+
 // ------------------------------------------------------------------------------------------------------------
 // THE MARCH (wavefront.js:834-1005): persistent -- a few CTAs an SM whose warps claim CLAIM queue entries at a time
 // (the autotuner's claim) and refill a lane the moment its ray ends; a ray marches at most MARCH_CHUNK evaluations (the
 // autotuner's chunk) a launch (the last
 // iteration's launch to its end) and goes to the hit queue or the next iteration's march queue.
+// MEDIA: compiled in for a scene with a haze box or a material that scatters inside. In the haze a leg's collision ends
+// the march (a vertex: haze.js mediumVertex); in a scattering material the march itself turns the ray at each collision
+// and marches on (haze.js:574-650 THE MEDIUM'S WALK): a free flight -ln(1 - u) / sigma drawn as a leg starts, from its
+// vertex, each collision taken back to along the line the ray came, turned by Henyey-Greenstein and given its next
+// flight, a march step against maxiter; a surface met first ends the leg as it would have.
 // ------------------------------------------------------------------------------------------------------------
-template <class SC, bool HAZE, bool INST, bool COUNT>
+template <class SC, bool MEDIA, bool INST, bool COUNT>
 __global__ void __launch_bounds__(256, 4) k_march(WaveArgs a, int cur, int nxt, int last) {
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ __align__(8) uint64_t mbar;
@@ -63,6 +75,9 @@ __global__ void __launch_bounds__(256, 4) k_march(WaveArgs a, int cur, int nxt, 
     uint32_t slot = INVALID_SLOT;
     f3 pos = mk(0.f), dir = mk(0.f);
     float ltot = 0.f, n = 1.f, tmax = 0.f;
+    float wsig = 0.f, wg = 0.f;                     // the walk's medium: its scattering coefficient (0: none) and g
+    uint32_t wid = 0;
+    bool walked = false;                            // a collision turned the ray in this launch
     uint32_t steps = 0, evals_here = 0;
     uint32_t wpos = 0, wend = 0;
     bool exhausted = false;
@@ -88,11 +103,27 @@ __global__ void __launch_bounds__(256, 4) k_march(WaveArgs a, int cur, int nxt, 
                     float4 p4 = a.pb.pos[slot], d4 = a.pb.dir[slot];
                     pos = xyz(p4); ltot = p4.w; dir = xyz(d4); n = d4.w;
                     uint4 m4 = a.pb.meta[slot];
-                    steps = m4.z;
+                    steps = m4.z & META_STEPS;
                     evals_here = 0;
                     if (INST) { uint2 rg = a.inst_range[m4.w]; pfirst = rg.x; pcount = rg.y; }
-                    tmax = HAZE ? a.pb.rad[slot].w : 0.f;
-                    if (HAZE && tmax == 0.f) {
+                    tmax = MEDIA ? a.pb.rad[slot].w : 0.f;
+                    wsig = 0.f;
+                    walked = false;
+                    wid = m4.x;
+                    if (MEDIA && a.u.scatter_on) {                    // the medium the ray is in, if it scatters
+                        const uint32_t med = m4.z >> MEDIUM_SHIFT;
+                        if (med != 0u && med < a.u.n_mats && (m4.y & META_PROBE) == 0u) {
+                            const float sd = a.mats[med].scatter_distance;
+                            if (sd > 0.f) { wsig = 1.f / sd; wg = clampf(a.mats[med].scatter_g, -0.95f, 0.95f); }
+                        }
+                    }
+                    if (MEDIA && wsig > 0.f && tmax == 0.f) {
+                        // THE LEG'S FLIGHT (haze.js:598-618 mediumDraw), from its vertex (absLtot): a collision the
+                        // step off the surface already passed is taken back to below
+                        Rng wr = walk_rng(a, slot, m4.x, ST_SALT_WALK + steps);
+                        const float4 r4 = wr.next();
+                        tmax = fmaxf(fminf(__uint_as_float(m4.w), ltot) - logf(1.f - r4.x) / wsig * n, 1e-30f);
+                    } else if (MEDIA && a.u.haze_on && wsig == 0.f && tmax == 0.f) {
                         // THE LEG'S COLLISION, drawn as it starts (haze.js:255-273 hazeDraw)
                         const Uni& u = a.u;
                         tmax = -1.f;
@@ -123,14 +154,28 @@ __global__ void __launch_bounds__(256, 4) k_march(WaveArgs a, int cur, int nxt, 
         bool fin = false, more = false;
         uint32_t state = RAY_ACTIVE;
         float dh = 0.f;
-        if (slot != INVALID_SLOT) {
+        if (slot != INVALID_SLOT && MEDIA && wsig > 0.f && ltot >= tmax) {
+            // A COLLISION IN THE MATERIAL (haze.js:619-650 mediumArrived, mediumBack, mediumCollide): back to it along
+            // the line the ray came, turned by the phase function, its next flight drawn
+            pos = pos - dir * ((ltot - tmax) / fmaxf(n, 1e-4f));
+            ltot = tmax;
+            Rng wr = walk_rng(a, slot, wid, ST_SALT_WALK_HIT + steps);
+            const float4 r4 = wr.next();
+            dir = hg_sample(dir, wg, r4.x, r4.y);
+            tmax = fmaxf(ltot - logf(1.f - r4.z) / wsig * n, 1e-30f);
+            steps += 1;
+            evals_here += 1;
+            walked = true;
+            if (steps > maxiter) { state = RAY_MAXITER; fin = true; dh = 1e7f; }
+            else if (evals_here >= chunk) more = true;
+        } else if (slot != INVALID_SLOT) {
             // THE STEP CACHE (wavefront.js:901-912): a ball that holds the ray far enough moves it with no distance;
             // a step that carries it past its collision in the haze is taken back to it below, as a distance step's
             // is. Up to SC_BURST balls in a row: a lane in empty space goes on while its warp's others ask the scene,
             // then asks it too where no ball holds it, so the warp's distance pass is not spent waiting on it
             uint32_t burst = 0;
             if (!INST && a.u.sc_looks) {
-                while (burst < SC_BURST && !(HAZE && tmax > 0.f && ltot >= tmax)) {
+                while (burst < SC_BURST && !(MEDIA && tmax > 0.f && ltot >= tmax)) {
                     const float sc = sc_step(a.u, pos, dir);
                     if (!(sc > 0.f)) break;
                     steps += 1;
@@ -141,10 +186,12 @@ __global__ void __launch_bounds__(256, 4) k_march(WaveArgs a, int cur, int nxt, 
                 }
                 evals_here += burst;
             }
+            // (a ray in a scattering material that passed its collision takes it on its next step, above)
+            const bool hz = MEDIA && wsig == 0.f;
             if (burst == SC_BURST || (burst && evals_here >= chunk)) {
-                if (HAZE && tmax > 0.f && ltot >= tmax) { state = RAY_SCATTER; fin = true; }
+                if (hz && tmax > 0.f && ltot >= tmax) { state = RAY_SCATTER; fin = true; }
                 else if (evals_here >= chunk) more = true;
-            } else if (HAZE && tmax > 0.f && ltot >= tmax) {
+            } else if (hz && tmax > 0.f && ltot >= tmax) {
                 state = RAY_SCATTER;
                 fin = true;
             } else {
@@ -163,7 +210,7 @@ __global__ void __launch_bounds__(256, 4) k_march(WaveArgs a, int cur, int nxt, 
                     f3 off = dir * (ea * stepscale);
                     pos = pos + off;
                     ltot += length(off) * n;
-                    if (HAZE && tmax > 0.f && ltot >= tmax) { state = RAY_SCATTER; fin = true; }
+                    if (hz && tmax > 0.f && ltot >= tmax) { state = RAY_SCATTER; fin = true; }
                     else if (evals_here >= chunk) more = true;
                 }
             }
@@ -178,9 +225,19 @@ __global__ void __launch_bounds__(256, 4) k_march(WaveArgs a, int cur, int nxt, 
             a.pb.pos[slot] = make_float4(pos.x, pos.y, pos.z, ltot);
             uint4 m = a.pb.meta[slot];
             m.y = (m.y & ~0x00ff0000u) | (state << 16);               // the classes above it kept
-            m.z = steps;
+            m.z = (m.z & ~META_STEPS) | min(steps, META_STEPS);        // the medium above it kept
             a.pb.meta[slot] = m;
-            if (HAZE) a.pb.rad[slot].w = tmax;
+            if (MEDIA) a.pb.rad[slot].w = tmax;
+            if (MEDIA && walked) {
+                a.pb.dir[slot] = make_float4(dir.x, dir.y, dir.z, n);
+                // a path that collided goes on as one light sampling could not have made (prevPdf -1, sunmis 1): the
+                // light it meets takes its whole weight (a photon's fields there are its own)
+                if (!a.u.photon_pass) {
+                    reinterpret_cast<float*>(&a.pb.beta[slot])[3] = 1.f;
+                    if (a.em.on) a.em.w[slot] = 1.f;
+                    if (a.lf.n) a.pb.lprev[slot].x = -1.f;
+                }
+            }
             if (fin) { a.q.hit[qp] = slot; a.q.hitd[qp] = dh; }
             else outq[cp] = slot;
             slot = INVALID_SLOT;

@@ -111,7 +111,8 @@ def prim(type_, pos=(0, 0, 0), params=(), material=1, op=ST_OP_ITEM, k=0.0, rot=
 
 
 def material(base=(0.8, 0.8, 0.8), metallic=0.0, roughness=0.5, specular=0.5, specular_tint=0.0,
-             transmission=0.0, ior=1.0, abbe=0.0, attenuation=0.0, detector=0.0, emissive=(0, 0, 0)):
+             transmission=0.0, ior=1.0, abbe=0.0, attenuation=0.0, detector=0.0, emissive=(0, 0, 0),
+             scatter_distance=0.0, scatter_g=0.0):
     """makeDefaultMaterial's defaults (core/materials.js:170-191), then the fields given."""
     m = StMaterial()
     for i in range(3):
@@ -120,6 +121,7 @@ def material(base=(0.8, 0.8, 0.8), metallic=0.0, roughness=0.5, specular=0.5, sp
     m.metallic, m.roughness, m.specular, m.specular_tint = metallic, roughness, specular, specular_tint
     m.transmission, m.ior, m.abbe, m.attenuation, m.detector = transmission, ior, abbe, attenuation, detector
     m.coat_edge, m.coat_width, m.coat_index = 550.0, 0.0, 1.8          # read only where coat != 0
+    m.scatter_distance, m.scatter_g = scatter_distance, scatter_g
     return m
 
 
@@ -1157,4 +1159,56 @@ def coated_spheres(width=64, height=48, maxbounce=12, seed=1, furnace=False, whe
     s.params = default_params(width=width, height=height, maxbounce=maxbounce, sun_elevation=40.0, sun_azimuth=30.0,
                               sun_illuminance=100000.0, sky_luminance=3000.0, ground_luminance=0.0, seed=seed)
     s.view = look_at((0.0, -3.0, 1.4), (0.0, 0.0, 0.3), 40.0, width / height)
+    return s
+
+
+# ------------------------------------------------------------------------------------------------------------
+# Scattering inside a material (materials.js scatterDistance; haze.js THE MEDIUM'S WALK).
+# ------------------------------------------------------------------------------------------------------------
+def volume_slab(tau=1.0, g=0.0, width=32, height=32, thickness=0.1, le=1000.0, maxiter=20000, seed=1):
+    """An index-matched slab (ior 1: its faces do nothing) 0.1 m thick and 10 m wide, its mean free path thickness / tau
+    and Henyey-Greenstein asymmetry g, seen head-on (a 6 degree view from 1 m) in front of a glowing plane of `le`
+    cd/m^2, in a black world: each pixel reads le x what the slab passes of a beam at normal incidence -- the walk's
+    transmission T(tau, g), which radiative transfer pins (exp(-tau) of it never collides; T + R = 1; deep in the slab
+    T (tau + 2 q) stops depending on tau, q = 0.7104 for isotropic scattering)."""
+    slab = material(base=(1, 1, 1), roughness=0.0, specular=0.0, transmission=1.0, ior=1.0,
+                    scatter_distance=thickness / tau, scatter_g=g)
+    glow = material(base=(0, 0, 0), specular=0.0, emissive=(le, le, le))
+    mats = [air(), slab, glow]
+    prims = [prim(ST_PRIM_BOX, pos=(0, 0, 0), params=(5.0, 5.0, thickness / 2), material=1),
+             prim(ST_PRIM_BOX, pos=(0, 0, -0.5), params=(49.99, 49.99, 0.001), material=2)]
+    s = Scene(prims, mats, env_radius=80.0, name="volume-slab")
+    s.params = default_params(width=width, height=height, maxbounce=16, env_uniform=1e-6, sun_hint=0, seed=seed)
+    s.params.maxiter = maxiter
+    s.params.emit_off = 1
+    s.view = look_at((0.0, 0.0, 1.0), (0.0, 0.0, 0.0), 6.0, width / height, up=(0.0, 1.0, 0.0))
+    s.info = {"closed_form": None, "le": le, "tau": tau, "g": g}
+    return s
+
+
+def milky_spheres(width=64, height=48, maxbounce=12, seed=1, furnace=False, maxiter=4000):
+    """Milky glass: a clear glass sphere (n 1.5) whose volume scatters (mean free path 5 cm, g 0.6) and a diffusing
+    opal-coloured one (mean free path 2 cm, g 0, a colour depth of 20 cm at (0.9, 0.7, 0.5)), on a grey floor under
+    the sun and sky; `furnace`: the first alone in a uniform environment, where it absorbs nothing and must vanish."""
+    milky = material(base=(1, 1, 1), roughness=0.0, specular=0.5, transmission=1.0, ior=1.5, scatter_distance=0.05,
+                     scatter_g=0.6)
+    if furnace:
+        s = Scene([prim(ST_PRIM_SPHERE, pos=(0.0, 0.0, 1.0), params=(0.3,), material=1)], [air(), milky],
+                  env_radius=40.0, name="milky-furnace")
+        # (inside glass most of a walk's arrivals at the wall are past the critical angle: bounces enough for them)
+        s.params = default_params(width=width, height=height, maxbounce=max(maxbounce, 128), env_uniform=1000.0,
+                                  sun_hint=0, seed=seed)
+        s.params.maxiter = maxiter
+        s.view = look_at((0.0, -1.6, 1.0), (0.0, 0.0, 1.0), 40.0, width / height)
+        s.info = {"closed_form": 1000.0}
+        return s
+    opal = material(base=(0.9, 0.7, 0.5), roughness=0.0, specular=0.5, transmission=1.0, ior=1.45, attenuation=0.2,
+                    scatter_distance=0.02, scatter_g=0.0)
+    s = Scene([prim(ST_PRIM_PLANE, material=1), prim(ST_PRIM_SPHERE, pos=(-0.45, 0.0, 0.35), params=(0.35,), material=2),
+               prim(ST_PRIM_SPHERE, pos=(0.45, 0.1, 0.3), params=(0.3,), material=3)],
+              [air(), diffuse((0.6, 0.6, 0.6)), milky, opal], env_radius=20.0, name="milky-spheres")
+    s.params = default_params(width=width, height=height, maxbounce=maxbounce, sun_elevation=40.0, sun_azimuth=30.0,
+                              sun_illuminance=100000.0, sky_luminance=3000.0, ground_luminance=0.0, seed=seed)
+    s.params.maxiter = maxiter
+    s.view = look_at((0.0, -2.6, 1.2), (0.0, 0.0, 0.3), 40.0, width / height)
     return s

@@ -37,7 +37,8 @@ class StMaterial(C.Structure):
                 ("attenuation", C.c_float), ("detector", C.c_float),
                 ("emissive", C.c_float * 3), ("beam_cos", C.c_float), ("haze", C.c_float), ("anisotropy", C.c_float),
                 ("coat", C.c_uint32), ("coat_lo", C.c_float), ("coat_hi", C.c_float), ("coat_edge", C.c_float),
-                ("coat_width", C.c_float), ("coat_index", C.c_float)]
+                ("coat_width", C.c_float), ("coat_index", C.c_float),
+                ("scatter_distance", C.c_float), ("scatter_g", C.c_float), ("pad", C.c_float * 2)]
 
 
 ST_LIGHT_DISC, ST_LIGHT_RECTANGLE = 1, 2

@@ -59,7 +59,7 @@ def test_struct_sizes_match_the_mirrors(lib):
 def test_fixed_record_sizes():
     from shadytracer_gb300 import st_types as T
     assert C.sizeof(T.StPrim) == 128
-    assert C.sizeof(T.StMaterial) == 96
+    assert C.sizeof(T.StMaterial) == 112
 
 
 def test_abi_version(lib):
