@@ -1196,8 +1196,7 @@ def milky_spheres(width=64, height=48, maxbounce=12, seed=1, furnace=False, maxi
         s = Scene([prim(ST_PRIM_SPHERE, pos=(0.0, 0.0, 1.0), params=(0.3,), material=1)], [air(), milky],
                   env_radius=40.0, name="milky-furnace")
         # (inside glass most of a walk's arrivals at the wall are past the critical angle: bounces enough for them)
-        s.params = default_params(width=width, height=height, maxbounce=max(maxbounce, 128), env_uniform=1000.0,
-                                  sun_hint=0, seed=seed)
+        s.params = default_params(width=width, height=height, maxbounce=64, env_uniform=1000.0, sun_hint=0, seed=seed)
         s.params.maxiter = maxiter
         s.view = look_at((0.0, -1.6, 1.0), (0.0, 0.0, 1.0), 40.0, width / height)
         s.info = {"closed_form": 1000.0}
