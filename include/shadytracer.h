@@ -277,6 +277,12 @@ typedef struct st_params {
      * the preset itself is asked */
     uint32_t env_cache;           /* 1 on                                                           */
     uint32_t env_cache_size;      /* 1024, 2048 or 4096 (0: 2048)                                  */
+    /* THE PHOTON MAP IN THE VOLUME (sppm.js:497-511 sppmGatherVolume, haze.js mediumStore): with the map on in a scene
+     * with a material that scatters inside, the sun's photons store a record where they collide inside it (past a
+     * delta event, as at a surface), and a camera ray that came in through delta events alone gathers at its first
+     * collision sum p(l . v) Phi / (sigma_s 4/3 pi R^3) / n^2 over the records within R, then walks on. R is the
+     * first sample's volume radius shrunk as a volume: R_k^3 = R_1^3 prod_{i<k} (i + alpha) / (i + 1). */
+    float    sppm_r1_volume;      /* metres (0: 4 x the surface's first radius)                       */
 } st_params;
 
 #define ST_ENV_ANALYTIC 0u

@@ -32,7 +32,7 @@ namespace {
 // the most SDF evaluations a ray takes in one iteration's march (the product's MARCH_CHUNK)
 const uint32_t MARCH_CHUNK = 48;
 const uint32_t RAY_ACTIVE = 0, RAY_ABSORBED = 1, RAY_ESCAPED = 2, RAY_MAXITER = 4, RAY_SOURCE = 5,
-               RAY_TERMINATED = 8, RAY_SCATTER = 9;
+               RAY_TERMINATED = 8, RAY_SCATTER = 9, RAY_GATHER = 10;
 
 struct Stats {
     std::atomic<uint64_t> paths{0}, segments{0}, march_steps{0}, shadow_rays{0}, shadow_steps{0};
@@ -75,6 +75,8 @@ template <class T> struct Ctx {
     const SppmGrid* grid = nullptr;
     float sp_r2 = 0, sp_cell = 0, sp_half = 0;
     double sp_inv_area = 0;
+    float sp_vr2 = 0, sp_vcell = 0;                 // in the volume (sppmRadiusVolume): R^2, the records' cell 2R
+    double sp_inv_vol = 0;                          // 3 / (4 pi R^3)
     uint32_t sp_budget = 512;
     // the learned emission map (wavefront.js:628-711): on, the photons sent and stored per cell, the CDF
     bool sp_learn = false;
@@ -174,6 +176,11 @@ template <class T> struct Ray {
     uint32_t bounces, steps, state, pix;
 };
 
+struct PhotonRec { float pos[3], power[3]; uint32_t dir, nrm, flags; };
+// a walk's seed and what it does with the photon map in the volume: 1 a photon that stores where it collides, 2 a
+// camera ray handed to the gather at its first collision
+struct WalkIO { U4 ps; uint32_t id; int map; std::vector<PhotonRec>* out; };
+
 template <class T> inline void move_by(Ray<T>& r, const V3<T>& off) {       // tracebasics.js:562-567 moveBy
     r.pos += off;
     r.ltot += length(off) * r.n;
@@ -204,17 +211,17 @@ template <class T> inline void deposit(Frame<T>& f, uint32_t pix, const V3<T>& c
 // THE MEDIUM'S WALK): a free flight -ln(1 - u) / sigma drawn as its leg starts, from its vertex; at each collision
 // taken back to it, turned by Henyey-Greenstein, its next flight drawn, a march step; what it meets after that takes
 // its whole weight (prevPdf -1, sunmis 1). A collision counts as an evaluation in the chunks an iteration marches.
-const uint32_t SEED_SALT_WALK = 0x57410000u, SEED_SALT_WALK_HIT = 0x57480000u;
+const uint32_t SEED_SALT_WALK = 0x57410000u, SEED_SALT_WALK_HIT = 0x57480000u, SEED_SALT_VOL_STORE = 0x564F4C53u;
 // whether the ray is in a material that scatters inside (the haze's draw is then not its)
 template <class T> inline bool walks(const Ctx<T>& C, const Ray<T>& r) {
     return C.scatter_on && r.medium != 0 && r.medium < C.s->n_materials && C.s->materials[r.medium].scatter_distance > 0.f;
 }
 template <class T> inline T march(const Ctx<T>& C, Ray<T>& r, Stats& st, bool use_haze, uint32_t& evals_out,
-                                  const U4* wps = nullptr, uint32_t wid = 0) {
+                                  const WalkIO* wio = nullptr) {
     uint64_t steps = 0;
     T dh = T(1e7);
     T wsig = T(0), wg = T(0);
-    if (wps && C.scatter_on && r.medium != 0 && r.medium < C.s->n_materials) {
+    if (wio && C.scatter_on && r.medium != 0 && r.medium < C.s->n_materials) {
         const st_material& mm = C.s->materials[r.medium];
         if (mm.scatter_distance > 0.f) {
             wsig = T(1) / T(mm.scatter_distance);
@@ -222,7 +229,7 @@ template <class T> inline T march(const Ctx<T>& C, Ray<T>& r, Stats& st, bool us
         }
     }
     if (wsig > T(0) && r.tmax == T(0)) {                                       // haze.js:598-618 mediumDraw
-        Rng wr = path_rng(*wps, wid, SEED_SALT_WALK + r.steps);
+        Rng wr = path_rng(wio->ps, wio->id, SEED_SALT_WALK + r.steps);
         T u[4]; wr.next4(u);
         r.tmax = std::max(std::min(r.absLtot, r.ltot) - std::log(T(1) - u[0]) / wsig * r.n, T(1e-30));
     }
@@ -230,13 +237,36 @@ template <class T> inline T march(const Ctx<T>& C, Ray<T>& r, Stats& st, bool us
         if (wsig > T(0) && r.ltot >= r.tmax) {                                // haze.js:619-650 mediumCollide
             r.pos = r.pos - r.dir * ((r.ltot - r.tmax) / std::max(r.n, T(1e-4)));
             r.ltot = r.tmax;
-            Rng wr = path_rng(*wps, wid, SEED_SALT_WALK_HIT + r.steps);
+            if (wio->map == 2) { r.state = RAY_GATHER; break; }          // the map gathers here (RAY_GATHER)
+            Rng wr = path_rng(wio->ps, wio->id, SEED_SALT_WALK_HIT + r.steps);
             T u[4]; wr.next4(u);
+            const V3<T> din = r.dir;
             r.dir = hg_sample(r.dir, wg, u[0], u[1]);
             r.tmax = std::max(r.ltot - std::log(T(1) - u[2]) / wsig * r.n, T(1e-30));
             r.steps += 1;
             steps++;
             r.sunmis = T(1); r.emw = T(1); r.lpx = T(-1);
+            if (wio->map == 1) {                                               // haze.js:680-690 mediumStore
+                const st_material& mm = C.s->materials[r.medium];
+                V3<T> pw = r.rad * r.beta;
+                if (mm.attenuation > 0.f) {
+                    const T dl = std::max(r.ltot - r.absLtot, T(0)) / std::max(r.n, T(1e-4)) / T(mm.attenuation);
+                    pw.x *= std::exp(std::log(std::min(std::max(T(mm.base[0]), T(1e-6)), T(1))) * dl);
+                    pw.y *= std::exp(std::log(std::min(std::max(T(mm.base[1]), T(1e-6)), T(1))) * dl);
+                    pw.z *= std::exp(std::log(std::min(std::max(T(mm.base[2]), T(1e-6)), T(1))) * dl);
+                }
+                Rng sr = path_rng(wio->ps, wio->id, SEED_SALT_VOL_STORE + r.steps);
+                T us[4]; sr.next4(us);
+                const uint32_t sub = std::min((uint32_t)(us[1] * T(SPPM_SUBS)), SPPM_SUBS - 1);
+                PhotonRec rec;
+                rec.pos[0] = (float)r.pos.x; rec.pos[1] = (float)r.pos.y; rec.pos[2] = (float)r.pos.z;
+                rec.power[0] = (float)pw.x; rec.power[1] = (float)pw.y; rec.power[2] = (float)pw.z;
+                const float dv[3] = {(float)-din.x, (float)-din.y, (float)-din.z};
+                rec.dir = sppm_oct(dv);
+                rec.nrm = 0;
+                rec.flags = (r.bounces + 1) | (sub << SPPM_SUB_SHIFT) | SPPM_VOL;
+                wio->out->push_back(rec);
+            }
             if (r.steps > C.p.maxiter) { r.state = RAY_MAXITER; break; }
             continue;
         }
@@ -454,6 +484,7 @@ inline V3<T> sppm_gather_lobes(const Ctx<T>& C, const V3<T>& X, const V3<T>& nrm
                 if (!whole && ((b >> SPPM_SUB_SHIFT) & (SPPM_SUBS - 1)) != s) continue;
                 if (visits >= hard) { cut = true; break; }
                 visits++;
+                if (b & SPPM_VOL) continue;                                     // the volume's gather's
                 const float* p = &g.pos[3 * idx];
                 int32_t pc[3];
                 sppm_cell(p, csz, pc);
@@ -893,6 +924,89 @@ void medium_vertex(const Ctx<T>& C, Ray<T>& r, Rng& rng, bool last, Frame<T>& fr
     if (r.bounces > C.p.maxbounce) r.state = RAY_TERMINATED;
 }
 
+// THE GATHER IN A VOLUME (sppm.js:497-511 sppmGatherVolume through sppmWalk :305-360): the records photons stored where
+// they collided (SPPM_VOL) within R in the eight cells of the volume's grid round x, each through the phase function
+// from the way it came to the way to the camera, sum p(l . v) Phi / (sigma 4/3 pi R^3); whole cells within their share
+// of the budget, else m sub-lists from a drawn start weighing 32 / m; the walk cut at the hard cap
+template <class T>
+inline V3<T> sppm_gather_volume(const Ctx<T>& C, const V3<T>& X, const V3<T>& v, uint32_t bc, T g, T sigma, Rng& rng) {
+    const SppmGrid& gr = *C.grid;
+    if (!(sigma > T(0)) || gr.flags.empty()) return V3<T>(T(0));
+    const float csz = gr.vcell;
+    const float x[3] = {(float)X.x, (float)X.y, (float)X.z};
+    int32_t c0[3], side[3];
+    for (int a = 0; a < 3; a++) {
+        const float gx = x[a] / csz;
+        c0[a] = (int32_t)std::floor(gx);
+        side[a] = (gx - std::floor(gx) >= 0.5f) ? 1 : -1;
+    }
+    const uint32_t share = std::max(1u, C.sp_budget / 8);
+    const uint64_t hard = (uint64_t)SPPM_VISIT_HARD * C.sp_budget;
+    uint64_t visits = 0;
+    bool cut = false;
+    V3<T> sum(T(0));
+    for (uint32_t k = 0; k < 8 && !cut; k++) {
+        const int32_t cell[3] = {c0[0] + ((k & 1) ? side[0] : 0), c0[1] + ((k & 2) ? side[1] : 0),
+                                 c0[2] + ((k & 4) ? side[2] : 0)};
+        const std::vector<uint32_t>& L = gr.lists[sppm_hash(cell[0], cell[1], cell[2])];
+        const uint32_t count = (uint32_t)L.size();
+        const bool whole = count <= share;
+        const uint32_t subs = whole ? 1 : std::max(1u, (SPPM_SUBS * share) / std::max(count, 1u));
+        const T w = whole ? T(1) : T(SPPM_SUBS) / T(subs);
+        float u4[4];
+        rng.next4(u4);
+        const uint32_t start = std::min((uint32_t)(u4[0] * (float)SPPM_SUBS), SPPM_SUBS - 1);
+        for (uint32_t j = 0; j < subs && !cut; j++) {
+            const uint32_t s = (start + j) % SPPM_SUBS;
+            for (uint32_t idx : L) {
+                const uint32_t b = gr.flags[idx];
+                if (!whole && ((b >> SPPM_SUB_SHIFT) & (SPPM_SUBS - 1)) != s) continue;
+                if (visits >= hard) { cut = true; break; }
+                visits++;
+                if (!(b & SPPM_VOL) || bc + (b & SPPM_B_MASK) > C.p.maxbounce + 1) continue;
+                const float* p = &gr.pos[3 * idx];
+                int32_t pc[3];
+                sppm_cell(p, csz, pc);
+                if (pc[0] != cell[0] || pc[1] != cell[1] || pc[2] != cell[2]) continue;
+                const float d[3] = {p[0] - x[0], p[1] - x[1], p[2] - x[2]};
+                float dd = d[0] * d[0] + d[1] * d[1];
+                dd = dd + d[2] * d[2];
+                if (dd > C.sp_vr2) continue;
+                float l[3];
+                sppm_unoct(gr.dir[idx], l);
+                const T f = hg_eval(T(l[0]) * v.x + T(l[1]) * v.y + T(l[2]) * v.z, g);
+                sum += V3<T>(T(gr.power[3 * idx]), T(gr.power[3 * idx + 1]), T(gr.power[3 * idx + 2])) * (w * f);
+            }
+        }
+    }
+    return sum * T(C.sp_inv_vol / (double)sigma);
+}
+// THE MAP GATHERED AT A COLLISION (haze.js:692-707 mediumGathered): the throughput absorbed to here, the photons'
+// in-scattered light over n^2, then the ray turned there -- a vertex, the map's D: a bounce, its lens field 2, light
+// sampling's MIS halves cleared, its next flight drawn from here
+template <class T> inline void medium_gathered(const Ctx<T>& C, Ray<T>& r, Rng& rng, Rng& grng, bool last) {
+    const st_material& mm = C.s->materials[std::min(r.medium, C.s->n_materials - 1)];
+    const T sig = mm.scatter_distance > 0.f ? T(1) / T(mm.scatter_distance) : T(0);
+    const T g = clampT(T(mm.scatter_g), T(-0.95), T(0.95));
+    if (mm.attenuation > 0.f) {
+        const T dl = std::max(r.ltot - r.absLtot, T(0)) / std::max(r.n, T(1e-4)) / T(mm.attenuation);
+        r.beta.x *= std::exp(std::log(std::min(std::max(T(mm.base[0]), T(1e-6)), T(1))) * dl);
+        r.beta.y *= std::exp(std::log(std::min(std::max(T(mm.base[1]), T(1e-6)), T(1))) * dl);
+        r.beta.z *= std::exp(std::log(std::min(std::max(T(mm.base[2]), T(1e-6)), T(1))) * dl);
+    }
+    r.absLtot = r.ltot;
+    const V3<T> Lv = sppm_gather_volume(C, r.pos, r.dir, r.bounces + 1, g, sig, grng);
+    r.rad += r.beta * Lv * (T(1) / std::max(r.n * r.n, T(1e-8)));
+    r.state = RAY_ACTIVE;
+    r.bounces += 1;
+    r.lens = 2;
+    r.cls = 0;
+    T u[4]; rng.next4(u);
+    r.dir = hg_sample(r.dir, g, u[0], u[1]);
+    r.sunmis = T(1); r.emw = T(1); r.lpx = T(-1); r.lpy = r.ltot;
+    if (last || r.bounces > C.p.maxbounce) r.state = RAY_TERMINATED;
+}
+
 template <class T>
 void trace_path(const Ctx<T>& C, U4 sseed, uint32_t tile, const st_view& v, uint32_t W, uint32_t H,
                 Frame<T>& fr, Stats& st) {
@@ -946,7 +1060,8 @@ void trace_path(const Ctx<T>& C, U4 sseed, uint32_t tile, const st_view& v, uint
             r.tmax = C.haze.draw(A, r.dir, r.absLtot, r.n, T(C.d.env_radius), hr);
         }
         uint32_t evals = 0;
-        T dh = march(C, r, st, use_haze, evals, &sseed, tile);
+        const WalkIO wio{sseed, tile, (C.sppm && r.lens == 1) ? 2 : 0, nullptr};
+        T dh = march(C, r, st, use_haze, evals, &wio);
         uint32_t chunks = std::max(1u, (evals + MARCH_CHUNK - 1) / MARCH_CHUNK);
         it = std::min(it + chunks - 1, C.budget - 1);
         bool last = it + 1 == C.budget;
@@ -958,11 +1073,13 @@ void trace_path(const Ctx<T>& C, U4 sseed, uint32_t tile, const st_view& v, uint
             r.rad += r.beta * (owned ? C.env.sky_only(r.dir) : C.env.radiance(r.dir)) * r.sunmis;
             break;
         }
-        if (r.state != RAY_ACTIVE && r.state != RAY_SCATTER) break;                // out of steps or length
+        if (r.state != RAY_ACTIVE && r.state != RAY_SCATTER && r.state != RAY_GATHER) break;   // out of steps or length
         Rng rng = path_rng(sseed, tile, 1 + seg);
         Rng grng = path_rng(sseed, tile, SPPM_STORE_SALT + seg);                   // the gather's own stream
         seg++;
-        if (r.state == RAY_SCATTER) {
+        if (r.state == RAY_GATHER) {
+            medium_gathered(C, r, rng, grng, last);
+        } else if (r.state == RAY_SCATTER) {
             r.absLtot = r.ltot;                                                    // absorbAlong on arrival
             medium_vertex(C, r, rng, last, fr, st);
             r.lens = 0;                                                            // haze.js:539
@@ -1120,7 +1237,6 @@ template <> const MfTables* tables<double>() {
 // photon's shade): a direction in the sun's cone, a point uniform over the square of half width sp_half across the
 // sun, flux L_disc cos Omega / (N pdf_area); at each hit stored where it has passed delta events only, at least one,
 // on an evaluable surface within the cap, else bounced -- a delta lobe keeps it, anything else ends it
-struct PhotonRec { float pos[3], power[3]; uint32_t dir, nrm, flags; };
 const uint32_t LT_LENS_SALT = 0x4C54434Eu;      // a connection's point of the lens, from the photon's own stream
 
 // A PHOTON'S CONNECTION TO THE CAMERA (materials_pbr.js:672-830 ltConnect, :598-612 camFootprint, lens.js lensDisc,
@@ -1412,7 +1528,8 @@ void photon_walk(const Ctx<T>& C, U4 ps, uint32_t id, Ray<T>& r, uint32_t it, ui
             r.tmax = C.haze.draw(A, r.dir, r.absLtot, r.n, T(C.d.env_radius), hr);
         }
         uint32_t evals = 0;
-        T dh = march(C, r, st, use_haze, evals, &ps, id);
+        const WalkIO wio{ps, id, (C.sppm && r.passed && r.bounces + 2 <= C.p.maxbounce) ? 1 : 0, &out};
+        T dh = march(C, r, st, use_haze, evals, &wio);
         uint32_t chunks = std::max(1u, (evals + MARCH_CHUNK - 1) / MARCH_CHUNK);
         it = std::min(it + chunks - 1, C.budget - 1);
         bool last = it + 1 == C.budget;
@@ -1661,6 +1778,11 @@ static int render_impl(const st_scene_desc* s, const st_params* p, const st_view
             C.sp_r2 = (float)rk * (float)rk;
             C.sp_cell = (float)(2.0 * rk);
             C.sp_inv_area = 1.0 / (PI_D * rk * rk);
+            const double r1v = p->sppm_r1_volume > 0.f ? p->sppm_r1_volume : 4.0 * (double)(float)r1;
+            const double rv = sppm_radius_volume((double)(float)r1v, (int)(sample0 + si + 1), al);
+            C.sp_vr2 = (float)rv * (float)rv;
+            C.sp_vcell = (float)(2.0 * rv);
+            C.sp_inv_vol = 3.0 / (4.0 * PI_D * rv * rv * rv);
             const U4 ps = sample_seed(p->seed ^ PHOTON_SEED_SALT, sample0 + si);
             const uint32_t kk = sample0 + si;
             if (C.sp_learn && kk > 0 && (kk & 3u) == 0) lt_build(lt_emit.data(), lt_hit.data(), lt_cdf.data());
@@ -1684,7 +1806,8 @@ static int render_impl(const st_scene_desc* s, const st_params* p, const st_view
                     dirs.push_back(rr.dir); nrms.push_back(rr.nrm); flags.push_back(rr.flags);
                 }
             if (sppm_on) {
-                sppm_build(grid, pos.data(), pw.data(), nrms.data(), flags.data(), (uint32_t)flags.size(), C.sp_cell);
+                sppm_build(grid, pos.data(), pw.data(), nrms.data(), flags.data(), (uint32_t)flags.size(), C.sp_cell,
+                           C.sp_vcell);
                 grid.dir = dirs;
             }
         }

@@ -17,6 +17,7 @@ const uint32_t SPPM_VISIT_HARD = 8;       // sppm.js:114
 const float SPPM_NORMAL_DOT = 0.9f;       // sppm.js:135
 const double SPPM_FILL = 0.85;            // sppm.js:124
 const uint32_t SPPM_B_MASK = 0xFFFFu, SPPM_SUB_SHIFT = 16;
+const uint32_t SPPM_VOL = 0x40000000u;      // a record where a photon collided inside a medium (sppm.js:93-95)
 
 // the cell a point is in, in f32 as the kernel computes it: floor(pos / cell) (sppm.js:381, WGSL vec3<i32>(floor(...)))
 inline void sppm_cell(const float* p, float c, int32_t out[3]) {
@@ -31,6 +32,12 @@ inline double sppm_radius(double r1, int k, double alpha) {
     double s = 1;
     for (int i = 1; i < std::max(1, k); i++) s *= (i + alpha) / (i + 1);
     return r1 * std::sqrt(s);
+}
+// ...and in a volume (sppm.js:182-191 sppmRadiusVolume): R^3 shrinks by the factor r^2 does
+inline double sppm_radius_volume(double r1, int k, double alpha) {
+    double s = 1;
+    for (int i = 1; i < std::max(1, k); i++) s *= (i + alpha) / (i + 1);
+    return r1 * std::cbrt(s);
 }
 // the keep (sppm.js:156-157)
 inline double sppm_keep(double capacity, double demand) {
@@ -77,14 +84,15 @@ inline void sppm_unoct(uint32_t w, float* out) {
 // THE GRID, as the reference's lists define it: for every record its cell's hash, per hash its records (the
 // list's membership; the list's order is the atomics' and not part of the answer)
 struct SppmGrid {
-    float cell;
+    float cell, vcell = 0;                       // the surface records' cell, the volume records' (sppm.js sppmPut)
     std::vector<float> pos, power;
     std::vector<uint32_t> nrm, flags, key, dir;
     std::vector<std::vector<uint32_t>> lists;   // per hash: record indices, ascending
 };
 inline void sppm_build(SppmGrid& g, const float* pos, const float* power, const uint32_t* nrm, const uint32_t* flags,
-                       uint32_t n, float cell) {
+                       uint32_t n, float cell, float vcell = 0) {
     g.cell = cell;
+    g.vcell = vcell > 0 ? vcell : cell;
     g.pos.assign(pos, pos + 3 * (size_t)n);
     g.power.assign(power, power + 3 * (size_t)n);
     g.nrm.assign(nrm, nrm + n);
@@ -93,7 +101,7 @@ inline void sppm_build(SppmGrid& g, const float* pos, const float* power, const 
     g.lists.assign(SPPM_HEADS, {});
     for (uint32_t i = 0; i < n; i++) {
         int32_t c[3];
-        sppm_cell(&pos[3 * i], cell, c);
+        sppm_cell(&pos[3 * i], (flags[i] & SPPM_VOL) ? g.vcell : cell, c);
         uint32_t h = sppm_hash(c[0], c[1], c[2]);
         g.key[i] = h;
         g.lists[h].push_back(i);
@@ -151,7 +159,7 @@ inline void sppm_gather(const SppmGrid& g, const float* x, const float* n, const
                 float dd = d[0] * d[0] + d[1] * d[1];
                 dd = dd + d[2] * d[2];
                 if (dd > r2) continue;
-                if (bc + (b & SPPM_B_MASK) > maxbounce + 1) continue;
+                if ((b & SPPM_VOL) || bc + (b & SPPM_B_MASK) > maxbounce + 1) continue;
                 float pn[3];
                 sppm_unoct(g.nrm[idx], pn);
                 float nd = pn[0] * n[0] + pn[1] * n[1];

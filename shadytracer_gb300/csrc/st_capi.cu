@@ -539,6 +539,7 @@ static WaveArgs wave_args(st_ctx* ctx, uint32_t w) {
         a.u.sppm_half = ctx->params.sppm_half > 0.f ? ctx->params.sppm_half : std::min(15.f, a.u.envR);
         a.u.sppm_r1 = ctx->params.sppm_r1 > 0.f ? ctx->params.sppm_r1 : 0.005f;
         a.u.sppm_alpha = ctx->params.sppm_alpha > 0.f ? ctx->params.sppm_alpha : (float)(2.0 / 3.0);
+        a.u.sppm_r1v = ctx->params.sppm_r1_volume > 0.f ? ctx->params.sppm_r1_volume : 4.f * a.u.sppm_r1;
         a.u.sppm_learn = ctx->params.sppm_learn ? 1u : 0u;
         a.sp = sppm_bufs(ctx_ext(ctx).sppm);
     }

@@ -137,6 +137,7 @@ struct Uni {
     uint32_t sort_on; f3 glo, ginv;
     // the photon map (st_photons.cu): photons a sample, the sun photons' square, the radius schedule, the budget
     uint32_t sppm_on, sppm_n, sppm_budget, sppm_learn; float sppm_half, sppm_r1, sppm_alpha;
+    float sppm_r1v;              // the volume's first radius (st_params.sppm_r1_volume)
     // light tracing to the camera (st_photons.cu lt_connect): the photons above connect where they land
     uint32_t lt_on;
     uint32_t photon_pass;        // the wave's photon pass: its rays are photons, seeded by the photon's own stream

@@ -17,6 +17,7 @@ namespace st {
 #define RAY_SOURCE 5u
 #define RAY_TERMINATED 8u
 #define RAY_SCATTER 9u
+#define RAY_GATHER 10u                    // a camera ray's collision in a scattering material the map gathers at
 
 // A MARCH CHUNK: the most SDF evaluations a ray takes in one launch of the march or the occlusion pass before it is
 // handed to the next iteration (the reference's MARCH_STEPS, wavefront.js:870, is 32); the last iteration's launches
@@ -104,6 +105,9 @@ struct SppmDev {
     uint32_t count, cap, dropped, gathers;   // records stored (may pass cap: the rest are dropped), capacity
     float r, cell, inv_area, r2;              // this sample's radius, the grid's cell (2r), 1 / (pi r^2), r^2
     unsigned long long visits, stores;
+    // in the volume (sppm.js sppmRadiusVolume): the radius, its records' cell (2R), 3 / (4 pi R^3), R^2
+    float vr, vcell, inv_vol, vr2;
+    uint32_t vstores, vgathers;
 };
 struct SppmBufs {
     SppmDev* dev = nullptr;

@@ -37,7 +37,9 @@ __device__ __forceinline__ bool sppm_evaluable(const st_material& m, bool all) {
 
 // THE SAMPLE'S RADIUS (sppm.js:177-181): r_k^2 = r_1^2 prod_{i<k} (i + alpha) / (i + 1), k the sample's number from
 // 1; the grid's cell is 2 r; the count of records cleared
-__global__ void k_sppm_begin(SppmDev* __restrict__ d, const DevCtr* __restrict__ ctr, float r1, float alpha, uint32_t cap) {
+// AND IN THE VOLUME (sppm.js:182-191 sppmRadiusVolume): R_k^3 = R_1^3 times the same product, its records' cell 2 R
+__global__ void k_sppm_begin(SppmDev* __restrict__ d, const DevCtr* __restrict__ ctr, float r1, float alpha, uint32_t cap,
+                             float r1v) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     const uint32_t k = ctr->sample + 1u;
     double s = 1.0;
@@ -47,6 +49,13 @@ __global__ void k_sppm_begin(SppmDev* __restrict__ d, const DevCtr* __restrict__
     d->r2 = (float)r * (float)r;
     d->cell = (float)(2.0 * r);
     d->inv_area = (float)(1.0 / (3.14159265358979323846 * r * r));
+    const double rv = (double)r1v * cbrt(s);
+    d->vr = (float)rv;
+    d->vr2 = (float)rv * (float)rv;
+    d->vcell = (float)(2.0 * rv);
+    d->inv_vol = (float)(3.0 / (4.0 * 3.14159265358979323846 * rv * rv * rv));
+    d->vstores = 0u;
+    d->vgathers = 0u;
     d->count = 0u;
     d->cap = cap;
     d->dropped = 0u;
@@ -592,6 +601,7 @@ __device__ __forceinline__ f3 gather_record(const WaveArgs& a, const GatherQuery
     const float dd = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
     if (dd > r2) return mk(0.f);
     const uint32_t b = a.sp.sflags[rec];
+    if (b & SPPM_VOL) return mk(0.f);                               // a record in a volume is the volume's gather's
     if ((g.my & 0xffu) + 1u + (b & SPPM_B_MASK) > a.u.maxbounce + 1u) return mk(0.f);
     const f3 pn = unoct(a.sp.snrm[rec]);
     const float nd = __fadd_rn(__fadd_rn(__fmul_rn(pn.x, g.nrm.x), __fmul_rn(pn.y, g.nrm.y)), __fmul_rn(pn.z, g.nrm.z));
@@ -810,7 +820,7 @@ __global__ void __launch_bounds__(256, 2) k_gather(WaveArgs a) {
 }
 
 cudaError_t launch_sppm_begin(const WaveArgs& a, cudaStream_t s) {
-    k_sppm_begin<<<1, 32, 0, s>>>(a.sp.dev, a.ctr, a.u.sppm_r1, a.u.sppm_alpha, a.sp.cap);
+    k_sppm_begin<<<1, 32, 0, s>>>(a.sp.dev, a.ctr, a.u.sppm_r1, a.u.sppm_alpha, a.sp.cap, a.u.sppm_r1v);
     return cudaGetLastError();
 }
 cudaError_t launch_lt_build(const WaveArgs& a, cudaStream_t s) {

@@ -258,6 +258,56 @@ __global__ void __launch_bounds__(256) k_sort_scatter(const uint32_t* __restrict
 // ------------------------------------------------------------------------------------------------------------
 struct ShadowOut { bool valid, emit, face; f3 org, dir, rad; float n, dist; };
 
+// THE GATHER IN A VOLUME (sppm.js:497-511 sppmGatherVolume through sppmWalk :305-360): at a camera ray's collision in a
+// scattering material, the records photons stored at their own collisions (SPPM_VOL) within R in the eight cells of
+// the volume's grid round x, each through the phase function from the way it came to the way to the camera,
+// sum p(l . v) Phi / (sigma 4/3 pi R^3); a cell's records whole while their count is within its share of the budget,
+// else m of its sub-lists from a drawn start, each record then weighing 32 / m; the walk cut at the hard cap.
+#define SPPM_GATHER_SALT 0x53505031u            // the map's own stream (wavefront.js:1186): shade's draws do not move
+__device__ __forceinline__ f3 volume_gather(const WaveArgs& a, f3 x, f3 v, uint32_t bc, float g, float sigma, Rng& rng) {
+    const SppmDev* d = a.sp.dev;
+    const uint32_t nrec = min(d->count, d->cap);
+    if (nrec == 0u || !(sigma > 0.f)) return mk(0.f);
+    const float csz = d->vcell, r2 = d->vr2;
+    const float gx[3] = {__fdiv_rn(x.x, csz), __fdiv_rn(x.y, csz), __fdiv_rn(x.z, csz)};
+    int32_t c0[3], sd[3];
+    for (int k = 0; k < 3; k++) {
+        c0[k] = (int32_t)floorf(gx[k]);
+        sd[k] = __fsub_rn(gx[k], floorf(gx[k])) >= 0.5f ? 1 : -1;
+    }
+    const uint32_t budget = a.u.sppm_budget, share = max(1u, budget / 8u), hard = SPPM_VISIT_HARD * budget;
+    f3 sum = mk(0.f);
+    uint32_t visits = 0;
+    bool cut = false;
+    for (uint32_t k = 0; k < 8u && !cut; k++) {
+        const int32_t cx = c0[0] + ((k & 1u) ? sd[0] : 0), cy = c0[1] + ((k & 2u) ? sd[1] : 0),
+                      cz = c0[2] + ((k & 4u) ? sd[2] : 0);
+        const uint32_t h = sppm_hash(cx, cy, cz);
+        const uint32_t a0 = __ldg(&a.sp.heads[h]), a1 = __ldg(&a.sp.heads[h + 1u]), cnt = a1 - a0;
+        const bool whole = cnt <= share;
+        const uint32_t subs = whole ? 1u : max(1u, (SPPM_SUBS * share) / max(cnt, 1u));
+        const float w = whole ? 1.f : (float)SPPM_SUBS / (float)subs;
+        const uint32_t start = min((uint32_t)(rng.next().x * (float)SPPM_SUBS), SPPM_SUBS - 1u);
+        for (uint32_t j = 0; j < subs && !cut; j++) {
+            const uint32_t s = (start + j) % SPPM_SUBS;
+            const uint32_t lo = whole ? a0 : __ldg(&a.sp.start[h * SPPM_SUBS + s]);
+            const uint32_t hi = whole ? a1 : __ldg(&a.sp.start[h * SPPM_SUBS + s + 1u]);
+            for (uint32_t q = lo; q < hi; q++) {
+                if (visits >= hard) { cut = true; break; }
+                visits++;
+                const uint32_t b = a.sp.sflags[q];
+                if (!(b & SPPM_VOL) || bc + (b & SPPM_B_MASK) > a.u.maxbounce + 1u) continue;
+                const float4 pp = a.sp.spos[q];
+                if (cell_of(pp.x, csz) != cx || cell_of(pp.y, csz) != cy || cell_of(pp.z, csz) != cz) continue;
+                const float dx = __fsub_rn(pp.x, x.x), dy = __fsub_rn(pp.y, x.y), dz = __fsub_rn(pp.z, x.z);
+                if (__fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz)) > r2) continue;
+                sum = sum + xyz(a.sp.spow[q]) * (w * hg_eval(dot(unoct(a.sp.sdir[q]), v), g));
+            }
+        }
+    }
+    return sum * (d->inv_vol / sigma);
+}
+
 template <bool GUIDE>
 __device__ __forceinline__ void shade_surface(const WaveArgs& a, const st_material* sm, float4 surf,
                                               f3& pos, f3& dir, float& ltot, float& n, f3& beta, float& sunmis,
@@ -636,7 +686,7 @@ __global__ void __launch_bounds__(256) k_shade(WaveArgs a, int nxt, int side, in
                                     (u.lt_on && (m4.y & (META_CAND | META_SPEC)) == (META_CAND | META_SPEC))) &&
                                    sppm_covers(u, pos, dir);
                 rad = rad + beta * (owned ? env_sky(u, dir) : env_radiance(u, dir)) * sunmis;
-            } else if (state == RAY_ACTIVE || state == RAY_SCATTER) {
+            } else if (state == RAY_ACTIVE || state == RAY_SCATTER || state == RAY_GATHER) {
                 train_nee = GUIDE && (m4.y & META_TRAIN) != 0u;       // light found past a record's vertex counts
                 if (a.em.on) emw = a.em.w[slot];
                 if (a.lf.n) lp = a.pb.lprev[slot];
@@ -644,7 +694,36 @@ __global__ void __launch_bounds__(256) k_shade(WaveArgs a, int nxt, int side, in
                 Rng rng = path_rng(sample_seed(u.seed, a.ctr->sample + j), tile, 1u + seg);
                 seg += 1;
                 float absL = __uint_as_float(m4.w);                   // absorbAlong: ltot on arrival at the last vertex
-                if (state == RAY_SCATTER) {
+                if (state == RAY_GATHER) {
+                    // THE MAP GATHERED AT A COLLISION (haze.js:692-707 mediumGathered; wavefront.js:1179-1183): the
+                    // throughput absorbed to here, the photons' in-scattered light over n^2, then turned there as the
+                    // march would have -- a vertex now, the map's D: a bounce, its lens field moved on, light sampling's
+                    // MIS halves cleared, its next flight drawn from here
+                    const uint32_t med = m4.z >> MEDIUM_SHIFT;
+                    const st_material& mm = sm[min(med, u.n_mats - 1u)];
+                    const float sd = mm.scatter_distance, sig = sd > 0.f ? 1.f / sd : 0.f;
+                    const float g = clampf(mm.scatter_g, -0.95f, 0.95f);
+                    if (mm.attenuation > 0.f) {
+                        const float dl = fmaxf(ltot - absL, 0.f) / fmaxf(n, 1e-4f) / mm.attenuation;
+                        beta = beta * mk(__expf(logf(fminf(fmaxf(mm.base[0], 1e-6f), 1.f)) * dl),
+                                         __expf(logf(fminf(fmaxf(mm.base[1], 1e-6f), 1.f)) * dl),
+                                         __expf(logf(fminf(fmaxf(mm.base[2], 1e-6f), 1.f)) * dl));
+                    }
+                    m4.w = __float_as_uint(ltot);
+                    Rng grng = path_rng(sample_seed(u.seed, a.ctr->sample + j), tile, SPPM_GATHER_SALT + (seg - 1u));
+                    const f3 Lv = volume_gather(a, pos, dir, bounces + 1u, g, sig, grng);
+                    rad = rad + beta * Lv * (1.f / fmaxf(n * n, 1e-8f));
+                    if (Lv.x != 0.f || Lv.y != 0.f || Lv.z != 0.f) atomicAdd(&a.sp.dev->vgathers, 1u);
+                    state = RAY_ACTIVE;
+                    bounces += 1;
+                    m4.y = (m4.y & ~((3u << META_LENS_SHIFT) | META_CAND | META_SPEC)) | (2u << META_LENS_SHIFT);
+                    const float4 rh = rng.next();
+                    dir = hg_sample(dir, g, rh.x, rh.y);
+                    sunmis = 1.f;
+                    emw = 1.f;
+                    lp = make_float2(-1.f, ltot);
+                    if (last || bounces > u.maxbounce) state = RAY_TERMINATED;
+                } else if (state == RAY_SCATTER) {
                     m4.w = __float_as_uint(ltot);
                     shade_medium(a, pos, dir, beta, sunmis, bounces, state, n, rng, last != 0, sh, emw, ltot, lp);
                     // haze.js:539: the air is no delta event (out of the map's class); light tracing's class begins

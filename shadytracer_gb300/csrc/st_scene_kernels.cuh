@@ -19,6 +19,7 @@
 #pragma once
 #include "st_emit.cuh"
 #include "st_kernels.cuh"
+#include "st_sppm_dev.cuh"
 
 namespace st {
 
@@ -34,6 +35,7 @@ struct TableScene {
     __device__ static __forceinline__ SceneHit full(const DPrim* sp, uint32_t n, f3 p) { return scene_full(sp, n, p); }
 };
 
+#define ST_SALT_VOL_STORE 0x564F4C53u      // a photon's record in a volume: its sub-list (haze.js mediumStore)
 // a scattering material's walk draws from the path's own streams (a photon's from its id), by the path's steps so far
 __device__ __forceinline__ Rng walk_rng(const WaveArgs& a, uint32_t slot, uint32_t id, uint32_t salt) {
     const Uni& u = a.u;
@@ -76,7 +78,10 @@ __global__ void __launch_bounds__(256, 4) k_march(WaveArgs a, int cur, int nxt, 
     f3 pos = mk(0.f), dir = mk(0.f);
     float ltot = 0.f, n = 1.f, tmax = 0.f;
     float wsig = 0.f, wg = 0.f;                     // the walk's medium: its scattering coefficient (0: none) and g
-    uint32_t wid = 0;
+    uint32_t wid = 0, wmed = 0;
+    uint32_t wmap = 0;                              // the photon map in the volume: 1 a photon that stores at its
+                                                    // collisions, 2 a camera ray that gathers at its first
+    float wabs = 0.f;                               // absLtot: where the ray arrived last (its absorption since)
     bool walked = false;                            // a collision turned the ray in this launch
     uint32_t steps = 0, evals_here = 0;
     uint32_t wpos = 0, wend = 0;
@@ -110,11 +115,23 @@ __global__ void __launch_bounds__(256, 4) k_march(WaveArgs a, int cur, int nxt, 
                     wsig = 0.f;
                     walked = false;
                     wid = m4.x;
+                    wmap = 0u;
                     if (MEDIA && a.u.scatter_on) {                    // the medium the ray is in, if it scatters
                         const uint32_t med = m4.z >> MEDIUM_SHIFT;
                         if (med != 0u && med < a.u.n_mats && (m4.y & META_PROBE) == 0u) {
                             const float sd = a.mats[med].scatter_distance;
                             if (sd > 0.f) { wsig = 1.f / sd; wg = clampf(a.mats[med].scatter_g, -0.95f, 0.95f); }
+                        }
+                        wmed = med;
+                        wabs = __uint_as_float(m4.w);
+                        // the map in the volume (haze.js:651-690): a photon past a delta event stores at its collisions
+                        // within the bounce cap a gather can accept; a camera ray that came in by delta events alone
+                        // (its lens field 1) gathers at its first
+                        if (wsig > 0.f && a.u.sppm_on) {
+                            if (a.u.photon_pass)
+                                wmap = ((m4.y & META_PASSED) && (m4.y & 0xffu) + 2u <= a.u.maxbounce) ? 1u : 0u;
+                            else
+                                wmap = ((m4.y >> META_LENS_SHIFT) & 3u) == 1u ? 2u : 0u;
                         }
                     }
                     if (MEDIA && wsig > 0.f && tmax == 0.f) {
@@ -151,23 +168,32 @@ __global__ void __launch_bounds__(256, 4) k_march(WaveArgs a, int cur, int nxt, 
         if (__ballot_sync(FULL_MASK, slot != INVALID_SLOT) == 0) break;
 
         // ---- one step ----
-        bool fin = false, more = false;
+        bool fin = false, more = false, vstore = false;
         uint32_t state = RAY_ACTIVE;
         float dh = 0.f;
+        f3 vin = dir;
         if (slot != INVALID_SLOT && MEDIA && wsig > 0.f && ltot >= tmax) {
             // A COLLISION IN THE MATERIAL (haze.js:619-650 mediumArrived, mediumBack, mediumCollide): back to it along
             // the line the ray came, turned by the phase function, its next flight drawn
             pos = pos - dir * ((ltot - tmax) / fmaxf(n, 1e-4f));
             ltot = tmax;
-            Rng wr = walk_rng(a, slot, wid, ST_SALT_WALK_HIT + steps);
-            const float4 r4 = wr.next();
-            dir = hg_sample(dir, wg, r4.x, r4.y);
-            tmax = fmaxf(ltot - logf(1.f - r4.z) / wsig * n, 1e-30f);
-            steps += 1;
-            evals_here += 1;
-            walked = true;
-            if (steps > maxiter) { state = RAY_MAXITER; fin = true; dh = 1e7f; }
-            else if (evals_here >= chunk) more = true;
+            if (wmap == 2u) {
+                // handed to shade, where the map gathers and the ray is turned (wavefront.js:881-892, RAY_GATHER)
+                state = RAY_GATHER;
+                fin = true;
+                dh = 1e7f;
+            } else {
+                Rng wr = walk_rng(a, slot, wid, ST_SALT_WALK_HIT + steps);
+                const float4 r4 = wr.next();
+                vstore = wmap == 1u;                              // a photon's record where it collided
+                dir = hg_sample(dir, wg, r4.x, r4.y);
+                tmax = fmaxf(ltot - logf(1.f - r4.z) / wsig * n, 1e-30f);
+                steps += 1;
+                evals_here += 1;
+                walked = true;
+                if (steps > maxiter) { state = RAY_MAXITER; fin = true; dh = 1e7f; }
+                else if (evals_here >= chunk) more = true;
+            }
         } else if (slot != INVALID_SLOT) {
             // THE STEP CACHE (wavefront.js:901-912): a ball that holds the ray far enough moves it with no distance;
             // a step that carries it past its collision in the haze is taken back to it below, as a distance step's
@@ -217,6 +243,34 @@ __global__ void __launch_bounds__(256, 4) k_march(WaveArgs a, int cur, int nxt, 
             if (state == RAY_SCATTER) {                                 // hazeAt: back to the collision
                 pos = pos - dir * ((ltot - tmax) / fmaxf(n, 1e-4f));
                 ltot = tmax;
+            }
+        }
+        if (MEDIA && a.u.sppm_on && a.u.photon_pass && a.u.scatter_on) {
+            // THE RECORD (haze.js:680-690 mediumStore, sppm.js sppmPut): its point, the way it came, its power with
+            // the absorption since its vertex, its bounce, the volume's flag and a sub-list
+            SppmDev* d = a.sp.dev;
+            const uint32_t at = warp_append(&d->count, vstore);
+            if (vstore) {
+                if (at < d->cap) {
+                    const st_material& mm = a.mats[wmed];
+                    f3 pw = xyz(a.pb.rad[slot]) * xyz(a.pb.beta[slot]);
+                    if (mm.attenuation > 0.f) {
+                        const float dl = fmaxf(ltot - wabs, 0.f) / fmaxf(n, 1e-4f) / mm.attenuation;
+                        pw = pw * mk(__expf(logf(fminf(fmaxf(mm.base[0], 1e-6f), 1.f)) * dl),
+                                     __expf(logf(fminf(fmaxf(mm.base[1], 1e-6f), 1.f)) * dl),
+                                     __expf(logf(fminf(fmaxf(mm.base[2], 1e-6f), 1.f)) * dl));
+                    }
+                    Rng sr = walk_rng(a, slot, wid, ST_SALT_VOL_STORE + steps);
+                    const uint32_t sub = min((uint32_t)(sr.next().y * (float)SPPM_SUBS), SPPM_SUBS - 1u);
+                    a.sp.pos[at] = make_float4(pos.x, pos.y, pos.z, 0.f);
+                    a.sp.power[at] = make_float4(pw.x, pw.y, pw.z, 0.f);
+                    a.sp.dir_oct[at] = oct_word(-vin);
+                    a.sp.nrm_oct[at] = 0u;
+                    a.sp.flags[at] = ((a.pb.meta[slot].y & 0xffu) + 1u) | (sub << SPPM_SUB_SHIFT) | SPPM_VOL;
+                    atomicAdd(&d->vstores, 1u);
+                } else {
+                    atomicAdd(&d->dropped, 1u);
+                }
             }
         }
         uint32_t qp = warp_append(&a.ctr->hitCount, fin);

@@ -38,9 +38,9 @@ __global__ void __launch_bounds__(256) k_sppm_key(const float4* __restrict__ pos
                                                   uint32_t* __restrict__ bucket, uint32_t* __restrict__ rank,
                                                   uint32_t* __restrict__ counts) {
     const uint32_t n = min(d->count, d->cap);
-    const float cell = d->cell;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         float4 p = pos[i];
+        const float cell = (flags[i] & SPPM_VOL) ? d->vcell : d->cell;   // a volume's records on their own cells
         uint32_t h = sppm_hash(cell_of(p.x, cell), cell_of(p.y, cell), cell_of(p.z, cell));
         uint32_t b = h * SPPM_SUBS + ((flags[i] >> SPPM_SUB_SHIFT) & (SPPM_SUBS - 1));
         key[i] = h;
@@ -212,7 +212,7 @@ __global__ void __launch_bounds__(128) k_sppm_gather(const float* __restrict__ q
                 float dd = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
                 if (dd > r2) continue;
                 const uint32_t b = sflags[q];
-                if (bc + (b & SPPM_B_MASK) > maxbounce + 1) continue;
+                if ((b & SPPM_VOL) || bc + (b & SPPM_B_MASK) > maxbounce + 1) continue;
                 f3 pn = unoct(snrm[q]);
                 float nd = __fadd_rn(__fadd_rn(__fmul_rn(pn.x, nq.x), __fmul_rn(pn.y, nq.y)), __fmul_rn(pn.z, nq.z));
                 if (nd < 0.9f) continue;
@@ -329,7 +329,7 @@ int st_sppm_build(st_ctx* ctx, const float* pos, const float* power, const uint3
     }
     s.wave = false;
     SppmDev hd{};
-    hd.count = n; hd.cap = s.cap; hd.cell = cell;
+    hd.count = n; hd.cap = s.cap; hd.cell = cell; hd.vcell = cell;   // (records given here are a surface's)
     if (!ck(cudaMemcpyAsync(s.dev, &hd, sizeof(hd), cudaMemcpyHostToDevice, st), "photon upload") || !ck(cudaMemcpyAsync(s.pos, p4.data(), (size_t)n * 16, cudaMemcpyHostToDevice, st), "photon upload") ||
         !ck(cudaMemcpyAsync(s.power, w4.data(), (size_t)n * 16, cudaMemcpyHostToDevice, st), "photon upload") ||
         !ck(cudaMemcpyAsync(s.nrm_oct, nrm_oct, (size_t)n * 4, cudaMemcpyHostToDevice, st), "photon upload") ||

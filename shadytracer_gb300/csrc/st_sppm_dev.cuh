@@ -12,6 +12,7 @@
 #define SPPM_SUB_SHIFT 16u
 #define SPPM_B_MASK 0xFFFFu
 #define SPPM_NORMAL_DOT 0.9f
+#define SPPM_VOL 0x40000000u              // a record stored where a photon collided inside a medium (sppm.js:93-95)
 #define SPPM_BUDGET 512u                  // records a gather may walk before it subsamples (sppm.js SPPM_VISIT)
 #define LT_MIN_ALPHA 0.05f                // from it up a glossy lobe is evaluable (tracebasics.js:299)
 

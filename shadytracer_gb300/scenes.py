@@ -1211,3 +1211,30 @@ def milky_spheres(width=64, height=48, maxbounce=12, seed=1, furnace=False, maxi
     s.params.maxiter = maxiter
     s.view = look_at((0.0, -2.6, 1.2), (0.0, 0.0, 0.3), 40.0, width / height)
     return s
+
+
+def milky_slab(width=64, height=48, photons=200_000, r1=0.01, r1v=0.02, sun_diameter=5.0, seed=1, sppm=True,
+               maxiter=4000):
+    """The photon map in the volume: a slab of milky glass (n 1.5, 0.6 x 0.6 x 0.1 m, mean free path 3 cm, g 0.5) 0.25 m
+    over a grey floor, lit by the sun alone (50 degrees up; its disc `sun_diameter` wide so the camera's own paths find
+    it through the walk often enough to check the map against), seen from the side and above. With the map on, the sun's
+    photons walk the slab and store where they collide; a camera ray that came in through the slab's face gathers them
+    at its first collision; the floor under it gathers what the slab let through."""
+    milky = material(base=(1, 1, 1), roughness=0.0, specular=0.5, transmission=1.0, ior=1.5, scatter_distance=0.03,
+                     scatter_g=0.5)
+    s = Scene([prim(ST_PRIM_PLANE, material=1), prim(ST_PRIM_BOX, pos=(0.0, 0.0, 0.3), params=(0.3, 0.3, 0.05),
+                                                     material=2)],
+              [air(), diffuse((0.6, 0.6, 0.6)), milky], env_radius=10.0, name="milky-slab")
+    s.params = default_params(width=width, height=height, maxbounce=16, sun_elevation=50.0, sun_azimuth=30.0,
+                              sun_illuminance=100000.0, sun_diameter=sun_diameter, sky_luminance=0.0,
+                              ground_luminance=0.0, seed=seed)
+    s.params.maxiter = maxiter
+    if sppm:
+        s.params.sppm = 1
+        s.params.sppm_photons = photons
+        s.params.sppm_r1 = r1
+        s.params.sppm_r1_volume = r1v
+        s.params.sppm_alpha = 0.7
+        s.params.sppm_half = 0.6
+    s.view = look_at((0.0, -1.4, 0.75), (0.0, 0.0, 0.2), 45.0, width / height)
+    return s

@@ -80,7 +80,8 @@ class StParams(C.Structure):
                 ("lt", C.c_uint32), ("lt_photons", C.c_uint32),
                 ("env_mode", C.c_uint32), ("sun_outside", C.c_float), ("sky_turbidity", C.c_float),
                 ("studio_illuminance", C.c_float), ("studio_top", C.c_float), ("studio_color", C.c_float * 3),
-                ("lt_emit_share", C.c_float), ("env_cache", C.c_uint32), ("env_cache_size", C.c_uint32)]
+                ("lt_emit_share", C.c_float), ("env_cache", C.c_uint32), ("env_cache_size", C.c_uint32),
+                ("sppm_r1_volume", C.c_float)]
 
 
 class StView(C.Structure):
@@ -197,6 +198,7 @@ def default_params(**kw):
     p.emit_off = 0
     p.env_cache = 1                   # the environment's presets from a texture (UniformSpec envCache: on)
     p.env_cache_size = 2048
+    p.sppm_r1_volume = 0.0
     for k, v in kw.items():
         if not hasattr(p, k):
             raise KeyError(k)

@@ -78,3 +78,28 @@ def test_a_clear_volume_is_the_glass_alone():
             rt.step(4)
             out.append(rt.read_accum()[0])
     assert np.array_equal(out[0], out[1])
+
+
+def render(s, n):
+    with create_path_tracer(s, device=0) as rt:
+        rt.step(n)
+        rgb, V, S, cnt = rt.read_accum()
+        return rgb @ LUMA, V, S, rt.counters()
+
+
+def test_the_map_in_the_volume_matches_the_oracle():
+    """The photons' records where they collide in the slab, gathered at the camera's first collision: the GPU's picture
+    against the oracle's, band by band within their error bars, and both against the camera's own paths."""
+    s = scenes.milky_slab(sppm=True)
+    L, V, S, c = render(s, 16)
+    assert c["nonfinite"] == 0
+    ref = oracle.render(s, 16)
+    Lr = ref.luma()
+    sd = np.sqrt(se_of(V, S) ** 2 + np.nan_to_num(ref.se()) ** 2)
+    for r0 in range(0, 48, 8):
+        band = slice(r0, r0 + 8)
+        e = np.sqrt(np.sum(sd[band] ** 2)) / sd[band].size
+        assert abs(L[band].mean() - Lr[band].mean()) < 4 * e + 0.01 * Lr[band].mean(), (r0, L[band].mean(), Lr[band].mean())
+    P, Vp, Sp, _ = render(scenes.milky_slab(sppm=False), 512)
+    e = math.hypot(np.sqrt(np.sum(se_of(V, S) ** 2)) / V.size, np.sqrt(np.sum(se_of(Vp, Sp) ** 2)) / Vp.size)
+    assert abs(L.mean() - P.mean()) < 4 * e + 0.01 * P.mean(), (L.mean(), P.mean())

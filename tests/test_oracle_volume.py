@@ -75,3 +75,25 @@ def test_a_clear_volume_is_the_glass_alone():
         s2.materials[i].scatter_g = 0.9
     c = oracle.render(s2, 2).rgb
     assert np.array_equal(b, c) and not np.allclose(a, b)
+
+
+def test_the_map_in_the_volume_agrees_with_the_camera_alone():
+    """The photon map in the volume (sppm.js sppmGatherVolume, haze.js mediumStore): a milky slab lit by the sun only;
+    with the map on, the sun's photons store where they collide in it and a camera ray that came in through its face
+    gathers them at its first collision (and the floor under it, what the slab let through); with it off, the camera's
+    paths find the sun through the walk by chance (its disc made 5 degrees wide). The same picture on average."""
+    a = oracle.render(scenes.milky_slab(sppm=True), 16)
+    b = oracle.render(scenes.milky_slab(sppm=False), 512)
+    A, B = a.luma(), b.luma()
+    se_b = np.sqrt(np.sum(np.nan_to_num(b.se()) ** 2)) / B.size
+    se_a = np.sqrt(np.sum(np.nan_to_num(a.se()) ** 2)) / A.size
+    assert abs(A.mean() - B.mean()) < 4 * math.hypot(se_a, se_b) + 0.01 * B.mean(), (A.mean(), B.mean(), se_a, se_b)
+
+
+def test_the_slab_glows_from_the_map_alone():
+    """With the sun's true disc (0.53 degrees) the camera's own paths almost never find it through the walk; the map's
+    photons carry its light into the slab, which glows."""
+    a = oracle.render(scenes.milky_slab(sppm=True, sun_diameter=0.53), 8).luma()
+    b = oracle.render(scenes.milky_slab(sppm=False, sun_diameter=0.53), 8).luma()
+    rows = slice(8, 32)                                        # the slab's face and the floor it shades
+    assert a[rows].mean() > 1.15 * b[rows].mean(), (a[rows].mean(), b[rows].mean())
