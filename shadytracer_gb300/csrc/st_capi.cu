@@ -417,8 +417,12 @@ static bool has_emitters(const st_ctx* ctx) {
 
 static int ensure_wave(st_ctx* ctx) {
     if (photons_run(ctx)) {
-        // the map's records (light tracing alone stores none) and the emission map's counts
-        int rc = sppm_ensure(ctx, sppm_runs(ctx) ? sppm_photons(ctx) : 1024u);
+        // the map's records (light tracing alone stores none) and the emission map's counts: a record a photon at
+        // most on surfaces; in a scene that scatters inside a material, one at each collision too -- room for 32 a
+        // photon, at most 64 M records, a sample's stores past its share thinned without bias (k_sppm_begin's keep)
+        uint32_t need = sppm_runs(ctx) ? sppm_photons(ctx) : 1024u;
+        if (sppm_runs(ctx) && make_uni(ctx).scatter_on) need = (uint32_t)std::min<uint64_t>((uint64_t)need * 32u, 64u << 20);
+        int rc = sppm_ensure(ctx, need);
         if (rc) return rc;
         if (sppm_runs(ctx)) ctx_ext(ctx).sppm.wave = true;
     }

@@ -108,6 +108,10 @@ struct SppmDev {
     // in the volume (sppm.js sppmRadiusVolume): the radius, its records' cell (2R), 3 / (4 pi R^3), R^2
     float vr, vcell, inv_vol, vr2;
     uint32_t vstores, vgathers;
+    // ...and its thinning (sppm.js:150-158 sppmKeep): the share of a sample's collisions kept as records, each then
+    // carrying its power over the share -- from the last sample's demand, so the records fit half the capacity
+    float vkeep;
+    uint32_t vdemand;
 };
 struct SppmBufs {
     SppmDev* dev = nullptr;

@@ -56,6 +56,9 @@ __global__ void k_sppm_begin(SppmDev* __restrict__ d, const DevCtr* __restrict__
     d->inv_vol = (float)(3.0 / (4.0 * 3.14159265358979323846 * rv * rv * rv));
     d->vstores = 0u;
     d->vgathers = 0u;
+    const float room = 0.5f * (float)cap;
+    d->vkeep = (k > 1u && (float)d->vdemand > room) ? room / (float)d->vdemand : 1.f;
+    d->vdemand = 0u;
     d->count = 0u;
     d->cap = cap;
     d->dropped = 0u;

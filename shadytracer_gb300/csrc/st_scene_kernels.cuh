@@ -36,6 +36,7 @@ struct TableScene {
 };
 
 #define ST_SALT_VOL_STORE 0x564F4C53u      // a photon's record in a volume: its sub-list (haze.js mediumStore)
+#define ST_SALT_VOL_KEEP 0x4B454550u       // ...and whether the sample's thinning keeps it
 // a scattering material's walk draws from the path's own streams (a photon's from its id), by the path's steps so far
 __device__ __forceinline__ Rng walk_rng(const WaveArgs& a, uint32_t slot, uint32_t id, uint32_t salt) {
     const Uni& u = a.u;
@@ -249,11 +250,16 @@ __global__ void __launch_bounds__(256, 4) k_march(WaveArgs a, int cur, int nxt, 
             // THE RECORD (haze.js:680-690 mediumStore, sppm.js sppmPut): its point, the way it came, its power with
             // the absorption since its vertex, its bounce, the volume's flag and a sub-list
             SppmDev* d = a.sp.dev;
+            warp_append(&d->vdemand, vstore);                            // the collisions that would store
+            if (vstore) {                                                // ...each kept with the sample's share
+                Rng kr = walk_rng(a, slot, wid, ST_SALT_VOL_KEEP + steps);
+                vstore = kr.next().x < d->vkeep;
+            }
             const uint32_t at = warp_append(&d->count, vstore);
             if (vstore) {
                 if (at < d->cap) {
                     const st_material& mm = a.mats[wmed];
-                    f3 pw = xyz(a.pb.rad[slot]) * xyz(a.pb.beta[slot]);
+                    f3 pw = xyz(a.pb.rad[slot]) * xyz(a.pb.beta[slot]) * (1.f / d->vkeep);
                     if (mm.attenuation > 0.f) {
                         const float dl = fmaxf(ltot - wabs, 0.f) / fmaxf(n, 1e-4f) / mm.attenuation;
                         pw = pw * mk(__expf(logf(fminf(fmaxf(mm.base[0], 1e-6f), 1.f)) * dl),

@@ -81,10 +81,17 @@ def test_a_clear_volume_is_the_glass_alone():
 
 
 def render(s, n):
+    import ctypes as C
+    from shadytracer_gb300 import st_types as T
     with create_path_tracer(s, device=0) as rt:
         rt.step(n)
         rgb, V, S, cnt = rt.read_accum()
-        return rgb @ LUMA, V, S, rt.counters()
+        c = rt.counters()
+        if s.params.sppm:
+            stt = T.StSppmStats()
+            assert rt.L.st_sppm_stats_read(rt.ctx, C.byref(stt)) == 0
+            c["stored"], c["dropped"] = stt.stored, stt.cut
+        return rgb @ LUMA, V, S, c
 
 
 def test_the_map_in_the_volume_matches_the_oracle():
@@ -93,6 +100,8 @@ def test_the_map_in_the_volume_matches_the_oracle():
     s = scenes.milky_slab(sppm=True)
     L, V, S, c = render(s, 16)
     assert c["nonfinite"] == 0
+    # records where the photons collided in the slab too, none dropped
+    assert c["stored"] > s.params.sppm_photons and c["dropped"] == 0, (c["stored"], c["dropped"])
     ref = oracle.render(s, 16)
     Lr = ref.luma()
     sd = np.sqrt(se_of(V, S) ** 2 + np.nan_to_num(ref.se()) ** 2)
