@@ -633,6 +633,7 @@ static cudaError_t record_wave(st_ctx* ctx, const WaveArgs& a) {
     }
     ctx->rec_launches++;
     if (a.gd.train && (e = guide_wave_begin(ctx, a.slots, s))) return e;
+    if (a.gd.on && (e = guide_stamps_clear(ctx, ctx->nv * ctx->P, s))) return e;
     if ((e = launch_iter_begin(a, 0, 1, 1, s))) return e;
     if ((e = timed("genrays", [&] { return launch_genrays(a, ctx->sms, s); }))) return e;
     int cur = 0;

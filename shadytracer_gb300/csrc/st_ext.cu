@@ -9,7 +9,8 @@ void ext_free(StExt& e) {
     for (void* p : ps)
         if (p) cudaFree(p);
     GuideState& g = e.guide;
-    void* gs[] = {g.param, g.grad, g.m1, g.m2, g.wbf, (void*)g.dev, (void*)g.samp, g.act, g.mix, (void*)g.rec, g.acc};
+    void* gs[] = {g.param, g.grad, g.m1, g.m2, g.wbf, (void*)g.dev, (void*)g.samp, g.act, g.mix, (void*)g.stamp,
+                  (void*)g.rec, g.acc};
     for (void* p : gs)
         if (p) cudaFree(p);
     EmitState& m = e.emit;

@@ -70,6 +70,7 @@ struct GuideState {
     st::GuideSample* samp = nullptr;
     uint16_t* act = nullptr;
     uint2* mix = nullptr;
+    uint32_t* stamp = nullptr;       // per pixel of the wave's views: its mixture inferred this wave (1) or not (0)
     uint32_t mix_cap = 0;
     st::GuideRec* rec = nullptr;
     float* acc = nullptr;
@@ -80,6 +81,7 @@ int guide_ensure(st_ctx* ctx, uint32_t queue_cap, uint32_t slots, uint32_t seed)
 int guide_upload(st_ctx* ctx, const float* h);
 st::GuideBufs guide_bufs(st_ctx* ctx, uint32_t on, uint32_t train, float alpha, uint32_t slots);
 cudaError_t guide_wave_begin(st_ctx* ctx, uint32_t slots, cudaStream_t st);
+cudaError_t guide_stamps_clear(st_ctx* ctx, uint32_t pixels, cudaStream_t st);
 cudaError_t guide_train_launch(st_ctx* ctx, float lr, int sms, cudaStream_t st, int* launches);
 cudaError_t guide_eval_launch(st_ctx* ctx, uint32_t n, float* d_raw, uint2* d_mix, cudaStream_t st);
 int guide_eval(st_ctx* ctx, const float* pos, const float* nrm, uint32_t n, float* raw, float* mix);

@@ -2,7 +2,7 @@
 // batch made from the camera paths' records at a wave's end, and the training step (forward and backward on the
 // tensor cores, the weight gradients as one GEMM over the batch, Adam), with the C ABI's st_mlp_* entry points.
 //
-//   k_guide_infer     after the surface kernel: each guided vertex's mixture (8 packed vMF lobes), 16 vertices a warp
+//   k_guide_infer     after the surface kernel: one mixture (8 packed vMF lobes) a pixel a wave, at its first guided vertex
 //   k_guide_collect   a wave's end: each path's record -> (position, normal, direction, f cos L_in / pdf)
 //   k_guide_train     a mini-batch: forward, the loss's gradient at the 40 outputs, backward to the 48 inputs; the
 //                     activations and their gradients (BF16) for the weight GEMM; the hash grid's gradient by atomics
@@ -471,9 +471,15 @@ int guide_ensure(st_ctx* ctx, uint32_t queue_cap, uint32_t slots, uint32_t seed)
     }
     if (queue_cap > g.mix_cap) {
         if (g.mix) cudaFree(g.mix);
+        if (g.stamp) cudaFree(g.stamp);
         g.mix = nullptr;
+        g.stamp = nullptr;
         g.mix_cap = 0;
-        if (cudaMalloc(&g.mix, (size_t)queue_cap * GUIDE_LOBES * sizeof(uint2))) return fail("cudaMalloc learned proposal");
+        if (cudaMalloc(&g.mix, (size_t)queue_cap * GUIDE_LOBES * sizeof(uint2)) ||
+            cudaMalloc(&g.stamp, (size_t)queue_cap * 4) ||
+            cudaMemset(g.mix, 0, (size_t)queue_cap * GUIDE_LOBES * sizeof(uint2)) ||
+            cudaMemset(g.stamp, 0, (size_t)queue_cap * 4))
+            return fail("cudaMalloc learned proposal");
         g.mix_cap = queue_cap;
     }
     if (slots > g.rec_cap) {
@@ -511,6 +517,7 @@ GuideBufs guide_bufs(st_ctx* ctx, uint32_t on, uint32_t train, float alpha, uint
     b.table = reinterpret_cast<const float2*>(g.param + GUIDE_NW);
     b.wbf = g.wbf;
     b.mix = g.mix;
+    b.stamp = g.stamp;
     b.rec = g.rec;
     b.acc = g.acc;
     b.samp = g.samp;
@@ -519,6 +526,11 @@ GuideBufs guide_bufs(st_ctx* ctx, uint32_t on, uint32_t train, float alpha, uint
     const double f = std::min(1.0, (double)GUIDE_CAP / std::max(slots, 1u));
     b.keep = f >= 1.0 ? 0xffffffffu : (uint32_t)(f * 4294967296.0);
     return b;
+}
+// a wave's start with guiding on: no pixel's mixture inferred yet
+cudaError_t guide_stamps_clear(st_ctx* ctx, uint32_t pixels, cudaStream_t st) {
+    GuideState& g = ctx_ext(ctx).guide;
+    return cudaMemsetAsync(g.stamp, 0, (size_t)std::min(pixels, g.mix_cap) * 4, st);
 }
 // a wave's start: the records cleared, the batch emptied
 cudaError_t guide_wave_begin(st_ctx* ctx, uint32_t slots, cudaStream_t st) {

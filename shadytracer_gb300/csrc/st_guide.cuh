@@ -114,6 +114,10 @@ __device__ __forceinline__ bool guide_vertex(const st_material& m) {
 __device__ __forceinline__ float guide_share(float alpha, const uint32_t* step, uint32_t train) {
     return train ? alpha * fminf(1.f, (float)*step / GUIDE_RAMP) : alpha;
 }
+// a path's pixel among the wave's views (its slot's frame, its pixel): the one mixture its first vertex samples from
+__device__ __forceinline__ uint32_t guide_pixel(const Uni& u, uint32_t slot, uint32_t pix) {
+    return slot_view(u, slot) * u.P + pix;
+}
 
 // ---------------------------------------------------------------------------------------------------------------
 // THE MIXTURE, as the sampler reads it: per lobe the mean direction (octahedral, two 16-bit snorms) and kappa and

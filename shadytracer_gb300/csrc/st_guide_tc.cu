@@ -140,7 +140,10 @@ __device__ __forceinline__ void tc_end(TcCta& c, uint64_t* mbar, bool failed, De
     }
 }
 
-// INFERENCE OVER THE HIT QUEUE: per round the block's 128 entries whose vertex is guided, compacted, one tile
+// INFERENCE OVER THE HIT QUEUE: per round the block's 128 entries whose vertex is guided, compacted, one tile. ONE A
+// PIXEL A WAVE: a pixel's paths meet their first vertices within its footprint, and the first of them to reach the
+// network claims the pixel (its stamp) and has its mixture inferred there; the pixel's other paths sample from that
+// mixture -- a density fixed before they draw, so the one-sample MIS estimator stays unbiased whichever vertex made it
 __global__ void __launch_bounds__(128) k_guide_infer_tc(WaveArgs a) {
     extern __shared__ __align__(1024) unsigned char smem[];
     __shared__ __align__(8) uint64_t mbar, mbar_t;
@@ -163,8 +166,9 @@ __global__ void __launch_bounds__(128) k_guide_infer_tc(WaveArgs a) {
             const uint32_t slot = a.q.hit[q];
             const uint32_t my = a.pb.meta[slot].y;
             const uint32_t ids = __float_as_uint(a.q.hsurf[q].w);
-            if (((my >> 16) & 0xffu) == RAY_ACTIVE && (my & 0xffu) == 0u && ids != SURF_LEAVING && a.q.hitd[q] >= 0.f)
-                want = guide_vertex(sm[ids & 0xffffu]);
+            if (((my >> 16) & 0xffu) == RAY_ACTIVE && (my & 0xffu) == 0u && ids != SURF_LEAVING && a.q.hitd[q] >= 0.f &&
+                guide_vertex(sm[ids & 0xffffu]))
+                want = atomicExch(&a.gd.stamp[guide_pixel(u, slot, a.pb.meta[slot].x)], 1u) == 0u;
         }
         const uint32_t m = __ballot_sync(FULL_MASK, want);
         if (lane == 0u) wcnt[warp] = __popc(m);
@@ -190,7 +194,8 @@ __global__ void __launch_bounds__(128) k_guide_infer_tc(WaveArgs a) {
         if (threadIdx.x < n) {
             uint2 out[GUIDE_LOBES];
             guide_decode(y, out);
-            uint2* dst = a.gd.mix + (size_t)list[threadIdx.x] * GUIDE_LOBES;
+            const uint32_t sl = a.q.hit[list[threadIdx.x]];
+            uint2* dst = a.gd.mix + (size_t)guide_pixel(u, sl, a.pb.meta[sl].x) * GUIDE_LOBES;
 #pragma unroll
             for (uint32_t k = 0; k < GUIDE_LOBES; k++) dst[k] = out[k];
         }

@@ -150,7 +150,8 @@ struct GuideBufs {
     float inv_ext = 1.f;
     const float2* table = nullptr;        // hash-grid features, FP32
     const uint16_t* wbf = nullptr;        // the network's weights, BF16 bits, [out][in] row-major, W1 W2 W3 W4
-    uint2* mix = nullptr;                 // 8 packed lobes a hit-queue entry
+    uint2* mix = nullptr;                 // 8 packed lobes a pixel of the wave's views (view * P + pixel)
+    uint32_t* stamp = nullptr;            // ...and whether a path of the pixel has had it inferred this wave
     GuideRec* rec = nullptr;              // a path's record (by its pixel in the wave's frames)
     float* acc = nullptr;                 // ...and the luminance found after its vertex
     GuideSample* samp = nullptr;          // the training batch

@@ -417,8 +417,10 @@ __device__ __forceinline__ void shade_surface(const WaveArgs& a, const st_materi
     // the network's mixture with probability alpha, else from the BSDF, and weighed by f cos / (alpha q + (1 - alpha)
     // p_bsdf) -- one-sample MIS, so the estimator stays unbiased whatever the network says; the environment's MIS
     // weights take the same combined density on both sides
-    const bool guided = GUIDE && a.gd.on != 0u && !last && !inside && bounces == 1u && guide_vertex(m);
-    const uint2* __restrict__ gmix = a.gd.mix + (size_t)q * GUIDE_LOBES;
+    const uint32_t gpx = GUIDE ? guide_pixel(u, gpix, gpix % u.P) : 0u;
+    const bool guided = GUIDE && a.gd.on != 0u && !last && !inside && bounces == 1u && guide_vertex(m) &&
+                        a.gd.stamp[gpx] != 0u;                        // (its pixel's mixture inferred this wave)
+    const uint2* __restrict__ gmix = a.gd.mix + (size_t)gpx * GUIDE_LOBES;
     const float galpha = guided ? guide_share(a.gd.alpha, &a.gd.dev->step, a.gd.train) : 0.f;
     // the discovered emitters' share of the light samples (materials_pbr.js:1216-1330): 0 while nothing is listed,
     // when the environment's draw is the one it always was
