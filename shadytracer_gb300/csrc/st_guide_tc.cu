@@ -144,17 +144,18 @@ __device__ __forceinline__ void tc_end(TcCta& c, uint64_t* mbar, bool failed, De
 // PIXEL A WAVE: a pixel's paths meet their first vertices within its footprint, and the first of them to reach the
 // network claims the pixel (its stamp) and has its mixture inferred there; the pixel's other paths sample from that
 // mixture -- a density fixed before they draw, so the one-sample MIS estimator stays unbiased whichever vertex made it
+// A CTA stages the weights and takes its tensor memory only at its first round with a vertex to infer: past the
+// wave's first iterations most rounds find none (a pixel's mixture is made once), and such a CTA only scans.
 __global__ void __launch_bounds__(128) k_guide_infer_tc(WaveArgs a) {
     extern __shared__ __align__(1024) unsigned char smem[];
-    __shared__ __align__(8) uint64_t mbar, mbar_t;
+    __shared__ __align__(8) uint64_t mbar;
     __shared__ uint32_t tmem_slot;
     __shared__ uint32_t list[128];
     __shared__ uint32_t wcnt[4];
     const Uni& u = a.u;
     unsigned char* s = smem;
-    st_material* sm = reinterpret_cast<st_material*>(smem + TC_BYTES);
-    if (!stage_table(sm, a.mats, u.n_mats * (uint32_t)sizeof(st_material), &mbar_t, a.ctr)) return;
-    TcCta c = tc_begin(s, a.gd.wbf, &tmem_slot, &mbar);
+    TcCta c{0u, 0u};
+    bool begun = false;
     const uint32_t wl = a.ctr->wait_limit ? a.ctr->wait_limit : WAIT_LIMIT;
     const uint32_t count = a.ctr->hitCount;
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
@@ -167,7 +168,7 @@ __global__ void __launch_bounds__(128) k_guide_infer_tc(WaveArgs a) {
             const uint32_t my = a.pb.meta[slot].y;
             const uint32_t ids = __float_as_uint(a.q.hsurf[q].w);
             if (((my >> 16) & 0xffu) == RAY_ACTIVE && (my & 0xffu) == 0u && ids != SURF_LEAVING && a.q.hitd[q] >= 0.f &&
-                guide_vertex(sm[ids & 0xffffu]))
+                guide_vertex(a.mats[min(ids & 0xffffu, u.n_mats - 1u)]))
                 want = atomicExch(&a.gd.stamp[guide_pixel(u, slot, a.pb.meta[slot].x)], 1u) == 0u;
         }
         const uint32_t m = __ballot_sync(FULL_MASK, want);
@@ -179,6 +180,10 @@ __global__ void __launch_bounds__(128) k_guide_infer_tc(WaveArgs a) {
         if (threadIdx.x == 0u && n) atomicAdd(&a.gd.dev->inferred, n);
         __syncthreads();
         if (n == 0u) continue;                                      // the whole block agrees
+        if (!begun) {
+            c = tc_begin(s, a.gd.wbf, &tmem_slot, &mbar);
+            begun = true;
+        }
         float x[GUIDE_IN];
         if (threadIdx.x < n) {
             const uint32_t qq = list[threadIdx.x];
@@ -200,7 +205,7 @@ __global__ void __launch_bounds__(128) k_guide_infer_tc(WaveArgs a) {
             for (uint32_t k = 0; k < GUIDE_LOBES; k++) dst[k] = out[k];
         }
     }
-    tc_end(c, &mbar, failed, a.ctr);
+    if (begun) tc_end(c, &mbar, failed, a.ctr);
 }
 
 // THE NETWORK AT GIVEN POINTS (st_mlp_eval): the samples' positions and normals in, the 40 outputs and the mixture out
@@ -234,7 +239,7 @@ __global__ void __launch_bounds__(128) k_guide_eval_tc(const GuideSample* __rest
     tc_end(c, &mbar, failed, nullptr);
 }
 
-static size_t tc_infer_smem(uint32_t n_mats) { return TC_BYTES + (size_t)n_mats * sizeof(st_material); }
+static size_t tc_infer_smem(uint32_t) { return TC_BYTES; }
 
 cudaError_t launch_guide_infer(const WaveArgs& a, int sms, cudaStream_t s) {
     const size_t smem = tc_infer_smem(a.u.n_mats);
