@@ -411,18 +411,32 @@ MLP_TRAIN_FLOPS = 3 * MLP_FWD_FLOPS                               # forward, bac
 
 
 def mlp_leg(args, dev):
-    """The learned proposal: the diffuse room lit by the sun's patch (sky almost black), 160 x 90, plain and guided
-    (trained online from the first wave) against a plain render of 8192 samples: relative RMSE and GPU time at 1024
-    samples; the network's inference (BF16 tensor-core flops a second at the vertices it ran at) and training."""
+    """The learned proposal, plain and guided (trained online from the first wave), 160 x 90, relative RMSE and GPU time
+    at 1024 samples against a plain render of 8192 on seeds of its own, on two rooms: the diffuse room lit by the sun's
+    patch alone (sky almost black: the light every vertex sees is indirect) and the headline's room as configured (the
+    physical sun and sky through the window, the mixed finish: the sky's light through the window is what light
+    sampling's cosine draw finds worst); the network's inference and training on the first."""
+    W, H = (96, 54) if args.small else (160, 90)
+    ref_spp, spp = (1024, 256) if args.small else (8192, 1024)
+    out = {"metric": "relative RMSE at equal samples", "workloads": {}}
+    for name, kw in (("diffuse_sun_patch", dict(finish="diffuse", sky_illuminance=10.0, ground_luminance=1.0)),
+                     ("configured", dict(sky="physical"))):
+        out["workloads"][name] = mlp_workload(args, dev, W, H, spp, ref_spp, kw, stats=name == "diffuse_sun_patch")
+    d = out["workloads"]["diffuse_sun_patch"]
+    for k in ("legs", "rmse_ratio_guided_over_plain", "time_ratio_guided_over_plain", "speedup_to_equal_rmse", "workload"):
+        out[k] = d[k]
+    out["speedup_to_equal_rmse_configured"] = out["workloads"]["configured"]["speedup_to_equal_rmse"]
+    return out
+
+
+def mlp_workload(args, dev, W, H, spp, ref_spp, kw, stats):
     import torch
     from shadytracer_gb300 import scenes
     from shadytracer_gb300.renderer import create_path_tracer
-    W, H = (96, 54) if args.small else (160, 90)
-    ref_spp, spp = (1024, 256) if args.small else (8192, 1024)
     luma = np.array([0.2126, 0.7152, 0.0722])
 
     def scene(guide):
-        s = scenes.sdf_room(width=W, height=H, spp=spp, finish="diffuse", sky_illuminance=10.0, ground_luminance=1.0)
+        s = scenes.sdf_room(width=W, height=H, spp=spp, **kw)
         s.params.guide = guide
         return s
     # the reference on seeds of its own: a plain run on the same seeds would share its first samples with it and read
@@ -442,9 +456,9 @@ def mlp_leg(args, dev):
     se2[ok] = S[ok] * V[ok] / (1 - S[ok])
     ref_noise = float(np.mean(se2))                 # the reference's own variance, taken out of each run's error
     rt.close()
-    out = {"workload": "room24 diffuse, sun patch only (sky 10 lx), %dx%d, %d samples against a %d-sample plain render "
-                       "on seeds of its own (its own noise taken out)" % (W, H, spp, ref_spp),
-           "metric": "relative RMSE at equal samples", "legs": {}}
+    out = {"workload": "room24 %s, %dx%d, %d samples against a %d-sample plain render on seeds of its own (its own "
+                       "noise taken out)" % (", ".join("%s=%s" % kv for kv in kw.items()), W, H, spp, ref_spp),
+           "legs": {}}
     for guide in (0, 1):
         rt = create_path_tracer(scene(guide), device=dev, code=True)
         stream = torch.cuda.ExternalStream(rt.stream(), device=torch.device("cuda", dev))
@@ -457,7 +471,7 @@ def mlp_leg(args, dev):
         L = rt.read_accum()[0] @ luma
         leg = {"rmse": float(np.sqrt(max(np.mean((L - Lref) ** 2) - ref_noise, 0.0)) / Lref.mean()),
                "ms": e0.elapsed_time(e1)}
-        if guide:
+        if guide and stats:
             st = rt.mlp_stats()
             rt.enable_kernel_times(True)
             rt.reset_kernel_times()

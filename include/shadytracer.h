@@ -489,6 +489,14 @@ typedef struct st_optics_source {
     uint32_t instance;            /* which instance of a batch it belongs to                        */
     uint32_t ray_first, ray_count;/* a ray set's rays in the ray table: each traced ray takes one at
                                      random, as it is, carrying its weight (kernels.js:320-336)       */
+    /* THE LIGHT'S COLOUR (builder/sources.js colour, planck, spectrum; optics/spectral.js sourceSpectrum): its rays
+     * carry this linear Rec.709 colour at the flux's luminance (0, 0, 0: white). The trace by wavelength
+     * (st_optics_batch.spectral) draws them from its spectrum: row `spectrum` - 1 of st_optics_set_spectra's table when
+     * set, else a blackbody of `cct` kelvin when set, else a stand-in spectrum of exactly the colour's XYZ. */
+    float    colour[3];
+    float    cct;
+    uint32_t spectrum;
+    uint32_t pad[5];              /* 128 bytes                                                      */
 } st_optics_source;
 
 typedef struct st_optics_far {
@@ -508,6 +516,13 @@ typedef struct st_optics_batch {
     float    lux_height;          /* its distance from the source along the axis, metres            */
     uint32_t maxbounce;           /* 0 = 32                                                         */
     uint32_t seed;
+    /* THE TRACE BY WAVELENGTH (optics/spectral.js, the scene's `spectral` feature): 1 -- each ray carries three
+     * wavelengths of its light's spectrum, drawn stratified through x-bar + y-bar + z-bar (u, u + 1/3, u + 2/3), a
+     * weight each S(l) / (3 p(l)); a material's colour is a reflectance at each (sum_c rgb_c B_c(l), B the clipped
+     * Rec.709 colour-matching functions over their sum), a coating its R at each, and a dispersive glass refracts
+     * the first and drops the other two (the ray's weights become 3 w_1, 0, 0); tallies count Y = sum_k w_k y-bar(l_k)
+     * and the detector's hits its X and Z. 0: the rays carry a colour, as the renderer's do. */
+    uint32_t spectral;
 } st_optics_batch;
 
 typedef struct st_optics_totals {
@@ -534,6 +549,11 @@ int  st_optics_set_far(st_ctx* ctx, const st_optics_far* far);
  * optics/zemax.js): n rays of 8 floats -- position (metres, world), weight (its flux over its set's mean),
  * direction (unit), wavelength (nm, 0 none). */
 int  st_optics_set_rays(st_ctx* ctx, const float* rays, uint32_t n);
+/* THE SPECTRA a source may name (st_optics_source.spectrum): n rows of ST_SPECTRUM_NODES values, a spectral power
+ * distribution at 1 nm from ST_SPECTRUM_LO nm (any scale: each is normalised to luminance 1), replacing the table. */
+#define ST_SPECTRUM_LO    360
+#define ST_SPECTRUM_NODES 471
+int  st_optics_set_spectra(st_ctx* ctx, const float* values, uint32_t n);
 /* Traces every instance of the batch; far (n_instances*nG*nC) and lux (n_instances*cells^2) are the
  * FP64 tallies in ray weight (the host multiplies by flux / rays); totals per instance. */
 int  st_optics_run(st_ctx* ctx, const st_optics_batch* batch, double* far, double* lux,

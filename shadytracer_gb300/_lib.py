@@ -26,6 +26,7 @@ SIGNATURES = {
     "st_compile_scene": ([C.c_char_p, C.c_char_p, C.c_size_t, C.POINTER(C.c_double)], C.c_int),
     "st_set_env_image": ([P, P, C.c_uint32, C.c_uint32, C.c_float, C.c_float], C.c_int),
     "st_optics_set_rays": ([P, P, C.c_uint32], C.c_int),
+    "st_optics_set_spectra": ([P, P, C.c_uint32], C.c_int),
     "st_env_map_tables": ([P, P], C.c_int),
     "st_invalidate": ([P], C.c_int),
     "st_step": ([P, C.c_int], C.c_int),

@@ -945,8 +945,10 @@ __device__ __forceinline__ void coat_pick(Lobes& lb, f3 beta) {
 // transm, spec and hz: the material's transmission, specular and haze, or the part of the face drawn from inside
 // n0 the index of the medium the view is in, inside whether it is seen from within (the normal turned), lam the
 // ray's own wavelength (0 none): a coating reads all three (materials_pbr.js:164 makeLobes)
+// (lam3: the trace by wavelength's three wavelengths, one a channel, where the coating is taken at each)
 __device__ __forceinline__ Lobes make_lobes(f3 n, f3 v, const st_material& m, float eta, const MfTab& t,
-                                            float transm, float spec, float hz, float n0, bool inside, float lam) {
+                                            float transm, float spec, float hz, float n0, bool inside, float lam,
+                                            const f3* lam3 = nullptr) {
     Lobes lb;
     lb.through = false;
     f3 s = fabsf(n.z) < 0.999f ? normalize(cross(n, mk(0, 0, 1))) : normalize(cross(n, mk(0, 1, 0)));
@@ -988,7 +990,11 @@ __device__ __forceinline__ Lobes make_lobes(f3 n, f3 v, const st_material& m, fl
             const float sin0 = sqrtf(fmaxf(0.f, 1.f - lb.o.z * lb.o.z));
             const float lo = sat(m.coat_lo), hi = sat(m.coat_hi), w = fmaxf(m.coat_width, 0.f);
             const float edge = coat_edge_at(m.coat_edge, n0 * sin0, fmaxf(m.coat_index, 1.f));
-            lb.coatR = lam > 0.f ? mk(coat_edge_at_lambda(lo, hi, edge, w, lam)) : coat_edge_rgb(t.coat, lo, hi, edge, w);
+            if (lam3)
+                lb.coatR = mk(coat_edge_at_lambda(lo, hi, edge, w, lam3->x), coat_edge_at_lambda(lo, hi, edge, w, lam3->y),
+                              coat_edge_at_lambda(lo, hi, edge, w, lam3->z));
+            else
+                lb.coatR = lam > 0.f ? mk(coat_edge_at_lambda(lo, hi, edge, w, lam)) : coat_edge_rgb(t.coat, lo, hi, edge, w);
             lb.coated = true;
         } else if (coat == 1u) {
             lb.coated = true;

@@ -55,6 +55,7 @@ struct OpticsState {
     uint64_t sources_gen = 0;    // the sources' and the ray table's changes (a batch's graph is recorded with them)
     uint64_t launches = 0;       // kernels the batches' graphs ran
     uint32_t tune_claim = 0, tune_chunk = 0;   // the optics autotuner's picks (st_optics_autotune); 0, the defaults
+    std::vector<float> spectra;  // st_optics_set_spectra's rows, ST_SPECTRUM_NODES values each
     void* scratch = nullptr;     // the run's device buffers (st_optics.cu OptBuf), grown as needed
 };
 

@@ -21,6 +21,7 @@
 
 #include "st_ext.h"
 #include "st_kernels.cuh"
+#include "st_spectral.h"
 
 using namespace st;
 
@@ -78,7 +79,59 @@ struct OptArgs {
     uint32_t* vcount;               // n_inst * path_rays
     uint32_t path_rays, path_verts;
     float esc_len;                  // an escaped ray's last vertex, this far past its last interaction
+    // THE TRACE BY WAVELENGTH (optics/spectral.js): on, and its tables -- the draw's CDF, the colour-matching
+    // functions, the basis an RGB colour becomes a spectrum by (SPO_NODES values each), then each source's spectrum
+    // (in src's order) at luminance 1
+    uint32_t spectral;
+    const float* spo;
 };
+
+// ---- the trace by wavelength's device half (optics/spectral.js SPECTRAL_CORE_WGSL, specOfRGB) ----
+#define SPO_NODES 471u
+#define SPO_LO 360.f
+// a table at l, linear between its 1 nm nodes
+__device__ __forceinline__ float spo_node(const float* __restrict__ t, uint32_t off, float l) {
+    const float x = l - SPO_LO;
+    const uint32_t i = (uint32_t)fminf(fmaxf(floorf(x), 0.f), (float)(SPO_NODES - 2u));
+    const float f = fminf(fmaxf(x - (float)i, 0.f), 1.f);
+    const float a = __ldg(&t[off + i]), b = __ldg(&t[off + i + 1u]);
+    return a + f * (b - a);
+}
+// the draw: u to (l, its density per nm) through the CDF of x-bar + y-bar + z-bar
+__device__ __forceinline__ float2 spo_lambda(const float* __restrict__ t, float u) {
+    uint32_t lo = 0u, hi = SPO_NODES - 1u;
+    while (hi - lo > 1u) {
+        const uint32_t m = (lo + hi) >> 1;
+        if (__ldg(&t[m]) <= u) lo = m;
+        else hi = m;
+    }
+    const float c0 = __ldg(&t[lo]), mass = __ldg(&t[hi]) - c0;
+    const float f = mass > 0.f ? fminf(fmaxf((u - c0) / mass, 0.f), 1.f) : 0.5f;
+    return make_float2(SPO_LO + (float)lo + f, mass);
+}
+// a ray's three wavelengths, u, u + 1/3, u + 2/3 (mod 1) through the draw
+__device__ __forceinline__ f3 spo_lams(const float* t, float u) {
+    float u1 = u + 1.f / 3.f, u2 = u + 2.f / 3.f;
+    if (u1 >= 1.f) u1 -= 1.f;
+    if (u2 >= 1.f) u2 -= 1.f;
+    return mk(spo_lambda(t, u).x, spo_lambda(t, u1).x, spo_lambda(t, u2).x);
+}
+__device__ __forceinline__ f3 spo_cmf(const float* t, float l) {
+    return mk(spo_node(t, SPO_NODES, l), spo_node(t, 2u * SPO_NODES, l), spo_node(t, 3u * SPO_NODES, l));
+}
+__device__ __forceinline__ f3 spo_basis(const float* t, float l) {
+    return mk(spo_node(t, 4u * SPO_NODES, l), spo_node(t, 5u * SPO_NODES, l), spo_node(t, 6u * SPO_NODES, l));
+}
+// what a ray carries as XYZ: each wavelength's weight times the colour-matching functions there (specXYZ)
+__device__ __forceinline__ f3 spo_xyz(const float* t, f3 c, f3 l) {
+    return spo_cmf(t, l.x) * c.x + spo_cmf(t, l.y) * c.y + spo_cmf(t, l.z) * c.z;
+}
+// a ray's wavelength word (PathBuf.lam): its u, or u + 2 once a dispersive glass collapsed it to its first wavelength
+__device__ __forceinline__ float spo_u(float w) { return w >= 2.f ? w - 2.f : w; }
+// optWeight: what a ray carries, as luminance -- its colour's, or by wavelength its Y
+__device__ __forceinline__ float opt_weight(const OptArgs& o, f3 beta, float lamw) {
+    return o.spectral ? spo_xyz(o.spo, beta, spo_lams(o.spo, spo_u(lamw))).y : luma(beta);
+}
 
 __device__ __forceinline__ long long fx(float w) { return __double2ll_rn((double)w * OPT_FX); }
 
@@ -172,11 +225,12 @@ __device__ __forceinline__ uint32_t far_bin(const OptArgs& o, f3 d) {
 // A SOURCE'S RAY (kernels.js:299-408 optSourceRay): the source by flux, a point on it, the side, the direction from
 // its distribution, two march tolerances off the sheet when it is geometry
 __device__ __forceinline__ void source_ray(const OptArgs& o, uint32_t inst, Rng& rng, f3& org, f3& dir, float& en,
-                                           float& w) {
+                                           float& w, uint32_t& ks) {
     const uint2 rg = o.src_range[inst];
     float4 pick = rng.next();
     uint32_t k = rg.x;
     for (uint32_t i = 0; i < rg.y; i++) { k = rg.x + i; if (pick.x <= o.cdf[rg.x + i]) break; }
+    ks = k;
     const st_optics_source& s = o.src[k];
     w = 1.f;
     if (s.shape == 3u) {                                              // A RAY SET: one of its rays, as it is, weighted
@@ -240,14 +294,38 @@ __global__ void __launch_bounds__(256) k_opt_gen(OptArgs o) {
         rng.seed(0x9E3779B9u);
         f3 org, dir;
         float en, w;
-        source_ray(o, inst, rng, org, dir, en, w);
+        uint32_t ks = 0;
+        source_ray(o, inst, rng, org, dir, en, w, ks);
         a.pb.pos[i] = make_float4(org.x, org.y, org.z, 0.f);
         a.pb.dir[i] = make_float4(dir.x, dir.y, dir.z, en);
-        a.pb.beta[i] = make_float4(w, w, w, 1.f);                       // a ray set's ray carries its weight
+        // a ray set's ray carries its weight; a light its colour at that luminance -- or, by wavelength, three
+        // wavelengths of its spectrum, each weighing S(l) / (3 p(l)) (optics/spectral.js: sum_k w_k y-bar(l_k) is w
+        // on average)
+        const st_optics_source& s = o.src[ks];
+        f3 c = mk(w);
+        if (o.spectral) {
+            const float4 ur = rng.next();
+            const float* sp = o.spo + 7u * SPO_NODES + (size_t)ks * SPO_NODES;
+            float uk = ur.x;
+            float b[3];
+            for (int k = 0; k < 3; k++) {
+                const float2 lp = spo_lambda(o.spo, uk);
+                b[k] = lp.y > 0.f ? w * spo_node(sp, 0u, lp.x) / (3.f * lp.y) : 0.f;
+                uk += 1.f / 3.f;
+                if (uk >= 1.f) uk -= 1.f;
+            }
+            c = mk(b[0], b[1], b[2]);
+            a.pb.lam[i] = ur.x;
+        } else if (s.colour[0] != 0.f || s.colour[1] != 0.f || s.colour[2] != 0.f) {
+            const f3 col = mk(s.colour[0], s.colour[1], s.colour[2]);
+            const float y = luma(col);
+            if (y > 0.f) c = col * (w / y);
+        }
+        a.pb.beta[i] = make_float4(c.x, c.y, c.z, 1.f);
         if (o.has_sets) atomicAdd(&o.tot[(size_t)inst * OPT_TOT + T_EMIT], (unsigned long long)fx(w));
         if (id < o.path_rays) {                                         // a kept path starts where the ray leaves
             o.vcount[(size_t)inst * o.path_rays + id] = 0u;
-            opt_vertex(o, inst, id, org, w, 0.f, mk(w));
+            opt_vertex(o, inst, id, org, w, 0.f, c);
         }
         a.pb.rad[i] = make_float4(1.f, 1.f, 1.f, 0.f);          // a photon's radiance field is its flux: weight 1
         a.pb.meta[i] = make_uint4(id, meta_y(0, 0, RAY_ACTIVE), 0u, inst);
@@ -297,7 +375,8 @@ __global__ void __launch_bounds__(256) k_opt_shade(OptArgs o, int nxt, int last)
             inst = m4.w;
             const uint32_t id = m4.x;
             uint32_t bounces = m4.y & 0xffu, state = (m4.y >> 16) & 0xffu;
-            const float wIn = luma(beta);                             // optWeight: beta x radiance (1), as luminance
+            const float lamw = o.spectral ? a.pb.lam[slot] : 0.f;      // the trace by wavelength: its u (and collapse)
+            const float wIn = opt_weight(o, beta, lamw);             // optWeight: beta x radiance (1), as luminance
             if (state == RAY_ESCAPED) {                               // kernels.js:609-625
                 tv[T_ESC] = fx(wIn);
                 tv[T_NESC] = 1;
@@ -360,9 +439,14 @@ __global__ void __launch_bounds__(256) k_opt_shade(OptArgs o, int nxt, int last)
                         float4* d = o.det + (size_t)k * DET_F4;
                         d[0] = f4(pos, wIn);
                         d[1] = make_float4(dir.x, dir.y, dir.z, __uint_as_float(tag | (inst << 16)));
-                        // the colour as CIE X and Z of its linear Rec.709 rgb (Y is the weight)
-                        d[2] = make_float4(0.4124f * beta.x + 0.3576f * beta.y + 0.1805f * beta.z,
-                                           0.0193f * beta.x + 0.1192f * beta.y + 0.9505f * beta.z, 0.f, 0.f);
+                        // the colour as CIE X and Z of its linear Rec.709 rgb, or by wavelength its XYZ (Y is the weight)
+                        if (o.spectral) {
+                            const f3 X = spo_xyz(o.spo, beta, spo_lams(o.spo, spo_u(lamw)));
+                            d[2] = make_float4(X.x, X.z, 0.f, 0.f);
+                        } else {
+                            d[2] = make_float4(0.4124f * beta.x + 0.3576f * beta.y + 0.1805f * beta.z,
+                                               0.0193f * beta.x + 0.1192f * beta.y + 0.9505f * beta.z, 0.f, 0.f);
+                        }
                     }
                 } else if (dot(-dir, nrm) < 0.f) {                    // seen from behind: moved on, no interaction
                     f3 off = dir * otol;
@@ -377,10 +461,26 @@ __global__ void __launch_bounds__(256) k_opt_shade(OptArgs o, int nxt, int last)
                     bounces += 1;
                     const f3 hit_pos = pos, beta_in = beta;
                     const float hit_ltot = ltot;
-                    float n0 = n, n1 = fmaxf(m.ior, n0);
+                    float n0 = n, n1 = fmaxf(m.ior, n0), v1 = 0.f;
                     if (m.transmission > 0.f && m.metallic < 1.f) {
                         SceneHit mb = scene_full(ip, np, pos + (-nrm) * (otol * 2.f));
                         n1 = sm[min(mb.a, u.n_mats - 1)].ior;
+                        v1 = sm[min(mb.a, u.n_mats - 1)].abbe;
+                    }
+                    // BY WAVELENGTH (optics/spectral.js WHAT A MATERIAL IS AT A WAVELENGTH): the colour a reflectance at
+                    // each of the ray's wavelengths, the coating taken at each; a dispersive glass beyond refracts the
+                    // first wavelength (at its n, the pick the d line's) and drops the other two
+                    st_material mw = m;
+                    f3 l3 = mk(0.f);
+                    float nT = n1;
+                    bool collapse = false;
+                    if (o.spectral) {
+                        l3 = spo_lams(o.spo, spo_u(lamw));
+                        const f3 rgb = mk(m.base[0], m.base[1], m.base[2]);
+                        mw.base[0] = dot(rgb, spo_basis(o.spo, l3.x));
+                        mw.base[1] = dot(rgb, spo_basis(o.spo, l3.y));
+                        mw.base[2] = dot(rgb, spo_basis(o.spo, l3.z));
+                        if (v1 > 0.f) { nT = cauchy_n(n1, v1, l3.x); collapse = lamw < 2.f; }
                     }
                     float pG = refract_share_of(m.transmission, m.haze), trans = m.transmission, specv = m.specular;
                     float hz = m.haze;
@@ -395,20 +495,26 @@ __global__ void __launch_bounds__(256) k_opt_shade(OptArgs o, int nxt, int last)
                         }
                     }
                     float etaFace = diffFace ? fminf(n0, n1) / fmaxf(n0, n1) : n0 / n1;
-                    Lobes lb = make_lobes(nrm, -dir, m, etaFace, a.tab, trans, specv, hz, n0, inside, 0.f);
-                    lb.etaT = n0 / n1;
+                    Lobes lb = make_lobes(nrm, -dir, mw, etaFace, a.tab, trans, specv, hz, n0, inside, 0.f,
+                                          o.spectral ? &l3 : nullptr);
+                    lb.etaT = n0 / nT;
                     coat_pick(lb, beta);
                     LobeSample smp = lobes_sample(lb, a.tab, rng.next());
                     dir = smp.dir;
                     beta = beta * smp.w;
-                    if (smp.transmitted) n = n1;
+                    float lamo = lamw;
+                    if (smp.transmitted) {
+                        n = nT;
+                        if (collapse) { beta = mk(3.f * beta.x, 0.f, 0.f); lamo = lamw + 2.f; }
+                    }
                     uint32_t st = RAY_ACTIVE;
                     if (max3(smp.w) <= 0.f) st = RAY_ABSORBED;
                     f3 off = dir * otol;
                     pos = pos + off; ltot += length(off) * n;
                     if (bounces > u.maxbounce) st = RAY_TERMINATED;
                     bool goesOn = st == RAY_ACTIVE || st == RAY_TERMINATED;
-                    float wOut = goesOn ? luma(beta) : 0.f;
+                    float wOut = goesOn ? opt_weight(o, beta, lamo) : 0.f;
+                    if (o.spectral && lamo != lamw) a.pb.lam[slot] = lamo;
                     tv[T_INTER] = 1;
                     tv[T_ABS] = fx(wIn) - fx(wOut);
                     if (!goesOn) tv[T_NABS] = 1;
@@ -487,6 +593,9 @@ struct OptBuf {
     DevCtr* ctr = nullptr; size_t nctr = 0;
     float4 *det = nullptr, *verts = nullptr; size_t ndet = 0, nverts = 0;
     uint32_t *det_n = nullptr, *vcount = nullptr; size_t ndetn = 0, nvcount = 0;
+    float* lam = nullptr; size_t nlam = 0;      // the trace by wavelength: each ray's u (and whether it collapsed)
+    float* spo = nullptr; size_t nspo = 0;      // ...its tables and the sources' spectra
+    uint64_t spo_gen = 0;                       // the spectra's change the tables were made with
     // the last run, kept for the readings after it (st_optics_tallies / _hits / _paths)
     uint32_t last_ni = 0, last_mats = 0, last_det_cap = 0, last_path_rays = 0, last_path_verts = 0;
     // THE BATCH AS ONE CUDA GRAPH: its whole chain captured at its first run and replayed while nothing it was
@@ -504,7 +613,7 @@ void optics_free(OpticsState& os) {
     OptBuf* B = static_cast<OptBuf*>(os.scratch);
     void* ps[] = {B->pos, B->dir, B->beta, B->rad, B->meta, B->ray0, B->ray1, B->hit, B->hitd, B->far, B->lux, B->tot,
                   B->tag, B->mat, B->src, B->cdf, B->range, B->srange, B->origin, B->wfirst, B->wpre, B->ctr, B->det,
-                  B->verts, B->det_n, B->vcount};
+                  B->verts, B->det_n, B->vcount, B->lam, B->spo};
     for (void* p : ps)
         if (p) cudaFree(p);
     if (B->graph) cudaGraphExecDestroy(B->graph);
@@ -523,6 +632,14 @@ int st_optics_set_sources(st_ctx* ctx, const st_optics_source* src, uint32_t n) 
         }
     ctx_ext(ctx).optics.sources.assign(src, src + n);
     ctx_ext(ctx).optics.sources_gen++;
+    return ST_OK;
+}
+
+int st_optics_set_spectra(st_ctx* ctx, const float* values, uint32_t n) {
+    if (!ctx || (n && !values)) return ST_ERR_ARG;
+    OpticsState& os = ctx_ext(ctx).optics;
+    os.spectra.assign(values, values + (size_t)n * ST_SPECTRUM_NODES);
+    os.sources_gen++;
     return ST_OK;
 }
 
@@ -650,8 +767,29 @@ int st_optics_run(st_ctx* ctx, const st_optics_batch* b, double* far_out, double
         (e = grow(B.wpre, B.nwpre, (size_t)(NI + 1) * K)) || (e = grow(B.ctr, B.nctr, (size_t)1)) ||
         (e = grow(B.det, B.ndet, std::max<size_t>((size_t)D.det_cap * DET_F4, 1))) ||
         (e = grow(B.det_n, B.ndetn, (size_t)1)) || (e = grow(B.verts, B.nverts, std::max<size_t>(nverts, 1))) ||
-        (e = grow(B.vcount, B.nvcount, std::max<size_t>((size_t)NI * D.path_rays, 1))))
+        (e = grow(B.vcount, B.nvcount, std::max<size_t>((size_t)NI * D.path_rays, 1))) ||
+        (b->spectral && (e = grow(B.lam, B.nlam, W))) ||
+        (b->spectral && (e = grow(B.spo, B.nspo, (size_t)(7 + src.size()) * SPO_N))))
         return fail(e, "cudaMalloc optics buffers");
+    // THE TRACE BY WAVELENGTH's tables and each source's spectrum at luminance 1 (optics/spectral.js spectralBuffer)
+    if (b->spectral) {
+        for (const st_optics_source& q : src)
+            if (q.spectrum && (size_t)q.spectrum * ST_SPECTRUM_NODES > os.spectra.size()) {
+                ctx_set_error(ctx, "a source names spectrum " + std::to_string(q.spectrum) + " past the table");
+                return ST_ERR_ARG;
+            }
+        const std::vector<double> tab = spo_tables();
+        std::vector<float> h((size_t)(7 + src.size()) * SPO_N);
+        for (size_t i = 0; i < tab.size(); i++) h[i] = (float)tab[i];
+        for (size_t k = 0; k < src.size(); k++) {
+            const st_optics_source& q = src[k];
+            const float* row = q.spectrum ? os.spectra.data() + (size_t)(q.spectrum - 1) * ST_SPECTRUM_NODES : nullptr;
+            const std::vector<double> sv = spo_source(tab, row, q.cct, q.colour);
+            for (int i = 0; i < SPO_N; i++) h[(7 + k) * SPO_N + i] = (float)sv[i];
+        }
+        if ((e = cudaMemcpyAsync(B.spo, h.data(), h.size() * 4, cudaMemcpyHostToDevice, st)))
+            return fail(e, "optics spectra upload");
+    }
     // the waves: each instance's rays split evenly over K of them (photons.js:31-62 splitPart), all K tables at once
     std::vector<uint32_t> wf((size_t)NI * K), wp((size_t)(NI + 1) * K, 0);
     std::vector<uint32_t> wslots(K);
@@ -697,6 +835,9 @@ int st_optics_run(st_ctx* ctx, const st_optics_batch* b, double* far_out, double
     o.w.mats = ctx_d_mats(ctx);
     o.w.tab = ctx_tab(ctx);
     o.w.pb = PathBuf{B.pos, B.dir, B.beta, B.rad, B.meta};
+    o.w.pb.lam = b->spectral ? B.lam : nullptr;
+    o.spectral = b->spectral ? 1u : 0u;
+    o.spo = b->spectral ? B.spo : nullptr;
     o.w.q = Queues{};
     o.w.q.ray[0] = B.ray0; o.w.q.ray[1] = B.ray1; o.w.q.hit = B.hit; o.w.q.hitd = B.hitd;
     o.w.q.cap = (uint32_t)W;
@@ -770,7 +911,7 @@ int st_optics_run(st_ctx* ctx, const st_optics_batch* b, double* far_out, double
                                  (uint64_t)(uintptr_t)os.rays, D.det_cap, D.path_rays, D.path_verts,
                                  (uint64_t)__float_as_uint_host(o.esc_len), F.nC, F.nG,
                                  (uint64_t)__float_as_uint_host(b->lux_half), (uint64_t)__float_as_uint_host(b->lux_height),
-                                 u.claim, u.chunk};
+                                 u.claim, u.chunk, b->spectral, (uint64_t)(uintptr_t)B.lam, (uint64_t)(uintptr_t)B.spo};
     for (int k = 0; k < 3; k++) {
         key.push_back(__float_as_uint_host(F.axis[k]));
         key.push_back(__float_as_uint_host(F.c0[k]));

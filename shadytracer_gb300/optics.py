@@ -51,14 +51,22 @@ class Optics:
         check(self.L.st_optics_set_far(self.rt.ctx, C.byref(f)), self.rt.ctx, "st_optics_set_far")
         self.far = f
 
-    def run(self, ray_counts, lux_cells=512, lux_half=1.0, lux_height=1.0, maxbounce=32, seed=1):
+    def set_spectra(self, spectra):
+        """The spectra a source may name (st_optics_source.spectrum, 1-based): rows of ST_SPECTRUM_NODES values at 1 nm
+        from 360 nm, any scale."""
+        a = np.ascontiguousarray(np.asarray(spectra, np.float32).reshape(-1, 471))
+        check(self.L.st_optics_set_spectra(self.rt.ctx, a.ctypes.data_as(C.c_void_p), len(a)), self.rt.ctx,
+              "st_optics_set_spectra")
+        self.spectra = a
+
+    def run(self, ray_counts, lux_cells=512, lux_half=1.0, lux_height=1.0, maxbounce=32, seed=1, spectral=0):
         n = len(ray_counts)
         rc = (C.c_uint32 * n)(*[int(x) for x in ray_counts])
         b = T.StOpticsBatch()
         b.n_instances = n
         b.ray_count = C.cast(rc, C.POINTER(C.c_uint32))
         b.lux_cells, b.lux_half, b.lux_height = lux_cells, lux_half, lux_height
-        b.maxbounce, b.seed = maxbounce, seed
+        b.maxbounce, b.seed, b.spectral = maxbounce, seed, int(spectral)
         nG, nC = self.far.nG, self.far.nC
         far = np.zeros((n, nG, nC), np.float64)
         lux = np.zeros((n, lux_cells, lux_cells), np.float64)

@@ -127,7 +127,8 @@ class StOpticsSource(C.Structure):
                 ("tangent", C.c_float * 3), ("size_x", C.c_float),
                 ("size_y", C.c_float), ("dist", C.c_uint32), ("cos_half", C.c_float), ("n_exp", C.c_float),
                 ("emit_n", C.c_float), ("two_sided", C.c_uint32), ("on_surface", C.c_uint32),
-                ("instance", C.c_uint32), ("ray_first", C.c_uint32), ("ray_count", C.c_uint32)]
+                ("instance", C.c_uint32), ("ray_first", C.c_uint32), ("ray_count", C.c_uint32),
+                ("colour", C.c_float * 3), ("cct", C.c_float), ("spectrum", C.c_uint32), ("pad", C.c_uint32 * 5)]
 
 
 class StOpticsFar(C.Structure):
@@ -137,7 +138,7 @@ class StOpticsFar(C.Structure):
 class StOpticsBatch(C.Structure):
     _fields_ = [("n_instances", C.c_uint32), ("ray_count", C.POINTER(C.c_uint32)),
                 ("lux_cells", C.c_uint32), ("lux_half", C.c_float), ("lux_height", C.c_float),
-                ("maxbounce", C.c_uint32), ("seed", C.c_uint32)]
+                ("maxbounce", C.c_uint32), ("seed", C.c_uint32), ("spectral", C.c_uint32)]
 
 
 class StOpticsTotals(C.Structure):
