@@ -1456,3 +1456,4 @@ bool ctx_has_scene(st_ctx* ctx) { return ctx->has_scene; }
 uint64_t ctx_scene_gen(st_ctx* ctx) { return ctx->scene_gen; }
 DevCtr* ctx_counters(st_ctx* ctx) { return ctx->d_ctr; }
 MfTab ctx_tab(st_ctx* ctx) { return MfTab{ctx->d_ec, ctx->d_ecavg, ctx->d_e1, ctx->d_coat}; }
+const float4* ctx_spec(st_ctx* ctx) { return ctx->d_spec; }

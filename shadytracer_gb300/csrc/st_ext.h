@@ -130,3 +130,4 @@ bool ctx_has_scene(st_ctx* ctx);
 uint64_t ctx_scene_gen(st_ctx* ctx);
 st::DevCtr* ctx_counters(st_ctx* ctx);     // a count of the scenes set (a graph recorded with one is stale after)
 st::MfTab ctx_tab(st_ctx* ctx);
+const float4* ctx_spec(st_ctx* ctx);

@@ -316,10 +316,13 @@ __global__ void __launch_bounds__(256) k_opt_gen(OptArgs o) {
             }
             c = mk(b[0], b[1], b[2]);
             a.pb.lam[i] = ur.x;
-        } else if (s.colour[0] != 0.f || s.colour[1] != 0.f || s.colour[2] != 0.f) {
-            const f3 col = mk(s.colour[0], s.colour[1], s.colour[2]);
-            const float y = luma(col);
-            if (y > 0.f) c = col * (w / y);
+        } else {
+            a.pb.lam[i] = 0.f;                                          // no wavelength yet
+            if (s.colour[0] != 0.f || s.colour[1] != 0.f || s.colour[2] != 0.f) {
+                const f3 col = mk(s.colour[0], s.colour[1], s.colour[2]);
+                const float y = luma(col);
+                if (y > 0.f) c = col * (w / y);
+            }
         }
         a.pb.beta[i] = make_float4(c.x, c.y, c.z, 1.f);
         if (o.has_sets) atomicAdd(&o.tot[(size_t)inst * OPT_TOT + T_EMIT], (unsigned long long)fx(w));
@@ -375,7 +378,8 @@ __global__ void __launch_bounds__(256) k_opt_shade(OptArgs o, int nxt, int last)
             inst = m4.w;
             const uint32_t id = m4.x;
             uint32_t bounces = m4.y & 0xffu, state = (m4.y >> 16) & 0xffu;
-            const float lamw = o.spectral ? a.pb.lam[slot] : 0.f;      // the trace by wavelength: its u (and collapse)
+            // by wavelength its u (and whether it collapsed); in colour the wavelength a dispersive glass gave it (0 none)
+            const float lamw = a.pb.lam[slot];
             const float wIn = opt_weight(o, beta, lamw);             // optWeight: beta x radiance (1), as luminance
             if (state == RAY_ESCAPED) {                               // kernels.js:609-625
                 tv[T_ESC] = fx(wIn);
@@ -474,6 +478,8 @@ __global__ void __launch_bounds__(256) k_opt_shade(OptArgs o, int nxt, int last)
                     f3 l3 = mk(0.f);
                     float nT = n1;
                     bool collapse = false;
+                    SpecDraw sd;
+                    bool draw = false;
                     if (o.spectral) {
                         l3 = spo_lams(o.spo, spo_u(lamw));
                         const f3 rgb = mk(m.base[0], m.base[1], m.base[2]);
@@ -481,6 +487,18 @@ __global__ void __launch_bounds__(256) k_opt_shade(OptArgs o, int nxt, int last)
                         mw.base[1] = dot(rgb, spo_basis(o.spo, l3.y));
                         mw.base[2] = dot(rgb, spo_basis(o.spo, l3.z));
                         if (v1 > 0.f) { nT = cauchy_n(n1, v1, l3.x); collapse = lamw < 2.f; }
+                    } else if (v1 > 0.f) {
+                        // IN COLOUR (materials_pbr.js:1116-1139, as the renderer's): a ray with a wavelength meets the
+                        // dispersive glass at n(its wavelength); one without draws one from the camera's table, used
+                        // if it refracts, its channels weighed by what that wavelength is to them; the pick the d line's
+                        if (lamw > 0.f) nT = cauchy_n(n1, v1, lamw);
+                        else {
+                            const float4 rl = rng.next();
+                            sd = spec_draw(a.spec, rl.x);
+                            sd.lam = lambda_coded(sd.lam);
+                            nT = cauchy_n(n1, v1, sd.lam);
+                            draw = true;
+                        }
                     }
                     float pG = refract_share_of(m.transmission, m.haze), trans = m.transmission, specv = m.specular;
                     float hz = m.haze;
@@ -506,6 +524,7 @@ __global__ void __launch_bounds__(256) k_opt_shade(OptArgs o, int nxt, int last)
                     if (smp.transmitted) {
                         n = nT;
                         if (collapse) { beta = mk(3.f * beta.x, 0.f, 0.f); lamo = lamw + 2.f; }
+                        if (draw) { beta = beta * sd.w; lamo = sd.lam; }
                     }
                     uint32_t st = RAY_ACTIVE;
                     if (max3(smp.w) <= 0.f) st = RAY_ABSORBED;
@@ -514,7 +533,7 @@ __global__ void __launch_bounds__(256) k_opt_shade(OptArgs o, int nxt, int last)
                     if (bounces > u.maxbounce) st = RAY_TERMINATED;
                     bool goesOn = st == RAY_ACTIVE || st == RAY_TERMINATED;
                     float wOut = goesOn ? opt_weight(o, beta, lamo) : 0.f;
-                    if (o.spectral && lamo != lamw) a.pb.lam[slot] = lamo;
+                    if (lamo != lamw) a.pb.lam[slot] = lamo;
                     tv[T_INTER] = 1;
                     tv[T_ABS] = fx(wIn) - fx(wOut);
                     if (!goesOn) tv[T_NABS] = 1;
@@ -768,7 +787,7 @@ int st_optics_run(st_ctx* ctx, const st_optics_batch* b, double* far_out, double
         (e = grow(B.det, B.ndet, std::max<size_t>((size_t)D.det_cap * DET_F4, 1))) ||
         (e = grow(B.det_n, B.ndetn, (size_t)1)) || (e = grow(B.verts, B.nverts, std::max<size_t>(nverts, 1))) ||
         (e = grow(B.vcount, B.nvcount, std::max<size_t>((size_t)NI * D.path_rays, 1))) ||
-        (b->spectral && (e = grow(B.lam, B.nlam, W))) ||
+        (e = grow(B.lam, B.nlam, W)) ||
         (b->spectral && (e = grow(B.spo, B.nspo, (size_t)(7 + src.size()) * SPO_N))))
         return fail(e, "cudaMalloc optics buffers");
     // THE TRACE BY WAVELENGTH's tables and each source's spectrum at luminance 1 (optics/spectral.js spectralBuffer)
@@ -835,7 +854,8 @@ int st_optics_run(st_ctx* ctx, const st_optics_batch* b, double* far_out, double
     o.w.mats = ctx_d_mats(ctx);
     o.w.tab = ctx_tab(ctx);
     o.w.pb = PathBuf{B.pos, B.dir, B.beta, B.rad, B.meta};
-    o.w.pb.lam = b->spectral ? B.lam : nullptr;
+    o.w.pb.lam = B.lam;                 // by wavelength its u; in colour the wavelength a dispersive glass gave it
+    o.w.spec = ctx_spec(ctx);
     o.spectral = b->spectral ? 1u : 0u;
     o.spo = b->spectral ? B.spo : nullptr;
     o.w.q = Queues{};

@@ -1238,3 +1238,49 @@ def milky_slab(width=64, height=48, photons=200_000, r1=0.01, r1v=0.02, sun_diam
         s.params.sppm_half = 0.6
     s.view = look_at((0.0, -1.4, 0.75), (0.0, 0.0, 0.2), 45.0, width / height)
     return s
+
+
+def dispersive_wedge(abbe=28.0, ior=1.75, wedge_deg=30.0, rays=100_000):
+    """optics-dispersion's bench (lib/pathtracer/tests.js testScene 'wedge'): a collimated white beam (a disc of 0.1 m
+    at z 1) straight down through a glass wedge -- a block whose top face is tilted `wedge_deg` about y (outward normal
+    (sin a, 0, cos a)) and whose bottom is level -- of index `ior` at the d line and Abbe number `abbe`, onto a black
+    detector floor. Each ray refracted into the glass takes a wavelength and refracts at n(l): the beam fans out."""
+    from .st_types import StOpticsSource
+    a = math.radians(wedge_deg)
+    glass_m = material(base=(1, 1, 1), roughness=0.0, specular=0.5, transmission=1.0, ior=ior, abbe=abbe)
+    det = material(base=(0, 0, 0), specular=0.0, detector=1.0)
+    # the tilted top: a half-space subtracted from the block, its local z (into the wedge) -(sin a, 0, cos a)
+    rot = (-math.cos(a), 0.0, math.sin(a), 0.0, 1.0, 0.0, -math.sin(a), 0.0, -math.cos(a))
+    prims = [prim(ST_PRIM_BOX, pos=(0, 0, 0.5), params=(0.5, 0.5, 0.2), material=1),
+             prim(ST_PRIM_PLANE, pos=(0, 0, 0.55), material=1, op=ST_OP_SUB, rot=rot),
+             prim(ST_PRIM_BOX, pos=(0, 0, -0.05), params=(8.0, 8.0, 0.05), material=2)]
+    s = Scene(prims, [air(), glass_m, det], env_radius=20.0, tolerance=1e-5, name="dispersive-wedge")
+    s.params = default_params(width=16, height=16, maxbounce=32)
+    s.view = look_at((0, -3, 2), (0, 0, 0.5), 40.0, 1.0)
+    src = StOpticsSource()
+    for i, v in enumerate((0.0, 0.0, 1.0)):
+        src.centre[i] = v
+    for i, v in enumerate((0.0, 0.0, -1.0)):
+        src.axis[i] = v
+    for i, v in enumerate((0.0, 1.0, 0.0)):
+        src.tangent[i] = v
+    src.flux, src.shape, src.size_x, src.size_y = 1000.0, 1, 0.1, 0.1
+    src.dist, src.cos_half, src.n_exp, src.emit_n = 0, 1.0, 1.0, 1.0
+    s.info = {"sources": [src], "rays": [rays], "workload": "dispersive-wedge"}
+    return s
+
+
+def wedge_exit_deg(wedge_deg, n):
+    """optics/fresnel.js wedgeExitDeg: the beam straight down refracted into the wedge's tilted top (into index n) and
+    out of its level bottom; the leaving ray's angle from straight down, degrees, signed as atan2(x, -z)."""
+    def refract(d, nrm, eta):
+        c = -(d[0] * nrm[0] + d[1] * nrm[1] + d[2] * nrm[2])
+        k = 1 - eta * eta * (1 - c * c)
+        if k < 0:
+            return None
+        t = eta * c - math.sqrt(k)
+        return [eta * d[i] + t * nrm[i] for i in range(3)]
+    a = math.radians(wedge_deg)
+    inside = refract([0.0, 0.0, -1.0], [math.sin(a), 0.0, math.cos(a)], 1.0 / n)
+    out = inside and refract(inside, [0.0, 0.0, 1.0], n)
+    return math.degrees(math.atan2(out[0], -out[2])) if out else None

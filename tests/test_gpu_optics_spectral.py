@@ -94,3 +94,45 @@ def test_a_red_light_through_the_dichroic_in_colour():
     R = S.coat_edge_rgb(0.0, 1.0, 600.0, 20.0)
     share, c, _ = run(slab(where=S.COAT_AR_BACK, colour=(1.0, 0.0, 0.0), n=n), n, spectral=0)
     assert abs(share - (1 - R[0])) < 4 * math.sqrt((1 - R[0]) * R[0] / n) + 2e-3, (share, 1 - R[0])
+
+
+def channel_weights():
+    """The camera's wavelength table as the draw reads it (st_spectral.h spectral_table): per 1 nm cell from 380 nm,
+    each channel's clipped Rec.709 colour-matching function averaged over the cell (8 midpoints), normalised."""
+    l = 380.0 + (np.arange(400 * 8) + 0.5) / 8.0
+    rgb = np.maximum(F.XYZ_TO_RGB @ F.cmf(l), 0.0).reshape(3, 400, 8).mean(axis=2)
+    return rgb / rgb.sum(axis=1, keepdims=True), 380.0 + np.arange(400) + 0.5
+
+
+def cauchy(nd, vd, l):
+    B = (nd - 1) / (vd * (1 / 486.13 ** 2 - 1 / 656.27 ** 2))
+    return nd + B * (1 / l ** 2 - 1 / 587.56 ** 2)
+
+
+@pytest.mark.parametrize("abbe", [0.0, 28.0])
+def test_a_dispersive_wedge_fans_the_beam(abbe):
+    """optics-dispersion (lib/pathtracer/tests.js:1331-1390): a collimated white beam through a 30 degree wedge of n_d
+    1.75; each ray refracted into the glass takes a wavelength and refracts at n(l), so each channel's mean exit angle
+    over the detector hits is Snell's at each wavelength averaged with that channel's weights; Abbe 0, one angle."""
+    n = 200_000
+    s = S.dispersive_wedge(abbe=abbe, rays=n)
+    with create_path_tracer(s, device=0) as rt:
+        O = optics.Optics(rt)
+        O.set_sources(s.info["sources"])
+        O.set_far(nC=36, nG=19)
+        O.set_detail(det_cap=1 << 20)
+        O.run([n], lux_cells=8)
+        hits, nh = O.hits()
+    ang = np.degrees(np.arctan2(hits[:, 4], -hits[:, 6]))
+    ok = (ang > -30.0) & (ang < -18.0)
+    assert ok.mean() > 0.8, ok.mean()
+    rgb = (F.XYZ_TO_RGB @ np.stack([hits[ok, 9], hits[ok, 3], hits[ok, 10]])).astype(np.float64)
+    got = (rgb * ang[ok]).sum(axis=1) / rgb.sum(axis=1)
+    if abbe == 0.0:
+        assert np.allclose(got, S.wedge_exit_deg(30.0, 1.75), atol=2e-3), got
+        return
+    W, lc = channel_weights()
+    a = np.array([S.wedge_exit_deg(30.0, cauchy(1.75, abbe, x)) for x in lc])
+    expect = W @ a
+    assert np.all(np.diff(got) < 0), got                       # blue bent most, red least
+    assert np.allclose(got, expect, atol=0.01), (got, expect)
