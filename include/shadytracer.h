@@ -421,6 +421,17 @@ int  st_set_tune(st_ctx* ctx, const st_tune* t);    /* set them (claim, chunk; 0
 
 /* ---- readings (caller-owned buffers, width*height entries each; NULL skips one) ---- */
 int  st_read_accum(st_ctx* ctx, double* rgb, double* V, double* S, uint32_t* count);
+/* CHECKPOINT AND RESUME: the render's state between samples as one blob -- the FP64 accumulation of every view (mean
+ * rgb and count), the error bar's moments, light tracing's splat buffer and connection counts, and the sample index the
+ * next samples are seeded by. Loaded into a context with the same scene, settings and picture (after st_sync, before
+ * its next step), the render goes on where it stopped: the samples after it take the random numbers they would have
+ * taken, so a render saved at N samples and resumed to N + M is the one rendered to N + M at once. What learns across
+ * samples is the caller's to carry (the proposal's weights, st_mlp_get_weights / st_mlp_set_weights); the emitters'
+ * list and the learned emission map start over. The blob is st_checkpoint_size's bytes; a load of another picture's
+ * blob (its width, height or views) is ST_ERR_ARG. */
+int  st_checkpoint_size(st_ctx* ctx, size_t* bytes);
+int  st_checkpoint_save(st_ctx* ctx, void* out, size_t bytes);
+int  st_checkpoint_load(st_ctx* ctx, const void* in, size_t bytes);
 int  st_image_stats(st_ctx* ctx, st_image_stats_t* out);
 int  st_read_counters(st_ctx* ctx, st_counters_t* out);
 /* The scene's signed distance at n points (3n floats, metres) into out (n floats), as the march folds the table

@@ -27,6 +27,9 @@ SIGNATURES = {
     "st_set_env_image": ([P, P, C.c_uint32, C.c_uint32, C.c_float, C.c_float], C.c_int),
     "st_optics_set_rays": ([P, P, C.c_uint32], C.c_int),
     "st_optics_set_spectra": ([P, P, C.c_uint32], C.c_int),
+    "st_checkpoint_size": ([P, C.POINTER(C.c_size_t)], C.c_int),
+    "st_checkpoint_save": ([P, P, C.c_size_t], C.c_int),
+    "st_checkpoint_load": ([P, P, C.c_size_t], C.c_int),
     "st_env_map_tables": ([P, P], C.c_int),
     "st_invalidate": ([P], C.c_int),
     "st_step": ([P, C.c_int], C.c_int),

@@ -1206,6 +1206,69 @@ int st_step(st_ctx* ctx, int n) {
     return st_sync(ctx, -1);
 }
 
+// THE CHECKPOINT: a header (magic, version, width, height, views, samples), then the accumulation, the moments, the
+// splat buffer and the connection counts as the device holds them
+struct CkHeader { uint32_t magic, version, W, H, nv, samples, pad0, pad1; };
+static constexpr uint32_t CK_MAGIC = 0x4B435453u;             // "STCK"
+static size_t ck_bytes(const st_ctx* ctx) {
+    return sizeof(CkHeader) + (size_t)ctx->acc_views * ctx->P * (sizeof(Acc4) + sizeof(double2)) +
+           (size_t)ctx->P * (sizeof(float4) + sizeof(uint32_t));
+}
+int st_checkpoint_size(st_ctx* ctx, size_t* bytes) {
+    if (!ctx || !bytes) return ST_ERR_ARG;
+    if (!ctx->d_acc) return fail(ctx, ST_ERR_STATE, "nothing rendered yet");
+    *bytes = ck_bytes(ctx);
+    return ST_OK;
+}
+int st_checkpoint_save(st_ctx* ctx, void* out, size_t bytes) {
+    if (!ctx || !out) return ST_ERR_ARG;
+    if (ctx->in_flight) return fail(ctx, ST_ERR_BUSY, "a trace is in flight: st_sync first");
+    if (!ctx->d_acc) return fail(ctx, ST_ERR_STATE, "nothing rendered yet");
+    if (bytes < ck_bytes(ctx)) return fail(ctx, ST_ERR_ARG, "the checkpoint's buffer is too small");
+    cudaSetDevice(ctx->device);
+    unsigned char* o = static_cast<unsigned char*>(out);
+    const CkHeader h{CK_MAGIC, 1u, ctx->W, ctx->H, ctx->acc_views, (uint32_t)ctx->samples, 0u, 0u};
+    std::memcpy(o, &h, sizeof(h));
+    o += sizeof(h);
+    const size_t na = (size_t)ctx->acc_views * ctx->P;
+    CK(cudaMemcpyAsync(o, ctx->d_acc, na * sizeof(Acc4), cudaMemcpyDeviceToHost, ctx->stream), "checkpoint");
+    o += na * sizeof(Acc4);
+    CK(cudaMemcpyAsync(o, ctx->d_mom, na * sizeof(double2), cudaMemcpyDeviceToHost, ctx->stream), "checkpoint");
+    o += na * sizeof(double2);
+    CK(cudaMemcpyAsync(o, ctx->d_splat, (size_t)ctx->P * sizeof(float4), cudaMemcpyDeviceToHost, ctx->stream), "checkpoint");
+    o += (size_t)ctx->P * sizeof(float4);
+    CK(cudaMemcpyAsync(o, ctx->d_ltcount, (size_t)ctx->P * 4, cudaMemcpyDeviceToHost, ctx->stream), "checkpoint");
+    CK(cudaStreamSynchronize(ctx->stream), "checkpoint");
+    return ST_OK;
+}
+int st_checkpoint_load(st_ctx* ctx, const void* in, size_t bytes) {
+    if (!ctx || !in || bytes < sizeof(CkHeader)) return ST_ERR_ARG;
+    if (ctx->in_flight) return fail(ctx, ST_ERR_BUSY, "a trace is in flight: st_sync first");
+    if (!ctx->has_scene || !ctx->has_params) return fail(ctx, ST_ERR_STATE, "set the scene and the settings first");
+    CkHeader h;
+    std::memcpy(&h, in, sizeof(h));
+    if (h.magic != CK_MAGIC || h.version != 1u) return fail(ctx, ST_ERR_ARG, "not a checkpoint");
+    if (h.W != ctx->W || h.H != ctx->H || h.nv != std::max(ctx->nv, 1u))
+        return fail(ctx, ST_ERR_ARG, "the checkpoint is of another picture (its width, height or views)");
+    cudaSetDevice(ctx->device);
+    int rc = ensure_wave(ctx);
+    if (rc) return rc;
+    if (bytes < ck_bytes(ctx)) return fail(ctx, ST_ERR_ARG, "the checkpoint is short");
+    const unsigned char* p = static_cast<const unsigned char*>(in) + sizeof(h);
+    const size_t na = (size_t)ctx->acc_views * ctx->P;
+    CK(cudaMemcpyAsync(ctx->d_acc, p, na * sizeof(Acc4), cudaMemcpyHostToDevice, ctx->stream), "resume");
+    p += na * sizeof(Acc4);
+    CK(cudaMemcpyAsync(ctx->d_mom, p, na * sizeof(double2), cudaMemcpyHostToDevice, ctx->stream), "resume");
+    p += na * sizeof(double2);
+    CK(cudaMemcpyAsync(ctx->d_splat, p, (size_t)ctx->P * sizeof(float4), cudaMemcpyHostToDevice, ctx->stream), "resume");
+    p += (size_t)ctx->P * sizeof(float4);
+    CK(cudaMemcpyAsync(ctx->d_ltcount, p, (size_t)ctx->P * 4, cudaMemcpyHostToDevice, ctx->stream), "resume");
+    CK(cudaMemcpyAsync(&ctx->d_ctr->sample, &h.samples, sizeof(uint32_t), cudaMemcpyHostToDevice, ctx->stream), "resume");
+    CK(cudaStreamSynchronize(ctx->stream), "resume");
+    ctx->samples = h.samples;
+    return ST_OK;
+}
+
 int st_read_accum(st_ctx* ctx, double* rgb, double* V, double* S, uint32_t* count) {
     return st_read_accum_view(ctx, 0, rgb, V, S, count);
 }

@@ -168,6 +168,19 @@ class PathTracer:
                                         S.ctypes.data_as(P), cnt.ctypes.data_as(P)), self.ctx, "st_read_accum_view")
         return rgb, V, S, cnt
 
+    def checkpoint(self):
+        """The render's state between samples (st_checkpoint_save): bytes a later resume() continues from."""
+        n = C.c_size_t()
+        check(self.L.st_checkpoint_size(self.ctx, C.byref(n)), self.ctx, "st_checkpoint_size")
+        buf = C.create_string_buffer(n.value)
+        check(self.L.st_checkpoint_save(self.ctx, buf, n.value), self.ctx, "st_checkpoint_save")
+        return buf.raw
+
+    def resume(self, blob):
+        """Go on from a checkpoint of the same scene, settings and picture (st_checkpoint_load)."""
+        buf = C.create_string_buffer(bytes(blob), len(blob))
+        check(self.L.st_checkpoint_load(self.ctx, buf, len(blob)), self.ctx, "st_checkpoint_load")
+
     def image_stats(self):
         s = T.StImageStats()
         check(self.L.st_image_stats(self.ctx, C.byref(s)), self.ctx, "st_image_stats")

@@ -1254,7 +1254,9 @@ def dispersive_wedge(abbe=28.0, ior=1.75, wedge_deg=30.0, rays=100_000):
     prims = [prim(ST_PRIM_BOX, pos=(0, 0, 0.5), params=(0.5, 0.5, 0.2), material=1),
              prim(ST_PRIM_PLANE, pos=(0, 0, 0.55), material=1, op=ST_OP_SUB, rot=rot),
              prim(ST_PRIM_BOX, pos=(0, 0, -0.05), params=(8.0, 8.0, 0.05), material=2)]
-    s = Scene(prims, [air(), glass_m, det], env_radius=20.0, tolerance=1e-5, name="dispersive-wedge")
+    # (the surface tolerance the normal's differences are taken at: at 1e-5 m a tilted face's f32 differences turn the
+    # normal by about 0.03 degree, at 1e-3 m a hundred times less)
+    s = Scene(prims, [air(), glass_m, det], env_radius=20.0, tolerance=1e-3, name="dispersive-wedge")
     s.params = default_params(width=16, height=16, maxbounce=32)
     s.view = look_at((0, -3, 2), (0, 0, 0.5), 40.0, 1.0)
     src = StOpticsSource()
