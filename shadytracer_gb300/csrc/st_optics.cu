@@ -128,6 +128,18 @@ __device__ __forceinline__ f3 spo_xyz(const float* t, f3 c, f3 l) {
 }
 // a ray's wavelength word (PathBuf.lam): its u, or u + 2 once a dispersive glass collapsed it to its first wavelength
 __device__ __forceinline__ float spo_u(float w) { return w >= 2.f ? w - 2.f : w; }
+// THE LOBES AT THE RAY'S WAVELENGTHS (optics/spectral.js specOfRGB): the material's colour a reflectance at each, the
+// coating taken at each -- out of line, so the trace in colour keeps its registers
+__device__ __noinline__ void spectral_lobes(const float* spo, f3 l3, f3 nrm, f3 v, const st_material& m, float eta,
+                                            const MfTab& tab, float trans, float spec, float hz, float n0, bool inside,
+                                            Lobes& out) {
+    st_material mw = m;
+    const f3 rgb = mk(m.base[0], m.base[1], m.base[2]);
+    mw.base[0] = dot(rgb, spo_basis(spo, l3.x));
+    mw.base[1] = dot(rgb, spo_basis(spo, l3.y));
+    mw.base[2] = dot(rgb, spo_basis(spo, l3.z));
+    out = make_lobes(nrm, v, mw, eta, tab, trans, spec, hz, n0, inside, 0.f, &l3);
+}
 // optWeight: what a ray carries, as luminance -- its colour's, or by wavelength its Y
 __device__ __forceinline__ float opt_weight(const OptArgs& o, f3 beta, float lamw) {
     return o.spectral ? spo_xyz(o.spo, beta, spo_lams(o.spo, spo_u(lamw))).y : luma(beta);
@@ -474,7 +486,6 @@ __global__ void __launch_bounds__(256) k_opt_shade(OptArgs o, int nxt, int last)
                     // BY WAVELENGTH (optics/spectral.js WHAT A MATERIAL IS AT A WAVELENGTH): the colour a reflectance at
                     // each of the ray's wavelengths, the coating taken at each; a dispersive glass beyond refracts the
                     // first wavelength (at its n, the pick the d line's) and drops the other two
-                    st_material mw = m;
                     f3 l3 = mk(0.f);
                     float nT = n1;
                     bool collapse = false;
@@ -482,10 +493,6 @@ __global__ void __launch_bounds__(256) k_opt_shade(OptArgs o, int nxt, int last)
                     bool draw = false;
                     if (o.spectral) {
                         l3 = spo_lams(o.spo, spo_u(lamw));
-                        const f3 rgb = mk(m.base[0], m.base[1], m.base[2]);
-                        mw.base[0] = dot(rgb, spo_basis(o.spo, l3.x));
-                        mw.base[1] = dot(rgb, spo_basis(o.spo, l3.y));
-                        mw.base[2] = dot(rgb, spo_basis(o.spo, l3.z));
                         if (v1 > 0.f) { nT = cauchy_n(n1, v1, l3.x); collapse = lamw < 2.f; }
                     } else if (v1 > 0.f) {
                         // IN COLOUR (materials_pbr.js:1116-1139, as the renderer's): a ray with a wavelength meets the
@@ -513,8 +520,9 @@ __global__ void __launch_bounds__(256) k_opt_shade(OptArgs o, int nxt, int last)
                         }
                     }
                     float etaFace = diffFace ? fminf(n0, n1) / fmaxf(n0, n1) : n0 / n1;
-                    Lobes lb = make_lobes(nrm, -dir, mw, etaFace, a.tab, trans, specv, hz, n0, inside, 0.f,
-                                          o.spectral ? &l3 : nullptr);
+                    Lobes lb;
+                    if (o.spectral) spectral_lobes(o.spo, l3, nrm, -dir, m, etaFace, a.tab, trans, specv, hz, n0, inside, lb);
+                    else lb = make_lobes(nrm, -dir, m, etaFace, a.tab, trans, specv, hz, n0, inside, 0.f);
                     lb.etaT = n0 / nT;
                     coat_pick(lb, beta);
                     LobeSample smp = lobes_sample(lb, a.tab, rng.next());
