@@ -336,7 +336,12 @@ __global__ void __launch_bounds__(256) k_opt_gen(OptArgs o) {
                 if (y > 0.f) c = col * (w / y);
             }
         }
-        a.pb.beta[i] = make_float4(c.x, c.y, c.z, 1.f);
+        // w: what it carries as luminance (optWeight), carried with it so that every interaction's weight in is exactly
+        // the last one's weight out, and the tallies' sums telescope to what was emitted bit for bit (a weight worked
+        // out again from the stored colour could round to another integer of the fixed point)
+        const float wt = o.spectral ? spo_xyz(o.spo, c, spo_lams(o.spo, a.pb.lam[i])).y
+                                    : ((c.x == c.y && c.y == c.z) ? c.x : luma(c));
+        a.pb.beta[i] = make_float4(c.x, c.y, c.z, wt);
         if (o.has_sets) atomicAdd(&o.tot[(size_t)inst * OPT_TOT + T_EMIT], (unsigned long long)fx(w));
         if (id < o.path_rays) {                                         // a kept path starts where the ray leaves
             o.vcount[(size_t)inst * o.path_rays + id] = 0u;
@@ -373,6 +378,7 @@ __global__ void __launch_bounds__(256) k_opt_shade(OptArgs o, int nxt, int last)
     for (uint32_t r = 0; r < nrounds; r++) {
         uint32_t q = r * stride + blockIdx.x * blockDim.x + threadIdx.x;
         bool cont = false;
+        float wcar = 0.f;                                            // the weight a ray going on carries
         uint32_t slot = 0, inst = 0, tag = 0, mati = 0;
         f3 pos, dir, beta;
         float ltot = 0.f, n = 1.f;
@@ -392,7 +398,8 @@ __global__ void __launch_bounds__(256) k_opt_shade(OptArgs o, int nxt, int last)
             uint32_t bounces = m4.y & 0xffu, state = (m4.y >> 16) & 0xffu;
             // by wavelength its u (and whether it collapsed); in colour the wavelength a dispersive glass gave it (0 none)
             const float lamw = a.pb.lam[slot];
-            const float wIn = opt_weight(o, beta, lamw);             // optWeight: beta x radiance (1), as luminance
+            const float wIn = b4.w;                                   // optWeight: beta x radiance (1), as luminance
+            wcar = wIn;
             if (state == RAY_ESCAPED) {                               // kernels.js:609-625
                 tv[T_ESC] = fx(wIn);
                 tv[T_NESC] = 1;
@@ -541,6 +548,7 @@ __global__ void __launch_bounds__(256) k_opt_shade(OptArgs o, int nxt, int last)
                     if (bounces > u.maxbounce) st = RAY_TERMINATED;
                     bool goesOn = st == RAY_ACTIVE || st == RAY_TERMINATED;
                     float wOut = goesOn ? opt_weight(o, beta, lamo) : 0.f;
+                    wcar = wOut;
                     if (lamo != lamw) a.pb.lam[slot] = lamo;
                     tv[T_INTER] = 1;
                     tv[T_ABS] = fx(wIn) - fx(wOut);
@@ -564,7 +572,7 @@ __global__ void __launch_bounds__(256) k_opt_shade(OptArgs o, int nxt, int last)
         if (cont) {
             a.pb.pos[slot] = f4(pos, ltot);
             a.pb.dir[slot] = f4(dir, n);
-            a.pb.beta[slot] = f4(beta, 1.f);
+            a.pb.beta[slot] = f4(beta, wcar);
             m4.y = (m4.y & 0xffffu) | (RAY_ACTIVE << 16);
             a.pb.meta[slot] = m4;
             outq[rq] = slot;
