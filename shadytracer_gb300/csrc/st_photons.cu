@@ -497,7 +497,7 @@ __global__ void __launch_bounds__(256) k_photon_shade(WaveArgs a, int nxt, int l
                             // the medium it is in now, the one beyond the face (tracebasics.js enterMedium)
                             const uint32_t med = (ids >> 16) != SURF_NONE ? (ids >> 16)
                                                                           : (inside ? 0u : (ids & 0xffffu));
-                            m4.z = (m4.z & META_STEPS) | (min(med, 255u) << MEDIUM_SHIFT);
+                            if (a.u.scatter_on) m4.z = (m4.z & META_STEPS) | (min(med, 255u) << MEDIUM_SHIFT);
                         }
                         const f3 off = dir * otol;
                         pos = pos + off; ltot += length(off) * n;

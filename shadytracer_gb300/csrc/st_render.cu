@@ -518,9 +518,10 @@ __device__ __forceinline__ void shade_surface(const WaveArgs& a, const st_materi
     if (smp.transmitted) {
         n = nT;                                                       // n(lambda) where the ray has a wavelength
         if (draw) { beta = beta * spec.w; lam = spec.lam; }           // ...and the one it was refracted at, kept
-        // ...and the medium it is in now, the one beyond the face (tracebasics.js:522-530 enterMedium)
+        // ...and the medium it is in now, the one beyond the face (tracebasics.js:522-530 enterMedium), where a
+        // material scatters inside: the march reads it there alone, and elsewhere meta.z stays the steps it was
         const uint32_t med = (ids >> 16) != SURF_NONE ? (ids >> 16) : (inside ? 0u : (ids & 0xffffu));
-        mz = (mz & META_STEPS) | (min(med, 255u) << MEDIUM_SHIFT);
+        if (a.u.scatter_on) mz = (mz & META_STEPS) | (min(med, 255u) << MEDIUM_SHIFT);
     }
     if (u.sppm_on) {                                                  // materials_pbr.js:862-873 lensStep
         const bool delta = smp.ev == EV_DELTA;
